@@ -1,0 +1,181 @@
+/*
+ * osl-gb300: C ABI of the GB300 batched shading executor.
+ *
+ * This is the drop-in boundary for OSL's data-parallel hot path: running an
+ * optimized ShaderGroup over many shading points. Each entry point replaces
+ * one member of the reference's C++ API (paths relative to the
+ * OpenShadingLanguage source tree); the C++ facade and the ctypes binding
+ * in INTEGRATION.md bind to exactly these symbols.
+ *
+ * Conventions: plain pointers and sizes only; every call returns an int
+ * status (OSLG_OK == 0) and the message of the last failure is available
+ * from oslg_last_error(). No C++ exception crosses this boundary.
+ * Device pointers are CUDA device addresses on the current device;
+ * `stream` is a cudaStream_t (NULL = legacy default stream).
+ */
+#ifndef OSLG_H
+#define OSLG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OSLG_OK 0
+#define OSLG_ERR_ARG 1        /* bad argument or unknown name */
+#define OSLG_ERR_PARSE 2      /* .oso text could not be read */
+#define OSLG_ERR_LOWER 3      /* group uses something the executor lacks */
+#define OSLG_ERR_CUDA 4       /* a CUDA call failed */
+#define OSLG_ERR_STATE 5      /* call out of order (e.g. execute before end) */
+#define OSLG_ERR_DEVICE 6     /* the kernel reported a status bit */
+
+typedef struct oslg_system oslg_system;
+typedef struct oslg_group oslg_group;
+
+/* OIIO TypeDesc numbering (basetype / aggregate / vecsemantics), so a
+ * caller holding an OIIO::TypeDesc can pass its fields straight through. */
+#define OSLG_BASE_INT32 7
+#define OSLG_BASE_FLOAT 11
+#define OSLG_BASE_STRING 13
+#define OSLG_AGG_SCALAR 1
+#define OSLG_AGG_VEC3 3
+#define OSLG_AGG_MATRIX44 16
+#define OSLG_VEC_NOXFORM 0
+#define OSLG_VEC_COLOR 1
+#define OSLG_VEC_POINT 2
+#define OSLG_VEC_VECTOR 3
+#define OSLG_VEC_NORMAL 4
+
+typedef struct oslg_typedesc {
+    int32_t basetype;
+    int32_t aggregate;
+    int32_t vecsemantics;
+    int32_t arraylen;
+} oslg_typedesc;
+
+/* SymArena (src/include/OSL/oslexec.h:57-63) */
+#define OSLG_ARENA_HEAP 1
+#define OSLG_ARENA_OUTPUTS 2
+#define OSLG_ARENA_USERDATA 3
+
+/* SymLocationDesc (src/include/OSL/oslexec.h:69-105): point i of symbol
+ * `name` lives at base + offset + i * stride; with derivs the value is
+ * followed by its x and y derivatives. */
+typedef struct oslg_symloc {
+    const char* name;
+    oslg_typedesc type;
+    int32_t derivs;
+    int32_t arena;
+    int64_t offset;
+    int64_t stride;
+} oslg_symloc;
+
+/* One shader-global field. `data` == NULL means every point uses `value`;
+ * otherwise data points to SoA planes on the device: component c of point
+ * i is data[c * plane_stride + i]. */
+typedef struct oslg_field {
+    const float* data;
+    int64_t plane_stride;
+    float value[3];
+    float pad;
+} oslg_field;
+
+/* Device-side BatchedShaderGlobals: the varying members of
+ * src/include/OSL/batched_shaderglobals.h:77-197 over N points. Fields the
+ * group does not read may be left zeroed. */
+typedef struct oslg_shaderglobals {
+    oslg_field P, dPdx, dPdy, dPdz;
+    oslg_field I, dIdx, dIdy;
+    oslg_field N, Ng;
+    oslg_field u, dudx, dudy;
+    oslg_field v, dvdx, dvdy;
+    oslg_field dPdu, dPdv;
+    oslg_field time, dtime, dPdtime;
+    oslg_field Ps, dPsdx, dPsdy;
+    oslg_field surfacearea;
+} oslg_shaderglobals;
+
+/* ---- ShadingSystem ------------------------------------------------------ */
+
+/* ShadingSystem::ShadingSystem (src/include/OSL/oslexec.h:170) */
+int oslg_create_system(oslg_system** out);
+/* ShadingSystem::~ShadingSystem */
+int oslg_destroy_system(oslg_system* sys);
+/* ShadingSystem::attribute(name, TypeDesc, const void*) (oslexec.h:324).
+ * Integer options: "max_closure_components", "max_closure_terms",
+ * "gpu_block", "gpu_points_per_thread", "gpu_heap_placement" (0 HBM, 1 smem,
+ * -1 auto), "debug". */
+int oslg_attribute_int(oslg_system* sys, const char* name, int value);
+/* ShadingSystem::register_closure (oslexec.h:1041). Parameters are taken
+ * positionally from the `closure` op's arguments. */
+int oslg_register_closure(oslg_system* sys, const char* name, int id);
+/* ShadingSystem::LoadMemoryCompiledShader (oslexec.h:608) */
+int oslg_load_memory_compiled_shader(oslg_system* sys, const char* shadername,
+                                     const char* oso_text);
+/* Message of the last failed call on this system (ShadingSystem errors are
+ * reported through an ErrorHandler in the reference). */
+const char* oslg_last_error(oslg_system* sys);
+
+/* ---- group construction (oslexec.h:634-771) ---------------------------- */
+
+/* ShadingSystem::ShaderGroupBegin (oslexec.h:634) */
+int oslg_shader_group_begin(oslg_system* sys, const char* groupname, oslg_group** out);
+/* ShadingSystem::Parameter (oslexec.h:656): applies to the next Shader()
+ * call, as in the reference. `value` holds arraylen (or 1) elements of the
+ * type; strings are passed as an array of const char*. */
+int oslg_parameter(oslg_system* sys, oslg_group* group, const char* name,
+                   oslg_typedesc type, const void* value, int lockgeom);
+/* ShadingSystem::Shader (oslexec.h:723) */
+int oslg_shader(oslg_system* sys, oslg_group* group, const char* shaderusage,
+                const char* shadername, const char* layername);
+/* ShadingSystem::ConnectShaders (oslexec.h:740) */
+int oslg_connect_shaders(oslg_system* sys, oslg_group* group, const char* srclayer,
+                         const char* srcparam, const char* dstlayer, const char* dstparam);
+/* ShadingSystem::ShaderGroupEnd (oslexec.h:650) */
+int oslg_shader_group_end(oslg_system* sys, oslg_group* group);
+/* ShadingSystem::attribute(group, "renderer_outputs", ...) (oslexec.h:360) */
+int oslg_group_renderer_outputs(oslg_system* sys, oslg_group* group, const char** names, int n);
+/* ShadingSystem::add_symlocs(group, symlocs) (oslexec.h:1076) */
+int oslg_add_symlocs(oslg_system* sys, oslg_group* group, const oslg_symloc* locs, int n);
+/* ShadingSystem::optimize_group (oslexec.h:1093) + BatchedExecutor::jit_group
+ * (oslexec.h:993): lowers the group to a device op program and uploads it. */
+int oslg_optimize_group(oslg_system* sys, oslg_group* group);
+/* ShaderGroupRef release */
+int oslg_release_group(oslg_system* sys, oslg_group* group);
+
+/* The lowered op program (no reference counterpart: it replaces the JIT'd
+ * LLVM module). Copies up to `cap` bytes into `buf` and returns the size
+ * through `size`. Lets a caller cache or inspect what will run. */
+int oslg_group_program(oslg_system* sys, oslg_group* group, void* buf, size_t cap, size_t* size);
+
+/* ---- execution ------------------------------------------------------------ */
+
+/* BatchedExecutor<W>::execute (oslexec.h:1000-1004, shadingsys.cpp:329),
+ * over npoints device-resident points instead of one W-lane batch:
+ * globals as above, userdata/outputs arenas addressed by the symlocs.
+ * Stream-ordered; returns once the launch is enqueued. */
+int oslg_execute_batch(oslg_system* sys, oslg_group* group, int64_t npoints,
+                       const oslg_shaderglobals* globals, void* userdata_base,
+                       void* output_base, void* stream);
+
+/* Same as oslg_execute_batch, then waits for the stream and reports any
+ * status bit the kernel raised (closure arena overflow, bad opcode, array
+ * bounds) as OSLG_ERR_DEVICE (context.cpp:443-451 flushes errors the same
+ * way at execute_cleanup). */
+int oslg_execute_batch_sync(oslg_system* sys, oslg_group* group, int64_t npoints,
+                            const oslg_shaderglobals* globals, void* userdata_base,
+                            void* output_base, void* stream);
+
+/* Status bits raised by kernels since the last call (and clears them). */
+int oslg_device_status(oslg_system* sys, uint32_t* bits);
+
+/* Launch shape the next execute uses: threads per block, points per
+ * thread, heap placement (0 HBM scratch, 1 shared memory, -1 auto). */
+int oslg_set_launch(oslg_system* sys, int block, int points_per_thread, int heap_smem);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OSLG_H */

@@ -1,0 +1,103 @@
+"""ctypes binding of include/oslg.h (the library's C ABI).
+
+The native library is required: importing this module raises if
+liboslg_gb300.so has not been built (there is no CPU fallback).
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "liboslg_gb300.so")
+
+OSLG_OK = 0
+OSLG_ERR_DEVICE = 6
+
+BASE_INT32 = 7
+BASE_FLOAT = 11
+BASE_STRING = 13
+AGG_SCALAR = 1
+AGG_VEC3 = 3
+AGG_MATRIX44 = 16
+VEC_NOXFORM, VEC_COLOR, VEC_POINT, VEC_VECTOR, VEC_NORMAL = 0, 1, 2, 3, 4
+
+ARENA_HEAP = 1
+ARENA_OUTPUTS = 2
+ARENA_USERDATA = 3
+
+
+class TypeDescC(ctypes.Structure):
+    _fields_ = [("basetype", ctypes.c_int32), ("aggregate", ctypes.c_int32),
+                ("vecsemantics", ctypes.c_int32), ("arraylen", ctypes.c_int32)]
+
+
+class SymLocC(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char_p), ("type", TypeDescC), ("derivs", ctypes.c_int32),
+                ("arena", ctypes.c_int32), ("offset", ctypes.c_int64), ("stride", ctypes.c_int64)]
+
+
+class FieldC(ctypes.Structure):
+    _fields_ = [("data", ctypes.c_void_p), ("plane_stride", ctypes.c_int64),
+                ("value", ctypes.c_float * 3), ("pad", ctypes.c_float)]
+
+
+GLOBAL_FIELDS = ["P", "dPdx", "dPdy", "dPdz", "I", "dIdx", "dIdy", "N", "Ng", "u", "dudx", "dudy",
+                 "v", "dvdx", "dvdy", "dPdu", "dPdv", "time", "dtime", "dPdtime", "Ps", "dPsdx",
+                 "dPsdy", "surfacearea"]
+
+
+class ShaderGlobalsC(ctypes.Structure):
+    _fields_ = [(n, FieldC) for n in GLOBAL_FIELDS]
+
+
+_EXPORTS = {
+    "oslg_create_system": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p)]),
+    "oslg_destroy_system": (ctypes.c_int, [ctypes.c_void_p]),
+    "oslg_attribute_int": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int]),
+    "oslg_register_closure": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int]),
+    "oslg_load_memory_compiled_shader": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p]),
+    "oslg_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
+    "oslg_shader_group_begin": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)]),
+    "oslg_parameter": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p, TypeDescC,
+                                      ctypes.c_void_p, ctypes.c_int]),
+    "oslg_shader": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p,
+                                   ctypes.c_char_p]),
+    "oslg_connect_shaders": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p,
+                                            ctypes.c_char_p, ctypes.c_char_p]),
+    "oslg_shader_group_end": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "oslg_group_renderer_outputs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p,
+                                                   ctypes.POINTER(ctypes.c_char_p), ctypes.c_int]),
+    "oslg_add_symlocs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(SymLocC), ctypes.c_int]),
+    "oslg_optimize_group": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "oslg_release_group": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "oslg_group_program": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                          ctypes.POINTER(ctypes.c_size_t)]),
+    "oslg_execute_batch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                          ctypes.POINTER(ShaderGlobalsC), ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_void_p]),
+    "oslg_execute_batch_sync": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                               ctypes.POINTER(ShaderGlobalsC), ctypes.c_void_p, ctypes.c_void_p,
+                                               ctypes.c_void_p]),
+    "oslg_device_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint32)]),
+    "oslg_set_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+}
+
+_lib = None
+
+
+def lib():
+    """Load the native library (raises if it is missing: no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("liboslg_gb300.so is not built; run openshadinglanguage_gb300/build.py")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in _EXPORTS.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def exported_symbols():
+    return list(_EXPORTS.keys())

@@ -1,0 +1,77 @@
+"""In-tree build of the native library: host C++ (group model, .oso reader,
+lowering, C ABI) with g++ and the sm_103a interpreter with nvcc, linked
+into openshadinglanguage_gb300/liboslg_gb300.so.
+
+Translation units compile in parallel; the whole build takes well under a
+minute. Nothing here depends on torch.
+"""
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "liboslg_gb300.so")
+CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+HOST_SOURCES = ["oslg_oso.cpp", "oslg_lower.cpp", "oslg_capi.cpp"]
+CUDA_SOURCES = ["oslg_kernels.cu"]
+
+
+def _run(cmd):
+    p = subprocess.run(cmd, capture_output=True, text=True)
+    if p.returncode != 0:
+        raise RuntimeError("build step failed:\n%s\n%s%s" % (" ".join(cmd), p.stdout, p.stderr))
+    return p.stdout + p.stderr
+
+
+def _newer(target, deps):
+    if not os.path.exists(target):
+        return False
+    t = os.path.getmtime(target)
+    return all(os.path.getmtime(d) <= t for d in deps)
+
+
+def build(verbose=False, ptxas_verbose=False):
+    os.makedirs(BUILD, exist_ok=True)
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
+    headers.append(os.path.join(HERE, "..", "include", "oslg.h"))
+    jobs, objs = [], []
+    for src in HOST_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(BUILD, src + ".o")
+        objs.append(o)
+        if not _newer(o, [s] + headers):
+            jobs.append(["g++", "-std=c++17", "-O2", "-fPIC", "-Wall", "-Wno-unused-function",
+                         "-I", os.path.join(CUDA_HOME, "include"), "-c", s, "-o", o])
+    for src in CUDA_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(BUILD, src + ".o")
+        objs.append(o)
+        if not _newer(o, [s] + headers) or ptxas_verbose:
+            cmd = [NVCC] + ARCH + ["-std=c++17", "-O3", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC",
+                                   "-c", s, "-o", o]
+            if ptxas_verbose:
+                cmd.insert(1, "-Xptxas=-v")
+            jobs.append(cmd)
+    outs = []
+    if jobs:
+        with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 1))) as ex:
+            outs = list(ex.map(_run, jobs))
+    if verbose or ptxas_verbose:
+        for o in outs:
+            if o.strip():
+                print(o)
+    if jobs or not os.path.exists(LIB):
+        _run([NVCC] + ARCH + ["-shared", "-cudart", "shared", "-o", LIB] + objs
+             + ["-Xlinker", "-rpath=" + os.path.join(CUDA_HOME, "lib64")])
+    return LIB
+
+
+if __name__ == "__main__":
+    build(verbose=True, ptxas_verbose="-v" in sys.argv)
+    print(LIB)

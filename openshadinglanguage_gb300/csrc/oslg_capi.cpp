@@ -1,0 +1,377 @@
+// C ABI over the host model (oslg_host.h), the lowering (oslg_lower.cpp) and
+// the device interpreter (oslg_kernels.cu). Every entry point returns an int
+// status and leaves a message in oslg_last_error(); no C++ exception crosses
+// the boundary (the reference reports through bool returns and an
+// ErrorHandler, src/liboslexec/context.cpp:443-451).
+#include <cstring>
+#include <exception>
+#include <new>
+
+#include "../../include/oslg.h"
+#include "oslg_exec.h"
+#include "oslg_host.h"
+
+struct oslg_system {
+    oslg::ShadingSystem ss;
+    oslg::DeviceState dev;
+    oslg::LaunchConfig launch;
+    std::string err;
+    std::vector<oslg::InstanceParam> pending_params;  // Parameter() before Shader()
+};
+
+struct oslg_group {
+    oslg::ShaderGroup g;
+};
+
+namespace oslg {
+
+ShadingSystem::ShadingSystem() {
+    // closure ids follow the testrender registration order
+    // (src/testrender/shading.h:25-61 ClosureIDs)
+    static const char* names[] = { "emission", "background", "diffuse", "oren_nayar", "translucent",
+                                   "phong", "ward", "microfacet", "reflection", "refraction",
+                                   "transparent", "holdout" };
+    for (int i = 0; i < (int)(sizeof(names) / sizeof(names[0])); ++i) closure_ids[names[i]] = i + 1;
+}
+
+bool ShadingSystem::load_memory_compiled_shader(const std::string& name, const std::string& oso) {
+    auto m = std::make_shared<ShaderMaster>();
+    std::string err;
+    if (!parse_oso(oso, *m, err)) return error("parse of " + name + " failed: " + err);
+    std::lock_guard<std::mutex> lock(mutex);
+    masters[name] = m;
+    return true;
+}
+
+std::shared_ptr<ShaderMaster> ShadingSystem::find_master(const std::string& name) {
+    std::lock_guard<std::mutex> lock(mutex);
+    auto it = masters.find(name);
+    return it == masters.end() ? nullptr : it->second;
+}
+
+int ShaderGroup::find_layer(const std::string& n) const {
+    for (size_t i = 0; i < layers.size(); ++i)
+        if (layers[i].layername == n) return (int)i;
+    return -1;
+}
+
+}  // namespace oslg
+
+namespace {
+
+using namespace oslg;
+
+int fail(oslg_system* sys, int code, const std::string& msg) {
+    if (sys) sys->err = msg;
+    return code;
+}
+
+bool typedesc_to_spec(const oslg_typedesc& t, TypeSpec& ts) {
+    ts = TypeSpec();
+    ts.arraylen = t.arraylen;
+    if (t.basetype == OSLG_BASE_INT32) ts.base = BT_INT;
+    else if (t.basetype == OSLG_BASE_STRING) ts.base = BT_STRING;
+    else if (t.basetype == OSLG_BASE_FLOAT) {
+        if (t.aggregate == OSLG_AGG_VEC3) {
+            ts.base = BT_TRIPLE;
+            ts.vecsem = t.vecsemantics == OSLG_VEC_COLOR ? VS_COLOR
+                      : t.vecsemantics == OSLG_VEC_POINT ? VS_POINT
+                      : t.vecsemantics == OSLG_VEC_NORMAL ? VS_NORMAL : VS_VECTOR;
+        } else if (t.aggregate == OSLG_AGG_MATRIX44) {
+            ts.base = BT_MATRIX;
+        } else {
+            ts.base = BT_FLOAT;
+        }
+    } else {
+        return false;
+    }
+    return true;
+}
+
+template <class F> int guarded(oslg_system* sys, F&& f) {
+    try {
+        return f();
+    } catch (const std::bad_alloc&) {
+        return fail(sys, OSLG_ERR_ARG, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(sys, OSLG_ERR_ARG, e.what());
+    } catch (...) {
+        return fail(sys, OSLG_ERR_ARG, "unknown C++ exception");
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int oslg_create_system(oslg_system** out) {
+    if (!out) return OSLG_ERR_ARG;
+    try {
+        *out = new oslg_system();
+    } catch (...) {
+        return OSLG_ERR_ARG;
+    }
+    return OSLG_OK;
+}
+
+int oslg_destroy_system(oslg_system* sys) {
+    if (!sys) return OSLG_ERR_ARG;
+    if (sys->dev.gheap) device_free(sys->dev.gheap);
+    if (sys->dev.d_status) device_free(sys->dev.d_status);
+    delete sys;
+    return OSLG_OK;
+}
+
+int oslg_attribute_int(oslg_system* sys, const char* name, int value) {
+    if (!sys || !name) return OSLG_ERR_ARG;
+    std::string n(name);
+    if (n == "max_closure_components") sys->ss.opts.max_closure_components = value;
+    else if (n == "max_closure_terms") sys->ss.opts.max_closure_terms = value;
+    else if (n == "gpu_block") sys->launch.block = value;
+    else if (n == "gpu_points_per_thread") sys->launch.points_per_thread = value;
+    else if (n == "gpu_heap_placement") sys->launch.heap_smem = value;
+    else if (n == "gpu_grid") sys->launch.grid = value;
+    else if (n == "debug") sys->ss.opts.debug = value;
+    else return fail(sys, OSLG_ERR_ARG, "unknown attribute '" + n + "'");
+    if (sys->ss.opts.max_closure_terms > 0xFFFF || sys->ss.opts.max_closure_components > 0xFFFF)
+        return fail(sys, OSLG_ERR_ARG, "closure pool capacity must stay below 65536");
+    return OSLG_OK;
+}
+
+int oslg_register_closure(oslg_system* sys, const char* name, int id) {
+    if (!sys || !name) return OSLG_ERR_ARG;
+    sys->ss.closure_ids[name] = id;
+    return OSLG_OK;
+}
+
+int oslg_load_memory_compiled_shader(oslg_system* sys, const char* shadername, const char* oso_text) {
+    if (!sys || !shadername || !oso_text) return OSLG_ERR_ARG;
+    return guarded(sys, [&]() {
+        if (!sys->ss.load_memory_compiled_shader(shadername, oso_text))
+            return fail(sys, OSLG_ERR_PARSE, sys->ss.last_error);
+        return OSLG_OK;
+    });
+}
+
+const char* oslg_last_error(oslg_system* sys) { return sys ? sys->err.c_str() : "null system"; }
+
+int oslg_shader_group_begin(oslg_system* sys, const char* groupname, oslg_group** out) {
+    if (!sys || !out) return OSLG_ERR_ARG;
+    return guarded(sys, [&]() {
+        oslg_group* g = new oslg_group();
+        g->g.name = groupname ? groupname : "";
+        sys->pending_params.clear();
+        *out = g;
+        return OSLG_OK;
+    });
+}
+
+int oslg_parameter(oslg_system* sys, oslg_group* group, const char* name, oslg_typedesc type,
+                   const void* value, int lockgeom) {
+    if (!sys || !group || !name || !value) return OSLG_ERR_ARG;
+    return guarded(sys, [&]() {
+        if (group->g.ended) return fail(sys, OSLG_ERR_STATE, "Parameter() after ShaderGroupEnd");
+        InstanceParam p;
+        p.name = name;
+        p.lockgeom = lockgeom != 0;
+        if (!typedesc_to_spec(type, p.type)) return fail(sys, OSLG_ERR_ARG, "unsupported parameter type");
+        int elems = type.arraylen > 0 ? type.arraylen : 1;
+        if (p.type.base == BT_STRING) {
+            const char* const* sv = static_cast<const char* const*>(value);
+            for (int i = 0; i < elems; ++i) p.svals.push_back(sv[i] ? sv[i] : "");
+        } else if (p.type.base == BT_INT) {
+            const int* iv = static_cast<const int*>(value);
+            for (int i = 0; i < elems; ++i) p.fvals.push_back((float)iv[i]);
+        } else {
+            const float* fv = static_cast<const float*>(value);
+            int n = elems * p.type.ncomp();
+            for (int i = 0; i < n; ++i) p.fvals.push_back(fv[i]);
+        }
+        sys->pending_params.push_back(p);
+        return OSLG_OK;
+    });
+}
+
+int oslg_shader(oslg_system* sys, oslg_group* group, const char* shaderusage, const char* shadername,
+                const char* layername) {
+    if (!sys || !group || !shadername) return OSLG_ERR_ARG;
+    return guarded(sys, [&]() {
+        if (group->g.ended) return fail(sys, OSLG_ERR_STATE, "Shader() after ShaderGroupEnd");
+        auto m = sys->ss.find_master(shadername);
+        if (!m) return fail(sys, OSLG_ERR_ARG, std::string("shader '") + shadername + "' is not loaded");
+        Layer L;
+        L.master = m;
+        L.usage = shaderusage ? shaderusage : "surface";
+        L.layername = (layername && *layername) ? layername : m->name;
+        for (const InstanceParam& p : sys->pending_params) {
+            int si = m->find_symbol(p.name);
+            if (si < 0 || (m->symbols[si].kind != SK_PARAM && m->symbols[si].kind != SK_OPARAM))
+                return fail(sys, OSLG_ERR_ARG, "shader '" + m->name + "' has no parameter '" + p.name + "'");
+            InstanceParam q = p;
+            // keep the declared type (e.g. a float value for a color param broadcasts)
+            const TypeSpec& decl = m->symbols[si].type;
+            if (q.type.base == BT_FLOAT && decl.base == BT_TRIPLE && q.fvals.size() == 1)
+                q.fvals = { q.fvals[0], q.fvals[0], q.fvals[0] };
+            q.type = decl;
+            L.params.push_back(q);
+        }
+        sys->pending_params.clear();
+        group->g.layers.push_back(L);
+        return OSLG_OK;
+    });
+}
+
+int oslg_connect_shaders(oslg_system* sys, oslg_group* group, const char* srclayer, const char* srcparam,
+                         const char* dstlayer, const char* dstparam) {
+    if (!sys || !group || !srclayer || !srcparam || !dstlayer || !dstparam) return OSLG_ERR_ARG;
+    return guarded(sys, [&]() {
+        ShaderGroup& g = group->g;
+        int s = g.find_layer(srclayer), d = g.find_layer(dstlayer);
+        if (s < 0 || d < 0) return fail(sys, OSLG_ERR_ARG, "ConnectShaders: unknown layer");
+        if (s >= d) return fail(sys, OSLG_ERR_ARG, "ConnectShaders: source layer must precede destination");
+        if (g.layers[s].master->find_symbol(srcparam) < 0)
+            return fail(sys, OSLG_ERR_ARG, std::string("ConnectShaders: no source param ") + srcparam);
+        int di = g.layers[d].master->find_symbol(dstparam);
+        if (di < 0 || g.layers[d].master->symbols[di].kind != SK_PARAM)
+            return fail(sys, OSLG_ERR_ARG, std::string("ConnectShaders: no input param ") + dstparam);
+        g.layers[d].connections.push_back({ s, srcparam, dstparam });
+        return OSLG_OK;
+    });
+}
+
+int oslg_shader_group_end(oslg_system* sys, oslg_group* group) {
+    if (!sys || !group) return OSLG_ERR_ARG;
+    if (group->g.layers.empty()) return fail(sys, OSLG_ERR_STATE, "ShaderGroupEnd on an empty group");
+    group->g.ended = true;
+    return OSLG_OK;
+}
+
+int oslg_group_renderer_outputs(oslg_system* sys, oslg_group* group, const char** names, int n) {
+    if (!sys || !group || (n > 0 && !names)) return OSLG_ERR_ARG;
+    return guarded(sys, [&]() {
+        group->g.renderer_outputs.clear();
+        for (int i = 0; i < n; ++i) group->g.renderer_outputs.push_back(names[i]);
+        return OSLG_OK;
+    });
+}
+
+int oslg_add_symlocs(oslg_system* sys, oslg_group* group, const oslg_symloc* locs, int n) {
+    if (!sys || !group || (n > 0 && !locs)) return OSLG_ERR_ARG;
+    return guarded(sys, [&]() {
+        for (int i = 0; i < n; ++i) {
+            SymLoc sl;
+            if (!locs[i].name) return fail(sys, OSLG_ERR_ARG, "symloc without a name");
+            sl.name = locs[i].name;
+            if (!typedesc_to_spec(locs[i].type, sl.type) && locs[i].type.basetype != 0)
+                return fail(sys, OSLG_ERR_ARG, "symloc type not supported");
+            sl.derivs = locs[i].derivs != 0;
+            sl.arena = (SymArena)locs[i].arena;
+            sl.offset = locs[i].offset;
+            sl.stride = locs[i].stride;
+            if (sl.offset < 0 || (sl.offset & 3) || (sl.stride & 3))
+                return fail(sys, OSLG_ERR_ARG, "symloc offset and stride must be non-negative multiples of 4 bytes");
+            group->g.symlocs.push_back(sl);
+        }
+        std::lock_guard<std::mutex> lock(group->g.mutex);
+        group->g.compiled.reset();  // placement changed: lower again
+        return OSLG_OK;
+    });
+}
+
+static int ensure_compiled(oslg_system* sys, oslg_group* group, bool upload) {
+    ShaderGroup& g = group->g;
+    if (!g.ended) return fail(sys, OSLG_ERR_STATE, "group used before ShaderGroupEnd");
+    std::lock_guard<std::mutex> lock(g.mutex);
+    if (!g.compiled) {
+        auto cg = std::make_unique<CompiledGroup>();
+        std::string err;
+        if (!lower_group(sys->ss, g, *cg, err)) return fail(sys, OSLG_ERR_LOWER, "group '" + g.name + "': " + err);
+        g.compiled = std::move(cg);
+    }
+    if (upload && !g.compiled->d_blob) {
+        std::string err;
+        int rc = device_init(sys->dev, &err);
+        if (rc != OSLG_OK) return fail(sys, rc, err);
+        rc = device_upload_program(g.compiled->blob.data(), g.compiled->blob.size(), &g.compiled->d_blob, &err);
+        if (rc != OSLG_OK) return fail(sys, rc, err);
+        g.compiled->device = sys->dev.device;
+    }
+    return OSLG_OK;
+}
+
+int oslg_optimize_group(oslg_system* sys, oslg_group* group) {
+    if (!sys || !group) return OSLG_ERR_ARG;
+    return guarded(sys, [&]() { return ensure_compiled(sys, group, false); });
+}
+
+int oslg_release_group(oslg_system* sys, oslg_group* group) {
+    if (!group) return OSLG_ERR_ARG;
+    if (group->g.compiled && group->g.compiled->d_blob) device_free(group->g.compiled->d_blob);
+    delete group;
+    (void)sys;
+    return OSLG_OK;
+}
+
+int oslg_group_program(oslg_system* sys, oslg_group* group, void* buf, size_t cap, size_t* size) {
+    if (!sys || !group) return OSLG_ERR_ARG;
+    return guarded(sys, [&]() {
+        int rc = ensure_compiled(sys, group, false);
+        if (rc != OSLG_OK) return rc;
+        const std::vector<uint8_t>& b = group->g.compiled->blob;
+        if (size) *size = b.size();
+        if (buf) std::memcpy(buf, b.data(), std::min(cap, b.size()));
+        return OSLG_OK;
+    });
+}
+
+int oslg_execute_batch(oslg_system* sys, oslg_group* group, int64_t npoints, const oslg_shaderglobals* globals,
+                       void* userdata_base, void* output_base, void* stream) {
+    if (!sys || !group || !globals || npoints < 0) return OSLG_ERR_ARG;
+    return guarded(sys, [&]() {
+        int rc = ensure_compiled(sys, group, true);
+        if (rc != OSLG_OK) return rc;
+        std::string err;
+        rc = device_execute(sys->dev, group->g.compiled->header, group->g.compiled->d_blob, npoints, *globals,
+                            userdata_base, output_base, stream, sys->launch, &err);
+        if (rc != OSLG_OK) return fail(sys, rc, err);
+        return OSLG_OK;
+    });
+}
+
+int oslg_execute_batch_sync(oslg_system* sys, oslg_group* group, int64_t npoints,
+                            const oslg_shaderglobals* globals, void* userdata_base, void* output_base,
+                            void* stream) {
+    int rc = oslg_execute_batch(sys, group, npoints, globals, userdata_base, output_base, stream);
+    if (rc != OSLG_OK) return rc;
+    uint32_t bits = 0;
+    std::string err;
+    rc = device_read_status(sys->dev, stream, &bits, &err);
+    if (rc != OSLG_OK) return fail(sys, rc, err);
+    if (bits) {
+        std::string m = "kernel status:";
+        if (bits & ST_CLOSURE_OVERFLOW) m += " closure-arena-overflow";
+        if (bits & ST_BAD_OPCODE) m += " bad-opcode";
+        if (bits & ST_ARRAY_BOUNDS) m += " index-out-of-range";
+        if (bits & ST_TIMEOUT) m += " loop-iteration-limit";
+        return fail(sys, OSLG_ERR_DEVICE, m);
+    }
+    return OSLG_OK;
+}
+
+int oslg_device_status(oslg_system* sys, uint32_t* bits) {
+    if (!sys || !bits) return OSLG_ERR_ARG;
+    std::string err;
+    int rc = device_read_status(sys->dev, nullptr, bits, &err);
+    if (rc != OSLG_OK) return fail(sys, rc, err);
+    return OSLG_OK;
+}
+
+int oslg_set_launch(oslg_system* sys, int block, int points_per_thread, int heap_smem) {
+    if (!sys) return OSLG_ERR_ARG;
+    if (block > 0) sys->launch.block = block;
+    if (points_per_thread > 0) sys->launch.points_per_thread = points_per_thread;
+    sys->launch.heap_smem = heap_smem;
+    return OSLG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,42 @@
+// Host-callable launch interface of the device interpreter (oslg_kernels.cu).
+#pragma once
+#include <cstdint>
+#include <string>
+
+#include "../../include/oslg.h"
+#include "oslg_program.h"
+
+namespace oslg {
+
+struct LaunchConfig {
+    int block = 256;           // threads per CTA
+    int points_per_thread = 1; // points each thread interleaves
+    int heap_smem = -1;        // 1 shared-memory heap, 0 HBM scratch heap, -1 auto
+    int grid = 0;              // 0: as many CTAs as the point count needs
+};
+
+// Per-device executor state: scratch heap, status word.
+struct DeviceState {
+    int device = -1;
+    int sm_count = 0;
+    size_t smem_optin = 0;
+    float* gheap = nullptr;
+    size_t gheap_bytes = 0;
+    uint32_t* d_status = nullptr;
+};
+
+// Upload a program blob to the device (returns device pointer).
+int device_upload_program(const void* blob, size_t bytes, void** d_blob, std::string* err);
+void device_free(void* p);
+
+// Enqueue one plain per-group launch over [0, npoints).
+int device_execute(DeviceState& ds, const ProgramHeader& hdr, const void* d_blob, int64_t npoints,
+                   const oslg_shaderglobals& G, void* userdata, void* outputs, void* stream,
+                   const LaunchConfig& cfg, std::string* err);
+
+// Read-and-clear the device status word (synchronises the stream).
+int device_read_status(DeviceState& ds, void* stream, uint32_t* bits, std::string* err);
+
+int device_init(DeviceState& ds, std::string* err);
+
+}  // namespace oslg

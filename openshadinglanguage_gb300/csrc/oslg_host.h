@@ -1,0 +1,171 @@
+// Host-side model of OSL shader masters, groups and the shading system,
+// kept to the shape of the reference API so a renderer written against
+// ShadingSystem / ShaderGroup can drive this executor:
+//   ShadingSystem        src/include/OSL/oslexec.h:170
+//   ShaderGroupBegin/End, Parameter, Shader, ConnectShaders  oslexec.h:634-771
+//   SymLocationDesc / add_symlocs                            oslexec.h:69-105, :1075
+//   BatchedExecutor<W>::execute                              oslexec.h:982-1033
+// Masters are read from .oso text (the oslc output format; see
+// src/liboslexec/osogram.y and testsuite/*/test.oso).
+#pragma once
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "oslg_program.h"
+
+namespace oslg {
+
+enum BaseType { BT_INT, BT_FLOAT, BT_TRIPLE, BT_MATRIX, BT_STRING, BT_CLOSURE, BT_VOID };
+enum VecSem { VS_NONE, VS_POINT, VS_VECTOR, VS_NORMAL, VS_COLOR };
+
+struct TypeSpec {
+    BaseType base = BT_FLOAT;
+    VecSem vecsem = VS_NONE;
+    int arraylen = 0;  // 0: scalar, >0 fixed array, -1 unsized
+    bool is_array() const { return arraylen != 0; }
+    int ncomp() const {
+        switch (base) {
+        case BT_TRIPLE: return 3;
+        case BT_MATRIX: return 16;
+        case BT_VOID: return 0;
+        default: return 1;
+        }
+    }
+    int elems() const { return arraylen > 0 ? arraylen : 1; }
+    bool is_float_based() const { return base == BT_FLOAT || base == BT_TRIPLE || base == BT_MATRIX; }
+    bool derivable() const { return base == BT_FLOAT || base == BT_TRIPLE; }
+    uint32_t tclass() const {
+        switch (base) {
+        case BT_INT: return TC_INT;
+        case BT_TRIPLE: return TC_TRIPLE;
+        case BT_MATRIX: return TC_MATRIX;
+        case BT_CLOSURE: return TC_CLOSURE;
+        case BT_STRING: return TC_STRING;
+        default: return TC_FLOAT;
+        }
+    }
+    std::string str() const;
+};
+bool parse_typespec(const std::string& tok1, const std::string& tok2, TypeSpec& ts, int& consumed);
+
+enum SymKind { SK_PARAM, SK_OPARAM, SK_GLOBAL, SK_LOCAL, SK_TEMP, SK_CONST };
+
+// Symbol (src/liboslexec/osl_pvt.h:474)
+struct Symbol {
+    std::string name;
+    SymKind kind = SK_LOCAL;
+    TypeSpec type;
+    std::vector<float> fdefault;       // numeric defaults (ints stored as values)
+    std::vector<std::string> sdefault; // string defaults
+    bool lockgeom = true;              // [[ int lockgeom = 0 ]] makes it varying
+    bool has_init_ops = false;
+    int initbegin = 0, initend = 0;    // op range of the default-value code
+};
+
+// Opcode (src/liboslexec/osl_pvt.h:955)
+struct OsoOp {
+    std::string name;
+    std::vector<int> args;   // symbol indices
+    std::vector<int> jumps;  // absolute op indices
+    std::string argrw;
+    int line = 0;
+};
+
+// ShaderMaster (src/liboslexec/oslexec_pvt.h:409)
+struct ShaderMaster {
+    std::string name;
+    std::string shadertype;
+    std::vector<Symbol> symbols;
+    std::vector<OsoOp> ops;
+    int maincodebegin = 0, maincodeend = 0;
+    int find_symbol(const std::string& n) const;
+};
+bool parse_oso(const std::string& text, ShaderMaster& m, std::string& err);
+
+struct InstanceParam {
+    std::string name;
+    TypeSpec type;
+    std::vector<float> fvals;
+    std::vector<std::string> svals;
+    bool lockgeom = true;
+};
+
+struct Connection {
+    int srclayer;
+    std::string srcparam;
+    std::string dstparam;
+};
+
+// ShaderInstance (oslexec_pvt.h:1231)
+struct Layer {
+    std::string layername;
+    std::string usage;
+    std::shared_ptr<ShaderMaster> master;
+    std::vector<InstanceParam> params;
+    std::vector<Connection> connections;  // inbound connections to this layer
+};
+
+// SymLocationDesc (oslexec.h:69-105)
+enum SymArena { ARENA_UNKNOWN = 0, ARENA_HEAP = 1, ARENA_OUTPUTS = 2, ARENA_USERDATA = 3 };
+struct SymLoc {
+    std::string name;   // "layer.sym" or "sym"
+    TypeSpec type;
+    bool derivs = false;
+    SymArena arena = ARENA_OUTPUTS;
+    int64_t offset = 0;
+    int64_t stride = 0;
+};
+
+// A lowered group ready to run: the op program plus a serialized blob the
+// device (or a checker) consumes.
+struct CompiledGroup {
+    std::vector<uint8_t> blob;   // ProgramHeader + ops + const pool
+    ProgramHeader header{};
+    std::vector<std::string> op_names;  // reference op each device op came from
+    void* d_blob = nullptr;             // device copy (owned by the executor)
+    int device = -1;
+};
+
+// ShaderGroup (oslexec_pvt.h:1777)
+struct ShaderGroup {
+    std::string name;
+    std::vector<Layer> layers;
+    std::vector<std::string> renderer_outputs;
+    std::vector<SymLoc> symlocs;
+    bool ended = false;
+    std::mutex mutex;  // lowering happens once, under this lock
+    std::unique_ptr<CompiledGroup> compiled;
+    int find_layer(const std::string& n) const;
+};
+
+struct SystemOptions {
+    int debug = 0;
+    int max_closure_components = 8;
+    int max_closure_terms = 16;
+    int heap_in_smem = -1;  // -1 auto
+    int threads_per_block = 256;
+    int points_per_thread = 1;
+};
+
+class ShadingSystem {
+public:
+    std::map<std::string, std::shared_ptr<ShaderMaster>> masters;
+    std::map<std::string, int> closure_ids;  // registered closure name -> id
+    SystemOptions opts;
+    std::string last_error;
+    std::mutex mutex;
+
+    ShadingSystem();
+    bool load_memory_compiled_shader(const std::string& name, const std::string& oso);
+    std::shared_ptr<ShaderMaster> find_master(const std::string& name);
+    bool error(const std::string& msg) { last_error = msg; return false; }
+};
+
+// Lowering entry point: group -> device op program (oslg_lower.cpp).
+bool lower_group(ShadingSystem& ss, ShaderGroup& g, CompiledGroup& out, std::string& err);
+
+}  // namespace oslg

@@ -1,0 +1,864 @@
+// Lowering of an optimized ShaderGroup into the device op program.
+//
+// What the reference does at this point is JIT the group: BatchedAnalysis
+// (src/liboslexec/batched_analysis.cpp:1326, :2882) decides which symbols
+// are varying and how control flow is masked, the RuntimeOptimizer marks
+// which symbols carry derivatives (runtimeoptimize.cpp:3218-3234), and
+// BatchedBackendLLVM lays out the SoA groupdata heap
+// (batched_llvm_instance.cpp:918-1054) and emits one masked function per
+// layer. Here the same decisions are made once on the host and written out
+// as a compact op stream:
+//   * derivative marking: a symbol carries [val,dx,dy] if a renderer output
+//     asks for derivatives or a deriv-consuming op (Dx/Dy/area/filterwidth)
+//     reads it, propagated backwards through every op whose result
+//     derivatives depend on its inputs;
+//   * constant pooling: const symbols and parameters that no op writes and
+//     nothing binds (no connection, no userdata) are uniform values;
+//   * layout: everything else gets heap slots ([val][dx][dy] blocks);
+//   * control flow: if/loops become mask ops (OP_IF/ELSE/ENDIF, OP_LOOP_*).
+//   * layers run in group order; a connection copies the upstream output
+//     into the downstream parameter before that layer's body.
+#include <algorithm>
+#include <cstring>
+#include <functional>
+#include <set>
+#include <sstream>
+
+#include "oslg_host.h"
+
+namespace oslg {
+
+namespace {
+
+struct GSym {
+    int layer = -1;
+    std::string name;
+    TypeSpec type;
+    SymKind kind = SK_LOCAL;
+    bool derivs = false;
+    bool is_const = false;
+    std::vector<float> cval;
+    std::vector<std::string> sval;
+    int global_id = -1;
+    int slot = -1;
+    bool written = false;
+    bool referenced = false;
+};
+
+struct LOp {
+    std::string name;
+    std::vector<int> args;   // gsym indices
+    std::vector<int> jumps;  // LOp indices
+    int layer = -1;
+    bool param_init = false;     // assign that sets a parameter to its value
+    int param_gsym = -1;
+    int64_t imm[4] = { 0, 0, 0, 0 };
+    std::string argrw;
+};
+
+const char* kGlobalNames[G_COUNT] = { "P", "dPdx", "dPdy", "dPdz", "I", "dIdx", "dIdy", "N", "Ng",
+                                      "u", "dudx", "dudy", "v", "dvdx", "dvdy", "dPdu", "dPdv",
+                                      "time", "dtime", "dPdtime", "Ps", "dPsdx", "dPsdy",
+                                      "surfacearea" };
+
+int global_id_of(const std::string& n) {
+    for (int i = 0; i < G_COUNT; ++i)
+        if (n == kGlobalNames[i]) return i;
+    return -1;
+}
+
+// Globals whose derivatives the caller supplies (dPdx/dPdy style fields).
+bool global_has_derivs(int gid) {
+    return gid == G_P || gid == G_I || gid == G_U || gid == G_V || gid == G_PS;
+}
+
+uint32_t string_hash(const std::string& s) {
+    // FNV-1a: strings only need stable equality on the device
+    uint32_t h = 2166136261u;
+    for (unsigned char c : s) { h ^= c; h *= 16777619u; }
+    return h;
+}
+
+// Ops whose result derivatives are a function of their inputs' derivatives.
+const std::set<std::string>& deriv_propagating_ops() {
+    static const std::set<std::string> s = {
+        "assign", "add", "sub", "mul", "div", "neg", "compref", "compassign", "point", "vector",
+        "normal", "color", "aref", "aassign", "sin", "cos", "tan", "asin", "acos", "atan", "atan2",
+        "sinh", "cosh", "tanh", "exp", "exp2", "expm1", "log", "log2", "log10", "pow", "sqrt",
+        "inversesqrt", "cbrt", "abs", "fabs", "mix", "clamp", "min", "max", "smoothstep", "select",
+        "dot", "cross", "length", "normalize", "distance", "transform", "transformv", "transformn",
+        "noise", "snoise", "pnoise", "psnoise", "spline", "mod", "fmod", "luminance", "radians",
+        "degrees", "erf", "erfc" };
+    return s;
+}
+
+struct Lowerer {
+    ShadingSystem& ss;
+    ShaderGroup& g;
+    std::string& err;
+    std::vector<GSym> syms;
+    std::vector<LOp> lops;
+    std::map<std::pair<int, int>, int> layer_sym;  // (layer, master sym) -> gsym
+    std::map<std::string, int> globals;
+    std::vector<int> const_cache_f;                 // unused bookkeeping
+    // outputs
+    std::vector<Op> ops;
+    std::vector<std::string> op_names;
+    std::vector<uint32_t> pool;  // constant pool words
+    uint32_t heap_top = 0;
+    uint32_t max_depth = 0;
+    bool uses_closures = false;
+
+    Lowerer(ShadingSystem& s, ShaderGroup& gg, std::string& e) : ss(s), g(gg), err(e) {}
+
+    bool fail(const std::string& m) { err = m; return false; }
+
+    int add_sym(const GSym& s) { syms.push_back(s); return (int)syms.size() - 1; }
+
+    int const_float(float v) {
+        GSym s; s.name = "$c"; s.type.base = BT_FLOAT; s.kind = SK_CONST; s.is_const = true;
+        s.cval = { v };
+        return add_sym(s);
+    }
+    int const_int(int v) {
+        GSym s; s.name = "$ci"; s.type.base = BT_INT; s.kind = SK_CONST; s.is_const = true;
+        s.cval = { (float)v };
+        return add_sym(s);
+    }
+
+    int global_sym(const std::string& name, const TypeSpec& ts) {
+        auto it = globals.find(name);
+        if (it != globals.end()) return it->second;
+        GSym s;
+        s.name = name; s.type = ts; s.kind = SK_GLOBAL; s.global_id = global_id_of(name);
+        int id = add_sym(s);
+        globals[name] = id;
+        return id;
+    }
+
+    // gsym for master symbol `msi` of layer `li`
+    int sym_of(int li, int msi) {
+        auto key = std::make_pair(li, msi);
+        auto it = layer_sym.find(key);
+        if (it != layer_sym.end()) return it->second;
+        const Symbol& ms = g.layers[li].master->symbols[msi];
+        int id;
+        if (ms.kind == SK_GLOBAL) {
+            id = global_sym(ms.name, ms.type);
+        } else {
+            GSym s;
+            s.layer = li; s.name = ms.name; s.type = ms.type; s.kind = ms.kind;
+            if (ms.kind == SK_CONST) {
+                s.is_const = true;
+                s.cval = ms.fdefault;
+                s.sval = ms.sdefault;
+            }
+            id = add_sym(s);
+        }
+        layer_sym[key] = id;
+        return id;
+    }
+
+    const SymLoc* find_symloc(int li, const std::string& name, SymArena arena) {
+        const std::string& lname = g.layers[li].layername;
+        for (const SymLoc& sl : g.symlocs) {
+            if (sl.arena != arena) continue;
+            if (sl.name == lname + "." + name) return &sl;
+        }
+        for (const SymLoc& sl : g.symlocs) {
+            if (sl.arena != arena) continue;
+            if (sl.name == name) return &sl;
+        }
+        return nullptr;
+    }
+
+    // Copy master ops [b,e) of layer li into lops, remapping jumps.
+    void copy_section(int li, int b, int e) {
+        const ShaderMaster& m = *g.layers[li].master;
+        int base = (int)lops.size();
+        for (int k = b; k < e; ++k) {
+            const OsoOp& mo = m.ops[k];
+            LOp op;
+            op.name = mo.name;
+            op.layer = li;
+            op.argrw = mo.argrw;
+            for (int a : mo.args) op.args.push_back(sym_of(li, a));
+            for (int j : mo.jumps) op.jumps.push_back(base + (j - b));
+            if (op.name == "end") op.name = "nop";
+            lops.push_back(op);
+        }
+    }
+
+    bool build_lops() {
+        for (int li = 0; li < (int)g.layers.size(); ++li) {
+            Layer& L = g.layers[li];
+            const ShaderMaster& m = *L.master;
+            for (int msi = 0; msi < (int)m.symbols.size(); ++msi) {
+                const Symbol& ms = m.symbols[msi];
+                if (ms.kind != SK_PARAM && ms.kind != SK_OPARAM) continue;
+                int gs = sym_of(li, msi);
+                // 1. connection into this parameter
+                const Connection* conn = nullptr;
+                for (const Connection& c : L.connections)
+                    if (c.dstparam == ms.name) conn = &c;
+                if (conn) {
+                    int srcm = g.layers[conn->srclayer].master->find_symbol(conn->srcparam);
+                    if (srcm < 0)
+                        return fail("connection source " + conn->srcparam + " not found in layer "
+                                    + g.layers[conn->srclayer].layername);
+                    int src = sym_of(conn->srclayer, srcm);
+                    LOp op; op.name = "assign"; op.layer = li; op.args = { gs, src };
+                    lops.push_back(op);
+                    continue;
+                }
+                // instance value / lockgeom
+                const InstanceParam* ip = nullptr;
+                for (const InstanceParam& p : L.params)
+                    if (p.name == ms.name) ip = &p;
+                bool lockgeom = ip ? ip->lockgeom : ms.lockgeom;
+                // 2. userdata binding for varying (lockgeom=0) parameters
+                if (!lockgeom) {
+                    const SymLoc* sl = find_symloc(li, ms.name, ARENA_USERDATA);
+                    if (sl) {
+                        LOp op; op.name = "__load_userdata"; op.layer = li; op.args = { gs };
+                        op.imm[0] = sl->offset; op.imm[1] = sl->stride;
+                        op.imm[2] = sl->derivs ? 1 : 0;
+                        lops.push_back(op);
+                        continue;
+                    }
+                }
+                // 3. explicit instance value
+                if (ip) {
+                    GSym c; c.name = "$pv"; c.type = ms.type; c.kind = SK_CONST; c.is_const = true;
+                    c.cval = ip->fvals; c.sval = ip->svals;
+                    int cs = add_sym(c);
+                    LOp op; op.name = "assign"; op.layer = li; op.args = { gs, cs };
+                    op.param_init = lockgeom; op.param_gsym = gs;
+                    lops.push_back(op);
+                    continue;
+                }
+                // 4. default-value code
+                if (ms.has_init_ops && ms.initend > ms.initbegin) {
+                    copy_section(li, ms.initbegin, ms.initend);
+                    continue;
+                }
+                // 5. plain default
+                GSym c; c.name = "$pd"; c.type = ms.type; c.kind = SK_CONST; c.is_const = true;
+                c.cval = ms.fdefault; c.sval = ms.sdefault;
+                int cs = add_sym(c);
+                LOp op; op.name = "assign"; op.layer = li; op.args = { gs, cs };
+                op.param_init = lockgeom; op.param_gsym = gs;
+                lops.push_back(op);
+            }
+            copy_section(li, m.maincodebegin, m.maincodeend);
+            LOp le; le.name = "__layer_end"; le.layer = li;
+            lops.push_back(le);
+        }
+        // renderer outputs placed through symlocs
+        for (const SymLoc& sl : g.symlocs) {
+            if (sl.arena != ARENA_OUTPUTS) continue;
+            int gs = resolve_symloc(sl);
+            if (gs < 0) return fail("symloc '" + sl.name + "' does not name a symbol of the group");
+            LOp op; op.name = "__store_output"; op.args = { gs };
+            op.imm[0] = sl.offset; op.imm[1] = sl.stride; op.imm[2] = sl.derivs ? 1 : 0;
+            lops.push_back(op);
+        }
+        return true;
+    }
+
+    int resolve_symloc(const SymLoc& sl) {
+        std::string lname, sname = sl.name;
+        size_t dot = sl.name.find('.');
+        if (dot != std::string::npos) {
+            lname = sl.name.substr(0, dot);
+            sname = sl.name.substr(dot + 1);
+        }
+        for (int li = (int)g.layers.size() - 1; li >= 0; --li) {
+            if (!lname.empty() && g.layers[li].layername != lname) continue;
+            int msi = g.layers[li].master->find_symbol(sname);
+            if (msi >= 0) return sym_of(li, msi);
+        }
+        return -1;
+    }
+
+    // ---- analysis ----------------------------------------------------------
+    static bool writes_arg(const LOp& op, int i) {
+        if (!op.argrw.empty() && i < (int)op.argrw.size())
+            return op.argrw[i] == 'w' || op.argrw[i] == 'W';
+        static const std::set<std::string> nowrite = {
+            "if", "for", "while", "dowhile", "break", "continue", "return", "exit", "nop",
+            "useparam", "__layer_end", "__store_output", "functioncall", "functioncall_nr",
+            "printf", "warning", "error", "fprintf" };
+        if (nowrite.count(op.name)) return false;
+        if (op.name == "sincos") return i == 1 || i == 2;
+        return i == 0;
+    }
+
+    void analyze() {
+        for (const LOp& op : lops) {
+            if (op.param_init) continue;
+            for (size_t i = 0; i < op.args.size(); ++i)
+                if (writes_arg(op, (int)i)) syms[op.args[i]].written = true;
+        }
+        // parameters nobody writes and nothing binds become uniform constants
+        for (LOp& op : lops) {
+            if (!op.param_init) continue;
+            GSym& p = syms[op.param_gsym];
+            if (!p.written && !p.type.is_array() && p.type.base != BT_CLOSURE) {
+                const GSym& c = syms[op.args[1]];
+                p.is_const = true;
+                p.cval = c.cval;
+                p.sval = c.sval;
+                op.name = "nop";
+                op.args.clear();
+            }
+        }
+        // derivative seeds
+        for (const LOp& op : lops) {
+            if ((op.name == "Dx" || op.name == "Dy" || op.name == "Dz" || op.name == "area"
+                 || op.name == "filterwidth" || op.name == "calculatenormal")
+                && op.args.size() > 1)
+                mark_derivs(op.args[1]);
+            if (op.name == "__store_output" && op.imm[2]) mark_derivs(op.args[0]);
+            if (op.name == "__load_userdata" && op.imm[2]) mark_derivs(op.args[0]);
+        }
+        const auto& prop = deriv_propagating_ops();
+        bool changed = true;
+        while (changed) {
+            changed = false;
+            for (int k = (int)lops.size() - 1; k >= 0; --k) {
+                const LOp& op = lops[k];
+                if (!prop.count(op.name) || op.args.empty()) continue;
+                bool res_needs = false;
+                for (size_t i = 0; i < op.args.size(); ++i)
+                    if (writes_arg(op, (int)i) && syms[op.args[i]].derivs) res_needs = true;
+                if (!res_needs) continue;
+                for (size_t i = 0; i < op.args.size(); ++i) {
+                    if (writes_arg(op, (int)i) && op.name != "compassign" && op.name != "aassign")
+                        continue;
+                    // index operands of compref/aref/compassign/aassign carry no derivs
+                    if ((op.name == "compref" || op.name == "aref") && i == 2) continue;
+                    if ((op.name == "compassign" || op.name == "aassign") && i == 1) continue;
+                    if (op.name == "spline" && i == 1) continue;  // basis name
+                    if ((op.name == "noise" || op.name == "snoise" || op.name == "pnoise"
+                         || op.name == "psnoise")
+                        && i == 1 && syms[op.args[1]].type.base == BT_STRING)
+                        continue;
+                    int a = op.args[i];
+                    if (!syms[a].derivs && syms[a].type.derivable() && !syms[a].is_const) {
+                        syms[a].derivs = true;
+                        changed = true;
+                    }
+                }
+            }
+        }
+        for (GSym& s : syms)
+            if (s.is_const) s.derivs = false;
+    }
+
+    void mark_derivs(int s) {
+        if (syms[s].type.derivable() && !syms[s].is_const) syms[s].derivs = true;
+    }
+
+    // ---- storage -------------------------------------------------------------
+    uint32_t pool_add(const GSym& s) {
+        uint32_t off = (uint32_t)pool.size();
+        int n = s.type.ncomp() * s.type.elems();
+        if (s.type.base == BT_STRING) {
+            for (int i = 0; i < s.type.elems(); ++i) {
+                std::string v = i < (int)s.sval.size() ? s.sval[i] : std::string();
+                pool.push_back(string_hash(v));
+            }
+            return off;
+        }
+        for (int i = 0; i < n; ++i) {
+            float v = 0.0f;
+            if (!s.cval.empty()) v = s.cval[std::min<size_t>(i, s.cval.size() - 1)];
+            if (s.type.base == BT_MATRIX && s.cval.size() == 1) v = (i % 5 == 0) ? s.cval[0] : 0.0f;
+            if (s.type.base == BT_TRIPLE && s.cval.size() == 1) v = s.cval[0];
+            uint32_t w;
+            if (s.type.base == BT_INT || s.type.base == BT_CLOSURE) {
+                int iv = (int)v;
+                std::memcpy(&w, &iv, 4);
+            } else {
+                std::memcpy(&w, &v, 4);
+            }
+            pool.push_back(w);
+        }
+        return off;
+    }
+
+    void assign_storage() {
+        for (const LOp& op : lops)
+            for (int a : op.args) syms[a].referenced = true;
+        for (GSym& s : syms) {
+            if (!s.referenced) continue;
+            if (s.is_const) {
+                s.slot = (int)pool_add(s);
+                continue;
+            }
+            int n = s.type.ncomp() * s.type.elems() * (s.derivs ? 3 : 1);
+            if (s.type.base == BT_VOID) n = 0;
+            s.slot = (int)heap_top;
+            heap_top += (uint32_t)n;
+        }
+    }
+
+    uint32_t A(int gs) {
+        const GSym& s = syms[gs];
+        return arg_make((uint32_t)s.slot, s.is_const, s.derivs, s.type.tclass());
+    }
+
+    // ---- emission ------------------------------------------------------------
+    int emit(uint16_t code, std::initializer_list<uint32_t> a, const std::string& name) {
+        Op op;
+        std::memset(&op, 0, sizeof(op));
+        op.code = code;
+        int i = 0;
+        for (uint32_t v : a) {
+            if (i < 7) op.a[i++] = v;
+        }
+        op.nargs = (uint8_t)i;
+        ops.push_back(op);
+        op_names.push_back(name);
+        return (int)ops.size() - 1;
+    }
+
+    bool emit_range(int b, int e, int depth, int loopl) {
+        for (int k = b; k < e;) {
+            const LOp& op = lops[k];
+            if (op.name == "if") {
+                if (op.jumps.size() < 2) return fail("if without jump targets");
+                int je = op.jumps[0], jend = op.jumps[1];
+                if ((uint32_t)depth + 1 > max_depth) max_depth = depth + 1;
+                if (depth >= 31) return fail("control flow nested too deeply");
+                int ifop = emit(OP_IF, { A(op.args[0]), (uint32_t)depth, 0u, (uint32_t)loopl }, "if");
+                if (!emit_range(k + 1, je, depth + 1, loopl)) return false;
+                int elop = emit(OP_ELSE, { 0u, (uint32_t)depth, 0u, (uint32_t)loopl }, "if");
+                ops[ifop].a[2] = (uint32_t)elop;
+                if (!emit_range(je, jend, depth + 1, loopl)) return false;
+                int enop = emit(OP_ENDIF, { 0u, (uint32_t)depth, 0u, (uint32_t)loopl }, "if");
+                ops[elop].a[2] = (uint32_t)enop;
+                k = jend;
+                continue;
+            }
+            if (op.name == "for" || op.name == "while" || op.name == "dowhile") {
+                if (op.jumps.size() < 4) return fail(op.name + " without jump targets");
+                int jc = op.jumps[0], jb = op.jumps[1], js = op.jumps[2], jend = op.jumps[3];
+                if ((uint32_t)depth + 1 > max_depth) max_depth = depth + 1;
+                if (depth >= 31) return fail("control flow nested too deeply");
+                uint32_t ll = (uint32_t)depth + 1;  // loop level tag = its depth + 1
+                emit(OP_LOOP_BEGIN, { 0u, (uint32_t)depth, 0u, ll }, op.name);
+                if (!emit_range(k + 1, jc, depth + 1, (int)ll)) return false;
+                int jmp_body = -1;
+                if (op.name == "dowhile") jmp_body = emit(OP_JUMP, { 0u, 0u, 0u, 0u }, op.name);
+                int cond_start = (int)ops.size();
+                if (!emit_range(jc, jb, depth + 1, (int)ll)) return false;
+                int test = emit(OP_LOOP_TEST, { A(op.args[0]), (uint32_t)depth, 0u, ll }, op.name);
+                if (jmp_body >= 0) ops[jmp_body].a[2] = (uint32_t)ops.size();
+                if (!emit_range(jb, js, depth + 1, (int)ll)) return false;
+                emit(OP_LOOP_STEP, { 0u, (uint32_t)depth, 0u, ll }, op.name);
+                if (!emit_range(js, jend, depth + 1, (int)ll)) return false;
+                emit(OP_JUMP, { 0u, 0u, (uint32_t)cond_start, 0u }, op.name);
+                int endop = emit(OP_LOOP_END, { 0u, (uint32_t)depth, 0u, ll }, op.name);
+                ops[test].a[2] = (uint32_t)endop;
+                k = jend;
+                continue;
+            }
+            if (!lower_op(op, depth, loopl)) return false;
+            ++k;
+        }
+        return true;
+    }
+
+    bool lower_all() {
+        // global loads first
+        for (auto& kv : globals) {
+            const GSym& s = syms[kv.second];
+            if (!s.referenced || s.global_id < 0) {
+                if (s.referenced && s.global_id < 0)
+                    return fail("shader global '" + s.name + "' is not supported");
+                continue;
+            }
+            emit(OP_LOAD_GLOBAL, { A(kv.second), (uint32_t)s.global_id }, "global");
+        }
+        // the body of each layer is a structured range of lops
+        return emit_range(0, (int)lops.size(), 0, 0);
+    }
+
+    int tc(int gs) const { return (int)syms[gs].type.tclass(); }
+    bool is_int(int gs) const { return syms[gs].type.base == BT_INT; }
+    bool is_closure(int gs) const { return syms[gs].type.base == BT_CLOSURE; }
+    bool is_matrix(int gs) const { return syms[gs].type.base == BT_MATRIX; }
+    bool is_triple(int gs) const { return syms[gs].type.base == BT_TRIPLE; }
+    bool is_string(int gs) const { return syms[gs].type.base == BT_STRING; }
+
+    std::string const_string(int gs) const {
+        const GSym& s = syms[gs];
+        if (s.is_const && !s.sval.empty()) return s.sval[0];
+        return std::string();
+    }
+
+    bool lower_noise(const LOp& op) {
+        // noise-family ops: (result, [name], S, [T], [Speriod, [Tperiod]], [options...])
+        // name mapping follows src/liboslexec/batched_llvm_gen.cpp:6094-6146
+        bool periodic = op.name == "pnoise" || op.name == "psnoise";
+        size_t ai = 1;
+        std::string name;
+        if (op.args.size() > 1 && is_string(op.args[1])) {
+            name = const_string(op.args[1]);
+            if (name.empty() && !syms[op.args[1]].is_const)
+                return fail("noise type must be a constant string in this executor");
+            ai = 2;
+        } else {
+            name = op.name;
+        }
+        int R = op.args[0];
+        if (ai >= op.args.size()) return fail("noise op without coordinates");
+        int S = op.args[ai++];
+        int T = -1, Sp = -1, Tp = -1;
+        int dims = is_triple(S) ? 3 : 1;
+        if (periodic) {
+            if (ai + 1 < op.args.size() && !is_string(op.args[ai + 1])
+                && (syms[op.args[ai]].type.base == BT_FLOAT || is_triple(op.args[ai]))
+                && (syms[op.args[ai]].type.base == BT_FLOAT)) {
+                T = op.args[ai++];
+                ++dims;
+            }
+            if (ai < op.args.size()) Sp = op.args[ai++];
+            if ((dims == 2 || dims == 4) && ai < op.args.size()) Tp = op.args[ai++];
+        } else if (ai < op.args.size() && syms[op.args[ai]].type.base == BT_FLOAT) {
+            T = op.args[ai++];
+            ++dims;
+        }
+        uint32_t kind;
+        if (name == "perlin" || name == "snoise" || name == "psnoise") kind = NK_PERLIN;
+        else if (name == "uperlin" || name == "noise" || name == "pnoise") kind = NK_UPERLIN;
+        else if (name == "cell" || name == "cellnoise") kind = NK_CELL;
+        else if (name == "hash" || name == "hashnoise") kind = NK_HASH;
+        else if (name == "simplex" && !periodic) kind = NK_SIMPLEX;
+        else if (name == "usimplex" && !periodic) kind = NK_USIMPLEX;
+        else if (name == "gabor") kind = NK_GABOR;
+        else if (name == "null") kind = NK_NULL;
+        else if (name == "unull") kind = NK_UNULL;
+        else return fail("noise type \"" + name + "\" is unknown");
+        bool derivs = syms[R].derivs && (syms[S].derivs || (T >= 0 && syms[T].derivs));
+        if (kind == NK_CELL || kind == NK_HASH) derivs = false;
+        if (kind == NK_GABOR) {
+            // options follow as (name, value) pairs; supported subset lowered
+            // into fixed operands: anisotropic, direction, bandwidth, impulses, do_filter
+            int aniso = const_int(0), dir = -1, bw = const_float(1.0f), imp = const_float(16.0f),
+                filt = const_int(1);
+            for (; ai + 1 < op.args.size(); ai += 2) {
+                std::string on = const_string(op.args[ai]);
+                int v = op.args[ai + 1];
+                if (on == "anisotropic") aniso = v;
+                else if (on == "direction") dir = v;
+                else if (on == "bandwidth") bw = v;
+                else if (on == "impulses") imp = v;
+                else if (on == "do_filter") filt = v;
+            }
+            if (dir < 0) {
+                GSym d; d.name = "$dir"; d.type.base = BT_TRIPLE; d.type.vecsem = VS_VECTOR;
+                d.kind = SK_CONST; d.is_const = true; d.cval = { 1.0f, 0.0f, 0.0f };
+                dir = add_sym(d);
+                syms[dir].slot = (int)pool_add(syms[dir]);
+            }
+            for (int x : { aniso, bw, imp, filt })
+                if (syms[x].slot < 0) syms[x].slot = (int)pool_add(syms[x]);
+            // pack the option operands: a4 = anisotropic(int) a5 = direction a6 = bandwidth
+            // impulses and do_filter go in a second op word pair via OP_NOP carrier
+            uint32_t kw = noise_word(kind, periodic, dims, is_triple(R), true);
+            emit(OP_GABOR, { A(R), A(S), T >= 0 ? A(T) : kNoArg, kw, A(aniso), A(dir), A(bw) }, op.name);
+            emit(OP_NOP, { A(imp), A(filt), Sp >= 0 ? A(Sp) : kNoArg, Tp >= 0 ? A(Tp) : kNoArg },
+                 "gabor-options");
+            return true;
+        }
+        uint32_t kw = noise_word(kind, periodic, dims, is_triple(R), derivs);
+        emit(OP_NOISE, { A(R), A(S), T >= 0 ? A(T) : kNoArg, kw, Sp >= 0 ? A(Sp) : kNoArg,
+                         Tp >= 0 ? A(Tp) : kNoArg },
+             op.name);
+        return true;
+    }
+
+    bool lower_op(const LOp& op, int depth, int loopl) {
+        const std::string& n = op.name;
+        auto a = [&](int i) { return A(op.args[i]); };
+        size_t na = op.args.size();
+        if (n == "nop" || n == "useparam" || n == "end") return true;
+        if (n == "break") { emit(OP_BREAK, { 0u, 0u, 0u, (uint32_t)loopl }, n); return true; }
+        if (n == "continue") { emit(OP_CONTINUE, { 0u, 0u, 0u, (uint32_t)loopl }, n); return true; }
+        if (n == "return") { emit(OP_RETURN, {}, n); return true; }
+        if (n == "exit") { emit(OP_EXIT, {}, n); return true; }
+        if (n == "__layer_end") { emit(OP_LAYER_END, {}, "layer"); return true; }
+        if (n == "__load_userdata") {
+            int s = op.args[0];
+            emit(OP_LOAD_USERDATA, { a(0), (uint32_t)op.imm[0], (uint32_t)op.imm[1],
+                                     is_int(s) ? 1u : 0u },
+                 "userdata");
+            return true;
+        }
+        if (n == "__store_output") {
+            int s = op.args[0];
+            if (is_closure(s)) {
+                emit(OP_STORE_CLOSURE, { a(0), (uint32_t)op.imm[0], (uint32_t)op.imm[1],
+                                         (uint32_t)ss.opts.max_closure_terms },
+                     "output");
+                return true;
+            }
+            uint32_t flags = (op.imm[2] ? 1u : 0u) | (is_int(s) ? 2u : 0u);
+            emit(OP_STORE_OUTPUT, { a(0), (uint32_t)op.imm[0], (uint32_t)op.imm[1], flags,
+                                    (uint32_t)syms[s].type.elems() },
+                 "output");
+            return true;
+        }
+        if (n == "assign") {
+            if (na < 2) return fail("assign needs 2 args");
+            int r = op.args[0], s = op.args[1];
+            if (is_closure(r)) {
+                emit(OP_ASSIGN, { a(0), a(1), (uint32_t)syms[r].type.elems() }, n);
+                return true;
+            }
+            emit(OP_ASSIGN, { a(0), a(1), (uint32_t)std::min(syms[r].type.elems(), syms[s].type.elems()),
+                              (uint32_t)syms[r].type.elems(), (uint32_t)syms[s].type.elems() },
+                 n);
+            return true;
+        }
+        static const std::map<std::string, std::pair<uint16_t, uint16_t>> arith = {
+            { "add", { OP_ADD, OP_IADD } }, { "sub", { OP_SUB, OP_ISUB } },
+            { "mul", { OP_MUL, OP_IMUL } }, { "div", { OP_DIV, OP_IDIV } },
+            { "mod", { OP_MOD, OP_IMOD } } };
+        auto ar = arith.find(n);
+        if (ar != arith.end()) {
+            if (na < 3) return fail(n + " needs 3 args");
+            int r = op.args[0], x = op.args[1], y = op.args[2];
+            if (is_closure(r)) {
+                uses_closures = true;
+                if (n == "add") { emit(OP_CLOSURE_ADD, { a(0), a(1), a(2) }, n); return true; }
+                if (n == "mul") {
+                    if (is_closure(x)) emit(OP_CLOSURE_MUL, { a(0), a(1), a(2) }, n);
+                    else emit(OP_CLOSURE_MUL, { a(0), a(2), a(1) }, n);
+                    return true;
+                }
+                return fail("closure " + n + " is not an OSL operation");
+            }
+            if (is_int(r) && is_int(x) && is_int(y)) {
+                emit(ar->second.second, { a(0), a(1), a(2) }, n);
+                return true;
+            }
+            if ((n == "mul" || n == "div") && (is_matrix(x) || is_matrix(y)) && is_matrix(r)) {
+                emit(n == "mul" ? OP_MMUL : OP_MDIV, { a(0), a(1), a(2) }, n);
+                return true;
+            }
+            emit(ar->second.first, { a(0), a(1), a(2) }, n);
+            return true;
+        }
+        if (n == "neg") {
+            emit(is_int(op.args[0]) ? OP_INEG : OP_NEG, { a(0), a(1) }, n);
+            return true;
+        }
+        static const std::map<std::string, uint16_t> cmp = {
+            { "eq", OP_EQ }, { "neq", OP_NEQ }, { "lt", OP_LT }, { "gt", OP_GT }, { "le", OP_LE },
+            { "ge", OP_GE }, { "and", OP_AND }, { "or", OP_OR }, { "bitand", OP_BITAND },
+            { "bitor", OP_BITOR }, { "xor", OP_XOR }, { "shl", OP_SHL }, { "shr", OP_SHR } };
+        auto cm = cmp.find(n);
+        if (cm != cmp.end()) {
+            if (na < 3) return fail(n + " needs 3 args");
+            emit(cm->second, { a(0), a(1), a(2) }, n);
+            return true;
+        }
+        if (n == "compl") { emit(OP_COMPL, { a(0), a(1) }, n); return true; }
+        static const std::map<std::string, uint16_t> unary = {
+            { "floor", OP_FLOOR }, { "ceil", OP_CEIL }, { "round", OP_ROUND }, { "trunc", OP_TRUNC },
+            { "sign", OP_SIGN }, { "sqrt", OP_SQRT }, { "inversesqrt", OP_INVSQRT },
+            { "cbrt", OP_CBRT }, { "sin", OP_SIN }, { "cos", OP_COS }, { "tan", OP_TAN },
+            { "asin", OP_ASIN }, { "acos", OP_ACOS }, { "atan", OP_ATAN }, { "sinh", OP_SINH },
+            { "cosh", OP_COSH }, { "tanh", OP_TANH }, { "exp", OP_EXP }, { "exp2", OP_EXP2 },
+            { "expm1", OP_EXPM1 }, { "log", OP_LOG }, { "log2", OP_LOG2 }, { "log10", OP_LOG10 },
+            { "radians", OP_RADIANS }, { "degrees", OP_DEGREES }, { "isnan", OP_ISNAN },
+            { "isinf", OP_ISINF }, { "isfinite", OP_ISFINITE } };
+        if (n == "abs" || n == "fabs") {
+            emit(is_int(op.args[0]) ? OP_IABS : OP_ABS, { a(0), a(1) }, n);
+            return true;
+        }
+        auto un = unary.find(n);
+        if (un != unary.end()) {
+            if (na < 2) return fail(n + " needs 2 args");
+            emit(un->second, { a(0), a(1) }, n);
+            return true;
+        }
+        if (n == "pow" || n == "atan2" || n == "fmod") {
+            emit(n == "pow" ? OP_POW : n == "atan2" ? OP_ATAN2 : OP_FMOD, { a(0), a(1), a(2) }, n);
+            return true;
+        }
+        if (n == "min" || n == "max") {
+            bool ints = is_int(op.args[0]);
+            emit(n == "min" ? (ints ? OP_IMIN : OP_MIN) : (ints ? OP_IMAX : OP_MAX), { a(0), a(1), a(2) }, n);
+            return true;
+        }
+        if (n == "clamp") { emit(OP_CLAMP, { a(0), a(1), a(2), a(3) }, n); return true; }
+        if (n == "mix") { emit(OP_MIX, { a(0), a(1), a(2), a(3) }, n); return true; }
+        if (n == "select") { emit(OP_SELECT, { a(0), a(1), a(2), a(3) }, n); return true; }
+        if (n == "step") { emit(OP_STEP, { a(0), a(1), a(2) }, n); return true; }
+        if (n == "smoothstep") { emit(OP_SMOOTHSTEP, { a(0), a(1), a(2), a(3) }, n); return true; }
+        if (n == "dot") { emit(OP_DOT, { a(0), a(1), a(2) }, n); return true; }
+        if (n == "cross") { emit(OP_CROSS, { a(0), a(1), a(2) }, n); return true; }
+        if (n == "length") { emit(OP_LENGTH, { a(0), a(1) }, n); return true; }
+        if (n == "normalize") { emit(OP_NORMALIZE, { a(0), a(1) }, n); return true; }
+        if (n == "distance") { emit(OP_DISTANCE, { a(0), a(1), a(2) }, n); return true; }
+        if (n == "Dx") { emit(OP_DX, { a(0), a(1) }, n); return true; }
+        if (n == "Dy") { emit(OP_DY, { a(0), a(1) }, n); return true; }
+        if (n == "area") { emit(OP_AREA, { a(0), a(1) }, n); return true; }
+        if (n == "filterwidth") { emit(OP_FILTERWIDTH, { a(0), a(1) }, n); return true; }
+        if (n == "compref") { emit(OP_COMPREF, { a(0), a(1), a(2) }, n); return true; }
+        if (n == "compassign") { emit(OP_COMPASSIGN, { a(0), a(1), a(2) }, n); return true; }
+        if (n == "mxcompref") { emit(OP_MXCOMPREF, { a(0), a(1), a(2), a(3) }, n); return true; }
+        if (n == "mxcompassign") { emit(OP_MXCOMPASSIGN, { a(0), a(1), a(2), a(3) }, n); return true; }
+        if (n == "aref") {
+            emit(OP_AREF, { a(0), a(1), a(2), (uint32_t)syms[op.args[1]].type.elems() }, n);
+            return true;
+        }
+        if (n == "aassign") {
+            emit(OP_AASSIGN, { a(0), a(1), a(2), (uint32_t)syms[op.args[0]].type.elems() }, n);
+            return true;
+        }
+        if (n == "arraylength") {
+            int c = const_int(syms[op.args[1]].type.elems());
+            syms[c].slot = (int)pool_add(syms[c]);
+            emit(OP_ASSIGN, { a(0), A(c), 1u, 1u, 1u }, n);
+            return true;
+        }
+        if (n == "point" || n == "vector" || n == "normal" || n == "color") {
+            if (na == 4) { emit(OP_CONSTRUCT3, { a(0), a(1), a(2), a(3) }, n); return true; }
+            if (na == 2) { emit(OP_ASSIGN, { a(0), a(1), 1u, 1u, 1u }, n); return true; }
+            return fail(n + "(\"space\", ...) construction is not supported yet");
+        }
+        if (n == "matrix") {
+            int r = op.args[0];
+            if (na == 2 && !is_string(op.args[1])) {
+                emit(OP_MATRIX_DIAG, { a(0), a(1) }, n);
+                return true;
+            }
+            if (na == 17) {
+                int zero = const_float(0.0f);
+                syms[zero].slot = (int)pool_add(syms[zero]);
+                emit(OP_MATRIX_DIAG, { a(0), A(zero) }, n);
+                for (int i = 0; i < 16; ++i) {
+                    int ri = const_int(i / 4), ci = const_int(i % 4);
+                    syms[ri].slot = (int)pool_add(syms[ri]);
+                    syms[ci].slot = (int)pool_add(syms[ci]);
+                    emit(OP_MXCOMPASSIGN, { A(r), A(ri), A(ci), a(1 + i) }, n);
+                }
+                return true;
+            }
+            return fail("matrix construction from named spaces is not supported yet");
+        }
+        if (n == "transpose") { emit(OP_TRANSPOSE, { a(0), a(1) }, n); return true; }
+        if (n == "determinant") { emit(OP_DETERMINANT, { a(0), a(1) }, n); return true; }
+        if (n == "transform" || n == "transformv" || n == "transformn") {
+            // transform r M p  (matrix form); named-space forms need the renderer
+            if (na == 3 && is_matrix(op.args[1])) {
+                uint32_t kind = n == "transform" ? 0u : n == "transformv" ? 1u : 2u;
+                if (n == "transform" && syms[op.args[2]].type.vecsem == VS_VECTOR) kind = 1u;
+                if (n == "transform" && syms[op.args[2]].type.vecsem == VS_NORMAL) kind = 2u;
+                emit(OP_TRANSFORM, { a(0), a(2), a(1), kind }, n);
+                return true;
+            }
+            return fail("transform between named spaces is not supported yet");
+        }
+        if (n == "noise" || n == "snoise" || n == "pnoise" || n == "psnoise" || n == "cellnoise"
+            || n == "hashnoise")
+            return lower_noise(op);
+        if (n == "hash") {
+            emit(OP_HASH, { a(0), a(1), na > 2 ? a(2) : kNoArg }, n);
+            return true;
+        }
+        if (n == "spline") {
+            // spline r basis x [nknots] knots  (src/liboslexec/opspline.cpp)
+            if (na < 4) return fail("spline needs at least 4 args");
+            std::string basis = const_string(op.args[1]);
+            static const std::map<std::string, int> bases = { { "catmull-rom", 0 }, { "bezier", 1 },
+                                                              { "bspline", 2 }, { "hermite", 3 },
+                                                              { "linear", 4 }, { "constant", 5 } };
+            auto bi = bases.find(basis);
+            if (bi == bases.end()) return fail("unknown spline basis '" + basis + "'");
+            int knots = op.args[na - 1];
+            int nknots_sym = na == 5 ? op.args[3] : -1;
+            uint32_t nk = nknots_sym >= 0 ? A(nknots_sym) : kNoArg;
+            emit(OP_SPLINE, { a(0), a(2), A(knots), (uint32_t)bi->second, nk,
+                              (uint32_t)syms[knots].type.elems() },
+                 n);
+            return true;
+        }
+        if (n == "blackbody") { emit(OP_BLACKBODY, { a(0), a(1) }, n); return true; }
+        if (n == "luminance") { emit(OP_LUMINANCE, { a(0), a(1) }, n); return true; }
+        if (n == "closure") {
+            // closure r [weight] name args...
+            uses_closures = true;
+            size_t ni = 1;
+            int weight = -1;
+            if (na > 1 && !is_string(op.args[1])) { weight = op.args[1]; ni = 2; }
+            std::string cname = const_string(op.args[ni]);
+            auto it = ss.closure_ids.find(cname);
+            if (it == ss.closure_ids.end()) return fail("closure '" + cname + "' is not registered");
+            std::vector<uint32_t> params;
+            for (size_t i = ni + 1; i < na && params.size() < 5; ++i) params.push_back(A(op.args[i]));
+            while (params.size() < 5) params.push_back(kNoArg);
+            emit(OP_CLOSURE, { a(0), (uint32_t)it->second, params[0], params[1], params[2], params[3], params[4] },
+                 n);
+            if (na > ni + 6) {
+                std::vector<uint32_t> more;
+                for (size_t i = ni + 6; i < na && more.size() < 7; ++i) more.push_back(A(op.args[i]));
+                while (more.size() < 7) more.push_back(kNoArg);
+                emit(OP_NOP, { more[0], more[1], more[2], more[3], more[4], more[5], more[6] },
+                     "closure-params");
+            }
+            if (weight >= 0) emit(OP_CLOSURE_MUL, { a(0), a(0), A(weight) }, n);
+            return true;
+        }
+        return fail("op '" + n + "' is not supported by this executor");
+    }
+
+    bool run(CompiledGroup& out) {
+        if (g.layers.empty()) return fail("group has no layers");
+        if (!build_lops()) return false;
+        analyze();
+        assign_storage();
+        if (!lower_all()) return false;
+        // closure pools live after the symbol heap
+        ProgramHeader h;
+        std::memset(&h, 0, sizeof(h));
+        h.magic = kProgramMagic;
+        h.version = kProgramVersion;
+        h.nops = (uint32_t)ops.size();
+        h.nconst = (uint32_t)pool.size();
+        h.closure_base = heap_top;
+        h.max_comps = uses_closures ? (uint32_t)ss.opts.max_closure_components : 0u;
+        h.max_terms = uses_closures ? (uint32_t)ss.opts.max_closure_terms : 0u;
+        uint32_t closure_slots = uses_closures ? 1 + h.max_comps * kCompFloats + h.max_terms * kTermFloats : 0;
+        h.heap_slots = heap_top + closure_slots;
+        if (h.heap_slots == 0) h.heap_slots = 1;
+        h.flags = (uses_closures ? 1u : 0u);
+        for (const GSym& s : syms)
+            if (s.referenced && s.derivs) h.flags |= 2u;
+        h.max_depth = max_depth;
+        if (h.heap_slots > kArgOffsetMask) return fail("symbol heap too large");
+        out.header = h;
+        out.blob.resize(sizeof(h) + ops.size() * sizeof(Op) + pool.size() * 4);
+        std::memcpy(out.blob.data(), &h, sizeof(h));
+        if (!ops.empty()) std::memcpy(out.blob.data() + sizeof(h), ops.data(), ops.size() * sizeof(Op));
+        if (!pool.empty())
+            std::memcpy(out.blob.data() + sizeof(h) + ops.size() * sizeof(Op), pool.data(), pool.size() * 4);
+        out.op_names = op_names;
+        return true;
+    }
+};
+
+}  // namespace
+
+bool lower_group(ShadingSystem& ss, ShaderGroup& g, CompiledGroup& out, std::string& err) {
+    Lowerer L(ss, g, err);
+    return L.run(out);
+}
+
+}  // namespace oslg

@@ -1,0 +1,204 @@
+// Device op-program format: what the host lowering produces from an
+// optimized ShaderGroup and what the sm_103a interpreter executes.
+//
+// A program is one flat op stream for the whole group: global loads, every
+// layer's parameter initialisation and body in layer order, and the stores
+// of the renderer outputs (the reference runs the same layers, see
+// src/liboslexec/context.cpp:360-396 and batched_llvm_instance.cpp:2060+).
+// Structured control flow of the .oso form (if / for / while / dowhile with
+// jump targets, src/liboslexec/batched_llvm_gen.cpp:1068, :3806) is
+// rewritten into explicit mask ops so that every lane of a warp walks the
+// same op index and varying branches become lane masks.
+//
+// Per-point values live in a slot heap: slot s of point p is
+// heap[s * stride + p] (slot-major, point-minor, so a warp touching one slot
+// touches consecutive words). Uniform values live in a constant pool that
+// every CTA stages into shared memory.
+#pragma once
+#include <stdint.h>
+
+namespace oslg {
+
+static const uint32_t kProgramMagic = 0x4f534c47u;  // "OSLG"
+static const uint32_t kProgramVersion = 3;
+
+// ---- operand words ----------------------------------------------------------
+// bits 0..19  slot offset (heap) or index (constant pool)
+// bit  20     operand lives in the constant pool
+// bit  21     operand carries derivatives ([val][dx][dy] blocks)
+// bits 22..24 type class
+// bits 25..31 unused
+enum TypeClass : uint32_t {
+    TC_FLOAT = 0,
+    TC_INT = 1,
+    TC_TRIPLE = 2,
+    TC_MATRIX = 3,
+    TC_CLOSURE = 4,
+    TC_STRING = 5,
+};
+static const uint32_t kArgOffsetMask = 0xFFFFFu;
+static const uint32_t kArgConst = 1u << 20;
+static const uint32_t kArgDerivs = 1u << 21;
+static const uint32_t kArgTCShift = 22;
+
+inline uint32_t arg_make(uint32_t off, bool is_const, bool derivs, uint32_t tc) {
+    return (off & kArgOffsetMask) | (is_const ? kArgConst : 0u) | (derivs ? kArgDerivs : 0u)
+         | (tc << kArgTCShift);
+}
+
+// ---- opcodes ------------------------------------------------------------------
+// Grouped by handler family; the reference op each implements is named in
+// the lowering (oslg_lower.cpp) next to the name table.
+enum OpCode : uint16_t {
+    OP_NOP = 0,
+    // control (mask) ops; a[] holds immediates
+    OP_IF,          // a0=cond  a1=depth  a2=pc_else    (else marker index)
+    OP_ELSE,        // a1=depth a2=pc_endif a3=loop level+1 (0 = none)
+    OP_ENDIF,       // a1=depth a3=loop level+1
+    OP_LOOP_BEGIN,  // a1=depth a3=loop level+1
+    OP_LOOP_TEST,   // a0=cond a1=depth a2=pc_loop_end a3=loop level+1
+    OP_LOOP_STEP,   // a3=loop level+1
+    OP_JUMP,        // a2=pc
+    OP_LOOP_END,    // a1=depth a3=loop level+1
+    OP_BREAK,       // a3=loop level+1
+    OP_CONTINUE,    // a3=loop level+1
+    OP_RETURN,      // ends the current layer for the active lanes
+    OP_EXIT,        // ends the whole group for the active lanes
+    OP_LAYER_END,   // re-enables lanes that returned from this layer
+    // data movement
+    OP_LOAD_GLOBAL,   // a0=dst a1=global id
+    OP_LOAD_USERDATA, // a0=dst a1=byte offset a2=byte stride a3=base type (0 float,1 int)
+    OP_STORE_OUTPUT,  // a0=src a1=byte offset a2=byte stride a3=flags(bit0 derivs, bit1 int)
+    OP_ASSIGN,        // a0=r a1=src
+    OP_ZERO_DERIVS,   // a0=r
+    OP_COMPREF,       // a0=r a1=triple a2=index
+    OP_COMPASSIGN,    // a0=r a1=index a2=value
+    OP_MXCOMPREF,     // a0=r a1=matrix a2=row a3=col
+    OP_MXCOMPASSIGN,  // a0=r a1=row a2=col a3=value
+    OP_CONSTRUCT3,    // a0=r a1=x a2=y a3=z
+    OP_AREF,          // a0=r a1=array a2=index a3=arraylen
+    OP_AASSIGN,       // a0=array a1=index a2=value a3=arraylen
+    OP_MATRIX_DIAG,   // a0=r a1=scalar
+    OP_MATRIX16,      // a0=r a1..: first of 16 consecutive scalar operands stored in a[1] as base list (see lowering)
+    // arithmetic (float/triple with scalar broadcast; int when every operand is int)
+    OP_ADD, OP_SUB, OP_MUL, OP_DIV, OP_MOD, OP_NEG,
+    OP_IADD, OP_ISUB, OP_IMUL, OP_IDIV, OP_IMOD, OP_INEG,
+    OP_MMUL,          // matrix * matrix / matrix*scalar
+    OP_MDIV,          // matrix / matrix (a*inverse(b))
+    OP_TRANSPOSE, OP_DETERMINANT,
+    // compare / logic (result int)
+    OP_EQ, OP_NEQ, OP_LT, OP_GT, OP_LE, OP_GE,
+    OP_AND, OP_OR,
+    OP_BITAND, OP_BITOR, OP_XOR, OP_SHL, OP_SHR, OP_COMPL,
+    // unary math on float/triple (componentwise, Dual2-aware)
+    OP_ABS, OP_FLOOR, OP_CEIL, OP_ROUND, OP_TRUNC, OP_SIGN,
+    OP_SQRT, OP_INVSQRT, OP_CBRT,
+    OP_SIN, OP_COS, OP_TAN, OP_ASIN, OP_ACOS, OP_ATAN, OP_SINH, OP_COSH, OP_TANH,
+    OP_EXP, OP_EXP2, OP_EXPM1, OP_LOG, OP_LOG2, OP_LOG10,
+    OP_RADIANS, OP_DEGREES,
+    OP_ISNAN, OP_ISINF, OP_ISFINITE,
+    OP_IABS,
+    // binary / ternary math
+    OP_POW, OP_ATAN2, OP_FMOD, OP_MIN, OP_MAX, OP_IMIN, OP_IMAX,
+    OP_CLAMP, OP_MIX, OP_STEP, OP_SMOOTHSTEP, OP_SELECT,
+    // vector
+    OP_DOT, OP_CROSS, OP_LENGTH, OP_NORMALIZE, OP_DISTANCE,
+    // derivatives
+    OP_DX, OP_DY, OP_AREA, OP_FILTERWIDTH,
+    // matrix / transforms (a2 = matrix operand, a3 = kind: 0 point, 1 vector, 2 normal)
+    OP_TRANSFORM,
+    // noise family (a3 = NoiseKind | flags, see below)
+    OP_NOISE,        // a0=r a1=S a2=T (or 0xFFFFFFFF) a3=kind word a4=Speriod a5=Tperiod
+    OP_GABOR,        // a0=r a1=S a2=T a3=kind word a4..a6 option operands
+    OP_HASH,         // a0=r(int) a1=x a2=y (or none)
+    // spline: a0=r a1=x a2=knots (array) a3=basis id a4=nknots
+    OP_SPLINE,
+    // color
+    OP_BLACKBODY, OP_LUMINANCE,
+    // closures: a0=r a1=closure id a2.. params (see lowering)
+    OP_CLOSURE,
+    OP_CLOSURE_MUL,  // a0=r a1=closure a2=weight (float or color)
+    OP_CLOSURE_ADD,  // a0=r a1=a a2=b
+    OP_STORE_CLOSURE,// a0=src a1=byte offset a2=byte stride a3=max components
+    OP_COUNT
+};
+
+// noise kind word (OP_NOISE a3): bits 0..3 kind, bit 4 periodic, bits 5..7 dims,
+// bit 8 result is a triple, bit 9 compute derivatives
+enum NoiseKind : uint32_t {
+    NK_PERLIN = 0,   // signed ("perlin" / "snoise")
+    NK_UPERLIN = 1,  // unsigned ("uperlin" / "noise")
+    NK_CELL = 2,
+    NK_HASH = 3,
+    NK_SIMPLEX = 4,
+    NK_USIMPLEX = 5,
+    NK_GABOR = 6,
+    NK_NULL = 7,
+    NK_UNULL = 8,
+};
+inline uint32_t noise_word(uint32_t kind, bool periodic, int dims, bool vec, bool derivs) {
+    return kind | (periodic ? 16u : 0u) | ((uint32_t)dims << 5) | (vec ? 256u : 0u)
+         | (derivs ? 512u : 0u);
+}
+
+static const uint32_t kNoArg = 0xFFFFFFFFu;
+
+// Shader-globals the program can load (OP_LOAD_GLOBAL a1). Each triple
+// global with derivatives names its dx / dy fields so the loader can fill
+// a Dual2 in one op. Matches the varying members of BatchedShaderGlobals
+// (src/include/OSL/batched_shaderglobals.h:77-197).
+enum GlobalId : uint32_t {
+    G_P = 0, G_DPDX, G_DPDY, G_DPDZ,
+    G_I, G_DIDX, G_DIDY,
+    G_N, G_NG,
+    G_U, G_DUDX, G_DUDY,
+    G_V, G_DVDX, G_DVDY,
+    G_DPDU, G_DPDV,
+    G_TIME, G_DTIME, G_DPDTIME,
+    G_PS, G_DPSDX, G_DPSDY,
+    G_SURFACEAREA,
+    G_COUNT
+};
+
+struct Op {
+    uint16_t code;
+    uint8_t nargs;
+    uint8_t flags;
+    uint32_t a[7];
+};
+static_assert(sizeof(Op) == 32, "Op must be 32 bytes");
+
+// Closure storage inside the heap (per point): a component pool and a
+// term pool. A closure value (one heap slot, int bits) is (first term << 16)
+// | term count. Each term is (component index, weight rgb); each component
+// is (closure id, params...). The layout mirrors ClosureComponent
+// {id, w, params} of src/include/OSL/oslclosure.h:65-147 after the
+// renderer's tree walk has folded the MUL weights into each component.
+static const int kClosureParamFloats = 12;
+static const int kCompFloats = 1 + kClosureParamFloats;  // id + params
+static const int kTermFloats = 4;                        // comp idx + rgb
+
+struct ProgramHeader {
+    uint32_t magic;
+    uint32_t version;
+    uint32_t nops;
+    uint32_t nconst;        // floats in the constant pool
+    uint32_t heap_slots;    // floats per point
+    uint32_t flags;         // bit0 uses closures, bit1 uses derivatives
+    uint32_t closure_base;  // heap slot of the closure pools (if bit0)
+    uint32_t max_comps;     // component pool capacity
+    uint32_t max_terms;     // term pool capacity
+    uint32_t max_depth;     // deepest if/loop nesting (<= 32)
+    uint32_t reserved[6];
+};
+static_assert(sizeof(ProgramHeader) == 64, "header must be 64 bytes");
+
+// Status bits a kernel reports back (OR-ed across points).
+enum StatusBits : uint32_t {
+    ST_CLOSURE_OVERFLOW = 1u,
+    ST_BAD_OPCODE = 2u,
+    ST_ARRAY_BOUNDS = 4u,
+    ST_TIMEOUT = 8u,
+};
+
+}  // namespace oslg

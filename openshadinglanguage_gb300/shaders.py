@@ -1,0 +1,248 @@
+"""Shader programs used by the benchmarks and tests, written as the .oso
+that oslc plus the runtime optimizer would hand the executor (no oslc runs
+here; see OsoBuilder).
+"""
+from .oso import OsoBuilder
+
+
+def fbm_cell():
+    """fBm of vector Perlin noise with derivatives plus a hashed cell id.
+
+        shader fbm_cell(int octaves = 4, float lacunarity = 2, float gain = 0.5,
+                        output color Cout = 0, output int cellhash = 0)
+        {
+            point p = point(8*u, 8*v, 0);
+            color sum = 0; float amp = 1; point pp = p;
+            for (int i = 0; i < octaves; ++i) {
+                sum += amp * (color) noise("perlin", pp);
+                pp *= lacunarity; amp *= gain;
+            }
+            Cout = sum;
+            cellhash = hash(cellnoise(p * 4));
+        }
+    """
+    b = OsoBuilder("fbm_cell")
+    octaves = b.param("int", "octaves", 4)
+    lac = b.param("float", "lacunarity", 2.0)
+    gain = b.param("float", "gain", 0.5)
+    Cout = b.param("color", "Cout", [0, 0, 0], output=True)
+    cellhash = b.param("int", "cellhash", 0, output=True)
+    u = b.glob("float", "u")
+    v = b.glob("float", "v")
+    p = b.local("point", "p")
+    s = b.local("color", "sum")
+    amp = b.local("float", "amp")
+    pp = b.local("point", "pp")
+    i = b.local("int", "i")
+    t1, t2 = b.tmp("float"), b.tmp("float")
+    c8, c0, c1, c4 = b.const("float", 8.0), b.const("float", 0.0), b.const("float", 1.0), b.const("float", 4.0)
+    i0, i1 = b.const("int", 0), b.const("int", 1)
+    perlin = b.const("string", "perlin")
+    b.op("mul", t1, c8, u)
+    b.op("mul", t2, c8, v)
+    b.op("point", p, t1, t2, c0)
+    b.op("assign", s, c0)
+    b.op("assign", amp, c1)
+    b.op("assign", pp, p)
+    cond = b.tmp("int")
+    with b.loop("for", cond) as L:
+        b.op("assign", i, i0)
+        L.cond()
+        b.op("lt", cond, i, octaves)
+        L.body()
+        n = b.tmp("color")
+        m = b.tmp("color")
+        b.op("noise", n, perlin, pp)
+        b.op("mul", m, amp, n)
+        b.op("add", s, s, m)
+        b.op("mul", pp, pp, lac)
+        b.op("mul", amp, amp, gain)
+        L.step()
+        b.op("add", i, i, i1)
+    b.op("assign", Cout, s)
+    p4 = b.tmp("point")
+    cn = b.tmp("float")
+    b.op("mul", p4, p, c4)
+    b.op("cellnoise", cn, p4)
+    b.op("hash", cellhash, cn)
+    return b.text()
+
+
+def _testnoise_common(b, inscale_name="inscale", angle_default=10.0, inscale_default=20.0, hard_trig=False):
+    """Coordinates shared by the testsuite noise shaders:
+        float theta = radians(angle);
+        float s = mod(u,0.25) - 0.125;  float t = mod(v,0.5) - 0.25;
+        float ru = cos(theta)*s + sin(theta)*t;  float rv = sin(theta)*s - cos(theta)*t;
+        ru *= inscale; rv *= inscale;
+        float rz = (inscale*(s+t)) / M_SQRT2;  float ttime = s*inscale;
+    mod() is stdosl.h's a - b*floor(a/b), inlined as oslc does."""
+    angle = b.param("float", "angle", angle_default)
+    inscale = b.param("float", inscale_name, inscale_default)
+    u = b.glob("float", "u")
+    v = b.glob("float", "v")
+    theta, s, t = b.local("float", "theta"), b.local("float", "s"), b.local("float", "t")
+    ru, rv, rz, ttime = (b.local("float", n) for n in ("ru", "rv", "rz", "ttime"))
+    ct, st = b.local("float", "cos_theta"), b.local("float", "sin_theta")
+    b.op("radians", theta, angle)
+    if hard_trig:
+        # testsuite/hashnoise/test.osl hard-codes the angle=10 values
+        b.op("assign", ct, b.const("float", 0.984807729721069335))
+        b.op("assign", st, b.const("float", 0.173648148775100708))
+    else:
+        b.op("cos", ct, theta)
+        b.op("sin", st, theta)
+
+    def mod(dst, a, m):
+        q, f, pr = b.tmp("float"), b.tmp("float"), b.tmp("float")
+        b.op("div", q, a, m)
+        b.op("floor", f, q)
+        b.op("mul", pr, m, f)
+        b.op("sub", dst, a, pr)
+
+    ms, mt = b.tmp("float"), b.tmp("float")
+    mod(ms, u, b.const("float", 0.25))
+    b.op("sub", s, ms, b.const("float", 0.125))
+    mod(mt, v, b.const("float", 0.5))
+    b.op("sub", t, mt, b.const("float", 0.25))
+    a1, a2, a3, a4 = (b.tmp("float") for _ in range(4))
+    b.op("mul", a1, ct, s)
+    b.op("mul", a2, st, t)
+    b.op("add", ru, a1, a2)
+    b.op("mul", a3, st, s)
+    b.op("mul", a4, ct, t)
+    b.op("sub", rv, a3, a4)
+    b.op("mul", ru, ru, inscale)
+    b.op("mul", rv, rv, inscale)
+    st_, prod = b.tmp("float"), b.tmp("float")
+    b.op("add", st_, s, t)
+    b.op("mul", prod, inscale, st_)
+    b.op("div", rz, prod, b.const("float", 1.4142135623730951))
+    b.op("mul", ttime, s, inscale)
+    return u, v, ru, rv, rz, ttime
+
+
+def _quadrants(b, u, v, emit):
+    """The testsuite shaders' layout: float noise for v<0.49, color noise for
+    v>0.51; 1D/2D/3D/4D in the four u bands."""
+    c = lambda x: b.const("float", x)
+    ci = b.tmp("int")
+
+    def bands(vec):
+        b1 = b.tmp("int")
+        b.op("lt", b1, u, c(0.24))
+        with b.if_(b1) as br1:
+            emit(vec, 1)
+            br1.else_()
+            g, l, a = b.tmp("int"), b.tmp("int"), b.tmp("int")
+            b.op("gt", g, u, c(0.26))
+            b.op("lt", l, u, c(0.49))
+            b.op("and", a, g, l)
+            with b.if_(a) as br2:
+                emit(vec, 2)
+                br2.else_()
+                g2, l2, a2 = b.tmp("int"), b.tmp("int"), b.tmp("int")
+                b.op("gt", g2, u, c(0.51))
+                b.op("lt", l2, u, c(0.74))
+                b.op("and", a2, g2, l2)
+                with b.if_(a2) as br3:
+                    emit(vec, 3)
+                    br3.else_()
+                    g3 = b.tmp("int")
+                    b.op("gt", g3, u, c(0.76))
+                    with b.if_(g3):
+                        emit(vec, 4)
+
+    b.op("lt", ci, v, c(0.49))
+    with b.if_(ci) as top:
+        bands(False)
+        top.else_()
+        c2 = b.tmp("int")
+        b.op("gt", c2, v, c(0.51))
+        with b.if_(c2):
+            bands(True)
+
+
+def testnoise(shader_name="testnoise", noisename_default="noise", offset_default=0.5, scale_default=0.5,
+              with_name=True, opname=None):
+    """testsuite/common/shaders/testnoise.osl (with_name=True) and the
+    per-noise test.osl shaders of testsuite/{noise,cellnoise,hashnoise}."""
+    b = OsoBuilder(shader_name)
+    noisename = b.param("string", "noisename", noisename_default) if with_name else None
+    offset = b.param("float", "offset", offset_default)
+    scale = b.param("float", "scale", scale_default)
+    Cout = b.param("color", "Cout", [0, 0, 0], output=True)
+    u, v, ru, rv, rz, ttime = _testnoise_common(b, hard_trig=(opname == "hashnoise"))
+    b.op("assign", Cout, b.const("float", 0.0))
+
+    def emit(vec, dim):
+        r = b.tmp("color" if vec else "float")
+        args = []
+        if dim in (1, 2):
+            args = [ru] if dim == 1 else [ru, rv]
+        else:
+            pt = b.tmp("point")
+            b.op("point", pt, ru, rv, rz)
+            args = [pt] if dim == 3 else [pt, ttime]
+        if with_name:
+            b.op("noise", r, noisename, *args)
+        else:
+            b.op(opname, r, *args)
+        m, a = b.tmp("color" if vec else "float"), b.tmp("color" if vec else "float")
+        b.op("mul", m, scale, r)
+        b.op("add", a, offset, m)
+        b.op("assign", Cout, a)
+
+    _quadrants(b, u, v, emit)
+    return b.text()
+
+
+def getP():
+    """testsuite/example-batched-deformer/getP.osl: output point out = P"""
+    b = OsoBuilder("getP")
+    out = b.param("point", "out", [0, 0, 0], output=True)
+    P = b.glob("point", "P")
+    b.op("assign", out, P)
+    return b.text()
+
+
+def vfBm3d():
+    """testsuite/example-batched-deformer/vfBm3d.osl"""
+    b = OsoBuilder("vfBm3d")
+    position = b.param("point", "position", [0, 0, 0], lockgeom=False)
+    frequency = b.param("float", "frequency", 1.0)
+    amplitude = b.param("float", "amplitude", 1.0, lockgeom=False)
+    octaves = b.param("int", "octaves", 1)
+    lac = b.param("float", "lacunarity", 2.0)
+    gain = b.param("float", "gain", 0.5)
+    noisetype = b.param("string", "noisetype", "snoise")
+    out = b.param("vector", "out", [0, 0, 0], output=True)
+    r, p, amp, i = b.local("vector", "r"), b.local("point", "p"), b.local("float", "amp"), b.local("int", "i")
+    b.op("assign", r, b.const("float", 0.0))
+    b.op("mul", p, position, frequency)
+    b.op("assign", amp, amplitude)
+    cond = b.tmp("int")
+    with b.loop("for", cond) as L:
+        b.op("assign", i, b.const("int", 0))
+        L.cond()
+        b.op("lt", cond, i, octaves)
+        L.body()
+        n, m = b.tmp("vector"), b.tmp("vector")
+        b.op("noise", n, noisetype, p)
+        b.op("mul", m, amp, n)
+        b.op("add", r, r, m)
+        b.op("mul", p, p, lac)
+        b.op("mul", amp, amp, gain)
+        L.step()
+        b.op("add", i, i, b.const("int", 1))
+    b.op("assign", out, r)
+    return b.text()
+
+
+def vadd():
+    """testsuite/example-batched-deformer/vadd.osl: out = a + b"""
+    b = OsoBuilder("vadd")
+    a = b.param("vector", "a", [0, 0, 0])
+    bb = b.param("vector", "b", [0, 0, 0])
+    out = b.param("vector", "out", [0, 0, 0], output=True)
+    b.op("add", out, a, bb)
+    return b.text()

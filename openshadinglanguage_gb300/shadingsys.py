@@ -1,0 +1,191 @@
+"""Python mirror of the reference's ShadingSystem API over the C ABI.
+
+Names and argument meaning follow src/include/OSL/oslexec.h
+(ShaderGroupBegin / Parameter / Shader / ConnectShaders / ShaderGroupEnd,
+attribute, add_symlocs, optimize_group, batched<W>().execute): a test
+written against the reference reads the same here. Errors raise OSLError
+carrying the library's message (the reference reports through bool
+returns plus an ErrorHandler).
+"""
+import ctypes
+from dataclasses import dataclass
+
+from . import _capi as C
+
+
+class OSLError(RuntimeError):
+    pass
+
+
+@dataclass(frozen=True)
+class TypeDesc:
+    basetype: int
+    aggregate: int = C.AGG_SCALAR
+    vecsemantics: int = C.VEC_NOXFORM
+    arraylen: int = 0
+
+    def c(self):
+        return C.TypeDescC(self.basetype, self.aggregate, self.vecsemantics, self.arraylen)
+
+    def array(self, n):
+        return TypeDesc(self.basetype, self.aggregate, self.vecsemantics, n)
+
+    @property
+    def nfloats(self):
+        return self.aggregate * max(1, self.arraylen)
+
+
+TypeInt = TypeDesc(C.BASE_INT32)
+TypeFloat = TypeDesc(C.BASE_FLOAT)
+TypeString = TypeDesc(C.BASE_STRING)
+TypeColor = TypeDesc(C.BASE_FLOAT, C.AGG_VEC3, C.VEC_COLOR)
+TypePoint = TypeDesc(C.BASE_FLOAT, C.AGG_VEC3, C.VEC_POINT)
+TypeVector = TypeDesc(C.BASE_FLOAT, C.AGG_VEC3, C.VEC_VECTOR)
+TypeNormal = TypeDesc(C.BASE_FLOAT, C.AGG_VEC3, C.VEC_NORMAL)
+TypeMatrix = TypeDesc(C.BASE_FLOAT, C.AGG_MATRIX44)
+TypeClosure = TypeDesc(0)
+
+SymArenaHeap = C.ARENA_HEAP
+SymArenaOutputs = C.ARENA_OUTPUTS
+SymArenaUserData = C.ARENA_USERDATA
+
+
+@dataclass
+class SymLocationDesc:
+    """SymLocationDesc (oslexec.h:69-105): point i of `name` lives at
+    base + offset + i*stride; with derivs the value is followed by its
+    x and y partials."""
+    name: str
+    type: TypeDesc
+    derivs: bool = False
+    arena: int = SymArenaOutputs
+    offset: int = 0
+    stride: int = 0
+
+
+class ShaderGroup:
+    def __init__(self, ss, handle, name):
+        self._ss, self._h, self.name = ss, handle, name
+
+    @property
+    def handle(self):
+        return self._h
+
+    def program_bytes(self):
+        """The lowered op program (what replaces the JIT'd module)."""
+        L = C.lib()
+        size = ctypes.c_size_t(0)
+        self._ss._check(L.oslg_group_program(self._ss._h, self._h, None, 0, ctypes.byref(size)))
+        buf = ctypes.create_string_buffer(size.value)
+        self._ss._check(L.oslg_group_program(self._ss._h, self._h, buf, size.value, ctypes.byref(size)))
+        return buf.raw[: size.value]
+
+    def release(self):
+        if self._h:
+            C.lib().oslg_release_group(self._ss._h, self._h)
+            self._h = None
+
+
+class ShadingSystem:
+    def __init__(self):
+        L = C.lib()
+        h = ctypes.c_void_p()
+        if L.oslg_create_system(ctypes.byref(h)) != C.OSLG_OK:
+            raise OSLError("could not create the shading system")
+        self._h = h
+        self._keep = []
+
+    def close(self):
+        if self._h:
+            C.lib().oslg_destroy_system(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != C.OSLG_OK:
+            msg = C.lib().oslg_last_error(self._h)
+            raise OSLError("osl-gb300 error %d: %s" % (rc, msg.decode() if msg else ""))
+
+    # ---- configuration -------------------------------------------------------
+    def attribute(self, name, value):
+        self._check(C.lib().oslg_attribute_int(self._h, name.encode(), int(value)))
+
+    def register_closure(self, name, closure_id):
+        self._check(C.lib().oslg_register_closure(self._h, name.encode(), int(closure_id)))
+
+    def LoadMemoryCompiledShader(self, shadername, oso_text):
+        self._check(C.lib().oslg_load_memory_compiled_shader(self._h, shadername.encode(), oso_text.encode()))
+        return True
+
+    # ---- groups --------------------------------------------------------------
+    def ShaderGroupBegin(self, groupname=""):
+        g = ctypes.c_void_p()
+        self._check(C.lib().oslg_shader_group_begin(self._h, groupname.encode(), ctypes.byref(g)))
+        return ShaderGroup(self, g, groupname)
+
+    def Parameter(self, group, name, type_, value, lockgeom=True):
+        if type_.basetype == C.BASE_STRING:
+            vals = value if isinstance(value, (list, tuple)) else [value]
+            arr = (ctypes.c_char_p * len(vals))(*[v.encode() for v in vals])
+            ptr = ctypes.cast(arr, ctypes.c_void_p)
+        elif type_.basetype == C.BASE_INT32:
+            vals = value if isinstance(value, (list, tuple)) else [value]
+            arr = (ctypes.c_int * len(vals))(*[int(v) for v in vals])
+            ptr = ctypes.cast(arr, ctypes.c_void_p)
+        else:
+            vals = value if isinstance(value, (list, tuple)) else [value] * type_.nfloats
+            arr = (ctypes.c_float * len(vals))(*[float(v) for v in vals])
+            ptr = ctypes.cast(arr, ctypes.c_void_p)
+        self._keep.append(arr)
+        self._check(C.lib().oslg_parameter(self._h, group.handle, name.encode(), type_.c(), ptr,
+                                           1 if lockgeom else 0))
+
+    def Shader(self, group, shaderusage, shadername, layername=""):
+        self._check(C.lib().oslg_shader(self._h, group.handle, shaderusage.encode(), shadername.encode(),
+                                        layername.encode()))
+
+    def ConnectShaders(self, group, srclayer, srcparam, dstlayer, dstparam):
+        self._check(C.lib().oslg_connect_shaders(self._h, group.handle, srclayer.encode(), srcparam.encode(),
+                                                 dstlayer.encode(), dstparam.encode()))
+
+    def ShaderGroupEnd(self, group):
+        self._check(C.lib().oslg_shader_group_end(self._h, group.handle))
+
+    def renderer_outputs(self, group, names):
+        arr = (ctypes.c_char_p * len(names))(*[n.encode() for n in names])
+        self._check(C.lib().oslg_group_renderer_outputs(self._h, group.handle, arr, len(names)))
+
+    def add_symlocs(self, group, symlocs):
+        locs = symlocs if isinstance(symlocs, (list, tuple)) else [symlocs]
+        arr = (C.SymLocC * len(locs))()
+        names = []
+        for i, s in enumerate(locs):
+            nm = s.name.encode()
+            names.append(nm)
+            arr[i] = C.SymLocC(nm, s.type.c(), 1 if s.derivs else 0, s.arena, s.offset, s.stride)
+        self._check(C.lib().oslg_add_symlocs(self._h, group.handle, arr, len(locs)))
+
+    def optimize_group(self, group):
+        self._check(C.lib().oslg_optimize_group(self._h, group.handle))
+
+    def set_launch(self, block=256, points_per_thread=1, heap_smem=-1):
+        self._check(C.lib().oslg_set_launch(self._h, block, points_per_thread, heap_smem))
+
+    # ---- execution --------------------------------------------------------------
+    def execute_batch(self, group, npoints, globals_c, userdata_ptr=0, output_ptr=0, stream=0, sync=False):
+        """BatchedExecutor::execute over npoints device-resident points.
+        globals_c is a ShaderGlobalsC (see globals.make_globals)."""
+        fn = C.lib().oslg_execute_batch_sync if sync else C.lib().oslg_execute_batch
+        self._check(fn(self._h, group.handle, int(npoints), ctypes.byref(globals_c),
+                       ctypes.c_void_p(userdata_ptr or None), ctypes.c_void_p(output_ptr or None),
+                       ctypes.c_void_p(stream or None)))
+
+    def device_status(self):
+        bits = ctypes.c_uint32(0)
+        self._check(C.lib().oslg_device_status(self._h, ctypes.byref(bits)))
+        return bits.value

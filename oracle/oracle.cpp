@@ -1,0 +1,1030 @@
+// ORACLE — test infrastructure only. Not part of the shipped library; only
+// the tests, the smoke check and the CPU-baseline leg of bench.py load it.
+//
+// CPU restatement of OSL's batched execution semantics for one lowered
+// shader group, used to check the GPU interpreter point for point:
+//   * control flow runs per point with a real program counter (jumps), the
+//     scalar reading of what the batched backend does with lane masks
+//     (src/liboslexec/batched_llvm_gen.cpp:1068 if, :3806-4250 loops and
+//     break/continue; src/liboslexec/llvm_gen.cpp for the scalar ops);
+//   * op results follow the reference's shadeops: Dual2 arithmetic
+//     (src/include/OSL/dual.h), vector ops (dual_vec.h), noise
+//     (oslnoise.h, simplexnoise.cpp), min/max/clamp selection
+//     (llvm_gen.cpp:1345-1380, :1170-1210), normalize/length/distance
+//     (llvm_ops.cpp:850-915), transforms (dual_vec.h:336-400).
+// Transcendental functions are evaluated in double precision and rounded to
+// float (correctly rounded results), the same definition the device uses.
+// It reads the op-program format (openshadinglanguage_gb300/csrc/
+// oslg_program.h) as a file format; it shares no code with the executor.
+//
+// Build: oracle/build.py (g++ -O2 -ffp-contract=off -fopenmp).
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "../include/oslg.h"
+#include "../openshadinglanguage_gb300/csrc/oslg_program.h"
+#include "oracle_simplex.h"
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+using namespace oracle;
+using oslg::Op;
+
+namespace {
+
+struct Prog {
+    const oslg::ProgramHeader* h;
+    const Op* ops;
+    const uint32_t* pool;
+    // control-flow partners, resolved once
+    std::vector<int> loop_end_of_level;  // per op: for BREAK/CONTINUE
+    std::vector<int> partner;            // IF->ELSE, ELSE->ENDIF, LOOP_TEST->LOOP_END
+    std::vector<int> break_target, continue_target;
+    std::vector<int> layer_end_after;    // RETURN -> next LAYER_END
+    int outputs_start = 0;               // first op after the last LAYER_END
+};
+
+struct Point {
+    std::vector<uint32_t> heap;
+    const uint32_t* pool;
+    int64_t pt;
+    uint32_t status = 0;
+};
+
+inline uint32_t aoff(uint32_t a) { return a & oslg::kArgOffsetMask; }
+inline bool aconst(uint32_t a) { return (a & oslg::kArgConst) != 0; }
+inline bool ader(uint32_t a) { return (a & oslg::kArgDerivs) != 0; }
+inline uint32_t atc(uint32_t a) { return (a >> oslg::kArgTCShift) & 7u; }
+inline int anc(uint32_t a) {
+    uint32_t t = atc(a);
+    return t == oslg::TC_TRIPLE ? 3 : (t == oslg::TC_MATRIX ? 16 : 1);
+}
+
+inline uint32_t word(const Point& P, uint32_t a, int idx) {
+    uint32_t o = aoff(a) + (uint32_t)idx;
+    return aconst(a) ? P.pool[o] : P.heap[o];
+}
+inline void setw(Point& P, uint32_t a, int idx, uint32_t v) { P.heap[aoff(a) + (uint32_t)idx] = v; }
+inline void setf(Point& P, uint32_t a, int idx, float v) { setw(P, a, idx, fbits(v)); }
+
+// component c (scalars broadcast) of value / x / y partial; ints convert
+inline float getf(const Point& P, uint32_t a, int c, int d) {
+    int nc = anc(a);
+    if (d && !ader(a)) return 0.0f;
+    uint32_t w = word(P, a, d * nc + (nc == 1 ? 0 : c));
+    return atc(a) == oslg::TC_INT ? (float)(int32_t)w : bitsf(w);
+}
+inline DF getd(const Point& P, uint32_t a, int c) { return DF(getf(P, a, c, 0), getf(P, a, c, 1), getf(P, a, c, 2)); }
+inline int geti(const Point& P, uint32_t a, int c) {
+    uint32_t t = atc(a);
+    uint32_t w = word(P, a, t == oslg::TC_TRIPLE ? c : 0);
+    if (t == oslg::TC_FLOAT || t == oslg::TC_TRIPLE) return (int)bitsf(w);
+    return (int32_t)w;
+}
+// store a dual into component c of r; only the value if r has no partials
+inline void putd(Point& P, uint32_t r, int c, const DF& v) {
+    if (atc(r) == oslg::TC_INT) { setw(P, r, c, (uint32_t)(int)v.v); return; }
+    int nc = anc(r);
+    setf(P, r, c, v.v);
+    if (ader(r)) { setf(P, r, nc + c, v.dx); setf(P, r, 2 * nc + c, v.dy); }
+}
+inline void putv(Point& P, uint32_t r, int c, float v) { putd(P, r, c, DF(v)); }
+
+// ---- math: correctly rounded through double --------------------------------
+inline float f_sin(float x) { return (float)std::sin((double)x); }
+inline float f_cos(float x) { return (float)std::cos((double)x); }
+const float kMin = FLT_MIN;
+// OIIO safe_log / safe_pow / safe_fmod
+inline float safe_log(float x) { return (float)std::log((double)(x < kMin ? kMin : x)); }
+inline float safe_log2(float x) { return (float)std::log2((double)(x < kMin ? kMin : x)); }
+inline float safe_log10(float x) { return (float)std::log10((double)(x < kMin ? kMin : x)); }
+inline float safe_pow(float x, float y) {
+    if (y == 0.0f) return 1.0f;
+    if (x == 0.0f) return 0.0f;
+    if (x < 0.0f && y != std::floor(y)) return 0.0f;
+    float r = (float)std::pow((double)x, (double)y);
+    return std::min(std::max(r, -FLT_MAX), FLT_MAX);
+}
+inline float safe_fmod(float a, float b) {
+    if (b != 0.0f) {
+        int N = (int)(a / b);
+        return a - (float)N * b;
+    }
+    return 0.0f;
+}
+
+// dualfunc (dual.h:760-775)
+inline DF dualfunc(const DF& u, float f, float df) { return DF(f, df * u.dx, df * u.dy); }
+
+// ---- ops -------------------------------------------------------------------------
+void op_assign(Point& P, const uint32_t* a) {
+    uint32_t r = a[0], s = a[1];
+    uint32_t tr = atc(r), ts = atc(s);
+    if (tr == oslg::TC_CLOSURE) { setw(P, r, 0, ts == oslg::TC_CLOSURE ? word(P, s, 0) : 0u); return; }
+    if (tr == oslg::TC_STRING) { setw(P, r, 0, word(P, s, 0)); return; }
+    if (tr == oslg::TC_MATRIX) {
+        if (ts == oslg::TC_MATRIX) for (int i = 0; i < 16; ++i) setw(P, r, i, word(P, s, i));
+        else {
+            float v = getf(P, s, 0, 0);
+            for (int i = 0; i < 16; ++i) setf(P, r, i, i % 5 == 0 ? v : 0.0f);
+        }
+        return;
+    }
+    int count = (int)a[2], ralen = std::max(1, (int)a[3]), salen = std::max(1, (int)a[4]);
+    int nr = anc(r), ns = anc(s);
+    for (int e = 0; e < count; ++e)
+        for (int c = 0; c < nr; ++c) {
+            int sc = ns == 1 ? 0 : c;
+            uint32_t sw = word(P, s, e * ns + sc);
+            if (tr == oslg::TC_INT) {
+                setw(P, r, e * nr + c, (uint32_t)(ts == oslg::TC_INT ? (int32_t)sw : (int)bitsf(sw)));
+                continue;
+            }
+            setf(P, r, e * nr + c, ts == oslg::TC_INT ? (float)(int32_t)sw : bitsf(sw));
+            if (ader(r)) {
+                float dx = 0, dy = 0;
+                if (ader(s)) {
+                    dx = bitsf(word(P, s, salen * ns + e * ns + sc));
+                    dy = bitsf(word(P, s, 2 * salen * ns + e * ns + sc));
+                }
+                setf(P, r, ralen * nr + e * nr + c, dx);
+                setf(P, r, 2 * ralen * nr + e * nr + c, dy);
+            }
+        }
+}
+
+// add / sub / mul / div / mod with dual.h semantics per operand kind
+void op_arith(Point& P, const uint32_t* a, int K) {
+    uint32_t r = a[0], x = a[1], y = a[2];
+    int nc = anc(r);
+    for (int c = 0; c < nc; ++c) {
+        float xv = getf(P, x, c, 0), yv = getf(P, y, c, 0);
+        DF X(xv, getf(P, x, c, 1), getf(P, x, c, 2)), Y(yv, getf(P, y, c, 1), getf(P, y, c, 2));
+        bool xd = ader(x), yd = ader(y);
+        DF res;
+        switch (K) {
+        case 0:
+            if (xd && yd) res = X + Y;
+            else if (xd) res = X + yv;
+            else if (yd) res = xv + Y;
+            else res = DF(xv + yv);
+            break;
+        case 1:
+            if (xd && yd) res = X - Y;
+            else if (xd) res = X - yv;
+            else if (yd) res = xv - Y;
+            else res = DF(xv - yv);
+            break;
+        case 2:
+            if (xd && yd) res = X * Y;
+            else if (xd) res = X * yv;
+            else if (yd) res = Y * xv;
+            else res = DF(xv * yv);
+            break;
+        case 3:
+            // safe division (the reference's div codegen returns 0 for x/0)
+            if (yv == 0.0f) res = DF(0.0f);
+            else if (xd && yd) res = X / Y;
+            else if (xd) res = X / yv;
+            else if (yd) res = xv / Y;
+            else res = DF(xv / yv);
+            break;
+        default:
+            res = DF(yv == 0.0f ? 0.0f : std::fmod(xv, yv), X.dx, X.dy);
+            break;
+        }
+        if (atc(r) == oslg::TC_INT) { setw(P, r, c, (uint32_t)(int)res.v); continue; }
+        putd(P, r, c, res);
+    }
+}
+
+void op_iarith(Point& P, const uint32_t* a, int K) {
+    int x = geti(P, a[1], 0), y = geti(P, a[2], 0), v;
+    switch (K) {
+    case 0: v = (int)((uint32_t)x + (uint32_t)y); break;
+    case 1: v = (int)((uint32_t)x - (uint32_t)y); break;
+    case 2: v = (int)((uint32_t)x * (uint32_t)y); break;
+    case 3: v = (y == 0 || (x == INT32_MIN && y == -1)) ? 0 : x / y; break;
+    default: v = (y == 0 || (x == INT32_MIN && y == -1)) ? 0 : x % y; break;
+    }
+    setw(P, a[0], 0, (uint32_t)v);
+}
+
+bool truth(const Point& P, uint32_t a) {
+    uint32_t t = atc(a);
+    if (t == oslg::TC_FLOAT) return getf(P, a, 0, 0) != 0.0f;
+    if (t == oslg::TC_TRIPLE) return getf(P, a, 0, 0) != 0.0f || getf(P, a, 1, 0) != 0.0f || getf(P, a, 2, 0) != 0.0f;
+    return word(P, a, 0) != 0u;
+}
+
+void op_cmp(Point& P, const uint32_t* a, int K) {
+    uint32_t x = a[1], y = a[2];
+    bool ints = (atc(x) == oslg::TC_INT || atc(x) == oslg::TC_STRING)
+             && (atc(y) == oslg::TC_INT || atc(y) == oslg::TC_STRING);
+    bool res;
+    if (ints) {
+        int32_t xi = (int32_t)word(P, x, 0), yi = (int32_t)word(P, y, 0);
+        const bool rs[6] = { xi == yi, xi != yi, xi < yi, xi > yi, xi <= yi, xi >= yi };
+        res = rs[K];
+    } else if (K <= 1) {
+        int n = std::max(anc(x), anc(y));
+        bool eq = true;
+        for (int c = 0; c < n; ++c) eq = eq && getf(P, x, c, 0) == getf(P, y, c, 0);
+        res = K == 0 ? eq : !eq;
+    } else {
+        float xv = getf(P, x, 0, 0), yv = getf(P, y, 0, 0);
+        const bool rs[6] = { false, false, xv < yv, xv > yv, xv <= yv, xv >= yv };
+        res = rs[K];
+    }
+    setw(P, a[0], 0, res ? 1u : 0u);
+}
+
+// unary math per component (dual.h:829-1260 derivative rules)
+void op_unary(Point& P, const uint32_t* a, uint16_t code) {
+    uint32_t r = a[0], x = a[1];
+    int nc = anc(r);
+    for (int c = 0; c < nc; ++c) {
+        DF X = getd(P, x, c);
+        float v = X.v;
+        DF res;
+        bool has = ader(x);
+        switch (code) {
+        case oslg::OP_NEG: res = -X; break;
+        case oslg::OP_ABS: res = v >= 0.0f ? DF(std::fabs(v), X.dx, X.dy) : -X; break;
+        case oslg::OP_FLOOR: res = DF(std::floor(v)); break;
+        case oslg::OP_CEIL: res = DF(std::ceil(v)); break;
+        case oslg::OP_ROUND: res = DF(std::round(v)); break;
+        case oslg::OP_TRUNC: res = DF(std::trunc(v)); break;
+        case oslg::OP_SIGN: res = DF(v < 0.0f ? -1.0f : (v == 0.0f ? 0.0f : 1.0f)); break;
+        case oslg::OP_SQRT:
+            if (v > 0.0f) { float f = std::sqrt(v); res = dualfunc(X, f, 0.5f / f); } else res = DF(0.0f);
+            break;
+        case oslg::OP_INVSQRT:
+            if (v > 0.0f) { float f = 1.0f / std::sqrt(v); res = dualfunc(X, f, -0.5f * f / v); } else res = DF(0.0f);
+            break;
+        case oslg::OP_CBRT:
+            if (v != 0.0f) { float f = (float)std::cbrt((double)v); res = dualfunc(X, f, 1.0f / (3.0f * f * f)); }
+            else res = DF(0.0f);
+            break;
+        case oslg::OP_SIN: res = dualfunc(X, f_sin(v), f_cos(v)); break;
+        case oslg::OP_COS: res = dualfunc(X, f_cos(v), -f_sin(v)); break;
+        case oslg::OP_TAN: { float cs = f_cos(v); res = dualfunc(X, (float)std::tan((double)v), 1.0f / (cs * cs)); break; }
+        case oslg::OP_ASIN:
+            if (v >= 1.0f) res = DF(1.57079632679489661923f);
+            else if (v <= -1.0f) res = DF(-1.57079632679489661923f);
+            else res = dualfunc(X, (float)std::asin((double)v), 1.0f / std::sqrt(1.0f - v * v));
+            break;
+        case oslg::OP_ACOS:
+            if (v >= 1.0f) res = DF(0.0f);
+            else if (v <= -1.0f) res = DF(3.14159265358979323846f);
+            else res = dualfunc(X, (float)std::acos((double)v), -1.0f / std::sqrt(1.0f - v * v));
+            break;
+        case oslg::OP_ATAN: res = dualfunc(X, (float)std::atan((double)v), 1.0f / (1.0f + v * v)); break;
+        case oslg::OP_SINH: res = dualfunc(X, (float)std::sinh((double)v), (float)std::cosh((double)v)); break;
+        case oslg::OP_COSH: res = dualfunc(X, (float)std::cosh((double)v), (float)std::sinh((double)v)); break;
+        case oslg::OP_TANH: {
+            float ch = (float)std::cosh((double)v);
+            res = dualfunc(X, (float)std::tanh((double)v), 1.0f / (ch * ch));
+            break;
+        }
+        case oslg::OP_EXP: { float f = (float)std::exp((double)v); res = dualfunc(X, f, f); break; }
+        case oslg::OP_EXP2: { float f = (float)std::exp2((double)v); res = dualfunc(X, f, f * 0.693147180559945309417f); break; }
+        case oslg::OP_EXPM1: res = dualfunc(X, (float)std::expm1((double)v), (float)std::exp((double)v)); break;
+        case oslg::OP_LOG: res = dualfunc(X, safe_log(v), v < kMin ? 0.0f : 1.0f / v); break;
+        case oslg::OP_LOG2: res = dualfunc(X, safe_log2(v), v < kMin ? 0.0f : 1.0f / (v * 0.693147180559945309417f)); break;
+        case oslg::OP_LOG10: res = dualfunc(X, safe_log10(v), v < kMin ? 0.0f : 1.0f / (v * 2.30258509299404568402f)); break;
+        case oslg::OP_RADIANS: res = X * (3.14159265358979323846f / 180.0f); break;
+        case oslg::OP_DEGREES: res = X * (180.0f / 3.14159265358979323846f); break;
+        default: res = X; break;
+        }
+        if (!has && res.dx != 0.0f) res.dx = 0.0f;
+        if (!has && res.dy != 0.0f) res.dy = 0.0f;
+        if (atc(r) == oslg::TC_INT) { setw(P, r, c, (uint32_t)(int)res.v); continue; }
+        putd(P, r, c, res);
+    }
+}
+
+void op_binary(Point& P, const uint32_t* a, uint16_t code) {
+    uint32_t r = a[0], x = a[1], y = a[2];
+    int nc = anc(r);
+    bool rd = ader(r);
+    for (int c = 0; c < nc; ++c) {
+        DF u = getd(P, x, c), v = getd(P, y, c);
+        DF res;
+        switch (code) {
+        case oslg::OP_POW:
+            if (rd && (ader(x) || ader(y))) {
+                // dual.h:1059-1067
+                float powuvm1 = safe_pow(u.v, v.v - 1.0f);
+                float powuv = powuvm1 * u.v;
+                float logu = u.v > 0.0f ? safe_log(u.v) : 0.0f;
+                float du = v.v * powuvm1, dv = logu * powuv;
+                res = DF(powuv, du * u.dx + dv * v.dx, du * u.dy + dv * v.dy);
+            } else {
+                res = DF(safe_pow(u.v, v.v));
+            }
+            break;
+        case oslg::OP_ATAN2: {
+            // dual.h:1018-1023 (y = first operand)
+            float f = (float)std::atan2((double)u.v, (double)v.v);
+            float denom = (v.v == 0.0f && u.v == 0.0f) ? 0.0f : 1.0f / (v.v * v.v + u.v * u.v);
+            float dfdy = -v.v * denom, dfdx = u.v * denom;
+            res = DF(f, dfdy * u.dx + dfdx * v.dx, dfdy * u.dy + dfdx * v.dy);
+            break;
+        }
+        case oslg::OP_FMOD: res = DF(safe_fmod(u.v, v.v), u.dx, u.dy); break;
+        case oslg::OP_MIN: res = u.v <= v.v ? u : v; break;
+        case oslg::OP_MAX: res = u.v > v.v ? u : v; break;
+        default: res = DF(v.v < u.v ? 0.0f : 1.0f); break;  // step(edge, x)
+        }
+        if (!rd) { putv(P, r, c, res.v); continue; }
+        putd(P, r, c, res);
+    }
+}
+
+void op_dot(Point& P, const uint32_t* a) {
+    DF ax = getd(P, a[1], 0), ay = getd(P, a[1], 1), az = getd(P, a[1], 2);
+    DF bx = getd(P, a[2], 0), by = getd(P, a[2], 1), bz = getd(P, a[2], 2);
+    if (!ader(a[0])) { putv(P, a[0], 0, ax.v * bx.v + ay.v * by.v + az.v * bz.v); return; }
+    putd(P, a[0], 0, ax * bx + ay * by + az * bz);
+}
+void op_cross(Point& P, const uint32_t* a) {
+    DF ax = getd(P, a[1], 0), ay = getd(P, a[1], 1), az = getd(P, a[1], 2);
+    DF bx = getd(P, a[2], 0), by = getd(P, a[2], 1), bz = getd(P, a[2], 2);
+    if (!ader(a[0])) {
+        putv(P, a[0], 0, ay.v * bz.v - az.v * by.v);
+        putv(P, a[0], 1, az.v * bx.v - ax.v * bz.v);
+        putv(P, a[0], 2, ax.v * by.v - ay.v * bx.v);
+        return;
+    }
+    putd(P, a[0], 0, ay * bz - az * by);
+    putd(P, a[0], 1, az * bx - ax * bz);
+    putd(P, a[0], 2, ax * by - ay * bx);
+}
+inline DF dsqrt(const DF& a) {
+    if (a.v > 0.0f) { float f = std::sqrt(a.v); return dualfunc(a, f, 0.5f / f); }
+    return DF(0.0f);
+}
+// Imath Vec3<float>::length()
+float imath_length(float x, float y, float z) {
+    float l2 = x * x + y * y + z * z;
+    if (l2 < 2.0f * FLT_MIN) {
+        float m = std::max(std::fabs(x), std::max(std::fabs(y), std::fabs(z)));
+        if (m == 0.0f) return 0.0f;
+        x /= m; y /= m; z /= m;
+        return m * std::sqrt(x * x + y * y + z * z);
+    }
+    return std::sqrt(l2);
+}
+void op_length(Point& P, const uint32_t* a, bool distance) {
+    DF x = getd(P, a[1], 0), y = getd(P, a[1], 1), z = getd(P, a[1], 2);
+    if (distance) { x = x - getd(P, a[2], 0); y = y - getd(P, a[2], 1); z = z - getd(P, a[2], 2); }
+    if (!ader(a[0])) {
+        putv(P, a[0], 0, distance ? std::sqrt(x.v * x.v + y.v * y.v + z.v * z.v) : imath_length(x.v, y.v, z.v));
+        return;
+    }
+    putd(P, a[0], 0, dsqrt(x * x + y * y + z * z));
+}
+void op_normalize(Point& P, const uint32_t* a) {
+    DF x = getd(P, a[1], 0), y = getd(P, a[1], 1), z = getd(P, a[1], 2);
+    if (!ader(a[0])) {
+        float len = std::sqrt(x.v * x.v + y.v * y.v + z.v * z.v);
+        float inv = len > 0.0f ? 1.0f / len : 0.0f;
+        if (len > 0.0f) { putv(P, a[0], 0, x.v * inv); putv(P, a[0], 1, y.v * inv); putv(P, a[0], 2, z.v * inv); }
+        else for (int c = 0; c < 3; ++c) putv(P, a[0], c, 0.0f);
+        return;
+    }
+    DF len = dsqrt(x * x + y * y + z * z);
+    if (len.v > 0.0f) {
+        DF inv = 1.0f / len;
+        putd(P, a[0], 0, x * inv); putd(P, a[0], 1, y * inv); putd(P, a[0], 2, z * inv);
+    } else {
+        for (int c = 0; c < 3; ++c) putd(P, a[0], c, DF(0.0f));
+    }
+}
+void op_transform(Point& P, const uint32_t* a) {
+    uint32_t r = a[0], p = a[1], m = a[2];
+    float M[4][4];
+    for (int i = 0; i < 16; ++i) M[i / 4][i % 4] = bitsf(word(P, m, i));
+    DF x = getd(P, p, 0), y = getd(P, p, 1), z = getd(P, p, 2);
+    if (a[3] == 0) {
+        if (!ader(r)) {
+            float A = x.v * M[0][0] + y.v * M[1][0] + z.v * M[2][0] + M[3][0];
+            float B = x.v * M[0][1] + y.v * M[1][1] + z.v * M[2][1] + M[3][1];
+            float C = x.v * M[0][2] + y.v * M[1][2] + z.v * M[2][2] + M[3][2];
+            float W = x.v * M[0][3] + y.v * M[1][3] + z.v * M[2][3] + M[3][3];
+            if (W != 0.0f) { putv(P, r, 0, A / W); putv(P, r, 1, B / W); putv(P, r, 2, C / W); }
+            else for (int c = 0; c < 3; ++c) putv(P, r, c, 0.0f);
+            return;
+        }
+        DF A = x * M[0][0] + y * M[1][0] + z * M[2][0] + M[3][0];
+        DF B = x * M[0][1] + y * M[1][1] + z * M[2][1] + M[3][1];
+        DF C = x * M[0][2] + y * M[1][2] + z * M[2][2] + M[3][2];
+        DF W = x * M[0][3] + y * M[1][3] + z * M[2][3] + M[3][3];
+        if (W.v != 0.0f) { putd(P, r, 0, A / W); putd(P, r, 1, B / W); putd(P, r, 2, C / W); }
+        else for (int c = 0; c < 3; ++c) putd(P, r, c, DF(0.0f));
+        return;
+    }
+    float in[3][3] = { { x.v, y.v, z.v }, { x.dx, y.dx, z.dx }, { x.dy, y.dy, z.dy } };
+    int nd = ader(r) ? 3 : 1;
+    for (int d = 0; d < nd; ++d) {
+        float X = in[d][0], Y = in[d][1], Z = in[d][2];
+        setf(P, r, d * 3 + 0, X * M[0][0] + Y * M[1][0] + Z * M[2][0]);
+        setf(P, r, d * 3 + 1, X * M[0][1] + Y * M[1][1] + Z * M[2][1]);
+        setf(P, r, d * 3 + 2, X * M[0][2] + Y * M[1][2] + Z * M[2][2]);
+    }
+}
+
+// noise (batched_llvm_gen.cpp:6032-6190 kinds; oslnoise.h wrappers)
+void op_noise(Point& P, const uint32_t* a) {
+    uint32_t r = a[0], S = a[1], T = a[2], kw = a[3];
+    int kind = (int)(kw & 15u);
+    bool periodic = (kw & 16u) != 0;
+    int dims = (int)((kw >> 5) & 7u);
+    bool vec = (kw & 256u) != 0;
+    bool derivs = (kw & 512u) != 0;
+    int ns = anc(S), nc = vec ? 3 : 1;
+    DF res[3];
+    Hasher H;
+    if (periodic) {
+        H.periodic = true;
+        if (ns == 3) {
+            H.px = Hasher::per(getf(P, a[4], 0, 0)); H.py = Hasher::per(getf(P, a[4], 1, 0));
+            H.pz = Hasher::per(getf(P, a[4], 2, 0));
+            if (dims == 4) H.pw = Hasher::per(getf(P, a[5], 0, 0));
+        } else {
+            H.px = Hasher::per(getf(P, a[4], 0, 0));
+            if (dims == 2) H.py = Hasher::per(getf(P, a[5], 0, 0));
+        }
+    }
+    DF xs[4];
+    for (int i = 0; i < ns; ++i) xs[i] = getd(P, S, i);
+    if (T != oslg::kNoArg) xs[ns] = getd(P, T, 0);
+    if (kind == oslg::NK_CELL || kind == oslg::NK_HASH) {
+        float v[4];
+        for (int i = 0; i < dims; ++i) v[i] = xs[i].v;
+        if (periodic) {
+            if (ns == 3) {
+                for (int i = 0; i < 3; ++i) v[i] = pwrap(v[i], getf(P, a[4], i, 0));
+                if (dims == 4) v[3] = pwrap(v[3], getf(P, a[5], 0, 0));
+            } else {
+                v[0] = pwrap(v[0], getf(P, a[4], 0, 0));
+                if (dims == 2) v[1] = pwrap(v[1], getf(P, a[5], 0, 0));
+            }
+        }
+        bool cell = kind == oslg::NK_CELL;
+        if (!vec) {
+            float f;
+            if (cell) f = dims == 1 ? intnoise1<CellKey>(v[0]) : dims == 2 ? intnoise2<CellKey>(v[0], v[1])
+                        : dims == 3 ? intnoise3<CellKey>(v[0], v[1], v[2]) : intnoise4<CellKey>(v[0], v[1], v[2], v[3]);
+            else f = dims == 1 ? intnoise1<HashKey>(v[0]) : dims == 2 ? intnoise2<HashKey>(v[0], v[1])
+                   : dims == 3 ? intnoise3<HashKey>(v[0], v[1], v[2]) : intnoise4<HashKey>(v[0], v[1], v[2], v[3]);
+            res[0] = DF(f);
+        } else {
+            V3 f;
+            if (cell) f = dims == 1 ? vintnoise1<CellKey>(v[0]) : dims == 2 ? vintnoise2<CellKey>(v[0], v[1])
+                        : dims == 3 ? vintnoise3<CellKey>(v[0], v[1], v[2]) : vintnoise4<CellKey>(v[0], v[1], v[2], v[3]);
+            else f = dims == 1 ? vintnoise1<HashKey>(v[0]) : dims == 2 ? vintnoise2<HashKey>(v[0], v[1])
+                   : dims == 3 ? vintnoise3<HashKey>(v[0], v[1], v[2]) : vintnoise4<HashKey>(v[0], v[1], v[2], v[3]);
+            for (int c = 0; c < 3; ++c) res[c] = DF(f[c]);
+        }
+    } else if (kind == oslg::NK_PERLIN || kind == oslg::NK_UPERLIN) {
+        for (int c = 0; c < nc; ++c) {
+            if (derivs) {
+                DF o = perlin_n<DF>(H, c, dims, xs);
+                res[c] = kind == oslg::NK_UPERLIN ? unsigned_of(o) : o;
+            } else {
+                float v[4];
+                for (int i = 0; i < dims; ++i) v[i] = xs[i].v;
+                float o = perlin_n<float>(H, c, dims, v);
+                res[c] = DF(kind == oslg::NK_UPERLIN ? unsigned_of(o) : o);
+            }
+        }
+    } else if (kind == oslg::NK_SIMPLEX || kind == oslg::NK_USIMPLEX) {
+        for (int c = 0; c < nc; ++c) {
+            DF o;
+            if (derivs) o = simplex_dual(dims, xs, c);
+            else {
+                float v[4];
+                for (int i = 0; i < dims; ++i) v[i] = xs[i].v;
+                o = DF(simplex_val(dims, v, c));
+            }
+            if (kind == oslg::NK_USIMPLEX) o = 0.5f * (o + 1.0f);
+            res[c] = o;
+        }
+    } else if (kind == oslg::NK_UNULL) {
+        for (int c = 0; c < nc; ++c) res[c] = DF(0.5f);
+    } else {
+        for (int c = 0; c < nc; ++c) res[c] = DF(0.0f);
+    }
+    int rn = anc(r);
+    for (int c = 0; c < rn; ++c) putd(P, r, c, res[nc == 1 ? 0 : c]);
+}
+
+void op_hash(Point& P, const uint32_t* a) {
+    uint32_t x = a[1], y = a[2];
+    int h;
+    uint32_t tx = atc(x);
+    if (tx == oslg::TC_INT) h = hash_i((int32_t)word(P, x, 0));
+    else if (tx == oslg::TC_STRING) h = (int)word(P, x, 0);
+    else if (tx == oslg::TC_TRIPLE) {
+        V3 p(bitsf(word(P, x, 0)), bitsf(word(P, x, 1)), bitsf(word(P, x, 2)));
+        h = y == oslg::kNoArg ? hash_v(p) : hash_vf(p, getf(P, y, 0, 0));
+    } else {
+        h = y == oslg::kNoArg ? hash_f(getf(P, x, 0, 0)) : hash_ff(getf(P, x, 0, 0), getf(P, y, 0, 0));
+    }
+    setw(P, a[0], 0, (uint32_t)h);
+}
+
+const oslg_field& gfield(const oslg_shaderglobals& G, int id) {
+    const oslg_field* f = &G.P;  // fields are laid out in GlobalId order
+    return f[id];
+}
+float fld(const oslg_field& f, int c, int64_t pt) { return f.data ? f.data[c * f.plane_stride + pt] : f.value[c]; }
+
+void op_load_global(Point& P, const uint32_t* a, const oslg_shaderglobals& G) {
+    uint32_t r = a[0];
+    int id = (int)a[1];
+    int nc = anc(r);
+    for (int c = 0; c < nc; ++c) setf(P, r, c, fld(gfield(G, id), c, P.pt));
+    if (ader(r)) {
+        int dxid = -1, dyid = -1;
+        if (id == oslg::G_P) { dxid = oslg::G_DPDX; dyid = oslg::G_DPDY; }
+        else if (id == oslg::G_I) { dxid = oslg::G_DIDX; dyid = oslg::G_DIDY; }
+        else if (id == oslg::G_U) { dxid = oslg::G_DUDX; dyid = oslg::G_DUDY; }
+        else if (id == oslg::G_V) { dxid = oslg::G_DVDX; dyid = oslg::G_DVDY; }
+        else if (id == oslg::G_PS) { dxid = oslg::G_DPSDX; dyid = oslg::G_DPSDY; }
+        for (int c = 0; c < nc; ++c) {
+            setf(P, r, nc + c, dxid >= 0 ? fld(gfield(G, dxid), c, P.pt) : 0.0f);
+            setf(P, r, 2 * nc + c, dyid >= 0 ? fld(gfield(G, dyid), c, P.pt) : 0.0f);
+        }
+    }
+}
+
+// closure pools, same layout the device uses (oslg_program.h)
+struct CPools { uint32_t base, maxc, maxt; };
+uint32_t tslot(const CPools& C, uint32_t i) { return C.base + 1 + C.maxc * oslg::kCompFloats + i * oslg::kTermFloats; }
+uint32_t cslot(const CPools& C, uint32_t i) { return C.base + 1 + i * oslg::kCompFloats; }
+bool alloc_terms(Point& P, const CPools& C, uint32_t n, uint32_t& first) {
+    uint32_t w = P.heap[C.base], top = w >> 16;
+    if (top + n > C.maxt) { P.status |= oslg::ST_CLOSURE_OVERFLOW; return false; }
+    first = top;
+    P.heap[C.base] = (w & 0xFFFFu) | ((top + n) << 16);
+    return true;
+}
+
+struct Runner {
+    const Prog& prog;
+    const oslg_shaderglobals& G;
+    char* userdata;
+    char* outputs;
+
+    void run_point(Point& P) {
+        const oslg::ProgramHeader& h = *prog.h;
+        CPools C{ h.closure_base, h.max_comps, h.max_terms };
+        if (h.flags & 1u) P.heap[C.base] = 0u;
+        int nops = (int)h.nops;
+        long long guard = 0;
+        for (int pc = 0; pc < nops;) {
+            const Op& op = prog.ops[pc];
+            const uint32_t* a = op.a;
+            if (++guard > (1ll << 30)) { P.status |= oslg::ST_TIMEOUT; return; }
+            switch (op.code) {
+            case oslg::OP_IF:
+                pc = truth(P, a[0]) ? pc + 1 : prog.partner[pc] + 1;
+                continue;
+            case oslg::OP_ELSE:  // reached at the end of the then-block
+                pc = prog.partner[pc];
+                continue;
+            case oslg::OP_LOOP_TEST:
+                pc = truth(P, a[0]) ? pc + 1 : prog.partner[pc];
+                continue;
+            case oslg::OP_JUMP: pc = (int)a[2]; continue;
+            case oslg::OP_BREAK: pc = prog.break_target[pc]; continue;
+            case oslg::OP_CONTINUE: pc = prog.continue_target[pc]; continue;
+            case oslg::OP_RETURN: pc = prog.layer_end_after[pc]; continue;
+            case oslg::OP_EXIT: pc = prog.outputs_start; continue;
+            case oslg::OP_NOP: case oslg::OP_ENDIF: case oslg::OP_LOOP_BEGIN: case oslg::OP_LOOP_STEP:
+            case oslg::OP_LOOP_END: case oslg::OP_LAYER_END:
+                break;
+            case oslg::OP_LOAD_GLOBAL: op_load_global(P, a, G); break;
+            case oslg::OP_LOAD_USERDATA: {
+                const uint32_t* q = reinterpret_cast<const uint32_t*>(userdata + (int64_t)a[1] + P.pt * (int64_t)(int32_t)a[2]);
+                int n = anc(a[0]) * (ader(a[0]) ? 3 : 1);
+                for (int i = 0; i < n; ++i) setw(P, a[0], i, q[i]);
+                break;
+            }
+            case oslg::OP_STORE_OUTPUT: {
+                uint32_t s = a[0], flags = a[3];
+                int elems = std::max(1, (int)a[4]);
+                int total = anc(s) * elems;
+                uint32_t* q = reinterpret_cast<uint32_t*>(outputs + (int64_t)a[1] + P.pt * (int64_t)(int32_t)a[2]);
+                int nd = (flags & 1u) ? 3 : 1;
+                for (int d = 0; d < nd; ++d)
+                    for (int i = 0; i < total; ++i) {
+                        uint32_t w;
+                        if (d > 0 && !ader(s)) w = 0u;
+                        else if (flags & 2u) w = (uint32_t)geti(P, s, i);
+                        else w = word(P, s, d * total + i);
+                        if (!(flags & 2u) && atc(s) == oslg::TC_INT) w = fbits((float)(int32_t)w);
+                        q[d * total + i] = w;
+                    }
+                break;
+            }
+            case oslg::OP_ASSIGN: op_assign(P, a); break;
+            case oslg::OP_COMPREF: {
+                int i = geti(P, a[2], 0);
+                if (i < 0 || i > 2) { P.status |= oslg::ST_ARRAY_BOUNDS; i = std::min(std::max(i, 0), 2); }
+                putd(P, a[0], 0, ader(a[1]) ? getd(P, a[1], i) : DF(getf(P, a[1], i, 0)));
+                break;
+            }
+            case oslg::OP_COMPASSIGN: {
+                int i = geti(P, a[1], 0);
+                if (i < 0 || i > 2) { P.status |= oslg::ST_ARRAY_BOUNDS; i = std::min(std::max(i, 0), 2); }
+                putd(P, a[0], i, getd(P, a[2], 0));
+                break;
+            }
+            case oslg::OP_MXCOMPREF: {
+                int rr = std::min(std::max(geti(P, a[2], 0), 0), 3), cc = std::min(std::max(geti(P, a[3], 0), 0), 3);
+                putv(P, a[0], 0, bitsf(word(P, a[1], rr * 4 + cc)));
+                break;
+            }
+            case oslg::OP_MXCOMPASSIGN: {
+                int rr = std::min(std::max(geti(P, a[1], 0), 0), 3), cc = std::min(std::max(geti(P, a[2], 0), 0), 3);
+                setf(P, a[0], rr * 4 + cc, getf(P, a[3], 0, 0));
+                break;
+            }
+            case oslg::OP_CONSTRUCT3:
+                for (int c = 0; c < 3; ++c) putd(P, a[0], c, getd(P, a[1 + c], 0));
+                break;
+            case oslg::OP_AREF: {
+                uint32_t r = a[0], arr = a[1];
+                int alen = (int)a[3], i = geti(P, a[2], 0);
+                if (i < 0 || i >= alen) { P.status |= oslg::ST_ARRAY_BOUNDS; i = std::min(std::max(i, 0), alen - 1); }
+                int nc = anc(arr);
+                for (int c = 0; c < nc; ++c) {
+                    uint32_t w = word(P, arr, i * nc + c);
+                    uint32_t tr = atc(r);
+                    if (tr == oslg::TC_INT || tr == oslg::TC_STRING || tr == oslg::TC_CLOSURE) { setw(P, r, c, w); continue; }
+                    float dx = 0, dy = 0;
+                    if (ader(arr)) {
+                        dx = bitsf(word(P, arr, alen * nc + i * nc + c));
+                        dy = bitsf(word(P, arr, 2 * alen * nc + i * nc + c));
+                    }
+                    putd(P, r, c, DF(atc(arr) == oslg::TC_INT ? (float)(int32_t)w : bitsf(w), dx, dy));
+                }
+                break;
+            }
+            case oslg::OP_AASSIGN: {
+                uint32_t arr = a[0], v = a[2];
+                int alen = (int)a[3], i = geti(P, a[1], 0);
+                if (i < 0 || i >= alen) { P.status |= oslg::ST_ARRAY_BOUNDS; i = std::min(std::max(i, 0), alen - 1); }
+                int nc = anc(arr);
+                for (int c = 0; c < nc; ++c) {
+                    int vc = anc(v) == 1 ? 0 : c;
+                    uint32_t ta = atc(arr);
+                    if (ta == oslg::TC_INT || ta == oslg::TC_STRING || ta == oslg::TC_CLOSURE) {
+                        setw(P, arr, i * nc + c, ta == oslg::TC_INT ? (uint32_t)geti(P, v, vc) : word(P, v, vc));
+                        continue;
+                    }
+                    setf(P, arr, i * nc + c, getf(P, v, vc, 0));
+                    if (ader(arr)) {
+                        setf(P, arr, alen * nc + i * nc + c, getf(P, v, vc, 1));
+                        setf(P, arr, 2 * alen * nc + i * nc + c, getf(P, v, vc, 2));
+                    }
+                }
+                break;
+            }
+            case oslg::OP_MATRIX_DIAG: {
+                float v = getf(P, a[1], 0, 0);
+                for (int i = 0; i < 16; ++i) setf(P, a[0], i, i % 5 == 0 ? v : 0.0f);
+                break;
+            }
+            case oslg::OP_ADD: op_arith(P, a, 0); break;
+            case oslg::OP_SUB: op_arith(P, a, 1); break;
+            case oslg::OP_MUL: op_arith(P, a, 2); break;
+            case oslg::OP_DIV: op_arith(P, a, 3); break;
+            case oslg::OP_MOD: op_arith(P, a, 4); break;
+            case oslg::OP_IADD: op_iarith(P, a, 0); break;
+            case oslg::OP_ISUB: op_iarith(P, a, 1); break;
+            case oslg::OP_IMUL: op_iarith(P, a, 2); break;
+            case oslg::OP_IDIV: op_iarith(P, a, 3); break;
+            case oslg::OP_IMOD: op_iarith(P, a, 4); break;
+            case oslg::OP_INEG: setw(P, a[0], 0, (uint32_t)(-geti(P, a[1], 0))); break;
+            case oslg::OP_MMUL: {
+                float out[16];
+                if (atc(a[1]) == oslg::TC_MATRIX && atc(a[2]) == oslg::TC_MATRIX) {
+                    float A[16], B[16];
+                    for (int i = 0; i < 16; ++i) { A[i] = bitsf(word(P, a[1], i)); B[i] = bitsf(word(P, a[2], i)); }
+                    for (int i = 0; i < 4; ++i)
+                        for (int j = 0; j < 4; ++j)
+                            out[i * 4 + j] = A[i * 4 + 0] * B[0 * 4 + j] + A[i * 4 + 1] * B[1 * 4 + j]
+                                           + A[i * 4 + 2] * B[2 * 4 + j] + A[i * 4 + 3] * B[3 * 4 + j];
+                } else {
+                    uint32_t m = atc(a[1]) == oslg::TC_MATRIX ? a[1] : a[2], s = atc(a[1]) == oslg::TC_MATRIX ? a[2] : a[1];
+                    float f = getf(P, s, 0, 0);
+                    for (int i = 0; i < 16; ++i) out[i] = bitsf(word(P, m, i)) * f;
+                }
+                for (int i = 0; i < 16; ++i) setf(P, a[0], i, out[i]);
+                break;
+            }
+            case oslg::OP_EQ: op_cmp(P, a, 0); break;
+            case oslg::OP_NEQ: op_cmp(P, a, 1); break;
+            case oslg::OP_LT: op_cmp(P, a, 2); break;
+            case oslg::OP_GT: op_cmp(P, a, 3); break;
+            case oslg::OP_LE: op_cmp(P, a, 4); break;
+            case oslg::OP_GE: op_cmp(P, a, 5); break;
+            case oslg::OP_AND: setw(P, a[0], 0, truth(P, a[1]) && truth(P, a[2]) ? 1u : 0u); break;
+            case oslg::OP_OR: setw(P, a[0], 0, truth(P, a[1]) || truth(P, a[2]) ? 1u : 0u); break;
+            case oslg::OP_BITAND: setw(P, a[0], 0, (uint32_t)(geti(P, a[1], 0) & geti(P, a[2], 0))); break;
+            case oslg::OP_BITOR: setw(P, a[0], 0, (uint32_t)(geti(P, a[1], 0) | geti(P, a[2], 0))); break;
+            case oslg::OP_XOR: setw(P, a[0], 0, (uint32_t)(geti(P, a[1], 0) ^ geti(P, a[2], 0))); break;
+            case oslg::OP_SHL: setw(P, a[0], 0, (uint32_t)geti(P, a[1], 0) << (geti(P, a[2], 0) & 31)); break;
+            case oslg::OP_SHR: setw(P, a[0], 0, (uint32_t)(geti(P, a[1], 0) >> (geti(P, a[2], 0) & 31))); break;
+            case oslg::OP_COMPL: setw(P, a[0], 0, ~(uint32_t)geti(P, a[1], 0)); break;
+            case oslg::OP_IABS: { int v = geti(P, a[1], 0); setw(P, a[0], 0, (uint32_t)(v < 0 ? -v : v)); break; }
+            case oslg::OP_NEG: case oslg::OP_ABS: case oslg::OP_FLOOR: case oslg::OP_CEIL: case oslg::OP_ROUND:
+            case oslg::OP_TRUNC: case oslg::OP_SIGN: case oslg::OP_SQRT: case oslg::OP_INVSQRT: case oslg::OP_CBRT:
+            case oslg::OP_SIN: case oslg::OP_COS: case oslg::OP_TAN: case oslg::OP_ASIN: case oslg::OP_ACOS:
+            case oslg::OP_ATAN: case oslg::OP_SINH: case oslg::OP_COSH: case oslg::OP_TANH: case oslg::OP_EXP:
+            case oslg::OP_EXP2: case oslg::OP_EXPM1: case oslg::OP_LOG: case oslg::OP_LOG2: case oslg::OP_LOG10:
+            case oslg::OP_RADIANS: case oslg::OP_DEGREES:
+                op_unary(P, a, op.code);
+                break;
+            case oslg::OP_ISNAN: setw(P, a[0], 0, std::isnan(getf(P, a[1], 0, 0)) ? 1u : 0u); break;
+            case oslg::OP_ISINF: setw(P, a[0], 0, std::isinf(getf(P, a[1], 0, 0)) ? 1u : 0u); break;
+            case oslg::OP_ISFINITE: setw(P, a[0], 0, std::isfinite(getf(P, a[1], 0, 0)) ? 1u : 0u); break;
+            case oslg::OP_POW: case oslg::OP_ATAN2: case oslg::OP_FMOD: case oslg::OP_MIN: case oslg::OP_MAX:
+            case oslg::OP_STEP:
+                op_binary(P, a, op.code);
+                break;
+            case oslg::OP_IMIN: { int x = geti(P, a[1], 0), y = geti(P, a[2], 0); setw(P, a[0], 0, (uint32_t)(x <= y ? x : y)); break; }
+            case oslg::OP_IMAX: { int x = geti(P, a[1], 0), y = geti(P, a[2], 0); setw(P, a[0], 0, (uint32_t)(x > y ? x : y)); break; }
+            case oslg::OP_CLAMP: {
+                int nc = anc(a[0]);
+                for (int c = 0; c < nc; ++c) {
+                    if (atc(a[0]) == oslg::TC_INT) {
+                        int x = geti(P, a[1], c), lo = geti(P, a[2], c), hi = geti(P, a[3], c);
+                        x = x < lo ? lo : x;
+                        x = x > hi ? hi : x;
+                        setw(P, a[0], c, (uint32_t)x);
+                        continue;
+                    }
+                    DF x = getd(P, a[1], c), lo = getd(P, a[2], c), hi = getd(P, a[3], c);
+                    DF v = x.v < lo.v ? lo : x;
+                    v = v.v > hi.v ? hi : v;
+                    putd(P, a[0], c, v);
+                }
+                break;
+            }
+            case oslg::OP_MIX: {
+                int nc = anc(a[0]);
+                for (int c = 0; c < nc; ++c) {
+                    DF x = getd(P, a[1], c), y = getd(P, a[2], c), t = getd(P, a[3], c);
+                    // dual.h:1267-1272 via dualfunc of three variables
+                    float one_t = 1.0f - t.v;
+                    float v = x.v * one_t + y.v * t.v;
+                    float ymx = y.v - x.v;
+                    putd(P, a[0], c, DF(v, one_t * x.dx + t.v * y.dx + ymx * t.dx, one_t * x.dy + t.v * y.dy + ymx * t.dy));
+                }
+                break;
+            }
+            case oslg::OP_SMOOTHSTEP: {
+                int nc = anc(a[0]);
+                for (int c = 0; c < nc; ++c) {
+                    DF e0 = getd(P, a[1], c), e1 = getd(P, a[2], c), x = getd(P, a[3], c);
+                    DF res;
+                    if (x.v < e0.v) res = DF(0.0f);
+                    else if (x.v >= e1.v) res = DF(1.0f);
+                    else if (!ader(a[0])) {
+                        float t = (x.v - e0.v) / (e1.v - e0.v);
+                        res = DF((3.0f - 2.0f * t) * (t * t));
+                    } else {
+                        // dual.h:1325-1336
+                        DF t = (x - e0) / (e1 - e0);
+                        res = (3.0f - 2.0f * t) * t * t;
+                    }
+                    putd(P, a[0], c, res);
+                }
+                break;
+            }
+            case oslg::OP_SELECT: {
+                int nc = anc(a[0]);
+                for (int c = 0; c < nc; ++c) {
+                    bool cond = atc(a[3]) == oslg::TC_TRIPLE ? getf(P, a[3], c, 0) != 0.0f : truth(P, a[3]);
+                    if (atc(a[0]) == oslg::TC_INT) { setw(P, a[0], c, (uint32_t)geti(P, cond ? a[2] : a[1], c)); continue; }
+                    putd(P, a[0], c, getd(P, cond ? a[2] : a[1], c));
+                }
+                break;
+            }
+            case oslg::OP_DOT: op_dot(P, a); break;
+            case oslg::OP_CROSS: op_cross(P, a); break;
+            case oslg::OP_LENGTH: op_length(P, a, false); break;
+            case oslg::OP_DISTANCE: op_length(P, a, true); break;
+            case oslg::OP_NORMALIZE: op_normalize(P, a); break;
+            case oslg::OP_DX: case oslg::OP_DY: {
+                int d = op.code == oslg::OP_DX ? 1 : 2;
+                for (int c = 0; c < anc(a[0]); ++c) putv(P, a[0], c, getf(P, a[1], c, d));
+                break;
+            }
+            case oslg::OP_TRANSFORM: op_transform(P, a); break;
+            case oslg::OP_NOISE: op_noise(P, a); break;
+            case oslg::OP_HASH: op_hash(P, a); break;
+            case oslg::OP_CLOSURE: {
+                uint32_t w = P.heap[C.base], n = w & 0xFFFFu;
+                if (n >= C.maxc) { P.status |= oslg::ST_CLOSURE_OVERFLOW; setw(P, a[0], 0, 0u); break; }
+                uint32_t cs = cslot(C, n);
+                P.heap[cs] = a[1];
+                uint32_t params[14];
+                int np = 0;
+                for (int i = 2; i < 7; ++i) params[np++] = a[i];
+                if (pc + 1 < nops && prog.ops[pc + 1].code == oslg::OP_NOP && prog.ops[pc + 1].nargs == 7)
+                    for (int i = 0; i < 7; ++i) params[np++] = prog.ops[pc + 1].a[i];
+                int k = 0;
+                for (int i = 0; i < np && k < oslg::kClosureParamFloats; ++i) {
+                    if (params[i] == oslg::kNoArg) break;
+                    for (int c = 0; c < anc(params[i]) && k < oslg::kClosureParamFloats; ++c) {
+                        uint32_t t = atc(params[i]);
+                        P.heap[cs + 1 + k++] = (t == oslg::TC_INT || t == oslg::TC_STRING) ? word(P, params[i], c)
+                                                                                            : fbits(getf(P, params[i], c, 0));
+                    }
+                }
+                P.heap[C.base] = (w & 0xFFFF0000u) | (n + 1);
+                uint32_t first;
+                if (!alloc_terms(P, C, 1, first)) { setw(P, a[0], 0, 0u); break; }
+                uint32_t ts = tslot(C, first);
+                P.heap[ts] = n;
+                P.heap[ts + 1] = P.heap[ts + 2] = P.heap[ts + 3] = fbits(1.0f);
+                setw(P, a[0], 0, (first << 16) | 1u);
+                break;
+            }
+            case oslg::OP_CLOSURE_MUL: {
+                uint32_t hh = word(P, a[1], 0), cnt = hh & 0xFFFFu, src = hh >> 16;
+                if (!cnt) { setw(P, a[0], 0, 0u); break; }
+                float w[3] = { getf(P, a[2], 0, 0), getf(P, a[2], 1, 0), getf(P, a[2], 2, 0) };
+                uint32_t first;
+                if (!alloc_terms(P, C, cnt, first)) { setw(P, a[0], 0, 0u); break; }
+                for (uint32_t i = 0; i < cnt; ++i) {
+                    uint32_t s = tslot(C, src + i), d = tslot(C, first + i);
+                    P.heap[d] = P.heap[s];
+                    for (int k = 0; k < 3; ++k) P.heap[d + 1 + k] = fbits(bitsf(P.heap[s + 1 + k]) * w[k]);
+                }
+                setw(P, a[0], 0, (first << 16) | cnt);
+                break;
+            }
+            case oslg::OP_CLOSURE_ADD: {
+                uint32_t ha = word(P, a[1], 0), hb = word(P, a[2], 0), ca = ha & 0xFFFFu, cb = hb & 0xFFFFu;
+                if (ca + cb == 0) { setw(P, a[0], 0, 0u); break; }
+                uint32_t first;
+                if (!alloc_terms(P, C, ca + cb, first)) { setw(P, a[0], 0, 0u); break; }
+                for (uint32_t i = 0; i < ca + cb; ++i) {
+                    uint32_t s = i < ca ? tslot(C, (ha >> 16) + i) : tslot(C, (hb >> 16) + i - ca), d = tslot(C, first + i);
+                    for (int k = 0; k < 4; ++k) P.heap[d + k] = P.heap[s + k];
+                }
+                setw(P, a[0], 0, (first << 16) | (ca + cb));
+                break;
+            }
+            case oslg::OP_STORE_CLOSURE: {
+                uint32_t hh = word(P, a[0], 0), cnt = hh & 0xFFFFu, first = hh >> 16, maxc = a[3];
+                uint32_t* q = reinterpret_cast<uint32_t*>(outputs + (int64_t)a[1] + P.pt * (int64_t)(int32_t)a[2]);
+                uint32_t n = std::min(cnt, maxc);
+                q[0] = n;
+                for (uint32_t i = 0; i < n; ++i) {
+                    uint32_t ts = tslot(C, first + i), cs = cslot(C, P.heap[ts]);
+                    uint32_t* rec = q + 1 + i * (4 + oslg::kClosureParamFloats);
+                    rec[0] = P.heap[cs];
+                    for (int k = 0; k < 3; ++k) rec[1 + k] = P.heap[ts + 1 + k];
+                    for (int k = 0; k < oslg::kClosureParamFloats; ++k) rec[4 + k] = P.heap[cs + 1 + k];
+                }
+                break;
+            }
+            default:
+                P.status |= oslg::ST_BAD_OPCODE;
+                break;
+            }
+            ++pc;
+        }
+    }
+};
+
+bool resolve(Prog& p, const void* blob, size_t bytes) {
+    if (bytes < sizeof(oslg::ProgramHeader)) return false;
+    p.h = static_cast<const oslg::ProgramHeader*>(blob);
+    if (p.h->magic != oslg::kProgramMagic) return false;
+    size_t need = sizeof(oslg::ProgramHeader) + (size_t)p.h->nops * sizeof(Op) + (size_t)p.h->nconst * 4;
+    if (bytes < need) return false;
+    p.ops = reinterpret_cast<const Op*>(static_cast<const uint8_t*>(blob) + sizeof(oslg::ProgramHeader));
+    p.pool = reinterpret_cast<const uint32_t*>(p.ops + p.h->nops);
+    int n = (int)p.h->nops;
+    p.partner.assign(n, n);
+    p.break_target.assign(n, n);
+    p.continue_target.assign(n, n);
+    p.layer_end_after.assign(n, n);
+    for (int i = 0; i < n; ++i) {
+        const Op& o = p.ops[i];
+        if (o.code == oslg::OP_IF || o.code == oslg::OP_ELSE || o.code == oslg::OP_LOOP_TEST) p.partner[i] = (int)o.a[2];
+    }
+    // BREAK/CONTINUE: the enclosing loop's LOOP_END / LOOP_STEP with the same level tag
+    for (int i = 0; i < n; ++i) {
+        const Op& o = p.ops[i];
+        if (o.code == oslg::OP_BREAK || o.code == oslg::OP_CONTINUE) {
+            for (int j = i + 1; j < n; ++j) {
+                const Op& q = p.ops[j];
+                if (q.a[3] != o.a[3]) continue;
+                if (o.code == oslg::OP_BREAK && q.code == oslg::OP_LOOP_END) { p.break_target[i] = j; break; }
+                if (o.code == oslg::OP_CONTINUE && q.code == oslg::OP_LOOP_STEP) { p.continue_target[i] = j; break; }
+            }
+        }
+        if (o.code == oslg::OP_RETURN)
+            for (int j = i + 1; j < n; ++j)
+                if (p.ops[j].code == oslg::OP_LAYER_END) { p.layer_end_after[i] = j; break; }
+    }
+    p.outputs_start = n;
+    for (int j = n - 1; j >= 0; --j)
+        if (p.ops[j].code == oslg::OP_LAYER_END) { p.outputs_start = j + 1; break; }
+    return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Run a lowered program over points [begin, end) on the host. Globals,
+// userdata and outputs are host memory with the device layout.
+int oracle_run(const void* blob, size_t bytes, int64_t begin, int64_t end, const oslg_shaderglobals* G,
+               void* userdata, void* outputs, int nthreads, uint32_t* status_out) {
+    Prog p;
+    if (!resolve(p, blob, bytes)) return 1;
+    uint32_t status = 0;
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel num_threads(nthreads) reduction(| : status)
+#endif
+    {
+        Runner R{ p, *G, static_cast<char*>(userdata), static_cast<char*>(outputs) };
+        Point P;
+        P.heap.assign(p.h->heap_slots + 1, 0u);
+        P.pool = p.pool;
+#ifdef _OPENMP
+#pragma omp for schedule(static, 16)
+#endif
+        for (int64_t i = begin; i < end; ++i) {
+            P.pt = i;
+            P.status = 0;
+            R.run_point(P);
+            status |= P.status;
+        }
+    }
+    if (status_out) *status_out = status;
+    return 0;
+}
+
+// Scalar noise entry for known-answer tests: kind as NoiseKind, `in` holds
+// up to 4 Dual2 inputs (val,dx,dy each), out 3 Dual2 results.
+void oracle_noise(int kind, int dims, int vec, int derivs, int periodic, const float* in, const float* periods,
+                  float* out) {
+    Point P;
+    // lay the operands out in a tiny heap: S (3 comps + derivs) at 0, T at 9,
+    // result at 12, periods at 21..24
+    P.heap.assign(32, 0u);
+    P.pool = nullptr;
+    P.pt = 0;
+    int ns = dims >= 3 ? 3 : 1;
+    for (int c = 0; c < ns; ++c)
+        for (int d = 0; d < 3; ++d) P.heap[d * ns + c] = fbits(in[c * 3 + d]);
+    if (dims == 2 || dims == 4)
+        for (int d = 0; d < 3; ++d) P.heap[9 + d] = fbits(in[ns * 3 + d]);
+    for (int i = 0; i < 4; ++i) P.heap[21 + i] = fbits(periods ? periods[i] : 1.0f);
+    uint32_t a[7];
+    a[0] = oslg::arg_make(12, false, true, vec ? oslg::TC_TRIPLE : oslg::TC_FLOAT);
+    a[1] = oslg::arg_make(0, false, true, ns == 3 ? oslg::TC_TRIPLE : oslg::TC_FLOAT);
+    a[2] = (dims == 2 || dims == 4) ? oslg::arg_make(9, false, true, oslg::TC_FLOAT) : oslg::kNoArg;
+    a[3] = oslg::noise_word((uint32_t)kind, periodic != 0, dims, vec != 0, derivs != 0);
+    a[4] = oslg::arg_make(21, false, false, ns == 3 ? oslg::TC_TRIPLE : oslg::TC_FLOAT);
+    a[5] = oslg::arg_make(24, false, false, oslg::TC_FLOAT);
+    a[6] = 0;
+    if (!periodic && ns == 1 && dims == 2) a[4] = oslg::kNoArg;
+    op_noise(P, a);
+    int nr = vec ? 3 : 1;
+    for (int c = 0; c < nr; ++c)
+        for (int d = 0; d < 3; ++d) out[c * 3 + d] = bitsf(P.heap[12 + d * nr + c]);
+}
+
+int oracle_hash_f(float x) { return hash_f(x); }
+uint32_t oracle_inthash(const uint32_t* k, int n) {
+    switch (n) {
+    case 1: return inthash(k[0]);
+    case 2: return inthash(k[0], k[1]);
+    case 3: return inthash(k[0], k[1], k[2]);
+    case 4: return inthash(k[0], k[1], k[2], k[3]);
+    default: return inthash(k[0], k[1], k[2], k[3], k[4]);
+    }
+}
+
+}  // extern "C"

@@ -1,0 +1,118 @@
+"""Generate the committed golden fixtures from the reference's own test data.
+
+Reads (in this container only) the reference testsuite's expected images
+and text outputs and writes small fixtures next to this script:
+  * noise-family images (uint8 TIFF, Deflate) -> <name>.npz, subsampled;
+  * testsuite/example-batched-deformer/ref/out.txt -> deformer_out.txt;
+  * src/liboslnoise/oslnoise_test.cpp known answers -> oslnoise_known.json.
+The GPU machine never reads the reference; tests read only these fixtures.
+
+TIFF decoding is a minimal baseline-TIFF reader (strips, Deflate or no
+compression, optional horizontal predictor) on top of zlib and numpy.
+"""
+import json
+import os
+import re
+import struct
+import sys
+import zlib
+
+import numpy as np
+
+REF = "/root/reference"
+HERE = os.path.dirname(os.path.abspath(__file__))
+STEP = 4  # keep every 4th pixel in x and y
+
+
+def read_tiff(path):
+    data = open(path, "rb").read()
+    bo = "<" if data[:2] == b"II" else ">"
+    (ifd,) = struct.unpack(bo + "I", data[4:8])
+    (n,) = struct.unpack(bo + "H", data[ifd:ifd + 2])
+    tags = {}
+    tsize = {1: 1, 2: 1, 3: 2, 4: 4, 5: 8, 7: 1, 11: 4, 12: 8, 16: 8}
+    tfmt = {1: "B", 2: "c", 3: "H", 4: "I", 7: "B", 16: "Q"}
+    for i in range(n):
+        e = data[ifd + 2 + 12 * i: ifd + 14 + 12 * i]
+        tag, typ, cnt = struct.unpack(bo + "HHI", e[:8])
+        sz = tsize.get(typ, 1) * cnt
+        raw = e[8:12] if sz <= 4 else data[struct.unpack(bo + "I", e[8:12])[0]:][:sz]
+        if typ in tfmt:
+            vals = struct.unpack(bo + tfmt[typ] * cnt, raw[:sz])
+        else:
+            vals = raw
+        tags[tag] = vals
+    W, H = tags[256][0], tags[257][0]
+    spp = tags.get(277, (1,))[0]
+    bps = tags.get(258, (8,))[0]
+    comp = tags.get(259, (1,))[0]
+    pred = tags.get(317, (1,))[0]
+    offs, cnts = tags[273], tags[279]
+    rps = tags.get(278, (H,))[0]
+    assert bps == 8, "only 8-bit images are expected"
+    rows = []
+    for o, c in zip(offs, cnts):
+        chunk = data[o:o + c]
+        if comp in (8, 32946):
+            chunk = zlib.decompress(chunk)
+        elif comp != 1:
+            raise ValueError("compression %d not supported" % comp)
+        rows.append(np.frombuffer(chunk, np.uint8))
+    img = np.concatenate(rows)[: W * H * spp].reshape(H, W, spp).copy()
+    if pred == 2:
+        img = np.cumsum(img.astype(np.uint16), axis=1).astype(np.uint8)
+    return img
+
+
+IMAGES = {
+    # fixture name: (reference path, note)
+    "noise": "testsuite/noise/ref/out.tif",
+    "cellnoise": "testsuite/cellnoise/ref/out.tif",
+    "hashnoise": "testsuite/hashnoise/ref/out.tif",
+    "hashnoise_alt_batch": "testsuite/hashnoise/ref/out-alt-batch.tif",
+    "hashnoise_fma": "testsuite/hashnoise/ref/out_LLVM_JIT_FMA.tif",
+    "noise_perlin": "testsuite/noise-perlin/ref/out.tif",
+    "noise_cell": "testsuite/noise-cell/ref/out.tif",
+    "noise_simplex": "testsuite/noise-simplex/ref/out.tif",
+    "noise_gabor": "testsuite/noise-gabor/ref/out.tif",
+}
+
+
+def known_answers():
+    src = open(os.path.join(REF, "src/liboslnoise/oslnoise_test.cpp")).read()
+    out = {}
+    for name in ["results_1d", "results_2d", "results_3d", "results_4d"]:
+        for fn in ["test_perlin", "test_cell"]:
+            body = src.split("void\n" + fn)[1].split("\n}\n")[0]
+            m = re.search(r"static float %s\[[^\]]*\]\s*=\s*\{([^}]*)\}" % name, body)
+            if m:
+                out[fn + "." + name] = [float(x) for x in m.group(1).replace("\n", " ").split(",") if x.strip()]
+        for fn in ["test_perlin", "test_cell"]:
+            body = src.split("void\n" + fn)[1].split("\n}\n")[0]
+            m = re.search(r"static Vec3 v%s\[[^\]]*\]\s*=\s*\{(.*?)\};" % name, body, re.S)
+            if m:
+                vecs = re.findall(r"Vec3\(([^)]*)\)", m.group(1))
+                out[fn + ".v" + name] = [[float(t) for t in v.split(",")] for v in vecs]
+    return out
+
+
+def main():
+    if not os.path.isdir(REF):
+        print("reference tree not present; fixtures are already committed")
+        return 0
+    for name, rel in IMAGES.items():
+        img = read_tiff(os.path.join(REF, rel))
+        H, W = img.shape[:2]
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), img=img[::STEP, ::STEP], full_w=W, full_h=H,
+                            step=STEP)
+        print(name, img.shape)
+    ref_txt = open(os.path.join(REF, "testsuite/example-batched-deformer/ref/out.txt")).read()
+    open(os.path.join(HERE, "deformer_out.txt"), "w").write(ref_txt)
+    ka = known_answers()
+    json.dump(ka, open(os.path.join(HERE, "oslnoise_known.json"), "w"), indent=1)
+    print("known answers:", sorted(ka))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
