@@ -1,0 +1,344 @@
+"""Benchmark: shading throughput of the GB300 executor.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl ours|reference]
+
+One step = one pass of the hot path (ShadingSystem batched execute of the
+workload's shader group) over the workload's points, inputs resident in
+HBM. Device time is measured with CUDA events on the launching stream
+around each step; L2 is flushed (a 512 MiB write) between timed steps, so
+every step reads its inputs from HBM. `e2e` repeats the measurement
+through the public API with host buffers: pinned host->device copy of the
+per-point inputs, the launch, device->host copy of the outputs.
+
+--impl reference times the reference's batched CPU semantics on this
+host's cores: the reference itself cannot be built here (LLVM, OIIO,
+Imath absent) and its batched targets are x86-only, so the CPU port of
+the reference algorithm (oracle/) stands in, with every host thread.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+METRIC = "Mpoints/s shaded at stated ulp match; p50/p99 latency: served vs plain GPU"
+UNIT = "Mpoints/s"
+
+
+def _peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu=0):
+        self.gpu, self.rows, self.proc = gpu, [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        return False
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, n in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+# ---- workloads ----------------------------------------------------------------------------
+class FbmCell:
+    """Single-layer pattern shader: 4-octave vector Perlin fBm with Dual2
+    derivatives at P=(8u,8v,0) plus hash(cellnoise(P*4)); 1024x1024 grid,
+    u,v at pixel centres; outputs Cout with x/y derivatives and the int."""
+    name = "fbm_cell_1024x1024"
+    rec = 10  # Cout val/dx/dy (9 floats) + cellhash
+
+    def __init__(self, W=1024, H=1024):
+        self.W, self.H, self.n = W, H, W * H
+
+    def build(self, torch, og, shaders):
+        from helpers import grid_globals, pixel_grid, single_layer_group
+        self.ss = og.ShadingSystem()
+        self.g = single_layer_group(self.ss, "fbm_cell", shaders.fbm_cell(), outputs=[
+            og.SymLocationDesc("layer1.Cout", og.TypeColor, True, og.SymArenaOutputs, 0, 4 * self.rec),
+            og.SymLocationDesc("layer1.cellhash", og.TypeInt, False, og.SymArenaOutputs, 36, 4 * self.rec)])
+        self.ss.optimize_group(self.g)
+        u, v = pixel_grid(self.W, self.H, centers=True)
+        self.h_u, self.h_v = u, v
+        self.d_uv = torch.from_numpy(np.stack([u, v])).cuda()
+        self.G = grid_globals(self.d_uv[0], self.d_uv[1], self.W, self.H, centers=True)
+        self.out = torch.zeros(self.n * self.rec, dtype=torch.float32, device="cuda")
+        # e2e buffers: pinned host inputs and outputs
+        self.pin_uv = torch.from_numpy(np.stack([u, v])).pin_memory()
+        self.pin_out = torch.zeros(self.n * self.rec, dtype=torch.float32).pin_memory()
+        self.bytes_in = 8 * self.n
+        self.bytes_out = 4 * self.rec * self.n
+
+    def step(self, stream):
+        self.ss.execute_batch(self.g, self.n, self.G, 0, self.out.data_ptr(), stream)
+
+    def e2e_step(self, torch, stream):
+        self.d_uv.copy_(self.pin_uv, non_blocking=True)
+        self.ss.execute_batch(self.g, self.n, self.G, 0, self.out.data_ptr(), stream)
+        self.pin_out.copy_(self.out, non_blocking=True)
+
+    def algorithmic_bytes(self):
+        # read u,v (8 B) + write Cout val/dx/dy (36 B) + cell hash (4 B)
+        return 48 * self.n
+
+    def lane_ops_per_point(self):
+        # FP32+INT32 operations of the reference algorithm per point, counted
+        # from its operation sequence: one Dual2<Vec3> 3-D Perlin lookup is
+        # 1184 (floorfrac 9, 3 Dual2 fades 99, 8 lookup3 hashes 200, 3 channels
+        # x (8 Dual2 grads 160 + Dual2 trilerp 128 + scale 3)), each octave adds
+        # 45 for the Dual2 fBm accumulate; cell noise + hash + setup 80.
+        return 4 * (1184 + 45) + 80
+
+    def oracle_sample(self, oracle_run, og, n):
+        from helpers import grid_globals
+        n = min(n, self.n)
+        G = grid_globals(self.h_u, self.h_v, self.W, self.H, centers=True)
+        out = np.zeros((self.n, self.rec), np.float32)
+        return lambda: oracle_run(self.g.program_bytes(), n, G, out)
+
+
+WORKLOADS = {FbmCell.name: FbmCell}
+DEFAULT_WORKLOAD = FbmCell.name
+
+
+def cpu_reference(wl, og, budget_s=2.0):
+    """Time the CPU port of the reference semantics on all host threads."""
+    from helpers import oracle_run
+    n = 4096
+    while True:
+        run = wl.oracle_sample(oracle_run, og, n)
+        t0 = time.perf_counter()
+        run()
+        dt = time.perf_counter() - t0
+        if dt > 0.25 * budget_s or n >= wl.n:
+            break
+        n = min(wl.n, n * 4)
+    reps = max(1, int(budget_s / max(dt, 1e-6)))
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        run()
+    dt = (time.perf_counter() - t0) / reps
+    return n / dt / 1e6, n, reps
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    import openshadinglanguage_gb300 as og
+    from openshadinglanguage_gb300 import shaders
+    from oracle.build import build as build_oracle
+
+    wl = WORKLOADS[args.workload]()
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        build_oracle()
+        import torch  # noqa: F401  (import order matches the GPU arm)
+        # the oracle needs the lowered program; lowering is host-only
+        wl.ss = og.ShadingSystem()
+        from helpers import single_layer_group  # noqa: F401
+        wl.build_host_only = True
+        _build_host(wl, og, shaders)
+        rates = []
+        for _ in range(args.warmup):
+            cpu_reference(wl, og, budget_s=0.5)
+        for _ in range(args.steps):
+            r, n, reps = cpu_reference(wl, og, budget_s=1.0)
+            rates.append(r)
+        v = float(np.mean(rates))
+        cores = os.cpu_count()
+        line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1e3 * n / (v * 1e6), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "impl": "reference",
+                "config": {"workload": wl.name, "points": wl.n, "sample_points_per_step": n},
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                                 "sample": "%d of %d points per step, OpenMP over %d threads" % (n, wl.n, cores)},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                "note": "reference batched CPU path not buildable here (LLVM/OIIO/Imath absent) and x86-only; "
+                        "timed: the CPU port of its semantics (oracle/)"}
+        print(json.dumps(line))
+        return 0
+
+    import torch
+    from openshadinglanguage_gb300.build import build as build_native
+    build_native()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    wl.build(torch, og, shaders)
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    for _ in range(args.warmup):
+        wl.step(sh)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier()
+    with ClockSampler(local_rank) as clk:
+        for i in range(args.steps):
+            flush.zero_()
+            evs[i][0].record(stream)
+            wl.step(sh)
+            evs[i][1].record(stream)
+        barrier()
+    times = [a.elapsed_time(b) for a, b in evs]  # ms
+    total_ms = float(np.sum(times))
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = wl.n * world / (ms_per_step * 1e-3) / 1e6
+    status = wl.ss.device_status()
+
+    # end to end through the public API with host buffers
+    for _ in range(2):
+        wl.e2e_step(torch, sh)
+    torch.cuda.synchronize()
+    e_evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier()
+    for i in range(args.steps):
+        flush.zero_()
+        e_evs[i][0].record(stream)
+        wl.e2e_step(torch, sh)
+        e_evs[i][1].record(stream)
+    barrier()
+    e_ms = float(np.mean([a.elapsed_time(b) for a, b in e_evs]))
+    e2e_value = wl.n * world / (e_ms * 1e-3) / 1e6
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return 0
+
+    peaks = _peaks()
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    clocks = clk.summary()
+    achieved_gbs = wl.algorithmic_bytes() / (ms_per_step * 1e-3) / 1e9
+    ops = wl.lane_ops_per_point() * wl.n / (ms_per_step * 1e-3) / 1e12
+    mhz_max = peaks.get("sm_max_mhz", 2070.0)
+    mhz_load = clocks.get("sm_mhz") or peaks.get("clocks_under_load", {}).get("sm_mhz_median", 1417.0)
+    alu_peak_max = sms * 128 * mhz_max * 1e6 / 1e12
+    alu_peak_load = sms * 128 * mhz_load * 1e6 / 1e12
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "traffic_%s.json" % wl.name)
+    if os.path.exists(prof):
+        traffic = json.load(open(prof)).get("bytes_per_launch")
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": wl.name, "points": wl.n, "l2": "flushed (512 MiB write) between timed steps",
+                   "parity": "bit-exact to the CPU oracle (non-FMA reference order) for floats and ints"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": wl.bytes_in,
+                "d2h_bytes_per_step": wl.bytes_out, "ms_per_step": e_ms},
+        "gpu_launches": args.steps,
+        "clocks": clocks,
+        "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved_gbs / hbm, "traffic": traffic,
+                     "note": "of measured HBM peak; the interpreter is ALU-issue bound, see roofline_alu"},
+        "roofline_alu": {"bound": "alu", "achieved": ops, "unit": "Tlane-op/s",
+                         "ops_per_point": wl.lane_ops_per_point(),
+                         "peak_at_max_clock": alu_peak_max, "frac_at_max_clock": ops / alu_peak_max,
+                         "peak_at_sampled_clock": alu_peak_load, "frac_at_sampled_clock": ops / alu_peak_load,
+                         "sms": sms},
+        "device_status": status,
+    }
+    if not args.no_cpu_baseline:
+        from helpers import oracle_run  # noqa: F401
+        build_oracle()
+        r, n, reps = cpu_reference(wl, og, budget_s=2.0)
+        line["cpu_baseline"] = {"value": r, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                                "sample": "%d of %d points, %d reps, OpenMP over all host threads" % (n, wl.n, reps)}
+    print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def _build_host(wl, og, shaders):
+    """Host-only setup for the CPU arm: lower the group and make inputs."""
+    from helpers import pixel_grid, single_layer_group
+    if isinstance(wl, FbmCell):
+        wl.g = single_layer_group(wl.ss, "fbm_cell", shaders.fbm_cell(), outputs=[
+            og.SymLocationDesc("layer1.Cout", og.TypeColor, True, og.SymArenaOutputs, 0, 4 * wl.rec),
+            og.SymLocationDesc("layer1.cellhash", og.TypeInt, False, og.SymArenaOutputs, 36, 4 * wl.rec)])
+        wl.h_u, wl.h_v = pixel_grid(wl.W, wl.H, centers=True)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

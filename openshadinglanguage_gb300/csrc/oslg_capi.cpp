@@ -205,8 +205,10 @@ int oslg_shader(oslg_system* sys, oslg_group* group, const char* shaderusage, co
         L.layername = (layername && *layername) ? layername : m->name;
         for (const InstanceParam& p : sys->pending_params) {
             int si = m->find_symbol(p.name);
-            if (si < 0 || (m->symbols[si].kind != SK_PARAM && m->symbols[si].kind != SK_OPARAM))
+            if (si < 0 || (m->symbols[si].kind != SK_PARAM && m->symbols[si].kind != SK_OPARAM)) {
+                sys->pending_params.clear();
                 return fail(sys, OSLG_ERR_ARG, "shader '" + m->name + "' has no parameter '" + p.name + "'");
+            }
             InstanceParam q = p;
             // keep the declared type (e.g. a float value for a color param broadcasts)
             const TypeSpec& decl = m->symbols[si].type;

@@ -246,3 +246,102 @@ def vadd():
     out = b.param("vector", "out", [0, 0, 0], output=True)
     b.op("add", out, a, bb)
     return b.text()
+
+
+def ctrlflow():
+    """Varying control flow: data-dependent trip counts, continue, break,
+    while, do-while, nested if/else and an early return.
+
+        shader ctrlflow(output float r = 0, output int count = 0)
+        {
+            float acc = 0;
+            int n = (int)(cellnoise(u*8, v*8) * 16);
+            for (int i = 0; i < n; ++i) {
+                if (i == 3) continue;
+                float x = noise("perlin", u*4 + i);
+                if (x > 0.3) { acc += x; if (acc > 2) break; }
+                else acc -= 0.1*x;
+                count += 1;
+            }
+            int j = 0;
+            while (j < n) { j += 2; if (j > 9) break; }
+            do { acc += 0.01; j -= 3; } while (j > 0);
+            if (v > 0.9) { r = acc; return; }
+            r = acc * 2 + j;
+        }
+    """
+    b = OsoBuilder("ctrlflow")
+    r = b.param("float", "r", 0.0, output=True)
+    count = b.param("int", "count", 0, output=True)
+    u, v = b.glob("float", "u"), b.glob("float", "v")
+    cf = lambda x: b.const("float", x)
+    ci = lambda x: b.const("int", x)
+    acc, n, i, x, j = (b.local(t, nm) for t, nm in
+                       (("float", "acc"), ("int", "n"), ("int", "i"), ("float", "x"), ("int", "j")))
+    b.op("assign", acc, cf(0.0))
+    u8, v8, cn, cn16 = b.tmp("float"), b.tmp("float"), b.tmp("float"), b.tmp("float")
+    b.op("mul", u8, u, cf(8.0))
+    b.op("mul", v8, v, cf(8.0))
+    b.op("cellnoise", cn, u8, v8)
+    b.op("mul", cn16, cn, cf(16.0))
+    b.op("assign", n, cn16)
+    cond = b.tmp("int")
+    with b.loop("for", cond) as L:
+        b.op("assign", i, ci(0))
+        L.cond()
+        b.op("lt", cond, i, n)
+        L.body()
+        e3 = b.tmp("int")
+        b.op("eq", e3, i, ci(3))
+        with b.if_(e3):
+            b.op("continue")
+        u4, fi, arg = b.tmp("float"), b.tmp("float"), b.tmp("float")
+        b.op("mul", u4, u, cf(4.0))
+        b.op("assign", fi, i)
+        b.op("add", arg, u4, fi)
+        b.op("noise", x, b.const("string", "perlin"), arg)
+        g = b.tmp("int")
+        b.op("gt", g, x, cf(0.3))
+        with b.if_(g) as br:
+            b.op("add", acc, acc, x)
+            g2 = b.tmp("int")
+            b.op("gt", g2, acc, cf(2.0))
+            with b.if_(g2):
+                b.op("break")
+            br.else_()
+            t = b.tmp("float")
+            b.op("mul", t, cf(0.1), x)
+            b.op("sub", acc, acc, t)
+        b.op("add", count, count, ci(1))
+        L.step()
+        b.op("add", i, i, ci(1))
+    b.op("assign", j, ci(0))
+    wc = b.tmp("int")
+    with b.loop("while", wc) as L:
+        L.cond()
+        b.op("lt", wc, j, n)
+        L.body()
+        b.op("add", j, j, ci(2))
+        g3 = b.tmp("int")
+        b.op("gt", g3, j, ci(9))
+        with b.if_(g3):
+            b.op("break")
+        L.step()
+    dc = b.tmp("int")
+    with b.loop("dowhile", dc) as L:
+        L.cond()
+        b.op("gt", dc, j, ci(0))
+        L.body()
+        b.op("add", acc, acc, cf(0.01))
+        b.op("sub", j, j, ci(3))
+        L.step()
+    g4 = b.tmp("int")
+    b.op("gt", g4, v, cf(0.9))
+    with b.if_(g4):
+        b.op("assign", r, acc)
+        b.op("return")
+    t2, fj = b.tmp("float"), b.tmp("float")
+    b.op("mul", t2, acc, cf(2.0))
+    b.op("assign", fj, j)
+    b.op("add", r, t2, fj)
+    return b.text()

@@ -62,7 +62,7 @@ def pixel_grid(W, H, centers=False):
     return uu, vv
 
 
-def testshade_globals(u, v, W, H, P=None, centers=False):
+def grid_globals(u, v, W, H, P=None, centers=False):
     """Uniform fields as testshade's setup_uniform_shaderglobals
     (testshade.cpp:1681-1775)."""
     du = 1.0 / W if centers else 1.0 / max(1, W - 1)
