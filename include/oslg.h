@@ -175,6 +175,27 @@ int oslg_device_status(oslg_system* sys, uint32_t* bits);
  * thread, heap placement (0 HBM scratch, 1 shared memory, -1 auto). */
 int oslg_set_launch(oslg_system* sys, int block, int points_per_thread, int heap_smem);
 
+/* Allocation-free variant of oslg_execute_batch. It has no counterpart in
+ * the reference. It is for callers that cannot allocate device memory: a
+ * renderer that hands out all HBM from its own pool under a fixed budget,
+ * or code that must not pay the implicit device synchronisation of
+ * cudaMalloc/cudaFree. It calls no allocation routine: the lowered program,
+ * the symbol heap and the status word live in one static device array of
+ * 32 MiB that every GPU loading the library holds until exit. Limits: the
+ * lowered program must be at most 64 KiB and one CTA's symbol heap must fit
+ * the rest of the array (otherwise OSLG_ERR_ARG with a message). The group
+ * must already be lowered (oslg_optimize_group), else OSLG_ERR_STATE.
+ * The first call on a device does a one-time set-up (resolves the array's
+ * device address, uploads a constant table); make that first call before
+ * any stream capture. Calls share the array and leave their contents in it
+ * (the status word is cleared at the start of each call); calls that
+ * overlap on the GPU race. With status_out == NULL the call only enqueues
+ * work; otherwise it waits for the stream, stores the kernel status bits
+ * and returns OSLG_ERR_DEVICE if any is set. */
+int oslg_execute_batch_noalloc(oslg_system* sys, oslg_group* group, int64_t npoints,
+                               const oslg_shaderglobals* globals, void* userdata_base,
+                               void* output_base, void* stream, uint32_t* status_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -79,6 +79,10 @@ _EXPORTS = {
                                                ctypes.c_void_p]),
     "oslg_device_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint32)]),
     "oslg_set_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "oslg_execute_batch_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                                  ctypes.POINTER(ShaderGlobalsC), ctypes.c_void_p,
+                                                  ctypes.c_void_p, ctypes.c_void_p,
+                                                  ctypes.POINTER(ctypes.c_uint32)]),
 }
 
 _lib = None

@@ -376,4 +376,26 @@ int oslg_set_launch(oslg_system* sys, int block, int points_per_thread, int heap
     return OSLG_OK;
 }
 
+// Allocation-free execute (see include/oslg.h): no lowering, no upload, no
+// device allocation; everything the kernel needs goes to a static array.
+int oslg_execute_batch_noalloc(oslg_system* sys, oslg_group* group, int64_t npoints,
+                               const oslg_shaderglobals* globals, void* userdata_base, void* output_base,
+                               void* stream, uint32_t* status_out) {
+    if (!sys || !group || !globals || npoints < 0) return OSLG_ERR_ARG;
+    ShaderGroup& g = group->g;
+    std::lock_guard<std::mutex> lock(g.mutex);
+    if (!g.compiled) return fail(sys, OSLG_ERR_STATE, "group must be lowered with oslg_optimize_group first");
+    std::string err;
+    uint32_t bits = 0;
+    int rc = device_execute_noalloc(g.compiled->blob.data(), g.compiled->blob.size(), g.compiled->header, npoints,
+                                    *globals, userdata_base, output_base, stream, sys->launch,
+                                    status_out ? &bits : nullptr, &err);
+    if (rc != OSLG_OK) return fail(sys, rc, err);
+    if (status_out) {
+        *status_out = bits;
+        if (bits) return fail(sys, OSLG_ERR_DEVICE, "kernel status bits " + std::to_string(bits));
+    }
+    return OSLG_OK;
+}
+
 }  // extern "C"

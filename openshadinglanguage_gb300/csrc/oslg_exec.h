@@ -39,4 +39,13 @@ int device_read_status(DeviceState& ds, void* stream, uint32_t* bits, std::strin
 
 int device_init(DeviceState& ds, std::string* err);
 
+// Allocation-free launch: the program, heap and status word live in a
+// fixed-size static device array (see oslg_kernels.cu). Copies the host
+// program blob into it, launches, and optionally waits and reports status.
+static const size_t kNoAllocScratchBytes = 32u << 20;  // whole static array
+static const size_t kNoAllocProgramBytes = 64u << 10;  // program area
+int device_execute_noalloc(const void* blob, size_t blob_bytes, const ProgramHeader& hdr, int64_t npoints,
+                           const oslg_shaderglobals& G, void* userdata, void* outputs, void* stream,
+                           const LaunchConfig& cfg, uint32_t* status_out, std::string* err);
+
 }  // namespace oslg

@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 
 #include "oslg_exec.h"
@@ -1361,6 +1362,133 @@ int device_read_status(DeviceState& ds, void* stream, uint32_t* bits, std::strin
     if (!cuda_ok(cudaMemsetAsync(ds.d_status, 0, 4, s), err, "status clear")) return OSLG_ERR_CUDA;
     if (!cuda_ok(cudaStreamSynchronize(s), err, "sync")) return OSLG_ERR_CUDA;
     *bits = v;
+    return OSLG_OK;
+}
+
+// ---- allocation-free entry ------------------------------------------------------------
+// For callers that cannot allocate device memory: a renderer that hands out
+// all HBM from its own pool under a fixed budget, or code that must not pay
+// the implicit device synchronisation of cudaMalloc/cudaFree between
+// launches. The HBM-heap interpreter runs with every piece of scratch it
+// needs inside one file-scope array of kNoAllocScratchBytes (32 MiB), held
+// by every GPU that loads this library until the process exits:
+//   [0, 256)                      status word
+//   [256, 256 + 64 KiB)           copy of the lowered program
+//   [256 + 64 KiB, 32 MiB)        symbol heap, one slice per resident CTA
+// Every call shares the array and leaves its contents behind; the status
+// word is cleared at the start of each call. Calls that overlap on the GPU
+// (different streams, or the same group from two host threads) race on it.
+namespace dev {
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+}
+
+namespace {
+struct NoAllocDevice {
+    bool ready = false;
+    unsigned char* base = nullptr;
+    int sm_count = 0;
+    int smem_optin = 0;
+};
+std::mutex g_noalloc_mutex;
+NoAllocDevice g_noalloc_dev[128];
+
+// One-time set-up per device, with that device current: resolve the
+// array's device address (the host-side symbol is only a stand-in) and
+// upload the simplex traversal table. Runs on the first call on a device.
+int noalloc_setup(int dev, NoAllocDevice& d, std::string* err) {
+    if (d.ready) return OSLG_OK;
+    void* p = nullptr;
+    if (!cuda_ok(cudaGetSymbolAddress(&p, dev::g_noalloc_scratch), err, "cudaGetSymbolAddress(scratch)"))
+        return OSLG_ERR_CUDA;
+    unsigned char t[64][4];
+    build_simplex4(t);
+    if (!cuda_ok(cudaMemcpyToSymbol(dev::c_simplex4, t, sizeof(t)), err, "simplex table")) return OSLG_ERR_CUDA;
+    if (!cuda_ok(cudaDeviceGetAttribute(&d.sm_count, cudaDevAttrMultiProcessorCount, dev), err, "sm count"))
+        return OSLG_ERR_CUDA;
+    cudaDeviceGetAttribute(&d.smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (!cuda_ok(cudaFuncSetAttribute(dev::interp_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      d.smem_optin),
+                 err, "kernel attribute"))
+        return OSLG_ERR_CUDA;
+    d.base = static_cast<unsigned char*>(p);
+    d.ready = true;
+    return OSLG_OK;
+}
+}  // namespace
+
+int device_execute_noalloc(const void* blob, size_t blob_bytes, const ProgramHeader& hdr, int64_t npoints,
+                           const oslg_shaderglobals& G, void* userdata, void* outputs, void* stream,
+                           const LaunchConfig& cfg, uint32_t* status_out, std::string* err) {
+    if (status_out) *status_out = 0;
+    if (blob_bytes > kNoAllocProgramBytes) {
+        if (err) *err = "program is " + std::to_string(blob_bytes) + " bytes; the allocation-free entry holds at most "
+                      + std::to_string(kNoAllocProgramBytes);
+        return OSLG_ERR_ARG;
+    }
+    int block = cfg.block > 0 ? cfg.block : 256;
+    if (block > 256) block = 256;
+    block = (block + 31) & ~31;
+    const size_t heap_area = kNoAllocScratchBytes - 256 - kNoAllocProgramBytes;
+    const size_t heap_per_cta = (size_t)hdr.heap_slots * block * sizeof(float);
+    if (heap_per_cta > heap_area) {
+        if (err) *err = "symbol heap of one CTA (" + std::to_string(heap_per_cta) + " bytes) exceeds the "
+                      + std::to_string(heap_area) + "-byte heap area of the allocation-free entry";
+        return OSLG_ERR_ARG;
+    }
+    int devid = 0;
+    if (!cuda_ok(cudaGetDevice(&devid), err, "cudaGetDevice")) return OSLG_ERR_CUDA;
+    if (devid < 0 || devid >= 128) {
+        if (err) *err = "device ordinal out of range";
+        return OSLG_ERR_ARG;
+    }
+    NoAllocDevice* d;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+        int rc = noalloc_setup(devid, g_noalloc_dev[devid], err);
+        if (rc != OSLG_OK) return rc;
+        d = &g_noalloc_dev[devid];
+    }
+    size_t static_bytes = (size_t)hdr.nops * sizeof(Op) + (size_t)((hdr.nconst + 3) & ~3u) * 4;
+    if (static_bytes > (size_t)d->smem_optin) {
+        if (err) *err = "program does not fit in shared memory";
+        return OSLG_ERR_LOWER;
+    }
+    int per_sm = 0;
+    if (!cuda_ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::interp_kernel<false>, block, static_bytes),
+                 err, "occupancy"))
+        return OSLG_ERR_CUDA;
+    if (per_sm < 1) per_sm = 1;
+    int64_t tiles = (npoints + block - 1) / block;
+    int64_t grid = (int64_t)d->sm_count * per_sm;
+    int64_t fit = (int64_t)(heap_area / heap_per_cta);
+    if (grid > fit) grid = fit;
+    if (grid > tiles) grid = tiles;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    uint32_t* status = reinterpret_cast<uint32_t*>(d->base);
+    unsigned char* prog = d->base + 256;
+    float* heap = reinterpret_cast<float*>(d->base + 256 + kNoAllocProgramBytes);
+    if (!cuda_ok(cudaMemsetAsync(status, 0, sizeof(uint32_t), s), err, "clear status")) return OSLG_ERR_CUDA;
+    if (npoints > 0) {
+        if (!cuda_ok(cudaMemcpyAsync(prog, blob, blob_bytes, cudaMemcpyHostToDevice, s), err, "program copy"))
+            return OSLG_ERR_CUDA;
+        dev::KArgs k;
+        k.blob = prog;
+        k.npoints = npoints;
+        k.userdata = static_cast<char*>(userdata);
+        k.outputs = static_cast<char*>(outputs);
+        k.gheap = heap;
+        k.status = status;
+        k.G = G;
+        dev::interp_kernel<false><<<(unsigned)grid, block, static_bytes, s>>>(k);
+        if (!cuda_ok(cudaGetLastError(), err, "launch")) return OSLG_ERR_CUDA;
+    }
+    if (status_out) {
+        uint32_t v = 0;
+        if (!cuda_ok(cudaMemcpyAsync(&v, status, sizeof(v), cudaMemcpyDeviceToHost, s), err, "status copy"))
+            return OSLG_ERR_CUDA;
+        if (!cuda_ok(cudaStreamSynchronize(s), err, "sync")) return OSLG_ERR_CUDA;
+        *status_out = v;
+    }
     return OSLG_OK;
 }
 
