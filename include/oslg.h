@@ -139,6 +139,15 @@ int oslg_shader_group_end(oslg_system* sys, oslg_group* group);
 int oslg_group_renderer_outputs(oslg_system* sys, oslg_group* group, const char** names, int n);
 /* ShadingSystem::add_symlocs(group, symlocs) (oslexec.h:1076) */
 int oslg_add_symlocs(oslg_system* sys, oslg_group* group, const oslg_symloc* locs, int n);
+/* Renderer-side evaluation of a closure output: after the group runs, the
+ * closure symbol `closure` ("layer.sym" or "sym") is walked and evaluated
+ * as testrender's CompositeBSDF at wo = -I and the light direction wi
+ * (src/testrender/shading.cpp:1450-1500 walk, shading.h:322-374 prepare and
+ * eval). Writes {weight.r, weight.g, weight.b, pdf} (4 floats) at
+ * output_base + offset + i*stride. Lobes: diffuse, microfacet "ggx"
+ * reflection; other closure ids contribute nothing. */
+int oslg_group_bsdf_eval(oslg_system* sys, oslg_group* group, const char* closure,
+                         const float wi[3], int64_t offset, int64_t stride);
 /* ShadingSystem::optimize_group (oslexec.h:1093) + BatchedExecutor::jit_group
  * (oslexec.h:993): lowers the group to a device op program and uploads it. */
 int oslg_optimize_group(oslg_system* sys, oslg_group* group);

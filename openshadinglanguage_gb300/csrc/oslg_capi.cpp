@@ -26,11 +26,14 @@ struct oslg_group {
 namespace oslg {
 
 ShadingSystem::ShadingSystem() {
-    // closure ids follow the testrender registration order
-    // (src/testrender/shading.h:25-61 ClosureIDs)
+    // closure ids follow testrender's ClosureIDs (src/testrender/shading.h:25-61)
     static const char* names[] = { "emission", "background", "diffuse", "oren_nayar", "translucent",
-                                   "phong", "ward", "microfacet", "reflection", "refraction",
-                                   "transparent", "holdout" };
+                                   "phong", "ward", "microfacet", "reflection", "fresnel_reflection",
+                                   "refraction", "transparent", "debug", "holdout",
+                                   "oren_nayar_diffuse_bsdf", "burley_diffuse_bsdf", "dielectric_bsdf",
+                                   "conductor_bsdf", "generalized_schlick_bsdf", "translucent_bsdf",
+                                   "transparent_bsdf", "subsurface_bssrdf", "sheen_bsdf", "uniform_edf",
+                                   "anisotropic_vdf", "medium_vdf", "layer" };
     for (int i = 0; i < (int)(sizeof(names) / sizeof(names[0])); ++i) closure_ids[names[i]] = i + 1;
 }
 
@@ -264,8 +267,12 @@ int oslg_add_symlocs(oslg_system* sys, oslg_group* group, const oslg_symloc* loc
             SymLoc sl;
             if (!locs[i].name) return fail(sys, OSLG_ERR_ARG, "symloc without a name");
             sl.name = locs[i].name;
-            if (!typedesc_to_spec(locs[i].type, sl.type) && locs[i].type.basetype != 0)
-                return fail(sys, OSLG_ERR_ARG, "symloc type not supported");
+            if (!typedesc_to_spec(locs[i].type, sl.type)) {
+                if (locs[i].type.basetype != 0) return fail(sys, OSLG_ERR_ARG, "symloc type not supported");
+                sl.type = TypeSpec();
+                sl.type.base = BT_CLOSURE;  // basetype 0: a closure output record
+                sl.type.arraylen = locs[i].type.arraylen;
+            }
             sl.derivs = locs[i].derivs != 0;
             sl.arena = (SymArena)locs[i].arena;
             sl.offset = locs[i].offset;
@@ -276,6 +283,24 @@ int oslg_add_symlocs(oslg_system* sys, oslg_group* group, const oslg_symloc* loc
         }
         std::lock_guard<std::mutex> lock(group->g.mutex);
         group->g.compiled.reset();  // placement changed: lower again
+        return OSLG_OK;
+    });
+}
+
+int oslg_group_bsdf_eval(oslg_system* sys, oslg_group* group, const char* closure, const float wi[3],
+                         int64_t offset, int64_t stride) {
+    if (!sys || !group || !closure || !wi) return OSLG_ERR_ARG;
+    return guarded(sys, [&]() {
+        if (offset < 0 || (offset & 3) || (stride & 3))
+            return fail(sys, OSLG_ERR_ARG, "bsdf eval offset and stride must be non-negative multiples of 4 bytes");
+        BsdfEvalRequest r;
+        r.closure = closure;
+        for (int i = 0; i < 3; ++i) r.wi[i] = wi[i];
+        r.offset = offset;
+        r.stride = stride;
+        std::lock_guard<std::mutex> lock(group->g.mutex);
+        group->g.bsdf_evals.push_back(r);
+        group->g.compiled.reset();
         return OSLG_OK;
     });
 }

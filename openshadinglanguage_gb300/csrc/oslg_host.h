@@ -120,6 +120,15 @@ struct SymLoc {
     int64_t stride = 0;
 };
 
+// Renderer-side evaluation of a closure output at one light direction
+// (testrender's CompositeBSDF::eval): weight rgb + pdf per point.
+struct BsdfEvalRequest {
+    std::string closure;  // "layer.sym" or "sym"
+    float wi[3] = { 0, 0, 1 };
+    int64_t offset = 0;
+    int64_t stride = 16;
+};
+
 // A lowered group ready to run: the op program plus a serialized blob the
 // device (or a checker) consumes.
 struct CompiledGroup {
@@ -136,6 +145,7 @@ struct ShaderGroup {
     std::vector<Layer> layers;
     std::vector<std::string> renderer_outputs;
     std::vector<SymLoc> symlocs;
+    std::vector<BsdfEvalRequest> bsdf_evals;
     bool ended = false;
     std::mutex mutex;  // lowering happens once, under this lock
     std::unique_ptr<CompiledGroup> compiled;
@@ -144,7 +154,7 @@ struct ShaderGroup {
 
 struct SystemOptions {
     int debug = 0;
-    int max_closure_components = 8;
+    int max_closure_components = 16;  // closure tree nodes per point
     int max_closure_terms = 16;
     int heap_in_smem = -1;  // -1 auto
     int threads_per_block = 256;

@@ -26,6 +26,7 @@
 
 #include "oslg_exec.h"
 #include "oslg_noise.cuh"
+#include "oslg_shading.cuh"
 
 namespace oslg {
 namespace dev {
@@ -865,112 +866,258 @@ __device__ void h_aassign(const Lane& L, const uint32_t* a, uint32_t* st) {
     }
 }
 
-// ---- closures ------------------------------------------------------------------------
-// Pools at header.closure_base: [ncomps][comps: id, params...][terms: comp, r,g,b]
+// ---- closures (reference closure tree, node pool in the heap) -------------------------
 struct ClosurePools {
-    uint32_t base, max_comps, max_terms;
+    uint32_t base, max_nodes;
 };
-__device__ __forceinline__ uint32_t cl_ncomp_slot(const ClosurePools& P) { return P.base; }
-__device__ __forceinline__ uint32_t cl_comp_slot(const ClosurePools& P, uint32_t i) { return P.base + 1 + i * kCompFloats; }
-__device__ __forceinline__ uint32_t cl_term_slot(const ClosurePools& P, uint32_t i) {
-    return P.base + 1 + P.max_comps * kCompFloats + i * kTermFloats;
-}
 __device__ __forceinline__ float hget(const Lane& L, uint32_t slot) { return L.heap[(size_t)slot * L.hs + L.li]; }
 __device__ __forceinline__ void hset(const Lane& L, uint32_t slot, float v) { L.heap[(size_t)slot * L.hs + L.li] = v; }
 __device__ __forceinline__ uint32_t hgetu(const Lane& L, uint32_t slot) { return __float_as_uint(hget(L, slot)); }
 __device__ __forceinline__ void hsetu(const Lane& L, uint32_t slot, uint32_t v) { hset(L, slot, __uint_as_float(v)); }
-
-// term allocation: the term pool is a bump allocator; its top is kept in the
-// high half of the ncomp word
-__device__ __forceinline__ bool cl_alloc_terms(const Lane& L, const ClosurePools& P, uint32_t n, uint32_t& first,
-                                                uint32_t* st) {
-    uint32_t w = hgetu(L, cl_ncomp_slot(P));
-    uint32_t top = w >> 16;
-    if (top + n > P.max_terms) { raise_status(st, ST_CLOSURE_OVERFLOW); return false; }
-    first = top;
-    hsetu(L, cl_ncomp_slot(P), (w & 0xFFFFu) | ((top + n) << 16));
-    return true;
+__device__ __forceinline__ uint32_t node_slot(const ClosurePools& P, uint32_t node) {
+    return P.base + 1 + node * kNodeFloats;
+}
+// returns node index + 1, or 0 when the pool is full
+__device__ __forceinline__ uint32_t cl_alloc(const Lane& L, const ClosurePools& P, uint32_t* st) {
+    uint32_t n = hgetu(L, P.base);
+    if (n >= P.max_nodes) { raise_status(st, ST_CLOSURE_OVERFLOW); return 0u; }
+    hsetu(L, P.base, n + 1);
+    return n + 1;
 }
 
+// osl_allocate_(weighted_)closure_component (opclosure.cpp:83-117)
 __device__ void h_closure(const Lane& L, const uint32_t* a, const uint32_t* extra, const ClosurePools& P,
                           uint32_t* st) {
-    uint32_t w = hgetu(L, cl_ncomp_slot(P));
-    uint32_t nco = w & 0xFFFFu;
-    if (nco >= P.max_comps) { raise_status(st, ST_CLOSURE_OVERFLOW); stw(L, a[0], 0, 0u); return; }
-    uint32_t cs = cl_comp_slot(P, nco);
-    hsetu(L, cs, a[1]);
-    int k = 0;
-    uint32_t params[12];
+    float w[3] = { 1.0f, 1.0f, 1.0f };
+    if (a[2] != kNoArg) {
+        for (int c = 0; c < 3; ++c) w[c] = ldf(L, a[2], c, 0);
+        if (w[0] == 0.0f && w[1] == 0.0f && w[2] == 0.0f) { stw(L, a[0], 0, 0u); return; }
+    }
+    uint32_t h = cl_alloc(L, P, st);
+    if (!h) { stw(L, a[0], 0, 0u); return; }
+    uint32_t ns = node_slot(P, h - 1);
+    hsetu(L, ns, a[1]);
+    for (int c = 0; c < 3; ++c) hset(L, ns + 1 + c, w[c]);
+    uint32_t params[11];
     int np = 0;
-    for (int i = 2; i < 7; ++i) params[np++] = a[i];
+    for (int i = 3; i < 7; ++i) params[np++] = a[i];
     if (extra)
         for (int i = 0; i < 7; ++i) params[np++] = extra[i];
+    int k = 0;
     for (int i = 0; i < np && k < kClosureParamFloats; ++i) {
         uint32_t p = params[i];
         if (p == kNoArg) break;
         int nc = anc(p);
-        for (int c = 0; c < nc && k < kClosureParamFloats; ++c) {
-            uint32_t t = atc(p);
-            float v = (t == TC_INT || t == TC_STRING) ? __uint_as_float(ldw(L, p, c)) : ldf(L, p, c, 0);
-            hset(L, cs + 1 + k++, v);
+        uint32_t t = atc(p);
+        for (int c = 0; c < nc && k < kClosureParamFloats; ++c)
+            hsetu(L, ns + 4 + k++, (t == TC_INT || t == TC_STRING) ? ldw(L, p, c) : __float_as_uint(ldf(L, p, c, 0)));
+    }
+    for (; k < kClosureParamFloats; ++k) hset(L, ns + 4 + k, 0.0f);
+    stw(L, a[0], 0, h);
+}
+
+// osl_mul_closure_color / osl_mul_closure_float (opclosure.cpp:35-80)
+__device__ void h_closure_mul(const Lane& L, const uint32_t* a, const ClosurePools& P, uint32_t* st) {
+    uint32_t c = ldw(L, a[1], 0);
+    float w[3] = { ldf(L, a[2], 0, 0), ldf(L, a[2], 1, 0), ldf(L, a[2], 2, 0) };
+    if (c == 0u || (w[0] == 0.0f && w[1] == 0.0f && w[2] == 0.0f)) { stw(L, a[0], 0, 0u); return; }
+    if (w[0] == 1.0f && w[1] == 1.0f && w[2] == 1.0f) { stw(L, a[0], 0, c); return; }
+    uint32_t h = cl_alloc(L, P, st);
+    if (!h) { stw(L, a[0], 0, 0u); return; }
+    uint32_t ns = node_slot(P, h - 1);
+    hsetu(L, ns, (uint32_t)kClosureMul);
+    for (int k = 0; k < 3; ++k) hset(L, ns + 1 + k, w[k]);
+    hsetu(L, ns + 4, c);
+    stw(L, a[0], 0, h);
+}
+
+// osl_add_closure_closure (opclosure.cpp:15-33)
+__device__ void h_closure_add(const Lane& L, const uint32_t* a, const ClosurePools& P, uint32_t* st) {
+    uint32_t x = ldw(L, a[1], 0), y = ldw(L, a[2], 0);
+    if (x == 0u) { stw(L, a[0], 0, y); return; }
+    if (y == 0u) { stw(L, a[0], 0, x); return; }
+    uint32_t h = cl_alloc(L, P, st);
+    if (!h) { stw(L, a[0], 0, 0u); return; }
+    uint32_t ns = node_slot(P, h - 1);
+    hsetu(L, ns, (uint32_t)kClosureAdd);
+    hsetu(L, ns + 4, x);
+    hsetu(L, ns + 5, y);
+    stw(L, a[0], 0, h);
+}
+
+// testrender's non-recursive walk (shading.cpp:1450-1500): visits the
+// components in order with the accumulated weight weight*comp.w.
+template <class F>
+__device__ void closure_walk(const Lane& L, const ClosurePools& P, uint32_t root, uint32_t* st, F&& visit) {
+    uint32_t stack_node[kClosureWalkStack];
+    float stack_w[kClosureWalkStack][3];
+    int sp = 0;
+    float w[3] = { 1.0f, 1.0f, 1.0f };
+    uint32_t cur = root;
+    int guard = 0;
+    while (cur != 0u && cur <= P.max_nodes) {
+        if (++guard > 4 * (int)P.max_nodes + 8) break;
+        uint32_t ns = node_slot(P, cur - 1);
+        int id = (int)hgetu(L, ns);
+        if (id == kClosureMul) {
+            for (int k = 0; k < 3; ++k) w[k] = w[k] * hget(L, ns + 1 + k);
+            cur = hgetu(L, ns + 4);
+        } else if (id == kClosureAdd) {
+            if (sp < kClosureWalkStack) {
+                stack_node[sp] = hgetu(L, ns + 5);
+                for (int k = 0; k < 3; ++k) stack_w[sp][k] = w[k];
+                ++sp;
+            } else {
+                raise_status(st, ST_CLOSURE_OVERFLOW);
+            }
+            cur = hgetu(L, ns + 4);
+        } else {
+            float cw[3];
+            for (int k = 0; k < 3; ++k) cw[k] = w[k] * hget(L, ns + 1 + k);
+            visit(id, cw, ns + 4);
+            cur = 0u;
+        }
+        if (cur == 0u && sp > 0) {
+            --sp;
+            cur = stack_node[sp];
+            for (int k = 0; k < 3; ++k) w[k] = stack_w[sp][k];
         }
     }
-    hsetu(L, cl_ncomp_slot(P), (w & 0xFFFF0000u) | (nco + 1));
-    uint32_t first;
-    if (!cl_alloc_terms(L, P, 1, first, st)) { stw(L, a[0], 0, 0u); return; }
-    uint32_t ts = cl_term_slot(P, first);
-    hsetu(L, ts, nco);
-    hset(L, ts + 1, 1.0f); hset(L, ts + 2, 1.0f); hset(L, ts + 3, 1.0f);
-    stw(L, a[0], 0, (first << 16) | 1u);
 }
 
-__device__ void h_closure_mul(const Lane& L, const uint32_t* a, const ClosurePools& P, uint32_t* st) {
-    uint32_t h = ldw(L, a[1], 0);
-    uint32_t cnt = h & 0xFFFFu, src = h >> 16;
-    if (cnt == 0) { stw(L, a[0], 0, 0u); return; }
-    float wr = ldf(L, a[2], 0, 0), wg = ldf(L, a[2], 1, 0), wb = ldf(L, a[2], 2, 0);
-    uint32_t first;
-    if (!cl_alloc_terms(L, P, cnt, first, st)) { stw(L, a[0], 0, 0u); return; }
-    for (uint32_t i = 0; i < cnt; ++i) {
-        uint32_t s = cl_term_slot(P, src + i), d = cl_term_slot(P, first + i);
-        hsetu(L, d, hgetu(L, s));
-        hset(L, d + 1, hget(L, s + 1) * wr);
-        hset(L, d + 2, hget(L, s + 2) * wg);
-        hset(L, d + 3, hget(L, s + 3) * wb);
-    }
-    stw(L, a[0], 0, (first << 16) | cnt);
-}
-
-__device__ void h_closure_add(const Lane& L, const uint32_t* a, const ClosurePools& P, uint32_t* st) {
-    uint32_t ha = ldw(L, a[1], 0), hb = ldw(L, a[2], 0);
-    uint32_t ca = ha & 0xFFFFu, cb = hb & 0xFFFFu;
-    if (ca + cb == 0) { stw(L, a[0], 0, 0u); return; }
-    uint32_t first;
-    if (!cl_alloc_terms(L, P, ca + cb, first, st)) { stw(L, a[0], 0, 0u); return; }
-    for (uint32_t i = 0; i < ca + cb; ++i) {
-        uint32_t s = i < ca ? cl_term_slot(P, (ha >> 16) + i) : cl_term_slot(P, (hb >> 16) + (i - ca));
-        uint32_t d = cl_term_slot(P, first + i);
-        for (int k = 0; k < 4; ++k) hsetu(L, d + k, hgetu(L, s + k));
-    }
-    stw(L, a[0], 0, (first << 16) | (ca + cb));
-}
-
-// Output record per point: [count][per term: id, w.rgb, params x12]
-__device__ void h_store_closure(const Lane& L, const uint32_t* a, char* base, const ClosurePools& P) {
-    uint32_t h = ldw(L, a[0], 0);
-    uint32_t cnt = h & 0xFFFFu, first = h >> 16, maxc = a[3];
-    char* p = base + (int64_t)a[1] + L.pt * (int64_t)(int32_t)a[2];
-    uint32_t n = cnt < maxc ? cnt : maxc;
-    uint32_t* o = reinterpret_cast<uint32_t*>(p);
+// Output record per point: [count][per component: id, w.rgb, params x12]
+__device__ void h_store_closure(const Lane& L, const uint32_t* a, char* base, const ClosurePools& P, uint32_t* st) {
+    uint32_t root = ldw(L, a[0], 0), maxc = a[3];
+    uint32_t* o = reinterpret_cast<uint32_t*>(base + (int64_t)a[1] + L.pt * (int64_t)(int32_t)a[2]);
+    uint32_t n = 0;
+    closure_walk(L, P, root, st, [&](int id, const float* cw, uint32_t params) {
+        if (n >= maxc) return;
+        uint32_t* q = o + 1 + n * kNodeFloats;
+        q[0] = (uint32_t)id;
+        for (int k = 0; k < 3; ++k) q[1 + k] = __float_as_uint(cw[k]);
+        for (int k = 0; k < kClosureParamFloats; ++k) q[4 + k] = hgetu(L, params + k);
+        ++n;
+    });
     o[0] = n;
-    for (uint32_t i = 0; i < n; ++i) {
-        uint32_t ts = cl_term_slot(P, first + i);
-        uint32_t comp = hgetu(L, ts);
-        uint32_t cs = cl_comp_slot(P, comp);
-        uint32_t* q = o + 1 + i * (4 + kClosureParamFloats);
-        q[0] = hgetu(L, cs);
-        for (int k = 0; k < 3; ++k) q[1 + k] = hgetu(L, ts + 1 + k);
-        for (int k = 0; k < kClosureParamFloats; ++k) q[4 + k] = hgetu(L, cs + 1 + k);
+}
+
+// CompositeBSDF::prepare + eval (shading.h:322-374) over the lobes the walk
+// finds: diffuse, and microfacet "ggx" reflection; other ids add nothing.
+__device__ void h_bsdf_eval(const Lane& L, const uint32_t* a, char* base, const ClosurePools& P, uint32_t* st) {
+    uint32_t root = ldw(L, a[0], 0);
+    const V3 wi = v3(ldf(L, a[3], 0, 0), ldf(L, a[3], 1, 0), ldf(L, a[3], 2, 0));
+    const V3 wo = v3(-ldf(L, a[4], 0, 0), -ldf(L, a[4], 1, 0), -ldf(L, a[4], 2, 0));
+    const uint32_t ggx = a[5];
+    int nl = 0;
+    int kind[kBsdfMaxLobes];
+    float lw[kBsdfMaxLobes][3];
+    uint32_t lp[kBsdfMaxLobes];
+    closure_walk(L, P, root, st, [&](int id, const float* cw, uint32_t params) {
+        int k = -1;
+        if (id == 3) k = 0;  // DIFFUSE_ID
+        else if (id == 8 && hgetu(L, params + 0) == ggx && (int)hgetu(L, params + 10) == 0) k = 1;  // MICROFACET_ID
+        if (k < 0 || nl >= kBsdfMaxLobes) return;
+        kind[nl] = k;
+        for (int c = 0; c < 3; ++c) lw[nl][c] = cw[c];
+        lp[nl] = params;
+        ++nl;
+    });
+    // prepare(wo, path_weight = 1, absorb = false)
+    float pdfs[kBsdfMaxLobes];
+    float total = 0.0f;
+    for (int i = 0; i < nl; ++i) {
+        float alb = 1.0f;
+        if (kind[i] == 1) {
+            V3 N = v3(hget(L, lp[i] + 1), hget(L, lp[i] + 2), hget(L, lp[i] + 3));
+            alb = fresnel_dielectric(vdot(N, wo), hget(L, lp[i] + 9));
+        }
+        pdfs[i] = (lw[i][0] * (1.0f * alb) + lw[i][1] * (1.0f * alb) + lw[i][2] * (1.0f * alb)) / (1.0f + 1.0f + 1.0f);
+        total += pdfs[i];
+    }
+    if (total > 0.0f || total > 1.0f)
+        for (int i = 0; i < nl; ++i) pdfs[i] /= total;
+    float sw[3] = { 0.0f, 0.0f, 0.0f }, spdf = 0.0f, srough = 0.0f;
+    for (int i = 0; i < nl; ++i) {
+        BsdfSample b;
+        if (kind[i] == 0) {
+            b = diffuse_eval(v3(hget(L, lp[i] + 0), hget(L, lp[i] + 1), hget(L, lp[i] + 2)), wi);
+        } else {
+            V3 N = v3(hget(L, lp[i] + 1), hget(L, lp[i] + 2), hget(L, lp[i] + 3));
+            V3 U = v3(hget(L, lp[i] + 4), hget(L, lp[i] + 5), hget(L, lp[i] + 6));
+            Frame tf = frame_from_normal_and_tangent(N, U);
+            b = microfacet_ggx_refl_eval(tf, hget(L, lp[i] + 7), hget(L, lp[i] + 8), hget(L, lp[i] + 9), wo, wi);
+        }
+        for (int c = 0; c < 3; ++c) b.w[c] *= lw[i][c];
+        mis_update_eval(sw, &spdf, b.w, b.pdf, pdfs[i]);
+        srough += b.roughness * pdfs[i];
+    }
+    float* o = reinterpret_cast<float*>(base + (int64_t)a[1] + L.pt * (int64_t)(int32_t)a[2]);
+    o[0] = sw[0]; o[1] = sw[1]; o[2] = sw[2]; o[3] = spdf;
+}
+
+// ---- spline (splineimpl.h:191-239) -----------------------------------------------------
+__device__ void h_spline(const Lane& L, const uint32_t* a) {
+    uint32_t r = a[0], xa = a[1], kn = a[2];
+    const SplineBasisDev& B = c_spline_basis[a[3] < 6u ? a[3] : 0u];
+    int alen = (int)a[5];
+    int knot_count = a[4] != kNoArg ? ldi(L, a[4], 0) : alen;
+    if (knot_count > alen) knot_count = alen;
+    int nc = anc(r);
+    int kc = anc(kn);
+    bool xd = ader(xa), kd = ader(kn), rd = ader(r);
+    D2 x = ldd(L, xa, 0);
+    if (!(0.0f <= x.v)) x = d2c(0.0f);
+    if (x.v > 1.0f) x = d2c(1.0f);
+    int nsegs = ((knot_count - 4) / B.step) + 1;
+    x = x * (float)nsegs;
+    int segnum = (int)x.v;
+    if (segnum < 0) segnum = 0;
+    if (segnum > nsegs - 1) segnum = nsegs - 1;
+    if (a[3] == 5u) {  // constant basis
+        for (int c = 0; c < nc; ++c) stval(L, r, c, __uint_as_float(ldw(L, kn, (segnum + 1) * kc + (kc == 1 ? 0 : c))));
+        return;
+    }
+    x = x - (float)segnum;
+    int s = segnum * B.step;
+    for (int c = 0; c < nc; ++c) {
+        int cc = kc == 1 ? 0 : c;
+        D2 P[4];
+        for (int k = 0; k < 4; ++k) {
+            float v = __uint_as_float(ldw(L, kn, (s + k) * kc + cc));
+            float dx = kd ? __uint_as_float(ldw(L, kn, alen * kc + (s + k) * kc + cc)) : 0.0f;
+            float dy = kd ? __uint_as_float(ldw(L, kn, 2 * alen * kc + (s + k) * kc + cc)) : 0.0f;
+            P[k] = d2(v, dx, dy);
+        }
+        D2 tk[4];
+        for (int k = 0; k < 4; ++k) {
+            // basis[k][j] * P[j], summed left to right (float * CTYPE)
+            D2 t0 = P[0] * B.m[k][0], t1 = P[1] * B.m[k][1], t2 = P[2] * B.m[k][2], t3 = P[3] * B.m[k][3];
+            tk[k] = ((t0 + t1) + t2) + t3;
+        }
+        D2 res;
+        if (!xd && !kd) {
+            float xv = x.v;
+            float t = tk[0].v * xv + tk[1].v;
+            t = t * xv + tk[2].v;
+            t = t * xv + tk[3].v;
+            res = d2c(t);
+        } else if (!kd) {
+            // CTYPE without partials times a Dual2 x: tk*x scales every element
+            D2 t = x * tk[0].v;
+            t = t + tk[1].v;
+            t = t * x;
+            t = t + tk[2].v;
+            t = t * x;
+            t = t + tk[3].v;
+            res = t;
+        } else {
+            D2 t = tk[0] * x + tk[1];
+            t = t * x + tk[2];
+            t = t * x + tk[3];
+            res = t;
+        }
+        if (!rd) stval(L, r, c, res.v);
+        else std2(L, r, c, res);
     }
 }
 
@@ -998,8 +1145,7 @@ __global__ void __launch_bounds__(256) interp_kernel(KArgs k) {
     __syncthreads();
     ClosurePools CP;
     CP.base = H->closure_base;
-    CP.max_comps = H->max_comps;
-    CP.max_terms = H->max_terms;
+    CP.max_nodes = H->max_comps;
     const bool uses_closures = (H->flags & 1u) != 0;
 
     Lane L;
@@ -1015,7 +1161,7 @@ __global__ void __launch_bounds__(256) interp_kernel(KArgs k) {
         bool act = valid, ext = false, lret = false;
         uint32_t stk = 0, cnd = 0, brk = 0, cnt = 0;
         long long backedges = 0;
-        if (uses_closures && valid) hsetu(L, cl_ncomp_slot(CP), 0u);
+        if (uses_closures && valid) hsetu(L, CP.base, 0u);
         int pc = 0;
         while (pc < nops) {
             const uint4* ow = reinterpret_cast<const uint4*>(sops + pc);
@@ -1226,7 +1372,9 @@ __global__ void __launch_bounds__(256) interp_kernel(KArgs k) {
                     }
                     case OP_CLOSURE_MUL: h_closure_mul(L, a, CP, k.status); break;
                     case OP_CLOSURE_ADD: h_closure_add(L, a, CP, k.status); break;
-                    case OP_STORE_CLOSURE: h_store_closure(L, a, k.outputs, CP); break;
+                    case OP_STORE_CLOSURE: h_store_closure(L, a, k.outputs, CP, k.status); break;
+                    case OP_BSDF_EVAL: h_bsdf_eval(L, a, k.outputs, CP, k.status); break;
+                    case OP_SPLINE: h_spline(L, a); break;
                     default: raise_status(k.status, ST_BAD_OPCODE); break;
                     }
                 }

@@ -254,6 +254,22 @@ struct Lowerer {
             LOp le; le.name = "__layer_end"; le.layer = li;
             lops.push_back(le);
         }
+        // renderer-side BSDF evaluation of closure outputs
+        for (const BsdfEvalRequest& be : g.bsdf_evals) {
+            SymLoc tmp;
+            tmp.name = be.closure;
+            int gs = resolve_symloc(tmp);
+            if (gs < 0 || syms[gs].type.base != BT_CLOSURE)
+                return fail("bsdf eval: '" + be.closure + "' is not a closure of the group");
+            GSym d; d.name = "$wi"; d.type.base = BT_TRIPLE; d.type.vecsem = VS_VECTOR; d.kind = SK_CONST;
+            d.is_const = true; d.cval = { be.wi[0], be.wi[1], be.wi[2] };
+            int wi = add_sym(d);
+            TypeSpec vt; vt.base = BT_TRIPLE; vt.vecsem = VS_VECTOR;
+            int I = global_sym("I", vt);
+            LOp op; op.name = "__bsdf_eval"; op.args = { gs, wi, I };
+            op.imm[0] = be.offset; op.imm[1] = be.stride;
+            lops.push_back(op);
+        }
         // renderer outputs placed through symlocs
         for (const SymLoc& sl : g.symlocs) {
             if (sl.arena != ARENA_OUTPUTS) continue;
@@ -261,6 +277,7 @@ struct Lowerer {
             if (gs < 0) return fail("symloc '" + sl.name + "' does not name a symbol of the group");
             LOp op; op.name = "__store_output"; op.args = { gs };
             op.imm[0] = sl.offset; op.imm[1] = sl.stride; op.imm[2] = sl.derivs ? 1 : 0;
+            op.imm[3] = sl.type.arraylen > 0 ? sl.type.arraylen : 4;  // closure records kept
             lops.push_back(op);
         }
         return true;
@@ -287,7 +304,7 @@ struct Lowerer {
             return op.argrw[i] == 'w' || op.argrw[i] == 'W';
         static const std::set<std::string> nowrite = {
             "if", "for", "while", "dowhile", "break", "continue", "return", "exit", "nop",
-            "useparam", "__layer_end", "__store_output", "functioncall", "functioncall_nr",
+            "useparam", "__layer_end", "__store_output", "__bsdf_eval", "functioncall", "functioncall_nr",
             "printf", "warning", "error", "fprintf" };
         if (nowrite.count(op.name)) return false;
         if (op.name == "sincos") return i == 1 || i == 2;
@@ -304,7 +321,7 @@ struct Lowerer {
         for (LOp& op : lops) {
             if (!op.param_init) continue;
             GSym& p = syms[op.param_gsym];
-            if (!p.written && !p.type.is_array() && p.type.base != BT_CLOSURE) {
+            if (!p.written && p.type.base != BT_CLOSURE) {
                 const GSym& c = syms[op.args[1]];
                 p.is_const = true;
                 p.cval = c.cval;
@@ -475,10 +492,16 @@ struct Lowerer {
         // global loads first
         for (auto& kv : globals) {
             const GSym& s = syms[kv.second];
-            if (!s.referenced || s.global_id < 0) {
-                if (s.referenced && s.global_id < 0)
-                    return fail("shader global '" + s.name + "' is not supported");
-                continue;
+            if (!s.referenced) continue;
+            if (s.global_id < 0) {
+                if (s.type.base == BT_CLOSURE) {
+                    // Ci and other closure globals start as the null closure
+                    int z = const_int(0);
+                    syms[z].slot = (int)pool_add(syms[z]);
+                    emit(OP_ASSIGN, { A(kv.second), A(z), 1u }, "global");
+                    continue;
+                }
+                return fail("shader global '" + s.name + "' is not supported");
             }
             emit(OP_LOAD_GLOBAL, { A(kv.second), (uint32_t)s.global_id }, "global");
         }
@@ -598,11 +621,18 @@ struct Lowerer {
                  "userdata");
             return true;
         }
+        if (n == "__bsdf_eval") {
+            // renderer-side evaluation of a closure output (testrender's
+            // CompositeBSDF::eval, src/testrender/shading.h:364-374)
+            uses_closures = true;
+            emit(OP_BSDF_EVAL, { a(0), (uint32_t)op.imm[0], (uint32_t)op.imm[1], a(1), a(2), string_hash("ggx") },
+                 "bsdf_eval");
+            return true;
+        }
         if (n == "__store_output") {
             int s = op.args[0];
             if (is_closure(s)) {
-                emit(OP_STORE_CLOSURE, { a(0), (uint32_t)op.imm[0], (uint32_t)op.imm[1],
-                                         (uint32_t)ss.opts.max_closure_terms },
+                emit(OP_STORE_CLOSURE, { a(0), (uint32_t)op.imm[0], (uint32_t)op.imm[1], (uint32_t)op.imm[3] },
                      "output");
                 return true;
             }
@@ -793,7 +823,7 @@ struct Lowerer {
         if (n == "blackbody") { emit(OP_BLACKBODY, { a(0), a(1) }, n); return true; }
         if (n == "luminance") { emit(OP_LUMINANCE, { a(0), a(1) }, n); return true; }
         if (n == "closure") {
-            // closure r [weight] name args...
+            // closure r [weight] name args...   (llvm_gen_closure, batched_llvm_gen.cpp:7310)
             uses_closures = true;
             size_t ni = 1;
             int weight = -1;
@@ -802,18 +832,14 @@ struct Lowerer {
             auto it = ss.closure_ids.find(cname);
             if (it == ss.closure_ids.end()) return fail("closure '" + cname + "' is not registered");
             std::vector<uint32_t> params;
-            for (size_t i = ni + 1; i < na && params.size() < 5; ++i) params.push_back(A(op.args[i]));
-            while (params.size() < 5) params.push_back(kNoArg);
-            emit(OP_CLOSURE, { a(0), (uint32_t)it->second, params[0], params[1], params[2], params[3], params[4] },
+            for (size_t i = ni + 1; i < na && params.size() < 11; ++i) params.push_back(A(op.args[i]));
+            while (params.size() < 11) params.push_back(kNoArg);
+            emit(OP_CLOSURE, { a(0), (uint32_t)it->second, weight >= 0 ? A(weight) : kNoArg, params[0], params[1],
+                               params[2], params[3] },
                  n);
-            if (na > ni + 6) {
-                std::vector<uint32_t> more;
-                for (size_t i = ni + 6; i < na && more.size() < 7; ++i) more.push_back(A(op.args[i]));
-                while (more.size() < 7) more.push_back(kNoArg);
-                emit(OP_NOP, { more[0], more[1], more[2], more[3], more[4], more[5], more[6] },
+            if (na > ni + 5)
+                emit(OP_NOP, { params[4], params[5], params[6], params[7], params[8], params[9], params[10] },
                      "closure-params");
-            }
-            if (weight >= 0) emit(OP_CLOSURE_MUL, { a(0), a(0), A(weight) }, n);
             return true;
         }
         return fail("op '" + n + "' is not supported by this executor");
@@ -834,8 +860,8 @@ struct Lowerer {
         h.nconst = (uint32_t)pool.size();
         h.closure_base = heap_top;
         h.max_comps = uses_closures ? (uint32_t)ss.opts.max_closure_components : 0u;
-        h.max_terms = uses_closures ? (uint32_t)ss.opts.max_closure_terms : 0u;
-        uint32_t closure_slots = uses_closures ? 1 + h.max_comps * kCompFloats + h.max_terms * kTermFloats : 0;
+        h.max_terms = 0u;
+        uint32_t closure_slots = uses_closures ? 1 + h.max_comps * kNodeFloats : 0;
         h.heap_slots = heap_top + closure_slots;
         if (h.heap_slots == 0) h.heap_slots = 1;
         h.flags = (uses_closures ? 1u : 0u);

@@ -116,10 +116,13 @@ enum OpCode : uint16_t {
     // color
     OP_BLACKBODY, OP_LUMINANCE,
     // closures: a0=r a1=closure id a2.. params (see lowering)
-    OP_CLOSURE,
+    OP_CLOSURE,      // a0=r a1=closure id a2=weight (or kNoArg) a3..a6 first params;
+                     // an OP_NOP carrier with 7 operands may follow with more params
     OP_CLOSURE_MUL,  // a0=r a1=closure a2=weight (float or color)
     OP_CLOSURE_ADD,  // a0=r a1=a a2=b
     OP_STORE_CLOSURE,// a0=src a1=byte offset a2=byte stride a3=max components
+    OP_BSDF_EVAL,    // a0=closure a1=byte offset a2=byte stride a3=wi (triple)
+                     // a4=I (triple global) a5=hash("ggx")
     OP_COUNT
 };
 
@@ -168,15 +171,19 @@ struct Op {
 };
 static_assert(sizeof(Op) == 32, "Op must be 32 bytes");
 
-// Closure storage inside the heap (per point): a component pool and a
-// term pool. A closure value (one heap slot, int bits) is (first term << 16)
-// | term count. Each term is (component index, weight rgb); each component
-// is (closure id, params...). The layout mirrors ClosureComponent
-// {id, w, params} of src/include/OSL/oslclosure.h:65-147 after the
-// renderer's tree walk has folded the MUL weights into each component.
+// Closure storage inside the heap (per point): a node pool holding the
+// reference's closure tree (src/include/OSL/oslclosure.h:65-147):
+//   component  [id >= 0][w.r w.g w.b][params x 12]
+//   MUL        [-1][w.r w.g w.b][child]
+//   ADD        [-2][.  .  .  ][A][B]
+// The pool starts with its node count. A closure value (one heap slot, int
+// bits) is node index + 1; 0 is the null closure.
 static const int kClosureParamFloats = 12;
-static const int kCompFloats = 1 + kClosureParamFloats;  // id + params
-static const int kTermFloats = 4;                        // comp idx + rgb
+static const int kNodeFloats = 16;
+static const int kClosureMul = -1;
+static const int kClosureAdd = -2;
+static const int kClosureWalkStack = 16;  // testrender's traversal stack
+static const int kBsdfMaxLobes = 8;       // CompositeBSDF::MaxEntries
 
 struct ProgramHeader {
     uint32_t magic;
@@ -186,8 +193,8 @@ struct ProgramHeader {
     uint32_t heap_slots;    // floats per point
     uint32_t flags;         // bit0 uses closures, bit1 uses derivatives
     uint32_t closure_base;  // heap slot of the closure pools (if bit0)
-    uint32_t max_comps;     // component pool capacity
-    uint32_t max_terms;     // term pool capacity
+    uint32_t max_comps;     // closure node pool capacity
+    uint32_t max_terms;     // unused
     uint32_t max_depth;     // deepest if/loop nesting (<= 32)
     uint32_t reserved[6];
 };

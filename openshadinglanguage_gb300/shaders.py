@@ -345,3 +345,83 @@ def ctrlflow():
     b.op("assign", fj, j)
     b.op("add", r, t2, fj)
     return b.text()
+
+
+# ---- 3-layer closure group (pattern -> color ramp -> surface) -----------------------
+def c2_pattern():
+    """Layer A: simplex noise plus cell noise on P*16, P = (u, v, 0).
+
+        shader c2_pattern(float scale = 16, output float a = 0)
+        {
+            point p = point(u, v, 0) * scale;
+            a = 0.8 * noise("usimplex", p) + 0.2 * cellnoise(p);
+        }
+    """
+    b = OsoBuilder("c2_pattern")
+    scale = b.param("float", "scale", 16.0)
+    a = b.param("float", "a", 0.0, output=True)
+    u, v = b.glob("float", "u"), b.glob("float", "v")
+    p0, p = b.tmp("point"), b.tmp("point")
+    b.op("point", p0, u, v, b.const("float", 0.0))
+    b.op("mul", p, p0, scale)
+    s, c, t1, t2 = b.tmp("float"), b.tmp("float"), b.tmp("float"), b.tmp("float")
+    b.op("noise", s, b.const("string", "usimplex"), p)
+    b.op("cellnoise", c, p)
+    b.op("mul", t1, b.const("float", 0.8), s)
+    b.op("mul", t2, b.const("float", 0.2), c)
+    b.op("add", a, t1, t2)
+    return b.text()
+
+
+def c2_ramp():
+    """Layer B: 8-knot catmull-rom color ramp.
+
+        shader c2_ramp(float x = 0, color knots[8] = {...}, output color Cout = 0)
+        {
+            Cout = spline("catmull-rom", x, knots);
+        }
+    """
+    b = OsoBuilder("c2_ramp")
+    x = b.param("float", "x", 0.0)
+    knots = b.param("color[8]", "knots", [0.5] * 24)
+    Cout = b.param("color", "Cout", [0, 0, 0], output=True)
+    b.op("spline", Cout, b.const("string", "catmull-rom"), x, knots)
+    return b.text()
+
+
+def c2_surface():
+    """Layer C: a closure sum with GGX roughness driven by the pattern.
+
+        surface c2_surface(float a = 0, color tint = 1)
+        {
+            float alpha = 0.05 + 0.75 * a;
+            Ci = 0.6 * tint * diffuse(N)
+               + 0.4 * microfacet("ggx", N, dPdu, alpha, alpha, 1.5, 0);
+        }
+    """
+    b = OsoBuilder("c2_surface", "surface")
+    a = b.param("float", "a", 0.0)
+    tint = b.param("color", "tint", [1, 1, 1])
+    Ci = b.glob("closure color", "Ci")
+    N = b.glob("normal", "N")
+    dPdu = b.glob("vector", "dPdu")
+    alpha, t = b.local("float", "alpha"), b.tmp("float")
+    b.op("mul", t, b.const("float", 0.75), a)
+    b.op("add", alpha, b.const("float", 0.05), t)
+    w, d, dw = b.tmp("color"), b.tmp("closure color"), b.tmp("closure color")
+    b.op("mul", w, b.const("float", 0.6), tint)
+    b.op("closure", d, b.const("string", "diffuse"), N)
+    b.op("mul", dw, d, w)
+    m, mw = b.tmp("closure color"), b.tmp("closure color")
+    b.op("closure", m, b.const("string", "microfacet"), b.const("string", "ggx"), N, dPdu, alpha, alpha,
+         b.const("float", 1.5), b.const("int", 0))
+    b.op("mul", mw, m, b.const("float", 0.4))
+    b.op("add", Ci, dw, mw)
+    return b.text()
+
+
+def c2_knots(seed=0xC2B):
+    """The ramp's 8 knot colors, seeded."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    return [float(x) for x in rng.uniform(0.05, 0.95, 24).astype(np.float32)]

@@ -170,6 +170,12 @@ class ShadingSystem:
             arr[i] = C.SymLocC(nm, s.type.c(), 1 if s.derivs else 0, s.arena, s.offset, s.stride)
         self._check(C.lib().oslg_add_symlocs(self._h, group.handle, arr, len(locs)))
 
+    def bsdf_eval_output(self, group, closure, wi, offset, stride):
+        """Evaluate closure output `closure` as testrender's CompositeBSDF at
+        wo = -I and light direction wi; writes weight rgb + pdf per point."""
+        w = (ctypes.c_float * 3)(*[float(x) for x in wi])
+        self._check(C.lib().oslg_group_bsdf_eval(self._h, group.handle, closure.encode(), w, offset, stride))
+
     def optimize_group(self, group):
         self._check(C.lib().oslg_optimize_group(self._h, group.handle))
 

@@ -27,6 +27,7 @@
 
 #include "../include/oslg.h"
 #include "../openshadinglanguage_gb300/csrc/oslg_program.h"
+#include "oracle_shading.h"
 #include "oracle_simplex.h"
 
 #ifdef _OPENMP
@@ -567,16 +568,54 @@ void op_load_global(Point& P, const uint32_t* a, const oslg_shaderglobals& G) {
     }
 }
 
-// closure pools, same layout the device uses (oslg_program.h)
-struct CPools { uint32_t base, maxc, maxt; };
-uint32_t tslot(const CPools& C, uint32_t i) { return C.base + 1 + C.maxc * oslg::kCompFloats + i * oslg::kTermFloats; }
-uint32_t cslot(const CPools& C, uint32_t i) { return C.base + 1 + i * oslg::kCompFloats; }
-bool alloc_terms(Point& P, const CPools& C, uint32_t n, uint32_t& first) {
-    uint32_t w = P.heap[C.base], top = w >> 16;
-    if (top + n > C.maxt) { P.status |= oslg::ST_CLOSURE_OVERFLOW; return false; }
-    first = top;
-    P.heap[C.base] = (w & 0xFFFFu) | ((top + n) << 16);
-    return true;
+// Closure tree (src/include/OSL/oslclosure.h:65-147) in a per-point node
+// pool: [count][nodes of kNodeFloats]; a closure value is node index + 1.
+struct CPools { uint32_t base, maxn; };
+inline uint32_t nslot(const CPools& C, uint32_t node) { return C.base + 1 + node * oslg::kNodeFloats; }
+inline uint32_t cl_alloc(Point& P, const CPools& C) {
+    uint32_t n = P.heap[C.base];
+    if (n >= C.maxn) { P.status |= oslg::ST_CLOSURE_OVERFLOW; return 0u; }
+    P.heap[C.base] = n + 1;
+    return n + 1;
+}
+
+// testrender's traversal (src/testrender/shading.cpp:1450-1500): MUL scales
+// the running weight, ADD pushes its B branch with the current weight and
+// follows A, a component is visited with weight * comp.w.
+template <class F> void closure_walk(Point& P, const CPools& C, uint32_t root, F&& visit) {
+    uint32_t stack_node[oslg::kClosureWalkStack];
+    V3 stack_w[oslg::kClosureWalkStack];
+    int sp = 0;
+    V3 w(1.0f);
+    uint32_t cur = root;
+    int guard = 0;
+    while (cur != 0u && cur <= C.maxn) {
+        if (++guard > 4 * (int)C.maxn + 8) break;
+        uint32_t ns = nslot(C, cur - 1);
+        int id = (int32_t)P.heap[ns];
+        if (id == oslg::kClosureMul) {
+            w = w * V3(bitsf(P.heap[ns + 1]), bitsf(P.heap[ns + 2]), bitsf(P.heap[ns + 3]));
+            cur = P.heap[ns + 4];
+        } else if (id == oslg::kClosureAdd) {
+            if (sp < oslg::kClosureWalkStack) {
+                stack_node[sp] = P.heap[ns + 5];
+                stack_w[sp] = w;
+                ++sp;
+            } else {
+                P.status |= oslg::ST_CLOSURE_OVERFLOW;
+            }
+            cur = P.heap[ns + 4];
+        } else {
+            V3 cw = w * V3(bitsf(P.heap[ns + 1]), bitsf(P.heap[ns + 2]), bitsf(P.heap[ns + 3]));
+            visit(id, cw, ns + 4);
+            cur = 0u;
+        }
+        if (cur == 0u && sp > 0) {
+            --sp;
+            cur = stack_node[sp];
+            w = stack_w[sp];
+        }
+    }
 }
 
 struct Runner {
@@ -587,7 +626,7 @@ struct Runner {
 
     void run_point(Point& P) {
         const oslg::ProgramHeader& h = *prog.h;
-        CPools C{ h.closure_base, h.max_comps, h.max_terms };
+        CPools C{ h.closure_base, h.max_comps };
         if (h.flags & 1u) P.heap[C.base] = 0u;
         int nops = (int)h.nops;
         long long guard = 0;
@@ -837,70 +876,147 @@ struct Runner {
             case oslg::OP_NOISE: op_noise(P, a); break;
             case oslg::OP_HASH: op_hash(P, a); break;
             case oslg::OP_CLOSURE: {
-                uint32_t w = P.heap[C.base], n = w & 0xFFFFu;
-                if (n >= C.maxc) { P.status |= oslg::ST_CLOSURE_OVERFLOW; setw(P, a[0], 0, 0u); break; }
-                uint32_t cs = cslot(C, n);
-                P.heap[cs] = a[1];
-                uint32_t params[14];
+                // osl_allocate_(weighted_)closure_component (opclosure.cpp:83-117)
+                V3 w(1.0f);
+                if (a[2] != oslg::kNoArg) {
+                    w = V3(getf(P, a[2], 0, 0), getf(P, a[2], 1, 0), getf(P, a[2], 2, 0));
+                    if (w.x == 0.0f && w.y == 0.0f && w.z == 0.0f) { setw(P, a[0], 0, 0u); break; }
+                }
+                uint32_t h = cl_alloc(P, C);
+                if (!h) { setw(P, a[0], 0, 0u); break; }
+                uint32_t ns = nslot(C, h - 1);
+                P.heap[ns] = a[1];
+                P.heap[ns + 1] = fbits(w.x); P.heap[ns + 2] = fbits(w.y); P.heap[ns + 3] = fbits(w.z);
+                uint32_t params[11];
                 int np = 0;
-                for (int i = 2; i < 7; ++i) params[np++] = a[i];
+                for (int i = 3; i < 7; ++i) params[np++] = a[i];
                 if (pc + 1 < nops && prog.ops[pc + 1].code == oslg::OP_NOP && prog.ops[pc + 1].nargs == 7)
                     for (int i = 0; i < 7; ++i) params[np++] = prog.ops[pc + 1].a[i];
                 int k = 0;
                 for (int i = 0; i < np && k < oslg::kClosureParamFloats; ++i) {
                     if (params[i] == oslg::kNoArg) break;
-                    for (int c = 0; c < anc(params[i]) && k < oslg::kClosureParamFloats; ++c) {
-                        uint32_t t = atc(params[i]);
-                        P.heap[cs + 1 + k++] = (t == oslg::TC_INT || t == oslg::TC_STRING) ? word(P, params[i], c)
+                    uint32_t t = atc(params[i]);
+                    for (int c = 0; c < anc(params[i]) && k < oslg::kClosureParamFloats; ++c)
+                        P.heap[ns + 4 + k++] = (t == oslg::TC_INT || t == oslg::TC_STRING) ? word(P, params[i], c)
                                                                                             : fbits(getf(P, params[i], c, 0));
-                    }
                 }
-                P.heap[C.base] = (w & 0xFFFF0000u) | (n + 1);
-                uint32_t first;
-                if (!alloc_terms(P, C, 1, first)) { setw(P, a[0], 0, 0u); break; }
-                uint32_t ts = tslot(C, first);
-                P.heap[ts] = n;
-                P.heap[ts + 1] = P.heap[ts + 2] = P.heap[ts + 3] = fbits(1.0f);
-                setw(P, a[0], 0, (first << 16) | 1u);
+                for (; k < oslg::kClosureParamFloats; ++k) P.heap[ns + 4 + k] = fbits(0.0f);
+                setw(P, a[0], 0, h);
                 break;
             }
             case oslg::OP_CLOSURE_MUL: {
-                uint32_t hh = word(P, a[1], 0), cnt = hh & 0xFFFFu, src = hh >> 16;
-                if (!cnt) { setw(P, a[0], 0, 0u); break; }
-                float w[3] = { getf(P, a[2], 0, 0), getf(P, a[2], 1, 0), getf(P, a[2], 2, 0) };
-                uint32_t first;
-                if (!alloc_terms(P, C, cnt, first)) { setw(P, a[0], 0, 0u); break; }
-                for (uint32_t i = 0; i < cnt; ++i) {
-                    uint32_t s = tslot(C, src + i), d = tslot(C, first + i);
-                    P.heap[d] = P.heap[s];
-                    for (int k = 0; k < 3; ++k) P.heap[d + 1 + k] = fbits(bitsf(P.heap[s + 1 + k]) * w[k]);
-                }
-                setw(P, a[0], 0, (first << 16) | cnt);
+                // osl_mul_closure_color / _float (opclosure.cpp:35-80)
+                uint32_t c = word(P, a[1], 0);
+                V3 w(getf(P, a[2], 0, 0), getf(P, a[2], 1, 0), getf(P, a[2], 2, 0));
+                if (c == 0u || (w.x == 0.0f && w.y == 0.0f && w.z == 0.0f)) { setw(P, a[0], 0, 0u); break; }
+                if (w.x == 1.0f && w.y == 1.0f && w.z == 1.0f) { setw(P, a[0], 0, c); break; }
+                uint32_t h = cl_alloc(P, C);
+                if (!h) { setw(P, a[0], 0, 0u); break; }
+                uint32_t ns = nslot(C, h - 1);
+                P.heap[ns] = (uint32_t)oslg::kClosureMul;
+                P.heap[ns + 1] = fbits(w.x); P.heap[ns + 2] = fbits(w.y); P.heap[ns + 3] = fbits(w.z);
+                P.heap[ns + 4] = c;
+                setw(P, a[0], 0, h);
                 break;
             }
             case oslg::OP_CLOSURE_ADD: {
-                uint32_t ha = word(P, a[1], 0), hb = word(P, a[2], 0), ca = ha & 0xFFFFu, cb = hb & 0xFFFFu;
-                if (ca + cb == 0) { setw(P, a[0], 0, 0u); break; }
-                uint32_t first;
-                if (!alloc_terms(P, C, ca + cb, first)) { setw(P, a[0], 0, 0u); break; }
-                for (uint32_t i = 0; i < ca + cb; ++i) {
-                    uint32_t s = i < ca ? tslot(C, (ha >> 16) + i) : tslot(C, (hb >> 16) + i - ca), d = tslot(C, first + i);
-                    for (int k = 0; k < 4; ++k) P.heap[d + k] = P.heap[s + k];
-                }
-                setw(P, a[0], 0, (first << 16) | (ca + cb));
+                // osl_add_closure_closure (opclosure.cpp:15-33)
+                uint32_t x = word(P, a[1], 0), y = word(P, a[2], 0);
+                if (x == 0u) { setw(P, a[0], 0, y); break; }
+                if (y == 0u) { setw(P, a[0], 0, x); break; }
+                uint32_t h = cl_alloc(P, C);
+                if (!h) { setw(P, a[0], 0, 0u); break; }
+                uint32_t ns = nslot(C, h - 1);
+                P.heap[ns] = (uint32_t)oslg::kClosureAdd;
+                P.heap[ns + 4] = x;
+                P.heap[ns + 5] = y;
+                setw(P, a[0], 0, h);
                 break;
             }
             case oslg::OP_STORE_CLOSURE: {
-                uint32_t hh = word(P, a[0], 0), cnt = hh & 0xFFFFu, first = hh >> 16, maxc = a[3];
+                uint32_t root = word(P, a[0], 0), maxc = a[3];
                 uint32_t* q = reinterpret_cast<uint32_t*>(outputs + (int64_t)a[1] + P.pt * (int64_t)(int32_t)a[2]);
-                uint32_t n = std::min(cnt, maxc);
+                uint32_t n = 0;
+                closure_walk(P, C, root, [&](int id, const V3& cw, uint32_t params) {
+                    if (n >= maxc) return;
+                    uint32_t* rec = q + 1 + n * oslg::kNodeFloats;
+                    rec[0] = (uint32_t)id;
+                    rec[1] = fbits(cw.x); rec[2] = fbits(cw.y); rec[3] = fbits(cw.z);
+                    for (int k = 0; k < oslg::kClosureParamFloats; ++k) rec[4 + k] = P.heap[params + k];
+                    ++n;
+                });
                 q[0] = n;
-                for (uint32_t i = 0; i < n; ++i) {
-                    uint32_t ts = tslot(C, first + i), cs = cslot(C, P.heap[ts]);
-                    uint32_t* rec = q + 1 + i * (4 + oslg::kClosureParamFloats);
-                    rec[0] = P.heap[cs];
-                    for (int k = 0; k < 3; ++k) rec[1 + k] = P.heap[ts + 1 + k];
-                    for (int k = 0; k < oslg::kClosureParamFloats; ++k) rec[4 + k] = P.heap[cs + 1 + k];
+                break;
+            }
+            case oslg::OP_BSDF_EVAL: {
+                // testrender CompositeBSDF built by the closure walk, then
+                // prepare(wo, 1, absorb=false) and eval(wo, wi) (shading.h:322-374)
+                uint32_t root = word(P, a[0], 0);
+                V3 wi(getf(P, a[3], 0, 0), getf(P, a[3], 1, 0), getf(P, a[3], 2, 0));
+                V3 wo(-getf(P, a[4], 0, 0), -getf(P, a[4], 1, 0), -getf(P, a[4], 2, 0));
+                struct Lobe { int kind; V3 w; uint32_t params; };
+                Lobe lobes[oslg::kBsdfMaxLobes];
+                int nl = 0;
+                closure_walk(P, C, root, [&](int id, const V3& cw, uint32_t params) {
+                    int kind = -1;
+                    if (id == 3) kind = 0;  // DIFFUSE_ID
+                    else if (id == 8 && P.heap[params] == a[5] && (int32_t)P.heap[params + 10] == 0) kind = 1;
+                    if (kind < 0 || nl >= oslg::kBsdfMaxLobes) return;
+                    lobes[nl++] = { kind, cw, params };
+                });
+                auto f = [&](uint32_t s) { return bitsf(P.heap[s]); };
+                float pdfs[oslg::kBsdfMaxLobes];
+                float total = 0;
+                V3 path_weight(1.0f);
+                for (int i = 0; i < nl; ++i) {
+                    V3 alb(1.0f);
+                    if (lobes[i].kind == 1) {
+                        uint32_t p = lobes[i].params;
+                        MicrofacetGGXRefl m(V3(f(p + 1), f(p + 2), f(p + 3)), V3(f(p + 4), f(p + 5), f(p + 6)), f(p + 7),
+                                            f(p + 8), f(p + 9));
+                        alb = m.albedo(wo);
+                    }
+                    pdfs[i] = dotv(lobes[i].w, path_weight * alb) / (path_weight.x + path_weight.y + path_weight.z);
+                    total += pdfs[i];
+                }
+                if (total > 0 || total > 1)
+                    for (int i = 0; i < nl; ++i) pdfs[i] /= total;
+                Sample sres;
+                for (int i = 0; i < nl; ++i) {
+                    uint32_t p = lobes[i].params;
+                    Sample b;
+                    if (lobes[i].kind == 0) b = diffuse_eval(V3(f(p + 0), f(p + 1), f(p + 2)), wi);
+                    else {
+                        MicrofacetGGXRefl m(V3(f(p + 1), f(p + 2), f(p + 3)), V3(f(p + 4), f(p + 5), f(p + 6)), f(p + 7),
+                                            f(p + 8), f(p + 9));
+                        b = m.eval(wo, wi);
+                    }
+                    b.weight = b.weight * lobes[i].w;
+                    mis_update_eval(&sres.weight, &sres.pdf, b.weight, b.pdf, pdfs[i]);
+                    sres.roughness += b.roughness * pdfs[i];
+                }
+                float* o = reinterpret_cast<float*>(outputs + (int64_t)a[1] + P.pt * (int64_t)(int32_t)a[2]);
+                o[0] = sres.weight.x; o[1] = sres.weight.y; o[2] = sres.weight.z; o[3] = sres.pdf;
+                break;
+            }
+            case oslg::OP_SPLINE: {
+                uint32_t r = a[0], xa = a[1], kn = a[2];
+                int alen = (int)a[5];
+                int kcount = a[4] != oslg::kNoArg ? geti(P, a[4], 0) : alen;
+                if (kcount > alen) kcount = alen;
+                int nc = anc(r), kc = anc(kn);
+                bool kd = ader(kn);
+                for (int c = 0; c < nc; ++c) {
+                    int cc = kc == 1 ? 0 : c;
+                    auto knot = [&](int k) {
+                        float v = bitsf(word(P, kn, k * kc + cc));
+                        if (!kd) return DF(v);
+                        return DF(v, bitsf(word(P, kn, alen * kc + k * kc + cc)),
+                                  bitsf(word(P, kn, 2 * alen * kc + k * kc + cc)));
+                    };
+                    DF res = spline_channel((int)a[3], getd(P, xa, 0), ader(xa), kd, kcount, knot);
+                    if (!ader(r)) putv(P, r, c, res.v);
+                    else putd(P, r, c, res);
                 }
                 break;
             }

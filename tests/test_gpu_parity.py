@@ -139,3 +139,21 @@ def test_empty_and_single_point_batches():
     ref = np.zeros((1, rec), np.float32)
     oracle_run(g.program_bytes(), 1, grid_globals(u, v, 1, 1, centers=True), ref)
     assert_same(got, ref, int_cols=(rec - 1,))
+
+
+@pytest.mark.parametrize("heap", [1, 0])
+def test_layered_closure_group_matches_oracle(heap):
+    from openshadinglanguage_gb300 import workloads
+    ss = og.ShadingSystem()
+    ss.set_launch(block=256, heap_smem=heap)
+    g = workloads.c2_group(ss)
+    W = H = 256
+    u, v, I = workloads.c2_inputs(W, H)
+    du, dv, dI = dev(u), dev(v), dev(I)
+    Gd = workloads.c2_globals(og.make_globals, du, dv, dI)
+    rec = workloads.C2_STRIDE // 4
+    got = gpu_run(ss, g, W * H, Gd, rec)
+    ref = np.zeros((W * H, rec), np.float32)
+    assert oracle_run(g.program_bytes(), W * H, workloads.c2_globals(og.make_globals, u, v, I), ref) == 0
+    int_cols = [0] + [1 + 16 * k for k in range(workloads.C2_CLOSURE_RECORDS)] + [5 + 16]  # counts, ids, dist hash
+    assert_same(got, ref, int_cols=tuple(int_cols))
