@@ -9,7 +9,7 @@
 namespace oslg {
 
 struct LaunchConfig {
-    int block = 256;           // threads per CTA
+    int block = 0;             // threads per CTA (0: chosen from the heap size)
     int points_per_thread = 1; // points each thread interleaves
     int heap_smem = -1;        // 1 shared-memory heap, 0 HBM scratch heap, -1 auto
     int grid = 0;              // 0: as many CTAs as the point count needs

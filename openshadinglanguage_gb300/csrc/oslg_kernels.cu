@@ -200,6 +200,126 @@ __device__ void h_assign(const Lane& L, const uint32_t* a, uint32_t* st) {
     }
 }
 
+// ---- decoded operands ------------------------------------------------------------------
+// A float-based operand decoded once per op: component c, partial d (1 = x,
+// 2 = y) lives at p[c*cs + d*ds]; scalars broadcast (cs = 0); operands
+// without partials read zero partials.
+struct Opd {
+    float* p;
+    int cs, ds;
+    bool hasd;
+};
+__device__ __forceinline__ Opd dec(const Lane& L, uint32_t a) {
+    Opd o;
+    int nc = anc(a);
+    int unit;
+    if (aconst(a)) {
+        o.p = const_cast<float*>(reinterpret_cast<const float*>(L.pool)) + aoff(a);
+        unit = 1;
+    } else {
+        o.p = L.heap + (size_t)aoff(a) * L.hs + L.li;
+        unit = L.hs;
+    }
+    o.cs = nc == 1 ? 0 : unit;
+    o.ds = nc * unit;
+    o.hasd = ader(a);
+    return o;
+}
+__device__ __forceinline__ float gv(const Opd& o, int c) { return o.p[c * o.cs]; }
+__device__ __forceinline__ float gd(const Opd& o, int c, int d) { return o.hasd ? o.p[c * o.cs + d * o.ds] : 0.0f; }
+__device__ __forceinline__ void sv(const Opd& o, int c, float v) { o.p[c * o.cs] = v; }
+__device__ __forceinline__ void sd(const Opd& o, int c, int d, float v) { o.p[c * o.cs + d * o.ds] = v; }
+__device__ __forceinline__ bool no_ints(uint32_t a, uint32_t b, uint32_t c) {
+    return atc(a) != TC_INT && atc(b) != TC_INT && atc(c) != TC_INT;
+}
+
+// add/sub/mul/div over NC components of float-based operands (same Dual2
+// rules as h_arith below, with the operand decode hoisted out of the loop)
+template <int K, int NC>
+__device__ __forceinline__ void arith_fast_n(const Opd& R, const Opd& X, const Opd& Y, bool rd) {
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+        float xv = gv(X, c), yv = gv(Y, c);
+        float v;
+        if (K == 0) v = xv + yv;
+        else if (K == 1) v = xv - yv;
+        else if (K == 2) v = xv * yv;
+        else v = (yv == 0.0f) ? 0.0f : xv / yv;
+        sv(R, c, v);
+        if (!rd) continue;
+        float dx, dy;
+        if (K == 0 || K == 1) {
+            if (X.hasd && Y.hasd) {
+                float xdx = gd(X, c, 1), xdy = gd(X, c, 2), ydx = gd(Y, c, 1), ydy = gd(Y, c, 2);
+                dx = K == 0 ? xdx + ydx : xdx - ydx;
+                dy = K == 0 ? xdy + ydy : xdy - ydy;
+            } else if (X.hasd) {
+                dx = gd(X, c, 1); dy = gd(X, c, 2);
+            } else if (Y.hasd) {
+                dx = K == 0 ? gd(Y, c, 1) : -gd(Y, c, 1);
+                dy = K == 0 ? gd(Y, c, 2) : -gd(Y, c, 2);
+            } else { dx = 0.0f; dy = 0.0f; }
+        } else if (K == 2) {
+            if (X.hasd && Y.hasd) {
+                dx = xv * gd(Y, c, 1) + gd(X, c, 1) * yv;
+                dy = xv * gd(Y, c, 2) + gd(X, c, 2) * yv;
+            } else if (X.hasd) {
+                dx = gd(X, c, 1) * yv; dy = gd(X, c, 2) * yv;
+            } else if (Y.hasd) {
+                dx = gd(Y, c, 1) * xv; dy = gd(Y, c, 2) * xv;
+            } else { dx = 0.0f; dy = 0.0f; }
+        } else {
+            if (yv == 0.0f) { dx = 0.0f; dy = 0.0f; }
+            else {
+                float binv = 1.0f / yv, q = xv / yv;
+                if (X.hasd && Y.hasd) {
+                    dx = binv * (gd(X, c, 1) - q * gd(Y, c, 1));
+                    dy = binv * (gd(X, c, 2) - q * gd(Y, c, 2));
+                } else if (X.hasd) {
+                    dx = binv * gd(X, c, 1); dy = binv * gd(X, c, 2);
+                } else if (Y.hasd) {
+                    dx = binv * (-q * gd(Y, c, 1)); dy = binv * (-q * gd(Y, c, 2));
+                } else { dx = 0.0f; dy = 0.0f; }
+            }
+        }
+        sd(R, c, 1, dx);
+        sd(R, c, 2, dy);
+    }
+}
+
+template <int K>
+__device__ void h_arith(const Lane& L, const uint32_t* a);
+
+template <int K>
+__device__ __forceinline__ void h_arith_fast(const Lane& L, const uint32_t* a) {
+    uint32_t r = a[0], x = a[1], y = a[2];
+    if (!no_ints(r, x, y)) { h_arith<K>(L, a); return; }
+    Opd R = dec(L, r), X = dec(L, x), Y = dec(L, y);
+    bool rd = ader(r);
+    int nc = anc(r);
+    if (nc == 3) arith_fast_n<K, 3>(R, X, Y, rd);
+    else if (nc == 1) arith_fast_n<K, 1>(R, X, Y, rd);
+    else h_arith<K>(L, a);
+}
+
+// assign of a non-array float-based value (broadcasting scalars)
+__device__ void h_assign(const Lane& L, const uint32_t* a, uint32_t* st);
+__device__ __forceinline__ void h_assign_fast(const Lane& L, const uint32_t* a, uint32_t* st) {
+    uint32_t r = a[0], s = a[1];
+    uint32_t tr = atc(r), ts = atc(s);
+    if ((tr != TC_FLOAT && tr != TC_TRIPLE) || (ts != TC_FLOAT && ts != TC_TRIPLE) || a[3] > 1u || a[4] > 1u) {
+        h_assign(L, a, st);
+        return;
+    }
+    Opd R = dec(L, r), S = dec(L, s);
+    int nc = anc(r);
+    bool rd = ader(r);
+    for (int c = 0; c < nc; ++c) {
+        sv(R, c, gv(S, c));
+        if (rd) { sd(R, c, 1, gd(S, c, 1)); sd(R, c, 2, gd(S, c, 2)); }
+    }
+}
+
 // add/sub/mul/div/mod on float-based values, componentwise with scalar
 // broadcast; derivatives follow src/include/OSL/dual.h:403-620
 template <int K>
@@ -1253,7 +1373,7 @@ __global__ void __launch_bounds__(256) interp_kernel(KArgs k) {
                     case OP_LOAD_GLOBAL: h_load_global(L, a, k.G); break;
                     case OP_LOAD_USERDATA: h_load_userdata(L, a, k.userdata); break;
                     case OP_STORE_OUTPUT: h_store_output(L, a, k.outputs); break;
-                    case OP_ASSIGN: h_assign(L, a, k.status); break;
+                    case OP_ASSIGN: h_assign_fast(L, a, k.status); break;
                     case OP_COMPREF: h_compref(L, a, k.status); break;
                     case OP_COMPASSIGN: h_compassign(L, a, k.status); break;
                     case OP_MXCOMPREF: {
@@ -1276,10 +1396,10 @@ __global__ void __launch_bounds__(256) interp_kernel(KArgs k) {
                         for (int i = 0; i < 16; ++i) stf(L, a[0], i, (i % 5 == 0) ? v : 0.0f);
                         break;
                     }
-                    case OP_ADD: h_arith<0>(L, a); break;
-                    case OP_SUB: h_arith<1>(L, a); break;
-                    case OP_MUL: h_arith<2>(L, a); break;
-                    case OP_DIV: h_arith<3>(L, a); break;
+                    case OP_ADD: h_arith_fast<0>(L, a); break;
+                    case OP_SUB: h_arith_fast<1>(L, a); break;
+                    case OP_MUL: h_arith_fast<2>(L, a); break;
+                    case OP_DIV: h_arith_fast<3>(L, a); break;
                     case OP_MOD: h_arith<4>(L, a); break;
                     case OP_NEG: h_unary<OP_NEG>(L, a); break;
                     case OP_IADD: h_iarith<0>(L, a); break;
@@ -1452,13 +1572,29 @@ int device_execute(DeviceState& ds, const ProgramHeader& hdr, const void* d_blob
     if (npoints <= 0) return OSLG_OK;
     int rc = device_init(ds, err);
     if (rc != OSLG_OK) return rc;
-    int block = cfg.block > 0 ? cfg.block : 256;
-    if (block > 256) block = 256;
-    block = (block + 31) & ~31;
     size_t static_bytes = (size_t)hdr.nops * sizeof(Op) + (size_t)((hdr.nconst + 3) & ~3u) * 4;
+    // Launch shape: an explicit block/heap placement is honoured; otherwise
+    // pick the largest block (256, 128, 64) whose shared-memory heap fits
+    // 100 KiB per CTA (two CTAs per SM), else the HBM heap with 256 threads.
+    int block = cfg.block > 0 ? cfg.block : 0;
+    bool smem;
+    if (block > 0) {
+        if (block > 256) block = 256;
+        block = (block + 31) & ~31;
+        size_t hb = (size_t)hdr.heap_slots * block * sizeof(float);
+        smem = cfg.heap_smem == 1 || (cfg.heap_smem < 0 && static_bytes + hb <= 100 * 1024);
+    } else if (cfg.heap_smem == 0) {
+        block = 256;
+        smem = false;
+    } else {
+        block = 0;
+        for (int b : { 256, 128, 64 }) {
+            if (static_bytes + (size_t)hdr.heap_slots * b * sizeof(float) <= 100 * 1024) { block = b; break; }
+        }
+        smem = block > 0;
+        if (!smem) block = 256;
+    }
     size_t heap_bytes = (size_t)hdr.heap_slots * block * sizeof(float);
-    bool smem = cfg.heap_smem == 1;
-    if (cfg.heap_smem < 0) smem = static_bytes + heap_bytes <= 96 * 1024;
     if (smem && static_bytes + heap_bytes > ds.smem_optin) smem = false;
     size_t shmem = static_bytes + (smem ? heap_bytes : 0);
     if (shmem > ds.smem_optin) {

@@ -405,21 +405,96 @@ struct Lowerer {
         return off;
     }
 
+    // Live interval of every heap symbol over the linear op list, widened to
+    // cover each loop that references it (a value can flow around the back
+    // edge). Symbols whose intervals do not overlap share heap slots.
     void assign_storage() {
         for (const LOp& op : lops)
             for (int a : op.args) syms[a].referenced = true;
-        for (GSym& s : syms) {
+        const int n = (int)lops.size();
+        std::vector<int> first(syms.size(), n), last(syms.size(), -1);
+        for (int k = 0; k < n; ++k)
+            for (int a : lops[k].args) {
+                first[a] = std::min(first[a], k);
+                last[a] = std::max(last[a], k);
+            }
+        // loops as [begin, end] op ranges
+        std::vector<std::pair<int, int>> loops;
+        for (int k = 0; k < n; ++k) {
+            const LOp& op = lops[k];
+            if ((op.name == "for" || op.name == "while" || op.name == "dowhile") && op.jumps.size() >= 4)
+                loops.push_back({ k, op.jumps[3] });
+        }
+        for (size_t si = 0; si < syms.size(); ++si) {
+            if (last[si] < 0) continue;
+            bool changed = true;
+            while (changed) {
+                changed = false;
+                for (auto& L : loops) {
+                    bool touches = !(last[si] < L.first || first[si] > L.second);
+                    if (touches && (first[si] > L.first || last[si] < L.second)) {
+                        first[si] = std::min(first[si], L.first);
+                        last[si] = std::max(last[si], L.second);
+                        changed = true;
+                    }
+                }
+            }
+        }
+        // globals are loaded before op 0; keep them live from the start
+        for (auto& kv : globals)
+            if (syms[kv.second].referenced) first[kv.second] = -1;
+        std::vector<int> order;
+        for (size_t si = 0; si < syms.size(); ++si) {
+            GSym& s = syms[si];
             if (!s.referenced) continue;
             if (s.is_const) {
                 s.slot = (int)pool_add(s);
                 continue;
             }
-            int n = s.type.ncomp() * s.type.elems() * (s.derivs ? 3 : 1);
-            if (s.type.base == BT_VOID) n = 0;
-            s.slot = (int)heap_top;
-            heap_top += (uint32_t)n;
+            order.push_back((int)si);
         }
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return first[a] < first[b]; });
+        // first-fit reuse of freed slot ranges with the same size
+        std::multimap<int, uint32_t> free_by_size;          // size -> slot
+        std::multimap<int, std::pair<int, int>> active;     // last use -> (sym, size)
+        for (int si : order) {
+            GSym& s = syms[si];
+            int sz = s.type.ncomp() * s.type.elems() * (s.derivs ? 3 : 1);
+            if (s.type.base == BT_VOID) sz = 0;
+            while (!active.empty() && active.begin()->first < first[si]) {
+                auto it = active.begin();
+                free_by_size.insert({ it->second.second, (uint32_t)syms[it->second.first].slot });
+                active.erase(it);
+            }
+            auto f = free_by_size.find(sz);
+            if (f != free_by_size.end()) {
+                s.slot = (int)f->second;
+                free_by_size.erase(f);
+            } else {
+                s.slot = (int)heap_top;
+                heap_top += (uint32_t)sz;
+            }
+            active.insert({ last[si], { si, sz } });
+        }
+        // closure node pool: one node per closure-creating op when none sits
+        // inside a loop, else the configured capacity
+        int nclosure_ops = 0;
+        bool closure_in_loop = false;
+        for (int k = 0; k < n; ++k) {
+            const LOp& op = lops[k];
+            bool creates = op.name == "closure"
+                        || ((op.name == "mul" || op.name == "add") && !op.args.empty()
+                            && syms[op.args[0]].type.base == BT_CLOSURE);
+            if (!creates) continue;
+            ++nclosure_ops;
+            for (auto& L : loops)
+                if (k > L.first && k < L.second) closure_in_loop = true;
+        }
+        closure_nodes = closure_in_loop ? ss.opts.max_closure_components
+                                        : std::min(nclosure_ops, ss.opts.max_closure_components);
+        if (closure_nodes < 1) closure_nodes = 1;
     }
+    int closure_nodes = 0;
 
     uint32_t A(int gs) {
         const GSym& s = syms[gs];
@@ -859,7 +934,7 @@ struct Lowerer {
         h.nops = (uint32_t)ops.size();
         h.nconst = (uint32_t)pool.size();
         h.closure_base = heap_top;
-        h.max_comps = uses_closures ? (uint32_t)ss.opts.max_closure_components : 0u;
+        h.max_comps = uses_closures ? (uint32_t)closure_nodes : 0u;
         h.max_terms = 0u;
         uint32_t closure_slots = uses_closures ? 1 + h.max_comps * kNodeFloats : 0;
         h.heap_slots = heap_top + closure_slots;
