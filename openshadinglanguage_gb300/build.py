@@ -19,7 +19,10 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 HOST_SOURCES = ["oslg_oso.cpp", "oslg_lower.cpp", "oslg_capi.cpp"]
-CUDA_SOURCES = ["oslg_kernels.cu"]
+# (source, object name, extra flags): the interpreter is compiled once per
+# feature tier (oslg_tier.cu with -DOSLG_TIER=N), in parallel
+CUDA_SOURCES = [("oslg_kernels.cu", "oslg_kernels", [])] + [
+    ("oslg_tier.cu", "oslg_tier%d" % t, ["-DOSLG_TIER=%d" % t]) for t in range(8)]
 
 
 def _run(cmd):
@@ -48,13 +51,13 @@ def build(verbose=False, ptxas_verbose=False):
         if not _newer(o, [s] + headers):
             jobs.append(["g++", "-std=c++17", "-O2", "-fPIC", "-Wall", "-Wno-unused-function",
                          "-I", os.path.join(CUDA_HOME, "include"), "-c", s, "-o", o])
-    for src in CUDA_SOURCES:
+    for src, name, extra in CUDA_SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src + ".o")
+        o = os.path.join(BUILD, name + ".o")
         objs.append(o)
         if not _newer(o, [s] + headers) or ptxas_verbose:
-            cmd = [NVCC] + ARCH + ["-std=c++17", "-O3", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC",
-                                   "-c", s, "-o", o]
+            cmd = [NVCC] + ARCH + ["-std=c++17", "-O3", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC"] + extra + [
+                "-c", s, "-o", o]
             if ptxas_verbose:
                 cmd.insert(1, "-Xptxas=-v")
             jobs.append(cmd)

@@ -8,6 +8,29 @@
 
 namespace oslg {
 
+namespace dev {
+// Kernel arguments of the interpreter (oslg_interp.cuh).
+struct KArgs {
+    const uint8_t* blob;
+    int64_t npoints;
+    char* userdata;
+    char* outputs;
+    float* gheap;
+    uint32_t* status;
+    oslg_shaderglobals G;
+};
+}  // namespace dev
+
+// One interpreter instantiation per feature tier (oslg_tier.cu compiled with
+// -DOSLG_TIER=N): TIER bits 1 noise/hash, 2 closures/BSDF/spline, 4 math.
+static const int kNumTiers = 8;
+struct TierFns {
+    int (*launch)(bool smem_heap, unsigned grid, unsigned block, size_t shmem, void* stream, const dev::KArgs& k);
+    int (*occupancy)(bool smem_heap, int block, size_t shmem, int* per_sm);
+    int (*set_smem_limit)(int bytes);
+};
+const TierFns& tier_fns(int tier);
+
 struct LaunchConfig {
     int block = 0;             // threads per CTA (0: chosen from the heap size)
     int points_per_thread = 1; // points each thread interleaves

@@ -1,21 +1,6 @@
-// sm_103a interpreter for lowered OSL shader groups.
-//
-// One thread shades one point. All lanes of a warp walk the same op index
-// (the program counter is warp-uniform), so the big dispatch switch never
-// diverges; varying control flow is carried by a per-lane `act` flag and
-// per-depth bit stacks, the same masked-SIMD model the reference's batched
-// backend uses (src/liboslexec/batched_llvm_gen.cpp:1068 if, :3806-4250
-// loops, break/continue), with __any_sync skipping blocks no lane enters.
-//
-// Memory: the op stream and the constant pool are staged once per CTA in
-// shared memory (warp-uniform broadcast reads). Per-point symbol values
-// live in a slot-major heap, either in shared memory (heap_smem=1) or in a
-// per-CTA slice of an HBM scratch buffer sized to the resident grid, which
-// stays L2-resident (heap_smem=0). Grid-stride tiles keep the grid at the
-// resident CTA count.
-//
-// Built with -fmad=false: every float result equals the non-FMA reference
-// arithmetic bit for bit (see oslg_noise.cuh).
+// Host side of the sm_103a interpreter: device set-up, launch-shape choice,
+// the per-group launch (oslg_execute_batch) and the allocation-free launch.
+// The kernels themselves live in the tier translation units (oslg_tier.cu).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -25,1489 +10,31 @@
 #include <string>
 
 #include "oslg_exec.h"
-#include "oslg_noise.cuh"
-#include "oslg_shading.cuh"
 
 namespace oslg {
-namespace dev {
 
+const TierFns& tier_fns_0();
+const TierFns& tier_fns_1();
+const TierFns& tier_fns_2();
+const TierFns& tier_fns_3();
+const TierFns& tier_fns_4();
+const TierFns& tier_fns_5();
+const TierFns& tier_fns_6();
+const TierFns& tier_fns_7();
 
-// blackbody / closure helpers live further down
-static const unsigned FULL = 0xFFFFFFFFu;
-
-struct KArgs {
-    const uint8_t* blob;
-    int64_t npoints;
-    char* userdata;
-    char* outputs;
-    float* gheap;
-    uint32_t* status;
-    oslg_shaderglobals G;
-};
-
-struct Lane {
-    float* heap;
-    const uint32_t* pool;
-    int hs;      // heap stride (points per CTA tile)
-    int li;      // lane index within the tile
-    int64_t pt;  // global point index
-};
-
-__device__ __forceinline__ uint32_t aoff(uint32_t a) { return a & kArgOffsetMask; }
-__device__ __forceinline__ bool aconst(uint32_t a) { return (a & kArgConst) != 0; }
-__device__ __forceinline__ bool ader(uint32_t a) { return (a & kArgDerivs) != 0; }
-__device__ __forceinline__ uint32_t atc(uint32_t a) { return (a >> kArgTCShift) & 7u; }
-__device__ __forceinline__ int anc(uint32_t a) {
-    uint32_t t = atc(a);
-    return t == TC_TRIPLE ? 3 : (t == TC_MATRIX ? 16 : 1);
-}
-
-__device__ __forceinline__ uint32_t ldw(const Lane& L, uint32_t a, int idx) {
-    uint32_t o = aoff(a) + (uint32_t)idx;
-    if (aconst(a)) return L.pool[o];
-    return __float_as_uint(L.heap[(size_t)o * L.hs + L.li]);
-}
-__device__ __forceinline__ void stw(const Lane& L, uint32_t a, int idx, uint32_t v) {
-    L.heap[(size_t)(aoff(a) + (uint32_t)idx) * L.hs + L.li] = __uint_as_float(v);
-}
-__device__ __forceinline__ void stf(const Lane& L, uint32_t a, int idx, float v) { stw(L, a, idx, __float_as_uint(v)); }
-
-// value (d=0) or x/y partial (d=1,2) of component c; scalars broadcast,
-// ints convert, missing partials read as zero
-__device__ __forceinline__ float ldf(const Lane& L, uint32_t a, int c, int d) {
-    int nc = anc(a);
-    if (d && !ader(a)) return 0.0f;
-    uint32_t w = ldw(L, a, d * nc + (nc == 1 ? 0 : c));
-    return atc(a) == TC_INT ? (float)(int)w : __uint_as_float(w);
-}
-__device__ __forceinline__ D2 ldd(const Lane& L, uint32_t a, int c) {
-    return d2(ldf(L, a, c, 0), ldf(L, a, c, 1), ldf(L, a, c, 2));
-}
-__device__ __forceinline__ int ldi(const Lane& L, uint32_t a, int c) {
-    uint32_t t = atc(a);
-    uint32_t w = ldw(L, a, t == TC_TRIPLE ? c : 0);
-    if (t == TC_FLOAT || t == TC_TRIPLE) return (int)__uint_as_float(w);
-    return (int)w;
-}
-// store a Dual2 into component c of r (partials only if r carries them)
-__device__ __forceinline__ void std2(const Lane& L, uint32_t r, int c, D2 v) {
-    int nc = anc(r);
-    if (atc(r) == TC_INT) { stw(L, r, c, (uint32_t)(int)v.v); return; }
-    stf(L, r, c, v.v);
-    if (ader(r)) {
-        stf(L, r, nc + c, v.dx);
-        stf(L, r, 2 * nc + c, v.dy);
-    }
-}
-__device__ __forceinline__ void stval(const Lane& L, uint32_t r, int c, float v) {
-    if (atc(r) == TC_INT) { stw(L, r, c, (uint32_t)(int)v); return; }
-    int nc = anc(r);
-    stf(L, r, c, v);
-    if (ader(r)) {
-        stf(L, r, nc + c, 0.0f);
-        stf(L, r, 2 * nc + c, 0.0f);
-    }
-}
-__device__ __forceinline__ void raise_status(uint32_t* st, uint32_t bit) { atomicOr(st, bit); }
-
-// ---- math helpers (values through double precision: correctly rounded
-// float results, identical on every platform that rounds double libm
-// results correctly to float) --------------------------------------------------
-__device__ __forceinline__ float fsin(float x) { return (float)sin((double)x); }
-__device__ __forceinline__ float fcos(float x) { return (float)cos((double)x); }
-__device__ __forceinline__ float ftan(float x) { return (float)tan((double)x); }
-__device__ __forceinline__ float fasin(float x) { return (float)asin((double)x); }
-__device__ __forceinline__ float facos(float x) { return (float)acos((double)x); }
-__device__ __forceinline__ float fatan(float x) { return (float)atan((double)x); }
-__device__ __forceinline__ float fatan2(float y, float x) { return (float)atan2((double)y, (double)x); }
-__device__ __forceinline__ float fsinh(float x) { return (float)sinh((double)x); }
-__device__ __forceinline__ float fcosh(float x) { return (float)cosh((double)x); }
-__device__ __forceinline__ float ftanh(float x) { return (float)tanh((double)x); }
-__device__ __forceinline__ float fexp(float x) { return (float)exp((double)x); }
-__device__ __forceinline__ float fexp2(float x) { return (float)exp2((double)x); }
-__device__ __forceinline__ float fexpm1(float x) { return (float)expm1((double)x); }
-__device__ __forceinline__ float fcbrt(float x) { return (float)cbrt((double)x); }
-__device__ __forceinline__ float flog_raw(float x) { return (float)log((double)x); }
-__device__ __forceinline__ float flog2_raw(float x) { return (float)log2((double)x); }
-__device__ __forceinline__ float flog10_raw(float x) { return (float)log10((double)x); }
-__device__ __forceinline__ float fpow_raw(float x, float y) { return (float)pow((double)x, (double)y); }
-static const float kFltMin = 1.17549435e-38f;
-static const float kFltMax = 3.40282347e+38f;
-// OIIO safe_log/log2/log10: clamp the argument to the smallest normal
-__device__ __forceinline__ float safe_log(float x) { return flog_raw(x < kFltMin ? kFltMin : x); }
-__device__ __forceinline__ float safe_log2(float x) { return flog2_raw(x < kFltMin ? kFltMin : x); }
-__device__ __forceinline__ float safe_log10(float x) { return flog10_raw(x < kFltMin ? kFltMin : x); }
-// OIIO safe_pow: integer powers only for negative bases; no infinities
-__device__ __forceinline__ float safe_pow(float x, float y) {
-    if (y == 0.0f) return 1.0f;
-    if (x == 0.0f) return 0.0f;
-    if (x < 0.0f && y != floorf(y)) return 0.0f;
-    float r = fpow_raw(x, y);
-    return fminf(fmaxf(r, -kFltMax), kFltMax);
-}
-__device__ __forceinline__ float safe_fmod(float a, float b) {
-    if (b != 0.0f) {
-        int N = (int)(a / b);
-        return a - (float)N * b;
-    }
-    return 0.0f;
-}
-
-// ---- handlers -------------------------------------------------------------------
-__device__ void h_assign(const Lane& L, const uint32_t* a, uint32_t* st) {
-    uint32_t r = a[0], s = a[1];
-    uint32_t tr = atc(r), ts = atc(s);
-    int count = (int)a[2];
-    if (tr == TC_CLOSURE) {
-        stw(L, r, 0, ts == TC_CLOSURE ? ldw(L, s, 0) : 0u);
-        return;
-    }
-    if (tr == TC_STRING) { stw(L, r, 0, ldw(L, s, 0)); return; }
-    if (tr == TC_MATRIX) {
-        if (ts == TC_MATRIX) {
-            for (int i = 0; i < 16; ++i) stw(L, r, i, ldw(L, s, i));
-        } else {
-            float v = ldf(L, s, 0, 0);
-            for (int i = 0; i < 16; ++i) stf(L, r, i, (i % 5 == 0) ? v : 0.0f);
-        }
-        return;
-    }
-    int ralen = (int)a[3], salen = (int)a[4];
-    if (ralen < 1) ralen = 1;
-    if (salen < 1) salen = 1;
-    int nr = anc(r), ns = anc(s);
-    for (int e = 0; e < count; ++e) {
-        for (int c = 0; c < nr; ++c) {
-            int sc = ns == 1 ? 0 : c;
-            uint32_t sw = ldw(L, s, e * ns + sc);
-            if (tr == TC_INT) {
-                int iv = ts == TC_INT ? (int)sw : (int)__uint_as_float(sw);
-                stw(L, r, e * nr + c, (uint32_t)iv);
-                continue;
-            }
-            float v = ts == TC_INT ? (float)(int)sw : __uint_as_float(sw);
-            stf(L, r, e * nr + c, v);
-            if (ader(r)) {
-                float dx = 0.0f, dy = 0.0f;
-                if (ader(s)) {
-                    dx = __uint_as_float(ldw(L, s, salen * ns + e * ns + sc));
-                    dy = __uint_as_float(ldw(L, s, 2 * salen * ns + e * ns + sc));
-                }
-                stf(L, r, ralen * nr + e * nr + c, dx);
-                stf(L, r, 2 * ralen * nr + e * nr + c, dy);
-            }
-        }
+const TierFns& tier_fns(int tier) {
+    switch (tier & 7) {
+    case 0: return tier_fns_0();
+    case 1: return tier_fns_1();
+    case 2: return tier_fns_2();
+    case 3: return tier_fns_3();
+    case 4: return tier_fns_4();
+    case 5: return tier_fns_5();
+    case 6: return tier_fns_6();
+    default: return tier_fns_7();
     }
 }
 
-// ---- decoded operands ------------------------------------------------------------------
-// A float-based operand decoded once per op: component c, partial d (1 = x,
-// 2 = y) lives at p[c*cs + d*ds]; scalars broadcast (cs = 0); operands
-// without partials read zero partials.
-struct Opd {
-    float* p;
-    int cs, ds;
-    bool hasd;
-};
-__device__ __forceinline__ Opd dec(const Lane& L, uint32_t a) {
-    Opd o;
-    int nc = anc(a);
-    int unit;
-    if (aconst(a)) {
-        o.p = const_cast<float*>(reinterpret_cast<const float*>(L.pool)) + aoff(a);
-        unit = 1;
-    } else {
-        o.p = L.heap + (size_t)aoff(a) * L.hs + L.li;
-        unit = L.hs;
-    }
-    o.cs = nc == 1 ? 0 : unit;
-    o.ds = nc * unit;
-    o.hasd = ader(a);
-    return o;
-}
-__device__ __forceinline__ float gv(const Opd& o, int c) { return o.p[c * o.cs]; }
-__device__ __forceinline__ float gd(const Opd& o, int c, int d) { return o.hasd ? o.p[c * o.cs + d * o.ds] : 0.0f; }
-__device__ __forceinline__ void sv(const Opd& o, int c, float v) { o.p[c * o.cs] = v; }
-__device__ __forceinline__ void sd(const Opd& o, int c, int d, float v) { o.p[c * o.cs + d * o.ds] = v; }
-__device__ __forceinline__ bool no_ints(uint32_t a, uint32_t b, uint32_t c) {
-    return atc(a) != TC_INT && atc(b) != TC_INT && atc(c) != TC_INT;
-}
-
-// add/sub/mul/div over NC components of float-based operands (same Dual2
-// rules as h_arith below, with the operand decode hoisted out of the loop)
-template <int K, int NC>
-__device__ __forceinline__ void arith_fast_n(const Opd& R, const Opd& X, const Opd& Y, bool rd) {
-#pragma unroll
-    for (int c = 0; c < NC; ++c) {
-        float xv = gv(X, c), yv = gv(Y, c);
-        float v;
-        if (K == 0) v = xv + yv;
-        else if (K == 1) v = xv - yv;
-        else if (K == 2) v = xv * yv;
-        else v = (yv == 0.0f) ? 0.0f : xv / yv;
-        sv(R, c, v);
-        if (!rd) continue;
-        float dx, dy;
-        if (K == 0 || K == 1) {
-            if (X.hasd && Y.hasd) {
-                float xdx = gd(X, c, 1), xdy = gd(X, c, 2), ydx = gd(Y, c, 1), ydy = gd(Y, c, 2);
-                dx = K == 0 ? xdx + ydx : xdx - ydx;
-                dy = K == 0 ? xdy + ydy : xdy - ydy;
-            } else if (X.hasd) {
-                dx = gd(X, c, 1); dy = gd(X, c, 2);
-            } else if (Y.hasd) {
-                dx = K == 0 ? gd(Y, c, 1) : -gd(Y, c, 1);
-                dy = K == 0 ? gd(Y, c, 2) : -gd(Y, c, 2);
-            } else { dx = 0.0f; dy = 0.0f; }
-        } else if (K == 2) {
-            if (X.hasd && Y.hasd) {
-                dx = xv * gd(Y, c, 1) + gd(X, c, 1) * yv;
-                dy = xv * gd(Y, c, 2) + gd(X, c, 2) * yv;
-            } else if (X.hasd) {
-                dx = gd(X, c, 1) * yv; dy = gd(X, c, 2) * yv;
-            } else if (Y.hasd) {
-                dx = gd(Y, c, 1) * xv; dy = gd(Y, c, 2) * xv;
-            } else { dx = 0.0f; dy = 0.0f; }
-        } else {
-            if (yv == 0.0f) { dx = 0.0f; dy = 0.0f; }
-            else {
-                float binv = 1.0f / yv, q = xv / yv;
-                if (X.hasd && Y.hasd) {
-                    dx = binv * (gd(X, c, 1) - q * gd(Y, c, 1));
-                    dy = binv * (gd(X, c, 2) - q * gd(Y, c, 2));
-                } else if (X.hasd) {
-                    dx = binv * gd(X, c, 1); dy = binv * gd(X, c, 2);
-                } else if (Y.hasd) {
-                    dx = binv * (-q * gd(Y, c, 1)); dy = binv * (-q * gd(Y, c, 2));
-                } else { dx = 0.0f; dy = 0.0f; }
-            }
-        }
-        sd(R, c, 1, dx);
-        sd(R, c, 2, dy);
-    }
-}
-
-template <int K>
-__device__ void h_arith(const Lane& L, const uint32_t* a);
-
-template <int K>
-__device__ __forceinline__ void h_arith_fast(const Lane& L, const uint32_t* a) {
-    uint32_t r = a[0], x = a[1], y = a[2];
-    if (!no_ints(r, x, y)) { h_arith<K>(L, a); return; }
-    Opd R = dec(L, r), X = dec(L, x), Y = dec(L, y);
-    bool rd = ader(r);
-    int nc = anc(r);
-    if (nc == 3) arith_fast_n<K, 3>(R, X, Y, rd);
-    else if (nc == 1) arith_fast_n<K, 1>(R, X, Y, rd);
-    else h_arith<K>(L, a);
-}
-
-// assign of a non-array float-based value (broadcasting scalars)
-__device__ void h_assign(const Lane& L, const uint32_t* a, uint32_t* st);
-__device__ __forceinline__ void h_assign_fast(const Lane& L, const uint32_t* a, uint32_t* st) {
-    uint32_t r = a[0], s = a[1];
-    uint32_t tr = atc(r), ts = atc(s);
-    if ((tr != TC_FLOAT && tr != TC_TRIPLE) || (ts != TC_FLOAT && ts != TC_TRIPLE) || a[3] > 1u || a[4] > 1u) {
-        h_assign(L, a, st);
-        return;
-    }
-    Opd R = dec(L, r), S = dec(L, s);
-    int nc = anc(r);
-    bool rd = ader(r);
-    for (int c = 0; c < nc; ++c) {
-        sv(R, c, gv(S, c));
-        if (rd) { sd(R, c, 1, gd(S, c, 1)); sd(R, c, 2, gd(S, c, 2)); }
-    }
-}
-
-// add/sub/mul/div/mod on float-based values, componentwise with scalar
-// broadcast; derivatives follow src/include/OSL/dual.h:403-620
-template <int K>
-__device__ void h_arith(const Lane& L, const uint32_t* a) {
-    uint32_t r = a[0], x = a[1], y = a[2];
-    int nc = anc(r);
-    bool rd = ader(r), xd = ader(x), yd = ader(y);
-    for (int c = 0; c < nc; ++c) {
-        float xv = ldf(L, x, c, 0), yv = ldf(L, y, c, 0);
-        float v;
-        if (K == 0) v = xv + yv;
-        else if (K == 1) v = xv - yv;
-        else if (K == 2) v = xv * yv;
-        else if (K == 3) v = (yv == 0.0f) ? 0.0f : xv / yv;
-        else v = (yv == 0.0f) ? 0.0f : fmodf(xv, yv);
-        if (atc(r) == TC_INT) { stw(L, r, c, (uint32_t)(int)v); continue; }
-        stf(L, r, c, v);
-        if (!rd) continue;
-        float dx, dy;
-        if (K == 0 || K == 1) {
-            float xdx = ldf(L, x, c, 1), xdy = ldf(L, x, c, 2), ydx = ldf(L, y, c, 1), ydy = ldf(L, y, c, 2);
-            if (K == 0) { dx = xdx + ydx; dy = xdy + ydy; }
-            else { dx = xdx - ydx; dy = xdy - ydy; }
-            if (!yd) { dx = xdx; dy = xdy; if (K == 1 && !xd) { dx = 0.0f; dy = 0.0f; } }
-            if (!xd && yd) { dx = K == 0 ? ydx : -ydx; dy = K == 0 ? ydy : -ydy; }
-        } else if (K == 2) {
-            if (xd && yd) {
-                dx = xv * ldf(L, y, c, 1) + ldf(L, x, c, 1) * yv;
-                dy = xv * ldf(L, y, c, 2) + ldf(L, x, c, 2) * yv;
-            } else if (xd) {
-                dx = ldf(L, x, c, 1) * yv; dy = ldf(L, x, c, 2) * yv;
-            } else if (yd) {
-                dx = ldf(L, y, c, 1) * xv; dy = ldf(L, y, c, 2) * xv;
-            } else { dx = 0.0f; dy = 0.0f; }
-        } else if (K == 3) {
-            if (yv == 0.0f) { dx = 0.0f; dy = 0.0f; }
-            else {
-                float binv = 1.0f / yv, q = xv / yv;
-                if (xd && yd) {
-                    dx = binv * (ldf(L, x, c, 1) - q * ldf(L, y, c, 1));
-                    dy = binv * (ldf(L, x, c, 2) - q * ldf(L, y, c, 2));
-                } else if (xd) {
-                    dx = binv * ldf(L, x, c, 1); dy = binv * ldf(L, x, c, 2);
-                } else if (yd) {
-                    dx = binv * (-q * ldf(L, y, c, 1)); dy = binv * (-q * ldf(L, y, c, 2));
-                } else { dx = 0.0f; dy = 0.0f; }
-            }
-        } else {
-            dx = ldf(L, x, c, 1); dy = ldf(L, x, c, 2);
-        }
-        stf(L, r, nc + c, dx);
-        stf(L, r, 2 * nc + c, dy);
-    }
-}
-
-template <int K>
-__device__ void h_iarith(const Lane& L, const uint32_t* a) {
-    int x = ldi(L, a[1], 0), y = ldi(L, a[2], 0), v;
-    if (K == 0) v = (int)((uint32_t)x + (uint32_t)y);
-    else if (K == 1) v = (int)((uint32_t)x - (uint32_t)y);
-    else if (K == 2) v = (int)((uint32_t)x * (uint32_t)y);
-    else if (K == 3) v = (y == 0 || (x == INT_MIN && y == -1)) ? 0 : x / y;
-    else v = (y == 0 || (x == INT_MIN && y == -1)) ? 0 : x % y;
-    stw(L, a[0], 0, (uint32_t)v);
-}
-
-__device__ void h_mmul(const Lane& L, const uint32_t* a) {
-    uint32_t r = a[0], x = a[1], y = a[2];
-    float out[16];
-    if (atc(x) == TC_MATRIX && atc(y) == TC_MATRIX) {
-        float A[16], B[16];
-        for (int i = 0; i < 16; ++i) { A[i] = __uint_as_float(ldw(L, x, i)); B[i] = __uint_as_float(ldw(L, y, i)); }
-        for (int i = 0; i < 4; ++i)
-            for (int j = 0; j < 4; ++j)
-                out[i * 4 + j] = A[i * 4 + 0] * B[0 * 4 + j] + A[i * 4 + 1] * B[1 * 4 + j]
-                               + A[i * 4 + 2] * B[2 * 4 + j] + A[i * 4 + 3] * B[3 * 4 + j];
-    } else {
-        uint32_t m = atc(x) == TC_MATRIX ? x : y, s = atc(x) == TC_MATRIX ? y : x;
-        float f = ldf(L, s, 0, 0);
-        for (int i = 0; i < 16; ++i) out[i] = __uint_as_float(ldw(L, m, i)) * f;
-    }
-    for (int i = 0; i < 16; ++i) stf(L, r, i, out[i]);
-}
-
-// comparisons: float compare unless both operands are ints (or strings)
-template <int K>
-__device__ void h_cmp(const Lane& L, const uint32_t* a) {
-    uint32_t x = a[1], y = a[2];
-    bool ints = (atc(x) == TC_INT || atc(x) == TC_STRING) && (atc(y) == TC_INT || atc(y) == TC_STRING);
-    int n = anc(x) > anc(y) ? anc(x) : anc(y);
-    bool res;
-    if (ints) {
-        int xi = (int)ldw(L, x, 0), yi = (int)ldw(L, y, 0);
-        if (K == 0) res = xi == yi; else if (K == 1) res = xi != yi; else if (K == 2) res = xi < yi;
-        else if (K == 3) res = xi > yi; else if (K == 4) res = xi <= yi; else res = xi >= yi;
-    } else if (K == 0 || K == 1) {
-        bool eq = true;
-        for (int c = 0; c < n; ++c) eq = eq && (ldf(L, x, c, 0) == ldf(L, y, c, 0));
-        res = K == 0 ? eq : !eq;
-    } else {
-        float xv = ldf(L, x, 0, 0), yv = ldf(L, y, 0, 0);
-        if (K == 2) res = xv < yv; else if (K == 3) res = xv > yv; else if (K == 4) res = xv <= yv; else res = xv >= yv;
-    }
-    stw(L, a[0], 0, res ? 1u : 0u);
-}
-
-__device__ __forceinline__ bool truth(const Lane& L, uint32_t a) {
-    uint32_t t = atc(a);
-    if (t == TC_FLOAT) return ldf(L, a, 0, 0) != 0.0f;
-    if (t == TC_TRIPLE) return ldf(L, a, 0, 0) != 0.0f || ldf(L, a, 1, 0) != 0.0f || ldf(L, a, 2, 0) != 0.0f;
-    return ldw(L, a, 0) != 0u;
-}
-
-// componentwise unary math with dual.h derivative rules
-template <int OPC>
-__device__ void h_unary(const Lane& L, const uint32_t* a) {
-    uint32_t r = a[0], x = a[1];
-    int nc = anc(r);
-    bool rd = ader(r);
-    for (int c = 0; c < nc; ++c) {
-        float v = ldf(L, x, c, 0);
-        float f, df = 0.0f;
-        bool zero_derivs = false;
-        switch (OPC) {
-        case OP_ABS: f = fabsf(v); df = v >= 0.0f ? 1.0f : -1.0f; break;
-        case OP_FLOOR: f = floorf(v); zero_derivs = true; break;
-        case OP_CEIL: f = ceilf(v); zero_derivs = true; break;
-        case OP_ROUND: f = roundf(v); zero_derivs = true; break;
-        case OP_TRUNC: f = truncf(v); zero_derivs = true; break;
-        case OP_SIGN: f = v < 0.0f ? -1.0f : (v == 0.0f ? 0.0f : 1.0f); zero_derivs = true; break;
-        case OP_SQRT:
-            if (v > 0.0f) { f = sqrtf(v); df = 0.5f / f; } else { f = 0.0f; zero_derivs = true; }
-            break;
-        case OP_INVSQRT:
-            if (v > 0.0f) { f = 1.0f / sqrtf(v); df = -0.5f * f / v; } else { f = 0.0f; zero_derivs = true; }
-            break;
-        case OP_CBRT:
-            if (v != 0.0f) { f = fcbrt(v); df = 1.0f / (3.0f * f * f); } else { f = 0.0f; zero_derivs = true; }
-            break;
-        case OP_SIN: f = fsin(v); df = fcos(v); break;
-        case OP_COS: f = fcos(v); df = -fsin(v); break;
-        case OP_TAN: { f = ftan(v); float cs = fcos(v); df = 1.0f / (cs * cs); break; }
-        case OP_ASIN:
-            if (v >= 1.0f) { f = 1.57079632679489661923f; zero_derivs = true; }
-            else if (v <= -1.0f) { f = -1.57079632679489661923f; zero_derivs = true; }
-            else { f = fasin(v); df = 1.0f / sqrtf(1.0f - v * v); }
-            break;
-        case OP_ACOS:
-            if (v >= 1.0f) { f = 0.0f; zero_derivs = true; }
-            else if (v <= -1.0f) { f = 3.14159265358979323846f; zero_derivs = true; }
-            else { f = facos(v); df = -1.0f / sqrtf(1.0f - v * v); }
-            break;
-        case OP_ATAN: f = fatan(v); df = 1.0f / (1.0f + v * v); break;
-        case OP_SINH: f = fsinh(v); df = fcosh(v); break;
-        case OP_COSH: f = fcosh(v); df = fsinh(v); break;
-        case OP_TANH: { f = ftanh(v); float ch = fcosh(v); df = 1.0f / (ch * ch); break; }
-        case OP_EXP: f = fexp(v); df = f; break;
-        case OP_EXP2: f = fexp2(v); df = f * 0.693147180559945309417f; break;
-        case OP_EXPM1: f = fexpm1(v); df = fexp(v); break;
-        case OP_LOG: f = safe_log(v); df = v < kFltMin ? 0.0f : 1.0f / v; break;
-        case OP_LOG2: f = safe_log2(v); df = v < kFltMin ? 0.0f : 1.0f / (v * 0.693147180559945309417f); break;
-        case OP_LOG10: f = safe_log10(v); df = v < kFltMin ? 0.0f : 1.0f / (v * 2.30258509299404568402f); break;
-        case OP_RADIANS: f = v * (3.14159265358979323846f / 180.0f); df = 3.14159265358979323846f / 180.0f; break;
-        case OP_DEGREES: f = v * (180.0f / 3.14159265358979323846f); df = 180.0f / 3.14159265358979323846f; break;
-        case OP_NEG: f = -v; df = -1.0f; break;
-        default: f = v; break;
-        }
-        if (atc(r) == TC_INT) { stw(L, r, c, (uint32_t)(int)f); continue; }
-        stf(L, r, c, f);
-        if (!rd) continue;
-        float dx = 0.0f, dy = 0.0f;
-        if (!zero_derivs && ader(x)) {
-            if (OPC == OP_NEG) { dx = -ldf(L, x, c, 1); dy = -ldf(L, x, c, 2); }
-            else if (OPC == OP_ABS) {
-                // fabs of a dual negates the whole dual when val < 0
-                dx = v >= 0.0f ? ldf(L, x, c, 1) : -ldf(L, x, c, 1);
-                dy = v >= 0.0f ? ldf(L, x, c, 2) : -ldf(L, x, c, 2);
-            } else if (OPC == OP_RADIANS || OPC == OP_DEGREES) {
-                dx = ldf(L, x, c, 1) * df; dy = ldf(L, x, c, 2) * df;
-            } else { dx = df * ldf(L, x, c, 1); dy = df * ldf(L, x, c, 2); }
-        }
-        stf(L, r, nc + c, dx);
-        stf(L, r, 2 * nc + c, dy);
-    }
-}
-
-template <int OPC>
-__device__ void h_binary(const Lane& L, const uint32_t* a) {
-    uint32_t r = a[0], x = a[1], y = a[2];
-    int nc = anc(r);
-    bool rd = ader(r);
-    for (int c = 0; c < nc; ++c) {
-        D2 u = ldd(L, x, c), v = ldd(L, y, c);
-        D2 res;
-        if (OPC == OP_POW) {
-            if (rd && (ader(x) || ader(y))) {
-                float powuvm1 = safe_pow(u.v, v.v - 1.0f);
-                float powuv = powuvm1 * u.v;
-                float logu = u.v > 0.0f ? safe_log(u.v) : 0.0f;
-                float du = v.v * powuvm1, dv = logu * powuv;
-                res = d2(powuv, du * u.dx + dv * v.dx, du * u.dy + dv * v.dy);
-            } else {
-                res = d2c(safe_pow(u.v, v.v));
-            }
-        } else if (OPC == OP_ATAN2) {
-            float f = fatan2(u.v, v.v);
-            float denom = (v.v == 0.0f && u.v == 0.0f) ? 0.0f : 1.0f / (v.v * v.v + u.v * u.v);
-            float dfdy = -v.v * denom, dfdx = u.v * denom;
-            res = d2(f, dfdy * u.dx + dfdx * v.dx, dfdy * u.dy + dfdx * v.dy);
-        } else if (OPC == OP_FMOD) {
-            res = d2(safe_fmod(u.v, v.v), u.dx, u.dy);
-        } else if (OPC == OP_MIN) {
-            res = u.v <= v.v ? u : v;
-        } else if (OPC == OP_MAX) {
-            res = u.v > v.v ? u : v;
-        } else {  // OP_STEP: step(edge, x)
-            res = d2c(v.v < u.v ? 0.0f : 1.0f);
-        }
-        if (!rd) { stval(L, r, c, res.v); continue; }
-        std2(L, r, c, res);
-    }
-}
-
-__device__ void h_clamp(const Lane& L, const uint32_t* a) {
-    uint32_t r = a[0];
-    int nc = anc(r);
-    for (int c = 0; c < nc; ++c) {
-        D2 x = ldd(L, a[1], c), lo = ldd(L, a[2], c), hi = ldd(L, a[3], c);
-        if (atc(r) == TC_INT) {
-            int xi = ldi(L, a[1], c), li = ldi(L, a[2], c), hiv = ldi(L, a[3], c);
-            xi = xi < li ? li : xi;
-            xi = xi > hiv ? hiv : xi;
-            stw(L, r, c, (uint32_t)xi);
-            continue;
-        }
-        D2 v = x.v < lo.v ? lo : x;
-        v = v.v > hi.v ? hi : v;
-        std2(L, r, c, v);
-    }
-}
-
-__device__ void h_mix(const Lane& L, const uint32_t* a) {
-    uint32_t r = a[0];
-    int nc = anc(r);
-    for (int c = 0; c < nc; ++c) {
-        D2 x = ldd(L, a[1], c), y = ldd(L, a[2], c), t = ldd(L, a[3], c);
-        float one_t = 1.0f - t.v;
-        float v = x.v * one_t + y.v * t.v;
-        float ymx = y.v - x.v;
-        D2 res = d2(v, one_t * x.dx + t.v * y.dx + ymx * t.dx, one_t * x.dy + t.v * y.dy + ymx * t.dy);
-        std2(L, r, c, res);
-    }
-}
-
-__device__ void h_smoothstep(const Lane& L, const uint32_t* a) {
-    uint32_t r = a[0];
-    int nc = anc(r);
-    for (int c = 0; c < nc; ++c) {
-        D2 e0 = ldd(L, a[1], c), e1 = ldd(L, a[2], c), x = ldd(L, a[3], c);
-        D2 res;
-        if (x.v < e0.v) res = d2c(0.0f);
-        else if (x.v >= e1.v) res = d2c(1.0f);
-        else if (!ader(r)) {
-            float t = (x.v - e0.v) / (e1.v - e0.v);
-            res = d2c((3.0f - 2.0f * t) * (t * t));
-        } else {
-            // Dual2: t = (x-e0)/(e1-e0); (3 - 2t)*t*t
-            D2 num = x - e0, den = e1 - e0;
-            float binv = 1.0f / den.v, q = num.v / den.v;
-            D2 t = d2(q, binv * (num.dx - q * den.dx), binv * (num.dy - q * den.dy));
-            D2 k = d2(3.0f - 2.0f * t.v, -(t.dx * 2.0f), -(t.dy * 2.0f));
-            res = (k * t) * t;
-        }
-        std2(L, r, c, res);
-    }
-}
-
-__device__ void h_select(const Lane& L, const uint32_t* a) {
-    uint32_t r = a[0];
-    int nc = anc(r);
-    for (int c = 0; c < nc; ++c) {
-        bool cond = atc(a[3]) == TC_TRIPLE ? ldf(L, a[3], c, 0) != 0.0f : truth(L, a[3]);
-        D2 v = cond ? ldd(L, a[2], c) : ldd(L, a[1], c);
-        if (atc(r) == TC_INT) { stw(L, r, c, (uint32_t)ldi(L, cond ? a[2] : a[1], c)); continue; }
-        std2(L, r, c, v);
-    }
-}
-
-// ---- vector ops (dual_vec.h) ----------------------------------------------------
-__device__ void h_dot(const Lane& L, const uint32_t* a) {
-    D2 ax = ldd(L, a[1], 0), ay = ldd(L, a[1], 1), az = ldd(L, a[1], 2);
-    D2 bx = ldd(L, a[2], 0), by = ldd(L, a[2], 1), bz = ldd(L, a[2], 2);
-    if (!ader(a[0])) { stval(L, a[0], 0, ax.v * bx.v + ay.v * by.v + az.v * bz.v); return; }
-    std2(L, a[0], 0, ax * bx + ay * by + az * bz);
-}
-__device__ void h_cross(const Lane& L, const uint32_t* a) {
-    D2 ax = ldd(L, a[1], 0), ay = ldd(L, a[1], 1), az = ldd(L, a[1], 2);
-    D2 bx = ldd(L, a[2], 0), by = ldd(L, a[2], 1), bz = ldd(L, a[2], 2);
-    if (!ader(a[0])) {
-        stval(L, a[0], 0, ay.v * bz.v - az.v * by.v);
-        stval(L, a[0], 1, az.v * bx.v - ax.v * bz.v);
-        stval(L, a[0], 2, ax.v * by.v - ay.v * bx.v);
-        return;
-    }
-    std2(L, a[0], 0, ay * bz - az * by);
-    std2(L, a[0], 1, az * bx - ax * bz);
-    std2(L, a[0], 2, ax * by - ay * bx);
-}
-__device__ __forceinline__ D2 dsqrt(D2 a) {
-    if (a.v > 0.0f) { float f = sqrtf(a.v), df = 0.5f / f; return d2(f, df * a.dx, df * a.dy); }
-    return d2c(0.0f);
-}
-// Imath Vec3::length() for the value-only path
-__device__ __forceinline__ float vlength(float x, float y, float z) {
-    float l2 = x * x + y * y + z * z;
-    if (l2 < 2.0f * kFltMin) {
-        // lengthTiny: rescale by the largest component
-        float m = fmaxf(fabsf(x), fmaxf(fabsf(y), fabsf(z)));
-        if (m == 0.0f) return 0.0f;
-        x /= m; y /= m; z /= m;
-        return m * sqrtf(x * x + y * y + z * z);
-    }
-    return sqrtf(l2);
-}
-__device__ void h_length(const Lane& L, const uint32_t* a, bool distance) {
-    D2 x = ldd(L, a[1], 0), y = ldd(L, a[1], 1), z = ldd(L, a[1], 2);
-    if (distance) { x = x - ldd(L, a[2], 0); y = y - ldd(L, a[2], 1); z = z - ldd(L, a[2], 2); }
-    if (!ader(a[0])) {
-        float v = distance ? sqrtf(x.v * x.v + y.v * y.v + z.v * z.v) : vlength(x.v, y.v, z.v);
-        stval(L, a[0], 0, v);
-        return;
-    }
-    std2(L, a[0], 0, dsqrt(x * x + y * y + z * z));
-}
-__device__ void h_normalize(const Lane& L, const uint32_t* a) {
-    D2 x = ldd(L, a[1], 0), y = ldd(L, a[1], 1), z = ldd(L, a[1], 2);
-    if (!ader(a[0])) {
-        float len = sqrtf(x.v * x.v + y.v * y.v + z.v * z.v);
-        if (len > 0.0f) {
-            float inv = 1.0f / len;
-            stval(L, a[0], 0, x.v * inv); stval(L, a[0], 1, y.v * inv); stval(L, a[0], 2, z.v * inv);
-        } else {
-            stval(L, a[0], 0, 0.0f); stval(L, a[0], 1, 0.0f); stval(L, a[0], 2, 0.0f);
-        }
-        return;
-    }
-    D2 len = dsqrt(x * x + y * y + z * z);
-    if (len.v > 0.0f) {
-        float binv = 1.0f / len.v, q = 1.0f / len.v;
-        D2 inv = d2(q, binv * (-q * len.dx), binv * (-q * len.dy));
-        std2(L, a[0], 0, x * inv); std2(L, a[0], 1, y * inv); std2(L, a[0], 2, z * inv);
-    } else {
-        for (int c = 0; c < 3; ++c) std2(L, a[0], c, d2c(0.0f));
-    }
-}
-
-// ---- transforms (dual_vec.h:336-400, opmatrix.cpp:86-131) ---------------------
-__device__ void h_transform(const Lane& L, const uint32_t* a) {
-    uint32_t r = a[0], p = a[1], m = a[2];
-    int kind = (int)a[3];
-    float M[16];
-    for (int i = 0; i < 16; ++i) M[i] = __uint_as_float(ldw(L, m, i));
-    D2 x = ldd(L, p, 0), y = ldd(L, p, 1), z = ldd(L, p, 2);
-    if (kind == 0) {
-        // robust_multVecMatrix: homogeneous point, divide by w unless w == 0
-        if (!ader(r)) {
-            float A = x.v * M[0] + y.v * M[4] + z.v * M[8] + M[12];
-            float B = x.v * M[1] + y.v * M[5] + z.v * M[9] + M[13];
-            float C = x.v * M[2] + y.v * M[6] + z.v * M[10] + M[14];
-            float W = x.v * M[3] + y.v * M[7] + z.v * M[11] + M[15];
-            if (W != 0.0f) { stval(L, r, 0, A / W); stval(L, r, 1, B / W); stval(L, r, 2, C / W); }
-            else { stval(L, r, 0, 0.0f); stval(L, r, 1, 0.0f); stval(L, r, 2, 0.0f); }
-            return;
-        }
-        D2 A = x * M[0] + y * M[4] + z * M[8] + M[12];
-        D2 B = x * M[1] + y * M[5] + z * M[9] + M[13];
-        D2 C = x * M[2] + y * M[6] + z * M[10] + M[14];
-        D2 W = x * M[3] + y * M[7] + z * M[11] + M[15];
-        if (W.v != 0.0f) {
-            float binv = 1.0f / W.v;
-            D2 o[3] = { A, B, C };
-            for (int c = 0; c < 3; ++c) {
-                float q = o[c].v / W.v;
-                std2(L, r, c, d2(q, binv * (o[c].dx - q * W.dx), binv * (o[c].dy - q * W.dy)));
-            }
-        } else {
-            for (int c = 0; c < 3; ++c) std2(L, r, c, d2c(0.0f));
-        }
-        return;
-    }
-    // vector (multDirMatrix on value and each partial)
-    float in[3][3] = { { x.v, y.v, z.v }, { x.dx, y.dx, z.dx }, { x.dy, y.dy, z.dy } };
-    int nd = ader(r) ? 3 : 1;
-    for (int d = 0; d < nd; ++d) {
-        float X = in[d][0], Y = in[d][1], Z = in[d][2];
-        float o0 = X * M[0] + Y * M[4] + Z * M[8];
-        float o1 = X * M[1] + Y * M[5] + Z * M[9];
-        float o2 = X * M[2] + Y * M[6] + Z * M[10];
-        stf(L, r, d * 3 + 0, o0); stf(L, r, d * 3 + 1, o1); stf(L, r, d * 3 + 2, o2);
-    }
-}
-
-// ---- noise ---------------------------------------------------------------------
-__device__ void h_noise(const Lane& L, const uint32_t* a) {
-    uint32_t r = a[0], S = a[1], T = a[2], kw = a[3];
-    int kind = (int)(kw & 15u);
-    bool periodic = (kw & 16u) != 0;
-    int dims = (int)((kw >> 5) & 7u);
-    bool vec = (kw & 256u) != 0;
-    bool derivs = (kw & 512u) != 0;
-    int ns = anc(S);
-    int nc = vec ? 3 : 1;
-    float res[3], rdx[3] = { 0, 0, 0 }, rdy[3] = { 0, 0, 0 };
-    Hasher H;
-    H.periodic = periodic;
-    H.px = H.py = H.pz = H.pw = 1;
-    if (periodic) {
-        uint32_t SP = a[4], TP = a[5];
-        if (ns == 3) {
-            H.px = period_of(ldf(L, SP, 0, 0)); H.py = period_of(ldf(L, SP, 1, 0)); H.pz = period_of(ldf(L, SP, 2, 0));
-            if (dims == 4) H.pw = period_of(ldf(L, TP, 0, 0));
-        } else {
-            H.px = period_of(ldf(L, SP, 0, 0));
-            if (dims == 2) H.py = period_of(ldf(L, TP, 0, 0));
-        }
-    }
-    if (kind == NK_CELL || kind == NK_HASH) {
-        float xs[4];
-        for (int i = 0; i < ns; ++i) xs[i] = ldf(L, S, i, 0);
-        if (T != kNoArg) xs[ns] = ldf(L, T, 0, 0);
-        if (periodic) {
-            if (ns == 3) {
-                xs[0] = pwrap(xs[0], ldf(L, a[4], 0, 0)); xs[1] = pwrap(xs[1], ldf(L, a[4], 1, 0));
-                xs[2] = pwrap(xs[2], ldf(L, a[4], 2, 0));
-                if (dims == 4) xs[3] = pwrap(xs[3], ldf(L, a[5], 0, 0));
-            } else {
-                xs[0] = pwrap(xs[0], ldf(L, a[4], 0, 0));
-                if (dims == 2) xs[1] = pwrap(xs[1], ldf(L, a[5], 0, 0));
-            }
-        }
-        intnoise(kind == NK_CELL, dims, xs, nc, res);
-    } else if (kind == NK_PERLIN || kind == NK_UPERLIN) {
-        if (derivs) {
-            D2 xs[4];
-            for (int i = 0; i < ns; ++i) xs[i] = ldd(L, S, i);
-            if (T != kNoArg) xs[ns] = ldd(L, T, 0);
-            D2 o[3];
-            if (vec) {
-                switch (dims) {
-                case 1: perlin1<D2, 3>(H, xs[0], o); break;
-                case 2: perlin2<D2, 3>(H, xs[0], xs[1], o); break;
-                case 3: perlin3<D2, 3>(H, xs[0], xs[1], xs[2], o); break;
-                default: perlin4<D2, 3>(H, xs[0], xs[1], xs[2], xs[3], o); break;
-                }
-            } else {
-                switch (dims) {
-                case 1: perlin1<D2, 1>(H, xs[0], o); break;
-                case 2: perlin2<D2, 1>(H, xs[0], xs[1], o); break;
-                case 3: perlin3<D2, 1>(H, xs[0], xs[1], xs[2], o); break;
-                default: perlin4<D2, 1>(H, xs[0], xs[1], xs[2], xs[3], o); break;
-                }
-            }
-            for (int c = 0; c < nc; ++c) {
-                if (kind == NK_UPERLIN) o[c] = (o[c] + 1.0f) * 0.5f;
-                res[c] = o[c].v; rdx[c] = o[c].dx; rdy[c] = o[c].dy;
-            }
-        } else {
-            float xs[4];
-            for (int i = 0; i < ns; ++i) xs[i] = ldf(L, S, i, 0);
-            if (T != kNoArg) xs[ns] = ldf(L, T, 0, 0);
-            if (vec) {
-                switch (dims) {
-                case 1: perlin1<float, 3>(H, xs[0], res); break;
-                case 2: perlin2<float, 3>(H, xs[0], xs[1], res); break;
-                case 3: perlin3<float, 3>(H, xs[0], xs[1], xs[2], res); break;
-                default: perlin4<float, 3>(H, xs[0], xs[1], xs[2], xs[3], res); break;
-                }
-            } else {
-                switch (dims) {
-                case 1: perlin1<float, 1>(H, xs[0], res); break;
-                case 2: perlin2<float, 1>(H, xs[0], xs[1], res); break;
-                case 3: perlin3<float, 1>(H, xs[0], xs[1], xs[2], res); break;
-                default: perlin4<float, 1>(H, xs[0], xs[1], xs[2], xs[3], res); break;
-                }
-            }
-            if (kind == NK_UPERLIN)
-                for (int c = 0; c < nc; ++c) res[c] = 0.5f * (res[c] + 1.0f);
-        }
-    } else if (kind == NK_SIMPLEX || kind == NK_USIMPLEX) {
-        D2 xs[4];
-        for (int i = 0; i < ns; ++i) xs[i] = ldd(L, S, i);
-        if (T != kNoArg) xs[ns] = ldd(L, T, 0);
-        for (int c = 0; c < nc; ++c) {
-            float g[4] = { 0, 0, 0, 0 };
-            float v;
-            switch (dims) {
-            case 1: v = simplex1(xs[0].v, c, derivs ? &g[0] : nullptr); break;
-            case 2: v = simplex2(xs[0].v, xs[1].v, c, derivs ? &g[0] : nullptr, &g[1]); break;
-            case 3: v = simplex3(xs[0].v, xs[1].v, xs[2].v, c, derivs ? &g[0] : nullptr, &g[1], &g[2]); break;
-            default: v = simplex4(xs[0].v, xs[1].v, xs[2].v, xs[3].v, c, derivs ? g : nullptr); break;
-            }
-            D2 o = d2c(v);
-            if (derivs) {
-                float dx = g[0] * xs[0].dx, dy = g[0] * xs[0].dy;
-                for (int i = 1; i < dims; ++i) { dx = dx + g[i] * xs[i].dx; dy = dy + g[i] * xs[i].dy; }
-                o = d2(v, dx, dy);
-            }
-            if (kind == NK_USIMPLEX) o = (o + 1.0f) * 0.5f;
-            res[c] = o.v; rdx[c] = o.dx; rdy[c] = o.dy;
-        }
-    } else if (kind == NK_NULL || kind == NK_UNULL) {
-        for (int c = 0; c < nc; ++c) res[c] = kind == NK_UNULL ? 0.5f : 0.0f;
-    } else {
-        for (int c = 0; c < nc; ++c) res[c] = 0.0f;
-    }
-    // float result from triple request or vice versa is handled by lowering;
-    // scalar noise into a triple symbol broadcasts
-    int rn = anc(r);
-    for (int c = 0; c < rn; ++c) {
-        int sc = nc == 1 ? 0 : c;
-        stf(L, r, c, res[sc]);
-        if (ader(r)) {
-            stf(L, r, rn + c, rdx[sc]);
-            stf(L, r, 2 * rn + c, rdy[sc]);
-        }
-    }
-}
-
-__device__ void h_hash(const Lane& L, const uint32_t* a) {
-    uint32_t x = a[1], y = a[2];
-    uint32_t h;
-    uint32_t tx = atc(x);
-    if (tx == TC_INT) h = inthash1(ldw(L, x, 0));
-    else if (tx == TC_STRING) h = ldw(L, x, 0);
-    else if (tx == TC_TRIPLE) {
-        if (y == kNoArg) h = inthash3(ldw(L, x, 0), ldw(L, x, 1), ldw(L, x, 2));
-        else h = inthash4(ldw(L, x, 0), ldw(L, x, 1), ldw(L, x, 2), __float_as_uint(ldf(L, y, 0, 0)));
-    } else {
-        if (y == kNoArg) h = inthash1(__float_as_uint(ldf(L, x, 0, 0)));
-        else h = inthash2(__float_as_uint(ldf(L, x, 0, 0)), __float_as_uint(ldf(L, y, 0, 0)));
-    }
-    stw(L, a[0], 0, h);
-}
-
-// ---- globals / arenas -------------------------------------------------------------
-__device__ __forceinline__ const oslg_field& gfield(const oslg_shaderglobals& G, int id) {
-    switch (id) {
-    case G_P: return G.P; case G_DPDX: return G.dPdx; case G_DPDY: return G.dPdy; case G_DPDZ: return G.dPdz;
-    case G_I: return G.I; case G_DIDX: return G.dIdx; case G_DIDY: return G.dIdy;
-    case G_N: return G.N; case G_NG: return G.Ng;
-    case G_U: return G.u; case G_DUDX: return G.dudx; case G_DUDY: return G.dudy;
-    case G_V: return G.v; case G_DVDX: return G.dvdx; case G_DVDY: return G.dvdy;
-    case G_DPDU: return G.dPdu; case G_DPDV: return G.dPdv;
-    case G_TIME: return G.time; case G_DTIME: return G.dtime; case G_DPDTIME: return G.dPdtime;
-    case G_PS: return G.Ps; case G_DPSDX: return G.dPsdx; case G_DPSDY: return G.dPsdy;
-    default: return G.surfacearea;
-    }
-}
-__device__ __forceinline__ float fld(const oslg_field& f, int c, int64_t pt) {
-    return f.data ? __ldg(f.data + c * f.plane_stride + pt) : f.value[c];
-}
-
-__device__ void h_load_global(const Lane& L, const uint32_t* a, const oslg_shaderglobals& G) {
-    uint32_t r = a[0];
-    int id = (int)a[1];
-    int nc = anc(r);
-    const oslg_field& f = gfield(G, id);
-    for (int c = 0; c < nc; ++c) stf(L, r, c, fld(f, c, L.pt));
-    if (ader(r)) {
-        int dxid = -1, dyid = -1;
-        if (id == G_P) { dxid = G_DPDX; dyid = G_DPDY; }
-        else if (id == G_I) { dxid = G_DIDX; dyid = G_DIDY; }
-        else if (id == G_U) { dxid = G_DUDX; dyid = G_DUDY; }
-        else if (id == G_V) { dxid = G_DVDX; dyid = G_DVDY; }
-        else if (id == G_PS) { dxid = G_DPSDX; dyid = G_DPSDY; }
-        for (int c = 0; c < nc; ++c) {
-            stf(L, r, nc + c, dxid >= 0 ? fld(gfield(G, dxid), c, L.pt) : 0.0f);
-            stf(L, r, 2 * nc + c, dyid >= 0 ? fld(gfield(G, dyid), c, L.pt) : 0.0f);
-        }
-    }
-}
-
-__device__ void h_load_userdata(const Lane& L, const uint32_t* a, char* base) {
-    uint32_t r = a[0];
-    int nc = anc(r);
-    const char* p = base + (int64_t)a[1] + L.pt * (int64_t)(int32_t)a[2];
-    int nd = ader(r) ? 3 : 1;
-    const uint32_t* q = reinterpret_cast<const uint32_t*>(p);
-    for (int i = 0; i < nc * nd; ++i) stw(L, r, i, q[i]);
-}
-
-__device__ void h_store_output(const Lane& L, const uint32_t* a, char* base) {
-    uint32_t s = a[0];
-    int nc = anc(s);
-    uint32_t flags = a[3];
-    int elems = (int)a[4];
-    if (elems < 1) elems = 1;
-    char* p = base + (int64_t)a[1] + L.pt * (int64_t)(int32_t)a[2];
-    int total = nc * elems;
-    int nd = (flags & 1u) ? 3 : 1;
-    for (int d = 0; d < nd; ++d)
-        for (int i = 0; i < total; ++i) {
-            uint32_t w;
-            if (d > 0 && !ader(s)) w = 0u;
-            else if (flags & 2u) w = (uint32_t)ldi(L, s, i);
-            else w = ldw(L, s, d * total + i);
-            if (!(flags & 2u) && atc(s) == TC_INT) w = __float_as_uint((float)(int)w);
-            reinterpret_cast<uint32_t*>(p)[d * total + i] = w;
-        }
-}
-
-__device__ void h_compref(const Lane& L, const uint32_t* a, uint32_t* st) {
-    int i = ldi(L, a[2], 0);
-    if (i < 0 || i > 2) { raise_status(st, ST_ARRAY_BOUNDS); i = i < 0 ? 0 : 2; }
-    std2(L, a[0], 0, ader(a[1]) ? ldd(L, a[1], i) : d2c(ldf(L, a[1], i, 0)));
-}
-__device__ void h_compassign(const Lane& L, const uint32_t* a, uint32_t* st) {
-    int i = ldi(L, a[1], 0);
-    if (i < 0 || i > 2) { raise_status(st, ST_ARRAY_BOUNDS); i = i < 0 ? 0 : 2; }
-    std2(L, a[0], i, ldd(L, a[2], 0));
-}
-__device__ void h_construct3(const Lane& L, const uint32_t* a) {
-    for (int c = 0; c < 3; ++c) std2(L, a[0], c, ldd(L, a[1 + c], 0));
-}
-__device__ void h_aref(const Lane& L, const uint32_t* a, uint32_t* st) {
-    uint32_t r = a[0], arr = a[1];
-    int alen = (int)a[3];
-    int i = ldi(L, a[2], 0);
-    if (i < 0 || i >= alen) { raise_status(st, ST_ARRAY_BOUNDS); i = i < 0 ? 0 : alen - 1; }
-    int nc = anc(arr);
-    for (int c = 0; c < nc; ++c) {
-        uint32_t w = ldw(L, arr, i * nc + c);
-        if (atc(r) == TC_INT || atc(r) == TC_STRING || atc(r) == TC_CLOSURE) { stw(L, r, c, w); continue; }
-        float v = atc(arr) == TC_INT ? (float)(int)w : __uint_as_float(w);
-        stf(L, r, c, v);
-        if (ader(r)) {
-            float dx = 0.0f, dy = 0.0f;
-            if (ader(arr)) {
-                dx = __uint_as_float(ldw(L, arr, alen * nc + i * nc + c));
-                dy = __uint_as_float(ldw(L, arr, 2 * alen * nc + i * nc + c));
-            }
-            stf(L, r, nc + c, dx);
-            stf(L, r, 2 * nc + c, dy);
-        }
-    }
-}
-__device__ void h_aassign(const Lane& L, const uint32_t* a, uint32_t* st) {
-    uint32_t arr = a[0], v = a[2];
-    int alen = (int)a[3];
-    int i = ldi(L, a[1], 0);
-    if (i < 0 || i >= alen) { raise_status(st, ST_ARRAY_BOUNDS); i = i < 0 ? 0 : alen - 1; }
-    int nc = anc(arr);
-    for (int c = 0; c < nc; ++c) {
-        int vc = anc(v) == 1 ? 0 : c;
-        if (atc(arr) == TC_INT || atc(arr) == TC_STRING || atc(arr) == TC_CLOSURE) {
-            stw(L, arr, i * nc + c, atc(arr) == TC_INT ? (uint32_t)ldi(L, v, vc) : ldw(L, v, vc));
-            continue;
-        }
-        stf(L, arr, i * nc + c, ldf(L, v, vc, 0));
-        if (ader(arr)) {
-            stf(L, arr, alen * nc + i * nc + c, ldf(L, v, vc, 1));
-            stf(L, arr, 2 * alen * nc + i * nc + c, ldf(L, v, vc, 2));
-        }
-    }
-}
-
-// ---- closures (reference closure tree, node pool in the heap) -------------------------
-struct ClosurePools {
-    uint32_t base, max_nodes;
-};
-__device__ __forceinline__ float hget(const Lane& L, uint32_t slot) { return L.heap[(size_t)slot * L.hs + L.li]; }
-__device__ __forceinline__ void hset(const Lane& L, uint32_t slot, float v) { L.heap[(size_t)slot * L.hs + L.li] = v; }
-__device__ __forceinline__ uint32_t hgetu(const Lane& L, uint32_t slot) { return __float_as_uint(hget(L, slot)); }
-__device__ __forceinline__ void hsetu(const Lane& L, uint32_t slot, uint32_t v) { hset(L, slot, __uint_as_float(v)); }
-__device__ __forceinline__ uint32_t node_slot(const ClosurePools& P, uint32_t node) {
-    return P.base + 1 + node * kNodeFloats;
-}
-// returns node index + 1, or 0 when the pool is full
-__device__ __forceinline__ uint32_t cl_alloc(const Lane& L, const ClosurePools& P, uint32_t* st) {
-    uint32_t n = hgetu(L, P.base);
-    if (n >= P.max_nodes) { raise_status(st, ST_CLOSURE_OVERFLOW); return 0u; }
-    hsetu(L, P.base, n + 1);
-    return n + 1;
-}
-
-// osl_allocate_(weighted_)closure_component (opclosure.cpp:83-117)
-__device__ void h_closure(const Lane& L, const uint32_t* a, const uint32_t* extra, const ClosurePools& P,
-                          uint32_t* st) {
-    float w[3] = { 1.0f, 1.0f, 1.0f };
-    if (a[2] != kNoArg) {
-        for (int c = 0; c < 3; ++c) w[c] = ldf(L, a[2], c, 0);
-        if (w[0] == 0.0f && w[1] == 0.0f && w[2] == 0.0f) { stw(L, a[0], 0, 0u); return; }
-    }
-    uint32_t h = cl_alloc(L, P, st);
-    if (!h) { stw(L, a[0], 0, 0u); return; }
-    uint32_t ns = node_slot(P, h - 1);
-    hsetu(L, ns, a[1]);
-    for (int c = 0; c < 3; ++c) hset(L, ns + 1 + c, w[c]);
-    uint32_t params[11];
-    int np = 0;
-    for (int i = 3; i < 7; ++i) params[np++] = a[i];
-    if (extra)
-        for (int i = 0; i < 7; ++i) params[np++] = extra[i];
-    int k = 0;
-    for (int i = 0; i < np && k < kClosureParamFloats; ++i) {
-        uint32_t p = params[i];
-        if (p == kNoArg) break;
-        int nc = anc(p);
-        uint32_t t = atc(p);
-        for (int c = 0; c < nc && k < kClosureParamFloats; ++c)
-            hsetu(L, ns + 4 + k++, (t == TC_INT || t == TC_STRING) ? ldw(L, p, c) : __float_as_uint(ldf(L, p, c, 0)));
-    }
-    for (; k < kClosureParamFloats; ++k) hset(L, ns + 4 + k, 0.0f);
-    stw(L, a[0], 0, h);
-}
-
-// osl_mul_closure_color / osl_mul_closure_float (opclosure.cpp:35-80)
-__device__ void h_closure_mul(const Lane& L, const uint32_t* a, const ClosurePools& P, uint32_t* st) {
-    uint32_t c = ldw(L, a[1], 0);
-    float w[3] = { ldf(L, a[2], 0, 0), ldf(L, a[2], 1, 0), ldf(L, a[2], 2, 0) };
-    if (c == 0u || (w[0] == 0.0f && w[1] == 0.0f && w[2] == 0.0f)) { stw(L, a[0], 0, 0u); return; }
-    if (w[0] == 1.0f && w[1] == 1.0f && w[2] == 1.0f) { stw(L, a[0], 0, c); return; }
-    uint32_t h = cl_alloc(L, P, st);
-    if (!h) { stw(L, a[0], 0, 0u); return; }
-    uint32_t ns = node_slot(P, h - 1);
-    hsetu(L, ns, (uint32_t)kClosureMul);
-    for (int k = 0; k < 3; ++k) hset(L, ns + 1 + k, w[k]);
-    hsetu(L, ns + 4, c);
-    stw(L, a[0], 0, h);
-}
-
-// osl_add_closure_closure (opclosure.cpp:15-33)
-__device__ void h_closure_add(const Lane& L, const uint32_t* a, const ClosurePools& P, uint32_t* st) {
-    uint32_t x = ldw(L, a[1], 0), y = ldw(L, a[2], 0);
-    if (x == 0u) { stw(L, a[0], 0, y); return; }
-    if (y == 0u) { stw(L, a[0], 0, x); return; }
-    uint32_t h = cl_alloc(L, P, st);
-    if (!h) { stw(L, a[0], 0, 0u); return; }
-    uint32_t ns = node_slot(P, h - 1);
-    hsetu(L, ns, (uint32_t)kClosureAdd);
-    hsetu(L, ns + 4, x);
-    hsetu(L, ns + 5, y);
-    stw(L, a[0], 0, h);
-}
-
-// testrender's non-recursive walk (shading.cpp:1450-1500): visits the
-// components in order with the accumulated weight weight*comp.w.
-template <class F>
-__device__ void closure_walk(const Lane& L, const ClosurePools& P, uint32_t root, uint32_t* st, F&& visit) {
-    uint32_t stack_node[kClosureWalkStack];
-    float stack_w[kClosureWalkStack][3];
-    int sp = 0;
-    float w[3] = { 1.0f, 1.0f, 1.0f };
-    uint32_t cur = root;
-    int guard = 0;
-    while (cur != 0u && cur <= P.max_nodes) {
-        if (++guard > 4 * (int)P.max_nodes + 8) break;
-        uint32_t ns = node_slot(P, cur - 1);
-        int id = (int)hgetu(L, ns);
-        if (id == kClosureMul) {
-            for (int k = 0; k < 3; ++k) w[k] = w[k] * hget(L, ns + 1 + k);
-            cur = hgetu(L, ns + 4);
-        } else if (id == kClosureAdd) {
-            if (sp < kClosureWalkStack) {
-                stack_node[sp] = hgetu(L, ns + 5);
-                for (int k = 0; k < 3; ++k) stack_w[sp][k] = w[k];
-                ++sp;
-            } else {
-                raise_status(st, ST_CLOSURE_OVERFLOW);
-            }
-            cur = hgetu(L, ns + 4);
-        } else {
-            float cw[3];
-            for (int k = 0; k < 3; ++k) cw[k] = w[k] * hget(L, ns + 1 + k);
-            visit(id, cw, ns + 4);
-            cur = 0u;
-        }
-        if (cur == 0u && sp > 0) {
-            --sp;
-            cur = stack_node[sp];
-            for (int k = 0; k < 3; ++k) w[k] = stack_w[sp][k];
-        }
-    }
-}
-
-// Output record per point: [count][per component: id, w.rgb, params x12]
-__device__ void h_store_closure(const Lane& L, const uint32_t* a, char* base, const ClosurePools& P, uint32_t* st) {
-    uint32_t root = ldw(L, a[0], 0), maxc = a[3];
-    uint32_t* o = reinterpret_cast<uint32_t*>(base + (int64_t)a[1] + L.pt * (int64_t)(int32_t)a[2]);
-    uint32_t n = 0;
-    closure_walk(L, P, root, st, [&](int id, const float* cw, uint32_t params) {
-        if (n >= maxc) return;
-        uint32_t* q = o + 1 + n * kNodeFloats;
-        q[0] = (uint32_t)id;
-        for (int k = 0; k < 3; ++k) q[1 + k] = __float_as_uint(cw[k]);
-        for (int k = 0; k < kClosureParamFloats; ++k) q[4 + k] = hgetu(L, params + k);
-        ++n;
-    });
-    o[0] = n;
-}
-
-// CompositeBSDF::prepare + eval (shading.h:322-374) over the lobes the walk
-// finds: diffuse, and microfacet "ggx" reflection; other ids add nothing.
-__device__ void h_bsdf_eval(const Lane& L, const uint32_t* a, char* base, const ClosurePools& P, uint32_t* st) {
-    uint32_t root = ldw(L, a[0], 0);
-    const V3 wi = v3(ldf(L, a[3], 0, 0), ldf(L, a[3], 1, 0), ldf(L, a[3], 2, 0));
-    const V3 wo = v3(-ldf(L, a[4], 0, 0), -ldf(L, a[4], 1, 0), -ldf(L, a[4], 2, 0));
-    const uint32_t ggx = a[5];
-    int nl = 0;
-    int kind[kBsdfMaxLobes];
-    float lw[kBsdfMaxLobes][3];
-    uint32_t lp[kBsdfMaxLobes];
-    closure_walk(L, P, root, st, [&](int id, const float* cw, uint32_t params) {
-        int k = -1;
-        if (id == 3) k = 0;  // DIFFUSE_ID
-        else if (id == 8 && hgetu(L, params + 0) == ggx && (int)hgetu(L, params + 10) == 0) k = 1;  // MICROFACET_ID
-        if (k < 0 || nl >= kBsdfMaxLobes) return;
-        kind[nl] = k;
-        for (int c = 0; c < 3; ++c) lw[nl][c] = cw[c];
-        lp[nl] = params;
-        ++nl;
-    });
-    // prepare(wo, path_weight = 1, absorb = false)
-    float pdfs[kBsdfMaxLobes];
-    float total = 0.0f;
-    for (int i = 0; i < nl; ++i) {
-        float alb = 1.0f;
-        if (kind[i] == 1) {
-            V3 N = v3(hget(L, lp[i] + 1), hget(L, lp[i] + 2), hget(L, lp[i] + 3));
-            alb = fresnel_dielectric(vdot(N, wo), hget(L, lp[i] + 9));
-        }
-        pdfs[i] = (lw[i][0] * (1.0f * alb) + lw[i][1] * (1.0f * alb) + lw[i][2] * (1.0f * alb)) / (1.0f + 1.0f + 1.0f);
-        total += pdfs[i];
-    }
-    if (total > 0.0f || total > 1.0f)
-        for (int i = 0; i < nl; ++i) pdfs[i] /= total;
-    float sw[3] = { 0.0f, 0.0f, 0.0f }, spdf = 0.0f, srough = 0.0f;
-    for (int i = 0; i < nl; ++i) {
-        BsdfSample b;
-        if (kind[i] == 0) {
-            b = diffuse_eval(v3(hget(L, lp[i] + 0), hget(L, lp[i] + 1), hget(L, lp[i] + 2)), wi);
-        } else {
-            V3 N = v3(hget(L, lp[i] + 1), hget(L, lp[i] + 2), hget(L, lp[i] + 3));
-            V3 U = v3(hget(L, lp[i] + 4), hget(L, lp[i] + 5), hget(L, lp[i] + 6));
-            Frame tf = frame_from_normal_and_tangent(N, U);
-            b = microfacet_ggx_refl_eval(tf, hget(L, lp[i] + 7), hget(L, lp[i] + 8), hget(L, lp[i] + 9), wo, wi);
-        }
-        for (int c = 0; c < 3; ++c) b.w[c] *= lw[i][c];
-        mis_update_eval(sw, &spdf, b.w, b.pdf, pdfs[i]);
-        srough += b.roughness * pdfs[i];
-    }
-    float* o = reinterpret_cast<float*>(base + (int64_t)a[1] + L.pt * (int64_t)(int32_t)a[2]);
-    o[0] = sw[0]; o[1] = sw[1]; o[2] = sw[2]; o[3] = spdf;
-}
-
-// ---- spline (splineimpl.h:191-239) -----------------------------------------------------
-__device__ void h_spline(const Lane& L, const uint32_t* a) {
-    uint32_t r = a[0], xa = a[1], kn = a[2];
-    const SplineBasisDev& B = c_spline_basis[a[3] < 6u ? a[3] : 0u];
-    int alen = (int)a[5];
-    int knot_count = a[4] != kNoArg ? ldi(L, a[4], 0) : alen;
-    if (knot_count > alen) knot_count = alen;
-    int nc = anc(r);
-    int kc = anc(kn);
-    bool xd = ader(xa), kd = ader(kn), rd = ader(r);
-    D2 x = ldd(L, xa, 0);
-    if (!(0.0f <= x.v)) x = d2c(0.0f);
-    if (x.v > 1.0f) x = d2c(1.0f);
-    int nsegs = ((knot_count - 4) / B.step) + 1;
-    x = x * (float)nsegs;
-    int segnum = (int)x.v;
-    if (segnum < 0) segnum = 0;
-    if (segnum > nsegs - 1) segnum = nsegs - 1;
-    if (a[3] == 5u) {  // constant basis
-        for (int c = 0; c < nc; ++c) stval(L, r, c, __uint_as_float(ldw(L, kn, (segnum + 1) * kc + (kc == 1 ? 0 : c))));
-        return;
-    }
-    x = x - (float)segnum;
-    int s = segnum * B.step;
-    for (int c = 0; c < nc; ++c) {
-        int cc = kc == 1 ? 0 : c;
-        D2 P[4];
-        for (int k = 0; k < 4; ++k) {
-            float v = __uint_as_float(ldw(L, kn, (s + k) * kc + cc));
-            float dx = kd ? __uint_as_float(ldw(L, kn, alen * kc + (s + k) * kc + cc)) : 0.0f;
-            float dy = kd ? __uint_as_float(ldw(L, kn, 2 * alen * kc + (s + k) * kc + cc)) : 0.0f;
-            P[k] = d2(v, dx, dy);
-        }
-        D2 tk[4];
-        for (int k = 0; k < 4; ++k) {
-            // basis[k][j] * P[j], summed left to right (float * CTYPE)
-            D2 t0 = P[0] * B.m[k][0], t1 = P[1] * B.m[k][1], t2 = P[2] * B.m[k][2], t3 = P[3] * B.m[k][3];
-            tk[k] = ((t0 + t1) + t2) + t3;
-        }
-        D2 res;
-        if (!xd && !kd) {
-            float xv = x.v;
-            float t = tk[0].v * xv + tk[1].v;
-            t = t * xv + tk[2].v;
-            t = t * xv + tk[3].v;
-            res = d2c(t);
-        } else if (!kd) {
-            // CTYPE without partials times a Dual2 x: tk*x scales every element
-            D2 t = x * tk[0].v;
-            t = t + tk[1].v;
-            t = t * x;
-            t = t + tk[2].v;
-            t = t * x;
-            t = t + tk[3].v;
-            res = t;
-        } else {
-            D2 t = tk[0] * x + tk[1];
-            t = t * x + tk[2];
-            t = t * x + tk[3];
-            res = t;
-        }
-        if (!rd) stval(L, r, c, res.v);
-        else std2(L, r, c, res);
-    }
-}
-
-// ---- the interpreter -----------------------------------------------------------------
-__device__ __forceinline__ bool bit(uint32_t m, int d) { return (m >> d) & 1u; }
-__device__ __forceinline__ uint32_t setbit(uint32_t m, int d, bool v) { return v ? (m | (1u << d)) : (m & ~(1u << d)); }
-
-static const long long kMaxBackEdges = 1ll << 24;
-
-template <bool SMEM>
-__global__ void __launch_bounds__(256) interp_kernel(KArgs k) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    const ProgramHeader* H = reinterpret_cast<const ProgramHeader*>(k.blob);
-    const int nops = (int)H->nops, nconst = (int)H->nconst, slots = (int)H->heap_slots;
-    Op* sops = reinterpret_cast<Op*>(smem);
-    uint32_t* spool = reinterpret_cast<uint32_t*>(smem + (size_t)nops * sizeof(Op));
-    float* sheap = reinterpret_cast<float*>(spool + ((nconst + 3) & ~3));
-    {
-        const uint4* gops = reinterpret_cast<const uint4*>(k.blob + sizeof(ProgramHeader));
-        uint4* so = reinterpret_cast<uint4*>(sops);
-        for (int i = threadIdx.x; i < nops * 2; i += blockDim.x) so[i] = gops[i];
-        const uint32_t* gpool = reinterpret_cast<const uint32_t*>(k.blob + sizeof(ProgramHeader) + (size_t)nops * sizeof(Op));
-        for (int i = threadIdx.x; i < nconst; i += blockDim.x) spool[i] = gpool[i];
-    }
-    __syncthreads();
-    ClosurePools CP;
-    CP.base = H->closure_base;
-    CP.max_nodes = H->max_comps;
-    const bool uses_closures = (H->flags & 1u) != 0;
-
-    Lane L;
-    L.pool = spool;
-    L.hs = blockDim.x;
-    L.li = threadIdx.x;
-    L.heap = SMEM ? sheap : (k.gheap + (size_t)blockIdx.x * (size_t)slots * blockDim.x);
-
-    const int64_t ntiles = (k.npoints + blockDim.x - 1) / blockDim.x;
-    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        L.pt = tile * blockDim.x + threadIdx.x;
-        const bool valid = L.pt < k.npoints;
-        bool act = valid, ext = false, lret = false;
-        uint32_t stk = 0, cnd = 0, brk = 0, cnt = 0;
-        long long backedges = 0;
-        if (uses_closures && valid) hsetu(L, CP.base, 0u);
-        int pc = 0;
-        while (pc < nops) {
-            const uint4* ow = reinterpret_cast<const uint4*>(sops + pc);
-            const uint4 w0 = ow[0], w1 = ow[1];
-            const uint32_t code = w0.x & 0xFFFFu;
-            const uint32_t a[7] = { w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w };
-            switch (code) {
-            case OP_NOP: break;
-            case OP_IF: {
-                int d = (int)a[1];
-                bool c = act && truth(L, a[0]);
-                stk = setbit(stk, d, act);
-                cnd = setbit(cnd, d, c);
-                act = c;
-                if (!__any_sync(FULL, act)) { pc = (int)a[2]; continue; }
-                break;
-            }
-            case OP_ELSE: {
-                int d = (int)a[1];
-                int ll = (int)a[3];
-                bool off = ext || lret || (ll && (bit(brk, ll - 1) || bit(cnt, ll - 1)));
-                act = bit(stk, d) && !bit(cnd, d) && !off;
-                if (!__any_sync(FULL, act)) { pc = (int)a[2]; continue; }
-                break;
-            }
-            case OP_ENDIF: {
-                int d = (int)a[1];
-                int ll = (int)a[3];
-                bool off = ext || lret || (ll && (bit(brk, ll - 1) || bit(cnt, ll - 1)));
-                act = bit(stk, d) && !off;
-                break;
-            }
-            case OP_LOOP_BEGIN: {
-                int d = (int)a[1];
-                int ll = (int)a[3];
-                stk = setbit(stk, d, act);
-                brk = setbit(brk, ll - 1, false);
-                cnt = setbit(cnt, ll - 1, false);
-                break;
-            }
-            case OP_LOOP_TEST: {
-                act = act && truth(L, a[0]);
-                if (!__any_sync(FULL, act)) { pc = (int)a[2]; continue; }
-                break;
-            }
-            case OP_LOOP_STEP: {
-                int ll = (int)a[3];
-                act = (act || bit(cnt, ll - 1)) && !bit(brk, ll - 1) && !ext && !lret;
-                cnt = setbit(cnt, ll - 1, false);
-                break;
-            }
-            case OP_JUMP: {
-                if (++backedges > kMaxBackEdges) {
-                    if (threadIdx.x % 32 == 0) raise_status(k.status, ST_TIMEOUT);
-                    pc = nops;
-                    continue;
-                }
-                pc = (int)a[2];
-                continue;
-            }
-            case OP_LOOP_END: {
-                int d = (int)a[1];
-                int ll = (int)a[3];
-                brk = setbit(brk, ll - 1, false);
-                cnt = setbit(cnt, ll - 1, false);
-                // lanes that broke out of an enclosing loop stay off via the
-                // enclosing ENDIF/LOOP_STEP recomputation
-                act = bit(stk, d) && !ext && !lret;
-                break;
-            }
-            case OP_BREAK: {
-                int ll = (int)a[3];
-                if (act && ll) brk = setbit(brk, ll - 1, true);
-                act = false;
-                break;
-            }
-            case OP_CONTINUE: {
-                int ll = (int)a[3];
-                if (act && ll) cnt = setbit(cnt, ll - 1, true);
-                act = false;
-                break;
-            }
-            case OP_RETURN: if (act) lret = true; act = false; break;
-            case OP_EXIT: if (act) ext = true; act = false; break;
-            case OP_LAYER_END: lret = false; act = valid && !ext; break;
-            default:
-                if (act) {
-                    switch (code) {
-                    case OP_LOAD_GLOBAL: h_load_global(L, a, k.G); break;
-                    case OP_LOAD_USERDATA: h_load_userdata(L, a, k.userdata); break;
-                    case OP_STORE_OUTPUT: h_store_output(L, a, k.outputs); break;
-                    case OP_ASSIGN: h_assign_fast(L, a, k.status); break;
-                    case OP_COMPREF: h_compref(L, a, k.status); break;
-                    case OP_COMPASSIGN: h_compassign(L, a, k.status); break;
-                    case OP_MXCOMPREF: {
-                        int r = ldi(L, a[2], 0), c = ldi(L, a[3], 0);
-                        r = r < 0 ? 0 : (r > 3 ? 3 : r); c = c < 0 ? 0 : (c > 3 ? 3 : c);
-                        stval(L, a[0], 0, __uint_as_float(ldw(L, a[1], r * 4 + c)));
-                        break;
-                    }
-                    case OP_MXCOMPASSIGN: {
-                        int r = ldi(L, a[1], 0), c = ldi(L, a[2], 0);
-                        r = r < 0 ? 0 : (r > 3 ? 3 : r); c = c < 0 ? 0 : (c > 3 ? 3 : c);
-                        stf(L, a[0], r * 4 + c, ldf(L, a[3], 0, 0));
-                        break;
-                    }
-                    case OP_CONSTRUCT3: h_construct3(L, a); break;
-                    case OP_AREF: h_aref(L, a, k.status); break;
-                    case OP_AASSIGN: h_aassign(L, a, k.status); break;
-                    case OP_MATRIX_DIAG: {
-                        float v = ldf(L, a[1], 0, 0);
-                        for (int i = 0; i < 16; ++i) stf(L, a[0], i, (i % 5 == 0) ? v : 0.0f);
-                        break;
-                    }
-                    case OP_ADD: h_arith_fast<0>(L, a); break;
-                    case OP_SUB: h_arith_fast<1>(L, a); break;
-                    case OP_MUL: h_arith_fast<2>(L, a); break;
-                    case OP_DIV: h_arith_fast<3>(L, a); break;
-                    case OP_MOD: h_arith<4>(L, a); break;
-                    case OP_NEG: h_unary<OP_NEG>(L, a); break;
-                    case OP_IADD: h_iarith<0>(L, a); break;
-                    case OP_ISUB: h_iarith<1>(L, a); break;
-                    case OP_IMUL: h_iarith<2>(L, a); break;
-                    case OP_IDIV: h_iarith<3>(L, a); break;
-                    case OP_IMOD: h_iarith<4>(L, a); break;
-                    case OP_INEG: stw(L, a[0], 0, (uint32_t)(-ldi(L, a[1], 0))); break;
-                    case OP_MMUL: h_mmul(L, a); break;
-                    case OP_EQ: h_cmp<0>(L, a); break;
-                    case OP_NEQ: h_cmp<1>(L, a); break;
-                    case OP_LT: h_cmp<2>(L, a); break;
-                    case OP_GT: h_cmp<3>(L, a); break;
-                    case OP_LE: h_cmp<4>(L, a); break;
-                    case OP_GE: h_cmp<5>(L, a); break;
-                    case OP_AND: stw(L, a[0], 0, (truth(L, a[1]) && truth(L, a[2])) ? 1u : 0u); break;
-                    case OP_OR: stw(L, a[0], 0, (truth(L, a[1]) || truth(L, a[2])) ? 1u : 0u); break;
-                    case OP_BITAND: stw(L, a[0], 0, (uint32_t)(ldi(L, a[1], 0) & ldi(L, a[2], 0))); break;
-                    case OP_BITOR: stw(L, a[0], 0, (uint32_t)(ldi(L, a[1], 0) | ldi(L, a[2], 0))); break;
-                    case OP_XOR: stw(L, a[0], 0, (uint32_t)(ldi(L, a[1], 0) ^ ldi(L, a[2], 0))); break;
-                    case OP_SHL: stw(L, a[0], 0, (uint32_t)ldi(L, a[1], 0) << (ldi(L, a[2], 0) & 31)); break;
-                    case OP_SHR: stw(L, a[0], 0, (uint32_t)(ldi(L, a[1], 0) >> (ldi(L, a[2], 0) & 31))); break;
-                    case OP_COMPL: stw(L, a[0], 0, ~(uint32_t)ldi(L, a[1], 0)); break;
-                    case OP_ABS: h_unary<OP_ABS>(L, a); break;
-                    case OP_IABS: { int v = ldi(L, a[1], 0); stw(L, a[0], 0, (uint32_t)(v < 0 ? -v : v)); break; }
-                    case OP_FLOOR: h_unary<OP_FLOOR>(L, a); break;
-                    case OP_CEIL: h_unary<OP_CEIL>(L, a); break;
-                    case OP_ROUND: h_unary<OP_ROUND>(L, a); break;
-                    case OP_TRUNC: h_unary<OP_TRUNC>(L, a); break;
-                    case OP_SIGN: h_unary<OP_SIGN>(L, a); break;
-                    case OP_SQRT: h_unary<OP_SQRT>(L, a); break;
-                    case OP_INVSQRT: h_unary<OP_INVSQRT>(L, a); break;
-                    case OP_CBRT: h_unary<OP_CBRT>(L, a); break;
-                    case OP_SIN: h_unary<OP_SIN>(L, a); break;
-                    case OP_COS: h_unary<OP_COS>(L, a); break;
-                    case OP_TAN: h_unary<OP_TAN>(L, a); break;
-                    case OP_ASIN: h_unary<OP_ASIN>(L, a); break;
-                    case OP_ACOS: h_unary<OP_ACOS>(L, a); break;
-                    case OP_ATAN: h_unary<OP_ATAN>(L, a); break;
-                    case OP_SINH: h_unary<OP_SINH>(L, a); break;
-                    case OP_COSH: h_unary<OP_COSH>(L, a); break;
-                    case OP_TANH: h_unary<OP_TANH>(L, a); break;
-                    case OP_EXP: h_unary<OP_EXP>(L, a); break;
-                    case OP_EXP2: h_unary<OP_EXP2>(L, a); break;
-                    case OP_EXPM1: h_unary<OP_EXPM1>(L, a); break;
-                    case OP_LOG: h_unary<OP_LOG>(L, a); break;
-                    case OP_LOG2: h_unary<OP_LOG2>(L, a); break;
-                    case OP_LOG10: h_unary<OP_LOG10>(L, a); break;
-                    case OP_RADIANS: h_unary<OP_RADIANS>(L, a); break;
-                    case OP_DEGREES: h_unary<OP_DEGREES>(L, a); break;
-                    case OP_ISNAN: stw(L, a[0], 0, isnan(ldf(L, a[1], 0, 0)) ? 1u : 0u); break;
-                    case OP_ISINF: stw(L, a[0], 0, isinf(ldf(L, a[1], 0, 0)) ? 1u : 0u); break;
-                    case OP_ISFINITE: stw(L, a[0], 0, isfinite(ldf(L, a[1], 0, 0)) ? 1u : 0u); break;
-                    case OP_POW: h_binary<OP_POW>(L, a); break;
-                    case OP_ATAN2: h_binary<OP_ATAN2>(L, a); break;
-                    case OP_FMOD: h_binary<OP_FMOD>(L, a); break;
-                    case OP_MIN: h_binary<OP_MIN>(L, a); break;
-                    case OP_MAX: h_binary<OP_MAX>(L, a); break;
-                    case OP_STEP: h_binary<OP_STEP>(L, a); break;
-                    case OP_IMIN: { int x = ldi(L, a[1], 0), y = ldi(L, a[2], 0); stw(L, a[0], 0, (uint32_t)(x <= y ? x : y)); break; }
-                    case OP_IMAX: { int x = ldi(L, a[1], 0), y = ldi(L, a[2], 0); stw(L, a[0], 0, (uint32_t)(x > y ? x : y)); break; }
-                    case OP_CLAMP: h_clamp(L, a); break;
-                    case OP_MIX: h_mix(L, a); break;
-                    case OP_SMOOTHSTEP: h_smoothstep(L, a); break;
-                    case OP_SELECT: h_select(L, a); break;
-                    case OP_DOT: h_dot(L, a); break;
-                    case OP_CROSS: h_cross(L, a); break;
-                    case OP_LENGTH: h_length(L, a, false); break;
-                    case OP_DISTANCE: h_length(L, a, true); break;
-                    case OP_NORMALIZE: h_normalize(L, a); break;
-                    case OP_DX:
-                    case OP_DY: {
-                        int d = code == OP_DX ? 1 : 2;
-                        int nc = anc(a[0]);
-                        for (int c = 0; c < nc; ++c) stval(L, a[0], c, ldf(L, a[1], c, d));
-                        break;
-                    }
-                    case OP_TRANSFORM: h_transform(L, a); break;
-                    case OP_NOISE: h_noise(L, a); break;
-                    case OP_HASH: h_hash(L, a); break;
-                    case OP_CLOSURE: {
-                        const uint32_t* extra = nullptr;
-                        uint32_t ex[7];
-                        if (pc + 1 < nops && sops[pc + 1].code == OP_NOP && sops[pc + 1].nargs == 7) {
-                            for (int i = 0; i < 7; ++i) ex[i] = sops[pc + 1].a[i];
-                            extra = ex;
-                        }
-                        h_closure(L, a, extra, CP, k.status);
-                        break;
-                    }
-                    case OP_CLOSURE_MUL: h_closure_mul(L, a, CP, k.status); break;
-                    case OP_CLOSURE_ADD: h_closure_add(L, a, CP, k.status); break;
-                    case OP_STORE_CLOSURE: h_store_closure(L, a, k.outputs, CP, k.status); break;
-                    case OP_BSDF_EVAL: h_bsdf_eval(L, a, k.outputs, CP, k.status); break;
-                    case OP_SPLINE: h_spline(L, a); break;
-                    default: raise_status(k.status, ST_BAD_OPCODE); break;
-                    }
-                }
-                break;
-            }
-            ++pc;
-        }
-    }
-}
-
-}  // namespace dev
-
-// ---- host side ---------------------------------------------------------------------------
 namespace {
 bool cuda_ok(cudaError_t e, std::string* err, const char* what) {
     if (e == cudaSuccess) return true;
@@ -1515,19 +42,6 @@ bool cuda_ok(cudaError_t e, std::string* err, const char* what) {
     return false;
 }
 
-// 4D simplex traversal table (simplexnoise.cpp:108-126): entry c ranks each
-// axis 0..3 by magnitude; impossible comparison patterns stay {0,0,0,0}.
-void build_simplex4(unsigned char t[64][4]) {
-    std::memset(t, 0, 64 * 4);
-    int perm[4] = { 0, 1, 2, 3 };
-    do {
-        int r[4];
-        for (int a = 0; a < 4; ++a) r[a] = perm[a];
-        int c = (r[0] > r[1] ? 32 : 0) | (r[0] > r[2] ? 16 : 0) | (r[1] > r[2] ? 8 : 0) | (r[0] > r[3] ? 4 : 0)
-              | (r[1] > r[3] ? 2 : 0) | (r[2] > r[3] ? 1 : 0);
-        for (int a = 0; a < 4; ++a) t[c][a] = (unsigned char)r[a];
-    } while (std::next_permutation(perm, perm + 4));
-}
 }  // namespace
 
 int device_init(DeviceState& ds, std::string* err) {
@@ -1542,12 +56,8 @@ int device_init(DeviceState& ds, std::string* err) {
     ds.smem_optin = (size_t)optin;
     if (!cuda_ok(cudaMalloc(&ds.d_status, sizeof(uint32_t)), err, "cudaMalloc status")) return OSLG_ERR_CUDA;
     if (!cuda_ok(cudaMemset(ds.d_status, 0, sizeof(uint32_t)), err, "cudaMemset status")) return OSLG_ERR_CUDA;
-    unsigned char t[64][4];
-    build_simplex4(t);
-    if (!cuda_ok(cudaMemcpyToSymbol(dev::c_simplex4, t, sizeof(t)), err, "simplex table")) return OSLG_ERR_CUDA;
     // the kernels may use up to the opt-in shared memory size
-    cudaFuncSetAttribute(dev::interp_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-    cudaFuncSetAttribute(dev::interp_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    for (int t = 0; t < kNumTiers; ++t) tier_fns(t).set_smem_limit(optin);
     return OSLG_OK;
 }
 
@@ -1601,11 +111,9 @@ int device_execute(DeviceState& ds, const ProgramHeader& hdr, const void* d_blob
         if (err) *err = "program does not fit in shared memory";
         return OSLG_ERR_LOWER;
     }
+    const TierFns& fns = tier_fns((int)((hdr.flags >> 8) & 7u));
     int per_sm = 0;
-    cudaError_t e;
-    if (smem) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::interp_kernel<true>, block, shmem);
-    else e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::interp_kernel<false>, block, shmem);
-    if (!cuda_ok(e, err, "occupancy")) return OSLG_ERR_CUDA;
+    if (!cuda_ok((cudaError_t)fns.occupancy(smem, block, shmem, &per_sm), err, "occupancy")) return OSLG_ERR_CUDA;
     if (per_sm < 1) per_sm = 1;
     int64_t tiles = (npoints + block - 1) / block;
     int64_t grid = (int64_t)ds.sm_count * per_sm;
@@ -1630,10 +138,8 @@ int device_execute(DeviceState& ds, const ProgramHeader& hdr, const void* d_blob
         }
         k.gheap = ds.gheap;
     }
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if (smem) dev::interp_kernel<true><<<(unsigned)grid, block, shmem, s>>>(k);
-    else dev::interp_kernel<false><<<(unsigned)grid, block, shmem, s>>>(k);
-    if (!cuda_ok(cudaGetLastError(), err, "launch")) return OSLG_ERR_CUDA;
+    if (!cuda_ok((cudaError_t)fns.launch(smem, (unsigned)grid, (unsigned)block, shmem, stream, k), err, "launch"))
+        return OSLG_ERR_CUDA;
     return OSLG_OK;
 }
 
@@ -1678,22 +184,18 @@ NoAllocDevice g_noalloc_dev[128];
 
 // One-time set-up per device, with that device current: resolve the
 // array's device address (the host-side symbol is only a stand-in) and
-// upload the simplex traversal table. Runs on the first call on a device.
+// allow the kernels their shared memory. Runs on the first call on a device.
 int noalloc_setup(int dev, NoAllocDevice& d, std::string* err) {
     if (d.ready) return OSLG_OK;
     void* p = nullptr;
     if (!cuda_ok(cudaGetSymbolAddress(&p, dev::g_noalloc_scratch), err, "cudaGetSymbolAddress(scratch)"))
         return OSLG_ERR_CUDA;
-    unsigned char t[64][4];
-    build_simplex4(t);
-    if (!cuda_ok(cudaMemcpyToSymbol(dev::c_simplex4, t, sizeof(t)), err, "simplex table")) return OSLG_ERR_CUDA;
     if (!cuda_ok(cudaDeviceGetAttribute(&d.sm_count, cudaDevAttrMultiProcessorCount, dev), err, "sm count"))
         return OSLG_ERR_CUDA;
     cudaDeviceGetAttribute(&d.smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    if (!cuda_ok(cudaFuncSetAttribute(dev::interp_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      d.smem_optin),
-                 err, "kernel attribute"))
-        return OSLG_ERR_CUDA;
+    for (int t = 0; t < kNumTiers; ++t)
+        if (!cuda_ok((cudaError_t)tier_fns(t).set_smem_limit(d.smem_optin), err, "kernel attribute"))
+            return OSLG_ERR_CUDA;
     d.base = static_cast<unsigned char*>(p);
     d.ready = true;
     return OSLG_OK;
@@ -1737,9 +239,9 @@ int device_execute_noalloc(const void* blob, size_t blob_bytes, const ProgramHea
         if (err) *err = "program does not fit in shared memory";
         return OSLG_ERR_LOWER;
     }
+    const TierFns& fns = tier_fns((int)((hdr.flags >> 8) & 7u));
     int per_sm = 0;
-    if (!cuda_ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::interp_kernel<false>, block, static_bytes),
-                 err, "occupancy"))
+    if (!cuda_ok((cudaError_t)fns.occupancy(false, block, static_bytes, &per_sm), err, "occupancy"))
         return OSLG_ERR_CUDA;
     if (per_sm < 1) per_sm = 1;
     int64_t tiles = (npoints + block - 1) / block;
@@ -1763,8 +265,9 @@ int device_execute_noalloc(const void* blob, size_t blob_bytes, const ProgramHea
         k.gheap = heap;
         k.status = status;
         k.G = G;
-        dev::interp_kernel<false><<<(unsigned)grid, block, static_bytes, s>>>(k);
-        if (!cuda_ok(cudaGetLastError(), err, "launch")) return OSLG_ERR_CUDA;
+        if (!cuda_ok((cudaError_t)fns.launch(false, (unsigned)grid, (unsigned)block, static_bytes, stream, k), err,
+                     "launch"))
+            return OSLG_ERR_CUDA;
     }
     if (status_out) {
         uint32_t v = 0;

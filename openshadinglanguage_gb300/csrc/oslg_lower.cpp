@@ -920,6 +920,30 @@ struct Lowerer {
         return fail("op '" + n + "' is not supported by this executor");
     }
 
+    // Interpreter feature tier the program needs (oslg_exec.h TierFns):
+    // bit 0 noise/hash, bit 1 closures/BSDF/spline, bit 2 math/vector/matrix.
+    uint32_t program_tier() const {
+        uint32_t t = 0;
+        for (const Op& op : ops) {
+            switch (op.code) {
+            case OP_NOISE: case OP_HASH: case OP_GABOR: t |= 1u; break;
+            case OP_CLOSURE: case OP_CLOSURE_MUL: case OP_CLOSURE_ADD: case OP_STORE_CLOSURE: case OP_BSDF_EVAL:
+            case OP_SPLINE:
+                t |= 2u;
+                break;
+            case OP_CBRT: case OP_SIN: case OP_COS: case OP_TAN: case OP_ASIN: case OP_ACOS: case OP_ATAN:
+            case OP_SINH: case OP_COSH: case OP_TANH: case OP_EXP: case OP_EXP2: case OP_EXPM1: case OP_LOG:
+            case OP_LOG2: case OP_LOG10: case OP_POW: case OP_ATAN2: case OP_FMOD: case OP_CLAMP: case OP_MIX:
+            case OP_SMOOTHSTEP: case OP_SELECT: case OP_DOT: case OP_CROSS: case OP_LENGTH: case OP_DISTANCE:
+            case OP_NORMALIZE: case OP_TRANSFORM: case OP_MMUL: case OP_AREF: case OP_AASSIGN:
+                t |= 4u;
+                break;
+            default: break;
+            }
+        }
+        return t;
+    }
+
     bool run(CompiledGroup& out) {
         if (g.layers.empty()) return fail("group has no layers");
         if (!build_lops()) return false;
@@ -943,6 +967,7 @@ struct Lowerer {
         for (const GSym& s : syms)
             if (s.referenced && s.derivs) h.flags |= 2u;
         h.max_depth = max_depth;
+        h.flags |= program_tier() << 8;
         if (h.heap_slots > kArgOffsetMask) return fail("symbol heap too large");
         out.header = h;
         out.blob.resize(sizeof(h) + ops.size() * sizeof(Op) + pool.size() * 4);

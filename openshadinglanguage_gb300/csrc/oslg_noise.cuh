@@ -482,19 +482,18 @@ __device__ __forceinline__ float simplex3(float x, float y, float z, int seed, f
     return noise;
 }
 
-// 4D traversal table (simplexnoise.cpp:108-126), built on the host and
-// placed in constant memory by the interpreter TU.
-__constant__ unsigned char c_simplex4[64][4];
-
 __device__ __forceinline__ float simplex4(float x, float y, float z, float w, int seed, float* dd) {
     const float F4 = 0.309016994f, G4 = 0.138196601f;
     float s = (x + y + z + w) * F4;
     int i = ifloor(x + s), j = ifloor(y + s), k = ifloor(z + s), l = ifloor(w + s);
     float t = (float)(i + j + k + l) * G4;
     float x0 = x - ((float)i - t), y0 = y - ((float)j - t), z0 = z - ((float)k - t), w0 = w - ((float)l - t);
-    int c = (x0 > y0 ? 32 : 0) | (x0 > z0 ? 16 : 0) | (y0 > z0 ? 8 : 0) | (x0 > w0 ? 4 : 0)
-          | (y0 > w0 ? 2 : 0) | (z0 > w0 ? 1 : 0);
-    int sc[4] = { c_simplex4[c][0], c_simplex4[c][1], c_simplex4[c][2], c_simplex4[c][3] };
+    // simplexnoise.cpp:108-126 looks the axis ranks up in a table indexed by
+    // six pairwise comparisons; with strict '>' every comparison pattern is
+    // that of a strict order (ties favour the later axis), and each entry is
+    // the number of axes that axis beats, counted here directly.
+    const int c1 = x0 > y0, c2 = x0 > z0, c3 = y0 > z0, c4 = x0 > w0, c5 = y0 > w0, c6 = z0 > w0;
+    int sc[4] = { c1 + c2 + c4, (1 - c1) + c3 + c5, (1 - c2) + (1 - c3) + c6, (1 - c4) + (1 - c5) + (1 - c6) };
     float cx[5], cy[5], cz[5], cw[5];
     int ci[5], cj[5], ck[5], cl[5];
     cx[0] = x0; cy[0] = y0; cz[0] = z0; cw[0] = w0;

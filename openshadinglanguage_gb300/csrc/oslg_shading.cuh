@@ -23,7 +23,7 @@ struct SplineBasisDev {
     int step;
     float m[4][4];
 };
-__constant__ SplineBasisDev c_spline_basis[6] = {
+static __constant__ SplineBasisDev c_spline_basis[6] = {
     { 1, { { -1.0f / 2.0f, 3.0f / 2.0f, -3.0f / 2.0f, 1.0f / 2.0f },
            { 2.0f / 2.0f, -5.0f / 2.0f, 4.0f / 2.0f, -1.0f / 2.0f },
            { -1.0f / 2.0f, 0.0f / 2.0f, 1.0f / 2.0f, 0.0f / 2.0f },
