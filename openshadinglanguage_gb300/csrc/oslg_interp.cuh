@@ -28,6 +28,7 @@
 #include <string>
 
 #include "oslg_exec.h"
+#include "oslg_gabor.cuh"
 #include "oslg_noise.cuh"
 #include "oslg_shading.cuh"
 
@@ -717,7 +718,199 @@ static __device__ void h_transform(const Lane& L, const uint32_t* a) {
     }
 }
 
+// ---- matrix extras ---------------------------------------------------------------
+// 4x4 inverse by Gauss-Jordan elimination with partial pivoting; a singular
+// matrix gives the identity (Imath's inverse() with exceptions off returns
+// identity). Same steps as the host statement in the oracle.
+__device__ __forceinline__ void m44_inverse(const float* A, float* out) {
+    float t[16], s[16];
+    for (int i = 0; i < 16; ++i) { t[i] = A[i]; s[i] = (i % 5 == 0) ? 1.0f : 0.0f; }
+    for (int i = 0; i < 4; ++i) {
+        int piv = i;
+        float pmax = fabsf(t[i * 4 + i]);
+        for (int j = i + 1; j < 4; ++j)
+            if (fabsf(t[j * 4 + i]) > pmax) { pmax = fabsf(t[j * 4 + i]); piv = j; }
+        if (pmax == 0.0f) {
+            for (int k = 0; k < 16; ++k) out[k] = (k % 5 == 0) ? 1.0f : 0.0f;
+            return;
+        }
+        if (piv != i)
+            for (int k = 0; k < 4; ++k) {
+                float u = t[i * 4 + k]; t[i * 4 + k] = t[piv * 4 + k]; t[piv * 4 + k] = u;
+                u = s[i * 4 + k]; s[i * 4 + k] = s[piv * 4 + k]; s[piv * 4 + k] = u;
+            }
+        for (int j = 0; j < 4; ++j) {
+            if (j == i) continue;
+            const float f = t[j * 4 + i] / t[i * 4 + i];
+            for (int k = 0; k < 4; ++k) {
+                t[j * 4 + k] = t[j * 4 + k] - f * t[i * 4 + k];
+                s[j * 4 + k] = s[j * 4 + k] - f * s[i * 4 + k];
+            }
+        }
+    }
+    for (int i = 0; i < 4; ++i) {
+        const float f = t[i * 4 + i];
+        for (int k = 0; k < 4; ++k) out[i * 4 + k] = s[i * 4 + k] / f;
+    }
+}
+__device__ __forceinline__ void m44_mul(const float* A, const float* B, float* out) {
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j)
+            out[i * 4 + j] = A[i * 4 + 0] * B[0 * 4 + j] + A[i * 4 + 1] * B[1 * 4 + j] + A[i * 4 + 2] * B[2 * 4 + j]
+                           + A[i * 4 + 3] * B[3 * 4 + j];
+}
+// Imathx.h:456-492
+__device__ __forceinline__ float det2(float a, float b, float c, float d) { return a * d - b * c; }
+__device__ __forceinline__ float det3(float a1, float a2, float a3, float b1, float b2, float b3, float c1, float c2,
+                                      float c3) {
+    return a1 * det2(b2, b3, c2, c3) - b1 * det2(a2, a3, c2, c3) + c1 * det2(a2, a3, b2, b3);
+}
+__device__ __forceinline__ float det4(const float* m) {
+    const float a1 = m[0], b1 = m[1], c1 = m[2], d1 = m[3];
+    const float a2 = m[4], b2 = m[5], c2 = m[6], d2_ = m[7];
+    const float a3 = m[8], b3 = m[9], c3 = m[10], d3 = m[11];
+    const float a4 = m[12], b4 = m[13], c4 = m[14], d4 = m[15];
+    return a1 * det3(b2, b3, b4, c2, c3, c4, d2_, d3, d4) - b1 * det3(a2, a3, a4, c2, c3, c4, d2_, d3, d4)
+         + c1 * det3(a2, a3, a4, b2, b3, b4, d2_, d3, d4) - d1 * det3(a2, a3, a4, b2, b3, b4, c2, c3, c4);
+}
+
+// matrix division (src/liboslexec/opmatrix.cpp:49-73)
+static __device__ void h_mdiv(const Lane& L, const uint32_t* a) {
+    const uint32_t r = a[0], x = a[1], y = a[2];
+    float out[16];
+    const bool mx = atc(x) == TC_MATRIX, my = atc(y) == TC_MATRIX;
+    if (mx && my) {
+        float A[16], B[16], Bi[16];
+        for (int i = 0; i < 16; ++i) { A[i] = __uint_as_float(ldw(L, x, i)); B[i] = __uint_as_float(ldw(L, y, i)); }
+        m44_inverse(B, Bi);
+        m44_mul(A, Bi, out);
+    } else if (mx) {
+        const float f = 1.0f / ldf(L, y, 0, 0);
+        for (int i = 0; i < 16; ++i) out[i] = __uint_as_float(ldw(L, x, i)) * f;
+    } else if (my) {
+        float B[16], Bi[16];
+        for (int i = 0; i < 16; ++i) B[i] = __uint_as_float(ldw(L, y, i));
+        m44_inverse(B, Bi);
+        const float f = ldf(L, x, 0, 0);
+        for (int i = 0; i < 16; ++i) out[i] = Bi[i] * f;
+    } else {
+        const float av = ldf(L, x, 0, 0), bv = ldf(L, y, 0, 0);
+        const float f = (bv == 0.0f) ? 0.0f : (av / bv);
+        for (int i = 0; i < 16; ++i) out[i] = (i % 5 == 0) ? f : 0.0f;
+    }
+    for (int i = 0; i < 16; ++i) stf(L, r, i, out[i]);
+}
+
+// transformn: multDirMatrix by the transposed inverse (opmatrix.cpp:122-137)
+static __device__ void h_transformn(const Lane& L, const uint32_t* a) {
+    const uint32_t r = a[0], p = a[1], m = a[2];
+    float M[16], Mi[16], T[16];
+    for (int i = 0; i < 16; ++i) M[i] = __uint_as_float(ldw(L, m, i));
+    m44_inverse(M, Mi);
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) T[i * 4 + j] = Mi[j * 4 + i];
+    const int nd = ader(r) ? 3 : 1;
+    for (int d = 0; d < nd; ++d) {
+        const float X = ldf(L, p, 0, d), Y = ldf(L, p, 1, d), Z = ldf(L, p, 2, d);
+        stf(L, r, d * 3 + 0, X * T[0] + Y * T[4] + Z * T[8]);
+        stf(L, r, d * 3 + 1, X * T[1] + Y * T[5] + Z * T[9]);
+        stf(L, r, d * 3 + 2, X * T[2] + Y * T[6] + Z * T[10]);
+    }
+}
+
+static __device__ void h_matrix_misc(const Lane& L, uint32_t code, const uint32_t* a) {
+    const uint32_t r = a[0], x = a[1];
+    if (code == OP_TRANSPOSE) {
+        float M[16];
+        for (int i = 0; i < 16; ++i) M[i] = __uint_as_float(ldw(L, x, i));
+        for (int i = 0; i < 4; ++i)
+            for (int j = 0; j < 4; ++j) stf(L, r, i * 4 + j, M[j * 4 + i]);
+    } else {  // OP_DETERMINANT
+        float M[16];
+        for (int i = 0; i < 16; ++i) M[i] = __uint_as_float(ldw(L, x, i));
+        stval(L, r, 0, det4(M));
+    }
+}
+
+// area (llvm_ops.cpp:915-941) and filterwidth (:944-965): value-only results
+static __device__ void h_deriv_misc(const Lane& L, uint32_t code, const uint32_t* a) {
+    const uint32_t r = a[0], x = a[1];
+    if (code == OP_AREA) {
+        const V3 dx = v3(ldf(L, x, 0, 1), ldf(L, x, 1, 1), ldf(L, x, 2, 1));
+        const V3 dy = v3(ldf(L, x, 0, 2), ldf(L, x, 1, 2), ldf(L, x, 2, 2));
+        stval(L, r, 0, vlen_imath(vcross(dx, dy)));
+    } else {
+        const int n = anc(x);
+        for (int c = 0; c < n; ++c) {
+            const float dx = ldf(L, x, c, 1), dy = ldf(L, x, c, 2);
+            stval(L, r, c, sqrtf(dx * dx + dy * dy));
+        }
+    }
+}
+
+// luminance: dot with the colour system's luminance scale (a2, a constant
+// triple the lowering computes; opcolor.cpp:461-476)
+static __device__ void h_luminance(const Lane& L, const uint32_t* a) {
+    const uint32_t r = a[0], c = a[1], s = a[2];
+    const float sx = ldf(L, s, 0, 0), sy = ldf(L, s, 1, 0), sz = ldf(L, s, 2, 0);
+    const int nd = ader(r) ? 3 : 1;
+    for (int d = 0; d < nd; ++d)
+        stf(L, r, d, ldf(L, c, 0, d) * sx + ldf(L, c, 1, d) * sy + ldf(L, c, 2, d) * sz);
+}
+
 // ---- noise ---------------------------------------------------------------------
+// gabor / pgabor: a = r, S, T, kind word, anisotropic, direction,
+// bandwidth; b (the carrier op that follows) = impulses, do_filter,
+// Speriod, Tperiod. 1-D and 2-D positions slice to 3-D and the 4-D forms
+// drop t (src/liboslexec/opnoise.cpp:484-640).
+static __device__ void h_gabor(const Lane& L, const uint32_t* a, const uint32_t* b) {
+    const uint32_t r = a[0], S = a[1], kw = a[3];
+    const bool periodic = (kw & 16u) != 0;
+    const int dims = (int)((kw >> 5) & 7u);
+    const int nc = (kw & 256u) ? 3 : 1;
+    const int ns = anc(S);
+    GOpts o;
+    o.anisotropic = ldi(L, a[4], 0);
+    o.direction = v3(ldf(L, a[5], 0, 0), ldf(L, a[5], 1, 0), ldf(L, a[5], 2, 0));
+    o.bandwidth = ldf(L, a[6], 0, 0);
+    o.impulses = ldf(L, b[0], 0, 0);
+    o.do_filter = ldi(L, b[1], 0);
+    DV3 X;
+    X.v = X.dx = X.dy = v3(0.0f, 0.0f, 0.0f);
+    {
+        const D2 x0 = ldd(L, S, 0);
+        X.v.x = x0.v; X.dx.x = x0.dx; X.dy.x = x0.dy;
+        if (ns == 3) {
+            const D2 x1 = ldd(L, S, 1), x2 = ldd(L, S, 2);
+            X.v.y = x1.v; X.dx.y = x1.dx; X.dy.y = x1.dy;
+            X.v.z = x2.v; X.dx.z = x2.dx; X.dy.z = x2.dy;
+        } else if (dims == 2) {
+            const D2 x1 = ldd(L, a[2], 0);
+            X.v.y = x1.v; X.dx.y = x1.dx; X.dy.y = x1.dy;
+        }
+    }
+    V3 period = v3(0.0f, 0.0f, 0.0f);
+    if (periodic) {
+        if (ns == 3) {
+            period = v3(ldf(L, b[2], 0, 0), ldf(L, b[2], 1, 0), ldf(L, b[2], 2, 0));
+        } else {
+            period.x = ldf(L, b[2], 0, 0);
+            if (dims == 2) period.y = ldf(L, b[3], 0, 0);
+        }
+    }
+    D2 res[3];
+    gabor_eval(o, X, periodic, period, nc, res);
+    const int rn = anc(r);
+    for (int c = 0; c < rn; ++c) {
+        const D2 v = res[nc == 1 ? 0 : c];
+        stf(L, r, c, v.v);
+        if (ader(r)) {
+            stf(L, r, rn + c, v.dx);
+            stf(L, r, 2 * rn + c, v.dy);
+        }
+    }
+}
+
 static __device__ void h_noise(const Lane& L, const uint32_t* a) {
     uint32_t r = a[0], S = a[1], T = a[2], kw = a[3];
     int kind = (int)(kw & 15u);
@@ -1482,8 +1675,26 @@ __global__ void __launch_bounds__(256) interp_kernel(KArgs k) {
                         for (int c = 0; c < nc; ++c) stval(L, a[0], c, ldf(L, a[1], c, d));
                         break;
                     }
-                    case OP_TRANSFORM: OSLG_TIER_CASE(4, h_transform(L, a)) break;
+                    case OP_TRANSFORM:
+                        if (a[3] == 2u) { OSLG_TIER_CASE(4, h_transformn(L, a)) }
+                        else { OSLG_TIER_CASE(4, h_transform(L, a)) }
+                        break;
+                    case OP_MDIV: OSLG_TIER_CASE(4, h_mdiv(L, a)) break;
+                    case OP_TRANSPOSE:
+                    case OP_DETERMINANT: OSLG_TIER_CASE(4, h_matrix_misc(L, code, a)) break;
+                    case OP_AREA:
+                    case OP_FILTERWIDTH: OSLG_TIER_CASE(4, h_deriv_misc(L, code, a)) break;
+                    case OP_LUMINANCE: OSLG_TIER_CASE(4, h_luminance(L, a)) break;
                     case OP_NOISE: OSLG_TIER_CASE(1, h_noise(L, a)) break;
+                    case OP_GABOR: {
+                        if constexpr ((TIER & 1) != 0) {
+                            if (pc + 1 < nops) h_gabor(L, a, sops[pc + 1].a);
+                            else raise_status(k.status, ST_BAD_OPCODE);
+                        } else {
+                            raise_status(k.status, ST_BAD_OPCODE);
+                        }
+                        break;
+                    }
                     case OP_HASH: OSLG_TIER_CASE(1, h_hash(L, a)) break;
                     case OP_CLOSURE: {
                         if constexpr ((TIER & 2) != 0) {

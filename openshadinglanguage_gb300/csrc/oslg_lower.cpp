@@ -19,6 +19,8 @@
 //   * layers run in group order; a connection copies the upstream output
 //     into the downstream parameter before that layer's body.
 #include <algorithm>
+#include <array>
+#include <cmath>
 #include <cstring>
 #include <functional>
 #include <set>
@@ -336,6 +338,12 @@ struct Lowerer {
                  || op.name == "filterwidth" || op.name == "calculatenormal")
                 && op.args.size() > 1)
                 mark_derivs(op.args[1]);
+            // gabor noise always takes derivatives of its positions
+            // (src/liboslcomp/typecheck.cpp:1363-1378)
+            if ((op.name == "noise" || op.name == "pnoise") && op.args.size() > 2 && is_string(op.args[1])
+                && syms[op.args[1]].is_const && const_string(op.args[1]) == "gabor") {
+                for (size_t i = 2; i < op.args.size() && !is_string(op.args[i]); ++i) mark_derivs(op.args[i]);
+            }
             if (op.name == "__store_output" && op.imm[2]) mark_derivs(op.args[0]);
             if (op.name == "__load_userdata" && op.imm[2]) mark_derivs(op.args[0]);
         }
@@ -597,6 +605,53 @@ struct Lowerer {
         return std::string();
     }
 
+    // Rec709 luminance weights as ColorSystem::set_colorspace derives them
+    // (src/liboslexec/opcolor.cpp:140-190): XYZ->RGB from the primaries and
+    // the D65 white point, inverted (cofactors over the determinant), and
+    // the middle column of RGB->XYZ.
+    static std::array<float, 3> luminance_scale() {
+        const float xr = 0.64f, yr = 0.33f, xg = 0.30f, yg = 0.60f, xb = 0.15f, yb = 0.06f, xw = 0.3127f,
+                    yw = 0.3291f;
+        const float R[3] = { xr, yr, 1.0f - (xr + yr) }, G[3] = { xg, yg, 1.0f - (xg + yg) },
+                    B[3] = { xb, yb, 1.0f - (xb + yb) }, W[3] = { xw, yw, 1.0f - (xw + yw) };
+        float r[3] = { G[1] * B[2] - B[1] * G[2], B[0] * G[2] - G[0] * B[2], G[0] * B[1] - B[0] * G[1] };
+        float g[3] = { B[1] * R[2] - R[1] * B[2], R[0] * B[2] - B[0] * R[2], B[0] * R[1] - R[0] * B[1] };
+        float b[3] = { R[1] * G[2] - G[1] * R[2], G[0] * R[2] - R[0] * G[2], R[0] * G[1] - G[0] * R[1] };
+        float w[3] = { r[0] * W[0] + r[1] * W[1] + r[2] * W[2], g[0] * W[0] + g[1] * W[1] + g[2] * W[2],
+                       b[0] * W[0] + b[1] * W[1] + b[2] * W[2] };
+        const float ws = 1.0f / W[1];
+        for (float& x : w) x *= ws;
+        for (int i = 0; i < 3; ++i) { r[i] /= w[0]; g[i] /= w[1]; b[i] /= w[2]; }
+        const float M[3][3] = { { r[0], g[0], b[0] }, { r[1], g[1], b[1] }, { r[2], g[2], b[2] } };
+        float C[3][3];  // cofactor matrix transposed (adjugate)
+        C[0][0] = M[1][1] * M[2][2] - M[2][1] * M[1][2];
+        C[0][1] = M[2][1] * M[0][2] - M[0][1] * M[2][2];
+        C[0][2] = M[0][1] * M[1][2] - M[1][1] * M[0][2];
+        C[1][0] = M[2][0] * M[1][2] - M[1][0] * M[2][2];
+        C[1][1] = M[0][0] * M[2][2] - M[2][0] * M[0][2];
+        C[1][2] = M[1][0] * M[0][2] - M[0][0] * M[1][2];
+        C[2][0] = M[1][0] * M[2][1] - M[2][0] * M[1][1];
+        C[2][1] = M[2][0] * M[0][1] - M[0][0] * M[2][1];
+        C[2][2] = M[0][0] * M[1][1] - M[1][0] * M[0][1];
+        const float det = M[0][0] * C[0][0] + M[0][1] * C[1][0] + M[0][2] * C[2][0];
+        std::array<float, 3> l = { C[0][1] / det, C[1][1] / det, C[2][1] / det };
+        const float lum2 = 1.0f - l[0] - l[1];
+        if (std::fabs(lum2 - l[2]) < 0.001f) l[2] = lum2;
+        return l;
+    }
+    int const_triple(const std::array<float, 3>& v) {
+        GSym d;
+        d.name = "$triple";
+        d.type.base = BT_TRIPLE;
+        d.type.vecsem = VS_COLOR;
+        d.kind = SK_CONST;
+        d.is_const = true;
+        d.cval = { v[0], v[1], v[2] };
+        int k = add_sym(d);
+        syms[k].slot = (int)pool_add(syms[k]);
+        return k;
+    }
+
     bool lower_noise(const LOp& op) {
         // noise-family ops: (result, [name], S, [T], [Speriod, [Tperiod]], [options...])
         // name mapping follows src/liboslexec/batched_llvm_gen.cpp:6094-6146
@@ -751,7 +806,7 @@ struct Lowerer {
                 emit(ar->second.second, { a(0), a(1), a(2) }, n);
                 return true;
             }
-            if ((n == "mul" || n == "div") && (is_matrix(x) || is_matrix(y)) && is_matrix(r)) {
+            if ((n == "mul" || n == "div") && is_matrix(r) && (is_matrix(x) || is_matrix(y) || n == "div")) {
                 emit(n == "mul" ? OP_MMUL : OP_MDIV, { a(0), a(1), a(2) }, n);
                 return true;
             }
@@ -896,7 +951,11 @@ struct Lowerer {
             return true;
         }
         if (n == "blackbody") { emit(OP_BLACKBODY, { a(0), a(1) }, n); return true; }
-        if (n == "luminance") { emit(OP_LUMINANCE, { a(0), a(1) }, n); return true; }
+        if (n == "luminance") {
+            int sc = const_triple(luminance_scale());
+            emit(OP_LUMINANCE, { a(0), a(1), A(sc) }, n);
+            return true;
+        }
         if (n == "closure") {
             // closure r [weight] name args...   (llvm_gen_closure, batched_llvm_gen.cpp:7310)
             uses_closures = true;

@@ -196,6 +196,161 @@ def testnoise(shader_name="testnoise", noisename_default="noise", offset_default
     return b.text()
 
 
+def testpnoise(shader_name="testpnoise", noisename_default="noise", offset_default=0.5, scale_default=0.5,
+               period_default=3.0):
+    """testsuite/common/shaders/testpnoise.osl: periodic noise with the
+    testnoise layout, angle 0, inscale 30, period 3."""
+    b = OsoBuilder(shader_name)
+    noisename = b.param("string", "noisename", noisename_default)
+    offset = b.param("float", "offset", offset_default)
+    scale = b.param("float", "scale", scale_default)
+    period = b.param("float", "period", period_default)
+    Cout = b.param("color", "Cout", [0, 0, 0], output=True)
+    u, v, ru, rv, rz, ttime = _testnoise_common(b, angle_default=0.0, inscale_default=30.0)
+    b.op("assign", Cout, b.const("float", 0.0))
+
+    def emit(vec, dim):
+        r = b.tmp("color" if vec else "float")
+        if dim == 1:
+            b.op("pnoise", r, noisename, ru, period)
+        elif dim == 2:
+            b.op("pnoise", r, noisename, ru, rv, period, period)
+        else:
+            pt, pp = b.tmp("point"), b.tmp("point")
+            b.op("point", pt, ru, rv, rz)
+            b.op("assign", pp, period)
+            if dim == 3:
+                b.op("pnoise", r, noisename, pt, pp)
+            else:
+                b.op("pnoise", r, noisename, pt, ttime, pp, period)
+        m, a = b.tmp("color" if vec else "float"), b.tmp("color" if vec else "float")
+        b.op("mul", m, scale, r)
+        b.op("add", a, offset, m)
+        b.op("assign", Cout, a)
+
+    _quadrants(b, u, v, emit)
+    return b.text()
+
+
+def gabor_options(shader_name="test_gabor_options", anisotropic=0, direction=(1.0, 0.0, 0.0), bandwidth=4.0,
+                  impulses=16.0, do_filter=1):
+    """testsuite/noise-gabor-reg/test_gabor_options.osl: the testnoise layout
+    with every Gabor option passed by name from a shader parameter."""
+    b = OsoBuilder(shader_name)
+    offset = b.param("float", "offset", 0.5)
+    scale = b.param("float", "scale", 0.5)
+    aniso = b.param("int", "anisotropic", anisotropic)
+    direc = b.param("vector", "direction", list(direction))
+    bw = b.param("float", "bandwidth", bandwidth)
+    imp = b.param("float", "impulses", impulses)
+    filt = b.param("int", "do_filter", do_filter)
+    Cout = b.param("color", "Cout", [0, 0, 0], output=True)
+    u, v, ru, rv, rz, ttime = _testnoise_common(b)
+    b.op("assign", Cout, b.const("float", 0.0))
+    gname = b.const("string", "gabor")
+    opts = [b.const("string", "anisotropic"), aniso, b.const("string", "direction"), direc,
+            b.const("string", "bandwidth"), bw, b.const("string", "impulses"), imp,
+            b.const("string", "do_filter"), filt]
+
+    def emit(vec, dim):
+        r = b.tmp("color" if vec else "float")
+        if dim in (1, 2):
+            args = [ru] if dim == 1 else [ru, rv]
+        else:
+            pt = b.tmp("point")
+            b.op("point", pt, ru, rv, rz)
+            args = [pt] if dim == 3 else [pt, ttime]
+        b.op("noise", r, gname, *args, *opts)
+        m, a = b.tmp("color" if vec else "float"), b.tmp("color" if vec else "float")
+        b.op("mul", m, scale, r)
+        b.op("add", a, offset, m)
+        b.op("assign", Cout, a)
+
+    _quadrants(b, u, v, emit)
+    return b.text()
+
+
+def gabor_filter_test(dims, shader_name=None, freq=5.0):
+    """testsuite/noise-gabor{2d,3d}-filter/test.osl: p = P*freq*(1+10*v*v)*(1+10*u*u),
+    Cout = noise("gabor", p[0], p[1]) (2-D) or noise("gabor", p) (3-D), *0.5+0.5."""
+    b = OsoBuilder(shader_name or "gabor%dd_filter" % dims, "surface")
+    noisename = b.param("string", "noisename", "gabor")
+    fr = b.param("float", "freq", freq)
+    Cout = b.param("color", "Cout", [0, 0, 0], output=True)
+    P, u, v = b.glob("point", "P"), b.glob("float", "u"), b.glob("float", "v")
+    c = lambda x: b.const("float", x)
+    p, t1, t2, t3, t4, t5, t6 = b.tmp("point"), *(b.tmp("float") for _ in range(6))
+    b.op("mul", p, P, fr)
+    b.op("mul", t1, c(10.0), v)  # 10*v*v parses as (10*v)*v
+    b.op("mul", t2, t1, v)
+    b.op("add", t3, c(1.0), t2)
+    b.op("mul", p, p, t3)
+    b.op("mul", t4, c(10.0), u)
+    b.op("mul", t5, t4, u)
+    b.op("add", t6, c(1.0), t5)
+    b.op("mul", p, p, t6)
+    n = b.tmp("float")
+    if dims == 2:
+        px, py = b.tmp("float"), b.tmp("float")
+        b.op("compref", px, p, b.const("int", 0))
+        b.op("compref", py, p, b.const("int", 1))
+        b.op("noise", n, noisename, px, py)
+    else:
+        b.op("noise", n, noisename, p)
+    h, o = b.tmp("float"), b.tmp("float")
+    b.op("mul", h, n, c(0.5))
+    b.op("add", o, h, c(0.5))
+    b.op("assign", Cout, o)
+    return b.text()
+
+
+def matrix_ops(M, M2):
+    """Matrix and derivative ops on a per-point matrix: Mv = M * (1 + u)
+    (varying), then transpose, determinant, M / M2, 1 / M, transform /
+    transformv / transformn of P, area(P), filterwidth(u) and luminance of a
+    colour built from P. Outputs: det, Pt, Vt, Nt, area, fw, lum, and the
+    first rows of transpose(Mv), Mv / M2 and 1 / Mv."""
+    b = OsoBuilder("matrix_ops")
+    Mp = b.param("matrix", "M", list(M))
+    M2p = b.param("matrix", "M2", list(M2))
+    det = b.param("float", "det", 0.0, output=True)
+    Pt = b.param("point", "Pt", [0, 0, 0], output=True)
+    Vt = b.param("vector", "Vt", [0, 0, 0], output=True)
+    Nt = b.param("normal", "Nt", [0, 0, 0], output=True)
+    ar = b.param("float", "area", 0.0, output=True)
+    fw = b.param("float", "fw", 0.0, output=True)
+    lum = b.param("float", "lum", 0.0, output=True)
+    rowT = b.param("color", "rowT", [0, 0, 0], output=True)
+    rowD = b.param("color", "rowD", [0, 0, 0], output=True)
+    rowI = b.param("color", "rowI", [0, 0, 0], output=True)
+    P, u = b.glob("point", "P"), b.glob("float", "u")
+    c = lambda x: b.const("float", x)
+    s, Mv, T, D, I = b.tmp("float"), b.tmp("matrix"), b.tmp("matrix"), b.tmp("matrix"), b.tmp("matrix")
+    b.op("add", s, c(1.0), u)
+    b.op("mul", Mv, Mp, s)
+    b.op("transpose", T, Mv)
+    b.op("determinant", det, Mv)
+    b.op("div", D, Mv, M2p)
+    b.op("div", I, c(1.0), Mv)
+    b.op("transform", Pt, Mv, P)
+    V, Nn = b.tmp("vector"), b.tmp("normal")
+    b.op("vector", V, P)
+    b.op("normal", Nn, P)
+    b.op("transformv", Vt, Mv, V)
+    b.op("transformn", Nt, Mv, Nn)
+    b.op("area", ar, P)
+    b.op("filterwidth", fw, u)
+    col = b.tmp("color")
+    b.op("color", col, P)
+    b.op("luminance", lum, col)
+    for row, src in ((rowT, T), (rowD, D), (rowI, I)):
+        for j in range(3):
+            t = b.tmp("float")
+            b.op("mxcompref", t, src, b.const("int", 0), b.const("int", j))
+            b.op("compassign", row, b.const("int", j), t)
+    return b.text()
+
+
 def getP():
     """testsuite/example-batched-deformer/getP.osl: output point out = P"""
     b = OsoBuilder("getP")

@@ -27,6 +27,7 @@
 
 #include "../include/oslg.h"
 #include "../openshadinglanguage_gb300/csrc/oslg_program.h"
+#include "oracle_gabor.h"
 #include "oracle_shading.h"
 #include "oracle_simplex.h"
 
@@ -442,6 +443,125 @@ void op_transform(Point& P, const uint32_t* a) {
     }
 }
 
+// 4x4 inverse by Gauss-Jordan elimination with partial pivoting; singular
+// gives the identity (Imath's inverse() with exceptions off). Imath is not
+// in the reference tree, so inverse-dependent results (matrix division,
+// transformn) are pinned to this algorithm, not to Imath's bits.
+void m44_inverse(const float* A, float* out) {
+    float t[16], s[16];
+    for (int i = 0; i < 16; ++i) { t[i] = A[i]; s[i] = (i % 5 == 0) ? 1.0f : 0.0f; }
+    for (int i = 0; i < 4; ++i) {
+        int piv = i;
+        float pmax = std::fabs(t[i * 4 + i]);
+        for (int j = i + 1; j < 4; ++j)
+            if (std::fabs(t[j * 4 + i]) > pmax) { pmax = std::fabs(t[j * 4 + i]); piv = j; }
+        if (pmax == 0.0f) {
+            for (int k = 0; k < 16; ++k) out[k] = (k % 5 == 0) ? 1.0f : 0.0f;
+            return;
+        }
+        if (piv != i)
+            for (int k = 0; k < 4; ++k) {
+                std::swap(t[i * 4 + k], t[piv * 4 + k]);
+                std::swap(s[i * 4 + k], s[piv * 4 + k]);
+            }
+        for (int j = 0; j < 4; ++j) {
+            if (j == i) continue;
+            float f = t[j * 4 + i] / t[i * 4 + i];
+            for (int k = 0; k < 4; ++k) {
+                t[j * 4 + k] = t[j * 4 + k] - f * t[i * 4 + k];
+                s[j * 4 + k] = s[j * 4 + k] - f * s[i * 4 + k];
+            }
+        }
+    }
+    for (int i = 0; i < 4; ++i) {
+        float f = t[i * 4 + i];
+        for (int k = 0; k < 4; ++k) out[i * 4 + k] = s[i * 4 + k] / f;
+    }
+}
+void m44_mul(const float* A, const float* B, float* out) {
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j)
+            out[i * 4 + j] = A[i * 4 + 0] * B[0 * 4 + j] + A[i * 4 + 1] * B[1 * 4 + j] + A[i * 4 + 2] * B[2 * 4 + j]
+                           + A[i * 4 + 3] * B[3 * 4 + j];
+}
+// Imathx.h:456-492
+inline float det2(float a, float b, float c, float d) { return a * d - b * c; }
+inline float det3(float a1, float a2, float a3, float b1, float b2, float b3, float c1, float c2, float c3) {
+    return a1 * det2(b2, b3, c2, c3) - b1 * det2(a2, a3, c2, c3) + c1 * det2(a2, a3, b2, b3);
+}
+float det4(const float* m) {
+    float a1 = m[0], b1 = m[1], c1 = m[2], d1 = m[3];
+    float a2 = m[4], b2 = m[5], c2 = m[6], d2 = m[7];
+    float a3 = m[8], b3 = m[9], c3 = m[10], d3 = m[11];
+    float a4 = m[12], b4 = m[13], c4 = m[14], d4 = m[15];
+    return a1 * det3(b2, b3, b4, c2, c3, c4, d2, d3, d4) - b1 * det3(a2, a3, a4, c2, c3, c4, d2, d3, d4)
+         + c1 * det3(a2, a3, a4, b2, b3, b4, d2, d3, d4) - d1 * det3(a2, a3, a4, b2, b3, b4, c2, c3, c4);
+}
+
+// matrix division (src/liboslexec/opmatrix.cpp:49-73)
+void op_mdiv(Point& P, const uint32_t* a) {
+    uint32_t r = a[0], x = a[1], y = a[2];
+    float out[16];
+    bool mx = atc(x) == oslg::TC_MATRIX, my = atc(y) == oslg::TC_MATRIX;
+    if (mx && my) {
+        float A[16], B[16], Bi[16];
+        for (int i = 0; i < 16; ++i) { A[i] = bitsf(word(P, x, i)); B[i] = bitsf(word(P, y, i)); }
+        m44_inverse(B, Bi);
+        m44_mul(A, Bi, out);
+    } else if (mx) {
+        float f = 1.0f / getf(P, y, 0, 0);
+        for (int i = 0; i < 16; ++i) out[i] = bitsf(word(P, x, i)) * f;
+    } else if (my) {
+        float B[16], Bi[16];
+        for (int i = 0; i < 16; ++i) B[i] = bitsf(word(P, y, i));
+        m44_inverse(B, Bi);
+        float f = getf(P, x, 0, 0);
+        for (int i = 0; i < 16; ++i) out[i] = Bi[i] * f;
+    } else {
+        float av = getf(P, x, 0, 0), bv = getf(P, y, 0, 0);
+        float f = (bv == 0.0f) ? 0.0f : (av / bv);
+        for (int i = 0; i < 16; ++i) out[i] = (i % 5 == 0) ? f : 0.0f;
+    }
+    for (int i = 0; i < 16; ++i) setf(P, r, i, out[i]);
+}
+
+// transformn: multDirMatrix by the transposed inverse (opmatrix.cpp:122-137)
+void op_transformn(Point& P, const uint32_t* a) {
+    uint32_t r = a[0], p = a[1], m = a[2];
+    float M[16], Mi[16], T[16];
+    for (int i = 0; i < 16; ++i) M[i] = bitsf(word(P, m, i));
+    m44_inverse(M, Mi);
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) T[i * 4 + j] = Mi[j * 4 + i];
+    int nd = ader(r) ? 3 : 1;
+    for (int d = 0; d < nd; ++d) {
+        float X = getf(P, p, 0, d), Y = getf(P, p, 1, d), Z = getf(P, p, 2, d);
+        setf(P, r, d * 3 + 0, X * T[0] + Y * T[4] + Z * T[8]);
+        setf(P, r, d * 3 + 1, X * T[1] + Y * T[5] + Z * T[9]);
+        setf(P, r, d * 3 + 2, X * T[2] + Y * T[6] + Z * T[10]);
+    }
+}
+
+// area (llvm_ops.cpp:915-941): length of cross(dPdx, dPdy); filterwidth
+// (:944-965): sqrt(dx*dx + dy*dy) per component
+void op_area(Point& P, const uint32_t* a) {
+    V3 dx(getf(P, a[1], 0, 1), getf(P, a[1], 1, 1), getf(P, a[1], 2, 1));
+    V3 dy(getf(P, a[1], 0, 2), getf(P, a[1], 1, 2), getf(P, a[1], 2, 2));
+    putv(P, a[0], 0, v3_length(v3_cross(dx, dy)));
+}
+void op_filterwidth(Point& P, const uint32_t* a) {
+    for (int c = 0; c < anc(a[1]); ++c) {
+        float dx = getf(P, a[1], c, 1), dy = getf(P, a[1], c, 2);
+        putv(P, a[0], c, std::sqrt(dx * dx + dy * dy));
+    }
+}
+// luminance (opcolor.cpp:461-476, opcolor.h:59-62); a2 = scale triple
+void op_luminance(Point& P, const uint32_t* a) {
+    float sx = getf(P, a[2], 0, 0), sy = getf(P, a[2], 1, 0), sz = getf(P, a[2], 2, 0);
+    int nd = ader(a[0]) ? 3 : 1;
+    for (int d = 0; d < nd; ++d) setf(P, a[0], d, getf(P, a[1], 0, d) * sx + getf(P, a[1], 1, d) * sy + getf(P, a[1], 2, d) * sz);
+}
+
 // noise (batched_llvm_gen.cpp:6032-6190 kinds; oslnoise.h wrappers)
 void op_noise(Point& P, const uint32_t* a) {
     uint32_t r = a[0], S = a[1], T = a[2], kw = a[3];
@@ -524,6 +644,43 @@ void op_noise(Point& P, const uint32_t* a) {
     } else {
         for (int c = 0; c < nc; ++c) res[c] = DF(0.0f);
     }
+    int rn = anc(r);
+    for (int c = 0; c < rn; ++c) putd(P, r, c, res[nc == 1 ? 0 : c]);
+}
+
+// gabor / pgabor (opnoise.cpp:484-640 forms; sfm_gabornoise.h:490-660).
+// a: r, S, T, kind word, anisotropic, direction, bandwidth; the carrier op
+// that follows holds impulses, do_filter, Speriod, Tperiod.
+void op_gabor(Point& P, const uint32_t* a, const uint32_t* b) {
+    uint32_t r = a[0], S = a[1], kw = a[3];
+    bool periodic = (kw & 16u) != 0;
+    int dims = (int)((kw >> 5) & 7u);
+    bool vec = (kw & 256u) != 0;
+    int ns = anc(S), nc = vec ? 3 : 1;
+    GaborOptions o;
+    o.anisotropic = geti(P, a[4], 0);
+    o.direction = V3(getf(P, a[5], 0, 0), getf(P, a[5], 1, 0), getf(P, a[5], 2, 0));
+    o.bandwidth = getf(P, a[6], 0, 0);
+    o.impulses = getf(P, b[0], 0, 0);
+    o.do_filter = geti(P, b[1], 0);
+    // position as Dual2<Vec3>: 1-D and 2-D slice to 3-D, the 4-D forms drop t
+    DV X;
+    if (ns == 3) {
+        for (int c = 0; c < 3; ++c) setcomp(X, c, getd(P, S, c));
+    } else {
+        setcomp(X, 0, getd(P, S, 0));
+        if (dims == 2) setcomp(X, 1, getd(P, a[2], 0));
+    }
+    V3 period(0.0f);
+    if (periodic) {
+        if (ns == 3) period = V3(getf(P, b[2], 0, 0), getf(P, b[2], 1, 0), getf(P, b[2], 2, 0));
+        else {
+            period.x = getf(P, b[2], 0, 0);
+            if (dims == 2) period.y = getf(P, b[3], 0, 0);
+        }
+    }
+    DF res[3];
+    gabor_eval<OwnMath>(o, X, periodic, period, nc, res);
     int rn = anc(r);
     for (int c = 0; c < rn; ++c) putd(P, r, c, res[nc == 1 ? 0 : c]);
 }
@@ -872,8 +1029,29 @@ struct Runner {
                 for (int c = 0; c < anc(a[0]); ++c) putv(P, a[0], c, getf(P, a[1], c, d));
                 break;
             }
-            case oslg::OP_TRANSFORM: op_transform(P, a); break;
+            case oslg::OP_TRANSFORM:
+                if (a[3] == 2u) op_transformn(P, a);
+                else op_transform(P, a);
+                break;
+            case oslg::OP_MDIV: op_mdiv(P, a); break;
+            case oslg::OP_TRANSPOSE: {
+                float M[16];
+                for (int i = 0; i < 16; ++i) M[i] = bitsf(word(P, a[1], i));
+                for (int i = 0; i < 4; ++i)
+                    for (int j = 0; j < 4; ++j) setf(P, a[0], i * 4 + j, M[j * 4 + i]);
+                break;
+            }
+            case oslg::OP_DETERMINANT: {
+                float M[16];
+                for (int i = 0; i < 16; ++i) M[i] = bitsf(word(P, a[1], i));
+                putv(P, a[0], 0, det4(M));
+                break;
+            }
+            case oslg::OP_AREA: op_area(P, a); break;
+            case oslg::OP_FILTERWIDTH: op_filterwidth(P, a); break;
+            case oslg::OP_LUMINANCE: op_luminance(P, a); break;
             case oslg::OP_NOISE: op_noise(P, a); break;
+            case oslg::OP_GABOR: op_gabor(P, a, prog.ops[pc + 1].a); break;
             case oslg::OP_HASH: op_hash(P, a); break;
             case oslg::OP_CLOSURE: {
                 // osl_allocate_(weighted_)closure_component (opclosure.cpp:83-117)
@@ -1130,6 +1308,30 @@ void oracle_noise(int kind, int dims, int vec, int derivs, int periodic, const f
     int nr = vec ? 3 : 1;
     for (int c = 0; c < nr; ++c)
         for (int d = 0; d < 3; ++d) out[c * 3 + d] = bitsf(P.heap[12 + d * nr + c]);
+}
+
+// Gabor of one Dual2<Vec3> position (in: val xyz, dx xyz, dy xyz) with the
+// executor's own exp/sincos (libm = 0) or libm's (libm = 1); out: nc x
+// (val, dx, dy).
+void oracle_gabor(int anisotropic, int do_filter, const float* direction, float bandwidth, float impulses,
+                  const float* in, int periodic, const float* period, int nc, int libm, float* out) {
+    GaborOptions o;
+    o.anisotropic = anisotropic;
+    o.do_filter = do_filter;
+    o.direction = V3(direction[0], direction[1], direction[2]);
+    o.bandwidth = bandwidth;
+    o.impulses = impulses;
+    DV X(V3(in[0], in[1], in[2]), V3(in[3], in[4], in[5]), V3(in[6], in[7], in[8]));
+    V3 per = period ? V3(period[0], period[1], period[2]) : V3(0.0f);
+    DF res[3];
+    if (libm) gabor_eval<LibmMath>(o, X, periodic != 0, per, nc, res);
+    else gabor_eval<OwnMath>(o, X, periodic != 0, per, nc, res);
+    for (int c = 0; c < nc; ++c) { out[c * 3] = res[c].v; out[c * 3 + 1] = res[c].dx; out[c * 3 + 2] = res[c].dy; }
+}
+// the executor's own exp and sincos over an array (accuracy tests)
+void oracle_own_exp(const float* x, int n, float* y) { for (int i = 0; i < n; ++i) y[i] = own_exp(x[i]); }
+void oracle_own_sincos(const float* x, int n, float* s, float* c) {
+    for (int i = 0; i < n; ++i) own_sincos(x[i], &s[i], &c[i]);
 }
 
 int oracle_hash_f(float x) { return hash_f(x); }

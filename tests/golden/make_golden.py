@@ -75,6 +75,11 @@ IMAGES = {
     "noise_cell": "testsuite/noise-cell/ref/out.tif",
     "noise_simplex": "testsuite/noise-simplex/ref/out.tif",
     "noise_gabor": "testsuite/noise-gabor/ref/out.tif",
+    "pnoise_gabor": "testsuite/pnoise-gabor/ref/out.tif",
+    "noise_gabor2d_filter": "testsuite/noise-gabor2d-filter/ref/out.tif",
+    "noise_gabor3d_filter": "testsuite/noise-gabor3d-filter/ref/out.tif",
+    "pnoise_perlin": "testsuite/pnoise-perlin/ref/out.tif",
+    "pnoise_cell": "testsuite/pnoise-cell/ref/out.tif",
 }
 
 

@@ -8,7 +8,8 @@ import pytest
 
 from helpers import (float_equal, golden_image, grid_globals, image_diff_ok, og, oracle_run, pixel_grid,
                      shaders, single_layer_group, to_uint8)
-from test_oracle_golden import TESTSUITE, deformer_expected, deformer_group, deformer_inputs, fmt_g3, suite_program
+from test_oracle_golden import (TESTSUITE, deformer_expected, deformer_group, deformer_inputs, fmt_g3, suite_P,
+                                suite_program)
 
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
@@ -93,11 +94,13 @@ def test_testsuite_shaders_match_oracle_and_golden(name, kw):
     ss, g = suite_program(name, kw)
     ref_img, W, H, step = golden_image(name)
     u, v = pixel_grid(W, H)
-    got = gpu_run(ss, g, W * H, device_grid_globals(u, v, W, H), 3)
+    P = suite_P(kw, u, v)
+    got = gpu_run(ss, g, W * H, device_grid_globals(u, v, W, H, P=P), 3)
     ref = np.zeros((W * H, 3), np.float32)
-    assert oracle_run(g.program_bytes(), W * H, grid_globals(u, v, W, H), ref) == 0
+    assert oracle_run(g.program_bytes(), W * H, grid_globals(u, v, W, H, P=P), ref) == 0
     assert_same(got, ref)
-    ok, frac, mx = image_diff_ok(to_uint8(got.reshape(H, W, 3))[::step, ::step], ref_img)
+    ok, frac, mx = image_diff_ok(to_uint8(got.reshape(H, W, 3))[::step, ::step], ref_img,
+                                 failpercent=kw.get("failpercent", 0.02))
     assert ok, (frac, mx)
 
 
@@ -157,3 +160,30 @@ def test_layered_closure_group_matches_oracle(heap):
     assert oracle_run(g.program_bytes(), W * H, workloads.c2_globals(og.make_globals, u, v, I), ref) == 0
     int_cols = [0] + [1 + 16 * k for k in range(workloads.C2_CLOSURE_RECORDS)] + [5 + 16]  # counts, ids, dist hash
     assert_same(got, ref, int_cols=tuple(int_cols))
+
+
+@pytest.mark.parametrize("opts", [dict(anisotropic=0, bandwidth=1.0), dict(anisotropic=1, direction=(2.0, 0.5, 0.0)),
+                                  dict(anisotropic=2, direction=(1.5, 1.0, 0.25), impulses=8.0),
+                                  dict(do_filter=0, bandwidth=4.0)])
+def test_gabor_options_match_oracle(opts):
+    ss = og.ShadingSystem()
+    g = single_layer_group(ss, "tgo", shaders.gabor_options(**opts),
+                           outputs=[og.SymLocationDesc("Cout", og.TypeColor, False, og.SymArenaOutputs, 0, 12)])
+    W = H = 128
+    u, v = pixel_grid(W, H, centers=True)
+    got = gpu_run(ss, g, W * H, device_grid_globals(u, v, W, H, centers=True), 3)
+    ref = np.zeros((W * H, 3), np.float32)
+    assert oracle_run(g.program_bytes(), W * H, grid_globals(u, v, W, H, centers=True), ref) == 0
+    assert_same(got, ref)
+
+
+def test_matrix_ops_match_oracle():
+    from test_matrix_ops import REC, inputs, matrix_group
+    ss = og.ShadingSystem()
+    g, _, _ = matrix_group(ss)
+    W = H = 64
+    u, v, P = inputs(W, H)
+    got = gpu_run(ss, g, W * H, device_grid_globals(u, v, W, H, centers=True, P=P), REC)
+    ref = np.zeros((W * H, REC), np.float32)
+    assert oracle_run(g.program_bytes(), W * H, grid_globals(u, v, W, H, P=P, centers=True), ref) == 0
+    assert_same(got, ref)

@@ -150,15 +150,36 @@ TESTSUITE = [
     ("noise_perlin", dict(noisename_default="perlin")),
     ("noise_cell", dict(noisename_default="cell", offset_default=0.0, scale_default=1.0)),
     ("noise_simplex", dict(noisename_default="simplex")),
+    ("noise_gabor", dict(noisename_default="gabor", failpercent=0.05)),
+    ("pnoise_perlin", dict(builder="testpnoise", noisename_default="perlin")),
+    ("pnoise_cell", dict(builder="testpnoise", noisename_default="cell", offset_default=0.0, scale_default=1.0)),
+    ("pnoise_gabor", dict(builder="testpnoise", noisename_default="gabor", failpercent=0.05)),
+    ("noise_gabor2d_filter", dict(builder="gabor_filter", dims=2, failpercent=0.05)),
+    ("noise_gabor3d_filter", dict(builder="gabor_filter", dims=3, failpercent=0.05)),
 ]
 
 
 def suite_program(name, kw):
+    kw = dict(kw)
+    builder = kw.pop("builder", "testnoise")
+    kw.pop("failpercent", None)
     ss = og.ShadingSystem()
-    oso = shaders.testnoise(shader_name="t_" + name, **kw)
+    if builder == "gabor_filter":
+        oso = shaders.gabor_filter_test(kw["dims"], shader_name="t_" + name)
+    elif builder == "testpnoise":
+        oso = shaders.testpnoise(shader_name="t_" + name, **kw)
+    else:
+        oso = shaders.testnoise(shader_name="t_" + name, **kw)
     g = single_layer_group(ss, "t_" + name, oso,
                            outputs=[og.SymLocationDesc("Cout", og.TypeColor, False, og.SymArenaOutputs, 0, 12)])
     return ss, g
+
+
+def suite_P(kw, u, v):
+    """testshade's P = (u, v, 1) for the shaders that read P, else None."""
+    if kw.get("builder") != "gabor_filter":
+        return None
+    return np.stack([u, v, np.ones_like(u)]).astype(np.float32)
 
 
 @pytest.mark.parametrize("name,kw", TESTSUITE)
@@ -167,13 +188,13 @@ def test_oracle_matches_testsuite_images(name, kw):
     blob = g.program_bytes()
     ref, W, H, step = golden_image(name)
     u, v = pixel_grid(W, H)
-    G = grid_globals(u, v, W, H)
+    G = grid_globals(u, v, W, H, P=suite_P(kw, u, v))
     out = np.zeros((W * H, 3), np.float32)
     assert oracle_run(blob, W * H, G, out) == 0
     img = to_uint8(out.reshape(H, W, 3))[::step, ::step]
-    ok, frac, mx = image_diff_ok(img, ref)
+    ok, frac, mx = image_diff_ok(img, ref, failpercent=kw.get("failpercent", 0.02))
     assert ok, (name, frac, mx)
-    # in practice the oracle reproduces every sampled pixel exactly
+    # in practice the oracle reproduces every sampled pixel to within 1/255
     assert frac == 0.0
 
 
