@@ -205,6 +205,46 @@ int oslg_execute_batch_noalloc(oslg_system* sys, oslg_group* group, int64_t npoi
                                const oslg_shaderglobals* globals, void* userdata_base,
                                void* output_base, void* stream, uint32_t* status_out);
 
+/* ---- persistent batch executor --------------------------------------------
+ * No counterpart in the reference: its renderers call execute() once per
+ * group and batch (src/liboslexec/shadingsys.cpp:329-394, the loop in
+ * src/testshade/testshade.cpp:1864-1881). A batch collects requests of many
+ * groups (each with the same arguments as oslg_execute_batch) and runs them
+ * all in one persistent kernel launch that takes (group, tile) work items
+ * from a device counter, heaviest groups first. The step is captured as a
+ * CUDA graph on first execute and replayed while the batch is unchanged.
+ * Results are identical to one oslg_execute_batch call per request. The
+ * caller keeps every globals/userdata/output buffer alive and in place until
+ * the batch is cleared or destroyed; requests must not overlap in output. */
+typedef struct oslg_batch oslg_batch;
+
+typedef struct oslg_batch_tuning {
+    int block;       /* threads per CTA = points per work item */
+    int heap_smem;   /* 1 symbol heap in shared memory, 0 in HBM */
+    int grid;        /* persistent CTAs */
+    int ctas_per_sm; /* resident CTAs per SM for this shape */
+    float ms;        /* measured milliseconds per launch (autotune only) */
+} oslg_batch_tuning;
+
+int oslg_batch_create(oslg_system* sys, oslg_batch** out);
+int oslg_batch_destroy(oslg_batch* batch);
+/* Drop all requests (device tables are kept for reuse). */
+int oslg_batch_clear(oslg_batch* batch);
+/* Append one request; lowers and uploads the group on first use. */
+int oslg_batch_add(oslg_batch* batch, oslg_group* group, int64_t npoints, const oslg_shaderglobals* globals,
+                   void* userdata_base, void* output_base);
+/* block 0 keeps the current size; heap_smem -1 auto; use_graph 0/1. */
+int oslg_batch_set_launch(oslg_batch* batch, int block, int heap_smem, int use_graph);
+/* Enqueue every request on `stream` (asynchronous). */
+int oslg_batch_execute(oslg_batch* batch, void* stream);
+/* Time `reps` launches of each block size {128, 256, 512} x heap placement
+ * {shared, HBM} that fits, keep the fastest for later executes. Writes up
+ * to `cap` measured candidates to `results` and their count to `n`. */
+int oslg_batch_autotune(oslg_batch* batch, void* stream, int reps, oslg_batch_tuning* results, int cap, int* n,
+                        oslg_batch_tuning* best);
+/* Launch shape of the last built batch. */
+int oslg_batch_last_launch(oslg_batch* batch, oslg_batch_tuning* out);
+
 #ifdef __cplusplus
 }
 #endif

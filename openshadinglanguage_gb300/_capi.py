@@ -45,6 +45,11 @@ GLOBAL_FIELDS = ["P", "dPdx", "dPdy", "dPdz", "I", "dIdx", "dIdy", "N", "Ng", "u
                  "dPsdy", "surfacearea"]
 
 
+class BatchTuningC(ctypes.Structure):
+    _fields_ = [("block", ctypes.c_int), ("heap_smem", ctypes.c_int), ("grid", ctypes.c_int),
+                ("ctas_per_sm", ctypes.c_int), ("ms", ctypes.c_float)]
+
+
 class ShaderGlobalsC(ctypes.Structure):
     _fields_ = [(n, FieldC) for n in GLOBAL_FIELDS]
 
@@ -85,6 +90,16 @@ _EXPORTS = {
                                                   ctypes.POINTER(ShaderGlobalsC), ctypes.c_void_p,
                                                   ctypes.c_void_p, ctypes.c_void_p,
                                                   ctypes.POINTER(ctypes.c_uint32)]),
+    "oslg_batch_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
+    "oslg_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "oslg_batch_clear": (ctypes.c_int, [ctypes.c_void_p]),
+    "oslg_batch_add": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ShaderGlobalsC),
+                                      ctypes.c_void_p, ctypes.c_void_p]),
+    "oslg_batch_set_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "oslg_batch_execute": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "oslg_batch_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(BatchTuningC),
+                                           ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(BatchTuningC)]),
+    "oslg_batch_last_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BatchTuningC)]),
 }
 
 _lib = None

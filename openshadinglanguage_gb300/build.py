@@ -21,8 +21,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST_SOURCES = ["oslg_oso.cpp", "oslg_lower.cpp", "oslg_capi.cpp"]
 # (source, object name, extra flags): the interpreter is compiled once per
 # feature tier (oslg_tier.cu with -DOSLG_TIER=N), in parallel
-CUDA_SOURCES = [("oslg_kernels.cu", "oslg_kernels", [])] + [
-    ("oslg_tier.cu", "oslg_tier%d" % t, ["-DOSLG_TIER=%d" % t]) for t in range(8)]
+CUDA_SOURCES = [("oslg_kernels.cu", "oslg_kernels", []), ("oslg_batch_host.cu", "oslg_batch_host", [])] + [
+    ("oslg_tier.cu", "oslg_tier%d" % t, ["-DOSLG_TIER=%d" % t]) for t in range(8)] + [
+    ("oslg_batch.cu", "oslg_batch%d" % m, ["-DOSLG_BATCH_MAXT=%d" % m]) for m in (256, 512)]
 
 
 def _run(cmd):

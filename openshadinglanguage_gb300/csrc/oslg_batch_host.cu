@@ -1,0 +1,361 @@
+// Host side of the persistent batch executor: job table and work list,
+// launch-shape choice, CUDA-graph capture and replay, and the autotuner.
+//
+// A batch holds requests (group, point count, globals, arenas) of many
+// different groups. One launch of batch_kernel runs all of them: the work
+// list has one item per (job, tile of `block` points), jobs ordered by
+// their estimated cost per point, heaviest first, so that long tiles start
+// early and short ones fill the tail. The whole step (counter reset +
+// launch) is captured once as a CUDA graph and replayed while the batch is
+// unchanged. The reference runs groups one execute() call at a time
+// (src/liboslexec/shadingsys.cpp:329-394); nothing in it corresponds to
+// this layer.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "oslg_batch.h"
+
+namespace oslg {
+
+int batch_launch_256(bool, unsigned, unsigned, size_t, void*, const dev::BatchArgs&);
+int batch_launch_512(bool, unsigned, unsigned, size_t, void*, const dev::BatchArgs&);
+int batch_occupancy_256(bool, int, size_t, int*);
+int batch_occupancy_512(bool, int, size_t, int*);
+int batch_smem_limit_256(int);
+int batch_smem_limit_512(int);
+
+namespace {
+const size_t kBatchStaticSmem = 256;
+bool ok(cudaError_t e, std::string* err, const char* what) {
+    if (e == cudaSuccess) return true;
+    if (err) *err = std::string(what) + ": " + cudaGetErrorString(e);
+    return false;
+}
+int launch_batch(bool smem, int maxt, unsigned grid, unsigned block, size_t shmem, void* stream,
+                 const dev::BatchArgs& b) {
+    return maxt > 256 ? batch_launch_512(smem, grid, block, shmem, stream, b)
+                      : batch_launch_256(smem, grid, block, shmem, stream, b);
+}
+int occupancy_batch(bool smem, int maxt, int block, size_t shmem, int* per_sm) {
+    return maxt > 256 ? batch_occupancy_512(smem, block, shmem, per_sm)
+                      : batch_occupancy_256(smem, block, shmem, per_sm);
+}
+}  // namespace
+
+// Estimated cost of one point of a program: one unit per op, noise and
+// transcendental ops weighted by their measured relative cost, ops inside
+// loops by an expected trip count of 8 per nesting level.
+double program_cost(const ProgramHeader& hdr, const Op* ops) {
+    double cost = 0.0, mult = 1.0;
+    for (uint32_t i = 0; i < hdr.nops; ++i) {
+        const Op& o = ops[i];
+        double w = 1.0;
+        switch (o.code) {
+        case OP_LOOP_BEGIN: mult *= 8.0; break;
+        case OP_LOOP_END: mult = std::max(1.0, mult / 8.0); break;
+        case OP_GABOR: w = (o.a[3] & 256u) ? 600.0 : 200.0; break;
+        case OP_NOISE: {
+            uint32_t kind = o.a[3] & 15u;
+            bool vec = (o.a[3] & 256u) != 0, der = (o.a[3] & 512u) != 0;
+            w = (kind == NK_CELL || kind == NK_HASH) ? 3.0 : (kind == NK_SIMPLEX || kind == NK_USIMPLEX) ? 6.0 : 7.0;
+            if (vec) w *= 2.5;
+            if (der) w *= 2.0;
+            break;
+        }
+        case OP_SIN: case OP_COS: case OP_TAN: case OP_EXP: case OP_LOG: case OP_POW: case OP_ATAN2:
+            w = 12.0;
+            break;
+        case OP_TRANSFORM: case OP_MDIV: w = 3.0; break;
+        default: break;
+        }
+        cost += w * mult;
+    }
+    return cost;
+}
+
+BatchExecutor::~BatchExecutor() { release(); }
+
+void BatchExecutor::release() {
+    if (gexec_) cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(gexec_));
+    if (graph_) cudaGraphDestroy(static_cast<cudaGraph_t>(graph_));
+    if (cap_stream_) cudaStreamDestroy(static_cast<cudaStream_t>(cap_stream_));
+    gexec_ = graph_ = cap_stream_ = nullptr;
+    cudaFree(d_jobs_);
+    cudaFree(d_items_);
+    cudaFree(d_counter_);
+    cudaFree(d_heap_);
+    d_jobs_ = nullptr;
+    d_items_ = nullptr;
+    d_counter_ = nullptr;
+    d_heap_ = nullptr;
+    jobs_cap_ = items_cap_ = heap_bytes_ = 0;
+}
+
+void BatchExecutor::clear() {
+    entries_.clear();
+    dirty_ = true;
+}
+
+void BatchExecutor::add(const CompiledGroup& cg, int64_t npoints, const oslg_shaderglobals& G, void* userdata,
+                        void* outputs) {
+    BatchEntry e;
+    e.cg = &cg;
+    e.npoints = npoints;
+    e.G = G;
+    e.userdata = userdata;
+    e.outputs = outputs;
+    e.cost = program_cost(cg.header, reinterpret_cast<const Op*>(cg.blob.data() + sizeof(ProgramHeader)));
+    entries_.push_back(e);
+    dirty_ = true;
+}
+
+void BatchExecutor::set_launch(const BatchLaunch& l) {
+    want_ = l;
+    dirty_ = true;
+}
+
+int BatchExecutor::ensure_ready(DeviceState& ds, std::string* err) {
+    if (!ds_ready_) {
+        // dynamic shared memory may use the opt-in size less the kernel's
+        // static work-item slot (kBatchStaticSmem covers it)
+        int dyn = (int)ds.smem_optin - (int)kBatchStaticSmem;
+        if (!ok((cudaError_t)batch_smem_limit_256(dyn), err, "batch kernel attribute")) return OSLG_ERR_CUDA;
+        if (!ok((cudaError_t)batch_smem_limit_512(dyn), err, "batch kernel attribute")) return OSLG_ERR_CUDA;
+        if (!ok(cudaMalloc(&d_counter_, sizeof(uint32_t)), err, "cudaMalloc counter")) return OSLG_ERR_CUDA;
+        ds_ready_ = true;
+    }
+    return OSLG_OK;
+}
+
+// Work list, job table, heap and launch shape for the requested launch.
+int BatchExecutor::build(DeviceState& ds, std::string* err) {
+    int rc = ensure_ready(ds, err);
+    if (rc != OSLG_OK) return rc;
+    BatchLaunch L = want_;
+    int block = L.block > 0 ? L.block : 256;
+    block = std::max(32, std::min(512, (block + 31) & ~31));
+    const int maxt = block > 256 ? 512 : 256;
+    uint32_t prog_bytes = 0, slots = 0;
+    for (const BatchEntry& e : entries_) {
+        const ProgramHeader& h = e.cg->header;
+        uint32_t pb = h.nops * (uint32_t)sizeof(Op) + ((h.nconst + 3u) & ~3u) * 4u;
+        prog_bytes = std::max(prog_bytes, pb);
+        slots = std::max(slots, h.heap_slots);
+    }
+    prog_bytes = (prog_bytes + 15u) & ~15u;
+    const size_t heap_b = (size_t)slots * block * sizeof(float);
+    bool smem = L.heap_smem == 1 || (L.heap_smem < 0 && prog_bytes + heap_b <= 100 * 1024);
+    if (smem && prog_bytes + heap_b + kBatchStaticSmem > ds.smem_optin) smem = false;
+    const size_t shmem = prog_bytes + (smem ? heap_b : 0);
+    if (shmem + kBatchStaticSmem > ds.smem_optin) {
+        if (err) *err = "batch programs do not fit in shared memory";
+        return OSLG_ERR_LOWER;
+    }
+    int per_sm = 0;
+    if (!ok((cudaError_t)occupancy_batch(smem, maxt, block, shmem, &per_sm), err, "occupancy")) return OSLG_ERR_CUDA;
+    if (per_sm < 1) {
+        if (err) *err = "batch launch shape does not fit on an SM";
+        return OSLG_ERR_LOWER;
+    }
+    int grid = ds.sm_count * per_sm;
+    if (L.grid > 0) grid = L.grid;
+
+    // jobs by estimated cost per point, heaviest first; ties keep insertion order
+    std::vector<int> order(entries_.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return entries_[a].cost > entries_[b].cost; });
+    std::vector<dev::BatchJob> jobs(entries_.size());
+    std::vector<uint2> items;
+    for (size_t j = 0; j < order.size(); ++j) {
+        const BatchEntry& e = entries_[order[j]];
+        dev::BatchJob& J = jobs[j];
+        J.blob = static_cast<const uint8_t*>(e.cg->d_blob);
+        J.npoints = e.npoints;
+        J.userdata = static_cast<char*>(e.userdata);
+        J.outputs = static_cast<char*>(e.outputs);
+        J.G = e.G;
+        const int64_t tiles = (e.npoints + block - 1) / block;
+        for (int64_t t = 0; t < tiles; ++t) items.push_back(make_uint2((unsigned)j, (unsigned)t));
+    }
+    if (jobs.size() > jobs_cap_) {
+        cudaFree(d_jobs_);
+        d_jobs_ = nullptr;
+        if (!ok(cudaMalloc(&d_jobs_, jobs.size() * sizeof(dev::BatchJob)), err, "cudaMalloc jobs")) return OSLG_ERR_CUDA;
+        jobs_cap_ = jobs.size();
+    }
+    if (items.size() > items_cap_) {
+        cudaFree(d_items_);
+        d_items_ = nullptr;
+        if (!ok(cudaMalloc(&d_items_, items.size() * sizeof(uint2)), err, "cudaMalloc items")) return OSLG_ERR_CUDA;
+        items_cap_ = items.size();
+    }
+    if (!jobs.empty() &&
+        !ok(cudaMemcpy(d_jobs_, jobs.data(), jobs.size() * sizeof(dev::BatchJob), cudaMemcpyHostToDevice), err,
+            "upload jobs"))
+        return OSLG_ERR_CUDA;
+    if (!items.empty() &&
+        !ok(cudaMemcpy(d_items_, items.data(), items.size() * sizeof(uint2), cudaMemcpyHostToDevice), err,
+            "upload items"))
+        return OSLG_ERR_CUDA;
+    if (!smem) {
+        size_t need = (size_t)grid * heap_b;
+        if (need > heap_bytes_) {
+            cudaFree(d_heap_);
+            d_heap_ = nullptr;
+            heap_bytes_ = 0;
+            if (!ok(cudaMalloc(&d_heap_, need), err, "cudaMalloc batch heap")) return OSLG_ERR_CUDA;
+            heap_bytes_ = need;
+        }
+    }
+    args_.jobs = d_jobs_;
+    args_.items = d_items_;
+    args_.nitems = (uint32_t)items.size();
+    args_.counter = d_counter_;
+    args_.gheap = smem ? nullptr : d_heap_;
+    args_.status = ds.d_status;
+    args_.prog_bytes = prog_bytes;
+    args_.heap_slots = slots;
+    cur_.block = block;
+    cur_.heap_smem = smem ? 1 : 0;
+    cur_.grid = grid;
+    cur_.use_graph = L.use_graph;
+    shmem_ = shmem;
+    maxt_ = maxt;
+    per_sm_ = per_sm;
+    // any captured graph refers to the old tables
+    if (gexec_) cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(gexec_));
+    if (graph_) cudaGraphDestroy(static_cast<cudaGraph_t>(graph_));
+    gexec_ = graph_ = nullptr;
+    dirty_ = false;
+    return OSLG_OK;
+}
+
+int BatchExecutor::enqueue(void* stream, std::string* err) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (!ok(cudaMemsetAsync(d_counter_, 0, sizeof(uint32_t), s), err, "counter reset")) return OSLG_ERR_CUDA;
+    if (args_.nitems == 0) return OSLG_OK;
+    if (!ok((cudaError_t)launch_batch(cur_.heap_smem == 1, maxt_, (unsigned)cur_.grid, (unsigned)cur_.block, shmem_,
+                                      stream, args_),
+            err, "batch launch"))
+        return OSLG_ERR_CUDA;
+    return OSLG_OK;
+}
+
+int BatchExecutor::execute(DeviceState& ds, void* stream, std::string* err) {
+    if (dirty_) {
+        int rc = build(ds, err);
+        if (rc != OSLG_OK) return rc;
+    }
+    if (!cur_.use_graph) return enqueue(stream, err);
+    if (!gexec_) {
+        // capture on a private stream (the caller's may be the legacy default
+        // stream, which cannot be captured); the graph replays on any stream
+        if (!cap_stream_) {
+            cudaStream_t cs;
+            if (!ok(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), err, "capture stream")) return OSLG_ERR_CUDA;
+            cap_stream_ = cs;
+        }
+        cudaStream_t cs = static_cast<cudaStream_t>(cap_stream_);
+        if (!ok(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), err, "begin capture")) return OSLG_ERR_CUDA;
+        std::string e2;
+        int rc = enqueue(cs, &e2);
+        cudaGraph_t g = nullptr;
+        cudaError_t ce = cudaStreamEndCapture(cs, &g);
+        if (rc != OSLG_OK) {
+            if (g) cudaGraphDestroy(g);
+            if (err) *err = e2;
+            return rc;
+        }
+        if (!ok(ce, err, "end capture")) return OSLG_ERR_CUDA;
+        cudaGraphExec_t ge = nullptr;
+        if (!ok(cudaGraphInstantiate(&ge, g, 0), err, "graph instantiate")) {
+            cudaGraphDestroy(g);
+            return OSLG_ERR_CUDA;
+        }
+        graph_ = g;
+        gexec_ = ge;
+    }
+    if (!ok(cudaGraphLaunch(static_cast<cudaGraphExec_t>(gexec_), static_cast<cudaStream_t>(stream)), err,
+            "graph launch"))
+        return OSLG_ERR_CUDA;
+    return OSLG_OK;
+}
+
+// Sweep block size x heap placement, timing `reps` launches of each with
+// CUDA events on the caller's stream; keep the fastest. Candidates whose
+// shared-memory heap does not fit are skipped.
+int BatchExecutor::autotune(DeviceState& ds, void* stream, int reps, BatchTuneResult* results, int cap, int* n,
+                            BatchLaunch* best, std::string* err) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const BatchLaunch keep = want_;
+    float best_ms = 1e30f;
+    BatchLaunch best_l = keep;
+    int count = 0;
+    cudaEvent_t e0, e1;
+    if (!ok(cudaEventCreate(&e0), err, "event")) return OSLG_ERR_CUDA;
+    if (!ok(cudaEventCreate(&e1), err, "event")) {
+        cudaEventDestroy(e0);
+        return OSLG_ERR_CUDA;
+    }
+    int rc = OSLG_OK;
+    for (int block : { 128, 256, 512 }) {
+        for (int heap : { 1, 0 }) {
+            BatchLaunch l = keep;
+            l.block = block;
+            l.heap_smem = heap;
+            l.use_graph = 0;
+            want_ = l;
+            dirty_ = true;
+            std::string e2;
+            int r2 = build(ds, &e2);
+            if (r2 != OSLG_OK || cur_.heap_smem != heap) continue;  // does not fit: skip
+            if ((rc = enqueue(stream, err)) != OSLG_OK) break;      // warm-up
+            if (!ok(cudaEventRecord(e0, s), err, "event record")) { rc = OSLG_ERR_CUDA; break; }
+            for (int r = 0; r < std::max(1, reps) && rc == OSLG_OK; ++r) rc = enqueue(stream, err);
+            if (rc != OSLG_OK) break;
+            if (!ok(cudaEventRecord(e1, s), err, "event record") || !ok(cudaEventSynchronize(e1), err, "event sync")) {
+                rc = OSLG_ERR_CUDA;
+                break;
+            }
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            ms /= (float)std::max(1, reps);
+            if (results && count < cap) {
+                results[count].block = cur_.block;
+                results[count].heap_smem = cur_.heap_smem;
+                results[count].grid = cur_.grid;
+                results[count].ctas_per_sm = per_sm_;
+                results[count].ms = ms;
+            }
+            ++count;
+            if (ms < best_ms) {
+                best_ms = ms;
+                best_l = l;
+            }
+        }
+        if (rc != OSLG_OK) break;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (n) *n = count;
+    best_l.use_graph = keep.use_graph;
+    want_ = best_l;
+    dirty_ = true;
+    if (best) *best = best_l;
+    return rc;
+}
+
+void BatchExecutor::last_launch(BatchTuneResult* r) const {
+    r->block = cur_.block;
+    r->heap_smem = cur_.heap_smem;
+    r->grid = cur_.grid;
+    r->ctas_per_sm = per_sm_;
+    r->ms = 0.0f;
+}
+
+}  // namespace oslg

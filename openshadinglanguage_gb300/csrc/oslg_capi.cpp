@@ -8,6 +8,7 @@
 #include <new>
 
 #include "../../include/oslg.h"
+#include "oslg_batch.h"
 #include "oslg_exec.h"
 #include "oslg_host.h"
 
@@ -21,6 +22,11 @@ struct oslg_system {
 
 struct oslg_group {
     oslg::ShaderGroup g;
+};
+
+struct oslg_batch {
+    oslg_system* sys;
+    oslg::BatchExecutor ex;
 };
 
 namespace oslg {
@@ -424,3 +430,103 @@ int oslg_execute_batch_noalloc(oslg_system* sys, oslg_group* group, int64_t npoi
 }
 
 }  // extern "C"
+
+// ---- persistent batch executor ----------------------------------------------------
+int oslg_batch_create(oslg_system* sys, oslg_batch** out) {
+    if (!sys || !out) return OSLG_ERR_ARG;
+    return guarded(sys, [&]() {
+        oslg_batch* b = new oslg_batch;
+        b->sys = sys;
+        *out = b;
+        return OSLG_OK;
+    });
+}
+
+int oslg_batch_destroy(oslg_batch* batch) {
+    delete batch;
+    return OSLG_OK;
+}
+
+int oslg_batch_clear(oslg_batch* batch) {
+    if (!batch) return OSLG_ERR_ARG;
+    batch->ex.clear();
+    return OSLG_OK;
+}
+
+int oslg_batch_add(oslg_batch* batch, oslg_group* group, int64_t npoints, const oslg_shaderglobals* globals,
+                   void* userdata_base, void* output_base) {
+    if (!batch || !group || !globals || npoints < 0) return OSLG_ERR_ARG;
+    oslg_system* sys = batch->sys;
+    return guarded(sys, [&]() {
+        int rc = ensure_compiled(sys, group, true);
+        if (rc != OSLG_OK) return rc;
+        if (npoints == 0) return OSLG_OK;
+        batch->ex.add(*group->g.compiled, npoints, *globals, userdata_base, output_base);
+        return OSLG_OK;
+    });
+}
+
+int oslg_batch_set_launch(oslg_batch* batch, int block, int heap_smem, int use_graph) {
+    if (!batch || block < 0 || block > 512 || heap_smem < -1 || heap_smem > 1) return OSLG_ERR_ARG;
+    BatchLaunch l;
+    BatchTuneResult cur;
+    batch->ex.last_launch(&cur);
+    l.block = block > 0 ? block : (cur.block > 0 ? cur.block : 256);
+    l.heap_smem = heap_smem;
+    l.use_graph = use_graph ? 1 : 0;
+    batch->ex.set_launch(l);
+    return OSLG_OK;
+}
+
+int oslg_batch_execute(oslg_batch* batch, void* stream) {
+    if (!batch) return OSLG_ERR_ARG;
+    oslg_system* sys = batch->sys;
+    return guarded(sys, [&]() {
+        std::string err;
+        int rc = device_init(sys->dev, &err);
+        if (rc != OSLG_OK) return fail(sys, rc, err);
+        rc = batch->ex.execute(sys->dev, stream, &err);
+        if (rc != OSLG_OK) return fail(sys, rc, err);
+        return OSLG_OK;
+    });
+}
+
+static void to_c(const BatchTuneResult& r, oslg_batch_tuning* o) {
+    o->block = r.block;
+    o->heap_smem = r.heap_smem;
+    o->grid = r.grid;
+    o->ctas_per_sm = r.ctas_per_sm;
+    o->ms = r.ms;
+}
+
+int oslg_batch_autotune(oslg_batch* batch, void* stream, int reps, oslg_batch_tuning* results, int cap, int* n,
+                        oslg_batch_tuning* best) {
+    if (!batch || cap < 0) return OSLG_ERR_ARG;
+    oslg_system* sys = batch->sys;
+    return guarded(sys, [&]() {
+        std::string err;
+        int rc = device_init(sys->dev, &err);
+        if (rc != OSLG_OK) return fail(sys, rc, err);
+        std::vector<BatchTuneResult> res((size_t)std::max(cap, 8));
+        int cnt = 0;
+        BatchLaunch bl;
+        rc = batch->ex.autotune(sys->dev, stream, reps, res.data(), (int)res.size(), &cnt, &bl, &err);
+        if (rc != OSLG_OK) return fail(sys, rc, err);
+        if (n) *n = std::min(cnt, cap);
+        for (int i = 0; i < std::min(cnt, cap) && results; ++i) to_c(res[i], &results[i]);
+        if (best) {
+            float bm = 1e30f;
+            for (int i = 0; i < std::min(cnt, (int)res.size()); ++i)
+                if (res[i].ms < bm) { bm = res[i].ms; to_c(res[i], best); }
+        }
+        return OSLG_OK;
+    });
+}
+
+int oslg_batch_last_launch(oslg_batch* batch, oslg_batch_tuning* out) {
+    if (!batch || !out) return OSLG_ERR_ARG;
+    BatchTuneResult r;
+    batch->ex.last_launch(&r);
+    to_c(r, out);
+    return OSLG_OK;
+}

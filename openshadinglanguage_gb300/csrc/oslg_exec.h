@@ -2,6 +2,9 @@
 #pragma once
 #include <cstdint>
 #include <string>
+#include <vector>
+
+#include <vector_types.h>
 
 #include "../../include/oslg.h"
 #include "oslg_program.h"
@@ -19,6 +22,27 @@ struct KArgs {
     uint32_t* status;
     oslg_shaderglobals G;
 };
+
+// One group's request inside a persistent batch launch.
+struct BatchJob {
+    const uint8_t* blob;  // lowered program (device)
+    int64_t npoints;
+    char* userdata;
+    char* outputs;
+    oslg_shaderglobals G;
+};
+// Arguments of the persistent batch kernel: items are (job, tile) pairs,
+// taken in order through *counter (reset to 0 before every launch).
+struct BatchArgs {
+    const BatchJob* jobs;
+    const uint2* items;
+    uint32_t nitems;
+    uint32_t* counter;
+    float* gheap;          // HBM heap: heap_slots x block floats per CTA
+    uint32_t* status;
+    uint32_t prog_bytes;   // shared-memory bytes reserved for the largest program
+    uint32_t heap_slots;   // largest heap of any job (floats per point)
+};
 }  // namespace dev
 
 // One interpreter instantiation per feature tier (oslg_tier.cu compiled with
@@ -30,6 +54,16 @@ struct TierFns {
     int (*set_smem_limit)(int bytes);
 };
 const TierFns& tier_fns(int tier);
+
+// Persistent batch kernels (oslg_batch.cu): every op family, heap in shared
+// memory or HBM, launch bounds of 256 or 512 threads.
+struct BatchFns {
+    int (*launch)(bool smem_heap, int maxt, unsigned grid, unsigned block, size_t shmem, void* stream,
+                  const dev::BatchArgs& b);
+    int (*occupancy)(bool smem_heap, int maxt, int block, size_t shmem, int* per_sm);
+    int (*set_smem_limit)(int bytes);
+};
+const BatchFns& batch_fns();
 
 struct LaunchConfig {
     int block = 0;             // threads per CTA (0: chosen from the heap size)

@@ -1442,11 +1442,276 @@ static const long long kMaxBackEdges = 1ll << 24;
     if constexpr ((TIER & (bit)) != 0) {          \
         stmt;                                     \
     } else {                                      \
-        raise_status(k.status, ST_BAD_OPCODE);    \
+        raise_status(R.status, ST_BAD_OPCODE);    \
     }
 
+// Everything a program run needs besides the lane: the staged op stream,
+// closure pools and the caller's arenas.
+struct RunCtx {
+    const Op* sops;
+    int nops;
+    ClosurePools CP;
+    bool uses_closures;
+    const oslg_shaderglobals* G;
+    char* userdata;
+    char* outputs;
+    uint32_t* status;
+};
+
+// Run the whole program for one point per thread (L.pt; lanes past npoints
+// take part in the warp-uniform walk with no active bits).
+template <int TIER>
+__device__ __forceinline__ void run_tile(const RunCtx& R, Lane& L, int64_t npoints) {
+    const bool valid = L.pt < npoints;
+    bool act = valid, ext = false, lret = false;
+    uint32_t stk = 0, cnd = 0, brk = 0, cnt = 0;
+    long long backedges = 0;
+    if (R.uses_closures && valid) hsetu(L, R.CP.base, 0u);
+    int pc = 0;
+    while (pc < R.nops) {
+        const uint4* ow = reinterpret_cast<const uint4*>(R.sops + pc);
+        const uint4 w0 = ow[0], w1 = ow[1];
+        const uint32_t code = w0.x & 0xFFFFu;
+        const uint32_t a[7] = { w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w };
+        switch (code) {
+        case OP_NOP: break;
+        case OP_IF: {
+            int d = (int)a[1];
+            bool c = act && truth(L, a[0]);
+            stk = setbit(stk, d, act);
+            cnd = setbit(cnd, d, c);
+            act = c;
+            if (!__any_sync(FULL, act)) { pc = (int)a[2]; continue; }
+            break;
+        }
+        case OP_ELSE: {
+            int d = (int)a[1];
+            int ll = (int)a[3];
+            bool off = ext || lret || (ll && (bit(brk, ll - 1) || bit(cnt, ll - 1)));
+            act = bit(stk, d) && !bit(cnd, d) && !off;
+            if (!__any_sync(FULL, act)) { pc = (int)a[2]; continue; }
+            break;
+        }
+        case OP_ENDIF: {
+            int d = (int)a[1];
+            int ll = (int)a[3];
+            bool off = ext || lret || (ll && (bit(brk, ll - 1) || bit(cnt, ll - 1)));
+            act = bit(stk, d) && !off;
+            break;
+        }
+        case OP_LOOP_BEGIN: {
+            int d = (int)a[1];
+            int ll = (int)a[3];
+            stk = setbit(stk, d, act);
+            brk = setbit(brk, ll - 1, false);
+            cnt = setbit(cnt, ll - 1, false);
+            break;
+        }
+        case OP_LOOP_TEST: {
+            act = act && truth(L, a[0]);
+            if (!__any_sync(FULL, act)) { pc = (int)a[2]; continue; }
+            break;
+        }
+        case OP_LOOP_STEP: {
+            int ll = (int)a[3];
+            act = (act || bit(cnt, ll - 1)) && !bit(brk, ll - 1) && !ext && !lret;
+            cnt = setbit(cnt, ll - 1, false);
+            break;
+        }
+        case OP_JUMP: {
+            if (++backedges > kMaxBackEdges) {
+                if (threadIdx.x % 32 == 0) raise_status(R.status, ST_TIMEOUT);
+                pc = R.nops;
+                continue;
+            }
+            pc = (int)a[2];
+            continue;
+        }
+        case OP_LOOP_END: {
+            int d = (int)a[1];
+            int ll = (int)a[3];
+            brk = setbit(brk, ll - 1, false);
+            cnt = setbit(cnt, ll - 1, false);
+            // lanes that broke out of an enclosing loop stay off via the
+            // enclosing ENDIF/LOOP_STEP recomputation
+            act = bit(stk, d) && !ext && !lret;
+            break;
+        }
+        case OP_BREAK: {
+            int ll = (int)a[3];
+            if (act && ll) brk = setbit(brk, ll - 1, true);
+            act = false;
+            break;
+        }
+        case OP_CONTINUE: {
+            int ll = (int)a[3];
+            if (act && ll) cnt = setbit(cnt, ll - 1, true);
+            act = false;
+            break;
+        }
+        case OP_RETURN: if (act) lret = true; act = false; break;
+        case OP_EXIT: if (act) ext = true; act = false; break;
+        case OP_LAYER_END: lret = false; act = valid && !ext; break;
+        default:
+            if (act) {
+                switch (code) {
+                case OP_LOAD_GLOBAL: h_load_global(L, a, (*R.G)); break;
+                case OP_LOAD_USERDATA: h_load_userdata(L, a, R.userdata); break;
+                case OP_STORE_OUTPUT: h_store_output(L, a, R.outputs); break;
+                case OP_ASSIGN: h_assign_fast(L, a, R.status); break;
+                case OP_COMPREF: h_compref(L, a, R.status); break;
+                case OP_COMPASSIGN: h_compassign(L, a, R.status); break;
+                case OP_MXCOMPREF: {
+                    int r = ldi(L, a[2], 0), c = ldi(L, a[3], 0);
+                    r = r < 0 ? 0 : (r > 3 ? 3 : r); c = c < 0 ? 0 : (c > 3 ? 3 : c);
+                    stval(L, a[0], 0, __uint_as_float(ldw(L, a[1], r * 4 + c)));
+                    break;
+                }
+                case OP_MXCOMPASSIGN: {
+                    int r = ldi(L, a[1], 0), c = ldi(L, a[2], 0);
+                    r = r < 0 ? 0 : (r > 3 ? 3 : r); c = c < 0 ? 0 : (c > 3 ? 3 : c);
+                    stf(L, a[0], r * 4 + c, ldf(L, a[3], 0, 0));
+                    break;
+                }
+                case OP_CONSTRUCT3: h_construct3(L, a); break;
+                case OP_AREF: OSLG_TIER_CASE(4, h_aref(L, a, R.status)) break;
+                case OP_AASSIGN: OSLG_TIER_CASE(4, h_aassign(L, a, R.status)) break;
+                case OP_MATRIX_DIAG: {
+                    float v = ldf(L, a[1], 0, 0);
+                    for (int i = 0; i < 16; ++i) stf(L, a[0], i, (i % 5 == 0) ? v : 0.0f);
+                    break;
+                }
+                case OP_ADD: h_arith_fast<0>(L, a); break;
+                case OP_SUB: h_arith_fast<1>(L, a); break;
+                case OP_MUL: h_arith_fast<2>(L, a); break;
+                case OP_DIV: h_arith_fast<3>(L, a); break;
+                case OP_MOD: h_arith<4>(L, a); break;
+                case OP_NEG: h_unary<OP_NEG>(L, a); break;
+                case OP_IADD: h_iarith<0>(L, a); break;
+                case OP_ISUB: h_iarith<1>(L, a); break;
+                case OP_IMUL: h_iarith<2>(L, a); break;
+                case OP_IDIV: h_iarith<3>(L, a); break;
+                case OP_IMOD: h_iarith<4>(L, a); break;
+                case OP_INEG: stw(L, a[0], 0, (uint32_t)(-ldi(L, a[1], 0))); break;
+                case OP_MMUL: OSLG_TIER_CASE(4, h_mmul(L, a)) break;
+                case OP_EQ: h_cmp<0>(L, a); break;
+                case OP_NEQ: h_cmp<1>(L, a); break;
+                case OP_LT: h_cmp<2>(L, a); break;
+                case OP_GT: h_cmp<3>(L, a); break;
+                case OP_LE: h_cmp<4>(L, a); break;
+                case OP_GE: h_cmp<5>(L, a); break;
+                case OP_AND: stw(L, a[0], 0, (truth(L, a[1]) && truth(L, a[2])) ? 1u : 0u); break;
+                case OP_OR: stw(L, a[0], 0, (truth(L, a[1]) || truth(L, a[2])) ? 1u : 0u); break;
+                case OP_BITAND: stw(L, a[0], 0, (uint32_t)(ldi(L, a[1], 0) & ldi(L, a[2], 0))); break;
+                case OP_BITOR: stw(L, a[0], 0, (uint32_t)(ldi(L, a[1], 0) | ldi(L, a[2], 0))); break;
+                case OP_XOR: stw(L, a[0], 0, (uint32_t)(ldi(L, a[1], 0) ^ ldi(L, a[2], 0))); break;
+                case OP_SHL: stw(L, a[0], 0, (uint32_t)ldi(L, a[1], 0) << (ldi(L, a[2], 0) & 31)); break;
+                case OP_SHR: stw(L, a[0], 0, (uint32_t)(ldi(L, a[1], 0) >> (ldi(L, a[2], 0) & 31))); break;
+                case OP_COMPL: stw(L, a[0], 0, ~(uint32_t)ldi(L, a[1], 0)); break;
+                case OP_ABS: h_unary<OP_ABS>(L, a); break;
+                case OP_IABS: { int v = ldi(L, a[1], 0); stw(L, a[0], 0, (uint32_t)(v < 0 ? -v : v)); break; }
+                case OP_FLOOR: h_unary<OP_FLOOR>(L, a); break;
+                case OP_CEIL: h_unary<OP_CEIL>(L, a); break;
+                case OP_ROUND: h_unary<OP_ROUND>(L, a); break;
+                case OP_TRUNC: h_unary<OP_TRUNC>(L, a); break;
+                case OP_SIGN: h_unary<OP_SIGN>(L, a); break;
+                case OP_SQRT: h_unary<OP_SQRT>(L, a); break;
+                case OP_INVSQRT: h_unary<OP_INVSQRT>(L, a); break;
+                case OP_CBRT: OSLG_TIER_CASE(4, h_unary<OP_CBRT>(L, a)) break;
+                case OP_SIN: OSLG_TIER_CASE(4, h_unary<OP_SIN>(L, a)) break;
+                case OP_COS: OSLG_TIER_CASE(4, h_unary<OP_COS>(L, a)) break;
+                case OP_TAN: OSLG_TIER_CASE(4, h_unary<OP_TAN>(L, a)) break;
+                case OP_ASIN: OSLG_TIER_CASE(4, h_unary<OP_ASIN>(L, a)) break;
+                case OP_ACOS: OSLG_TIER_CASE(4, h_unary<OP_ACOS>(L, a)) break;
+                case OP_ATAN: OSLG_TIER_CASE(4, h_unary<OP_ATAN>(L, a)) break;
+                case OP_SINH: OSLG_TIER_CASE(4, h_unary<OP_SINH>(L, a)) break;
+                case OP_COSH: OSLG_TIER_CASE(4, h_unary<OP_COSH>(L, a)) break;
+                case OP_TANH: OSLG_TIER_CASE(4, h_unary<OP_TANH>(L, a)) break;
+                case OP_EXP: OSLG_TIER_CASE(4, h_unary<OP_EXP>(L, a)) break;
+                case OP_EXP2: OSLG_TIER_CASE(4, h_unary<OP_EXP2>(L, a)) break;
+                case OP_EXPM1: OSLG_TIER_CASE(4, h_unary<OP_EXPM1>(L, a)) break;
+                case OP_LOG: OSLG_TIER_CASE(4, h_unary<OP_LOG>(L, a)) break;
+                case OP_LOG2: OSLG_TIER_CASE(4, h_unary<OP_LOG2>(L, a)) break;
+                case OP_LOG10: OSLG_TIER_CASE(4, h_unary<OP_LOG10>(L, a)) break;
+                case OP_RADIANS: h_unary<OP_RADIANS>(L, a); break;
+                case OP_DEGREES: h_unary<OP_DEGREES>(L, a); break;
+                case OP_ISNAN: stw(L, a[0], 0, isnan(ldf(L, a[1], 0, 0)) ? 1u : 0u); break;
+                case OP_ISINF: stw(L, a[0], 0, isinf(ldf(L, a[1], 0, 0)) ? 1u : 0u); break;
+                case OP_ISFINITE: stw(L, a[0], 0, isfinite(ldf(L, a[1], 0, 0)) ? 1u : 0u); break;
+                case OP_POW: OSLG_TIER_CASE(4, h_binary<OP_POW>(L, a)) break;
+                case OP_ATAN2: OSLG_TIER_CASE(4, h_binary<OP_ATAN2>(L, a)) break;
+                case OP_FMOD: OSLG_TIER_CASE(4, h_binary<OP_FMOD>(L, a)) break;
+                case OP_MIN: h_binary<OP_MIN>(L, a); break;
+                case OP_MAX: h_binary<OP_MAX>(L, a); break;
+                case OP_STEP: h_binary<OP_STEP>(L, a); break;
+                case OP_IMIN: { int x = ldi(L, a[1], 0), y = ldi(L, a[2], 0); stw(L, a[0], 0, (uint32_t)(x <= y ? x : y)); break; }
+                case OP_IMAX: { int x = ldi(L, a[1], 0), y = ldi(L, a[2], 0); stw(L, a[0], 0, (uint32_t)(x > y ? x : y)); break; }
+                case OP_CLAMP: OSLG_TIER_CASE(4, h_clamp(L, a)) break;
+                case OP_MIX: OSLG_TIER_CASE(4, h_mix(L, a)) break;
+                case OP_SMOOTHSTEP: OSLG_TIER_CASE(4, h_smoothstep(L, a)) break;
+                case OP_SELECT: OSLG_TIER_CASE(4, h_select(L, a)) break;
+                case OP_DOT: OSLG_TIER_CASE(4, h_dot(L, a)) break;
+                case OP_CROSS: OSLG_TIER_CASE(4, h_cross(L, a)) break;
+                case OP_LENGTH: OSLG_TIER_CASE(4, h_length(L, a, false)) break;
+                case OP_DISTANCE: OSLG_TIER_CASE(4, h_length(L, a, true)) break;
+                case OP_NORMALIZE: OSLG_TIER_CASE(4, h_normalize(L, a)) break;
+                case OP_DX:
+                case OP_DY: {
+                    int d = code == OP_DX ? 1 : 2;
+                    int nc = anc(a[0]);
+                    for (int c = 0; c < nc; ++c) stval(L, a[0], c, ldf(L, a[1], c, d));
+                    break;
+                }
+                case OP_TRANSFORM:
+                    if (a[3] == 2u) { OSLG_TIER_CASE(4, h_transformn(L, a)) }
+                    else { OSLG_TIER_CASE(4, h_transform(L, a)) }
+                    break;
+                case OP_MDIV: OSLG_TIER_CASE(4, h_mdiv(L, a)) break;
+                case OP_TRANSPOSE:
+                case OP_DETERMINANT: OSLG_TIER_CASE(4, h_matrix_misc(L, code, a)) break;
+                case OP_AREA:
+                case OP_FILTERWIDTH: OSLG_TIER_CASE(4, h_deriv_misc(L, code, a)) break;
+                case OP_LUMINANCE: OSLG_TIER_CASE(4, h_luminance(L, a)) break;
+                case OP_NOISE: OSLG_TIER_CASE(1, h_noise(L, a)) break;
+                case OP_GABOR: {
+                    if constexpr ((TIER & 1) != 0) {
+                        if (pc + 1 < R.nops) h_gabor(L, a, R.sops[pc + 1].a);
+                        else raise_status(R.status, ST_BAD_OPCODE);
+                    } else {
+                        raise_status(R.status, ST_BAD_OPCODE);
+                    }
+                    break;
+                }
+                case OP_HASH: OSLG_TIER_CASE(1, h_hash(L, a)) break;
+                case OP_CLOSURE: {
+                    if constexpr ((TIER & 2) != 0) {
+                        const uint32_t* extra = nullptr;
+                        if (pc + 1 < R.nops && R.sops[pc + 1].code == OP_NOP && R.sops[pc + 1].nargs == 7)
+                            extra = R.sops[pc + 1].a;
+                        h_closure(L, a, extra, R.CP, R.status);
+                    } else {
+                        raise_status(R.status, ST_BAD_OPCODE);
+                    }
+                    break;
+                }
+                case OP_CLOSURE_MUL: OSLG_TIER_CASE(2, h_closure_mul(L, a, R.CP, R.status)) break;
+                case OP_CLOSURE_ADD: OSLG_TIER_CASE(2, h_closure_add(L, a, R.CP, R.status)) break;
+                case OP_STORE_CLOSURE: OSLG_TIER_CASE(2, h_store_closure(L, a, R.outputs, R.CP, R.status)) break;
+                case OP_BSDF_EVAL: OSLG_TIER_CASE(2, h_bsdf_eval(L, a, R.outputs, R.CP, R.status)) break;
+                case OP_SPLINE: OSLG_TIER_CASE(2, h_spline(L, a)) break;
+                default: raise_status(R.status, ST_BAD_OPCODE); break;
+                }
+            }
+            break;
+        }
+        ++pc;
+    }
+}
+
+
 template <bool SMEM, int TIER>
-__global__ void __launch_bounds__(256) interp_kernel(KArgs k) {
+// at least two CTAs of 256 per SM: the register budget is 128 per thread
+__global__ void __launch_bounds__(256, 2) interp_kernel(const __grid_constant__ KArgs k) {
     extern __shared__ __align__(16) unsigned char smem[];
     const ProgramHeader* H = reinterpret_cast<const ProgramHeader*>(k.blob);
     const int nops = (int)H->nops, nconst = (int)H->nconst, slots = (int)H->heap_slots;
@@ -1461,10 +1726,16 @@ __global__ void __launch_bounds__(256) interp_kernel(KArgs k) {
         for (int i = threadIdx.x; i < nconst; i += blockDim.x) spool[i] = gpool[i];
     }
     __syncthreads();
-    ClosurePools CP;
-    CP.base = H->closure_base;
-    CP.max_nodes = H->max_comps;
-    const bool uses_closures = (H->flags & 1u) != 0;
+    RunCtx R;
+    R.sops = sops;
+    R.nops = nops;
+    R.CP.base = H->closure_base;
+    R.CP.max_nodes = H->max_comps;
+    R.uses_closures = (H->flags & 1u) != 0;
+    R.G = &k.G;
+    R.userdata = k.userdata;
+    R.outputs = k.outputs;
+    R.status = k.status;
 
     Lane L;
     L.pool = spool;
@@ -1475,250 +1746,59 @@ __global__ void __launch_bounds__(256) interp_kernel(KArgs k) {
     const int64_t ntiles = (k.npoints + blockDim.x - 1) / blockDim.x;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         L.pt = tile * blockDim.x + threadIdx.x;
-        const bool valid = L.pt < k.npoints;
-        bool act = valid, ext = false, lret = false;
-        uint32_t stk = 0, cnd = 0, brk = 0, cnt = 0;
-        long long backedges = 0;
-        if (uses_closures && valid) hsetu(L, CP.base, 0u);
-        int pc = 0;
-        while (pc < nops) {
-            const uint4* ow = reinterpret_cast<const uint4*>(sops + pc);
-            const uint4 w0 = ow[0], w1 = ow[1];
-            const uint32_t code = w0.x & 0xFFFFu;
-            const uint32_t a[7] = { w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w };
-            switch (code) {
-            case OP_NOP: break;
-            case OP_IF: {
-                int d = (int)a[1];
-                bool c = act && truth(L, a[0]);
-                stk = setbit(stk, d, act);
-                cnd = setbit(cnd, d, c);
-                act = c;
-                if (!__any_sync(FULL, act)) { pc = (int)a[2]; continue; }
-                break;
-            }
-            case OP_ELSE: {
-                int d = (int)a[1];
-                int ll = (int)a[3];
-                bool off = ext || lret || (ll && (bit(brk, ll - 1) || bit(cnt, ll - 1)));
-                act = bit(stk, d) && !bit(cnd, d) && !off;
-                if (!__any_sync(FULL, act)) { pc = (int)a[2]; continue; }
-                break;
-            }
-            case OP_ENDIF: {
-                int d = (int)a[1];
-                int ll = (int)a[3];
-                bool off = ext || lret || (ll && (bit(brk, ll - 1) || bit(cnt, ll - 1)));
-                act = bit(stk, d) && !off;
-                break;
-            }
-            case OP_LOOP_BEGIN: {
-                int d = (int)a[1];
-                int ll = (int)a[3];
-                stk = setbit(stk, d, act);
-                brk = setbit(brk, ll - 1, false);
-                cnt = setbit(cnt, ll - 1, false);
-                break;
-            }
-            case OP_LOOP_TEST: {
-                act = act && truth(L, a[0]);
-                if (!__any_sync(FULL, act)) { pc = (int)a[2]; continue; }
-                break;
-            }
-            case OP_LOOP_STEP: {
-                int ll = (int)a[3];
-                act = (act || bit(cnt, ll - 1)) && !bit(brk, ll - 1) && !ext && !lret;
-                cnt = setbit(cnt, ll - 1, false);
-                break;
-            }
-            case OP_JUMP: {
-                if (++backedges > kMaxBackEdges) {
-                    if (threadIdx.x % 32 == 0) raise_status(k.status, ST_TIMEOUT);
-                    pc = nops;
-                    continue;
-                }
-                pc = (int)a[2];
-                continue;
-            }
-            case OP_LOOP_END: {
-                int d = (int)a[1];
-                int ll = (int)a[3];
-                brk = setbit(brk, ll - 1, false);
-                cnt = setbit(cnt, ll - 1, false);
-                // lanes that broke out of an enclosing loop stay off via the
-                // enclosing ENDIF/LOOP_STEP recomputation
-                act = bit(stk, d) && !ext && !lret;
-                break;
-            }
-            case OP_BREAK: {
-                int ll = (int)a[3];
-                if (act && ll) brk = setbit(brk, ll - 1, true);
-                act = false;
-                break;
-            }
-            case OP_CONTINUE: {
-                int ll = (int)a[3];
-                if (act && ll) cnt = setbit(cnt, ll - 1, true);
-                act = false;
-                break;
-            }
-            case OP_RETURN: if (act) lret = true; act = false; break;
-            case OP_EXIT: if (act) ext = true; act = false; break;
-            case OP_LAYER_END: lret = false; act = valid && !ext; break;
-            default:
-                if (act) {
-                    switch (code) {
-                    case OP_LOAD_GLOBAL: h_load_global(L, a, k.G); break;
-                    case OP_LOAD_USERDATA: h_load_userdata(L, a, k.userdata); break;
-                    case OP_STORE_OUTPUT: h_store_output(L, a, k.outputs); break;
-                    case OP_ASSIGN: h_assign_fast(L, a, k.status); break;
-                    case OP_COMPREF: h_compref(L, a, k.status); break;
-                    case OP_COMPASSIGN: h_compassign(L, a, k.status); break;
-                    case OP_MXCOMPREF: {
-                        int r = ldi(L, a[2], 0), c = ldi(L, a[3], 0);
-                        r = r < 0 ? 0 : (r > 3 ? 3 : r); c = c < 0 ? 0 : (c > 3 ? 3 : c);
-                        stval(L, a[0], 0, __uint_as_float(ldw(L, a[1], r * 4 + c)));
-                        break;
-                    }
-                    case OP_MXCOMPASSIGN: {
-                        int r = ldi(L, a[1], 0), c = ldi(L, a[2], 0);
-                        r = r < 0 ? 0 : (r > 3 ? 3 : r); c = c < 0 ? 0 : (c > 3 ? 3 : c);
-                        stf(L, a[0], r * 4 + c, ldf(L, a[3], 0, 0));
-                        break;
-                    }
-                    case OP_CONSTRUCT3: h_construct3(L, a); break;
-                    case OP_AREF: OSLG_TIER_CASE(4, h_aref(L, a, k.status)) break;
-                    case OP_AASSIGN: OSLG_TIER_CASE(4, h_aassign(L, a, k.status)) break;
-                    case OP_MATRIX_DIAG: {
-                        float v = ldf(L, a[1], 0, 0);
-                        for (int i = 0; i < 16; ++i) stf(L, a[0], i, (i % 5 == 0) ? v : 0.0f);
-                        break;
-                    }
-                    case OP_ADD: h_arith_fast<0>(L, a); break;
-                    case OP_SUB: h_arith_fast<1>(L, a); break;
-                    case OP_MUL: h_arith_fast<2>(L, a); break;
-                    case OP_DIV: h_arith_fast<3>(L, a); break;
-                    case OP_MOD: h_arith<4>(L, a); break;
-                    case OP_NEG: h_unary<OP_NEG>(L, a); break;
-                    case OP_IADD: h_iarith<0>(L, a); break;
-                    case OP_ISUB: h_iarith<1>(L, a); break;
-                    case OP_IMUL: h_iarith<2>(L, a); break;
-                    case OP_IDIV: h_iarith<3>(L, a); break;
-                    case OP_IMOD: h_iarith<4>(L, a); break;
-                    case OP_INEG: stw(L, a[0], 0, (uint32_t)(-ldi(L, a[1], 0))); break;
-                    case OP_MMUL: OSLG_TIER_CASE(4, h_mmul(L, a)) break;
-                    case OP_EQ: h_cmp<0>(L, a); break;
-                    case OP_NEQ: h_cmp<1>(L, a); break;
-                    case OP_LT: h_cmp<2>(L, a); break;
-                    case OP_GT: h_cmp<3>(L, a); break;
-                    case OP_LE: h_cmp<4>(L, a); break;
-                    case OP_GE: h_cmp<5>(L, a); break;
-                    case OP_AND: stw(L, a[0], 0, (truth(L, a[1]) && truth(L, a[2])) ? 1u : 0u); break;
-                    case OP_OR: stw(L, a[0], 0, (truth(L, a[1]) || truth(L, a[2])) ? 1u : 0u); break;
-                    case OP_BITAND: stw(L, a[0], 0, (uint32_t)(ldi(L, a[1], 0) & ldi(L, a[2], 0))); break;
-                    case OP_BITOR: stw(L, a[0], 0, (uint32_t)(ldi(L, a[1], 0) | ldi(L, a[2], 0))); break;
-                    case OP_XOR: stw(L, a[0], 0, (uint32_t)(ldi(L, a[1], 0) ^ ldi(L, a[2], 0))); break;
-                    case OP_SHL: stw(L, a[0], 0, (uint32_t)ldi(L, a[1], 0) << (ldi(L, a[2], 0) & 31)); break;
-                    case OP_SHR: stw(L, a[0], 0, (uint32_t)(ldi(L, a[1], 0) >> (ldi(L, a[2], 0) & 31))); break;
-                    case OP_COMPL: stw(L, a[0], 0, ~(uint32_t)ldi(L, a[1], 0)); break;
-                    case OP_ABS: h_unary<OP_ABS>(L, a); break;
-                    case OP_IABS: { int v = ldi(L, a[1], 0); stw(L, a[0], 0, (uint32_t)(v < 0 ? -v : v)); break; }
-                    case OP_FLOOR: h_unary<OP_FLOOR>(L, a); break;
-                    case OP_CEIL: h_unary<OP_CEIL>(L, a); break;
-                    case OP_ROUND: h_unary<OP_ROUND>(L, a); break;
-                    case OP_TRUNC: h_unary<OP_TRUNC>(L, a); break;
-                    case OP_SIGN: h_unary<OP_SIGN>(L, a); break;
-                    case OP_SQRT: h_unary<OP_SQRT>(L, a); break;
-                    case OP_INVSQRT: h_unary<OP_INVSQRT>(L, a); break;
-                    case OP_CBRT: OSLG_TIER_CASE(4, h_unary<OP_CBRT>(L, a)) break;
-                    case OP_SIN: OSLG_TIER_CASE(4, h_unary<OP_SIN>(L, a)) break;
-                    case OP_COS: OSLG_TIER_CASE(4, h_unary<OP_COS>(L, a)) break;
-                    case OP_TAN: OSLG_TIER_CASE(4, h_unary<OP_TAN>(L, a)) break;
-                    case OP_ASIN: OSLG_TIER_CASE(4, h_unary<OP_ASIN>(L, a)) break;
-                    case OP_ACOS: OSLG_TIER_CASE(4, h_unary<OP_ACOS>(L, a)) break;
-                    case OP_ATAN: OSLG_TIER_CASE(4, h_unary<OP_ATAN>(L, a)) break;
-                    case OP_SINH: OSLG_TIER_CASE(4, h_unary<OP_SINH>(L, a)) break;
-                    case OP_COSH: OSLG_TIER_CASE(4, h_unary<OP_COSH>(L, a)) break;
-                    case OP_TANH: OSLG_TIER_CASE(4, h_unary<OP_TANH>(L, a)) break;
-                    case OP_EXP: OSLG_TIER_CASE(4, h_unary<OP_EXP>(L, a)) break;
-                    case OP_EXP2: OSLG_TIER_CASE(4, h_unary<OP_EXP2>(L, a)) break;
-                    case OP_EXPM1: OSLG_TIER_CASE(4, h_unary<OP_EXPM1>(L, a)) break;
-                    case OP_LOG: OSLG_TIER_CASE(4, h_unary<OP_LOG>(L, a)) break;
-                    case OP_LOG2: OSLG_TIER_CASE(4, h_unary<OP_LOG2>(L, a)) break;
-                    case OP_LOG10: OSLG_TIER_CASE(4, h_unary<OP_LOG10>(L, a)) break;
-                    case OP_RADIANS: h_unary<OP_RADIANS>(L, a); break;
-                    case OP_DEGREES: h_unary<OP_DEGREES>(L, a); break;
-                    case OP_ISNAN: stw(L, a[0], 0, isnan(ldf(L, a[1], 0, 0)) ? 1u : 0u); break;
-                    case OP_ISINF: stw(L, a[0], 0, isinf(ldf(L, a[1], 0, 0)) ? 1u : 0u); break;
-                    case OP_ISFINITE: stw(L, a[0], 0, isfinite(ldf(L, a[1], 0, 0)) ? 1u : 0u); break;
-                    case OP_POW: OSLG_TIER_CASE(4, h_binary<OP_POW>(L, a)) break;
-                    case OP_ATAN2: OSLG_TIER_CASE(4, h_binary<OP_ATAN2>(L, a)) break;
-                    case OP_FMOD: OSLG_TIER_CASE(4, h_binary<OP_FMOD>(L, a)) break;
-                    case OP_MIN: h_binary<OP_MIN>(L, a); break;
-                    case OP_MAX: h_binary<OP_MAX>(L, a); break;
-                    case OP_STEP: h_binary<OP_STEP>(L, a); break;
-                    case OP_IMIN: { int x = ldi(L, a[1], 0), y = ldi(L, a[2], 0); stw(L, a[0], 0, (uint32_t)(x <= y ? x : y)); break; }
-                    case OP_IMAX: { int x = ldi(L, a[1], 0), y = ldi(L, a[2], 0); stw(L, a[0], 0, (uint32_t)(x > y ? x : y)); break; }
-                    case OP_CLAMP: OSLG_TIER_CASE(4, h_clamp(L, a)) break;
-                    case OP_MIX: OSLG_TIER_CASE(4, h_mix(L, a)) break;
-                    case OP_SMOOTHSTEP: OSLG_TIER_CASE(4, h_smoothstep(L, a)) break;
-                    case OP_SELECT: OSLG_TIER_CASE(4, h_select(L, a)) break;
-                    case OP_DOT: OSLG_TIER_CASE(4, h_dot(L, a)) break;
-                    case OP_CROSS: OSLG_TIER_CASE(4, h_cross(L, a)) break;
-                    case OP_LENGTH: OSLG_TIER_CASE(4, h_length(L, a, false)) break;
-                    case OP_DISTANCE: OSLG_TIER_CASE(4, h_length(L, a, true)) break;
-                    case OP_NORMALIZE: OSLG_TIER_CASE(4, h_normalize(L, a)) break;
-                    case OP_DX:
-                    case OP_DY: {
-                        int d = code == OP_DX ? 1 : 2;
-                        int nc = anc(a[0]);
-                        for (int c = 0; c < nc; ++c) stval(L, a[0], c, ldf(L, a[1], c, d));
-                        break;
-                    }
-                    case OP_TRANSFORM:
-                        if (a[3] == 2u) { OSLG_TIER_CASE(4, h_transformn(L, a)) }
-                        else { OSLG_TIER_CASE(4, h_transform(L, a)) }
-                        break;
-                    case OP_MDIV: OSLG_TIER_CASE(4, h_mdiv(L, a)) break;
-                    case OP_TRANSPOSE:
-                    case OP_DETERMINANT: OSLG_TIER_CASE(4, h_matrix_misc(L, code, a)) break;
-                    case OP_AREA:
-                    case OP_FILTERWIDTH: OSLG_TIER_CASE(4, h_deriv_misc(L, code, a)) break;
-                    case OP_LUMINANCE: OSLG_TIER_CASE(4, h_luminance(L, a)) break;
-                    case OP_NOISE: OSLG_TIER_CASE(1, h_noise(L, a)) break;
-                    case OP_GABOR: {
-                        if constexpr ((TIER & 1) != 0) {
-                            if (pc + 1 < nops) h_gabor(L, a, sops[pc + 1].a);
-                            else raise_status(k.status, ST_BAD_OPCODE);
-                        } else {
-                            raise_status(k.status, ST_BAD_OPCODE);
-                        }
-                        break;
-                    }
-                    case OP_HASH: OSLG_TIER_CASE(1, h_hash(L, a)) break;
-                    case OP_CLOSURE: {
-                        if constexpr ((TIER & 2) != 0) {
-                            const uint32_t* extra = nullptr;
-                            if (pc + 1 < nops && sops[pc + 1].code == OP_NOP && sops[pc + 1].nargs == 7)
-                                extra = sops[pc + 1].a;
-                            h_closure(L, a, extra, CP, k.status);
-                        } else {
-                            raise_status(k.status, ST_BAD_OPCODE);
-                        }
-                        break;
-                    }
-                    case OP_CLOSURE_MUL: OSLG_TIER_CASE(2, h_closure_mul(L, a, CP, k.status)) break;
-                    case OP_CLOSURE_ADD: OSLG_TIER_CASE(2, h_closure_add(L, a, CP, k.status)) break;
-                    case OP_STORE_CLOSURE: OSLG_TIER_CASE(2, h_store_closure(L, a, k.outputs, CP, k.status)) break;
-                    case OP_BSDF_EVAL: OSLG_TIER_CASE(2, h_bsdf_eval(L, a, k.outputs, CP, k.status)) break;
-                    case OP_SPLINE: OSLG_TIER_CASE(2, h_spline(L, a)) break;
-                    default: raise_status(k.status, ST_BAD_OPCODE); break;
-                    }
-                }
-                break;
-            }
-            ++pc;
+        run_tile<TIER>(R, L, k.npoints);
+    }
+}
+
+// Persistent batch kernel: CTAs take work items (job, tile) from a device
+// counter until the list is exhausted, staging each job's program into
+// shared memory when the job changes. One launch runs every group of the
+// batch; items are ordered so that a CTA mostly stays on one job.
+template <bool SMEM, int TIER, int MAXT>
+__global__ void __launch_bounds__(MAXT, 512 / MAXT) batch_kernel(const __grid_constant__ BatchArgs b) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ uint32_t s_item;
+    Op* sops = reinterpret_cast<Op*>(smem);
+    float* sheap = reinterpret_cast<float*>(smem + (size_t)b.prog_bytes);
+    Lane L;
+    L.hs = blockDim.x;
+    L.li = threadIdx.x;
+    L.heap = SMEM ? sheap : (b.gheap + (size_t)blockIdx.x * (size_t)b.heap_slots * blockDim.x);
+    L.pool = nullptr;
+    RunCtx R;
+    R.sops = sops;
+    int cur = -1;
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(b.counter, 1u);
+        __syncthreads();
+        const uint32_t it = s_item;
+        __syncthreads();
+        if (it >= b.nitems) break;
+        const uint2 w = b.items[it];
+        const BatchJob* J = b.jobs + w.x;
+        if ((int)w.x != cur) {
+            const ProgramHeader* H = reinterpret_cast<const ProgramHeader*>(J->blob);
+            const int nops = (int)H->nops, nconst = (int)H->nconst;
+            uint32_t* spool = reinterpret_cast<uint32_t*>(smem + (size_t)nops * sizeof(Op));
+            const uint4* gops = reinterpret_cast<const uint4*>(J->blob + sizeof(ProgramHeader));
+            uint4* so = reinterpret_cast<uint4*>(sops);
+            for (int i = threadIdx.x; i < nops * 2; i += blockDim.x) so[i] = gops[i];
+            const uint32_t* gpool = reinterpret_cast<const uint32_t*>(J->blob + sizeof(ProgramHeader) + (size_t)nops * sizeof(Op));
+            for (int i = threadIdx.x; i < nconst; i += blockDim.x) spool[i] = gpool[i];
+            __syncthreads();
+            R.nops = nops;
+            R.CP.base = H->closure_base;
+            R.CP.max_nodes = H->max_comps;
+            R.uses_closures = (H->flags & 1u) != 0;
+            R.G = &J->G;
+            R.userdata = J->userdata;
+            R.outputs = J->outputs;
+            R.status = b.status;
+            L.pool = spool;
+            cur = (int)w.x;
         }
+        L.pt = (int64_t)w.y * blockDim.x + threadIdx.x;
+        run_tile<TIER>(R, L, J->npoints);
     }
 }
 

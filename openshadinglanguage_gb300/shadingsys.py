@@ -191,7 +191,70 @@ class ShadingSystem:
                        ctypes.c_void_p(userdata_ptr or None), ctypes.c_void_p(output_ptr or None),
                        ctypes.c_void_p(stream or None)))
 
+    def batch(self):
+        """A persistent multi-group batch on this system (see Batch)."""
+        return Batch(self)
+
     def device_status(self):
         bits = ctypes.c_uint32(0)
         self._check(C.lib().oslg_device_status(self._h, ctypes.byref(bits)))
         return bits.value
+
+
+class Batch:
+    """Many groups' requests run in one persistent kernel launch, replayed
+    as a CUDA graph while unchanged (include/oslg.h, oslg_batch_*). Results
+    equal one execute_batch call per request. Keep every globals structure
+    and device buffer alive until clear() or close()."""
+
+    def __init__(self, ss):
+        self._ss = ss
+        h = ctypes.c_void_p()
+        ss._check(C.lib().oslg_batch_create(ss._h, ctypes.byref(h)))
+        self._h = h
+        self._keep = []
+
+    def close(self):
+        if self._h:
+            C.lib().oslg_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def clear(self):
+        self._ss._check(C.lib().oslg_batch_clear(self._h))
+        self._keep = []
+
+    def add(self, group, npoints, globals_c, userdata_ptr=0, output_ptr=0):
+        self._keep.append(globals_c)
+        self._ss._check(C.lib().oslg_batch_add(self._h, group.handle, int(npoints), ctypes.byref(globals_c),
+                                               ctypes.c_void_p(userdata_ptr or None),
+                                               ctypes.c_void_p(output_ptr or None)))
+
+    def set_launch(self, block=0, heap_smem=-1, use_graph=True):
+        self._ss._check(C.lib().oslg_batch_set_launch(self._h, int(block), int(heap_smem), 1 if use_graph else 0))
+
+    def execute(self, stream=0):
+        self._ss._check(C.lib().oslg_batch_execute(self._h, ctypes.c_void_p(stream or None)))
+
+    @staticmethod
+    def _tuning(t):
+        return dict(block=t.block, heap_smem=t.heap_smem, grid=t.grid, ctas_per_sm=t.ctas_per_sm, ms=t.ms)
+
+    def autotune(self, stream=0, reps=3):
+        """Sweep block {128,256,512} x heap {shared, HBM}; returns (best, all)."""
+        res = (C.BatchTuningC * 8)()
+        n = ctypes.c_int(0)
+        best = C.BatchTuningC()
+        self._ss._check(C.lib().oslg_batch_autotune(self._h, ctypes.c_void_p(stream or None), int(reps), res, 8,
+                                                    ctypes.byref(n), ctypes.byref(best)))
+        return self._tuning(best), [self._tuning(res[i]) for i in range(n.value)]
+
+    def last_launch(self):
+        t = C.BatchTuningC()
+        self._ss._check(C.lib().oslg_batch_last_launch(self._h, ctypes.byref(t)))
+        return self._tuning(t)

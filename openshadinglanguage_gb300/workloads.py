@@ -3,6 +3,9 @@
 C1  fbm_cell        single-layer fBm + hashed cell id, 1024x1024 grid
 C2  layered_closure 3-layer pattern -> ramp -> closure group with BSDF eval,
                     2048x2048 grid
+C3  random groups   64 seeded random op DAGs of 20-200 ops with noise,
+                    transforms, if/else and data-dependent loops; point
+                    counts log-uniform in [1K, 1M], P uniform in [-10,10]^3
 """
 import numpy as np
 
@@ -62,3 +65,276 @@ def c2_inputs(W, H, seed=0xC2):
 def c2_globals(make_globals, u, v, I):
     return make_globals(u=u, v=v, I=I, N=(0.0, 0.0, 1.0), Ng=(0.0, 0.0, 1.0), dPdu=(1.0, 0.0, 0.0),
                         dPdv=(0.0, 1.0, 0.0))
+
+
+# ---- C3 ------------------------------------------------------------------------------
+C3_SEED = 0xC3
+C3_GROUPS = 64
+C3_REC = 4  # Cout.rgb, Fout
+
+
+class _RandomShader:
+    """Builds one random shader as a stream of OSL statements over a pool of
+    float, vector and matrix variables. Statements only read variables
+    assigned in an enclosing scope, so every value a point reads was written
+    for that point (no dependence on heap contents)."""
+
+    NOISE_KINDS = (("perlin", 0.28), ("uperlin", 0.1), ("simplex", 0.22), ("usimplex", 0.05), ("cell", 0.25),
+                   ("gabor", 0.10))
+
+    def __init__(self, name, rng, target_ops):
+        from .oso import OsoBuilder
+        self.b = b = OsoBuilder(name)
+        self.rng = rng
+        self.target = target_ops
+        self.Cout = b.param("color", "Cout", [0, 0, 0], output=True)
+        self.Fout = b.param("float", "Fout", 0.0, output=True)
+        self.mats = []
+        for k in range(3):
+            m = rng.uniform(-1.0, 1.0, (4, 4))
+            m[:3, :3] += 1.5 * np.eye(3)
+            m[3, :3] *= 0.5
+            m[:3, 3] = 0.0
+            m[3, 3] = 1.0
+            self.mats.append(b.param("matrix", "M%d" % k, [float(np.float32(x)) for x in m.ravel()]))
+        P = b.glob("point", "P")
+        self.F, self.V = [], []
+        self.V.append(P)
+        for c in range(3):
+            f = self.newf()
+            b.op("compref", f, P, b.const("int", c))
+            self.F.append(f)
+
+    def c(self, x):
+        return self.b.const("float", float(np.float32(x)))
+
+    def newf(self):
+        return self.b.tmp("float")
+
+    def newv(self):
+        return self.b.tmp("vector")
+
+    def nops(self):
+        return len(self.b.ops)
+
+    def pickf(self, pool):
+        return pool[self.rng.integers(len(pool))]
+
+    # -- statements ------------------------------------------------------------------------
+    def st_farith(self, F, V):
+        b, r = self.b, self.rng
+        x, y, f = self.pickf(F), self.pickf(F), self.newf()
+        k = r.integers(4)
+        if k == 3:
+            t, d = self.newf(), self.newf()
+            b.op("abs", t, y)
+            b.op("add", d, t, self.c(0.5))
+            b.op("div", f, x, d)
+        else:
+            b.op(("add", "sub", "mul")[k], f, x, y)
+        F.append(f)
+
+    def st_varith(self, F, V):
+        b, r = self.b, self.rng
+        x, v = self.pickf(V), self.newv()
+        k = r.integers(4)
+        if k == 3:
+            b.op("mul", v, x, self.pickf(F))
+        else:
+            b.op(("add", "sub", "mul")[k], v, x, self.pickf(V))
+        V.append(v)
+
+    def st_unary(self, F, V):
+        b, r = self.b, self.rng
+        x, f = self.pickf(F), self.newf()
+        k = r.integers(6)
+        if k < 4:
+            b.op(("sin", "cos", "abs", "floor")[k], f, x)
+        elif k == 4:
+            t = self.newf()
+            b.op("abs", t, x)
+            b.op("sqrt", f, t)
+        else:
+            t, u = self.newf(), self.newf()
+            b.op("abs", t, x)
+            b.op("neg", u, t)
+            b.op("exp", f, u)
+        F.append(f)
+
+    def st_vector(self, F, V):
+        b, r = self.b, self.rng
+        k = r.integers(6)
+        a, c = self.pickf(V), self.pickf(V)
+        if k == 0:
+            f = self.newf(); b.op("dot", f, a, c); F.append(f)
+        elif k == 1:
+            f = self.newf(); b.op("length", f, a); F.append(f)
+        elif k == 2:
+            v = self.newv(); b.op("normalize", v, a); V.append(v)
+        elif k == 3:
+            v = self.newv(); b.op("cross", v, a, c); V.append(v)
+        elif k == 4:
+            t, v = self.newf(), self.newv()
+            b.op("clamp", t, self.pickf(F), self.c(0.0), self.c(1.0))
+            b.op("mix", v, a, c, t)
+            V.append(v)
+        else:
+            v = self.newv(); b.op("max", v, a, c); V.append(v)
+
+    def st_matrix(self, F, V):
+        b, r = self.b, self.rng
+        k = r.integers(4)
+        M = self.mats[r.integers(len(self.mats))]
+        if k == 3:
+            M2 = self.mats[r.integers(len(self.mats))]
+            Mm = b.tmp("matrix")
+            b.op("mul", Mm, M, M2)
+            M = Mm
+            k = r.integers(3)
+        src = self.pickf(V)
+        if k == 0:
+            pt, v = b.tmp("point"), b.tmp("point")
+            b.op("point", pt, src)
+            b.op("transform", v, M, pt)
+        elif k == 1:
+            v = self.newv()
+            b.op("transformv", v, M, src)
+        else:
+            nn, v = b.tmp("normal"), b.tmp("normal")
+            b.op("normal", nn, src)
+            b.op("transformn", v, M, nn)
+        V.append(v)
+
+    def noise_kind(self, allow_gabor=True):
+        names = [k for k, _ in self.NOISE_KINDS if allow_gabor or k != "gabor"]
+        w = np.array([p for k, p in self.NOISE_KINDS if allow_gabor or k != "gabor"])
+        return names[self.rng.choice(len(names), p=w / w.sum())]
+
+    def st_noise(self, F, V, depth=0, loop=False):
+        b, r = self.b, self.rng
+        kind = self.noise_kind(allow_gabor=not loop)
+        src, sc = self.pickf(V), b.tmp("point")
+        b.op("mul", sc, src, self.c(r.uniform(0.2, 2.5)))
+        if r.random() < 0.6:
+            f = self.newf()
+            b.op("noise", f, b.const("string", kind), sc)
+            F.append(f)
+        else:
+            v = self.newv()
+            b.op("noise", v, b.const("string", kind), sc)
+            V.append(v)
+
+    def block(self, F, V, n, depth, loop):
+        for _ in range(n):
+            if self.nops() >= self.target:
+                return
+            self.statement(F, V, depth, loop)
+
+    def st_if(self, F, V, depth, loop):
+        b, r = self.b, self.rng
+        f, cond = self.newf(), b.tmp("int")
+        src, sc = self.pickf(V), b.tmp("point")
+        b.op("mul", sc, src, self.c(r.uniform(0.3, 1.5)))
+        b.op("noise", f, b.const("string", "uperlin" if r.random() < 0.5 else "cell"), sc)
+        b.op("gt", cond, f, self.c(r.uniform(0.3, 0.7)))
+        acc_f, acc_v = self.pickf(F), self.pickf(V)
+        with b.if_(cond) as br:
+            F2, V2 = list(F), list(V)
+            self.block(F2, V2, int(r.integers(1, 4)), depth + 1, loop)
+            b.op("add", acc_f, acc_f, self.pickf(F2))
+            b.op("add", acc_v, acc_v, self.pickf(V2))
+            br.else_()
+            F3, V3 = list(F), list(V)
+            self.block(F3, V3, int(r.integers(1, 3)), depth + 1, loop)
+            b.op("sub", acc_f, acc_f, self.pickf(F3))
+
+    def st_loop(self, F, V, depth):
+        """for (i = 0; i < n; ++i) with n = 1 + int(15.99 * cellnoise(p)):
+        a data-dependent trip count in [1, 16]."""
+        b, r = self.b, self.rng
+        cn, t, nf = self.newf(), self.newf(), self.newf()
+        n, i, cond = b.tmp("int"), b.tmp("int"), b.tmp("int")
+        sc = b.tmp("point")
+        b.op("mul", sc, self.pickf(V), self.c(r.uniform(0.5, 3.0)))
+        b.op("cellnoise", cn, sc)
+        b.op("mul", t, cn, self.c(15.99))
+        b.op("add", nf, t, self.c(1.0))
+        b.op("assign", n, nf)
+        acc_f, acc_v = self.pickf(F), self.pickf(V)
+        p = self.newv()
+        b.op("assign", p, self.pickf(V))
+        with b.loop("for", cond) as L:
+            b.op("assign", i, b.const("int", 0))
+            L.cond()
+            b.op("lt", cond, i, n)
+            L.body()
+            F2, V2 = list(F) + [acc_f], list(V) + [p, acc_v]
+            self.block(F2, V2, int(r.integers(2, 5)), depth + 1, True)
+            b.op("add", acc_f, acc_f, self.pickf(F2))
+            b.op("add", acc_v, acc_v, self.pickf(V2))
+            b.op("mul", p, p, self.c(1.7))
+            b.op("add", p, p, self.c(0.37))
+            L.step()
+            b.op("add", i, i, b.const("int", 1))
+
+    def statement(self, F, V, depth=0, loop=False):
+        r = self.rng
+        kinds = ["farith", "varith", "unary", "vector", "matrix", "noise"]
+        w = [0.18, 0.16, 0.12, 0.14, 0.12, 0.18]
+        if depth < 2:
+            kinds += ["if", "loop"] if not loop else ["if"]
+            w += [0.06, 0.04] if not loop else [0.06]
+        w = np.array(w) / np.sum(w)
+        k = kinds[r.choice(len(kinds), p=w)]
+        if k == "if":
+            self.st_if(F, V, depth, loop)
+        elif k == "loop":
+            self.st_loop(F, V, depth)
+        elif k == "noise":
+            self.st_noise(F, V, depth, loop)
+        else:
+            getattr(self, "st_" + k)(F, V)
+
+    def build(self):
+        b = self.b
+        while self.nops() < self.target:
+            self.statement(self.F, self.V)
+        # outputs: a colour from the last vectors and a float from the last floats
+        v = self.newv()
+        b.op("add", v, self.V[-1], self.V[-2] if len(self.V) > 1 else self.V[-1])
+        b.op("assign", self.Cout, v)
+        f = self.newf()
+        b.op("add", f, self.F[-1], self.F[-2] if len(self.F) > 1 else self.F[-1])
+        b.op("assign", self.Fout, f)
+        return b.text()
+
+
+def c3_specs(seed=C3_SEED, ngroups=C3_GROUPS, min_points=1000, max_points=1000000):
+    """Per group: (name, oso text, point count, op count target). Target op
+    counts are uniform in [20, 200]; point counts log-uniform in
+    [min_points, max_points]."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for k in range(ngroups):
+        target = int(rng.integers(20, 201))
+        npts = int(np.exp(rng.uniform(np.log(min_points), np.log(max_points))))
+        name = "c3_g%02d" % k
+        oso = _RandomShader(name, np.random.default_rng([seed, k]), target).build()
+        specs.append((name, oso, npts, target))
+    return specs
+
+
+def c3_group(ss, name, oso):
+    ss.LoadMemoryCompiledShader(name, oso)
+    g = ss.ShaderGroupBegin(name + "_group")
+    ss.Shader(g, "surface", name, "L")
+    ss.ShaderGroupEnd(g)
+    ss.add_symlocs(g, [SymLocationDesc("L.Cout", TypeColor, False, SymArenaOutputs, 0, 4 * C3_REC),
+                       SymLocationDesc("L.Fout", TypeDesc(BASE_FLOAT), False, SymArenaOutputs, 12, 4 * C3_REC)])
+    return g
+
+
+def c3_points(k, npts, seed=C3_SEED):
+    """P uniform in [-10, 10]^3 from the group's own stream, SoA (3, n)."""
+    rng = np.random.default_rng([seed, 0x50, k])
+    return rng.uniform(-10.0, 10.0, (3, npts)).astype(np.float32)
