@@ -219,7 +219,8 @@ int oslg_execute_batch_noalloc(oslg_system* sys, oslg_group* group, int64_t npoi
 typedef struct oslg_batch oslg_batch;
 
 typedef struct oslg_batch_tuning {
-    int block;       /* threads per CTA = points per work item */
+    int block;       /* threads per CTA */
+    int points_per_thread; /* 1, 2 or 4: a work item is block * points_per_thread points */
     int heap_smem;   /* 1 symbol heap in shared memory, 0 in HBM */
     int grid;        /* persistent CTAs */
     int ctas_per_sm; /* resident CTAs per SM for this shape */
@@ -233,12 +234,14 @@ int oslg_batch_clear(oslg_batch* batch);
 /* Append one request; lowers and uploads the group on first use. */
 int oslg_batch_add(oslg_batch* batch, oslg_group* group, int64_t npoints, const oslg_shaderglobals* globals,
                    void* userdata_base, void* output_base);
-/* block 0 keeps the current size; heap_smem -1 auto; use_graph 0/1. */
-int oslg_batch_set_launch(oslg_batch* batch, int block, int heap_smem, int use_graph);
+/* block 0 keeps the current size; points_per_thread 1/2/4 (0 keeps);
+ * heap_smem -1 auto; use_graph 0/1. */
+int oslg_batch_set_launch(oslg_batch* batch, int block, int points_per_thread, int heap_smem, int use_graph);
 /* Enqueue every request on `stream` (asynchronous). */
 int oslg_batch_execute(oslg_batch* batch, void* stream);
-/* Time `reps` launches of each block size {128, 256, 512} x heap placement
- * {shared, HBM} that fits, keep the fastest for later executes. Writes up
+/* Time `reps` launches of each points-per-thread {1, 2, 4} x block size
+ * {128, 256, 512} x heap placement {shared, HBM} that fits, keep the
+ * fastest for later executes. Writes up
  * to `cap` measured candidates to `results` and their count to `n`. */
 int oslg_batch_autotune(oslg_batch* batch, void* stream, int reps, oslg_batch_tuning* results, int cap, int* n,
                         oslg_batch_tuning* best);

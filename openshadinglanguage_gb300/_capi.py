@@ -46,7 +46,8 @@ GLOBAL_FIELDS = ["P", "dPdx", "dPdy", "dPdz", "I", "dIdx", "dIdy", "N", "Ng", "u
 
 
 class BatchTuningC(ctypes.Structure):
-    _fields_ = [("block", ctypes.c_int), ("heap_smem", ctypes.c_int), ("grid", ctypes.c_int),
+    _fields_ = [("block", ctypes.c_int), ("points_per_thread", ctypes.c_int), ("heap_smem", ctypes.c_int),
+                ("grid", ctypes.c_int),
                 ("ctas_per_sm", ctypes.c_int), ("ms", ctypes.c_float)]
 
 
@@ -95,7 +96,7 @@ _EXPORTS = {
     "oslg_batch_clear": (ctypes.c_int, [ctypes.c_void_p]),
     "oslg_batch_add": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ShaderGlobalsC),
                                       ctypes.c_void_p, ctypes.c_void_p]),
-    "oslg_batch_set_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "oslg_batch_set_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "oslg_batch_execute": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "oslg_batch_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(BatchTuningC),
                                            ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(BatchTuningC)]),

@@ -23,7 +23,8 @@ HOST_SOURCES = ["oslg_oso.cpp", "oslg_lower.cpp", "oslg_capi.cpp"]
 # feature tier (oslg_tier.cu with -DOSLG_TIER=N), in parallel
 CUDA_SOURCES = [("oslg_kernels.cu", "oslg_kernels", []), ("oslg_batch_host.cu", "oslg_batch_host", [])] + [
     ("oslg_tier.cu", "oslg_tier%d" % t, ["-DOSLG_TIER=%d" % t]) for t in range(8)] + [
-    ("oslg_batch.cu", "oslg_batch%d" % m, ["-DOSLG_BATCH_MAXT=%d" % m]) for m in (256, 512)]
+    ("oslg_batch.cu", "oslg_batch%d_%d" % (m, q), ["-DOSLG_BATCH_MAXT=%d" % m, "-DOSLG_BATCH_PPT=%d" % q])
+    for m in (256, 512) for q in (1, 2, 4)]
 
 
 def _run(cmd):

@@ -10,7 +10,8 @@
 namespace oslg {
 
 struct BatchLaunch {
-    int block = 256;     // threads per CTA (points per tile)
+    int block = 256;     // threads per CTA
+    int points_per_thread = 1;  // 1, 2 or 4: a tile is block * points_per_thread points
     int heap_smem = -1;  // 1 shared memory, 0 HBM, -1 shared memory when it fits 100 KiB
     int grid = 0;        // 0: SMs x resident CTAs per SM
     int use_graph = 1;   // replay a captured CUDA graph
@@ -18,6 +19,7 @@ struct BatchLaunch {
 
 struct BatchTuneResult {
     int block;
+    int points_per_thread;
     int heap_smem;
     int grid;
     int ctas_per_sm;

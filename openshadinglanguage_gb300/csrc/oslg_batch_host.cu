@@ -21,12 +21,17 @@
 
 namespace oslg {
 
-int batch_launch_256(bool, unsigned, unsigned, size_t, void*, const dev::BatchArgs&);
-int batch_launch_512(bool, unsigned, unsigned, size_t, void*, const dev::BatchArgs&);
-int batch_occupancy_256(bool, int, size_t, int*);
-int batch_occupancy_512(bool, int, size_t, int*);
-int batch_smem_limit_256(int);
-int batch_smem_limit_512(int);
+#define OSLG_BATCH_VARIANT(M, P)                                                                     \
+    int batch_launch_##M##_##P(bool, unsigned, unsigned, size_t, void*, const dev::BatchArgs&);          \
+    int batch_occupancy_##M##_##P(bool, int, size_t, int*);                                              \
+    int batch_smem_limit_##M##_##P(int);
+OSLG_BATCH_VARIANT(256, 1)
+OSLG_BATCH_VARIANT(256, 2)
+OSLG_BATCH_VARIANT(256, 4)
+OSLG_BATCH_VARIANT(512, 1)
+OSLG_BATCH_VARIANT(512, 2)
+OSLG_BATCH_VARIANT(512, 4)
+#undef OSLG_BATCH_VARIANT
 
 namespace {
 const size_t kBatchStaticSmem = 256;
@@ -35,15 +40,23 @@ bool ok(cudaError_t e, std::string* err, const char* what) {
     if (err) *err = std::string(what) + ": " + cudaGetErrorString(e);
     return false;
 }
-int launch_batch(bool smem, int maxt, unsigned grid, unsigned block, size_t shmem, void* stream,
-                 const dev::BatchArgs& b) {
-    return maxt > 256 ? batch_launch_512(smem, grid, block, shmem, stream, b)
-                      : batch_launch_256(smem, grid, block, shmem, stream, b);
+struct VariantFns {
+    int (*launch)(bool, unsigned, unsigned, size_t, void*, const dev::BatchArgs&);
+    int (*occupancy)(bool, int, size_t, int*);
+    int (*smem_limit)(int);
+};
+// indexed [maxt == 512][log2(ppt)]
+const VariantFns kVariants[2][3] = {
+    { { batch_launch_256_1, batch_occupancy_256_1, batch_smem_limit_256_1 },
+      { batch_launch_256_2, batch_occupancy_256_2, batch_smem_limit_256_2 },
+      { batch_launch_256_4, batch_occupancy_256_4, batch_smem_limit_256_4 } },
+    { { batch_launch_512_1, batch_occupancy_512_1, batch_smem_limit_512_1 },
+      { batch_launch_512_2, batch_occupancy_512_2, batch_smem_limit_512_2 },
+      { batch_launch_512_4, batch_occupancy_512_4, batch_smem_limit_512_4 } } };
+const VariantFns& variant(int maxt, int ppt) {
+    return kVariants[maxt > 256 ? 1 : 0][ppt >= 4 ? 2 : (ppt == 2 ? 1 : 0)];
 }
-int occupancy_batch(bool smem, int maxt, int block, size_t shmem, int* per_sm) {
-    return maxt > 256 ? batch_occupancy_512(smem, block, shmem, per_sm)
-                      : batch_occupancy_256(smem, block, shmem, per_sm);
-}
+int norm_ppt(int p) { return p >= 4 ? 4 : (p == 2 || p == 3 ? 2 : 1); }
 }  // namespace
 
 // Estimated cost of one point of a program: one unit per op, noise and
@@ -123,8 +136,10 @@ int BatchExecutor::ensure_ready(DeviceState& ds, std::string* err) {
         // dynamic shared memory may use the opt-in size less the kernel's
         // static work-item slot (kBatchStaticSmem covers it)
         int dyn = (int)ds.smem_optin - (int)kBatchStaticSmem;
-        if (!ok((cudaError_t)batch_smem_limit_256(dyn), err, "batch kernel attribute")) return OSLG_ERR_CUDA;
-        if (!ok((cudaError_t)batch_smem_limit_512(dyn), err, "batch kernel attribute")) return OSLG_ERR_CUDA;
+        for (int m = 0; m < 2; ++m)
+            for (int q = 0; q < 3; ++q)
+                if (!ok((cudaError_t)kVariants[m][q].smem_limit(dyn), err, "batch kernel attribute"))
+                    return OSLG_ERR_CUDA;
         if (!ok(cudaMalloc(&d_counter_, sizeof(uint32_t)), err, "cudaMalloc counter")) return OSLG_ERR_CUDA;
         ds_ready_ = true;
     }
@@ -139,6 +154,8 @@ int BatchExecutor::build(DeviceState& ds, std::string* err) {
     int block = L.block > 0 ? L.block : 256;
     block = std::max(32, std::min(512, (block + 31) & ~31));
     const int maxt = block > 256 ? 512 : 256;
+    const int ppt = norm_ppt(L.points_per_thread);
+    const int tile = block * ppt;
     uint32_t prog_bytes = 0, slots = 0;
     for (const BatchEntry& e : entries_) {
         const ProgramHeader& h = e.cg->header;
@@ -147,7 +164,7 @@ int BatchExecutor::build(DeviceState& ds, std::string* err) {
         slots = std::max(slots, h.heap_slots);
     }
     prog_bytes = (prog_bytes + 15u) & ~15u;
-    const size_t heap_b = (size_t)slots * block * sizeof(float);
+    const size_t heap_b = (size_t)slots * tile * sizeof(float);
     bool smem = L.heap_smem == 1 || (L.heap_smem < 0 && prog_bytes + heap_b <= 100 * 1024);
     if (smem && prog_bytes + heap_b + kBatchStaticSmem > ds.smem_optin) smem = false;
     const size_t shmem = prog_bytes + (smem ? heap_b : 0);
@@ -156,7 +173,8 @@ int BatchExecutor::build(DeviceState& ds, std::string* err) {
         return OSLG_ERR_LOWER;
     }
     int per_sm = 0;
-    if (!ok((cudaError_t)occupancy_batch(smem, maxt, block, shmem, &per_sm), err, "occupancy")) return OSLG_ERR_CUDA;
+    if (!ok((cudaError_t)variant(maxt, ppt).occupancy(smem, block, shmem, &per_sm), err, "occupancy"))
+        return OSLG_ERR_CUDA;
     if (per_sm < 1) {
         if (err) *err = "batch launch shape does not fit on an SM";
         return OSLG_ERR_LOWER;
@@ -179,7 +197,7 @@ int BatchExecutor::build(DeviceState& ds, std::string* err) {
         J.userdata = static_cast<char*>(e.userdata);
         J.outputs = static_cast<char*>(e.outputs);
         J.G = e.G;
-        const int64_t tiles = (e.npoints + block - 1) / block;
+        const int64_t tiles = (e.npoints + tile - 1) / tile;
         for (int64_t t = 0; t < tiles; ++t) items.push_back(make_uint2((unsigned)j, (unsigned)t));
     }
     if (jobs.size() > jobs_cap_) {
@@ -221,6 +239,7 @@ int BatchExecutor::build(DeviceState& ds, std::string* err) {
     args_.prog_bytes = prog_bytes;
     args_.heap_slots = slots;
     cur_.block = block;
+    cur_.points_per_thread = ppt;
     cur_.heap_smem = smem ? 1 : 0;
     cur_.grid = grid;
     cur_.use_graph = L.use_graph;
@@ -239,8 +258,8 @@ int BatchExecutor::enqueue(void* stream, std::string* err) {
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (!ok(cudaMemsetAsync(d_counter_, 0, sizeof(uint32_t), s), err, "counter reset")) return OSLG_ERR_CUDA;
     if (args_.nitems == 0) return OSLG_OK;
-    if (!ok((cudaError_t)launch_batch(cur_.heap_smem == 1, maxt_, (unsigned)cur_.grid, (unsigned)cur_.block, shmem_,
-                                      stream, args_),
+    if (!ok((cudaError_t)variant(maxt_, cur_.points_per_thread)
+                .launch(cur_.heap_smem == 1, (unsigned)cur_.grid, (unsigned)cur_.block, shmem_, stream, args_),
             err, "batch launch"))
         return OSLG_ERR_CUDA;
     return OSLG_OK;
@@ -286,7 +305,7 @@ int BatchExecutor::execute(DeviceState& ds, void* stream, std::string* err) {
     return OSLG_OK;
 }
 
-// Sweep block size x heap placement, timing `reps` launches of each with
+// Sweep points per thread x block size x heap placement, timing `reps` launches of each with
 // CUDA events on the caller's stream; keep the fastest. Candidates whose
 // shared-memory heap does not fit are skipped.
 int BatchExecutor::autotune(DeviceState& ds, void* stream, int reps, BatchTuneResult* results, int cap, int* n,
@@ -303,10 +322,12 @@ int BatchExecutor::autotune(DeviceState& ds, void* stream, int reps, BatchTuneRe
         return OSLG_ERR_CUDA;
     }
     int rc = OSLG_OK;
+    for (int ppt : { 1, 2, 4 }) {
     for (int block : { 128, 256, 512 }) {
         for (int heap : { 1, 0 }) {
             BatchLaunch l = keep;
             l.block = block;
+            l.points_per_thread = ppt;
             l.heap_smem = heap;
             l.use_graph = 0;
             want_ = l;
@@ -327,6 +348,7 @@ int BatchExecutor::autotune(DeviceState& ds, void* stream, int reps, BatchTuneRe
             ms /= (float)std::max(1, reps);
             if (results && count < cap) {
                 results[count].block = cur_.block;
+                results[count].points_per_thread = cur_.points_per_thread;
                 results[count].heap_smem = cur_.heap_smem;
                 results[count].grid = cur_.grid;
                 results[count].ctas_per_sm = per_sm_;
@@ -340,6 +362,8 @@ int BatchExecutor::autotune(DeviceState& ds, void* stream, int reps, BatchTuneRe
         }
         if (rc != OSLG_OK) break;
     }
+    if (rc != OSLG_OK) break;
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (n) *n = count;
@@ -352,6 +376,7 @@ int BatchExecutor::autotune(DeviceState& ds, void* stream, int reps, BatchTuneRe
 
 void BatchExecutor::last_launch(BatchTuneResult* r) const {
     r->block = cur_.block;
+    r->points_per_thread = cur_.points_per_thread;
     r->heap_smem = cur_.heap_smem;
     r->grid = cur_.grid;
     r->ctas_per_sm = per_sm_;

@@ -466,12 +466,15 @@ int oslg_batch_add(oslg_batch* batch, oslg_group* group, int64_t npoints, const 
     });
 }
 
-int oslg_batch_set_launch(oslg_batch* batch, int block, int heap_smem, int use_graph) {
+int oslg_batch_set_launch(oslg_batch* batch, int block, int points_per_thread, int heap_smem, int use_graph) {
     if (!batch || block < 0 || block > 512 || heap_smem < -1 || heap_smem > 1) return OSLG_ERR_ARG;
+    if (points_per_thread != 0 && points_per_thread != 1 && points_per_thread != 2 && points_per_thread != 4)
+        return OSLG_ERR_ARG;
     BatchLaunch l;
     BatchTuneResult cur;
     batch->ex.last_launch(&cur);
     l.block = block > 0 ? block : (cur.block > 0 ? cur.block : 256);
+    l.points_per_thread = points_per_thread > 0 ? points_per_thread : (cur.points_per_thread > 0 ? cur.points_per_thread : 1);
     l.heap_smem = heap_smem;
     l.use_graph = use_graph ? 1 : 0;
     batch->ex.set_launch(l);
@@ -493,6 +496,7 @@ int oslg_batch_execute(oslg_batch* batch, void* stream) {
 
 static void to_c(const BatchTuneResult& r, oslg_batch_tuning* o) {
     o->block = r.block;
+    o->points_per_thread = r.points_per_thread;
     o->heap_smem = r.heap_smem;
     o->grid = r.grid;
     o->ctas_per_sm = r.ctas_per_sm;
@@ -507,7 +511,7 @@ int oslg_batch_autotune(oslg_batch* batch, void* stream, int reps, oslg_batch_tu
         std::string err;
         int rc = device_init(sys->dev, &err);
         if (rc != OSLG_OK) return fail(sys, rc, err);
-        std::vector<BatchTuneResult> res((size_t)std::max(cap, 8));
+        std::vector<BatchTuneResult> res((size_t)std::max(cap, 32));
         int cnt = 0;
         BatchLaunch bl;
         rc = batch->ex.autotune(sys->dev, stream, reps, res.data(), (int)res.size(), &cnt, &bl, &err);

@@ -1460,13 +1460,31 @@ struct RunCtx {
 
 // Run the whole program for one point per thread (L.pt; lanes past npoints
 // take part in the warp-uniform walk with no active bits).
-template <int TIER>
+template <int TIER, int PPT = 1>
 __device__ __forceinline__ void run_tile(const RunCtx& R, Lane& L, int64_t npoints) {
-    const bool valid = L.pt < npoints;
-    bool act = valid, ext = false, lret = false;
-    uint32_t stk = 0, cnd = 0, brk = 0, cnt = 0;
+    // Each thread carries PPT points of the tile: lane slot li0 + j*blockDim
+    // (heap column) and point pt0 + j*blockDim. Ops are decoded once and run
+    // for every active point of the thread; control state is per point.
+    const uint32_t li0 = L.li;
+    const int64_t pt0 = L.pt;
+    uint32_t validm = 0, actm, extm = 0, lretm = 0;
+    uint32_t stk[PPT], cnd[PPT], brk[PPT], cnt[PPT];
+#pragma unroll
+    for (int j = 0; j < PPT; ++j) {
+        stk[j] = cnd[j] = brk[j] = cnt[j] = 0;
+        if (pt0 + (int64_t)j * blockDim.x < npoints) validm |= 1u << j;
+    }
+    actm = validm;
     long long backedges = 0;
-    if (R.uses_closures && valid) hsetu(L, R.CP.base, 0u);
+    if (R.uses_closures) {
+#pragma unroll
+        for (int j = 0; j < PPT; ++j)
+            if (validm & (1u << j)) {
+                L.li = li0 + j * blockDim.x;
+                hsetu(L, R.CP.base, 0u);
+            }
+        L.li = li0;
+    }
     int pc = 0;
     while (pc < R.nops) {
         const uint4* ow = reinterpret_cast<const uint4*>(R.sops + pc);
@@ -1476,46 +1494,80 @@ __device__ __forceinline__ void run_tile(const RunCtx& R, Lane& L, int64_t npoin
         switch (code) {
         case OP_NOP: break;
         case OP_IF: {
-            int d = (int)a[1];
-            bool c = act && truth(L, a[0]);
-            stk = setbit(stk, d, act);
-            cnd = setbit(cnd, d, c);
-            act = c;
-            if (!__any_sync(FULL, act)) { pc = (int)a[2]; continue; }
+            const int d = (int)a[1];
+            uint32_t nm = 0;
+#pragma unroll
+            for (int j = 0; j < PPT; ++j) {
+                const bool aj = (actm >> j) & 1u;
+                L.li = li0 + j * blockDim.x;
+                const bool c = aj && truth(L, a[0]);
+                stk[j] = setbit(stk[j], d, aj);
+                cnd[j] = setbit(cnd[j], d, c);
+                if (c) nm |= 1u << j;
+            }
+            L.li = li0;
+            actm = nm;
+            if (!__any_sync(FULL, actm != 0)) { pc = (int)a[2]; continue; }
             break;
         }
         case OP_ELSE: {
-            int d = (int)a[1];
-            int ll = (int)a[3];
-            bool off = ext || lret || (ll && (bit(brk, ll - 1) || bit(cnt, ll - 1)));
-            act = bit(stk, d) && !bit(cnd, d) && !off;
-            if (!__any_sync(FULL, act)) { pc = (int)a[2]; continue; }
+            const int d = (int)a[1];
+            const int ll = (int)a[3];
+            uint32_t nm = 0;
+#pragma unroll
+            for (int j = 0; j < PPT; ++j) {
+                const bool off = ((extm | lretm) >> j & 1u) || (ll && (bit(brk[j], ll - 1) || bit(cnt[j], ll - 1)));
+                if (bit(stk[j], d) && !bit(cnd[j], d) && !off) nm |= 1u << j;
+            }
+            actm = nm;
+            if (!__any_sync(FULL, actm != 0)) { pc = (int)a[2]; continue; }
             break;
         }
         case OP_ENDIF: {
-            int d = (int)a[1];
-            int ll = (int)a[3];
-            bool off = ext || lret || (ll && (bit(brk, ll - 1) || bit(cnt, ll - 1)));
-            act = bit(stk, d) && !off;
+            const int d = (int)a[1];
+            const int ll = (int)a[3];
+            uint32_t nm = 0;
+#pragma unroll
+            for (int j = 0; j < PPT; ++j) {
+                const bool off = ((extm | lretm) >> j & 1u) || (ll && (bit(brk[j], ll - 1) || bit(cnt[j], ll - 1)));
+                if (bit(stk[j], d) && !off) nm |= 1u << j;
+            }
+            actm = nm;
             break;
         }
         case OP_LOOP_BEGIN: {
-            int d = (int)a[1];
-            int ll = (int)a[3];
-            stk = setbit(stk, d, act);
-            brk = setbit(brk, ll - 1, false);
-            cnt = setbit(cnt, ll - 1, false);
+            const int d = (int)a[1];
+            const int ll = (int)a[3];
+#pragma unroll
+            for (int j = 0; j < PPT; ++j) {
+                stk[j] = setbit(stk[j], d, (actm >> j) & 1u);
+                brk[j] = setbit(brk[j], ll - 1, false);
+                cnt[j] = setbit(cnt[j], ll - 1, false);
+            }
             break;
         }
         case OP_LOOP_TEST: {
-            act = act && truth(L, a[0]);
-            if (!__any_sync(FULL, act)) { pc = (int)a[2]; continue; }
+            uint32_t nm = 0;
+#pragma unroll
+            for (int j = 0; j < PPT; ++j) {
+                L.li = li0 + j * blockDim.x;
+                if (((actm >> j) & 1u) && truth(L, a[0])) nm |= 1u << j;
+            }
+            L.li = li0;
+            actm = nm;
+            if (!__any_sync(FULL, actm != 0)) { pc = (int)a[2]; continue; }
             break;
         }
         case OP_LOOP_STEP: {
-            int ll = (int)a[3];
-            act = (act || bit(cnt, ll - 1)) && !bit(brk, ll - 1) && !ext && !lret;
-            cnt = setbit(cnt, ll - 1, false);
+            const int ll = (int)a[3];
+            uint32_t nm = 0;
+#pragma unroll
+            for (int j = 0; j < PPT; ++j) {
+                if ((((actm >> j) & 1u) || bit(cnt[j], ll - 1)) && !bit(brk[j], ll - 1) && !((extm | lretm) >> j & 1u))
+                    nm |= 1u << j;
+                cnt[j] = setbit(cnt[j], ll - 1, false);
+            }
+            actm = nm;
             break;
         }
         case OP_JUMP: {
@@ -1528,32 +1580,46 @@ __device__ __forceinline__ void run_tile(const RunCtx& R, Lane& L, int64_t npoin
             continue;
         }
         case OP_LOOP_END: {
-            int d = (int)a[1];
-            int ll = (int)a[3];
-            brk = setbit(brk, ll - 1, false);
-            cnt = setbit(cnt, ll - 1, false);
-            // lanes that broke out of an enclosing loop stay off via the
-            // enclosing ENDIF/LOOP_STEP recomputation
-            act = bit(stk, d) && !ext && !lret;
+            const int d = (int)a[1];
+            const int ll = (int)a[3];
+            uint32_t nm = 0;
+#pragma unroll
+            for (int j = 0; j < PPT; ++j) {
+                brk[j] = setbit(brk[j], ll - 1, false);
+                cnt[j] = setbit(cnt[j], ll - 1, false);
+                // lanes that broke out of an enclosing loop stay off via the
+                // enclosing ENDIF/LOOP_STEP recomputation
+                if (bit(stk[j], d) && !((extm | lretm) >> j & 1u)) nm |= 1u << j;
+            }
+            actm = nm;
             break;
         }
         case OP_BREAK: {
-            int ll = (int)a[3];
-            if (act && ll) brk = setbit(brk, ll - 1, true);
-            act = false;
+            const int ll = (int)a[3];
+#pragma unroll
+            for (int j = 0; j < PPT; ++j)
+                if (((actm >> j) & 1u) && ll) brk[j] = setbit(brk[j], ll - 1, true);
+            actm = 0;
             break;
         }
         case OP_CONTINUE: {
-            int ll = (int)a[3];
-            if (act && ll) cnt = setbit(cnt, ll - 1, true);
-            act = false;
+            const int ll = (int)a[3];
+#pragma unroll
+            for (int j = 0; j < PPT; ++j)
+                if (((actm >> j) & 1u) && ll) cnt[j] = setbit(cnt[j], ll - 1, true);
+            actm = 0;
             break;
         }
-        case OP_RETURN: if (act) lret = true; act = false; break;
-        case OP_EXIT: if (act) ext = true; act = false; break;
-        case OP_LAYER_END: lret = false; act = valid && !ext; break;
-        default:
-            if (act) {
+        case OP_RETURN: lretm |= actm; actm = 0; break;
+        case OP_EXIT: extm |= actm; actm = 0; break;
+        case OP_LAYER_END: lretm = 0; actm = validm & ~extm; break;
+        default: {
+            uint32_t todo = actm;
+#pragma unroll 1
+            for (int j = 0; todo; ++j, todo >>= 1) {
+                if (!(todo & 1u)) continue;
+                L.li = li0 + j * blockDim.x;
+                L.pt = pt0 + (int64_t)j * blockDim.x;
                 switch (code) {
                 case OP_LOAD_GLOBAL: h_load_global(L, a, (*R.G)); break;
                 case OP_LOAD_USERDATA: h_load_userdata(L, a, R.userdata); break;
@@ -1702,7 +1768,10 @@ __device__ __forceinline__ void run_tile(const RunCtx& R, Lane& L, int64_t npoin
                 default: raise_status(R.status, ST_BAD_OPCODE); break;
                 }
             }
+            L.li = li0;
+            L.pt = pt0;
             break;
+        }
         }
         ++pc;
     }
@@ -1753,17 +1822,19 @@ __global__ void __launch_bounds__(256, 2) interp_kernel(const __grid_constant__ 
 // Persistent batch kernel: CTAs take work items (job, tile) from a device
 // counter until the list is exhausted, staging each job's program into
 // shared memory when the job changes. One launch runs every group of the
-// batch; items are ordered so that a CTA mostly stays on one job.
-template <bool SMEM, int TIER, int MAXT>
+// batch; items are ordered so that a CTA mostly stays on one job. A tile is
+// blockDim * PPT points; each thread interleaves PPT of them.
+template <bool SMEM, int TIER, int MAXT, int PPT>
 __global__ void __launch_bounds__(MAXT, 512 / MAXT) batch_kernel(const __grid_constant__ BatchArgs b) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ uint32_t s_item;
     Op* sops = reinterpret_cast<Op*>(smem);
     float* sheap = reinterpret_cast<float*>(smem + (size_t)b.prog_bytes);
+    const uint32_t tile_pts = blockDim.x * PPT;
     Lane L;
-    L.hs = blockDim.x;
+    L.hs = tile_pts;
     L.li = threadIdx.x;
-    L.heap = SMEM ? sheap : (b.gheap + (size_t)blockIdx.x * (size_t)b.heap_slots * blockDim.x);
+    L.heap = SMEM ? sheap : (b.gheap + (size_t)blockIdx.x * (size_t)b.heap_slots * tile_pts);
     L.pool = nullptr;
     RunCtx R;
     R.sops = sops;
@@ -1797,8 +1868,9 @@ __global__ void __launch_bounds__(MAXT, 512 / MAXT) batch_kernel(const __grid_co
             L.pool = spool;
             cur = (int)w.x;
         }
-        L.pt = (int64_t)w.y * blockDim.x + threadIdx.x;
-        run_tile<TIER>(R, L, J->npoints);
+        L.li = threadIdx.x;
+        L.pt = (int64_t)w.y * tile_pts + threadIdx.x;
+        run_tile<TIER, PPT>(R, L, J->npoints);
     }
 }
 

@@ -84,25 +84,16 @@ int device_execute(DeviceState& ds, const ProgramHeader& hdr, const void* d_blob
     if (rc != OSLG_OK) return rc;
     size_t static_bytes = (size_t)hdr.nops * sizeof(Op) + (size_t)((hdr.nconst + 3) & ~3u) * 4;
     // Launch shape: an explicit block/heap placement is honoured; otherwise
-    // pick the largest block (256, 128, 64) whose shared-memory heap fits
-    // 100 KiB per CTA (two CTAs per SM), else the HBM heap with 256 threads.
-    int block = cfg.block > 0 ? cfg.block : 0;
+    // 256 threads, with the symbol heap in shared memory when it fits
+    // 100 KiB per CTA (two CTAs per SM), else in HBM (measured faster than
+    // shrinking the block to fit shared memory).
+    int block = cfg.block > 0 ? cfg.block : 256;
+    if (block > 256) block = 256;
+    block = (block + 31) & ~31;
     bool smem;
-    if (block > 0) {
-        if (block > 256) block = 256;
-        block = (block + 31) & ~31;
+    {
         size_t hb = (size_t)hdr.heap_slots * block * sizeof(float);
         smem = cfg.heap_smem == 1 || (cfg.heap_smem < 0 && static_bytes + hb <= 100 * 1024);
-    } else if (cfg.heap_smem == 0) {
-        block = 256;
-        smem = false;
-    } else {
-        block = 0;
-        for (int b : { 256, 128, 64 }) {
-            if (static_bytes + (size_t)hdr.heap_slots * b * sizeof(float) <= 100 * 1024) { block = b; break; }
-        }
-        smem = block > 0;
-        if (!smem) block = 256;
     }
     size_t heap_bytes = (size_t)hdr.heap_slots * block * sizeof(float);
     if (smem && static_bytes + heap_bytes > ds.smem_optin) smem = false;
@@ -115,8 +106,13 @@ int device_execute(DeviceState& ds, const ProgramHeader& hdr, const void* d_blob
     int per_sm = 0;
     if (!cuda_ok((cudaError_t)fns.occupancy(smem, block, shmem, &per_sm), err, "occupancy")) return OSLG_ERR_CUDA;
     if (per_sm < 1) per_sm = 1;
+    // With the heap in shared memory: one CTA per tile, so the hardware
+    // scheduler balances tiles of uneven cost (data-dependent loops). With
+    // the HBM heap each resident CTA owns one heap slice, so the grid is
+    // the resident CTA count and CTAs stride over the tiles. An explicit
+    // grid always strides.
     int64_t tiles = (npoints + block - 1) / block;
-    int64_t grid = (int64_t)ds.sm_count * per_sm;
+    int64_t grid = smem ? std::min<int64_t>(tiles, 0x7FFFFFFF) : (int64_t)ds.sm_count * per_sm;
     if (cfg.grid > 0) grid = cfg.grid;
     if (grid > tiles) grid = tiles;
     dev::KArgs k;

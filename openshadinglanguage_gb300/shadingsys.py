@@ -235,22 +235,25 @@ class Batch:
                                                ctypes.c_void_p(userdata_ptr or None),
                                                ctypes.c_void_p(output_ptr or None)))
 
-    def set_launch(self, block=0, heap_smem=-1, use_graph=True):
-        self._ss._check(C.lib().oslg_batch_set_launch(self._h, int(block), int(heap_smem), 1 if use_graph else 0))
+    def set_launch(self, block=0, heap_smem=-1, use_graph=True, points_per_thread=0):
+        self._ss._check(C.lib().oslg_batch_set_launch(self._h, int(block), int(points_per_thread), int(heap_smem),
+                                                      1 if use_graph else 0))
 
     def execute(self, stream=0):
         self._ss._check(C.lib().oslg_batch_execute(self._h, ctypes.c_void_p(stream or None)))
 
     @staticmethod
     def _tuning(t):
-        return dict(block=t.block, heap_smem=t.heap_smem, grid=t.grid, ctas_per_sm=t.ctas_per_sm, ms=t.ms)
+        return dict(block=t.block, points_per_thread=t.points_per_thread, heap_smem=t.heap_smem, grid=t.grid,
+                    ctas_per_sm=t.ctas_per_sm, ms=t.ms)
 
     def autotune(self, stream=0, reps=3):
-        """Sweep block {128,256,512} x heap {shared, HBM}; returns (best, all)."""
-        res = (C.BatchTuningC * 8)()
+        """Sweep points per thread {1,2,4} x block {128,256,512} x heap
+        {shared, HBM}; returns (best, all measured)."""
+        res = (C.BatchTuningC * 32)()
         n = ctypes.c_int(0)
         best = C.BatchTuningC()
-        self._ss._check(C.lib().oslg_batch_autotune(self._h, ctypes.c_void_p(stream or None), int(reps), res, 8,
+        self._ss._check(C.lib().oslg_batch_autotune(self._h, ctypes.c_void_p(stream or None), int(reps), res, 32,
                                                     ctypes.byref(n), ctypes.byref(best)))
         return self._tuning(best), [self._tuning(res[i]) for i in range(n.value)]
 

@@ -57,12 +57,12 @@ def run_plain(ss, reqs):
     return [o.cpu().numpy() for o in outs]
 
 
-def run_batch(ss, reqs, use_graph, block=256, heap=-1, times=1, tune=False):
+def run_batch(ss, reqs, use_graph, block=256, heap=-1, times=1, tune=False, ppt=1):
     outs = outputs(reqs)
     b = ss.batch()
     for r, o in zip(reqs, outs):
         b.add(r.g, r.n, r.G, 0, o.data_ptr())
-    b.set_launch(block=block, heap_smem=heap, use_graph=use_graph)
+    b.set_launch(block=block, heap_smem=heap, use_graph=use_graph, points_per_thread=ppt)
     st = torch.cuda.current_stream().cuda_stream
     tuned = None
     if tune:
@@ -95,11 +95,12 @@ def test_plain_matches_oracle(c3):
         assert same(p.reshape(r.n, r.rec), ref), r.name
 
 
-@pytest.mark.parametrize("block,heap", [(256, -1), (128, 1), (512, 0), (256, 0)])
-def test_persistent_batch_matches_plain(c3, block, heap):
+@pytest.mark.parametrize("block,heap,ppt", [(256, -1, 1), (128, 1, 1), (512, 0, 1), (256, 0, 2), (32, 1, 4),
+                                            (512, 0, 4), (64, 1, 2)])
+def test_persistent_batch_matches_plain(c3, block, heap, ppt):
     ss, reqs, plain = c3
-    got, launch, _ = run_batch(ss, reqs, use_graph=False, block=block, heap=heap)
-    assert launch["block"] == block
+    got, launch, _ = run_batch(ss, reqs, use_graph=False, block=block, heap=heap, ppt=ppt)
+    assert launch["block"] == block and launch["points_per_thread"] == ppt
     if heap >= 0:
         assert launch["heap_smem"] == heap
     for r, a, b in zip(reqs, got, plain):
@@ -117,7 +118,8 @@ def test_graph_replay_matches_plain(c3):
 def test_autotuned_batch_matches_plain(c3):
     ss, reqs, plain = c3
     got, launch, (best, cands) = run_batch(ss, reqs, use_graph=True, tune=True)
-    assert len(cands) >= 3
+    assert len(cands) >= 9
+    assert {c["points_per_thread"] for c in cands} == {1, 2, 4}
     assert best["ms"] == min(c["ms"] for c in cands)
     assert launch["block"] == best["block"] and launch["heap_smem"] == best["heap_smem"]
     for r, a, b in zip(reqs, got, plain):
