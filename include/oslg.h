@@ -248,6 +248,57 @@ int oslg_batch_autotune(oslg_batch* batch, void* stream, int reps, oslg_batch_tu
 /* Launch shape of the last built batch. */
 int oslg_batch_last_launch(oslg_batch* batch, oslg_batch_tuning* out);
 
+/* ---- shading server ---------------------------------------------------------
+ * No counterpart in the reference (renderers call execute() per batch). A
+ * server keeps programs resident and runs requests submitted from any host
+ * thread with continuous batching: a worker admits waiting requests, in
+ * arrival order, into "waves" while device memory (an arena sized from
+ * budget_bytes) and stream slots allow, copies their inputs from host
+ * memory, runs each wave as one persistent batch launch and copies the
+ * outputs back; several waves are in flight at once. Inputs are the host
+ * fields of `host_globals` (data != NULL: SoA planes of npoints floats,
+ * plane_stride apart); they and `host_output` must stay valid until the
+ * request completes (pinned memory makes the copies asynchronous).
+ * Outputs are written as oslg_execute_batch would write them into a zeroed
+ * buffer of output_bytes. Userdata is not supported in served requests. */
+typedef struct oslg_server oslg_server;
+
+typedef struct oslg_server_options {
+    size_t budget_bytes;    /* device memory for arena + scratch heaps (default 40 GiB) */
+    int streams;            /* waves in flight (default 3) */
+    int block;              /* threads per CTA of a wave (default 512) */
+    int points_per_thread;  /* 1, 2 or 4 (default 1) */
+    int64_t max_wave_points;
+    int max_wave_requests;
+    size_t arena_bytes;     /* request memory (0: what the budget leaves) */
+} oslg_server_options;
+
+typedef struct oslg_request_stats {
+    int64_t submit_ns, admit_ns, done_ns;  /* host steady clock */
+    int wave;
+    int status;
+} oslg_request_stats;
+
+typedef struct oslg_server_stats {
+    uint64_t submitted, completed, failed, waves;
+    int64_t points_done;
+    size_t arena_capacity, arena_high_water, program_bytes, scratch_bytes;
+    int in_flight_waves, pending;
+} oslg_server_stats;
+
+/* opts NULL: defaults. Starts the worker thread. */
+int oslg_server_create(oslg_system* sys, const oslg_server_options* opts, oslg_server** out);
+/* Finishes every submitted request, then stops. */
+int oslg_server_destroy(oslg_server* server);
+/* Lower, upload and keep a group resident ahead of its first request. */
+int oslg_server_register(oslg_server* server, oslg_group* group);
+int oslg_server_submit(oslg_server* server, oslg_group* group, int64_t npoints, const oslg_shaderglobals* host_globals,
+                       void* host_output, size_t output_bytes, uint64_t* ticket);
+/* timeout_ms < 0 waits forever; a finished request's ticket is released. */
+int oslg_server_wait(oslg_server* server, uint64_t ticket, int timeout_ms, oslg_request_stats* stats);
+int oslg_server_poll(oslg_server* server, uint64_t ticket, int* done, oslg_request_stats* stats);
+int oslg_server_get_stats(oslg_server* server, oslg_server_stats* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -51,6 +51,24 @@ class BatchTuningC(ctypes.Structure):
                 ("ctas_per_sm", ctypes.c_int), ("ms", ctypes.c_float)]
 
 
+class ServerOptionsC(ctypes.Structure):
+    _fields_ = [("budget_bytes", ctypes.c_size_t), ("streams", ctypes.c_int), ("block", ctypes.c_int),
+                ("points_per_thread", ctypes.c_int), ("max_wave_points", ctypes.c_int64),
+                ("max_wave_requests", ctypes.c_int), ("arena_bytes", ctypes.c_size_t)]
+
+
+class RequestStatsC(ctypes.Structure):
+    _fields_ = [("submit_ns", ctypes.c_int64), ("admit_ns", ctypes.c_int64), ("done_ns", ctypes.c_int64),
+                ("wave", ctypes.c_int), ("status", ctypes.c_int)]
+
+
+class ServerStatsC(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("failed", ctypes.c_uint64),
+                ("waves", ctypes.c_uint64), ("points_done", ctypes.c_int64), ("arena_capacity", ctypes.c_size_t),
+                ("arena_high_water", ctypes.c_size_t), ("program_bytes", ctypes.c_size_t),
+                ("scratch_bytes", ctypes.c_size_t), ("in_flight_waves", ctypes.c_int), ("pending", ctypes.c_int)]
+
+
 class ShaderGlobalsC(ctypes.Structure):
     _fields_ = [(n, FieldC) for n in GLOBAL_FIELDS]
 
@@ -101,6 +119,18 @@ _EXPORTS = {
     "oslg_batch_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(BatchTuningC),
                                            ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(BatchTuningC)]),
     "oslg_batch_last_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BatchTuningC)]),
+    "oslg_server_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ServerOptionsC),
+                                          ctypes.POINTER(ctypes.c_void_p)]),
+    "oslg_server_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "oslg_server_register": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "oslg_server_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                          ctypes.POINTER(ShaderGlobalsC), ctypes.c_void_p, ctypes.c_size_t,
+                                          ctypes.POINTER(ctypes.c_uint64)]),
+    "oslg_server_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int,
+                                        ctypes.POINTER(RequestStatsC)]),
+    "oslg_server_poll": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.POINTER(ctypes.c_int),
+                                        ctypes.POINTER(RequestStatsC)]),
+    "oslg_server_get_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ServerStatsC)]),
 }
 
 _lib = None

@@ -21,7 +21,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST_SOURCES = ["oslg_oso.cpp", "oslg_lower.cpp", "oslg_capi.cpp"]
 # (source, object name, extra flags): the interpreter is compiled once per
 # feature tier (oslg_tier.cu with -DOSLG_TIER=N), in parallel
-CUDA_SOURCES = [("oslg_kernels.cu", "oslg_kernels", []), ("oslg_batch_host.cu", "oslg_batch_host", [])] + [
+CUDA_SOURCES = [("oslg_kernels.cu", "oslg_kernels", []), ("oslg_batch_host.cu", "oslg_batch_host", []),
+                ("oslg_serve.cu", "oslg_serve", [])] + [
     ("oslg_tier.cu", "oslg_tier%d" % t, ["-DOSLG_TIER=%d" % t]) for t in range(8)] + [
     ("oslg_batch.cu", "oslg_batch%d_%d" % (m, q), ["-DOSLG_BATCH_MAXT=%d" % m, "-DOSLG_BATCH_PPT=%d" % q])
     for m in (256, 512) for q in (1, 2, 4)]

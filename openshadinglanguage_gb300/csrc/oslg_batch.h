@@ -28,6 +28,14 @@ struct BatchTuneResult {
 
 double program_cost(const ProgramHeader& hdr, const Op* ops);
 
+// Launch one variant of the batch kernel (maxt 256/512, ppt 1/2/4).
+int batch_variant_launch(int maxt, int ppt, bool smem, unsigned grid, unsigned block, size_t shmem, void* stream,
+                         const dev::BatchArgs& b);
+int batch_variant_occupancy(int maxt, int ppt, bool smem, int block, size_t shmem, int* per_sm);
+// Allow every variant its dynamic shared memory (once per device).
+int batch_variants_prepare(const DeviceState& ds);
+size_t batch_static_smem();
+
 class BatchExecutor {
 public:
     ~BatchExecutor();

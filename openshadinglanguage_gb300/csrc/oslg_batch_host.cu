@@ -59,6 +59,25 @@ const VariantFns& variant(int maxt, int ppt) {
 int norm_ppt(int p) { return p >= 4 ? 4 : (p == 2 || p == 3 ? 2 : 1); }
 }  // namespace
 
+// Shared entry points for other launchers of the batch kernel (the server).
+int batch_variant_launch(int maxt, int ppt, bool smem, unsigned grid, unsigned block, size_t shmem, void* stream,
+                         const dev::BatchArgs& b) {
+    return variant(maxt, norm_ppt(ppt)).launch(smem, grid, block, shmem, stream, b);
+}
+int batch_variant_occupancy(int maxt, int ppt, bool smem, int block, size_t shmem, int* per_sm) {
+    return variant(maxt, norm_ppt(ppt)).occupancy(smem, block, shmem, per_sm);
+}
+int batch_variants_prepare(const DeviceState& ds) {
+    int dyn = (int)ds.smem_optin - (int)kBatchStaticSmem;
+    for (int m = 0; m < 2; ++m)
+        for (int q = 0; q < 3; ++q) {
+            int e = kVariants[m][q].smem_limit(dyn);
+            if (e != 0) return e;
+        }
+    return 0;
+}
+size_t batch_static_smem() { return kBatchStaticSmem; }
+
 // Estimated cost of one point of a program: one unit per op, noise and
 // transcendental ops weighted by their measured relative cost, ops inside
 // loops by an expected trip count of 8 per nesting level.

@@ -5,10 +5,12 @@
 // ErrorHandler, src/liboslexec/context.cpp:443-451).
 #include <cstring>
 #include <exception>
+#include <memory>
 #include <new>
 
 #include "../../include/oslg.h"
 #include "oslg_batch.h"
+#include "oslg_serve.h"
 #include "oslg_exec.h"
 #include "oslg_host.h"
 
@@ -27,6 +29,11 @@ struct oslg_group {
 struct oslg_batch {
     oslg_system* sys;
     oslg::BatchExecutor ex;
+};
+
+struct oslg_server {
+    oslg_system* sys;
+    std::unique_ptr<oslg::ShadingServer> srv;
 };
 
 namespace oslg {
@@ -532,5 +539,116 @@ int oslg_batch_last_launch(oslg_batch* batch, oslg_batch_tuning* out) {
     BatchTuneResult r;
     batch->ex.last_launch(&r);
     to_c(r, out);
+    return OSLG_OK;
+}
+
+// ---- shading server ---------------------------------------------------------------
+int oslg_server_create(oslg_system* sys, const oslg_server_options* opts, oslg_server** out) {
+    if (!sys || !out) return OSLG_ERR_ARG;
+    return guarded(sys, [&]() {
+        std::string err;
+        int rc = device_init(sys->dev, &err);
+        if (rc != OSLG_OK) return fail(sys, rc, err);
+        ServerOptions o;
+        if (opts) {
+            if (opts->budget_bytes) o.budget_bytes = opts->budget_bytes;
+            if (opts->streams) o.streams = opts->streams;
+            if (opts->block) o.block = opts->block;
+            if (opts->points_per_thread) o.points_per_thread = opts->points_per_thread;
+            if (opts->max_wave_points) o.max_wave_points = opts->max_wave_points;
+            if (opts->max_wave_requests) o.max_wave_requests = opts->max_wave_requests;
+            o.arena_bytes = opts->arena_bytes;
+        }
+        if (o.points_per_thread != 1 && o.points_per_thread != 2 && o.points_per_thread != 4)
+            return fail(sys, OSLG_ERR_ARG, "points_per_thread must be 1, 2 or 4");
+        std::unique_ptr<oslg_server> s(new oslg_server);
+        s->sys = sys;
+        s->srv.reset(new ShadingServer(sys->dev, o));
+        rc = s->srv->start(&err);
+        if (rc != OSLG_OK) return fail(sys, rc, err);
+        *out = s.release();
+        return OSLG_OK;
+    });
+}
+
+int oslg_server_destroy(oslg_server* server) {
+    if (!server) return OSLG_ERR_ARG;
+    server->srv->stop();
+    delete server;
+    return OSLG_OK;
+}
+
+int oslg_server_register(oslg_server* server, oslg_group* group) {
+    if (!server || !group) return OSLG_ERR_ARG;
+    oslg_system* sys = server->sys;
+    return guarded(sys, [&]() {
+        int rc = ensure_compiled(sys, group, true);
+        if (rc != OSLG_OK) return rc;
+        std::string err;
+        rc = server->srv->register_program(*group->g.compiled, &err);
+        if (rc != OSLG_OK) return fail(sys, rc, err);
+        return OSLG_OK;
+    });
+}
+
+int oslg_server_submit(oslg_server* server, oslg_group* group, int64_t npoints, const oslg_shaderglobals* host_globals,
+                       void* host_output, size_t output_bytes, uint64_t* ticket) {
+    if (!server || !group || !host_globals || !ticket || npoints < 0) return OSLG_ERR_ARG;
+    oslg_system* sys = server->sys;
+    return guarded(sys, [&]() {
+        int rc = ensure_compiled(sys, group, true);
+        if (rc != OSLG_OK) return rc;
+        std::string err;
+        rc = server->srv->submit(*group->g.compiled, npoints, *host_globals, host_output, output_bytes, ticket, &err);
+        if (rc != OSLG_OK) return fail(sys, rc, err);
+        return OSLG_OK;
+    });
+}
+
+static void to_c(const RequestStats& r, oslg_request_stats* o) {
+    o->submit_ns = r.submit_ns;
+    o->admit_ns = r.admit_ns;
+    o->done_ns = r.done_ns;
+    o->wave = r.wave;
+    o->status = r.status;
+}
+
+int oslg_server_wait(oslg_server* server, uint64_t ticket, int timeout_ms, oslg_request_stats* stats) {
+    if (!server) return OSLG_ERR_ARG;
+    RequestStats st;
+    std::string err;
+    int rc = server->srv->wait(ticket, timeout_ms, &st, &err);
+    if (stats) to_c(st, stats);
+    if (rc != OSLG_OK) return fail(server->sys, rc, err);
+    return OSLG_OK;
+}
+
+int oslg_server_poll(oslg_server* server, uint64_t ticket, int* done, oslg_request_stats* stats) {
+    if (!server || !done) return OSLG_ERR_ARG;
+    RequestStats st;
+    std::string err;
+    bool d = false;
+    int rc = server->srv->poll(ticket, &d, &st, &err);
+    *done = d ? 1 : 0;
+    if (d && stats) to_c(st, stats);
+    if (rc != OSLG_OK) return fail(server->sys, rc, err);
+    return OSLG_OK;
+}
+
+int oslg_server_get_stats(oslg_server* server, oslg_server_stats* out) {
+    if (!server || !out) return OSLG_ERR_ARG;
+    ServerStats s;
+    server->srv->stats(&s);
+    out->submitted = s.submitted;
+    out->completed = s.completed;
+    out->failed = s.failed;
+    out->waves = s.waves;
+    out->points_done = s.points_done;
+    out->arena_capacity = s.arena_capacity;
+    out->arena_high_water = s.arena_high_water;
+    out->program_bytes = s.program_bytes;
+    out->scratch_bytes = s.scratch_bytes;
+    out->in_flight_waves = s.in_flight_waves;
+    out->pending = s.pending;
     return OSLG_OK;
 }

@@ -195,6 +195,10 @@ class ShadingSystem:
         """A persistent multi-group batch on this system (see Batch)."""
         return Batch(self)
 
+    def server(self, **options):
+        """A continuous-batching shading server on this system (see Server)."""
+        return Server(self, **options)
+
     def device_status(self):
         bits = ctypes.c_uint32(0)
         self._check(C.lib().oslg_device_status(self._h, ctypes.byref(bits)))
@@ -261,3 +265,76 @@ class Batch:
         t = C.BatchTuningC()
         self._ss._check(C.lib().oslg_batch_last_launch(self._h, ctypes.byref(t)))
         return self._tuning(t)
+
+
+class Server:
+    """Continuous-batching request server (include/oslg.h, oslg_server_*).
+    Requests carry host inputs (globals whose per-point fields are host
+    arrays) and a host output buffer; submit() returns a ticket, wait()
+    blocks until that request's outputs are in the host buffer and returns
+    its timing (host steady-clock nanoseconds)."""
+
+    def __init__(self, ss, budget_bytes=40 << 30, streams=3, block=512, points_per_thread=1,
+                 max_wave_points=8 << 20, max_wave_requests=512, arena_bytes=0):
+        self._ss = ss
+        o = C.ServerOptionsC(int(budget_bytes), int(streams), int(block), int(points_per_thread),
+                             int(max_wave_points), int(max_wave_requests), int(arena_bytes))
+        h = ctypes.c_void_p()
+        ss._check(C.lib().oslg_server_create(ss._h, ctypes.byref(o), ctypes.byref(h)))
+        self._h = h
+        self._keep = {}
+
+    def close(self):
+        if self._h:
+            C.lib().oslg_server_destroy(self._h)
+            self._h = None
+            self._keep = {}
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def register(self, group):
+        self._ss._check(C.lib().oslg_server_register(self._h, group.handle))
+
+    def submit(self, group, npoints, globals_c, output, output_bytes=None):
+        """output: a host array (numpy or CPU tensor) or an address with
+        output_bytes. Inputs and output must stay alive until wait()."""
+        if hasattr(output, "data_ptr"):
+            ptr, nb = output.data_ptr(), output.numel() * output.element_size()
+        elif hasattr(output, "ctypes"):
+            ptr, nb = output.ctypes.data, output.nbytes
+        else:
+            ptr, nb = int(output), int(output_bytes)
+        t = ctypes.c_uint64(0)
+        self._ss._check(C.lib().oslg_server_submit(self._h, group.handle, int(npoints), ctypes.byref(globals_c),
+                                                   ctypes.c_void_p(ptr), ctypes.c_size_t(nb), ctypes.byref(t)))
+        self._keep[t.value] = (globals_c, output)
+        return t.value
+
+    @staticmethod
+    def _stats(st):
+        return dict(submit_ns=st.submit_ns, admit_ns=st.admit_ns, done_ns=st.done_ns, wave=st.wave, status=st.status)
+
+    def wait(self, ticket, timeout_ms=-1):
+        st = C.RequestStatsC()
+        rc = C.lib().oslg_server_wait(self._h, ctypes.c_uint64(ticket), int(timeout_ms), ctypes.byref(st))
+        self._keep.pop(ticket, None)
+        self._ss._check(rc)
+        return self._stats(st)
+
+    def poll(self, ticket):
+        st = C.RequestStatsC()
+        done = ctypes.c_int(0)
+        rc = C.lib().oslg_server_poll(self._h, ctypes.c_uint64(ticket), ctypes.byref(done), ctypes.byref(st))
+        if done.value:
+            self._keep.pop(ticket, None)
+        self._ss._check(rc)
+        return self._stats(st) if done.value else None
+
+    def stats(self):
+        s = C.ServerStatsC()
+        self._ss._check(C.lib().oslg_server_get_stats(self._h, ctypes.byref(s)))
+        return {k: getattr(s, k) for k, _ in C.ServerStatsC._fields_}

@@ -49,3 +49,18 @@ def test_batch_handle_on_cpu():
     b.set_launch(block=128, heap_smem=0, use_graph=False)
     b.clear()
     b.close()
+
+
+def test_serving_load_generator():
+    torch = pytest.importorskip("torch")
+    from openshadinglanguage_gb300 import serving
+    arr = serving.poisson_arrivals(1000.0, 20000, seed=3)
+    gaps = np.diff(np.concatenate([[0.0], arr]))
+    assert abs(gaps.mean() - 1e-3) < 5e-5 and np.all(gaps > 0)
+    assert np.all(serving.poisson_arrivals(None, 5) == 0)
+    groups = ["g%d" % i for i in range(64)]
+    reqs = serving.make_requests(torch, groups, 50, seed=0xC4, pin=False)
+    again = serving.make_requests(torch, groups, 50, seed=0xC4, pin=False)
+    assert [r.n for r in reqs] == [r.n for r in again]
+    assert all(256 <= r.n <= 262144 for r in reqs)
+    assert all(r.P.shape == (3, r.n) and float(r.P.abs().max()) <= 10.0 for r in reqs)
