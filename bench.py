@@ -99,6 +99,7 @@ class FbmCell:
 
     def __init__(self, W=1024, H=1024):
         self.W, self.H, self.n = W, H, W * H
+        self.name = "fbm_cell_%dx%d" % (W, H)
 
     def build(self, torch, og, shaders):
         from helpers import grid_globals, pixel_grid, single_layer_group
@@ -157,6 +158,7 @@ class LayeredClosure:
         from openshadinglanguage_gb300 import workloads
         self.wl = workloads
         self.W, self.H, self.n = W, H, W * H
+        self.name = "layered_closure_%dx%d" % (W, H)
         self.rec = workloads.C2_STRIDE // 4
 
     def build_host(self, og, shaders):
@@ -203,7 +205,89 @@ class LayeredClosure:
 
 
 WORKLOADS = {FbmCell.name: FbmCell, LayeredClosure.name: LayeredClosure}
-DEFAULT_WORKLOAD = FbmCell.name
+DEFAULT_WORKLOAD = LayeredClosure.name
+
+
+def bench_batching(torch, og, reps=5):
+    """64 seeded random groups (20-200 ops, log-uniform 1K-1M points): the
+    plain executor launched per group against the persistent batch launch
+    (autotuned, CUDA-graph replay). Same outputs bit for bit."""
+    from openshadinglanguage_gb300 import workloads
+    ss = og.ShadingSystem()
+    specs = workloads.c3_specs()
+    reqs = []
+    for k, (name, oso, npts, _) in enumerate(specs):
+        g = workloads.c3_group(ss, name, oso)
+        dP = torch.from_numpy(workloads.c3_points(k, npts)).cuda()
+        reqs.append((g, npts, og.make_globals(P=dP), dP, torch.zeros(npts * workloads.C3_REC, device="cuda")))
+    total = sum(r[1] for r in reqs)
+    st = torch.cuda.current_stream()
+    sh = st.cuda_stream
+
+    def timed(fn):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(reps):
+            fn()
+        e1.record(st)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    def plain():
+        for g, n, G, _, o in reqs:
+            ss.execute_batch(g, n, G, 0, o.data_ptr(), sh)
+
+    t_plain = timed(plain)
+    b = ss.batch()
+    for g, n, G, _, o in reqs:
+        b.add(g, n, G, 0, o.data_ptr())
+    best, cands = b.autotune(sh, reps=2)
+    b.set_launch(block=best["block"], heap_smem=best["heap_smem"], use_graph=True,
+                 points_per_thread=best["points_per_thread"])
+    t_batch = timed(lambda: b.execute(sh))
+    b.close()
+    return {"workload": "64 random groups, %d points, seed 0xC3" % total, "points": total,
+            "plain_ms": t_plain, "plain_mpts": total / t_plain / 1e3,
+            "persistent_ms": t_batch, "persistent_mpts": total / t_batch / 1e3,
+            "speedup_vs_plain": t_plain / t_batch,
+            "autotuned": {k: best[k] for k in ("block", "points_per_thread", "heap_smem", "grid")},
+            "candidates": len(cands), "launches_per_step": {"plain": len(reqs), "persistent": 1}}
+
+
+def bench_serving(torch, og, nreq=600):
+    """Poisson request stream over the 64 groups (point counts log-uniform
+    in [256, 262144]) at 10/50/90/100% of the server's measured peak, served
+    with continuous batching and by the plain executor per request."""
+    from openshadinglanguage_gb300 import serving, workloads
+    ss = og.ShadingSystem()
+    groups = [workloads.c3_group(ss, name, oso) for (name, oso, _, _) in workloads.c3_specs()]
+    reqs = serving.make_requests(torch, groups, nreq)
+    srv = ss.server(budget_bytes=40 << 30, streams=3)
+    for g in groups:
+        srv.register(g)
+    serving.run_server(srv, reqs[:50])
+    peak = serving.run_server(srv, reqs)
+    peak_rps = len(reqs) / peak["makespan_s"]
+    plain_peak = serving.run_plain(torch, ss, reqs)
+    loads = {}
+    for frac in (0.1, 0.5, 0.9, 1.0):
+        rate = frac * peak_rps
+        a = serving.run_server(srv, reqs, rate_rps=rate)
+        p = serving.run_plain(torch, ss, reqs, rate_rps=rate)
+        loads["%d%%" % int(frac * 100)] = {
+            "offered_rps": rate,
+            "served": {k: a[k] for k in ("p50_ms", "p99_ms", "throughput_mpts")},
+            "plain": {k: p[k] for k in ("p50_ms", "p99_ms", "throughput_mpts")}}
+    st = srv.stats()
+    srv.close()
+    return {"requests": nreq, "points": sum(r.n for r in reqs), "hbm_budget_gb": 40,
+            "peak_rps": peak_rps, "served_peak_mpts": peak["throughput_mpts"],
+            "plain_peak_mpts": plain_peak["throughput_mpts"], "loads": loads,
+            "arena_high_water_mb": st["arena_high_water"] / 2 ** 20, "waves": st["waves"],
+            "latency": "arrival to outputs in host memory (pinned), host monotonic clock"}
 
 
 def cpu_reference(wl, og, budget_s=2.0):
@@ -232,8 +316,12 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--size", type=int, default=0,
+                    help="grid width = height override (a smaller case of the workload, e.g. for profiling)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the 64-group batching and the serving measurements")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -245,7 +333,7 @@ def main():
     from openshadinglanguage_gb300 import shaders
     from oracle.build import build as build_oracle
 
-    wl = WORKLOADS[args.workload]()
+    wl = WORKLOADS[args.workload](args.size, args.size) if args.size > 0 else WORKLOADS[args.workload]()
 
     if args.impl == "reference":
         if rank != 0:
@@ -379,6 +467,9 @@ def main():
                          "sms": sms},
         "device_status": status,
     }
+    if not args.no_extras and world == 1:
+        line["batching"] = bench_batching(torch, og)
+        line["serving"] = bench_serving(torch, og)
     if not args.no_cpu_baseline:
         from helpers import oracle_run  # noqa: F401
         build_oracle()

@@ -84,16 +84,24 @@ int device_execute(DeviceState& ds, const ProgramHeader& hdr, const void* d_blob
     if (rc != OSLG_OK) return rc;
     size_t static_bytes = (size_t)hdr.nops * sizeof(Op) + (size_t)((hdr.nconst + 3) & ~3u) * 4;
     // Launch shape: an explicit block/heap placement is honoured; otherwise
-    // 256 threads, with the symbol heap in shared memory when it fits
-    // 100 KiB per CTA (two CTAs per SM), else in HBM (measured faster than
-    // shrinking the block to fit shared memory).
+    // 256 threads, with the symbol heap in shared memory when that keeps as
+    // many CTAs resident per SM as the HBM-heap kernel gets (its registers
+    // allow two), else in HBM (measured faster than shrinking the block to
+    // fit shared memory).
+    const TierFns& fns = tier_fns((int)((hdr.flags >> 8) & 7u));
     int block = cfg.block > 0 ? cfg.block : 256;
     if (block > 256) block = 256;
     block = (block + 31) & ~31;
-    bool smem;
-    {
+    bool smem = cfg.heap_smem == 1;
+    if (cfg.heap_smem < 0) {
         size_t hb = (size_t)hdr.heap_slots * block * sizeof(float);
-        smem = cfg.heap_smem == 1 || (cfg.heap_smem < 0 && static_bytes + hb <= 100 * 1024);
+        if (static_bytes + hb <= ds.smem_optin) {
+            int occ_s = 0, occ_h = 0;
+            if (!cuda_ok((cudaError_t)fns.occupancy(true, block, static_bytes + hb, &occ_s), err, "occupancy") ||
+                !cuda_ok((cudaError_t)fns.occupancy(false, block, static_bytes, &occ_h), err, "occupancy"))
+                return OSLG_ERR_CUDA;
+            smem = occ_s >= 1 && occ_s >= std::min(occ_h, 2);
+        }
     }
     size_t heap_bytes = (size_t)hdr.heap_slots * block * sizeof(float);
     if (smem && static_bytes + heap_bytes > ds.smem_optin) smem = false;
@@ -102,7 +110,6 @@ int device_execute(DeviceState& ds, const ProgramHeader& hdr, const void* d_blob
         if (err) *err = "program does not fit in shared memory";
         return OSLG_ERR_LOWER;
     }
-    const TierFns& fns = tier_fns((int)((hdr.flags >> 8) & 7u));
     int per_sm = 0;
     if (!cuda_ok((cudaError_t)fns.occupancy(smem, block, shmem, &per_sm), err, "occupancy")) return OSLG_ERR_CUDA;
     if (per_sm < 1) per_sm = 1;
