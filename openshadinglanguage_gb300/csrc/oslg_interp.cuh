@@ -858,6 +858,53 @@ static __device__ void h_luminance(const Lane& L, const uint32_t* a) {
         stf(L, r, d, ldf(L, c, 0, d) * sx + ldf(L, c, 1, d) * sy + ldf(L, c, 2, d) * sz);
 }
 
+// blackbody (src/liboslexec/opcolor_impl.h:510-575): a2 = constant table
+// of N RGB^(1/5) entries, then the XYZ->RGB matrix and the CIE table; a3 = N
+static __device__ void h_blackbody(const Lane& L, const uint32_t* a) {
+    const uint32_t r = a[0];
+    const float T = ldf(L, a[1], 0, 0);
+    const uint32_t tb = a[2];
+    const int N = (int)a[3];
+    float rgb[3];
+    if (T < 800.0f) {
+        rgb[0] = 1.0e-6f; rgb[1] = 0.0f; rgb[2] = 0.0f;
+    } else if (T < 12000.0f) {
+        const float ic = (float)cbrt((double)((T - 800.0f) / 2.0f));
+        const float t = ic * ic;
+        int ti = (int)t;
+        if (ti > N - 2) ti = N - 2;
+        const float rem = t - (float)ti;
+        for (int c = 0; c < 3; ++c) {
+            const float x0 = __uint_as_float(ldw(L, tb, ti * 3 + c)), x1 = __uint_as_float(ldw(L, tb, ti * 3 + 3 + c));
+            const float v = x0 * (1.0f - rem) + x1 * rem;
+            const float v2 = v * v, v4 = v2 * v2;
+            rgb[c] = v4 * v;
+        }
+    } else {
+        float X = 0.0f, Y = 0.0f, Z = 0.0f;
+        const float dlambda = (float)(5.0f * 1e-9);
+        const int cie = N * 3 + 9;
+        for (int i = 0; i < 81; ++i) {
+            const float lambda = 380.0f + 5.0f * (float)i;
+            const float wlm = lambda * 1e-9f;
+            const float wlm2 = wlm * wlm, wlm4 = wlm2 * wlm2, wlm5 = wlm4 * wlm;
+            const float inv5 = 1.0f / wlm5;
+            const float e = (float)expm1((double)(1.4388e-2f / (wlm * T)));
+            const float Me = ((3.74183e-16f * inv5) / e) * dlambda;
+            X += Me * __uint_as_float(ldw(L, tb, cie + i * 3 + 0));
+            Y += Me * __uint_as_float(ldw(L, tb, cie + i * 3 + 1));
+            Z += Me * __uint_as_float(ldw(L, tb, cie + i * 3 + 2));
+        }
+        const int mx = N * 3;
+        for (int c = 0; c < 3; ++c) {
+            const float v = X * __uint_as_float(ldw(L, tb, mx + c)) + Y * __uint_as_float(ldw(L, tb, mx + 3 + c))
+                          + Z * __uint_as_float(ldw(L, tb, mx + 6 + c));
+            rgb[c] = v < 0.0f ? 0.0f : v;
+        }
+    }
+    for (int c = 0; c < 3; ++c) stval(L, r, c, rgb[c]);
+}
+
 // ---- noise ---------------------------------------------------------------------
 // gabor / pgabor: a = r, S, T, kind word, anisotropic, direction,
 // bandwidth; b (the carrier op that follows) = impulses, do_filter,
@@ -1738,6 +1785,7 @@ __device__ __forceinline__ void run_tile(const RunCtx& R, Lane& L, int64_t npoin
                 case OP_AREA:
                 case OP_FILTERWIDTH: OSLG_TIER_CASE(4, h_deriv_misc(L, code, a)) break;
                 case OP_LUMINANCE: OSLG_TIER_CASE(4, h_luminance(L, a)) break;
+                case OP_BLACKBODY: OSLG_TIER_CASE(4, h_blackbody(L, a)) break;
                 case OP_NOISE: OSLG_TIER_CASE(1, h_noise(L, a)) break;
                 case OP_GABOR: {
                     if constexpr ((TIER & 1) != 0) {

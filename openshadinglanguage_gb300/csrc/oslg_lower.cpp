@@ -81,6 +81,93 @@ uint32_t string_hash(const std::string& s) {
     return h;
 }
 
+// CIE 1931 2-degree colour matching functions (x-bar, y-bar, z-bar) at 5 nm
+// from 380 to 780 nm, four decimals: the published CIE data the reference's
+// blackbody integrates against (src/liboslexec/opcolor_impl.h:55-93).
+const float kCIE[81][3] = {
+    { 0.0014f, 0.0000f, 0.0065f },  // 380 nm
+    { 0.0022f, 0.0001f, 0.0105f },  // 385 nm
+    { 0.0042f, 0.0001f, 0.0201f },  // 390 nm
+    { 0.0076f, 0.0002f, 0.0362f },  // 395 nm
+    { 0.0143f, 0.0004f, 0.0679f },  // 400 nm
+    { 0.0232f, 0.0006f, 0.1102f },  // 405 nm
+    { 0.0435f, 0.0012f, 0.2074f },  // 410 nm
+    { 0.0776f, 0.0022f, 0.3713f },  // 415 nm
+    { 0.1344f, 0.0040f, 0.6456f },  // 420 nm
+    { 0.2148f, 0.0073f, 1.0391f },  // 425 nm
+    { 0.2839f, 0.0116f, 1.3856f },  // 430 nm
+    { 0.3285f, 0.0168f, 1.6230f },  // 435 nm
+    { 0.3483f, 0.0230f, 1.7471f },  // 440 nm
+    { 0.3481f, 0.0298f, 1.7826f },  // 445 nm
+    { 0.3362f, 0.0380f, 1.7721f },  // 450 nm
+    { 0.3187f, 0.0480f, 1.7441f },  // 455 nm
+    { 0.2908f, 0.0600f, 1.6692f },  // 460 nm
+    { 0.2511f, 0.0739f, 1.5281f },  // 465 nm
+    { 0.1954f, 0.0910f, 1.2876f },  // 470 nm
+    { 0.1421f, 0.1126f, 1.0419f },  // 475 nm
+    { 0.0956f, 0.1390f, 0.8130f },  // 480 nm
+    { 0.0580f, 0.1693f, 0.6162f },  // 485 nm
+    { 0.0320f, 0.2080f, 0.4652f },  // 490 nm
+    { 0.0147f, 0.2586f, 0.3533f },  // 495 nm
+    { 0.0049f, 0.3230f, 0.2720f },  // 500 nm
+    { 0.0024f, 0.4073f, 0.2123f },  // 505 nm
+    { 0.0093f, 0.5030f, 0.1582f },  // 510 nm
+    { 0.0291f, 0.6082f, 0.1117f },  // 515 nm
+    { 0.0633f, 0.7100f, 0.0782f },  // 520 nm
+    { 0.1096f, 0.7932f, 0.0573f },  // 525 nm
+    { 0.1655f, 0.8620f, 0.0422f },  // 530 nm
+    { 0.2257f, 0.9149f, 0.0298f },  // 535 nm
+    { 0.2904f, 0.9540f, 0.0203f },  // 540 nm
+    { 0.3597f, 0.9803f, 0.0134f },  // 545 nm
+    { 0.4334f, 0.9950f, 0.0087f },  // 550 nm
+    { 0.5121f, 1.0000f, 0.0057f },  // 555 nm
+    { 0.5945f, 0.9950f, 0.0039f },  // 560 nm
+    { 0.6784f, 0.9786f, 0.0027f },  // 565 nm
+    { 0.7621f, 0.9520f, 0.0021f },  // 570 nm
+    { 0.8425f, 0.9154f, 0.0018f },  // 575 nm
+    { 0.9163f, 0.8700f, 0.0017f },  // 580 nm
+    { 0.9786f, 0.8163f, 0.0014f },  // 585 nm
+    { 1.0263f, 0.7570f, 0.0011f },  // 590 nm
+    { 1.0567f, 0.6949f, 0.0010f },  // 595 nm
+    { 1.0622f, 0.6310f, 0.0008f },  // 600 nm
+    { 1.0456f, 0.5668f, 0.0006f },  // 605 nm
+    { 1.0026f, 0.5030f, 0.0003f },  // 610 nm
+    { 0.9384f, 0.4412f, 0.0002f },  // 615 nm
+    { 0.8544f, 0.3810f, 0.0002f },  // 620 nm
+    { 0.7514f, 0.3210f, 0.0001f },  // 625 nm
+    { 0.6424f, 0.2650f, 0.0000f },  // 630 nm
+    { 0.5419f, 0.2170f, 0.0000f },  // 635 nm
+    { 0.4479f, 0.1750f, 0.0000f },  // 640 nm
+    { 0.3608f, 0.1382f, 0.0000f },  // 645 nm
+    { 0.2835f, 0.1070f, 0.0000f },  // 650 nm
+    { 0.2187f, 0.0816f, 0.0000f },  // 655 nm
+    { 0.1649f, 0.0610f, 0.0000f },  // 660 nm
+    { 0.1212f, 0.0446f, 0.0000f },  // 665 nm
+    { 0.0874f, 0.0320f, 0.0000f },  // 670 nm
+    { 0.0636f, 0.0232f, 0.0000f },  // 675 nm
+    { 0.0468f, 0.0170f, 0.0000f },  // 680 nm
+    { 0.0329f, 0.0119f, 0.0000f },  // 685 nm
+    { 0.0227f, 0.0082f, 0.0000f },  // 690 nm
+    { 0.0158f, 0.0057f, 0.0000f },  // 695 nm
+    { 0.0114f, 0.0041f, 0.0000f },  // 700 nm
+    { 0.0081f, 0.0029f, 0.0000f },  // 705 nm
+    { 0.0058f, 0.0021f, 0.0000f },  // 710 nm
+    { 0.0041f, 0.0015f, 0.0000f },  // 715 nm
+    { 0.0029f, 0.0010f, 0.0000f },  // 720 nm
+    { 0.0020f, 0.0007f, 0.0000f },  // 725 nm
+    { 0.0014f, 0.0005f, 0.0000f },  // 730 nm
+    { 0.0010f, 0.0004f, 0.0000f },  // 735 nm
+    { 0.0007f, 0.0002f, 0.0000f },  // 740 nm
+    { 0.0005f, 0.0002f, 0.0000f },  // 745 nm
+    { 0.0003f, 0.0001f, 0.0000f },  // 750 nm
+    { 0.0002f, 0.0001f, 0.0000f },  // 755 nm
+    { 0.0002f, 0.0001f, 0.0000f },  // 760 nm
+    { 0.0001f, 0.0000f, 0.0000f },  // 765 nm
+    { 0.0001f, 0.0000f, 0.0000f },  // 770 nm
+    { 0.0001f, 0.0000f, 0.0000f },  // 775 nm
+    { 0.0000f, 0.0000f, 0.0000f },  // 780 nm
+};
+
 // Ops whose result derivatives are a function of their inputs' derivatives.
 const std::set<std::string>& deriv_propagating_ops() {
     static const std::set<std::string> s = {
@@ -605,39 +692,110 @@ struct Lowerer {
         return std::string();
     }
 
-    // Rec709 luminance weights as ColorSystem::set_colorspace derives them
+    // Rec709 colour system as ColorSystem::set_colorspace derives it
     // (src/liboslexec/opcolor.cpp:140-190): XYZ->RGB from the primaries and
-    // the D65 white point, inverted (cofactors over the determinant), and
-    // the middle column of RGB->XYZ.
-    static std::array<float, 3> luminance_scale() {
-        const float xr = 0.64f, yr = 0.33f, xg = 0.30f, yg = 0.60f, xb = 0.15f, yb = 0.06f, xw = 0.3127f,
-                    yw = 0.3291f;
-        const float R[3] = { xr, yr, 1.0f - (xr + yr) }, G[3] = { xg, yg, 1.0f - (xg + yg) },
-                    B[3] = { xb, yb, 1.0f - (xb + yb) }, W[3] = { xw, yw, 1.0f - (xw + yw) };
-        float r[3] = { G[1] * B[2] - B[1] * G[2], B[0] * G[2] - G[0] * B[2], G[0] * B[1] - B[0] * G[1] };
-        float g[3] = { B[1] * R[2] - R[1] * B[2], R[0] * B[2] - B[0] * R[2], B[0] * R[1] - R[0] * B[1] };
-        float b[3] = { R[1] * G[2] - G[1] * R[2], G[0] * R[2] - R[0] * G[2], R[0] * G[1] - G[0] * R[1] };
-        float w[3] = { r[0] * W[0] + r[1] * W[1] + r[2] * W[2], g[0] * W[0] + g[1] * W[1] + g[2] * W[2],
-                       b[0] * W[0] + b[1] * W[1] + b[2] * W[2] };
-        const float ws = 1.0f / W[1];
-        for (float& x : w) x *= ws;
-        for (int i = 0; i < 3; ++i) { r[i] /= w[0]; g[i] /= w[1]; b[i] /= w[2]; }
-        const float M[3][3] = { { r[0], g[0], b[0] }, { r[1], g[1], b[1] }, { r[2], g[2], b[2] } };
-        float C[3][3];  // cofactor matrix transposed (adjugate)
-        C[0][0] = M[1][1] * M[2][2] - M[2][1] * M[1][2];
-        C[0][1] = M[2][1] * M[0][2] - M[0][1] * M[2][2];
-        C[0][2] = M[0][1] * M[1][2] - M[1][1] * M[0][2];
-        C[1][0] = M[2][0] * M[1][2] - M[1][0] * M[2][2];
-        C[1][1] = M[0][0] * M[2][2] - M[2][0] * M[0][2];
-        C[1][2] = M[1][0] * M[0][2] - M[0][0] * M[1][2];
-        C[2][0] = M[1][0] * M[2][1] - M[2][0] * M[1][1];
-        C[2][1] = M[2][0] * M[0][1] - M[0][0] * M[2][1];
-        C[2][2] = M[0][0] * M[1][1] - M[1][0] * M[0][1];
-        const float det = M[0][0] * C[0][0] + M[0][1] * C[1][0] + M[0][2] * C[2][0];
-        std::array<float, 3> l = { C[0][1] / det, C[1][1] / det, C[2][1] / det };
-        const float lum2 = 1.0f - l[0] - l[1];
-        if (std::fabs(lum2 - l[2]) < 0.001f) l[2] = lum2;
-        return l;
+    // the D65 white point, and the luminance weights = the middle column of
+    // its inverse (cofactors over the determinant).
+    struct ColorSys {
+        float xyz2rgb[3][3];  // row-vector convention: rgb = XYZ * M
+        std::array<float, 3> lum;
+    };
+    static const ColorSys& rec709() {
+        static const ColorSys cs = []() {
+            ColorSys c;
+            const float xr = 0.64f, yr = 0.33f, xg = 0.30f, yg = 0.60f, xb = 0.15f, yb = 0.06f, xw = 0.3127f,
+                        yw = 0.3291f;
+            const float R[3] = { xr, yr, 1.0f - (xr + yr) }, G[3] = { xg, yg, 1.0f - (xg + yg) },
+                        B[3] = { xb, yb, 1.0f - (xb + yb) }, W[3] = { xw, yw, 1.0f - (xw + yw) };
+            float r[3] = { G[1] * B[2] - B[1] * G[2], B[0] * G[2] - G[0] * B[2], G[0] * B[1] - B[0] * G[1] };
+            float g[3] = { B[1] * R[2] - R[1] * B[2], R[0] * B[2] - B[0] * R[2], B[0] * R[1] - R[0] * B[1] };
+            float b[3] = { R[1] * G[2] - G[1] * R[2], G[0] * R[2] - R[0] * G[2], R[0] * G[1] - G[0] * R[1] };
+            float w[3] = { r[0] * W[0] + r[1] * W[1] + r[2] * W[2], g[0] * W[0] + g[1] * W[1] + g[2] * W[2],
+                           b[0] * W[0] + b[1] * W[1] + b[2] * W[2] };
+            const float ws = 1.0f / W[1];
+            for (float& x : w) x *= ws;
+            for (int i = 0; i < 3; ++i) { r[i] /= w[0]; g[i] /= w[1]; b[i] /= w[2]; }
+            const float M[3][3] = { { r[0], g[0], b[0] }, { r[1], g[1], b[1] }, { r[2], g[2], b[2] } };
+            std::memcpy(c.xyz2rgb, M, sizeof(M));
+            float C[3][3];  // adjugate
+            C[0][0] = M[1][1] * M[2][2] - M[2][1] * M[1][2];
+            C[0][1] = M[2][1] * M[0][2] - M[0][1] * M[2][2];
+            C[0][2] = M[0][1] * M[1][2] - M[1][1] * M[0][2];
+            C[1][0] = M[2][0] * M[1][2] - M[1][0] * M[2][2];
+            C[1][1] = M[0][0] * M[2][2] - M[2][0] * M[0][2];
+            C[1][2] = M[1][0] * M[0][2] - M[0][0] * M[1][2];
+            C[2][0] = M[1][0] * M[2][1] - M[2][0] * M[1][1];
+            C[2][1] = M[2][0] * M[0][1] - M[0][0] * M[2][1];
+            C[2][2] = M[0][0] * M[1][1] - M[1][0] * M[0][1];
+            const float det = M[0][0] * C[0][0] + M[0][1] * C[1][0] + M[0][2] * C[2][0];
+            c.lum = { C[0][1] / det, C[1][1] / det, C[2][1] / det };
+            const float lum2 = 1.0f - c.lum[0] - c.lum[1];
+            if (std::fabs(lum2 - c.lum[2]) < 0.001f) c.lum[2] = lum2;
+            return c;
+        }();
+        return cs;
+    }
+    static std::array<float, 3> luminance_scale() { return rec709().lum; }
+
+    // Blackbody table (src/liboslexec/opcolor.cpp:191-205,
+    // opcolor_impl.h:131-260): Planck spectra at temperatures
+    // T_i = 2 i^1.5 + 800 up to 12000 K, integrated against the CIE 1931
+    // matching functions, converted to RGB, clamped at zero and stored to
+    // the power 1/5. Followed by the XYZ->RGB matrix and the CIE table for
+    // temperatures past the table. expm1, cbrt and pow are evaluated in double precision
+    // (the reference uses OIIO's fast approximations).
+    static const std::vector<float>& blackbody_pool() {
+        static const std::vector<float> pool = []() {
+            std::vector<float> t;
+            const ColorSys& cs = rec709();
+            float lastT = 0.0f;
+            for (int i = 0; lastT <= 12000.0f; ++i) {
+                const float is = std::sqrt((float)i);
+                const float T = is * is * is * 2.0f + 800.0f;
+                lastT = T;
+                float rgb[3];
+                blackbody_spectral_rgb(T, cs, rgb);
+                for (int c = 0; c < 3; ++c) t.push_back((float)std::pow((double)rgb[c], (double)(1.0f / 5.0f)));
+            }
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) t.push_back(cs.xyz2rgb[i][j]);
+            for (int i = 0; i < 81; ++i)
+                for (int j = 0; j < 3; ++j) t.push_back(kCIE[i][j]);
+            return t;
+        }();
+        return pool;
+    }
+    // compute_blackbody_rgb (opcolor_impl.h:557-566)
+    static void blackbody_spectral_rgb(float T, const ColorSys& cs, float* rgb) {
+        float X = 0.0f, Y = 0.0f, Z = 0.0f;
+        const float dlambda = (float)(5.0f * 1e-9);
+        for (int i = 0; i < 81; ++i) {
+            const float lambda = 380.0f + 5.0f * (float)i;
+            const float wlm = lambda * 1e-9f;
+            const float wlm2 = wlm * wlm, wlm4 = wlm2 * wlm2, wlm5 = wlm4 * wlm;
+            const float inv5 = 1.0f / wlm5;
+            const float e = (float)std::expm1((double)(1.4388e-2f / (wlm * T)));
+            const float Me = ((3.74183e-16f * inv5) / e) * dlambda;
+            X += Me * kCIE[i][0];
+            Y += Me * kCIE[i][1];
+            Z += Me * kCIE[i][2];
+        }
+        for (int c = 0; c < 3; ++c) {
+            float v = X * cs.xyz2rgb[0][c] + Y * cs.xyz2rgb[1][c] + Z * cs.xyz2rgb[2][c];
+            rgb[c] = v < 0.0f ? 0.0f : v;
+        }
+    }
+    int const_floats(const std::vector<float>& v) {
+        GSym d;
+        d.name = "$table";
+        d.type.base = BT_FLOAT;
+        d.type.arraylen = (int)v.size();
+        d.kind = SK_CONST;
+        d.is_const = true;
+        d.cval = v;
+        int k = add_sym(d);
+        syms[k].slot = (int)pool_add(syms[k]);
+        return k;
     }
     int const_triple(const std::array<float, 3>& v) {
         GSym d;
@@ -950,7 +1108,12 @@ struct Lowerer {
                  n);
             return true;
         }
-        if (n == "blackbody") { emit(OP_BLACKBODY, { a(0), a(1) }, n); return true; }
+        if (n == "blackbody") {
+            const std::vector<float>& t = blackbody_pool();
+            int tb = const_floats(t);
+            emit(OP_BLACKBODY, { a(0), a(1), A(tb), (uint32_t)((t.size() - 9 - 243) / 3) }, n);
+            return true;
+        }
         if (n == "luminance") {
             int sc = const_triple(luminance_scale());
             emit(OP_LUMINANCE, { a(0), a(1), A(sc) }, n);
@@ -995,6 +1158,8 @@ struct Lowerer {
             case OP_LOG2: case OP_LOG10: case OP_POW: case OP_ATAN2: case OP_FMOD: case OP_CLAMP: case OP_MIX:
             case OP_SMOOTHSTEP: case OP_SELECT: case OP_DOT: case OP_CROSS: case OP_LENGTH: case OP_DISTANCE:
             case OP_NORMALIZE: case OP_TRANSFORM: case OP_MMUL: case OP_AREF: case OP_AASSIGN:
+            case OP_MDIV: case OP_TRANSPOSE: case OP_DETERMINANT: case OP_AREA: case OP_FILTERWIDTH:
+            case OP_LUMINANCE: case OP_BLACKBODY:
                 t |= 4u;
                 break;
             default: break;

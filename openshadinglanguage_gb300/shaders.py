@@ -351,6 +351,26 @@ def matrix_ops(M, M2):
     return b.text()
 
 
+def blackbody_test(temp_scale=10000.0):
+    """testsuite/blackbody/test.osl: T = 10000*u; Cout = blackbody(T)/10000;
+    for v > 0.5, Cout *= 0.7/luminance(Cout). temp_scale replaces the
+    10000 K of T (past 12000 K the spectral path runs)."""
+    b = OsoBuilder("test")
+    Cout = b.param("color", "Cout", [0, 0, 0], output=True)
+    u, v = b.glob("float", "u"), b.glob("float", "v")
+    c = lambda x: b.const("float", x)
+    T, bb, lum, sc, cond = b.tmp("float"), b.tmp("color"), b.tmp("float"), b.tmp("float"), b.tmp("int")
+    b.op("mul", T, c(temp_scale), u)
+    b.op("blackbody", bb, T)
+    b.op("div", Cout, bb, c(10000.0))
+    b.op("gt", cond, v, c(0.5))
+    with b.if_(cond):
+        b.op("luminance", lum, Cout)
+        b.op("div", sc, c(0.7), lum)
+        b.op("mul", Cout, Cout, sc)
+    return b.text()
+
+
 def getP():
     """testsuite/example-batched-deformer/getP.osl: output point out = P"""
     b = OsoBuilder("getP")

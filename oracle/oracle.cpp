@@ -562,6 +562,51 @@ void op_luminance(Point& P, const uint32_t* a) {
     for (int d = 0; d < nd; ++d) setf(P, a[0], d, getf(P, a[1], 0, d) * sx + getf(P, a[1], 1, d) * sy + getf(P, a[1], 2, d) * sz);
 }
 
+// blackbody (src/liboslexec/opcolor_impl.h:510-575, opcolor.cpp:438-442):
+// a2 = constant table (N entries of RGB^(1/5), XYZ->RGB matrix, CIE table)
+void op_blackbody(Point& P, const uint32_t* a) {
+    float T = getf(P, a[1], 0, 0);
+    uint32_t tb = a[2];
+    int N = (int)a[3];
+    auto tab = [&](int i) { return bitsf(word(P, tb, i)); };
+    float rgb[3];
+    if (T < 800.0f) {
+        rgb[0] = 1.0e-6f; rgb[1] = 0.0f; rgb[2] = 0.0f;
+    } else if (T < 12000.0f) {
+        float ic = (float)std::cbrt((double)((T - 800.0f) / 2.0f));
+        float t = ic * ic;
+        int ti = (int)t;
+        if (ti > N - 2) ti = N - 2;
+        float rem = t - (float)ti;
+        for (int c = 0; c < 3; ++c) {
+            float v = tab(ti * 3 + c) * (1.0f - rem) + tab(ti * 3 + 3 + c) * rem;
+            float v2 = v * v, v4 = v2 * v2;
+            rgb[c] = v4 * v;
+        }
+    } else {
+        float X = 0.0f, Y = 0.0f, Z = 0.0f;
+        const float dlambda = (float)(5.0f * 1e-9);
+        int cie = N * 3 + 9;
+        for (int i = 0; i < 81; ++i) {
+            float lambda = 380.0f + 5.0f * (float)i;
+            float wlm = lambda * 1e-9f;
+            float wlm2 = wlm * wlm, wlm4 = wlm2 * wlm2, wlm5 = wlm4 * wlm;
+            float inv5 = 1.0f / wlm5;
+            float e = (float)std::expm1((double)(1.4388e-2f / (wlm * T)));
+            float Me = ((3.74183e-16f * inv5) / e) * dlambda;
+            X += Me * tab(cie + i * 3 + 0);
+            Y += Me * tab(cie + i * 3 + 1);
+            Z += Me * tab(cie + i * 3 + 2);
+        }
+        int mx = N * 3;
+        for (int c = 0; c < 3; ++c) {
+            float v = X * tab(mx + c) + Y * tab(mx + 3 + c) + Z * tab(mx + 6 + c);
+            rgb[c] = v < 0.0f ? 0.0f : v;
+        }
+    }
+    for (int c = 0; c < 3; ++c) putv(P, a[0], c, rgb[c]);
+}
+
 // noise (batched_llvm_gen.cpp:6032-6190 kinds; oslnoise.h wrappers)
 void op_noise(Point& P, const uint32_t* a) {
     uint32_t r = a[0], S = a[1], T = a[2], kw = a[3];
@@ -1050,6 +1095,7 @@ struct Runner {
             case oslg::OP_AREA: op_area(P, a); break;
             case oslg::OP_FILTERWIDTH: op_filterwidth(P, a); break;
             case oslg::OP_LUMINANCE: op_luminance(P, a); break;
+            case oslg::OP_BLACKBODY: op_blackbody(P, a); break;
             case oslg::OP_NOISE: op_noise(P, a); break;
             case oslg::OP_GABOR: op_gabor(P, a, prog.ops[pc + 1].a); break;
             case oslg::OP_HASH: op_hash(P, a); break;

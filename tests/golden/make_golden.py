@@ -64,6 +64,61 @@ def read_tiff(path):
     return img
 
 
+def read_exr(path):
+    """Scanline OpenEXR with ZIP compression (16 lines per block) and HALF
+    channels, as written by the reference's testshade -od half: zlib, then
+    undo the byte predictor and the even/odd byte split of the format."""
+    d = open(path, "rb").read()
+    assert d[:4] == b"\x76\x2f\x31\x01", "not an OpenEXR file"
+    i, attrs = 8, {}
+    while d[i] != 0:
+        n = d.index(b"\0", i)
+        name = d[i:n].decode()
+        i = n + 1
+        n = d.index(b"\0", i)
+        i = n + 1
+        (sz,) = struct.unpack("<i", d[i:i + 4])
+        i += 4
+        attrs[name] = d[i:i + sz]
+        i += sz
+    i += 1
+    assert attrs["compression"][0] == 3, "only ZIP compression is read here"
+    x0, y0, x1, y1 = struct.unpack("<4i", attrs["dataWindow"])
+    W, H = x1 - x0 + 1, y1 - y0 + 1
+    chans, c = [], attrs["channels"]
+    j = 0
+    while c[j] != 0:
+        n = c.index(b"\0", j)
+        nm = c[j:n].decode()
+        (ptype,) = struct.unpack("<i", c[n + 1:n + 5])
+        assert ptype == 1, "only HALF channels are read here"
+        chans.append(nm)
+        j = n + 17
+    nblocks = (H + 15) // 16
+    offsets = struct.unpack("<%dQ" % nblocks, d[i:i + 8 * nblocks])
+    img = np.zeros((H, W, len(chans)), np.float32)
+    for off in offsets:
+        y, size = struct.unpack("<ii", d[off:off + 8])
+        raw = np.frombuffer(zlib.decompress(d[off + 8:off + 8 + size]), np.uint8).astype(np.int32)
+        t = np.cumsum(np.concatenate([raw[:1], raw[1:] - 128])) & 0xFF
+        t = t.astype(np.uint8)
+        half = (len(t) + 1) // 2
+        inter = np.empty(len(t), np.uint8)
+        inter[0::2] = t[:half]
+        inter[1::2] = t[half:]
+        lines = min(16, H - (y - y0))
+        vals = np.frombuffer(inter.tobytes(), np.float16).reshape(lines, len(chans), W)
+        img[y - y0:y - y0 + lines] = vals.transpose(0, 2, 1).astype(np.float32)
+    return img, chans
+
+
+EXR_IMAGES = {
+    # every reference image of the test: runtest accepts a match with any
+    "blackbody": ["testsuite/blackbody/ref/out.exr", "testsuite/blackbody/ref/out.alt.exr",
+                  "testsuite/blackbody/ref/out2.exr", "testsuite/blackbody/ref/out3.exr",
+                  "testsuite/blackbody/ref/out4.exr", "testsuite/blackbody/ref/out5.exr"],
+}
+
 IMAGES = {
     # fixture name: (reference path, note)
     "noise": "testsuite/noise/ref/out.tif",
@@ -111,6 +166,16 @@ def main():
         np.savez_compressed(os.path.join(HERE, name + ".npz"), img=img[::STEP, ::STEP], full_w=W, full_h=H,
                             step=STEP)
         print(name, img.shape)
+    for name, rels in EXR_IMAGES.items():
+        imgs = []
+        for rel in rels:
+            img, chans = read_exr(os.path.join(REF, rel))
+            order = [chans.index(c) for c in ("R", "G", "B")]
+            imgs.append(img[:, :, order])
+        stack = np.stack(imgs)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), imgs=stack, full_w=stack.shape[2],
+                            full_h=stack.shape[1])
+        print(name, stack.shape)
     ref_txt = open(os.path.join(REF, "testsuite/example-batched-deformer/ref/out.txt")).read()
     open(os.path.join(HERE, "deformer_out.txt"), "w").write(ref_txt)
     ka = known_answers()

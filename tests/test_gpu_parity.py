@@ -187,3 +187,35 @@ def test_matrix_ops_match_oracle():
     ref = np.zeros((W * H, REC), np.float32)
     assert oracle_run(g.program_bytes(), W * H, grid_globals(u, v, W, H, P=P, centers=True), ref) == 0
     assert_same(got, ref)
+
+
+@pytest.mark.parametrize("scale", [10000.0, 30000.0])
+def test_blackbody_matches_oracle(scale):
+    from test_oracle_golden import blackbody_program
+    ss = og.ShadingSystem()
+    g = blackbody_program(ss, scale)
+    W, H = 1000, 64
+    u, v = pixel_grid(W, H)
+    got = gpu_run(ss, g, W * H, device_grid_globals(u, v, W, H), 3)
+    ref = np.zeros((W * H, 3), np.float32)
+    assert oracle_run(g.program_bytes(), W * H, grid_globals(u, v, W, H), ref) == 0
+    assert_same(got, ref)
+
+
+def test_single_op_programs_pick_the_right_tier():
+    """A program whose only non-trivial op is one math-tier op runs (the
+    tier chosen at lowering carries the op's handler)."""
+    ss = og.ShadingSystem()
+    b = og.OsoBuilder("tdet")
+    M = b.param("matrix", "M", [float(i % 5 == 0) * 2.0 + 0.25 * (i % 3) for i in range(16)])
+    out = b.param("float", "d", 0.0, output=True)
+    b.op("determinant", out, M)
+    g = single_layer_group(ss, "tdet", b.text(), outputs=[
+        og.SymLocationDesc("d", og.TypeFloat, False, og.SymArenaOutputs, 0, 4)])
+    W, H = 64, 4
+    u_, v_ = pixel_grid(W, H)
+    got = gpu_run(ss, g, W * H, device_grid_globals(u_, v_, W, H), 1)
+    ref = np.zeros((W * H, 1), np.float32)
+    assert oracle_run(g.program_bytes(), W * H, grid_globals(u_, v_, W, H), ref) == 0
+    assert_same(got, ref)
+    assert ss.device_status() == 0

@@ -249,3 +249,23 @@ def test_oracle_matches_batched_deformer_output():
     exp = deformer_expected()
     got = [" ".join(fmt_g3(c) for c in row) for row in out]
     assert got == exp
+
+
+def blackbody_program(ss, scale=10000.0):
+    return single_layer_group(ss, "test", shaders.blackbody_test(scale),
+                              outputs=[og.SymLocationDesc("Cout", og.TypeColor, False, og.SymArenaOutputs, 0, 12)])
+
+
+def test_oracle_blackbody_matches_reference_image():
+    """testsuite/blackbody: 1000x64 half-float image, runtest thresholds
+    (failthresh 0.004, failpercent 0.05) against any of its reference images."""
+    ss = og.ShadingSystem()
+    g = blackbody_program(ss)
+    refs = np.load(os.path.join(GOLDEN, "blackbody.npz"))["imgs"]
+    W, H = 1000, 64
+    u, v = pixel_grid(W, H)
+    out = np.zeros((W * H, 3), np.float32)
+    assert oracle_run(g.program_bytes(), W * H, grid_globals(u, v, W, H), out) == 0
+    img = out.reshape(H, W, 3).astype(np.float16).astype(np.float32)
+    fracs = [100.0 * np.mean(np.abs(img - r) > 0.004 + 1e-9) for r in refs]
+    assert min(fracs) <= 0.05, fracs
