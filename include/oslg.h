@@ -144,10 +144,22 @@ int oslg_add_symlocs(oslg_system* sys, oslg_group* group, const oslg_symloc* loc
  * as testrender's CompositeBSDF at wo = -I and the light direction wi
  * (src/testrender/shading.cpp:1450-1500 walk, shading.h:322-374 prepare and
  * eval). Writes {weight.r, weight.g, weight.b, pdf} (4 floats) at
- * output_base + offset + i*stride. Lobes: diffuse, microfacet "ggx"
- * reflection; other closure ids contribute nothing. */
+ * output_base + offset + i*stride. Lobes: diffuse, oren_nayar, microfacet
+ * "ggx" (refract 0/1/2); other closure ids contribute nothing. */
 int oslg_group_bsdf_eval(oslg_system* sys, oslg_group* group, const char* closure,
                          const float wi[3], int64_t offset, int64_t stride);
+/* Renderer-side sampling of a closure output, the per-hit step of
+ * testrender's path loop (src/testrender/simpleraytracer.cpp:1038-1079):
+ * the closure tree is walked (emission adds to Le; diffuse, oren_nayar and
+ * microfacet "ggx" with refract 0/1/2 become lobes), prepared with the
+ * path weight and sampled (src/testrender/shading.h:322-398). Reads
+ * {rx, ry, rz, path_weight.rgb, absorb} (7 floats) per point at
+ * userdata_base + in_offset + i*in_stride; writes {wi.xyz, weight.rgb,
+ * pdf, Le.rgb, roughness} (11 floats) at output_base + offset + i*stride.
+ * No counterpart as one call in the reference, which does these steps in
+ * the renderer. */
+int oslg_group_bsdf_sample(oslg_system* sys, oslg_group* group, const char* closure, int64_t offset,
+                           int64_t stride, int64_t in_offset, int64_t in_stride);
 /* ShadingSystem::optimize_group (oslexec.h:1093) + BatchedExecutor::jit_group
  * (oslexec.h:993): lowers the group to a device op program and uploads it. */
 int oslg_optimize_group(oslg_system* sys, oslg_group* group);

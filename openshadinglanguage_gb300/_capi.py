@@ -93,6 +93,8 @@ _EXPORTS = {
     "oslg_add_symlocs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(SymLocC), ctypes.c_int]),
     "oslg_group_bsdf_eval": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p,
                                             ctypes.POINTER(ctypes.c_float), ctypes.c_int64, ctypes.c_int64]),
+    "oslg_group_bsdf_sample": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int64,
+                                              ctypes.c_int64, ctypes.c_int64, ctypes.c_int64]),
     "oslg_optimize_group": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "oslg_release_group": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "oslg_group_program": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,

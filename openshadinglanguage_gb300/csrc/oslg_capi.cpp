@@ -318,6 +318,25 @@ int oslg_group_bsdf_eval(oslg_system* sys, oslg_group* group, const char* closur
     });
 }
 
+int oslg_group_bsdf_sample(oslg_system* sys, oslg_group* group, const char* closure, int64_t offset, int64_t stride,
+                           int64_t in_offset, int64_t in_stride) {
+    if (!sys || !group || !closure) return OSLG_ERR_ARG;
+    return guarded(sys, [&]() {
+        if (offset < 0 || in_offset < 0 || ((offset | stride | in_offset | in_stride) & 3))
+            return fail(sys, OSLG_ERR_ARG, "bsdf sample offsets and strides must be non-negative multiples of 4 bytes");
+        BsdfSampleRequest r;
+        r.closure = closure;
+        r.offset = offset;
+        r.stride = stride;
+        r.in_offset = in_offset;
+        r.in_stride = in_stride;
+        std::lock_guard<std::mutex> lock(group->g.mutex);
+        group->g.bsdf_samples.push_back(r);
+        group->g.compiled.reset();
+        return OSLG_OK;
+    });
+}
+
 static int ensure_compiled(oslg_system* sys, oslg_group* group, bool upload) {
     ShaderGroup& g = group->g;
     if (!g.ended) return fail(sys, OSLG_ERR_STATE, "group used before ShaderGroupEnd");

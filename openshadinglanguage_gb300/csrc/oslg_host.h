@@ -129,6 +129,16 @@ struct BsdfEvalRequest {
     int64_t stride = 16;
 };
 
+// Renderer-side sampling of a closure output (testrender's
+// CompositeBSDF::prepare + sample): random numbers, path weight and the
+// absorb flag per point from the userdata arena; direction, weight, pdf,
+// emission and roughness per point into the output arena.
+struct BsdfSampleRequest {
+    std::string closure;
+    int64_t offset = 0, stride = 44;        // outputs
+    int64_t in_offset = 0, in_stride = 28;  // userdata
+};
+
 // A lowered group ready to run: the op program plus a serialized blob the
 // device (or a checker) consumes.
 struct CompiledGroup {
@@ -146,6 +156,7 @@ struct ShaderGroup {
     std::vector<std::string> renderer_outputs;
     std::vector<SymLoc> symlocs;
     std::vector<BsdfEvalRequest> bsdf_evals;
+    std::vector<BsdfSampleRequest> bsdf_samples;
     bool ended = false;
     std::mutex mutex;  // lowering happens once, under this lock
     std::unique_ptr<CompiledGroup> compiled;

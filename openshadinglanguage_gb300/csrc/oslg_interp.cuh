@@ -1358,56 +1358,167 @@ static __device__ void h_store_closure(const Lane& L, const uint32_t* a, char* b
 
 // CompositeBSDF::prepare + eval (shading.h:322-374) over the lobes the walk
 // finds: diffuse, and microfacet "ggx" reflection; other ids add nothing.
-static __device__ void h_bsdf_eval(const Lane& L, const uint32_t* a, char* base, const ClosurePools& P, uint32_t* st) {
-    uint32_t root = ldw(L, a[0], 0);
-    const V3 wi = v3(ldf(L, a[3], 0, 0), ldf(L, a[3], 1, 0), ldf(L, a[3], 2, 0));
-    const V3 wo = v3(-ldf(L, a[4], 0, 0), -ldf(L, a[4], 1, 0), -ldf(L, a[4], 2, 0));
-    const uint32_t ggx = a[5];
-    int nl = 0;
-    int kind[kBsdfMaxLobes];
-    float lw[kBsdfMaxLobes][3];
-    uint32_t lp[kBsdfMaxLobes];
+// The lobes testrender's process_closure builds from a closure tree
+// (shading.cpp:1481-1530): emission accumulates Le; diffuse, oren_nayar and
+// GGX microfacet (refract 0/1/2) become lobes in walk order. Lobe
+// parameters stay in the heap (node params) and are read when used.
+struct Lobes {
+    int n;
+    int kind[kBsdfMaxLobes];  // 0 diffuse, 1 ggx, 2 oren-nayar
+    float w[kBsdfMaxLobes][3];
+    float pdf[kBsdfMaxLobes];
+    uint32_t p[kBsdfMaxLobes];
+    float Le[3];
+};
+__device__ __forceinline__ void lobes_build(const Lane& L, const ClosurePools& P, uint32_t root, uint32_t ggx,
+                                            uint32_t* st, Lobes& B) {
+    B.n = 0;
+    B.Le[0] = B.Le[1] = B.Le[2] = 0.0f;
     closure_walk(L, P, root, st, [&](int id, const float* cw, uint32_t params) {
         int k = -1;
+        if (id == 1) {  // EMISSION_ID
+            for (int c = 0; c < 3; ++c) B.Le[c] = B.Le[c] + cw[c];
+            return;
+        }
         if (id == 3) k = 0;  // DIFFUSE_ID
-        else if (id == 8 && hgetu(L, params + 0) == ggx && (int)hgetu(L, params + 10) == 0) k = 1;  // MICROFACET_ID
-        if (k < 0 || nl >= kBsdfMaxLobes) return;
-        kind[nl] = k;
-        for (int c = 0; c < 3; ++c) lw[nl][c] = cw[c];
-        lp[nl] = params;
-        ++nl;
+        else if (id == 4) k = 2;  // OREN_NAYAR_ID
+        else if (id == 8 && hgetu(L, params + 0) == ggx) {  // MICROFACET_ID "ggx"
+            const int r = (int)hgetu(L, params + 10);
+            if (r >= 0 && r <= 2) k = 1;
+        }
+        if (k < 0 || B.n >= kBsdfMaxLobes) return;
+        B.kind[B.n] = k;
+        for (int c = 0; c < 3; ++c) B.w[B.n][c] = cw[c];
+        B.p[B.n] = params;
+        ++B.n;
     });
-    // prepare(wo, path_weight = 1, absorb = false)
-    float pdfs[kBsdfMaxLobes];
+}
+__device__ __forceinline__ GGXLobe lobe_ggx(const Lane& L, uint32_t p) {
+    GGXLobe g;
+    const V3 N = v3(hget(L, p + 1), hget(L, p + 2), hget(L, p + 3));
+    const V3 U = v3(hget(L, p + 4), hget(L, p + 5), hget(L, p + 6));
+    g.tf = frame_from_normal_and_tangent(N, U);
+    g.ax = hget(L, p + 7);
+    g.ay = hget(L, p + 8);
+    g.eta = hget(L, p + 9);
+    g.refract = (int)hgetu(L, p + 10);
+    return g;
+}
+__device__ __forceinline__ BsdfSample lobe_eval(const Lane& L, const Lobes& B, int i, V3 wo, V3 wi) {
+    const uint32_t p = B.p[i];
+    if (B.kind[i] == 0) {
+        BsdfSample s = diffuse_eval(v3(hget(L, p + 0), hget(L, p + 1), hget(L, p + 2)), wi);
+        s.wi = wi;
+        return s;
+    }
+    if (B.kind[i] == 1) return ggx_eval(lobe_ggx(L, p), wo, wi);
+    const V3 N = v3(hget(L, p + 0), hget(L, p + 1), hget(L, p + 2));
+    const Frame f = bsdl_frame(bsdl_visible_normal(wo, N, N));
+    BsdfSample s = on_eval_local(bsdl_clamp(hget(L, p + 3), 0.0f, 1.0f), tolocal(f, wo), tolocal(f, wi));
+    s.wi = wi;
+    return s;
+}
+__device__ __forceinline__ BsdfSample lobe_sample(const Lane& L, const Lobes& B, int i, V3 wo, float rx, float ry,
+                                                  float rz) {
+    const uint32_t p = B.p[i];
+    if (B.kind[i] == 0) return diffuse_sample(v3(hget(L, p + 0), hget(L, p + 1), hget(L, p + 2)), rx, ry);
+    if (B.kind[i] == 1) return ggx_sample(lobe_ggx(L, p), wo, rx, ry, rz);
+    const V3 N = v3(hget(L, p + 0), hget(L, p + 1), hget(L, p + 2));
+    const Frame f = bsdl_frame(bsdl_visible_normal(wo, N, N));
+    const V3 wo_l = tolocal(f, wo);
+    if (wo_l.z <= 0.0f) return bsdf_zero();
+    BsdfSample s = on_eval_local(bsdl_clamp(hget(L, p + 3), 0.0f, 1.0f), wo_l, bsdl_sample_cos_hemisphere(rx, ry));
+    s.wi = bsdl_world(f, s.wi);
+    return s;
+}
+// CompositeBSDF::prepare (shading.h:322-350)
+__device__ __forceinline__ void lobes_prepare(const Lane& L, Lobes& B, V3 wo, const float* pw, bool absorb) {
     float total = 0.0f;
-    for (int i = 0; i < nl; ++i) {
+    for (int i = 0; i < B.n; ++i) {
         float alb = 1.0f;
-        if (kind[i] == 1) {
-            V3 N = v3(hget(L, lp[i] + 1), hget(L, lp[i] + 2), hget(L, lp[i] + 3));
-            alb = fresnel_dielectric(vdot(N, wo), hget(L, lp[i] + 9));
+        if (B.kind[i] == 1) {
+            const uint32_t p = B.p[i];
+            const GGXLobe g = lobe_ggx(L, p);
+            alb = ggx_albedo(g, v3(hget(L, p + 1), hget(L, p + 2), hget(L, p + 3)), wo);
         }
-        pdfs[i] = (lw[i][0] * (1.0f * alb) + lw[i][1] * (1.0f * alb) + lw[i][2] * (1.0f * alb)) / (1.0f + 1.0f + 1.0f);
-        total += pdfs[i];
+        B.pdf[i] = (B.w[i][0] * (pw[0] * alb) + B.w[i][1] * (pw[1] * alb) + B.w[i][2] * (pw[2] * alb))
+                 / (pw[0] + pw[1] + pw[2]);
+        total += B.pdf[i];
     }
-    if (total > 0.0f || total > 1.0f)
-        for (int i = 0; i < nl; ++i) pdfs[i] /= total;
-    float sw[3] = { 0.0f, 0.0f, 0.0f }, spdf = 0.0f, srough = 0.0f;
-    for (int i = 0; i < nl; ++i) {
-        BsdfSample b;
-        if (kind[i] == 0) {
-            b = diffuse_eval(v3(hget(L, lp[i] + 0), hget(L, lp[i] + 1), hget(L, lp[i] + 2)), wi);
-        } else {
-            V3 N = v3(hget(L, lp[i] + 1), hget(L, lp[i] + 2), hget(L, lp[i] + 3));
-            V3 U = v3(hget(L, lp[i] + 4), hget(L, lp[i] + 5), hget(L, lp[i] + 6));
-            Frame tf = frame_from_normal_and_tangent(N, U);
-            b = microfacet_ggx_refl_eval(tf, hget(L, lp[i] + 7), hget(L, lp[i] + 8), hget(L, lp[i] + 9), wo, wi);
+    if ((!absorb && total > 0.0f) || total > 1.0f)
+        for (int i = 0; i < B.n; ++i) B.pdf[i] /= total;
+}
+// CompositeBSDF::eval (shading.h:360-370)
+__device__ __forceinline__ BsdfSample lobes_eval(const Lane& L, const Lobes& B, V3 wo, V3 wi) {
+    BsdfSample r = bsdf_zero();
+    for (int i = 0; i < B.n; ++i) {
+        BsdfSample b = lobe_eval(L, B, i, wo, wi);
+        for (int c = 0; c < 3; ++c) b.w[c] *= B.w[i][c];
+        mis_update_eval(r.w, &r.pdf, b.w, b.pdf, B.pdf[i]);
+        r.roughness += b.roughness * B.pdf[i];
+    }
+    return r;
+}
+// CompositeBSDF::sample (shading.h:372-398)
+__device__ __forceinline__ BsdfSample lobes_sample(const Lane& L, const Lobes& B, V3 wo, float rx, float ry, float rz) {
+    float accum = 0.0f;
+    for (int i = 0; i < B.n; ++i) {
+        if (rx < (B.pdf[i] + accum)) {
+            rx = (rx - accum) / B.pdf[i];
+            rx = fminf(rx, 0.99999994f);
+            BsdfSample s = lobe_sample(L, B, i, wo, rx, ry, rz);
+            const float inv = 1 / B.pdf[i];
+            for (int c = 0; c < 3; ++c) s.w[c] *= B.w[i][c] * inv;
+            s.pdf *= B.pdf[i];
+            if (s.pdf == 0.0f) return bsdf_zero();
+            for (int j = 0; j < B.n; ++j) {
+                if (i != j) {
+                    BsdfSample b = lobe_eval(L, B, j, wo, s.wi);
+                    for (int c = 0; c < 3; ++c) b.w[c] *= B.w[j][c];
+                    mis_update_eval(s.w, &s.pdf, b.w, b.pdf, B.pdf[j]);
+                }
+            }
+            return s;
         }
-        for (int c = 0; c < 3; ++c) b.w[c] *= lw[i][c];
-        mis_update_eval(sw, &spdf, b.w, b.pdf, pdfs[i]);
-        srough += b.roughness * pdfs[i];
+        accum += B.pdf[i];
     }
+    return bsdf_zero();
+}
+
+// Renderer-side BSDF evaluation of a closure output at a light direction:
+// prepare(wo, path_weight 1, absorb false) and eval (shading.h:322-374).
+static __device__ void h_bsdf_eval(const Lane& L, const uint32_t* a, char* base, const ClosurePools& P, uint32_t* st) {
+    const uint32_t root = ldw(L, a[0], 0);
+    const V3 wi = v3(ldf(L, a[3], 0, 0), ldf(L, a[3], 1, 0), ldf(L, a[3], 2, 0));
+    const V3 wo = v3(-ldf(L, a[4], 0, 0), -ldf(L, a[4], 1, 0), -ldf(L, a[4], 2, 0));
+    Lobes B;
+    lobes_build(L, P, root, a[5], st, B);
+    const float one[3] = { 1.0f, 1.0f, 1.0f };
+    lobes_prepare(L, B, wo, one, false);
+    const BsdfSample r = lobes_eval(L, B, wo, wi);
     float* o = reinterpret_cast<float*>(base + (int64_t)a[1] + L.pt * (int64_t)(int32_t)a[2]);
-    o[0] = sw[0]; o[1] = sw[1]; o[2] = sw[2]; o[3] = spdf;
+    o[0] = r.w[0]; o[1] = r.w[1]; o[2] = r.w[2]; o[3] = r.pdf;
+}
+
+// Renderer-side sampling of a closure output, the per-hit step of
+// testrender's path loop (simpleraytracer.cpp:1038-1079): userdata record
+// {rx, ry, rz, path weight rgb, absorb}; output {wi, weight, pdf, Le, roughness}.
+static __device__ void h_bsdf_sample(const Lane& L, const uint32_t* a, char* base, const char* ud,
+                                     const ClosurePools& P, uint32_t* st) {
+    const uint32_t root = ldw(L, a[0], 0);
+    const V3 wo = v3(-ldf(L, a[3], 0, 0), -ldf(L, a[3], 1, 0), -ldf(L, a[3], 2, 0));
+    const float* in = reinterpret_cast<const float*>(ud + (int64_t)a[5] + L.pt * (int64_t)(int32_t)a[6]);
+    Lobes B;
+    lobes_build(L, P, root, a[4], st, B);
+    const float pw[3] = { in[3], in[4], in[5] };
+    lobes_prepare(L, B, wo, pw, in[6] != 0.0f);
+    const BsdfSample r = lobes_sample(L, B, wo, in[0], in[1], in[2]);
+    float* o = reinterpret_cast<float*>(base + (int64_t)a[1] + L.pt * (int64_t)(int32_t)a[2]);
+    o[0] = r.wi.x; o[1] = r.wi.y; o[2] = r.wi.z;
+    o[3] = r.w[0]; o[4] = r.w[1]; o[5] = r.w[2];
+    o[6] = r.pdf;
+    o[7] = B.Le[0]; o[8] = B.Le[1]; o[9] = B.Le[2];
+    o[10] = r.roughness;
 }
 
 // ---- spline (splineimpl.h:191-239) -----------------------------------------------------
@@ -1812,6 +1923,7 @@ __device__ __forceinline__ void run_tile(const RunCtx& R, Lane& L, int64_t npoin
                 case OP_CLOSURE_ADD: OSLG_TIER_CASE(2, h_closure_add(L, a, R.CP, R.status)) break;
                 case OP_STORE_CLOSURE: OSLG_TIER_CASE(2, h_store_closure(L, a, R.outputs, R.CP, R.status)) break;
                 case OP_BSDF_EVAL: OSLG_TIER_CASE(2, h_bsdf_eval(L, a, R.outputs, R.CP, R.status)) break;
+                case OP_BSDF_SAMPLE: OSLG_TIER_CASE(2, h_bsdf_sample(L, a, R.outputs, R.userdata, R.CP, R.status)) break;
                 case OP_SPLINE: OSLG_TIER_CASE(2, h_spline(L, a)) break;
                 default: raise_status(R.status, ST_BAD_OPCODE); break;
                 }

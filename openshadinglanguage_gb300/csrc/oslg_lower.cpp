@@ -359,6 +359,18 @@ struct Lowerer {
             op.imm[0] = be.offset; op.imm[1] = be.stride;
             lops.push_back(op);
         }
+        for (const BsdfSampleRequest& bs : g.bsdf_samples) {
+            SymLoc tmp;
+            tmp.name = bs.closure;
+            int gs = resolve_symloc(tmp);
+            if (gs < 0 || syms[gs].type.base != BT_CLOSURE)
+                return fail("bsdf sample: '" + bs.closure + "' is not a closure of the group");
+            TypeSpec vt; vt.base = BT_TRIPLE; vt.vecsem = VS_VECTOR;
+            int I = global_sym("I", vt);
+            LOp op; op.name = "__bsdf_sample"; op.args = { gs, I };
+            op.imm[0] = bs.offset; op.imm[1] = bs.stride; op.imm[2] = bs.in_offset; op.imm[3] = bs.in_stride;
+            lops.push_back(op);
+        }
         // renderer outputs placed through symlocs
         for (const SymLoc& sl : g.symlocs) {
             if (sl.arena != ARENA_OUTPUTS) continue;
@@ -393,7 +405,8 @@ struct Lowerer {
             return op.argrw[i] == 'w' || op.argrw[i] == 'W';
         static const std::set<std::string> nowrite = {
             "if", "for", "while", "dowhile", "break", "continue", "return", "exit", "nop",
-            "useparam", "__layer_end", "__store_output", "__bsdf_eval", "functioncall", "functioncall_nr",
+            "useparam", "__layer_end", "__store_output", "__bsdf_eval", "__bsdf_sample", "functioncall",
+            "functioncall_nr",
             "printf", "warning", "error", "fprintf" };
         if (nowrite.count(op.name)) return false;
         if (op.name == "sincos") return i == 1 || i == 2;
@@ -917,6 +930,15 @@ struct Lowerer {
                  "bsdf_eval");
             return true;
         }
+        if (n == "__bsdf_sample") {
+            // renderer-side sampling of a closure output (testrender's
+            // CompositeBSDF::prepare + sample, src/testrender/shading.h:322-398)
+            uses_closures = true;
+            emit(OP_BSDF_SAMPLE, { a(0), (uint32_t)op.imm[0], (uint32_t)op.imm[1], a(1), string_hash("ggx"),
+                                   (uint32_t)op.imm[2], (uint32_t)op.imm[3] },
+                 "bsdf_sample");
+            return true;
+        }
         if (n == "__store_output") {
             int s = op.args[0];
             if (is_closure(s)) {
@@ -1150,6 +1172,7 @@ struct Lowerer {
             switch (op.code) {
             case OP_NOISE: case OP_HASH: case OP_GABOR: t |= 1u; break;
             case OP_CLOSURE: case OP_CLOSURE_MUL: case OP_CLOSURE_ADD: case OP_STORE_CLOSURE: case OP_BSDF_EVAL:
+            case OP_BSDF_SAMPLE:
             case OP_SPLINE:
                 t |= 2u;
                 break;

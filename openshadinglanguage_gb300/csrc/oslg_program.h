@@ -123,6 +123,8 @@ enum OpCode : uint16_t {
     OP_STORE_CLOSURE,// a0=src a1=byte offset a2=byte stride a3=max components
     OP_BSDF_EVAL,    // a0=closure a1=byte offset a2=byte stride a3=wi (triple)
                      // a4=I (triple global) a5=hash("ggx")
+    OP_BSDF_SAMPLE,  // a0=closure a1=out byte offset a2=out byte stride a3=I (triple
+                     // global) a4=hash("ggx") a5=userdata byte offset a6=userdata stride
     OP_COUNT
 };
 

@@ -12,6 +12,7 @@
 //   CompositeBSDF prepare/eval with MIS::update_eval (shading.h:319-374,
 //   sampling.h:175-205).
 #pragma once
+#include "oslg_fmath.cuh"
 #include "oslg_noise.cuh"
 #include "oslg_program.h"
 
@@ -116,7 +117,16 @@ struct BsdfSample {
     float w[3];
     float pdf;
     float roughness;
+    V3 wi;
 };
+__device__ __forceinline__ BsdfSample bsdf_zero() {
+    BsdfSample s;
+    s.w[0] = s.w[1] = s.w[2] = 0.0f;
+    s.pdf = 0.0f;
+    s.roughness = 0.0f;
+    s.wi = v3(0.0f, 0.0f, 0.0f);
+    return s;
+}
 
 // Diffuse<0>::eval (shading.cpp:307-311)
 __device__ __forceinline__ BsdfSample diffuse_eval(V3 N, V3 wi) {
@@ -190,6 +200,304 @@ __device__ __forceinline__ void mis_update_eval(float* w, float* pdf, const floa
         for (int c = 0; c < 3; ++c) w[c] = w[c] * (1.0f - mis) + ow[c] * mis;
         *pdf += opdf;
     }
+}
+
+
+// ---- sampling (wavefront path step) ------------------------------------------------
+// TangentFrame::get (sampling.h:44-47)
+__device__ __forceinline__ V3 frame_get(const Frame& f, float x, float y, float z) {
+    return vadd(vadd(vmul(f.u, x), vmul(f.v, y)), vmul(f.w, z));
+}
+__device__ __forceinline__ V3 vneg(V3 a) { return v3(-a.x, -a.y, -a.z); }
+
+// Sampling::to_unit_disk / sample_cosine_hemisphere (sampling.h:70-100); the
+// reference's OIIO::fast_sincos is the executor's own sincos here
+__device__ __forceinline__ void to_unit_disk(float& x, float& y) {
+    const float PI_OVER_4 = 0.785398163397448309616f, PI_OVER_2 = 1.57079632679489661923f;
+    float phi, r;
+    const float a = 2 * x - 1, b = 2 * y - 1;
+    if (a * a > b * b) {
+        r = a;
+        phi = PI_OVER_4 * (b / a);
+    } else if (b != 0) {
+        r = b;
+        phi = PI_OVER_2 - PI_OVER_4 * (a / b);
+    } else {
+        r = 0;
+        phi = 0;
+    }
+    own_sincos(phi, &x, &y);
+    x *= r;
+    y *= r;
+}
+// Diffuse<0>::sample (shading.cpp:313-319)
+__device__ __forceinline__ BsdfSample diffuse_sample(V3 N, float rx, float ry) {
+    to_unit_disk(rx, ry);
+    const float cos_theta = sqrtf(fmaxf(1 - rx * rx - ry * ry, 0.0f));
+    BsdfSample s;
+    s.wi = frame_get(frame_from_normal(N), rx, ry, cos_theta);
+    s.pdf = cos_theta * 0.318309886183790671538f;
+    s.w[0] = s.w[1] = s.w[2] = 1.0f;
+    s.roughness = 1.0f;
+    return s;
+}
+
+// optics.h:34-66
+__device__ __forceinline__ float fresnel_refraction(V3 I, V3 N, float eta, V3* T) {
+    float cosi = -vdot(I, N);
+    V3 Nn;
+    float neta;
+    if (cosi > 0) {
+        neta = 1 / eta;
+        Nn = N;
+    } else {
+        cosi = -cosi;
+        neta = eta;
+        Nn = vneg(N);
+    }
+    const float arg = 1.0f - (neta * neta * (1.0f - cosi * cosi));
+    if (arg >= 0) {
+        const float dnp = sqrtf(arg);
+        const float nK = (neta * cosi) - dnp;
+        *T = vadd(vmul(I, neta), vmul(Nn, nK));
+        return 1 - fresnel_dielectric(cosi, eta);
+    }
+    *T = v3(0.0f, 0.0f, 0.0f);
+    return 0;
+}
+
+struct GGXLobe {
+    Frame tf;
+    float ax, ay, eta;
+    int refract;
+};
+__device__ __forceinline__ float ggx_D(const GGXLobe& g, V3 m) { return mf_D(m, g.ax, g.ay); }
+__device__ __forceinline__ float ggx_albedo(const GGXLobe& g, V3 N, V3 wo) {
+    if (g.refract == 2) return 1.0f;
+    const float fr = fresnel_dielectric(vdot(N, wo), g.eta);
+    return g.refract ? 1 - fr : fr;
+}
+// Microfacet<GGXDist, Refract>::eval (shading.cpp:589-652)
+__device__ __forceinline__ BsdfSample ggx_eval(const GGXLobe& g, V3 wo, V3 wi) {
+    const V3 wo_l = tolocal(g.tf, wo), wi_l = tolocal(g.tf, wi);
+    BsdfSample s = bsdf_zero();
+    s.wi = wi;
+    if (g.refract == 0 || g.refract == 2) {
+        if (wo_l.z > 0 && wi_l.z > 0) {
+            const V3 m = vnormalize_imath(vadd(wi_l, wo_l));
+            const float D = ggx_D(g, m);
+            const float Lo = mf_lambda(wo_l, g.ax, g.ay), Li = mf_lambda(wi_l, g.ax, g.ay);
+            const float G2 = 1 / (Lo + Li + 1), G1 = 1 / (Lo + 1);
+            const float Fr = fresnel_dielectric(vdot(m, wo_l), g.eta);
+            const float pdf = (G1 * D * 0.25f) / wo_l.z;
+            const float out = G2 / G1;
+            s.roughness = fmaxf(g.ax, g.ay);
+            if (g.refract == 2) {
+                s.pdf = pdf * Fr;
+                s.w[0] = s.w[1] = s.w[2] = out;
+            } else {
+                s.pdf = pdf;
+                s.w[0] = s.w[1] = s.w[2] = out * Fr;
+            }
+            return s;
+        }
+    }
+    if (g.refract == 1 || g.refract == 2) {
+        if (wi_l.z < 0 && wo_l.z > 0.0f) {
+            V3 ht = vneg(vadd(vmul(wi_l, g.eta), wo_l));
+            if (g.eta < 1.0f) ht = vneg(ht);
+            const V3 Ht = vnormalize_imath(ht);
+            const float cosHO = vdot(Ht, wo_l);
+            const float Ft = 1.0f - fresnel_dielectric(cosHO, g.eta);
+            if (Ft > 0) {
+                const float cosHI = vdot(Ht, wi_l);
+                if (Ht.z <= 0.0f) return bsdf_zero();
+                const float Dt = ggx_D(g, Ht);
+                const float Lo = mf_lambda(wo_l, g.ax, g.ay), Li = mf_lambda(wi_l, g.ax, g.ay);
+                const float G2 = 1 / (Lo + Li + 1), G1 = 1 / (Lo + 1);
+                const float invHt2 = 1 / vdot(ht, ht);
+                const float pdf = (fabsf(cosHI * cosHO) * (g.eta * g.eta) * (G1 * Dt) * invHt2) / wo_l.z;
+                const float out = G2 / G1;
+                s.roughness = fmaxf(g.ax, g.ay);
+                if (g.refract == 2) {
+                    s.pdf = pdf * Ft;
+                    s.w[0] = s.w[1] = s.w[2] = out;
+                } else {
+                    s.pdf = pdf;
+                    s.w[0] = s.w[1] = s.w[2] = out * Ft;
+                }
+                return s;
+            }
+        }
+    }
+    return bsdf_zero();
+}
+// GGXDist::sampleSlope (shading.cpp:480-508)
+__device__ __forceinline__ void ggx_sample_slope(float cos_theta, float randu, float randv, float* sx, float* sy) {
+    const float c = cos_theta < 1e-6f ? 1e-6f : cos_theta;
+    const float Q = (1 + c) * randu - c;
+    const float num = c * sqrtf((1 - c) * (1 + c)) - Q * sqrtf((1 - Q) * (1 + Q));
+    float den = (Q - c) * (Q + c);
+    const float eps = 1.0f / 4294967296.0f;
+    den = fabsf(den) < eps ? copysignf(eps, den) : den;
+    *sx = num / den;
+    const float Ru = 1 - 2 * randv;
+    const float u2 = fabsf(Ru);
+    const float z = (u2 * (u2 * (u2 * 0.27385f - 0.73369f) + 0.46341f))
+                  / (u2 * (u2 * (u2 * 0.093073f + 0.309420f) - 1.0f) + 0.597999f);
+    *sy = copysignf(1.0f, Ru) * z * sqrtf(1.0f + *sx * *sx);
+}
+// Microfacet::sampleMicronormal (shading.cpp:754-787)
+__device__ __forceinline__ V3 ggx_sample_micronormal(const GGXLobe& g, V3 wo, float randu, float randv) {
+    V3 swo = wo;
+    swo.x *= g.ax;
+    swo.y *= g.ay;
+    swo = vnormalize_imath(swo);
+    const float cos_theta = fmaxf(swo.z, 0.0f);
+    float cos_phi = 1, sin_phi = 0;
+    if (cos_theta < 0.99999f) {
+        const float invnorm = 1 / sqrtf(swo.x * swo.x + swo.y * swo.y);
+        cos_phi = swo.x * invnorm;
+        sin_phi = swo.y * invnorm;
+    }
+    float slx, sly;
+    ggx_sample_slope(cos_theta, randu, randv, &slx, &sly);
+    float sx = cos_phi * slx - sin_phi * sly;
+    float sy = sin_phi * slx + cos_phi * sly;
+    sx *= g.ax;
+    sy *= g.ay;
+    const float mlen = sqrtf(sx * sx + sy * sy + 1);
+    return v3(fabsf(sx) < mlen ? -sx / mlen : 1.0f, fabsf(sy) < mlen ? -sy / mlen : 1.0f, 1.0f / mlen);
+}
+// Microfacet::sample (shading.cpp:628-700)
+__device__ __forceinline__ BsdfSample ggx_sample(const GGXLobe& g, V3 wo, float rx, float ry, float rz) {
+    const V3 wo_l = tolocal(g.tf, wo);
+    const float cosNO = wo_l.z;
+    if (!(cosNO > 0)) return bsdf_zero();
+    const V3 m = ggx_sample_micronormal(g, wo_l, rx, ry);
+    const float cosMO = vdot(m, wo_l);
+    const float F = fresnel_dielectric(cosMO, g.eta);
+    BsdfSample s = bsdf_zero();
+    if (g.refract == 0 || (g.refract == 2 && rz < F)) {
+        const V3 wi_l = vsub(vmul(m, 2.0f * cosMO), wo_l);
+        const float D = ggx_D(g, m);
+        const float Lo = mf_lambda(wo_l, g.ax, g.ay), Li = mf_lambda(wi_l, g.ax, g.ay);
+        const float G2 = 1 / (Lo + Li + 1), G1 = 1 / (Lo + 1);
+        s.wi = frame_get(g.tf, wi_l.x, wi_l.y, wi_l.z);
+        const float pdf = (G1 * D * 0.25f) / cosNO;
+        const float out = G2 / G1;
+        s.roughness = fmaxf(g.ax, g.ay);
+        if (g.refract == 2) {
+            s.pdf = pdf * F;
+            s.w[0] = s.w[1] = s.w[2] = out;
+        } else {
+            s.pdf = pdf;
+            s.w[0] = s.w[1] = s.w[2] = F * out;
+        }
+        return s;
+    }
+    const V3 M = frame_get(g.tf, m.x, m.y, m.z);
+    V3 wi;
+    const float Ft = fresnel_refraction(vneg(wo), M, g.eta, &wi);
+    const V3 wi_l = tolocal(g.tf, wi);
+    const float cosHO = vdot(m, wo_l), cosHI = vdot(m, wi_l);
+    const float D = ggx_D(g, m);
+    const float Lo = mf_lambda(wo_l, g.ax, g.ay), Li = mf_lambda(wi_l, g.ax, g.ay);
+    const float G2 = 1 / (Lo + Li + 1), G1 = 1 / (Lo + 1);
+    const V3 ht = vneg(vadd(vmul(wi_l, g.eta), wo_l));
+    const float invHt2 = 1.0f / vdot(ht, ht);
+    const float pdf = (fabsf(cosHI * cosHO) * (g.eta * g.eta) * (G1 * D) * invHt2) / fabsf(wo_l.z);
+    const float out = G2 / G1;
+    s.wi = wi;
+    s.roughness = fmaxf(g.ax, g.ay);
+    if (g.refract == 2) {
+        s.pdf = pdf * Ft;
+        s.w[0] = s.w[1] = s.w[2] = out;
+    } else {
+        s.pdf = pdf;
+        s.w[0] = s.w[1] = s.w[2] = Ft * out;
+    }
+    return s;
+}
+
+// BSDL (libbsdl/include/BSDL/tools.h:196-275, :459-508; bsdf_impl.h:51-78)
+__device__ __forceinline__ float bsdl_cos_quadrant(float x) {
+    const float x2 = x * x;
+    float cp = 0.01578646f + -0.00029826362f * x2;
+    cp = -0.30837047f + cp * x2;
+    cp = 0.99998736f + cp * x2;
+    return cp;
+}
+__device__ __forceinline__ float bsdl_sin_quadrant(float x) {
+    const float x2 = x * x;
+    float sp = 0.0024843954015523195266723632812500f + -0.0000341485538228880614042282104492f * x2;
+    sp = -0.0807407423853874206542968750000000f + sp * x2;
+    sp = 0.7853975892066955566406250000000000f + sp * x2;
+    return sp * x;
+}
+__device__ __forceinline__ V3 bsdl_sample_cos_hemisphere(float randu, float randv) {
+    const float a = 2 * randu - 1, qa = fabsf(a);
+    const float b = 2 * randv - 1, qb = fabsf(b);
+    const float rad = qa > qb ? qa : qb;
+    const float phi = qa > qb ? qb / qa : ((qa == qb) ? 1.0f : 2 - qa / qb);
+    const float x = copysignf(rad * bsdl_cos_quadrant(phi), a);
+    const float y = copysignf(rad * bsdl_sin_quadrant(phi), b);
+    return v3(x, y, sqrtf(1 - rad * rad));
+}
+__device__ __forceinline__ Frame bsdl_frame(V3 z) {
+    const float s = copysignf(1.0f, z.z);
+    const float a = -1.0f / (s + z.z);
+    const float b = z.x * z.y * a;
+    Frame f;
+    f.u = v3(1.0f + s * z.x * z.x * a, s * b, -s * z.x);
+    f.v = v3(b, s + z.y * z.y * a, -z.y);
+    f.w = z;
+    return f;
+}
+__device__ __forceinline__ V3 bsdl_world(const Frame& f, V3 a) {
+    return v3(f.u.x * a.x + f.v.x * a.y + f.w.x * a.z, f.u.y * a.x + f.v.y * a.y + f.w.y * a.z,
+              f.u.z * a.x + f.v.z * a.y + f.w.z * a.z);
+}
+__device__ __forceinline__ float bsdl_max_abs(V3 v) { return fmaxf(fabsf(v.x), fmaxf(fabsf(v.y), fabsf(v.z))); }
+__device__ __forceinline__ V3 bsdl_visible_normal(V3 wo, V3 Ngf, V3 N) {
+    if (vdot(wo, N) > 0.0f) return N;
+    V3 V = vcross(wo, N);
+    if (bsdl_max_abs(V) < 1e-4f) {
+        V = vcross(wo, Ngf);
+        if (bsdl_max_abs(V) < 1e-4f) {
+            const float s = copysignf(1.0f, wo.z);
+            const float a = -1.0f / (s + wo.z);
+            V = v3(wo.x * wo.y * a, s + wo.y * wo.y * a, -wo.y);
+        } else {
+            V = vnormalize_imath(V);
+        }
+    } else {
+        V = vnormalize_imath(V);
+    }
+    return vnormalize_imath(vadd(vcross(V, wo), vmul(wo, 1e-4f)));
+}
+__device__ __forceinline__ float bsdl_clamp(float x, float a, float b) { return fminf(fmaxf(x, a), b); }
+
+// oren_nayar as testrender builds it: BSDL OrenNayarDiffuseLobe, energy
+// compensation off, albedo 1 (libbsdl MTX/bsdf_oren_nayar_diffuse_impl.h:41-113)
+__device__ __forceinline__ BsdfSample on_eval_local(float rough, V3 wo, V3 wi) {
+    BsdfSample s = bsdf_zero();
+    const float cosNI = bsdl_clamp(wi.z, 0.0f, 1.0f);
+    const float cosNO = bsdl_clamp(wo.z, 0.0f, 1.0f);
+    if (cosNI <= 0.0f || cosNO <= 0.0f) return s;
+    const float cosIO = bsdl_clamp(vdot(wo, wi), -1.0f, 1.0f);
+    const float sv = cosIO - cosNI * cosNO;
+    const float pdf = cosNI * (1.0f / 3.14159265358979323846f);
+    const float s2 = rough * rough;
+    const float A = 1.0f - 0.50f * s2 / (s2 + 0.33f);
+    const float B = 0.45f * s2 / (s2 + 0.09f);
+    const float stinv = sv > 0.0f ? sv / fmaxf(cosNI, cosNO) : 0.0f;
+    const float f_ss = A + B * stinv;
+    s.wi = wi;
+    s.w[0] = s.w[1] = s.w[2] = 1.0f * f_ss;
+    s.pdf = pdf;
+    s.roughness = 1.0f;
+    return s;
 }
 
 }  // namespace dev

@@ -39,6 +39,8 @@ def make_globals(**fields):
         else:
             if hasattr(val, "is_contiguous") and not val.is_contiguous():
                 raise ValueError("global '%s' must be contiguous" % name)
+            if hasattr(val, "flags") and not val.flags["C_CONTIGUOUS"]:
+                raise ValueError("global '%s' must be C-contiguous (x, y, z planes)" % name)
             f.data = ctypes.c_void_p(_addr(val))
             f.plane_stride = int(val.shape[-1]) if len(val.shape) == 2 else 0
             keep.append(val)

@@ -170,6 +170,13 @@ class ShadingSystem:
             arr[i] = C.SymLocC(nm, s.type.c(), 1 if s.derivs else 0, s.arena, s.offset, s.stride)
         self._check(C.lib().oslg_add_symlocs(self._h, group.handle, arr, len(locs)))
 
+    def bsdf_sample_output(self, group, closure, offset, stride, in_offset, in_stride):
+        """Per point: read {rx, ry, rz, path_weight.rgb, absorb} from the
+        userdata arena, write {wi.xyz, weight.rgb, pdf, Le.rgb, roughness}
+        to the output arena (include/oslg.h, oslg_group_bsdf_sample)."""
+        self._check(C.lib().oslg_group_bsdf_sample(self._h, group.handle, closure.encode(), int(offset), int(stride),
+                                                   int(in_offset), int(in_stride)))
+
     def bsdf_eval_output(self, group, closure, wi, offset, stride):
         """Evaluate closure output `closure` as testrender's CompositeBSDF at
         wo = -I and light direction wi; writes weight rgb + pdf per point."""

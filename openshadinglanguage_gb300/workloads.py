@@ -6,6 +6,10 @@ C2  layered_closure 3-layer pattern -> ramp -> closure group with BSDF eval,
 C3  random groups   64 seeded random op DAGs of 20-200 ops with noise,
                     transforms, if/else and data-dependent loops; point
                     counts log-uniform in [1K, 1M], P uniform in [-10,10]^3
+C5  materials       16 seeded 2-4 layer material groups (noise patterns,
+                    tint, a closure sum of diffuse / oren_nayar / GGX
+                    microfacet / GGX dielectric / emission) with a BSDF
+                    sample output for the wavefront path tracer
 """
 import numpy as np
 
@@ -338,3 +342,156 @@ def c3_points(k, npts, seed=C3_SEED):
     """P uniform in [-10, 10]^3 from the group's own stream, SoA (3, n)."""
     rng = np.random.default_rng([seed, 0x50, k])
     return rng.uniform(-10.0, 10.0, (3, npts)).astype(np.float32)
+
+
+# ---- C5 ------------------------------------------------------------------------------
+C5_SEED = 0xC5
+C5_MATERIALS = 16
+C5_IN_FLOATS = 7    # rx, ry, rz, path weight rgb, absorb
+C5_OUT_FLOATS = 11  # wi xyz, weight rgb, pdf, Le rgb, roughness
+
+
+def _c5_pattern(name, kind, freq):
+    from .oso import OsoBuilder
+    b = OsoBuilder(name)
+    a = b.param("float", "a", 0.0, output=True)
+    P = b.glob("point", "P")
+    p = b.tmp("point")
+    b.op("mul", p, P, b.const("float", float(np.float32(freq))))
+    if kind == "cell":
+        b.op("cellnoise", a, p)
+    else:
+        b.op("noise", a, b.const("string", kind), p)
+    return b.text()
+
+
+def _c5_tint(name, c0, c1):
+    from .oso import OsoBuilder
+    b = OsoBuilder(name)
+    x = b.param("float", "x", 0.5)
+    tint = b.param("color", "tint", [1, 1, 1], output=True)
+    b.op("mix", tint, b.const("color", [float(np.float32(v)) for v in c0]),
+         b.const("color", [float(np.float32(v)) for v in c1]), x)
+    return b.text()
+
+
+def _c5_surface(name, lobes):
+    """lobes: list of (kind, weight, extra) with kind in diffuse, oren_nayar,
+    ggx, dielectric, emission; the closure sum is Ci."""
+    from .oso import OsoBuilder
+    b = OsoBuilder(name, "surface")
+    a = b.param("float", "a", 0.5)
+    r = b.param("float", "r", 0.5)
+    tint = b.param("color", "tint", [1, 1, 1])
+    Ci = b.glob("closure color", "Ci")
+    N, dPdu = b.glob("normal", "N"), b.glob("vector", "dPdu")
+    c = lambda x: b.const("float", float(np.float32(x)))
+    acc = None
+    for kind, weight, extra in lobes:
+        cl, w, cw = b.tmp("closure color"), b.tmp("color"), b.tmp("closure color")
+        if kind == "diffuse":
+            b.op("closure", cl, b.const("string", "diffuse"), N)
+        elif kind == "oren_nayar":
+            b.op("closure", cl, b.const("string", "oren_nayar"), N, c(extra))
+        elif kind in ("ggx", "dielectric"):
+            alpha, t = b.tmp("float"), b.tmp("float")
+            b.op("mul", t, c(0.6), r)
+            b.op("add", alpha, c(0.05), t)
+            eta = extra if kind == "dielectric" else 1.5
+            b.op("closure", cl, b.const("string", "microfacet"), b.const("string", "ggx"), N, dPdu, alpha, alpha,
+                 c(eta), b.const("int", 2 if kind == "dielectric" else 0))
+        else:  # emission, modulated by the pattern
+            b.op("closure", cl, b.const("string", "emission"))
+        tw = b.tmp("color")
+        b.op("mul", tw, tint, c(weight))
+        if kind == "emission":
+            b.op("mul", w, tw, a)
+            b.op("mul", w, w, c(extra))
+        else:
+            b.op("assign", w, tw)
+        b.op("mul", cw, cl, w)
+        if acc is None:
+            acc = cw
+        else:
+            s2 = b.tmp("closure color")
+            b.op("add", s2, acc, cw)
+            acc = s2
+    b.op("assign", Ci, acc)
+    return b.text()
+
+
+def c5_material_specs(seed=C5_SEED, n=C5_MATERIALS):
+    """Per material: pattern layers (kind, frequency), tint colours or None,
+    and the closure lobes. Two materials emit."""
+    rng = np.random.default_rng([seed, 0x11])
+    specs = []
+    for k in range(n):
+        nl = int(rng.integers(2, 5))  # 2..4 layers
+        pats = [(str(rng.choice(["usimplex", "uperlin", "cell"])), float(rng.uniform(0.5, 4.0)))]
+        if nl >= 3:
+            pats.append((str(rng.choice(["usimplex", "uperlin"])), float(rng.uniform(1.0, 8.0))))
+        tint = None
+        if nl == 4:
+            tint = (tuple(rng.uniform(0.1, 0.9, 3)), tuple(rng.uniform(0.1, 0.9, 3)))
+        if k in (3, 11):
+            lobes = [("emission", 1.0, float(rng.uniform(2.0, 8.0))), ("diffuse", 0.5, 0.0)]
+        else:
+            base = str(rng.choice(["diffuse", "oren_nayar"]))
+            lobes = [(base, float(rng.uniform(0.4, 0.8)), float(rng.uniform(0.0, 0.5)))]
+            extra = str(rng.choice(["ggx", "dielectric", "none"]))
+            if extra != "none":
+                lobes.append((extra, float(rng.uniform(0.2, 0.6)), float(rng.uniform(1.3, 1.7))))
+            if rng.random() < 0.3:
+                lobes.append(("oren_nayar" if base == "diffuse" else "diffuse", 0.2, float(rng.uniform(0.0, 0.5))))
+        specs.append((pats, tint, lobes))
+    return specs
+
+
+def c5_material_group(ss, k, spec, out_offset=0, out_stride=4 * C5_OUT_FLOATS, in_offset=0,
+                      in_stride=4 * C5_IN_FLOATS):
+    """Build material k: pattern layer(s) -> optional tint -> surface; the
+    surface's Ci is sampled per point (bsdf_sample_output)."""
+    pats, tint, lobes = spec
+    tag = "c5m%02d" % k
+    g = ss.ShaderGroupBegin(tag)
+    for i, (kind, freq) in enumerate(pats):
+        nm = "%s_p%d" % (tag, i)
+        ss.LoadMemoryCompiledShader(nm, _c5_pattern(nm, kind, freq))
+        ss.Shader(g, "surface", nm, "P%d" % i)
+    if tint is not None:
+        nm = tag + "_tint"
+        ss.LoadMemoryCompiledShader(nm, _c5_tint(nm, tint[0], tint[1]))
+        ss.Shader(g, "surface", nm, "T")
+        ss.ConnectShaders(g, "P0", "a", "T", "x")
+    nm = tag + "_surf"
+    ss.LoadMemoryCompiledShader(nm, _c5_surface(nm, lobes))
+    ss.Shader(g, "surface", nm, "S")
+    ss.ConnectShaders(g, "P0", "a", "S", "a")
+    ss.ConnectShaders(g, "P%d" % (len(pats) - 1), "a", "S", "r")
+    if tint is not None:
+        ss.ConnectShaders(g, "T", "tint", "S", "tint")
+    ss.ShaderGroupEnd(g)
+    ss.bsdf_sample_output(g, "S.Ci", out_offset, out_stride, in_offset, in_stride)
+    return g
+
+
+def c5_hits(n, seed=0xC5A):
+    """Seeded hit records for sampling tests: P in [-5, 5]^3, unit N facing
+    the incoming direction, dPdu orthogonal to N, random inputs of the
+    sample step (rx, ry, rz in [0, 1), path weight in [0.2, 1], absorb 0/1)."""
+    rng = np.random.default_rng(seed)
+    P = rng.uniform(-5, 5, (3, n)).astype(np.float32)
+    N = rng.normal(size=(3, n))
+    N /= np.linalg.norm(N, axis=0)
+    I = rng.normal(size=(3, n))
+    I /= np.linalg.norm(I, axis=0)
+    flip = np.sum(I * N, axis=0) > 0
+    I[:, flip] *= -1.0
+    T = np.cross(N.T, rng.normal(size=(n, 3))).T
+    T /= np.linalg.norm(T, axis=0)
+    rnd = np.zeros((n, C5_IN_FLOATS), np.float32)
+    rnd[:, 0:3] = rng.random((n, 3), dtype=np.float32) * np.float32(0.99999994)
+    rnd[:, 3:6] = rng.uniform(0.2, 1.0, (n, 3))
+    rnd[:, 6] = (rng.random(n) < 0.3).astype(np.float32)
+    f32 = lambda a: np.ascontiguousarray(a, dtype=np.float32)
+    return (P, f32(N), f32(I), f32(T), rnd)

@@ -27,6 +27,7 @@
 
 #include "../include/oslg.h"
 #include "../openshadinglanguage_gb300/csrc/oslg_program.h"
+#include "oracle_bsdf.h"
 #include "oracle_gabor.h"
 #include "oracle_shading.h"
 #include "oracle_simplex.h"
@@ -820,6 +821,28 @@ template <class F> void closure_walk(Point& P, const CPools& C, uint32_t root, F
     }
 }
 
+// process_closure's lobe construction for the lobes the executor shades
+// (src/testrender/shading.cpp:1481-1530): emission accumulates Le,
+// diffuse / oren_nayar / GGX microfacet (params: dist, N, U, xalpha,
+// yalpha, eta, refract) become lobes in walk order; ggx_hash names "ggx".
+void build_lobes(Point& P, const CPools& C, uint32_t root, const V3& wo, uint32_t ggx_hash, CompositeLobes* L) {
+    auto f = [&](uint32_t s) { return bitsf(P.heap[s]); };
+    closure_walk(P, C, root, [&](int id, const V3& cw, uint32_t p) {
+        if (id == 1) {  // EMISSION_ID
+            L->Le = L->Le + cw;
+        } else if (id == 3) {  // DIFFUSE_ID
+            L->add_diffuse(cw, V3(f(p + 0), f(p + 1), f(p + 2)));
+        } else if (id == 4) {  // OREN_NAYAR_ID
+            L->add_on(cw, OrenNayarQON(V3(f(p + 0), f(p + 1), f(p + 2)), f(p + 3), wo));
+        } else if (id == 8 && P.heap[p] == ggx_hash) {  // MICROFACET_ID, "ggx"
+            int refract = (int32_t)P.heap[p + 10];
+            if (refract < 0 || refract > 2) return;
+            L->add_ggx(cw, MicrofacetGGX(V3(f(p + 1), f(p + 2), f(p + 3)), V3(f(p + 4), f(p + 5), f(p + 6)), f(p + 7),
+                                         f(p + 8), f(p + 9), refract));
+        }
+    });
+}
+
 struct Runner {
     const Prog& prog;
     const oslg_shaderglobals& G;
@@ -1178,49 +1201,32 @@ struct Runner {
                 uint32_t root = word(P, a[0], 0);
                 V3 wi(getf(P, a[3], 0, 0), getf(P, a[3], 1, 0), getf(P, a[3], 2, 0));
                 V3 wo(-getf(P, a[4], 0, 0), -getf(P, a[4], 1, 0), -getf(P, a[4], 2, 0));
-                struct Lobe { int kind; V3 w; uint32_t params; };
-                Lobe lobes[oslg::kBsdfMaxLobes];
-                int nl = 0;
-                closure_walk(P, C, root, [&](int id, const V3& cw, uint32_t params) {
-                    int kind = -1;
-                    if (id == 3) kind = 0;  // DIFFUSE_ID
-                    else if (id == 8 && P.heap[params] == a[5] && (int32_t)P.heap[params + 10] == 0) kind = 1;
-                    if (kind < 0 || nl >= oslg::kBsdfMaxLobes) return;
-                    lobes[nl++] = { kind, cw, params };
-                });
-                auto f = [&](uint32_t s) { return bitsf(P.heap[s]); };
-                float pdfs[oslg::kBsdfMaxLobes];
-                float total = 0;
-                V3 path_weight(1.0f);
-                for (int i = 0; i < nl; ++i) {
-                    V3 alb(1.0f);
-                    if (lobes[i].kind == 1) {
-                        uint32_t p = lobes[i].params;
-                        MicrofacetGGXRefl m(V3(f(p + 1), f(p + 2), f(p + 3)), V3(f(p + 4), f(p + 5), f(p + 6)), f(p + 7),
-                                            f(p + 8), f(p + 9));
-                        alb = m.albedo(wo);
-                    }
-                    pdfs[i] = dotv(lobes[i].w, path_weight * alb) / (path_weight.x + path_weight.y + path_weight.z);
-                    total += pdfs[i];
-                }
-                if (total > 0 || total > 1)
-                    for (int i = 0; i < nl; ++i) pdfs[i] /= total;
-                Sample sres;
-                for (int i = 0; i < nl; ++i) {
-                    uint32_t p = lobes[i].params;
-                    Sample b;
-                    if (lobes[i].kind == 0) b = diffuse_eval(V3(f(p + 0), f(p + 1), f(p + 2)), wi);
-                    else {
-                        MicrofacetGGXRefl m(V3(f(p + 1), f(p + 2), f(p + 3)), V3(f(p + 4), f(p + 5), f(p + 6)), f(p + 7),
-                                            f(p + 8), f(p + 9));
-                        b = m.eval(wo, wi);
-                    }
-                    b.weight = b.weight * lobes[i].w;
-                    mis_update_eval(&sres.weight, &sres.pdf, b.weight, b.pdf, pdfs[i]);
-                    sres.roughness += b.roughness * pdfs[i];
-                }
+                CompositeLobes L;
+                build_lobes(P, C, root, wo, a[5], &L);
+                L.prepare(wo, V3(1.0f), false);
+                Sample sres = L.eval(wo, wi);
                 float* o = reinterpret_cast<float*>(outputs + (int64_t)a[1] + P.pt * (int64_t)(int32_t)a[2]);
                 o[0] = sres.weight.x; o[1] = sres.weight.y; o[2] = sres.weight.z; o[3] = sres.pdf;
+                break;
+            }
+            case oslg::OP_BSDF_SAMPLE: {
+                // process_closure + prepare(wo, path_weight, absorb) + sample
+                // (simpleraytracer.cpp:1038-1079, shading.h:322-398). Userdata
+                // record: rx ry rz, path weight rgb, absorb; output record:
+                // wi xyz, weight rgb, pdf, Le rgb, roughness.
+                uint32_t root = word(P, a[0], 0);
+                V3 wo(-getf(P, a[3], 0, 0), -getf(P, a[3], 1, 0), -getf(P, a[3], 2, 0));
+                const float* in = reinterpret_cast<const float*>(userdata + (int64_t)a[5] + P.pt * (int64_t)(int32_t)a[6]);
+                CompositeLobes L;
+                build_lobes(P, C, root, wo, a[4], &L);
+                L.prepare(wo, V3(in[3], in[4], in[5]), in[6] != 0.0f);
+                Sample sres = L.sample(wo, in[0], in[1], in[2]);
+                float* o = reinterpret_cast<float*>(outputs + (int64_t)a[1] + P.pt * (int64_t)(int32_t)a[2]);
+                o[0] = sres.wi.x; o[1] = sres.wi.y; o[2] = sres.wi.z;
+                o[3] = sres.weight.x; o[4] = sres.weight.y; o[5] = sres.weight.z;
+                o[6] = sres.pdf;
+                o[7] = L.Le.x; o[8] = L.Le.y; o[9] = L.Le.z;
+                o[10] = sres.roughness;
                 break;
             }
             case oslg::OP_SPLINE: {

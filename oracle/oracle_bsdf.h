@@ -1,0 +1,449 @@
+// ORACLE — test infrastructure only. Not part of the shipped library.
+//
+// CPU restatement of testrender's BSDF sampling for the lobes of the
+// wavefront workload, on top of oracle_shading.h:
+//   * Diffuse<0>::sample (src/testrender/shading.cpp:301-320) with
+//     Sampling::sample_cosine_hemisphere / to_unit_disk (sampling.h:70-100);
+//   * Microfacet<GGXDist, Refract> for Refract 0, 1, 2 — eval and sample
+//     (shading.cpp:571-760, GGXDist::sampleSlope :480-508), fresnel_refraction
+//     (optics.h:34-66);
+//   * the oren_nayar closure as testrender builds it: BSDL's
+//     OrenNayarDiffuseLobe without energy compensation, albedo 1
+//     (shading.cpp:1496-1502; libbsdl MTX/bsdf_oren_nayar_diffuse_impl.h:
+//     41-113) in BSDL's Frame (tools.h:459-508) around the visible normal
+//     (bsdf_impl.h:51-84), cosine hemisphere via the square-to-disc map with
+//     Clarberg's quadrant polynomials (tools.h:196-275);
+//   * CompositeBSDF::prepare / eval / sample (shading.h:319-402);
+//   * emission adds the component weight to Le (shading.cpp:1485-1486).
+// The reference's OIIO::fast_sincos in to_unit_disk is replaced by the
+// executor's own sincos (oracle_fmath.h); OIIO's source is not in the tree.
+#pragma once
+#include <algorithm>
+#include <cmath>
+#include <new>
+
+#include "oracle_fmath.h"
+#include "oracle_shading.h"
+
+namespace oracle {
+
+static const int kMaxLobes = 8;  // CompositeBSDF::MaxEntries
+
+inline V3 frame_get(const TangentFrame& f, float x, float y, float z) { return f.u * x + f.v * y + f.w * z; }
+
+// sampling.h:70-100
+inline void to_unit_disk(float& x, float& y) {
+    const float PI_OVER_4 = float(M_PI_4), PI_OVER_2 = float(M_PI_2);
+    float phi, r;
+    float a = 2 * x - 1, b = 2 * y - 1;
+    if (a * a > b * b) {
+        r = a;
+        phi = PI_OVER_4 * (b / a);
+    } else if (b != 0) {
+        r = b;
+        phi = PI_OVER_2 - PI_OVER_4 * (a / b);
+    } else {
+        r = 0;
+        phi = 0;
+    }
+    own_sincos(phi, &x, &y);
+    x *= r;
+    y *= r;
+}
+inline void sample_cosine_hemisphere(const V3& N, float rx, float ry, V3* out, float* pdf) {
+    to_unit_disk(rx, ry);
+    float cos_theta = std::sqrt(std::max(1 - rx * rx - ry * ry, 0.0f));
+    *out = frame_get(TangentFrame::from_normal(N), rx, ry, cos_theta);
+    *pdf = cos_theta * float(M_1_PI);
+}
+
+inline Sample diffuse_sample(const V3& N, float rx, float ry) {
+    Sample s;
+    V3 wi;
+    float pdf;
+    sample_cosine_hemisphere(N, rx, ry, &wi, &pdf);
+    s.wi = wi;
+    s.weight = V3(1.0f);
+    s.pdf = pdf;
+    s.roughness = 1.0f;
+    return s;
+}
+
+// optics.h:34-66
+inline float fresnel_refraction(const V3& I, const V3& N, float eta, V3* T) {
+    float cosi = -dotv(I, N);
+    V3 Nn;
+    float neta;
+    if (cosi > 0) {
+        neta = 1 / eta;
+        Nn = N;
+    } else {
+        cosi = -cosi;
+        neta = eta;
+        Nn = -N;
+    }
+    float arg = 1.0f - (neta * neta * (1.0f - cosi * cosi));
+    if (arg >= 0) {
+        float dnp = std::sqrt(arg);
+        float nK = (neta * cosi) - dnp;
+        *T = I * neta + Nn * nK;
+        return 1 - fresnel_dielectric(cosi, eta);
+    }
+    *T = V3(0.0f);
+    return 0;
+}
+
+// Microfacet<GGXDist, Refract>
+struct MicrofacetGGX : MicrofacetGGXRefl {
+    int refract;
+    MicrofacetGGX(const V3& n, const V3& u, float ax, float ay, float e, int r)
+        : MicrofacetGGXRefl(n, u, ax, ay, e), refract(r) {}
+    V3 albedo(const V3& wo) const {
+        if (refract == 2) return V3(1.0f);
+        float fr = fresnel_dielectric(dotv(N, wo), eta);
+        return V3(refract ? 1 - fr : fr);
+    }
+    Sample eval(const V3& wo, const V3& wi) const {
+        const V3 wo_l = tf.tolocal(wo);
+        const V3 wi_l = tf.tolocal(wi);
+        Sample s;
+        s.wi = wi;
+        if (refract == 0 || refract == 2) {
+            if (wo_l.z > 0 && wi_l.z > 0) {
+                const V3 m = imath_normalize(wi_l + wo_l);
+                const float D = evalD(m);
+                const float Lo = evalLambda(wo_l), Li = evalLambda(wi_l);
+                const float G2 = 1 / (Lo + Li + 1), G1 = 1 / (Lo + 1);
+                const float Fr = fresnel_dielectric(dotv(m, wo_l), eta);
+                float pdf = (G1 * D * 0.25f) / wo_l.z;
+                float out = G2 / G1;
+                s.roughness = std::max(xalpha, yalpha);
+                if (refract == 2) {
+                    s.pdf = pdf * Fr;
+                    s.weight = V3(out);
+                } else {
+                    s.pdf = pdf;
+                    s.weight = V3(out * Fr);
+                }
+                return s;
+            }
+        }
+        if (refract == 1 || refract == 2) {
+            if (wi_l.z < 0 && wo_l.z > 0.0f) {
+                V3 ht = -(wi_l * eta + wo_l);
+                if (eta < 1.0f) ht = -ht;
+                V3 Ht = imath_normalize(ht);
+                const float cosHO = dotv(Ht, wo_l);
+                const float Ft = 1.0f - fresnel_dielectric(cosHO, eta);
+                if (Ft > 0) {
+                    const float cosHI = dotv(Ht, wi_l);
+                    const float cosThetaM = Ht.z;
+                    if (cosThetaM <= 0.0f) return Sample();
+                    const float Dt = evalD(Ht);
+                    const float Lo = evalLambda(wo_l), Li = evalLambda(wi_l);
+                    const float G2 = 1 / (Lo + Li + 1), G1 = 1 / (Lo + 1);
+                    float invHt2 = 1 / dotv(ht, ht);
+                    float pdf = (std::fabs(cosHI * cosHO) * (eta * eta) * (G1 * Dt) * invHt2) / wo_l.z;
+                    float out = G2 / G1;
+                    s.roughness = std::max(xalpha, yalpha);
+                    if (refract == 2) {
+                        s.pdf = pdf * Ft;
+                        s.weight = V3(out);
+                    } else {
+                        s.pdf = pdf;
+                        s.weight = V3(out * Ft);
+                    }
+                    return s;
+                }
+            }
+        }
+        return Sample();
+    }
+    // GGXDist::sampleSlope (shading.cpp:480-508)
+    static void sample_slope(float cos_theta, float randu, float randv, float* sx, float* sy) {
+        float c = cos_theta < 1e-6f ? 1e-6f : cos_theta;
+        float Q = (1 + c) * randu - c;
+        float num = c * std::sqrt((1 - c) * (1 + c)) - Q * std::sqrt((1 - Q) * (1 + Q));
+        float den = (Q - c) * (Q + c);
+        float eps = 1.0f / 4294967296.0f;
+        den = std::fabs(den) < eps ? std::copysign(eps, den) : den;
+        *sx = num / den;
+        float Ru = 1 - 2 * randv;
+        float u2 = std::fabs(Ru);
+        float z = (u2 * (u2 * (u2 * 0.27385f - 0.73369f) + 0.46341f))
+                / (u2 * (u2 * (u2 * 0.093073f + 0.309420f) - 1.0f) + 0.597999f);
+        *sy = std::copysign(1.0f, Ru) * z * std::sqrt(1.0f + *sx * *sx);
+    }
+    // Microfacet::sampleMicronormal (shading.cpp:754-787)
+    V3 sample_micronormal(const V3& wo, float randu, float randv) const {
+        V3 swo = wo;
+        swo.x *= xalpha;
+        swo.y *= yalpha;
+        swo = imath_normalize(swo);
+        float cos_theta = std::max(swo.z, 0.0f);
+        float cos_phi = 1, sin_phi = 0;
+        if (cos_theta < 0.99999f) {
+            float invnorm = 1 / std::sqrt(SQR(swo.x) + SQR(swo.y));
+            cos_phi = swo.x * invnorm;
+            sin_phi = swo.y * invnorm;
+        }
+        float slx, sly;
+        sample_slope(cos_theta, randu, randv, &slx, &sly);
+        float sx = cos_phi * slx - sin_phi * sly;
+        float sy = sin_phi * slx + cos_phi * sly;
+        sx *= xalpha;
+        sy *= yalpha;
+        float mlen = std::sqrt(sx * sx + sy * sy + 1);
+        return V3(std::fabs(sx) < mlen ? -sx / mlen : 1.0f, std::fabs(sy) < mlen ? -sy / mlen : 1.0f, 1.0f / mlen);
+    }
+    // Microfacet::sample (shading.cpp:628-700)
+    Sample sample(const V3& wo, float rx, float ry, float rz) const {
+        const V3 wo_l = tf.tolocal(wo);
+        const float cosNO = wo_l.z;
+        if (!(cosNO > 0)) return Sample();
+        const V3 m = sample_micronormal(wo_l, rx, ry);
+        const float cosMO = dotv(m, wo_l);
+        const float F = fresnel_dielectric(cosMO, eta);
+        Sample s;
+        if (refract == 0 || (refract == 2 && rz < F)) {
+            const V3 wi_l = m * (2.0f * cosMO) - wo_l;
+            const float D = evalD(m);
+            const float Lo = evalLambda(wo_l), Li = evalLambda(wi_l);
+            const float G2 = 1 / (Lo + Li + 1), G1 = 1 / (Lo + 1);
+            s.wi = frame_get(tf, wi_l.x, wi_l.y, wi_l.z);
+            float pdf = (G1 * D * 0.25f) / cosNO;
+            float out = G2 / G1;
+            s.roughness = std::max(xalpha, yalpha);
+            if (refract == 2) {
+                s.pdf = pdf * F;
+                s.weight = V3(out);
+            } else {
+                s.pdf = pdf;
+                s.weight = V3(F * out);
+            }
+            return s;
+        }
+        const V3 M = frame_get(tf, m.x, m.y, m.z);
+        V3 wi;
+        float Ft = fresnel_refraction(-wo, M, eta, &wi);
+        const V3 wi_l = tf.tolocal(wi);
+        const float cosHO = dotv(m, wo_l), cosHI = dotv(m, wi_l);
+        const float D = evalD(m);
+        const float Lo = evalLambda(wo_l), Li = evalLambda(wi_l);
+        const float G2 = 1 / (Lo + Li + 1), G1 = 1 / (Lo + 1);
+        const V3 ht = -(wi_l * eta + wo_l);
+        const float invHt2 = 1.0f / dotv(ht, ht);
+        float pdf = (std::fabs(cosHI * cosHO) * (eta * eta) * (G1 * D) * invHt2) / std::fabs(wo_l.z);
+        float out = G2 / G1;
+        s.wi = wi;
+        s.roughness = std::max(xalpha, yalpha);
+        if (refract == 2) {
+            s.pdf = pdf * Ft;
+            s.weight = V3(out);
+        } else {
+            s.pdf = pdf;
+            s.weight = V3(Ft * out);
+        }
+        return s;
+    }
+};
+
+// BSDL pieces (libbsdl/include/BSDL/tools.h)
+inline float bsdl_cos_quadrant(float x) {
+    float x2 = x * x;
+    float cp = 0.01578646f + -0.00029826362f * x2;
+    cp = -0.30837047f + cp * x2;
+    cp = 0.99998736f + cp * x2;
+    return cp;
+}
+inline float bsdl_sin_quadrant(float x) {
+    float x2 = x * x;
+    float sp = 0.0024843954015523195266723632812500f + -0.0000341485538228880614042282104492f * x2;
+    sp = -0.0807407423853874206542968750000000f + sp * x2;
+    sp = 0.7853975892066955566406250000000000f + sp * x2;
+    return sp * x;
+}
+inline V3 bsdl_sample_cos_hemisphere(float randu, float randv) {
+    const float a = 2 * randu - 1, qa = std::fabs(a);
+    const float b = 2 * randv - 1, qb = std::fabs(b);
+    const float rad = qa > qb ? qa : qb;
+    const float phi = qa > qb ? qb / qa : ((qa == qb) ? 1.0f : 2 - qa / qb);
+    const float x = std::copysign(rad * bsdl_cos_quadrant(phi), a);
+    const float y = std::copysign(rad * bsdl_sin_quadrant(phi), b);
+    return V3(x, y, std::sqrt(1 - rad * rad));
+}
+struct BsdlFrame {
+    V3 X, Y, Z;
+    explicit BsdlFrame(const V3& z) : Z(z) {
+        const float s = std::copysign(1.0f, z.z);
+        const float a = -1.0f / (s + z.z);
+        const float b = z.x * z.y * a;
+        X = V3(1.0f + s * z.x * z.x * a, s * b, -s * z.x);
+        Y = V3(b, s + z.y * z.y * a, -z.y);
+    }
+    V3 local(const V3& a) const { return V3(dotv(a, X), dotv(a, Y), dotv(a, Z)); }
+    V3 world(const V3& a) const {
+        return V3(X.x * a.x + Y.x * a.y + Z.x * a.z, X.y * a.x + Y.y * a.y + Z.y * a.z, X.z * a.x + Y.z * a.y + Z.z * a.z);
+    }
+};
+inline float bsdl_max_abs(const V3& v) { return std::max(std::fabs(v.x), std::max(std::fabs(v.y), std::fabs(v.z))); }
+// BsdfGlobals::visible_normal (bsdf_impl.h:51-78)
+inline V3 bsdl_visible_normal(const V3& wo, const V3& Ngf, const V3& N) {
+    if (dotv(wo, N) > 0.0f) return N;
+    V3 V = crossv(wo, N);
+    if (bsdl_max_abs(V) < 1e-4f) {
+        V = crossv(wo, Ngf);
+        if (bsdl_max_abs(V) < 1e-4f) {
+            const float s = std::copysign(1.0f, wo.z);
+            const float a = -1.0f / (s + wo.z);
+            V = V3(wo.x * wo.y * a, s + wo.y * wo.y * a, -wo.y);
+        } else {
+            V = imath_normalize(V);
+        }
+    } else {
+        V = imath_normalize(V);
+    }
+    return imath_normalize(crossv(V, wo) + wo * 1e-4f);
+}
+inline float bsdl_clamp(float x, float a, float b) { return std::min(std::max(x, a), b); }
+
+// oren_nayar as testrender builds it (energy compensation off, albedo 1)
+struct OrenNayarQON {
+    BsdlFrame frame;
+    float rough;
+    OrenNayarQON(const V3& N, float sigma, const V3& wo)
+        : frame(bsdl_visible_normal(wo, N, N)), rough(bsdl_clamp(sigma, 0.0f, 1.0f)) {}
+    Sample eval_local(const V3& wo, const V3& wi) const {
+        Sample s;
+        const float cosNI = bsdl_clamp(wi.z, 0.0f, 1.0f);
+        const float cosNO = bsdl_clamp(wo.z, 0.0f, 1.0f);
+        if (cosNI <= 0.0f || cosNO <= 0.0f) return s;
+        const float cosIO = bsdl_clamp(dotv(wo, wi), -1.0f, 1.0f);
+        const float sv = cosIO - cosNI * cosNO;
+        const float pdf = cosNI * (1 / float(M_PI));
+        const float s2 = rough * rough;
+        const float A = 1.0f - 0.50f * s2 / (s2 + 0.33f);
+        const float B = 0.45f * s2 / (s2 + 0.09f);
+        const float stinv = sv > 0.0f ? sv / std::max(cosNI, cosNO) : 0.0f;
+        const float f_ss = A + B * stinv;
+        s.wi = wi;
+        s.weight = V3(1.0f) * f_ss;
+        s.pdf = pdf;
+        s.roughness = 1.0f;
+        return s;
+    }
+    Sample eval(const V3& wo, const V3& wi) const {
+        Sample s = eval_local(frame.local(wo), frame.local(wi));
+        s.wi = wi;
+        return s;
+    }
+    Sample sample(const V3& wo, float rx, float ry) const {
+        const V3 wo_l = frame.local(wo);
+        if (wo_l.z <= 0.0f) return Sample();
+        Sample s = eval_local(wo_l, bsdl_sample_cos_hemisphere(rx, ry));
+        s.wi = frame.world(s.wi);
+        return s;
+    }
+};
+
+// The lobes testrender builds from a closure tree, with their weights.
+struct CompositeLobes {
+    enum Kind { DIFFUSE, GGX, OREN_NAYAR };
+    int kind[kMaxLobes];
+    V3 w[kMaxLobes];
+    float pdfs[kMaxLobes];
+    unsigned char storage[kMaxLobes][sizeof(MicrofacetGGX) > sizeof(OrenNayarQON) ? sizeof(MicrofacetGGX)
+                                                                                   : sizeof(OrenNayarQON)];
+    V3 N[kMaxLobes];
+    int n = 0;
+    V3 Le = V3(0.0f);
+
+    OrenNayarQON& on(int i) { return *reinterpret_cast<OrenNayarQON*>(storage[i]); }
+    const OrenNayarQON& on(int i) const { return *reinterpret_cast<const OrenNayarQON*>(storage[i]); }
+    const MicrofacetGGX& mf(int i) const { return *reinterpret_cast<const MicrofacetGGX*>(storage[i]); }
+
+    void add_diffuse(const V3& cw, const V3& normal) {
+        if (n_full()) return;
+        kind[n] = DIFFUSE; w[n] = cw; N[n] = normal;
+        ++n;
+    }
+    void add_ggx(const V3& cw, const MicrofacetGGX& m) {
+        if (n_full()) return;
+        kind[n] = GGX; w[n] = cw;
+        new (storage[n]) MicrofacetGGX(m);
+        ++n;
+    }
+    void add_on(const V3& cw, const OrenNayarQON& o) {
+        if (n_full()) return;
+        kind[n] = OREN_NAYAR; w[n] = cw;
+        new (storage[n]) OrenNayarQON(o);
+        ++n;
+    }
+    bool n_full() const { return n >= kMaxLobes; }
+
+    V3 albedo(int i, const V3& wo) const {
+        if (kind[i] == GGX) return mf(i).albedo(wo);
+        return V3(1.0f);
+    }
+    Sample eval_lobe(int i, const V3& wo, const V3& wi) const {
+        if (kind[i] == DIFFUSE) {
+            Sample s = diffuse_eval(N[i], wi);
+            s.wi = wi;
+            return s;
+        }
+        if (kind[i] == GGX) return mf(i).eval(wo, wi);
+        return on(i).eval(wo, wi);
+    }
+    Sample sample_lobe(int i, const V3& wo, float rx, float ry, float rz) const {
+        if (kind[i] == DIFFUSE) return diffuse_sample(N[i], rx, ry);
+        if (kind[i] == GGX) return mf(i).sample(wo, rx, ry, rz);
+        return on(i).sample(wo, rx, ry);
+    }
+    // CompositeBSDF::prepare (shading.h:322-350)
+    void prepare(const V3& wo, const V3& path_weight, bool absorb) {
+        float total = 0;
+        for (int i = 0; i < n; ++i) {
+            pdfs[i] = dotv(w[i], path_weight * albedo(i, wo)) / (path_weight.x + path_weight.y + path_weight.z);
+            total += pdfs[i];
+        }
+        if ((!absorb && total > 0) || total > 1)
+            for (int i = 0; i < n; ++i) pdfs[i] /= total;
+    }
+    // CompositeBSDF::eval (shading.h:360-370)
+    Sample eval(const V3& wo, const V3& wi) const {
+        Sample s;
+        for (int i = 0; i < n; ++i) {
+            Sample b = eval_lobe(i, wo, wi);
+            b.weight = b.weight * w[i];
+            mis_update_eval(&s.weight, &s.pdf, b.weight, b.pdf, pdfs[i]);
+            s.roughness += b.roughness * pdfs[i];
+        }
+        return s;
+    }
+    // CompositeBSDF::sample (shading.h:372-398)
+    Sample sample(const V3& wo, float rx, float ry, float rz) const {
+        float accum = 0;
+        for (int i = 0; i < n; ++i) {
+            if (rx < (pdfs[i] + accum)) {
+                rx = (rx - accum) / pdfs[i];
+                rx = std::min(rx, 0.99999994f);
+                Sample s = sample_lobe(i, wo, rx, ry, rz);
+                s.weight = s.weight * (w[i] * (1 / pdfs[i]));
+                s.pdf *= pdfs[i];
+                if (s.pdf == 0.0f) return Sample();
+                for (int j = 0; j < n; ++j) {
+                    if (i != j) {
+                        Sample b = eval_lobe(j, wo, s.wi);
+                        b.weight = b.weight * w[j];
+                        mis_update_eval(&s.weight, &s.pdf, b.weight, b.pdf, pdfs[j]);
+                    }
+                }
+                return s;
+            }
+            accum += pdfs[i];
+        }
+        return Sample();
+    }
+};
+
+}  // namespace oracle

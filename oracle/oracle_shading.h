@@ -134,6 +134,7 @@ inline float fresnel_dielectric(float cosi, float eta) {
 }
 
 struct Sample {
+    V3 wi = V3(0.0f);
     V3 weight = V3(0.0f);
     float pdf = 0.0f;
     float roughness = 0.0f;

@@ -219,3 +219,20 @@ def test_single_op_programs_pick_the_right_tier():
     assert oracle_run(g.program_bytes(), W * H, grid_globals(u_, v_, W, H), ref) == 0
     assert_same(got, ref)
     assert ss.device_status() == 0
+
+
+def test_c5_material_sampling_matches_oracle():
+    from openshadinglanguage_gb300 import workloads as W
+    n = 8192
+    P, N, I, T, rnd = W.c5_hits(n)
+    ss = og.ShadingSystem()
+    dP, dN, dI, dT, drnd = (dev(x) for x in (P, N, I, T, rnd))
+    Gd = og.make_globals(P=dP, N=dN, Ng=dN, I=dI, dPdu=dT)
+    Gh = og.make_globals(P=P, N=N, Ng=N, I=I, dPdu=T)
+    for k, spec in enumerate(W.c5_material_specs()):
+        g = W.c5_material_group(ss, k, spec)
+        got = gpu_run(ss, g, n, Gd, W.C5_OUT_FLOATS, userdata=rnd)
+        ref = np.zeros((n, W.C5_OUT_FLOATS), np.float32)
+        assert oracle_run(g.program_bytes(), n, Gh, ref, userdata=rnd) == 0
+        assert_same(got, ref)
+    assert ss.device_status() == 0
