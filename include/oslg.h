@@ -311,6 +311,70 @@ int oslg_server_wait(oslg_server* server, uint64_t ticket, int timeout_ms, oslg_
 int oslg_server_poll(oslg_server* server, uint64_t ticket, int* done, oslg_request_stats* stats);
 int oslg_server_get_stats(oslg_server* server, oslg_server_stats* out);
 
+/* ---- wavefront path tracing -------------------------------------------------
+ * testrender's per-sample path loop (src/testrender/simpleraytracer.cpp:
+ * 960-1184: trace, globals_from_hit, execute, process_closure, add
+ * emission, prepare + sample, continue) run for every path of a frame at
+ * once, one bounce per wavefront, with the hits of each bounce sorted by
+ * material and shaded by the persistent batch kernel. The scene is analytic
+ * spheres and rectangles (testrender tessellates its spheres and quads,
+ * src/testrender/scene.cpp; here they are intersected exactly). Material k
+ * is a group whose closure output is sampled with
+ * oslg_group_bsdf_sample(..., offset 0, stride 44, in_offset 0, in_stride
+ * 28). Differences from testrender, by design: no light sampling (emission
+ * is gathered by BSDF sampling, MIS weight 1), no background importance
+ * sampling or media, and Russian roulette with a fixed survival
+ * probability after every hit. */
+typedef struct oslg_wavefront oslg_wavefront;
+
+#define OSLG_PRIM_SPHERE 0
+#define OSLG_PRIM_QUAD 1 /* rectangle p + s*ex + t*ey, s,t in [0,1], ex orthogonal to ey */
+
+typedef struct oslg_primitive {
+    int32_t kind;      /* OSLG_PRIM_SPHERE or OSLG_PRIM_QUAD */
+    int32_t material;  /* index into the materials array */
+    float p[3];        /* sphere centre or rectangle corner */
+    float ex[3];       /* rectangle edges */
+    float ey[3];
+    float radius;      /* sphere radius */
+} oslg_primitive;
+
+typedef struct oslg_wavefront_options {
+    int32_t width, height, spp;  /* paths = width * height * spp */
+    int32_t max_hits;            /* shading points per path at most (<= 16) */
+    float rr_survival;           /* Russian roulette survival probability per hit */
+    float eye[3], look[3], up[3];
+    float fov_deg;               /* vertical field of view */
+    float background[3];         /* radiance of rays that leave the scene */
+    uint32_t seed;
+    int32_t block;               /* shading launch: threads per CTA (0: 256) */
+    int32_t points_per_thread;   /* 1, 2 or 4 (0: 1) */
+    int32_t heap_smem;           /* 1 shared memory, 2 HBM, 0: shared memory when it fits */
+    int32_t use_graph;           /* replay the frame as a CUDA graph (default 1; pass -1 for 0) */
+} oslg_wavefront_options;
+
+typedef struct oslg_wavefront_stats {
+    int64_t paths;
+    int64_t hits[16];      /* shading points per bounce of the last frame */
+    int64_t total_hits;
+    int32_t bounces;       /* bounces with at least one hit */
+    float ms_total;        /* last frame, CUDA events on the render stream */
+    float ms_stage[5];     /* trace, plan, scatter, shade, update (profiled frames) */
+} oslg_wavefront_stats;
+
+int oslg_wavefront_create(oslg_system* sys, const oslg_wavefront_options* opts, const oslg_primitive* prims,
+                          int nprims, oslg_group* const* materials, int nmaterials, oslg_wavefront** out);
+int oslg_wavefront_destroy(oslg_wavefront* wf);
+/* One frame. d_path_radiance (3 planes of paths floats; path index
+ * (y * width + x) * spp + s) and d_image (width * height * 3, the mean of
+ * the pixel's samples) are device buffers; either may be NULL. */
+int oslg_wavefront_render(oslg_wavefront* wf, float* d_path_radiance, float* d_image, void* stream);
+/* One frame launched stage by stage with CUDA events between the stages
+ * (no graph); ms_stage of the stats holds the sums over bounces. */
+int oslg_wavefront_render_profiled(oslg_wavefront* wf, float* d_path_radiance, float* d_image, void* stream);
+/* Synchronises with the last frame. */
+int oslg_wavefront_get_stats(oslg_wavefront* wf, oslg_wavefront_stats* out);
+
 #ifdef __cplusplus
 }
 #endif

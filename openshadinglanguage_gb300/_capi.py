@@ -69,6 +69,24 @@ class ServerStatsC(ctypes.Structure):
                 ("scratch_bytes", ctypes.c_size_t), ("in_flight_waves", ctypes.c_int), ("pending", ctypes.c_int)]
 
 
+class PrimitiveC(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("material", ctypes.c_int32), ("p", ctypes.c_float * 3),
+                ("ex", ctypes.c_float * 3), ("ey", ctypes.c_float * 3), ("radius", ctypes.c_float)]
+
+
+class WavefrontOptionsC(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_int32), ("height", ctypes.c_int32), ("spp", ctypes.c_int32),
+                ("max_hits", ctypes.c_int32), ("rr_survival", ctypes.c_float), ("eye", ctypes.c_float * 3),
+                ("look", ctypes.c_float * 3), ("up", ctypes.c_float * 3), ("fov_deg", ctypes.c_float),
+                ("background", ctypes.c_float * 3), ("seed", ctypes.c_uint32), ("block", ctypes.c_int32),
+                ("points_per_thread", ctypes.c_int32), ("heap_smem", ctypes.c_int32), ("use_graph", ctypes.c_int32)]
+
+
+class WavefrontStatsC(ctypes.Structure):
+    _fields_ = [("paths", ctypes.c_int64), ("hits", ctypes.c_int64 * 16), ("total_hits", ctypes.c_int64),
+                ("bounces", ctypes.c_int32), ("ms_total", ctypes.c_float), ("ms_stage", ctypes.c_float * 5)]
+
+
 class ShaderGlobalsC(ctypes.Structure):
     _fields_ = [(n, FieldC) for n in GLOBAL_FIELDS]
 
@@ -133,6 +151,15 @@ _EXPORTS = {
     "oslg_server_poll": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.POINTER(ctypes.c_int),
                                         ctypes.POINTER(RequestStatsC)]),
     "oslg_server_get_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ServerStatsC)]),
+    "oslg_wavefront_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(WavefrontOptionsC),
+                                             ctypes.POINTER(PrimitiveC), ctypes.c_int,
+                                             ctypes.POINTER(ctypes.c_void_p), ctypes.c_int,
+                                             ctypes.POINTER(ctypes.c_void_p)]),
+    "oslg_wavefront_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "oslg_wavefront_render": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "oslg_wavefront_render_profiled": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                      ctypes.c_void_p]),
+    "oslg_wavefront_get_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(WavefrontStatsC)]),
 }
 
 _lib = None

@@ -22,7 +22,7 @@ HOST_SOURCES = ["oslg_oso.cpp", "oslg_lower.cpp", "oslg_capi.cpp"]
 # (source, object name, extra flags): the interpreter is compiled once per
 # feature tier (oslg_tier.cu with -DOSLG_TIER=N), in parallel
 CUDA_SOURCES = [("oslg_kernels.cu", "oslg_kernels", []), ("oslg_batch_host.cu", "oslg_batch_host", []),
-                ("oslg_serve.cu", "oslg_serve", [])] + [
+                ("oslg_serve.cu", "oslg_serve", []), ("oslg_wavefront.cu", "oslg_wavefront", [])] + [
     ("oslg_tier.cu", "oslg_tier%d" % t, ["-DOSLG_TIER=%d" % t]) for t in range(8)] + [
     ("oslg_batch.cu", "oslg_batch%d_%d" % (m, q), ["-DOSLG_BATCH_MAXT=%d" % m, "-DOSLG_BATCH_PPT=%d" % q])
     for m in (256, 512) for q in (1, 2, 4)]
@@ -52,7 +52,7 @@ def build(verbose=False, ptxas_verbose=False):
         o = os.path.join(BUILD, src + ".o")
         objs.append(o)
         if not _newer(o, [s] + headers):
-            jobs.append(["g++", "-std=c++17", "-O2", "-fPIC", "-Wall", "-Wno-unused-function",
+            jobs.append(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-Wall", "-Wno-unused-function",
                          "-I", os.path.join(CUDA_HOME, "include"), "-c", s, "-o", o])
     for src, name, extra in CUDA_SOURCES:
         s = os.path.join(CSRC, src)

@@ -3,6 +3,7 @@
 // status and leaves a message in oslg_last_error(); no C++ exception crosses
 // the boundary (the reference reports through bool returns and an
 // ErrorHandler, src/liboslexec/context.cpp:443-451).
+#include <cmath>
 #include <cstring>
 #include <exception>
 #include <memory>
@@ -13,6 +14,7 @@
 #include "oslg_serve.h"
 #include "oslg_exec.h"
 #include "oslg_host.h"
+#include "oslg_wavefront.h"
 
 struct oslg_system {
     oslg::ShadingSystem ss;
@@ -34,6 +36,11 @@ struct oslg_batch {
 struct oslg_server {
     oslg_system* sys;
     std::unique_ptr<oslg::ShadingServer> srv;
+};
+
+struct oslg_wavefront {
+    oslg_system* sys;
+    std::unique_ptr<oslg::Wavefront> wf;
 };
 
 namespace oslg {
@@ -670,4 +677,113 @@ int oslg_server_get_stats(oslg_server* server, oslg_server_stats* out) {
     out->in_flight_waves = s.in_flight_waves;
     out->pending = s.pending;
     return OSLG_OK;
+}
+
+// ---- wavefront path tracing ---------------------------------------------------------
+static bool wf_check_options(const oslg_wavefront_options& o, std::string* why) {
+    if (o.width < 1 || o.height < 1 || o.spp < 1) return *why = "width, height and spp must be positive", false;
+    if ((int64_t)o.width * o.height * o.spp > (int64_t)1 << 30) return *why = "more than 2^30 paths", false;
+    if (o.max_hits < 1 || o.max_hits > oslg::kWfMaxHits) return *why = "max_hits must be in [1, 16]", false;
+    if (!(o.rr_survival > 0.0f && o.rr_survival <= 1.0f)) return *why = "rr_survival must be in (0, 1]", false;
+    if (!(o.fov_deg > 0.0f && o.fov_deg < 180.0f)) return *why = "fov_deg must be in (0, 180)", false;
+    if (o.block < 0 || o.block > 512) return *why = "block must be in [0, 512]", false;
+    return true;
+}
+
+static bool wf_check_prim(const oslg_primitive& q, int nmat, std::string* why) {
+    if (q.material < 0 || q.material >= nmat) return *why = "material index out of range", false;
+    for (int k = 0; k < 3; ++k)
+        if (!std::isfinite(q.p[k]) || !std::isfinite(q.ex[k]) || !std::isfinite(q.ey[k]))
+            return *why = "non-finite coordinate", false;
+    if (q.kind == OSLG_PRIM_SPHERE) {
+        if (!(q.radius > 0.0f) || !std::isfinite(q.radius)) return *why = "sphere radius must be positive", false;
+        return true;
+    }
+    if (q.kind != OSLG_PRIM_QUAD) return *why = "unknown primitive kind", false;
+    const double lx = (double)q.ex[0] * q.ex[0] + (double)q.ex[1] * q.ex[1] + (double)q.ex[2] * q.ex[2];
+    const double ly = (double)q.ey[0] * q.ey[0] + (double)q.ey[1] * q.ey[1] + (double)q.ey[2] * q.ey[2];
+    const double dxy = (double)q.ex[0] * q.ey[0] + (double)q.ex[1] * q.ey[1] + (double)q.ex[2] * q.ey[2];
+    if (!(lx > 0.0 && ly > 0.0)) return *why = "rectangle edge of zero length", false;
+    if (std::fabs(dxy) > 1e-5 * std::sqrt(lx * ly)) return *why = "rectangle edges are not orthogonal", false;
+    return true;
+}
+
+int oslg_wavefront_create(oslg_system* sys, const oslg_wavefront_options* opts, const oslg_primitive* prims,
+                          int nprims, oslg_group* const* materials, int nmaterials, oslg_wavefront** out) {
+    if (!sys || !opts || !out || nprims < 0 || (nprims > 0 && !prims) || !materials) return OSLG_ERR_ARG;
+    return guarded(sys, [&]() {
+        std::string why;
+        if (!wf_check_options(*opts, &why)) return fail(sys, OSLG_ERR_ARG, "wavefront: " + why);
+        if (nmaterials < 1 || nmaterials > oslg::kWfMaxMaterials)
+            return fail(sys, OSLG_ERR_ARG, "wavefront: 1 to 64 materials");
+        for (int i = 0; i < nprims; ++i)
+            if (!wf_check_prim(prims[i], nmaterials, &why))
+                return fail(sys, OSLG_ERR_ARG, "wavefront: primitive " + std::to_string(i) + ": " + why);
+        std::vector<const CompiledGroup*> mats;
+        for (int m = 0; m < nmaterials; ++m) {
+            oslg_group* g = materials[m];
+            if (!g) return fail(sys, OSLG_ERR_ARG, "wavefront: null material group");
+            bool found = false;
+            for (const BsdfSampleRequest& r : g->g.bsdf_samples)
+                found = found || (r.offset == 0 && r.stride == 4 * oslg::kWfOutFloats && r.in_offset == 0 &&
+                                  r.in_stride == 4 * oslg::kWfInFloats);
+            if (!found)
+                return fail(sys, OSLG_ERR_ARG,
+                            "wavefront: material group '" + g->g.name +
+                                "' has no bsdf_sample output at offset 0, stride 44, in_offset 0, in_stride 28");
+            int rc = ensure_compiled(sys, g, true);
+            if (rc != OSLG_OK) return rc;
+            mats.push_back(g->g.compiled.get());
+        }
+        auto w = std::make_unique<oslg_wavefront>();
+        w->sys = sys;
+        w->wf = std::make_unique<oslg::Wavefront>();
+        std::string err;
+        int rc = w->wf->init(sys->dev, *opts, prims, nprims, mats, &err);
+        if (rc != OSLG_OK) return fail(sys, rc, "wavefront: " + err);
+        *out = w.release();
+        return OSLG_OK;
+    });
+}
+
+int oslg_wavefront_destroy(oslg_wavefront* wf) {
+    delete wf;
+    return OSLG_OK;
+}
+
+static int wf_render(oslg_wavefront* wf, float* d_path_radiance, float* d_image, void* stream, bool profile) {
+    if (!wf) return OSLG_ERR_ARG;
+    oslg_system* sys = wf->sys;
+    return guarded(sys, [&]() {
+        std::string err;
+        int rc = wf->wf->render(d_path_radiance, d_image, stream, profile, &err);
+        if (rc != OSLG_OK) return fail(sys, rc, "wavefront: " + err);
+        return OSLG_OK;
+    });
+}
+
+int oslg_wavefront_render(oslg_wavefront* wf, float* d_path_radiance, float* d_image, void* stream) {
+    return wf_render(wf, d_path_radiance, d_image, stream, false);
+}
+
+int oslg_wavefront_render_profiled(oslg_wavefront* wf, float* d_path_radiance, float* d_image, void* stream) {
+    return wf_render(wf, d_path_radiance, d_image, stream, true);
+}
+
+int oslg_wavefront_get_stats(oslg_wavefront* wf, oslg_wavefront_stats* out) {
+    if (!wf || !out) return OSLG_ERR_ARG;
+    oslg_system* sys = wf->sys;
+    return guarded(sys, [&]() {
+        oslg::WavefrontStats s;
+        std::string err;
+        int rc = wf->wf->stats(&s, &err);
+        if (rc != OSLG_OK) return fail(sys, rc, "wavefront: " + err);
+        out->paths = s.paths;
+        for (int b = 0; b < 16; ++b) out->hits[b] = s.hits[b];
+        out->total_hits = s.total_hits;
+        out->bounces = s.bounces;
+        out->ms_total = s.ms_total;
+        for (int k = 0; k < 5; ++k) out->ms_stage[k] = s.ms_stage[k];
+        return OSLG_OK;
+    });
 }

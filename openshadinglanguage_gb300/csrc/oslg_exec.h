@@ -42,6 +42,9 @@ struct BatchArgs {
     uint32_t* status;
     uint32_t prog_bytes;   // shared-memory bytes reserved for the largest program
     uint32_t heap_slots;   // largest heap of any job (floats per point)
+    // When set, the item count is read from device memory at kernel start
+    // (work lists planned on the device, e.g. by the wavefront driver).
+    const uint32_t* nitems_dev = nullptr;
 };
 }  // namespace dev
 

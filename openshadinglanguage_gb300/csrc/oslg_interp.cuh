@@ -1999,12 +1999,13 @@ __global__ void __launch_bounds__(MAXT, 512 / MAXT) batch_kernel(const __grid_co
     RunCtx R;
     R.sops = sops;
     int cur = -1;
+    const uint32_t nitems = b.nitems_dev ? *b.nitems_dev : b.nitems;
     for (;;) {
         if (threadIdx.x == 0) s_item = atomicAdd(b.counter, 1u);
         __syncthreads();
         const uint32_t it = s_item;
         __syncthreads();
-        if (it >= b.nitems) break;
+        if (it >= nitems) break;
         const uint2 w = b.items[it];
         const BatchJob* J = b.jobs + w.x;
         if ((int)w.x != cur) {

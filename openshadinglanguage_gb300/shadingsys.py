@@ -206,6 +206,10 @@ class ShadingSystem:
         """A continuous-batching shading server on this system (see Server)."""
         return Server(self, **options)
 
+    def wavefront(self, prims, materials, **options):
+        """A wavefront path tracer over `prims` shaded by `materials` (see Wavefront)."""
+        return Wavefront(self, prims, materials, **options)
+
     def device_status(self):
         bits = ctypes.c_uint32(0)
         self._check(C.lib().oslg_device_status(self._h, ctypes.byref(bits)))
@@ -345,3 +349,90 @@ class Server:
         s = C.ServerStatsC()
         self._ss._check(C.lib().oslg_server_get_stats(self._h, ctypes.byref(s)))
         return {k: getattr(s, k) for k, _ in C.ServerStatsC._fields_}
+
+
+class Wavefront:
+    """Wavefront path tracing of a frame (include/oslg.h, oslg_wavefront_*):
+    every camera path advances one bounce per wavefront; the hits of a
+    bounce are sorted by material and shaded by the persistent batch
+    kernel. `prims` is a sequence of (kind, material, p, ex, ey, radius)
+    tuples or a numpy structured array with those fields; `materials` are
+    groups whose closure output is sampled with bsdf_sample_output(offset 0,
+    stride 44, in_offset 0, in_stride 28)."""
+
+    OPTION_DEFAULTS = dict(width=1920, height=1080, spp=4, max_hits=8, rr_survival=0.8, eye=(0.0, 6.0, 30.0),
+                           look=(0.0, 2.0, -10.0), up=(0.0, 1.0, 0.0), fov_deg=50.0,
+                           background=(0.25, 0.3, 0.4), seed=0xC5, block=0, points_per_thread=0, heap_smem=0,
+                           use_graph=0)
+
+    def __init__(self, ss, prims, materials, **options):
+        self._ss = ss
+        o = dict(self.OPTION_DEFAULTS)
+        for k in options:
+            if k not in o:
+                raise KeyError("unknown wavefront option '%s'" % k)
+        o.update(options)
+        self.options = o
+        self._opts = options_c(o)
+        arr = prims_c(prims)
+        mats = (ctypes.c_void_p * len(materials))(*[m.handle.value if hasattr(m.handle, "value") else m.handle
+                                                   for m in materials])
+        h = ctypes.c_void_p()
+        ss._check(C.lib().oslg_wavefront_create(ss._h, ctypes.byref(self._opts), arr, len(arr), mats,
+                                                len(materials), ctypes.byref(h)))
+        self._h = h
+        self._materials = list(materials)
+        self.paths = o["width"] * o["height"] * o["spp"]
+
+    def close(self):
+        if self._h:
+            C.lib().oslg_wavefront_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def render(self, path_radiance=0, image=0, stream=0, profile=False):
+        """Enqueue one frame on `stream`. path_radiance: device address of 3
+        planes of `paths` floats; image: device address of width*height*3
+        floats (0 to skip either)."""
+        fn = C.lib().oslg_wavefront_render_profiled if profile else C.lib().oslg_wavefront_render
+        self._ss._check(fn(self._h, ctypes.c_void_p(int(path_radiance) or None),
+                           ctypes.c_void_p(int(image) or None), ctypes.c_void_p(int(stream) or None)))
+
+    def stats(self):
+        s = C.WavefrontStatsC()
+        self._ss._check(C.lib().oslg_wavefront_get_stats(self._h, ctypes.byref(s)))
+        return dict(paths=s.paths, hits=list(s.hits), total_hits=s.total_hits, bounces=s.bounces,
+                    ms_total=s.ms_total, ms_stage=list(s.ms_stage))
+
+
+def options_c(o):
+    """oslg_wavefront_options from a dict of Wavefront.OPTION_DEFAULTS keys."""
+    f3 = lambda v: (ctypes.c_float * 3)(*[float(x) for x in v])
+    return C.WavefrontOptionsC(int(o["width"]), int(o["height"]), int(o["spp"]), int(o["max_hits"]),
+                               float(o["rr_survival"]), f3(o["eye"]), f3(o["look"]), f3(o["up"]),
+                               float(o["fov_deg"]), f3(o["background"]), int(o["seed"]) & 0xFFFFFFFF,
+                               int(o["block"]), int(o["points_per_thread"]), int(o["heap_smem"]),
+                               int(o["use_graph"]))
+
+
+def prims_c(prims):
+    """oslg_primitive array from tuples or a structured array."""
+    n = len(prims)
+    arr = (C.PrimitiveC * max(1, n))()
+    for i in range(n):
+        q = prims[i]
+        kind, mat, p, ex, ey, r = (q["kind"], q["material"], q["p"], q["ex"], q["ey"], q["radius"]) \
+            if hasattr(q, "dtype") else q
+        arr[i].kind = int(kind)
+        arr[i].material = int(mat)
+        for k in range(3):
+            arr[i].p[k] = float(p[k])
+            arr[i].ex[k] = float(ex[k])
+            arr[i].ey[k] = float(ey[k])
+        arr[i].radius = float(r)
+    return arr if n else (C.PrimitiveC * 0)()

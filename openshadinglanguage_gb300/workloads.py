@@ -495,3 +495,50 @@ def c5_hits(n, seed=0xC5A):
     rnd[:, 6] = (rng.random(n) < 0.3).astype(np.float32)
     f32 = lambda a: np.ascontiguousarray(a, dtype=np.float32)
     return (P, f32(N), f32(I), f32(T), rnd)
+
+
+PRIM_DTYPE = np.dtype([("kind", np.int32), ("material", np.int32), ("p", np.float32, 3), ("ex", np.float32, 3),
+                       ("ey", np.float32, 3), ("radius", np.float32)])
+
+
+def c5_scene(nprims=1000, seed=C5_SEED, nmat=C5_MATERIALS):
+    """Seeded scene of spheres and rectangles ("planes"): a 200 x 200
+    ground, a back wall, 24 tilted panels and spheres for the rest (70%
+    resting on the ground, 30% floating), material uniform over nmat."""
+    rng = np.random.default_rng([seed, 0x5C])
+    prims = np.zeros(nprims, PRIM_DTYPE)
+
+    def rect(i, p, ex, ey):
+        prims[i]["kind"] = 1
+        prims[i]["p"], prims[i]["ex"], prims[i]["ey"] = p, ex, ey
+
+    rect(0, (-100.0, 0.0, -100.0), (0.0, 0.0, 200.0), (200.0, 0.0, 0.0))
+    rect(1, (-60.0, 0.0, -45.0), (120.0, 0.0, 0.0), (0.0, 30.0, 0.0))
+    npanels = min(24, max(0, nprims - 2))
+    for k in range(npanels):
+        i = 2 + k
+        a, b = rng.uniform(0, 2 * np.pi), rng.uniform(0.3, 1.2)
+        ex = np.array([np.cos(a), 0.0, np.sin(a)]) * rng.uniform(1.5, 4.0)
+        up = np.array([-np.sin(a) * np.cos(b), np.sin(b), np.cos(a) * np.cos(b)])
+        ey = up * rng.uniform(1.5, 4.0)
+        p = (rng.uniform(-25, 25), rng.uniform(0.0, 4.0), rng.uniform(-40, 10))
+        rect(i, p, ex.astype(np.float32), ey.astype(np.float32))
+        # keep the edges orthogonal in float32
+        e0 = prims[i]["ex"].astype(np.float64)
+        e1 = prims[i]["ey"].astype(np.float64)
+        e1 = e1 - e0 * (e0 @ e1) / (e0 @ e0)
+        prims[i]["ey"] = e1.astype(np.float32)
+    for i in range(2 + npanels, nprims):
+        r = rng.uniform(0.3, 2.0)
+        x, z = rng.uniform(-28, 28), rng.uniform(-42, 12)
+        y = r if rng.random() < 0.7 else r + rng.uniform(0.5, 10.0)
+        prims[i]["kind"] = 0
+        prims[i]["p"] = (x, y, z)
+        prims[i]["radius"] = r
+    prims["material"] = rng.integers(0, nmat, nprims)
+    return prims
+
+
+def c5_materials(ss):
+    """The 16 material groups, sampled with the wavefront record layout."""
+    return [c5_material_group(ss, k, spec) for k, spec in enumerate(c5_material_specs())]

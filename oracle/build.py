@@ -12,8 +12,8 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "liboslg_oracle.so")
-SOURCES = ["oracle.cpp"]
-HEADERS = ["oracle_dual.h", "oracle_noise.h", "oracle_simplex.h"]
+SOURCES = ["oracle.cpp", "oracle_wavefront.cpp"]
+HEADERS = sorted(f for f in os.listdir(HERE) if f.endswith(".h"))
 
 
 def build(force=False):

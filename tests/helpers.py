@@ -33,6 +33,12 @@ def oracle():
         L.oracle_hash_f.restype = ctypes.c_int
         L.oracle_inthash.argtypes = [ctypes.POINTER(ctypes.c_uint32), ctypes.c_int]
         L.oracle_inthash.restype = ctypes.c_uint32
+        L.oracle_wavefront.argtypes = [ctypes.POINTER(_capi.WavefrontOptionsC), ctypes.POINTER(_capi.PrimitiveC),
+                                       ctypes.c_int, ctypes.POINTER(ctypes.c_void_p),
+                                       ctypes.POINTER(ctypes.c_size_t), ctypes.c_int, ctypes.c_int64,
+                                       ctypes.c_int64, ctypes.c_int64, ctypes.c_int,
+                                       ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int64)]
+        L.oracle_wavefront.restype = ctypes.c_int
         _oracle = L
     return _oracle
 
@@ -44,6 +50,30 @@ def oracle_run(blob, npoints, G, outputs, userdata=None, nthreads=0, begin=0):
                              nthreads, ctypes.byref(st))
     assert rc == 0, "oracle rejected the program"
     return st.value
+
+
+def oracle_wavefront(options, prims, groups, begin=0, count=None, step=1, nthreads=0):
+    """The oracle's path tracer over paths begin + k*step: returns
+    (radiance float32 (3, count), hits per bounce int64 (16,), status)."""
+    from openshadinglanguage_gb300.shadingsys import Wavefront, options_c, prims_c
+    o = dict(Wavefront.OPTION_DEFAULTS)
+    o.update(options)
+    npaths = o["width"] * o["height"] * o["spp"]
+    if count is None:
+        count = (npaths - begin + step - 1) // step
+    blobs = [g.program_bytes() for g in groups]
+    bufs = [ctypes.create_string_buffer(b, len(b)) for b in blobs]
+    ptrs = (ctypes.c_void_p * len(bufs))(*[ctypes.addressof(b) for b in bufs])
+    sizes = (ctypes.c_size_t * len(bufs))(*[len(b) for b in blobs])
+    oc = options_c(o)
+    arr = prims_c(prims)
+    rad = np.zeros((3, count), np.float32)
+    hits = np.zeros(16, np.int64)
+    st = oracle().oracle_wavefront(ctypes.byref(oc), arr, len(prims), ptrs, sizes, len(groups), begin, count, step,
+                                   nthreads, rad.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                   hits.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
+    assert st >= 0, "oracle rejected a material program"
+    return rad, hits, st
 
 
 def pixel_grid(W, H, centers=False):
