@@ -290,6 +290,62 @@ def bench_serving(torch, og, nreq=600):
             "latency": "arrival to outputs in host memory (pinned), host monotonic clock"}
 
 
+def bench_wavefront(torch, og, frames=3, cpu_step=97, size=None):
+    """Wavefront path tracing of the seeded 1000-primitive scene with the 16
+    layered materials: 1920x1080x4 paths, up to 8 hits, Russian roulette
+    survival 0.8. A frame (all bounces) is one CUDA-graph replay; a
+    profiled frame gives the per-stage split. The oracle's path loop renders
+    every cpu_step-th path on all host threads for the CPU figure."""
+    from openshadinglanguage_gb300 import workloads
+    from helpers import oracle_wavefront
+    ss = og.ShadingSystem()
+    mats = workloads.c5_materials(ss)
+    prims = workloads.c5_scene()
+    dims = {}
+    if size:
+        w, h, spp = (int(x) for x in size.split("x"))
+        dims = dict(width=w, height=h, spp=spp)
+    wf = ss.wavefront(prims, mats, **dims)
+    o = wf.options
+    rad = torch.empty(3 * wf.paths, dtype=torch.float32, device="cuda")
+    img = torch.empty(o["width"] * o["height"] * 3, dtype=torch.float32, device="cuda")
+    st = torch.cuda.current_stream()
+    for _ in range(2):
+        wf.render(rad.data_ptr(), img.data_ptr(), st.cuda_stream)
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(frames)]
+    for a, b in evs:
+        a.record(st)
+        wf.render(rad.data_ptr(), img.data_ptr(), st.cuda_stream)
+        b.record(st)
+    torch.cuda.synchronize()
+    ms = float(np.mean([a.elapsed_time(b) for a, b in evs]))
+    s = wf.stats()
+    wf.render(rad.data_ptr(), img.data_ptr(), st.cuda_stream, profile=True)
+    prof = wf.stats()
+    status = ss.device_status()
+    nhits = s["total_hits"]
+    # CPU: the oracle's path loop over a strided sample of the same frame
+    oracle_wavefront(o, prims, mats, begin=0, step=cpu_step * 8)  # warm-up on a smaller sample
+    t0 = time.perf_counter()
+    crad, chits, _ = oracle_wavefront(o, prims, mats, begin=0, step=cpu_step)
+    cpu_s = time.perf_counter() - t0
+    ncpu = crad.shape[1]
+    wf.close()
+    stages = dict(zip(("trace", "plan", "scatter", "shade", "update"), prof["ms_stage"]))
+    return {"workload": "wavefront %dx%dx%d spp, <=8 hits, RR 0.8, 1000 spheres/rectangles seed 0xC5, "
+                        "16 materials" % (o["width"], o["height"], o["spp"]), "paths": wf.paths, "frame_ms": ms,
+            "mpaths_per_s": wf.paths / ms / 1e3, "shading_points": nhits,
+            "mhits_per_s": nhits / ms / 1e3, "hits_per_bounce": s["hits"][:o["max_hits"]],
+            "profiled_stage_ms": stages, "device_status": status,
+            "launches_per_frame": 2 + 5 * o["max_hits"] + 1,
+            "cpu": {"paths": ncpu, "hits": int(chits.sum()), "seconds": cpu_s,
+                    "mpaths_per_s": ncpu / cpu_s / 1e6, "mhits_per_s": float(chits.sum()) / cpu_s / 1e6,
+                    "threads": os.cpu_count(), "kind": "port",
+                    "sample": "every %dth path of the frame, oracle path loop (brute-force intersection, "
+                              "batched shading per material)" % cpu_step}}
+
+
 def cpu_reference(wl, og, budget_s=2.0):
     """Time the CPU port of the reference semantics on all host threads."""
     from helpers import oracle_run
@@ -321,9 +377,22 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
-                    help="skip the 64-group batching and the serving measurements")
+                    help="skip the 64-group batching, serving and wavefront measurements")
+    ap.add_argument("--section", choices=["batching", "serving", "wavefront"],
+                    help="run only this measurement section and print it as one JSON line")
+    ap.add_argument("--wf-size", default=None, help="wavefront frame WxHxSPP (default 1920x1080x4)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
+    if args.section:
+        import torch
+        import openshadinglanguage_gb300 as og
+        from openshadinglanguage_gb300.build import build as build_native
+        build_native()
+        torch.cuda.set_device(0)
+        fn = {"batching": lambda: bench_batching(torch, og), "serving": lambda: bench_serving(torch, og),
+              "wavefront": lambda: bench_wavefront(torch, og, size=args.wf_size)}[args.section]
+        print(json.dumps({"section": args.section, args.section: fn()}))
+        return 0
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -470,6 +539,7 @@ def main():
     if not args.no_extras and world == 1:
         line["batching"] = bench_batching(torch, og)
         line["serving"] = bench_serving(torch, og)
+        line["wavefront"] = bench_wavefront(torch, og)
     if not args.no_cpu_baseline:
         from helpers import oracle_run  # noqa: F401
         build_oracle()
