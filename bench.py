@@ -378,6 +378,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the 64-group batching, serving and wavefront measurements")
+    ap.add_argument("--jit", type=int, default=0,
+                    help="1: run the group's specialized kernel (attribute jit), 0: the interpreter")
     ap.add_argument("--section", choices=["batching", "serving", "wavefront"],
                     help="run only this measurement section and print it as one JSON line")
     ap.add_argument("--wf-size", default=None, help="wavefront frame WxHxSPP (default 1920x1080x4)")
@@ -445,6 +447,8 @@ def main():
     else:
         torch.cuda.set_device(0)
     wl.build(torch, og, shaders)
+    if args.jit:
+        wl.ss.attribute("jit", 1)  # the first launch (warm-up) builds and loads the kernel
     stream = torch.cuda.current_stream()
     sh = stream.cuda_stream
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -521,6 +525,7 @@ def main():
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": wl.name, "points": wl.n, "l2": "flushed (512 MiB write) between timed steps",
+                   "kernel": "specialized per group (jit)" if args.jit else "interpreter",
                    "parity": "bit-exact to the CPU oracle (non-FMA reference order) for floats and ints"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": wl.bytes_in,
                 "d2h_bytes_per_step": wl.bytes_out, "ms_per_step": e_ms},

@@ -106,7 +106,9 @@ int oslg_destroy_system(oslg_system* sys);
 /* ShadingSystem::attribute(name, TypeDesc, const void*) (oslexec.h:324).
  * Integer options: "max_closure_components", "max_closure_terms",
  * "gpu_block", "gpu_points_per_thread", "gpu_heap_placement" (0 HBM, 1 smem,
- * -1 auto), "debug". */
+ * -1 auto), "debug", "jit" (1: optimize builds a kernel specialized to the
+ * group, see oslg_group_specialized_source; the counterpart of the
+ * reference's per-group JIT). */
 int oslg_attribute_int(oslg_system* sys, const char* name, int value);
 /* ShadingSystem::register_closure (oslexec.h:1041). Parameters are taken
  * positionally from the `closure` op's arguments. */
@@ -163,6 +165,16 @@ int oslg_group_bsdf_sample(oslg_system* sys, oslg_group* group, const char* clos
 /* ShadingSystem::optimize_group (oslexec.h:1093) + BatchedExecutor::jit_group
  * (oslexec.h:993): lowers the group to a device op program and uploads it. */
 int oslg_optimize_group(oslg_system* sys, oslg_group* group);
+/* The CUDA source of the kernel specialized to this group (each op a call
+ * of the interpreter's handler with constant operands, control flow as
+ * gotos, constants in constant memory). With attribute "jit" = 1 it is
+ * compiled for sm_103a when the group is first uploaded (cubins cached by
+ * content hash) and oslg_execute_batch launches it instead of the
+ * interpreter. Replaces BatchedBackendLLVM code generation
+ * (src/liboslexec/batched_backendllvm.cpp). `size` gets the length + 1. */
+int oslg_group_specialized_source(oslg_system* sys, oslg_group* group, char* buf, size_t cap, size_t* size);
+/* 1 when the group runs its specialized kernel. */
+int oslg_group_is_specialized(oslg_system* sys, oslg_group* group, int* out);
 /* ShaderGroupRef release */
 int oslg_release_group(oslg_system* sys, oslg_group* group);
 

@@ -18,7 +18,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-HOST_SOURCES = ["oslg_oso.cpp", "oslg_lower.cpp", "oslg_capi.cpp"]
+HOST_SOURCES = ["oslg_oso.cpp", "oslg_lower.cpp", "oslg_capi.cpp", "oslg_spec.cpp"]
 # (source, object name, extra flags): the interpreter is compiled once per
 # feature tier (oslg_tier.cu with -DOSLG_TIER=N), in parallel
 CUDA_SOURCES = [("oslg_kernels.cu", "oslg_kernels", []), ("oslg_batch_host.cu", "oslg_batch_host", []),
@@ -74,7 +74,7 @@ def build(verbose=False, ptxas_verbose=False):
                 print(o)
     if jobs or not os.path.exists(LIB):
         _run([NVCC] + ARCH + ["-shared", "-cudart", "shared", "-o", LIB] + objs
-             + ["-Xlinker", "-rpath=" + os.path.join(CUDA_HOME, "lib64")])
+             + ["-ldl", "-Xlinker", "-rpath=" + os.path.join(CUDA_HOME, "lib64")])
     return LIB
 
 

@@ -14,12 +14,16 @@
 #include "oslg_serve.h"
 #include "oslg_exec.h"
 #include "oslg_host.h"
+#include "oslg_spec.h"
 #include "oslg_wavefront.h"
+
+#include <dlfcn.h>
 
 struct oslg_system {
     oslg::ShadingSystem ss;
     oslg::DeviceState dev;
     oslg::LaunchConfig launch;
+    int jit = 0;  // build a specialized kernel per group at optimize time
     std::string err;
     std::vector<oslg::InstanceParam> pending_params;  // Parameter() before Shader()
 };
@@ -155,6 +159,7 @@ int oslg_attribute_int(oslg_system* sys, const char* name, int value) {
     else if (n == "gpu_heap_placement") sys->launch.heap_smem = value;
     else if (n == "gpu_grid") sys->launch.grid = value;
     else if (n == "debug") sys->ss.opts.debug = value;
+    else if (n == "jit") sys->jit = value;
     else return fail(sys, OSLG_ERR_ARG, "unknown attribute '" + n + "'");
     if (sys->ss.opts.max_closure_terms > 0xFFFF || sys->ss.opts.max_closure_components > 0xFFFF)
         return fail(sys, OSLG_ERR_ARG, "closure pool capacity must stay below 65536");
@@ -344,6 +349,17 @@ int oslg_group_bsdf_sample(oslg_system* sys, oslg_group* group, const char* clos
     });
 }
 
+// Folder of this library (the interpreter headers live in its csrc/).
+static std::string library_dir() {
+    Dl_info info;
+    if (dladdr(reinterpret_cast<void*>(&oslg_create_system), &info) && info.dli_fname) {
+        std::string p = info.dli_fname;
+        size_t k = p.rfind('/');
+        if (k != std::string::npos) return p.substr(0, k);
+    }
+    return ".";
+}
+
 static int ensure_compiled(oslg_system* sys, oslg_group* group, bool upload) {
     ShaderGroup& g = group->g;
     if (!g.ended) return fail(sys, OSLG_ERR_STATE, "group used before ShaderGroupEnd");
@@ -361,6 +377,14 @@ static int ensure_compiled(oslg_system* sys, oslg_group* group, bool upload) {
         rc = device_upload_program(g.compiled->blob.data(), g.compiled->blob.size(), &g.compiled->d_blob, &err);
         if (rc != OSLG_OK) return fail(sys, rc, err);
         g.compiled->device = sys->dev.device;
+    }
+    if (upload && sys->jit && !g.compiled->spec) {
+        auto sk = std::make_shared<SpecKernel>();
+        std::string err;
+        const std::string dir = library_dir();
+        int rc = spec_build(*g.compiled, dir + "/csrc", dir + "/_build/jit", sk.get(), &err);
+        if (rc != OSLG_OK) return fail(sys, rc, "group '" + g.name + "': " + err);
+        g.compiled->spec = sk;
     }
     return OSLG_OK;
 }
@@ -397,11 +421,37 @@ int oslg_execute_batch(oslg_system* sys, oslg_group* group, int64_t npoints, con
         int rc = ensure_compiled(sys, group, true);
         if (rc != OSLG_OK) return rc;
         std::string err;
-        rc = device_execute(sys->dev, group->g.compiled->header, group->g.compiled->d_blob, npoints, *globals,
-                            userdata_base, output_base, stream, sys->launch, &err);
+        const CompiledGroup& cg = *group->g.compiled;
+        if (cg.spec)
+            rc = spec_launch(sys->dev, *cg.spec, cg, npoints, *globals, userdata_base, output_base, stream, &err);
+        else
+            rc = device_execute(sys->dev, cg.header, cg.d_blob, npoints, *globals, userdata_base, output_base,
+                                stream, sys->launch, &err);
         if (rc != OSLG_OK) return fail(sys, rc, err);
         return OSLG_OK;
     });
+}
+
+int oslg_group_specialized_source(oslg_system* sys, oslg_group* group, char* buf, size_t cap, size_t* size) {
+    if (!sys || !group) return OSLG_ERR_ARG;
+    return guarded(sys, [&]() {
+        int rc = ensure_compiled(sys, group, false);
+        if (rc != OSLG_OK) return rc;
+        const std::string src = spec_source(*group->g.compiled);
+        if (size) *size = src.size() + 1;
+        if (buf && cap) {
+            const size_t n = std::min(cap - 1, src.size());
+            std::memcpy(buf, src.data(), n);
+            buf[n] = 0;
+        }
+        return OSLG_OK;
+    });
+}
+
+int oslg_group_is_specialized(oslg_system* sys, oslg_group* group, int* out) {
+    if (!sys || !group || !out) return OSLG_ERR_ARG;
+    *out = group->g.compiled && group->g.compiled->spec ? 1 : 0;
+    return OSLG_OK;
 }
 
 int oslg_execute_batch_sync(oslg_system* sys, oslg_group* group, int64_t npoints,

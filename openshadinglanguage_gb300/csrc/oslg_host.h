@@ -139,6 +139,8 @@ struct BsdfSampleRequest {
     int64_t in_offset = 0, in_stride = 28;  // userdata
 };
 
+struct SpecKernel;  // oslg_spec.h
+
 // A lowered group ready to run: the op program plus a serialized blob the
 // device (or a checker) consumes.
 struct CompiledGroup {
@@ -147,6 +149,7 @@ struct CompiledGroup {
     std::vector<std::string> op_names;  // reference op each device op came from
     void* d_blob = nullptr;             // device copy (owned by the executor)
     int device = -1;
+    std::shared_ptr<SpecKernel> spec;   // specialized kernel, when built
 };
 
 // ShaderGroup (oslexec_pvt.h:1777)

@@ -47,6 +47,14 @@ struct Lane {
     int hs;      // heap stride (points per CTA tile)
     int li;      // lane index within the tile
     int64_t pt;  // global point index
+#ifdef OSLG_SPEC
+    // A specialized kernel keeps symbol slots in a thread-local array (hs 1,
+    // li 0, constant offsets: registers) and the closure node pools, which
+    // are indexed at run time, in a separate slot-major heap.
+    float* cheap;
+    int chs, cli;
+    uint32_t cbase;
+#endif
 };
 
 __device__ __forceinline__ uint32_t aoff(uint32_t a) { return a & kArgOffsetMask; }
@@ -1225,8 +1233,14 @@ static __device__ void h_aassign(const Lane& L, const uint32_t* a, uint32_t* st)
 struct ClosurePools {
     uint32_t base, max_nodes;
 };
+// closure node pool access (slots at and above the program's closure base)
+#ifdef OSLG_SPEC
+__device__ __forceinline__ float hget(const Lane& L, uint32_t slot) { return L.cheap[(size_t)(slot - L.cbase) * L.chs + L.cli]; }
+__device__ __forceinline__ void hset(const Lane& L, uint32_t slot, float v) { L.cheap[(size_t)(slot - L.cbase) * L.chs + L.cli] = v; }
+#else
 __device__ __forceinline__ float hget(const Lane& L, uint32_t slot) { return L.heap[(size_t)slot * L.hs + L.li]; }
 __device__ __forceinline__ void hset(const Lane& L, uint32_t slot, float v) { L.heap[(size_t)slot * L.hs + L.li] = v; }
+#endif
 __device__ __forceinline__ uint32_t hgetu(const Lane& L, uint32_t slot) { return __float_as_uint(hget(L, slot)); }
 __device__ __forceinline__ void hsetu(const Lane& L, uint32_t slot, uint32_t v) { hset(L, slot, __uint_as_float(v)); }
 __device__ __forceinline__ uint32_t node_slot(const ClosurePools& P, uint32_t node) {
@@ -1616,8 +1630,317 @@ struct RunCtx {
     uint32_t* status;
 };
 
+// Control state of the masked walk: per thread, PPT points with their
+// active / valid / exited / returned bits and per-depth if and loop stacks.
+template <int PPT>
+struct Ctl {
+    uint32_t validm, actm, extm, lretm;
+    uint32_t stk[PPT], cnd[PPT], brk[PPT], cnt[PPT];
+};
+
+template <int PPT>
+__device__ __forceinline__ void ctl_init(Ctl<PPT>& C, const RunCtx& R, Lane& L, int64_t npoints) {
+    const uint32_t li0 = L.li;
+    const int64_t pt0 = L.pt;
+    C.validm = 0;
+    C.extm = 0;
+    C.lretm = 0;
+#pragma unroll
+    for (int j = 0; j < PPT; ++j) {
+        C.stk[j] = C.cnd[j] = C.brk[j] = C.cnt[j] = 0;
+        if (pt0 + (int64_t)j * blockDim.x < npoints) C.validm |= 1u << j;
+    }
+    C.actm = C.validm;
+    if (R.uses_closures) {
+#pragma unroll
+        for (int j = 0; j < PPT; ++j)
+            if (C.validm & (1u << j)) {
+                L.li = li0 + j * blockDim.x;
+                hsetu(L, R.CP.base, 0u);
+            }
+        L.li = li0;
+    }
+}
+
+// The mask ops. Those that can skip a block return true when no lane of the
+// warp stays active (the caller then jumps to a[2]).
+template <int PPT>
+__device__ __forceinline__ bool ctl_if(Ctl<PPT>& C, Lane& L, uint32_t li0, const uint32_t* a) {
+    const int d = (int)a[1];
+    uint32_t nm = 0;
+#pragma unroll
+    for (int j = 0; j < PPT; ++j) {
+        const bool aj = (C.actm >> j) & 1u;
+        L.li = li0 + j * blockDim.x;
+        const bool c = aj && truth(L, a[0]);
+        C.stk[j] = setbit(C.stk[j], d, aj);
+        C.cnd[j] = setbit(C.cnd[j], d, c);
+        if (c) nm |= 1u << j;
+    }
+    L.li = li0;
+    C.actm = nm;
+    return !__any_sync(FULL, C.actm != 0);
+}
+template <int PPT>
+__device__ __forceinline__ bool ctl_else(Ctl<PPT>& C, const uint32_t* a) {
+    const int d = (int)a[1];
+    const int ll = (int)a[3];
+    uint32_t nm = 0;
+#pragma unroll
+    for (int j = 0; j < PPT; ++j) {
+        const bool off = ((C.extm | C.lretm) >> j & 1u) || (ll && (bit(C.brk[j], ll - 1) || bit(C.cnt[j], ll - 1)));
+        if (bit(C.stk[j], d) && !bit(C.cnd[j], d) && !off) nm |= 1u << j;
+    }
+    C.actm = nm;
+    return !__any_sync(FULL, C.actm != 0);
+}
+template <int PPT>
+__device__ __forceinline__ void ctl_endif(Ctl<PPT>& C, const uint32_t* a) {
+    const int d = (int)a[1];
+    const int ll = (int)a[3];
+    uint32_t nm = 0;
+#pragma unroll
+    for (int j = 0; j < PPT; ++j) {
+        const bool off = ((C.extm | C.lretm) >> j & 1u) || (ll && (bit(C.brk[j], ll - 1) || bit(C.cnt[j], ll - 1)));
+        if (bit(C.stk[j], d) && !off) nm |= 1u << j;
+    }
+    C.actm = nm;
+}
+template <int PPT>
+__device__ __forceinline__ void ctl_loop_begin(Ctl<PPT>& C, const uint32_t* a) {
+    const int d = (int)a[1];
+    const int ll = (int)a[3];
+#pragma unroll
+    for (int j = 0; j < PPT; ++j) {
+        C.stk[j] = setbit(C.stk[j], d, (C.actm >> j) & 1u);
+        C.brk[j] = setbit(C.brk[j], ll - 1, false);
+        C.cnt[j] = setbit(C.cnt[j], ll - 1, false);
+    }
+}
+template <int PPT>
+__device__ __forceinline__ bool ctl_loop_test(Ctl<PPT>& C, Lane& L, uint32_t li0, const uint32_t* a) {
+    uint32_t nm = 0;
+#pragma unroll
+    for (int j = 0; j < PPT; ++j) {
+        L.li = li0 + j * blockDim.x;
+        if (((C.actm >> j) & 1u) && truth(L, a[0])) nm |= 1u << j;
+    }
+    L.li = li0;
+    C.actm = nm;
+    return !__any_sync(FULL, C.actm != 0);
+}
+template <int PPT>
+__device__ __forceinline__ void ctl_loop_step(Ctl<PPT>& C, const uint32_t* a) {
+    const int ll = (int)a[3];
+    uint32_t nm = 0;
+#pragma unroll
+    for (int j = 0; j < PPT; ++j) {
+        if ((((C.actm >> j) & 1u) || bit(C.cnt[j], ll - 1)) && !bit(C.brk[j], ll - 1) && !((C.extm | C.lretm) >> j & 1u))
+            nm |= 1u << j;
+        C.cnt[j] = setbit(C.cnt[j], ll - 1, false);
+    }
+    C.actm = nm;
+}
+template <int PPT>
+__device__ __forceinline__ void ctl_loop_end(Ctl<PPT>& C, const uint32_t* a) {
+    const int d = (int)a[1];
+    const int ll = (int)a[3];
+    uint32_t nm = 0;
+#pragma unroll
+    for (int j = 0; j < PPT; ++j) {
+        C.brk[j] = setbit(C.brk[j], ll - 1, false);
+        C.cnt[j] = setbit(C.cnt[j], ll - 1, false);
+        // lanes that broke out of an enclosing loop stay off via the
+        // enclosing ENDIF/LOOP_STEP recomputation
+        if (bit(C.stk[j], d) && !((C.extm | C.lretm) >> j & 1u)) nm |= 1u << j;
+    }
+    C.actm = nm;
+}
+template <int PPT>
+__device__ __forceinline__ void ctl_break(Ctl<PPT>& C, const uint32_t* a) {
+    const int ll = (int)a[3];
+#pragma unroll
+    for (int j = 0; j < PPT; ++j)
+        if (((C.actm >> j) & 1u) && ll) C.brk[j] = setbit(C.brk[j], ll - 1, true);
+    C.actm = 0;
+}
+template <int PPT>
+__device__ __forceinline__ void ctl_continue(Ctl<PPT>& C, const uint32_t* a) {
+    const int ll = (int)a[3];
+#pragma unroll
+    for (int j = 0; j < PPT; ++j)
+        if (((C.actm >> j) & 1u) && ll) C.cnt[j] = setbit(C.cnt[j], ll - 1, true);
+    C.actm = 0;
+}
+template <int PPT>
+__device__ __forceinline__ void ctl_return(Ctl<PPT>& C) { C.lretm |= C.actm; C.actm = 0; }
+template <int PPT>
+__device__ __forceinline__ void ctl_exit(Ctl<PPT>& C) { C.extm |= C.actm; C.actm = 0; }
+template <int PPT>
+__device__ __forceinline__ void ctl_layer_end(Ctl<PPT>& C) { C.lretm = 0; C.actm = C.validm & ~C.extm; }
+
+// One data op for the point L addresses. next() gives the following op
+// (the closure and Gabor ops carry extra operands there) or null at the end;
+// it is called only by those ops.
+template <int TIER, class NextOp>
+__device__ __forceinline__ void exec_op(const RunCtx& R, Lane& L, uint32_t code, const uint32_t* a, NextOp next_op) {
+    switch (code) {
+    case OP_LOAD_GLOBAL: h_load_global(L, a, (*R.G)); break;
+    case OP_LOAD_USERDATA: h_load_userdata(L, a, R.userdata); break;
+    case OP_STORE_OUTPUT: h_store_output(L, a, R.outputs); break;
+    case OP_ASSIGN: h_assign_fast(L, a, R.status); break;
+    case OP_COMPREF: h_compref(L, a, R.status); break;
+    case OP_COMPASSIGN: h_compassign(L, a, R.status); break;
+    case OP_MXCOMPREF: {
+        int r = ldi(L, a[2], 0), c = ldi(L, a[3], 0);
+        r = r < 0 ? 0 : (r > 3 ? 3 : r); c = c < 0 ? 0 : (c > 3 ? 3 : c);
+        stval(L, a[0], 0, __uint_as_float(ldw(L, a[1], r * 4 + c)));
+        break;
+    }
+    case OP_MXCOMPASSIGN: {
+        int r = ldi(L, a[1], 0), c = ldi(L, a[2], 0);
+        r = r < 0 ? 0 : (r > 3 ? 3 : r); c = c < 0 ? 0 : (c > 3 ? 3 : c);
+        stf(L, a[0], r * 4 + c, ldf(L, a[3], 0, 0));
+        break;
+    }
+    case OP_CONSTRUCT3: h_construct3(L, a); break;
+    case OP_AREF: OSLG_TIER_CASE(4, h_aref(L, a, R.status)) break;
+    case OP_AASSIGN: OSLG_TIER_CASE(4, h_aassign(L, a, R.status)) break;
+    case OP_MATRIX_DIAG: {
+        float v = ldf(L, a[1], 0, 0);
+        for (int i = 0; i < 16; ++i) stf(L, a[0], i, (i % 5 == 0) ? v : 0.0f);
+        break;
+    }
+    case OP_ADD: h_arith_fast<0>(L, a); break;
+    case OP_SUB: h_arith_fast<1>(L, a); break;
+    case OP_MUL: h_arith_fast<2>(L, a); break;
+    case OP_DIV: h_arith_fast<3>(L, a); break;
+    case OP_MOD: h_arith<4>(L, a); break;
+    case OP_NEG: h_unary<OP_NEG>(L, a); break;
+    case OP_IADD: h_iarith<0>(L, a); break;
+    case OP_ISUB: h_iarith<1>(L, a); break;
+    case OP_IMUL: h_iarith<2>(L, a); break;
+    case OP_IDIV: h_iarith<3>(L, a); break;
+    case OP_IMOD: h_iarith<4>(L, a); break;
+    case OP_INEG: stw(L, a[0], 0, (uint32_t)(-ldi(L, a[1], 0))); break;
+    case OP_MMUL: OSLG_TIER_CASE(4, h_mmul(L, a)) break;
+    case OP_EQ: h_cmp<0>(L, a); break;
+    case OP_NEQ: h_cmp<1>(L, a); break;
+    case OP_LT: h_cmp<2>(L, a); break;
+    case OP_GT: h_cmp<3>(L, a); break;
+    case OP_LE: h_cmp<4>(L, a); break;
+    case OP_GE: h_cmp<5>(L, a); break;
+    case OP_AND: stw(L, a[0], 0, (truth(L, a[1]) && truth(L, a[2])) ? 1u : 0u); break;
+    case OP_OR: stw(L, a[0], 0, (truth(L, a[1]) || truth(L, a[2])) ? 1u : 0u); break;
+    case OP_BITAND: stw(L, a[0], 0, (uint32_t)(ldi(L, a[1], 0) & ldi(L, a[2], 0))); break;
+    case OP_BITOR: stw(L, a[0], 0, (uint32_t)(ldi(L, a[1], 0) | ldi(L, a[2], 0))); break;
+    case OP_XOR: stw(L, a[0], 0, (uint32_t)(ldi(L, a[1], 0) ^ ldi(L, a[2], 0))); break;
+    case OP_SHL: stw(L, a[0], 0, (uint32_t)ldi(L, a[1], 0) << (ldi(L, a[2], 0) & 31)); break;
+    case OP_SHR: stw(L, a[0], 0, (uint32_t)(ldi(L, a[1], 0) >> (ldi(L, a[2], 0) & 31))); break;
+    case OP_COMPL: stw(L, a[0], 0, ~(uint32_t)ldi(L, a[1], 0)); break;
+    case OP_ABS: h_unary<OP_ABS>(L, a); break;
+    case OP_IABS: { int v = ldi(L, a[1], 0); stw(L, a[0], 0, (uint32_t)(v < 0 ? -v : v)); break; }
+    case OP_FLOOR: h_unary<OP_FLOOR>(L, a); break;
+    case OP_CEIL: h_unary<OP_CEIL>(L, a); break;
+    case OP_ROUND: h_unary<OP_ROUND>(L, a); break;
+    case OP_TRUNC: h_unary<OP_TRUNC>(L, a); break;
+    case OP_SIGN: h_unary<OP_SIGN>(L, a); break;
+    case OP_SQRT: h_unary<OP_SQRT>(L, a); break;
+    case OP_INVSQRT: h_unary<OP_INVSQRT>(L, a); break;
+    case OP_CBRT: OSLG_TIER_CASE(4, h_unary<OP_CBRT>(L, a)) break;
+    case OP_SIN: OSLG_TIER_CASE(4, h_unary<OP_SIN>(L, a)) break;
+    case OP_COS: OSLG_TIER_CASE(4, h_unary<OP_COS>(L, a)) break;
+    case OP_TAN: OSLG_TIER_CASE(4, h_unary<OP_TAN>(L, a)) break;
+    case OP_ASIN: OSLG_TIER_CASE(4, h_unary<OP_ASIN>(L, a)) break;
+    case OP_ACOS: OSLG_TIER_CASE(4, h_unary<OP_ACOS>(L, a)) break;
+    case OP_ATAN: OSLG_TIER_CASE(4, h_unary<OP_ATAN>(L, a)) break;
+    case OP_SINH: OSLG_TIER_CASE(4, h_unary<OP_SINH>(L, a)) break;
+    case OP_COSH: OSLG_TIER_CASE(4, h_unary<OP_COSH>(L, a)) break;
+    case OP_TANH: OSLG_TIER_CASE(4, h_unary<OP_TANH>(L, a)) break;
+    case OP_EXP: OSLG_TIER_CASE(4, h_unary<OP_EXP>(L, a)) break;
+    case OP_EXP2: OSLG_TIER_CASE(4, h_unary<OP_EXP2>(L, a)) break;
+    case OP_EXPM1: OSLG_TIER_CASE(4, h_unary<OP_EXPM1>(L, a)) break;
+    case OP_LOG: OSLG_TIER_CASE(4, h_unary<OP_LOG>(L, a)) break;
+    case OP_LOG2: OSLG_TIER_CASE(4, h_unary<OP_LOG2>(L, a)) break;
+    case OP_LOG10: OSLG_TIER_CASE(4, h_unary<OP_LOG10>(L, a)) break;
+    case OP_RADIANS: h_unary<OP_RADIANS>(L, a); break;
+    case OP_DEGREES: h_unary<OP_DEGREES>(L, a); break;
+    case OP_ISNAN: stw(L, a[0], 0, isnan(ldf(L, a[1], 0, 0)) ? 1u : 0u); break;
+    case OP_ISINF: stw(L, a[0], 0, isinf(ldf(L, a[1], 0, 0)) ? 1u : 0u); break;
+    case OP_ISFINITE: stw(L, a[0], 0, isfinite(ldf(L, a[1], 0, 0)) ? 1u : 0u); break;
+    case OP_POW: OSLG_TIER_CASE(4, h_binary<OP_POW>(L, a)) break;
+    case OP_ATAN2: OSLG_TIER_CASE(4, h_binary<OP_ATAN2>(L, a)) break;
+    case OP_FMOD: OSLG_TIER_CASE(4, h_binary<OP_FMOD>(L, a)) break;
+    case OP_MIN: h_binary<OP_MIN>(L, a); break;
+    case OP_MAX: h_binary<OP_MAX>(L, a); break;
+    case OP_STEP: h_binary<OP_STEP>(L, a); break;
+    case OP_IMIN: { int x = ldi(L, a[1], 0), y = ldi(L, a[2], 0); stw(L, a[0], 0, (uint32_t)(x <= y ? x : y)); break; }
+    case OP_IMAX: { int x = ldi(L, a[1], 0), y = ldi(L, a[2], 0); stw(L, a[0], 0, (uint32_t)(x > y ? x : y)); break; }
+    case OP_CLAMP: OSLG_TIER_CASE(4, h_clamp(L, a)) break;
+    case OP_MIX: OSLG_TIER_CASE(4, h_mix(L, a)) break;
+    case OP_SMOOTHSTEP: OSLG_TIER_CASE(4, h_smoothstep(L, a)) break;
+    case OP_SELECT: OSLG_TIER_CASE(4, h_select(L, a)) break;
+    case OP_DOT: OSLG_TIER_CASE(4, h_dot(L, a)) break;
+    case OP_CROSS: OSLG_TIER_CASE(4, h_cross(L, a)) break;
+    case OP_LENGTH: OSLG_TIER_CASE(4, h_length(L, a, false)) break;
+    case OP_DISTANCE: OSLG_TIER_CASE(4, h_length(L, a, true)) break;
+    case OP_NORMALIZE: OSLG_TIER_CASE(4, h_normalize(L, a)) break;
+    case OP_DX:
+    case OP_DY: {
+        int d = code == OP_DX ? 1 : 2;
+        int nc = anc(a[0]);
+        for (int c = 0; c < nc; ++c) stval(L, a[0], c, ldf(L, a[1], c, d));
+        break;
+    }
+    case OP_TRANSFORM:
+        if (a[3] == 2u) { OSLG_TIER_CASE(4, h_transformn(L, a)) }
+        else { OSLG_TIER_CASE(4, h_transform(L, a)) }
+        break;
+    case OP_MDIV: OSLG_TIER_CASE(4, h_mdiv(L, a)) break;
+    case OP_TRANSPOSE:
+    case OP_DETERMINANT: OSLG_TIER_CASE(4, h_matrix_misc(L, code, a)) break;
+    case OP_AREA:
+    case OP_FILTERWIDTH: OSLG_TIER_CASE(4, h_deriv_misc(L, code, a)) break;
+    case OP_LUMINANCE: OSLG_TIER_CASE(4, h_luminance(L, a)) break;
+    case OP_BLACKBODY: OSLG_TIER_CASE(4, h_blackbody(L, a)) break;
+    case OP_NOISE: OSLG_TIER_CASE(1, h_noise(L, a)) break;
+    case OP_GABOR: {
+        if constexpr ((TIER & 1) != 0) {
+            const Op* next = next_op();
+            if (next) h_gabor(L, a, next->a);
+            else raise_status(R.status, ST_BAD_OPCODE);
+        } else {
+            raise_status(R.status, ST_BAD_OPCODE);
+        }
+        break;
+    }
+    case OP_HASH: OSLG_TIER_CASE(1, h_hash(L, a)) break;
+    case OP_CLOSURE: {
+        if constexpr ((TIER & 2) != 0) {
+            const uint32_t* extra = nullptr;
+            const Op* next = next_op();
+            if (next && next->code == OP_NOP && next->nargs == 7) extra = next->a;
+            h_closure(L, a, extra, R.CP, R.status);
+        } else {
+            raise_status(R.status, ST_BAD_OPCODE);
+        }
+        break;
+    }
+    case OP_CLOSURE_MUL: OSLG_TIER_CASE(2, h_closure_mul(L, a, R.CP, R.status)) break;
+    case OP_CLOSURE_ADD: OSLG_TIER_CASE(2, h_closure_add(L, a, R.CP, R.status)) break;
+    case OP_STORE_CLOSURE: OSLG_TIER_CASE(2, h_store_closure(L, a, R.outputs, R.CP, R.status)) break;
+    case OP_BSDF_EVAL: OSLG_TIER_CASE(2, h_bsdf_eval(L, a, R.outputs, R.CP, R.status)) break;
+    case OP_BSDF_SAMPLE: OSLG_TIER_CASE(2, h_bsdf_sample(L, a, R.outputs, R.userdata, R.CP, R.status)) break;
+    case OP_SPLINE: OSLG_TIER_CASE(2, h_spline(L, a)) break;
+    default: raise_status(R.status, ST_BAD_OPCODE); break;
+    }
+}
+
 // Run the whole program for one point per thread (L.pt; lanes past npoints
-// take part in the warp-uniform walk with no active bits).
+// take part in the warp-uniform walk with no active bits). The mask ops
+// here are the ctl_* functions above written out over plain locals (the
+// struct form costs the interpreter registers); a specialized kernel calls
+// ctl_* and exec_op directly.
 template <int TIER, int PPT = 1>
 __device__ __forceinline__ void run_tile(const RunCtx& R, Lane& L, int64_t npoints) {
     // Each thread carries PPT points of the tile: lane slot li0 + j*blockDim
@@ -1772,161 +2095,14 @@ __device__ __forceinline__ void run_tile(const RunCtx& R, Lane& L, int64_t npoin
         case OP_EXIT: extm |= actm; actm = 0; break;
         case OP_LAYER_END: lretm = 0; actm = validm & ~extm; break;
         default: {
+            auto next = [&]() -> const Op* { return pc + 1 < R.nops ? R.sops + pc + 1 : nullptr; };
             uint32_t todo = actm;
 #pragma unroll 1
             for (int j = 0; todo; ++j, todo >>= 1) {
                 if (!(todo & 1u)) continue;
                 L.li = li0 + j * blockDim.x;
                 L.pt = pt0 + (int64_t)j * blockDim.x;
-                switch (code) {
-                case OP_LOAD_GLOBAL: h_load_global(L, a, (*R.G)); break;
-                case OP_LOAD_USERDATA: h_load_userdata(L, a, R.userdata); break;
-                case OP_STORE_OUTPUT: h_store_output(L, a, R.outputs); break;
-                case OP_ASSIGN: h_assign_fast(L, a, R.status); break;
-                case OP_COMPREF: h_compref(L, a, R.status); break;
-                case OP_COMPASSIGN: h_compassign(L, a, R.status); break;
-                case OP_MXCOMPREF: {
-                    int r = ldi(L, a[2], 0), c = ldi(L, a[3], 0);
-                    r = r < 0 ? 0 : (r > 3 ? 3 : r); c = c < 0 ? 0 : (c > 3 ? 3 : c);
-                    stval(L, a[0], 0, __uint_as_float(ldw(L, a[1], r * 4 + c)));
-                    break;
-                }
-                case OP_MXCOMPASSIGN: {
-                    int r = ldi(L, a[1], 0), c = ldi(L, a[2], 0);
-                    r = r < 0 ? 0 : (r > 3 ? 3 : r); c = c < 0 ? 0 : (c > 3 ? 3 : c);
-                    stf(L, a[0], r * 4 + c, ldf(L, a[3], 0, 0));
-                    break;
-                }
-                case OP_CONSTRUCT3: h_construct3(L, a); break;
-                case OP_AREF: OSLG_TIER_CASE(4, h_aref(L, a, R.status)) break;
-                case OP_AASSIGN: OSLG_TIER_CASE(4, h_aassign(L, a, R.status)) break;
-                case OP_MATRIX_DIAG: {
-                    float v = ldf(L, a[1], 0, 0);
-                    for (int i = 0; i < 16; ++i) stf(L, a[0], i, (i % 5 == 0) ? v : 0.0f);
-                    break;
-                }
-                case OP_ADD: h_arith_fast<0>(L, a); break;
-                case OP_SUB: h_arith_fast<1>(L, a); break;
-                case OP_MUL: h_arith_fast<2>(L, a); break;
-                case OP_DIV: h_arith_fast<3>(L, a); break;
-                case OP_MOD: h_arith<4>(L, a); break;
-                case OP_NEG: h_unary<OP_NEG>(L, a); break;
-                case OP_IADD: h_iarith<0>(L, a); break;
-                case OP_ISUB: h_iarith<1>(L, a); break;
-                case OP_IMUL: h_iarith<2>(L, a); break;
-                case OP_IDIV: h_iarith<3>(L, a); break;
-                case OP_IMOD: h_iarith<4>(L, a); break;
-                case OP_INEG: stw(L, a[0], 0, (uint32_t)(-ldi(L, a[1], 0))); break;
-                case OP_MMUL: OSLG_TIER_CASE(4, h_mmul(L, a)) break;
-                case OP_EQ: h_cmp<0>(L, a); break;
-                case OP_NEQ: h_cmp<1>(L, a); break;
-                case OP_LT: h_cmp<2>(L, a); break;
-                case OP_GT: h_cmp<3>(L, a); break;
-                case OP_LE: h_cmp<4>(L, a); break;
-                case OP_GE: h_cmp<5>(L, a); break;
-                case OP_AND: stw(L, a[0], 0, (truth(L, a[1]) && truth(L, a[2])) ? 1u : 0u); break;
-                case OP_OR: stw(L, a[0], 0, (truth(L, a[1]) || truth(L, a[2])) ? 1u : 0u); break;
-                case OP_BITAND: stw(L, a[0], 0, (uint32_t)(ldi(L, a[1], 0) & ldi(L, a[2], 0))); break;
-                case OP_BITOR: stw(L, a[0], 0, (uint32_t)(ldi(L, a[1], 0) | ldi(L, a[2], 0))); break;
-                case OP_XOR: stw(L, a[0], 0, (uint32_t)(ldi(L, a[1], 0) ^ ldi(L, a[2], 0))); break;
-                case OP_SHL: stw(L, a[0], 0, (uint32_t)ldi(L, a[1], 0) << (ldi(L, a[2], 0) & 31)); break;
-                case OP_SHR: stw(L, a[0], 0, (uint32_t)(ldi(L, a[1], 0) >> (ldi(L, a[2], 0) & 31))); break;
-                case OP_COMPL: stw(L, a[0], 0, ~(uint32_t)ldi(L, a[1], 0)); break;
-                case OP_ABS: h_unary<OP_ABS>(L, a); break;
-                case OP_IABS: { int v = ldi(L, a[1], 0); stw(L, a[0], 0, (uint32_t)(v < 0 ? -v : v)); break; }
-                case OP_FLOOR: h_unary<OP_FLOOR>(L, a); break;
-                case OP_CEIL: h_unary<OP_CEIL>(L, a); break;
-                case OP_ROUND: h_unary<OP_ROUND>(L, a); break;
-                case OP_TRUNC: h_unary<OP_TRUNC>(L, a); break;
-                case OP_SIGN: h_unary<OP_SIGN>(L, a); break;
-                case OP_SQRT: h_unary<OP_SQRT>(L, a); break;
-                case OP_INVSQRT: h_unary<OP_INVSQRT>(L, a); break;
-                case OP_CBRT: OSLG_TIER_CASE(4, h_unary<OP_CBRT>(L, a)) break;
-                case OP_SIN: OSLG_TIER_CASE(4, h_unary<OP_SIN>(L, a)) break;
-                case OP_COS: OSLG_TIER_CASE(4, h_unary<OP_COS>(L, a)) break;
-                case OP_TAN: OSLG_TIER_CASE(4, h_unary<OP_TAN>(L, a)) break;
-                case OP_ASIN: OSLG_TIER_CASE(4, h_unary<OP_ASIN>(L, a)) break;
-                case OP_ACOS: OSLG_TIER_CASE(4, h_unary<OP_ACOS>(L, a)) break;
-                case OP_ATAN: OSLG_TIER_CASE(4, h_unary<OP_ATAN>(L, a)) break;
-                case OP_SINH: OSLG_TIER_CASE(4, h_unary<OP_SINH>(L, a)) break;
-                case OP_COSH: OSLG_TIER_CASE(4, h_unary<OP_COSH>(L, a)) break;
-                case OP_TANH: OSLG_TIER_CASE(4, h_unary<OP_TANH>(L, a)) break;
-                case OP_EXP: OSLG_TIER_CASE(4, h_unary<OP_EXP>(L, a)) break;
-                case OP_EXP2: OSLG_TIER_CASE(4, h_unary<OP_EXP2>(L, a)) break;
-                case OP_EXPM1: OSLG_TIER_CASE(4, h_unary<OP_EXPM1>(L, a)) break;
-                case OP_LOG: OSLG_TIER_CASE(4, h_unary<OP_LOG>(L, a)) break;
-                case OP_LOG2: OSLG_TIER_CASE(4, h_unary<OP_LOG2>(L, a)) break;
-                case OP_LOG10: OSLG_TIER_CASE(4, h_unary<OP_LOG10>(L, a)) break;
-                case OP_RADIANS: h_unary<OP_RADIANS>(L, a); break;
-                case OP_DEGREES: h_unary<OP_DEGREES>(L, a); break;
-                case OP_ISNAN: stw(L, a[0], 0, isnan(ldf(L, a[1], 0, 0)) ? 1u : 0u); break;
-                case OP_ISINF: stw(L, a[0], 0, isinf(ldf(L, a[1], 0, 0)) ? 1u : 0u); break;
-                case OP_ISFINITE: stw(L, a[0], 0, isfinite(ldf(L, a[1], 0, 0)) ? 1u : 0u); break;
-                case OP_POW: OSLG_TIER_CASE(4, h_binary<OP_POW>(L, a)) break;
-                case OP_ATAN2: OSLG_TIER_CASE(4, h_binary<OP_ATAN2>(L, a)) break;
-                case OP_FMOD: OSLG_TIER_CASE(4, h_binary<OP_FMOD>(L, a)) break;
-                case OP_MIN: h_binary<OP_MIN>(L, a); break;
-                case OP_MAX: h_binary<OP_MAX>(L, a); break;
-                case OP_STEP: h_binary<OP_STEP>(L, a); break;
-                case OP_IMIN: { int x = ldi(L, a[1], 0), y = ldi(L, a[2], 0); stw(L, a[0], 0, (uint32_t)(x <= y ? x : y)); break; }
-                case OP_IMAX: { int x = ldi(L, a[1], 0), y = ldi(L, a[2], 0); stw(L, a[0], 0, (uint32_t)(x > y ? x : y)); break; }
-                case OP_CLAMP: OSLG_TIER_CASE(4, h_clamp(L, a)) break;
-                case OP_MIX: OSLG_TIER_CASE(4, h_mix(L, a)) break;
-                case OP_SMOOTHSTEP: OSLG_TIER_CASE(4, h_smoothstep(L, a)) break;
-                case OP_SELECT: OSLG_TIER_CASE(4, h_select(L, a)) break;
-                case OP_DOT: OSLG_TIER_CASE(4, h_dot(L, a)) break;
-                case OP_CROSS: OSLG_TIER_CASE(4, h_cross(L, a)) break;
-                case OP_LENGTH: OSLG_TIER_CASE(4, h_length(L, a, false)) break;
-                case OP_DISTANCE: OSLG_TIER_CASE(4, h_length(L, a, true)) break;
-                case OP_NORMALIZE: OSLG_TIER_CASE(4, h_normalize(L, a)) break;
-                case OP_DX:
-                case OP_DY: {
-                    int d = code == OP_DX ? 1 : 2;
-                    int nc = anc(a[0]);
-                    for (int c = 0; c < nc; ++c) stval(L, a[0], c, ldf(L, a[1], c, d));
-                    break;
-                }
-                case OP_TRANSFORM:
-                    if (a[3] == 2u) { OSLG_TIER_CASE(4, h_transformn(L, a)) }
-                    else { OSLG_TIER_CASE(4, h_transform(L, a)) }
-                    break;
-                case OP_MDIV: OSLG_TIER_CASE(4, h_mdiv(L, a)) break;
-                case OP_TRANSPOSE:
-                case OP_DETERMINANT: OSLG_TIER_CASE(4, h_matrix_misc(L, code, a)) break;
-                case OP_AREA:
-                case OP_FILTERWIDTH: OSLG_TIER_CASE(4, h_deriv_misc(L, code, a)) break;
-                case OP_LUMINANCE: OSLG_TIER_CASE(4, h_luminance(L, a)) break;
-                case OP_BLACKBODY: OSLG_TIER_CASE(4, h_blackbody(L, a)) break;
-                case OP_NOISE: OSLG_TIER_CASE(1, h_noise(L, a)) break;
-                case OP_GABOR: {
-                    if constexpr ((TIER & 1) != 0) {
-                        if (pc + 1 < R.nops) h_gabor(L, a, R.sops[pc + 1].a);
-                        else raise_status(R.status, ST_BAD_OPCODE);
-                    } else {
-                        raise_status(R.status, ST_BAD_OPCODE);
-                    }
-                    break;
-                }
-                case OP_HASH: OSLG_TIER_CASE(1, h_hash(L, a)) break;
-                case OP_CLOSURE: {
-                    if constexpr ((TIER & 2) != 0) {
-                        const uint32_t* extra = nullptr;
-                        if (pc + 1 < R.nops && R.sops[pc + 1].code == OP_NOP && R.sops[pc + 1].nargs == 7)
-                            extra = R.sops[pc + 1].a;
-                        h_closure(L, a, extra, R.CP, R.status);
-                    } else {
-                        raise_status(R.status, ST_BAD_OPCODE);
-                    }
-                    break;
-                }
-                case OP_CLOSURE_MUL: OSLG_TIER_CASE(2, h_closure_mul(L, a, R.CP, R.status)) break;
-                case OP_CLOSURE_ADD: OSLG_TIER_CASE(2, h_closure_add(L, a, R.CP, R.status)) break;
-                case OP_STORE_CLOSURE: OSLG_TIER_CASE(2, h_store_closure(L, a, R.outputs, R.CP, R.status)) break;
-                case OP_BSDF_EVAL: OSLG_TIER_CASE(2, h_bsdf_eval(L, a, R.outputs, R.CP, R.status)) break;
-                case OP_BSDF_SAMPLE: OSLG_TIER_CASE(2, h_bsdf_sample(L, a, R.outputs, R.userdata, R.CP, R.status)) break;
-                case OP_SPLINE: OSLG_TIER_CASE(2, h_spline(L, a)) break;
-                default: raise_status(R.status, ST_BAD_OPCODE); break;
-                }
+                exec_op<TIER>(R, L, code, a, next);
             }
             L.li = li0;
             L.pt = pt0;

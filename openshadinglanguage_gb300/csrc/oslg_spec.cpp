@@ -1,0 +1,271 @@
+// Per-group kernel specialization: source generation, nvcc build with a
+// content-addressed cubin cache, loading and launch (see oslg_spec.h).
+#include "oslg_spec.h"
+
+#include <cuda_runtime.h>
+#include <dirent.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <mutex>
+#include <sstream>
+#include <vector>
+
+namespace oslg {
+
+namespace {
+
+bool ok(cudaError_t e, std::string* err, const char* what) {
+    if (e == cudaSuccess) return true;
+    if (err) *err = std::string(what) + ": " + cudaGetErrorString(e);
+    return false;
+}
+
+uint64_t fnv1a(const std::string& s, uint64_t h = 1469598103934665603ull) {
+    for (unsigned char c : s) {
+        h ^= c;
+        h *= 1099511628211ull;
+    }
+    return h;
+}
+
+std::string read_file(const std::string& p) {
+    std::ifstream f(p, std::ios::binary);
+    std::stringstream ss;
+    ss << f.rdbuf();
+    return ss.str();
+}
+
+// Hash of every header the generated source includes (so that a changed
+// interpreter never reuses a stale cubin).
+uint64_t headers_hash(const std::string& csrc) {
+    static std::mutex mu;
+    static std::string dir;
+    static uint64_t h = 0;
+    std::lock_guard<std::mutex> lock(mu);
+    if (dir == csrc && h) return h;
+    std::vector<std::string> names;
+    if (DIR* d = opendir(csrc.c_str())) {
+        while (dirent* e = readdir(d)) {
+            std::string n = e->d_name;
+            if (n.size() > 3 && (n.compare(n.size() - 4, 4, ".cuh") == 0 || n.compare(n.size() - 2, 2, ".h") == 0))
+                names.push_back(n);
+        }
+        closedir(d);
+    }
+    std::sort(names.begin(), names.end());
+    uint64_t x = 1469598103934665603ull;
+    for (const std::string& n : names) x = fnv1a(n + "\n" + read_file(csrc + "/" + n), x);
+    x = fnv1a(read_file(csrc + "/../../include/oslg.h"), x);
+    dir = csrc;
+    h = x;
+    return h;
+}
+
+const char* kKernelName = "oslg_spec_kernel";
+const char* kFlags = "-cubin -gencode arch=compute_103a,code=sm_103a -std=c++17 -O3 -fmad=false";
+
+bool jump_op(uint16_t c) { return c == OP_IF || c == OP_ELSE || c == OP_LOOP_TEST || c == OP_JUMP; }
+
+void put_args(std::ostringstream& o, const uint32_t* a) {
+    o << "{";
+    for (int i = 0; i < 7; ++i) o << (i ? ", " : "") << a[i] << "u";
+    o << "}";
+}
+
+}  // namespace
+
+SpecKernel::~SpecKernel() {
+    if (library) cudaLibraryUnload(static_cast<cudaLibrary_t>(library));
+}
+
+std::string spec_source(const CompiledGroup& cg) {
+    const ProgramHeader& h = cg.header;
+    const Op* ops = reinterpret_cast<const Op*>(cg.blob.data() + sizeof(ProgramHeader));
+    const uint32_t* pool =
+        reinterpret_cast<const uint32_t*>(cg.blob.data() + sizeof(ProgramHeader) + (size_t)h.nops * sizeof(Op));
+    const int n = (int)h.nops;
+    const bool uses_cl = (h.flags & 1u) != 0;
+    const uint32_t sym = uses_cl ? h.closure_base : h.heap_slots;
+    const uint32_t cpool = uses_cl ? h.heap_slots - h.closure_base : 0;
+    std::vector<char> target(n + 1, 0);
+    for (int i = 0; i < n; ++i)
+        if (jump_op(ops[i].code) && ops[i].a[2] <= (uint32_t)n) target[ops[i].a[2]] = 1;
+
+    std::ostringstream o;
+    o << "// generated: kernel specialized to one lowered program (" << n << " ops, " << sym
+      << " symbol slots, " << cpool << " closure-pool slots)\n";
+    o << "#define OSLG_SPEC 1\n#include \"oslg_interp.cuh\"\n\nnamespace {\n";
+    o << "using namespace oslg;\nusing namespace oslg::dev;\n\n";
+    o << "__constant__ const uint32_t kPool[" << std::max(1u, h.nconst) << "] = {";
+    for (uint32_t i = 0; i < h.nconst; ++i) o << (i ? ", " : "") << pool[i] << "u";
+    if (!h.nconst) o << "0u";
+    o << "};\n\n";
+    o << "__device__ __forceinline__ void spec_body(const RunCtx& R, Lane& L, int64_t npoints) {\n";
+    o << "    Ctl<1> C;\n    ctl_init<1>(C, R, L, npoints);\n    long long backedges = 0;\n";
+    o << "    const uint32_t li0 = L.li;\n    (void)backedges;\n    (void)li0;\n";
+    for (int i = 0; i < n; ++i) {
+        const Op& op = ops[i];
+        if (target[i]) o << "op_" << i << ":;\n";
+        const uint32_t* a = op.a;
+        auto dst = [&](uint32_t t) { return "op_" + std::to_string(std::min<uint32_t>(t, (uint32_t)n)); };
+        o << "    {  // " << i << ": code " << op.code << "\n        const uint32_t a[7] = ";
+        put_args(o, a);
+        o << ";\n";
+        switch (op.code) {
+        case OP_NOP: o << "        (void)a;\n"; break;
+        case OP_IF: o << "        if (ctl_if<1>(C, L, li0, a)) goto " << dst(a[2]) << ";\n"; break;
+        case OP_ELSE: o << "        if (ctl_else<1>(C, a)) goto " << dst(a[2]) << ";\n"; break;
+        case OP_ENDIF: o << "        ctl_endif<1>(C, a);\n"; break;
+        case OP_LOOP_BEGIN: o << "        ctl_loop_begin<1>(C, a);\n"; break;
+        case OP_LOOP_TEST: o << "        if (ctl_loop_test<1>(C, L, li0, a)) goto " << dst(a[2]) << ";\n"; break;
+        case OP_LOOP_STEP: o << "        ctl_loop_step<1>(C, a);\n"; break;
+        case OP_JUMP:
+            o << "        (void)a;\n        if (++backedges > kMaxBackEdges) {\n"
+                 "            if (threadIdx.x % 32 == 0) raise_status(R.status, ST_TIMEOUT);\n"
+                 "            goto op_" << n << ";\n        }\n        goto " << dst(a[2]) << ";\n";
+            break;
+        case OP_LOOP_END: o << "        ctl_loop_end<1>(C, a);\n"; break;
+        case OP_BREAK: o << "        ctl_break<1>(C, a);\n"; break;
+        case OP_CONTINUE: o << "        ctl_continue<1>(C, a);\n"; break;
+        case OP_RETURN: o << "        (void)a;\n        ctl_return<1>(C);\n"; break;
+        case OP_EXIT: o << "        (void)a;\n        ctl_exit<1>(C);\n"; break;
+        case OP_LAYER_END: o << "        (void)a;\n        ctl_layer_end<1>(C);\n"; break;
+        default:
+            if (i + 1 < n) {
+                const Op& nx = ops[i + 1];
+                o << "        const Op nx = {" << nx.code << ", " << (unsigned)nx.nargs << ", " << (unsigned)nx.flags
+                  << ", ";
+                put_args(o, nx.a);
+                o << "};\n        if (C.actm) exec_op<7>(R, L, " << op.code
+                  << "u, a, [&]() -> const Op* { return &nx; });\n";
+            } else {
+                o << "        if (C.actm) exec_op<7>(R, L, " << op.code
+                  << "u, a, []() -> const Op* { return nullptr; });\n";
+            }
+            break;
+        }
+        o << "    }\n";
+    }
+    o << "op_" << n << ":;\n}\n\n}  // namespace\n\n";
+    o << "extern \"C\" __global__ void __launch_bounds__(256, 2) " << kKernelName
+      << "(const __grid_constant__ oslg::dev::KArgs k, int pool_in_smem) {\n";
+    o << "    using namespace oslg;\n    using namespace oslg::dev;\n";
+    o << "    extern __shared__ __align__(16) unsigned char smem[];\n";
+    o << "    RunCtx R;\n    R.sops = nullptr;\n    R.nops = " << n << ";\n";
+    o << "    R.CP.base = " << h.closure_base << "u;\n    R.CP.max_nodes = " << h.max_comps << "u;\n";
+    o << "    R.uses_closures = " << (uses_cl ? "true" : "false") << ";\n";
+    o << "    R.G = &k.G;\n    R.userdata = k.userdata;\n    R.outputs = k.outputs;\n    R.status = k.status;\n";
+    o << "    float hreg[" << std::max(1u, sym) << "];\n";
+    o << "    Lane L;\n    L.heap = hreg;\n    L.pool = kPool;\n    L.hs = 1;\n    L.li = 0;\n    L.pt = 0;\n";
+    o << "    L.cheap = pool_in_smem ? reinterpret_cast<float*>(smem) : k.gheap + (size_t)blockIdx.x * "
+      << std::max(1u, cpool) << "u * blockDim.x;\n";
+    o << "    L.chs = blockDim.x;\n    L.cli = threadIdx.x;\n    L.cbase = " << h.closure_base << "u;\n";
+    o << "    const int64_t ntiles = (k.npoints + blockDim.x - 1) / blockDim.x;\n";
+    o << "    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {\n";
+    o << "        L.pt = tile * blockDim.x + threadIdx.x;\n        spec_body(R, L, k.npoints);\n    }\n}\n";
+    return o.str();
+}
+
+int spec_build(const CompiledGroup& cg, const std::string& csrc, const std::string& cache, SpecKernel* out,
+               std::string* err) {
+    const std::string src = spec_source(cg);
+    const uint64_t key = fnv1a(std::string(kFlags) + "\n" + src, headers_hash(csrc));
+    char hex[17];
+    snprintf(hex, sizeof(hex), "%016llx", (unsigned long long)key);
+    const std::string base = cache + "/spec_" + hex;
+    const std::string cubin = base + ".cubin";
+    struct stat stt;
+    if (stat(cubin.c_str(), &stt) != 0) {
+        mkdir(cache.c_str(), 0755);
+        const std::string cu = base + ".cu";
+        {
+            std::ofstream f(cu, std::ios::binary);
+            f << src;
+        }
+        const char* ch = getenv("CUDA_HOME");
+        const std::string nvcc = std::string(ch && *ch ? ch : "/usr/local/cuda") + "/bin/nvcc";
+        const std::string tmp = base + "." + std::to_string((long long)getpid()) + ".tmp";
+        const std::string cmd = nvcc + " " + kFlags + " -I" + csrc + " -o " + tmp + " " + cu + " > " + base +
+                                ".log 2>&1";
+        const int rc = std::system(cmd.c_str());
+        if (rc != 0 || stat(tmp.c_str(), &stt) != 0) {
+            if (err) *err = "specialized kernel build failed (" + cmd + "): " + read_file(base + ".log").substr(0, 2000);
+            return OSLG_ERR_LOWER;
+        }
+        if (std::rename(tmp.c_str(), cubin.c_str()) != 0) {
+            if (err) *err = "cannot place " + cubin;
+            return OSLG_ERR_LOWER;
+        }
+    }
+    cudaLibrary_t lib = nullptr;
+    if (!ok(cudaLibraryLoadFromFile(&lib, cubin.c_str(), nullptr, nullptr, 0, nullptr, nullptr, 0), err,
+            "load specialized kernel"))
+        return OSLG_ERR_CUDA;
+    cudaKernel_t kern = nullptr;
+    if (!ok(cudaLibraryGetKernel(&kern, lib, kKernelName), err, "specialized kernel lookup")) {
+        cudaLibraryUnload(lib);
+        return OSLG_ERR_CUDA;
+    }
+    out->library = lib;
+    out->kernel = kern;
+    out->key = hex;
+    const bool uses_cl = (cg.header.flags & 1u) != 0;
+    out->sym_slots = uses_cl ? cg.header.closure_base : cg.header.heap_slots;
+    out->pool_slots = uses_cl ? cg.header.heap_slots - cg.header.closure_base : 0;
+    return OSLG_OK;
+}
+
+int spec_launch(DeviceState& ds, const SpecKernel& sk, const CompiledGroup& cg, int64_t npoints,
+                const oslg_shaderglobals& G, void* userdata, void* outputs, void* stream, std::string* err) {
+    if (npoints <= 0) return OSLG_OK;
+    int rc = device_init(ds, err);
+    if (rc != OSLG_OK) return rc;
+    const void* fn = reinterpret_cast<const void*>(sk.kernel);
+    const int block = 256;
+    const size_t pool_bytes = (size_t)sk.pool_slots * block * sizeof(float);
+    int in_smem = pool_bytes > 0 && pool_bytes <= 100 * 1024 ? 1 : 0;
+    const size_t shmem = in_smem ? pool_bytes : 0;
+    if (shmem > 48 * 1024 &&
+        !ok(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shmem), err,
+            "specialized kernel attribute"))
+        return OSLG_ERR_CUDA;
+    const int64_t ntiles = (npoints + block - 1) / block;
+    int64_t grid = ntiles;
+    dev::KArgs k;
+    k.blob = static_cast<const uint8_t*>(cg.d_blob);
+    k.npoints = npoints;
+    k.userdata = static_cast<char*>(userdata);
+    k.outputs = static_cast<char*>(outputs);
+    k.status = ds.d_status;
+    k.G = G;
+    k.gheap = nullptr;
+    if (sk.pool_slots > 0 && !in_smem) {
+        int per_sm = 0;
+        if (!ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, block, 0), err, "occupancy"))
+            return OSLG_ERR_CUDA;
+        grid = std::min<int64_t>(ntiles, (int64_t)ds.sm_count * std::max(1, per_sm));
+        const size_t need = (size_t)grid * pool_bytes;
+        if (need > ds.gheap_bytes) {
+            if (ds.gheap) cudaFree(ds.gheap);
+            ds.gheap = nullptr;
+            ds.gheap_bytes = 0;
+            if (!ok(cudaMalloc(&ds.gheap, need), err, "cudaMalloc heap")) return OSLG_ERR_CUDA;
+            ds.gheap_bytes = need;
+        }
+        k.gheap = ds.gheap;
+    }
+    grid = std::min<int64_t>(grid, 0x7FFFFFFF);
+    void* args[] = { &k, &in_smem };
+    if (!ok(cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(block), args, shmem, static_cast<cudaStream_t>(stream)),
+            err, "specialized kernel launch"))
+        return OSLG_ERR_CUDA;
+    return OSLG_OK;
+}
+
+}  // namespace oslg

@@ -1,0 +1,44 @@
+// Per-group kernel specialization (oslg_spec.cpp).
+//
+// The reference JIT-compiles every optimized group to native code
+// (BatchedBackendLLVM, src/liboslexec/batched_backendllvm.cpp; jit_group,
+// src/liboslexec/shadingsys.cpp:4111-4181). The executor's counterpart
+// writes CUDA source for one lowered program — each op becomes a call of the
+// interpreter's own handler with its operand words as constants, control
+// flow becomes gotos between op labels, the constant pool becomes constant
+// memory — compiles it for sm_103a with nvcc, caches the cubin by content
+// hash and loads it with the CUDA library API. Symbol slots then live in a
+// thread-local array with constant indices (registers); only the closure
+// node pools, indexed at run time, keep a slot-major heap.
+#pragma once
+#include <cstdint>
+#include <string>
+
+#include "oslg_exec.h"
+#include "oslg_host.h"
+
+namespace oslg {
+
+struct SpecKernel {
+    void* library = nullptr;  // cudaLibrary_t
+    void* kernel = nullptr;   // cudaKernel_t
+    std::string key;          // content hash of the source
+    uint32_t sym_slots = 0;   // thread-local floats
+    uint32_t pool_slots = 0;  // closure-pool floats per point (slot-major heap)
+    ~SpecKernel();
+};
+
+// CUDA source of the specialized kernel for one lowered program.
+std::string spec_source(const CompiledGroup& cg);
+
+// Build (or take from the cache) and load the kernel. `csrc_dir` holds the
+// interpreter headers, `cache_dir` the generated sources and cubins.
+int spec_build(const CompiledGroup& cg, const std::string& csrc_dir, const std::string& cache_dir,
+               SpecKernel* out, std::string* err);
+
+// Launch over [0, npoints): one CTA of 256 points per tile, closure pools in
+// shared memory when they fit, else in the executor's HBM scratch.
+int spec_launch(DeviceState& ds, const SpecKernel& k, const CompiledGroup& cg, int64_t npoints,
+                const oslg_shaderglobals& G, void* userdata, void* outputs, void* stream, std::string* err);
+
+}  // namespace oslg

@@ -71,6 +71,20 @@ class ShaderGroup:
     def handle(self):
         return self._h
 
+    def specialized_source(self):
+        """CUDA source of the kernel specialized to this group."""
+        L = C.lib()
+        size = ctypes.c_size_t(0)
+        self._ss._check(L.oslg_group_specialized_source(self._ss._h, self._h, None, 0, ctypes.byref(size)))
+        buf = ctypes.create_string_buffer(size.value)
+        self._ss._check(L.oslg_group_specialized_source(self._ss._h, self._h, buf, size.value, ctypes.byref(size)))
+        return buf.value.decode()
+
+    def is_specialized(self):
+        out = ctypes.c_int(0)
+        self._ss._check(C.lib().oslg_group_is_specialized(self._ss._h, self._h, ctypes.byref(out)))
+        return bool(out.value)
+
     def program_bytes(self):
         """The lowered op program (what replaces the JIT'd module)."""
         L = C.lib()
