@@ -380,6 +380,8 @@ def main():
                     help="skip the 64-group batching, serving and wavefront measurements")
     ap.add_argument("--jit", type=int, default=0,
                     help="1: run the group's specialized kernel (attribute jit), 0: the interpreter")
+    ap.add_argument("--jit-block", type=int, default=0, help="specialized launch: threads per CTA")
+    ap.add_argument("--jit-pool-smem", type=int, default=-1, help="specialized launch: closure pools in smem (1/0)")
     ap.add_argument("--section", choices=["batching", "serving", "wavefront"],
                     help="run only this measurement section and print it as one JSON line")
     ap.add_argument("--wf-size", default=None, help="wavefront frame WxHxSPP (default 1920x1080x4)")
@@ -449,6 +451,10 @@ def main():
     wl.build(torch, og, shaders)
     if args.jit:
         wl.ss.attribute("jit", 1)  # the first launch (warm-up) builds and loads the kernel
+        if args.jit_block:
+            wl.ss.attribute("jit_block", args.jit_block)
+        if args.jit_pool_smem >= 0:
+            wl.ss.attribute("jit_pool_smem", args.jit_pool_smem)
     stream = torch.cuda.current_stream()
     sh = stream.cuda_stream
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")

@@ -108,7 +108,9 @@ int oslg_destroy_system(oslg_system* sys);
  * "gpu_block", "gpu_points_per_thread", "gpu_heap_placement" (0 HBM, 1 smem,
  * -1 auto), "debug", "jit" (1: optimize builds a kernel specialized to the
  * group, see oslg_group_specialized_source; the counterpart of the
- * reference's per-group JIT). */
+ * reference's per-group JIT), "jit_block" (64/128/256 threads per CTA of a
+ * specialized launch), "jit_pool_smem" (closure pools in shared memory 1,
+ * HBM scratch 0, automatic -1). */
 int oslg_attribute_int(oslg_system* sys, const char* name, int value);
 /* ShadingSystem::register_closure (oslexec.h:1041). Parameters are taken
  * positionally from the `closure` op's arguments. */

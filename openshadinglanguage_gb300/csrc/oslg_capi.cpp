@@ -24,6 +24,8 @@ struct oslg_system {
     oslg::DeviceState dev;
     oslg::LaunchConfig launch;
     int jit = 0;  // build a specialized kernel per group at optimize time
+    int jit_block = 0;       // specialized launch: threads per CTA (0: 256)
+    int jit_pool_smem = -1;  // closure pools: 1 shared memory, 0 HBM, -1 shared when it fits
     std::string err;
     std::vector<oslg::InstanceParam> pending_params;  // Parameter() before Shader()
 };
@@ -160,6 +162,8 @@ int oslg_attribute_int(oslg_system* sys, const char* name, int value) {
     else if (n == "gpu_grid") sys->launch.grid = value;
     else if (n == "debug") sys->ss.opts.debug = value;
     else if (n == "jit") sys->jit = value;
+    else if (n == "jit_block") sys->jit_block = value;
+    else if (n == "jit_pool_smem") sys->jit_pool_smem = value;
     else return fail(sys, OSLG_ERR_ARG, "unknown attribute '" + n + "'");
     if (sys->ss.opts.max_closure_terms > 0xFFFF || sys->ss.opts.max_closure_components > 0xFFFF)
         return fail(sys, OSLG_ERR_ARG, "closure pool capacity must stay below 65536");
@@ -423,7 +427,8 @@ int oslg_execute_batch(oslg_system* sys, oslg_group* group, int64_t npoints, con
         std::string err;
         const CompiledGroup& cg = *group->g.compiled;
         if (cg.spec)
-            rc = spec_launch(sys->dev, *cg.spec, cg, npoints, *globals, userdata_base, output_base, stream, &err);
+            rc = spec_launch(sys->dev, *cg.spec, cg, npoints, *globals, userdata_base, output_base, stream, &err,
+                             sys->jit_block, sys->jit_pool_smem);
         else
             rc = device_execute(sys->dev, cg.header, cg.d_blob, npoints, *globals, userdata_base, output_base,
                                 stream, sys->launch, &err);

@@ -39,6 +39,26 @@ namespace dev {
 // blackbody / closure helpers live further down
 static const unsigned FULL = 0xFFFFFFFFu;
 
+// Capacities of the closure walk stack and of the BSDF lobe list. A
+// specialized kernel whose program has no loops defines smaller bounds that
+// its closure ops cannot exceed (walk depth <= ADD ops, lobes <= 2^ADD ops),
+// and indexes these arrays with compile-time indices (OSLG_FIXED_INDEX) so
+// that they stay in registers; results are the same as with the defaults.
+// Component loops whose trip count is a per-op constant: a specialized
+// kernel unrolls them so that symbol indices are compile-time constants
+// (its symbol array then stays in registers).
+#ifdef OSLG_SPEC
+#define OSLG_SPEC_UNROLL _Pragma("unroll")
+#else
+#define OSLG_SPEC_UNROLL
+#endif
+#ifndef OSLG_WALK_STACK
+#define OSLG_WALK_STACK kClosureWalkStack
+#endif
+#ifndef OSLG_LOBES_MAX
+#define OSLG_LOBES_MAX kBsdfMaxLobes
+#endif
+
 // KArgs: see oslg_exec.h
 
 struct Lane {
@@ -180,7 +200,9 @@ static __device__ void h_assign(const Lane& L, const uint32_t* a, uint32_t* st) 
     if (ralen < 1) ralen = 1;
     if (salen < 1) salen = 1;
     int nr = anc(r), ns = anc(s);
+    OSLG_SPEC_UNROLL
     for (int e = 0; e < count; ++e) {
+        OSLG_SPEC_UNROLL
         for (int c = 0; c < nr; ++c) {
             int sc = ns == 1 ? 0 : c;
             uint32_t sw = ldw(L, s, e * ns + sc);
@@ -318,6 +340,7 @@ __device__ __forceinline__ void h_assign_fast(const Lane& L, const uint32_t* a, 
     Opd R = dec(L, r), S = dec(L, s);
     int nc = anc(r);
     bool rd = ader(r);
+    OSLG_SPEC_UNROLL
     for (int c = 0; c < nc; ++c) {
         sv(R, c, gv(S, c));
         if (rd) { sd(R, c, 1, gd(S, c, 1)); sd(R, c, 2, gd(S, c, 2)); }
@@ -331,6 +354,7 @@ static __device__ void h_arith(const Lane& L, const uint32_t* a) {
     uint32_t r = a[0], x = a[1], y = a[2];
     int nc = anc(r);
     bool rd = ader(r), xd = ader(x), yd = ader(y);
+    OSLG_SPEC_UNROLL
     for (int c = 0; c < nc; ++c) {
         float xv = ldf(L, x, c, 0), yv = ldf(L, y, c, 0);
         float v;
@@ -421,6 +445,7 @@ static __device__ void h_cmp(const Lane& L, const uint32_t* a) {
         else if (K == 3) res = xi > yi; else if (K == 4) res = xi <= yi; else res = xi >= yi;
     } else if (K == 0 || K == 1) {
         bool eq = true;
+        OSLG_SPEC_UNROLL
         for (int c = 0; c < n; ++c) eq = eq && (ldf(L, x, c, 0) == ldf(L, y, c, 0));
         res = K == 0 ? eq : !eq;
     } else {
@@ -443,6 +468,7 @@ static __device__ void h_unary(const Lane& L, const uint32_t* a) {
     uint32_t r = a[0], x = a[1];
     int nc = anc(r);
     bool rd = ader(r);
+    OSLG_SPEC_UNROLL
     for (int c = 0; c < nc; ++c) {
         float v = ldf(L, x, c, 0);
         float f, df = 0.0f;
@@ -515,6 +541,7 @@ static __device__ void h_binary(const Lane& L, const uint32_t* a) {
     uint32_t r = a[0], x = a[1], y = a[2];
     int nc = anc(r);
     bool rd = ader(r);
+    OSLG_SPEC_UNROLL
     for (int c = 0; c < nc; ++c) {
         D2 u = ldd(L, x, c), v = ldd(L, y, c);
         D2 res;
@@ -550,6 +577,7 @@ static __device__ void h_binary(const Lane& L, const uint32_t* a) {
 static __device__ void h_clamp(const Lane& L, const uint32_t* a) {
     uint32_t r = a[0];
     int nc = anc(r);
+    OSLG_SPEC_UNROLL
     for (int c = 0; c < nc; ++c) {
         D2 x = ldd(L, a[1], c), lo = ldd(L, a[2], c), hi = ldd(L, a[3], c);
         if (atc(r) == TC_INT) {
@@ -568,6 +596,7 @@ static __device__ void h_clamp(const Lane& L, const uint32_t* a) {
 static __device__ void h_mix(const Lane& L, const uint32_t* a) {
     uint32_t r = a[0];
     int nc = anc(r);
+    OSLG_SPEC_UNROLL
     for (int c = 0; c < nc; ++c) {
         D2 x = ldd(L, a[1], c), y = ldd(L, a[2], c), t = ldd(L, a[3], c);
         float one_t = 1.0f - t.v;
@@ -581,6 +610,7 @@ static __device__ void h_mix(const Lane& L, const uint32_t* a) {
 static __device__ void h_smoothstep(const Lane& L, const uint32_t* a) {
     uint32_t r = a[0];
     int nc = anc(r);
+    OSLG_SPEC_UNROLL
     for (int c = 0; c < nc; ++c) {
         D2 e0 = ldd(L, a[1], c), e1 = ldd(L, a[2], c), x = ldd(L, a[3], c);
         D2 res;
@@ -604,6 +634,7 @@ static __device__ void h_smoothstep(const Lane& L, const uint32_t* a) {
 static __device__ void h_select(const Lane& L, const uint32_t* a) {
     uint32_t r = a[0];
     int nc = anc(r);
+    OSLG_SPEC_UNROLL
     for (int c = 0; c < nc; ++c) {
         bool cond = atc(a[3]) == TC_TRIPLE ? ldf(L, a[3], c, 0) != 0.0f : truth(L, a[3]);
         D2 v = cond ? ldd(L, a[2], c) : ldd(L, a[1], c);
@@ -717,6 +748,7 @@ static __device__ void h_transform(const Lane& L, const uint32_t* a) {
     // vector (multDirMatrix on value and each partial)
     float in[3][3] = { { x.v, y.v, z.v }, { x.dx, y.dx, z.dx }, { x.dy, y.dy, z.dy } };
     int nd = ader(r) ? 3 : 1;
+    OSLG_SPEC_UNROLL
     for (int d = 0; d < nd; ++d) {
         float X = in[d][0], Y = in[d][1], Z = in[d][2];
         float o0 = X * M[0] + Y * M[4] + Z * M[8];
@@ -818,6 +850,7 @@ static __device__ void h_transformn(const Lane& L, const uint32_t* a) {
     for (int i = 0; i < 4; ++i)
         for (int j = 0; j < 4; ++j) T[i * 4 + j] = Mi[j * 4 + i];
     const int nd = ader(r) ? 3 : 1;
+    OSLG_SPEC_UNROLL
     for (int d = 0; d < nd; ++d) {
         const float X = ldf(L, p, 0, d), Y = ldf(L, p, 1, d), Z = ldf(L, p, 2, d);
         stf(L, r, d * 3 + 0, X * T[0] + Y * T[4] + Z * T[8]);
@@ -849,6 +882,7 @@ static __device__ void h_deriv_misc(const Lane& L, uint32_t code, const uint32_t
         stval(L, r, 0, vlen_imath(vcross(dx, dy)));
     } else {
         const int n = anc(x);
+        OSLG_SPEC_UNROLL
         for (int c = 0; c < n; ++c) {
             const float dx = ldf(L, x, c, 1), dy = ldf(L, x, c, 2);
             stval(L, r, c, sqrtf(dx * dx + dy * dy));
@@ -862,6 +896,7 @@ static __device__ void h_luminance(const Lane& L, const uint32_t* a) {
     const uint32_t r = a[0], c = a[1], s = a[2];
     const float sx = ldf(L, s, 0, 0), sy = ldf(L, s, 1, 0), sz = ldf(L, s, 2, 0);
     const int nd = ader(r) ? 3 : 1;
+    OSLG_SPEC_UNROLL
     for (int d = 0; d < nd; ++d)
         stf(L, r, d, ldf(L, c, 0, d) * sx + ldf(L, c, 1, d) * sy + ldf(L, c, 2, d) * sz);
 }
@@ -956,6 +991,7 @@ static __device__ void h_gabor(const Lane& L, const uint32_t* a, const uint32_t*
     D2 res[3];
     gabor_eval(o, X, periodic, period, nc, res);
     const int rn = anc(r);
+    OSLG_SPEC_UNROLL
     for (int c = 0; c < rn; ++c) {
         const D2 v = res[nc == 1 ? 0 : c];
         stf(L, r, c, v.v);
@@ -991,6 +1027,7 @@ static __device__ void h_noise(const Lane& L, const uint32_t* a) {
     }
     if (kind == NK_CELL || kind == NK_HASH) {
         float xs[4];
+        OSLG_SPEC_UNROLL
         for (int i = 0; i < ns; ++i) xs[i] = ldf(L, S, i, 0);
         if (T != kNoArg) xs[ns] = ldf(L, T, 0, 0);
         if (periodic) {
@@ -1007,6 +1044,7 @@ static __device__ void h_noise(const Lane& L, const uint32_t* a) {
     } else if (kind == NK_PERLIN || kind == NK_UPERLIN) {
         if (derivs) {
             D2 xs[4];
+            OSLG_SPEC_UNROLL
             for (int i = 0; i < ns; ++i) xs[i] = ldd(L, S, i);
             if (T != kNoArg) xs[ns] = ldd(L, T, 0);
             D2 o[3];
@@ -1025,12 +1063,14 @@ static __device__ void h_noise(const Lane& L, const uint32_t* a) {
                 default: perlin4<D2, 1>(H, xs[0], xs[1], xs[2], xs[3], o); break;
                 }
             }
+            OSLG_SPEC_UNROLL
             for (int c = 0; c < nc; ++c) {
                 if (kind == NK_UPERLIN) o[c] = (o[c] + 1.0f) * 0.5f;
                 res[c] = o[c].v; rdx[c] = o[c].dx; rdy[c] = o[c].dy;
             }
         } else {
             float xs[4];
+            OSLG_SPEC_UNROLL
             for (int i = 0; i < ns; ++i) xs[i] = ldf(L, S, i, 0);
             if (T != kNoArg) xs[ns] = ldf(L, T, 0, 0);
             if (vec) {
@@ -1049,12 +1089,15 @@ static __device__ void h_noise(const Lane& L, const uint32_t* a) {
                 }
             }
             if (kind == NK_UPERLIN)
+                OSLG_SPEC_UNROLL
                 for (int c = 0; c < nc; ++c) res[c] = 0.5f * (res[c] + 1.0f);
         }
     } else if (kind == NK_SIMPLEX || kind == NK_USIMPLEX) {
         D2 xs[4];
+        OSLG_SPEC_UNROLL
         for (int i = 0; i < ns; ++i) xs[i] = ldd(L, S, i);
         if (T != kNoArg) xs[ns] = ldd(L, T, 0);
+        OSLG_SPEC_UNROLL
         for (int c = 0; c < nc; ++c) {
             float g[4] = { 0, 0, 0, 0 };
             float v;
@@ -1074,13 +1117,16 @@ static __device__ void h_noise(const Lane& L, const uint32_t* a) {
             res[c] = o.v; rdx[c] = o.dx; rdy[c] = o.dy;
         }
     } else if (kind == NK_NULL || kind == NK_UNULL) {
+        OSLG_SPEC_UNROLL
         for (int c = 0; c < nc; ++c) res[c] = kind == NK_UNULL ? 0.5f : 0.0f;
     } else {
+        OSLG_SPEC_UNROLL
         for (int c = 0; c < nc; ++c) res[c] = 0.0f;
     }
     // float result from triple request or vice versa is handled by lowering;
     // scalar noise into a triple symbol broadcasts
     int rn = anc(r);
+    OSLG_SPEC_UNROLL
     for (int c = 0; c < rn; ++c) {
         int sc = nc == 1 ? 0 : c;
         stf(L, r, c, res[sc]);
@@ -1130,6 +1176,7 @@ static __device__ void h_load_global(const Lane& L, const uint32_t* a, const osl
     int id = (int)a[1];
     int nc = anc(r);
     const oslg_field& f = gfield(G, id);
+    OSLG_SPEC_UNROLL
     for (int c = 0; c < nc; ++c) stf(L, r, c, fld(f, c, L.pt));
     if (ader(r)) {
         int dxid = -1, dyid = -1;
@@ -1138,6 +1185,7 @@ static __device__ void h_load_global(const Lane& L, const uint32_t* a, const osl
         else if (id == G_U) { dxid = G_DUDX; dyid = G_DUDY; }
         else if (id == G_V) { dxid = G_DVDX; dyid = G_DVDY; }
         else if (id == G_PS) { dxid = G_DPSDX; dyid = G_DPSDY; }
+        OSLG_SPEC_UNROLL
         for (int c = 0; c < nc; ++c) {
             stf(L, r, nc + c, dxid >= 0 ? fld(gfield(G, dxid), c, L.pt) : 0.0f);
             stf(L, r, 2 * nc + c, dyid >= 0 ? fld(gfield(G, dyid), c, L.pt) : 0.0f);
@@ -1163,7 +1211,9 @@ static __device__ void h_store_output(const Lane& L, const uint32_t* a, char* ba
     char* p = base + (int64_t)a[1] + L.pt * (int64_t)(int32_t)a[2];
     int total = nc * elems;
     int nd = (flags & 1u) ? 3 : 1;
+    OSLG_SPEC_UNROLL
     for (int d = 0; d < nd; ++d)
+        OSLG_SPEC_UNROLL
         for (int i = 0; i < total; ++i) {
             uint32_t w;
             if (d > 0 && !ader(s)) w = 0u;
@@ -1193,6 +1243,7 @@ static __device__ void h_aref(const Lane& L, const uint32_t* a, uint32_t* st) {
     int i = ldi(L, a[2], 0);
     if (i < 0 || i >= alen) { raise_status(st, ST_ARRAY_BOUNDS); i = i < 0 ? 0 : alen - 1; }
     int nc = anc(arr);
+    OSLG_SPEC_UNROLL
     for (int c = 0; c < nc; ++c) {
         uint32_t w = ldw(L, arr, i * nc + c);
         if (atc(r) == TC_INT || atc(r) == TC_STRING || atc(r) == TC_CLOSURE) { stw(L, r, c, w); continue; }
@@ -1215,6 +1266,7 @@ static __device__ void h_aassign(const Lane& L, const uint32_t* a, uint32_t* st)
     int i = ldi(L, a[1], 0);
     if (i < 0 || i >= alen) { raise_status(st, ST_ARRAY_BOUNDS); i = i < 0 ? 0 : alen - 1; }
     int nc = anc(arr);
+    OSLG_SPEC_UNROLL
     for (int c = 0; c < nc; ++c) {
         int vc = anc(v) == 1 ? 0 : c;
         if (atc(arr) == TC_INT || atc(arr) == TC_STRING || atc(arr) == TC_CLOSURE) {
@@ -1273,13 +1325,20 @@ static __device__ void h_closure(const Lane& L, const uint32_t* a, const uint32_
     if (extra)
         for (int i = 0; i < 7; ++i) params[np++] = extra[i];
     int k = 0;
-    for (int i = 0; i < np && k < kClosureParamFloats; ++i) {
+    // fixed trip counts with early exits (a specialized kernel unrolls them
+    // into constant operand indices)
+    OSLG_SPEC_UNROLL
+    for (int i = 0; i < 11; ++i) {
+        if (i >= np || k >= kClosureParamFloats) break;
         uint32_t p = params[i];
         if (p == kNoArg) break;
         int nc = anc(p);
         uint32_t t = atc(p);
-        for (int c = 0; c < nc && k < kClosureParamFloats; ++c)
+        OSLG_SPEC_UNROLL
+        for (int c = 0; c < 16; ++c) {
+            if (c >= nc || k >= kClosureParamFloats) break;
             hsetu(L, ns + 4 + k++, (t == TC_INT || t == TC_STRING) ? ldw(L, p, c) : __float_as_uint(ldf(L, p, c, 0)));
+        }
     }
     for (; k < kClosureParamFloats; ++k) hset(L, ns + 4 + k, 0.0f);
     stw(L, a[0], 0, h);
@@ -1318,8 +1377,8 @@ static __device__ void h_closure_add(const Lane& L, const uint32_t* a, const Clo
 // components in order with the accumulated weight weight*comp.w.
 template <class F>
 __device__ void closure_walk(const Lane& L, const ClosurePools& P, uint32_t root, uint32_t* st, F&& visit) {
-    uint32_t stack_node[kClosureWalkStack];
-    float stack_w[kClosureWalkStack][3];
+    uint32_t stack_node[OSLG_WALK_STACK];
+    float stack_w[OSLG_WALK_STACK][3];
     int sp = 0;
     float w[3] = { 1.0f, 1.0f, 1.0f };
     uint32_t cur = root;
@@ -1332,9 +1391,19 @@ __device__ void closure_walk(const Lane& L, const ClosurePools& P, uint32_t root
             for (int k = 0; k < 3; ++k) w[k] = w[k] * hget(L, ns + 1 + k);
             cur = hgetu(L, ns + 4);
         } else if (id == kClosureAdd) {
-            if (sp < kClosureWalkStack) {
-                stack_node[sp] = hgetu(L, ns + 5);
+            if (sp < OSLG_WALK_STACK) {
+                const uint32_t right = hgetu(L, ns + 5);
+#ifdef OSLG_FIXED_INDEX
+#pragma unroll
+                for (int j = 0; j < OSLG_WALK_STACK; ++j)
+                    if (j == sp) {
+                        stack_node[j] = right;
+                        for (int k = 0; k < 3; ++k) stack_w[j][k] = w[k];
+                    }
+#else
+                stack_node[sp] = right;
                 for (int k = 0; k < 3; ++k) stack_w[sp][k] = w[k];
+#endif
                 ++sp;
             } else {
                 raise_status(st, ST_CLOSURE_OVERFLOW);
@@ -1348,8 +1417,17 @@ __device__ void closure_walk(const Lane& L, const ClosurePools& P, uint32_t root
         }
         if (cur == 0u && sp > 0) {
             --sp;
+#ifdef OSLG_FIXED_INDEX
+#pragma unroll
+            for (int j = 0; j < OSLG_WALK_STACK; ++j)
+                if (j == sp) {
+                    cur = stack_node[j];
+                    for (int k = 0; k < 3; ++k) w[k] = stack_w[j][k];
+                }
+#else
             cur = stack_node[sp];
             for (int k = 0; k < 3; ++k) w[k] = stack_w[sp][k];
+#endif
         }
     }
 }
@@ -1378,12 +1456,19 @@ static __device__ void h_store_closure(const Lane& L, const uint32_t* a, char* b
 // parameters stay in the heap (node params) and are read when used.
 struct Lobes {
     int n;
-    int kind[kBsdfMaxLobes];  // 0 diffuse, 1 ggx, 2 oren-nayar
-    float w[kBsdfMaxLobes][3];
-    float pdf[kBsdfMaxLobes];
-    uint32_t p[kBsdfMaxLobes];
+    int kind[OSLG_LOBES_MAX];  // 0 diffuse, 1 ggx, 2 oren-nayar
+    float w[OSLG_LOBES_MAX][3];
+    float pdf[OSLG_LOBES_MAX];
+    uint32_t p[OSLG_LOBES_MAX];
     float Le[3];
 };
+// Loops over the lobe list: unrolled over the capacity (constant indices)
+// in a fixed-index build, a plain loop over n otherwise.
+#ifdef OSLG_FIXED_INDEX
+#define OSLG_FOR_LOBES(i, B) _Pragma("unroll") for (int i = 0; i < OSLG_LOBES_MAX; ++i) if (i < (B).n)
+#else
+#define OSLG_FOR_LOBES(i, B) for (int i = 0; i < (B).n; ++i)
+#endif
 __device__ __forceinline__ void lobes_build(const Lane& L, const ClosurePools& P, uint32_t root, uint32_t ggx,
                                             uint32_t* st, Lobes& B) {
     B.n = 0;
@@ -1400,10 +1485,20 @@ __device__ __forceinline__ void lobes_build(const Lane& L, const ClosurePools& P
             const int r = (int)hgetu(L, params + 10);
             if (r >= 0 && r <= 2) k = 1;
         }
-        if (k < 0 || B.n >= kBsdfMaxLobes) return;
+        if (k < 0 || B.n >= OSLG_LOBES_MAX) return;
+#ifdef OSLG_FIXED_INDEX
+#pragma unroll
+        for (int j = 0; j < OSLG_LOBES_MAX; ++j)
+            if (j == B.n) {
+                B.kind[j] = k;
+                for (int c = 0; c < 3; ++c) B.w[j][c] = cw[c];
+                B.p[j] = params;
+            }
+#else
         B.kind[B.n] = k;
         for (int c = 0; c < 3; ++c) B.w[B.n][c] = cw[c];
         B.p[B.n] = params;
+#endif
         ++B.n;
     });
 }
@@ -1448,7 +1543,7 @@ __device__ __forceinline__ BsdfSample lobe_sample(const Lane& L, const Lobes& B,
 // CompositeBSDF::prepare (shading.h:322-350)
 __device__ __forceinline__ void lobes_prepare(const Lane& L, Lobes& B, V3 wo, const float* pw, bool absorb) {
     float total = 0.0f;
-    for (int i = 0; i < B.n; ++i) {
+    OSLG_FOR_LOBES(i, B) {
         float alb = 1.0f;
         if (B.kind[i] == 1) {
             const uint32_t p = B.p[i];
@@ -1460,12 +1555,12 @@ __device__ __forceinline__ void lobes_prepare(const Lane& L, Lobes& B, V3 wo, co
         total += B.pdf[i];
     }
     if ((!absorb && total > 0.0f) || total > 1.0f)
-        for (int i = 0; i < B.n; ++i) B.pdf[i] /= total;
+        OSLG_FOR_LOBES(i, B) B.pdf[i] /= total;
 }
 // CompositeBSDF::eval (shading.h:360-370)
 __device__ __forceinline__ BsdfSample lobes_eval(const Lane& L, const Lobes& B, V3 wo, V3 wi) {
     BsdfSample r = bsdf_zero();
-    for (int i = 0; i < B.n; ++i) {
+    OSLG_FOR_LOBES(i, B) {
         BsdfSample b = lobe_eval(L, B, i, wo, wi);
         for (int c = 0; c < 3; ++c) b.w[c] *= B.w[i][c];
         mis_update_eval(r.w, &r.pdf, b.w, b.pdf, B.pdf[i]);
@@ -1476,7 +1571,7 @@ __device__ __forceinline__ BsdfSample lobes_eval(const Lane& L, const Lobes& B, 
 // CompositeBSDF::sample (shading.h:372-398)
 __device__ __forceinline__ BsdfSample lobes_sample(const Lane& L, const Lobes& B, V3 wo, float rx, float ry, float rz) {
     float accum = 0.0f;
-    for (int i = 0; i < B.n; ++i) {
+    OSLG_FOR_LOBES(i, B) {
         if (rx < (B.pdf[i] + accum)) {
             rx = (rx - accum) / B.pdf[i];
             rx = fminf(rx, 0.99999994f);
@@ -1485,7 +1580,7 @@ __device__ __forceinline__ BsdfSample lobes_sample(const Lane& L, const Lobes& B
             for (int c = 0; c < 3; ++c) s.w[c] *= B.w[i][c] * inv;
             s.pdf *= B.pdf[i];
             if (s.pdf == 0.0f) return bsdf_zero();
-            for (int j = 0; j < B.n; ++j) {
+            OSLG_FOR_LOBES(j, B) {
                 if (i != j) {
                     BsdfSample b = lobe_eval(L, B, j, wo, s.wi);
                     for (int c = 0; c < 3; ++c) b.w[c] *= B.w[j][c];
@@ -1554,11 +1649,13 @@ static __device__ void h_spline(const Lane& L, const uint32_t* a) {
     if (segnum < 0) segnum = 0;
     if (segnum > nsegs - 1) segnum = nsegs - 1;
     if (a[3] == 5u) {  // constant basis
+        OSLG_SPEC_UNROLL
         for (int c = 0; c < nc; ++c) stval(L, r, c, __uint_as_float(ldw(L, kn, (segnum + 1) * kc + (kc == 1 ? 0 : c))));
         return;
     }
     x = x - (float)segnum;
     int s = segnum * B.step;
+    OSLG_SPEC_UNROLL
     for (int c = 0; c < nc; ++c) {
         int cc = kc == 1 ? 0 : c;
         D2 P[4];
@@ -1889,6 +1986,7 @@ __device__ __forceinline__ void exec_op(const RunCtx& R, Lane& L, uint32_t code,
     case OP_DY: {
         int d = code == OP_DX ? 1 : 2;
         int nc = anc(a[0]);
+        OSLG_SPEC_UNROLL
         for (int c = 0; c < nc; ++c) stval(L, a[0], c, ldf(L, a[1], c, d));
         break;
     }

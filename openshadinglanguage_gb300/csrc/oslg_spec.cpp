@@ -97,10 +97,25 @@ std::string spec_source(const CompiledGroup& cg) {
     for (int i = 0; i < n; ++i)
         if (jump_op(ops[i].code) && ops[i].a[2] <= (uint32_t)n) target[ops[i].a[2]] = 1;
 
+    // Loop-free programs execute each closure op at most once per point, so
+    // the closure walk is at most (ADD ops) deep and finds at most 2^(ADD ops)
+    // leaves: those bounds replace the reference capacities (16, 8).
+    bool loops = false;
+    int adds = 0;
+    for (int i = 0; i < n; ++i) {
+        loops = loops || ops[i].code == OP_LOOP_BEGIN || ops[i].code == OP_JUMP;
+        adds += ops[i].code == OP_CLOSURE_ADD;
+    }
     std::ostringstream o;
     o << "// generated: kernel specialized to one lowered program (" << n << " ops, " << sym
       << " symbol slots, " << cpool << " closure-pool slots)\n";
-    o << "#define OSLG_SPEC 1\n#include \"oslg_interp.cuh\"\n\nnamespace {\n";
+    o << "#define OSLG_SPEC 1\n";
+    if (uses_cl && !loops) {
+        o << "#define OSLG_FIXED_INDEX 1\n";
+        o << "#define OSLG_WALK_STACK " << std::max(1, std::min(adds, (int)kClosureWalkStack)) << "\n";
+        o << "#define OSLG_LOBES_MAX " << std::min((int)kBsdfMaxLobes, 1 << std::min(adds, 3)) << "\n";
+    }
+    o << "#include \"oslg_interp.cuh\"\n\nnamespace {\n";
     o << "using namespace oslg;\nusing namespace oslg::dev;\n\n";
     o << "__constant__ const uint32_t kPool[" << std::max(1u, h.nconst) << "] = {";
     for (uint32_t i = 0; i < h.nconst; ++i) o << (i ? ", " : "") << pool[i] << "u";
@@ -222,14 +237,17 @@ int spec_build(const CompiledGroup& cg, const std::string& csrc, const std::stri
 }
 
 int spec_launch(DeviceState& ds, const SpecKernel& sk, const CompiledGroup& cg, int64_t npoints,
-                const oslg_shaderglobals& G, void* userdata, void* outputs, void* stream, std::string* err) {
+                const oslg_shaderglobals& G, void* userdata, void* outputs, void* stream, std::string* err,
+                int block_req, int pool_req) {
     if (npoints <= 0) return OSLG_OK;
     int rc = device_init(ds, err);
     if (rc != OSLG_OK) return rc;
     const void* fn = reinterpret_cast<const void*>(sk.kernel);
-    const int block = 256;
+    const int block = block_req == 128 || block_req == 64 ? block_req : 256;
     const size_t pool_bytes = (size_t)sk.pool_slots * block * sizeof(float);
     int in_smem = pool_bytes > 0 && pool_bytes <= 100 * 1024 ? 1 : 0;
+    if (pool_req == 0) in_smem = 0;
+    if (pool_req == 1 && pool_bytes > 0 && pool_bytes + 1024 <= ds.smem_optin) in_smem = 1;
     const size_t shmem = in_smem ? pool_bytes : 0;
     if (shmem > 48 * 1024 &&
         !ok(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shmem), err,
