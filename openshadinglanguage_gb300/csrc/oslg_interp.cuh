@@ -77,6 +77,21 @@ struct Lane {
 #endif
 };
 
+// Output-arena stores. A specialized kernel that stages a tile's output
+// records in shared memory (OSLG_STAGE_STRIDE = record bytes) marks each
+// written word, so that only written words are copied out.
+#ifdef OSLG_STAGE_STRIDE
+extern __shared__ __align__(16) unsigned char oslg_smem[];
+__device__ __forceinline__ void ostore32(void* p, uint32_t w) {
+    *reinterpret_cast<uint32_t*>(p) = w;
+    const size_t word = (size_t)(reinterpret_cast<unsigned char*>(p) - oslg_smem) >> 2;
+    oslg_smem[(size_t)blockDim.x * OSLG_STAGE_STRIDE + word] = 1;
+}
+#else
+__device__ __forceinline__ void ostore32(void* p, uint32_t w) { *reinterpret_cast<uint32_t*>(p) = w; }
+#endif
+__device__ __forceinline__ void ostoref(void* p, float v) { ostore32(p, __float_as_uint(v)); }
+
 __device__ __forceinline__ uint32_t aoff(uint32_t a) { return a & kArgOffsetMask; }
 __device__ __forceinline__ bool aconst(uint32_t a) { return (a & kArgConst) != 0; }
 __device__ __forceinline__ bool ader(uint32_t a) { return (a & kArgDerivs) != 0; }
@@ -1220,7 +1235,7 @@ static __device__ void h_store_output(const Lane& L, const uint32_t* a, char* ba
             else if (flags & 2u) w = (uint32_t)ldi(L, s, i);
             else w = ldw(L, s, d * total + i);
             if (!(flags & 2u) && atc(s) == TC_INT) w = __float_as_uint((float)(int)w);
-            reinterpret_cast<uint32_t*>(p)[d * total + i] = w;
+            ostore32(reinterpret_cast<uint32_t*>(p) + d * total + i, w);
         }
 }
 
@@ -1440,12 +1455,12 @@ static __device__ void h_store_closure(const Lane& L, const uint32_t* a, char* b
     closure_walk(L, P, root, st, [&](int id, const float* cw, uint32_t params) {
         if (n >= maxc) return;
         uint32_t* q = o + 1 + n * kNodeFloats;
-        q[0] = (uint32_t)id;
-        for (int k = 0; k < 3; ++k) q[1 + k] = __float_as_uint(cw[k]);
-        for (int k = 0; k < kClosureParamFloats; ++k) q[4 + k] = hgetu(L, params + k);
+        ostore32(q, (uint32_t)id);
+        for (int k = 0; k < 3; ++k) ostore32(q + 1 + k, __float_as_uint(cw[k]));
+        for (int k = 0; k < kClosureParamFloats; ++k) ostore32(q + 4 + k, hgetu(L, params + k));
         ++n;
     });
-    o[0] = n;
+    ostore32(o, n);
 }
 
 // CompositeBSDF::prepare + eval (shading.h:322-374) over the lobes the walk
@@ -1606,7 +1621,10 @@ static __device__ void h_bsdf_eval(const Lane& L, const uint32_t* a, char* base,
     lobes_prepare(L, B, wo, one, false);
     const BsdfSample r = lobes_eval(L, B, wo, wi);
     float* o = reinterpret_cast<float*>(base + (int64_t)a[1] + L.pt * (int64_t)(int32_t)a[2]);
-    o[0] = r.w[0]; o[1] = r.w[1]; o[2] = r.w[2]; o[3] = r.pdf;
+    ostoref(o + 0, r.w[0]);
+    ostoref(o + 1, r.w[1]);
+    ostoref(o + 2, r.w[2]);
+    ostoref(o + 3, r.pdf);
 }
 
 // Renderer-side sampling of a closure output, the per-hit step of
@@ -1623,11 +1641,10 @@ static __device__ void h_bsdf_sample(const Lane& L, const uint32_t* a, char* bas
     lobes_prepare(L, B, wo, pw, in[6] != 0.0f);
     const BsdfSample r = lobes_sample(L, B, wo, in[0], in[1], in[2]);
     float* o = reinterpret_cast<float*>(base + (int64_t)a[1] + L.pt * (int64_t)(int32_t)a[2]);
-    o[0] = r.wi.x; o[1] = r.wi.y; o[2] = r.wi.z;
-    o[3] = r.w[0]; o[4] = r.w[1]; o[5] = r.w[2];
-    o[6] = r.pdf;
-    o[7] = B.Le[0]; o[8] = B.Le[1]; o[9] = B.Le[2];
-    o[10] = r.roughness;
+    const float vals[11] = { r.wi.x, r.wi.y, r.wi.z, r.w[0], r.w[1], r.w[2], r.pdf, B.Le[0], B.Le[1], B.Le[2],
+                             r.roughness };
+#pragma unroll
+    for (int k = 0; k < 11; ++k) ostoref(o + k, vals[k]);
 }
 
 // ---- spline (splineimpl.h:191-239) -----------------------------------------------------

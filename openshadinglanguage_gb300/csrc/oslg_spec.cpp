@@ -72,6 +72,40 @@ const char* kFlags = "-cubin -gencode arch=compute_103a,code=sm_103a -std=c++17 
 
 bool jump_op(uint16_t c) { return c == OP_IF || c == OP_ELSE || c == OP_LOOP_TEST || c == OP_JUMP; }
 
+uint32_t arg_ncomp(uint32_t a) {
+    const uint32_t t = (a >> kArgTCShift) & 7u;
+    return t == TC_TRIPLE ? 3u : (t == TC_MATRIX ? 16u : 1u);
+}
+
+// Record stride of the output arena when every output op writes inside
+// records of one common stride (then a tile's records can be staged in
+// shared memory and copied out whole); 0 otherwise.
+uint32_t staging_stride(const Op* ops, int n) {
+    int64_t stride = -1;
+    for (int i = 0; i < n; ++i) {
+        const Op& op = ops[i];
+        int64_t off, st, size;
+        switch (op.code) {
+        case OP_STORE_OUTPUT:
+            off = op.a[1];
+            st = (int32_t)op.a[2];
+            size = 4ll * arg_ncomp(op.a[0]) * std::max<uint32_t>(1u, op.a[4]) * ((op.a[3] & 1u) ? 3 : 1);
+            break;
+        case OP_STORE_CLOSURE:
+            off = op.a[1];
+            st = (int32_t)op.a[2];
+            size = 4ll * (1 + (int64_t)op.a[3] * kNodeFloats);
+            break;
+        case OP_BSDF_EVAL: off = op.a[1]; st = (int32_t)op.a[2]; size = 16; break;
+        case OP_BSDF_SAMPLE: off = op.a[1]; st = (int32_t)op.a[2]; size = 44; break;
+        default: continue;
+        }
+        if (st <= 0 || st % 4 || off % 4 || off + size > st || (stride >= 0 && st != stride)) return 0;
+        stride = st;
+    }
+    return stride > 0 && stride <= 512 ? (uint32_t)stride : 0;
+}
+
 void put_args(std::ostringstream& o, const uint32_t* a) {
     o << "{";
     for (int i = 0; i < 7; ++i) o << (i ? ", " : "") << a[i] << "u";
@@ -106,10 +140,12 @@ std::string spec_source(const CompiledGroup& cg) {
         loops = loops || ops[i].code == OP_LOOP_BEGIN || ops[i].code == OP_JUMP;
         adds += ops[i].code == OP_CLOSURE_ADD;
     }
+    const uint32_t stage = staging_stride(ops, n);
     std::ostringstream o;
     o << "// generated: kernel specialized to one lowered program (" << n << " ops, " << sym
       << " symbol slots, " << cpool << " closure-pool slots)\n";
     o << "#define OSLG_SPEC 1\n";
+    if (stage) o << "#define OSLG_STAGE_STRIDE " << stage << "\n";
     if (uses_cl && !loops) {
         o << "#define OSLG_FIXED_INDEX 1\n";
         o << "#define OSLG_WALK_STACK " << std::max(1, std::min(adds, (int)kClosureWalkStack)) << "\n";
@@ -171,19 +207,43 @@ std::string spec_source(const CompiledGroup& cg) {
     o << "extern \"C\" __global__ void __launch_bounds__(256, 2) " << kKernelName
       << "(const __grid_constant__ oslg::dev::KArgs k, int pool_in_smem) {\n";
     o << "    using namespace oslg;\n    using namespace oslg::dev;\n";
-    o << "    extern __shared__ __align__(16) unsigned char smem[];\n";
+    if (stage) o << "    unsigned char* smem = oslg_smem;\n";
+    else o << "    extern __shared__ __align__(16) unsigned char smem[];\n";
     o << "    RunCtx R;\n    R.sops = nullptr;\n    R.nops = " << n << ";\n";
     o << "    R.CP.base = " << h.closure_base << "u;\n    R.CP.max_nodes = " << h.max_comps << "u;\n";
     o << "    R.uses_closures = " << (uses_cl ? "true" : "false") << ";\n";
     o << "    R.G = &k.G;\n    R.userdata = k.userdata;\n    R.outputs = k.outputs;\n    R.status = k.status;\n";
     o << "    float hreg[" << std::max(1u, sym) << "];\n";
     o << "    Lane L;\n    L.heap = hreg;\n    L.pool = kPool;\n    L.hs = 1;\n    L.li = 0;\n    L.pt = 0;\n";
-    o << "    L.cheap = pool_in_smem ? reinterpret_cast<float*>(smem) : k.gheap + (size_t)blockIdx.x * "
+    // dynamic shared memory: [staged records | written flags] then the closure pools
+    o << "    const size_t stage_bytes = " << (stage ? "(size_t)blockDim.x * " + std::to_string(stage) + "u * 5u / 4u"
+                                                    : std::string("0")) << ";\n";
+    o << "    L.cheap = pool_in_smem ? reinterpret_cast<float*>(smem + stage_bytes) : k.gheap + (size_t)blockIdx.x * "
       << std::max(1u, cpool) << "u * blockDim.x;\n";
     o << "    L.chs = blockDim.x;\n    L.cli = threadIdx.x;\n    L.cbase = " << h.closure_base << "u;\n";
     o << "    const int64_t ntiles = (k.npoints + blockDim.x - 1) / blockDim.x;\n";
     o << "    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {\n";
-    o << "        L.pt = tile * blockDim.x + threadIdx.x;\n        spec_body(R, L, k.npoints);\n    }\n}\n";
+    if (stage) {
+        o << "        const size_t rec = " << stage << "u;\n";
+        o << "        unsigned char* flags = smem + (size_t)blockDim.x * rec;\n";
+        // one flag byte per staged word: blockDim * rec / 4 bytes, cleared as uint4
+        o << "        for (size_t i = threadIdx.x; i < (size_t)blockDim.x * rec / 64u; i += blockDim.x)\n";
+        o << "            reinterpret_cast<uint4*>(flags)[i] = make_uint4(0u, 0u, 0u, 0u);\n";
+        o << "        __syncthreads();\n";
+        o << "        R.outputs = reinterpret_cast<char*>(smem) - (ptrdiff_t)(tile * blockDim.x) * (ptrdiff_t)rec;\n";
+    }
+    o << "        L.pt = tile * blockDim.x + threadIdx.x;\n        spec_body(R, L, k.npoints);\n";
+    if (stage) {
+        o << "        __syncthreads();\n";
+        o << "        const int64_t npt = k.npoints - tile * blockDim.x < (int64_t)blockDim.x ? k.npoints - tile * "
+             "blockDim.x : (int64_t)blockDim.x;\n";
+        o << "        uint32_t* gout = reinterpret_cast<uint32_t*>(k.outputs + tile * blockDim.x * (int64_t)rec);\n";
+        o << "        const uint32_t* sw = reinterpret_cast<const uint32_t*>(smem);\n";
+        o << "        for (int64_t w = threadIdx.x; w < npt * (int64_t)(rec / 4u); w += blockDim.x)\n";
+        o << "            if (flags[w]) gout[w] = sw[w];\n";
+        o << "        __syncthreads();\n";
+    }
+    o << "    }\n}\n";
     return o.str();
 }
 
@@ -233,6 +293,8 @@ int spec_build(const CompiledGroup& cg, const std::string& csrc, const std::stri
     const bool uses_cl = (cg.header.flags & 1u) != 0;
     out->sym_slots = uses_cl ? cg.header.closure_base : cg.header.heap_slots;
     out->pool_slots = uses_cl ? cg.header.heap_slots - cg.header.closure_base : 0;
+    out->stage_stride = staging_stride(reinterpret_cast<const Op*>(cg.blob.data() + sizeof(ProgramHeader)),
+                                       (int)cg.header.nops);
     return OSLG_OK;
 }
 
@@ -243,12 +305,21 @@ int spec_launch(DeviceState& ds, const SpecKernel& sk, const CompiledGroup& cg, 
     int rc = device_init(ds, err);
     if (rc != OSLG_OK) return rc;
     const void* fn = reinterpret_cast<const void*>(sk.kernel);
+    // measured on the layered-closure workload: with staged output records,
+    // 128-thread CTAs and closure pools in HBM scratch (L2-resident) keep the
+    // most warps resident; without staging, 256 threads with the pools in
+    // shared memory
+    if (block_req == 0 && sk.stage_stride) block_req = 128;
+    if (pool_req < 0 && sk.stage_stride) pool_req = 0;
     const int block = block_req == 128 || block_req == 64 ? block_req : 256;
     const size_t pool_bytes = (size_t)sk.pool_slots * block * sizeof(float);
-    int in_smem = pool_bytes > 0 && pool_bytes <= 100 * 1024 ? 1 : 0;
+    const size_t stage_bytes = (size_t)block * sk.stage_stride * 5 / 4;
+    // closure pools in shared memory when they fit beside the staged records
+    // in 100 KiB (two CTAs per SM), else in HBM scratch
+    int in_smem = pool_bytes > 0 && stage_bytes + pool_bytes <= 100 * 1024 ? 1 : 0;
     if (pool_req == 0) in_smem = 0;
-    if (pool_req == 1 && pool_bytes > 0 && pool_bytes + 1024 <= ds.smem_optin) in_smem = 1;
-    const size_t shmem = in_smem ? pool_bytes : 0;
+    if (pool_req == 1 && pool_bytes > 0 && stage_bytes + pool_bytes + 1024 <= ds.smem_optin) in_smem = 1;
+    const size_t shmem = stage_bytes + (in_smem ? pool_bytes : 0);
     if (shmem > 48 * 1024 &&
         !ok(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shmem), err,
             "specialized kernel attribute"))

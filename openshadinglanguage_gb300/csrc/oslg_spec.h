@@ -25,6 +25,7 @@ struct SpecKernel {
     std::string key;          // content hash of the source
     uint32_t sym_slots = 0;   // thread-local floats
     uint32_t pool_slots = 0;  // closure-pool floats per point (slot-major heap)
+    uint32_t stage_stride = 0;  // output record bytes staged in shared memory (0: none)
     ~SpecKernel();
 };
 
