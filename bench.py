@@ -116,6 +116,7 @@ class FbmCell:
         # e2e buffers: pinned host inputs and outputs
         self.pin_uv = torch.from_numpy(np.stack([u, v])).pin_memory()
         self.pin_out = torch.zeros(self.n * self.rec, dtype=torch.float32).pin_memory()
+        self.G_host = grid_globals(self.pin_uv[0], self.pin_uv[1], self.W, self.H, centers=True)
         self.bytes_in = 8 * self.n
         self.bytes_out = 4 * self.rec * self.n
 
@@ -123,9 +124,8 @@ class FbmCell:
         self.ss.execute_batch(self.g, self.n, self.G, 0, self.out.data_ptr(), stream)
 
     def e2e_step(self, torch, stream):
-        self.d_uv.copy_(self.pin_uv, non_blocking=True)
-        self.ss.execute_batch(self.g, self.n, self.G, 0, self.out.data_ptr(), stream)
-        self.pin_out.copy_(self.out, non_blocking=True)
+        # host buffers in, host records out: the pipelined host-buffer entry
+        self.ss.execute_batch_host(self.g, self.n, self.G_host, self.pin_out, 4 * self.rec)
 
     def algorithmic_bytes(self):
         # read u,v (8 B) + write Cout val/dx/dy (36 B) + cell hash (4 B)
@@ -176,6 +176,8 @@ class LayeredClosure:
         self.out = torch.zeros(self.n * self.rec, dtype=torch.float32, device="cuda")
         self.pin_in = self.d_in.cpu().pin_memory()
         self.pin_out = torch.zeros(self.n * self.rec, dtype=torch.float32).pin_memory()
+        self.G_host = self.wl.c2_globals(og.make_globals, self.pin_in[0:n], self.pin_in[n:2 * n],
+                                         self.pin_in[2 * n:].view(3, n))
         self.bytes_in = 20 * self.n
         self.bytes_out = 4 * self.rec * self.n
 
@@ -183,9 +185,8 @@ class LayeredClosure:
         self.ss.execute_batch(self.g, self.n, self.G, 0, self.out.data_ptr(), stream)
 
     def e2e_step(self, torch, stream):
-        self.d_in.copy_(self.pin_in, non_blocking=True)
-        self.ss.execute_batch(self.g, self.n, self.G, 0, self.out.data_ptr(), stream)
-        self.pin_out.copy_(self.out, non_blocking=True)
+        # host buffers in, host records out: the pipelined host-buffer entry
+        self.ss.execute_batch_host(self.g, self.n, self.G_host, self.pin_out, 4 * self.rec)
 
     def algorithmic_bytes(self):
         # read u, v, I (20 B) + write 2 closure records with count (132 B) + eval (16 B)
@@ -378,7 +379,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the 64-group batching, serving and wavefront measurements")
-    ap.add_argument("--jit", type=int, default=0,
+    ap.add_argument("--jit", type=int, default=1,
                     help="1: run the group's specialized kernel (attribute jit), 0: the interpreter")
     ap.add_argument("--jit-block", type=int, default=0, help="specialized launch: threads per CTA")
     ap.add_argument("--jit-pool-smem", type=int, default=-1, help="specialized launch: closure pools in smem (1/0)")
@@ -496,15 +497,18 @@ def main():
     for _ in range(2):
         wl.e2e_step(torch, sh)
     torch.cuda.synchronize()
-    e_evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    # the host-buffer call returns when the outputs are in host memory: timed
+    # on the host clock, device idle and L2 flushed before each call
+    e_times = []
     barrier()
     for i in range(args.steps):
         flush.zero_()
-        e_evs[i][0].record(stream)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
         wl.e2e_step(torch, sh)
-        e_evs[i][1].record(stream)
+        e_times.append(time.perf_counter() - t0)
     barrier()
-    e_ms = float(np.mean([a.elapsed_time(b) for a, b in e_evs]))
+    e_ms = 1e3 * float(np.mean(e_times))
     e2e_value = wl.n * world / (e_ms * 1e-3) / 1e6
 
     if rank != 0:

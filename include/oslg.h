@@ -167,6 +167,20 @@ int oslg_group_bsdf_sample(oslg_system* sys, oslg_group* group, const char* clos
 /* ShadingSystem::optimize_group (oslexec.h:1093) + BatchedExecutor::jit_group
  * (oslexec.h:993): lowers the group to a device op program and uploads it. */
 int oslg_optimize_group(oslg_system* sys, oslg_group* group);
+/* BatchedExecutor::execute over HOST buffers (the reference's execute reads
+ * and writes host memory). Shader-global fields with data != NULL are host
+ * SoA planes (plane_stride apart); host_userdata and host_outputs hold one
+ * record per point, userdata_stride / output_stride bytes apart (the
+ * strides the group's symlocs use; 0 when the group has none). The points
+ * run in chunks whose input copies, launches and output copies overlap on
+ * three internal streams; returns when the outputs are in host memory.
+ * Output bytes the group does not write are zero, or keep their host values
+ * with OSLG_HOST_PRESERVE_OUTPUTS (which copies the records in first). Host
+ * memory should be pinned for the copies to run asynchronously. */
+#define OSLG_HOST_PRESERVE_OUTPUTS 1
+int oslg_execute_batch_host(oslg_system* sys, oslg_group* group, int64_t npoints,
+                            const oslg_shaderglobals* host_globals, const void* host_userdata,
+                            int64_t userdata_stride, void* host_outputs, int64_t output_stride, int flags);
 /* The CUDA source of the kernel specialized to this group (each op a call
  * of the interpreter's handler with constant operands, control flow as
  * gotos, constants in constant memory). With attribute "jit" = 1 it is

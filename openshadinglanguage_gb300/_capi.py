@@ -151,6 +151,9 @@ _EXPORTS = {
     "oslg_server_poll": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.POINTER(ctypes.c_int),
                                         ctypes.POINTER(RequestStatsC)]),
     "oslg_server_get_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ServerStatsC)]),
+    "oslg_execute_batch_host": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                               ctypes.POINTER(ShaderGlobalsC), ctypes.c_void_p, ctypes.c_int64,
+                                               ctypes.c_void_p, ctypes.c_int64, ctypes.c_int]),
     "oslg_group_specialized_source": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p,
                                                      ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
     "oslg_group_is_specialized": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),

@@ -3,6 +3,9 @@
 // status and leaves a message in oslg_last_error(); no C++ exception crosses
 // the boundary (the reference reports through bool returns and an
 // ErrorHandler, src/liboslexec/context.cpp:443-451).
+#include <cuda_runtime.h>
+
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <exception>
@@ -19,9 +22,23 @@
 
 #include <dlfcn.h>
 
+// One pipeline slot of oslg_execute_batch_host: a stream, device copies of
+// a chunk's inputs and outputs, and its own scratch heap (slots run
+// concurrently).
+struct HostSlot {
+    cudaStream_t stream = nullptr;
+    float* d_glob = nullptr;
+    char* d_ud = nullptr;
+    char* d_out = nullptr;
+    size_t glob_bytes = 0, ud_bytes = 0, out_bytes = 0;
+    float* gheap = nullptr;
+    size_t gheap_bytes = 0;
+};
+
 struct oslg_system {
     oslg::ShadingSystem ss;
     oslg::DeviceState dev;
+    std::vector<HostSlot> host_slots;
     oslg::LaunchConfig launch;
     int jit = 0;  // build a specialized kernel per group at optimize time
     int jit_block = 0;       // specialized launch: threads per CTA (0: 256)
@@ -147,6 +164,13 @@ int oslg_destroy_system(oslg_system* sys) {
     if (!sys) return OSLG_ERR_ARG;
     if (sys->dev.gheap) device_free(sys->dev.gheap);
     if (sys->dev.d_status) device_free(sys->dev.d_status);
+    for (HostSlot& S : sys->host_slots) {
+        if (S.stream) cudaStreamDestroy(S.stream);
+        cudaFree(S.d_glob);
+        cudaFree(S.d_ud);
+        cudaFree(S.d_out);
+        cudaFree(S.gheap);
+    }
     delete sys;
     return OSLG_OK;
 }
@@ -433,6 +457,132 @@ int oslg_execute_batch(oslg_system* sys, oslg_group* group, int64_t npoints, con
             rc = device_execute(sys->dev, cg.header, cg.d_blob, npoints, *globals, userdata_base, output_base,
                                 stream, sys->launch, &err);
         if (rc != OSLG_OK) return fail(sys, rc, err);
+        return OSLG_OK;
+    });
+}
+
+// ---- execution over host buffers --------------------------------------------------
+namespace {
+// components per shader-global field (GlobalId order)
+const int kGlobalComps[G_COUNT] = { 3, 3, 3, 3, 3, 3, 3, 3, 3, 1, 1, 1, 1, 1, 1, 3, 3, 1, 1, 3, 3, 3, 3, 1 };
+
+bool cu_ok(oslg_system* sys, cudaError_t e, const char* what, int* rc) {
+    if (e == cudaSuccess) return true;
+    fail(sys, OSLG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    *rc = OSLG_ERR_CUDA;
+    return false;
+}
+
+bool grow(void** p, size_t* have, size_t need) {
+    if (*have >= need) return true;
+    cudaFree(*p);
+    *p = nullptr;
+    *have = 0;
+    if (cudaMalloc(p, need) != cudaSuccess) return false;
+    *have = need;
+    return true;
+}
+}  // namespace
+
+int oslg_execute_batch_host(oslg_system* sys, oslg_group* group, int64_t npoints,
+                            const oslg_shaderglobals* host_globals, const void* host_userdata,
+                            int64_t userdata_stride, void* host_outputs, int64_t output_stride, int flags) {
+    if (!sys || !group || !host_globals || npoints < 0 || userdata_stride < 0 || output_stride < 0 ||
+        (npoints > 0 && output_stride > 0 && !host_outputs) || (userdata_stride > 0 && !host_userdata))
+        return OSLG_ERR_ARG;
+    return guarded(sys, [&]() {
+        int rc = ensure_compiled(sys, group, true);
+        if (rc != OSLG_OK) return rc;
+        const CompiledGroup& cg = *group->g.compiled;
+        if (npoints == 0) return OSLG_OK;
+        // every arena access of the program must fall inside its point's record
+        const Op* ops = reinterpret_cast<const Op*>(cg.blob.data() + sizeof(ProgramHeader));
+        for (uint32_t i = 0; i < cg.header.nops; ++i) {
+            const Op& op = ops[i];
+            const bool out = op.code == OP_STORE_OUTPUT || op.code == OP_STORE_CLOSURE || op.code == OP_BSDF_EVAL ||
+                             op.code == OP_BSDF_SAMPLE;
+            if (out && (int64_t)(int32_t)op.a[2] != output_stride)
+                return fail(sys, OSLG_ERR_ARG, "output_stride differs from the group's output record stride");
+            if (op.code == OP_LOAD_USERDATA && (int64_t)(int32_t)op.a[2] != userdata_stride)
+                return fail(sys, OSLG_ERR_ARG, "userdata_stride differs from the group's userdata record stride");
+            if (op.code == OP_BSDF_SAMPLE && (int64_t)(int32_t)op.a[6] != userdata_stride)
+                return fail(sys, OSLG_ERR_ARG, "userdata_stride differs from the group's sampling record stride");
+        }
+        // chunks of at most an eighth of the points (>= 64K), three slots in flight
+        const int nslots = 3;
+        const int64_t chunk = std::min<int64_t>(npoints, std::max<int64_t>(65536, ((npoints + 7) / 8 + 255) / 256 * 256));
+        int planes = 0;
+        const oslg_field* hf = reinterpret_cast<const oslg_field*>(host_globals);
+        for (int f = 0; f < G_COUNT; ++f)
+            if (hf[f].data) planes += kGlobalComps[f];
+        if ((int)sys->host_slots.size() < nslots) sys->host_slots.resize(nslots);
+        for (int k = 0; k < nslots; ++k) {
+            HostSlot& S = sys->host_slots[k];
+            if (!S.stream && !cu_ok(sys, cudaStreamCreateWithFlags(&S.stream, cudaStreamNonBlocking), "stream", &rc))
+                return rc;
+            if (!grow(reinterpret_cast<void**>(&S.d_glob), &S.glob_bytes, (size_t)std::max(1, planes) * chunk * 4) ||
+                !grow(reinterpret_cast<void**>(&S.d_ud), &S.ud_bytes, (size_t)std::max<int64_t>(4, userdata_stride * chunk)) ||
+                !grow(reinterpret_cast<void**>(&S.d_out), &S.out_bytes, (size_t)std::max<int64_t>(4, output_stride * chunk)))
+                return fail(sys, OSLG_ERR_CUDA, "cudaMalloc of the host-execution buffers failed");
+        }
+        const bool preserve = (flags & OSLG_HOST_PRESERVE_OUTPUTS) != 0;
+        const int64_t nchunks = (npoints + chunk - 1) / chunk;
+        for (int64_t c = 0; c < nchunks; ++c) {
+            HostSlot& S = sys->host_slots[c % nslots];
+            const int64_t start = c * chunk, n = std::min(chunk, npoints - start);
+            oslg_shaderglobals dg = *host_globals;
+            oslg_field* df = reinterpret_cast<oslg_field*>(&dg);
+            int plane = 0;
+            for (int f = 0; f < G_COUNT; ++f) {
+                if (!hf[f].data) continue;
+                float* base = S.d_glob + (size_t)plane * chunk;
+                for (int comp = 0; comp < kGlobalComps[f]; ++comp)
+                    if (!cu_ok(sys, cudaMemcpyAsync(base + (size_t)comp * chunk,
+                                                    hf[f].data + comp * hf[f].plane_stride + start, (size_t)n * 4,
+                                                    cudaMemcpyHostToDevice, S.stream),
+                               "input copy", &rc))
+                        return rc;
+                df[f].data = base;
+                df[f].plane_stride = chunk;
+                plane += kGlobalComps[f];
+            }
+            if (userdata_stride > 0 &&
+                !cu_ok(sys, cudaMemcpyAsync(S.d_ud, static_cast<const char*>(host_userdata) + start * userdata_stride,
+                                            (size_t)(n * userdata_stride), cudaMemcpyHostToDevice, S.stream),
+                       "userdata copy", &rc))
+                return rc;
+            if (output_stride > 0) {
+                char* hout = static_cast<char*>(host_outputs) + start * output_stride;
+                const cudaError_t e = preserve ? cudaMemcpyAsync(S.d_out, hout, (size_t)(n * output_stride),
+                                                                 cudaMemcpyHostToDevice, S.stream)
+                                               : cudaMemsetAsync(S.d_out, 0, (size_t)(n * output_stride), S.stream);
+                if (!cu_ok(sys, e, "output preparation", &rc)) return rc;
+            }
+            DeviceState ds = sys->dev;
+            ds.gheap = S.gheap;
+            ds.gheap_bytes = S.gheap_bytes;
+            std::string err;
+            if (cg.spec)
+                rc = spec_launch(ds, *cg.spec, cg, n, dg, S.d_ud, S.d_out, S.stream, &err, sys->jit_block,
+                                 sys->jit_pool_smem);
+            else
+                rc = device_execute(ds, cg.header, cg.d_blob, n, dg, S.d_ud, S.d_out, S.stream, sys->launch, &err);
+            S.gheap = ds.gheap;
+            S.gheap_bytes = ds.gheap_bytes;
+            if (rc != OSLG_OK) return fail(sys, rc, err);
+            if (output_stride > 0 &&
+                !cu_ok(sys, cudaMemcpyAsync(static_cast<char*>(host_outputs) + start * output_stride, S.d_out,
+                                            (size_t)(n * output_stride), cudaMemcpyDeviceToHost, S.stream),
+                       "output copy", &rc))
+                return rc;
+        }
+        for (int k = 0; k < nslots; ++k)
+            if (!cu_ok(sys, cudaStreamSynchronize(sys->host_slots[k].stream), "synchronize", &rc)) return rc;
+        uint32_t bits = 0;
+        std::string err;
+        rc = device_read_status(sys->dev, nullptr, &bits, &err);
+        if (rc != OSLG_OK) return fail(sys, rc, err);
+        if (bits) return fail(sys, OSLG_ERR_DEVICE, "kernel status bits " + std::to_string(bits));
         return OSLG_OK;
     });
 }

@@ -224,6 +224,24 @@ class ShadingSystem:
         """A wavefront path tracer over `prims` shaded by `materials` (see Wavefront)."""
         return Wavefront(self, prims, materials, **options)
 
+    def execute_batch_host(self, group, npoints, globals_c, outputs, output_stride, userdata=None,
+                           userdata_stride=0, preserve_outputs=False):
+        """BatchedExecutor::execute over host buffers (oslg_execute_batch_host):
+        globals_c has host SoA planes; outputs/userdata are host arrays or
+        CPU tensors (pinned for overlapped copies) of per-point records."""
+        def addr(x):
+            if x is None:
+                return None
+            if hasattr(x, "data_ptr"):
+                return x.data_ptr()
+            if hasattr(x, "ctypes"):
+                return x.ctypes.data
+            return int(x)
+        self._check(C.lib().oslg_execute_batch_host(self._h, group.handle, int(npoints), ctypes.byref(globals_c),
+                                                    ctypes.c_void_p(addr(userdata)), int(userdata_stride),
+                                                    ctypes.c_void_p(addr(outputs)), int(output_stride),
+                                                    1 if preserve_outputs else 0))
+
     def device_status(self):
         bits = ctypes.c_uint32(0)
         self._check(C.lib().oslg_device_status(self._h, ctypes.byref(bits)))
