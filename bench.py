@@ -291,7 +291,7 @@ def bench_serving(torch, og, nreq=600):
             "latency": "arrival to outputs in host memory (pinned), host monotonic clock"}
 
 
-def bench_wavefront(torch, og, frames=3, cpu_step=97, size=None):
+def bench_wavefront(torch, og, frames=3, cpu_step=97, size=None, jit=1):
     """Wavefront path tracing of the seeded 1000-primitive scene with the 16
     layered materials: 1920x1080x4 paths, up to 8 hits, Russian roulette
     survival 0.8. A frame (all bounces) is one CUDA-graph replay; a
@@ -300,13 +300,17 @@ def bench_wavefront(torch, og, frames=3, cpu_step=97, size=None):
     from openshadinglanguage_gb300 import workloads
     from helpers import oracle_wavefront
     ss = og.ShadingSystem()
+    if jit:
+        ss.attribute("jit", 1)  # materials shade in a batch kernel specialized to them (built at create)
     mats = workloads.c5_materials(ss)
     prims = workloads.c5_scene()
     dims = {}
     if size:
         w, h, spp = (int(x) for x in size.split("x"))
         dims = dict(width=w, height=h, spp=spp)
+    t_build = time.perf_counter()
     wf = ss.wavefront(prims, mats, **dims)
+    t_build = time.perf_counter() - t_build
     o = wf.options
     rad = torch.empty(3 * wf.paths, dtype=torch.float32, device="cuda")
     img = torch.empty(o["width"] * o["height"] * 3, dtype=torch.float32, device="cuda")
@@ -339,6 +343,8 @@ def bench_wavefront(torch, og, frames=3, cpu_step=97, size=None):
             "mpaths_per_s": wf.paths / ms / 1e3, "shading_points": nhits,
             "mhits_per_s": nhits / ms / 1e3, "hits_per_bounce": s["hits"][:o["max_hits"]],
             "profiled_stage_ms": stages, "device_status": status,
+            "shading_kernel": "specialized batch kernel (jit)" if jit else "interpreter batch kernel",
+            "create_s": t_build,
             "launches_per_frame": 2 + 5 * o["max_hits"] + 1,
             "cpu": {"paths": ncpu, "hits": int(chits.sum()), "seconds": cpu_s,
                     "mpaths_per_s": ncpu / cpu_s / 1e6, "mhits_per_s": float(chits.sum()) / cpu_s / 1e6,
@@ -395,7 +401,7 @@ def main():
         build_native()
         torch.cuda.set_device(0)
         fn = {"batching": lambda: bench_batching(torch, og), "serving": lambda: bench_serving(torch, og),
-              "wavefront": lambda: bench_wavefront(torch, og, size=args.wf_size)}[args.section]
+              "wavefront": lambda: bench_wavefront(torch, og, size=args.wf_size, jit=args.jit)}[args.section]
         print(json.dumps({"section": args.section, args.section: fn()}))
         return 0
 
@@ -554,7 +560,7 @@ def main():
     if not args.no_extras and world == 1:
         line["batching"] = bench_batching(torch, og)
         line["serving"] = bench_serving(torch, og)
-        line["wavefront"] = bench_wavefront(torch, og)
+        line["wavefront"] = bench_wavefront(torch, og, jit=args.jit)
     if not args.no_cpu_baseline:
         from helpers import oracle_run  # noqa: F401
         build_oracle()

@@ -189,6 +189,11 @@ int oslg_execute_batch_host(oslg_system* sys, oslg_group* group, int64_t npoints
  * interpreter. Replaces BatchedBackendLLVM code generation
  * (src/liboslexec/batched_backendllvm.cpp). `size` gets the length + 1. */
 int oslg_group_specialized_source(oslg_system* sys, oslg_group* group, char* buf, size_t cap, size_t* size);
+/* The CUDA source of a persistent batch kernel specialized to several
+ * groups (job i of a batch runs groups[i]'s body); with attribute "jit" the
+ * wavefront driver shades its materials with such a kernel. */
+int oslg_groups_specialized_batch_source(oslg_system* sys, oslg_group* const* groups, int ngroups, char* buf,
+                                         size_t cap, size_t* size);
 /* 1 when the group runs its specialized kernel. */
 int oslg_group_is_specialized(oslg_system* sys, oslg_group* group, int* out);
 /* ShaderGroupRef release */

@@ -156,6 +156,9 @@ _EXPORTS = {
                                                ctypes.c_void_p, ctypes.c_int64, ctypes.c_int]),
     "oslg_group_specialized_source": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p,
                                                      ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
+    "oslg_groups_specialized_batch_source": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p),
+                                                            ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t,
+                                                            ctypes.POINTER(ctypes.c_size_t)]),
     "oslg_group_is_specialized": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
     "oslg_wavefront_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(WavefrontOptionsC),
                                              ctypes.POINTER(PrimitiveC), ctypes.c_int,

@@ -603,6 +603,28 @@ int oslg_group_specialized_source(oslg_system* sys, oslg_group* group, char* buf
     });
 }
 
+int oslg_groups_specialized_batch_source(oslg_system* sys, oslg_group* const* groups, int ngroups, char* buf,
+                                         size_t cap, size_t* size) {
+    if (!sys || !groups || ngroups < 1) return OSLG_ERR_ARG;
+    return guarded(sys, [&]() {
+        std::vector<const CompiledGroup*> cgs;
+        for (int i = 0; i < ngroups; ++i) {
+            if (!groups[i]) return fail(sys, OSLG_ERR_ARG, "null group");
+            int rc = ensure_compiled(sys, groups[i], false);
+            if (rc != OSLG_OK) return rc;
+            cgs.push_back(groups[i]->g.compiled.get());
+        }
+        const std::string src = spec_batch_source(cgs);
+        if (size) *size = src.size() + 1;
+        if (buf && cap) {
+            const size_t n = std::min(cap - 1, src.size());
+            std::memcpy(buf, src.data(), n);
+            buf[n] = 0;
+        }
+        return OSLG_OK;
+    });
+}
+
 int oslg_group_is_specialized(oslg_system* sys, oslg_group* group, int* out) {
     if (!sys || !group || !out) return OSLG_ERR_ARG;
     *out = group->g.compiled && group->g.compiled->spec ? 1 : 0;
@@ -944,7 +966,9 @@ int oslg_wavefront_create(oslg_system* sys, const oslg_wavefront_options* opts, 
         w->sys = sys;
         w->wf = std::make_unique<oslg::Wavefront>();
         std::string err;
-        int rc = w->wf->init(sys->dev, *opts, prims, nprims, mats, &err);
+        const std::string dir = library_dir();
+        const std::string jit_dirs[2] = { dir + "/csrc", dir + "/_build/jit" };
+        int rc = w->wf->init(sys->dev, *opts, prims, nprims, mats, sys->jit ? jit_dirs : nullptr, &err);
         if (rc != OSLG_OK) return fail(sys, rc, "wavefront: " + err);
         *out = w.release();
         return OSLG_OK;

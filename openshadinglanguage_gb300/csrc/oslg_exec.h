@@ -30,6 +30,8 @@ struct BatchJob {
     char* userdata;
     char* outputs;
     oslg_shaderglobals G;
+    int32_t spec_case;    // program index inside a specialized batch kernel
+    int32_t pad_;
 };
 // Arguments of the persistent batch kernel: items are (job, tile) pairs,
 // taken in order through *counter (reset to 0 before every launch).

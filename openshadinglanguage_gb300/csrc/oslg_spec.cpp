@@ -69,6 +69,7 @@ uint64_t headers_hash(const std::string& csrc) {
 
 const char* kKernelName = "oslg_spec_kernel";
 const char* kFlags = "-cubin -gencode arch=compute_103a,code=sm_103a -std=c++17 -O3 -fmad=false";
+const char* kBatchFlags = "--split-compile=0";
 
 bool jump_op(uint16_t c) { return c == OP_IF || c == OP_ELSE || c == OP_LOOP_TEST || c == OP_JUMP; }
 
@@ -118,46 +119,68 @@ SpecKernel::~SpecKernel() {
     if (library) cudaLibraryUnload(static_cast<cudaLibrary_t>(library));
 }
 
-std::string spec_source(const CompiledGroup& cg) {
-    const ProgramHeader& h = cg.header;
-    const Op* ops = reinterpret_cast<const Op*>(cg.blob.data() + sizeof(ProgramHeader));
-    const uint32_t* pool =
-        reinterpret_cast<const uint32_t*>(cg.blob.data() + sizeof(ProgramHeader) + (size_t)h.nops * sizeof(Op));
-    const int n = (int)h.nops;
-    const bool uses_cl = (h.flags & 1u) != 0;
-    const uint32_t sym = uses_cl ? h.closure_base : h.heap_slots;
-    const uint32_t cpool = uses_cl ? h.heap_slots - h.closure_base : 0;
+namespace {
+
+struct ProgView {
+    const ProgramHeader* h;
+    const Op* ops;
+    const uint32_t* pool;
+    int n;
+    bool uses_cl;
+    uint32_t sym, cpool;
+};
+
+ProgView view(const CompiledGroup& cg) {
+    ProgView v;
+    v.h = &cg.header;
+    v.ops = reinterpret_cast<const Op*>(cg.blob.data() + sizeof(ProgramHeader));
+    v.pool = reinterpret_cast<const uint32_t*>(cg.blob.data() + sizeof(ProgramHeader) + (size_t)cg.header.nops * sizeof(Op));
+    v.n = (int)cg.header.nops;
+    v.uses_cl = (cg.header.flags & 1u) != 0;
+    v.sym = v.uses_cl ? cg.header.closure_base : cg.header.heap_slots;
+    v.cpool = v.uses_cl ? cg.header.heap_slots - cg.header.closure_base : 0;
+    return v;
+}
+
+// Loop-free programs execute each closure op at most once per point, so
+// the closure walk is at most (ADD ops) deep and finds at most 2^(ADD ops)
+// leaves: those bounds replace the reference capacities (16, 8).
+struct Bounds {
+    bool fixed = true;
+    int walk = 1, lobes = 1;
+};
+void add_bounds(Bounds& B, const ProgView& v) {
+    bool loops = false;
+    int adds = 0;
+    for (int i = 0; i < v.n; ++i) {
+        loops = loops || v.ops[i].code == OP_LOOP_BEGIN || v.ops[i].code == OP_JUMP;
+        adds += v.ops[i].code == OP_CLOSURE_ADD;
+    }
+    if (!v.uses_cl) return;
+    if (loops) B.fixed = false;
+    B.walk = std::max(B.walk, std::max(1, std::min(adds, (int)kClosureWalkStack)));
+    B.lobes = std::max(B.lobes, std::min((int)kBsdfMaxLobes, 1 << std::min(adds, 3)));
+}
+void emit_bounds(std::ostringstream& o, const Bounds& B, bool any_closures) {
+    if (!any_closures || !B.fixed) return;
+    o << "#define OSLG_FIXED_INDEX 1\n";
+    o << "#define OSLG_WALK_STACK " << B.walk << "\n";
+    o << "#define OSLG_LOBES_MAX " << B.lobes << "\n";
+}
+
+// The constant pool and the op sequence of one program as
+// spec_body<sfx>(R, L, npoints).
+void emit_body(std::ostringstream& o, const ProgView& v, const std::string& sfx) {
+    const int n = v.n;
+    const Op* ops = v.ops;
     std::vector<char> target(n + 1, 0);
     for (int i = 0; i < n; ++i)
         if (jump_op(ops[i].code) && ops[i].a[2] <= (uint32_t)n) target[ops[i].a[2]] = 1;
-
-    // Loop-free programs execute each closure op at most once per point, so
-    // the closure walk is at most (ADD ops) deep and finds at most 2^(ADD ops)
-    // leaves: those bounds replace the reference capacities (16, 8).
-    bool loops = false;
-    int adds = 0;
-    for (int i = 0; i < n; ++i) {
-        loops = loops || ops[i].code == OP_LOOP_BEGIN || ops[i].code == OP_JUMP;
-        adds += ops[i].code == OP_CLOSURE_ADD;
-    }
-    const uint32_t stage = staging_stride(ops, n);
-    std::ostringstream o;
-    o << "// generated: kernel specialized to one lowered program (" << n << " ops, " << sym
-      << " symbol slots, " << cpool << " closure-pool slots)\n";
-    o << "#define OSLG_SPEC 1\n";
-    if (stage) o << "#define OSLG_STAGE_STRIDE " << stage << "\n";
-    if (uses_cl && !loops) {
-        o << "#define OSLG_FIXED_INDEX 1\n";
-        o << "#define OSLG_WALK_STACK " << std::max(1, std::min(adds, (int)kClosureWalkStack)) << "\n";
-        o << "#define OSLG_LOBES_MAX " << std::min((int)kBsdfMaxLobes, 1 << std::min(adds, 3)) << "\n";
-    }
-    o << "#include \"oslg_interp.cuh\"\n\nnamespace {\n";
-    o << "using namespace oslg;\nusing namespace oslg::dev;\n\n";
-    o << "__constant__ const uint32_t kPool[" << std::max(1u, h.nconst) << "] = {";
-    for (uint32_t i = 0; i < h.nconst; ++i) o << (i ? ", " : "") << pool[i] << "u";
-    if (!h.nconst) o << "0u";
+    o << "__constant__ const uint32_t kPool" << sfx << "[" << std::max(1u, v.h->nconst) << "] = {";
+    for (uint32_t i = 0; i < v.h->nconst; ++i) o << (i ? ", " : "") << v.pool[i] << "u";
+    if (!v.h->nconst) o << "0u";
     o << "};\n\n";
-    o << "__device__ __forceinline__ void spec_body(const RunCtx& R, Lane& L, int64_t npoints) {\n";
+    o << "__device__ __forceinline__ void spec_body" << sfx << "(const RunCtx& R, Lane& L, int64_t npoints) {\n";
     o << "    Ctl<1> C;\n    ctl_init<1>(C, R, L, npoints);\n    long long backedges = 0;\n";
     o << "    const uint32_t li0 = L.li;\n    (void)backedges;\n    (void)li0;\n";
     for (int i = 0; i < n; ++i) {
@@ -203,7 +226,43 @@ std::string spec_source(const CompiledGroup& cg) {
         }
         o << "    }\n";
     }
-    o << "op_" << n << ":;\n}\n\n}  // namespace\n\n";
+    o << "op_" << n << ":;\n}\n\n";
+}
+
+// R/L set-up of one program and its body, for tile L.pt.
+// Batch kernels keep each program's body a separate function (built in
+// parallel by nvcc --split-compile, register allocation per program).
+void emit_job(std::ostringstream& o, const ProgView& v, const std::string& sfx) {
+    o << "__device__ __noinline__ void spec_job" << sfx << "(RunCtx& R, Lane& L, int64_t npoints) {\n";
+    o << "    R.nops = " << v.n << ";\n";
+    o << "    R.CP.base = " << v.h->closure_base << "u;\n    R.CP.max_nodes = " << v.h->max_comps << "u;\n";
+    o << "    R.uses_closures = " << (v.uses_cl ? "true" : "false") << ";\n";
+    o << "    float hreg[" << std::max(1u, v.sym) << "];\n";
+    o << "    L.heap = hreg;\n    L.pool = kPool" << sfx << ";\n    L.cbase = " << v.h->closure_base << "u;\n";
+    o << "    spec_body" << sfx << "(R, L, npoints);\n}\n\n";
+}
+
+}  // namespace
+
+std::string spec_source(const CompiledGroup& cg) {
+    const ProgView v = view(cg);
+    const int n = v.n;
+    const uint32_t sym = v.sym, cpool = v.cpool;
+    const bool uses_cl = v.uses_cl;
+    const ProgramHeader& h = cg.header;
+    Bounds B;
+    add_bounds(B, v);
+    const uint32_t stage = staging_stride(v.ops, n);
+    std::ostringstream o;
+    o << "// generated: kernel specialized to one lowered program (" << n << " ops, " << sym
+      << " symbol slots, " << cpool << " closure-pool slots)\n";
+    o << "#define OSLG_SPEC 1\n";
+    if (stage) o << "#define OSLG_STAGE_STRIDE " << stage << "\n";
+    emit_bounds(o, B, uses_cl);
+    o << "#include \"oslg_interp.cuh\"\n\nnamespace {\n";
+    o << "using namespace oslg;\nusing namespace oslg::dev;\n\n";
+    emit_body(o, v, "");
+    o << "}  // namespace\n\n";
     o << "extern \"C\" __global__ void __launch_bounds__(256, 2) " << kKernelName
       << "(const __grid_constant__ oslg::dev::KArgs k, int pool_in_smem) {\n";
     o << "    using namespace oslg;\n    using namespace oslg::dev;\n";
@@ -247,10 +306,91 @@ std::string spec_source(const CompiledGroup& cg) {
     return o.str();
 }
 
+SpecBatchKernel::~SpecBatchKernel() {
+    if (library) cudaLibraryUnload(static_cast<cudaLibrary_t>(library));
+}
+
+std::string spec_batch_source(const std::vector<const CompiledGroup*>& cases) {
+    Bounds B;
+    bool any_cl = false;
+    std::vector<ProgView> vs;
+    for (const CompiledGroup* cg : cases) {
+        vs.push_back(view(*cg));
+        add_bounds(B, vs.back());
+        any_cl = any_cl || vs.back().uses_cl;
+    }
+    std::ostringstream o;
+    o << "// generated: persistent batch kernel specialized to " << cases.size() << " lowered programs\n";
+    o << "#define OSLG_SPEC 1\n";
+    emit_bounds(o, B, any_cl);
+    o << "#include \"oslg_interp.cuh\"\n\nnamespace {\n";
+    o << "using namespace oslg;\nusing namespace oslg::dev;\n\n";
+    for (size_t j = 0; j < vs.size(); ++j) {
+        emit_body(o, vs[j], "_" + std::to_string(j));
+        emit_job(o, vs[j], "_" + std::to_string(j));
+    }
+    o << "}  // namespace\n\n";
+    o << "extern \"C\" __global__ void __launch_bounds__(256, 2) oslg_specbatch_kernel("
+         "const __grid_constant__ oslg::dev::BatchArgs b, int pool_in_smem) {\n";
+    o << "    using namespace oslg;\n    using namespace oslg::dev;\n";
+    o << "    extern __shared__ __align__(16) unsigned char smem[];\n";
+    o << "    __shared__ uint32_t s_item;\n";
+    o << "    const uint32_t nitems = b.nitems_dev ? *b.nitems_dev : b.nitems;\n";
+    o << "    Lane L;\n    L.hs = 1;\n    L.li = 0;\n    L.chs = blockDim.x;\n    L.cli = threadIdx.x;\n";
+    o << "    L.cheap = pool_in_smem ? reinterpret_cast<float*>(smem) : b.gheap + (size_t)blockIdx.x * b.heap_slots * "
+         "blockDim.x;\n";
+    o << "    RunCtx R;\n    R.sops = nullptr;\n    R.status = b.status;\n";
+    o << "    for (;;) {\n";
+    o << "        if (threadIdx.x == 0) s_item = atomicAdd(b.counter, 1u);\n";
+    o << "        __syncthreads();\n        const uint32_t it = s_item;\n        __syncthreads();\n";
+    o << "        if (it >= nitems) break;\n";
+    o << "        const uint2 w = b.items[it];\n        const BatchJob* J = b.jobs + w.x;\n";
+    o << "        R.G = &J->G;\n        R.userdata = J->userdata;\n        R.outputs = J->outputs;\n";
+    o << "        L.pt = (int64_t)w.y * blockDim.x + threadIdx.x;\n";
+    o << "        const int64_t np = J->npoints;\n";
+    o << "        switch (J->spec_case) {\n";
+    for (size_t j = 0; j < vs.size(); ++j)
+        o << "        case " << j << ": spec_job_" << j << "(R, L, np); break;\n";
+    o << "        default: if (threadIdx.x == 0) raise_status(b.status, ST_BAD_OPCODE); break;\n";
+    o << "        }\n    }\n}\n";
+    return o.str();
+}
+
+namespace {
+// nvcc the source into the cache (once per content hash) and load `kname`.
+int build_and_load(const std::string& src, const std::string& csrc, const std::string& cache, const char* kname,
+                   const char* extra_flags, void** lib_out, void** kern_out, std::string* key_out, std::string* err);
+}  // namespace
+
+int spec_batch_build(const std::vector<const CompiledGroup*>& cases, const std::string& csrc,
+                     const std::string& cache, SpecBatchKernel* out, std::string* err) {
+    int rc = build_and_load(spec_batch_source(cases), csrc, cache, "oslg_specbatch_kernel", kBatchFlags,
+                            &out->library, &out->kernel, &out->key, err);
+    if (rc != OSLG_OK) return rc;
+    out->cases = (int)cases.size();
+    out->pool_slots = 0;
+    for (const CompiledGroup* cg : cases) out->pool_slots = std::max(out->pool_slots, view(*cg).cpool);
+    return OSLG_OK;
+}
+
 int spec_build(const CompiledGroup& cg, const std::string& csrc, const std::string& cache, SpecKernel* out,
                std::string* err) {
-    const std::string src = spec_source(cg);
-    const uint64_t key = fnv1a(std::string(kFlags) + "\n" + src, headers_hash(csrc));
+    int rc = build_and_load(spec_source(cg), csrc, cache, kKernelName, "", &out->library, &out->kernel, &out->key,
+                            err);
+    if (rc != OSLG_OK) return rc;
+    const bool uses_cl = (cg.header.flags & 1u) != 0;
+    out->sym_slots = uses_cl ? cg.header.closure_base : cg.header.heap_slots;
+    out->pool_slots = uses_cl ? cg.header.heap_slots - cg.header.closure_base : 0;
+    out->stage_stride = staging_stride(reinterpret_cast<const Op*>(cg.blob.data() + sizeof(ProgramHeader)),
+                                       (int)cg.header.nops);
+    return OSLG_OK;
+}
+
+namespace {
+int build_and_load(const std::string& src, const std::string& csrc, const std::string& cache, const char* kname,
+                   const char* extra_flags, void** lib_out, void** kern_out, std::string* key_out, std::string* err) {
+    const std::string flags = std::string(kFlags) + " " + extra_flags;
+    const uint64_t key = fnv1a(flags + "\n" + src, headers_hash(csrc));
     char hex[17];
     snprintf(hex, sizeof(hex), "%016llx", (unsigned long long)key);
     const std::string base = cache + "/spec_" + hex;
@@ -266,7 +406,7 @@ int spec_build(const CompiledGroup& cg, const std::string& csrc, const std::stri
         const char* ch = getenv("CUDA_HOME");
         const std::string nvcc = std::string(ch && *ch ? ch : "/usr/local/cuda") + "/bin/nvcc";
         const std::string tmp = base + "." + std::to_string((long long)getpid()) + ".tmp";
-        const std::string cmd = nvcc + " " + kFlags + " -I" + csrc + " -o " + tmp + " " + cu + " > " + base +
+        const std::string cmd = nvcc + " " + flags + " -I" + csrc + " -o " + tmp + " " + cu + " > " + base +
                                 ".log 2>&1";
         const int rc = std::system(cmd.c_str());
         if (rc != 0 || stat(tmp.c_str(), &stt) != 0) {
@@ -283,20 +423,16 @@ int spec_build(const CompiledGroup& cg, const std::string& csrc, const std::stri
             "load specialized kernel"))
         return OSLG_ERR_CUDA;
     cudaKernel_t kern = nullptr;
-    if (!ok(cudaLibraryGetKernel(&kern, lib, kKernelName), err, "specialized kernel lookup")) {
+    if (!ok(cudaLibraryGetKernel(&kern, lib, kname), err, "specialized kernel lookup")) {
         cudaLibraryUnload(lib);
         return OSLG_ERR_CUDA;
     }
-    out->library = lib;
-    out->kernel = kern;
-    out->key = hex;
-    const bool uses_cl = (cg.header.flags & 1u) != 0;
-    out->sym_slots = uses_cl ? cg.header.closure_base : cg.header.heap_slots;
-    out->pool_slots = uses_cl ? cg.header.heap_slots - cg.header.closure_base : 0;
-    out->stage_stride = staging_stride(reinterpret_cast<const Op*>(cg.blob.data() + sizeof(ProgramHeader)),
-                                       (int)cg.header.nops);
+    *lib_out = lib;
+    *kern_out = kern;
+    *key_out = hex;
     return OSLG_OK;
 }
+}  // namespace
 
 int spec_launch(DeviceState& ds, const SpecKernel& sk, const CompiledGroup& cg, int64_t npoints,
                 const oslg_shaderglobals& G, void* userdata, void* outputs, void* stream, std::string* err,

@@ -13,6 +13,7 @@
 #pragma once
 #include <cstdint>
 #include <string>
+#include <vector>
 
 #include "oslg_exec.h"
 #include "oslg_host.h"
@@ -31,6 +32,23 @@ struct SpecKernel {
 
 // CUDA source of the specialized kernel for one lowered program.
 std::string spec_source(const CompiledGroup& cg);
+
+// A persistent batch kernel specialized to a list of programs: the
+// interpreter's batch_kernel work loop (items (job, tile) from a device
+// counter) with a switch over BatchJob::spec_case into each program's
+// specialized body. Closure pools live in BatchArgs::gheap (heap_slots =
+// the largest pool) or in shared memory.
+struct SpecBatchKernel {
+    void* library = nullptr;
+    void* kernel = nullptr;
+    std::string key;
+    uint32_t pool_slots = 0;  // largest closure pool (floats per point)
+    int cases = 0;
+    ~SpecBatchKernel();
+};
+std::string spec_batch_source(const std::vector<const CompiledGroup*>& cases);
+int spec_batch_build(const std::vector<const CompiledGroup*>& cases, const std::string& csrc_dir,
+                     const std::string& cache_dir, SpecBatchKernel* out, std::string* err);
 
 // Build (or take from the cache) and load the kernel. `csrc_dir` holds the
 // interpreter headers, `cache_dir` the generated sources and cubins.

@@ -323,6 +323,7 @@ __global__ void __launch_bounds__(1024) k_plan(const __grid_constant__ WfArgs a,
         BatchJob* J = a.jobs + m;
         const int64_t off = s_off[m];
         J->blob = T->blob;
+        J->spec_case = T->spec_case;
         J->npoints = s_cnt[m];
         J->userdata = reinterpret_cast<char*>(a.ud + off * kWfInFloats);
         J->outputs = reinterpret_cast<char*>(a.out + off * kWfOutFloats);
@@ -513,11 +514,11 @@ void Wavefront::release() {
             e = nullptr;
         }
     void* bufs[] = { d_prims_, d_nodes_, d_state_, d_active_, d_hit_rec_, d_hit_t_, d_hit_slot_, d_globals_,
-                     d_ud_, d_out_, d_ctl_, d_jobs_, d_templ_, d_items_, d_order_, d_heap_ };
+                     d_ud_, d_out_, d_ctl_, d_jobs_, d_templ_, d_items_, d_order_, d_heap_, d_spec_heap_ };
     for (void* b : bufs) cudaFree(b);
     d_prims_ = nullptr;
     d_nodes_ = nullptr;
-    d_state_ = d_hit_t_ = d_globals_ = d_ud_ = d_out_ = d_heap_ = nullptr;
+    d_state_ = d_hit_t_ = d_globals_ = d_ud_ = d_out_ = d_heap_ = d_spec_heap_ = nullptr;
     d_active_ = d_hit_slot_ = d_ctl_ = nullptr;
     d_hit_rec_ = d_order_ = nullptr;
     d_jobs_ = d_templ_ = nullptr;
@@ -525,15 +526,16 @@ void Wavefront::release() {
 }
 
 int Wavefront::init(DeviceState& ds, const oslg_wavefront_options& o, const oslg_primitive* prims, int nprims,
-                    const std::vector<const CompiledGroup*>& mats, std::string* err) {
+                    const std::vector<const CompiledGroup*>& mats, const std::string* jit_dirs, std::string* err) {
     ds_ = &ds;
     opt_ = o;
     nprims_ = nprims;
     nmat_ = (int)mats.size();
     npaths_ = (int64_t)o.width * o.height * o.spp;
     block_ = o.block > 0 ? std::max(32, std::min(512, (o.block + 31) & ~31)) : 256;
+    if (jit_dirs) block_ = o.block == 128 || o.block == 64 ? o.block : 256;  // specialized: one point per thread
     maxt_ = block_ > 256 ? 512 : 256;
-    ppt_ = o.points_per_thread >= 4 ? 4 : (o.points_per_thread >= 2 ? 2 : 1);
+    ppt_ = jit_dirs ? 1 : (o.points_per_thread >= 4 ? 4 : (o.points_per_thread >= 2 ? 2 : 1));
     tile_ = block_ * ppt_;
     cap_ = npaths_ + (int64_t)nmat_ * tile_;
 
@@ -657,6 +659,7 @@ int Wavefront::init(DeviceState& ds, const oslg_wavefront_options& o, const oslg
         dev::BatchJob& j = templ[m];
         std::memset(&j, 0, sizeof(j));
         j.blob = static_cast<const uint8_t*>(mats[m]->d_blob);
+        j.spec_case = m;
         j.npoints = 0;
         j.userdata = reinterpret_cast<char*>(d_ud_);
         j.outputs = reinterpret_cast<char*>(d_out_);
@@ -701,6 +704,30 @@ int Wavefront::init(DeviceState& ds, const oslg_wavefront_options& o, const oslg
     bargs_.status = ds.d_status;
     bargs_.prog_bytes = prog_bytes;
     bargs_.heap_slots = slots;
+    if (jit_dirs) {
+        // shading by a persistent kernel specialized to the materials
+        int rc = spec_batch_build(mats, jit_dirs[0], jit_dirs[1], &spec_, err);
+        if (rc != OSLG_OK) return rc;
+        const void* fn = reinterpret_cast<const void*>(spec_.kernel);
+        const size_t pool_b = (size_t)spec_.pool_slots * block_ * sizeof(float);
+        spec_pool_smem_ = pool_b > 0 && pool_b <= 100 * 1024 ? 1 : 0;
+        spec_shmem_ = spec_pool_smem_ ? pool_b : 0;
+        if (spec_shmem_ > 48 * 1024 &&
+            !ok(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)spec_shmem_), err,
+                "specialized kernel attribute"))
+            return OSLG_ERR_CUDA;
+        int per = 0;
+        if (!ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, block_, spec_shmem_), err, "occupancy"))
+            return OSLG_ERR_CUDA;
+        grid_spec_ = ds.sm_count * std::max(1, per);
+        if (!spec_pool_smem_ &&
+            !ok(cudaMalloc(&d_spec_heap_, (size_t)grid_spec_ * std::max<size_t>(4, pool_b) + 16), err,
+                "cudaMalloc shading heap"))
+            return OSLG_ERR_CUDA;
+        sbargs_ = bargs_;
+        sbargs_.gheap = d_spec_heap_;
+        sbargs_.heap_slots = spec_.pool_slots;
+    }
     for (void*& e : ev_) {
         cudaEvent_t ev;
         if (!ok(cudaEventCreate(&ev), err, "event")) return OSLG_ERR_CUDA;
@@ -765,10 +792,18 @@ int Wavefront::enqueue_frame(void* stream, bool profile, std::string* err) {
         dev::k_scatter<<<grid_stream_, 256, 0, s>>>(a, cur, b);
         if (profile) cudaEventRecord(pev[b * 5 + 3], s);
         if (!ok(cudaGetLastError(), err, "wavefront launch")) return OSLG_ERR_CUDA;
-        if (!ok((cudaError_t)batch_variant_launch(maxt_, ppt_, smem_heap_, (unsigned)grid_shade_, (unsigned)block_,
-                                                  shmem_, stream, bargs_),
-                err, "shading launch"))
+        if (spec_.kernel) {
+            int pool_smem = spec_pool_smem_;
+            void* args[] = { &sbargs_, &pool_smem };
+            if (!ok(cudaLaunchKernel(reinterpret_cast<const void*>(spec_.kernel), dim3((unsigned)grid_spec_),
+                                     dim3((unsigned)block_), args, spec_shmem_, s),
+                    err, "specialized shading launch"))
+                return OSLG_ERR_CUDA;
+        } else if (!ok((cudaError_t)batch_variant_launch(maxt_, ppt_, smem_heap_, (unsigned)grid_shade_,
+                                                         (unsigned)block_, shmem_, stream, bargs_),
+                       err, "shading launch")) {
             return OSLG_ERR_CUDA;
+        }
         if (profile) cudaEventRecord(pev[b * 5 + 4], s);
         dev::k_update<<<grid_stream_, 256, 0, s>>>(a, cur, b, b == opt_.max_hits - 1 ? 1 : 0);
         if (profile) cudaEventRecord(pev[b * 5 + 5], s);

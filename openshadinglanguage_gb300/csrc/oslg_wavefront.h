@@ -22,6 +22,7 @@
 #include "oslg_batch.h"
 #include "oslg_exec.h"
 #include "oslg_host.h"
+#include "oslg_spec.h"
 
 namespace oslg {
 
@@ -61,8 +62,11 @@ class Wavefront {
 public:
     ~Wavefront();
     // prims/materials validated by the caller (oslg_capi.cpp)
+    // jit_dirs: {interpreter headers, cubin cache} to shade with a batch
+    // kernel specialized to the materials, or null for the interpreter
     int init(DeviceState& ds, const oslg_wavefront_options& o, const oslg_primitive* prims, int nprims,
-             const std::vector<const CompiledGroup*>& materials, std::string* err);
+             const std::vector<const CompiledGroup*>& materials, const std::string* jit_dirs, std::string* err);
+    bool specialized() const { return spec_.kernel != nullptr; }
     int render(float* d_path_radiance, float* d_image, void* stream, bool profile, std::string* err);
     int stats(WavefrontStats* s, std::string* err);
     int64_t paths() const { return npaths_; }
@@ -80,6 +84,11 @@ private:
     int grid_shade_ = 0, grid_stream_ = 0;
     float cam_[12] = {};  // eye, dir, right*tan*aspect, up*tan
     dev::BatchArgs bargs_{};
+    SpecBatchKernel spec_;         // specialized shading kernel (when built)
+    dev::BatchArgs sbargs_{};
+    int grid_spec_ = 0, spec_pool_smem_ = 0;
+    size_t spec_shmem_ = 0;
+    float* d_spec_heap_ = nullptr;
 
     // device memory
     dev::WfPrim* d_prims_ = nullptr;

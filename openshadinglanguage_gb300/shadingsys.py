@@ -220,6 +220,17 @@ class ShadingSystem:
         """A continuous-batching shading server on this system (see Server)."""
         return Server(self, **options)
 
+    def specialized_batch_source(self, groups):
+        """CUDA source of a persistent batch kernel specialized to `groups`."""
+        L = C.lib()
+        arr = (ctypes.c_void_p * len(groups))(*[g.handle.value for g in groups])
+        size = ctypes.c_size_t(0)
+        self._check(L.oslg_groups_specialized_batch_source(self._h, arr, len(groups), None, 0, ctypes.byref(size)))
+        buf = ctypes.create_string_buffer(size.value)
+        self._check(L.oslg_groups_specialized_batch_source(self._h, arr, len(groups), buf, size.value,
+                                                           ctypes.byref(size)))
+        return buf.value.decode()
+
     def wavefront(self, prims, materials, **options):
         """A wavefront path tracer over `prims` shaded by `materials` (see Wavefront)."""
         return Wavefront(self, prims, materials, **options)

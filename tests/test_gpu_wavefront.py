@@ -99,3 +99,20 @@ def test_graph_replay_and_profiled_frames_agree(scene):
     assert all(x >= 0 for x in s["ms_stage"]) and sum(s["ms_stage"]) > 0
     nog = ss.wavefront(prims, mats, use_graph=-1, **opts)
     assert float_equal(render(nog), a).all()
+
+
+def test_specialized_shading_matches_oracle():
+    """Attribute jit: the materials shade in one persistent batch kernel
+    specialized to their programs; paths stay bit-exact."""
+    ss = og.ShadingSystem()
+    ss.attribute("jit", 1)
+    mats = W.c5_materials(ss)
+    prims = W.c5_scene()
+    opts = dict(width=64, height=36, spp=2)
+    wf = ss.wavefront(prims, mats, **opts)
+    gpu = render(wf)
+    ref, hits, st = oracle_wavefront(opts, prims, mats)
+    assert st == 0
+    assert_paths_equal(gpu, ref)
+    assert wf.stats()["hits"] == hits.tolist()
+    assert ss.device_status() == 0
