@@ -123,63 +123,91 @@ __device__ __forceinline__ bool hit_quad(const WfPrim& q, V o, V d, float* t) {
     return true;
 }
 
+// Slab test of one box: entry distance, or INFINITY when the box is missed
+// or starts beyond `best` (a box starting exactly at `best` is kept: a hit
+// at the same distance with a lower id may be inside).
+__device__ __forceinline__ float box_entry(float lx, float ly, float lz, float hx, float hy, float hz, V o, V inv,
+                                           float best) {
+    const float tx0 = (lx - o.x) * inv.x, tx1 = (hx - o.x) * inv.x;
+    const float ty0 = (ly - o.y) * inv.y, ty1 = (hy - o.y) * inv.y;
+    const float tz0 = (lz - o.z) * inv.z, tz1 = (hz - o.z) * inv.z;
+    const float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), 0.0f));
+    const float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
+    return (tn <= tf && tn <= best) ? tn : INFINITY;
+}
+
 // Nearest hit over the BVH; ties go to the lower primitive id, so the
-// result equals a scan of all primitives in id order.
+// result equals a scan of all primitives in id order. Children are visited
+// near first; stacked subtrees whose entry lies beyond the current best are
+// skipped when popped.
 __device__ void traverse(const WfNode* __restrict__ nodes, const WfPrim* __restrict__ prims, V o, V d, int skip,
                          int* rec_out, float* t_out) {
     const V inv = mk(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
     float best = INFINITY;
     int best_rec = -1, best_id = INT_MAX;
-    int stack[32];
-    int sp = 0, node = 0;
+    int stack_ref[kWfStack];
+    float stack_t[kWfStack];
+    int sp = 0;
+    int ref = 0;
     for (;;) {
-        const float4 n0 = __ldg(reinterpret_cast<const float4*>(nodes + node));
-        const float4 n1 = __ldg(reinterpret_cast<const float4*>(nodes + node) + 1);
-        const float tx0 = (n0.x - o.x) * inv.x, tx1 = (n1.x - o.x) * inv.x;
-        const float ty0 = (n0.y - o.y) * inv.y, ty1 = (n1.y - o.y) * inv.y;
-        const float tz0 = (n0.z - o.z) * inv.z, tz1 = (n1.z - o.z) * inv.z;
-        const float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), 0.0f));
-        const float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
-        if (tn <= tf && tn <= best) {
-            const int first = __float_as_int(n0.w), count = __float_as_int(n1.w);
-            if (count > 0) {
-                for (int k = first; k < first + count; ++k) {
-                    WfPrim q;
-                    const float4* src = reinterpret_cast<const float4*>(prims + k);
-                    q.r[0] = __ldg(src);
-                    q.r[2] = __ldg(src + 2);
-                    q.r[4] = __ldg(src + 4);
-                    const int id = prim_id(q);
-                    float t;
-                    bool h;
-                    if (prim_kind(q) == OSLG_PRIM_SPHERE) {
-                        h = hit_sphere(q, o, d, id == skip, &t);
-                    } else {
-                        if (id == skip) continue;
-                        q.r[3] = __ldg(src + 3);
-                        q.r[5] = __ldg(src + 5);
-                        h = hit_quad(q, o, d, &t);
-                    }
-                    if (h && (t < best || (t == best && id < best_id))) {
-                        best = t;
-                        best_rec = k;
-                        best_id = id;
-                    }
+        if (ref >= 0) {
+            const float4* nv = reinterpret_cast<const float4*>(nodes + ref);
+            const float4 na = __ldg(nv), nb = __ldg(nv + 1), nc = __ldg(nv + 2);
+            const int4 nd = __ldg(reinterpret_cast<const int4*>(nv + 3));
+            const float tl = box_entry(na.x, na.y, na.z, na.w, nb.x, nb.y, o, inv, best);
+            const float tr = box_entry(nb.z, nb.w, nc.x, nc.y, nc.z, nc.w, o, inv, best);
+            const bool hl = tl != INFINITY, hr = tr != INFINITY;
+            if (hl && hr) {
+                const bool lfirst = tl <= tr;
+                if (sp < kWfStack) {
+                    stack_ref[sp] = lfirst ? nd.y : nd.x;
+                    stack_t[sp] = lfirst ? tr : tl;
+                    ++sp;
                 }
-            } else {
-                const int axis = -count - 1;
-                const float da = axis == 0 ? d.x : (axis == 1 ? d.y : d.z);
-                const int nearc = da >= 0.0f ? first : first + 1;
-                if (sp < 32) stack[sp++] = nearc == first ? first + 1 : first;
-                node = nearc;
+                ref = lfirst ? nd.x : nd.y;
                 continue;
             }
+            if (hl) { ref = nd.x; continue; }
+            if (hr) { ref = nd.y; continue; }
+        } else {
+            const int x = ~ref;
+            const int first = x >> 4, count = x & 15;
+            for (int k = first; k < first + count; ++k) {
+                WfPrim q;
+                const float4* src = reinterpret_cast<const float4*>(prims + k);
+                q.r[0] = __ldg(src);
+                q.r[2] = __ldg(src + 2);
+                q.r[4] = __ldg(src + 4);
+                const int id = prim_id(q);
+                float t;
+                bool h;
+                if (prim_kind(q) == OSLG_PRIM_SPHERE) {
+                    h = hit_sphere(q, o, d, id == skip, &t);
+                } else {
+                    if (id == skip) continue;
+                    q.r[3] = __ldg(src + 3);
+                    q.r[5] = __ldg(src + 5);
+                    h = hit_quad(q, o, d, &t);
+                }
+                if (h && (t < best || (t == best && id < best_id))) {
+                    best = t;
+                    best_rec = k;
+                    best_id = id;
+                }
+            }
         }
-        if (sp == 0) break;
-        node = stack[--sp];
+        // next stacked subtree that can still hold the nearest hit
+        for (;;) {
+            if (sp == 0) {
+                *rec_out = best_rec;
+                *t_out = best;
+                return;
+            }
+            --sp;
+            if (!(stack_t[sp] > best)) break;
+        }
+        ref = stack_ref[sp];
     }
-    *rec_out = best_rec;
-    *t_out = best;
 }
 
 struct WfArgs {
@@ -461,44 +489,182 @@ struct BuildPrim {
     int id;
 };
 
-// Median-split BVH over primitive bounds, padded so that rounding in the
-// slab test never culls a primitive the exact scan would hit.
-void build_bvh(std::vector<BuildPrim>& bp, int begin, int end, int node, std::vector<dev::WfNode>& nodes) {
-    float lo[3] = { INFINITY, INFINITY, INFINITY }, hi[3] = { -INFINITY, -INFINITY, -INFINITY };
+// Binned-SAH BVH over padded primitive bounds (padding keeps rounding in
+// the slab test from culling a primitive the exact scan would hit). Leaves
+// hold up to 4 primitives; below a depth of 24 the split is the median so
+// that the traversal stack never overflows.
+struct TmpNode {
+    float lo[3], hi[3];
+    int left = -1, right = -1, first = 0, count = 0;
+};
+
+float half_area(const float* lo, const float* hi) {
+    const float dx = std::max(0.0f, hi[0] - lo[0]), dy = std::max(0.0f, hi[1] - lo[1]),
+                dz = std::max(0.0f, hi[2] - lo[2]);
+    return dx * dy + dy * dz + dz * dx;
+}
+
+int build_sah(std::vector<BuildPrim>& bp, int begin, int end, int depth, std::vector<TmpNode>& out) {
+    TmpNode N;
     float clo[3] = { INFINITY, INFINITY, INFINITY }, chi[3] = { -INFINITY, -INFINITY, -INFINITY };
+    for (int k = 0; k < 3; ++k) {
+        N.lo[k] = INFINITY;
+        N.hi[k] = -INFINITY;
+    }
     for (int i = begin; i < end; ++i)
         for (int k = 0; k < 3; ++k) {
-            lo[k] = std::min(lo[k], bp[i].lo[k]);
-            hi[k] = std::max(hi[k], bp[i].hi[k]);
+            N.lo[k] = std::min(N.lo[k], bp[i].lo[k]);
+            N.hi[k] = std::max(N.hi[k], bp[i].hi[k]);
             clo[k] = std::min(clo[k], bp[i].c[k]);
             chi[k] = std::max(chi[k], bp[i].c[k]);
         }
-    dev::WfNode& N = nodes[node];
-    for (int k = 0; k < 3; ++k) {
-        N.lo[k] = lo[k];
-        N.hi[k] = hi[k];
-    }
     const int n = end - begin;
-    if (n <= 2) {
-        N.first = begin;
-        N.count = n;
-        return;
+    const int me = (int)out.size();
+    out.push_back(N);
+    if (n <= 1) {
+        out[me].first = begin;
+        out[me].count = n;
+        return me;
     }
-    int axis = 0;
-    for (int k = 1; k < 3; ++k)
-        if (chi[k] - clo[k] > chi[axis] - clo[axis]) axis = k;
-    const int mid = begin + n / 2;
-    std::nth_element(bp.begin() + begin, bp.begin() + mid, bp.begin() + end,
-                     [axis](const BuildPrim& x, const BuildPrim& y) {
-                         return x.c[axis] < y.c[axis] || (x.c[axis] == y.c[axis] && x.id < y.id);
-                     });
-    const int left = (int)nodes.size();
-    nodes.emplace_back();
-    nodes.emplace_back();
-    nodes[node].first = left;
-    nodes[node].count = -axis - 1;
-    build_bvh(bp, begin, mid, left, nodes);
-    build_bvh(bp, mid, end, left + 1, nodes);
+    const int kBins = 16;
+    int best_axis = -1, best_split = 0;
+    float best_cost = INFINITY;
+    if (depth < 24) {
+        for (int ax = 0; ax < 3; ++ax) {
+            const float ext = chi[ax] - clo[ax];
+            if (!(ext > 0.0f)) continue;
+            int cnt[kBins] = {};
+            float blo[kBins][3], bhi[kBins][3];
+            for (int b = 0; b < kBins; ++b)
+                for (int k = 0; k < 3; ++k) {
+                    blo[b][k] = INFINITY;
+                    bhi[b][k] = -INFINITY;
+                }
+            for (int i = begin; i < end; ++i) {
+                int b = (int)((bp[i].c[ax] - clo[ax]) / ext * kBins);
+                b = std::min(kBins - 1, std::max(0, b));
+                ++cnt[b];
+                for (int k = 0; k < 3; ++k) {
+                    blo[b][k] = std::min(blo[b][k], bp[i].lo[k]);
+                    bhi[b][k] = std::max(bhi[b][k], bp[i].hi[k]);
+                }
+            }
+            for (int s = 1; s < kBins; ++s) {
+                float llo[3] = { INFINITY, INFINITY, INFINITY }, lhi[3] = { -INFINITY, -INFINITY, -INFINITY };
+                float rlo[3] = { INFINITY, INFINITY, INFINITY }, rhi[3] = { -INFINITY, -INFINITY, -INFINITY };
+                int nl = 0, nr = 0;
+                for (int b = 0; b < kBins; ++b) {
+                    float* lo = b < s ? llo : rlo;
+                    float* hi = b < s ? lhi : rhi;
+                    (b < s ? nl : nr) += cnt[b];
+                    for (int k = 0; k < 3; ++k) {
+                        lo[k] = std::min(lo[k], blo[b][k]);
+                        hi[k] = std::max(hi[k], bhi[b][k]);
+                    }
+                }
+                if (!nl || !nr) continue;
+                const float cost = half_area(llo, lhi) * nl + half_area(rlo, rhi) * nr;
+                if (cost < best_cost) {
+                    best_cost = cost;
+                    best_axis = ax;
+                    best_split = s;
+                }
+            }
+        }
+        // a leaf when splitting costs more than intersecting everything here
+        if (n <= 4 && !(best_cost + half_area(N.lo, N.hi) < half_area(N.lo, N.hi) * n)) best_axis = -2;
+    }
+    if (best_axis == -2) {
+        out[me].first = begin;
+        out[me].count = n;
+        return me;
+    }
+    int mid;
+    if (best_axis >= 0) {
+        const float ext = chi[best_axis] - clo[best_axis];
+        auto it = std::partition(bp.begin() + begin, bp.begin() + end, [&](const BuildPrim& p) {
+            int b = (int)((p.c[best_axis] - clo[best_axis]) / ext * kBins);
+            b = std::min(kBins - 1, std::max(0, b));
+            return b < best_split;
+        });
+        mid = (int)(it - bp.begin());
+    } else {
+        mid = begin;
+    }
+    if (mid == begin || mid == end) {  // median of the longest centroid axis
+        int axis = 0;
+        for (int k = 1; k < 3; ++k)
+            if (chi[k] - clo[k] > chi[axis] - clo[axis]) axis = k;
+        mid = begin + n / 2;
+        std::nth_element(bp.begin() + begin, bp.begin() + mid, bp.begin() + end,
+                         [axis](const BuildPrim& x, const BuildPrim& y) {
+                             return x.c[axis] < y.c[axis] || (x.c[axis] == y.c[axis] && x.id < y.id);
+                         });
+    }
+    const int l = build_sah(bp, begin, mid, depth + 1, out);
+    const int r = build_sah(bp, mid, end, depth + 1, out);
+    out[me].left = l;
+    out[me].right = r;
+    return me;
+}
+
+int tree_depth(const std::vector<TmpNode>& t, int i) {
+    if (t[i].left < 0) return 1;
+    return 1 + std::max(tree_depth(t, t[i].left), tree_depth(t, t[i].right));
+}
+
+// Flatten: one device node per inner node, children boxes in the parent.
+void flatten(const std::vector<TmpNode>& t, std::vector<dev::WfNode>& out) {
+    std::vector<int> index(t.size(), -1);
+    // inner nodes in depth-first order; node 0 is the root (a lone leaf root
+    // becomes a node with an empty right child)
+    std::vector<int> order;
+    std::vector<int> st = { 0 };
+    while (!st.empty()) {
+        const int i = st.back();
+        st.pop_back();
+        if (t[i].left < 0 && i != 0) continue;
+        index[i] = (int)order.size();
+        order.push_back(i);
+        if (t[i].left >= 0) {
+            st.push_back(t[i].right);
+            st.push_back(t[i].left);
+        }
+    }
+    auto ref_of = [&](int c) {
+        if (t[c].left >= 0) return index[c];
+        return ~((t[c].first << 4) | t[c].count);
+    };
+    out.resize(order.size());
+    for (size_t k = 0; k < order.size(); ++k) {
+        const TmpNode& N = t[order[k]];
+        dev::WfNode& D = out[k];
+        float llo[3], lhi[3], rlo[3], rhi[3];
+        int lref, rref;
+        if (N.left >= 0) {
+            for (int j = 0; j < 3; ++j) {
+                llo[j] = t[N.left].lo[j];
+                lhi[j] = t[N.left].hi[j];
+                rlo[j] = t[N.right].lo[j];
+                rhi[j] = t[N.right].hi[j];
+            }
+            lref = ref_of(N.left);
+            rref = ref_of(N.right);
+        } else {  // root leaf
+            for (int j = 0; j < 3; ++j) {
+                llo[j] = N.lo[j];
+                lhi[j] = N.hi[j];
+                rlo[j] = INFINITY;
+                rhi[j] = -INFINITY;
+            }
+            lref = ~((N.first << 4) | N.count);
+            rref = ~0;
+        }
+        D.a = make_float4(llo[0], llo[1], llo[2], lhi[0]);
+        D.b = make_float4(lhi[1], lhi[2], rlo[0], rlo[1]);
+        D.c = make_float4(rlo[2], rhi[0], rhi[1], rhi[2]);
+        D.d = make_int4(lref, rref, 0, 0);
+    }
 }
 }  // namespace
 
@@ -587,8 +753,25 @@ int Wavefront::init(DeviceState& ds, const oslg_wavefront_options& o, const oslg
             b.c[k] = 0.5f * (b.lo[k] + b.hi[k]);
         }
     }
-    std::vector<dev::WfNode> nodes(1);
-    build_bvh(bp, 0, nprims, 0, nodes);
+    std::vector<TmpNode> tree;
+    tree.reserve(2 * std::max(1, nprims));
+    if (nprims > 0) build_sah(bp, 0, nprims, 0, tree);
+    if (!tree.empty() && tree_depth(tree, 0) > dev::kWfStack - 1) {
+        // pathological scene: fall back to median splits (depth ~ log2 n)
+        tree.clear();
+        build_sah(bp, 0, nprims, 1 << 20, tree);
+    }
+    std::vector<dev::WfNode> nodes;
+    if (tree.empty()) {
+        dev::WfNode e;
+        e.a = make_float4(INFINITY, INFINITY, INFINITY, -INFINITY);
+        e.b = make_float4(-INFINITY, -INFINITY, INFINITY, INFINITY);
+        e.c = make_float4(INFINITY, -INFINITY, -INFINITY, -INFINITY);
+        e.d = make_int4(~0, ~0, 0, 0);
+        nodes.push_back(e);
+    } else {
+        flatten(tree, nodes);
+    }
     nnodes_ = (int)nodes.size();
     std::vector<int32_t> order(nprims);
     for (int i = 0; i < nprims; ++i) order[i] = bp[i].id;

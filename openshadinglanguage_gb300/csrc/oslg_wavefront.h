@@ -39,14 +39,16 @@ namespace dev {
 struct WfPrim {
     float4 r[6];
 };
-// BVH node (32 B): leaf when count > 0 (records [first, first+count)),
-// inner otherwise with children first, first+1 and split axis -count-1.
+// BVH node (64 B): the boxes of both children, so that one visit tests
+// both. A child reference >= 0 is an inner node; < 0 is a leaf ~(first << 4
+// | count): records [first, first + count), count <= 15.
 struct WfNode {
-    float lo[3];
-    int32_t first;
-    float hi[3];
-    int32_t count;
+    float4 a;  // left lo.xyz, left hi.x
+    float4 b;  // left hi.yz, right lo.xy
+    float4 c;  // right lo.z, right hi.xyz
+    int4 d;    // left ref, right ref, 0, 0
 };
+static const int kWfStack = 32;  // traversal stack; the build keeps the depth below it
 }  // namespace dev
 
 struct WavefrontStats {
