@@ -370,63 +370,98 @@ __global__ void __launch_bounds__(1024) k_plan(const __grid_constant__ WfArgs a,
 }
 
 // globals_from_hit (simpleraytracer.cpp:890-932) for the analytic
-// primitives, written material-sorted, plus the sampling record.
+// primitives, written material-sorted, plus the sampling record. Each CTA
+// takes 256 active hits, orders them by material in shared memory and
+// reserves one slot range per material, so that consecutive threads write
+// consecutive slots.
 __global__ void __launch_bounds__(256) k_scatter(const __grid_constant__ WfArgs a, int cur, int bounce) {
+    __shared__ uint32_t s_cnt[kWfMaxMaterials], s_pre[kWfMaxMaterials], s_base[kWfMaxMaterials];
+    __shared__ uint32_t s_order[256];
     const int64_t np = a.np, cap = a.cap;
     const uint32_t n = a.ctl[C_NACT + cur];
     const uint32_t* act = a.act + (int64_t)cur * np;
     const float* st = a.st;
     float* gl = a.gl;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const int rec = a.hit_rec[i];
-        if (rec < 0) continue;
-        WfPrim q;
-        const float4* src = reinterpret_cast<const float4*>(a.prims + rec);
-        for (int k = 0; k < 6; ++k) q.r[k] = __ldg(src + k);
-        const int m = prim_mat(q);
-        const int64_t slot = (int64_t)a.ctl[C_OFF + m] + agg_inc(a.ctl + C_CURSOR, m);
-        const int64_t p = act[i];
-        const V o = mk(st[(S_O + 0) * np + p], st[(S_O + 1) * np + p], st[(S_O + 2) * np + p]);
-        const V d = mk(st[(S_D + 0) * np + p], st[(S_D + 1) * np + p], st[(S_D + 2) * np + p]);
-        const float t = a.hit_t[i];
-        const V P = vadd(o, vmul(d, t));
-        V N, dPdu, dPdv;
-        float u, v;
-        if (prim_kind(q) == OSLG_PRIM_SPHERE) {
-            const float r = q.r[0].w;
-            N = vnorm(vsub(P, xyz(q.r[0])));
-            // ortho() of src/testrender/raytracer.h:41-47
-            const V x = vnorm(fabsf(N.x) > 0.01f ? mk(N.z, 0.0f, -N.x) : mk(0.0f, -N.z, N.y));
-            dPdu = vmul(x, r);
-            dPdv = vmul(vcross(N, x), r);
-            u = 0.5f * (N.x + 1.0f);
-            v = 0.5f * (N.y + 1.0f);
-        } else {
-            N = xyz(q.r[3]);
-            const V h = vsub(P, xyz(q.r[0]));
-            u = vdot(h, xyz(q.r[4]));
-            v = vdot(h, xyz(q.r[5]));
-            dPdu = xyz(q.r[1]);
-            dPdv = xyz(q.r[2]);
+    for (uint32_t chunk = blockIdx.x * 256u; chunk < n; chunk += gridDim.x * 256u) {
+        for (int m = threadIdx.x; m < a.nmat; m += blockDim.x) s_cnt[m] = 0;
+        __syncthreads();
+        const uint32_t i0 = chunk + threadIdx.x;
+        int mat = -1;
+        uint32_t rank = 0;
+        if (i0 < n) {
+            const int rec0 = a.hit_rec[i0];
+            if (rec0 >= 0) {
+                mat = __float_as_int(__ldg(&a.prims[rec0].r[3].w));
+                rank = atomicAdd(&s_cnt[mat], 1u);
+            }
         }
-        V Ng = N;
-        if (vdot(Ng, d) > 0.0f) {  // backfacing
-            N = vneg(N);
-            Ng = vneg(Ng);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t acc = 0;
+            for (int m = 0; m < a.nmat; ++m) {
+                s_pre[m] = acc;
+                acc += s_cnt[m];
+            }
         }
-        const float vals[G_PLANES] = { P.x, P.y, P.z, d.x, d.y, d.z, N.x, N.y, N.z, Ng.x, Ng.y, Ng.z,
-                                       u, v, dPdu.x, dPdu.y, dPdu.z, dPdv.x, dPdv.y, dPdv.z };
+        for (int m = threadIdx.x; m < a.nmat; m += blockDim.x)
+            s_base[m] = s_cnt[m] ? a.ctl[C_OFF + m] + atomicAdd(a.ctl + C_CURSOR + m, s_cnt[m]) : 0u;
+        __syncthreads();
+        if (mat >= 0) s_order[s_pre[mat] + rank] = i0;
+        uint32_t hits = 0;
+        for (int m = 0; m < a.nmat; ++m) hits += s_cnt[m];
+        __syncthreads();
+        if (threadIdx.x < hits) {
+            const uint32_t i = s_order[threadIdx.x];
+            const int rec = a.hit_rec[i];
+            WfPrim q;
+            const float4* src = reinterpret_cast<const float4*>(a.prims + rec);
+            for (int k = 0; k < 6; ++k) q.r[k] = __ldg(src + k);
+            const int m = prim_mat(q);
+            const int64_t slot = (int64_t)s_base[m] + (threadIdx.x - s_pre[m]);
+            const int64_t p = act[i];
+            const V o = mk(st[(S_O + 0) * np + p], st[(S_O + 1) * np + p], st[(S_O + 2) * np + p]);
+            const V d = mk(st[(S_D + 0) * np + p], st[(S_D + 1) * np + p], st[(S_D + 2) * np + p]);
+            const float t = a.hit_t[i];
+            const V P = vadd(o, vmul(d, t));
+            V N, dPdu, dPdv;
+            float u, v;
+            if (prim_kind(q) == OSLG_PRIM_SPHERE) {
+                const float r = q.r[0].w;
+                N = vnorm(vsub(P, xyz(q.r[0])));
+                // ortho() of src/testrender/raytracer.h:41-47
+                const V x = vnorm(fabsf(N.x) > 0.01f ? mk(N.z, 0.0f, -N.x) : mk(0.0f, -N.z, N.y));
+                dPdu = vmul(x, r);
+                dPdv = vmul(vcross(N, x), r);
+                u = 0.5f * (N.x + 1.0f);
+                v = 0.5f * (N.y + 1.0f);
+            } else {
+                N = xyz(q.r[3]);
+                const V h = vsub(P, xyz(q.r[0]));
+                u = vdot(h, xyz(q.r[4]));
+                v = vdot(h, xyz(q.r[5]));
+                dPdu = xyz(q.r[1]);
+                dPdv = xyz(q.r[2]);
+            }
+            V Ng = N;
+            if (vdot(Ng, d) > 0.0f) {  // backfacing
+                N = vneg(N);
+                Ng = vneg(Ng);
+            }
+            const float vals[G_PLANES] = { P.x, P.y, P.z, d.x, d.y, d.z, N.x, N.y, N.z, Ng.x, Ng.y, Ng.z,
+                                           u, v, dPdu.x, dPdu.y, dPdu.z, dPdv.x, dPdv.y, dPdv.z };
 #pragma unroll
-        for (int k = 0; k < G_PLANES; ++k) gl[k * cap + slot] = vals[k];
-        float* ud = a.ud + slot * kWfInFloats;
-        ud[0] = wf_rand(a.seed, (uint32_t)p, (uint32_t)bounce, 0u);
-        ud[1] = wf_rand(a.seed, (uint32_t)p, (uint32_t)bounce, 1u);
-        ud[2] = wf_rand(a.seed, (uint32_t)p, (uint32_t)bounce, 2u);
-        ud[3] = st[(S_TP + 0) * np + p];
-        ud[4] = st[(S_TP + 1) * np + p];
-        ud[5] = st[(S_TP + 2) * np + p];
-        ud[6] = 0.0f;
-        a.hit_slot[i] = (uint32_t)slot;
+            for (int k = 0; k < G_PLANES; ++k) gl[k * cap + slot] = vals[k];
+            float* ud = a.ud + slot * kWfInFloats;
+            ud[0] = wf_rand(a.seed, (uint32_t)p, (uint32_t)bounce, 0u);
+            ud[1] = wf_rand(a.seed, (uint32_t)p, (uint32_t)bounce, 1u);
+            ud[2] = wf_rand(a.seed, (uint32_t)p, (uint32_t)bounce, 2u);
+            ud[3] = st[(S_TP + 0) * np + p];
+            ud[4] = st[(S_TP + 1) * np + p];
+            ud[5] = st[(S_TP + 2) * np + p];
+            ud[6] = 0.0f;
+            a.hit_slot[i] = (uint32_t)slot;
+        }
+        __syncthreads();
     }
 }
 
@@ -811,7 +846,11 @@ int Wavefront::init(DeviceState& ds, const oslg_wavefront_options& o, const oslg
     int per_sm_trace = 0;
     if (!ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_trace, dev::k_trace, 256, 0), err, "occupancy"))
         return OSLG_ERR_CUDA;
-    grid_stream_ = ds.sm_count * std::max(1, per_sm_trace);
+    grid_trace_ = ds.sm_count * std::max(1, per_sm_trace);
+    int per_sm_scatter = 0;
+    if (!ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_scatter, dev::k_scatter, 256, 0), err, "occupancy"))
+        return OSLG_ERR_CUDA;
+    grid_stream_ = ds.sm_count * std::max(1, per_sm_scatter);
 
     // device memory
     const int64_t np = npaths_, cap = cap_;
@@ -968,7 +1007,7 @@ int Wavefront::enqueue_frame(void* stream, bool profile, std::string* err) {
     }
     for (int b = 0; b < opt_.max_hits; ++b) {
         const int cur = b & 1;
-        dev::k_trace<<<grid_stream_, 256, 0, s>>>(a, cur);
+        dev::k_trace<<<grid_trace_, 256, 0, s>>>(a, cur);
         if (profile) cudaEventRecord(pev[b * 5 + 1], s);
         dev::k_plan<<<1, 1024, 0, s>>>(a, cur, b);
         if (profile) cudaEventRecord(pev[b * 5 + 2], s);

@@ -83,7 +83,7 @@ private:
     int nprims_ = 0, nmat_ = 0, tile_ = 0, block_ = 256, ppt_ = 1, maxt_ = 256;
     bool smem_heap_ = false;
     size_t shmem_ = 0;
-    int grid_shade_ = 0, grid_stream_ = 0;
+    int grid_shade_ = 0, grid_stream_ = 0, grid_trace_ = 0;
     float cam_[12] = {};  // eye, dir, right*tan*aspect, up*tan
     dev::BatchArgs bargs_{};
     SpecBatchKernel spec_;         // specialized shading kernel (when built)
