@@ -155,9 +155,11 @@ int oslg_group_bsdf_eval(oslg_system* sys, oslg_group* group, const char* closur
 /* Renderer-side sampling of a closure output, the per-hit step of
  * testrender's path loop (src/testrender/simpleraytracer.cpp:1038-1079):
  * the closure tree is walked (emission adds to Le; diffuse, oren_nayar and
- * microfacet "ggx" with refract 0/1/2 become lobes), prepared with the
- * path weight and sampled (src/testrender/shading.h:322-398). Reads
- * {rx, ry, rz, path_weight.rgb, absorb} (7 floats) per point at
+ * microfacet "ggx" with refract 0/1/2 and sheen_bsdf become lobes),
+ * prepared with the path weight and sampled (src/testrender/shading.h:322-398).
+ * Reads {rx, ry, rz, path_weight.rgb, absorb, ray_roughness, backfacing}
+ * (9 floats; the last two feed BSDL's roughness regularization and
+ * backfacing rule) per point at
  * userdata_base + in_offset + i*in_stride; writes {wi.xyz, weight.rgb,
  * pdf, Le.rgb, roughness} (11 floats) at output_base + offset + i*stride.
  * No counterpart as one call in the reference, which does these steps in
@@ -354,7 +356,7 @@ int oslg_server_get_stats(oslg_server* server, oslg_server_stats* out);
  * src/testrender/scene.cpp; here they are intersected exactly). Material k
  * is a group whose closure output is sampled with
  * oslg_group_bsdf_sample(..., offset 0, stride 44, in_offset 0, in_stride
- * 28). Differences from testrender, by design: no light sampling (emission
+ * 36). Differences from testrender, by design: no light sampling (emission
  * is gathered by BSDF sampling, MIS weight 1), no background importance
  * sampling or media, and Russian roulette with a fixed survival
  * probability after every hit. */

@@ -957,7 +957,7 @@ int oslg_wavefront_create(oslg_system* sys, const oslg_wavefront_options* opts, 
             if (!found)
                 return fail(sys, OSLG_ERR_ARG,
                             "wavefront: material group '" + g->g.name +
-                                "' has no bsdf_sample output at offset 0, stride 44, in_offset 0, in_stride 28");
+                                "' has no bsdf_sample output at offset 0, stride 44, in_offset 0, in_stride 36");
             int rc = ensure_compiled(sys, g, true);
             if (rc != OSLG_OK) return rc;
             mats.push_back(g->g.compiled.get());

@@ -1,5 +1,6 @@
-// The executor's own single-precision exp and sincos for the Gabor impulse
-// loop, where libm-accurate double evaluation would run on the FP64 pipe.
+// The executor's own single-precision exp, sincos, log and power for the
+// Gabor impulse loop and the sheen distribution, where libm-accurate double
+// evaluation would run on the FP64 pipe.
 // Written from the mathematics: Cody & Waite argument reduction (a short
 // constant head whose products with the integer multiple are exact, plus a
 // tail), Taylor polynomials of the reduced argument in Horner form, and a
@@ -64,6 +65,45 @@ __device__ __forceinline__ void own_sincos(float x, float* s, float* c) {
     case 2: *s = -sp; *c = -cp; break;
     default: *s = -cp; *c = sp; break;
     }
+}
+
+
+// Natural log for x > 0 (0 -> -inf, negative or NaN -> NaN): exponent split,
+// mantissa folded into [sqrt(1/2), sqrt(2)), ln m = 2 atanh(s) with
+// s = (m-1)/(m+1) as an odd series to s^11, ln 2 in a head and tail.
+__device__ __forceinline__ float own_log(float x) {
+    if (!(x > 0.0f)) return x == 0.0f ? __int_as_float(0xff800000) : __int_as_float(0x7fc00000);
+    if (x == __int_as_float(0x7f800000)) return x;
+    int e = 0;
+    if (x < 1.17549435e-38f) {  // subnormal: scale into the normal range
+        x = x * 8388608.0f;
+        e = -23;
+    }
+    const uint32_t b = __float_as_uint(x);
+    e += (int)(b >> 23) - 127;
+    float m = __uint_as_float((b & 0x007fffffu) | 0x3f800000u);
+    if (m > 1.41421356f) {
+        m = m * 0.5f;
+        e += 1;
+    }
+    const float s = (m - 1.0f) / (m + 1.0f);
+    const float s2 = s * s;
+    float p = 0.0909090936f;
+    p = 0.111111112f + s2 * p;
+    p = 0.142857149f + s2 * p;
+    p = 0.200000003f + s2 * p;
+    p = 0.333333343f + s2 * p;
+    p = 1.0f + s2 * p;
+    const float fe = (float)e;
+    return fe * 0.693359375f + ((s + s) * p + fe * -0.00021219444170128554f);
+}
+
+// x^y for x >= 0, y > 0 as own_exp(y * own_log(x)) (about 1e-5 relative
+// for |y ln x| near 100): the sheen distribution's power.
+__device__ __forceinline__ float own_pow_pos(float x, float y) {
+    if (x == 0.0f) return 0.0f;
+    if (x == 1.0f) return 1.0f;
+    return own_exp(y * own_log(x));
 }
 
 }  // namespace dev

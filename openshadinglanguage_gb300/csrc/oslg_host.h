@@ -136,7 +136,7 @@ struct BsdfEvalRequest {
 struct BsdfSampleRequest {
     std::string closure;
     int64_t offset = 0, stride = 44;        // outputs
-    int64_t in_offset = 0, in_stride = 28;  // userdata
+    int64_t in_offset = 0, in_stride = 36;  // userdata
 };
 
 struct SpecKernel;  // oslg_spec.h

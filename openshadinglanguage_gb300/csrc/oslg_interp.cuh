@@ -1471,11 +1471,13 @@ static __device__ void h_store_closure(const Lane& L, const uint32_t* a, char* b
 // parameters stay in the heap (node params) and are read when used.
 struct Lobes {
     int n;
-    int kind[OSLG_LOBES_MAX];  // 0 diffuse, 1 ggx, 2 oren-nayar
+    int kind[OSLG_LOBES_MAX];  // 0 diffuse, 1 ggx, 2 oren-nayar, 3 sheen
     float w[OSLG_LOBES_MAX][3];
     float pdf[OSLG_LOBES_MAX];
     uint32_t p[OSLG_LOBES_MAX];
     float Le[3];
+    float path_rough;  // roughness of the incoming ray (BSDL regularization)
+    bool backfacing;
 };
 // Loops over the lobe list: unrolled over the capacity (constant indices)
 // in a fixed-index build, a plain loop over n otherwise.
@@ -1485,9 +1487,11 @@ struct Lobes {
 #define OSLG_FOR_LOBES(i, B) for (int i = 0; i < (B).n; ++i)
 #endif
 __device__ __forceinline__ void lobes_build(const Lane& L, const ClosurePools& P, uint32_t root, uint32_t ggx,
-                                            uint32_t* st, Lobes& B) {
+                                            uint32_t* st, Lobes& B, float path_rough = 0.0f, bool backfacing = false) {
     B.n = 0;
     B.Le[0] = B.Le[1] = B.Le[2] = 0.0f;
+    B.path_rough = path_rough;
+    B.backfacing = backfacing;
     closure_walk(L, P, root, st, [&](int id, const float* cw, uint32_t params) {
         int k = -1;
         if (id == 1) {  // EMISSION_ID
@@ -1496,6 +1500,7 @@ __device__ __forceinline__ void lobes_build(const Lane& L, const ClosurePools& P
         }
         if (id == 3) k = 0;  // DIFFUSE_ID
         else if (id == 4) k = 2;  // OREN_NAYAR_ID
+        else if (id == 23 && hgetu(L, params + 7) == 0u) k = 3;  // MX_SHEEN_ID, Conty-Kulla mode
         else if (id == 8 && hgetu(L, params + 0) == ggx) {  // MICROFACET_ID "ggx"
             const int r = (int)hgetu(L, params + 10);
             if (r >= 0 && r <= 2) k = 1;
@@ -1528,8 +1533,14 @@ __device__ __forceinline__ GGXLobe lobe_ggx(const Lane& L, uint32_t p) {
     g.refract = (int)hgetu(L, p + 10);
     return g;
 }
+__device__ __forceinline__ SheenLobeDev lobe_sheen(const Lane& L, const Lobes& B, uint32_t p, V3 wo) {
+    const float albedo[3] = { hget(L, p + 3), hget(L, p + 4), hget(L, p + 5) };
+    return sheen_make(v3(hget(L, p + 0), hget(L, p + 1), hget(L, p + 2)), albedo, hget(L, p + 6), wo, B.path_rough,
+                      B.backfacing);
+}
 __device__ __forceinline__ BsdfSample lobe_eval(const Lane& L, const Lobes& B, int i, V3 wo, V3 wi) {
     const uint32_t p = B.p[i];
+    if (B.kind[i] == 3) return sheen_eval(lobe_sheen(L, B, p, wo), wo, wi);
     if (B.kind[i] == 0) {
         BsdfSample s = diffuse_eval(v3(hget(L, p + 0), hget(L, p + 1), hget(L, p + 2)), wi);
         s.wi = wi;
@@ -1545,6 +1556,7 @@ __device__ __forceinline__ BsdfSample lobe_eval(const Lane& L, const Lobes& B, i
 __device__ __forceinline__ BsdfSample lobe_sample(const Lane& L, const Lobes& B, int i, V3 wo, float rx, float ry,
                                                   float rz) {
     const uint32_t p = B.p[i];
+    if (B.kind[i] == 3) return sheen_sample(lobe_sheen(L, B, p, wo), wo, rx, ry);
     if (B.kind[i] == 0) return diffuse_sample(v3(hget(L, p + 0), hget(L, p + 1), hget(L, p + 2)), rx, ry);
     if (B.kind[i] == 1) return ggx_sample(lobe_ggx(L, p), wo, rx, ry, rz);
     const V3 N = v3(hget(L, p + 0), hget(L, p + 1), hget(L, p + 2));
@@ -1559,13 +1571,16 @@ __device__ __forceinline__ BsdfSample lobe_sample(const Lane& L, const Lobes& B,
 __device__ __forceinline__ void lobes_prepare(const Lane& L, Lobes& B, V3 wo, const float* pw, bool absorb) {
     float total = 0.0f;
     OSLG_FOR_LOBES(i, B) {
-        float alb = 1.0f;
+        float alb[3] = { 1.0f, 1.0f, 1.0f };
         if (B.kind[i] == 1) {
             const uint32_t p = B.p[i];
             const GGXLobe g = lobe_ggx(L, p);
-            alb = ggx_albedo(g, v3(hget(L, p + 1), hget(L, p + 2), hget(L, p + 3)), wo);
+            alb[0] = alb[1] = alb[2] = ggx_albedo(g, v3(hget(L, p + 1), hget(L, p + 2), hget(L, p + 3)), wo);
+        } else if (B.kind[i] == 3) {
+            const SheenLobeDev sh = lobe_sheen(L, B, B.p[i], wo);
+            for (int c = 0; c < 3; ++c) alb[c] = sh.tint[c] * (1 - sh.emiss);
         }
-        B.pdf[i] = (B.w[i][0] * (pw[0] * alb) + B.w[i][1] * (pw[1] * alb) + B.w[i][2] * (pw[2] * alb))
+        B.pdf[i] = (B.w[i][0] * (pw[0] * alb[0]) + B.w[i][1] * (pw[1] * alb[1]) + B.w[i][2] * (pw[2] * alb[2]))
                  / (pw[0] + pw[1] + pw[2]);
         total += B.pdf[i];
     }
@@ -1629,14 +1644,15 @@ static __device__ void h_bsdf_eval(const Lane& L, const uint32_t* a, char* base,
 
 // Renderer-side sampling of a closure output, the per-hit step of
 // testrender's path loop (simpleraytracer.cpp:1038-1079): userdata record
-// {rx, ry, rz, path weight rgb, absorb}; output {wi, weight, pdf, Le, roughness}.
+// {rx, ry, rz, path weight rgb, absorb, ray roughness, backfacing};
+// output {wi, weight, pdf, Le, roughness}.
 static __device__ void h_bsdf_sample(const Lane& L, const uint32_t* a, char* base, const char* ud,
                                      const ClosurePools& P, uint32_t* st) {
     const uint32_t root = ldw(L, a[0], 0);
     const V3 wo = v3(-ldf(L, a[3], 0, 0), -ldf(L, a[3], 1, 0), -ldf(L, a[3], 2, 0));
     const float* in = reinterpret_cast<const float*>(ud + (int64_t)a[5] + L.pt * (int64_t)(int32_t)a[6]);
     Lobes B;
-    lobes_build(L, P, root, a[4], st, B);
+    lobes_build(L, P, root, a[4], st, B, in[7], in[8] != 0.0f);
     const float pw[3] = { in[3], in[4], in[5] };
     lobes_prepare(L, B, wo, pw, in[6] != 0.0f);
     const BsdfSample r = lobes_sample(L, B, wo, in[0], in[1], in[2]);

@@ -500,5 +500,94 @@ __device__ __forceinline__ BsdfSample on_eval_local(float rough, V3 wo, V3 wi) {
     return s;
 }
 
+// sheen_bsdf as testrender builds it: BSDL mtx::SheenLobe in its default
+// Conty-Kulla mode with the MaterialX albedo fit and the non-legacy
+// visibility term (libbsdl MTX/bsdf_sheen_impl.h:19-110, :120-260;
+// Conty Estevez and Kulla, "Production Friendly Microfacet Sheen BRDF",
+// 2017). sin^(1/a) uses the executor's own float power (own_pow_pos) where
+// BSDL calls OIIO::fast_pow.
+struct SheenLobeDev {
+    Frame f;
+    float tint[3];
+    float rough;  // regularized roughness (reported)
+    float a;      // distribution roughness, in [0.06, 1]
+    float emiss;
+    bool backfacing;
+};
+__device__ __forceinline__ float sheen_albedo_fit(float c, float r) {
+    float x = 13.67300f + -68.78018f * c;
+    float y = 1.0f + 61.57746f * c;
+    x = x + 799.08825f * r;
+    y = y + 442.78211f * r;
+    x = x + -905.00061f * c * r;
+    y = y + 2597.49308f * c * r;
+    x = x + 60.28956f * c * c;
+    y = y + 121.81241f * c * c;
+    x = x + 1086.96473f * r * r;
+    y = y + 3045.55075f * r * r;
+    return bsdl_clamp(x / y, 0.0f, 1.0f);
+}
+__device__ __forceinline__ SheenLobeDev sheen_make(V3 N, const float* albedo, float roughness, V3 wo,
+                                                   float path_roughness, bool backfacing) {
+    SheenLobeDev L;
+    L.f = bsdl_frame(bsdl_visible_normal(wo, N, N));
+    for (int c = 0; c < 3; ++c) L.tint[c] = albedo[c];
+    L.rough = 1.0f - (1.0f - bsdl_clamp(roughness, 0.0f, 1.0f)) * (1.0f - path_roughness);
+    L.a = bsdl_clamp(fmaxf(0.06f, L.rough), 0.06f, 1.0f);
+    L.backfacing = backfacing;
+    const float cosNO = bsdl_clamp(vdot(L.f.w, wo), 0.0f, 1.0f);
+    const float tmax = fmaxf(fmaxf(L.tint[0], L.tint[1]), L.tint[2]);
+    L.emiss = backfacing ? 1.0f : 1.0f - fminf(sheen_albedo_fit(cosNO, L.a) * tmax, 1.0f);
+    return L;
+}
+// SheenMicrofacet<ContyKullaDist<false>>::eval in the lobe frame
+__device__ __forceinline__ BsdfSample sheen_mf_eval(float a, V3 wo, V3 wi) {
+    BsdfSample s = bsdf_zero();
+    const float cosNO = wo.z, cosNI = wi.z;
+    if (cosNI <= 1e-5f || cosNO <= 1e-5f) return s;
+    const V3 H = vnormalize_imath(vadd(wo, wi));
+    const float ct = bsdl_clamp(H.z, 0.0f, 1.0f);
+    const float st = sqrtf(1.0f - ct * ct);
+    const float pi = 3.14159265358979323846f, one_over_pi = 1.0f / pi;
+    const float D = own_pow_pos(st, 1 / a) * (2 + 1 / a) * 0.5f * one_over_pi;
+    if (D < 1e-6f) return s;
+    const float ci = fminf(1.0f, wi.z), co = fminf(1.0f, wo.z);
+    const float G2 = (ci * co) / (ci + co - ci * co);
+    s.wi = wi;
+    s.w[0] = s.w[1] = s.w[2] = D * G2 * 0.5f * pi / cosNO;
+    s.pdf = 0.5f * one_over_pi;
+    return s;
+}
+__device__ __forceinline__ BsdfSample sheen_eval(const SheenLobeDev& L, V3 wo, V3 wi) {
+    const V3 wo_l = tolocal(L.f, wo), wi_l = tolocal(L.f, wi);
+    BsdfSample s = bsdf_zero();
+    if (!(wi_l.z > 0 && wo_l.z >= 0) || L.backfacing) {
+        s.wi = wi;
+        return s;
+    }
+    s = sheen_mf_eval(L.a, wo_l, wi_l);
+    for (int c = 0; c < 3; ++c) s.w[c] *= L.tint[c];
+    s.roughness = L.rough;
+    s.wi = wi;
+    return s;
+}
+__device__ __forceinline__ BsdfSample sheen_sample(const SheenLobeDev& L, V3 wo, float rx, float ry) {
+    if (L.backfacing) return bsdf_zero();
+    const float a = 2 * rx - 1, qa = fabsf(a);
+    const float b = 2 * ry - 1, qb = fabsf(b);
+    const float rad = qa > qb ? qa : qb;
+    const float phi = qa > qb ? qb / qa : ((qa == qb) ? 1.0f : 2 - qa / qb);
+    const float x = copysignf(rad * bsdl_cos_quadrant(phi), a);
+    const float y = copysignf(rad * bsdl_sin_quadrant(phi), b);
+    const float cos_theta = 1 - rad * rad;
+    const float sin_theta = sqrtf(2 - rad * rad);
+    const V3 wi_l = v3(sin_theta * x, sin_theta * y, cos_theta);
+    BsdfSample s = sheen_mf_eval(L.a, tolocal(L.f, wo), wi_l);
+    for (int c = 0; c < 3; ++c) s.w[c] *= L.tint[c];
+    s.roughness = L.rough;
+    s.wi = bsdl_world(L.f, s.wi);
+    return s;
+}
+
 }  // namespace dev
 }  // namespace oslg

@@ -22,7 +22,7 @@ namespace {
 // control words (uint32) in d_ctl_
 enum { C_NACT = 0, C_COUNTER = 2, C_NITEMS = 3, C_COUNTS = 4, C_OFF = 68, C_CURSOR = 132, C_HITS = 196, C_SIZE = 256 };
 // path-state planes (npaths floats each)
-enum { S_O = 0, S_D = 3, S_TP = 6, S_L = 9, S_SKIP = 12, S_PLANES = 13 };
+enum { S_O = 0, S_D = 3, S_TP = 6, S_L = 9, S_SKIP = 12, S_RO = 13, S_PLANES = 14 };
 // hit-globals planes (cap floats each)
 enum { G_P = 0, G_I = 3, G_N = 6, G_NG = 9, G_U = 12, G_V = 13, G_DPDU = 14, G_DPDV = 17, G_PLANES = 20 };
 
@@ -283,6 +283,7 @@ __global__ void k_camera(const __grid_constant__ WfArgs a) {
             st[(S_L + c) * np + p] = 0.0f;
         }
         st[S_SKIP * np + p] = __int_as_float(-1);
+        st[S_RO * np + p] = 0.0f;  // camera rays have no roughness
         a.act[p] = (uint32_t)p;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) a.ctl[C_NACT] = (uint32_t)np;
@@ -443,7 +444,8 @@ __global__ void __launch_bounds__(256) k_scatter(const __grid_constant__ WfArgs 
                 dPdv = xyz(q.r[2]);
             }
             V Ng = N;
-            if (vdot(Ng, d) > 0.0f) {  // backfacing
+            const bool backfacing = vdot(Ng, d) > 0.0f;
+            if (backfacing) {
                 N = vneg(N);
                 Ng = vneg(Ng);
             }
@@ -459,6 +461,8 @@ __global__ void __launch_bounds__(256) k_scatter(const __grid_constant__ WfArgs 
             ud[4] = st[(S_TP + 1) * np + p];
             ud[5] = st[(S_TP + 2) * np + p];
             ud[6] = 0.0f;
+            ud[7] = st[S_RO * np + p];
+            ud[8] = backfacing ? 1.0f : 0.0f;
             a.hit_slot[i] = (uint32_t)slot;
         }
         __syncthreads();
@@ -494,6 +498,7 @@ __global__ void __launch_bounds__(256) k_update(const __grid_constant__ WfArgs a
             st[(S_D + c) * np + p] = r[c];
         }
         st[S_SKIP * np + p] = __ldg(&a.prims[rec].r[4].w);  // primitive id bits
+        st[S_RO * np + p] = r[10];                           // r.roughness = p.roughness
         nxt[agg_inc(a.ctl + C_NACT + (cur ^ 1), 0)] = (uint32_t)p;
     }
 }

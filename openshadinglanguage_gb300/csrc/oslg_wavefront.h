@@ -28,7 +28,7 @@ namespace oslg {
 
 static const int kWfMaxMaterials = 64;
 static const int kWfMaxHits = 16;
-static const int kWfInFloats = 7;    // rx ry rz, path weight rgb, absorb
+static const int kWfInFloats = 9;    // rx ry rz, path weight rgb, absorb, ray roughness, backfacing
 static const int kWfOutFloats = 11;  // wi xyz, weight rgb, pdf, Le rgb, roughness
 
 namespace dev {
@@ -96,13 +96,13 @@ private:
     dev::WfPrim* d_prims_ = nullptr;
     dev::WfNode* d_nodes_ = nullptr;
     int nnodes_ = 0;
-    float* d_state_ = nullptr;       // 13 planes of npaths: o, d, tp, L, skip
+    float* d_state_ = nullptr;       // 14 planes of npaths: o, d, tp, L, skip, ray roughness
     uint32_t* d_active_ = nullptr;   // 2 x npaths path lists
     int32_t* d_hit_rec_ = nullptr;   // per active index: record or -1
     float* d_hit_t_ = nullptr;
     uint32_t* d_hit_slot_ = nullptr;
     float* d_globals_ = nullptr;     // 20 planes of cap: P I N Ng u v dPdu dPdv
-    float* d_ud_ = nullptr;          // cap x 7
+    float* d_ud_ = nullptr;          // cap x 9
     float* d_out_ = nullptr;         // cap x 11
     uint32_t* d_ctl_ = nullptr;      // counters (see oslg_wavefront.cu)
     dev::BatchJob* d_jobs_ = nullptr;      // nmat live jobs

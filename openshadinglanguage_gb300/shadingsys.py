@@ -401,7 +401,7 @@ class Wavefront:
     kernel. `prims` is a sequence of (kind, material, p, ex, ey, radius)
     tuples or a numpy structured array with those fields; `materials` are
     groups whose closure output is sampled with bsdf_sample_output(offset 0,
-    stride 44, in_offset 0, in_stride 28)."""
+    stride 44, in_offset 0, in_stride 36)."""
 
     OPTION_DEFAULTS = dict(width=1920, height=1080, spp=4, max_hits=8, rr_survival=0.8, eye=(0.0, 6.0, 30.0),
                            look=(0.0, 2.0, -10.0), up=(0.0, 1.0, 0.0), fov_deg=50.0,

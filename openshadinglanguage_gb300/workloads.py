@@ -347,7 +347,7 @@ def c3_points(k, npts, seed=C3_SEED):
 # ---- C5 ------------------------------------------------------------------------------
 C5_SEED = 0xC5
 C5_MATERIALS = 16
-C5_IN_FLOATS = 7    # rx, ry, rz, path weight rgb, absorb
+C5_IN_FLOATS = 9    # rx, ry, rz, path weight rgb, absorb, ray roughness, backfacing
 C5_OUT_FLOATS = 11  # wi xyz, weight rgb, pdf, Le rgb, roughness
 
 
@@ -377,7 +377,7 @@ def _c5_tint(name, c0, c1):
 
 def _c5_surface(name, lobes):
     """lobes: list of (kind, weight, extra) with kind in diffuse, oren_nayar,
-    ggx, dielectric, emission; the closure sum is Ci."""
+    ggx, dielectric, sheen, emission; the closure sum is Ci."""
     from .oso import OsoBuilder
     b = OsoBuilder(name, "surface")
     a = b.param("float", "a", 0.5)
@@ -393,6 +393,8 @@ def _c5_surface(name, lobes):
             b.op("closure", cl, b.const("string", "diffuse"), N)
         elif kind == "oren_nayar":
             b.op("closure", cl, b.const("string", "oren_nayar"), N, c(extra))
+        elif kind == "sheen":  # sheen_bsdf(N, albedo, roughness): albedo from the tint
+            b.op("closure", cl, b.const("string", "sheen_bsdf"), N, tint, c(extra))
         elif kind in ("ggx", "dielectric"):
             alpha, t = b.tmp("float"), b.tmp("float")
             b.op("mul", t, c(0.6), r)
@@ -441,6 +443,8 @@ def c5_material_specs(seed=C5_SEED, n=C5_MATERIALS):
             extra = str(rng.choice(["ggx", "dielectric", "none"]))
             if extra != "none":
                 lobes.append((extra, float(rng.uniform(0.2, 0.6)), float(rng.uniform(1.3, 1.7))))
+            if k % 3 == 1:  # sheen on every third material
+                lobes.append(("sheen", float(rng.uniform(0.3, 0.8)), float(rng.uniform(0.1, 0.9))))
             if rng.random() < 0.3:
                 lobes.append(("oren_nayar" if base == "diffuse" else "diffuse", 0.2, float(rng.uniform(0.0, 0.5))))
         specs.append((pats, tint, lobes))
@@ -478,7 +482,8 @@ def c5_material_group(ss, k, spec, out_offset=0, out_stride=4 * C5_OUT_FLOATS, i
 def c5_hits(n, seed=0xC5A):
     """Seeded hit records for sampling tests: P in [-5, 5]^3, unit N facing
     the incoming direction, dPdu orthogonal to N, random inputs of the
-    sample step (rx, ry, rz in [0, 1), path weight in [0.2, 1], absorb 0/1)."""
+    sample step (rx, ry, rz in [0, 1), path weight in [0.2, 1], absorb 0/1,
+    ray roughness, backfacing 0/1)."""
     rng = np.random.default_rng(seed)
     P = rng.uniform(-5, 5, (3, n)).astype(np.float32)
     N = rng.normal(size=(3, n))
@@ -493,6 +498,8 @@ def c5_hits(n, seed=0xC5A):
     rnd[:, 0:3] = rng.random((n, 3), dtype=np.float32) * np.float32(0.99999994)
     rnd[:, 3:6] = rng.uniform(0.2, 1.0, (n, 3))
     rnd[:, 6] = (rng.random(n) < 0.3).astype(np.float32)
+    rnd[:, 7] = np.where(rng.random(n) < 0.5, 0.0, rng.uniform(0.0, 0.8, n))  # ray roughness
+    rnd[:, 8] = (rng.random(n) < 0.2).astype(np.float32)  # backfacing
     f32 = lambda a: np.ascontiguousarray(a, dtype=np.float32)
     return (P, f32(N), f32(I), f32(T), rnd)
 

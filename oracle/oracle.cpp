@@ -825,7 +825,8 @@ template <class F> void closure_walk(Point& P, const CPools& C, uint32_t root, F
 // (src/testrender/shading.cpp:1481-1530): emission accumulates Le,
 // diffuse / oren_nayar / GGX microfacet (params: dist, N, U, xalpha,
 // yalpha, eta, refract) become lobes in walk order; ggx_hash names "ggx".
-void build_lobes(Point& P, const CPools& C, uint32_t root, const V3& wo, uint32_t ggx_hash, CompositeLobes* L) {
+void build_lobes(Point& P, const CPools& C, uint32_t root, const V3& wo, uint32_t ggx_hash, CompositeLobes* L,
+                 float path_roughness = 0.0f, bool backfacing = false) {
     auto f = [&](uint32_t s) { return bitsf(P.heap[s]); };
     closure_walk(P, C, root, [&](int id, const V3& cw, uint32_t p) {
         if (id == 1) {  // EMISSION_ID
@@ -834,6 +835,9 @@ void build_lobes(Point& P, const CPools& C, uint32_t root, const V3& wo, uint32_
             L->add_diffuse(cw, V3(f(p + 0), f(p + 1), f(p + 2)));
         } else if (id == 4) {  // OREN_NAYAR_ID
             L->add_on(cw, OrenNayarQON(V3(f(p + 0), f(p + 1), f(p + 2)), f(p + 3), wo));
+        } else if (id == 23 && P.heap[p + 7] == 0u) {  // MX_SHEEN_ID, Conty-Kulla mode
+            L->add_sheen(cw, SheenConty(V3(f(p + 0), f(p + 1), f(p + 2)), V3(f(p + 3), f(p + 4), f(p + 5)), f(p + 6), wo,
+                                        path_roughness, backfacing));
         } else if (id == 8 && P.heap[p] == ggx_hash) {  // MICROFACET_ID, "ggx"
             int refract = (int32_t)P.heap[p + 10];
             if (refract < 0 || refract > 2) return;
@@ -1212,13 +1216,14 @@ struct Runner {
             case oslg::OP_BSDF_SAMPLE: {
                 // process_closure + prepare(wo, path_weight, absorb) + sample
                 // (simpleraytracer.cpp:1038-1079, shading.h:322-398). Userdata
-                // record: rx ry rz, path weight rgb, absorb; output record:
-                // wi xyz, weight rgb, pdf, Le rgb, roughness.
+                // record: rx ry rz, path weight rgb, absorb, ray roughness,
+                // backfacing; output record: wi xyz, weight rgb, pdf, Le rgb,
+                // roughness.
                 uint32_t root = word(P, a[0], 0);
                 V3 wo(-getf(P, a[3], 0, 0), -getf(P, a[3], 1, 0), -getf(P, a[3], 2, 0));
                 const float* in = reinterpret_cast<const float*>(userdata + (int64_t)a[5] + P.pt * (int64_t)(int32_t)a[6]);
                 CompositeLobes L;
-                build_lobes(P, C, root, wo, a[4], &L);
+                build_lobes(P, C, root, wo, a[4], &L, in[7], in[8] != 0.0f);
                 L.prepare(wo, V3(in[3], in[4], in[5]), in[6] != 0.0f);
                 Sample sres = L.sample(wo, in[0], in[1], in[2]);
                 float* o = reinterpret_cast<float*>(outputs + (int64_t)a[1] + P.pt * (int64_t)(int32_t)a[2]);

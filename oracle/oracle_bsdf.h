@@ -346,14 +346,94 @@ struct OrenNayarQON {
     }
 };
 
+// sheen_bsdf as testrender builds it: BSDL mtx::SheenLobe, Conty-Kulla
+// mode, MaterialX albedo fit, non-legacy visibility term
+// (libbsdl MTX/bsdf_sheen_impl.h:19-110, :120-260). The power in the
+// distribution is the executor's own float power (OIIO::fast_pow in the
+// reference: parity unpinned there).
+inline float sheen_albedo_fit(float c, float r) {
+    float x = 13.67300f + -68.78018f * c;
+    float y = 1.0f + 61.57746f * c;
+    x = x + 799.08825f * r;
+    y = y + 442.78211f * r;
+    x = x + -905.00061f * c * r;
+    y = y + 2597.49308f * c * r;
+    x = x + 60.28956f * c * c;
+    y = y + 121.81241f * c * c;
+    x = x + 1086.96473f * r * r;
+    y = y + 3045.55075f * r * r;
+    return bsdl_clamp(x / y, 0.0f, 1.0f);
+}
+struct SheenConty {
+    BsdlFrame frame;
+    V3 tint;
+    float rough, a, emiss;
+    bool backfacing;
+    SheenConty(const V3& N, const V3& albedo, float roughness, const V3& wo, float path_roughness, bool bf)
+        : frame(bsdl_visible_normal(wo, N, N)), tint(albedo), backfacing(bf) {
+        rough = 1.0f - (1.0f - bsdl_clamp(roughness, 0.0f, 1.0f)) * (1.0f - path_roughness);
+        a = bsdl_clamp(std::max(0.06f, rough), 0.06f, 1.0f);
+        const float cosNO = bsdl_clamp(dotv(frame.Z, wo), 0.0f, 1.0f);
+        const float tmax = std::max(std::max(tint.x, tint.y), tint.z);
+        emiss = backfacing ? 1.0f : 1.0f - std::min(sheen_albedo_fit(cosNO, a) * tmax, 1.0f);
+    }
+    V3 albedo() const { return tint * (1 - emiss); }
+    static Sample mf_eval(float a, const V3& wo, const V3& wi) {
+        Sample s;
+        const float cosNO = wo.z, cosNI = wi.z;
+        if (cosNI <= 1e-5f || cosNO <= 1e-5f) return s;
+        const V3 H = imath_normalize(wo + wi);
+        const float ct = bsdl_clamp(H.z, 0.0f, 1.0f);
+        const float st = std::sqrt(1.0f - ct * ct);
+        const float pi = float(M_PI), one_over_pi = 1 / pi;
+        const float D = own_pow_pos(st, 1 / a) * (2 + 1 / a) * 0.5f * one_over_pi;
+        if (D < 1e-6f) return s;
+        const float ci = std::min(1.0f, wi.z), co = std::min(1.0f, wo.z);
+        const float G2 = (ci * co) / (ci + co - ci * co);
+        s.wi = wi;
+        s.weight = V3(D * G2 * 0.5f * pi / cosNO);
+        s.pdf = 0.5f * one_over_pi;
+        return s;
+    }
+    Sample eval(const V3& wo, const V3& wi) const {
+        const V3 wo_l = frame.local(wo), wi_l = frame.local(wi);
+        Sample s;
+        if (!(wi_l.z > 0 && wo_l.z >= 0) || backfacing) {
+            s.wi = wi;
+            return s;
+        }
+        s = mf_eval(a, wo_l, wi_l);
+        s.weight = s.weight * tint;
+        s.roughness = rough;
+        s.wi = wi;
+        return s;
+    }
+    Sample sample(const V3& wo, float rx, float ry) const {
+        if (backfacing) return Sample();
+        const float ua = 2 * rx - 1, qa = std::fabs(ua);
+        const float ub = 2 * ry - 1, qb = std::fabs(ub);
+        const float rad = qa > qb ? qa : qb;
+        const float phi = qa > qb ? qb / qa : ((qa == qb) ? 1.0f : 2 - qa / qb);
+        const float x = std::copysign(rad * bsdl_cos_quadrant(phi), ua);
+        const float y = std::copysign(rad * bsdl_sin_quadrant(phi), ub);
+        const float cos_theta = 1 - rad * rad;
+        const float sin_theta = std::sqrt(2 - rad * rad);
+        Sample s = mf_eval(a, frame.local(wo), V3(sin_theta * x, sin_theta * y, cos_theta));
+        s.weight = s.weight * tint;
+        s.roughness = rough;
+        s.wi = frame.world(s.wi);
+        return s;
+    }
+};
+
 // The lobes testrender builds from a closure tree, with their weights.
 struct CompositeLobes {
-    enum Kind { DIFFUSE, GGX, OREN_NAYAR };
+    enum Kind { DIFFUSE, GGX, OREN_NAYAR, SHEEN };
     int kind[kMaxLobes];
     V3 w[kMaxLobes];
     float pdfs[kMaxLobes];
-    unsigned char storage[kMaxLobes][sizeof(MicrofacetGGX) > sizeof(OrenNayarQON) ? sizeof(MicrofacetGGX)
-                                                                                   : sizeof(OrenNayarQON)];
+    static constexpr size_t kStore = std::max(sizeof(MicrofacetGGX), std::max(sizeof(OrenNayarQON), sizeof(SheenConty)));
+    alignas(16) unsigned char storage[kMaxLobes][kStore];
     V3 N[kMaxLobes];
     int n = 0;
     V3 Le = V3(0.0f);
@@ -361,6 +441,7 @@ struct CompositeLobes {
     OrenNayarQON& on(int i) { return *reinterpret_cast<OrenNayarQON*>(storage[i]); }
     const OrenNayarQON& on(int i) const { return *reinterpret_cast<const OrenNayarQON*>(storage[i]); }
     const MicrofacetGGX& mf(int i) const { return *reinterpret_cast<const MicrofacetGGX*>(storage[i]); }
+    const SheenConty& sh(int i) const { return *reinterpret_cast<const SheenConty*>(storage[i]); }
 
     void add_diffuse(const V3& cw, const V3& normal) {
         if (n_full()) return;
@@ -379,10 +460,17 @@ struct CompositeLobes {
         new (storage[n]) OrenNayarQON(o);
         ++n;
     }
+    void add_sheen(const V3& cw, const SheenConty& o) {
+        if (n_full()) return;
+        kind[n] = SHEEN; w[n] = cw;
+        new (storage[n]) SheenConty(o);
+        ++n;
+    }
     bool n_full() const { return n >= kMaxLobes; }
 
     V3 albedo(int i, const V3& wo) const {
         if (kind[i] == GGX) return mf(i).albedo(wo);
+        if (kind[i] == SHEEN) return sh(i).albedo();
         return V3(1.0f);
     }
     Sample eval_lobe(int i, const V3& wo, const V3& wi) const {
@@ -392,11 +480,13 @@ struct CompositeLobes {
             return s;
         }
         if (kind[i] == GGX) return mf(i).eval(wo, wi);
+        if (kind[i] == SHEEN) return sh(i).eval(wo, wi);
         return on(i).eval(wo, wi);
     }
     Sample sample_lobe(int i, const V3& wo, float rx, float ry, float rz) const {
         if (kind[i] == DIFFUSE) return diffuse_sample(N[i], rx, ry);
         if (kind[i] == GGX) return mf(i).sample(wo, rx, ry, rz);
+        if (kind[i] == SHEEN) return sh(i).sample(wo, rx, ry);
         return on(i).sample(wo, rx, ry);
     }
     // CompositeBSDF::prepare (shading.h:322-350)

@@ -81,4 +81,46 @@ inline void own_sincos(float x, float* s, float* c) {
     }
 }
 
+
+// Natural log for x > 0 (0 -> -inf, negative or NaN -> NaN): exponent split,
+// mantissa folded into [sqrt(1/2), sqrt(2)), ln m = 2 atanh(s) with
+// s = (m-1)/(m+1) as an odd series to s^11, ln 2 in a head and tail.
+inline float own_log(float x) {
+    if (!(x > 0.0f)) return x == 0.0f ? -INFINITY : NAN;
+    if (x == INFINITY) return x;
+    int e = 0;
+    if (x < 1.17549435e-38f) {  // subnormal: scale into the normal range
+        x = x * 8388608.0f;
+        e = -23;
+    }
+    uint32_t b;
+    std::memcpy(&b, &x, 4);
+    e += (int)(b >> 23) - 127;
+    const uint32_t mb = (b & 0x007fffffu) | 0x3f800000u;
+    float m;
+    std::memcpy(&m, &mb, 4);
+    if (m > 1.41421356f) {
+        m = m * 0.5f;
+        e += 1;
+    }
+    const float s = (m - 1.0f) / (m + 1.0f);
+    const float s2 = s * s;
+    float p = 0.0909090936f;
+    p = 0.111111112f + s2 * p;
+    p = 0.142857149f + s2 * p;
+    p = 0.200000003f + s2 * p;
+    p = 0.333333343f + s2 * p;
+    p = 1.0f + s2 * p;
+    const float fe = (float)e;
+    return fe * 0.693359375f + ((s + s) * p + fe * -0.00021219444170128554f);
+}
+
+// x^y for x >= 0, y > 0 as own_exp(y * own_log(x)) (about 1e-5 relative
+// for |y ln x| near 100): the sheen distribution's power.
+inline float own_pow_pos(float x, float y) {
+    if (x == 0.0f) return 0.0f;
+    if (x == 1.0f) return 1.0f;
+    return own_exp(y * own_log(x));
+}
+
 }  // namespace oracle

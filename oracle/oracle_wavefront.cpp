@@ -148,6 +148,7 @@ int intersect(const std::vector<Prim>& prims, V o, V d, int skip, float* t_out) 
 struct Path {
     V o, d;
     float tp[3], L[3];
+    float rough;  // roughness of the ray (the last sample's)
     int skip;
     uint32_t id;
 };
@@ -206,6 +207,7 @@ int oracle_wavefront(const oslg_wavefront_options* o, const oslg_primitive* raw,
             P.L[c] = 0.0f;
         }
         P.skip = -1;
+        P.rough = 0.0f;
         P.id = (uint32_t)p;
     }
     for (int b = 0; b < 16; ++b) hits[b] = 0;
@@ -237,7 +239,7 @@ int oracle_wavefront(const oslg_wavefront_options* o, const oslg_primitive* raw,
             const int64_t nm = (int64_t)sel.size();
             if (nm == 0) continue;
             hits[b] += nm;
-            std::vector<float> gl((size_t)nm * 20), ud((size_t)nm * 7), out((size_t)nm * 11, 0.0f);
+            std::vector<float> gl((size_t)nm * 20), ud((size_t)nm * 9), out((size_t)nm * 11, 0.0f);
             auto plane = [&](int k) { return gl.data() + (size_t)k * nm; };
             for (int64_t j = 0; j < nm; ++j) {
                 const int64_t i = sel[(size_t)j];
@@ -263,17 +265,20 @@ int oracle_wavefront(const oslg_wavefront_options* o, const oslg_primitive* raw,
                     dPdv = q.ey;
                 }
                 V Ng = N;
-                if (vdot(Ng, P.d) > 0.0f) {
+                const bool backfacing = vdot(Ng, P.d) > 0.0f;
+                if (backfacing) {
                     N = vneg(N);
                     Ng = vneg(Ng);
                 }
                 const float vals[20] = { Pt.x, Pt.y, Pt.z, P.d.x, P.d.y, P.d.z, N.x, N.y, N.z, Ng.x, Ng.y, Ng.z,
                                          u, v, dPdu.x, dPdu.y, dPdu.z, dPdv.x, dPdv.y, dPdv.z };
                 for (int k = 0; k < 20; ++k) plane(k)[j] = vals[k];
-                float* r = ud.data() + (size_t)j * 7;
+                float* r = ud.data() + (size_t)j * 9;
                 for (int c = 0; c < 3; ++c) r[c] = wf_rand(seed, P.id, (uint32_t)b, (uint32_t)c);
                 for (int c = 0; c < 3; ++c) r[3 + c] = P.tp[c];
                 r[6] = 0.0f;
+                r[7] = P.rough;
+                r[8] = backfacing ? 1.0f : 0.0f;
             }
             oslg_shaderglobals G;
             std::memset(&G, 0, sizeof(G));
@@ -310,6 +315,7 @@ int oracle_wavefront(const oslg_wavefront_options* o, const oslg_primitive* raw,
                 P.o = mk(plane(0)[j], plane(1)[j], plane(2)[j]);
                 P.d = mk(r[0], r[1], r[2]);
                 P.skip = hit_id[(size_t)i];
+                P.rough = r[10];
                 next.push_back(active[(size_t)i]);
             }
         }

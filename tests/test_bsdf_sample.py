@@ -75,3 +75,28 @@ def test_dielectric_reflects_and_refracts(hits):
     ok = out[:, 6] > 0
     side = np.sum(out[ok, 0:3] * N.T[ok], axis=1)
     assert (side > 0).mean() > 0.02 and (side < 0).mean() > 0.5
+
+
+def test_sheen_lobe_samples_the_uniform_hemisphere(hits):
+    """sheen_bsdf (Conty-Kulla mode): uniform hemisphere sampling, pdf
+    1/(2 pi) for a lone lobe, directions above the surface, weight
+    D*G2*pi/(2 cos_o) * tint * closure weight >= 0; nothing when the hit is
+    backfacing (BSDL's rule) and roughness regularized by the ray's."""
+    P, N, I, T, rnd = hits
+    rnd = rnd.copy()
+    rnd[:, 6] = 0.0
+    ss = og.ShadingSystem()
+    g = single_lobe_group(ss, "sheen_only", ("sheen", 0.7, 0.4))
+    G = og.make_globals(P=P, N=N, Ng=N, I=I, dPdu=T)
+    out = np.zeros((P.shape[1], W.C5_OUT_FLOATS), np.float32)
+    assert oracle_run(g.program_bytes(), P.shape[1], G, out, userdata=rnd) == 0
+    front = rnd[:, 8] == 0
+    ok = front & (out[:, 6] > 0)
+    assert ok.mean() > 0.5
+    assert np.allclose(out[ok, 6], np.float32(0.5) * (np.float32(1) / np.float32(np.pi)))
+    assert (np.einsum("ij,ji->i", out[ok, 0:3], N[:, ok]) > -1e-6).all()
+    assert (out[ok, 3:6] >= 0).all()
+    # reported roughness: 1 - (1 - 0.4) * (1 - ray roughness)
+    expect = (np.float32(1) - (np.float32(1) - np.float32(0.4)) * (np.float32(1) - rnd[ok, 7])).astype(np.float32)
+    assert np.array_equal(out[ok, 10], expect)
+    assert (out[~front, 6] == 0).all() and (out[~front, 3:6] == 0).all()
