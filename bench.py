@@ -389,6 +389,8 @@ def main():
                     help="1: run the group's specialized kernel (attribute jit), 0: the interpreter")
     ap.add_argument("--jit-block", type=int, default=0, help="specialized launch: threads per CTA")
     ap.add_argument("--jit-pool-smem", type=int, default=-1, help="specialized launch: closure pools in smem (1/0)")
+    ap.add_argument("--jit-min-blocks", type=int, default=0,
+                    help="specialized kernel register cap: 256-thread CTAs per SM it must fit (2..8)")
     ap.add_argument("--section", choices=["batching", "serving", "wavefront"],
                     help="run only this measurement section and print it as one JSON line")
     ap.add_argument("--wf-size", default=None, help="wavefront frame WxHxSPP (default 1920x1080x4)")
@@ -462,6 +464,8 @@ def main():
             wl.ss.attribute("jit_block", args.jit_block)
         if args.jit_pool_smem >= 0:
             wl.ss.attribute("jit_pool_smem", args.jit_pool_smem)
+        if args.jit_min_blocks:
+            wl.ss.attribute("jit_min_blocks", args.jit_min_blocks)
     stream = torch.cuda.current_stream()
     sh = stream.cuda_stream
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")

@@ -110,7 +110,8 @@ int oslg_destroy_system(oslg_system* sys);
  * group, see oslg_group_specialized_source; the counterpart of the
  * reference's per-group JIT), "jit_block" (64/128/256 threads per CTA of a
  * specialized launch), "jit_pool_smem" (closure pools in shared memory 1,
- * HBM scratch 0, automatic -1). */
+ * HBM scratch 0, automatic -1), "jit_min_blocks" (register cap of
+ * specialized kernels: 256-thread CTAs per SM that must fit, 2..8). */
 int oslg_attribute_int(oslg_system* sys, const char* name, int value);
 /* ShadingSystem::register_closure (oslexec.h:1041). Parameters are taken
  * positionally from the `closure` op's arguments. */

@@ -43,6 +43,7 @@ struct oslg_system {
     int jit = 0;  // build a specialized kernel per group at optimize time
     int jit_block = 0;       // specialized launch: threads per CTA (0: 256)
     int jit_pool_smem = -1;  // closure pools: 1 shared memory, 0 HBM, -1 shared when it fits
+    int jit_min_blocks = 0;  // register cap of specialized kernels (256-thread CTAs per SM; 0: automatic)
     std::string err;
     std::vector<oslg::InstanceParam> pending_params;  // Parameter() before Shader()
 };
@@ -188,6 +189,7 @@ int oslg_attribute_int(oslg_system* sys, const char* name, int value) {
     else if (n == "jit") sys->jit = value;
     else if (n == "jit_block") sys->jit_block = value;
     else if (n == "jit_pool_smem") sys->jit_pool_smem = value;
+    else if (n == "jit_min_blocks") sys->jit_min_blocks = value;
     else return fail(sys, OSLG_ERR_ARG, "unknown attribute '" + n + "'");
     if (sys->ss.opts.max_closure_terms > 0xFFFF || sys->ss.opts.max_closure_components > 0xFFFF)
         return fail(sys, OSLG_ERR_ARG, "closure pool capacity must stay below 65536");
@@ -410,7 +412,7 @@ static int ensure_compiled(oslg_system* sys, oslg_group* group, bool upload) {
         auto sk = std::make_shared<SpecKernel>();
         std::string err;
         const std::string dir = library_dir();
-        int rc = spec_build(*g.compiled, dir + "/csrc", dir + "/_build/jit", sk.get(), &err);
+        int rc = spec_build(*g.compiled, dir + "/csrc", dir + "/_build/jit", sk.get(), &err, sys->jit_min_blocks);
         if (rc != OSLG_OK) return fail(sys, rc, "group '" + g.name + "': " + err);
         g.compiled->spec = sk;
     }
@@ -592,7 +594,7 @@ int oslg_group_specialized_source(oslg_system* sys, oslg_group* group, char* buf
     return guarded(sys, [&]() {
         int rc = ensure_compiled(sys, group, false);
         if (rc != OSLG_OK) return rc;
-        const std::string src = spec_source(*group->g.compiled);
+        const std::string src = spec_source(*group->g.compiled, sys->jit_min_blocks);
         if (size) *size = src.size() + 1;
         if (buf && cap) {
             const size_t n = std::min(cap - 1, src.size());

@@ -31,7 +31,9 @@ struct SpecKernel {
 };
 
 // CUDA source of the specialized kernel for one lowered program.
-std::string spec_source(const CompiledGroup& cg);
+// min_blocks: resident 256-thread CTAs the register budget must allow
+// (2: up to 128 registers per thread, 4: 64; 0: chosen from the program).
+std::string spec_source(const CompiledGroup& cg, int min_blocks = 0);
 
 // A persistent batch kernel specialized to a list of programs: the
 // interpreter's batch_kernel work loop (items (job, tile) from a device
@@ -53,7 +55,7 @@ int spec_batch_build(const std::vector<const CompiledGroup*>& cases, const std::
 // Build (or take from the cache) and load the kernel. `csrc_dir` holds the
 // interpreter headers, `cache_dir` the generated sources and cubins.
 int spec_build(const CompiledGroup& cg, const std::string& csrc_dir, const std::string& cache_dir,
-               SpecKernel* out, std::string* err);
+               SpecKernel* out, std::string* err, int min_blocks = 0);
 
 // Launch over [0, npoints): one CTA of 256 points per tile, closure pools in
 // shared memory when they fit, else in the executor's HBM scratch.
