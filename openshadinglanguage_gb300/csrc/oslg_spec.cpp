@@ -335,6 +335,7 @@ std::string spec_batch_source(const std::vector<const CompiledGroup*>& cases) {
         emit_job(o, vs[j], "_" + std::to_string(j));
     }
     o << "}  // namespace\n\n";
+    // up to 128 registers: the material bodies spill under tighter caps
     o << "extern \"C\" __global__ void __launch_bounds__(256, 2) oslg_specbatch_kernel("
          "const __grid_constant__ oslg::dev::BatchArgs b, int pool_in_smem) {\n";
     o << "    using namespace oslg;\n    using namespace oslg::dev;\n";
