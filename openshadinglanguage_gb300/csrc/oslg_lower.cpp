@@ -16,6 +16,11 @@
 //     nothing binds (no connection, no userdata) are uniform values;
 //   * layout: everything else gets heap slots ([val][dx][dy] blocks);
 //   * control flow: if/loops become mask ops (OP_IF/ELSE/ENDIF, OP_LOOP_*).
+//   * dead ops: an op survives only if it has an effect outside the symbol
+//     heap (stores, BSDF output, control flow, messages) or writes a symbol
+//     a surviving op reads (the RuntimeOptimizer's dead-code removal,
+//     runtimeoptimize.cpp:2133-2186, done flow-insensitively here so that
+//     loops need no special case).
 //   * layers run in group order; a connection copies the upstream output
 //     into the downstream parameter before that layer's body.
 #include <algorithm>
@@ -479,6 +484,53 @@ struct Lowerer {
         }
         for (GSym& s : syms)
             if (s.is_const) s.derivs = false;
+    }
+
+    // ---- dead-op elimination ----------------------------------------------------
+    static bool has_effect(const LOp& op) {
+        static const std::set<std::string> effects = {
+            "if", "for", "while", "dowhile", "break", "continue", "return", "exit", "__layer_end",
+            "__store_output", "__bsdf_eval", "__bsdf_sample", "printf", "warning", "error", "fprintf",
+            "functioncall", "functioncall_nr", "useparam" };
+        return effects.count(op.name) != 0;
+    }
+    // ops that update part of their result keep its other components: the
+    // result is read as well as written
+    static bool partial_write(const LOp& op) {
+        return op.name == "compassign" || op.name == "aassign" || op.name == "mxcompassign";
+    }
+    int eliminate_dead_ops() {
+        std::vector<char> needed(syms.size(), 0), live(lops.size(), 0);
+        auto take = [&](int k) {
+            live[k] = 1;
+            const LOp& op = lops[k];
+            for (size_t i = 0; i < op.args.size(); ++i)
+                if (!writes_arg(op, (int)i) || partial_write(op)) needed[op.args[i]] = 1;
+        };
+        for (int k = 0; k < (int)lops.size(); ++k)
+            if (has_effect(lops[k])) take(k);
+        for (bool changed = true; changed;) {
+            changed = false;
+            for (int k = (int)lops.size() - 1; k >= 0; --k) {
+                if (live[k] || lops[k].name == "nop") continue;
+                const LOp& op = lops[k];
+                for (size_t i = 0; i < op.args.size(); ++i)
+                    if (writes_arg(op, (int)i) && needed[op.args[i]]) {
+                        take(k);
+                        changed = true;
+                        break;
+                    }
+            }
+        }
+        int removed = 0;
+        for (int k = 0; k < (int)lops.size(); ++k)
+            if (!live[k] && lops[k].name != "nop") {
+                lops[k].name = "nop";
+                lops[k].args.clear();
+                lops[k].param_init = false;
+                ++removed;
+            }
+        return removed;
     }
 
     void mark_derivs(int s) {
@@ -1194,6 +1246,7 @@ struct Lowerer {
     bool run(CompiledGroup& out) {
         if (g.layers.empty()) return fail("group has no layers");
         if (!build_lops()) return false;
+        eliminate_dead_ops();
         analyze();
         assign_storage();
         if (!lower_all()) return false;

@@ -35,8 +35,35 @@ def test_unknown_op_is_rejected_at_lowering(native):
     g = ss.ShaderGroupBegin("g")
     ss.Shader(g, "surface", "bad", "l1")
     ss.ShaderGroupEnd(g)
+    ss.add_symlocs(g, [og.SymLocationDesc("l1.x", og.TypeFloat, False, og.SymArenaOutputs, 0, 4)])
     with pytest.raises(og.OSLError, match="pointcloud_search"):
         ss.optimize_group(g)
+
+
+def test_dead_ops_are_removed(native):
+    """An op whose result nothing reads is dropped before lowering (the
+    RuntimeOptimizer's dead-code removal): even an unsupported one."""
+    import struct
+    ss = og.ShadingSystem()
+    b = og.OsoBuilder("deadops")
+    x = b.param("float", "x", 1.0, output=True)
+    y = b.param("float", "y", 0.0, output=True)
+    t = b.tmp("float")
+    b.op("pointcloud_search", t, x)  # result unused
+    b.op("add", y, x, b.const("float", 2.0))
+    b.op("mul", t, y, y)  # result unused
+    ss.LoadMemoryCompiledShader("deadops", b.text())
+    g = ss.ShaderGroupBegin("g")
+    ss.Shader(g, "surface", "deadops", "l1")
+    ss.ShaderGroupEnd(g)
+    ss.add_symlocs(g, [og.SymLocationDesc("l1.y", og.TypeFloat, False, og.SymArenaOutputs, 0, 4)])
+    blob = g.program_bytes()  # lowering succeeds: the unsupported op was dead
+    nops = struct.unpack("<I", blob[8:12])[0]
+    codes = [struct.unpack("<H", blob[64 + 32 * i:66 + 32 * i])[0] for i in range(nops)]
+    assert _opcode("OP_MUL") not in codes
+    assert codes.count(_opcode("OP_ADD")) == 1
+    # y's initial value, the add, the output store and the layer marker
+    assert len(codes) <= 4
 
 
 def test_malformed_oso_is_rejected(native):
@@ -87,7 +114,8 @@ def test_lowering_marks_derivatives_and_pools_constants(native):
     g = ss.ShaderGroupBegin("g")
     ss.Shader(g, "surface", "fbm_cell", "l1")
     ss.ShaderGroupEnd(g)
-    ss.add_symlocs(g, [og.SymLocationDesc("Cout", og.TypeColor, True, og.SymArenaOutputs, 0, 40)])
+    ss.add_symlocs(g, [og.SymLocationDesc("Cout", og.TypeColor, True, og.SymArenaOutputs, 0, 40),
+                       og.SymLocationDesc("cellhash", og.TypeInt, False, og.SymArenaOutputs, 36, 40)])
     blob = g.program_bytes()
     hdr = np.frombuffer(blob[:64], np.uint32)
     assert hdr[0] == 0x4F534C47
