@@ -199,6 +199,16 @@ int oslg_groups_specialized_batch_source(oslg_system* sys, oslg_group* const* gr
                                          size_t cap, size_t* size);
 /* 1 when the group runs its specialized kernel. */
 int oslg_group_is_specialized(oslg_system* sys, oslg_group* group, int* out);
+/* Register (or replace) the image that texture(name, s, t, ...) looks up:
+ * width x height texels of nchannels floats, channels interleaved, rows
+ * from the top (t = 0). A mip pyramid (2x2 box reductions) is built and kept
+ * in device memory; lookups are mipmapped bilinear with the level chosen
+ * from the s, t derivatives, wrap modes black/clamp/periodic/mirror. Stands
+ * in for OIIO's TextureSystem behind RendererServices::texture
+ * (src/include/OSL/rendererservices.h:361-383; the reference reads files).
+ * Groups naming the texture must be lowered after it is registered. */
+int oslg_texture_create(oslg_system* sys, const char* name, int width, int height, int nchannels,
+                        const float* texels, int* index);
 /* ShaderGroupRef release */
 int oslg_release_group(oslg_system* sys, oslg_group* group);
 

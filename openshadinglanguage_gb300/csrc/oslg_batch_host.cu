@@ -255,6 +255,8 @@ int BatchExecutor::build(DeviceState& ds, std::string* err) {
     args_.counter = d_counter_;
     args_.gheap = smem ? nullptr : d_heap_;
     args_.status = ds.d_status;
+    args_.textures = ds.d_textures;
+    args_.ntextures = ds.ntextures;
     args_.prog_bytes = prog_bytes;
     args_.heap_slots = slots;
     cur_.block = block;

@@ -39,6 +39,15 @@ struct oslg_system {
     oslg::ShadingSystem ss;
     oslg::DeviceState dev;
     std::vector<HostSlot> host_slots;
+    // registered textures: host pyramids, uploaded with the descriptor table
+    // before the next launch that may read them
+    struct Tex {
+        std::vector<float> pyramid;
+        oslg::TexDesc desc;
+        bool stale = true;  // pyramid not (or no longer) in device memory
+    };
+    std::vector<Tex> textures;
+    bool textures_dirty = false;
     oslg::LaunchConfig launch;
     int jit = 0;  // build a specialized kernel per group at optimize time
     int jit_block = 0;       // specialized launch: threads per CTA (0: 256)
@@ -165,6 +174,8 @@ int oslg_destroy_system(oslg_system* sys) {
     if (!sys) return OSLG_ERR_ARG;
     if (sys->dev.gheap) device_free(sys->dev.gheap);
     if (sys->dev.d_status) device_free(sys->dev.d_status);
+    for (const auto& t : sys->textures) cudaFree(const_cast<float*>(t.desc.data));
+    cudaFree(sys->dev.d_textures);
     for (HostSlot& S : sys->host_slots) {
         if (S.stream) cudaStreamDestroy(S.stream);
         cudaFree(S.d_glob);
@@ -390,9 +401,15 @@ static std::string library_dir() {
     return ".";
 }
 
+static int upload_textures(oslg_system* sys);
+
 static int ensure_compiled(oslg_system* sys, oslg_group* group, bool upload) {
     ShaderGroup& g = group->g;
     if (!g.ended) return fail(sys, OSLG_ERR_STATE, "group used before ShaderGroupEnd");
+    if (upload && sys->textures_dirty) {
+        int rc = upload_textures(sys);
+        if (rc != OSLG_OK) return rc;
+    }
     std::lock_guard<std::mutex> lock(g.mutex);
     if (!g.compiled) {
         auto cg = std::make_unique<CompiledGroup>();
@@ -461,6 +478,106 @@ int oslg_execute_batch(oslg_system* sys, oslg_group* group, int64_t npoints, con
         if (rc != OSLG_OK) return fail(sys, rc, err);
         return OSLG_OK;
     });
+}
+
+// ---- textures ---------------------------------------------------------------------
+namespace {
+// Mip pyramid: level 0 the image, each next level a 2x2 box average of the
+// one before (texel coordinates clamped at odd edges), down to 1x1 or
+// kTexMaxLevels levels.
+void build_pyramid(int w, int h, int nch, const float* src, std::vector<float>& out, TexDesc& d) {
+    d.nch = nch;
+    d.nlevels = 0;
+    out.assign(src, src + (size_t)w * h * nch);
+    int lw = w, lh = h;
+    size_t off = 0;
+    for (;;) {
+        const int lev = d.nlevels++;
+        d.w[lev] = lw;
+        d.h[lev] = lh;
+        d.off[lev] = (int64_t)off;
+        if ((lw == 1 && lh == 1) || d.nlevels == kTexMaxLevels) break;
+        const int nw = std::max(1, lw / 2), nh = std::max(1, lh / 2);
+        const size_t noff = out.size();
+        out.resize(noff + (size_t)nw * nh * nch);
+        const float* prev = out.data() + off;
+        float* next = out.data() + noff;
+        for (int y = 0; y < nh; ++y)
+            for (int x = 0; x < nw; ++x) {
+                const int x0 = std::min(2 * x, lw - 1), x1 = std::min(2 * x + 1, lw - 1);
+                const int y0 = std::min(2 * y, lh - 1), y1 = std::min(2 * y + 1, lh - 1);
+                for (int c = 0; c < nch; ++c) {
+                    const float a = prev[((size_t)y0 * lw + x0) * nch + c], b = prev[((size_t)y0 * lw + x1) * nch + c];
+                    const float e = prev[((size_t)y1 * lw + x0) * nch + c], f = prev[((size_t)y1 * lw + x1) * nch + c];
+                    next[((size_t)y * nw + x) * nch + c] = (((a + b) + e) + f) * 0.25f;
+                }
+            }
+        off = noff;
+        lw = nw;
+        lh = nh;
+    }
+}
+}  // namespace
+
+int oslg_texture_create(oslg_system* sys, const char* name, int width, int height, int nchannels,
+                        const float* texels, int* index) {
+    if (!sys || !name || !texels || width < 1 || height < 1 || nchannels < 1 || nchannels > 64) return OSLG_ERR_ARG;
+    return guarded(sys, [&]() {
+        oslg_system::Tex t;
+        std::memset(&t.desc, 0, sizeof(t.desc));
+        build_pyramid(width, height, nchannels, texels, t.pyramid, t.desc);
+        int id;
+        auto it = sys->ss.texture_ids.find(name);
+        if (it != sys->ss.texture_ids.end()) {  // replace in place: lowered programs keep the index
+            id = it->second;
+            t.desc.data = sys->textures[id].desc.data;  // the old pyramid, freed at the next upload
+            sys->textures[id] = std::move(t);
+        } else {
+            if (sys->textures.size() >= 256) return fail(sys, OSLG_ERR_ARG, "at most 256 textures");
+            id = (int)sys->textures.size();
+            sys->textures.push_back(std::move(t));
+            sys->ss.texture_ids[name] = id;
+        }
+        sys->textures_dirty = true;
+        if (index) *index = id;
+        return OSLG_OK;
+    });
+}
+
+// Upload new or replaced texture pyramids and the descriptor table.
+static int upload_textures(oslg_system* sys) {
+    if (!sys->textures_dirty) return OSLG_OK;
+    std::string err;
+    int rc = device_init(sys->dev, &err);
+    if (rc != OSLG_OK) return fail(sys, rc, err);
+    cudaDeviceSynchronize();  // no launch may still read the old table
+    std::vector<TexDesc> table;
+    for (auto& t : sys->textures) {
+        if (t.stale) {
+            cudaFree(const_cast<float*>(t.desc.data));
+            t.desc.data = nullptr;
+            float* dp = nullptr;
+            if (cudaMalloc(&dp, t.pyramid.size() * sizeof(float)) != cudaSuccess ||
+                cudaMemcpy(dp, t.pyramid.data(), t.pyramid.size() * sizeof(float), cudaMemcpyHostToDevice) !=
+                    cudaSuccess) {
+                cudaFree(dp);
+                return fail(sys, OSLG_ERR_CUDA, "texture upload failed");
+            }
+            t.desc.data = dp;
+            t.stale = false;
+        }
+        table.push_back(t.desc);
+    }
+    cudaFree(sys->dev.d_textures);
+    sys->dev.d_textures = nullptr;
+    if (!table.empty() &&
+        (cudaMalloc(&sys->dev.d_textures, table.size() * sizeof(TexDesc)) != cudaSuccess ||
+         cudaMemcpy(sys->dev.d_textures, table.data(), table.size() * sizeof(TexDesc), cudaMemcpyHostToDevice) !=
+             cudaSuccess))
+        return fail(sys, OSLG_ERR_CUDA, "texture table upload failed");
+    sys->dev.ntextures = (int32_t)table.size();
+    sys->textures_dirty = false;
+    return OSLG_OK;
 }
 
 // ---- execution over host buffers --------------------------------------------------

@@ -21,6 +21,8 @@ struct KArgs {
     float* gheap;
     uint32_t* status;
     oslg_shaderglobals G;
+    const TexDesc* textures = nullptr;  // the system's registered textures
+    int32_t ntextures = 0;
 };
 
 // One group's request inside a persistent batch launch.
@@ -47,6 +49,8 @@ struct BatchArgs {
     // When set, the item count is read from device memory at kernel start
     // (work lists planned on the device, e.g. by the wavefront driver).
     const uint32_t* nitems_dev = nullptr;
+    const TexDesc* textures = nullptr;
+    int32_t ntextures = 0;
 };
 }  // namespace dev
 
@@ -85,6 +89,8 @@ struct DeviceState {
     float* gheap = nullptr;
     size_t gheap_bytes = 0;
     uint32_t* d_status = nullptr;
+    TexDesc* d_textures = nullptr;  // descriptor table of the registered textures
+    int32_t ntextures = 0;
 };
 
 // Upload a program blob to the device (returns device pointer).

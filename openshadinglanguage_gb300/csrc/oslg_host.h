@@ -179,6 +179,7 @@ class ShadingSystem {
 public:
     std::map<std::string, std::shared_ptr<ShaderMaster>> masters;
     std::map<std::string, int> closure_ids;  // registered closure name -> id
+    std::map<std::string, int> texture_ids;  // registered texture name -> index
     SystemOptions opts;
     std::string last_error;
     std::mutex mutex;

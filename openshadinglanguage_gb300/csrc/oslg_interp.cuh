@@ -916,6 +916,91 @@ static __device__ void h_luminance(const Lane& L, const uint32_t* a) {
         stf(L, r, d, ldf(L, c, 0, d) * sx + ldf(L, c, 1, d) * sy + ldf(L, c, 2, d) * sz);
 }
 
+// ---- texture (src/liboslexec/optexture.cpp:54-111 osl_texture; the
+// filtering itself is OIIO's TextureSystem, which is not in the tree) ----
+// A mipmapped bilinear lookup: the footprint of (s, t)'s x/y derivatives in
+// level-0 texels (times "width") picks a level of detail log2(footprint),
+// the two nearest levels are sampled bilinearly at texel centres and
+// blended. Every step is single float operations (own_log for the level),
+// so the oracle's statement of the same steps gives the same bits.
+__device__ __forceinline__ int tex_wrap(int i, int n, uint32_t mode, bool* inside) {
+    *inside = true;
+    if (mode == TW_PERIODIC) {
+        int m = i % n;
+        return m < 0 ? m + n : m;
+    }
+    if (mode == TW_MIRROR) {
+        const int p = 2 * n;
+        int m = i % p;
+        if (m < 0) m += p;
+        return m < n ? m : p - 1 - m;
+    }
+    if (i < 0 || i >= n) {
+        *inside = mode != TW_BLACK;
+        return i < 0 ? 0 : n - 1;
+    }
+    return i;
+}
+__device__ __forceinline__ float tex_coord(float x) {
+    // finite and bounded before the float->int conversions (NaN -> 0)
+    return x == x ? fminf(fmaxf(x, -1.0e7f), 1.0e7f) : 0.0f;
+}
+__device__ __forceinline__ void tex_bilinear(const TexDesc& T, int lev, float s, float t, uint32_t sw, uint32_t tw,
+                                             int first, int nc, float* out) {
+    const int W = T.w[lev], H = T.h[lev];
+    const float* base = T.data + T.off[lev];
+    const float x = tex_coord(s * (float)W - 0.5f), y = tex_coord(t * (float)H - 0.5f);
+    const float x0 = floorf(x), y0 = floorf(y);
+    const float fx = x - x0, fy = y - y0;
+    const int ix = (int)x0, iy = (int)y0;
+    bool in_x0, in_x1, in_y0, in_y1;
+    const int cx0 = tex_wrap(ix, W, sw, &in_x0), cx1 = tex_wrap(ix + 1, W, sw, &in_x1);
+    const int cy0 = tex_wrap(iy, H, tw, &in_y0), cy1 = tex_wrap(iy + 1, H, tw, &in_y1);
+    for (int c = 0; c < nc; ++c) {
+        const int ch = first + c < T.nch ? first + c : (T.nch == 1 ? 0 : -1);
+        float v00 = 0.0f, v10 = 0.0f, v01 = 0.0f, v11 = 0.0f;
+        if (ch >= 0) {
+            if (in_x0 && in_y0) v00 = __ldg(base + ((int64_t)cy0 * W + cx0) * T.nch + ch);
+            if (in_x1 && in_y0) v10 = __ldg(base + ((int64_t)cy0 * W + cx1) * T.nch + ch);
+            if (in_x0 && in_y1) v01 = __ldg(base + ((int64_t)cy1 * W + cx0) * T.nch + ch);
+            if (in_x1 && in_y1) v11 = __ldg(base + ((int64_t)cy1 * W + cx1) * T.nch + ch);
+        }
+        const float top = (1.0f - fx) * v00 + fx * v10;
+        const float bot = (1.0f - fx) * v01 + fx * v11;
+        out[c] = (1.0f - fy) * top + fy * bot;
+    }
+}
+static __device__ void h_texture(const Lane& L, const uint32_t* a, const TexDesc* tex, int ntex, uint32_t* st) {
+    const uint32_t r = a[0];
+    const int nc = anc(r) == 3 ? 3 : 1;
+    const int id = (int)(a[3] & 0xFFu);
+    float res[3] = { 0.0f, 0.0f, 0.0f };
+    if (id < ntex) {
+        const TexDesc& T = tex[id];
+        const uint32_t sw = (a[3] >> 8) & 15u, tw = (a[3] >> 12) & 15u;
+        const int first = (int)((a[3] >> 16) & 0xFFu);
+        const D2 s = ldd(L, a[1], 0), t = ldd(L, a[2], 0);
+        const float width = ldf(L, a[4], 0, 0);
+        const float w0 = (float)T.w[0], h0 = (float)T.h[0];
+        const float dsx = s.dx * w0, dtx = t.dx * h0, dsy = s.dy * w0, dty = t.dy * h0;
+        const float len = fmaxf(sqrtf(dsx * dsx + dtx * dtx), sqrtf(dsy * dsy + dty * dty)) * width;
+        float lod = len > 1.0f ? own_log(len) * 1.44269504f : 0.0f;
+        lod = fminf(lod, (float)(T.nlevels - 1));
+        const int l0 = (int)lod;
+        const float f = lod - (float)l0;
+        tex_bilinear(T, l0, s.v, t.v, sw, tw, first, nc, res);
+        if (f > 0.0f && l0 + 1 < T.nlevels) {
+            float hi[3];
+            tex_bilinear(T, l0 + 1, s.v, t.v, sw, tw, first, nc, hi);
+            for (int c = 0; c < nc; ++c) res[c] = (1.0f - f) * res[c] + f * hi[c];
+        }
+    } else {
+        raise_status(st, ST_ARRAY_BOUNDS);
+    }
+    OSLG_SPEC_UNROLL
+    for (int c = 0; c < nc; ++c) std2(L, r, c, d2c(res[c]));
+}
+
 // blackbody (src/liboslexec/opcolor_impl.h:510-575): a2 = constant table
 // of N RGB^(1/5) entries, then the XYZ->RGB matrix and the CIE table; a3 = N
 static __device__ void h_blackbody(const Lane& L, const uint32_t* a) {
@@ -1752,6 +1837,8 @@ static const long long kMaxBackEdges = 1ll << 24;
 struct RunCtx {
     const Op* sops;
     int nops;
+    const TexDesc* textures = nullptr;
+    int ntextures = 0;
     ClosurePools CP;
     bool uses_closures;
     const oslg_shaderglobals* G;
@@ -2034,6 +2121,7 @@ __device__ __forceinline__ void exec_op(const RunCtx& R, Lane& L, uint32_t code,
     case OP_FILTERWIDTH: OSLG_TIER_CASE(4, h_deriv_misc(L, code, a)) break;
     case OP_LUMINANCE: OSLG_TIER_CASE(4, h_luminance(L, a)) break;
     case OP_BLACKBODY: OSLG_TIER_CASE(4, h_blackbody(L, a)) break;
+    case OP_TEXTURE: OSLG_TIER_CASE(4, h_texture(L, a, R.textures, R.ntextures, R.status)) break;
     case OP_NOISE: OSLG_TIER_CASE(1, h_noise(L, a)) break;
     case OP_GABOR: {
         if constexpr ((TIER & 1) != 0) {
@@ -2272,6 +2360,8 @@ __global__ void __launch_bounds__(256, 2) interp_kernel(const __grid_constant__ 
     R.userdata = k.userdata;
     R.outputs = k.outputs;
     R.status = k.status;
+    R.textures = k.textures;
+    R.ntextures = k.ntextures;
 
     Lane L;
     L.pool = spool;
@@ -2333,6 +2423,8 @@ __global__ void __launch_bounds__(MAXT, 512 / MAXT) batch_kernel(const __grid_co
             R.userdata = J->userdata;
             R.outputs = J->outputs;
             R.status = b.status;
+            R.textures = b.textures;
+            R.ntextures = b.ntextures;
             L.pool = spool;
             cur = (int)w.x;
         }

@@ -129,6 +129,8 @@ int device_execute(DeviceState& ds, const ProgramHeader& hdr, const void* d_blob
     k.outputs = static_cast<char*>(outputs);
     k.status = ds.d_status;
     k.G = G;
+    k.textures = ds.d_textures;
+    k.ntextures = ds.ntextures;
     k.gheap = nullptr;
     if (!smem) {
         size_t need = (size_t)grid * heap_bytes;

@@ -450,6 +450,11 @@ struct Lowerer {
                 for (size_t i = 2; i < op.args.size() && !is_string(op.args[i]); ++i) mark_derivs(op.args[i]);
             }
             if (op.name == "__store_output" && op.imm[2]) mark_derivs(op.args[0]);
+            // texture's footprint comes from the derivatives of s and t
+            if (op.name == "texture" && op.args.size() > 3) {
+                mark_derivs(op.args[2]);
+                mark_derivs(op.args[3]);
+            }
             if (op.name == "__load_userdata" && op.imm[2]) mark_derivs(op.args[0]);
         }
         const auto& prop = deriv_propagating_ops();
@@ -957,6 +962,57 @@ struct Lowerer {
         return true;
     }
 
+    // texture r filename s t ["option", value]... (osl_texture,
+    // src/liboslexec/optexture.cpp:54-111); the file must have been
+    // registered with oslg_texture_create. Options: wrap/swrap/twrap
+    // (black, clamp, periodic, mirror; OIIO's default is black), width,
+    // firstchannel.
+    bool lower_texture(const LOp& op) {
+        const size_t na = op.args.size();
+        if (na < 4) return fail("texture needs a result, a file name and s, t");
+        if (!is_string(op.args[1]) || !syms[op.args[1]].is_const)
+            return fail("texture: the file name must be a constant string");
+        const std::string fname = const_string(op.args[1]);
+        auto it = ss.texture_ids.find(fname);
+        if (it == ss.texture_ids.end()) return fail("texture '" + fname + "' is not registered");
+        if (na > 4 && !is_string(op.args[4]))
+            return fail("texture: explicit derivative arguments are not supported (the s, t derivatives are used)");
+        uint32_t sw = TW_BLACK, tw = TW_BLACK;
+        int first = 0;
+        float width = 1.0f;
+        for (size_t k = 4; k < na; k += 2) {
+            if (k + 1 >= na || !is_string(op.args[k]) || !syms[op.args[k]].is_const)
+                return fail("texture: options are constant name/value pairs");
+            const std::string on = const_string(op.args[k]);
+            const int v = op.args[k + 1];
+            if (!syms[v].is_const) return fail("texture option '" + on + "' must be a constant");
+            if (on == "wrap" || on == "swrap" || on == "twrap") {
+                const std::string m = is_string(v) ? const_string(v) : std::string();
+                uint32_t mode;
+                if (m == "black" || m == "default") mode = TW_BLACK;
+                else if (m == "clamp") mode = TW_CLAMP;
+                else if (m == "periodic") mode = TW_PERIODIC;
+                else if (m == "mirror") mode = TW_MIRROR;
+                else return fail("texture: wrap mode '" + m + "' is not supported");
+                if (on != "twrap") sw = mode;
+                if (on != "swrap") tw = mode;
+            } else if (on == "width" && !syms[v].cval.empty()) {
+                width = syms[v].cval[0];
+            } else if (on == "firstchannel" && !syms[v].cval.empty()) {
+                first = (int)syms[v].cval[0];
+                if (first < 0 || first > 255) return fail("texture: firstchannel out of range");
+            } else {
+                return fail("texture option '" + on + "' is not supported");
+            }
+        }
+        if (it->second > 255) return fail("too many textures");
+        const int wc = const_float(width);
+        syms[wc].slot = (int)pool_add(syms[wc]);
+        emit(OP_TEXTURE, { A(op.args[0]), A(op.args[2]), A(op.args[3]),
+                           (uint32_t)it->second | (sw << 8) | (tw << 12) | ((uint32_t)first << 16), A(wc) }, "texture");
+        return true;
+    }
+
     bool lower_op(const LOp& op, int depth, int loopl) {
         const std::string& n = op.name;
         auto a = [&](int i) { return A(op.args[i]); };
@@ -1188,6 +1244,7 @@ struct Lowerer {
             emit(OP_BLACKBODY, { a(0), a(1), A(tb), (uint32_t)((t.size() - 9 - 243) / 3) }, n);
             return true;
         }
+        if (n == "texture") return lower_texture(op);
         if (n == "luminance") {
             int sc = const_triple(luminance_scale());
             emit(OP_LUMINANCE, { a(0), a(1), A(sc) }, n);
@@ -1234,7 +1291,7 @@ struct Lowerer {
             case OP_SMOOTHSTEP: case OP_SELECT: case OP_DOT: case OP_CROSS: case OP_LENGTH: case OP_DISTANCE:
             case OP_NORMALIZE: case OP_TRANSFORM: case OP_MMUL: case OP_AREF: case OP_AASSIGN:
             case OP_MDIV: case OP_TRANSPOSE: case OP_DETERMINANT: case OP_AREA: case OP_FILTERWIDTH:
-            case OP_LUMINANCE: case OP_BLACKBODY:
+            case OP_LUMINANCE: case OP_BLACKBODY: case OP_TEXTURE:
                 t |= 4u;
                 break;
             default: break;

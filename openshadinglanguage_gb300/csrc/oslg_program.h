@@ -20,7 +20,7 @@
 namespace oslg {
 
 static const uint32_t kProgramMagic = 0x4f534c47u;  // "OSLG"
-static const uint32_t kProgramVersion = 3;
+static const uint32_t kProgramVersion = 4;
 
 // ---- operand words ----------------------------------------------------------
 // bits 0..19  slot offset (heap) or index (constant pool)
@@ -125,6 +125,8 @@ enum OpCode : uint16_t {
                      // a4=I (triple global) a5=hash("ggx")
     OP_BSDF_SAMPLE,  // a0=closure a1=out byte offset a2=out byte stride a3=I (triple
                      // global) a4=hash("ggx") a5=userdata byte offset a6=userdata stride
+    OP_TEXTURE,      // a0=r (float or triple) a1=s a2=t (Dual2: the footprint) a3=texture
+                     // index | swrap << 8 | twrap << 12 | firstchannel << 16 a4=width
     OP_COUNT
 };
 
@@ -201,6 +203,20 @@ struct ProgramHeader {
     uint32_t reserved[6];
 };
 static_assert(sizeof(ProgramHeader) == 64, "header must be 64 bytes");
+
+// Texture wrap modes (OP_TEXTURE), the names of OIIO's TextureOpt::Wrap.
+enum TexWrap : uint32_t { TW_PERIODIC = 0, TW_CLAMP = 1, TW_BLACK = 2, TW_MIRROR = 3 };
+static const int kTexMaxLevels = 16;
+
+// A registered texture: a mip pyramid of float texels (level 0 the image,
+// each next level a 2x2 box reduction), channels interleaved, rows from the
+// top (t = 0).
+struct TexDesc {
+    const float* data;  // device address of the whole pyramid
+    int32_t nch, nlevels;
+    int32_t w[kTexMaxLevels], h[kTexMaxLevels];
+    int64_t off[kTexMaxLevels];  // float offset of each level
+};
 
 // Status bits a kernel reports back (OR-ed across points).
 enum StatusBits : uint32_t {

@@ -363,6 +363,8 @@ int ShadingServer::launch_wave(Slot& s, std::vector<Request*>& wave, std::string
     a.counter = s.d_counter;
     a.gheap = s.d_heap;
     a.status = ds_.d_status;
+    a.textures = ds_.d_textures;
+    a.ntextures = ds_.ntextures;
     a.prog_bytes = pbytes;
     a.heap_slots = slots;
     if (!ok((cudaError_t)batch_variant_launch(maxt, opt_.points_per_thread, false, (unsigned)grid_,

@@ -277,6 +277,7 @@ std::string spec_source(const CompiledGroup& cg, int min_blocks) {
     o << "    R.CP.base = " << h.closure_base << "u;\n    R.CP.max_nodes = " << h.max_comps << "u;\n";
     o << "    R.uses_closures = " << (uses_cl ? "true" : "false") << ";\n";
     o << "    R.G = &k.G;\n    R.userdata = k.userdata;\n    R.outputs = k.outputs;\n    R.status = k.status;\n";
+    o << "    R.textures = k.textures;\n    R.ntextures = k.ntextures;\n";
     o << "    float hreg[" << std::max(1u, sym) << "];\n";
     o << "    Lane L;\n    L.heap = hreg;\n    L.pool = kPool;\n    L.hs = 1;\n    L.li = 0;\n    L.pt = 0;\n";
     // dynamic shared memory: [staged records | written flags] then the closure pools
@@ -346,6 +347,7 @@ std::string spec_batch_source(const std::vector<const CompiledGroup*>& cases) {
     o << "    L.cheap = pool_in_smem ? reinterpret_cast<float*>(smem) : b.gheap + (size_t)blockIdx.x * b.heap_slots * "
          "blockDim.x;\n";
     o << "    RunCtx R;\n    R.sops = nullptr;\n    R.status = b.status;\n";
+    o << "    R.textures = b.textures;\n    R.ntextures = b.ntextures;\n";
     o << "    for (;;) {\n";
     o << "        if (threadIdx.x == 0) s_item = atomicAdd(b.counter, 1u);\n";
     o << "        __syncthreads();\n        const uint32_t it = s_item;\n        __syncthreads();\n";
@@ -475,6 +477,8 @@ int spec_launch(DeviceState& ds, const SpecKernel& sk, const CompiledGroup& cg, 
     k.outputs = static_cast<char*>(outputs);
     k.status = ds.d_status;
     k.G = G;
+    k.textures = ds.d_textures;
+    k.ntextures = ds.ntextures;
     k.gheap = nullptr;
     if (sk.pool_slots > 0 && !in_smem) {
         int per_sm = 0;

@@ -929,6 +929,8 @@ int Wavefront::init(DeviceState& ds, const oslg_wavefront_options& o, const oslg
     bargs_.counter = d_ctl_ + dev::C_COUNTER;
     bargs_.gheap = smem_heap_ ? nullptr : d_heap_;
     bargs_.status = ds.d_status;
+    bargs_.textures = ds.d_textures;
+    bargs_.ntextures = ds.ntextures;
     bargs_.prog_bytes = prog_bytes;
     bargs_.heap_slots = slots;
     if (jit_dirs) {

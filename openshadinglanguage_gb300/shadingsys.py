@@ -235,6 +235,19 @@ class ShadingSystem:
         """A wavefront path tracer over `prims` shaded by `materials` (see Wavefront)."""
         return Wavefront(self, prims, materials, **options)
 
+    def texture_create(self, name, texels):
+        """Register an image for texture(name, ...): texels is a float32
+        array (height, width, nchannels) or (height, width); returns its index."""
+        import numpy as np
+        a = np.ascontiguousarray(texels, dtype=np.float32)
+        if a.ndim == 2:
+            a = a[:, :, None]
+        h, w, nch = a.shape
+        idx = ctypes.c_int(-1)
+        self._check(C.lib().oslg_texture_create(self._h, name.encode(), int(w), int(h), int(nch),
+                                                ctypes.c_void_p(a.ctypes.data), ctypes.byref(idx)))
+        return idx.value
+
     def execute_batch_host(self, group, npoints, globals_c, outputs, output_stride, userdata=None,
                            userdata_stride=0, preserve_outputs=False):
         """BatchedExecutor::execute over host buffers (oslg_execute_batch_host):

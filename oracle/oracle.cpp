@@ -563,6 +563,125 @@ void op_luminance(Point& P, const uint32_t* a) {
     for (int d = 0; d < nd; ++d) setf(P, a[0], d, getf(P, a[1], 0, d) * sx + getf(P, a[1], 1, d) * sy + getf(P, a[1], 2, d) * sz);
 }
 
+// ---- texture: mipmapped bilinear lookup (osl_texture, optexture.cpp:54-111;
+// the filter stands in for OIIO's TextureSystem, which is not in the tree) --
+struct OTexture {
+    int nch = 0, nlevels = 0;
+    int w[oslg::kTexMaxLevels] = {}, h[oslg::kTexMaxLevels] = {};
+    std::vector<std::vector<float>> level;
+};
+std::vector<OTexture>& otextures() {
+    static std::vector<OTexture> t;
+    return t;
+}
+// level 0 the image; each next level the 2x2 box average of the previous
+// (coordinates clamped at odd edges) down to 1x1 or 16 levels
+void otex_build(OTexture& T, int w, int h, int nch, const float* src) {
+    T.nch = nch;
+    T.level.clear();
+    T.level.emplace_back(src, src + (size_t)w * h * nch);
+    T.nlevels = 0;
+    int lw = w, lh = h;
+    for (;;) {
+        T.w[T.nlevels] = lw;
+        T.h[T.nlevels] = lh;
+        ++T.nlevels;
+        if ((lw == 1 && lh == 1) || T.nlevels == oslg::kTexMaxLevels) break;
+        const int nw = std::max(1, lw / 2), nh = std::max(1, lh / 2);
+        std::vector<float> next((size_t)nw * nh * nch);
+        const std::vector<float>& prev = T.level.back();
+        for (int y = 0; y < nh; ++y)
+            for (int x = 0; x < nw; ++x)
+                for (int c = 0; c < nch; ++c) {
+                    const int x0 = std::min(2 * x, lw - 1), x1 = std::min(2 * x + 1, lw - 1);
+                    const int y0 = std::min(2 * y, lh - 1), y1 = std::min(2 * y + 1, lh - 1);
+                    const float p00 = prev[((size_t)y0 * lw + x0) * nch + c];
+                    const float p10 = prev[((size_t)y0 * lw + x1) * nch + c];
+                    const float p01 = prev[((size_t)y1 * lw + x0) * nch + c];
+                    const float p11 = prev[((size_t)y1 * lw + x1) * nch + c];
+                    next[((size_t)y * nw + x) * nch + c] = (((p00 + p10) + p01) + p11) * 0.25f;
+                }
+        T.level.push_back(std::move(next));
+        lw = nw;
+        lh = nh;
+    }
+}
+// texel index under the wrap mode; `inside` false for black outside the image
+int otex_wrap(int i, int n, uint32_t mode, bool* inside) {
+    *inside = true;
+    if (mode == oslg::TW_PERIODIC) {
+        const int m = i % n;
+        return m < 0 ? m + n : m;
+    }
+    if (mode == oslg::TW_MIRROR) {
+        const int p = 2 * n;
+        int m = i % p;
+        if (m < 0) m += p;
+        return m < n ? m : p - 1 - m;
+    }
+    if (i < 0 || i >= n) {
+        *inside = mode != oslg::TW_BLACK;
+        return i < 0 ? 0 : n - 1;
+    }
+    return i;
+}
+float otex_coord(float x) { return x == x ? std::min(std::max(x, -1.0e7f), 1.0e7f) : 0.0f; }
+void otex_bilinear(const OTexture& T, int lev, float s, float t, uint32_t sw, uint32_t tw, int first, int nc,
+                   float* out) {
+    const int W = T.w[lev], H = T.h[lev];
+    const std::vector<float>& L = T.level[lev];
+    const float x = otex_coord(s * (float)W - 0.5f), y = otex_coord(t * (float)H - 0.5f);
+    const float x0 = std::floor(x), y0 = std::floor(y);
+    const float fx = x - x0, fy = y - y0;
+    const int ix = (int)x0, iy = (int)y0;
+    bool ix0, ix1, iy0, iy1;
+    const int cx0 = otex_wrap(ix, W, sw, &ix0), cx1 = otex_wrap(ix + 1, W, sw, &ix1);
+    const int cy0 = otex_wrap(iy, H, tw, &iy0), cy1 = otex_wrap(iy + 1, H, tw, &iy1);
+    for (int c = 0; c < nc; ++c) {
+        const int ch = first + c < T.nch ? first + c : (T.nch == 1 ? 0 : -1);
+        float v00 = 0.0f, v10 = 0.0f, v01 = 0.0f, v11 = 0.0f;
+        if (ch >= 0) {
+            if (ix0 && iy0) v00 = L[((size_t)cy0 * W + cx0) * T.nch + ch];
+            if (ix1 && iy0) v10 = L[((size_t)cy0 * W + cx1) * T.nch + ch];
+            if (ix0 && iy1) v01 = L[((size_t)cy1 * W + cx0) * T.nch + ch];
+            if (ix1 && iy1) v11 = L[((size_t)cy1 * W + cx1) * T.nch + ch];
+        }
+        const float top = (1.0f - fx) * v00 + fx * v10;
+        const float bot = (1.0f - fx) * v01 + fx * v11;
+        out[c] = (1.0f - fy) * top + fy * bot;
+    }
+}
+void op_texture(Point& P, const uint32_t* a) {
+    const uint32_t r = a[0];
+    const int nc = anc(r) == 3 ? 3 : 1;
+    const int id = (int)(a[3] & 0xFFu);
+    float res[3] = { 0.0f, 0.0f, 0.0f };
+    const std::vector<OTexture>& tex = otextures();
+    if (id < (int)tex.size() && tex[id].nlevels > 0) {
+        const OTexture& T = tex[id];
+        const uint32_t sw = (a[3] >> 8) & 15u, tw = (a[3] >> 12) & 15u;
+        const int first = (int)((a[3] >> 16) & 0xFFu);
+        const DF s = getd(P, a[1], 0), t = getd(P, a[2], 0);
+        const float width = getf(P, a[4], 0, 0);
+        const float w0 = (float)T.w[0], h0 = (float)T.h[0];
+        const float dsx = s.dx * w0, dtx = t.dx * h0, dsy = s.dy * w0, dty = t.dy * h0;
+        const float len = std::max(std::sqrt(dsx * dsx + dtx * dtx), std::sqrt(dsy * dsy + dty * dty)) * width;
+        float lod = len > 1.0f ? oracle::own_log(len) * 1.44269504f : 0.0f;
+        lod = std::min(lod, (float)(T.nlevels - 1));
+        const int l0 = (int)lod;
+        const float f = lod - (float)l0;
+        otex_bilinear(T, l0, s.v, t.v, sw, tw, first, nc, res);
+        if (f > 0.0f && l0 + 1 < T.nlevels) {
+            float hi[3];
+            otex_bilinear(T, l0 + 1, s.v, t.v, sw, tw, first, nc, hi);
+            for (int c = 0; c < nc; ++c) res[c] = (1.0f - f) * res[c] + f * hi[c];
+        }
+    } else {
+        P.status |= oslg::ST_ARRAY_BOUNDS;
+    }
+    for (int c = 0; c < nc; ++c) putd(P, r, c, DF(res[c]));
+}
+
 // blackbody (src/liboslexec/opcolor_impl.h:510-575, opcolor.cpp:438-442):
 // a2 = constant table (N entries of RGB^(1/5), XYZ->RGB matrix, CIE table)
 void op_blackbody(Point& P, const uint32_t* a) {
@@ -1123,6 +1242,7 @@ struct Runner {
             case oslg::OP_FILTERWIDTH: op_filterwidth(P, a); break;
             case oslg::OP_LUMINANCE: op_luminance(P, a); break;
             case oslg::OP_BLACKBODY: op_blackbody(P, a); break;
+            case oslg::OP_TEXTURE: op_texture(P, a); break;
             case oslg::OP_NOISE: op_noise(P, a); break;
             case oslg::OP_GABOR: op_gabor(P, a, prog.ops[pc + 1].a); break;
             case oslg::OP_HASH: op_hash(P, a); break;
@@ -1305,6 +1425,16 @@ bool resolve(Prog& p, const void* blob, size_t bytes) {
 }  // namespace
 
 extern "C" {
+
+// Register texture `id` (the same index the executor assigned) for the
+// oracle's texture lookups.
+int oracle_texture_create(int id, int width, int height, int nchannels, const float* texels) {
+    if (id < 0 || id > 255 || width < 1 || height < 1 || nchannels < 1) return -1;
+    std::vector<OTexture>& t = otextures();
+    if ((int)t.size() <= id) t.resize(id + 1);
+    otex_build(t[id], width, height, nchannels, texels);
+    return 0;
+}
 
 // Run a lowered program over points [begin, end) on the host. Globals,
 // userdata and outputs are host memory with the device layout.
