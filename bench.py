@@ -353,6 +353,65 @@ def bench_wavefront(torch, og, frames=3, cpu_step=97, size=None, jit=1):
                               "batched shading per material)" % cpu_step}}
 
 
+def bench_texture(torch, og, reps=10):
+    """texture() throughput: a 2048x2048 grid looking up a registered
+    1024x1024 RGB image (4 MB level 0, 11-level pyramid) at s, t = 1.7 u,
+    1.7 v (footprint between levels 0 and 1: two bilinear lookups blended),
+    periodic wrap; interpreter and specialized kernel; the oracle on a
+    sample of the points on all host threads. Image and grid stay in L2
+    between launches (4 MB + 32 MB in, 50 MB out): the number is the
+    filter's arithmetic rate, not an HBM figure."""
+    from helpers import grid_globals, oracle, oracle_run, pixel_grid, single_layer_group
+    from openshadinglanguage_gb300.shaders import texture_lookup as tex_shader
+    import ctypes
+    img = np.random.default_rng(7).random((1024, 1024, 3), dtype=np.float32)
+    W = H = 2048
+    n = W * H
+    u, v = pixel_grid(W, H, centers=True)
+    du, dv = torch.from_numpy(u).cuda(), torch.from_numpy(v).cuda()
+    out = torch.empty(n * 3, dtype=torch.float32, device="cuda")
+    st = torch.cuda.current_stream()
+    res = {"workload": "texture 2048x2048 lookups of a 1024x1024 RGB float image, trilinear, periodic"}
+    for jit in (0, 1):
+        ss = og.ShadingSystem()
+        if jit:
+            ss.attribute("jit", 1)
+        idx = ss.texture_create("img", img)
+        g = single_layer_group(ss, "btex", tex_shader("btex", 1.7, "periodic"),
+                               outputs=[og.SymLocationDesc("Cout", og.TypeColor, False, og.SymArenaOutputs, 0, 12)])
+        G = grid_globals(du, dv, W, H, centers=True)
+        for _ in range(3):
+            ss.execute_batch(g, n, G, 0, out.data_ptr(), st.cuda_stream)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(reps):
+            ss.execute_batch(g, n, G, 0, out.data_ptr(), st.cuda_stream)
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        res["specialized" if jit else "interpreter"] = {"ms": ms, "mpts_per_s": n / ms / 1e3,
+                                                         "device_status": ss.device_status()}
+        if not jit:
+            L = oracle()
+            L.oracle_texture_create.argtypes = [ctypes.c_int] * 4 + [ctypes.c_void_p]
+            L.oracle_texture_create(idx, 1024, 1024, 3, img.ctypes.data)
+            m = 1 << 20
+            ref = np.zeros((m, 3), np.float32)
+            Gh = grid_globals(u[:m], v[:m], W, H, centers=True)
+            t0 = time.perf_counter()
+            oracle_run(g.program_bytes(), m, Gh, ref)
+            dt = time.perf_counter() - t0
+            res["cpu"] = {"mpts_per_s": m / dt / 1e6, "points": m, "threads": os.cpu_count(), "kind": "port"}
+        out.zero_()
+        ss.execute_batch(g, n, G, 0, out.data_ptr(), st.cuda_stream)
+        torch.cuda.synchronize()
+        got = out.cpu().numpy().reshape(n, 3)[:m]
+        res["specialized" if jit else "interpreter"]["bit_exact_sample"] = bool(
+            np.array_equal(got.view(np.uint32), ref.view(np.uint32)))
+    return res
+
+
 def cpu_reference(wl, og, budget_s=2.0):
     """Time the CPU port of the reference semantics on all host threads."""
     from helpers import oracle_run
@@ -391,7 +450,7 @@ def main():
     ap.add_argument("--jit-pool-smem", type=int, default=-1, help="specialized launch: closure pools in smem (1/0)")
     ap.add_argument("--jit-min-blocks", type=int, default=0,
                     help="specialized kernel register cap: 256-thread CTAs per SM it must fit (2..8)")
-    ap.add_argument("--section", choices=["batching", "serving", "wavefront"],
+    ap.add_argument("--section", choices=["batching", "serving", "wavefront", "texture"],
                     help="run only this measurement section and print it as one JSON line")
     ap.add_argument("--wf-size", default=None, help="wavefront frame WxHxSPP (default 1920x1080x4)")
     args = ap.parse_args()
@@ -403,7 +462,8 @@ def main():
         build_native()
         torch.cuda.set_device(0)
         fn = {"batching": lambda: bench_batching(torch, og), "serving": lambda: bench_serving(torch, og),
-              "wavefront": lambda: bench_wavefront(torch, og, size=args.wf_size, jit=args.jit)}[args.section]
+              "wavefront": lambda: bench_wavefront(torch, og, size=args.wf_size, jit=args.jit),
+              "texture": lambda: bench_texture(torch, og)}[args.section]
         print(json.dumps({"section": args.section, args.section: fn()}))
         return 0
 
@@ -565,6 +625,7 @@ def main():
         line["batching"] = bench_batching(torch, og)
         line["serving"] = bench_serving(torch, og)
         line["wavefront"] = bench_wavefront(torch, og, jit=args.jit)
+        line["texture"] = bench_texture(torch, og)
     if not args.no_cpu_baseline:
         from helpers import oracle_run  # noqa: F401
         build_oracle()

@@ -600,3 +600,25 @@ def c2_knots(seed=0xC2B):
     import numpy as np
     rng = np.random.default_rng(seed)
     return [float(x) for x in rng.uniform(0.05, 0.95, 24).astype(np.float32)]
+
+
+def texture_lookup(name, scale, wrap=None, nc=3, width=None, first=None):
+    """Cout = texture("img", u * k, v * k, options): k = scale, so the lookup
+    footprint is scale / grid size in texture space (derivatives of u, v)."""
+    from .oso import OsoBuilder
+    b = OsoBuilder(name)
+    out = b.param("color" if nc == 3 else "float", "Cout", [0, 0, 0] if nc == 3 else 0.0, output=True)
+    u, v = b.glob("float", "u"), b.glob("float", "v")
+    s, t = b.tmp("float"), b.tmp("float")
+    k = b.param("float", "k", float(scale))
+    b.op("mul", s, u, k)
+    b.op("mul", t, v, k)
+    args = [out, b.const("string", "img"), s, t]
+    if wrap:
+        args += [b.const("string", "wrap"), b.const("string", wrap)]
+    if width is not None:
+        args += [b.const("string", "width"), b.const("float", float(width))]
+    if first is not None:
+        args += [b.const("string", "firstchannel"), b.const("int", int(first))]
+    b.op("texture", *args)
+    return b.text()

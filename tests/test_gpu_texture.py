@@ -11,7 +11,7 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 from test_gpu_parity import assert_same, device_grid_globals, gpu_run  # noqa: E402
-from test_texture import make_image, register, tex_shader  # noqa: E402
+from test_texture import make_image, register, tex_shader  # noqa: E402,F401
 
 
 @pytest.fixture(scope="module", autouse=True)

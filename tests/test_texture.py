@@ -8,27 +8,9 @@ import numpy as np
 import pytest
 
 from helpers import grid_globals, og, oracle, oracle_run, pixel_grid, single_layer_group
+from openshadinglanguage_gb300.shaders import texture_lookup as tex_shader
 
 WRAPS = ("black", "clamp", "periodic", "mirror")
-
-
-def tex_shader(name, scale, wrap=None, nc=3, width=None, first=None):
-    b = og.OsoBuilder(name)
-    out = b.param("color" if nc == 3 else "float", "Cout", [0, 0, 0] if nc == 3 else 0.0, output=True)
-    u, v = b.glob("float", "u"), b.glob("float", "v")
-    s, t = b.tmp("float"), b.tmp("float")
-    k = b.param("float", "k", float(scale))
-    b.op("mul", s, u, k)
-    b.op("mul", t, v, k)
-    args = [out, b.const("string", "img"), s, t]
-    if wrap:
-        args += [b.const("string", "wrap"), b.const("string", wrap)]
-    if width is not None:
-        args += [b.const("string", "width"), b.const("float", float(width))]
-    if first is not None:
-        args += [b.const("string", "firstchannel"), b.const("int", int(first))]
-    b.op("texture", *args)
-    return b.text()
 
 
 def make_image(h, w, nch, seed=5):
