@@ -209,6 +209,19 @@ int oslg_group_is_specialized(oslg_system* sys, oslg_group* group, int* out);
  * Groups naming the texture must be lowered after it is registered. */
 int oslg_texture_create(oslg_system* sys, const char* name, int width, int height, int nchannels,
                         const float* texels, int* index);
+/* Answer getattribute([object,] name, [index,] value) in shaders with a
+ * uniform value: the renderer side of RendererServices::get_attribute /
+ * get_array_attribute (src/include/OSL/rendererservices.h:278-288) and
+ * BatchedRendererServices::get_attribute_uniform
+ * (src/include/OSL/batched_rendererservices.h:143-156). object NULL or ""
+ * is the scene-wide name space that a lookup without an object name reads.
+ * data: max(1, arraylen) elements of the type (floats, int32, or
+ * const char* for strings). Lookups fold to constants when a group is
+ * lowered, as the reference's constant folder does
+ * (src/liboslexec/constfold.cpp:2262-2360); a name with no value makes
+ * getattribute return 0 and leave its destination unchanged. */
+int oslg_renderer_attribute(oslg_system* sys, const char* object, const char* name, oslg_typedesc type,
+                            const void* data);
 /* ShaderGroupRef release */
 int oslg_release_group(oslg_system* sys, oslg_group* group);
 

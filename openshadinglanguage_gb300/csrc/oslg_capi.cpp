@@ -197,6 +197,7 @@ int oslg_attribute_int(oslg_system* sys, const char* name, int value) {
     else if (n == "gpu_heap_placement") sys->launch.heap_smem = value;
     else if (n == "gpu_grid") sys->launch.grid = value;
     else if (n == "debug") sys->ss.opts.debug = value;
+    else if (n == "strict_messages") sys->ss.opts.strict_messages = value != 0;
     else if (n == "jit") sys->jit = value;
     else if (n == "jit_block") sys->jit_block = value;
     else if (n == "jit_pool_smem") sys->jit_pool_smem = value;
@@ -544,6 +545,26 @@ int oslg_texture_create(oslg_system* sys, const char* name, int width, int heigh
     });
 }
 
+int oslg_renderer_attribute(oslg_system* sys, const char* object, const char* name, oslg_typedesc type,
+                            const void* data) {
+    if (!sys || !name || !data) return OSLG_ERR_ARG;
+    return guarded(sys, [&]() {
+        RendererAttribute a;
+        if (!typedesc_to_spec(type, a.type) || a.type.arraylen < 0)
+            return fail(sys, OSLG_ERR_ARG, "unsupported attribute type");
+        const int elems = a.type.elems();
+        if (a.type.base == BT_STRING) {
+            const char* const* sv = static_cast<const char* const*>(data);
+            for (int i = 0; i < elems; ++i) a.strings.push_back(sv[i] ? sv[i] : "");
+        } else {
+            const uint32_t* w = static_cast<const uint32_t*>(data);
+            a.words.assign(w, w + (size_t)elems * a.type.ncomp());
+        }
+        sys->ss.attributes[{ object ? object : "", name }] = std::move(a);
+        return OSLG_OK;
+    });
+}
+
 // Upload new or replaced texture pyramids and the descriptor table.
 static int upload_textures(oslg_system* sys) {
     if (!sys->textures_dirty) return OSLG_OK;
@@ -765,6 +786,7 @@ int oslg_execute_batch_sync(oslg_system* sys, oslg_group* group, int64_t npoints
         if (bits & ST_BAD_OPCODE) m += " bad-opcode";
         if (bits & ST_ARRAY_BOUNDS) m += " index-out-of-range";
         if (bits & ST_TIMEOUT) m += " loop-iteration-limit";
+        if (bits & ST_MESSAGE) m += " message-error";
         return fail(sys, OSLG_ERR_DEVICE, m);
     }
     return OSLG_OK;

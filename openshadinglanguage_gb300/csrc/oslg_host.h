@@ -166,8 +166,23 @@ struct ShaderGroup {
     int find_layer(const std::string& n) const;
 };
 
+// The OSL release whose behaviour this executor follows (1.16.0), as
+// OSL_LIBRARY_VERSION_CODE: 10000 * major + 100 * minor + patch; what
+// getattribute("osl:version") answers.
+static const int kOslVersionCode = 11600;
+
+// A uniform attribute the renderer answers getattribute with
+// (RendererServices::get_attribute for one object, or scene-wide under the
+// empty object name); values as device words (strings hashed).
+struct RendererAttribute {
+    TypeSpec type;
+    std::vector<uint32_t> words;
+    std::vector<std::string> strings;
+};
+
 struct SystemOptions {
     int debug = 0;
+    int strict_messages = 1;  // ShadingSystem attribute "strict_messages" (shadingsys.cpp:1078)
     int max_closure_components = 16;  // closure tree nodes per point
     int max_closure_terms = 16;
     int heap_in_smem = -1;  // -1 auto
@@ -180,6 +195,7 @@ public:
     std::map<std::string, std::shared_ptr<ShaderMaster>> masters;
     std::map<std::string, int> closure_ids;  // registered closure name -> id
     std::map<std::string, int> texture_ids;  // registered texture name -> index
+    std::map<std::pair<std::string, std::string>, RendererAttribute> attributes;  // (object, name)
     SystemOptions opts;
     std::string last_error;
     std::mutex mutex;

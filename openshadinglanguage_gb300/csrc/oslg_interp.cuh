@@ -1001,6 +1001,49 @@ static __device__ void h_texture(const Lane& L, const uint32_t* a, const TexDesc
     for (int c = 0; c < nc; ++c) std2(L, r, c, d2c(res[c]));
 }
 
+// setmessage / getmessage between the layers of one point
+// (src/liboslexec/opmessage.cpp:19-138): a message name has one state word
+// per point (0 unset, 1 + type id once set, kMsgQueried after a strict query
+// that found nothing) and one store per type it is used with. Setting a
+// message twice, setting it after a failed strict query, or reading it as
+// another type is an error (status bit) that leaves the values unchanged.
+// Stored values carry no derivatives; a found message zeroes the
+// destination's.
+static __device__ void h_setmessage(const Lane& L, const uint32_t* a, uint32_t* st) {
+    const uint32_t state = a[0], store = a[1], src = a[2];
+    const int nw = (int)(a[3] & 0xFFFFu);
+    if (ldw(L, state, 0) != 0u) {
+        raise_status(st, ST_MESSAGE);
+        return;
+    }
+    stw(L, state, 0, 1u + (a[3] >> 16));
+    OSLG_SPEC_UNROLL
+    for (int i = 0; i < nw; ++i) stw(L, store, i, ldw(L, src, i));
+}
+static __device__ void h_getmessage(const Lane& L, const uint32_t* a, uint32_t* st) {
+    const uint32_t state = a[1], store = a[2], dst = a[3];
+    const int nw = (int)(a[4] & 0xFFFFu);
+    const uint32_t tid = (a[4] >> 16) & 0x7FFFu;
+    const uint32_t s = ldw(L, state, 0);
+    uint32_t found = 0u;
+    if (s == 0u) {
+        if (a[4] >> 31) stw(L, state, 0, kMsgQueried);
+    } else if (s != kMsgQueried) {
+        if (s != 1u + tid) {
+            raise_status(st, ST_MESSAGE);
+        } else {
+            OSLG_SPEC_UNROLL
+            for (int i = 0; i < nw; ++i) stw(L, dst, i, ldw(L, store, i));
+            if (ader(dst)) {
+                OSLG_SPEC_UNROLL
+                for (int i = nw; i < 3 * nw; ++i) stw(L, dst, i, 0u);
+            }
+            found = 1u;
+        }
+    }
+    stw(L, a[0], 0, found);
+}
+
 // blackbody (src/liboslexec/opcolor_impl.h:510-575): a2 = constant table
 // of N RGB^(1/5) entries, then the XYZ->RGB matrix and the CIE table; a3 = N
 static __device__ void h_blackbody(const Lane& L, const uint32_t* a) {
@@ -2122,6 +2165,8 @@ __device__ __forceinline__ void exec_op(const RunCtx& R, Lane& L, uint32_t code,
     case OP_LUMINANCE: OSLG_TIER_CASE(4, h_luminance(L, a)) break;
     case OP_BLACKBODY: OSLG_TIER_CASE(4, h_blackbody(L, a)) break;
     case OP_TEXTURE: OSLG_TIER_CASE(4, h_texture(L, a, R.textures, R.ntextures, R.status)) break;
+    case OP_SETMESSAGE: OSLG_TIER_CASE(4, h_setmessage(L, a, R.status)) break;
+    case OP_GETMESSAGE: OSLG_TIER_CASE(4, h_getmessage(L, a, R.status)) break;
     case OP_NOISE: OSLG_TIER_CASE(1, h_noise(L, a)) break;
     case OP_GABOR: {
         if constexpr ((TIER & 1) != 0) {

@@ -202,6 +202,10 @@ struct Lowerer {
     uint32_t heap_top = 0;
     uint32_t max_depth = 0;
     bool uses_closures = false;
+    // messages: per name a state symbol, per (name, type) a value store
+    std::map<std::string, int> msg_state;
+    std::map<std::string, int> msg_store;
+    std::map<std::string, int> msg_type_id;
 
     Lowerer(ShadingSystem& s, ShaderGroup& gg, std::string& e) : ss(s), g(gg), err(e) {}
 
@@ -406,6 +410,11 @@ struct Lowerer {
 
     // ---- analysis ----------------------------------------------------------
     static bool writes_arg(const LOp& op, int i) {
+        // after prepare_messages: setmessage (name, value, state, store),
+        // getmessage (result, name, dest, state, store)
+        if (op.name == "setmessage") return i == 2 || i == 3;
+        if (op.name == "getmessage") return i == 0 || i == 2 || i == 3;
+        if (op.name == "getattribute") return i == 0 || i == (int)op.args.size() - 1;
         if (!op.argrw.empty() && i < (int)op.argrw.size())
             return op.argrw[i] == 'w' || op.argrw[i] == 'W';
         static const std::set<std::string> nowrite = {
@@ -491,12 +500,110 @@ struct Lowerer {
             if (s.is_const) s.derivs = false;
     }
 
+    // ---- messages ------------------------------------------------------------
+    // setmessage/getmessage with constant names become ops on hidden
+    // per-point symbols. A getmessage that no earlier setmessage of its name
+    // precedes (in layer and op order) can never find a message and becomes
+    // `result = 0`, as constfold_getmessage does
+    // (src/liboslexec/constfold.cpp:2240-2258). A sourced getmessage asks
+    // the renderer, whose default answer is "not found"
+    // (batched_rendererservices.h getmessage): it folds to 0 as well.
+    static std::string msg_type_key(const TypeSpec& t) {
+        return std::to_string((int)t.base) + ":" + std::to_string((int)t.vecsem) + ":" + std::to_string(t.arraylen);
+    }
+    int msg_store_for(const std::string& name, const TypeSpec& t) {
+        const std::string key = name + "|" + msg_type_key(t);
+        auto it = msg_store.find(key);
+        if (it != msg_store.end()) return it->second;
+        GSym v; v.name = "$msg." + name; v.type = t; v.kind = SK_LOCAL;
+        int id = add_sym(v);
+        msg_store[key] = id;
+        return id;
+    }
+    uint32_t msg_tid(const TypeSpec& t) {
+        auto ins = msg_type_id.insert({ msg_type_key(t), (int)msg_type_id.size() });
+        return (uint32_t)ins.first->second;
+    }
+    // A layer other than the last with no outgoing connection and no
+    // renderer output is unused and removed, as ShaderInstance::unused()
+    // decides with the default lazyunconnected
+    // (src/liboslexec/oslexec_pvt.h:1477-1491): its messages are never sent.
+    bool layer_used(int li) {
+        if (li == (int)g.layers.size() - 1) return true;
+        for (size_t lj = (size_t)li + 1; lj < g.layers.size(); ++lj)
+            for (const Connection& c : g.layers[lj].connections)
+                if (c.srclayer == li) return true;
+        auto in_layer = [&](const std::string& nm) {
+            SymLoc tmp;
+            tmp.name = nm;
+            int gs = resolve_symloc(tmp);
+            return gs >= 0 && syms[gs].layer == li;
+        };
+        for (const SymLoc& sl : g.symlocs)
+            if (sl.arena == ARENA_OUTPUTS && in_layer(sl.name)) return true;
+        for (const BsdfEvalRequest& be : g.bsdf_evals)
+            if (in_layer(be.closure)) return true;
+        for (const BsdfSampleRequest& bs : g.bsdf_samples)
+            if (in_layer(bs.closure)) return true;
+        for (const std::string& ro : g.renderer_outputs)
+            if (g.layers[li].master->find_symbol(ro) >= 0) return true;
+        return false;
+    }
+    bool prepare_messages() {
+        std::set<std::string> sent;
+        std::vector<int> used(g.layers.size(), -1);
+        for (LOp& op : lops) {
+            if (op.name == "setmessage" && op.layer >= 0) {
+                if (used[op.layer] < 0) used[op.layer] = layer_used(op.layer) ? 1 : 0;
+                if (!used[op.layer]) {
+                    op.name = "nop";
+                    op.args.clear();
+                    continue;
+                }
+            }
+            if (op.name == "setmessage") {
+                if (op.args.size() != 2) return fail("setmessage takes a name and a value");
+                if (!is_string(op.args[0]) || !syms[op.args[0]].is_const)
+                    return fail("setmessage: the message name must be a constant string");
+                const std::string nm = const_string(op.args[0]);
+                if (!msg_state.count(nm)) {
+                    GSym st; st.name = "$msgstate." + nm; st.type.base = BT_INT; st.kind = SK_LOCAL;
+                    msg_state[nm] = add_sym(st);
+                }
+                const TypeSpec t = syms[op.args[1]].type;
+                op.imm[0] = msg_tid(t);
+                op.args = { op.args[0], op.args[1], msg_state[nm], msg_store_for(nm, t) };
+                op.argrw.clear();
+                sent.insert(nm);
+            } else if (op.name == "getmessage") {
+                const size_t na = op.args.size();
+                if (na != 3 && na != 4) return fail("getmessage takes ([source,] name, value)");
+                const int nsym = op.args[na - 2];
+                if (!is_string(nsym) || !syms[nsym].is_const)
+                    return fail("getmessage: the message name must be a constant string");
+                const std::string nm = const_string(nsym);
+                if (na == 4 || !sent.count(nm)) {
+                    int z = const_int(0);
+                    op.name = "assign";
+                    op.args = { op.args[0], z };
+                    op.argrw = "wr";
+                    continue;
+                }
+                const TypeSpec t = syms[op.args[2]].type;
+                op.imm[0] = msg_tid(t);
+                op.args = { op.args[0], nsym, op.args[2], msg_state[nm], msg_store_for(nm, t) };
+                op.argrw.clear();
+            }
+        }
+        return true;
+    }
+
     // ---- dead-op elimination ----------------------------------------------------
     static bool has_effect(const LOp& op) {
         static const std::set<std::string> effects = {
             "if", "for", "while", "dowhile", "break", "continue", "return", "exit", "__layer_end",
             "__store_output", "__bsdf_eval", "__bsdf_sample", "printf", "warning", "error", "fprintf",
-            "functioncall", "functioncall_nr", "useparam" };
+            "functioncall", "functioncall_nr", "useparam", "setmessage", "getmessage" };
         return effects.count(op.name) != 0;
     }
     // ops that update part of their result keep its other components: the
@@ -605,8 +712,11 @@ struct Lowerer {
                 }
             }
         }
-        // globals are loaded before op 0; keep them live from the start
+        // globals are loaded and message states cleared before op 0; keep
+        // them live from the start
         for (auto& kv : globals)
+            if (syms[kv.second].referenced) first[kv.second] = -1;
+        for (auto& kv : msg_state)
             if (syms[kv.second].referenced) first[kv.second] = -1;
         std::vector<int> order;
         for (size_t si = 0; si < syms.size(); ++si) {
@@ -744,6 +854,13 @@ struct Lowerer {
                 return fail("shader global '" + s.name + "' is not supported");
             }
             emit(OP_LOAD_GLOBAL, { A(kv.second), (uint32_t)s.global_id }, "global");
+        }
+        // every message starts unset
+        for (auto& kv : msg_state) {
+            if (!syms[kv.second].referenced) continue;
+            int z = const_int(0);
+            syms[z].slot = (int)pool_add(syms[z]);
+            emit(OP_ASSIGN, { A(kv.second), A(z), 1u, 1u, 1u }, "message");
         }
         // the body of each layer is a structured range of lops
         return emit_range(0, (int)lops.size(), 0, 0);
@@ -1013,6 +1130,92 @@ struct Lowerer {
         return true;
     }
 
+    // getattribute ([object,] name, [index,] dest) (osl_get_attribute,
+    // src/liboslexec/opattribute.cpp; folding as constfold_getattribute,
+    // src/liboslexec/constfold.cpp:2262-2360). The group's own names
+    // (osl:version, shader:shadername, shader:layername, shader:groupname)
+    // and the renderer's registered uniform attributes (the answers a
+    // BatchedRendererServices gives for uniform attributes,
+    // batched_rendererservices.h:118-170) become constants: `dest = value;
+    // result = 1`. A name nobody answers for gives `result = 0` and leaves
+    // dest unchanged, as the renderer's `false` does.
+    int const_words(const TypeSpec& t, const std::vector<uint32_t>& w) {
+        GSym d; d.name = "$attr"; d.type = t; d.kind = SK_CONST; d.is_const = true;
+        int k = add_sym(d);
+        syms[k].slot = (int)pool.size();
+        pool.insert(pool.end(), w.begin(), w.end());
+        return k;
+    }
+    bool lower_getattribute(const LOp& op) {
+        const size_t na = op.args.size();
+        if (na < 3 || na > 5) return fail("getattribute takes ([object,] name, [index,] value)");
+        const bool array_lookup = na >= 4 && is_int(op.args[na - 2]);
+        const bool object_lookup = na >= 4 && is_string(op.args[2]);
+        const int name_sym = op.args[object_lookup ? 2 : 1];
+        const int dest = op.args[na - 1];
+        auto constant = [&](int s) { return syms[s].is_const; };
+        if (!constant(name_sym) || (object_lookup && !constant(op.args[1]))
+            || (array_lookup && !constant(op.args[na - 2])))
+            return fail("getattribute: attribute names, object names and indices must be constants "
+                        "(per-point attribute lookups are not supported)");
+        const std::string attr = const_string(name_sym);
+        const std::string object = object_lookup ? const_string(op.args[1]) : std::string();
+        const TypeSpec& dt = syms[dest].type;
+        std::vector<uint32_t> words;
+        bool found = false;
+        auto one_string = [&](const std::string& v) {
+            if (dt.base == BT_STRING && !dt.is_array() && !array_lookup) {
+                words = { string_hash(v) };
+                found = true;
+            }
+        };
+        const int li = op.layer >= 0 ? op.layer : 0;
+        if (object.empty() && attr == "osl:version") {
+            if (dt.base == BT_INT && !dt.is_array() && !array_lookup) {
+                words = { (uint32_t)kOslVersionCode };
+                found = true;
+            }
+        } else if (object.empty() && attr == "shader:shadername") {
+            one_string(g.layers[li].master->name);
+        } else if (object.empty() && attr == "shader:layername") {
+            one_string(g.layers[li].layername);
+        } else if (object.empty() && attr == "shader:groupname") {
+            one_string(g.name);
+        } else {
+            auto it = ss.attributes.find({ object, attr });
+            if (it != ss.attributes.end()) {
+                const RendererAttribute& ra = it->second;
+                std::vector<uint32_t> rw = ra.words;
+                if (ra.type.base == BT_STRING) {
+                    rw.clear();
+                    for (const std::string& x : ra.strings) rw.push_back(string_hash(x));
+                }
+                const bool same_elem = ra.type.base == dt.base;
+                const size_t per = (size_t)ra.type.ncomp();
+                if (array_lookup) {
+                    const int idx = (int)syms[op.args[na - 2]].cval.at(0);
+                    if (same_elem && ra.type.is_array() && !dt.is_array() && idx >= 0 && idx < ra.type.elems()
+                        && rw.size() >= (size_t)(idx + 1) * per) {
+                        words.assign(rw.begin() + (size_t)idx * per, rw.begin() + (size_t)(idx + 1) * per);
+                        found = true;
+                    }
+                } else if (same_elem && ra.type.arraylen == dt.arraylen) {
+                    words = rw;
+                    found = true;
+                }
+            }
+        }
+        if (found) {
+            const int c = const_words(dt, words);
+            const uint32_t e = (uint32_t)dt.elems();
+            emit(OP_ASSIGN, { A(dest), A(c), e, e, e }, "getattribute");
+        }
+        const int r = const_int(found ? 1 : 0);
+        syms[r].slot = (int)pool_add(syms[r]);
+        emit(OP_ASSIGN, { A(op.args[0]), A(r), 1u, 1u, 1u }, "getattribute");
+        return true;
+    }
+
     bool lower_op(const LOp& op, int depth, int loopl) {
         const std::string& n = op.name;
         auto a = [&](int i) { return A(op.args[i]); };
@@ -1245,6 +1448,23 @@ struct Lowerer {
             return true;
         }
         if (n == "texture") return lower_texture(op);
+        if (n == "getattribute") return lower_getattribute(op);
+        if (n == "setmessage") {
+            const TypeSpec& t = syms[op.args[1]].type;
+            const uint32_t nw = (uint32_t)(t.ncomp() * t.elems());
+            if (nw > 0xFFFFu || op.imm[0] > 0x7FFF) return fail("setmessage: value too large");
+            emit(OP_SETMESSAGE, { a(2), a(3), a(1), nw | ((uint32_t)op.imm[0] << 16) }, n);
+            return true;
+        }
+        if (n == "getmessage") {
+            const TypeSpec& t = syms[op.args[2]].type;
+            const uint32_t nw = (uint32_t)(t.ncomp() * t.elems());
+            if (nw > 0xFFFFu || op.imm[0] > 0x7FFF) return fail("getmessage: value too large");
+            emit(OP_GETMESSAGE, { a(0), a(3), a(4), a(2),
+                                  nw | ((uint32_t)op.imm[0] << 16) | (ss.opts.strict_messages ? 0x80000000u : 0u) },
+                 n);
+            return true;
+        }
         if (n == "luminance") {
             int sc = const_triple(luminance_scale());
             emit(OP_LUMINANCE, { a(0), a(1), A(sc) }, n);
@@ -1291,7 +1511,7 @@ struct Lowerer {
             case OP_SMOOTHSTEP: case OP_SELECT: case OP_DOT: case OP_CROSS: case OP_LENGTH: case OP_DISTANCE:
             case OP_NORMALIZE: case OP_TRANSFORM: case OP_MMUL: case OP_AREF: case OP_AASSIGN:
             case OP_MDIV: case OP_TRANSPOSE: case OP_DETERMINANT: case OP_AREA: case OP_FILTERWIDTH:
-            case OP_LUMINANCE: case OP_BLACKBODY: case OP_TEXTURE:
+            case OP_LUMINANCE: case OP_BLACKBODY: case OP_TEXTURE: case OP_SETMESSAGE: case OP_GETMESSAGE:
                 t |= 4u;
                 break;
             default: break;
@@ -1303,6 +1523,7 @@ struct Lowerer {
     bool run(CompiledGroup& out) {
         if (g.layers.empty()) return fail("group has no layers");
         if (!build_lops()) return false;
+        if (!prepare_messages()) return false;
         eliminate_dead_ops();
         analyze();
         assign_storage();

@@ -20,7 +20,7 @@
 namespace oslg {
 
 static const uint32_t kProgramMagic = 0x4f534c47u;  // "OSLG"
-static const uint32_t kProgramVersion = 4;
+static const uint32_t kProgramVersion = 5;
 
 // ---- operand words ----------------------------------------------------------
 // bits 0..19  slot offset (heap) or index (constant pool)
@@ -127,6 +127,9 @@ enum OpCode : uint16_t {
                      // global) a4=hash("ggx") a5=userdata byte offset a6=userdata stride
     OP_TEXTURE,      // a0=r (float or triple) a1=s a2=t (Dual2: the footprint) a3=texture
                      // index | swrap << 8 | twrap << 12 | firstchannel << 16 a4=width
+    OP_SETMESSAGE,   // a0=state (int) a1=store a2=value a3=words | type id << 16
+    OP_GETMESSAGE,   // a0=r (int) a1=state a2=store a3=dest a4=words | type id << 16
+                     // | strict << 31
     OP_COUNT
 };
 
@@ -224,6 +227,11 @@ enum StatusBits : uint32_t {
     ST_BAD_OPCODE = 2u,
     ST_ARRAY_BOUNDS = 4u,
     ST_TIMEOUT = 8u,
+    ST_MESSAGE = 16u,  // message set twice, set after a failed query, or read as another type
 };
+
+// Per-point message state word (OP_SETMESSAGE / OP_GETMESSAGE): 0 never
+// set, 1 + type id once set, kMsgQueried after a query that found nothing.
+static const uint32_t kMsgQueried = 0xFFFFFFFFu;
 
 }  // namespace oslg

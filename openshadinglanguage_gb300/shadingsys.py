@@ -142,19 +142,30 @@ class ShadingSystem:
         self._check(C.lib().oslg_shader_group_begin(self._h, groupname.encode(), ctypes.byref(g)))
         return ShaderGroup(self, g, groupname)
 
-    def Parameter(self, group, name, type_, value, lockgeom=True):
+    def renderer_attribute(self, name, type_, value, object=""):
+        """RendererServices::get_attribute for a uniform attribute
+        (oslg_renderer_attribute): getattribute([object,] name, ...) in a
+        shader answers with `value` (a scalar, or a flat list for arrays and
+        triples). Register before the groups that read it are optimized."""
+        ptr, arr = self._values(type_, value)
+        self._keep.append(arr)
+        self._check(C.lib().oslg_renderer_attribute(self._h, object.encode(), name.encode(), type_.c(), ptr))
+
+    @staticmethod
+    def _values(type_, value):
         if type_.basetype == C.BASE_STRING:
             vals = value if isinstance(value, (list, tuple)) else [value]
             arr = (ctypes.c_char_p * len(vals))(*[v.encode() for v in vals])
-            ptr = ctypes.cast(arr, ctypes.c_void_p)
         elif type_.basetype == C.BASE_INT32:
             vals = value if isinstance(value, (list, tuple)) else [value]
             arr = (ctypes.c_int * len(vals))(*[int(v) for v in vals])
-            ptr = ctypes.cast(arr, ctypes.c_void_p)
         else:
             vals = value if isinstance(value, (list, tuple)) else [value] * type_.nfloats
             arr = (ctypes.c_float * len(vals))(*[float(v) for v in vals])
-            ptr = ctypes.cast(arr, ctypes.c_void_p)
+        return ctypes.cast(arr, ctypes.c_void_p), arr
+
+    def Parameter(self, group, name, type_, value, lockgeom=True):
+        ptr, arr = self._values(type_, value)
         self._keep.append(arr)
         self._check(C.lib().oslg_parameter(self._h, group.handle, name.encode(), type_.c(), ptr,
                                            1 if lockgeom else 0))

@@ -682,6 +682,41 @@ void op_texture(Point& P, const uint32_t* a) {
     for (int c = 0; c < nc; ++c) putd(P, r, c, DF(res[c]));
 }
 
+// setmessage / getmessage (src/liboslexec/opmessage.cpp:19-138): per point
+// and message name a state word (0 unset, 1 + type id once set, kMsgQueried
+// after a strict query that found nothing) and a store per type. Double
+// sets, sets after a failed strict query and reads as another type are
+// errors: status bit, values unchanged.
+void op_setmessage(Point& P, const uint32_t* a) {
+    const int nw = (int)(a[3] & 0xFFFFu);
+    if (word(P, a[0], 0) != 0u) {
+        P.status |= oslg::ST_MESSAGE;
+        return;
+    }
+    setw(P, a[0], 0, 1u + (a[3] >> 16));
+    for (int i = 0; i < nw; ++i) setw(P, a[1], i, word(P, a[2], i));
+}
+void op_getmessage(Point& P, const uint32_t* a) {
+    const int nw = (int)(a[4] & 0xFFFFu);
+    const uint32_t tid = (a[4] >> 16) & 0x7FFFu;
+    const bool strict = (a[4] >> 31) != 0u;
+    const uint32_t s = word(P, a[1], 0);
+    uint32_t found = 0u;
+    if (s == 0u) {
+        if (strict) setw(P, a[1], 0, oslg::kMsgQueried);
+    } else if (s == oslg::kMsgQueried) {
+        // queried before and not found: still not found
+    } else if (s != 1u + tid) {
+        P.status |= oslg::ST_MESSAGE;
+    } else {
+        for (int i = 0; i < nw; ++i) setw(P, a[3], i, word(P, a[2], i));
+        if (ader(a[3]))
+            for (int i = nw; i < 3 * nw; ++i) setw(P, a[3], i, 0u);
+        found = 1u;
+    }
+    setw(P, a[0], 0, found);
+}
+
 // blackbody (src/liboslexec/opcolor_impl.h:510-575, opcolor.cpp:438-442):
 // a2 = constant table (N entries of RGB^(1/5), XYZ->RGB matrix, CIE table)
 void op_blackbody(Point& P, const uint32_t* a) {
@@ -1243,6 +1278,8 @@ struct Runner {
             case oslg::OP_LUMINANCE: op_luminance(P, a); break;
             case oslg::OP_BLACKBODY: op_blackbody(P, a); break;
             case oslg::OP_TEXTURE: op_texture(P, a); break;
+            case oslg::OP_SETMESSAGE: op_setmessage(P, a); break;
+            case oslg::OP_GETMESSAGE: op_getmessage(P, a); break;
             case oslg::OP_NOISE: op_noise(P, a); break;
             case oslg::OP_GABOR: op_gabor(P, a, prog.ops[pc + 1].a); break;
             case oslg::OP_HASH: op_hash(P, a); break;

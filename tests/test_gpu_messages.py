@@ -1,0 +1,80 @@
+"""Messages between layers and folded getattribute on the GPU, interpreter
+and specialized kernel: outputs bit-exact to the oracle and the same
+message-error status."""
+import numpy as np
+import pytest
+
+from helpers import grid_globals, og, oracle_run, pixel_grid
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from test_gpu_parity import assert_same, device_grid_globals, gpu_run  # noqa: E402
+from test_messages_attributes import attribute_group, check_attributes, message_group  # noqa: E402
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _cuda():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    torch.cuda.init()
+
+
+CASES = {
+    "pass": dict(),
+    "derivs": dict(derivs=True),
+    "mismatch": dict(recv_kw=dict(col_type="point")),
+    "double": dict(send_kw=dict(double_set=True)),
+    "unconnected": dict(connect=False),
+}
+
+
+def both(ss, g, nfloats, W=67, H=29):
+    u, v = pixel_grid(W, H, centers=True)
+    n = W * H
+    got = gpu_run(ss, g, n, device_grid_globals(u, v, W, H, centers=True), nfloats, sync=False)
+    ref = np.zeros((n, nfloats), np.float32)
+    st = oracle_run(g.program_bytes(), n, grid_globals(u, v, W, H, centers=True), ref)
+    return got, ref, st
+
+
+@pytest.mark.parametrize("jit", [0, 1])
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_messages_match_oracle(case, jit):
+    ss = og.ShadingSystem()
+    if jit:
+        ss.attribute("jit", 1)
+    g, stride = message_group(ss, "g%s%d" % (case, jit), **CASES[case])
+    got, ref, st = both(ss, g, stride // 4)
+    assert_same(got, ref)
+    assert ss.device_status() == st
+    if jit:
+        assert g.is_specialized()
+
+
+@pytest.mark.parametrize("jit", [0, 1])
+@pytest.mark.parametrize("strict", [1, 0])
+def test_strict_messages_match_oracle(strict, jit):
+    ss = og.ShadingSystem()
+    ss.attribute("strict_messages", strict)
+    if jit:
+        ss.attribute("jit", 1)
+    extra = [("r1", og.TypeInt, 28, 4), ("r2", og.TypeInt, 32, 4), ("y", og.TypeFloat, 36, 4)]
+    g, stride = message_group(ss, "st%d%d" % (strict, jit), send_kw=dict(guarded_m=True),
+                              recv_kw=dict(strict_probe=True), extra=extra)
+    got, ref, st = both(ss, g, stride // 4)
+    assert_same(got, ref)
+    assert ss.device_status() == st
+    assert (st != 0) == bool(strict)
+
+
+@pytest.mark.parametrize("jit", [0, 1])
+def test_getattribute_matches_oracle(jit):
+    ss = og.ShadingSystem()
+    if jit:
+        ss.attribute("jit", 1)
+    g = attribute_group(ss, "j%d" % jit)
+    got, ref, st = both(ss, g, 17, W=33, H=5)
+    assert st == 0 and ss.device_status() == 0
+    assert_same(got, ref)
+    check_attributes(got)
