@@ -183,6 +183,8 @@ struct RendererAttribute {
 struct SystemOptions {
     int debug = 0;
     int strict_messages = 1;  // ShadingSystem attribute "strict_messages" (shadingsys.cpp:1078)
+    int opt_constant_fold = 1;       // "opt_constant_fold" (shadingsys.cpp:1641)
+    int opt_elide_useless_ops = 1;   // "opt_elide_useless_ops" (shadingsys.cpp:1643)
     int max_closure_components = 16;  // closure tree nodes per point
     int max_closure_terms = 16;
     int heap_in_smem = -1;  // -1 auto

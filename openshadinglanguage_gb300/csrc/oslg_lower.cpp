@@ -598,6 +598,227 @@ struct Lowerer {
         return true;
     }
 
+    // ---- constant folding ------------------------------------------------------
+    // Forward propagation of known values through straight-line code, as
+    // the RuntimeOptimizer's constant folding and block aliases do
+    // (src/liboslexec/runtimeoptimize.cpp, constfold.cpp): a symbol whose
+    // last write gave it a constant value is read as that constant, and an
+    // op whose inputs are all constants becomes an assignment of its
+    // result. Knowledge survives an `if` only for symbols neither branch
+    // writes; inside a loop nothing the loop writes is known. Folded
+    // arithmetic is IEEE single precision without contraction, as the
+    // kernels compute it; results that would be NaN or out of int range
+    // are left to run.
+    struct CVal {
+        uint32_t tc = TC_FLOAT;
+        int n = 1;
+        uint32_t w[3] = { 0, 0, 0 };
+        float f(int c) const {
+            uint32_t x = w[n == 1 ? 0 : c];
+            if (tc == TC_INT) return (float)(int32_t)x;
+            float v;
+            std::memcpy(&v, &x, 4);
+            return v;
+        }
+        bool truth() const {
+            if (tc == TC_INT) return w[0] != 0u;
+            for (int c = 0; c < n; ++c)
+                if (f(c) != 0.0f) return true;
+            return false;
+        }
+    };
+    static uint32_t fbits(float v) { uint32_t w; std::memcpy(&w, &v, 4); return w; }
+    bool cval_of(int s, CVal& v) const {
+        const GSym& g = syms[s];
+        if (!g.is_const || g.type.is_array()) return false;
+        if (g.type.base != BT_FLOAT && g.type.base != BT_INT && g.type.base != BT_TRIPLE) return false;
+        v.n = g.type.base == BT_TRIPLE ? 3 : 1;
+        v.tc = g.type.tclass();
+        for (int c = 0; c < v.n; ++c) {
+            if (g.slot >= 0) {  // a folded value: its pool words
+                v.w[c] = pool[(size_t)g.slot + c];
+                continue;
+            }
+            float x = g.cval.empty() ? 0.0f : g.cval[std::min<size_t>(c, g.cval.size() - 1)];
+            v.w[c] = v.tc == TC_INT ? (uint32_t)(int32_t)x : fbits(x);
+        }
+        return true;
+    }
+    // the value op would compute from its (constant) operands
+    bool fold_eval(const LOp& op, std::vector<uint32_t>& out) const {
+        const std::string& n = op.name;
+        const size_t na = op.args.size();
+        if (na < 2) return false;
+        const TypeSpec& rt = syms[op.args[0]].type;
+        if (rt.is_array() || (rt.base != BT_FLOAT && rt.base != BT_INT && rt.base != BT_TRIPLE)) return false;
+        const int nr = rt.base == BT_TRIPLE ? 3 : 1;
+        const bool rint = rt.base == BT_INT;
+        out.assign((size_t)nr, 0u);
+        auto put = [&](int c, float v) {
+            if (v != v) return false;
+            if (rint) {
+                if (!(v > -2147483648.0f && v < 2147483648.0f)) return false;
+                out[(size_t)c] = (uint32_t)(int32_t)v;
+            } else {
+                out[(size_t)c] = fbits(v);
+            }
+            return true;
+        };
+        CVal x, y, z;
+        const bool ctor = n == "color" || n == "point" || n == "vector" || n == "normal";
+        if (n == "assign" || (ctor && na == 2)) {
+            if (!cval_of(op.args[1], x) || (x.n == 3 && nr == 1)) return false;
+            for (int c = 0; c < nr; ++c) {
+                if (!rint && x.tc != TC_INT) out[(size_t)c] = x.w[x.n == 1 ? 0 : c];
+                else if (rint && x.tc == TC_INT) out[(size_t)c] = x.w[0];
+                else if (!put(c, x.f(c))) return false;
+            }
+            return true;
+        }
+        if (ctor && na == 4) {
+            for (int c = 0; c < 3; ++c)
+                if (!cval_of(op.args[1 + c], x) || x.n != 1 || !put(c, x.f(0))) return false;
+            return nr == 3;
+        }
+        if (n == "neg") {
+            if (!cval_of(op.args[1], x)) return false;
+            if (rint) {
+                if (x.tc != TC_INT) return false;
+                out[0] = 0u - x.w[0];
+                return true;
+            }
+            if (x.n == 3 && nr == 1) return false;
+            for (int c = 0; c < nr; ++c)
+                if (!put(c, -x.f(c))) return false;
+            return true;
+        }
+        if (n == "compref") {
+            if (!cval_of(op.args[1], x) || !cval_of(op.args[2], y) || x.n != 3 || y.tc != TC_INT || rint) return false;
+            const int i = (int)(int32_t)y.w[0];
+            if (i < 0 || i > 2) return false;
+            out[0] = x.w[i];
+            return nr == 1;
+        }
+        if (na < 3 || !cval_of(op.args[1], x) || !cval_of(op.args[2], y)) return false;
+        static const std::map<std::string, int> cmp = { { "eq", 0 }, { "neq", 1 }, { "lt", 2 },
+                                                        { "gt", 3 }, { "le", 4 }, { "ge", 5 } };
+        auto ci = cmp.find(n);
+        if (ci != cmp.end()) {
+            if (!rint) return false;
+            const int K = ci->second;
+            bool res;
+            if (x.tc == TC_INT && y.tc == TC_INT) {
+                const int32_t a = (int32_t)x.w[0], b = (int32_t)y.w[0];
+                res = K == 0 ? a == b : K == 1 ? a != b : K == 2 ? a < b : K == 3 ? a > b : K == 4 ? a <= b : a >= b;
+            } else if (K <= 1) {
+                bool eq = true;
+                for (int c = 0; c < std::max(x.n, y.n); ++c) eq = eq && x.f(c) == y.f(c);
+                res = K == 0 ? eq : !eq;
+            } else {
+                const float a = x.f(0), b = y.f(0);
+                res = K == 2 ? a < b : K == 3 ? a > b : K == 4 ? a <= b : a >= b;
+            }
+            out[0] = res ? 1u : 0u;
+            return true;
+        }
+        if (n == "and" || n == "or") {
+            if (!rint) return false;
+            out[0] = (n == "and" ? (x.truth() && y.truth()) : (x.truth() || y.truth())) ? 1u : 0u;
+            return true;
+        }
+        const int K = n == "add" ? 0 : n == "sub" ? 1 : n == "mul" ? 2 : n == "div" ? 3 : -1;
+        if (K < 0) return false;
+        if (rint && x.tc == TC_INT && y.tc == TC_INT) {
+            const int32_t a = (int32_t)x.w[0], b = (int32_t)y.w[0];
+            if (K == 0) out[0] = (uint32_t)a + (uint32_t)b;
+            else if (K == 1) out[0] = (uint32_t)a - (uint32_t)b;
+            else if (K == 2) out[0] = (uint32_t)a * (uint32_t)b;
+            else out[0] = (b == 0 || (a == INT32_MIN && b == -1)) ? 0u : (uint32_t)(a / b);
+            return true;
+        }
+        if ((x.n == 3 || y.n == 3) && nr == 1) return false;
+        for (int c = 0; c < nr; ++c) {
+            const float a = x.f(c), b = y.f(c);
+            float v;
+            if (K == 0) v = a + b;
+            else if (K == 1) v = a - b;
+            else if (K == 2) v = a * b;
+            else v = b == 0.0f ? 0.0f : a / b;
+            if (!put(c, v)) return false;
+        }
+        return true;
+    }
+    void written_in(int b, int e, std::set<int>& w) const {
+        for (int k = b; k < e; ++k)
+            for (size_t i = 0; i < lops[k].args.size(); ++i)
+                if (writes_arg(lops[k], (int)i)) w.insert(lops[k].args[i]);
+    }
+    int folded_ops = 0;
+    void fold_op(LOp& op, std::map<int, int>& K, const std::set<int>& blocked) {
+        static const std::set<std::string> control = { "if", "for", "while", "dowhile", "break", "continue",
+                                                       "return", "exit", "nop", "useparam", "functioncall",
+                                                       "functioncall_nr" };
+        if (control.count(op.name) || op.args.empty()) return;
+        if (op.param_init) {  // a parameter's uniform value
+            if (blocked.count(op.param_gsym)) K.erase(op.param_gsym);
+            else K[op.param_gsym] = op.args[1];
+            return;
+        }
+        for (size_t i = 0; i < op.args.size(); ++i) {
+            if (writes_arg(op, (int)i) || partial_write(op)) continue;
+            auto it = K.find(op.args[i]);
+            if (it != K.end()) op.args[i] = it->second;
+        }
+        std::vector<uint32_t> w;
+        if (fold_eval(op, w)) {
+            const int r = op.args[0];
+            const int c = const_words(syms[r].type, w);
+            if (op.name != "assign" || op.args[1] != c) ++folded_ops;
+            op.name = "assign";
+            op.args = { r, c };
+            op.argrw = "wr";
+            if (blocked.count(r)) K.erase(r);
+            else K[r] = c;
+            return;
+        }
+        for (size_t i = 0; i < op.args.size(); ++i)
+            if (writes_arg(op, (int)i)) K.erase(op.args[i]);
+    }
+    void fold_range(int b, int e, std::map<int, int>& K, const std::set<int>& blocked) {
+        for (int k = b; k < e;) {
+            LOp& op = lops[k];
+            if (op.name == "if" && op.jumps.size() >= 2) {
+                const int je = op.jumps[0], jend = op.jumps[1];
+                std::map<int, int> K1 = K, K2 = K;
+                fold_range(k + 1, je, K1, blocked);
+                fold_range(je, jend, K2, blocked);
+                std::set<int> w;
+                written_in(k + 1, jend, w);
+                for (int s : w) K.erase(s);
+                k = jend;
+                continue;
+            }
+            if ((op.name == "for" || op.name == "while" || op.name == "dowhile") && op.jumps.size() >= 4) {
+                const int jend = op.jumps[3];
+                std::set<int> w;
+                written_in(k + 1, jend, w);
+                for (int s : w) K.erase(s);
+                std::set<int> bl = blocked;
+                bl.insert(w.begin(), w.end());
+                std::map<int, int> K1 = K;
+                fold_range(k + 1, jend, K1, bl);
+                k = jend;
+                continue;
+            }
+            fold_op(op, K, blocked);
+            ++k;
+        }
+    }
+    void fold_constants() {
+        std::map<int, int> K;
+        fold_range(0, (int)lops.size(), K, std::set<int>());
+    }
+
     // ---- dead-op elimination ----------------------------------------------------
     static bool has_effect(const LOp& op) {
         static const std::set<std::string> effects = {
@@ -723,7 +944,7 @@ struct Lowerer {
             GSym& s = syms[si];
             if (!s.referenced) continue;
             if (s.is_const) {
-                s.slot = (int)pool_add(s);
+                if (s.slot < 0) s.slot = (int)pool_add(s);  // folded values already sit in the pool
                 continue;
             }
             order.push_back((int)si);
@@ -1524,7 +1745,8 @@ struct Lowerer {
         if (g.layers.empty()) return fail("group has no layers");
         if (!build_lops()) return false;
         if (!prepare_messages()) return false;
-        eliminate_dead_ops();
+        if (ss.opts.opt_constant_fold) fold_constants();
+        if (ss.opts.opt_elide_useless_ops) eliminate_dead_ops();
         analyze();
         assign_storage();
         if (!lower_all()) return false;
