@@ -222,6 +222,14 @@ int oslg_texture_create(oslg_system* sys, const char* name, int width, int heigh
  * getattribute return 0 and leave its destination unchanged. */
 int oslg_renderer_attribute(oslg_system* sys, const char* object, const char* name, oslg_typedesc type,
                             const void* data);
+/* The matrix from the named coordinate system to "common" (16 floats, row
+ * major, points as row vectors like Imath): the renderer side of
+ * RendererServices::get_matrix / get_inverse_matrix by name
+ * (src/include/OSL/rendererservices.h:96-145), and of the object and
+ * shader transforms when name is "object" or "shader". transform(),
+ * matrix(), getmatrix() with constant space names fold these (and inverses)
+ * into constant matrices when a group is lowered. */
+int oslg_renderer_matrix(oslg_system* sys, const char* name, const float* matrix16);
 /* ShaderGroupRef release */
 int oslg_release_group(oslg_system* sys, oslg_group* group);
 

@@ -567,6 +567,16 @@ int oslg_renderer_attribute(oslg_system* sys, const char* object, const char* na
     });
 }
 
+int oslg_renderer_matrix(oslg_system* sys, const char* name, const float* matrix16) {
+    if (!sys || !name || !matrix16) return OSLG_ERR_ARG;
+    return guarded(sys, [&]() {
+        std::array<float, 16> m;
+        std::memcpy(m.data(), matrix16, sizeof(m));
+        sys->ss.named_matrices[name] = m;
+        return OSLG_OK;
+    });
+}
+
 // Upload new or replaced texture pyramids and the descriptor table.
 static int upload_textures(oslg_system* sys) {
     if (!sys->textures_dirty) return OSLG_OK;

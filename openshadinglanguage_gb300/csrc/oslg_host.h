@@ -9,6 +9,7 @@
 // src/liboslexec/osogram.y and testsuite/*/test.oso).
 #pragma once
 #include <cstdint>
+#include <array>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -198,6 +199,7 @@ public:
     std::map<std::string, int> closure_ids;  // registered closure name -> id
     std::map<std::string, int> texture_ids;  // registered texture name -> index
     std::map<std::pair<std::string, std::string>, RendererAttribute> attributes;  // (object, name)
+    std::map<std::string, std::array<float, 16>> named_matrices;  // space -> space-to-common matrix
     SystemOptions opts;
     std::string last_error;
     std::mutex mutex;

@@ -415,6 +415,7 @@ struct Lowerer {
         if (op.name == "setmessage") return i == 2 || i == 3;
         if (op.name == "getmessage") return i == 0 || i == 2 || i == 3;
         if (op.name == "getattribute") return i == 0 || i == (int)op.args.size() - 1;
+        if (op.name == "getmatrix") return i == 0 || i == 3;
         if (!op.argrw.empty() && i < (int)op.argrw.size())
             return op.argrw[i] == 'w' || op.argrw[i] == 'W';
         static const std::set<std::string> nowrite = {
@@ -1084,7 +1085,30 @@ struct Lowerer {
             emit(OP_ASSIGN, { A(kv.second), A(z), 1u, 1u, 1u }, "message");
         }
         // the body of each layer is a structured range of lops
-        return emit_range(0, (int)lops.size(), 0, 0);
+        if (!emit_range(0, (int)lops.size(), 0, 0)) return false;
+        return check_destinations();
+    }
+
+    // Every op that writes its first operand must write a heap slot: a
+    // constant there would mean a write into the constant pool's offsets.
+    bool check_destinations() {
+        for (size_t k = 0; k < ops.size(); ++k) {
+            const Op& o = ops[k];
+            switch (o.code) {
+            case OP_NOP: case OP_IF: case OP_ELSE: case OP_ENDIF: case OP_LOOP_BEGIN: case OP_LOOP_TEST:
+            case OP_LOOP_STEP: case OP_LOOP_END: case OP_JUMP: case OP_BREAK: case OP_CONTINUE: case OP_RETURN:
+            case OP_EXIT: case OP_LAYER_END: case OP_STORE_OUTPUT: case OP_STORE_CLOSURE: case OP_BSDF_EVAL:
+            case OP_BSDF_SAMPLE:
+                continue;
+            default:
+                break;
+            }
+            bool bad = (o.a[0] & kArgConst) != 0;
+            if (o.code == OP_SETMESSAGE) bad = bad || (o.a[1] & kArgConst) != 0;
+            if (o.code == OP_GETMESSAGE) bad = bad || (o.a[3] & kArgConst) != 0;
+            if (bad) return fail("internal: op '" + op_names[k] + "' would write a constant");
+        }
+        return true;
     }
 
     int tc(int gs) const { return (int)syms[gs].type.tclass(); }
@@ -1437,6 +1461,109 @@ struct Lowerer {
         return true;
     }
 
+    // ---- named coordinate systems ---------------------------------------------
+    // Spaces resolve at lowering time to the renderer's registered uniform
+    // matrices (oslg_renderer_matrix: RendererServices::get_matrix for named
+    // spaces, and the object/shader to common transforms). "common" and its
+    // synonym "world" are the identity (osl_get_matrix / osl_get_inverse_matrix,
+    // src/liboslexec/opmatrix.cpp:141-196); inverses are taken in double
+    // precision (a singular matrix inverts to the identity, as Imath's
+    // non-throwing inverse does).
+    using M44 = std::array<float, 16>;
+    static M44 m_identity() {
+        M44 m{};
+        for (int i = 0; i < 4; ++i) m[(size_t)i * 5] = 1.0f;
+        return m;
+    }
+    static M44 m_mul(const M44& A, const M44& B) {
+        M44 c{};
+        for (int i = 0; i < 4; ++i)
+            for (int j = 0; j < 4; ++j)
+                c[(size_t)(i * 4 + j)] = A[(size_t)(i * 4 + 0)] * B[(size_t)(0 * 4 + j)]
+                                       + A[(size_t)(i * 4 + 1)] * B[(size_t)(1 * 4 + j)]
+                                       + A[(size_t)(i * 4 + 2)] * B[(size_t)(2 * 4 + j)]
+                                       + A[(size_t)(i * 4 + 3)] * B[(size_t)(3 * 4 + j)];
+        return c;
+    }
+    static M44 m_inverse(const M44& m) {
+        double a[4][8];
+        for (int i = 0; i < 4; ++i)
+            for (int j = 0; j < 8; ++j) a[i][j] = j < 4 ? (double)m[(size_t)(i * 4 + j)] : (j - 4 == i ? 1.0 : 0.0);
+        for (int c = 0; c < 4; ++c) {
+            int piv = c;
+            for (int r = c + 1; r < 4; ++r)
+                if (std::fabs(a[r][c]) > std::fabs(a[piv][c])) piv = r;
+            if (a[piv][c] == 0.0) return m_identity();
+            if (piv != c)
+                for (int j = 0; j < 8; ++j) std::swap(a[c][j], a[piv][j]);
+            const double d = a[c][c];
+            for (int j = 0; j < 8; ++j) a[c][j] /= d;
+            for (int r = 0; r < 4; ++r) {
+                if (r == c || a[r][c] == 0.0) continue;
+                const double f = a[r][c];
+                for (int j = 0; j < 8; ++j) a[r][j] -= f * a[c][j];
+            }
+        }
+        M44 inv{};
+        for (int i = 0; i < 4; ++i)
+            for (int j = 0; j < 4; ++j) inv[(size_t)(i * 4 + j)] = (float)a[i][j + 4];
+        return inv;
+    }
+    static std::string common_name(const std::string& s) { return s == "world" ? std::string("common") : s; }
+    bool space_to_common(const std::string& sp, M44& M) const {
+        if (sp == "common") { M = m_identity(); return true; }
+        auto it = ss.named_matrices.find(sp);
+        if (it == ss.named_matrices.end()) { M = m_identity(); return false; }
+        M = it->second;
+        return true;
+    }
+    // osl_get_from_to_matrix (opmatrix.cpp:231-240): get_matrix(from) *
+    // get_inverse_matrix(to), an unknown space contributing the identity
+    bool named_from_to(const LOp& op, int from_sym, int to_sym, M44& M, bool& ok) {
+        if (!syms[from_sym].is_const || !syms[to_sym].is_const)
+            return fail(op.name + ": space names must be constant strings");
+        const std::string from = common_name(const_string(from_sym)), to = common_name(const_string(to_sym));
+        M44 F, T;
+        ok = space_to_common(from, F);
+        ok = space_to_common(to, T) && ok;
+        M = m_mul(F, to == "common" ? m_identity() : m_inverse(T));
+        return true;
+    }
+    int const_matrix(const M44& M) {
+        TypeSpec t;
+        t.base = BT_MATRIX;
+        std::vector<uint32_t> w(16);
+        for (int i = 0; i < 16; ++i) std::memcpy(&w[(size_t)i], &M[(size_t)i], 4);
+        return const_words(t, w);
+    }
+    // transform{,v,n} ([from,] to, p) (llvm_gen_transform,
+    // src/liboslexec/llvm_gen.cpp:2025-2086; osl_transform_triple,
+    // opmatrix.cpp:244-300): the same space twice copies p; an unknown space
+    // copies p as well (the reference also reports it as an error).
+    bool lower_named_transform(const LOp& op) {
+        const std::string& n = op.name;
+        const size_t na = op.args.size();
+        if (na != 3 && na != 4) return fail(n + " takes ([from,] to, p) or (M, p)");
+        const int p = op.args[na - 1];
+        const int to = op.args[na - 2];
+        if (!is_string(to) || (na == 4 && !is_string(op.args[1]))) return fail(n + ": bad space arguments");
+        if (!syms[to].is_const || (na == 4 && !syms[op.args[1]].is_const))
+            return fail(n + ": space names must be constant strings");
+        const std::string from_s = na == 4 ? common_name(const_string(op.args[1])) : std::string("common");
+        const std::string to_s = common_name(const_string(to));
+        M44 F, T;
+        bool ok = space_to_common(from_s, F);
+        ok = space_to_common(to_s, T) && ok;
+        if (from_s == to_s || !ok) {
+            emit(OP_ASSIGN, { A(op.args[0]), A(p), 1u, 1u, 1u }, n);
+            return true;
+        }
+        const M44 M = from_s == "common" ? m_inverse(T) : to_s == "common" ? F : m_mul(F, m_inverse(T));
+        const uint32_t kind = n == "transform" ? 0u : n == "transformv" ? 1u : 2u;
+        emit(OP_TRANSFORM, { A(op.args[0]), A(p), A(const_matrix(M)), kind }, n);
+        return true;
+    }
+
     bool lower_op(const LOp& op, int depth, int loopl) {
         const std::string& n = op.name;
         auto a = [&](int i) { return A(op.args[i]); };
@@ -1611,6 +1738,37 @@ struct Lowerer {
                 emit(OP_MATRIX_DIAG, { a(0), a(1) }, n);
                 return true;
             }
+            if (na == 3 && is_string(op.args[1]) && is_string(op.args[2])) {  // matrix(from, to)
+                M44 M;
+                bool ok;
+                if (!named_from_to(op, op.args[1], op.args[2], M, ok)) return false;
+                emit(OP_ASSIGN, { a(0), A(const_matrix(M)), 1u, 1u, 1u }, n);
+                return true;
+            }
+            if ((na == 3 || na == 18) && is_string(op.args[1])) {
+                // matrix(space, f) / matrix(space, 16 floats): the values,
+                // then prepended by the space's matrix (osl_prepend_matrix_from,
+                // src/liboslexec/opmatrix.cpp:210-229); an unknown space
+                // leaves the values
+                if (!syms[op.args[1]].is_const) return fail("matrix: the space name must be a constant string");
+                if (na == 3) {
+                    emit(OP_MATRIX_DIAG, { a(0), a(2) }, n);
+                } else {
+                    int zero = const_float(0.0f);
+                    syms[zero].slot = (int)pool_add(syms[zero]);
+                    emit(OP_MATRIX_DIAG, { a(0), A(zero) }, n);
+                    for (int i = 0; i < 16; ++i) {
+                        int ri = const_int(i / 4), ci = const_int(i % 4);
+                        syms[ri].slot = (int)pool_add(syms[ri]);
+                        syms[ci].slot = (int)pool_add(syms[ci]);
+                        emit(OP_MXCOMPASSIGN, { A(r), A(ri), A(ci), a(2 + i) }, n);
+                    }
+                }
+                M44 Mf;
+                if (space_to_common(common_name(const_string(op.args[1])), Mf))
+                    emit(OP_MMUL, { a(0), A(const_matrix(Mf)), a(0) }, n);
+                return true;
+            }
             if (na == 17) {
                 int zero = const_float(0.0f);
                 syms[zero].slot = (int)pool_add(syms[zero]);
@@ -1628,7 +1786,7 @@ struct Lowerer {
         if (n == "transpose") { emit(OP_TRANSPOSE, { a(0), a(1) }, n); return true; }
         if (n == "determinant") { emit(OP_DETERMINANT, { a(0), a(1) }, n); return true; }
         if (n == "transform" || n == "transformv" || n == "transformn") {
-            // transform r M p  (matrix form); named-space forms need the renderer
+            // transform r M p  (matrix form)
             if (na == 3 && is_matrix(op.args[1])) {
                 uint32_t kind = n == "transform" ? 0u : n == "transformv" ? 1u : 2u;
                 if (n == "transform" && syms[op.args[2]].type.vecsem == VS_VECTOR) kind = 1u;
@@ -1636,7 +1794,19 @@ struct Lowerer {
                 emit(OP_TRANSFORM, { a(0), a(2), a(1), kind }, n);
                 return true;
             }
-            return fail("transform between named spaces is not supported yet");
+            return lower_named_transform(op);
+        }
+        if (n == "getmatrix") {
+            if (na != 4) return fail("getmatrix takes (from, to, M)");
+            M44 M;
+            bool ok;
+            if (!named_from_to(op, op.args[1], op.args[2], M, ok)) return false;
+            const int c = const_matrix(M);
+            emit(OP_ASSIGN, { a(3), A(c), 1u, 1u, 1u }, n);
+            const int r = const_int(ok ? 1 : 0);
+            syms[r].slot = (int)pool_add(syms[r]);
+            emit(OP_ASSIGN, { a(0), A(r), 1u, 1u, 1u }, n);
+            return true;
         }
         if (n == "noise" || n == "snoise" || n == "pnoise" || n == "psnoise" || n == "cellnoise"
             || n == "hashnoise")

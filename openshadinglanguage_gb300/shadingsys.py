@@ -151,6 +151,15 @@ class ShadingSystem:
         self._keep.append(arr)
         self._check(C.lib().oslg_renderer_attribute(self._h, object.encode(), name.encode(), type_.c(), ptr))
 
+    def renderer_matrix(self, name, matrix):
+        """RendererServices::get_matrix for a named space
+        (oslg_renderer_matrix): the 4x4 space-to-common matrix, row major,
+        points as row vectors. Register before the groups that use the
+        space are optimized."""
+        import numpy as np
+        m = np.ascontiguousarray(np.asarray(matrix, np.float32).reshape(16))
+        self._check(C.lib().oslg_renderer_matrix(self._h, name.encode(), ctypes.c_void_p(m.ctypes.data)))
+
     @staticmethod
     def _values(type_, value):
         if type_.basetype == C.BASE_STRING:

@@ -1,6 +1,6 @@
-"""Messages between layers and folded getattribute on the GPU, interpreter
-and specialized kernel: outputs bit-exact to the oracle and the same
-message-error status."""
+"""Renderer services on the GPU, interpreter and specialized kernel:
+messages between layers, folded getattribute and named coordinate systems;
+outputs bit-exact to the oracle and the same message-error status."""
 import numpy as np
 import pytest
 
@@ -9,8 +9,9 @@ from helpers import grid_globals, og, oracle_run, pixel_grid
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
-from test_gpu_parity import assert_same, device_grid_globals, gpu_run  # noqa: E402
+from test_gpu_parity import assert_same, dev, device_grid_globals, gpu_run  # noqa: E402
 from test_messages_attributes import attribute_group, check_attributes, message_group  # noqa: E402
+from test_named_spaces import NFLOATS, check, inputs, spaces_group  # noqa: E402
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -78,3 +79,20 @@ def test_getattribute_matches_oracle(jit):
     assert st == 0 and ss.device_status() == 0
     assert_same(got, ref)
     check_attributes(got)
+
+
+@pytest.mark.parametrize("jit", [0, 1])
+def test_named_spaces_match_oracle(jit):
+    ss = og.ShadingSystem()
+    if jit:
+        ss.attribute("jit", 1)
+    g = spaces_group(ss, "j%d" % jit)
+    n = 5000
+    P, N, T = inputs(n)
+    dP, dN, dT = dev(P), dev(N), dev(T)
+    got = gpu_run(ss, g, n, og.make_globals(P=dP, N=dN, dPdu=dT), NFLOATS)
+    ref = np.zeros((n, NFLOATS), np.float32)
+    assert oracle_run(g.program_bytes(), n, og.make_globals(P=P, N=N, dPdu=T), ref) == 0
+    assert_same(got, ref)
+    check(got, P, N, T)
+    assert ss.device_status() == 0
