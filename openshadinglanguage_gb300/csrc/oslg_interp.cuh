@@ -970,6 +970,23 @@ __device__ __forceinline__ void tex_bilinear(const TexDesc& T, int lev, float s,
         out[c] = (1.0f - fy) * top + fy * bot;
     }
 }
+// Mipmapped bilinear lookup: the footprint (level-0 texels along x and y,
+// times width) picks the level of detail; the two nearest levels blend.
+__device__ __forceinline__ void tex_filtered(const TexDesc& T, float s, float t, float dsx, float dtx, float dsy,
+                                             float dty, float width, uint32_t sw, uint32_t tw, int first, int nc,
+                                             float* res) {
+    const float len = fmaxf(sqrtf(dsx * dsx + dtx * dtx), sqrtf(dsy * dsy + dty * dty)) * width;
+    float lod = len > 1.0f ? own_log(len) * 1.44269504f : 0.0f;
+    lod = fminf(lod, (float)(T.nlevels - 1));
+    const int l0 = (int)lod;
+    const float f = lod - (float)l0;
+    tex_bilinear(T, l0, s, t, sw, tw, first, nc, res);
+    if (f > 0.0f && l0 + 1 < T.nlevels) {
+        float hi[3];
+        tex_bilinear(T, l0 + 1, s, t, sw, tw, first, nc, hi);
+        for (int c = 0; c < nc; ++c) res[c] = (1.0f - f) * res[c] + f * hi[c];
+    }
+}
 static __device__ void h_texture(const Lane& L, const uint32_t* a, const TexDesc* tex, int ntex, uint32_t* st) {
     const uint32_t r = a[0];
     const int nc = anc(r) == 3 ? 3 : 1;
@@ -982,18 +999,42 @@ static __device__ void h_texture(const Lane& L, const uint32_t* a, const TexDesc
         const D2 s = ldd(L, a[1], 0), t = ldd(L, a[2], 0);
         const float width = ldf(L, a[4], 0, 0);
         const float w0 = (float)T.w[0], h0 = (float)T.h[0];
-        const float dsx = s.dx * w0, dtx = t.dx * h0, dsy = s.dy * w0, dty = t.dy * h0;
-        const float len = fmaxf(sqrtf(dsx * dsx + dtx * dtx), sqrtf(dsy * dsy + dty * dty)) * width;
-        float lod = len > 1.0f ? own_log(len) * 1.44269504f : 0.0f;
-        lod = fminf(lod, (float)(T.nlevels - 1));
-        const int l0 = (int)lod;
-        const float f = lod - (float)l0;
-        tex_bilinear(T, l0, s.v, t.v, sw, tw, first, nc, res);
-        if (f > 0.0f && l0 + 1 < T.nlevels) {
-            float hi[3];
-            tex_bilinear(T, l0 + 1, s.v, t.v, sw, tw, first, nc, hi);
-            for (int c = 0; c < nc; ++c) res[c] = (1.0f - f) * res[c] + f * hi[c];
-        }
+        tex_filtered(T, s.v, t.v, s.dx * w0, t.dx * h0, s.dy * w0, t.dy * h0, width, sw, tw, first, nc, res);
+    } else {
+        raise_status(st, ST_ARRAY_BOUNDS);
+    }
+    OSLG_SPEC_UNROLL
+    for (int c = 0; c < nc; ++c) std2(L, r, c, d2c(res[c]));
+}
+
+// environment (osl_environment, src/liboslexec/optexture.cpp): a
+// latitude-longitude image looked up by direction, z up:
+// s = atan2(y, x) / 2pi + 0.5 (periodic), t = 0.5 - atan2(z, hypot(x, y)) / pi
+// (clamped). The footprint maps R + dR/dx and R + dR/dy the same way, the
+// s differences wrapped into [-0.5, 0.5] across the seam.
+__device__ __forceinline__ void env_st(float x, float y, float z, float* s, float* t) {
+    const float h = sqrtf(x * x + y * y);
+    *s = fatan2(y, x) * 0.159154943f + 0.5f;
+    *t = 0.5f - fatan2(z, h) * 0.318309886f;
+}
+__device__ __forceinline__ float env_wrap_ds(float d) { return d > 0.5f ? d - 1.0f : (d < -0.5f ? d + 1.0f : d); }
+static __device__ void h_environment(const Lane& L, const uint32_t* a, const TexDesc* tex, int ntex, uint32_t* st) {
+    const uint32_t r = a[0];
+    const int nc = anc(r) == 3 ? 3 : 1;
+    const int id = (int)(a[3] & 0xFFu);
+    float res[3] = { 0.0f, 0.0f, 0.0f };
+    if (id < ntex) {
+        const TexDesc& T = tex[id];
+        const int first = (int)((a[3] >> 16) & 0xFFu);
+        const D2 x = ldd(L, a[1], 0), y = ldd(L, a[1], 1), z = ldd(L, a[1], 2);
+        const float width = ldf(L, a[4], 0, 0);
+        float s, t, sx, tx, sy, ty;
+        env_st(x.v, y.v, z.v, &s, &t);
+        env_st(x.v + x.dx, y.v + y.dx, z.v + z.dx, &sx, &tx);
+        env_st(x.v + x.dy, y.v + y.dy, z.v + z.dy, &sy, &ty);
+        const float w0 = (float)T.w[0], h0 = (float)T.h[0];
+        tex_filtered(T, s, t, env_wrap_ds(sx - s) * w0, (tx - t) * h0, env_wrap_ds(sy - s) * w0, (ty - t) * h0,
+                     width, TW_PERIODIC, TW_CLAMP, first, nc, res);
     } else {
         raise_status(st, ST_ARRAY_BOUNDS);
     }
@@ -2165,6 +2206,7 @@ __device__ __forceinline__ void exec_op(const RunCtx& R, Lane& L, uint32_t code,
     case OP_LUMINANCE: OSLG_TIER_CASE(4, h_luminance(L, a)) break;
     case OP_BLACKBODY: OSLG_TIER_CASE(4, h_blackbody(L, a)) break;
     case OP_TEXTURE: OSLG_TIER_CASE(4, h_texture(L, a, R.textures, R.ntextures, R.status)) break;
+    case OP_ENVIRONMENT: OSLG_TIER_CASE(4, h_environment(L, a, R.textures, R.ntextures, R.status)) break;
     case OP_SETMESSAGE: OSLG_TIER_CASE(4, h_setmessage(L, a, R.status)) break;
     case OP_GETMESSAGE: OSLG_TIER_CASE(4, h_getmessage(L, a, R.status)) break;
     case OP_NOISE: OSLG_TIER_CASE(1, h_noise(L, a)) break;

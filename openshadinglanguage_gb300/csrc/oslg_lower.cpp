@@ -460,11 +460,13 @@ struct Lowerer {
                 for (size_t i = 2; i < op.args.size() && !is_string(op.args[i]); ++i) mark_derivs(op.args[i]);
             }
             if (op.name == "__store_output" && op.imm[2]) mark_derivs(op.args[0]);
-            // texture's footprint comes from the derivatives of s and t
+            // texture's footprint comes from the derivatives of s and t,
+            // environment's from those of the direction
             if (op.name == "texture" && op.args.size() > 3) {
                 mark_derivs(op.args[2]);
                 mark_derivs(op.args[3]);
             }
+            if (op.name == "environment" && op.args.size() > 2) mark_derivs(op.args[2]);
             if (op.name == "__load_userdata" && op.imm[2]) mark_derivs(op.args[0]);
         }
         const auto& prop = deriv_propagating_ops();
@@ -1564,6 +1566,42 @@ struct Lowerer {
         return true;
     }
 
+    // environment r filename R ["option", value]... (osl_environment,
+    // src/liboslexec/optexture.cpp): the registered image is a
+    // latitude-longitude map (z up); options width, firstchannel.
+    bool lower_environment(const LOp& op) {
+        const size_t na = op.args.size();
+        if (na < 3) return fail("environment needs a result, a file name and a direction");
+        if (!is_string(op.args[1]) || !syms[op.args[1]].is_const)
+            return fail("environment: the file name must be a constant string");
+        if (!is_triple(op.args[2])) return fail("environment: the direction must be a vector");
+        const std::string fname = const_string(op.args[1]);
+        auto it = ss.texture_ids.find(fname);
+        if (it == ss.texture_ids.end()) return fail("environment map '" + fname + "' is not registered");
+        if (na > 3 && !is_string(op.args[3]))
+            return fail("environment: explicit derivative arguments are not supported (those of R are used)");
+        int first = 0;
+        float width = 1.0f;
+        for (size_t k = 3; k < na; k += 2) {
+            if (k + 1 >= na || !is_string(op.args[k]) || !syms[op.args[k]].is_const)
+                return fail("environment: options are constant name/value pairs");
+            const std::string on = const_string(op.args[k]);
+            const int v = op.args[k + 1];
+            if (!syms[v].is_const || syms[v].cval.empty())
+                return fail("environment option '" + on + "' must be a numeric constant");
+            if (on == "width") width = syms[v].cval[0];
+            else if (on == "firstchannel") first = (int)syms[v].cval[0];
+            else return fail("environment option '" + on + "' is not supported");
+            if (first < 0 || first > 255) return fail("environment: firstchannel out of range");
+        }
+        if (it->second > 255) return fail("too many textures");
+        const int wc = const_float(width);
+        syms[wc].slot = (int)pool_add(syms[wc]);
+        emit(OP_ENVIRONMENT, { A(op.args[0]), A(op.args[2]), 0u, (uint32_t)it->second | ((uint32_t)first << 16), A(wc) },
+             "environment");
+        return true;
+    }
+
     bool lower_op(const LOp& op, int depth, int loopl) {
         const std::string& n = op.name;
         auto a = [&](int i) { return A(op.args[i]); };
@@ -1839,6 +1877,7 @@ struct Lowerer {
             return true;
         }
         if (n == "texture") return lower_texture(op);
+        if (n == "environment") return lower_environment(op);
         if (n == "getattribute") return lower_getattribute(op);
         if (n == "setmessage") {
             const TypeSpec& t = syms[op.args[1]].type;
@@ -1903,6 +1942,7 @@ struct Lowerer {
             case OP_NORMALIZE: case OP_TRANSFORM: case OP_MMUL: case OP_AREF: case OP_AASSIGN:
             case OP_MDIV: case OP_TRANSPOSE: case OP_DETERMINANT: case OP_AREA: case OP_FILTERWIDTH:
             case OP_LUMINANCE: case OP_BLACKBODY: case OP_TEXTURE: case OP_SETMESSAGE: case OP_GETMESSAGE:
+            case OP_ENVIRONMENT:
                 t |= 4u;
                 break;
             default: break;

@@ -130,6 +130,8 @@ enum OpCode : uint16_t {
     OP_SETMESSAGE,   // a0=state (int) a1=store a2=value a3=words | type id << 16
     OP_GETMESSAGE,   // a0=r (int) a1=state a2=store a3=dest a4=words | type id << 16
                      // | strict << 31
+    OP_ENVIRONMENT,  // a0=r (float or triple) a1=R (triple, Dual2: the footprint)
+                     // a3=texture index | firstchannel << 16 a4=width
     OP_COUNT
 };
 

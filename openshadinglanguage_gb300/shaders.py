@@ -622,3 +622,38 @@ def texture_lookup(name, scale, wrap=None, nc=3, width=None, first=None):
         args += [b.const("string", "firstchannel"), b.const("int", int(first))]
     b.op("texture", *args)
     return b.text()
+
+
+def environment_lookup(name, width=None, first=None):
+    """Cout = environment("env", R) with R the unit direction of the
+    (u, v) grid: phi = 2 pi u around z, theta = pi v from +z.
+
+        shader env(output color Cout = 0)
+        {
+            float phi = u * M_2PI, theta = v * M_PI, st = sin(theta);
+            Cout = environment("env", vector(cos(phi) * st, sin(phi) * st, cos(theta)));
+        }
+    """
+    from .oso import OsoBuilder
+    b = OsoBuilder(name)
+    cout = b.param("color", "Cout", [0, 0, 0], output=True)
+    u, v = b.glob("float", "u"), b.glob("float", "v")
+    phi, theta, st, cp, sp, ct = [b.tmp("float") for _ in range(6)]
+    x, y = b.tmp("float"), b.tmp("float")
+    R = b.tmp("vector")
+    b.op("mul", phi, u, b.const("float", 6.2831855))
+    b.op("mul", theta, v, b.const("float", 3.1415927))
+    b.op("sin", st, theta)
+    b.op("cos", cp, phi)
+    b.op("sin", sp, phi)
+    b.op("cos", ct, theta)
+    b.op("mul", x, cp, st)
+    b.op("mul", y, sp, st)
+    b.op("vector", R, x, y, ct)
+    args = [cout, b.const("string", "env"), R]
+    if width is not None:
+        args += [b.const("string", "width"), b.const("float", width)]
+    if first is not None:
+        args += [b.const("string", "firstchannel"), b.const("int", first)]
+    b.op("environment", *args)
+    return b.text()

@@ -651,6 +651,22 @@ void otex_bilinear(const OTexture& T, int lev, float s, float t, uint32_t sw, ui
         out[c] = (1.0f - fy) * top + fy * bot;
     }
 }
+// mipmapped bilinear: level of detail from the footprint in level-0
+// texels (times width), the two nearest levels blended
+void otex_filtered(const OTexture& T, float s, float t, float dsx, float dtx, float dsy, float dty, float width,
+                   uint32_t sw, uint32_t tw, int first, int nc, float* res) {
+    const float len = std::max(std::sqrt(dsx * dsx + dtx * dtx), std::sqrt(dsy * dsy + dty * dty)) * width;
+    float lod = len > 1.0f ? oracle::own_log(len) * 1.44269504f : 0.0f;
+    lod = std::min(lod, (float)(T.nlevels - 1));
+    const int l0 = (int)lod;
+    const float f = lod - (float)l0;
+    otex_bilinear(T, l0, s, t, sw, tw, first, nc, res);
+    if (f > 0.0f && l0 + 1 < T.nlevels) {
+        float hi[3];
+        otex_bilinear(T, l0 + 1, s, t, sw, tw, first, nc, hi);
+        for (int c = 0; c < nc; ++c) res[c] = (1.0f - f) * res[c] + f * hi[c];
+    }
+}
 void op_texture(Point& P, const uint32_t* a) {
     const uint32_t r = a[0];
     const int nc = anc(r) == 3 ? 3 : 1;
@@ -664,18 +680,42 @@ void op_texture(Point& P, const uint32_t* a) {
         const DF s = getd(P, a[1], 0), t = getd(P, a[2], 0);
         const float width = getf(P, a[4], 0, 0);
         const float w0 = (float)T.w[0], h0 = (float)T.h[0];
-        const float dsx = s.dx * w0, dtx = t.dx * h0, dsy = s.dy * w0, dty = t.dy * h0;
-        const float len = std::max(std::sqrt(dsx * dsx + dtx * dtx), std::sqrt(dsy * dsy + dty * dty)) * width;
-        float lod = len > 1.0f ? oracle::own_log(len) * 1.44269504f : 0.0f;
-        lod = std::min(lod, (float)(T.nlevels - 1));
-        const int l0 = (int)lod;
-        const float f = lod - (float)l0;
-        otex_bilinear(T, l0, s.v, t.v, sw, tw, first, nc, res);
-        if (f > 0.0f && l0 + 1 < T.nlevels) {
-            float hi[3];
-            otex_bilinear(T, l0 + 1, s.v, t.v, sw, tw, first, nc, hi);
-            for (int c = 0; c < nc; ++c) res[c] = (1.0f - f) * res[c] + f * hi[c];
-        }
+        otex_filtered(T, s.v, t.v, s.dx * w0, t.dx * h0, s.dy * w0, t.dy * h0, width, sw, tw, first, nc, res);
+    } else {
+        P.status |= oslg::ST_ARRAY_BOUNDS;
+    }
+    for (int c = 0; c < nc; ++c) putd(P, r, c, DF(res[c]));
+}
+
+// environment (osl_environment, src/liboslexec/optexture.cpp): a
+// latitude-longitude image by direction, z up: s = atan2(y, x) / 2pi + 0.5
+// (periodic), t = 0.5 - atan2(z, hypot(x, y)) / pi (clamped); the footprint
+// maps R + dR/dx, R + dR/dy the same way (s differences wrapped into
+// [-0.5, 0.5]).
+void oenv_st(float x, float y, float z, float* s, float* t) {
+    const float h = std::sqrt(x * x + y * y);
+    *s = (float)std::atan2((double)y, (double)x) * 0.159154943f + 0.5f;
+    *t = 0.5f - (float)std::atan2((double)z, (double)h) * 0.318309886f;
+}
+float oenv_wrap_ds(float d) { return d > 0.5f ? d - 1.0f : (d < -0.5f ? d + 1.0f : d); }
+void op_environment(Point& P, const uint32_t* a) {
+    const uint32_t r = a[0];
+    const int nc = anc(r) == 3 ? 3 : 1;
+    const int id = (int)(a[3] & 0xFFu);
+    float res[3] = { 0.0f, 0.0f, 0.0f };
+    const std::vector<OTexture>& tex = otextures();
+    if (id < (int)tex.size() && tex[id].nlevels > 0) {
+        const OTexture& T = tex[id];
+        const int first = (int)((a[3] >> 16) & 0xFFu);
+        const DF x = getd(P, a[1], 0), y = getd(P, a[1], 1), z = getd(P, a[1], 2);
+        const float width = getf(P, a[4], 0, 0);
+        float s, t, sx, tx, sy, ty;
+        oenv_st(x.v, y.v, z.v, &s, &t);
+        oenv_st(x.v + x.dx, y.v + y.dx, z.v + z.dx, &sx, &tx);
+        oenv_st(x.v + x.dy, y.v + y.dy, z.v + z.dy, &sy, &ty);
+        const float w0 = (float)T.w[0], h0 = (float)T.h[0];
+        otex_filtered(T, s, t, oenv_wrap_ds(sx - s) * w0, (tx - t) * h0, oenv_wrap_ds(sy - s) * w0, (ty - t) * h0,
+                      width, oslg::TW_PERIODIC, oslg::TW_CLAMP, first, nc, res);
     } else {
         P.status |= oslg::ST_ARRAY_BOUNDS;
     }
@@ -1278,6 +1318,7 @@ struct Runner {
             case oslg::OP_LUMINANCE: op_luminance(P, a); break;
             case oslg::OP_BLACKBODY: op_blackbody(P, a); break;
             case oslg::OP_TEXTURE: op_texture(P, a); break;
+            case oslg::OP_ENVIRONMENT: op_environment(P, a); break;
             case oslg::OP_SETMESSAGE: op_setmessage(P, a); break;
             case oslg::OP_GETMESSAGE: op_getmessage(P, a); break;
             case oslg::OP_NOISE: op_noise(P, a); break;

@@ -47,3 +47,26 @@ def test_texture_matches_oracle(case, jit):
     assert oracle_run(g.program_bytes(), W * H, grid_globals(u, v, W, H, centers=True), ref) == 0
     assert_same(got, ref)
     assert ss.device_status() == 0
+
+
+ENV_CASES = [dict(width=None), dict(width=3.0), dict(first=1)]
+
+
+@pytest.mark.parametrize("jit", [0, 1])
+@pytest.mark.parametrize("case", ENV_CASES, ids=lambda c: "-".join("%s%s" % kv for kv in c.items()))
+def test_environment_matches_oracle(case, jit):
+    from openshadinglanguage_gb300.shaders import environment_lookup
+    ss = og.ShadingSystem()
+    if jit:
+        ss.attribute("jit", 1)
+    register(ss, make_image(41, 83, 3, seed=2), "env")
+    name = "genv_%d" % abs(hash(tuple(sorted(case.items()))))
+    g = single_layer_group(ss, name, environment_lookup(name, **case),
+                           outputs=[og.SymLocationDesc("Cout", og.TypeColor, False, og.SymArenaOutputs, 0, 12)])
+    W, H = 97, 51
+    u, v = pixel_grid(W, H, centers=True)
+    got = gpu_run(ss, g, W * H, device_grid_globals(u, v, W, H, centers=True), 3)
+    ref = np.zeros((W * H, 3), np.float32)
+    assert oracle_run(g.program_bytes(), W * H, grid_globals(u, v, W, H, centers=True), ref) == 0
+    assert_same(got, ref)
+    assert ss.device_status() == 0

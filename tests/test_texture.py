@@ -17,8 +17,8 @@ def make_image(h, w, nch, seed=5):
     return np.random.default_rng(seed).random((h, w, nch), dtype=np.float32)
 
 
-def register(ss, img):
-    idx = ss.texture_create("img", img)
+def register(ss, img, name="img"):
+    idx = ss.texture_create(name, img)
     L = oracle()
     L.oracle_texture_create.argtypes = [ctypes.c_int] * 4 + [ctypes.c_void_p]
     a = np.ascontiguousarray(img, np.float32)
