@@ -1377,13 +1377,17 @@ static __device__ void h_load_global(const Lane& L, const uint32_t* a, const osl
     }
 }
 
+// a3 bit 1: the record carries [val][dx][dy]; a destination with
+// derivatives reads them, or gets zeros when the record has none
 static __device__ void h_load_userdata(const Lane& L, const uint32_t* a, char* base) {
     uint32_t r = a[0];
     int nc = anc(r);
     const char* p = base + (int64_t)a[1] + L.pt * (int64_t)(int32_t)a[2];
-    int nd = ader(r) ? 3 : 1;
+    const bool src_d = (a[3] & 2u) != 0u;
     const uint32_t* q = reinterpret_cast<const uint32_t*>(p);
-    for (int i = 0; i < nc * nd; ++i) stw(L, r, i, q[i]);
+    for (int i = 0; i < nc; ++i) stw(L, r, i, q[i]);
+    if (ader(r))
+        for (int i = nc; i < 3 * nc; ++i) stw(L, r, i, src_d ? q[i] : 0u);
 }
 
 static __device__ void h_store_output(const Lane& L, const uint32_t* a, char* base) {

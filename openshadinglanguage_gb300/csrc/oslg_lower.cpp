@@ -1393,6 +1393,28 @@ struct Lowerer {
         pool.insert(pool.end(), w.begin(), w.end());
         return k;
     }
+    // A per-point attribute of the shaded object: a userdata symloc with the
+    // attribute's name and type (the renderer's per-point answer, read from
+    // the userdata arena like an interpolated parameter). Looked up before
+    // the scene-wide registered attributes, as the reference searches the
+    // object first.
+    bool load_userdata_attribute(const std::string& attr, int dest, int result) {
+        const TypeSpec& dt = syms[dest].type;
+        for (const SymLoc& sl : g.symlocs) {
+            if (sl.arena != ARENA_USERDATA || sl.name != attr) continue;
+            if (sl.type.base != dt.base || sl.type.arraylen != dt.arraylen || dt.is_array()
+                || dt.base == BT_STRING || dt.base == BT_CLOSURE)
+                return false;
+            emit(OP_LOAD_USERDATA, { A(dest), (uint32_t)sl.offset, (uint32_t)sl.stride,
+                                     (dt.base == BT_INT ? 1u : 0u) | (sl.derivs ? 2u : 0u) },
+                 "getattribute");
+            const int r = const_int(1);
+            syms[r].slot = (int)pool_add(syms[r]);
+            emit(OP_ASSIGN, { A(result), A(r), 1u, 1u, 1u }, "getattribute");
+            return true;
+        }
+        return false;
+    }
     bool lower_getattribute(const LOp& op) {
         const size_t na = op.args.size();
         if (na < 3 || na > 5) return fail("getattribute takes ([object,] name, [index,] value)");
@@ -1428,6 +1450,8 @@ struct Lowerer {
             one_string(g.layers[li].layername);
         } else if (object.empty() && attr == "shader:groupname") {
             one_string(g.name);
+        } else if (!object_lookup && !array_lookup && load_userdata_attribute(attr, dest, op.args[0])) {
+            return true;
         } else {
             auto it = ss.attributes.find({ object, attr });
             if (it != ss.attributes.end()) {
@@ -1615,7 +1639,7 @@ struct Lowerer {
         if (n == "__load_userdata") {
             int s = op.args[0];
             emit(OP_LOAD_USERDATA, { a(0), (uint32_t)op.imm[0], (uint32_t)op.imm[1],
-                                     is_int(s) ? 1u : 0u },
+                                     (is_int(s) ? 1u : 0u) | (op.imm[2] ? 2u : 0u) },
                  "userdata");
             return true;
         }

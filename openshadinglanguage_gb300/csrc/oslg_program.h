@@ -67,7 +67,8 @@ enum OpCode : uint16_t {
     OP_LAYER_END,   // re-enables lanes that returned from this layer
     // data movement
     OP_LOAD_GLOBAL,   // a0=dst a1=global id
-    OP_LOAD_USERDATA, // a0=dst a1=byte offset a2=byte stride a3=base type (0 float,1 int)
+    OP_LOAD_USERDATA, // a0=dst a1=byte offset a2=byte stride a3=bit 0 int, bit 1 the
+                      // record carries derivatives
     OP_STORE_OUTPUT,  // a0=src a1=byte offset a2=byte stride a3=flags(bit0 derivs, bit1 int)
     OP_ASSIGN,        // a0=r a1=src
     OP_ZERO_DERIVS,   // a0=r

@@ -1078,8 +1078,11 @@ struct Runner {
             case oslg::OP_LOAD_GLOBAL: op_load_global(P, a, G); break;
             case oslg::OP_LOAD_USERDATA: {
                 const uint32_t* q = reinterpret_cast<const uint32_t*>(userdata + (int64_t)a[1] + P.pt * (int64_t)(int32_t)a[2]);
-                int n = anc(a[0]) * (ader(a[0]) ? 3 : 1);
-                for (int i = 0; i < n; ++i) setw(P, a[0], i, q[i]);
+                const int nc = anc(a[0]);
+                const bool src_d = (a[3] & 2u) != 0u;  // the record carries derivatives
+                for (int i = 0; i < nc; ++i) setw(P, a[0], i, q[i]);
+                if (ader(a[0]))
+                    for (int i = nc; i < 3 * nc; ++i) setw(P, a[0], i, src_d ? q[i] : 0u);
                 break;
             }
             case oslg::OP_STORE_OUTPUT: {

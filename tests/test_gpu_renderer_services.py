@@ -10,7 +10,8 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 from test_gpu_parity import assert_same, dev, device_grid_globals, gpu_run  # noqa: E402
-from test_messages_attributes import attribute_group, check_attributes, message_group  # noqa: E402
+from test_messages_attributes import (attribute_group, check_attributes, check_userdata_attributes,  # noqa: E402
+                                      message_group, userdata_attribute_group, userdata_records)
 from test_named_spaces import NFLOATS, check, inputs, spaces_group  # noqa: E402
 
 
@@ -95,4 +96,20 @@ def test_named_spaces_match_oracle(jit):
     assert oracle_run(g.program_bytes(), n, og.make_globals(P=P, N=N, dPdu=T), ref) == 0
     assert_same(got, ref)
     check(got, P, N, T)
+    assert ss.device_status() == 0
+
+
+@pytest.mark.parametrize("jit", [0, 1])
+def test_userdata_attributes_match_oracle(jit):
+    ss = og.ShadingSystem()
+    if jit:
+        ss.attribute("jit", 1)
+    g = userdata_attribute_group(ss, "j%d" % jit)
+    n = 3001
+    ud = userdata_records(n)
+    got = gpu_run(ss, g, n, og.make_globals(u=0.5), 15, userdata=ud)
+    ref = np.zeros((n, 15), np.float32)
+    assert oracle_run(g.program_bytes(), n, og.make_globals(u=0.5), ref, userdata=ud) == 0
+    assert_same(got, ref)
+    check_userdata_attributes(got, ud)
     assert ss.device_status() == 0

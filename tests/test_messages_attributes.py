@@ -313,3 +313,82 @@ def test_getattribute_needs_constant_names():
     ss.add_symlocs(g, [og.SymLocationDesc("l1.r", og.TypeInt, False, og.SymArenaOutputs, 0, 4)])
     with pytest.raises(og.OSLError, match="must be constants"):
         g.program_bytes()
+
+
+def userdata_attribute_group(ss, tag=""):
+    """getattribute of per-point attributes the renderer passes in the
+    userdata arena: a color with derivatives, an int, and the int read as
+    a float (type mismatch: not found)."""
+    b = og.OsoBuilder("uattr" + tag)
+    c = b.param("color", "c", 0.0, output=True)
+    i = b.param("int", "i", -1, output=True)
+    f = b.param("float", "f", 5.0, output=True)
+    r = [b.param("int", "r%d" % k, -5, output=True) for k in range(3)]
+    S = lambda s: b.const("string", s)
+    b.op("getattribute", r[0], S("uvw"), c)
+    b.op("getattribute", r[1], S("objid"), i)
+    b.op("getattribute", r[2], S("objid"), f)
+    ss.LoadMemoryCompiledShader("uattr" + tag, b.text())
+    g = ss.ShaderGroupBegin("guattr" + tag)
+    ss.Shader(g, "surface", "uattr" + tag, "l1")
+    ss.ShaderGroupEnd(g)
+    ss.add_symlocs(g, [og.SymLocationDesc("uvw", og.TypeColor, True, og.SymArenaUserData, 0, 40),
+                       og.SymLocationDesc("objid", og.TypeInt, False, og.SymArenaUserData, 36, 40),
+                       og.SymLocationDesc("l1.c", og.TypeColor, True, og.SymArenaOutputs, 0, 60),
+                       og.SymLocationDesc("l1.i", og.TypeInt, False, og.SymArenaOutputs, 36, 60),
+                       og.SymLocationDesc("l1.f", og.TypeFloat, False, og.SymArenaOutputs, 40, 60)]
+                  + [og.SymLocationDesc("l1.r%d" % k, og.TypeInt, False, og.SymArenaOutputs, 44 + 4 * k, 60)
+                     for k in range(3)])
+    return g
+
+
+def userdata_records(n, seed=21):
+    rng = np.random.default_rng(seed)
+    ud = rng.normal(size=(n, 10)).astype(np.float32)
+    ud.view(np.int32)[:, 9] = rng.integers(0, 1000, n)
+    return ud
+
+
+def check_userdata_attributes(out, ud):
+    assert np.array_equal(out[:, 0:9].view(np.uint32), ud[:, 0:9].view(np.uint32))
+    ints = out.view(np.int32)
+    assert np.array_equal(ints[:, 9], ud.view(np.int32)[:, 9])
+    assert np.all(out[:, 10] == 5.0)
+    assert ints[:, 11:14].tolist() == [[1, 1, 0]] * len(out)
+
+
+def test_getattribute_reads_per_point_userdata():
+    ss = og.ShadingSystem()
+    g = userdata_attribute_group(ss)
+    n = 200
+    ud = userdata_records(n)
+    out = np.zeros((n, 15), np.float32)
+    assert oracle_run(g.program_bytes(), n, og.make_globals(u=0.5), out, userdata=ud) == 0
+    check_userdata_attributes(out, ud)
+
+
+@pytest.mark.parametrize("with_derivs", [False, True])
+def test_userdata_parameter_derivatives(with_derivs):
+    """A varying parameter read from userdata whose derivatives are needed
+    downstream (Dx): the record's derivatives when it carries them, else 0
+    (never the words that follow the value)."""
+    ss = og.ShadingSystem()
+    b = og.OsoBuilder("udd%d" % with_derivs)
+    q = b.param("float", "q", 0.0, lockgeom=False)
+    o = b.param("float", "o", 0.0, output=True)
+    d = b.param("float", "d", 0.0, output=True)
+    b.op("assign", o, q)
+    b.op("Dx", d, q)
+    ss.LoadMemoryCompiledShader("udd%d" % with_derivs, b.text())
+    g = ss.ShaderGroupBegin("gudd%d" % with_derivs)
+    ss.Shader(g, "surface", "udd%d" % with_derivs, "l1")
+    ss.ShaderGroupEnd(g)
+    ss.add_symlocs(g, [og.SymLocationDesc("q", og.TypeFloat, with_derivs, og.SymArenaUserData, 0, 12),
+                       og.SymLocationDesc("l1.o", og.TypeFloat, False, og.SymArenaOutputs, 0, 8),
+                       og.SymLocationDesc("l1.d", og.TypeFloat, False, og.SymArenaOutputs, 4, 8)])
+    n = 64
+    ud = np.random.default_rng(1).normal(size=(n, 3)).astype(np.float32)
+    out = np.zeros((n, 2), np.float32)
+    assert oracle_run(g.program_bytes(), n, og.make_globals(u=0.5), out, userdata=ud) == 0
+    assert np.array_equal(out[:, 0], ud[:, 0])
+    assert np.array_equal(out[:, 1], ud[:, 1] if with_derivs else np.zeros(n, np.float32))
