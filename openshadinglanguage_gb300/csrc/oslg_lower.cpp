@@ -792,6 +792,26 @@ struct Lowerer {
             LOp& op = lops[k];
             if (op.name == "if" && op.jumps.size() >= 2) {
                 const int je = op.jumps[0], jend = op.jumps[1];
+                // a known condition: the branch not taken never runs; the
+                // taken one continues inline as straight-line code
+                CVal cv;
+                int cs = op.args.empty() ? -1 : op.args[0];
+                if (cs >= 0 && K.count(cs)) cs = K[cs];
+                if (cs >= 0 && cval_of(cs, cv)) {
+                    const bool taken = cv.truth();
+                    for (int q = taken ? je : k + 1; q < (taken ? jend : je); ++q) {
+                        lops[q].name = "nop";
+                        lops[q].args.clear();
+                        lops[q].jumps.clear();
+                        lops[q].param_init = false;
+                    }
+                    op.name = "nop";
+                    op.args.clear();
+                    op.jumps.clear();
+                    ++folded_ops;
+                    ++k;
+                    continue;
+                }
                 std::map<int, int> K1 = K, K2 = K;
                 fold_range(k + 1, je, K1, blocked);
                 fold_range(je, jend, K2, blocked);

@@ -26,7 +26,8 @@ def probe_shader(name="fold_probe"):
     cout = b.param("color", "Cout", 0.0, output=True)
     outs = [b.param("float", "d_out", 0.0, output=True), b.param("float", "e_out", 0.0, output=True),
             b.param("int", "j_out", 0, output=True), b.param("int", "k_out", 0, output=True),
-            b.param("int", "eq_out", 0, output=True), b.param("float", "m_out", 0.0, output=True)]
+            b.param("int", "eq_out", 0, output=True), b.param("float", "m_out", 0.0, output=True),
+            b.param("float", "br_out", 0.0, output=True), b.param("float", "kept_out", 0.0, output=True)]
     b.op("assign", a, F(2.0))
     b.op("mul", bb, a, F(3.0))             # 6
     b.op("color", cout, bb, a, F(1.0))     # (6, 2, 1)
@@ -54,6 +55,19 @@ def probe_shader(name="fold_probe"):
     b.op("assign", outs[5], m)
     for o, v in ((outs[0], d), (outs[1], e), (outs[2], j), (outs[3], k)):
         b.op("assign", o, v)
+    # constant conditions: only the taken branch remains
+    c1 = b.tmp("int")
+    b.op("gt", c1, j, I(20))               # 1
+    with b.if_(c1) as br:
+        b.op("add", outs[6], d, F(10.0))
+        br.else_()
+        b.op("assign", outs[6], F(-1.0))
+    c0 = b.tmp("int")
+    b.op("lt", c0, e, F(0.0))              # e is only known after the loop: kept
+    with b.if_(c0) as br:
+        b.op("assign", outs[7], F(1.0))
+        br.else_()
+        b.op("assign", outs[7], F(2.0))
     return b.text()
 
 
@@ -64,10 +78,10 @@ def probe_group(ss):
     ss.ShaderGroupEnd(g)
     names = [("Cout", og.TypeColor, 12), ("d_out", og.TypeFloat, 4), ("e_out", og.TypeFloat, 4),
              ("j_out", og.TypeInt, 4), ("k_out", og.TypeInt, 4), ("eq_out", og.TypeInt, 4),
-             ("m_out", og.TypeFloat, 4)]
+             ("m_out", og.TypeFloat, 4), ("br_out", og.TypeFloat, 4), ("kept_out", og.TypeFloat, 4)]
     locs, off = [], 0
     for nm, ty, sz in names:
-        locs.append(og.SymLocationDesc("l1." + nm, ty, False, og.SymArenaOutputs, off, 36))
+        locs.append(og.SymLocationDesc("l1." + nm, ty, False, og.SymArenaOutputs, off, 44))
         off += sz
     ss.add_symlocs(g, locs)
     return g
@@ -86,9 +100,10 @@ def test_probe_folds_and_keeps_results():
         ss = og.ShadingSystem()
         ss.attribute("opt_constant_fold", fold)
         g = probe_group(ss)
-        res[fold] = (nops(g),) + run_grid(g, 9)
+        res[fold] = (nops(g),) + run_grid(g, 11)
+        res[fold] += (g.program_bytes(),)
     assert res[1][0] < res[0][0]
-    u, out, st = res[1][1:]
+    u, out, st = res[1][1:4]
     assert st == 0
     assert np.array_equal(out.view(np.uint32), res[0][2].view(np.uint32))
     ints = out.view(np.int32)
@@ -98,6 +113,19 @@ def test_probe_folds_and_keeps_results():
     assert np.all(out[:, 4] == 18.0)
     assert np.all(ints[:, 5] == 21) and np.all(ints[:, 6] == 5) and np.all(ints[:, 7] == 1)
     assert np.all(out[:, 8] == 0.0)
+    assert np.array_equal(out[:, 9], (out[:, 3] + np.float32(10)).astype(np.float32))
+    assert np.all(out[:, 10] == 2.0)
+    # the constant-condition if is gone, the one on a loop result stays
+    import re
+    src = open(__file__.replace("test_constant_fold.py", "../openshadinglanguage_gb300/csrc/oslg_program.h")).read()
+    body = src.split("enum OpCode : uint16_t {")[1].split("};")[0]
+    names = []
+    for nm in re.findall(r"\b(OP_[A-Z0-9_]+)\b", body):
+        if nm not in names:
+            names.append(nm)
+    count_if = lambda blob: sum(1 for i in range(struct.unpack("<I", blob[8:12])[0])
+                                if struct.unpack("<H", blob[64 + 32 * i:66 + 32 * i])[0] == names.index("OP_IF"))
+    assert count_if(res[0][4]) == 3 and count_if(res[1][4]) == 2
 
 
 def both(build, nfloats, n_runs=(0, 1), G=None, n=None, userdata=None):
