@@ -448,6 +448,8 @@ def main():
                     help="1: run the group's specialized kernel (attribute jit), 0: the interpreter")
     ap.add_argument("--jit-block", type=int, default=0, help="specialized launch: threads per CTA")
     ap.add_argument("--jit-pool-smem", type=int, default=-1, help="specialized launch: closure pools in smem (1/0)")
+    ap.add_argument("--host-direct", type=int, default=1,
+                    help="e2e: the kernel writes pinned host output records directly (1) or via copies (0)")
     ap.add_argument("--jit-min-blocks", type=int, default=0,
                     help="specialized kernel register cap: 256-thread CTAs per SM it must fit (2..8)")
     ap.add_argument("--section", choices=["batching", "serving", "wavefront", "texture"],
@@ -526,6 +528,7 @@ def main():
             wl.ss.attribute("jit_pool_smem", args.jit_pool_smem)
         if args.jit_min_blocks:
             wl.ss.attribute("jit_min_blocks", args.jit_min_blocks)
+        wl.ss.attribute("host_direct_outputs", args.host_direct)
     stream = torch.cuda.current_stream()
     sh = stream.cuda_stream
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")

@@ -53,6 +53,7 @@ struct oslg_system {
     int jit_block = 0;       // specialized launch: threads per CTA (0: 256)
     int jit_pool_smem = -1;  // closure pools: 1 shared memory, 0 HBM, -1 shared when it fits
     int jit_min_blocks = 0;  // register cap of specialized kernels (256-thread CTAs per SM; 0: automatic)
+    int host_direct_outputs = 1;  // host-buffer execution: kernels write pinned output records directly
     std::string err;
     std::vector<oslg::InstanceParam> pending_params;  // Parameter() before Shader()
 };
@@ -204,6 +205,7 @@ int oslg_attribute_int(oslg_system* sys, const char* name, int value) {
     else if (n == "jit_block") sys->jit_block = value;
     else if (n == "jit_pool_smem") sys->jit_pool_smem = value;
     else if (n == "jit_min_blocks") sys->jit_min_blocks = value;
+    else if (n == "host_direct_outputs") sys->host_direct_outputs = value;
     else return fail(sys, OSLG_ERR_ARG, "unknown attribute '" + n + "'");
     if (sys->ss.opts.max_closure_terms > 0xFFFF || sys->ss.opts.max_closure_components > 0xFFFF)
         return fail(sys, OSLG_ERR_ARG, "closure pool capacity must stay below 65536");
@@ -678,6 +680,20 @@ int oslg_execute_batch_host(oslg_system* sys, oslg_group* group, int64_t npoints
                 return fail(sys, OSLG_ERR_CUDA, "cudaMalloc of the host-execution buffers failed");
         }
         const bool preserve = (flags & OSLG_HOST_PRESERVE_OUTPUTS) != 0;
+        // Pinned, device-mapped output records and a specialized kernel that
+        // stages whole records: the kernel writes the records straight into
+        // host memory (over the CPU-GPU link, overlapped with the shading;
+        // unwritten words are zeroed in the same pass, or kept when
+        // preserving). Otherwise device buffers and copies.
+        char* out_direct = nullptr;
+        if (sys->host_direct_outputs && output_stride > 0 && cg.spec && cg.spec->stage_stride == (uint32_t)output_stride) {
+            cudaPointerAttributes pa;
+            if (cudaPointerGetAttributes(&pa, host_outputs) == cudaSuccess && pa.type == cudaMemoryTypeHost &&
+                pa.devicePointer)
+                out_direct = static_cast<char*>(pa.devicePointer);
+            else
+                cudaGetLastError();
+        }
         const int64_t nchunks = (npoints + chunk - 1) / chunk;
         for (int64_t c = 0; c < nchunks; ++c) {
             HostSlot& S = sys->host_slots[c % nslots];
@@ -703,7 +719,7 @@ int oslg_execute_batch_host(oslg_system* sys, oslg_group* group, int64_t npoints
                                             (size_t)(n * userdata_stride), cudaMemcpyHostToDevice, S.stream),
                        "userdata copy", &rc))
                 return rc;
-            if (output_stride > 0) {
+            if (output_stride > 0 && !out_direct) {
                 char* hout = static_cast<char*>(host_outputs) + start * output_stride;
                 const cudaError_t e = preserve ? cudaMemcpyAsync(S.d_out, hout, (size_t)(n * output_stride),
                                                                  cudaMemcpyHostToDevice, S.stream)
@@ -715,14 +731,15 @@ int oslg_execute_batch_host(oslg_system* sys, oslg_group* group, int64_t npoints
             ds.gheap_bytes = S.gheap_bytes;
             std::string err;
             if (cg.spec)
-                rc = spec_launch(ds, *cg.spec, cg, n, dg, S.d_ud, S.d_out, S.stream, &err, sys->jit_block,
-                                 sys->jit_pool_smem);
+                rc = spec_launch(ds, *cg.spec, cg, n, dg, S.d_ud,
+                                 out_direct ? static_cast<void*>(out_direct + start * output_stride) : S.d_out,
+                                 S.stream, &err, sys->jit_block, sys->jit_pool_smem, out_direct && !preserve);
             else
                 rc = device_execute(ds, cg.header, cg.d_blob, n, dg, S.d_ud, S.d_out, S.stream, sys->launch, &err);
             S.gheap = ds.gheap;
             S.gheap_bytes = ds.gheap_bytes;
             if (rc != OSLG_OK) return fail(sys, rc, err);
-            if (output_stride > 0 &&
+            if (output_stride > 0 && !out_direct &&
                 !cu_ok(sys, cudaMemcpyAsync(static_cast<char*>(host_outputs) + start * output_stride, S.d_out,
                                             (size_t)(n * output_stride), cudaMemcpyDeviceToHost, S.stream),
                        "output copy", &rc))

@@ -269,7 +269,7 @@ std::string spec_source(const CompiledGroup& cg, int min_blocks) {
     if (min_blocks <= 0) min_blocks = uses_cl ? 4 : 3;
     o << "extern \"C\" __global__ void __launch_bounds__(256, " << std::max(2, std::min(8, min_blocks)) << ") "
       << kKernelName
-      << "(const __grid_constant__ oslg::dev::KArgs k, int pool_in_smem) {\n";
+      << "(const __grid_constant__ oslg::dev::KArgs k, int pool_in_smem, int fill_unwritten) {\n";
     o << "    using namespace oslg;\n    using namespace oslg::dev;\n";
     if (stage) o << "    unsigned char* smem = oslg_smem;\n";
     else o << "    extern __shared__ __align__(16) unsigned char smem[];\n";
@@ -306,6 +306,7 @@ std::string spec_source(const CompiledGroup& cg, int min_blocks) {
         o << "        const uint32_t* sw = reinterpret_cast<const uint32_t*>(smem);\n";
         o << "        for (int64_t w = threadIdx.x; w < npt * (int64_t)(rec / 4u); w += blockDim.x)\n";
         o << "            if (flags[w]) gout[w] = sw[w];\n";
+        o << "            else if (fill_unwritten) gout[w] = 0u;\n";
         o << "        __syncthreads();\n";
     }
     o << "    }\n}\n";
@@ -444,7 +445,7 @@ int build_and_load(const std::string& src, const std::string& csrc, const std::s
 
 int spec_launch(DeviceState& ds, const SpecKernel& sk, const CompiledGroup& cg, int64_t npoints,
                 const oslg_shaderglobals& G, void* userdata, void* outputs, void* stream, std::string* err,
-                int block_req, int pool_req) {
+                int block_req, int pool_req, bool fill_unwritten) {
     if (npoints <= 0) return OSLG_OK;
     int rc = device_init(ds, err);
     if (rc != OSLG_OK) return rc;
@@ -496,7 +497,8 @@ int spec_launch(DeviceState& ds, const SpecKernel& sk, const CompiledGroup& cg, 
         k.gheap = ds.gheap;
     }
     grid = std::min<int64_t>(grid, 0x7FFFFFFF);
-    void* args[] = { &k, &in_smem };
+    int fill = fill_unwritten ? 1 : 0;
+    void* args[] = { &k, &in_smem, &fill };
     if (!ok(cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(block), args, shmem, static_cast<cudaStream_t>(stream)),
             err, "specialized kernel launch"))
         return OSLG_ERR_CUDA;

@@ -59,9 +59,11 @@ int spec_build(const CompiledGroup& cg, const std::string& csrc_dir, const std::
 
 // Launch over [0, npoints): one CTA of 256 points per tile, closure pools in
 // shared memory when they fit, else in the executor's HBM scratch.
-// `block` 0 and `pool_smem` -1 choose automatically.
+// `block` 0 and `pool_smem` -1 choose automatically. With staged output
+// records, `fill_unwritten` writes zeros to the record words no output op
+// wrote (otherwise they keep what the buffer held).
 int spec_launch(DeviceState& ds, const SpecKernel& k, const CompiledGroup& cg, int64_t npoints,
                 const oslg_shaderglobals& G, void* userdata, void* outputs, void* stream, std::string* err,
-                int block = 0, int pool_smem = -1);
+                int block = 0, int pool_smem = -1, bool fill_unwritten = false);
 
 }  // namespace oslg

@@ -92,3 +92,33 @@ def test_mismatched_strides_are_rejected():
     out = np.zeros(n * 64, np.float32)
     with pytest.raises(og.OSLError, match="output_stride"):
         ss.execute_batch_host(g, n, G, out, wl.C2_STRIDE + 4)
+
+
+@pytest.mark.parametrize("direct", [1, 0])
+def test_pinned_outputs_direct_and_copied(direct):
+    """Pinned output records: the specialized kernel writes them straight
+    into host memory (attribute host_direct_outputs, the default) or through
+    device buffers and copies; both equal the device entry, zeroing or
+    preserving the bytes no output op writes."""
+    from helpers import grid_globals, pixel_grid, shaders, single_layer_group
+    ss = og.ShadingSystem()
+    ss.attribute("jit", 1)
+    ss.attribute("host_direct_outputs", direct)
+    g = single_layer_group(ss, "fbm_cell", shaders.fbm_cell(), outputs=[
+        og.SymLocationDesc("layer1.Cout", og.TypeColor, True, og.SymArenaOutputs, 0, 48),
+        og.SymLocationDesc("layer1.cellhash", og.TypeInt, False, og.SymArenaOutputs, 36, 48)])
+    W, H = 640, 331
+    n = W * H
+    u, v = pixel_grid(W, H, centers=True)
+    dout = torch.full((n * 12,), -3.5, dtype=torch.float32, device="cuda")
+    ss.execute_batch(g, n, grid_globals(dev(u), dev(v), W, H, centers=True), 0, dout.data_ptr(),
+                     torch.cuda.current_stream().cuda_stream, sync=True)
+    ref = dout.cpu().numpy().reshape(n, 12)
+    hu, hv = torch.from_numpy(u).pin_memory(), torch.from_numpy(v).pin_memory()
+    kept = torch.full((n * 12,), -3.5, dtype=torch.float32).pin_memory()
+    ss.execute_batch_host(g, n, grid_globals(hu, hv, W, H, centers=True), kept, 48, preserve_outputs=True)
+    assert np.array_equal(kept.numpy().reshape(n, 12).view(np.uint32), ref.view(np.uint32))
+    zeroed = torch.full((n * 12,), -3.5, dtype=torch.float32).pin_memory()
+    ss.execute_batch_host(g, n, grid_globals(hu, hv, W, H, centers=True), zeroed, 48)
+    z = zeroed.numpy().reshape(n, 12)
+    assert (z[:, 10:] == 0.0).all() and np.array_equal(z[:, :10].view(np.uint32), ref[:, :10].view(np.uint32))
