@@ -111,7 +111,11 @@ int oslg_destroy_system(oslg_system* sys);
  * reference's per-group JIT), "jit_block" (64/128/256 threads per CTA of a
  * specialized launch), "jit_pool_smem" (closure pools in shared memory 1,
  * HBM scratch 0, automatic -1), "jit_min_blocks" (register cap of
- * specialized kernels: 256-thread CTAs per SM that must fit, 2..8). */
+ * specialized kernels: 256-thread CTAs per SM that must fit, 2..8),
+ * "strict_messages", "opt_constant_fold", "opt_elide_useless_ops" (as the
+ * reference's ShadingSystem attributes of those names, shadingsys.cpp:1639-1684),
+ * "host_direct_outputs" (host-buffer execution writes pinned output records
+ * from the kernel, 1 by default). */
 int oslg_attribute_int(oslg_system* sys, const char* name, int value);
 /* ShadingSystem::register_closure (oslexec.h:1041). Parameters are taken
  * positionally from the `closure` op's arguments. */
@@ -197,6 +201,11 @@ int oslg_group_specialized_source(oslg_system* sys, oslg_group* group, char* buf
  * wavefront driver shades its materials with such a kernel. */
 int oslg_groups_specialized_batch_source(oslg_system* sys, oslg_group* const* groups, int ngroups, char* buf,
                                          size_t cap, size_t* size);
+/* The byte strides of the group's output and userdata records (0 when it
+ * has none), as its symlocs and BSDF requests place them; the group is
+ * optimized first. oslg_execute_batch_host takes these strides. */
+int oslg_group_record_strides(oslg_system* sys, oslg_group* group, int64_t* output_stride,
+                              int64_t* userdata_stride);
 /* 1 when the group runs its specialized kernel. */
 int oslg_group_is_specialized(oslg_system* sys, oslg_group* group, int* out);
 /* Register (or replace) the image that texture(name, s, t, ...) looks up:

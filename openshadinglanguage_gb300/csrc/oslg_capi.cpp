@@ -756,6 +756,27 @@ int oslg_execute_batch_host(oslg_system* sys, oslg_group* group, int64_t npoints
     });
 }
 
+int oslg_group_record_strides(oslg_system* sys, oslg_group* group, int64_t* output_stride, int64_t* userdata_stride) {
+    if (!sys || !group || !output_stride || !userdata_stride) return OSLG_ERR_ARG;
+    return guarded(sys, [&]() {
+        int rc = ensure_compiled(sys, group, false);
+        if (rc != OSLG_OK) return rc;
+        const CompiledGroup& cg = *group->g.compiled;
+        const Op* ops = reinterpret_cast<const Op*>(cg.blob.data() + sizeof(ProgramHeader));
+        *output_stride = 0;
+        *userdata_stride = 0;
+        for (uint32_t i = 0; i < cg.header.nops; ++i) {
+            const Op& op = ops[i];
+            if (op.code == OP_STORE_OUTPUT || op.code == OP_STORE_CLOSURE || op.code == OP_BSDF_EVAL ||
+                op.code == OP_BSDF_SAMPLE)
+                *output_stride = (int64_t)(int32_t)op.a[2];
+            if (op.code == OP_LOAD_USERDATA) *userdata_stride = (int64_t)(int32_t)op.a[2];
+            if (op.code == OP_BSDF_SAMPLE) *userdata_stride = (int64_t)(int32_t)op.a[6];
+        }
+        return OSLG_OK;
+    });
+}
+
 int oslg_group_specialized_source(oslg_system* sys, oslg_group* group, char* buf, size_t cap, size_t* size) {
     if (!sys || !group) return OSLG_ERR_ARG;
     return guarded(sys, [&]() {
