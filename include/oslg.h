@@ -201,6 +201,17 @@ int oslg_group_specialized_source(oslg_system* sys, oslg_group* group, char* buf
  * wavefront driver shades its materials with such a kernel. */
 int oslg_groups_specialized_batch_source(oslg_system* sys, oslg_group* const* groups, int ngroups, char* buf,
                                          size_t cap, size_t* size);
+/* BatchedExecutor::execute_init + execute_layer(layername)
+ * (src/include/OSL/oslexec.h:1006-1027): run the group's layers up to and
+ * including `layername` over N device points and store the outputs those
+ * layers write (outputs of later layers are left untouched). Each call is a
+ * complete launch; no per-point state is kept between calls. */
+int oslg_execute_layer(oslg_system* sys, oslg_group* group, const char* layername, int64_t npoints,
+                       const oslg_shaderglobals* globals, void* userdata_base, void* output_base, void* stream);
+/* The serialized program that runs layers [0, layername] (as
+ * oslg_group_program for the whole group). */
+int oslg_group_layer_program(oslg_system* sys, oslg_group* group, const char* layername, void* buf, size_t cap,
+                             size_t* size);
 /* The byte strides of the group's output and userdata records (0 when it
  * has none), as its symlocs and BSDF requests place them; the group is
  * optimized first. oslg_execute_batch_host takes these strides. */

@@ -155,6 +155,11 @@ _EXPORTS = {
                                            ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
     "oslg_renderer_attribute": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p, TypeDescC,
                                                ctypes.c_void_p]),
+    "oslg_execute_layer": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int64,
+                                          ctypes.POINTER(ShaderGlobalsC), ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_void_p]),
+    "oslg_group_layer_program": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p,
+                                                ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
     "oslg_group_record_strides": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64),
                                                  ctypes.POINTER(ctypes.c_int64)]),
     "oslg_renderer_matrix": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p]),

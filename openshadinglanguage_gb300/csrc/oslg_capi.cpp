@@ -449,6 +449,8 @@ int oslg_optimize_group(oslg_system* sys, oslg_group* group) {
 int oslg_release_group(oslg_system* sys, oslg_group* group) {
     if (!group) return OSLG_ERR_ARG;
     if (group->g.compiled && group->g.compiled->d_blob) device_free(group->g.compiled->d_blob);
+    for (auto& kv : group->g.layer_compiled)
+        if (kv.second && kv.second->d_blob) device_free(kv.second->d_blob);
     delete group;
     (void)sys;
     return OSLG_OK;
@@ -752,6 +754,76 @@ int oslg_execute_batch_host(oslg_system* sys, oslg_group* group, int64_t npoints
         rc = device_read_status(sys->dev, nullptr, &bits, &err);
         if (rc != OSLG_OK) return fail(sys, rc, err);
         if (bits) return fail(sys, OSLG_ERR_DEVICE, "kernel status bits " + std::to_string(bits));
+        return OSLG_OK;
+    });
+}
+
+// The program that runs layers [0, layer] of the group, lowered and
+// uploaded on first use.
+static int ensure_layer_compiled(oslg_system* sys, oslg_group* group, int layer, const CompiledGroup** out) {
+    ShaderGroup& g = group->g;
+    if (!g.ended) return fail(sys, OSLG_ERR_STATE, "group used before ShaderGroupEnd");
+    if (sys->textures_dirty) {
+        int rc = upload_textures(sys);
+        if (rc != OSLG_OK) return rc;
+    }
+    std::lock_guard<std::mutex> lock(g.mutex);
+    std::unique_ptr<CompiledGroup>& slot = g.layer_compiled[layer];
+    if (!slot) {
+        auto cg = std::make_unique<CompiledGroup>();
+        std::string err;
+        if (!lower_group(sys->ss, g, *cg, err, layer))
+            return fail(sys, OSLG_ERR_LOWER, "group '" + g.name + "' up to layer " + std::to_string(layer) + ": " + err);
+        slot = std::move(cg);
+    }
+    if (!slot->d_blob) {
+        std::string err;
+        int rc = device_init(sys->dev, &err);
+        if (rc != OSLG_OK) return fail(sys, rc, err);
+        rc = device_upload_program(slot->blob.data(), slot->blob.size(), &slot->d_blob, &err);
+        if (rc != OSLG_OK) return fail(sys, rc, err);
+        slot->device = sys->dev.device;
+    }
+    *out = slot.get();
+    return OSLG_OK;
+}
+
+int oslg_execute_layer(oslg_system* sys, oslg_group* group, const char* layername, int64_t npoints,
+                       const oslg_shaderglobals* globals, void* userdata_base, void* output_base, void* stream) {
+    if (!sys || !group || !layername || !globals || npoints < 0) return OSLG_ERR_ARG;
+    return guarded(sys, [&]() {
+        const int layer = group->g.find_layer(layername);
+        if (layer < 0) return fail(sys, OSLG_ERR_ARG, std::string("no layer '") + layername + "' in the group");
+        if (layer == (int)group->g.layers.size() - 1)
+            return oslg_execute_batch(sys, group, npoints, globals, userdata_base, output_base, stream);
+        const CompiledGroup* cg = nullptr;
+        int rc = ensure_layer_compiled(sys, group, layer, &cg);
+        if (rc != OSLG_OK) return rc;
+        std::string err;
+        rc = device_execute(sys->dev, cg->header, cg->d_blob, npoints, *globals, userdata_base, output_base, stream,
+                            sys->launch, &err);
+        if (rc != OSLG_OK) return fail(sys, rc, err);
+        return OSLG_OK;
+    });
+}
+
+int oslg_group_layer_program(oslg_system* sys, oslg_group* group, const char* layername, void* buf, size_t cap,
+                             size_t* size) {
+    if (!sys || !group || !layername) return OSLG_ERR_ARG;
+    return guarded(sys, [&]() {
+        const int layer = group->g.find_layer(layername);
+        if (layer < 0) return fail(sys, OSLG_ERR_ARG, std::string("no layer '") + layername + "' in the group");
+        std::lock_guard<std::mutex> lock(group->g.mutex);
+        std::unique_ptr<CompiledGroup>& slot = group->g.layer_compiled[layer];
+        if (!slot) {
+            auto cg = std::make_unique<CompiledGroup>();
+            std::string err;
+            if (!lower_group(sys->ss, group->g, *cg, err, layer))
+                return fail(sys, OSLG_ERR_LOWER, "group '" + group->g.name + "': " + err);
+            slot = std::move(cg);
+        }
+        if (size) *size = slot->blob.size();
+        if (buf) std::memcpy(buf, slot->blob.data(), std::min(cap, slot->blob.size()));
         return OSLG_OK;
     });
 }

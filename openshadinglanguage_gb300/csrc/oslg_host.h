@@ -164,6 +164,7 @@ struct ShaderGroup {
     bool ended = false;
     std::mutex mutex;  // lowering happens once, under this lock
     std::unique_ptr<CompiledGroup> compiled;
+    std::map<int, std::unique_ptr<CompiledGroup>> layer_compiled;  // programs ending at a layer
     int find_layer(const std::string& n) const;
 };
 
@@ -211,6 +212,8 @@ public:
 };
 
 // Lowering entry point: group -> device op program (oslg_lower.cpp).
-bool lower_group(ShadingSystem& ss, ShaderGroup& g, CompiledGroup& out, std::string& err);
+// stop_layer >= 0 lowers the layers [0, stop_layer] only, with the outputs
+// those layers write (execute_layer).
+bool lower_group(ShadingSystem& ss, ShaderGroup& g, CompiledGroup& out, std::string& err, int stop_layer = -1);
 
 }  // namespace oslg

@@ -207,7 +207,10 @@ struct Lowerer {
     std::map<std::string, int> msg_store;
     std::map<std::string, int> msg_type_id;
 
+    int stop_layer = -1;  // >= 0: run layers [0, stop_layer] only (execute_layer)
+
     Lowerer(ShadingSystem& s, ShaderGroup& gg, std::string& e) : ss(s), g(gg), err(e) {}
+    int last_layer() const { return stop_layer >= 0 ? stop_layer : (int)g.layers.size() - 1; }
 
     bool fail(const std::string& m) { err = m; return false; }
 
@@ -288,7 +291,7 @@ struct Lowerer {
     }
 
     bool build_lops() {
-        for (int li = 0; li < (int)g.layers.size(); ++li) {
+        for (int li = 0; li <= last_layer(); ++li) {
             Layer& L = g.layers[li];
             const ShaderMaster& m = *L.master;
             for (int msi = 0; msi < (int)m.symbols.size(); ++msi) {
@@ -356,6 +359,7 @@ struct Lowerer {
         for (const BsdfEvalRequest& be : g.bsdf_evals) {
             SymLoc tmp;
             tmp.name = be.closure;
+            if (beyond_stop(be.closure)) continue;
             int gs = resolve_symloc(tmp);
             if (gs < 0 || syms[gs].type.base != BT_CLOSURE)
                 return fail("bsdf eval: '" + be.closure + "' is not a closure of the group");
@@ -371,6 +375,7 @@ struct Lowerer {
         for (const BsdfSampleRequest& bs : g.bsdf_samples) {
             SymLoc tmp;
             tmp.name = bs.closure;
+            if (beyond_stop(bs.closure)) continue;
             int gs = resolve_symloc(tmp);
             if (gs < 0 || syms[gs].type.base != BT_CLOSURE)
                 return fail("bsdf sample: '" + bs.closure + "' is not a closure of the group");
@@ -383,6 +388,7 @@ struct Lowerer {
         // renderer outputs placed through symlocs
         for (const SymLoc& sl : g.symlocs) {
             if (sl.arena != ARENA_OUTPUTS) continue;
+            if (beyond_stop(sl.name)) continue;  // written by a layer that does not run
             int gs = resolve_symloc(sl);
             if (gs < 0) return fail("symloc '" + sl.name + "' does not name a symbol of the group");
             LOp op; op.name = "__store_output"; op.args = { gs };
@@ -393,6 +399,12 @@ struct Lowerer {
         return true;
     }
 
+    // a "layer.symbol" name of a layer past the stop layer
+    bool beyond_stop(const std::string& name) const {
+        const size_t dot = name.find('.');
+        if (dot == std::string::npos) return false;
+        return g.find_layer(name.substr(0, dot)) > last_layer();
+    }
     int resolve_symloc(const SymLoc& sl) {
         std::string lname, sname = sl.name;
         size_t dot = sl.name.find('.');
@@ -402,6 +414,7 @@ struct Lowerer {
         }
         for (int li = (int)g.layers.size() - 1; li >= 0; --li) {
             if (!lname.empty() && g.layers[li].layername != lname) continue;
+            if (lname.empty() && li > last_layer()) continue;
             int msi = g.layers[li].master->find_symbol(sname);
             if (msi >= 0) return sym_of(li, msi);
         }
@@ -532,9 +545,9 @@ struct Lowerer {
     // decides with the default lazyunconnected
     // (src/liboslexec/oslexec_pvt.h:1477-1491): its messages are never sent.
     bool layer_used(int li) {
-        if (li == (int)g.layers.size() - 1) return true;
-        for (size_t lj = (size_t)li + 1; lj < g.layers.size(); ++lj)
-            for (const Connection& c : g.layers[lj].connections)
+        if (li == last_layer()) return true;
+        for (int lj = li + 1; lj <= last_layer(); ++lj)
+            for (const Connection& c : g.layers[(size_t)lj].connections)
                 if (c.srclayer == li) return true;
         auto in_layer = [&](const std::string& nm) {
             SymLoc tmp;
@@ -2036,8 +2049,9 @@ struct Lowerer {
 
 }  // namespace
 
-bool lower_group(ShadingSystem& ss, ShaderGroup& g, CompiledGroup& out, std::string& err) {
+bool lower_group(ShadingSystem& ss, ShaderGroup& g, CompiledGroup& out, std::string& err, int stop_layer) {
     Lowerer L(ss, g, err);
+    L.stop_layer = stop_layer;
     return L.run(out);
 }
 

@@ -94,6 +94,17 @@ class ShaderGroup:
         self._ss._check(L.oslg_group_program(self._ss._h, self._h, buf, size.value, ctypes.byref(size)))
         return buf.raw[: size.value]
 
+    def layer_program_bytes(self, layername):
+        """The program that runs layers up to and including `layername`."""
+        L = C.lib()
+        size = ctypes.c_size_t(0)
+        self._ss._check(L.oslg_group_layer_program(self._ss._h, self._h, layername.encode(), None, 0,
+                                                   ctypes.byref(size)))
+        buf = ctypes.create_string_buffer(size.value)
+        self._ss._check(L.oslg_group_layer_program(self._ss._h, self._h, layername.encode(), buf, size.value,
+                                                   ctypes.byref(size)))
+        return buf.raw[: size.value]
+
     def release(self):
         if self._h:
             C.lib().oslg_release_group(self._ss._h, self._h)
@@ -231,6 +242,13 @@ class ShadingSystem:
         self._check(fn(self._h, group.handle, int(npoints), ctypes.byref(globals_c),
                        ctypes.c_void_p(userdata_ptr or None), ctypes.c_void_p(output_ptr or None),
                        ctypes.c_void_p(stream or None)))
+
+    def execute_layer(self, group, layername, npoints, globals_c, userdata_ptr=0, output_ptr=0, stream=0):
+        """BatchedExecutor::execute_init + execute_layer(layername): the
+        layers up to and including `layername`, over device points."""
+        self._check(C.lib().oslg_execute_layer(self._h, group.handle, layername.encode(), int(npoints),
+                                               ctypes.byref(globals_c), ctypes.c_void_p(userdata_ptr or None),
+                                               ctypes.c_void_p(output_ptr or None), ctypes.c_void_p(stream or None)))
 
     def batch(self):
         """A persistent multi-group batch on this system (see Batch)."""
