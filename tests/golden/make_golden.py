@@ -2,12 +2,13 @@
 
 Reads (in this container only) the reference testsuite's expected images
 and text outputs and writes small fixtures next to this script:
-  * noise-family images (uint8 TIFF, Deflate) -> <name>.npz, subsampled;
+  * noise-family and spline images (uint8 TIFF, Deflate) -> <name>.npz,
+    subsampled;
   * testsuite/example-batched-deformer/ref/out.txt -> deformer_out.txt;
   * src/liboslnoise/oslnoise_test.cpp known answers -> oslnoise_known.json.
 The GPU machine never reads the reference; tests read only these fixtures.
 
-TIFF decoding is a minimal baseline-TIFF reader (strips, Deflate or no
+TIFF decoding is a minimal baseline-TIFF reader (strips, Deflate, LZW or no
 compression, optional horizontal predictor) on top of zlib and numpy.
 """
 import json
@@ -22,6 +23,39 @@ import numpy as np
 REF = "/root/reference"
 HERE = os.path.dirname(os.path.abspath(__file__))
 STEP = 4  # keep every 4th pixel in x and y
+
+
+def lzw_decode(data):
+    """TIFF 6.0 LZW (section 13): MSB-first codes of 9..12 bits, 256 clears
+    the table, 257 ends the strip, the code width grows one code early."""
+    out = bytearray()
+    table = [bytes([i]) for i in range(256)] + [b"", b""]
+    width, pos, prev = 9, 0, None
+    nbits = len(data) * 8
+    while pos + width <= nbits:
+        byte, bit = divmod(pos, 8)
+        chunk = int.from_bytes(data[byte:byte + 3].ljust(3, b"\0"), "big")
+        code = (chunk >> (24 - bit - width)) & ((1 << width) - 1)
+        pos += width
+        if code == 257:
+            break
+        if code == 256:
+            table = table[:258]
+            width, prev = 9, None
+            continue
+        if prev is None:
+            entry = table[code]
+        elif code < len(table):
+            entry = table[code]
+            table.append(prev + entry[:1])
+        else:
+            entry = prev + prev[:1]
+            table.append(entry)
+        out += entry
+        prev = entry
+        if len(table) + 1 >= (1 << width) and width < 12:
+            width += 1
+    return bytes(out)
 
 
 def read_tiff(path):
@@ -55,6 +89,8 @@ def read_tiff(path):
         chunk = data[o:o + c]
         if comp in (8, 32946):
             chunk = zlib.decompress(chunk)
+        elif comp == 5:
+            chunk = lzw_decode(chunk)
         elif comp != 1:
             raise ValueError("compression %d not supported" % comp)
         rows.append(np.frombuffer(chunk, np.uint8))
@@ -135,6 +171,13 @@ IMAGES = {
     "noise_gabor3d_filter": "testsuite/noise-gabor3d-filter/ref/out.tif",
     "pnoise_perlin": "testsuite/pnoise-perlin/ref/out.tif",
     "pnoise_cell": "testsuite/pnoise-cell/ref/out.tif",
+    # testsuite/spline: Cspline, DxCspline, Fspline, DxFspline, NumKnots
+    "spline_color": "testsuite/spline/ref/color.tif",
+    "spline_dcolor": "testsuite/spline/ref/dcolor.tif",
+    "spline_dcolor_alt": "testsuite/spline/ref/dcolor-oiio2.2.tif",
+    "spline_float": "testsuite/spline/ref/float.tif",
+    "spline_dfloat": "testsuite/spline/ref/dfloat.tif",
+    "spline_numknots": "testsuite/spline/ref/numknots.tif",
 }
 
 
