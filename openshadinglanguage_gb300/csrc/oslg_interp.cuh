@@ -1836,14 +1836,134 @@ static __device__ void h_bsdf_sample(const Lane& L, const uint32_t* a, char* bas
     for (int k = 0; k < 11; ++k) ostoref(o + k, vals[k]);
 }
 
+// ---- splineinverse (splineimpl.h:241-296) ------------------------------------------------
+// The spline of float knots at a Dual2 position (SplineInterp::evaluate with
+// float knots): the root finder's function.
+struct SplineFn {
+    const Lane* L;
+    uint32_t kn;
+    int basis, count;
+    __device__ float knot(int k) const { return __uint_as_float(ldw(*L, kn, k)); }
+    __device__ D2 operator()(D2 xval) const {
+        const SplineBasisDev& B = c_spline_basis[basis];
+        D2 x = xval;
+        if (!(0.0f <= x.v)) x = d2c(0.0f);
+        if (x.v > 1.0f) x = d2c(1.0f);
+        const int nsegs = ((count - 4) / B.step) + 1;
+        x = x * (float)nsegs;
+        int segnum = (int)x.v;
+        if (segnum < 0) segnum = 0;
+        if (segnum > nsegs - 1) segnum = nsegs - 1;
+        if (basis == 5) return d2c(knot(segnum + 1));
+        x = x - (float)segnum;
+        const int s = segnum * B.step;
+        float tk[4];
+        for (int k = 0; k < 4; ++k)
+            tk[k] = ((knot(s) * B.m[k][0] + knot(s + 1) * B.m[k][1]) + knot(s + 2) * B.m[k][2]) + knot(s + 3) * B.m[k][3];
+        D2 t = x * tk[0];
+        t = t + tk[1];
+        t = t * x;
+        t = t + tk[2];
+        t = t * x;
+        t = t + tk[3];
+        return t;
+    }
+};
+__device__ __forceinline__ D2 d2_div(D2 a, D2 b) {
+    const float binv = 1.0f / b.v, ab = a.v / b.v;
+    return d2(ab, binv * (a.dx - ab * b.dx), binv * (a.dy - ab * b.dy));
+}
+// root of f(x) = y on [xmin, xmax]: regula falsi for the first three
+// quarters of the iterations (bisecting when the interpolant leaves the
+// bracket), then bisection; stops when the bracket or the residual is below
+// eps. Unbracketed: the end of the interval toward y. (OpenImageIO's
+// invert(), which the reference calls; the published method.)
+static __device__ D2 spline_root(const SplineFn& f, D2 y, D2 xmin, D2 xmax, int maxiters, float eps, bool* brack) {
+    D2 v0 = f(xmin), v1 = f(xmax);
+    D2 x = xmin, v = v0;
+    const bool increasing = v0.v < v1.v;
+    const float vmin = increasing ? v0.v : v1.v, vmax = increasing ? v1.v : v0.v;
+    const bool bracketed = y.v >= vmin && y.v <= vmax;
+    *brack = bracketed;
+    if (!bracketed) return ((y.v < vmin) == increasing) ? xmin : xmax;
+    if (fabsf(v0.v - v1.v) < eps) return x;
+    const int rfiters = (3 * maxiters) / 4;
+    for (int it = 0; it < maxiters; ++it) {
+        D2 t = d2c(0.5f);
+        if (it < rfiters) {
+            t = d2_div(y - v0, v1 - v0);
+            if (t.v <= 0.0f || t.v >= 1.0f) t = d2c(0.5f);
+        }
+        const D2 omt = d2(1.0f - t.v, -t.dx, -t.dy);
+        x = xmin * omt + xmax * t;
+        v = f(x);
+        if ((v.v < y.v) == increasing) {
+            xmin = x;
+            v0 = v;
+        } else {
+            xmax = x;
+            v1 = v;
+        }
+        if (fabsf(xmax.v - xmin.v) < eps || fabsf(v.v - y.v) < eps) return x;
+    }
+    return x;
+}
+static __device__ void h_splineinverse(const Lane& L, const uint32_t* a, uint32_t* st) {
+    const uint32_t r = a[0];
+    SplineFn f;
+    f.L = &L;
+    f.kn = a[2];
+    f.basis = a[3] < 6u ? (int)a[3] : 0;
+    const int alen = (int)a[5];
+    f.count = a[4] != kNoArg ? ldi(L, a[4], 0) : alen;
+    if (f.count > alen) f.count = alen;
+    if (f.count < 4) {  // a spline needs four knots
+        raise_status(st, ST_ARRAY_BOUNDS);
+        std2(L, r, 0, d2c(0.0f));
+        return;
+    }
+    const D2 y = ldd(L, a[1], 0);
+    const SplineBasisDev& B = c_spline_basis[f.basis];
+    const int lo = B.step == 1 ? 1 : 0, hi = B.step == 1 ? f.count - 2 : f.count - 1;
+    const bool increasing = f.knot(1) < f.knot(f.count - 2);
+    D2 x = d2c(0.0f);
+    bool done = false;
+    if (increasing) {
+        if (y.v <= f.knot(lo)) { x = d2c(0.0f); done = true; }
+        else if (y.v >= f.knot(hi)) { x = d2c(1.0f); done = true; }
+    } else {
+        if (y.v >= f.knot(lo)) { x = d2c(0.0f); done = true; }
+        else if (y.v <= f.knot(hi)) { x = d2c(1.0f); done = true; }
+    }
+    if (!done) {
+        const int nsegs = (f.count - 4) / B.step + 1;
+        const float nseginv = 1.0f / (float)nsegs;
+        D2 r0 = d2c(0.0f);
+        for (int s = 0; s < nsegs; ++s) {
+            const D2 r1 = d2c(nseginv * (float)(s + 1));
+            bool brack;
+            x = spline_root(f, y, r0, r1, 32, 1.0e-6f, &brack);
+            if (brack) break;
+            r0 = r1;
+        }
+    }
+    std2(L, r, 0, x);
+}
+
 // ---- spline (splineimpl.h:191-239) -----------------------------------------------------
-static __device__ void h_spline(const Lane& L, const uint32_t* a) {
+static __device__ void h_spline(const Lane& L, const uint32_t* a, uint32_t* st) {
     uint32_t r = a[0], xa = a[1], kn = a[2];
     const SplineBasisDev& B = c_spline_basis[a[3] < 6u ? a[3] : 0u];
     int alen = (int)a[5];
     int knot_count = a[4] != kNoArg ? ldi(L, a[4], 0) : alen;
     if (knot_count > alen) knot_count = alen;
     int nc = anc(r);
+    if (knot_count < 4) {  // a spline needs four knots
+        raise_status(st, ST_ARRAY_BOUNDS);
+        OSLG_SPEC_UNROLL
+        for (int c = 0; c < nc; ++c) std2(L, r, c, d2c(0.0f));
+        return;
+    }
     int kc = anc(kn);
     bool xd = ader(xa), kd = ader(kn), rd = ader(r);
     D2 x = ldd(L, xa, 0);
@@ -2241,7 +2361,8 @@ __device__ __forceinline__ void exec_op(const RunCtx& R, Lane& L, uint32_t code,
     case OP_STORE_CLOSURE: OSLG_TIER_CASE(2, h_store_closure(L, a, R.outputs, R.CP, R.status)) break;
     case OP_BSDF_EVAL: OSLG_TIER_CASE(2, h_bsdf_eval(L, a, R.outputs, R.CP, R.status)) break;
     case OP_BSDF_SAMPLE: OSLG_TIER_CASE(2, h_bsdf_sample(L, a, R.outputs, R.userdata, R.CP, R.status)) break;
-    case OP_SPLINE: OSLG_TIER_CASE(2, h_spline(L, a)) break;
+    case OP_SPLINE: OSLG_TIER_CASE(2, h_spline(L, a, R.status)) break;
+    case OP_SPLINEINV: OSLG_TIER_CASE(2, h_splineinverse(L, a, R.status)) break;
     default: raise_status(R.status, ST_BAD_OPCODE); break;
     }
 }

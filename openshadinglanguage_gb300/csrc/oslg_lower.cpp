@@ -181,7 +181,7 @@ const std::set<std::string>& deriv_propagating_ops() {
         "sinh", "cosh", "tanh", "exp", "exp2", "expm1", "log", "log2", "log10", "pow", "sqrt",
         "inversesqrt", "cbrt", "abs", "fabs", "mix", "clamp", "min", "max", "smoothstep", "select",
         "dot", "cross", "length", "normalize", "distance", "transform", "transformv", "transformn",
-        "noise", "snoise", "pnoise", "psnoise", "spline", "mod", "fmod", "luminance", "radians",
+        "noise", "snoise", "pnoise", "psnoise", "spline", "splineinverse", "mod", "fmod", "luminance", "radians",
         "degrees", "erf", "erfc" };
     return s;
 }
@@ -499,7 +499,10 @@ struct Lowerer {
                     // index operands of compref/aref/compassign/aassign carry no derivs
                     if ((op.name == "compref" || op.name == "aref") && i == 2) continue;
                     if ((op.name == "compassign" || op.name == "aassign") && i == 1) continue;
-                    if (op.name == "spline" && i == 1) continue;  // basis name
+                    if ((op.name == "spline" || op.name == "splineinverse") && i == 1) continue;  // basis name
+                    // the knot count; splineinverse ignores knot derivatives
+                    if ((op.name == "spline" || op.name == "splineinverse") && op.args.size() == 5 && i == 3) continue;
+                    if (op.name == "splineinverse" && i + 1 == op.args.size()) continue;
                     if ((op.name == "noise" || op.name == "snoise" || op.name == "pnoise"
                          || op.name == "psnoise")
                         && i == 1 && syms[op.args[1]].type.base == BT_STRING)
@@ -1927,6 +1930,26 @@ struct Lowerer {
                  n);
             return true;
         }
+        if (n == "splineinverse") {
+            // splineinverse r basis y [nknots] knots (float knots only), as
+            // src/liboslexec/opspline.cpp:115-153
+            if (na < 4) return fail("splineinverse needs at least 4 args");
+            std::string basis = const_string(op.args[1]);
+            static const std::map<std::string, int> bases = { { "catmull-rom", 0 }, { "bezier", 1 },
+                                                              { "bspline", 2 }, { "hermite", 3 },
+                                                              { "linear", 4 }, { "constant", 5 } };
+            auto bi = bases.find(basis);
+            if (bi == bases.end()) return fail("unknown spline basis '" + basis + "'");
+            int knots = op.args[na - 1];
+            if (syms[knots].type.base != BT_FLOAT || syms[op.args[0]].type.base != BT_FLOAT
+                || syms[op.args[2]].type.base != BT_FLOAT)
+                return fail("splineinverse takes and returns floats, with float knots");
+            uint32_t nk = na == 5 ? A(op.args[3]) : kNoArg;
+            emit(OP_SPLINEINV, { a(0), a(2), A(knots), (uint32_t)bi->second, nk,
+                                 (uint32_t)syms[knots].type.elems() },
+                 n);
+            return true;
+        }
         if (n == "blackbody") {
             const std::vector<float>& t = blackbody_pool();
             int tb = const_floats(t);
@@ -1989,7 +2012,7 @@ struct Lowerer {
             case OP_NOISE: case OP_HASH: case OP_GABOR: t |= 1u; break;
             case OP_CLOSURE: case OP_CLOSURE_MUL: case OP_CLOSURE_ADD: case OP_STORE_CLOSURE: case OP_BSDF_EVAL:
             case OP_BSDF_SAMPLE:
-            case OP_SPLINE:
+            case OP_SPLINE: case OP_SPLINEINV:
                 t |= 2u;
                 break;
             case OP_CBRT: case OP_SIN: case OP_COS: case OP_TAN: case OP_ASIN: case OP_ACOS: case OP_ATAN:

@@ -133,6 +133,8 @@ enum OpCode : uint16_t {
                      // | strict << 31
     OP_ENVIRONMENT,  // a0=r (float or triple) a1=R (triple, Dual2: the footprint)
                      // a3=texture index | firstchannel << 16 a4=width
+    OP_SPLINEINV,    // a0=r (float) a1=y (float) a2=knots (float array) a3=basis id
+                     // a4=knot count operand or kNoArg a5=array length
     OP_COUNT
 };
 

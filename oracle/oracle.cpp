@@ -722,6 +722,114 @@ void op_environment(Point& P, const uint32_t* a) {
     for (int c = 0; c < nc; ++c) putd(P, r, c, DF(res[c]));
 }
 
+// splineinverse (src/liboslexec/splineimpl.h:241-296): clamp outside the
+// knots' range, else search each segment for f(x) = y with OpenImageIO's
+// invert() (the reference calls it; restated from the published method:
+// regula falsi for three quarters of the iterations, bisecting when the
+// interpolant leaves the bracket, then bisection; stop when the bracket or
+// the residual is below eps; unbracketed -> the end toward y). Dual2
+// throughout, so the result carries derivatives as the reference's does.
+struct OSplineFn {
+    const Point* P;
+    uint32_t kn;
+    int basis, count;
+    float knot(int k) const { return bitsf(word(*P, kn, k)); }
+    DF operator()(DF xval) const {
+        const SplineBasis& B = spline_basis(basis);
+        DF x = xval;
+        if (!(0.0f <= x.v)) x = DF(0.0f);
+        if (x.v > 1.0f) x = DF(1.0f);
+        const int nsegs = ((count - 4) / B.step) + 1;
+        x = x * (float)nsegs;
+        int segnum = (int)x.v;
+        if (segnum < 0) segnum = 0;
+        if (segnum > nsegs - 1) segnum = nsegs - 1;
+        if (basis == 5) return DF(knot(segnum + 1));
+        x = x - (float)segnum;
+        const int s = segnum * B.step;
+        float tk[4];
+        for (int k = 0; k < 4; ++k)
+            tk[k] = ((knot(s) * B.m[k][0] + knot(s + 1) * B.m[k][1]) + knot(s + 2) * B.m[k][2]) + knot(s + 3) * B.m[k][3];
+        DF t = x * tk[0];
+        t = t + tk[1];
+        t = t * x;
+        t = t + tk[2];
+        t = t * x;
+        t = t + tk[3];
+        return t;
+    }
+};
+DF ospline_root(const OSplineFn& f, DF y, DF xmin, DF xmax, int maxiters, float eps, bool* brack) {
+    DF v0 = f(xmin), v1 = f(xmax);
+    DF x = xmin, v = v0;
+    const bool increasing = v0.v < v1.v;
+    const float vmin = increasing ? v0.v : v1.v, vmax = increasing ? v1.v : v0.v;
+    const bool bracketed = y.v >= vmin && y.v <= vmax;
+    *brack = bracketed;
+    if (!bracketed) return ((y.v < vmin) == increasing) ? xmin : xmax;
+    if (std::fabs(v0.v - v1.v) < eps) return x;
+    const int rfiters = (3 * maxiters) / 4;
+    for (int it = 0; it < maxiters; ++it) {
+        DF t = DF(0.5f);
+        if (it < rfiters) {
+            t = (y - v0) / (v1 - v0);
+            if (t.v <= 0.0f || t.v >= 1.0f) t = DF(0.5f);
+        }
+        const DF omt = 1.0f - t;
+        x = xmin * omt + xmax * t;
+        v = f(x);
+        if ((v.v < y.v) == increasing) {
+            xmin = x;
+            v0 = v;
+        } else {
+            xmax = x;
+            v1 = v;
+        }
+        if (std::fabs(xmax.v - xmin.v) < eps || std::fabs(v.v - y.v) < eps) return x;
+    }
+    return x;
+}
+void op_splineinverse(Point& P, const uint32_t* a) {
+    OSplineFn f;
+    f.P = &P;
+    f.kn = a[2];
+    f.basis = a[3] < 6u ? (int)a[3] : 0;
+    const int alen = (int)a[5];
+    f.count = a[4] != oslg::kNoArg ? geti(P, a[4], 0) : alen;
+    if (f.count > alen) f.count = alen;
+    if (f.count < 4) {
+        P.status |= oslg::ST_ARRAY_BOUNDS;
+        putd(P, a[0], 0, DF(0.0f));
+        return;
+    }
+    const DF y = getd(P, a[1], 0);
+    const SplineBasis& B = spline_basis(f.basis);
+    const int lo = B.step == 1 ? 1 : 0, hi = B.step == 1 ? f.count - 2 : f.count - 1;
+    const bool increasing = f.knot(1) < f.knot(f.count - 2);
+    DF x(0.0f);
+    bool done = false;
+    if (increasing) {
+        if (y.v <= f.knot(lo)) { x = DF(0.0f); done = true; }
+        else if (y.v >= f.knot(hi)) { x = DF(1.0f); done = true; }
+    } else {
+        if (y.v >= f.knot(lo)) { x = DF(0.0f); done = true; }
+        else if (y.v <= f.knot(hi)) { x = DF(1.0f); done = true; }
+    }
+    if (!done) {
+        const int nsegs = (f.count - 4) / B.step + 1;
+        const float nseginv = 1.0f / (float)nsegs;
+        DF r0(0.0f);
+        for (int s = 0; s < nsegs; ++s) {
+            const DF r1(nseginv * (float)(s + 1));
+            bool brack;
+            x = ospline_root(f, y, r0, r1, 32, 1.0e-6f, &brack);
+            if (brack) break;
+            r0 = r1;
+        }
+    }
+    putd(P, a[0], 0, x);
+}
+
 // setmessage / getmessage (src/liboslexec/opmessage.cpp:19-138): per point
 // and message name a state word (0 unset, 1 + type id once set, kMsgQueried
 // after a strict query that found nothing) and a store per type. Double
@@ -1435,12 +1543,18 @@ struct Runner {
                 o[10] = sres.roughness;
                 break;
             }
+            case oslg::OP_SPLINEINV: op_splineinverse(P, a); break;
             case oslg::OP_SPLINE: {
                 uint32_t r = a[0], xa = a[1], kn = a[2];
                 int alen = (int)a[5];
                 int kcount = a[4] != oslg::kNoArg ? geti(P, a[4], 0) : alen;
                 if (kcount > alen) kcount = alen;
                 int nc = anc(r), kc = anc(kn);
+                if (kcount < 4) {  // a spline needs four knots
+                    P.status |= oslg::ST_ARRAY_BOUNDS;
+                    for (int c = 0; c < nc; ++c) putd(P, r, c, DF(0.0f));
+                    break;
+                }
                 bool kd = ader(kn);
                 for (int c = 0; c < nc; ++c) {
                     int cc = kc == 1 ? 0 : c;

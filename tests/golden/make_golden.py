@@ -4,7 +4,8 @@ Reads (in this container only) the reference testsuite's expected images
 and text outputs and writes small fixtures next to this script:
   * noise-family and spline images (uint8 TIFF, Deflate) -> <name>.npz,
     subsampled;
-  * testsuite/example-batched-deformer/ref/out.txt -> deformer_out.txt;
+  * testsuite/example-batched-deformer/ref/out.txt -> deformer_out.txt and
+    testsuite/splineinverse/ref/out.txt -> splineinverse_out.txt;
   * src/liboslnoise/oslnoise_test.cpp known answers -> oslnoise_known.json.
 The GPU machine never reads the reference; tests read only these fixtures.
 
@@ -178,6 +179,13 @@ IMAGES = {
     "spline_float": "testsuite/spline/ref/float.tif",
     "spline_dfloat": "testsuite/spline/ref/dfloat.tif",
     "spline_numknots": "testsuite/spline/ref/numknots.tif",
+    "spline_nonuniform": "testsuite/spline-nonuniformknots/ref/out.tif",
+}
+
+TEXTS = {
+    # fixture file: reference path
+    "deformer_out.txt": "testsuite/example-batched-deformer/ref/out.txt",
+    "splineinverse_out.txt": "testsuite/splineinverse/ref/out.txt",
 }
 
 
@@ -219,8 +227,8 @@ def main():
         np.savez_compressed(os.path.join(HERE, name + ".npz"), imgs=stack, full_w=stack.shape[2],
                             full_h=stack.shape[1])
         print(name, stack.shape)
-    ref_txt = open(os.path.join(REF, "testsuite/example-batched-deformer/ref/out.txt")).read()
-    open(os.path.join(HERE, "deformer_out.txt"), "w").write(ref_txt)
+    for fixture, rel in TEXTS.items():
+        open(os.path.join(HERE, fixture), "w").write(open(os.path.join(REF, rel)).read())
     ka = known_answers()
     json.dump(ka, open(os.path.join(HERE, "oslnoise_known.json"), "w"), indent=1)
     print("known answers:", sorted(ka))

@@ -42,3 +42,21 @@ def test_spline_band_matches_oracle(k, jit):
     assert oracle_run(g.program_bytes(), W * H, grid_globals(u, v, W, H), ref) == 0
     assert_same(got, ref)
     assert ss.device_status() == 0
+
+
+@pytest.mark.parametrize("jit", [0, 1])
+@pytest.mark.parametrize("basis", ["linear", "catmull-rom", "bspline", "bezier", "hermite", "constant"])
+def test_splineinverse_matches_oracle(basis, jit):
+    from test_spline_golden import splineinverse_group
+    ss = og.ShadingSystem()
+    if jit:
+        ss.attribute("jit", 1)
+    knots = [0.0, 0.0, 0.05, 0.1, 0.3, 1.0, 1.0] if basis != "bezier" else [0.0, 0.1, 0.2, 0.4, 0.5, 0.8, 1.0]
+    g = splineinverse_group(ss, basis, knots, name="gsinv_%s_%d" % (basis.replace("-", "_"), jit))
+    W, H = 301, 7
+    u, v = pixel_grid(W, H)
+    got = gpu_run(ss, g, W * H, device_grid_globals(u, v, W, H), 2)
+    ref = np.zeros((W * H, 2), np.float32)
+    assert oracle_run(g.program_bytes(), W * H, grid_globals(u, v, W, H), ref) == 0
+    assert_same(got, ref)
+    assert ss.device_status() == 0

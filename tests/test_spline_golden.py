@@ -92,3 +92,75 @@ def test_oracle_matches_spline_images(image, name, cols, alts):
     assert any(r[0] for r in results), (name, [(r[1], r[2]) for r in results])
     # in practice every sampled pixel equals the primary reference image
     assert results[0][1] == 0.0 and results[0][2] == 0.0
+
+
+# ---- splineinverse --------------------------------------------------------------------------
+
+INV_KNOTS = [0.0, 0.0, 0.05, 0.1, 0.3, 1.0, 1.0]
+
+
+def splineinverse_group(ss, basis, knots=INV_KNOTS, name=None):
+    """x = splineinverse(basis, u, knots), with x and Dx(x) as outputs
+    (testsuite/splineinverse/test.osl)."""
+    name = name or "sinv_" + basis.replace("-", "_")
+    b = og.OsoBuilder(name)
+    x = b.param("float", "x", 0.0, output=True)
+    dx = b.param("float", "dx", 0.0, output=True)
+    u = b.glob("float", "u")
+    kn = b.param("float[%d]" % len(knots), "knots", list(knots))
+    b.op("splineinverse", x, b.const("string", basis), u, kn)
+    b.op("Dx", dx, x)
+    ss.LoadMemoryCompiledShader(name, b.text())
+    g = ss.ShaderGroupBegin(name + "_g")
+    ss.Shader(g, "surface", name, "l")
+    ss.ShaderGroupEnd(g)
+    ss.add_symlocs(g, [og.SymLocationDesc("l.x", og.TypeFloat, False, og.SymArenaOutputs, 0, 8),
+                       og.SymLocationDesc("l.dx", og.TypeFloat, False, og.SymArenaOutputs, 4, 8)])
+    return g
+
+
+def test_splineinverse_matches_reference_output():
+    """testshade -g 3 1 --center: u = 1/6, 1/2, 5/6 with Dx(u) = 1/3; the
+    printed values and x derivatives (%g) of every basis."""
+    import os
+    import re
+    from helpers import GOLDEN
+    txt = open(os.path.join(GOLDEN, "splineinverse_out.txt")).read()
+    expected = re.findall(r'splineinverse\("([a-z-]+)", ([0-9.e-]+)\) = ([0-9.e-]+)  \(derivs ([0-9.e-]+) ', txt)
+    assert len(expected) == 9
+    u, v = pixel_grid(3, 1, centers=True)
+    for basis in ("linear", "catmull-rom", "bspline"):
+        ss = og.ShadingSystem()
+        g = splineinverse_group(ss, basis)
+        out = np.zeros((3, 2), np.float32)
+        assert oracle_run(g.program_bytes(), 3, grid_globals(u, v, 3, 1, centers=True), out) == 0
+        got = [(basis, "%g" % uu, "%g" % out[i, 0], "%g" % out[i, 1]) for i, uu in enumerate(u)]
+        want = [e for e in expected if e[0] == basis]
+        assert got == want, (got, want)
+
+
+def test_spline_of_splineinverse_matches_nonuniform_knots_image():
+    """testsuite/spline-nonuniformknots (testshade -g 256 64): Cout =
+    spline("linear", splineinverse("linear", u, knots), colors)."""
+    ss = og.ShadingSystem()
+    b = og.OsoBuilder("nonuni")
+    cout = b.param("color", "Cout", 0.0, output=True)
+    u = b.glob("float", "u")
+    kn = b.param("float[5]", "knots", [0.2, 0.2, 0.5, 0.8, 0.8])
+    cols = b.param("color[5]", "colors", [1, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 1])
+    pos = b.tmp("float")
+    lin = b.const("string", "linear")
+    b.op("splineinverse", pos, lin, u, kn)
+    b.op("spline", cout, lin, pos, cols)
+    ss.LoadMemoryCompiledShader("nonuni", b.text())
+    g = ss.ShaderGroupBegin("gnonuni")
+    ss.Shader(g, "surface", "nonuni", "l")
+    ss.ShaderGroupEnd(g)
+    ss.add_symlocs(g, [og.SymLocationDesc("l.Cout", og.TypeColor, False, og.SymArenaOutputs, 0, 12)])
+    ref, W, H, step = golden_image("spline_nonuniform")
+    u, v = pixel_grid(W, H)
+    out = np.zeros((W * H, 3), np.float32)
+    assert oracle_run(g.program_bytes(), W * H, grid_globals(u, v, W, H), out) == 0
+    got = to_uint8(out.reshape(H, W, 3))[::step, ::step]
+    ok, frac, mx = image_diff_ok(got, ref)
+    assert ok and frac == 0.0, (frac, mx)
