@@ -180,6 +180,7 @@ IMAGES = {
     "spline_dfloat": "testsuite/spline/ref/dfloat.tif",
     "spline_numknots": "testsuite/spline/ref/numknots.tif",
     "spline_nonuniform": "testsuite/spline-nonuniformknots/ref/out.tif",
+    "splineinverse_ident": "testsuite/splineinverse-ident/ref/out.tif",
 }
 
 TEXTS = {

@@ -164,3 +164,68 @@ def test_spline_of_splineinverse_matches_nonuniform_knots_image():
     got = to_uint8(out.reshape(H, W, 3))[::step, ::step]
     ok, frac, mx = image_diff_ok(got, ref)
     assert ok and frac == 0.0, (frac, mx)
+
+
+def ident_shader(k):
+    """testsuite/splineinverse-ident/test.osl with the band's basis fixed:
+    spline, splineinverse of u and of the spline value; red where
+    splineinverse(spline(u)) strays from the spline value."""
+    basis = ["linear", "catmull-rom", "bspline", "bezier"][k]
+    cvs = [0.0, 1.0 / 3, 2.0 / 3, 1.0] if basis == "bezier" else [-1.0, 0.0, 1.0, 2.0]
+    b = og.OsoBuilder("sident%d" % k)
+    cout = b.param("color", "Cout", 0.0, output=True)
+    u, v = b.glob("float", "u"), b.glob("float", "v")
+    F = lambda x: b.const("float", x)
+    kn = b.param("float[4]", "cvs", [float(np.float32(c)) for c in cvs])
+    v4, vv = b.tmp("float"), b.tmp("float")
+    b.op("mul", v4, v, F(4.0))
+    b.op("fmod", vv, v4, F(1.0))
+    c1, c2, edge = b.tmp("int"), b.tmp("int"), b.tmp("int")
+    b.op("lt", c1, vv, F(0.1))
+    b.op("gt", c2, vv, F(0.9))
+    b.op("or", edge, c1, c2)
+    name = b.const("string", basis)
+    with b.if_(edge) as br:
+        b.op("assign", cout, F(0.0))
+        br.else_()
+        s, inv_u, invs = b.tmp("float"), b.tmp("float"), b.tmp("float")
+        b.op("spline", s, name, u, kn)
+        b.op("splineinverse", inv_u, name, u, kn)
+        b.op("splineinverse", invs, name, s, kn)
+        lower = b.tmp("int")
+        b.op("lt", lower, vv, F(0.5))
+        with b.if_(lower) as br2:
+            b.op("assign", cout, s)
+            br2.else_()
+            b.op("assign", cout, inv_u)
+        d, ad, big = b.tmp("float"), b.tmp("float"), b.tmp("int")
+        b.op("sub", d, s, invs)
+        b.op("abs", ad, d)
+        b.op("gt", big, ad, F(0.001))
+        with b.if_(big):
+            b.op("compassign", cout, b.const("int", 0), ad)
+    return b.text()
+
+
+def test_splineinverse_identity_image():
+    """testsuite/splineinverse-ident (testshade -g 256 256), one band per
+    basis: spline(u), splineinverse(u) and the red error marks."""
+    ref, W, H, step = golden_image("splineinverse_ident")
+    u, v = pixel_grid(W, H)
+    band = np.clip((v * np.float32(4.0)), 0, 3).astype(np.int32)
+    out = np.zeros((W * H, 3), np.float32)
+    for k in range(4):
+        ss = og.ShadingSystem()
+        ss.LoadMemoryCompiledShader("sident%d" % k, ident_shader(k))
+        g = ss.ShaderGroupBegin("gsident%d" % k)
+        ss.Shader(g, "surface", "sident%d" % k, "l")
+        ss.ShaderGroupEnd(g)
+        ss.add_symlocs(g, [og.SymLocationDesc("l.Cout", og.TypeColor, False, og.SymArenaOutputs, 0, 12)])
+        idx = np.nonzero(band == k)[0]
+        part = np.zeros((len(idx), 3), np.float32)
+        G = grid_globals(np.ascontiguousarray(u[idx]), np.ascontiguousarray(v[idx]), W, H)
+        assert oracle_run(g.program_bytes(), len(idx), G, part) == 0
+        out[idx] = part
+    got = to_uint8(out.reshape(H, W, 3))[::step, ::step]
+    ok, frac, mx = image_diff_ok(got, ref)
+    assert ok and frac == 0.0 and mx == 0.0, (frac, mx)  # every sampled pixel exact
