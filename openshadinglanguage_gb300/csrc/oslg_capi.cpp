@@ -669,7 +669,7 @@ int oslg_execute_batch_host(oslg_system* sys, oslg_group* group, int64_t npoints
         const int64_t chunk = std::min<int64_t>(npoints, std::max<int64_t>(65536, ((npoints + 7) / 8 + 255) / 256 * 256));
         int planes = 0;
         const oslg_field* hf = reinterpret_cast<const oslg_field*>(host_globals);
-        for (int f = 0; f < G_COUNT; ++f)
+        for (int f = 0; f < (int)G_COUNT; ++f)
             if (hf[f].data) planes += kGlobalComps[f];
         if ((int)sys->host_slots.size() < nslots) sys->host_slots.resize(nslots);
         for (int k = 0; k < nslots; ++k) {
@@ -703,7 +703,7 @@ int oslg_execute_batch_host(oslg_system* sys, oslg_group* group, int64_t npoints
             oslg_shaderglobals dg = *host_globals;
             oslg_field* df = reinterpret_cast<oslg_field*>(&dg);
             int plane = 0;
-            for (int f = 0; f < G_COUNT; ++f) {
+            for (int f = 0; f < (int)G_COUNT; ++f) {
                 if (!hf[f].data) continue;
                 float* base = S.d_glob + (size_t)plane * chunk;
                 for (int comp = 0; comp < kGlobalComps[f]; ++comp)

@@ -69,7 +69,7 @@ const char* kGlobalNames[G_COUNT] = { "P", "dPdx", "dPdy", "dPdz", "I", "dIdx", 
                                       "surfacearea" };
 
 int global_id_of(const std::string& n) {
-    for (int i = 0; i < G_COUNT; ++i)
+    for (int i = 0; i < (int)G_COUNT; ++i)
         if (n == kGlobalNames[i]) return i;
     return -1;
 }
@@ -194,7 +194,6 @@ struct Lowerer {
     std::vector<LOp> lops;
     std::map<std::pair<int, int>, int> layer_sym;  // (layer, master sym) -> gsym
     std::map<std::string, int> globals;
-    std::vector<int> const_cache_f;                 // unused bookkeeping
     // outputs
     std::vector<Op> ops;
     std::vector<std::string> op_names;
