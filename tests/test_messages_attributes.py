@@ -392,3 +392,93 @@ def test_userdata_parameter_derivatives(with_derivs):
     assert oracle_run(g.program_bytes(), n, og.make_globals(u=0.5), out, userdata=ud) == 0
     assert np.array_equal(out[:, 0], ud[:, 0])
     assert np.array_equal(out[:, 1], ud[:, 1] if with_derivs else np.zeros(n, np.float32))
+
+
+def test_message_no_closure_testsuite_case():
+    """testsuite/message-no-closure (a.osl -> b.osl, optimized: ref
+    out-opt.txt): the color message 'foo' = c_out / 2 = (0.125, 0.5, 0.5)
+    arrives; 'bar' was never sent (0, destination unchanged); 'foo' read as
+    a float is a type mismatch (0, unchanged); the float[4] message arrives
+    whole; a query before any send is folded away, so setting the message
+    afterwards is no error; a message set and read in the same layer
+    arrives; setting twice and reading as another type are errors."""
+    ss = og.ShadingSystem()
+    a = og.OsoBuilder("msg_a")
+    S = lambda b, s: b.const("string", s)
+    kd = a.param("float", "Kd", 0.5)
+    f_out = a.param("float", "f_out", 0.0, output=True)
+    c_out = a.param("color", "c_out", 0.0, output=True)
+    a.op("assign", f_out, kd)
+    h = a.tmp("float")
+    a.op("div", h, kd, a.const("float", 2.0))
+    a.op("color", c_out, h, a.const("float", 1.0), a.const("float", 1.0))
+    half = a.tmp("color")
+    a.op("div", half, c_out, a.const("float", 2.0))
+    a.op("setmessage", S(a, "foo"), half)
+    arr = a.param("float[4]", "arr", [42.0, 43.0, 44.0, 45.0])
+    a.op("setmessage", S(a, "array"), arr)
+    wd = a.param("int", "wd", -7, output=True)
+    wc = a.tmp("int")
+    a.op("getmessage", wd, S(a, "wrong_direction_test"), wc)
+    b = og.OsoBuilder("msg_b")
+    f_in = b.param("float", "f_in", 41.0)
+    c_in = b.param("color", "c_in", 42.0)
+    outs = {nm: b.param(ty, nm, 0.0 if ty != "int" else -7, output=True)
+            for nm, ty in [("foo", "color"), ("r_foo", "int"), ("bar", "float"), ("r_bar", "int"),
+                           ("r_wrong", "int"), ("array", "float[4]"), ("r_array", "int"), ("Cout", "color"),
+                           ("fin", "float")]}
+    b.op("assign", outs["fin"], f_in)
+    b.op("assign", outs["foo"], b.const("float", 0.0))
+    b.op("setmessage", S(b, "wrong_direction_test"), b.const("int", 3))
+    b.op("getmessage", outs["r_foo"], S(b, "foo"), outs["foo"])
+    b.op("getmessage", outs["r_bar"], S(b, "bar"), outs["bar"])
+    b.op("getmessage", outs["r_wrong"], S(b, "foo"), outs["bar"])
+    b.op("getmessage", outs["r_array"], S(b, "array"), outs["array"])
+    c = b.local("int", "c")
+    b.op("assign", c, b.const("int", 0))
+    b.op("getmessage", b.tmp("int"), S(b, "already_queried"), c)
+    b.op("setmessage", S(b, "already_queried"), b.const("int", 3))
+    b.op("setmessage", S(b, "message_on_same_layer"), b.const("int", 3))
+    b.op("getmessage", b.tmp("int"), S(b, "message_on_same_layer"), c)
+    b.op("setmessage", S(b, "set_twice"), b.const("int", 3))
+    b.op("setmessage", S(b, "set_twice"), b.const("int", 4))
+    N = b.glob("normal", "N")
+    b.op("setmessage", S(b, "set_get_int"), N)
+    b.op("getmessage", b.tmp("int"), S(b, "set_get_int"), c)
+    diff = b.local("color", "diff")
+    b.op("assign", diff, b.const("float", 0.0))
+    b.op("setmessage", S(b, "get_int_set"), b.const("int", 3))
+    b.op("getmessage", b.tmp("int"), S(b, "get_int_set"), diff)
+    fc, nc = b.tmp("float"), b.tmp("color")
+    b.op("assign", fc, c)
+    b.op("mul", nc, N, fc)
+    b.op("add", outs["Cout"], nc, diff)
+    ss.LoadMemoryCompiledShader("msg_a", a.text())
+    ss.LoadMemoryCompiledShader("msg_b", b.text())
+    g = ss.ShaderGroupBegin("gmsg")
+    ss.Shader(g, "surface", "msg_a", "alayer")
+    ss.Shader(g, "surface", "msg_b", "blayer")
+    ss.ConnectShaders(g, "alayer", "f_out", "blayer", "f_in")
+    ss.ConnectShaders(g, "alayer", "c_out", "blayer", "c_in")
+    ss.ShaderGroupEnd(g)
+    layout = [("blayer.foo", og.TypeColor, 3), ("blayer.r_foo", og.TypeInt, 1), ("blayer.bar", og.TypeFloat, 1),
+              ("blayer.r_bar", og.TypeInt, 1), ("blayer.r_wrong", og.TypeInt, 1),
+              ("blayer.array", og.TypeFloat.array(4), 4), ("blayer.r_array", og.TypeInt, 1),
+              ("blayer.Cout", og.TypeColor, 3), ("blayer.fin", og.TypeFloat, 1), ("alayer.wd", og.TypeInt, 1)]
+    locs, off = [], 0
+    for nm, ty, nw in layout:
+        locs.append(og.SymLocationDesc(nm, ty, False, og.SymArenaOutputs, off, 4 * 17))
+        off += 4 * nw
+    ss.add_symlocs(g, locs)
+    n = 16
+    Nv = np.random.default_rng(2).normal(size=(3, n)).astype(np.float32)
+    out = np.zeros((n, 17), np.float32)
+    st = oracle_run(g.program_bytes(), n, og.make_globals(N=Nv, u=0.25, v=0.75), out)
+    ints = out.view(np.int32)
+    assert st & ST_MESSAGE  # set_twice and the two type mismatches
+    assert np.all(out[:, 0:3] == np.float32([0.125, 0.5, 0.5])) and np.all(ints[:, 3] == 1)
+    assert np.all(out[:, 4] == 0.0) and np.all(ints[:, 5] == 0) and np.all(ints[:, 6] == 0)
+    assert np.all(out[:, 7:11] == np.float32([42, 43, 44, 45])) and np.all(ints[:, 11] == 1)
+    assert np.array_equal(out[:, 12:15], (Nv.T * np.float32(3.0)).astype(np.float32))
+    assert np.all(out[:, 15] == 0.5)
+    assert np.all(ints[:, 16] == 0)
