@@ -11,7 +11,8 @@ pytestmark = pytest.mark.gpu
 
 from test_gpu_parity import assert_same, dev, device_grid_globals, gpu_run  # noqa: E402
 from test_messages_attributes import (attribute_group, check_attributes, check_userdata_attributes,  # noqa: E402
-                                      message_group, userdata_attribute_group, userdata_records)
+                                      message_group, message_testsuite_group, userdata_attribute_group,
+                                      userdata_records)
 from test_named_spaces import NFLOATS, check, inputs, spaces_group  # noqa: E402
 
 
@@ -113,3 +114,20 @@ def test_userdata_attributes_match_oracle(jit):
     assert_same(got, ref)
     check_userdata_attributes(got, ud)
     assert ss.device_status() == 0
+
+
+@pytest.mark.parametrize("jit", [0, 1])
+def test_message_testsuite_case_matches_oracle(jit):
+    """color, float[4] and int messages and their error cases on the GPU"""
+    ss = og.ShadingSystem()
+    if jit:
+        ss.attribute("jit", 1)
+    g, rec = message_testsuite_group(ss)
+    n = 777
+    Nv = np.random.default_rng(2).normal(size=(3, n)).astype(np.float32)
+    dN = dev(Nv)
+    got = gpu_run(ss, g, n, og.make_globals(N=dN, u=0.25, v=0.75), rec, sync=False)
+    ref = np.zeros((n, rec), np.float32)
+    st = oracle_run(g.program_bytes(), n, og.make_globals(N=Nv, u=0.25, v=0.75), ref)
+    assert_same(got, ref)
+    assert ss.device_status() == st and st != 0

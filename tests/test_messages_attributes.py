@@ -394,15 +394,9 @@ def test_userdata_parameter_derivatives(with_derivs):
     assert np.array_equal(out[:, 1], ud[:, 1] if with_derivs else np.zeros(n, np.float32))
 
 
-def test_message_no_closure_testsuite_case():
-    """testsuite/message-no-closure (a.osl -> b.osl, optimized: ref
-    out-opt.txt): the color message 'foo' = c_out / 2 = (0.125, 0.5, 0.5)
-    arrives; 'bar' was never sent (0, destination unchanged); 'foo' read as
-    a float is a type mismatch (0, unchanged); the float[4] message arrives
-    whole; a query before any send is folded away, so setting the message
-    afterwards is no error; a message set and read in the same layer
-    arrives; setting twice and reading as another type are errors."""
-    ss = og.ShadingSystem()
+def message_testsuite_group(ss):
+    """testsuite/message-no-closure's a.osl -> b.osl as a group; returns
+    (group, floats per output record)."""
     a = og.OsoBuilder("msg_a")
     S = lambda b, s: b.const("string", s)
     kd = a.param("float", "Kd", 0.5)
@@ -470,6 +464,19 @@ def test_message_no_closure_testsuite_case():
         locs.append(og.SymLocationDesc(nm, ty, False, og.SymArenaOutputs, off, 4 * 17))
         off += 4 * nw
     ss.add_symlocs(g, locs)
+    return g, 17
+
+
+def test_message_no_closure_testsuite_case():
+    """testsuite/message-no-closure (a.osl -> b.osl, optimized: ref
+    out-opt.txt): the color message 'foo' = c_out / 2 = (0.125, 0.5, 0.5)
+    arrives; 'bar' was never sent (0, destination unchanged); 'foo' read as
+    a float is a type mismatch (0, unchanged); the float[4] message arrives
+    whole; a query before any send is folded away, so setting the message
+    afterwards is no error; a message set and read in the same layer
+    arrives; setting twice and reading as another type are errors."""
+    ss = og.ShadingSystem()
+    g, rec = message_testsuite_group(ss)
     n = 16
     Nv = np.random.default_rng(2).normal(size=(3, n)).astype(np.float32)
     out = np.zeros((n, 17), np.float32)
