@@ -229,3 +229,30 @@ def test_splineinverse_identity_image():
     got = to_uint8(out.reshape(H, W, 3))[::step, ::step]
     ok, frac, mx = image_diff_ok(got, ref)
     assert ok and frac == 0.0 and mx == 0.0, (frac, mx)  # every sampled pixel exact
+
+
+def test_spline_with_too_few_knots_reports_bounds():
+    """A knot count below four (here a varying count of 3) has no segment:
+    the result is 0 and the index-out-of-range status bit is set, for spline
+    and splineinverse alike."""
+    ss = og.ShadingSystem()
+    b = og.OsoBuilder("fewknots")
+    r1 = b.param("float", "r1", 9.0, output=True)
+    r2 = b.param("float", "r2", 9.0, output=True)
+    u = b.glob("float", "u")
+    kn = b.param("float[6]", "kn", [0.0, 0.1, 0.2, 0.3, 0.4, 0.5])
+    cnt = b.tmp("int")
+    b.op("assign", cnt, b.const("int", 3))
+    lin = b.const("string", "linear")
+    b.op("spline", r1, lin, u, cnt, kn)
+    b.op("splineinverse", r2, lin, u, cnt, kn)
+    ss.LoadMemoryCompiledShader("fewknots", b.text())
+    g = ss.ShaderGroupBegin("gfew")
+    ss.Shader(g, "surface", "fewknots", "l")
+    ss.ShaderGroupEnd(g)
+    ss.add_symlocs(g, [og.SymLocationDesc("l.r1", og.TypeFloat, False, og.SymArenaOutputs, 0, 8),
+                       og.SymLocationDesc("l.r2", og.TypeFloat, False, og.SymArenaOutputs, 4, 8)])
+    u, v = pixel_grid(8, 1)
+    out = np.zeros((8, 2), np.float32)
+    st = oracle_run(g.program_bytes(), 8, grid_globals(u, v, 8, 1), out)
+    assert st & 4 and np.all(out == 0.0)
