@@ -179,6 +179,7 @@ IMAGES = {
     "spline_float": "testsuite/spline/ref/float.tif",
     "spline_dfloat": "testsuite/spline/ref/dfloat.tif",
     "spline_numknots": "testsuite/spline/ref/numknots.tif",
+    "spline_constcolor": "testsuite/spline/ref/constcolor.tif",
     "spline_nonuniform": "testsuite/spline-nonuniformknots/ref/out.tif",
     "splineinverse_ident": "testsuite/splineinverse-ident/ref/out.tif",
 }

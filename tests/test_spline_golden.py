@@ -256,3 +256,31 @@ def test_spline_with_too_few_knots_reports_bounds():
     out = np.zeros((8, 2), np.float32)
     st = oracle_run(g.program_bytes(), 8, grid_globals(u, v, 8, 1), out)
     assert st & 4 and np.all(out == 0.0)
+
+
+def test_constant_and_linear_color_spline_image():
+    """testsuite/spline constspline (constcolor.tif): 9 color knots,
+    "constant" basis in the lower half (v < 0.5), "linear" in the upper."""
+    cols = [0, 0, 0, 0, 0, 1, 0, 1, 0, 0, 1, 1, 1, 0, 0, 1, 0, 1, 1, 1, 0, 1, 1, 1, 0, 0, 0]
+    ref, W, H, step = golden_image("spline_constcolor")
+    u, v = pixel_grid(W, H)
+    out = np.zeros((W * H, 3), np.float32)
+    for basis, sel in (("constant", v < 0.5), ("linear", v >= 0.5)):
+        ss = og.ShadingSystem()
+        b = og.OsoBuilder("cspl_" + basis)
+        cs = b.param("color", "Cspline", 0.0, output=True)
+        kn = b.param("color[9]", "colors", [float(c) for c in cols])
+        b.op("spline", cs, b.const("string", basis), b.glob("float", "u"), kn)
+        ss.LoadMemoryCompiledShader("cspl_" + basis, b.text())
+        g = ss.ShaderGroupBegin("gcspl_" + basis)
+        ss.Shader(g, "surface", "cspl_" + basis, "l")
+        ss.ShaderGroupEnd(g)
+        ss.add_symlocs(g, [og.SymLocationDesc("l.Cspline", og.TypeColor, False, og.SymArenaOutputs, 0, 12)])
+        idx = np.nonzero(sel)[0]
+        part = np.zeros((len(idx), 3), np.float32)
+        G = grid_globals(np.ascontiguousarray(u[idx]), np.ascontiguousarray(v[idx]), W, H)
+        assert oracle_run(g.program_bytes(), len(idx), G, part) == 0
+        out[idx] = part
+    got = to_uint8(out.reshape(H, W, 3))[::step, ::step]
+    ok, frac, mx = image_diff_ok(got, ref)
+    assert ok and frac == 0.0 and mx == 0.0, (frac, mx)
