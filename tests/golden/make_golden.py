@@ -180,6 +180,10 @@ IMAGES = {
     "spline_dfloat": "testsuite/spline/ref/dfloat.tif",
     "spline_numknots": "testsuite/spline/ref/numknots.tif",
     "spline_constcolor": "testsuite/spline/ref/constcolor.tif",
+    "spline_derivbug_color": "testsuite/spline-derivbug/ref/color.tif",
+    "spline_derivbug_dx": "testsuite/spline-derivbug/ref/dx.tif",
+    "spline_derivbug_dx_alt": "testsuite/spline-derivbug/ref/dx-oiio2.2.tif",
+    "spline_derivbug_dy": "testsuite/spline-derivbug/ref/dy.tif",
     "spline_nonuniform": "testsuite/spline-nonuniformknots/ref/out.tif",
     "splineinverse_ident": "testsuite/splineinverse-ident/ref/out.tif",
 }

@@ -284,3 +284,40 @@ def test_constant_and_linear_color_spline_image():
     got = to_uint8(out.reshape(H, W, 3))[::step, ::step]
     ok, frac, mx = image_diff_ok(got, ref)
     assert ok and frac == 0.0 and mx == 0.0, (frac, mx)
+
+
+@pytest.mark.parametrize("name,cols,alts", [("spline_derivbug_color", slice(0, 3), ()),
+                                            ("spline_derivbug_dx", slice(3, 6), ("spline_derivbug_dx_alt",)),
+                                            ("spline_derivbug_dy", slice(6, 9), ())])
+def test_spline_derivatives_image(name, cols, alts):
+    """testsuite/spline-derivbug (testshade -g 64 64): a bspline over 8
+    color knots with an explicit knot count; Cout, 0.5 + 10 Dx(Cout),
+    0.5 + 10 Dy(Cout)."""
+    vals = [0, 0, 0, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 1, 1, 1, 1, 1, 1, 1, 1]
+    b = og.OsoBuilder("derivbug")
+    cout = b.param("color", "Cout", 0.0, output=True)
+    cdx = b.param("color", "Cout_dx", 0.0, output=True)
+    cdy = b.param("color", "Cout_dy", 0.0, output=True)
+    kn = b.param("color[8]", "values", [float(x) for x in vals])
+    b.op("spline", cout, b.const("string", "bspline"), b.glob("float", "u"), b.const("int", 8), kn)
+    for out, op in ((cdx, "Dx"), (cdy, "Dy")):
+        d, t = b.tmp("color"), b.tmp("color")
+        b.op(op, d, cout)
+        b.op("mul", t, b.const("float", 10.0), d)
+        b.op("add", out, b.const("float", 0.5), t)
+    ss = og.ShadingSystem()
+    ss.LoadMemoryCompiledShader("derivbug", b.text())
+    g = ss.ShaderGroupBegin("gderivbug")
+    ss.Shader(g, "surface", "derivbug", "l")
+    ss.ShaderGroupEnd(g)
+    ss.add_symlocs(g, [og.SymLocationDesc("l." + nm, og.TypeColor, False, og.SymArenaOutputs, 12 * i, 36)
+                       for i, nm in enumerate(("Cout", "Cout_dx", "Cout_dy"))])
+    ref, W, H, step = golden_image(name)
+    u, v = pixel_grid(W, H)
+    out = np.zeros((W * H, 9), np.float32)
+    assert oracle_run(g.program_bytes(), W * H, grid_globals(u, v, W, H), out) == 0
+    results = []
+    for fixture in (name,) + alts:
+        r, W, H, step = golden_image(fixture)
+        results.append(image_diff_ok(to_uint8(out.reshape(H, W, 9)[:, :, cols])[::step, ::step], r))
+    assert any(r[0] for r in results), (name, [(r[1], r[2]) for r in results])
