@@ -4,8 +4,8 @@
  * This is the drop-in boundary for OSL's data-parallel hot path: running an
  * optimized ShaderGroup over many shading points. Each entry point replaces
  * one member of the reference's C++ API (paths relative to the
- * OpenShadingLanguage source tree); the C++ facade and the ctypes binding
- * in INTEGRATION.md bind to exactly these symbols.
+ * OpenShadingLanguage source tree); the C++ facade (oslg.hpp) and the
+ * Python ctypes binding bind to exactly these symbols.
  *
  * Conventions: plain pointers and sizes only; every call returns an int
  * status (OSLG_OK == 0) and the message of the last failure is available
@@ -114,6 +114,9 @@ int oslg_destroy_system(oslg_system* sys);
  * specialized kernels: 256-thread CTAs per SM that must fit, 2..8),
  * "strict_messages", "opt_constant_fold", "opt_elide_useless_ops" (as the
  * reference's ShadingSystem attributes of those names, shadingsys.cpp:1639-1684),
+ * "max_loop_iterations" (loop back edges one point may take, summed over
+ * the group's loops, before the launch ends with the loop-limit status
+ * bit; 0 keeps the default 2^24; the reference has no such limit),
  * "host_direct_outputs" (host-buffer execution writes pinned output records
  * from the kernel, 1 by default). */
 int oslg_attribute_int(oslg_system* sys, const char* name, int value);
@@ -276,7 +279,8 @@ int oslg_execute_batch_sync(oslg_system* sys, oslg_group* group, int64_t npoints
                             const oslg_shaderglobals* globals, void* userdata_base,
                             void* output_base, void* stream);
 
-/* Status bits raised by kernels since the last call (and clears them). */
+/* Status bits raised by kernels since the last call (and clears them),
+ * including those of allocation-free calls that did not collect theirs. */
 int oslg_device_status(oslg_system* sys, uint32_t* bits);
 
 /* Launch shape the next execute uses: threads per block, points per
@@ -293,12 +297,19 @@ int oslg_set_launch(oslg_system* sys, int block, int points_per_thread, int heap
  * lowered program must be at most 64 KiB and one CTA's symbol heap must fit
  * the rest of the array (otherwise OSLG_ERR_ARG with a message). The group
  * must already be lowered (oslg_optimize_group), else OSLG_ERR_STATE.
+ * A group that calls texture() or environment() reads the system's texture
+ * table, which only the allocating entries upload: it runs here once a
+ * group of this system has gone through oslg_execute_batch after the
+ * textures were registered, and is refused with OSLG_ERR_STATE before.
  * The first call on a device does a one-time set-up (resolves the array's
- * device address, uploads a constant table); make that first call before
- * any stream capture. Calls share the array and leave their contents in it
- * (the status word is cleared at the start of each call); calls that
- * overlap on the GPU race. With status_out == NULL the call only enqueues
- * work; otherwise it waits for the stream, stores the kernel status bits
+ * device address and sets the kernels' shared-memory limit); make that
+ * first call before any stream capture. Calls share the array and leave
+ * their contents in it: the status word is cleared at the start of each
+ * call and the program is copied in only when it differs from the one the
+ * last call on the same stream left there. Calls that overlap on the GPU
+ * race. With status_out == NULL the call only enqueues work and the status
+ * bits stay in the array, where oslg_device_status reads (and clears)
+ * them; otherwise it waits for the stream, stores the kernel status bits
  * and returns OSLG_ERR_DEVICE if any is set. */
 int oslg_execute_batch_noalloc(oslg_system* sys, oslg_group* group, int64_t npoints,
                                const oslg_shaderglobals* globals, void* userdata_base,

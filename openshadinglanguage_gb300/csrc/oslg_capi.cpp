@@ -193,6 +193,10 @@ int oslg_attribute_int(oslg_system* sys, const char* name, int value) {
     std::string n(name);
     if (n == "max_closure_components") sys->ss.opts.max_closure_components = value;
     else if (n == "max_closure_terms") sys->ss.opts.max_closure_terms = value;
+    else if (n == "max_loop_iterations") {
+        if (value < 0) return fail(sys, OSLG_ERR_ARG, "max_loop_iterations must be >= 0");
+        sys->ss.opts.max_loop_iterations = value;
+    }
     else if (n == "gpu_block") sys->launch.block = value;
     else if (n == "gpu_points_per_thread") sys->launch.points_per_thread = value;
     else if (n == "gpu_heap_placement") sys->launch.heap_smem = value;
@@ -919,6 +923,11 @@ int oslg_device_status(oslg_system* sys, uint32_t* bits) {
     std::string err;
     int rc = device_read_status(sys->dev, nullptr, bits, &err);
     if (rc != OSLG_OK) return fail(sys, rc, err);
+    // bits the allocation-free entry left when its caller did not ask for them
+    uint32_t na = 0;
+    rc = noalloc_read_status(nullptr, &na, &err);
+    if (rc != OSLG_OK) return fail(sys, rc, err);
+    *bits |= na;
     return OSLG_OK;
 }
 
@@ -939,11 +948,26 @@ int oslg_execute_batch_noalloc(oslg_system* sys, oslg_group* group, int64_t npoi
     ShaderGroup& g = group->g;
     std::lock_guard<std::mutex> lock(g.mutex);
     if (!g.compiled) return fail(sys, OSLG_ERR_STATE, "group must be lowered with oslg_optimize_group first");
+    // texture() and environment() read the system's descriptor table, which
+    // only the allocating entries upload (it takes device memory)
+    int max_tex = -1;
+    {
+        const CompiledGroup& cg = *g.compiled;
+        const Op* ops = reinterpret_cast<const Op*>(cg.blob.data() + sizeof(ProgramHeader));
+        for (uint32_t i = 0; i < cg.header.nops; ++i)
+            if (ops[i].code == OP_TEXTURE || ops[i].code == OP_ENVIRONMENT)
+                max_tex = std::max(max_tex, (int)(ops[i].a[3] & 0xFFu));
+    }
+    if (max_tex >= 0 && (sys->textures_dirty || !sys->dev.d_textures || max_tex >= sys->dev.ntextures))
+        return fail(sys, OSLG_ERR_STATE,
+                    "group looks up textures that are not in device memory yet: run a group of this system through "
+                    "oslg_execute_batch once after registering them");
     std::string err;
     uint32_t bits = 0;
     int rc = device_execute_noalloc(g.compiled->blob.data(), g.compiled->blob.size(), g.compiled->header, npoints,
                                     *globals, userdata_base, output_base, stream, sys->launch,
-                                    status_out ? &bits : nullptr, &err);
+                                    max_tex >= 0 ? sys->dev.d_textures : nullptr,
+                                    max_tex >= 0 ? sys->dev.ntextures : 0, status_out ? &bits : nullptr, &err);
     if (rc != OSLG_OK) return fail(sys, rc, err);
     if (status_out) {
         *status_out = bits;

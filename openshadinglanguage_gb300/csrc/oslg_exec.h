@@ -34,6 +34,7 @@ struct BatchJob {
     oslg_shaderglobals G;
     int32_t spec_case;    // program index inside a specialized batch kernel
     int32_t pad_;
+    uint32_t* status;     // this job's status word (null: the launch's BatchArgs::status)
 };
 // Arguments of the persistent batch kernel: items are (job, tile) pairs,
 // taken in order through *counter (reset to 0 before every launch).
@@ -112,8 +113,14 @@ int device_init(DeviceState& ds, std::string* err);
 // program blob into it, launches, and optionally waits and reports status.
 static const size_t kNoAllocScratchBytes = 32u << 20;  // whole static array
 static const size_t kNoAllocProgramBytes = 64u << 10;  // program area
+// Texture lookups read `textures` (a descriptor table already in device
+// memory, or null when the program looks up none).
 int device_execute_noalloc(const void* blob, size_t blob_bytes, const ProgramHeader& hdr, int64_t npoints,
                            const oslg_shaderglobals& G, void* userdata, void* outputs, void* stream,
-                           const LaunchConfig& cfg, uint32_t* status_out, std::string* err);
+                           const LaunchConfig& cfg, const TexDesc* textures, int32_t ntextures,
+                           uint32_t* status_out, std::string* err);
+// Read and clear the allocation-free entry's status word on the current
+// device (0 when that entry never ran there); synchronises the stream.
+int noalloc_read_status(void* stream, uint32_t* bits, std::string* err);
 
 }  // namespace oslg

@@ -189,6 +189,7 @@ struct SystemOptions {
     int opt_elide_useless_ops = 1;   // "opt_elide_useless_ops" (shadingsys.cpp:1643)
     int max_closure_components = 16;  // closure tree nodes per point
     int max_closure_terms = 16;
+    int max_loop_iterations = 0;  // loop back edges per point (0: the program format's default)
     int heap_in_smem = -1;  // -1 auto
     int threads_per_block = 256;
     int points_per_thread = 1;

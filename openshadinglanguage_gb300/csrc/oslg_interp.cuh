@@ -2028,7 +2028,6 @@ static __device__ void h_spline(const Lane& L, const uint32_t* a, uint32_t* st) 
 __device__ __forceinline__ bool bit(uint32_t m, int d) { return (m >> d) & 1u; }
 __device__ __forceinline__ uint32_t setbit(uint32_t m, int d, bool v) { return v ? (m | (1u << d)) : (m & ~(1u << d)); }
 
-static const long long kMaxBackEdges = 1ll << 24;
 
 // Feature tiers: a program only pays (in code size and instruction-cache
 // footprint) for the op families it uses. TIER bits: 1 noise/hash, 2
@@ -2053,14 +2052,16 @@ struct RunCtx {
     char* userdata;
     char* outputs;
     uint32_t* status;
+    uint32_t max_iters = kDefaultMaxLoopIterations;  // loop back edges per point
 };
 
 // Control state of the masked walk: per thread, PPT points with their
-// active / valid / exited / returned bits and per-depth if and loop stacks.
+// active / valid / exited / returned bits, per-depth if and loop stacks and
+// the loop back edges each point has taken.
 template <int PPT>
 struct Ctl {
     uint32_t validm, actm, extm, lretm;
-    uint32_t stk[PPT], cnd[PPT], brk[PPT], cnt[PPT];
+    uint32_t stk[PPT], cnd[PPT], brk[PPT], cnt[PPT], iters[PPT];
 };
 
 template <int PPT>
@@ -2072,7 +2073,7 @@ __device__ __forceinline__ void ctl_init(Ctl<PPT>& C, const RunCtx& R, Lane& L, 
     C.lretm = 0;
 #pragma unroll
     for (int j = 0; j < PPT; ++j) {
-        C.stk[j] = C.cnd[j] = C.brk[j] = C.cnt[j] = 0;
+        C.stk[j] = C.cnd[j] = C.brk[j] = C.cnt[j] = C.iters[j] = 0;
         if (pt0 + (int64_t)j * blockDim.x < npoints) C.validm |= 1u << j;
     }
     C.actm = C.validm;
@@ -2197,6 +2198,20 @@ __device__ __forceinline__ void ctl_continue(Ctl<PPT>& C, const uint32_t* a) {
         if (((C.actm >> j) & 1u) && ll) C.cnt[j] = setbit(C.cnt[j], ll - 1, true);
     C.actm = 0;
 }
+// A loop's back edge: each point still iterating counts one. When a point
+// passes `cap`, it raises ST_TIMEOUT and the whole warp stops its walk (the
+// decision is warp-uniform, as the program counter is); returns true then.
+template <int PPT>
+__device__ __forceinline__ bool ctl_back_edge(Ctl<PPT>& C, const RunCtx& R, uint32_t cap) {
+    bool over = false;
+#pragma unroll
+    for (int j = 0; j < PPT; ++j)
+        if (((C.actm >> j) & 1u) && ++C.iters[j] > cap) over = true;
+    if (!__any_sync(FULL, over)) return false;
+    if (over) raise_status(R.status, ST_TIMEOUT);
+    return true;
+}
+
 template <int PPT>
 __device__ __forceinline__ void ctl_return(Ctl<PPT>& C) { C.lretm |= C.actm; C.actm = 0; }
 template <int PPT>
@@ -2380,14 +2395,13 @@ __device__ __forceinline__ void run_tile(const RunCtx& R, Lane& L, int64_t npoin
     const uint32_t li0 = L.li;
     const int64_t pt0 = L.pt;
     uint32_t validm = 0, actm, extm = 0, lretm = 0;
-    uint32_t stk[PPT], cnd[PPT], brk[PPT], cnt[PPT];
+    uint32_t stk[PPT], cnd[PPT], brk[PPT], cnt[PPT], iters[PPT];
 #pragma unroll
     for (int j = 0; j < PPT; ++j) {
-        stk[j] = cnd[j] = brk[j] = cnt[j] = 0;
+        stk[j] = cnd[j] = brk[j] = cnt[j] = iters[j] = 0;
         if (pt0 + (int64_t)j * blockDim.x < npoints) validm |= 1u << j;
     }
     actm = validm;
-    long long backedges = 0;
     if (R.uses_closures) {
 #pragma unroll
         for (int j = 0; j < PPT; ++j)
@@ -2483,10 +2497,16 @@ __device__ __forceinline__ void run_tile(const RunCtx& R, Lane& L, int64_t npoin
             break;
         }
         case OP_JUMP: {
-            if (++backedges > kMaxBackEdges) {
-                if (threadIdx.x % 32 == 0) raise_status(R.status, ST_TIMEOUT);
-                pc = R.nops;
-                continue;
+            if (a[2] <= (uint32_t)pc) {  // a loop's back edge (as ctl_back_edge)
+                bool over = false;
+#pragma unroll
+                for (int j = 0; j < PPT; ++j)
+                    if (((actm >> j) & 1u) && ++iters[j] > R.max_iters) over = true;
+                if (__any_sync(FULL, over)) {
+                    if (over) raise_status(R.status, ST_TIMEOUT);
+                    pc = R.nops;
+                    continue;
+                }
             }
             pc = (int)a[2];
             continue;
@@ -2574,6 +2594,7 @@ __global__ void __launch_bounds__(256, 2) interp_kernel(const __grid_constant__ 
     R.status = k.status;
     R.textures = k.textures;
     R.ntextures = k.ntextures;
+    R.max_iters = max_loop_iterations(*H);
 
     Lane L;
     L.pool = spool;
@@ -2634,9 +2655,10 @@ __global__ void __launch_bounds__(MAXT, 512 / MAXT) batch_kernel(const __grid_co
             R.G = &J->G;
             R.userdata = J->userdata;
             R.outputs = J->outputs;
-            R.status = b.status;
+            R.status = J->status ? J->status : b.status;
             R.textures = b.textures;
             R.ntextures = b.ntextures;
+            R.max_iters = max_loop_iterations(*H);
             L.pool = spool;
             cur = (int)w.x;
         }

@@ -8,6 +8,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "oslg_exec.h"
 
@@ -171,8 +172,10 @@ int device_read_status(DeviceState& ds, void* stream, uint32_t* bits, std::strin
 //   [256, 256 + 64 KiB)           copy of the lowered program
 //   [256 + 64 KiB, 32 MiB)        symbol heap, one slice per resident CTA
 // Every call shares the array and leaves its contents behind; the status
-// word is cleared at the start of each call. Calls that overlap on the GPU
-// (different streams, or the same group from two host threads) race on it.
+// word is cleared at the start of each call, and the program is copied in
+// only when it differs from the one the last call on that stream left
+// there. Calls that overlap on the GPU (different streams, or the same
+// group from two host threads) race on it.
 namespace dev {
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 }
@@ -183,6 +186,8 @@ struct NoAllocDevice {
     unsigned char* base = nullptr;
     int sm_count = 0;
     int smem_optin = 0;
+    std::vector<unsigned char> resident;  // host copy of the program in the array
+    void* resident_stream = nullptr;      // the stream that copied it
 };
 std::mutex g_noalloc_mutex;
 NoAllocDevice g_noalloc_dev[128];
@@ -209,7 +214,8 @@ int noalloc_setup(int dev, NoAllocDevice& d, std::string* err) {
 
 int device_execute_noalloc(const void* blob, size_t blob_bytes, const ProgramHeader& hdr, int64_t npoints,
                            const oslg_shaderglobals& G, void* userdata, void* outputs, void* stream,
-                           const LaunchConfig& cfg, uint32_t* status_out, std::string* err) {
+                           const LaunchConfig& cfg, const TexDesc* textures, int32_t ntextures,
+                           uint32_t* status_out, std::string* err) {
     if (status_out) *status_out = 0;
     if (blob_bytes > kNoAllocProgramBytes) {
         if (err) *err = "program is " + std::to_string(blob_bytes) + " bytes; the allocation-free entry holds at most "
@@ -260,8 +266,17 @@ int device_execute_noalloc(const void* blob, size_t blob_bytes, const ProgramHea
     float* heap = reinterpret_cast<float*>(d->base + 256 + kNoAllocProgramBytes);
     if (!cuda_ok(cudaMemsetAsync(status, 0, sizeof(uint32_t), s), err, "clear status")) return OSLG_ERR_CUDA;
     if (npoints > 0) {
-        if (!cuda_ok(cudaMemcpyAsync(prog, blob, blob_bytes, cudaMemcpyHostToDevice, s), err, "program copy"))
-            return OSLG_ERR_CUDA;
+        {
+            std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+            const unsigned char* b = static_cast<const unsigned char*>(blob);
+            if (d->resident_stream != stream || d->resident.size() != blob_bytes ||
+                std::memcmp(d->resident.data(), b, blob_bytes) != 0) {
+                if (!cuda_ok(cudaMemcpyAsync(prog, blob, blob_bytes, cudaMemcpyHostToDevice, s), err, "program copy"))
+                    return OSLG_ERR_CUDA;
+                d->resident.assign(b, b + blob_bytes);
+                d->resident_stream = stream;
+            }
+        }
         dev::KArgs k;
         k.blob = prog;
         k.npoints = npoints;
@@ -270,6 +285,8 @@ int device_execute_noalloc(const void* blob, size_t blob_bytes, const ProgramHea
         k.gheap = heap;
         k.status = status;
         k.G = G;
+        k.textures = textures;
+        k.ntextures = ntextures;
         if (!cuda_ok((cudaError_t)fns.launch(false, (unsigned)grid, (unsigned)block, static_bytes, stream, k), err,
                      "launch"))
             return OSLG_ERR_CUDA;
@@ -281,6 +298,26 @@ int device_execute_noalloc(const void* blob, size_t blob_bytes, const ProgramHea
         if (!cuda_ok(cudaStreamSynchronize(s), err, "sync")) return OSLG_ERR_CUDA;
         *status_out = v;
     }
+    return OSLG_OK;
+}
+
+int noalloc_read_status(void* stream, uint32_t* bits, std::string* err) {
+    *bits = 0;
+    int devid = 0;
+    if (!cuda_ok(cudaGetDevice(&devid), err, "cudaGetDevice")) return OSLG_ERR_CUDA;
+    if (devid < 0 || devid >= 128) return OSLG_OK;
+    unsigned char* base = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+        if (g_noalloc_dev[devid].ready) base = g_noalloc_dev[devid].base;
+    }
+    if (!base) return OSLG_OK;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    uint32_t v = 0;
+    if (!cuda_ok(cudaMemcpyAsync(&v, base, 4, cudaMemcpyDeviceToHost, s), err, "status copy")) return OSLG_ERR_CUDA;
+    if (!cuda_ok(cudaMemsetAsync(base, 0, 4, s), err, "status clear")) return OSLG_ERR_CUDA;
+    if (!cuda_ok(cudaStreamSynchronize(s), err, "sync")) return OSLG_ERR_CUDA;
+    *bits = v;
     return OSLG_OK;
 }
 

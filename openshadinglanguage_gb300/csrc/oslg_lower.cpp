@@ -2056,6 +2056,7 @@ struct Lowerer {
         for (const GSym& s : syms)
             if (s.referenced && s.derivs) h.flags |= 2u;
         h.max_depth = max_depth;
+        h.max_loop_iterations = (uint32_t)ss.opts.max_loop_iterations;
         h.flags |= program_tier() << 8;
         if (h.heap_slots > kArgOffsetMask) return fail("symbol heap too large");
         out.header = h;

@@ -208,9 +208,24 @@ struct ProgramHeader {
     uint32_t max_comps;     // closure node pool capacity
     uint32_t max_terms;     // unused
     uint32_t max_depth;     // deepest if/loop nesting (<= 32)
-    uint32_t reserved[6];
+    uint32_t max_loop_iterations;  // loop back edges one point may take (0: kDefaultMaxLoopIterations)
+    uint32_t reserved[5];
 };
 static_assert(sizeof(ProgramHeader) == 64, "header must be 64 bytes");
+
+// A point that takes more loop back edges than this (summed over every loop
+// of the program) ends with ST_TIMEOUT instead of running on: the device
+// and the oracle count the same thing, one per iteration a point starts
+// again. The reference has no such limit (a shader that never leaves a
+// loop hangs the renderer); the system attribute "max_loop_iterations"
+// overrides the default per lowered program.
+static const uint32_t kDefaultMaxLoopIterations = 1u << 24;
+#ifdef __CUDACC__
+__host__ __device__
+#endif
+inline uint32_t max_loop_iterations(const ProgramHeader& h) {
+    return h.max_loop_iterations ? h.max_loop_iterations : kDefaultMaxLoopIterations;
+}
 
 // Texture wrap modes (OP_TEXTURE), the names of OIIO's TextureOpt::Wrap.
 enum TexWrap : uint32_t { TW_PERIODIC = 0, TW_CLAMP = 1, TW_BLACK = 2, TW_MIRROR = 3 };

@@ -153,7 +153,9 @@ int ShadingServer::start_resources(std::string* err) {
             !ok(cudaMalloc(&s.d_items, items_cap * sizeof(uint2)), err, "cudaMalloc items") ||
             !ok(cudaMalloc(&s.d_counter, sizeof(uint32_t)), err, "cudaMalloc counter") ||
             !ok(cudaMallocHost(&s.h_jobs, opt_.max_wave_requests * sizeof(dev::BatchJob)), err, "pinned jobs") ||
-            !ok(cudaMallocHost(&s.h_items, items_cap * sizeof(uint2)), err, "pinned items"))
+            !ok(cudaMallocHost(&s.h_items, items_cap * sizeof(uint2)), err, "pinned items") ||
+            !ok(cudaMalloc(&s.d_status, opt_.max_wave_requests * sizeof(uint32_t)), err, "cudaMalloc status") ||
+            !ok(cudaMallocHost(&s.h_status, opt_.max_wave_requests * sizeof(uint32_t)), err, "pinned status"))
             return OSLG_ERR_CUDA;
         s.items_cap = items_cap;
         s.heap_bytes = scratch_each;
@@ -185,6 +187,8 @@ void ShadingServer::release_resources() {
         cudaFree(s.d_heap);
         cudaFreeHost(s.h_jobs);
         cudaFreeHost(s.h_items);
+        cudaFree(s.d_status);
+        cudaFreeHost(s.h_status);
         if (s.stream) cudaStreamDestroy(static_cast<cudaStream_t>(s.stream));
     }
     slots_.clear();
@@ -264,7 +268,13 @@ void ShadingServer::on_wave_done(void* p) {
     ShadingServer* self = s->owner;
     int64_t t = now_ns();
     std::lock_guard<std::mutex> lk(self->mu_);
-    for (Request* r : s->reqs) r->st.done_ns = t;
+    for (Request* r : s->reqs) {
+        r->st.done_ns = t;
+        // a job that raised a status bit (closure overflow, index bounds,
+        // loop limit) fails its own request only
+        r->bits = s->h_status[r->job];
+        if (r->bits) r->st.status = OSLG_ERR_DEVICE;
+    }
     s->complete = true;
     self->cv_.notify_all();
 }
@@ -342,6 +352,8 @@ int ShadingServer::launch_wave(Slot& s, std::vector<Request*>& wave, std::string
         // the same in every mix
         if (!ok(cudaMemsetAsync(d_out, 0, r->out_bytes, st), err, "output clear")) return OSLG_ERR_CUDA;
         dev::BatchJob& J = s.h_jobs[j];
+        r->job = (int)j;
+        J.status = s.d_status + j;
         J.blob = static_cast<const uint8_t*>(r->cg->d_blob);
         J.npoints = r->n;
         J.userdata = nullptr;
@@ -354,7 +366,8 @@ int ShadingServer::launch_wave(Slot& s, std::vector<Request*>& wave, std::string
             "jobs copy") ||
         !ok(cudaMemcpyAsync(s.d_items, s.h_items, nitems * sizeof(uint2), cudaMemcpyHostToDevice, st), err,
             "items copy") ||
-        !ok(cudaMemsetAsync(s.d_counter, 0, sizeof(uint32_t), st), err, "counter reset"))
+        !ok(cudaMemsetAsync(s.d_counter, 0, sizeof(uint32_t), st), err, "counter reset") ||
+        !ok(cudaMemsetAsync(s.d_status, 0, order.size() * sizeof(uint32_t), st), err, "status clear"))
         return OSLG_ERR_CUDA;
     dev::BatchArgs a;
     a.jobs = s.d_jobs;
@@ -377,6 +390,9 @@ int ShadingServer::launch_wave(Slot& s, std::vector<Request*>& wave, std::string
         if (!ok(cudaMemcpyAsync(r->host_out, d_out, r->out_bytes, cudaMemcpyDeviceToHost, st), err, "output copy"))
             return OSLG_ERR_CUDA;
     }
+    if (!ok(cudaMemcpyAsync(s.h_status, s.d_status, order.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost, st), err,
+            "status copy"))
+        return OSLG_ERR_CUDA;
     if (!ok(cudaLaunchHostFunc(st, &ShadingServer::on_wave_done, &s), err, "completion callback"))
         return OSLG_ERR_CUDA;
     return OSLG_OK;
@@ -393,8 +409,12 @@ void ShadingServer::worker() {
                 for (Request* r : s.reqs) {
                     arena_.free(r->dev_off, r->dev_bytes);
                     r->done = true;
-                    stats_.completed++;
-                    stats_.points_done += r->n;
+                    if (r->st.status != OSLG_OK) {
+                        stats_.failed++;
+                    } else {
+                        stats_.completed++;
+                        stats_.points_done += r->n;
+                    }
                 }
                 s.reqs.clear();
                 s.busy = false;
@@ -477,9 +497,11 @@ int ShadingServer::wait(uint64_t ticket, int timeout_ms, RequestStats* st, std::
     }
     if (st) *st = r->st;
     int status = r->st.status;
+    const uint32_t bits = r->bits;
     reqs_.erase(it);
     delete r;
-    if (status != OSLG_OK && err) *err = "request failed: " + worker_error_;
+    if (status != OSLG_OK && err)
+        *err = bits ? "request failed: kernel status bits " + std::to_string(bits) : "request failed: " + worker_error_;
     return status;
 }
 
@@ -495,9 +517,11 @@ int ShadingServer::poll(uint64_t ticket, bool* done, RequestStats* st, std::stri
     if (!r->done) return OSLG_OK;
     if (st) *st = r->st;
     int status = r->st.status;
+    const uint32_t bits = r->bits;
     reqs_.erase(it);
     delete r;
-    if (status != OSLG_OK && err) *err = "request failed: " + worker_error_;
+    if (status != OSLG_OK && err)
+        *err = bits ? "request failed: kernel status bits " + std::to_string(bits) : "request failed: " + worker_error_;
     return status;
 }
 

@@ -95,6 +95,8 @@ private:
         size_t dev_off = 0, dev_bytes = 0;
         RequestStats st;
         bool done = false;
+        int job = 0;          // index of its job in the wave's launch
+        uint32_t bits = 0;    // kernel status bits its job raised
     };
     struct Slot {
         void* stream = nullptr;
@@ -105,6 +107,8 @@ private:
         size_t heap_bytes = 0;
         dev::BatchJob* h_jobs = nullptr;  // pinned staging
         uint2* h_items = nullptr;
+        uint32_t* d_status = nullptr;  // one status word per job of the wave
+        uint32_t* h_status = nullptr;  // pinned copy, read by the completion callback
         size_t items_cap = 0;
         std::vector<Request*> reqs;
         bool busy = false;

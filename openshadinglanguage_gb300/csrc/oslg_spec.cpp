@@ -181,8 +181,8 @@ void emit_body(std::ostringstream& o, const ProgView& v, const std::string& sfx)
     if (!v.h->nconst) o << "0u";
     o << "};\n\n";
     o << "__device__ __forceinline__ void spec_body" << sfx << "(const RunCtx& R, Lane& L, int64_t npoints) {\n";
-    o << "    Ctl<1> C;\n    ctl_init<1>(C, R, L, npoints);\n    long long backedges = 0;\n";
-    o << "    const uint32_t li0 = L.li;\n    (void)backedges;\n    (void)li0;\n";
+    o << "    Ctl<1> C;\n    ctl_init<1>(C, R, L, npoints);\n";
+    o << "    const uint32_t li0 = L.li;\n    (void)li0;\n";
     for (int i = 0; i < n; ++i) {
         const Op& op = ops[i];
         if (target[i]) o << "op_" << i << ":;\n";
@@ -200,9 +200,10 @@ void emit_body(std::ostringstream& o, const ProgView& v, const std::string& sfx)
         case OP_LOOP_TEST: o << "        if (ctl_loop_test<1>(C, L, li0, a)) goto " << dst(a[2]) << ";\n"; break;
         case OP_LOOP_STEP: o << "        ctl_loop_step<1>(C, a);\n"; break;
         case OP_JUMP:
-            o << "        (void)a;\n        if (++backedges > kMaxBackEdges) {\n"
-                 "            if (threadIdx.x % 32 == 0) raise_status(R.status, ST_TIMEOUT);\n"
-                 "            goto op_" << n << ";\n        }\n        goto " << dst(a[2]) << ";\n";
+            o << "        (void)a;\n";
+            if (a[2] <= (uint32_t)i)  // a loop's back edge
+                o << "        if (ctl_back_edge<1>(C, R, " << max_loop_iterations(*v.h) << "u)) goto op_" << n << ";\n";
+            o << "        goto " << dst(a[2]) << ";\n";
             break;
         case OP_LOOP_END: o << "        ctl_loop_end<1>(C, a);\n"; break;
         case OP_BREAK: o << "        ctl_break<1>(C, a);\n"; break;
@@ -355,6 +356,7 @@ std::string spec_batch_source(const std::vector<const CompiledGroup*>& cases) {
     o << "        if (it >= nitems) break;\n";
     o << "        const uint2 w = b.items[it];\n        const BatchJob* J = b.jobs + w.x;\n";
     o << "        R.G = &J->G;\n        R.userdata = J->userdata;\n        R.outputs = J->outputs;\n";
+    o << "        R.status = J->status ? J->status : b.status;\n";
     o << "        L.pt = (int64_t)w.y * blockDim.x + threadIdx.x;\n";
     o << "        const int64_t np = J->npoints;\n";
     o << "        switch (J->spec_case) {\n";

@@ -353,6 +353,7 @@ __global__ void __launch_bounds__(1024) k_plan(const __grid_constant__ WfArgs a,
         const int64_t off = s_off[m];
         J->blob = T->blob;
         J->spec_case = T->spec_case;
+        J->status = nullptr;
         J->npoints = s_cnt[m];
         J->userdata = reinterpret_cast<char*>(a.ud + off * kWfInFloats);
         J->outputs = reinterpret_cast<char*>(a.out + off * kWfOutFloats);

@@ -1160,11 +1160,12 @@ struct Runner {
         CPools C{ h.closure_base, h.max_comps };
         if (h.flags & 1u) P.heap[C.base] = 0u;
         int nops = (int)h.nops;
-        long long guard = 0;
+        // the loop limit: back edges this point takes, summed over every loop
+        const uint32_t cap = oslg::max_loop_iterations(h);
+        uint32_t iters = 0;
         for (int pc = 0; pc < nops;) {
             const Op& op = prog.ops[pc];
             const uint32_t* a = op.a;
-            if (++guard > (1ll << 30)) { P.status |= oslg::ST_TIMEOUT; return; }
             switch (op.code) {
             case oslg::OP_IF:
                 pc = truth(P, a[0]) ? pc + 1 : prog.partner[pc] + 1;
@@ -1175,7 +1176,10 @@ struct Runner {
             case oslg::OP_LOOP_TEST:
                 pc = truth(P, a[0]) ? pc + 1 : prog.partner[pc];
                 continue;
-            case oslg::OP_JUMP: pc = (int)a[2]; continue;
+            case oslg::OP_JUMP:
+                if ((int)a[2] <= pc && ++iters > cap) { P.status |= oslg::ST_TIMEOUT; return; }
+                pc = (int)a[2];
+                continue;
             case oslg::OP_BREAK: pc = prog.break_target[pc]; continue;
             case oslg::OP_CONTINUE: pc = prog.continue_target[pc]; continue;
             case oslg::OP_RETURN: pc = prog.layer_end_after[pc]; continue;

@@ -9,6 +9,9 @@ and text outputs and writes small fixtures next to this script:
   * src/liboslnoise/oslnoise_test.cpp known answers -> oslnoise_known.json.
 The GPU machine never reads the reference; tests read only these fixtures.
 
+Usage: python make_golden.py [REFERENCE_SOURCE_TREE]; the tree defaults to
+$OSL_REFERENCE_ROOT, else /root/reference.
+
 TIFF decoding is a minimal baseline-TIFF reader (strips, Deflate, LZW or no
 compression, optional horizontal predictor) on top of zlib and numpy.
 """
@@ -21,7 +24,7 @@ import zlib
 
 import numpy as np
 
-REF = "/root/reference"
+REF = os.environ.get("OSL_REFERENCE_ROOT", "/root/reference")
 HERE = os.path.dirname(os.path.abspath(__file__))
 STEP = 4  # keep every 4th pixel in x and y
 
@@ -242,4 +245,6 @@ def main():
 
 
 if __name__ == "__main__":
+    if len(sys.argv) > 1:
+        REF = sys.argv[1]
     sys.exit(main())

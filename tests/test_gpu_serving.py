@@ -122,3 +122,39 @@ def test_open_loop_poisson_run(setup):
     base = serving.run_plain(torch, ss, reqs, rate_rps=2000.0)
     assert base["requests"] == len(reqs)
     outputs_equal(reqs)
+
+
+def test_failed_request_fails_alone_in_a_mixed_wave(setup):
+    """A request whose kernel raises a status bit (here the loop limit) fails
+    with that status; the requests that shared its wave complete with their
+    plain-executor results, and no bit is left for a later call to find."""
+    from test_loop_limit import W, H, two_loops
+    from helpers import pixel_grid
+    ss, groups, reqs = setup
+    ss.attribute("max_loop_iterations", 5)
+    ss.LoadMemoryCompiledShader("two_loops_srv", two_loops(100).replace("two_loops", "two_loops_srv"))
+    lg = ss.ShaderGroupBegin("two_loops_srv_group")
+    ss.Shader(lg, "surface", "two_loops_srv", "layer1")
+    ss.ShaderGroupEnd(lg)
+    ss.add_symlocs(lg, [og.SymLocationDesc("count", og.TypeInt, False, og.SymArenaOutputs, 0, 4)])
+    ss.optimize_group(lg)  # lowered with the limit of 5 back edges per point
+    ss.attribute("max_loop_iterations", 0)
+    u, _ = pixel_grid(W, H)
+    lu = torch.from_numpy(u).pin_memory()
+    lout = torch.zeros(W * H, dtype=torch.int32).pin_memory()
+    srv = ss.server(budget_bytes=1 << 30, streams=1, max_wave_points=1 << 24)
+    part = reqs[:6]
+    for r in part:
+        r.out.zero_()
+    tickets = [srv.submit(r.group, r.n, r.G, r.out) for r in part[:3]]
+    bad = srv.submit(lg, W * H, og.make_globals(u=lu), lout)
+    tickets += [srv.submit(r.group, r.n, r.G, r.out) for r in part[3:]]
+    with pytest.raises(og.OSLError, match="status bits 8"):
+        srv.wait(bad)
+    stats = [srv.wait(t) for t in tickets]
+    assert all(st["status"] == 0 for st in stats)
+    outputs_equal(part)
+    s = srv.stats()
+    assert s["failed"] == 1 and s["completed"] == len(part)
+    srv.close()
+    assert ss.device_status() == 0
