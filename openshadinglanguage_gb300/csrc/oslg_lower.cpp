@@ -1011,7 +1011,8 @@ struct Lowerer {
             active.insert({ last[si], { si, sz } });
         }
         // closure node pool: one node per closure-creating op when none sits
-        // inside a loop, else the configured capacity
+        // inside a loop (each op makes at most one node, so the pool cannot
+        // overflow), else the configured capacity
         int nclosure_ops = 0;
         bool closure_in_loop = false;
         for (int k = 0; k < n; ++k) {
@@ -1024,8 +1025,7 @@ struct Lowerer {
             for (auto& L : loops)
                 if (k > L.first && k < L.second) closure_in_loop = true;
         }
-        closure_nodes = closure_in_loop ? ss.opts.max_closure_components
-                                        : std::min(nclosure_ops, ss.opts.max_closure_components);
+        closure_nodes = closure_in_loop ? ss.opts.max_closure_components : nclosure_ops;
         if (closure_nodes < 1) closure_nodes = 1;
     }
     int closure_nodes = 0;

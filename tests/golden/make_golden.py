@@ -4,8 +4,10 @@ Reads (in this container only) the reference testsuite's expected images
 and text outputs and writes small fixtures next to this script:
   * noise-family and spline images (uint8 TIFF, Deflate) -> <name>.npz,
     subsampled;
-  * testsuite/example-batched-deformer/ref/out.txt -> deformer_out.txt and
-    testsuite/splineinverse/ref/out.txt -> splineinverse_out.txt;
+  * testsuite/example-batched-deformer/ref/out.txt -> deformer_out.txt,
+    testsuite/splineinverse/ref/out.txt -> splineinverse_out.txt and the
+    closure print outputs of testsuite/closure, closure-zero and
+    closure-conditional -> closure_*out.txt;
   * src/liboslnoise/oslnoise_test.cpp known answers -> oslnoise_known.json.
 The GPU machine never reads the reference; tests read only these fixtures.
 
@@ -195,6 +197,9 @@ TEXTS = {
     # fixture file: reference path
     "deformer_out.txt": "testsuite/example-batched-deformer/ref/out.txt",
     "splineinverse_out.txt": "testsuite/splineinverse/ref/out.txt",
+    "closure_out.txt": "testsuite/closure/ref/out.txt",
+    "closure_zero_out.txt": "testsuite/closure-zero/ref/out.txt",
+    "closure_conditional_out.txt": "testsuite/closure-conditional/ref/out.txt",
 }
 
 

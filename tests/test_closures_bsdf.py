@@ -64,20 +64,27 @@ def test_zero_weight_closure_is_null_and_one_weight_is_identity():
 
 
 def test_closure_pool_overflow_sets_status():
+    """Closures made inside a loop draw on a pool of max_closure_components
+    nodes per point (a loop-free program gets one node per closure op and
+    cannot overflow); running past it raises the overflow status bit.
+
+        for (int i = 0; i < 20; ++i) Ci += diffuse(N);
+    """
     b = OsoBuilder("many", "surface")
     Ci = b.glob("closure color", "Ci")
     N = b.glob("normal", "N")
-    prev = None
-    for i in range(20):
+    i = b.local("int", "i")
+    c = b.tmp("int")
+    with b.loop("for", c) as L:
+        b.op("assign", i, b.const("int", 0))
+        L.cond()
+        b.op("lt", c, i, b.const("int", 20))
+        L.body()
         d = b.tmp("closure color")
         b.op("closure", d, b.const("string", "diffuse"), N)
-        if prev is not None:
-            s = b.tmp("closure color")
-            b.op("add", s, prev, d)
-            prev = s
-        else:
-            prev = d
-    b.op("assign", Ci, prev)
+        b.op("add", Ci, Ci, d)
+        L.step()
+        b.op("add", i, i, b.const("int", 1))
 
     def extra(ss, g):
         ss.attribute("max_closure_components", 8)
