@@ -7,7 +7,8 @@ and text outputs and writes small fixtures next to this script:
   * testsuite/example-batched-deformer/ref/out.txt -> deformer_out.txt,
     testsuite/splineinverse/ref/out.txt -> splineinverse_out.txt and the
     closure print outputs of testsuite/closure, closure-zero and
-    closure-conditional -> closure_*out.txt;
+    closure-conditional -> closure_*out.txt, testsuite/matrix and transform
+    ref/out.txt -> matrix_out.txt, transform_out.txt;
   * src/liboslnoise/oslnoise_test.cpp known answers -> oslnoise_known.json.
 The GPU machine never reads the reference; tests read only these fixtures.
 
@@ -200,6 +201,8 @@ TEXTS = {
     "closure_out.txt": "testsuite/closure/ref/out.txt",
     "closure_zero_out.txt": "testsuite/closure-zero/ref/out.txt",
     "closure_conditional_out.txt": "testsuite/closure-conditional/ref/out.txt",
+    "matrix_out.txt": "testsuite/matrix/ref/out.txt",
+    "transform_out.txt": "testsuite/transform/ref/out.txt",
 }
 
 
