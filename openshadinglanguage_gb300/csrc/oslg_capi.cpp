@@ -205,6 +205,7 @@ int oslg_attribute_int(oslg_system* sys, const char* name, int value) {
     else if (n == "strict_messages") sys->ss.opts.strict_messages = value != 0;
     else if (n == "opt_constant_fold") sys->ss.opts.opt_constant_fold = value != 0;
     else if (n == "opt_elide_useless_ops") sys->ss.opts.opt_elide_useless_ops = value != 0;
+    else if (n == "opt_static_closures") sys->ss.opts.opt_static_closures = value != 0;
     else if (n == "jit") sys->jit = value;
     else if (n == "jit_block") sys->jit_block = value;
     else if (n == "jit_pool_smem") sys->jit_pool_smem = value;

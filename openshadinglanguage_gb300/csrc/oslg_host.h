@@ -187,6 +187,7 @@ struct SystemOptions {
     int strict_messages = 1;  // ShadingSystem attribute "strict_messages" (shadingsys.cpp:1078)
     int opt_constant_fold = 1;       // "opt_constant_fold" (shadingsys.cpp:1641)
     int opt_elide_useless_ops = 1;   // "opt_elide_useless_ops" (shadingsys.cpp:1643)
+    int opt_static_closures = 1;     // closure trees the lowering knows become term tables
     int max_closure_components = 16;  // closure tree nodes per point when closures are made inside loops
     int max_closure_terms = 16;
     int max_loop_iterations = 0;  // loop back edges per point (0: the program format's default)

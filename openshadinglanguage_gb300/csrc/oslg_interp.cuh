@@ -24,6 +24,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <type_traits>
 #include <mutex>
 #include <string>
 
@@ -1483,6 +1484,22 @@ __device__ __forceinline__ void hset(const Lane& L, uint32_t slot, float v) { L.
 #endif
 __device__ __forceinline__ uint32_t hgetu(const Lane& L, uint32_t slot) { return __float_as_uint(hget(L, slot)); }
 __device__ __forceinline__ void hsetu(const Lane& L, uint32_t slot, uint32_t v) { hset(L, slot, __uint_as_float(v)); }
+// symbol-heap words (static closure nodes live among the symbols: registers
+// in a specialized kernel)
+__device__ __forceinline__ float sget(const Lane& L, uint32_t slot) { return L.heap[(size_t)slot * L.hs + L.li]; }
+__device__ __forceinline__ void sset(const Lane& L, uint32_t slot, float v) { L.heap[(size_t)slot * L.hs + L.li] = v; }
+__device__ __forceinline__ uint32_t sgetu(const Lane& L, uint32_t slot) { return __float_as_uint(sget(L, slot)); }
+__device__ __forceinline__ void ssetu(const Lane& L, uint32_t slot, uint32_t v) { sset(L, slot, __uint_as_float(v)); }
+// Where a lobe's node parameters are read: the closure node pool (trees
+// built at run time) or the symbol heap (static closures).
+struct PoolNodes {
+    static __device__ __forceinline__ float f(const Lane& L, uint32_t s) { return hget(L, s); }
+    static __device__ __forceinline__ uint32_t u(const Lane& L, uint32_t s) { return hgetu(L, s); }
+};
+struct SymNodes {
+    static __device__ __forceinline__ float f(const Lane& L, uint32_t s) { return sget(L, s); }
+    static __device__ __forceinline__ uint32_t u(const Lane& L, uint32_t s) { return sgetu(L, s); }
+};
 __device__ __forceinline__ uint32_t node_slot(const ClosurePools& P, uint32_t node) {
     return P.base + 1 + node * kNodeFloats;
 }
@@ -1494,19 +1511,18 @@ __device__ __forceinline__ uint32_t cl_alloc(const Lane& L, const ClosurePools& 
     return n + 1;
 }
 
-// osl_allocate_(weighted_)closure_component (opclosure.cpp:83-117)
-static __device__ void h_closure(const Lane& L, const uint32_t* a, const uint32_t* extra, const ClosurePools& P,
-                          uint32_t* st) {
-    float w[3] = { 1.0f, 1.0f, 1.0f };
-    if (a[2] != kNoArg) {
-        for (int c = 0; c < 3; ++c) w[c] = ldf(L, a[2], c, 0);
-        if (w[0] == 0.0f && w[1] == 0.0f && w[2] == 0.0f) { stw(L, a[0], 0, 0u); return; }
-    }
-    uint32_t h = cl_alloc(L, P, st);
-    if (!h) { stw(L, a[0], 0, 0u); return; }
-    uint32_t ns = node_slot(P, h - 1);
-    hsetu(L, ns, a[1]);
-    for (int c = 0; c < 3; ++c) hset(L, ns + 1 + c, w[c]);
+// A component node [id][w.rgb][12 parameter words] at slot ns: the
+// closure op's parameters in order, int and string operands as their
+// words, floats as values, zero-padded.
+template <class NODES>
+__device__ __forceinline__ void closure_fill(const Lane& L, uint32_t ns, const uint32_t* a, const uint32_t* extra,
+                                             const float* w) {
+    auto setu = [&](uint32_t s, uint32_t v) {
+        if constexpr (std::is_same<NODES, SymNodes>::value) ssetu(L, s, v);
+        else hsetu(L, s, v);
+    };
+    setu(ns, a[1]);
+    for (int c = 0; c < 3; ++c) setu(ns + 1 + c, __float_as_uint(w[c]));
     uint32_t params[11];
     int np = 0;
     for (int i = 3; i < 7; ++i) params[np++] = a[i];
@@ -1525,11 +1541,36 @@ static __device__ void h_closure(const Lane& L, const uint32_t* a, const uint32_
         OSLG_SPEC_UNROLL
         for (int c = 0; c < 16; ++c) {
             if (c >= nc || k >= kClosureParamFloats) break;
-            hsetu(L, ns + 4 + k++, (t == TC_INT || t == TC_STRING) ? ldw(L, p, c) : __float_as_uint(ldf(L, p, c, 0)));
+            setu(ns + 4 + k++, (t == TC_INT || t == TC_STRING) ? ldw(L, p, c) : __float_as_uint(ldf(L, p, c, 0)));
         }
     }
-    for (; k < kClosureParamFloats; ++k) hset(L, ns + 4 + k, 0.0f);
+    for (; k < kClosureParamFloats; ++k) setu(ns + 4 + k, 0u);
+}
+
+// osl_allocate_(weighted_)closure_component (opclosure.cpp:83-117)
+static __device__ void h_closure(const Lane& L, const uint32_t* a, const uint32_t* extra, const ClosurePools& P,
+                          uint32_t* st) {
+    float w[3] = { 1.0f, 1.0f, 1.0f };
+    if (a[2] != kNoArg) {
+        for (int c = 0; c < 3; ++c) w[c] = ldf(L, a[2], c, 0);
+        if (w[0] == 0.0f && w[1] == 0.0f && w[2] == 0.0f) { stw(L, a[0], 0, 0u); return; }
+    }
+    uint32_t h = cl_alloc(L, P, st);
+    if (!h) { stw(L, a[0], 0, 0u); return; }
+    closure_fill<PoolNodes>(L, node_slot(P, h - 1), a, extra, w);
     stw(L, a[0], 0, h);
+}
+
+// The static form: the node sits at the symbol-heap slot of operand a0; a
+// zero weight marks it absent (the reference returns a null closure).
+static __device__ void h_closure_node(const Lane& L, const uint32_t* a, const uint32_t* extra) {
+    const uint32_t ns = a[0] & kArgOffsetMask;
+    float w[3] = { 1.0f, 1.0f, 1.0f };
+    if (a[2] != kNoArg) {
+        for (int c = 0; c < 3; ++c) w[c] = ldf(L, a[2], c, 0);
+        if (w[0] == 0.0f && w[1] == 0.0f && w[2] == 0.0f) { ssetu(L, ns, (uint32_t)kClosureAbsent); return; }
+    }
+    closure_fill<SymNodes>(L, ns, a, extra, w);
 }
 
 // osl_mul_closure_color / osl_mul_closure_float (opclosure.cpp:35-80)
@@ -1659,13 +1700,17 @@ struct Lobes {
 #else
 #define OSLG_FOR_LOBES(i, B) for (int i = 0; i < (B).n; ++i)
 #endif
-__device__ __forceinline__ void lobes_build(const Lane& L, const ClosurePools& P, uint32_t root, uint32_t ggx,
-                                            uint32_t* st, Lobes& B, float path_rough = 0.0f, bool backfacing = false) {
+// process_closure's lobes (shading.cpp:1481-1530) from the components a walk
+// visits: `walk(visit)` calls visit(id, weight, parameter slot) for each
+// component in the walk's order.
+template <class NODES, class W>
+__device__ __forceinline__ void lobes_collect(const Lane& L, W&& walk, uint32_t ggx, Lobes& B, float path_rough,
+                                              bool backfacing) {
     B.n = 0;
     B.Le[0] = B.Le[1] = B.Le[2] = 0.0f;
     B.path_rough = path_rough;
     B.backfacing = backfacing;
-    closure_walk(L, P, root, st, [&](int id, const float* cw, uint32_t params) {
+    walk([&](int id, const float* cw, uint32_t params) {
         int k = -1;
         if (id == 1) {  // EMISSION_ID
             for (int c = 0; c < 3; ++c) B.Le[c] = B.Le[c] + cw[c];
@@ -1673,9 +1718,9 @@ __device__ __forceinline__ void lobes_build(const Lane& L, const ClosurePools& P
         }
         if (id == 3) k = 0;  // DIFFUSE_ID
         else if (id == 4) k = 2;  // OREN_NAYAR_ID
-        else if (id == 23 && hgetu(L, params + 7) == 0u) k = 3;  // MX_SHEEN_ID, Conty-Kulla mode
-        else if (id == 8 && hgetu(L, params + 0) == ggx) {  // MICROFACET_ID "ggx"
-            const int r = (int)hgetu(L, params + 10);
+        else if (id == 23 && NODES::u(L, params + 7) == 0u) k = 3;  // MX_SHEEN_ID, Conty-Kulla mode
+        else if (id == 8 && NODES::u(L, params + 0) == ggx) {  // MICROFACET_ID "ggx"
+            const int r = (int)NODES::u(L, params + 10);
             if (r >= 0 && r <= 2) k = 1;
         }
         if (k < 0 || B.n >= OSLG_LOBES_MAX) return;
@@ -1695,62 +1740,73 @@ __device__ __forceinline__ void lobes_build(const Lane& L, const ClosurePools& P
         ++B.n;
     });
 }
+// the lobes of a tree in the node pool, visited by testrender's walk
+__device__ __forceinline__ void lobes_build(const Lane& L, const ClosurePools& P, uint32_t root, uint32_t ggx,
+                                            uint32_t* st, Lobes& B, float path_rough = 0.0f, bool backfacing = false) {
+    lobes_collect<PoolNodes>(
+        L, [&](auto&& visit) { closure_walk(L, P, root, st, visit); }, ggx, B, path_rough, backfacing);
+}
+template <class NODES = PoolNodes>
 __device__ __forceinline__ GGXLobe lobe_ggx(const Lane& L, uint32_t p) {
     GGXLobe g;
-    const V3 N = v3(hget(L, p + 1), hget(L, p + 2), hget(L, p + 3));
-    const V3 U = v3(hget(L, p + 4), hget(L, p + 5), hget(L, p + 6));
+    const V3 N = v3(NODES::f(L, p + 1), NODES::f(L, p + 2), NODES::f(L, p + 3));
+    const V3 U = v3(NODES::f(L, p + 4), NODES::f(L, p + 5), NODES::f(L, p + 6));
     g.tf = frame_from_normal_and_tangent(N, U);
-    g.ax = hget(L, p + 7);
-    g.ay = hget(L, p + 8);
-    g.eta = hget(L, p + 9);
-    g.refract = (int)hgetu(L, p + 10);
+    g.ax = NODES::f(L, p + 7);
+    g.ay = NODES::f(L, p + 8);
+    g.eta = NODES::f(L, p + 9);
+    g.refract = (int)NODES::u(L, p + 10);
     return g;
 }
+template <class NODES = PoolNodes>
 __device__ __forceinline__ SheenLobeDev lobe_sheen(const Lane& L, const Lobes& B, uint32_t p, V3 wo) {
-    const float albedo[3] = { hget(L, p + 3), hget(L, p + 4), hget(L, p + 5) };
-    return sheen_make(v3(hget(L, p + 0), hget(L, p + 1), hget(L, p + 2)), albedo, hget(L, p + 6), wo, B.path_rough,
+    const float albedo[3] = { NODES::f(L, p + 3), NODES::f(L, p + 4), NODES::f(L, p + 5) };
+    return sheen_make(v3(NODES::f(L, p + 0), NODES::f(L, p + 1), NODES::f(L, p + 2)), albedo, NODES::f(L, p + 6), wo, B.path_rough,
                       B.backfacing);
 }
+template <class NODES = PoolNodes>
 __device__ __forceinline__ BsdfSample lobe_eval(const Lane& L, const Lobes& B, int i, V3 wo, V3 wi) {
     const uint32_t p = B.p[i];
-    if (B.kind[i] == 3) return sheen_eval(lobe_sheen(L, B, p, wo), wo, wi);
+    if (B.kind[i] == 3) return sheen_eval(lobe_sheen<NODES>(L, B, p, wo), wo, wi);
     if (B.kind[i] == 0) {
-        BsdfSample s = diffuse_eval(v3(hget(L, p + 0), hget(L, p + 1), hget(L, p + 2)), wi);
+        BsdfSample s = diffuse_eval(v3(NODES::f(L, p + 0), NODES::f(L, p + 1), NODES::f(L, p + 2)), wi);
         s.wi = wi;
         return s;
     }
-    if (B.kind[i] == 1) return ggx_eval(lobe_ggx(L, p), wo, wi);
-    const V3 N = v3(hget(L, p + 0), hget(L, p + 1), hget(L, p + 2));
+    if (B.kind[i] == 1) return ggx_eval(lobe_ggx<NODES>(L, p), wo, wi);
+    const V3 N = v3(NODES::f(L, p + 0), NODES::f(L, p + 1), NODES::f(L, p + 2));
     const Frame f = bsdl_frame(bsdl_visible_normal(wo, N, N));
-    BsdfSample s = on_eval_local(bsdl_clamp(hget(L, p + 3), 0.0f, 1.0f), tolocal(f, wo), tolocal(f, wi));
+    BsdfSample s = on_eval_local(bsdl_clamp(NODES::f(L, p + 3), 0.0f, 1.0f), tolocal(f, wo), tolocal(f, wi));
     s.wi = wi;
     return s;
 }
+template <class NODES = PoolNodes>
 __device__ __forceinline__ BsdfSample lobe_sample(const Lane& L, const Lobes& B, int i, V3 wo, float rx, float ry,
                                                   float rz) {
     const uint32_t p = B.p[i];
-    if (B.kind[i] == 3) return sheen_sample(lobe_sheen(L, B, p, wo), wo, rx, ry);
-    if (B.kind[i] == 0) return diffuse_sample(v3(hget(L, p + 0), hget(L, p + 1), hget(L, p + 2)), rx, ry);
-    if (B.kind[i] == 1) return ggx_sample(lobe_ggx(L, p), wo, rx, ry, rz);
-    const V3 N = v3(hget(L, p + 0), hget(L, p + 1), hget(L, p + 2));
+    if (B.kind[i] == 3) return sheen_sample(lobe_sheen<NODES>(L, B, p, wo), wo, rx, ry);
+    if (B.kind[i] == 0) return diffuse_sample(v3(NODES::f(L, p + 0), NODES::f(L, p + 1), NODES::f(L, p + 2)), rx, ry);
+    if (B.kind[i] == 1) return ggx_sample(lobe_ggx<NODES>(L, p), wo, rx, ry, rz);
+    const V3 N = v3(NODES::f(L, p + 0), NODES::f(L, p + 1), NODES::f(L, p + 2));
     const Frame f = bsdl_frame(bsdl_visible_normal(wo, N, N));
     const V3 wo_l = tolocal(f, wo);
     if (wo_l.z <= 0.0f) return bsdf_zero();
-    BsdfSample s = on_eval_local(bsdl_clamp(hget(L, p + 3), 0.0f, 1.0f), wo_l, bsdl_sample_cos_hemisphere(rx, ry));
+    BsdfSample s = on_eval_local(bsdl_clamp(NODES::f(L, p + 3), 0.0f, 1.0f), wo_l, bsdl_sample_cos_hemisphere(rx, ry));
     s.wi = bsdl_world(f, s.wi);
     return s;
 }
 // CompositeBSDF::prepare (shading.h:322-350)
+template <class NODES = PoolNodes>
 __device__ __forceinline__ void lobes_prepare(const Lane& L, Lobes& B, V3 wo, const float* pw, bool absorb) {
     float total = 0.0f;
     OSLG_FOR_LOBES(i, B) {
         float alb[3] = { 1.0f, 1.0f, 1.0f };
         if (B.kind[i] == 1) {
             const uint32_t p = B.p[i];
-            const GGXLobe g = lobe_ggx(L, p);
-            alb[0] = alb[1] = alb[2] = ggx_albedo(g, v3(hget(L, p + 1), hget(L, p + 2), hget(L, p + 3)), wo);
+            const GGXLobe g = lobe_ggx<NODES>(L, p);
+            alb[0] = alb[1] = alb[2] = ggx_albedo(g, v3(NODES::f(L, p + 1), NODES::f(L, p + 2), NODES::f(L, p + 3)), wo);
         } else if (B.kind[i] == 3) {
-            const SheenLobeDev sh = lobe_sheen(L, B, B.p[i], wo);
+            const SheenLobeDev sh = lobe_sheen<NODES>(L, B, B.p[i], wo);
             for (int c = 0; c < 3; ++c) alb[c] = sh.tint[c] * (1 - sh.emiss);
         }
         B.pdf[i] = (B.w[i][0] * (pw[0] * alb[0]) + B.w[i][1] * (pw[1] * alb[1]) + B.w[i][2] * (pw[2] * alb[2]))
@@ -1761,10 +1817,11 @@ __device__ __forceinline__ void lobes_prepare(const Lane& L, Lobes& B, V3 wo, co
         OSLG_FOR_LOBES(i, B) B.pdf[i] /= total;
 }
 // CompositeBSDF::eval (shading.h:360-370)
+template <class NODES = PoolNodes>
 __device__ __forceinline__ BsdfSample lobes_eval(const Lane& L, const Lobes& B, V3 wo, V3 wi) {
     BsdfSample r = bsdf_zero();
     OSLG_FOR_LOBES(i, B) {
-        BsdfSample b = lobe_eval(L, B, i, wo, wi);
+        BsdfSample b = lobe_eval<NODES>(L, B, i, wo, wi);
         for (int c = 0; c < 3; ++c) b.w[c] *= B.w[i][c];
         mis_update_eval(r.w, &r.pdf, b.w, b.pdf, B.pdf[i]);
         r.roughness += b.roughness * B.pdf[i];
@@ -1772,20 +1829,21 @@ __device__ __forceinline__ BsdfSample lobes_eval(const Lane& L, const Lobes& B, 
     return r;
 }
 // CompositeBSDF::sample (shading.h:372-398)
+template <class NODES = PoolNodes>
 __device__ __forceinline__ BsdfSample lobes_sample(const Lane& L, const Lobes& B, V3 wo, float rx, float ry, float rz) {
     float accum = 0.0f;
     OSLG_FOR_LOBES(i, B) {
         if (rx < (B.pdf[i] + accum)) {
             rx = (rx - accum) / B.pdf[i];
             rx = fminf(rx, 0.99999994f);
-            BsdfSample s = lobe_sample(L, B, i, wo, rx, ry, rz);
+            BsdfSample s = lobe_sample<NODES>(L, B, i, wo, rx, ry, rz);
             const float inv = 1 / B.pdf[i];
             for (int c = 0; c < 3; ++c) s.w[c] *= B.w[i][c] * inv;
             s.pdf *= B.pdf[i];
             if (s.pdf == 0.0f) return bsdf_zero();
             OSLG_FOR_LOBES(j, B) {
                 if (i != j) {
-                    BsdfSample b = lobe_eval(L, B, j, wo, s.wi);
+                    BsdfSample b = lobe_eval<NODES>(L, B, j, wo, s.wi);
                     for (int c = 0; c < 3; ++c) b.w[c] *= B.w[j][c];
                     mis_update_eval(s.w, &s.pdf, b.w, b.pdf, B.pdf[j]);
                 }
@@ -1829,6 +1887,74 @@ static __device__ void h_bsdf_sample(const Lane& L, const uint32_t* a, char* bas
     const float pw[3] = { in[3], in[4], in[5] };
     lobes_prepare(L, B, wo, pw, in[6] != 0.0f);
     const BsdfSample r = lobes_sample(L, B, wo, in[0], in[1], in[2]);
+    float* o = reinterpret_cast<float*>(base + (int64_t)a[1] + L.pt * (int64_t)(int32_t)a[2]);
+    const float vals[11] = { r.wi.x, r.wi.y, r.wi.z, r.w[0], r.w[1], r.w[2], r.pdf, B.Le[0], B.Le[1], B.Le[2],
+                             r.roughness };
+#pragma unroll
+    for (int k = 0; k < 11; ++k) ostoref(o + k, vals[k]);
+}
+
+// ---- static closures: consumers over a term table ---------------------------------
+// Term j of a static consumer is words 3*(j%2).. of the (j/2)-th carrier op
+// after it: {node slot, weight operand or kNoArg, presence operand or kNoArg}
+// (see kClosureAbsent). Visiting the present terms in table order is the
+// reference walk of the tree the lowering knew.
+__device__ __forceinline__ uint32_t term_word(const Op* tab, int j, int w) { return tab[j >> 1].a[3 * (j & 1) + w]; }
+template <class F>
+__device__ __forceinline__ void closure_walk_static(const Lane& L, const Op* tab, uint32_t nterms, F&& visit) {
+    OSLG_SPEC_UNROLL
+    for (int j = 0; j < kMaxStaticTerms; ++j) {
+        if (j >= (int)nterms) break;
+        const uint32_t ns = term_word(tab, j, 0), cwop = term_word(tab, j, 1), pop = term_word(tab, j, 2);
+        const int id = (int)sgetu(L, ns);
+        if (id == kClosureAbsent) continue;
+        if (pop != kNoArg && ldw(L, pop, 0) == 0u) continue;
+        float cw[3];
+        for (int k = 0; k < 3; ++k) cw[k] = cwop == kNoArg ? sget(L, ns + 1 + k) : ldf(L, cwop, k, 0);
+        visit(id, cw, ns + 4);
+    }
+}
+// records as h_store_closure writes them
+static __device__ void h_cl_store(const Lane& L, const uint32_t* a, const Op* tab, char* base) {
+    const uint32_t maxc = a[3];
+    uint32_t* o = reinterpret_cast<uint32_t*>(base + (int64_t)a[1] + L.pt * (int64_t)(int32_t)a[2]);
+    uint32_t n = 0;
+    closure_walk_static(L, tab, a[0], [&](int id, const float* cw, uint32_t params) {
+        if (n >= maxc) return;
+        uint32_t* q = o + 1 + n * kNodeFloats;
+        ostore32(q, (uint32_t)id);
+        for (int k = 0; k < 3; ++k) ostore32(q + 1 + k, __float_as_uint(cw[k]));
+        for (int k = 0; k < kClosureParamFloats; ++k) ostore32(q + 4 + k, sgetu(L, params + k));
+        ++n;
+    });
+    ostore32(o, n);
+}
+// as h_bsdf_eval
+static __device__ void h_cl_bsdf_eval(const Lane& L, const uint32_t* a, const Op* tab, char* base) {
+    const V3 wi = v3(ldf(L, a[3], 0, 0), ldf(L, a[3], 1, 0), ldf(L, a[3], 2, 0));
+    const V3 wo = v3(-ldf(L, a[4], 0, 0), -ldf(L, a[4], 1, 0), -ldf(L, a[4], 2, 0));
+    Lobes B;
+    lobes_collect<SymNodes>(
+        L, [&](auto&& visit) { closure_walk_static(L, tab, a[0], visit); }, a[5], B, 0.0f, false);
+    const float one[3] = { 1.0f, 1.0f, 1.0f };
+    lobes_prepare<SymNodes>(L, B, wo, one, false);
+    const BsdfSample r = lobes_eval<SymNodes>(L, B, wo, wi);
+    float* o = reinterpret_cast<float*>(base + (int64_t)a[1] + L.pt * (int64_t)(int32_t)a[2]);
+    ostoref(o + 0, r.w[0]);
+    ostoref(o + 1, r.w[1]);
+    ostoref(o + 2, r.w[2]);
+    ostoref(o + 3, r.pdf);
+}
+// as h_bsdf_sample
+static __device__ void h_cl_bsdf_sample(const Lane& L, const uint32_t* a, const Op* tab, char* base, const char* ud) {
+    const V3 wo = v3(-ldf(L, a[3], 0, 0), -ldf(L, a[3], 1, 0), -ldf(L, a[3], 2, 0));
+    const float* in = reinterpret_cast<const float*>(ud + (int64_t)a[5] + L.pt * (int64_t)(int32_t)a[6]);
+    Lobes B;
+    lobes_collect<SymNodes>(
+        L, [&](auto&& visit) { closure_walk_static(L, tab, a[0], visit); }, a[4], B, in[7], in[8] != 0.0f);
+    const float pw[3] = { in[3], in[4], in[5] };
+    lobes_prepare<SymNodes>(L, B, wo, pw, in[6] != 0.0f);
+    const BsdfSample r = lobes_sample<SymNodes>(L, B, wo, in[0], in[1], in[2]);
     float* o = reinterpret_cast<float*>(base + (int64_t)a[1] + L.pt * (int64_t)(int32_t)a[2]);
     const float vals[11] = { r.wi.x, r.wi.y, r.wi.z, r.w[0], r.w[1], r.w[2], r.pdf, B.Le[0], B.Le[1], B.Le[2],
                              r.roughness };
@@ -2371,6 +2497,20 @@ __device__ __forceinline__ void exec_op(const RunCtx& R, Lane& L, uint32_t code,
         }
         break;
     }
+    case OP_CLOSURE_NODE: {
+        if constexpr ((TIER & 2) != 0) {
+            const uint32_t* extra = nullptr;
+            const Op* next = next_op();
+            if (next && next->code == OP_NOP && next->nargs == 7) extra = next->a;
+            h_closure_node(L, a, extra);
+        } else {
+            raise_status(R.status, ST_BAD_OPCODE);
+        }
+        break;
+    }
+    case OP_CL_STORE: OSLG_TIER_CASE(2, h_cl_store(L, a, next_op(), R.outputs)) break;
+    case OP_CL_BSDF_EVAL: OSLG_TIER_CASE(2, h_cl_bsdf_eval(L, a, next_op(), R.outputs)) break;
+    case OP_CL_BSDF_SAMPLE: OSLG_TIER_CASE(2, h_cl_bsdf_sample(L, a, next_op(), R.outputs, R.userdata)) break;
     case OP_CLOSURE_MUL: OSLG_TIER_CASE(2, h_closure_mul(L, a, R.CP, R.status)) break;
     case OP_CLOSURE_ADD: OSLG_TIER_CASE(2, h_closure_add(L, a, R.CP, R.status)) break;
     case OP_STORE_CLOSURE: OSLG_TIER_CASE(2, h_store_closure(L, a, R.outputs, R.CP, R.status)) break;

@@ -432,7 +432,8 @@ struct Lowerer {
             return op.argrw[i] == 'w' || op.argrw[i] == 'W';
         static const std::set<std::string> nowrite = {
             "if", "for", "while", "dowhile", "break", "continue", "return", "exit", "nop",
-            "useparam", "__layer_end", "__store_output", "__bsdf_eval", "__bsdf_sample", "functioncall",
+            "useparam", "__layer_end", "__store_output", "__bsdf_eval", "__bsdf_sample", "__cl_store",
+            "__cl_bsdf_eval", "__cl_bsdf_sample", "functioncall",
             "functioncall_nr",
             "printf", "warning", "error", "fprintf" };
         if (nowrite.count(op.name)) return false;
@@ -939,6 +940,238 @@ struct Lowerer {
     // Live interval of every heap symbol over the linear op list, widened to
     // cover each loop that references it (a value can flow around the back
     // edge). Symbols whose intervals do not overlap share heap slots.
+    // ---- static closures ------------------------------------------------------
+    // When no closure value depends on control flow (every closure write is
+    // outside ifs and loops, there is no return or exit) this pass knows the
+    // tree of each closure value: a closure op is a component node; MUL
+    // wraps a subtree; ADD joins two. testrender's walk of such a tree
+    // (src/testrender/shading.cpp:1450-1500) visits the components in a
+    // fixed order, each with the product of the MUL weights above it, and a
+    // zero MUL weight or a zero component weight removes the subtree (the
+    // reference returns null closures, src/liboslexec/opclosure.cpp:15-117).
+    // So each closure op becomes a node at a fixed heap slot, MUL weights are
+    // kept, ADD and closure assignment disappear, and each consumer (record
+    // store, BSDF eval or sample) receives the walk unrolled as a term table
+    // whose weights and presence flags are computed by ordinary ops in the
+    // walk's order. Results are those of the tree walk.
+    struct ClTerm {
+        int node;                // the component's node block (gsym)
+        std::vector<int> chain;  // MUL weight gsyms, outermost first
+    };
+    bool closure_consumer(const LOp& op) const {
+        if (op.name == "__bsdf_eval" || op.name == "__bsdf_sample") return true;
+        return op.name == "__store_output" && !op.args.empty() && is_closure(op.args[0]);
+    }
+    bool closure_writer(const LOp& op) const {
+        if (op.args.empty() || !is_closure(op.args[0])) return false;
+        return op.name == "closure" || op.name == "add" || op.name == "mul" || op.name == "assign";
+    }
+    // a weight known to be zero (every component 0) or known to be nonzero
+    int const_zero(int gs) const {
+        CVal v;
+        if (!cval_of(gs, v)) return -1;
+        for (int c = 0; c < v.n; ++c) {
+            const float x = v.f(c);
+            if (x != 0.0f || x != x) return 0;
+        }
+        return 1;
+    }
+    int none_sym = -1;
+    int new_sym(const std::string& name, BaseType b, int arraylen = 0, VecSem vs = VS_NONE) {
+        GSym t;
+        t.name = name;
+        t.type.base = b;
+        t.type.arraylen = arraylen;
+        t.type.vecsem = vs;
+        t.kind = SK_LOCAL;
+        return add_sym(t);
+    }
+    bool static_closures() {
+        if (!ss.opts.opt_static_closures) return false;
+        const int n = (int)lops.size();
+        std::vector<int> depth(n + 1, 0);
+        bool any = false;
+        for (int k = 0; k < n; ++k) {
+            const LOp& op = lops[k];
+            int end = -1;
+            if (op.name == "if" && op.jumps.size() >= 2) end = op.jumps[1];
+            else if ((op.name == "for" || op.name == "while" || op.name == "dowhile") && op.jumps.size() >= 4)
+                end = op.jumps[3];
+            for (int j = k + 1; j < std::min(end, n); ++j) depth[j]++;
+            for (int a : op.args)
+                if (is_closure(a)) {
+                    any = true;
+                    if (syms[a].type.is_array()) return false;
+                }
+        }
+        if (!any) return false;
+        // eligibility, and a dry run of the term lists
+        std::map<int, std::vector<ClTerm>> val;
+        int adds = 0;
+        for (int k = 0; k < n; ++k) {
+            const LOp& op = lops[k];
+            if (op.name == "return" || op.name == "exit") return false;
+            bool refs = false;
+            for (int a : op.args) refs = refs || is_closure(a);
+            if (!refs || op.name == "useparam") continue;
+            if (closure_consumer(op)) {
+                if (depth[k]) return false;
+                if (val[op.args[0]].size() > (size_t)kMaxStaticTerms) return false;
+                continue;
+            }
+            if (!closure_writer(op) || depth[k]) return false;
+            const int r = op.args[0];
+            if (op.name == "closure") {
+                val[r] = { ClTerm{ -1, {} } };
+            } else if (op.name == "assign") {
+                val[r] = op.args.size() > 1 && is_closure(op.args[1]) ? val[op.args[1]] : std::vector<ClTerm>{};
+            } else if (op.name == "add") {
+                if (op.args.size() < 3 || !is_closure(op.args[1]) || !is_closure(op.args[2])) return false;
+                std::vector<ClTerm> t = val[op.args[1]];
+                for (const ClTerm& x : val[op.args[2]]) t.push_back(x);
+                val[r] = t;
+                ++adds;
+            } else {  // mul
+                if (op.args.size() < 3) return false;
+                const int c = is_closure(op.args[1]) ? op.args[1] : op.args[2];
+                val[r] = val[c];
+            }
+            if (val[r].size() > 64) return false;
+        }
+        // the reference walk keeps at most this many pending branches
+        if (adds > kClosureWalkStack) return false;
+
+        // the rewrite
+        GSym nn;
+        nn.name = "$noarg";
+        nn.type.base = BT_INT;
+        nn.kind = SK_CONST;
+        nn.is_const = true;
+        nn.cval = { 0.0f };
+        none_sym = add_sym(nn);
+        val.clear();
+        std::vector<LOp> out;
+        std::vector<int> newpos(n + 1, 0);
+        for (int k = 0; k < n; ++k) {
+            newpos[k] = (int)out.size();
+            const LOp& op = lops[k];
+            if (closure_writer(op)) {
+                const int r = op.args[0];
+                if (op.name == "closure") {
+                    const int b = new_sym("$clnode", BT_FLOAT, kNodeFloats);
+                    LOp nd = op;
+                    nd.name = "__cl_node";
+                    nd.args[0] = b;
+                    nd.argrw.clear();
+                    out.push_back(nd);
+                    val[r] = { ClTerm{ b, {} } };
+                } else if (op.name == "assign") {
+                    val[r] = op.args.size() > 1 && is_closure(op.args[1]) ? val[op.args[1]] : std::vector<ClTerm>{};
+                } else if (op.name == "add") {
+                    std::vector<ClTerm> t = val[op.args[1]];
+                    for (const ClTerm& x : val[op.args[2]]) t.push_back(x);
+                    val[r] = t;
+                } else {  // mul: keep the weight as it is now
+                    const bool cfirst = is_closure(op.args[1]);
+                    const int c = cfirst ? op.args[1] : op.args[2];
+                    int w = cfirst ? op.args[2] : op.args[1];
+                    std::vector<ClTerm> t;
+                    const int z = const_zero(w);
+                    if (z != 1) {  // a zero weight leaves the null closure
+                        if (!syms[w].is_const) {
+                            const int cap = new_sym("$clw", syms[w].type.base, 0, syms[w].type.vecsem);
+                            LOp as;
+                            as.name = "assign";
+                            as.layer = op.layer;
+                            as.args = { cap, w };
+                            out.push_back(as);
+                            w = cap;
+                        }
+                        for (const ClTerm& x : val[c]) {
+                            ClTerm y{ x.node, { w } };
+                            for (int m : x.chain) y.chain.push_back(m);
+                            t.push_back(y);
+                        }
+                    }
+                    val[r] = t;
+                }
+                continue;
+            }
+            if (closure_consumer(op)) {
+                // per term: its weight product and presence, then the consumer
+                LOp cons = op;
+                cons.argrw.clear();
+                cons.name = op.name == "__store_output" ? "__cl_store"
+                          : op.name == "__bsdf_eval"    ? "__cl_bsdf_eval"
+                                                        : "__cl_bsdf_sample";
+                cons.args.erase(cons.args.begin());
+                cons.imm[3] = op.imm[3];
+                for (const ClTerm& t : val[op.args[0]]) {
+                    int cw = none_sym, pres = none_sym;
+                    if (!t.chain.empty()) {
+                        const int acc = new_sym("$clacc", BT_TRIPLE, 0, VS_COLOR);
+                        LOp a0;
+                        a0.name = "assign";
+                        a0.args = { acc, t.chain[0] };
+                        out.push_back(a0);
+                        for (size_t j = 1; j < t.chain.size(); ++j) {
+                            LOp m;
+                            m.name = "mul";
+                            m.args = { acc, acc, t.chain[j] };
+                            out.push_back(m);
+                        }
+                        cw = new_sym("$clcw", BT_TRIPLE, 0, VS_COLOR);
+                        LOp mn;
+                        mn.name = "__cl_mulnode";
+                        mn.args = { cw, acc, t.node };
+                        out.push_back(mn);
+                        for (int m : t.chain) {
+                            if (const_zero(m) == 0) continue;  // a constant nonzero weight
+                            const int zero = syms[m].type.base == BT_TRIPLE
+                                               ? const_triple_sym({ 0.0f, 0.0f, 0.0f })
+                                               : const_float(0.0f);
+                            const int ne = new_sym("$clnz", BT_INT);
+                            LOp q;
+                            q.name = "neq";
+                            q.args = { ne, m, zero };
+                            out.push_back(q);
+                            if (pres == none_sym) {
+                                pres = ne;
+                            } else {
+                                LOp an;
+                                an.name = "and";
+                                an.args = { pres, pres, ne };
+                                out.push_back(an);
+                            }
+                        }
+                    }
+                    cons.args.push_back(t.node);
+                    cons.args.push_back(cw);
+                    cons.args.push_back(pres);
+                }
+                out.push_back(cons);
+                continue;
+            }
+            out.push_back(op);
+        }
+        newpos[n] = (int)out.size();
+        for (LOp& op : out)
+            for (int& j : op.jumps) j = newpos[std::min(std::max(j, 0), n)];
+        lops = std::move(out);
+        return true;
+    }
+    // a color constant created before storage assignment (no pool slot yet)
+    int const_triple_sym(const std::array<float, 3>& v) {
+        GSym d;
+        d.name = "$triple";
+        d.type.base = BT_TRIPLE;
+        d.type.vecsem = VS_COLOR;
+        d.kind = SK_CONST;
+        d.is_const = true;
+        d.cval = { v[0], v[1], v[2] };
+        return add_sym(d);
+    }
+
     void assign_storage() {
         for (const LOp& op : lops)
             for (int a : op.args) syms[a].referenced = true;
@@ -1678,6 +1911,56 @@ struct Lowerer {
                  "userdata");
             return true;
         }
+        if (n == "__cl_node") {
+            // a closure op whose node sits at a fixed heap slot (static closures)
+            size_t ni = 1;
+            int weight = -1;
+            if (na > 1 && !is_string(op.args[1])) { weight = op.args[1]; ni = 2; }
+            std::string cname = const_string(op.args[ni]);
+            auto it = ss.closure_ids.find(cname);
+            if (it == ss.closure_ids.end()) return fail("closure '" + cname + "' is not registered");
+            std::vector<uint32_t> params;
+            for (size_t i = ni + 1; i < na && params.size() < 11; ++i) params.push_back(A(op.args[i]));
+            while (params.size() < 11) params.push_back(kNoArg);
+            emit(OP_CLOSURE_NODE, { A(op.args[0]), (uint32_t)it->second, weight >= 0 ? A(weight) : kNoArg, params[0],
+                                    params[1], params[2], params[3] },
+                 "closure");
+            if (na > ni + 5)
+                emit(OP_NOP, { params[4], params[5], params[6], params[7], params[8], params[9], params[10] },
+                     "closure-params");
+            return true;
+        }
+        if (n == "__cl_mulnode") {
+            // cw = (MUL weight product) * the component's own weight (node words 1..3)
+            const uint32_t nw = arg_make((uint32_t)syms[op.args[2]].slot + 1u, false, false, TC_TRIPLE);
+            emit(OP_MUL, { a(0), a(1), nw }, "closure-weight");
+            return true;
+        }
+        if (n == "__cl_store" || n == "__cl_bsdf_eval" || n == "__cl_bsdf_sample") {
+            const size_t fixed = n == "__cl_store" ? 0 : (n == "__cl_bsdf_eval" ? 2 : 1);
+            const uint32_t nterms = (uint32_t)((na - fixed) / 3);
+            if (n == "__cl_store")
+                emit(OP_CL_STORE, { nterms, (uint32_t)op.imm[0], (uint32_t)op.imm[1], (uint32_t)op.imm[3] }, "output");
+            else if (n == "__cl_bsdf_eval")
+                emit(OP_CL_BSDF_EVAL, { nterms, (uint32_t)op.imm[0], (uint32_t)op.imm[1], a(0), a(1), string_hash("ggx") },
+                     "bsdf_eval");
+            else
+                emit(OP_CL_BSDF_SAMPLE, { nterms, (uint32_t)op.imm[0], (uint32_t)op.imm[1], a(0), string_hash("ggx"),
+                                          (uint32_t)op.imm[2], (uint32_t)op.imm[3] },
+                     "bsdf_sample");
+            // the term table: {node slot, weight operand, presence operand}, two per carrier
+            for (uint32_t j = 0; j < nterms; j += 2) {
+                uint32_t w[6] = { 0u, kNoArg, kNoArg, 0u, kNoArg, kNoArg };
+                for (uint32_t t = 0; t < 2 && j + t < nterms; ++t) {
+                    const size_t b = fixed + 3 * (j + t);
+                    w[3 * t + 0] = (uint32_t)syms[op.args[b]].slot;
+                    w[3 * t + 1] = op.args[b + 1] == none_sym ? kNoArg : A(op.args[b + 1]);
+                    w[3 * t + 2] = op.args[b + 2] == none_sym ? kNoArg : A(op.args[b + 2]);
+                }
+                emit(OP_NOP, { w[0], w[1], w[2], w[3], w[4], w[5], 0u }, "closure-terms");
+            }
+            return true;
+        }
         if (n == "__bsdf_eval") {
             // renderer-side evaluation of a closure output (testrender's
             // CompositeBSDF::eval, src/testrender/shading.h:364-374)
@@ -2010,7 +2293,7 @@ struct Lowerer {
             switch (op.code) {
             case OP_NOISE: case OP_HASH: case OP_GABOR: t |= 1u; break;
             case OP_CLOSURE: case OP_CLOSURE_MUL: case OP_CLOSURE_ADD: case OP_STORE_CLOSURE: case OP_BSDF_EVAL:
-            case OP_BSDF_SAMPLE:
+            case OP_BSDF_SAMPLE: case OP_CLOSURE_NODE: case OP_CL_STORE: case OP_CL_BSDF_EVAL: case OP_CL_BSDF_SAMPLE:
             case OP_SPLINE: case OP_SPLINEINV:
                 t |= 2u;
                 break;
@@ -2036,6 +2319,7 @@ struct Lowerer {
         if (!prepare_messages()) return false;
         if (ss.opts.opt_constant_fold) fold_constants();
         if (ss.opts.opt_elide_useless_ops) eliminate_dead_ops();
+        static_closures();
         analyze();
         assign_storage();
         if (!lower_all()) return false;

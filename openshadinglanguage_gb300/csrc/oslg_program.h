@@ -20,7 +20,7 @@
 namespace oslg {
 
 static const uint32_t kProgramMagic = 0x4f534c47u;  // "OSLG"
-static const uint32_t kProgramVersion = 5;
+static const uint32_t kProgramVersion = 6;
 
 // ---- operand words ----------------------------------------------------------
 // bits 0..19  slot offset (heap) or index (constant pool)
@@ -135,6 +135,15 @@ enum OpCode : uint16_t {
                      // a3=texture index | firstchannel << 16 a4=width
     OP_SPLINEINV,    // a0=r (float) a1=y (float) a2=knots (float array) a3=basis id
                      // a4=knot count operand or kNoArg a5=array length
+    // static closures (see kClosureAbsent): a closure tree whose shape the
+    // lowering knows is kept as one component node per closure op at a
+    // fixed heap slot; consumers visit a term table instead of walking
+    OP_CLOSURE_NODE, // as OP_CLOSURE, but a0 = the node's first heap slot (an int
+                     // operand) and no result handle
+    OP_CL_STORE,     // a0=terms a1=byte offset a2=byte stride a3=max components;
+                     // term table in the OP_NOP carriers that follow
+    OP_CL_BSDF_EVAL, // a0=terms a1..a5 as OP_BSDF_EVAL; term table follows
+    OP_CL_BSDF_SAMPLE,// a0=terms a1..a6 as OP_BSDF_SAMPLE; term table follows
     OP_COUNT
 };
 
@@ -195,6 +204,19 @@ static const int kNodeFloats = 16;
 static const int kClosureMul = -1;
 static const int kClosureAdd = -2;
 static const int kClosureWalkStack = 16;  // testrender's traversal stack
+// Static closures. When no closure value depends on control flow (no
+// closure write under an if or loop, no return or exit), the lowering knows
+// every closure's tree: each closure op gets a node at a fixed heap slot
+// ([id][w.rgb][12 params], id kClosureAbsent when its weight is zero), and
+// a consumer (record store, BSDF eval or sample) gets the walk of its tree
+// unrolled into a term table: per visited component, in the walk's order,
+// {node slot, weight operand, presence operand}. The weight operand is the
+// product of the MUL weights down to the component times its own weight,
+// computed by ordinary ops in the walk's order (kNoArg: the node's own
+// weight); the presence operand is an int that is 0 when some MUL weight
+// on the way is zero (kNoArg: always present). Two terms per carrier op.
+static const int kClosureAbsent = -3;
+static const int kMaxStaticTerms = 16;
 static const int kBsdfMaxLobes = 8;       // CompositeBSDF::MaxEntries
 
 struct ProgramHeader {

@@ -93,12 +93,15 @@ uint32_t staging_stride(const Op* ops, int n) {
             size = 4ll * arg_ncomp(op.a[0]) * std::max<uint32_t>(1u, op.a[4]) * ((op.a[3] & 1u) ? 3 : 1);
             break;
         case OP_STORE_CLOSURE:
+        case OP_CL_STORE:
             off = op.a[1];
             st = (int32_t)op.a[2];
             size = 4ll * (1 + (int64_t)op.a[3] * kNodeFloats);
             break;
-        case OP_BSDF_EVAL: off = op.a[1]; st = (int32_t)op.a[2]; size = 16; break;
-        case OP_BSDF_SAMPLE: off = op.a[1]; st = (int32_t)op.a[2]; size = 44; break;
+        case OP_BSDF_EVAL:
+        case OP_CL_BSDF_EVAL: off = op.a[1]; st = (int32_t)op.a[2]; size = 16; break;
+        case OP_BSDF_SAMPLE:
+        case OP_CL_BSDF_SAMPLE: off = op.a[1]; st = (int32_t)op.a[2]; size = 44; break;
         default: continue;
         }
         if (st <= 0 || st % 4 || off % 4 || off + size > st || (stride >= 0 && st != stride)) return 0;
@@ -144,9 +147,10 @@ ProgView view(const CompiledGroup& cg) {
 
 // Loop-free programs execute each closure op at most once per point, so
 // the closure walk is at most (ADD ops) deep and finds at most 2^(ADD ops)
-// leaves: those bounds replace the reference capacities (16, 8).
+// leaves: those bounds replace the reference capacities (16, 8). A static
+// consumer finds at most its term count of lobes.
 struct Bounds {
-    bool fixed = true;
+    bool fixed = true, any = false;
     int walk = 1, lobes = 1;
 };
 void add_bounds(Bounds& B, const ProgView& v) {
@@ -155,14 +159,19 @@ void add_bounds(Bounds& B, const ProgView& v) {
     for (int i = 0; i < v.n; ++i) {
         loops = loops || v.ops[i].code == OP_LOOP_BEGIN || v.ops[i].code == OP_JUMP;
         adds += v.ops[i].code == OP_CLOSURE_ADD;
+        if (v.ops[i].code == OP_CL_BSDF_EVAL || v.ops[i].code == OP_CL_BSDF_SAMPLE || v.ops[i].code == OP_CL_STORE) {
+            B.any = true;
+            B.lobes = std::max(B.lobes, std::min((int)kBsdfMaxLobes, std::max(1, (int)v.ops[i].a[0])));
+        }
     }
     if (!v.uses_cl) return;
+    B.any = true;
     if (loops) B.fixed = false;
     B.walk = std::max(B.walk, std::max(1, std::min(adds, (int)kClosureWalkStack)));
     B.lobes = std::max(B.lobes, std::min((int)kBsdfMaxLobes, 1 << std::min(adds, 3)));
 }
-void emit_bounds(std::ostringstream& o, const Bounds& B, bool any_closures) {
-    if (!any_closures || !B.fixed) return;
+void emit_bounds(std::ostringstream& o, const Bounds& B) {
+    if (!B.any || !B.fixed) return;
     o << "#define OSLG_FIXED_INDEX 1\n";
     o << "#define OSLG_WALK_STACK " << B.walk << "\n";
     o << "#define OSLG_LOBES_MAX " << B.lobes << "\n";
@@ -213,12 +222,21 @@ void emit_body(std::ostringstream& o, const ProgView& v, const std::string& sfx)
         case OP_LAYER_END: o << "        (void)a;\n        ctl_layer_end<1>(C);\n"; break;
         default:
             if (i + 1 < n) {
-                const Op& nx = ops[i + 1];
-                o << "        const Op nx = {" << nx.code << ", " << (unsigned)nx.nargs << ", " << (unsigned)nx.flags
-                  << ", ";
-                put_args(o, nx.a);
+                // the next op, or every OP_NOP carrier that follows (operand
+                // lists and term tables), as a literal array
+                int k = 1;
+                while (i + k < n && k < 9 && ops[i + k].code == OP_NOP) ++k;
+                if (k > 1) --k;
+                o << "        const Op nx[" << k << "] = {";
+                for (int j = 1; j <= k; ++j) {
+                    const Op& x = ops[i + j];
+                    o << (j > 1 ? ", " : "") << "{" << x.code << ", " << (unsigned)x.nargs << ", " << (unsigned)x.flags
+                      << ", ";
+                    put_args(o, x.a);
+                    o << "}";
+                }
                 o << "};\n        if (C.actm) exec_op<7>(R, L, " << op.code
-                  << "u, a, [&]() -> const Op* { return &nx; });\n";
+                  << "u, a, [&]() -> const Op* { return nx; });\n";
             } else {
                 o << "        if (C.actm) exec_op<7>(R, L, " << op.code
                   << "u, a, []() -> const Op* { return nullptr; });\n";
@@ -259,7 +277,7 @@ std::string spec_source(const CompiledGroup& cg, int min_blocks) {
       << " symbol slots, " << cpool << " closure-pool slots)\n";
     o << "#define OSLG_SPEC 1\n";
     if (stage) o << "#define OSLG_STAGE_STRIDE " << stage << "\n";
-    emit_bounds(o, B, uses_cl);
+    emit_bounds(o, B);
     o << "#include \"oslg_interp.cuh\"\n\nnamespace {\n";
     o << "using namespace oslg;\nusing namespace oslg::dev;\n\n";
     emit_body(o, v, "");
@@ -267,7 +285,7 @@ std::string spec_source(const CompiledGroup& cg, int min_blocks) {
     // registers per thread are capped at 65536 / (256 * min_blocks); by
     // default 64 for closure programs (latency-bound: more resident warps)
     // and 85 otherwise (measured on the layered-closure and fBm workloads)
-    if (min_blocks <= 0) min_blocks = uses_cl ? 4 : 3;
+    if (min_blocks <= 0) min_blocks = B.any ? 4 : 3;
     o << "extern \"C\" __global__ void __launch_bounds__(256, " << std::max(2, std::min(8, min_blocks)) << ") "
       << kKernelName
       << "(const __grid_constant__ oslg::dev::KArgs k, int pool_in_smem, int fill_unwritten) {\n";
@@ -320,17 +338,15 @@ SpecBatchKernel::~SpecBatchKernel() {
 
 std::string spec_batch_source(const std::vector<const CompiledGroup*>& cases) {
     Bounds B;
-    bool any_cl = false;
     std::vector<ProgView> vs;
     for (const CompiledGroup* cg : cases) {
         vs.push_back(view(*cg));
         add_bounds(B, vs.back());
-        any_cl = any_cl || vs.back().uses_cl;
     }
     std::ostringstream o;
     o << "// generated: persistent batch kernel specialized to " << cases.size() << " lowered programs\n";
     o << "#define OSLG_SPEC 1\n";
-    emit_bounds(o, B, any_cl);
+    emit_bounds(o, B);
     o << "#include \"oslg_interp.cuh\"\n\nnamespace {\n";
     o << "using namespace oslg;\nusing namespace oslg::dev;\n\n";
     for (size_t j = 0; j < vs.size(); ++j) {

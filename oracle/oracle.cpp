@@ -1127,10 +1127,11 @@ template <class F> void closure_walk(Point& P, const CPools& C, uint32_t root, F
 // (src/testrender/shading.cpp:1481-1530): emission accumulates Le,
 // diffuse / oren_nayar / GGX microfacet (params: dist, N, U, xalpha,
 // yalpha, eta, refract) become lobes in walk order; ggx_hash names "ggx".
-void build_lobes(Point& P, const CPools& C, uint32_t root, const V3& wo, uint32_t ggx_hash, CompositeLobes* L,
-                 float path_roughness = 0.0f, bool backfacing = false) {
+template <class WALK>
+void collect_lobes(Point& P, WALK&& walk, const V3& wo, uint32_t ggx_hash, CompositeLobes* L, float path_roughness,
+                   bool backfacing) {
     auto f = [&](uint32_t s) { return bitsf(P.heap[s]); };
-    closure_walk(P, C, root, [&](int id, const V3& cw, uint32_t p) {
+    walk([&](int id, const V3& cw, uint32_t p) {
         if (id == 1) {  // EMISSION_ID
             L->Le = L->Le + cw;
         } else if (id == 3) {  // DIFFUSE_ID
@@ -1147,6 +1148,29 @@ void build_lobes(Point& P, const CPools& C, uint32_t root, const V3& wo, uint32_
                                          f(p + 8), f(p + 9), refract));
         }
     });
+}
+void build_lobes(Point& P, const CPools& C, uint32_t root, const V3& wo, uint32_t ggx_hash, CompositeLobes* L,
+                 float path_roughness = 0.0f, bool backfacing = false) {
+    collect_lobes(
+        P, [&](auto&& visit) { closure_walk(P, C, root, visit); }, wo, ggx_hash, L, path_roughness, backfacing);
+}
+
+// Static closures (oslg_program.h kClosureAbsent): the components of a
+// known tree, visited in the walk's order from a consumer's term table
+// (term j in words 3*(j%2).. of the (j/2)-th carrier op after it:
+// node slot, weight operand or kNoArg, presence operand or kNoArg).
+template <class F>
+void closure_walk_static(Point& P, const oslg::Op* tab, uint32_t nterms, F&& visit) {
+    for (uint32_t j = 0; j < nterms; ++j) {
+        const uint32_t* t = tab[j / 2].a + 3 * (j % 2);
+        const uint32_t ns = t[0];
+        const int id = (int32_t)P.heap[ns];
+        if (id == oslg::kClosureAbsent) continue;
+        if (t[2] != oslg::kNoArg && word(P, t[2], 0) == 0u) continue;
+        V3 cw = t[1] == oslg::kNoArg ? V3(bitsf(P.heap[ns + 1]), bitsf(P.heap[ns + 2]), bitsf(P.heap[ns + 3]))
+                                     : V3(getf(P, t[1], 0, 0), getf(P, t[1], 1, 0), getf(P, t[1], 2, 0));
+        visit(id, cw, ns + 4);
+    }
 }
 
 struct Runner {
@@ -1439,16 +1463,29 @@ struct Runner {
             case oslg::OP_NOISE: op_noise(P, a); break;
             case oslg::OP_GABOR: op_gabor(P, a, prog.ops[pc + 1].a); break;
             case oslg::OP_HASH: op_hash(P, a); break;
-            case oslg::OP_CLOSURE: {
-                // osl_allocate_(weighted_)closure_component (opclosure.cpp:83-117)
+            case oslg::OP_CLOSURE:
+            case oslg::OP_CLOSURE_NODE: {
+                // osl_allocate_(weighted_)closure_component (opclosure.cpp:83-117);
+                // the static form writes its node at the slot of a0 and marks
+                // a zero-weight component absent instead of returning null
+                const bool stat = op.code == oslg::OP_CLOSURE_NODE;
                 V3 w(1.0f);
                 if (a[2] != oslg::kNoArg) {
                     w = V3(getf(P, a[2], 0, 0), getf(P, a[2], 1, 0), getf(P, a[2], 2, 0));
-                    if (w.x == 0.0f && w.y == 0.0f && w.z == 0.0f) { setw(P, a[0], 0, 0u); break; }
+                    if (w.x == 0.0f && w.y == 0.0f && w.z == 0.0f) {
+                        if (stat) P.heap[aoff(a[0])] = (uint32_t)oslg::kClosureAbsent;
+                        else setw(P, a[0], 0, 0u);
+                        break;
+                    }
                 }
-                uint32_t h = cl_alloc(P, C);
-                if (!h) { setw(P, a[0], 0, 0u); break; }
-                uint32_t ns = nslot(C, h - 1);
+                uint32_t h = 0, ns;
+                if (stat) {
+                    ns = aoff(a[0]);
+                } else {
+                    h = cl_alloc(P, C);
+                    if (!h) { setw(P, a[0], 0, 0u); break; }
+                    ns = nslot(C, h - 1);
+                }
                 P.heap[ns] = a[1];
                 P.heap[ns + 1] = fbits(w.x); P.heap[ns + 2] = fbits(w.y); P.heap[ns + 3] = fbits(w.z);
                 uint32_t params[11];
@@ -1465,7 +1502,7 @@ struct Runner {
                                                                                             : fbits(getf(P, params[i], c, 0));
                 }
                 for (; k < oslg::kClosureParamFloats; ++k) P.heap[ns + 4 + k] = fbits(0.0f);
-                setw(P, a[0], 0, h);
+                if (!stat) setw(P, a[0], 0, h);
                 break;
             }
             case oslg::OP_CLOSURE_MUL: {
@@ -1497,11 +1534,16 @@ struct Runner {
                 setw(P, a[0], 0, h);
                 break;
             }
-            case oslg::OP_STORE_CLOSURE: {
-                uint32_t root = word(P, a[0], 0), maxc = a[3];
+            case oslg::OP_STORE_CLOSURE:
+            case oslg::OP_CL_STORE: {
+                uint32_t maxc = a[3];
                 uint32_t* q = reinterpret_cast<uint32_t*>(outputs + (int64_t)a[1] + P.pt * (int64_t)(int32_t)a[2]);
                 uint32_t n = 0;
-                closure_walk(P, C, root, [&](int id, const V3& cw, uint32_t params) {
+                auto walk = [&](auto&& visit) {
+                    if (op.code == oslg::OP_CL_STORE) closure_walk_static(P, &prog.ops[pc + 1], a[0], visit);
+                    else closure_walk(P, C, word(P, a[0], 0), visit);
+                };
+                walk([&](int id, const V3& cw, uint32_t params) {
                     if (n >= maxc) return;
                     uint32_t* rec = q + 1 + n * oslg::kNodeFloats;
                     rec[0] = (uint32_t)id;
@@ -1512,31 +1554,41 @@ struct Runner {
                 q[0] = n;
                 break;
             }
-            case oslg::OP_BSDF_EVAL: {
+            case oslg::OP_BSDF_EVAL:
+            case oslg::OP_CL_BSDF_EVAL: {
                 // testrender CompositeBSDF built by the closure walk, then
                 // prepare(wo, 1, absorb=false) and eval(wo, wi) (shading.h:322-374)
-                uint32_t root = word(P, a[0], 0);
                 V3 wi(getf(P, a[3], 0, 0), getf(P, a[3], 1, 0), getf(P, a[3], 2, 0));
                 V3 wo(-getf(P, a[4], 0, 0), -getf(P, a[4], 1, 0), -getf(P, a[4], 2, 0));
                 CompositeLobes L;
-                build_lobes(P, C, root, wo, a[5], &L);
+                if (op.code == oslg::OP_CL_BSDF_EVAL)
+                    collect_lobes(
+                        P, [&](auto&& visit) { closure_walk_static(P, &prog.ops[pc + 1], a[0], visit); }, wo, a[5],
+                        &L, 0.0f, false);
+                else
+                    build_lobes(P, C, word(P, a[0], 0), wo, a[5], &L);
                 L.prepare(wo, V3(1.0f), false);
                 Sample sres = L.eval(wo, wi);
                 float* o = reinterpret_cast<float*>(outputs + (int64_t)a[1] + P.pt * (int64_t)(int32_t)a[2]);
                 o[0] = sres.weight.x; o[1] = sres.weight.y; o[2] = sres.weight.z; o[3] = sres.pdf;
                 break;
             }
-            case oslg::OP_BSDF_SAMPLE: {
+            case oslg::OP_BSDF_SAMPLE:
+            case oslg::OP_CL_BSDF_SAMPLE: {
                 // process_closure + prepare(wo, path_weight, absorb) + sample
                 // (simpleraytracer.cpp:1038-1079, shading.h:322-398). Userdata
                 // record: rx ry rz, path weight rgb, absorb, ray roughness,
                 // backfacing; output record: wi xyz, weight rgb, pdf, Le rgb,
                 // roughness.
-                uint32_t root = word(P, a[0], 0);
                 V3 wo(-getf(P, a[3], 0, 0), -getf(P, a[3], 1, 0), -getf(P, a[3], 2, 0));
                 const float* in = reinterpret_cast<const float*>(userdata + (int64_t)a[5] + P.pt * (int64_t)(int32_t)a[6]);
                 CompositeLobes L;
-                build_lobes(P, C, root, wo, a[4], &L, in[7], in[8] != 0.0f);
+                if (op.code == oslg::OP_CL_BSDF_SAMPLE)
+                    collect_lobes(
+                        P, [&](auto&& visit) { closure_walk_static(P, &prog.ops[pc + 1], a[0], visit); }, wo, a[4],
+                        &L, in[7], in[8] != 0.0f);
+                else
+                    build_lobes(P, C, word(P, a[0], 0), wo, a[4], &L, in[7], in[8] != 0.0f);
                 L.prepare(wo, V3(in[3], in[4], in[5]), in[6] != 0.0f);
                 Sample sres = L.sample(wo, in[0], in[1], in[2]);
                 float* o = reinterpret_cast<float*>(outputs + (int64_t)a[1] + P.pt * (int64_t)(int32_t)a[2]);
