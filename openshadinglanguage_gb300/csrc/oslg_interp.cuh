@@ -1695,10 +1695,12 @@ struct Lobes {
 };
 // Loops over the lobe list: unrolled over the capacity (constant indices)
 // in a fixed-index build, a plain loop over n otherwise.
+// A lobe position with kind < 0 holds no lobe (static term tables keep
+// one position per term).
 #ifdef OSLG_FIXED_INDEX
-#define OSLG_FOR_LOBES(i, B) _Pragma("unroll") for (int i = 0; i < OSLG_LOBES_MAX; ++i) if (i < (B).n)
+#define OSLG_FOR_LOBES(i, B) _Pragma("unroll") for (int i = 0; i < OSLG_LOBES_MAX; ++i) if (i < (B).n && (B).kind[i] >= 0)
 #else
-#define OSLG_FOR_LOBES(i, B) for (int i = 0; i < (B).n; ++i)
+#define OSLG_FOR_LOBES(i, B) for (int i = 0; i < (B).n; ++i) if ((B).kind[i] >= 0)
 #endif
 // process_closure's lobes (shading.cpp:1481-1530) from the components a walk
 // visits: `walk(visit)` calls visit(id, weight, parameter slot) for each
@@ -1914,6 +1916,47 @@ __device__ __forceinline__ void closure_walk_static(const Lane& L, const Op* tab
         visit(id, cw, ns + 4);
     }
 }
+// The lobes of a term table, one position per term (kind -1 where the term
+// is absent, is no lobe, or comes after CompositeBSDF's capacity is full),
+// so that every lobe's parameter slots stay compile-time constants in a
+// specialized kernel. Lobes in position order are the walk's lobes.
+__device__ __forceinline__ void lobes_collect_static(const Lane& L, const Op* tab, uint32_t nterms, uint32_t ggx,
+                                                     Lobes& B, float path_rough, bool backfacing) {
+    B.n = (int)nterms;
+    B.Le[0] = B.Le[1] = B.Le[2] = 0.0f;
+    B.path_rough = path_rough;
+    B.backfacing = backfacing;
+    int count = 0;
+    OSLG_SPEC_UNROLL
+    for (int j = 0; j < OSLG_LOBES_MAX; ++j) {
+        if (j >= (int)nterms) break;
+        B.kind[j] = -1;
+        const uint32_t ns = term_word(tab, j, 0), cwop = term_word(tab, j, 1), pop = term_word(tab, j, 2);
+        const int id = (int)sgetu(L, ns);
+        if (id == kClosureAbsent) continue;
+        if (pop != kNoArg && ldw(L, pop, 0) == 0u) continue;
+        float cw[3];
+        for (int k = 0; k < 3; ++k) cw[k] = cwop == kNoArg ? sget(L, ns + 1 + k) : ldf(L, cwop, k, 0);
+        const uint32_t params = ns + 4;
+        int k = -1;
+        if (id == 1) {  // EMISSION_ID
+            for (int c = 0; c < 3; ++c) B.Le[c] = B.Le[c] + cw[c];
+            continue;
+        }
+        if (id == 3) k = 0;  // DIFFUSE_ID
+        else if (id == 4) k = 2;  // OREN_NAYAR_ID
+        else if (id == 23 && sgetu(L, params + 7) == 0u) k = 3;  // MX_SHEEN_ID, Conty-Kulla mode
+        else if (id == 8 && sgetu(L, params + 0) == ggx) {  // MICROFACET_ID "ggx"
+            const int r = (int)sgetu(L, params + 10);
+            if (r >= 0 && r <= 2) k = 1;
+        }
+        if (k < 0 || count >= kBsdfMaxLobes) continue;
+        B.kind[j] = k;
+        for (int c = 0; c < 3; ++c) B.w[j][c] = cw[c];
+        B.p[j] = params;
+        ++count;
+    }
+}
 // records as h_store_closure writes them
 static __device__ void h_cl_store(const Lane& L, const uint32_t* a, const Op* tab, char* base) {
     const uint32_t maxc = a[3];
@@ -1934,8 +1977,7 @@ static __device__ void h_cl_bsdf_eval(const Lane& L, const uint32_t* a, const Op
     const V3 wi = v3(ldf(L, a[3], 0, 0), ldf(L, a[3], 1, 0), ldf(L, a[3], 2, 0));
     const V3 wo = v3(-ldf(L, a[4], 0, 0), -ldf(L, a[4], 1, 0), -ldf(L, a[4], 2, 0));
     Lobes B;
-    lobes_collect<SymNodes>(
-        L, [&](auto&& visit) { closure_walk_static(L, tab, a[0], visit); }, a[5], B, 0.0f, false);
+    lobes_collect_static(L, tab, a[0], a[5], B, 0.0f, false);
     const float one[3] = { 1.0f, 1.0f, 1.0f };
     lobes_prepare<SymNodes>(L, B, wo, one, false);
     const BsdfSample r = lobes_eval<SymNodes>(L, B, wo, wi);
@@ -1950,8 +1992,7 @@ static __device__ void h_cl_bsdf_sample(const Lane& L, const uint32_t* a, const 
     const V3 wo = v3(-ldf(L, a[3], 0, 0), -ldf(L, a[3], 1, 0), -ldf(L, a[3], 2, 0));
     const float* in = reinterpret_cast<const float*>(ud + (int64_t)a[5] + L.pt * (int64_t)(int32_t)a[6]);
     Lobes B;
-    lobes_collect<SymNodes>(
-        L, [&](auto&& visit) { closure_walk_static(L, tab, a[0], visit); }, a[4], B, in[7], in[8] != 0.0f);
+    lobes_collect_static(L, tab, a[0], a[4], B, in[7], in[8] != 0.0f);
     const float pw[3] = { in[3], in[4], in[5] };
     lobes_prepare<SymNodes>(L, B, wo, pw, in[6] != 0.0f);
     const BsdfSample r = lobes_sample<SymNodes>(L, B, wo, in[0], in[1], in[2]);

@@ -1016,7 +1016,9 @@ struct Lowerer {
             if (!refs || op.name == "useparam") continue;
             if (closure_consumer(op)) {
                 if (depth[k]) return false;
-                if (val[op.args[0]].size() > (size_t)kMaxStaticTerms) return false;
+                // a BSDF consumer keeps one lobe position per term
+                const size_t cap = op.name == "__store_output" ? kMaxStaticTerms : kBsdfMaxLobes;
+                if (val[op.args[0]].size() > cap) return false;
                 continue;
             }
             if (!closure_writer(op) || depth[k]) return false;

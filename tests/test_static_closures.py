@@ -33,9 +33,11 @@ def stress_shader():
         closure color w2 = color(u, v, 0.5) * (w1 + m);
         closure color w3 = 0.5 * (w2 + d + w1);
         closure color z = (closure weighted by v - 0.5) oren_nayar(N, 0.3);  // null at v == 0.5
-        Ci = w3 + w3 + (v * emission()) + z + 0 * d;  // the last term is null
+        Ci = w3 + (v * emission()) + z + 0 * d;  // the last term is null
+        big = w3 + w3 + (v * emission()) + z;    // 10 terms, 8 records kept
     """
     b = OsoBuilder("stat", "surface")
+    big = b.param("closure color", "big", 0.0, output=True)
     Ci, N, dPdu = b.glob("closure color", "Ci"), b.glob("normal", "N"), b.glob("vector", "dPdu")
     u, v = b.glob("float", "u"), b.glob("float", "v")
     cl = lambda: b.tmp("closure color")
@@ -60,18 +62,22 @@ def stress_shader():
     b.op("sub", vm, v, f(0.5))
     b.op("color", vw, vm, vm, vm)
     b.op("closure", z, vw, S("oren_nayar"), N, f(0.3))
-    t1, t2, t3, zd, t4 = cl(), cl(), cl(), cl(), cl()
-    b.op("add", t1, w3, w3)
-    b.op("add", t2, t1, ve)
+    t2, t3, zd, t4 = cl(), cl(), cl(), cl()
+    b.op("add", t2, w3, ve)
     b.op("add", t3, t2, z)
     b.op("mul", zd, f(0.0), d)
     b.op("add", t4, t3, zd)
     b.op("assign", Ci, t4)
+    b1, b2, b3 = cl(), cl(), cl()
+    b.op("add", b1, w3, w3)
+    b.op("add", b2, b1, ve)
+    b.op("add", b3, b2, z)
+    b.op("assign", big, b3)
     return b.text()
 
 
 REC = 1 + 16 * 8
-STRIDE = 4 * (REC + 4)
+STRIDE = 4 * (2 * REC + 4)
 
 
 def stress_group(ss):
@@ -79,8 +85,9 @@ def stress_group(ss):
     g = ss.ShaderGroupBegin("stat_group")
     ss.Shader(g, "surface", "stat", "L")
     ss.ShaderGroupEnd(g)
-    ss.add_symlocs(g, [og.SymLocationDesc("Ci", og.TypeClosure.array(8), False, og.SymArenaOutputs, 0, STRIDE)])
-    ss.bsdf_eval_output(g, "Ci", (0.3, 0.4, 0.866), 4 * REC, STRIDE)
+    ss.add_symlocs(g, [og.SymLocationDesc("Ci", og.TypeClosure.array(8), False, og.SymArenaOutputs, 0, STRIDE),
+                       og.SymLocationDesc("L.big", og.TypeClosure.array(8), False, og.SymArenaOutputs, 4 * REC, STRIDE)])
+    ss.bsdf_eval_output(g, "Ci", (0.3, 0.4, 0.866), 8 * REC, STRIDE)
     return g
 
 
@@ -121,8 +128,11 @@ def test_stress_group_static_equals_tree():
     counts = s[:, 0].view(np.int32)
     assert counts.min() < counts.max()  # nulls removed components at some points
     assert float_equal(s, t).all()
-    ids = s[:, 1:REC].reshape(n, 8, 16)[:, :, 0].view(np.int32)
-    assert np.array_equal(ids, t[:, 1:REC].reshape(n, 8, 16)[:, :, 0].view(np.int32))
+    assert np.array_equal(s.view(np.int32)[:, REC], t.view(np.int32)[:, REC])
+    assert s.view(np.int32)[:, REC].max() == 8  # the big sum keeps its first 8 components
+    for base in (0, REC):
+        ids = s[:, base + 1:base + REC].reshape(n, 8, 16)[:, :, 0].view(np.int32)
+        assert np.array_equal(ids, t[:, base + 1:base + REC].reshape(n, 8, 16)[:, :, 0].view(np.int32))
 
 
 def test_layered_closure_group_static_equals_tree():
