@@ -337,6 +337,10 @@ typedef struct oslg_batch_tuning {
     float ms;        /* measured milliseconds per launch (autotune only) */
 } oslg_batch_tuning;
 
+/* With the system attribute "jit" set when the batch is created, the batch
+ * runs one persistent kernel specialized to its distinct programs (each a
+ * specialized body, see oslg_group_specialized_source; built once per set
+ * of programs and cached), with the same results. */
 int oslg_batch_create(oslg_system* sys, oslg_batch** out);
 int oslg_batch_destroy(oslg_batch* batch);
 /* Drop all requests (device tables are kept for reuse). */

@@ -4,8 +4,11 @@
 #include <string>
 #include <vector>
 
+#include <memory>
+
 #include "oslg_exec.h"
 #include "oslg_host.h"
+#include "oslg_spec.h"
 
 namespace oslg {
 
@@ -15,6 +18,7 @@ struct BatchLaunch {
     int heap_smem = -1;  // 1 shared memory, 0 HBM, -1 shared memory when it fits 100 KiB
     int grid = 0;        // 0: SMs x resident CTAs per SM
     int use_graph = 1;   // replay a captured CUDA graph
+    int jit = 0;         // run the groups' specialized bodies (one kernel built for the batch's programs)
 };
 
 struct BatchTuneResult {
@@ -42,6 +46,11 @@ public:
     void clear();
     void add(const CompiledGroup& cg, int64_t npoints, const oslg_shaderglobals& G, void* userdata, void* outputs);
     void set_launch(const BatchLaunch& l);
+    // Where specialized kernels are generated from and cached (jit launches).
+    void set_jit_dirs(const std::string& csrc, const std::string& cache) {
+        jit_csrc_ = csrc;
+        jit_cache_ = cache;
+    }
     int execute(DeviceState& ds, void* stream, std::string* err);
     int autotune(DeviceState& ds, void* stream, int reps, BatchTuneResult* results, int cap, int* n,
                  BatchLaunch* best, std::string* err);
@@ -78,6 +87,14 @@ private:
     void* graph_ = nullptr;
     void* gexec_ = nullptr;
     void* cap_stream_ = nullptr;
+    // specialized persistent kernel (jit): one body per distinct program
+    std::string jit_csrc_, jit_cache_;
+    std::unique_ptr<SpecBatchKernel> spec_;
+    std::vector<const CompiledGroup*> spec_cases_;
+    int spec_pool_smem_ = 0;
+    float* d_spec_heap_ = nullptr;
+    size_t spec_heap_bytes_ = 0;
+    int build_jit(DeviceState& ds, std::string* err);
 };
 
 }  // namespace oslg

@@ -120,11 +120,15 @@ void BatchExecutor::release() {
     cudaFree(d_items_);
     cudaFree(d_counter_);
     cudaFree(d_heap_);
+    cudaFree(d_spec_heap_);
     d_jobs_ = nullptr;
     d_items_ = nullptr;
     d_counter_ = nullptr;
     d_heap_ = nullptr;
-    jobs_cap_ = items_cap_ = heap_bytes_ = 0;
+    d_spec_heap_ = nullptr;
+    jobs_cap_ = items_cap_ = heap_bytes_ = spec_heap_bytes_ = 0;
+    spec_.reset();
+    spec_cases_.clear();
 }
 
 void BatchExecutor::clear() {
@@ -165,10 +169,134 @@ int BatchExecutor::ensure_ready(DeviceState& ds, std::string* err) {
     return OSLG_OK;
 }
 
+// Upload the job table and work list (items (job, tile), heaviest jobs first).
+static int upload_tables(std::vector<dev::BatchJob>& jobs, std::vector<uint2>& items, dev::BatchJob** d_jobs,
+                         size_t* jobs_cap, uint2** d_items, size_t* items_cap, std::string* err) {
+    if (jobs.size() > *jobs_cap) {
+        cudaFree(*d_jobs);
+        *d_jobs = nullptr;
+        if (!ok(cudaMalloc(d_jobs, jobs.size() * sizeof(dev::BatchJob)), err, "cudaMalloc jobs")) return OSLG_ERR_CUDA;
+        *jobs_cap = jobs.size();
+    }
+    if (items.size() > *items_cap) {
+        cudaFree(*d_items);
+        *d_items = nullptr;
+        if (!ok(cudaMalloc(d_items, items.size() * sizeof(uint2)), err, "cudaMalloc items")) return OSLG_ERR_CUDA;
+        *items_cap = items.size();
+    }
+    if (!jobs.empty() &&
+        !ok(cudaMemcpy(*d_jobs, jobs.data(), jobs.size() * sizeof(dev::BatchJob), cudaMemcpyHostToDevice), err,
+            "upload jobs"))
+        return OSLG_ERR_CUDA;
+    if (!items.empty() &&
+        !ok(cudaMemcpy(*d_items, items.data(), items.size() * sizeof(uint2), cudaMemcpyHostToDevice), err,
+            "upload items"))
+        return OSLG_ERR_CUDA;
+    return OSLG_OK;
+}
+
+// The jit launch: a persistent kernel whose cases are the batch's distinct
+// programs, each a specialized body (the reference JITs each group, then
+// renderers call it per batch; here one launch runs them all). Tiles are
+// one point per thread; closure pools in shared memory when they fit.
+int BatchExecutor::build_jit(DeviceState& ds, std::string* err) {
+    std::vector<int> order(entries_.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return entries_[a].cost > entries_[b].cost; });
+    std::vector<const CompiledGroup*> cases;
+    std::vector<int> case_of(entries_.size(), 0);
+    for (int i : order) {
+        const CompiledGroup* cg = entries_[i].cg;
+        auto it = std::find(cases.begin(), cases.end(), cg);
+        case_of[i] = (int)(it - cases.begin());
+        if (it == cases.end()) cases.push_back(cg);
+    }
+    if (!spec_ || cases != spec_cases_) {
+        if (jit_csrc_.empty()) {
+            if (err) *err = "batch: no source directory for specialized kernels";
+            return OSLG_ERR_STATE;
+        }
+        auto k = std::make_unique<SpecBatchKernel>();
+        int rc = spec_batch_build(cases, jit_csrc_, jit_cache_, k.get(), err);
+        if (rc != OSLG_OK) return rc;
+        spec_ = std::move(k);
+        spec_cases_ = cases;
+    }
+    int block = want_.block > 0 ? want_.block : 256;
+    block = std::max(32, std::min(256, (block + 31) & ~31));
+    const void* fn = spec_->kernel;
+    const size_t pool_b = (size_t)spec_->pool_slots * block * sizeof(float);
+    const bool smem = pool_b > 0 && pool_b <= 100 * 1024 && want_.heap_smem != 0;
+    const size_t shmem = smem ? pool_b : 0;
+    if (shmem > 48 * 1024 &&
+        !ok(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shmem), err,
+            "specialized kernel attribute"))
+        return OSLG_ERR_CUDA;
+    int per_sm = 0;
+    if (!ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, block, shmem), err, "occupancy"))
+        return OSLG_ERR_CUDA;
+    if (per_sm < 1) {
+        if (err) *err = "specialized batch launch does not fit on an SM";
+        return OSLG_ERR_LOWER;
+    }
+    int grid = ds.sm_count * per_sm;
+    if (want_.grid > 0) grid = want_.grid;
+    std::vector<dev::BatchJob> jobs(entries_.size());
+    std::vector<uint2> items;
+    for (size_t j = 0; j < order.size(); ++j) {
+        const BatchEntry& e = entries_[order[j]];
+        dev::BatchJob& J = jobs[j];
+        J.blob = static_cast<const uint8_t*>(e.cg->d_blob);
+        J.npoints = e.npoints;
+        J.userdata = static_cast<char*>(e.userdata);
+        J.outputs = static_cast<char*>(e.outputs);
+        J.G = e.G;
+        J.spec_case = case_of[order[j]];
+        const int64_t tiles = (e.npoints + block - 1) / block;
+        for (int64_t t = 0; t < tiles; ++t) items.push_back(make_uint2((unsigned)j, (unsigned)t));
+    }
+    int rc = upload_tables(jobs, items, &d_jobs_, &jobs_cap_, &d_items_, &items_cap_, err);
+    if (rc != OSLG_OK) return rc;
+    if (!smem && pool_b > 0 && (size_t)grid * pool_b > spec_heap_bytes_) {
+        cudaFree(d_spec_heap_);
+        d_spec_heap_ = nullptr;
+        spec_heap_bytes_ = 0;
+        if (!ok(cudaMalloc(&d_spec_heap_, (size_t)grid * pool_b), err, "cudaMalloc closure pools"))
+            return OSLG_ERR_CUDA;
+        spec_heap_bytes_ = (size_t)grid * pool_b;
+    }
+    args_ = dev::BatchArgs{};
+    args_.jobs = d_jobs_;
+    args_.items = d_items_;
+    args_.nitems = (uint32_t)items.size();
+    args_.counter = d_counter_;
+    args_.gheap = smem ? nullptr : d_spec_heap_;
+    args_.status = ds.d_status;
+    args_.textures = ds.d_textures;
+    args_.ntextures = ds.ntextures;
+    args_.heap_slots = spec_->pool_slots;
+    spec_pool_smem_ = smem ? 1 : 0;
+    cur_.block = block;
+    cur_.points_per_thread = 1;
+    cur_.heap_smem = smem ? 1 : 0;
+    cur_.grid = grid;
+    cur_.use_graph = want_.use_graph;
+    cur_.jit = 1;
+    shmem_ = shmem;
+    per_sm_ = per_sm;
+    if (gexec_) cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(gexec_));
+    if (graph_) cudaGraphDestroy(static_cast<cudaGraph_t>(graph_));
+    gexec_ = graph_ = nullptr;
+    dirty_ = false;
+    return OSLG_OK;
+}
+
 // Work list, job table, heap and launch shape for the requested launch.
 int BatchExecutor::build(DeviceState& ds, std::string* err) {
     int rc = ensure_ready(ds, err);
     if (rc != OSLG_OK) return rc;
+    if (want_.jit) return build_jit(ds, err);
     BatchLaunch L = want_;
     int block = L.block > 0 ? L.block : 256;
     block = std::max(32, std::min(512, (block + 31) & ~31));
@@ -219,26 +347,8 @@ int BatchExecutor::build(DeviceState& ds, std::string* err) {
         const int64_t tiles = (e.npoints + tile - 1) / tile;
         for (int64_t t = 0; t < tiles; ++t) items.push_back(make_uint2((unsigned)j, (unsigned)t));
     }
-    if (jobs.size() > jobs_cap_) {
-        cudaFree(d_jobs_);
-        d_jobs_ = nullptr;
-        if (!ok(cudaMalloc(&d_jobs_, jobs.size() * sizeof(dev::BatchJob)), err, "cudaMalloc jobs")) return OSLG_ERR_CUDA;
-        jobs_cap_ = jobs.size();
-    }
-    if (items.size() > items_cap_) {
-        cudaFree(d_items_);
-        d_items_ = nullptr;
-        if (!ok(cudaMalloc(&d_items_, items.size() * sizeof(uint2)), err, "cudaMalloc items")) return OSLG_ERR_CUDA;
-        items_cap_ = items.size();
-    }
-    if (!jobs.empty() &&
-        !ok(cudaMemcpy(d_jobs_, jobs.data(), jobs.size() * sizeof(dev::BatchJob), cudaMemcpyHostToDevice), err,
-            "upload jobs"))
-        return OSLG_ERR_CUDA;
-    if (!items.empty() &&
-        !ok(cudaMemcpy(d_items_, items.data(), items.size() * sizeof(uint2), cudaMemcpyHostToDevice), err,
-            "upload items"))
-        return OSLG_ERR_CUDA;
+    rc = upload_tables(jobs, items, &d_jobs_, &jobs_cap_, &d_items_, &items_cap_, err);
+    if (rc != OSLG_OK) return rc;
     if (!smem) {
         size_t need = (size_t)grid * heap_b;
         if (need > heap_bytes_) {
@@ -264,6 +374,7 @@ int BatchExecutor::build(DeviceState& ds, std::string* err) {
     cur_.heap_smem = smem ? 1 : 0;
     cur_.grid = grid;
     cur_.use_graph = L.use_graph;
+    cur_.jit = 0;
     shmem_ = shmem;
     maxt_ = maxt;
     per_sm_ = per_sm;
@@ -279,6 +390,15 @@ int BatchExecutor::enqueue(void* stream, std::string* err) {
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (!ok(cudaMemsetAsync(d_counter_, 0, sizeof(uint32_t), s), err, "counter reset")) return OSLG_ERR_CUDA;
     if (args_.nitems == 0) return OSLG_OK;
+    if (cur_.jit) {
+        int pool_smem = spec_pool_smem_;
+        void* kargs[] = { &args_, &pool_smem };
+        if (!ok(cudaLaunchKernel(spec_->kernel, dim3((unsigned)cur_.grid), dim3((unsigned)cur_.block), kargs, shmem_,
+                                 s),
+                err, "specialized batch launch"))
+            return OSLG_ERR_CUDA;
+        return OSLG_OK;
+    }
     if (!ok((cudaError_t)variant(maxt_, cur_.points_per_thread)
                 .launch(cur_.heap_smem == 1, (unsigned)cur_.grid, (unsigned)cur_.block, shmem_, stream, args_),
             err, "batch launch"))
@@ -343,19 +463,24 @@ int BatchExecutor::autotune(DeviceState& ds, void* stream, int reps, BatchTuneRe
         return OSLG_ERR_CUDA;
     }
     int rc = OSLG_OK;
+    // a jit batch has one kernel: only its block size (128 or 256) is swept
+    const bool jit = keep.jit != 0;
     for (int ppt : { 1, 2, 4 }) {
+    if (jit && ppt != 1) break;
     for (int block : { 128, 256, 512 }) {
+        if (jit && block > 256) break;
         for (int heap : { 1, 0 }) {
             BatchLaunch l = keep;
             l.block = block;
             l.points_per_thread = ppt;
             l.heap_smem = heap;
             l.use_graph = 0;
+            if (jit && heap == 0) continue;  // pools placed automatically
             want_ = l;
             dirty_ = true;
             std::string e2;
             int r2 = build(ds, &e2);
-            if (r2 != OSLG_OK || cur_.heap_smem != heap) continue;  // does not fit: skip
+            if (r2 != OSLG_OK || (!jit && cur_.heap_smem != heap)) continue;  // does not fit: skip
             if ((rc = enqueue(stream, err)) != OSLG_OK) break;      // warm-up
             if (!ok(cudaEventRecord(e0, s), err, "event record")) { rc = OSLG_ERR_CUDA; break; }
             for (int r = 0; r < std::max(1, reps) && rc == OSLG_OK; ++r) rc = enqueue(stream, err);

@@ -65,6 +65,7 @@ struct oslg_group {
 struct oslg_batch {
     oslg_system* sys;
     oslg::BatchExecutor ex;
+    int jit = 0;  // the system's "jit" attribute when the batch was created
 };
 
 struct oslg_server {
@@ -985,6 +986,14 @@ int oslg_batch_create(oslg_system* sys, oslg_batch** out) {
     return guarded(sys, [&]() {
         oslg_batch* b = new oslg_batch;
         b->sys = sys;
+        b->jit = sys->jit ? 1 : 0;
+        if (b->jit) {
+            const std::string dir = library_dir();
+            b->ex.set_jit_dirs(dir + "/csrc", dir + "/_build/jit");
+            BatchLaunch l;
+            l.jit = 1;
+            b->ex.set_launch(l);
+        }
         *out = b;
         return OSLG_OK;
     });
@@ -1025,6 +1034,7 @@ int oslg_batch_set_launch(oslg_batch* batch, int block, int points_per_thread, i
     l.points_per_thread = points_per_thread > 0 ? points_per_thread : (cur.points_per_thread > 0 ? cur.points_per_thread : 1);
     l.heap_smem = heap_smem;
     l.use_graph = use_graph ? 1 : 0;
+    l.jit = batch->jit;
     batch->ex.set_launch(l);
     return OSLG_OK;
 }

@@ -126,6 +126,23 @@ def test_autotuned_batch_matches_plain(c3):
         assert same(a, b), r.name
 
 
+def test_jit_batch_matches_plain(c3):
+    """A batch created with the system attribute "jit" runs one persistent
+    kernel specialized to its programs: same bits as the plain interpreter
+    launches, with graph replay and after its (block size) autotune."""
+    ss, reqs, plain = c3
+    pick = list(range(0, len(reqs), 6))
+    ssj = og.ShadingSystem()
+    ssj.attribute("jit", 1)
+    jreqs = c3_requests(ssj, groups={reqs[i].k for i in pick})
+    got, launch, (best, cands) = run_batch(ssj, jreqs, use_graph=True, tune=True, times=2)
+    assert {c["block"] for c in cands} <= {128, 256} and len(cands) >= 1
+    assert launch["points_per_thread"] == 1
+    for i, r, a in zip(pick, jreqs, got):
+        assert same(a, plain[i]), r.name
+    assert ssj.device_status() == 0
+
+
 def test_batch_with_closure_group_and_empty_requests():
     ss = og.ShadingSystem()
     reqs = c3_requests(ss, scale=256, groups={1, 9, 30})
