@@ -209,10 +209,13 @@ WORKLOADS = {FbmCell.name: FbmCell, LayeredClosure.name: LayeredClosure}
 DEFAULT_WORKLOAD = LayeredClosure.name
 
 
-def bench_batching(torch, og, reps=5):
+def bench_batching(torch, og, reps=5, jit=1):
     """64 seeded random groups (20-200 ops, log-uniform 1K-1M points): the
     plain executor launched per group against the persistent batch launch
-    (autotuned, CUDA-graph replay). Same outputs bit for bit."""
+    (autotuned, CUDA-graph replay), interpreted and, with jit, as one
+    persistent kernel specialized to the 64 programs. Same outputs bit for
+    bit. The CPU figure is the oracle over a sample of every group's points
+    on all host threads."""
     from openshadinglanguage_gb300 import workloads
     ss = og.ShadingSystem()
     specs = workloads.c3_specs()
@@ -250,12 +253,60 @@ def bench_batching(torch, og, reps=5):
                  points_per_thread=best["points_per_thread"])
     t_batch = timed(lambda: b.execute(sh))
     b.close()
-    return {"workload": "64 random groups, %d points, seed 0xC3" % total, "points": total,
-            "plain_ms": t_plain, "plain_mpts": total / t_plain / 1e3,
-            "persistent_ms": t_batch, "persistent_mpts": total / t_batch / 1e3,
-            "speedup_vs_plain": t_plain / t_batch,
-            "autotuned": {k: best[k] for k in ("block", "points_per_thread", "heap_smem", "grid")},
-            "candidates": len(cands), "launches_per_step": {"plain": len(reqs), "persistent": 1}}
+    ref = [o.cpu().numpy().copy() for (_, _, _, _, o) in reqs]
+    out = {"workload": "64 random groups, %d points, seed 0xC3" % total, "points": total,
+           "plain_ms": t_plain, "plain_mpts": total / t_plain / 1e3,
+           "persistent_ms": t_batch, "persistent_mpts": total / t_batch / 1e3,
+           "speedup_vs_plain": t_plain / t_batch,
+           "autotuned": {k: best[k] for k in ("block", "points_per_thread", "heap_smem", "grid")},
+           "candidates": len(cands), "launches_per_step": {"plain": len(reqs), "persistent": 1}}
+    if jit:
+        # the same requests through a batch specialized to the 64 programs
+        ssj = og.ShadingSystem()
+        ssj.attribute("jit", 1)
+        bj = ssj.batch()
+        jouts = []
+        for k, (name, oso, npts, _) in enumerate(specs):
+            g = workloads.c3_group(ssj, name, oso)
+            o = torch.zeros(npts * workloads.C3_REC, device="cuda")
+            jouts.append(o)
+            bj.add(g, npts, reqs[k][2], 0, o.data_ptr())
+        t0 = time.perf_counter()
+        bestj, _ = bj.autotune(sh, reps=2)
+        t_build = time.perf_counter() - t0
+        bj.set_launch(block=bestj["block"], heap_smem=bestj["heap_smem"], use_graph=True, points_per_thread=1)
+        t_jit = timed(lambda: bj.execute(sh))
+        torch.cuda.synchronize()
+        same = all(bool(np.all((a == bb) | (np.isnan(a) & np.isnan(bb))))
+                   for a, bb in zip(ref, (o.cpu().numpy() for o in jouts)))
+        bj.close()
+        out.update({"persistent_jit_ms": t_jit, "persistent_jit_mpts": total / t_jit / 1e3,
+                    "jit_speedup_vs_plain": t_plain / t_jit, "jit_build_and_tune_s": t_build,
+                    "jit_block": bestj["block"], "jit_same_bits_as_plain": same})
+    out["cpu"] = c3_cpu_baseline(og, workloads, specs)
+    return out
+
+
+def c3_cpu_baseline(og, workloads, specs, frac=8):
+    """The oracle over every group's first n/frac points (at least 2000) on
+    all host threads: points per second over the sampled points."""
+    from helpers import oracle_run
+    from oracle.build import build as build_oracle
+    build_oracle()
+    ss = og.ShadingSystem()
+    pts, secs = 0, 0.0
+    for k, (name, oso, npts, _) in enumerate(specs):
+        g = workloads.c3_group(ss, name, oso)
+        m = min(npts, max(2000, npts // frac))
+        P = np.ascontiguousarray(workloads.c3_points(k, npts)[:, :m])
+        buf = np.zeros((m, workloads.C3_REC), np.float32)
+        blob = g.program_bytes()
+        t0 = time.perf_counter()
+        oracle_run(blob, m, og.make_globals(P=P), buf)
+        secs += time.perf_counter() - t0
+        pts += m
+    return {"mpts_per_s": pts / secs / 1e6, "points": pts, "seconds": secs, "threads": os.cpu_count(),
+            "kind": "port", "sample": "first n/%d points (at least 2000) of each of the 64 groups" % frac}
 
 
 def bench_serving(torch, og, nreq=600):
@@ -455,6 +506,8 @@ def main():
     ap.add_argument("--section", choices=["batching", "serving", "wavefront", "texture"],
                     help="run only this measurement section and print it as one JSON line")
     ap.add_argument("--wf-size", default=None, help="wavefront frame WxHxSPP (default 1920x1080x4)")
+    ap.add_argument("--batch-jit", type=int, default=0,
+                    help="batching section: also time the persistent kernel specialized to the 64 programs")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.section:
@@ -463,7 +516,8 @@ def main():
         from openshadinglanguage_gb300.build import build as build_native
         build_native()
         torch.cuda.set_device(0)
-        fn = {"batching": lambda: bench_batching(torch, og), "serving": lambda: bench_serving(torch, og),
+        fn = {"batching": lambda: bench_batching(torch, og, jit=args.batch_jit),
+              "serving": lambda: bench_serving(torch, og),
               "wavefront": lambda: bench_wavefront(torch, og, size=args.wf_size, jit=args.jit),
               "texture": lambda: bench_texture(torch, og)}[args.section]
         print(json.dumps({"section": args.section, args.section: fn()}))
@@ -625,10 +679,18 @@ def main():
         "device_status": status,
     }
     if not args.no_extras and world == 1:
-        line["batching"] = bench_batching(torch, og)
+        line["batching"] = bench_batching(torch, og, jit=args.batch_jit)
         line["serving"] = bench_serving(torch, og)
         line["wavefront"] = bench_wavefront(torch, og, jit=args.jit)
         line["texture"] = bench_texture(torch, og)
+        # the systems targets as top-level keys, ahead of the long sections
+        b, sv = line["batching"], line["serving"]
+        summary = {"speedup_vs_plain": b["speedup_vs_plain"],
+                   "jit_speedup_vs_plain": b.get("jit_speedup_vs_plain"),
+                   "served_over_plain_peak": sv["served_peak_mpts"] / sv["plain_peak_mpts"]}
+        keys = list(line)
+        at = keys.index("ms_per_step") + 1
+        line = dict([(k, line[k]) for k in keys[:at]] + list(summary.items()) + [(k, line[k]) for k in keys[at:]])
     if not args.no_cpu_baseline:
         from helpers import oracle_run  # noqa: F401
         build_oracle()
