@@ -1685,7 +1685,7 @@ static __device__ void h_store_closure(const Lane& L, const uint32_t* a, char* b
 // parameters stay in the heap (node params) and are read when used.
 struct Lobes {
     int n;
-    int kind[OSLG_LOBES_MAX];  // 0 diffuse, 1 ggx, 2 oren-nayar, 3 sheen
+    int kind[OSLG_LOBES_MAX];  // 0 diffuse, 1 ggx, 2 oren-nayar, 3 sheen, 4 oren_nayar_diffuse_bsdf
     float w[OSLG_LOBES_MAX][3];
     float pdf[OSLG_LOBES_MAX];
     uint32_t p[OSLG_LOBES_MAX];
@@ -1720,6 +1720,7 @@ __device__ __forceinline__ void lobes_collect(const Lane& L, W&& walk, uint32_t 
         }
         if (id == 3) k = 0;  // DIFFUSE_ID
         else if (id == 4) k = 2;  // OREN_NAYAR_ID
+        else if (id == kIdMxOrenNayarDiffuse) k = 4;
         else if (id == 23 && NODES::u(L, params + 7) == 0u) k = 3;  // MX_SHEEN_ID, Conty-Kulla mode
         else if (id == 8 && NODES::u(L, params + 0) == ggx) {  // MICROFACET_ID "ggx"
             const int r = (int)NODES::u(L, params + 10);
@@ -1766,6 +1767,46 @@ __device__ __forceinline__ SheenLobeDev lobe_sheen(const Lane& L, const Lobes& B
     return sheen_make(v3(NODES::f(L, p + 0), NODES::f(L, p + 1), NODES::f(L, p + 2)), albedo, NODES::f(L, p + 6), wo, B.path_rough,
                       B.backfacing);
 }
+// An int keyword parameter of a component (name hash, then the value) after
+// its fixed parameters; dflt when absent.
+template <class NODES>
+__device__ __forceinline__ int closure_keyword_int(const Lane& L, uint32_t params, int first, uint32_t key, int dflt) {
+    int v = dflt;
+    bool done = false;
+    OSLG_SPEC_UNROLL
+    for (int k = first; k + 1 < kClosureParamFloats; k += 2) {
+        const uint32_t w = NODES::u(L, params + k);
+        if (done || w == 0u) {
+            done = true;
+            continue;
+        }
+        if (w == key) {
+            v = (int)NODES::u(L, params + k + 1);
+            done = true;
+        }
+    }
+    return v;
+}
+// oren_nayar_diffuse_bsdf(N, albedo, roughness, "energy_compensation", int)
+template <class NODES>
+__device__ __forceinline__ BsdfSample lobe_mxon(const Lane& L, uint32_t p, V3 wo, V3 wi, bool sample, float rx,
+                                                float ry) {
+    const V3 N = v3(NODES::f(L, p + 0), NODES::f(L, p + 1), NODES::f(L, p + 2));
+    const float albedo[3] = { NODES::f(L, p + 3), NODES::f(L, p + 4), NODES::f(L, p + 5) };
+    const float rough = bsdl_clamp(NODES::f(L, p + 6), 0.0f, 1.0f);
+    const bool energy = closure_keyword_int<NODES>(L, p, 7, string_hash_const("energy_compensation"), 0) != 0;
+    const Frame f = bsdl_frame(bsdl_visible_normal(wo, N, N));
+    const V3 wo_l = tolocal(f, wo);
+    if (sample) {
+        if (wo_l.z <= 0.0f) return bsdf_zero();
+        BsdfSample s = on_mx_eval_local(rough, albedo, energy, wo_l, bsdl_sample_cos_hemisphere(rx, ry));
+        s.wi = bsdl_world(f, s.wi);
+        return s;
+    }
+    BsdfSample s = on_mx_eval_local(rough, albedo, energy, wo_l, tolocal(f, wi));
+    s.wi = wi;
+    return s;
+}
 template <class NODES = PoolNodes>
 __device__ __forceinline__ BsdfSample lobe_eval(const Lane& L, const Lobes& B, int i, V3 wo, V3 wi) {
     const uint32_t p = B.p[i];
@@ -1776,6 +1817,7 @@ __device__ __forceinline__ BsdfSample lobe_eval(const Lane& L, const Lobes& B, i
         return s;
     }
     if (B.kind[i] == 1) return ggx_eval(lobe_ggx<NODES>(L, p), wo, wi);
+    if (B.kind[i] == 4) return lobe_mxon<NODES>(L, p, wo, wi, false, 0.0f, 0.0f);
     const V3 N = v3(NODES::f(L, p + 0), NODES::f(L, p + 1), NODES::f(L, p + 2));
     const Frame f = bsdl_frame(bsdl_visible_normal(wo, N, N));
     BsdfSample s = on_eval_local(bsdl_clamp(NODES::f(L, p + 3), 0.0f, 1.0f), tolocal(f, wo), tolocal(f, wi));
@@ -1789,6 +1831,7 @@ __device__ __forceinline__ BsdfSample lobe_sample(const Lane& L, const Lobes& B,
     if (B.kind[i] == 3) return sheen_sample(lobe_sheen<NODES>(L, B, p, wo), wo, rx, ry);
     if (B.kind[i] == 0) return diffuse_sample(v3(NODES::f(L, p + 0), NODES::f(L, p + 1), NODES::f(L, p + 2)), rx, ry);
     if (B.kind[i] == 1) return ggx_sample(lobe_ggx<NODES>(L, p), wo, rx, ry, rz);
+    if (B.kind[i] == 4) return lobe_mxon<NODES>(L, p, wo, wo, true, rx, ry);
     const V3 N = v3(NODES::f(L, p + 0), NODES::f(L, p + 1), NODES::f(L, p + 2));
     const Frame f = bsdl_frame(bsdl_visible_normal(wo, N, N));
     const V3 wo_l = tolocal(f, wo);
@@ -1810,6 +1853,8 @@ __device__ __forceinline__ void lobes_prepare(const Lane& L, Lobes& B, V3 wo, co
         } else if (B.kind[i] == 3) {
             const SheenLobeDev sh = lobe_sheen<NODES>(L, B, B.p[i], wo);
             for (int c = 0; c < 3; ++c) alb[c] = sh.tint[c] * (1 - sh.emiss);
+        } else if (B.kind[i] == 4) {  // BSDL albedo_impl: the closure's albedo
+            for (int c = 0; c < 3; ++c) alb[c] = NODES::f(L, B.p[i] + 3 + c);
         }
         B.pdf[i] = (B.w[i][0] * (pw[0] * alb[0]) + B.w[i][1] * (pw[1] * alb[1]) + B.w[i][2] * (pw[2] * alb[2]))
                  / (pw[0] + pw[1] + pw[2]);
@@ -1945,6 +1990,7 @@ __device__ __forceinline__ void lobes_collect_static(const Lane& L, const Op* ta
         }
         if (id == 3) k = 0;  // DIFFUSE_ID
         else if (id == 4) k = 2;  // OREN_NAYAR_ID
+        else if (id == kIdMxOrenNayarDiffuse) k = 4;
         else if (id == 23 && sgetu(L, params + 7) == 0u) k = 3;  // MX_SHEEN_ID, Conty-Kulla mode
         else if (id == 8 && sgetu(L, params + 0) == ggx) {  // MICROFACET_ID "ggx"
             const int r = (int)sgetu(L, params + 10);

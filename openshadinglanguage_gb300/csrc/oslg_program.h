@@ -167,6 +167,18 @@ inline uint32_t noise_word(uint32_t kind, bool periodic, int dims, bool vec, boo
 
 static const uint32_t kNoArg = 0xFFFFFFFFu;
 
+// The string hash the lowering stores for string operands (FNV-1a, 32 bit),
+// usable in constant expressions (keyword names of closure parameters).
+#ifdef __CUDACC__
+__host__ __device__
+#endif
+constexpr uint32_t string_hash_const(const char* s, uint32_t h = 2166136261u) {
+    return *s ? string_hash_const(s + 1, (h ^ (uint32_t)(unsigned char)*s) * 16777619u) : h;
+}
+// testrender's closure ids (src/testrender/shading.h:25-61) the BSDF code reads
+static const int kIdEmission = 1, kIdDiffuse = 3, kIdOrenNayar = 4, kIdMicrofacet = 8,
+                 kIdMxOrenNayarDiffuse = 15, kIdMxSheen = 23;
+
 // Shader-globals the program can load (OP_LOAD_GLOBAL a1). Each triple
 // global with derivatives names its dx / dy fields so the loader can fill
 // a Dual2 in one op. Matches the varying members of BatchedShaderGlobals

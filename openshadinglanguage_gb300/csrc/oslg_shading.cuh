@@ -500,6 +500,54 @@ __device__ __forceinline__ BsdfSample on_eval_local(float rough, V3 wo, V3 wi) {
     return s;
 }
 
+// oren_nayar_diffuse_bsdf as testrender builds it: BSDL OrenNayarDiffuseLobe
+// with the closure's albedo, and with energy_compensation the energy
+// preserving "FON" form (libbsdl MTX/bsdf_oren_nayar_diffuse_impl.h:27-98:
+// single scattering AF (1 + sigma s/max(cosNI, cosNO)) plus the multiple
+// scattering term from the directional albedo E_FON). acos is evaluated
+// in double precision and rounded, where BSDL calls its fast acos.
+__device__ __forceinline__ float on_fon_E(float sigma, float mu) {
+    constexpr float c1 = 0.5f - 2.0f / (3.0f * 3.14159265358979323846f);
+    const float AF = 1.0f / (1.0f + c1 * sigma);
+    const float BF = sigma * AF;
+    const float Si = sqrtf(fmaxf(0.0f, 1.0f - mu * mu));
+    const float G = Si * ((float)acos((double)mu) - Si * mu)
+                  + 2.0f * ((Si / fmaxf(mu, 1e-7f)) * (1.0f - Si * Si * Si) - Si) * (1.0f / 3.0f);
+    return AF + (BF * (1 / 3.14159265358979323846f)) * G;
+}
+__device__ __forceinline__ BsdfSample on_mx_eval_local(float rough, const float* albedo, bool energy, V3 wo, V3 wi) {
+    if (!energy) {
+        BsdfSample s = on_eval_local(rough, wo, wi);
+        for (int c = 0; c < 3; ++c) s.w[c] = albedo[c] * s.w[c];
+        return s;
+    }
+    BsdfSample s = bsdf_zero();
+    const float cosNI = bsdl_clamp(wi.z, 0.0f, 1.0f);
+    const float cosNO = bsdl_clamp(wo.z, 0.0f, 1.0f);
+    if (cosNI <= 0.0f || cosNO <= 0.0f) return s;
+    const float cosIO = bsdl_clamp(vdot(wo, wi), -1.0f, 1.0f);
+    const float sv = cosIO - cosNI * cosNO;
+    const float pdf = cosNI * (1.0f / 3.14159265358979323846f);
+    constexpr float c1 = 0.5f - 2.0f / (3.0f * 3.14159265358979323846f);
+    constexpr float c2 = 2.0f / 3.0f - 28.0f / (15.0f * 3.14159265358979323846f);
+    const float AF = 1.0f / (1.0f + c1 * rough);
+    const float stinv = sv > 0.0f ? sv / fmaxf(cosNI, cosNO) : sv;
+    const float f_ss = AF * (1.0f + rough * stinv);
+    const float EFo = on_fon_E(rough, cosNO);
+    const float EFi = on_fon_E(rough, cosNI);
+    const float avgEF = AF * (1.0f + c2 * rough);
+    const float f_ms = fmaxf(1e-7f, 1.0f - EFo) * fmaxf(1e-7f, 1.0f - EFi) / fmaxf(1e-7f, 1.0f - avgEF);
+    for (int c = 0; c < 3; ++c) {
+        const float a = albedo[c];
+        const float rho_ms = (a * a) * avgEF / (1 - a * fmaxf(0.0f, 1.0f - avgEF));
+        s.w[c] = a * f_ss + rho_ms * f_ms;
+    }
+    s.wi = wi;
+    s.pdf = pdf;
+    s.roughness = 1.0f;
+    return s;
+}
+
 // sheen_bsdf as testrender builds it: BSDL mtx::SheenLobe in its default
 // Conty-Kulla mode with the MaterialX albedo fit and the non-legacy
 // visibility term (libbsdl MTX/bsdf_sheen_impl.h:19-110, :120-260;

@@ -1138,6 +1138,19 @@ void collect_lobes(Point& P, WALK&& walk, const V3& wo, uint32_t ggx_hash, Compo
             L->add_diffuse(cw, V3(f(p + 0), f(p + 1), f(p + 2)));
         } else if (id == 4) {  // OREN_NAYAR_ID
             L->add_on(cw, OrenNayarQON(V3(f(p + 0), f(p + 1), f(p + 2)), f(p + 3), wo));
+        } else if (id == oslg::kIdMxOrenNayarDiffuse) {
+            // oren_nayar_diffuse_bsdf(N, albedo, roughness, "energy_compensation", int)
+            int ec = 0;
+            for (int k = 7; k + 1 < oslg::kClosureParamFloats; k += 2) {
+                const uint32_t w = P.heap[p + k];
+                if (w == 0u) break;
+                if (w == oslg::string_hash_const("energy_compensation")) {
+                    ec = (int32_t)P.heap[p + k + 1];
+                    break;
+                }
+            }
+            L->add_on(cw, OrenNayarQON(V3(f(p + 0), f(p + 1), f(p + 2)), V3(f(p + 3), f(p + 4), f(p + 5)), f(p + 6),
+                                       ec != 0, wo));
         } else if (id == 23 && P.heap[p + 7] == 0u) {  // MX_SHEEN_ID, Conty-Kulla mode
             L->add_sheen(cw, SheenConty(V3(f(p + 0), f(p + 1), f(p + 2)), V3(f(p + 3), f(p + 4), f(p + 5)), f(p + 6), wo,
                                         path_roughness, backfacing));

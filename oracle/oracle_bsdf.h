@@ -308,12 +308,64 @@ inline V3 bsdl_visible_normal(const V3& wo, const V3& Ngf, const V3& N) {
 inline float bsdl_clamp(float x, float a, float b) { return std::min(std::max(x, a), b); }
 
 // oren_nayar as testrender builds it (energy compensation off, albedo 1)
+// BSDL OrenNayarDiffuseLobe (libbsdl MTX/bsdf_oren_nayar_diffuse_impl.h):
+// testrender's oren_nayar is the QON form with albedo 1;
+// oren_nayar_diffuse_bsdf carries its albedo and, with
+// energy_compensation, takes the energy preserving FON form (single
+// scattering plus a multiple scattering term from the analytic directional
+// albedo E_FON; acos in double precision, where BSDL calls its fast acos).
 struct OrenNayarQON {
     BsdlFrame frame;
     float rough;
+    V3 alb = V3(1.0f);
+    bool energy = false;
     OrenNayarQON(const V3& N, float sigma, const V3& wo)
         : frame(bsdl_visible_normal(wo, N, N)), rough(bsdl_clamp(sigma, 0.0f, 1.0f)) {}
+    OrenNayarQON(const V3& N, const V3& albedo, float sigma, bool ec, const V3& wo)
+        : frame(bsdl_visible_normal(wo, N, N)), rough(bsdl_clamp(sigma, 0.0f, 1.0f)), alb(albedo), energy(ec) {}
+    static constexpr float c1 = 0.5f - 2.0f / (3.0f * float(M_PI));
+    static constexpr float c2 = 2.0f / 3.0f - 28.0f / (15.0f * float(M_PI));
+    float E_fon(float mu) const {
+        const float AF = 1.0f / (1.0f + c1 * rough);
+        const float BF = rough * AF;
+        const float Si = std::sqrt(std::max(0.0f, 1.0f - mu * mu));
+        const float G = Si * ((float)std::acos((double)mu) - Si * mu)
+                      + 2.0f * ((Si / std::max(mu, 1e-7f)) * (1.0f - Si * Si * Si) - Si) * (1.0f / 3.0f);
+        return AF + (BF * (1 / float(M_PI))) * G;
+    }
     Sample eval_local(const V3& wo, const V3& wi) const {
+        if (energy) return eval_fon(wo, wi);
+        Sample s = eval_qon(wo, wi);
+        s.weight = V3(alb.x * s.weight.x, alb.y * s.weight.y, alb.z * s.weight.z);
+        return s;
+    }
+    Sample eval_fon(const V3& wo, const V3& wi) const {
+        Sample s;
+        const float cosNI = bsdl_clamp(wi.z, 0.0f, 1.0f);
+        const float cosNO = bsdl_clamp(wo.z, 0.0f, 1.0f);
+        if (cosNI <= 0.0f || cosNO <= 0.0f) return s;
+        const float cosIO = bsdl_clamp(dotv(wo, wi), -1.0f, 1.0f);
+        const float sv = cosIO - cosNI * cosNO;
+        const float pdf = cosNI * (1 / float(M_PI));
+        const float AF = 1.0f / (1.0f + c1 * rough);
+        const float stinv = sv > 0.0f ? sv / std::max(cosNI, cosNO) : sv;
+        const float f_ss = AF * (1.0f + rough * stinv);
+        const float EFo = E_fon(cosNO), EFi = E_fon(cosNI);
+        const float avgEF = AF * (1.0f + c2 * rough);
+        const float f_ms = std::max(1e-7f, 1.0f - EFo) * std::max(1e-7f, 1.0f - EFi) / std::max(1e-7f, 1.0f - avgEF);
+        const float a[3] = { alb.x, alb.y, alb.z };
+        float w[3];
+        for (int c = 0; c < 3; ++c) {
+            const float rho_ms = (a[c] * a[c]) * avgEF / (1 - a[c] * std::max(0.0f, 1.0f - avgEF));
+            w[c] = a[c] * f_ss + rho_ms * f_ms;
+        }
+        s.wi = wi;
+        s.weight = V3(w[0], w[1], w[2]);
+        s.pdf = pdf;
+        s.roughness = 1.0f;
+        return s;
+    }
+    Sample eval_qon(const V3& wo, const V3& wi) const {
         Sample s;
         const float cosNI = bsdl_clamp(wi.z, 0.0f, 1.0f);
         const float cosNO = bsdl_clamp(wo.z, 0.0f, 1.0f);
@@ -471,6 +523,7 @@ struct CompositeLobes {
     V3 albedo(int i, const V3& wo) const {
         if (kind[i] == GGX) return mf(i).albedo(wo);
         if (kind[i] == SHEEN) return sh(i).albedo();
+        if (kind[i] == OREN_NAYAR) return on(i).alb;
         return V3(1.0f);
     }
     Sample eval_lobe(int i, const V3& wo, const V3& wi) const {

@@ -160,6 +160,10 @@ EXR_IMAGES = {
     "blackbody": ["testsuite/blackbody/ref/out.exr", "testsuite/blackbody/ref/out.alt.exr",
                   "testsuite/blackbody/ref/out2.exr", "testsuite/blackbody/ref/out3.exr",
                   "testsuite/blackbody/ref/out4.exr", "testsuite/blackbody/ref/out5.exr"],
+    # testrender furnace scenes: spheres under a uniform environment
+    "furnace_diffuse": ["testsuite/render-furnace-diffuse/ref/out.exr"],
+    "furnace_oren_nayar": ["testsuite/render-mx-furnace-oren-nayar/ref/out.exr"],
+    "furnace_sheen": ["testsuite/render-mx-furnace-sheen/ref/out.exr"],
 }
 
 IMAGES = {
