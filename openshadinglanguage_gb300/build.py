@@ -44,7 +44,7 @@ def _newer(target, deps):
 
 def build(verbose=False, ptxas_verbose=False):
     os.makedirs(BUILD, exist_ok=True)
-    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh", ".inc"))]
     headers.append(os.path.join(HERE, "..", "include", "oslg.h"))
     jobs, objs = [], []
     for src in HOST_SOURCES:

@@ -1541,7 +1541,8 @@ __device__ __forceinline__ void closure_fill(const Lane& L, uint32_t ns, const u
         OSLG_SPEC_UNROLL
         for (int c = 0; c < 16; ++c) {
             if (c >= nc || k >= kClosureParamFloats) break;
-            setu(ns + 4 + k++, (t == TC_INT || t == TC_STRING) ? ldw(L, p, c) : __float_as_uint(ldf(L, p, c, 0)));
+            setu(ns + 4 + k++, (t == TC_INT || t == TC_STRING || t == TC_CLOSURE) ? ldw(L, p, c)
+                                                                               : __float_as_uint(ldf(L, p, c, 0)));
         }
     }
     for (; k < kClosureParamFloats; ++k) setu(ns + 4 + k, 0u);
@@ -1604,8 +1605,16 @@ static __device__ void h_closure_add(const Lane& L, const uint32_t* a, const Clo
 
 // testrender's non-recursive walk (shading.cpp:1450-1500): visits the
 // components in order with the accumulated weight weight*comp.w.
-template <class F>
-__device__ void closure_walk(const Lane& L, const ClosurePools& P, uint32_t root, uint32_t* st, F&& visit) {
+// With LAYERS, a layer(top, base) component (MaterialX layering as testrender
+// walks it, shading.cpp:1666-1681) continues into top with the layer's
+// weight and pushes base with the walk weight times (1 - clamp(opacity of
+// top)); `opacity(top, out)` gives that opacity.
+struct NoOpacity {
+    __device__ void operator()(uint32_t, float* o) const { o[0] = o[1] = o[2] = 0.0f; }
+};
+template <bool LAYERS = false, class F, class O = NoOpacity>
+__device__ void closure_walk(const Lane& L, const ClosurePools& P, uint32_t root, uint32_t* st, F&& visit,
+                             O&& opacity = O()) {
     uint32_t stack_node[OSLG_WALK_STACK];
     float stack_w[OSLG_WALK_STACK][3];
     int sp = 0;
@@ -1641,8 +1650,35 @@ __device__ void closure_walk(const Lane& L, const ClosurePools& P, uint32_t root
         } else {
             float cw[3];
             for (int k = 0; k < 3; ++k) cw[k] = w[k] * hget(L, ns + 1 + k);
-            visit(id, cw, ns + 4);
             cur = 0u;
+            if (LAYERS && id == kIdMxLayer) {
+                float op[3], bw[3];
+                opacity(hgetu(L, ns + 4), op);
+                for (int k = 0; k < 3; ++k) bw[k] = w[k] * (1.0f - bsdl_clamp(op[k], 0.0f, 1.0f));
+                if (bw[0] != 0.0f || bw[1] != 0.0f || bw[2] != 0.0f) {
+                    if (sp < OSLG_WALK_STACK) {
+                        const uint32_t base = hgetu(L, ns + 5);
+#ifdef OSLG_FIXED_INDEX
+#pragma unroll
+                        for (int j = 0; j < OSLG_WALK_STACK; ++j)
+                            if (j == sp) {
+                                stack_node[j] = base;
+                                for (int k = 0; k < 3; ++k) stack_w[j][k] = bw[k];
+                            }
+#else
+                        stack_node[sp] = base;
+                        for (int k = 0; k < 3; ++k) stack_w[sp][k] = bw[k];
+#endif
+                        ++sp;
+                    } else {
+                        raise_status(st, ST_CLOSURE_OVERFLOW);
+                    }
+                }
+                for (int k = 0; k < 3; ++k) w[k] = cw[k];
+                cur = hgetu(L, ns + 4);
+            } else {
+                visit(id, cw, ns + 4);
+            }
         }
         if (cur == 0u && sp > 0) {
             --sp;
@@ -1721,7 +1757,7 @@ __device__ __forceinline__ void lobes_collect(const Lane& L, W&& walk, uint32_t 
         if (id == 3) k = 0;  // DIFFUSE_ID
         else if (id == 4) k = 2;  // OREN_NAYAR_ID
         else if (id == kIdMxOrenNayarDiffuse) k = 4;
-        else if (id == 23 && NODES::u(L, params + 7) == 0u) k = 3;  // MX_SHEEN_ID, Conty-Kulla mode
+        else if (id == kIdMxSheen) k = 3;
         else if (id == 8 && NODES::u(L, params + 0) == ggx) {  // MICROFACET_ID "ggx"
             const int r = (int)NODES::u(L, params + 10);
             if (r >= 0 && r <= 2) k = 1;
@@ -1743,11 +1779,25 @@ __device__ __forceinline__ void lobes_collect(const Lane& L, W&& walk, uint32_t 
         ++B.n;
     });
 }
+// The opacity of a layer's top (testrender's evaluate_layer_opacity,
+// shading.cpp:1199-1281): its own walk, a nested layer continuing into its
+// top and pushing its base with weight * w, a sheen component scaling the
+// weight by w * (1 - E) with E the part of the light the sheen lets through,
+// any other component opaque. The walk's last weight is the opacity.
+__device__ __forceinline__ void layer_opacity(const Lane& L, const ClosurePools& P, uint32_t top, uint32_t* st, V3 wo,
+                                              float path_rough, bool backfacing, float* out);
 // the lobes of a tree in the node pool, visited by testrender's walk
 __device__ __forceinline__ void lobes_build(const Lane& L, const ClosurePools& P, uint32_t root, uint32_t ggx,
-                                            uint32_t* st, Lobes& B, float path_rough = 0.0f, bool backfacing = false) {
+                                            uint32_t* st, Lobes& B, float path_rough = 0.0f, bool backfacing = false,
+                                            V3 wo = V3{ 0.0f, 0.0f, 1.0f }) {
     lobes_collect<PoolNodes>(
-        L, [&](auto&& visit) { closure_walk(L, P, root, st, visit); }, ggx, B, path_rough, backfacing);
+        L,
+        [&](auto&& visit) {
+            closure_walk<true>(L, P, root, st, visit, [&](uint32_t top, float* o) {
+                layer_opacity(L, P, top, st, wo, path_rough, backfacing, o);
+            });
+        },
+        ggx, B, path_rough, backfacing);
 }
 template <class NODES = PoolNodes>
 __device__ __forceinline__ GGXLobe lobe_ggx(const Lane& L, uint32_t p) {
@@ -1760,12 +1810,6 @@ __device__ __forceinline__ GGXLobe lobe_ggx(const Lane& L, uint32_t p) {
     g.eta = NODES::f(L, p + 9);
     g.refract = (int)NODES::u(L, p + 10);
     return g;
-}
-template <class NODES = PoolNodes>
-__device__ __forceinline__ SheenLobeDev lobe_sheen(const Lane& L, const Lobes& B, uint32_t p, V3 wo) {
-    const float albedo[3] = { NODES::f(L, p + 3), NODES::f(L, p + 4), NODES::f(L, p + 5) };
-    return sheen_make(v3(NODES::f(L, p + 0), NODES::f(L, p + 1), NODES::f(L, p + 2)), albedo, NODES::f(L, p + 6), wo, B.path_rough,
-                      B.backfacing);
 }
 // An int keyword parameter of a component (name hash, then the value) after
 // its fixed parameters; dflt when absent.
@@ -1786,6 +1830,12 @@ __device__ __forceinline__ int closure_keyword_int(const Lane& L, uint32_t param
         }
     }
     return v;
+}
+template <class NODES = PoolNodes>
+__device__ __forceinline__ SheenLobeDev lobe_sheen(const Lane& L, const Lobes& B, uint32_t p, V3 wo) {
+    const float albedo[3] = { NODES::f(L, p + 3), NODES::f(L, p + 4), NODES::f(L, p + 5) };
+    return sheen_make(v3(NODES::f(L, p + 0), NODES::f(L, p + 1), NODES::f(L, p + 2)), albedo, NODES::f(L, p + 6), wo, B.path_rough,
+                      B.backfacing, closure_keyword_int<NODES>(L, p, 7, string_hash_const("mode"), 0));
 }
 // oren_nayar_diffuse_bsdf(N, albedo, roughness, "energy_compensation", int)
 template <class NODES>
@@ -1902,6 +1952,63 @@ __device__ __forceinline__ BsdfSample lobes_sample(const Lane& L, const Lobes& B
     return bsdf_zero();
 }
 
+__device__ __forceinline__ void layer_opacity(const Lane& L, const ClosurePools& P, uint32_t top, uint32_t* st, V3 wo,
+                                              float path_rough, bool backfacing, float* out) {
+    float w[3] = { 1.0f, 1.0f, 1.0f };
+    if (top == 0u) {  // a null top lets everything through
+        out[0] = out[1] = out[2] = 0.0f;
+        return;
+    }
+    uint32_t stack_node[kClosureWalkStack];
+    float stack_w[kClosureWalkStack][3];
+    int sp = 0, guard = 0;
+    uint32_t cur = top;
+    auto push = [&](uint32_t node, const float* pw) {
+        if (sp >= kClosureWalkStack) {
+            raise_status(st, ST_CLOSURE_OVERFLOW);
+            return;
+        }
+        stack_node[sp] = node;
+        for (int k = 0; k < 3; ++k) stack_w[sp][k] = pw[k];
+        ++sp;
+    };
+    while (cur != 0u && cur <= P.max_nodes) {
+        if (++guard > 4 * (int)P.max_nodes + 8) break;
+        const uint32_t ns = node_slot(P, cur - 1);
+        const int id = (int)hgetu(L, ns);
+        if (id == kClosureMul) {
+            for (int k = 0; k < 3; ++k) w[k] = w[k] * hget(L, ns + 1 + k);
+            cur = hgetu(L, ns + 4);
+        } else if (id == kClosureAdd) {
+            push(hgetu(L, ns + 5), w);
+            cur = hgetu(L, ns + 4);
+        } else {
+            const float cw[3] = { hget(L, ns + 1), hget(L, ns + 2), hget(L, ns + 3) };
+            const uint32_t p = ns + 4;
+            cur = 0u;
+            if (id == kIdMxLayer) {
+                float bw[3];
+                for (int k = 0; k < 3; ++k) bw[k] = w[k] * cw[k];
+                push(hgetu(L, p + 1), bw);
+                cur = hgetu(L, p);
+            } else if (id == kIdMxSheen) {
+                const float albedo[3] = { hget(L, p + 3), hget(L, p + 4), hget(L, p + 5) };
+                const SheenLobeDev sh =
+                    sheen_make(v3(hget(L, p + 0), hget(L, p + 1), hget(L, p + 2)), albedo, hget(L, p + 6), wo,
+                               path_rough, backfacing,
+                               closure_keyword_int<PoolNodes>(L, p, 7, string_hash_const("mode"), 0));
+                for (int k = 0; k < 3; ++k) w[k] = w[k] * (cw[k] * (1.0f - sh.emiss));
+            }
+        }
+        if (cur == 0u && sp > 0) {
+            --sp;
+            cur = stack_node[sp];
+            for (int k = 0; k < 3; ++k) w[k] = stack_w[sp][k];
+        }
+    }
+    for (int k = 0; k < 3; ++k) out[k] = w[k];
+}
+
 // Renderer-side BSDF evaluation of a closure output at a light direction:
 // prepare(wo, path_weight 1, absorb false) and eval (shading.h:322-374).
 static __device__ void h_bsdf_eval(const Lane& L, const uint32_t* a, char* base, const ClosurePools& P, uint32_t* st) {
@@ -1909,7 +2016,7 @@ static __device__ void h_bsdf_eval(const Lane& L, const uint32_t* a, char* base,
     const V3 wi = v3(ldf(L, a[3], 0, 0), ldf(L, a[3], 1, 0), ldf(L, a[3], 2, 0));
     const V3 wo = v3(-ldf(L, a[4], 0, 0), -ldf(L, a[4], 1, 0), -ldf(L, a[4], 2, 0));
     Lobes B;
-    lobes_build(L, P, root, a[5], st, B);
+    lobes_build(L, P, root, a[5], st, B, 0.0f, false, wo);
     const float one[3] = { 1.0f, 1.0f, 1.0f };
     lobes_prepare(L, B, wo, one, false);
     const BsdfSample r = lobes_eval(L, B, wo, wi);
@@ -1930,7 +2037,7 @@ static __device__ void h_bsdf_sample(const Lane& L, const uint32_t* a, char* bas
     const V3 wo = v3(-ldf(L, a[3], 0, 0), -ldf(L, a[3], 1, 0), -ldf(L, a[3], 2, 0));
     const float* in = reinterpret_cast<const float*>(ud + (int64_t)a[5] + L.pt * (int64_t)(int32_t)a[6]);
     Lobes B;
-    lobes_build(L, P, root, a[4], st, B, in[7], in[8] != 0.0f);
+    lobes_build(L, P, root, a[4], st, B, in[7], in[8] != 0.0f, wo);
     const float pw[3] = { in[3], in[4], in[5] };
     lobes_prepare(L, B, wo, pw, in[6] != 0.0f);
     const BsdfSample r = lobes_sample(L, B, wo, in[0], in[1], in[2]);
@@ -1991,7 +2098,7 @@ __device__ __forceinline__ void lobes_collect_static(const Lane& L, const Op* ta
         if (id == 3) k = 0;  // DIFFUSE_ID
         else if (id == 4) k = 2;  // OREN_NAYAR_ID
         else if (id == kIdMxOrenNayarDiffuse) k = 4;
-        else if (id == 23 && sgetu(L, params + 7) == 0u) k = 3;  // MX_SHEEN_ID, Conty-Kulla mode
+        else if (id == kIdMxSheen) k = 3;
         else if (id == 8 && sgetu(L, params + 0) == ggx) {  // MICROFACET_ID "ggx"
             const int r = (int)sgetu(L, params + 10);
             if (r >= 0 && r <= 2) k = 1;

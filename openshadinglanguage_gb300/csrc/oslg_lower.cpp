@@ -1024,6 +1024,9 @@ struct Lowerer {
             if (!closure_writer(op) || depth[k]) return false;
             const int r = op.args[0];
             if (op.name == "closure") {
+                // closures taking closures (layer) keep the run-time tree
+                for (size_t i = 1; i < op.args.size(); ++i)
+                    if (is_closure(op.args[i])) return false;
                 val[r] = { ClTerm{ -1, {} } };
             } else if (op.name == "assign") {
                 val[r] = op.args.size() > 1 && is_closure(op.args[1]) ? val[op.args[1]] : std::vector<ClTerm>{};

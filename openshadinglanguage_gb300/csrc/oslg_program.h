@@ -177,7 +177,7 @@ constexpr uint32_t string_hash_const(const char* s, uint32_t h = 2166136261u) {
 }
 // testrender's closure ids (src/testrender/shading.h:25-61) the BSDF code reads
 static const int kIdEmission = 1, kIdDiffuse = 3, kIdOrenNayar = 4, kIdMicrofacet = 8,
-                 kIdMxOrenNayarDiffuse = 15, kIdMxSheen = 23;
+                 kIdMxOrenNayarDiffuse = 15, kIdMxSheen = 23, kIdMxLayer = 27;
 
 // Shader-globals the program can load (OP_LOAD_GLOBAL a1). Each triple
 // global with derivatives names its dx / dy fields so the loader can fill

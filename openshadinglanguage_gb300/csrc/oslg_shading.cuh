@@ -548,20 +548,56 @@ __device__ __forceinline__ BsdfSample on_mx_eval_local(float rough, const float*
     return s;
 }
 
-// sheen_bsdf as testrender builds it: BSDL mtx::SheenLobe in its default
-// Conty-Kulla mode with the MaterialX albedo fit and the non-legacy
-// visibility term (libbsdl MTX/bsdf_sheen_impl.h:19-110, :120-260;
-// Conty Estevez and Kulla, "Production Friendly Microfacet Sheen BRDF",
-// 2017). sin^(1/a) uses the executor's own float power (own_pow_pos) where
-// BSDL calls OIIO::fast_pow.
+// sheen_bsdf as testrender builds it: BSDL mtx::SheenLobe (libbsdl
+// MTX/bsdf_sheen_impl.h:19-80). Mode 0: Conty-Kulla with the MaterialX
+// albedo fit and the non-legacy visibility term (:80-260; Conty Estevez and
+// Kulla, "Production Friendly Microfacet Sheen BRDF", 2017; sin^(1/a) uses
+// the executor's own float power where BSDL calls OIIO::fast_pow). Mode 1:
+// Zeltner, Burley and Chiang, "Practical Multiple-Scattering Sheen Using
+// Linearly Transformed Cosines" (2022): the LTC coefficients (A, B, R)
+// bilinearly interpolated from the paper's 32 x 32 table over roughness and
+// cos theta_o, sampled through the LTC, albedo R (:267-357).
 struct SheenLobeDev {
     Frame f;
     float tint[3];
     float rough;  // regularized roughness (reported)
-    float a;      // distribution roughness, in [0.06, 1]
+    float a;      // distribution roughness: [0.06, 1] (mode 0), [0.02, 1] (mode 1)
     float emiss;
     bool backfacing;
+    bool zeltner;
 };
+static __constant__ float c_zeltner_ltc[32 * 32 * 3] = {
+#include "oslg_zeltner_ltc.inc"
+};
+__device__ __forceinline__ void zeltner_fetch(float a, float cosNO, float* o) {
+    const float almost_one = 0.999999940395355224609375f;
+    const float row = bsdl_clamp(a, 0.0f, almost_one) * 31.0f;
+    const float col = bsdl_clamp(cosNO, 0.0f, almost_one) * 31.0f;
+    const float r = floorf(row), c = floorf(col);
+    const float rf = bsdl_clamp(row - r, 0.0f, 1.0f), cf = bsdl_clamp(col - c, 0.0f, 1.0f);
+    const int i0 = ((int)r * 32 + (int)c) * 3, i1 = i0 + 32 * 3;
+    for (int k = 0; k < 3; ++k) {
+        const float lo = (1 - cf) * c_zeltner_ltc[i0 + k] + cf * c_zeltner_ltc[i0 + 3 + k];
+        const float hi = (1 - cf) * c_zeltner_ltc[i1 + k] + cf * c_zeltner_ltc[i1 + 3 + k];
+        o[k] = (1 - rf) * lo + rf * hi;
+    }
+}
+// the LTC evaluation at local direction wi with coefficients ltc
+__device__ __forceinline__ BsdfSample zeltner_eval(float a, V3 wi, const float* ltc) {
+    BsdfSample s = bsdf_zero();
+    const float ai = ltc[0], bi = ltc[1];
+    const V3 o = v3(ai * wi.x + bi * wi.z, ai * wi.y, wi.z);
+    const float len2 = o.x * o.x + o.y * o.y + o.z * o.z;
+    const float j = ai / len2;
+    const float pdf = j * j * fmaxf(o.z, 0.0f) * (1.0f / 3.14159265358979323846f);
+    if (pdf > 1.17549435e-38f) {
+        s.wi = wi;
+        s.w[0] = s.w[1] = s.w[2] = ltc[2];
+        s.pdf = pdf;
+        s.roughness = a;
+    }
+    return s;
+}
 __device__ __forceinline__ float sheen_albedo_fit(float c, float r) {
     float x = 13.67300f + -68.78018f * c;
     float y = 1.0f + 61.57746f * c;
@@ -576,16 +612,26 @@ __device__ __forceinline__ float sheen_albedo_fit(float c, float r) {
     return bsdl_clamp(x / y, 0.0f, 1.0f);
 }
 __device__ __forceinline__ SheenLobeDev sheen_make(V3 N, const float* albedo, float roughness, V3 wo,
-                                                   float path_roughness, bool backfacing) {
+                                                   float path_roughness, bool backfacing, int mode = 0) {
     SheenLobeDev L;
     L.f = bsdl_frame(bsdl_visible_normal(wo, N, N));
     for (int c = 0; c < 3; ++c) L.tint[c] = albedo[c];
     L.rough = 1.0f - (1.0f - bsdl_clamp(roughness, 0.0f, 1.0f)) * (1.0f - path_roughness);
-    L.a = bsdl_clamp(fmaxf(0.06f, L.rough), 0.06f, 1.0f);
+    L.zeltner = mode == 1;
+    L.a = L.zeltner ? bsdl_clamp(fmaxf(0.02f, sqrtf(L.rough)), 0.02f, 1.0f)
+                    : bsdl_clamp(fmaxf(0.06f, L.rough), 0.06f, 1.0f);
     L.backfacing = backfacing;
     const float cosNO = bsdl_clamp(vdot(L.f.w, wo), 0.0f, 1.0f);
     const float tmax = fmaxf(fmaxf(L.tint[0], L.tint[1]), L.tint[2]);
-    L.emiss = backfacing ? 1.0f : 1.0f - fminf(sheen_albedo_fit(cosNO, L.a) * tmax, 1.0f);
+    float alb;
+    if (L.zeltner) {
+        float ltc[3];
+        zeltner_fetch(L.a, cosNO, ltc);
+        alb = ltc[2];
+    } else {
+        alb = sheen_albedo_fit(cosNO, L.a);
+    }
+    L.emiss = backfacing ? 1.0f : 1.0f - fminf(alb * tmax, 1.0f);
     return L;
 }
 // SheenMicrofacet<ContyKullaDist<false>>::eval in the lobe frame
@@ -613,7 +659,15 @@ __device__ __forceinline__ BsdfSample sheen_eval(const SheenLobeDev& L, V3 wo, V
         s.wi = wi;
         return s;
     }
-    s = sheen_mf_eval(L.a, wo_l, wi_l);
+    if (L.zeltner) {
+        if (wo_l.z >= 0 && wi_l.z > 0) {
+            float ltc[3];
+            zeltner_fetch(L.a, wo_l.z, ltc);
+            s = zeltner_eval(L.a, wi_l, ltc);
+        }
+    } else {
+        s = sheen_mf_eval(L.a, wo_l, wi_l);
+    }
     for (int c = 0; c < 3; ++c) s.w[c] *= L.tint[c];
     s.roughness = L.rough;
     s.wi = wi;
@@ -621,6 +675,18 @@ __device__ __forceinline__ BsdfSample sheen_eval(const SheenLobeDev& L, V3 wo, V
 }
 __device__ __forceinline__ BsdfSample sheen_sample(const SheenLobeDev& L, V3 wo, float rx, float ry) {
     if (L.backfacing) return bsdf_zero();
+    if (L.zeltner) {
+        const V3 wo_l = tolocal(L.f, wo);
+        if (wo_l.z < 0) return bsdf_zero();
+        float ltc[3];
+        zeltner_fetch(L.a, wo_l.z, ltc);
+        const V3 c = bsdl_sample_cos_hemisphere(rx, ry);
+        BsdfSample s = zeltner_eval(L.a, vnormalize_imath(v3(c.x - c.z * ltc[1], c.y, ltc[0] * c.z)), ltc);
+        for (int k = 0; k < 3; ++k) s.w[k] *= L.tint[k];
+        s.roughness = L.rough;
+        s.wi = bsdl_world(L.f, s.wi);
+        return s;
+    }
     const float a = 2 * rx - 1, qa = fabsf(a);
     const float b = 2 * ry - 1, qb = fabsf(b);
     const float rad = qa > qb ? qa : qb;

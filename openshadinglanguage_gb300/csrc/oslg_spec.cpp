@@ -53,7 +53,8 @@ uint64_t headers_hash(const std::string& csrc) {
     if (DIR* d = opendir(csrc.c_str())) {
         while (dirent* e = readdir(d)) {
             std::string n = e->d_name;
-            if (n.size() > 3 && (n.compare(n.size() - 4, 4, ".cuh") == 0 || n.compare(n.size() - 2, 2, ".h") == 0))
+            if (n.size() > 3 && (n.compare(n.size() - 4, 4, ".cuh") == 0 || n.compare(n.size() - 2, 2, ".h") == 0
+                                 || n.compare(n.size() - 4, 4, ".inc") == 0))
                 names.push_back(n);
         }
         closedir(d);

@@ -21,6 +21,7 @@ def build(force=False):
     deps = [os.path.join(HERE, f) for f in SOURCES + HEADERS]
     deps.append(os.path.join(HERE, "..", "openshadinglanguage_gb300", "csrc", "oslg_program.h"))
     deps.append(os.path.join(HERE, "..", "include", "oslg.h"))
+    deps.append(os.path.join(HERE, "..", "openshadinglanguage_gb300", "csrc", "oslg_zeltner_ltc.inc"))
     if not force and os.path.exists(LIB) and all(os.path.getmtime(d) <= os.path.getmtime(LIB) for d in deps):
         return LIB
     cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-shared",

@@ -23,6 +23,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "../include/oslg.h"
@@ -1087,7 +1088,12 @@ inline uint32_t cl_alloc(Point& P, const CPools& C) {
 // testrender's traversal (src/testrender/shading.cpp:1450-1500): MUL scales
 // the running weight, ADD pushes its B branch with the current weight and
 // follows A, a component is visited with weight * comp.w.
-template <class F> void closure_walk(Point& P, const CPools& C, uint32_t root, F&& visit) {
+// With an opacity function, a layer(top, base) component continues into
+// top with the layer's weight and pushes base with weight * (1 -
+// clamp(opacity(top))) (testrender's MX_LAYER_ID, shading.cpp:1666-1681).
+struct NoLayers {};
+template <class F, class O = NoLayers> void closure_walk(Point& P, const CPools& C, uint32_t root, F&& visit,
+                                                        O&& opacity = O()) {
     uint32_t stack_node[oslg::kClosureWalkStack];
     V3 stack_w[oslg::kClosureWalkStack];
     int sp = 0;
@@ -1112,9 +1118,29 @@ template <class F> void closure_walk(Point& P, const CPools& C, uint32_t root, F
             cur = P.heap[ns + 4];
         } else {
             V3 cw = w * V3(bitsf(P.heap[ns + 1]), bitsf(P.heap[ns + 2]), bitsf(P.heap[ns + 3]));
-            visit(id, cw, ns + 4);
             cur = 0u;
+            if constexpr (!std::is_same<std::decay_t<O>, NoLayers>::value) {
+                if (id == oslg::kIdMxLayer) {
+                    const V3 op = opacity(P.heap[ns + 4]);
+                    const V3 bw = w * V3(1.0f - bsdl_clamp(op.x, 0.0f, 1.0f), 1.0f - bsdl_clamp(op.y, 0.0f, 1.0f),
+                                         1.0f - bsdl_clamp(op.z, 0.0f, 1.0f));
+                    if (bw.x != 0.0f || bw.y != 0.0f || bw.z != 0.0f) {
+                        if (sp < oslg::kClosureWalkStack) {
+                            stack_node[sp] = P.heap[ns + 5];
+                            stack_w[sp] = bw;
+                            ++sp;
+                        } else {
+                            P.status |= oslg::ST_CLOSURE_OVERFLOW;
+                        }
+                    }
+                    w = cw;
+                    cur = P.heap[ns + 4];
+                    goto next;
+                }
+            }
+            visit(id, cw, ns + 4);
         }
+    next:
         if (cur == 0u && sp > 0) {
             --sp;
             cur = stack_node[sp];
@@ -1127,6 +1153,18 @@ template <class F> void closure_walk(Point& P, const CPools& C, uint32_t root, F
 // (src/testrender/shading.cpp:1481-1530): emission accumulates Le,
 // diffuse / oren_nayar / GGX microfacet (params: dist, N, U, xalpha,
 // yalpha, eta, refract) become lobes in walk order; ggx_hash names "ggx".
+// An int keyword parameter of a component (name hash, then the value) after
+// its fixed parameters; dflt when absent.
+inline int keyword_int(const Point& P, uint32_t p, int first, const char* name, int dflt) {
+    const uint32_t key = oslg::string_hash_const(name);
+    for (int k = first; k + 1 < oslg::kClosureParamFloats; k += 2) {
+        const uint32_t w = P.heap[p + k];
+        if (w == 0u) break;
+        if (w == key) return (int32_t)P.heap[p + k + 1];
+    }
+    return dflt;
+}
+
 template <class WALK>
 void collect_lobes(Point& P, WALK&& walk, const V3& wo, uint32_t ggx_hash, CompositeLobes* L, float path_roughness,
                    bool backfacing) {
@@ -1151,9 +1189,9 @@ void collect_lobes(Point& P, WALK&& walk, const V3& wo, uint32_t ggx_hash, Compo
             }
             L->add_on(cw, OrenNayarQON(V3(f(p + 0), f(p + 1), f(p + 2)), V3(f(p + 3), f(p + 4), f(p + 5)), f(p + 6),
                                        ec != 0, wo));
-        } else if (id == 23 && P.heap[p + 7] == 0u) {  // MX_SHEEN_ID, Conty-Kulla mode
+        } else if (id == oslg::kIdMxSheen) {  // sheen_bsdf(N, albedo, roughness, "mode", int)
             L->add_sheen(cw, SheenConty(V3(f(p + 0), f(p + 1), f(p + 2)), V3(f(p + 3), f(p + 4), f(p + 5)), f(p + 6), wo,
-                                        path_roughness, backfacing));
+                                        path_roughness, backfacing, keyword_int(P, p, 7, "mode", 0)));
         } else if (id == 8 && P.heap[p] == ggx_hash) {  // MICROFACET_ID, "ggx"
             int refract = (int32_t)P.heap[p + 10];
             if (refract < 0 || refract > 2) return;
@@ -1162,10 +1200,69 @@ void collect_lobes(Point& P, WALK&& walk, const V3& wo, uint32_t ggx_hash, Compo
         }
     });
 }
+// testrender's evaluate_layer_opacity (shading.cpp:1199-1281): a walk of
+// the layer's top in which a nested layer continues into its top (pushing
+// its base with weight * w), sheen scales the weight by w * (1 - E) (E the
+// part of the light the sheen lets through) and other components are
+// opaque; the walk's last weight is the opacity.
+V3 layer_opacity(Point& P, const CPools& C, uint32_t top, const V3& wo, float path_roughness, bool backfacing) {
+    if (top == 0u) return V3(0.0f);
+    uint32_t stack_node[oslg::kClosureWalkStack];
+    V3 stack_w[oslg::kClosureWalkStack];
+    int sp = 0, guard = 0;
+    V3 w(1.0f);
+    uint32_t cur = top;
+    auto push = [&](uint32_t node, const V3& pw) {
+        if (sp >= oslg::kClosureWalkStack) {
+            P.status |= oslg::ST_CLOSURE_OVERFLOW;
+            return;
+        }
+        stack_node[sp] = node;
+        stack_w[sp] = pw;
+        ++sp;
+    };
+    auto f = [&](uint32_t s) { return bitsf(P.heap[s]); };
+    while (cur != 0u && cur <= C.maxn) {
+        if (++guard > 4 * (int)C.maxn + 8) break;
+        const uint32_t ns = nslot(C, cur - 1);
+        const int id = (int32_t)P.heap[ns];
+        if (id == oslg::kClosureMul) {
+            w = w * V3(f(ns + 1), f(ns + 2), f(ns + 3));
+            cur = P.heap[ns + 4];
+        } else if (id == oslg::kClosureAdd) {
+            push(P.heap[ns + 5], w);
+            cur = P.heap[ns + 4];
+        } else {
+            const V3 cw(f(ns + 1), f(ns + 2), f(ns + 3));
+            const uint32_t p = ns + 4;
+            cur = 0u;
+            if (id == oslg::kIdMxLayer) {
+                push(P.heap[p + 1], w * cw);
+                cur = P.heap[p];
+            } else if (id == oslg::kIdMxSheen) {
+                const SheenConty sh(V3(f(p + 0), f(p + 1), f(p + 2)), V3(f(p + 3), f(p + 4), f(p + 5)), f(p + 6), wo,
+                                    path_roughness, backfacing, keyword_int(P, p, 7, "mode", 0));
+                w = w * (cw * V3(1.0f - sh.emiss));
+            }
+        }
+        if (cur == 0u && sp > 0) {
+            --sp;
+            cur = stack_node[sp];
+            w = stack_w[sp];
+        }
+    }
+    return w;
+}
+
 void build_lobes(Point& P, const CPools& C, uint32_t root, const V3& wo, uint32_t ggx_hash, CompositeLobes* L,
                  float path_roughness = 0.0f, bool backfacing = false) {
     collect_lobes(
-        P, [&](auto&& visit) { closure_walk(P, C, root, visit); }, wo, ggx_hash, L, path_roughness, backfacing);
+        P,
+        [&](auto&& visit) {
+            closure_walk(P, C, root, visit,
+                         [&](uint32_t top) { return layer_opacity(P, C, top, wo, path_roughness, backfacing); });
+        },
+        wo, ggx_hash, L, path_roughness, backfacing);
 }
 
 // Static closures (oslg_program.h kClosureAbsent): the components of a
@@ -1511,8 +1608,9 @@ struct Runner {
                     if (params[i] == oslg::kNoArg) break;
                     uint32_t t = atc(params[i]);
                     for (int c = 0; c < anc(params[i]) && k < oslg::kClosureParamFloats; ++c)
-                        P.heap[ns + 4 + k++] = (t == oslg::TC_INT || t == oslg::TC_STRING) ? word(P, params[i], c)
-                                                                                            : fbits(getf(P, params[i], c, 0));
+                        P.heap[ns + 4 + k++] = (t == oslg::TC_INT || t == oslg::TC_STRING || t == oslg::TC_CLOSURE)
+                                                   ? word(P, params[i], c)
+                                                   : fbits(getf(P, params[i], c, 0));
                 }
                 for (; k < oslg::kClosureParamFloats; ++k) P.heap[ns + 4 + k] = fbits(0.0f);
                 if (!stat) setw(P, a[0], 0, h);

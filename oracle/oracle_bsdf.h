@@ -416,18 +416,59 @@ inline float sheen_albedo_fit(float c, float r) {
     y = y + 3045.55075f * r * r;
     return bsdl_clamp(x / y, 0.0f, 1.0f);
 }
+// Zeltner, Burley and Chiang 2022 sheen (BSDL ZeltnerBurleySheen with LTC
+// sampling and LTC albedo, libbsdl MTX/bsdf_sheen_impl.h:267-357): the
+// paper's 32 x 32 table of LTC coefficients (A, B, R) over roughness and
+// cos theta_o, interpolated bilinearly (LERP clamps its factor).
+static const float kZeltnerLtc[32 * 32 * 3] = {
+#include "../openshadinglanguage_gb300/csrc/oslg_zeltner_ltc.inc"
+};
+inline V3 zeltner_fetch(float a, float cosNO) {
+    const float almost_one = 0.999999940395355224609375f;
+    const float row = bsdl_clamp(a, 0.0f, almost_one) * 31.0f, col = bsdl_clamp(cosNO, 0.0f, almost_one) * 31.0f;
+    const float r = std::floor(row), c = std::floor(col);
+    const float rf = bsdl_clamp(row - r, 0.0f, 1.0f), cf = bsdl_clamp(col - c, 0.0f, 1.0f);
+    const int i0 = ((int)r * 32 + (int)c) * 3, i1 = i0 + 96;
+    float o[3];
+    for (int k = 0; k < 3; ++k) {
+        const float lo = (1 - cf) * kZeltnerLtc[i0 + k] + cf * kZeltnerLtc[i0 + 3 + k];
+        const float hi = (1 - cf) * kZeltnerLtc[i1 + k] + cf * kZeltnerLtc[i1 + 3 + k];
+        o[k] = (1 - rf) * lo + rf * hi;
+    }
+    return V3(o[0], o[1], o[2]);
+}
+inline Sample zeltner_eval(float a, const V3& wi, const V3& ltc) {
+    Sample s;
+    const V3 o(ltc.x * wi.x + ltc.y * wi.z, ltc.x * wi.y, wi.z);
+    const float len2 = o.x * o.x + o.y * o.y + o.z * o.z;
+    const float j = ltc.x / len2;
+    const float pdf = j * j * std::max(o.z, 0.0f) * (1 / float(M_PI));
+    if (pdf > 1.17549435e-38f) {
+        s.wi = wi;
+        s.weight = V3(ltc.z);
+        s.pdf = pdf;
+        s.roughness = a;
+    }
+    return s;
+}
+
+// sheen_bsdf: mode 0 Conty-Kulla (above), mode 1 Zeltner-Burley
 struct SheenConty {
     BsdlFrame frame;
     V3 tint;
     float rough, a, emiss;
-    bool backfacing;
-    SheenConty(const V3& N, const V3& albedo, float roughness, const V3& wo, float path_roughness, bool bf)
+    bool backfacing, zeltner = false;
+    SheenConty(const V3& N, const V3& albedo, float roughness, const V3& wo, float path_roughness, bool bf,
+               int mode = 0)
         : frame(bsdl_visible_normal(wo, N, N)), tint(albedo), backfacing(bf) {
         rough = 1.0f - (1.0f - bsdl_clamp(roughness, 0.0f, 1.0f)) * (1.0f - path_roughness);
-        a = bsdl_clamp(std::max(0.06f, rough), 0.06f, 1.0f);
+        zeltner = mode == 1;
+        a = zeltner ? bsdl_clamp(std::max(0.02f, std::sqrt(rough)), 0.02f, 1.0f)
+                    : bsdl_clamp(std::max(0.06f, rough), 0.06f, 1.0f);
         const float cosNO = bsdl_clamp(dotv(frame.Z, wo), 0.0f, 1.0f);
         const float tmax = std::max(std::max(tint.x, tint.y), tint.z);
-        emiss = backfacing ? 1.0f : 1.0f - std::min(sheen_albedo_fit(cosNO, a) * tmax, 1.0f);
+        const float alb = zeltner ? zeltner_fetch(a, cosNO).z : sheen_albedo_fit(cosNO, a);
+        emiss = backfacing ? 1.0f : 1.0f - std::min(alb * tmax, 1.0f);
     }
     V3 albedo() const { return tint * (1 - emiss); }
     static Sample mf_eval(float a, const V3& wo, const V3& wi) {
@@ -454,7 +495,11 @@ struct SheenConty {
             s.wi = wi;
             return s;
         }
-        s = mf_eval(a, wo_l, wi_l);
+        if (zeltner) {
+            if (wo_l.z >= 0 && wi_l.z > 0) s = zeltner_eval(a, wi_l, zeltner_fetch(a, wo_l.z));
+        } else {
+            s = mf_eval(a, wo_l, wi_l);
+        }
         s.weight = s.weight * tint;
         s.roughness = rough;
         s.wi = wi;
@@ -462,6 +507,17 @@ struct SheenConty {
     }
     Sample sample(const V3& wo, float rx, float ry) const {
         if (backfacing) return Sample();
+        if (zeltner) {
+            const V3 wo_l = frame.local(wo);
+            if (wo_l.z < 0) return Sample();
+            const V3 ltc = zeltner_fetch(a, wo_l.z);
+            const V3 c = bsdl_sample_cos_hemisphere(rx, ry);
+            Sample s = zeltner_eval(a, imath_normalize(V3(c.x - c.z * ltc.y, c.y, ltc.x * c.z)), ltc);
+            s.weight = s.weight * tint;
+            s.roughness = rough;
+            s.wi = frame.world(s.wi);
+            return s;
+        }
         const float ua = 2 * rx - 1, qa = std::fabs(ua);
         const float ub = 2 * ry - 1, qb = std::fabs(ub);
         const float rad = qa > qb ? qa : qb;

@@ -181,13 +181,80 @@ def test_oren_nayar_furnace():
     assert want[-2, 0] < want[0, 0] - 0.08 and want[-1, 0] > 0.47
 
 
+def sheen_material(ss, name, roughness):
+    """surface sheen(color Cs = 1, float roughness)
+    {
+        if (N.y < 0) Ci = sheen_bsdf(N, Cs, roughness, "mode", 1);
+        else         Ci = sheen_bsdf(N, Cs, roughness);
+        Ci = layer(Ci, diffuse(N));
+    }   (testsuite/render-mx-furnace-sheen/sheen.osl)"""
+    b = OsoBuilder(name, "surface")
+    Cs = b.param("color", "Cs", [1.0, 1.0, 1.0])
+    r = b.param("float", "roughness", float(roughness))
+    Ci, N = b.glob("closure color", "Ci"), b.glob("normal", "N")
+    Ny, below = b.tmp("float"), b.tmp("int")
+    b.op("compref", Ny, N, b.const("int", 1))
+    b.op("lt", below, Ny, b.const("float", 0.0))
+    with b.if_(below) as br:
+        b.op("closure", Ci, b.const("string", "sheen_bsdf"), N, Cs, r, b.const("string", "mode"), b.const("int", 1))
+        br.else_()
+        b.op("closure", Ci, b.const("string", "sheen_bsdf"), N, Cs, r)
+    d, lay = b.tmp("closure color"), b.tmp("closure color")
+    b.op("closure", d, b.const("string", "diffuse"), N)
+    b.op("closure", lay, b.const("string", "layer"), Ci, d)
+    b.op("assign", Ci, lay)
+    ss.LoadMemoryCompiledShader(name, b.text())
+    g = ss.ShaderGroupBegin(name + "_g")
+    ss.Shader(g, "surface", name, "S")
+    ss.ShaderGroupEnd(g)
+    ss.bsdf_sample_output(g, "S.Ci", 0, 4 * W.C5_OUT_FLOATS, 0, 4 * W.C5_IN_FLOATS)
+    return g
+
+
+def sheen_setup():
+    ss = og.ShadingSystem()
+    mats = [sheen_material(ss, "fur_sheen_%d" % i, 0.1 * i) for i in range(11)]
+    W_, H_ = ON["res"]
+    # scene.xml sets max_bounces 5
+    opts = dict(width=W_, height=H_, eye=ON["eye"], look=ON["look"], up=(0.0, 1.0, 0.0),
+                fov_deg=framing_fov(ON["fov"]), background=(0.5, 0.5, 0.5), max_hits=6, rr_survival=0.8)
+    return ss, mats, spheres(ON["centers"], ON["radius"]), opts
+
+
+def test_sheen_layered_furnace():
+    """layer(sheen_bsdf, diffuse) over roughness 0..1: Conty-Kulla sheen on
+    the upper halves, Zeltner-Burley sheen on the lower halves; the diffuse
+    base receives what the sheen lets through, so the layered material
+    stays near the environment's 0.5."""
+    ss, mats, prims, opts = sheen_setup()
+    W_, H_ = ON["res"]
+    spp = 48
+    opts["spp"] = spp
+    y0, y1 = 16, 48
+    rad, _, st = oracle_wavefront(opts, prims, mats, begin=y0 * W_ * spp, count=(y1 - y0) * W_ * spp)
+    assert st == 0
+    img = np.zeros((H_, W_, 3), np.float32)
+    img[y0:y1] = rad.reshape(3, y1 - y0, W_, spp).mean(axis=3).transpose(1, 2, 0)
+    ref = reference("sheen")
+    got, want = [], []
+    for up, lo in regions(ON):
+        for m in (up, lo):
+            got.append(img[m].mean(axis=0))
+            want.append(ref[m].mean(axis=0))
+    got, want = np.array(got), np.array(want)
+    assert np.abs(got - want).max() < 0.01, np.abs(got - want).max(axis=1)
+
+
 @pytest.mark.gpu
-@pytest.mark.parametrize("scene,lobe", [(DIFFUSE, "diffuse"), (ON, "oren_nayar")], ids=["diffuse", "oren_nayar"])
-def test_gpu_furnace_paths_equal_the_oracle(scene, lobe):
+@pytest.mark.parametrize("case", ["diffuse", "oren_nayar", "sheen"])
+def test_gpu_furnace_paths_equal_the_oracle(case):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
-    ss, mats, prims, opts = furnace_setup(scene, lobe)
+    if case == "sheen":
+        ss, mats, prims, opts = sheen_setup()
+    else:
+        ss, mats, prims, opts = furnace_setup(DIFFUSE if case == "diffuse" else ON, case)
     opts["spp"] = 2
     wf = ss.wavefront(prims, mats, **opts)
     npaths = wf.paths
