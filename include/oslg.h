@@ -120,6 +120,13 @@ int oslg_destroy_system(oslg_system* sys);
  * "host_direct_outputs" (host-buffer execution writes pinned output records
  * from the kernel, 1 by default). */
 int oslg_attribute_int(oslg_system* sys, const char* name, int value);
+/* ShadingSystem::attribute(name, TypeString, &value) (oslexec.h:324).
+ * String options: "colorspace" (the colour system whose primaries rgb
+ * means: Rec709 (default), sRGB, NTSC, EBU, PAL, SECAM, SMPTE, HDTV, CIE,
+ * AdobeRGB, XYZ, ACES2065-1, ACEScg; src/liboslexec/opcolor.cpp:31-85,
+ * shadingsys.cpp:1613). Groups lowered afterwards use it for luminance,
+ * blackbody, wavelength_color and transformc. */
+int oslg_attribute_string(oslg_system* sys, const char* name, const char* value);
 /* ShadingSystem::register_closure (oslexec.h:1041). Parameters are taken
  * positionally from the `closure` op's arguments. */
 int oslg_register_closure(oslg_system* sys, const char* name, int id);

@@ -95,6 +95,7 @@ _EXPORTS = {
     "oslg_create_system": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p)]),
     "oslg_destroy_system": (ctypes.c_int, [ctypes.c_void_p]),
     "oslg_attribute_int": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int]),
+    "oslg_attribute_string": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p]),
     "oslg_register_closure": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int]),
     "oslg_load_memory_compiled_shader": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p]),
     "oslg_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),

@@ -218,6 +218,22 @@ int oslg_attribute_int(oslg_system* sys, const char* name, int value) {
     return OSLG_OK;
 }
 
+int oslg_attribute_string(oslg_system* sys, const char* name, const char* value) {
+    if (!sys || !name || !value) return OSLG_ERR_ARG;
+    std::string n(name), v(value);
+    if (n == "colorspace") {
+        static const char* known[] = { "Rec709", "sRGB", "NTSC", "EBU", "PAL", "SECAM", "SMPTE", "HDTV", "CIE",
+                                       "AdobeRGB", "XYZ", "ACES2065-1", "ACEScg" };
+        for (const char* k : known)
+            if (v == k) {
+                sys->ss.opts.colorspace = v;
+                return OSLG_OK;
+            }
+        return fail(sys, OSLG_ERR_ARG, "unknown colour space '" + v + "'");
+    }
+    return fail(sys, OSLG_ERR_ARG, "unknown string attribute '" + n + "'");
+}
+
 int oslg_register_closure(oslg_system* sys, const char* name, int id) {
     if (!sys || !name) return OSLG_ERR_ARG;
     sys->ss.closure_ids[name] = id;

@@ -188,6 +188,7 @@ struct SystemOptions {
     int opt_constant_fold = 1;       // "opt_constant_fold" (shadingsys.cpp:1641)
     int opt_elide_useless_ops = 1;   // "opt_elide_useless_ops" (shadingsys.cpp:1643)
     int opt_static_closures = 1;     // closure trees the lowering knows become term tables
+    std::string colorspace = "Rec709";  // "colorspace" (shadingsys.cpp:1613): the colour system's primaries
     int max_closure_components = 16;  // closure tree nodes per point when closures are made inside loops
     int max_closure_terms = 16;
     int max_loop_iterations = 0;  // loop back edges per point (0: the program format's default)

@@ -917,6 +917,187 @@ static __device__ void h_luminance(const Lane& L, const uint32_t* a) {
         stf(L, r, d, ldf(L, c, 0, d) * sx + ldf(L, c, 1, d) * sy + ldf(L, c, 2, d) * sz);
 }
 
+// ---- colour spaces (src/liboslexec/opcolor.cpp:270-380 ColorSystem::transformc,
+// opcolor_impl.h:240-490 the conversions; Foley & van Dam) on float or Dual2
+// components: comparisons and branches on values, arithmetic as dual.h ----
+__device__ __forceinline__ float cval(float x) { return x; }
+__device__ __forceinline__ float cval(D2 x) { return x.v; }
+template <class S> __device__ __forceinline__ S ck(float v);
+template <> __device__ __forceinline__ float ck<float>(float v) { return v; }
+template <> __device__ __forceinline__ D2 ck<D2>(float v) { return d2c(v); }
+template <class S> __device__ __forceinline__ S cmin(S a, S b) { return cval(a) < cval(b) ? a : b; }
+template <class S> __device__ __forceinline__ S cmax(S a, S b) { return cval(a) > cval(b) ? a : b; }
+template <class S> struct C3 { S x, y, z; };
+template <class S>
+__device__ __forceinline__ C3<S> hsv_to_rgb(C3<S> c) {
+    S h = c.x;
+    const S s = c.y, v = c.z;
+    if (cval(s) < 0.0001f) return { v, v, v };
+    h = 6.0f * (h - floorf(cval(h)));
+    const float fh = floorf(cval(h));
+    const int hi = fh != fh ? 0 : (int)fh;
+    const S f = h - (float)hi;
+    const S p = v * (1.0f - s);
+    const S q = v * (1.0f - s * f);
+    const S t = v * (1.0f - s * (1.0f - f));
+    if (hi == 0) return { v, t, p };
+    if (hi == 1) return { q, v, p };
+    if (hi == 2) return { p, v, t };
+    if (hi == 3) return { p, q, v };
+    if (hi == 4) return { t, p, v };
+    return { v, p, q };
+}
+template <class S>
+__device__ __forceinline__ C3<S> rgb_to_hsv(C3<S> c) {
+    const S mn = cmin(c.x, cmin(c.y, c.z)), mx = cmax(c.x, cmax(c.y, c.z));
+    const S delta = mx - mn;
+    const S v = mx;
+    S s = ck<S>(0.0f), h = ck<S>(0.0f);
+    if (cval(mx) > 0.0f) s = delta / mx;
+    if (cval(s) > 0.0f) {
+        float k;
+        S x, y;
+        if (cval(c.x) >= cval(mx)) { k = 0.0f / 6.0f; x = c.y; y = c.z; }
+        else if (cval(c.y) >= cval(mx)) { k = 2.0f / 6.0f; x = c.z; y = c.x; }
+        else { k = 4.0f / 6.0f; x = c.x; y = c.y; }
+        h = k + (x - y) / (6.0f * delta);
+        if (cval(h) < 0.0f) h = h + 1.0f;
+    }
+    return { h, s, v };
+}
+template <class S>
+__device__ __forceinline__ C3<S> hsl_to_rgb(C3<S> c) {
+    const S h = c.x, l = c.z;
+    S s = c.y;
+    const S v = cval(l) <= 0.5f ? l * (1.0f + s) : l * (1.0f - s) + s;
+    if (cval(v) <= 0.0f) return { ck<S>(0.0f), ck<S>(0.0f), ck<S>(0.0f) };
+    const S mn = 2.0f * l - v;
+    s = (v - mn) / v;
+    return hsv_to_rgb<S>({ h, s, v });
+}
+template <class S>
+__device__ __forceinline__ C3<S> rgb_to_hsl(C3<S> c) {
+    const S minval = cmin(c.x, cmin(c.y, c.z));
+    const C3<S> hsv = rgb_to_hsv(c);
+    const S maxval = hsv.z;
+    const S h = hsv.x, l = (minval + maxval) / 2.0f;
+    S s;
+    if (cval(minval) == cval(maxval)) {
+        s = ck<S>(0.0f);
+    } else {
+        const S m2m = maxval - minval;
+        const S divisor = cval(l) <= 0.5f ? maxval + minval : (2.0f - maxval) - minval;
+        s = m2m / divisor;
+    }
+    return { h, s, l };
+}
+// row vector times a 3x3 matrix m (rows of 3)
+template <class S>
+__device__ __forceinline__ C3<S> cmul33(C3<S> c, const float* m) {
+    return { c.x * m[0] + c.y * m[3] + c.z * m[6], c.x * m[1] + c.y * m[4] + c.z * m[7],
+             c.x * m[2] + c.y * m[5] + c.z * m[8] };
+}
+__device__ __constant__ const float c_yiq_to_rgb[9] = { 1.0000f, 1.0000f, 1.0000f, 0.9557f, -0.2716f, -1.1082f,
+                                                        0.6199f, -0.6469f, 1.7051f };
+__device__ __constant__ const float c_rgb_to_yiq[9] = { 0.299f, 0.596f, 0.212f, 0.587f, -0.275f, -0.523f,
+                                                        0.114f, -0.321f, 0.311f };
+template <class S>
+__device__ __forceinline__ C3<S> xyz_to_xyy(C3<S> c) {
+    const S n = (c.x + c.y) + c.z;
+    const S ninv = cval(n) >= 1.0e-6f ? 1.0f / n : ck<S>(0.0f);
+    return { c.x * ninv, c.y * ninv, c.y };
+}
+template <class S>
+__device__ __forceinline__ C3<S> xyy_to_xyz(C3<S> c) {
+    const S Y = c.z;
+    const S Y_y = cval(c.y) > 1.0e-6f ? Y / c.y : ck<S>(0.0f);
+    return { Y_y * c.x, Y, Y_y * ((1.0f - c.x) - c.y) };
+}
+__device__ __forceinline__ float cpow(float x, float y) { return safe_pow(x, y); }
+__device__ __forceinline__ D2 cpow(D2 u, float y) {  // dual.h safe_pow, the exponent a constant Dual2
+    const float powuvm1 = safe_pow(u.v, y - 1.0f);
+    const float powuv = powuvm1 * u.v;
+    const float logu = u.v > 0.0f ? safe_log(u.v) : 0.0f;
+    const float du = y * powuvm1, dv = logu * powuv;
+    return d2(powuv, du * u.dx + dv * 0.0f, du * u.dy + dv * 0.0f);
+}
+template <class S>
+__device__ __forceinline__ S srgb_to_linear1(S x) {
+    return cval(x) <= 0.04045f ? x * (1.0f / 12.92f) : cpow((x + 0.055f) * (1.0f / 1.055f), 2.4f);
+}
+template <class S>
+__device__ __forceinline__ S linear_to_srgb1(S x) {
+    return cval(x) <= 0.0031308f ? 12.92f * x : 1.055f * cpow(x, 1.f / 2.4f) - 0.055f;
+}
+template <class S>
+__device__ __forceinline__ C3<S> transformc_any(C3<S> c, uint32_t from, uint32_t to, const float* xyz2rgb,
+                                                const float* rgb2xyz) {
+    C3<S> rgb;
+    switch (from) {
+    case CS_HSV: rgb = hsv_to_rgb(c); break;
+    case CS_HSL: rgb = hsl_to_rgb(c); break;
+    case CS_YIQ: rgb = cmul33(c, c_yiq_to_rgb); break;
+    case CS_XYZ: rgb = cmul33(c, xyz2rgb); break;
+    case CS_XYY: rgb = cmul33(xyy_to_xyz(c), xyz2rgb); break;
+    case CS_SRGB: rgb = { srgb_to_linear1(c.x), srgb_to_linear1(c.y), srgb_to_linear1(c.z) }; break;
+    default: rgb = c; break;
+    }
+    switch (to) {
+    case CS_HSV: return rgb_to_hsv(rgb);
+    case CS_HSL: return rgb_to_hsl(rgb);
+    case CS_YIQ: return cmul33(rgb, c_rgb_to_yiq);
+    case CS_XYZ: return cmul33(rgb, rgb2xyz);
+    case CS_XYY: return xyz_to_xyy(cmul33(rgb, rgb2xyz));
+    case CS_SRGB: return { linear_to_srgb1(rgb.x), linear_to_srgb1(rgb.y), linear_to_srgb1(rgb.z) };
+    default: return rgb;
+    }
+}
+static __device__ void h_transformc(const Lane& L, const uint32_t* a) {
+    const uint32_t r = a[0], c = a[1];
+    float m[18];
+    OSLG_SPEC_UNROLL
+    for (int k = 0; k < 18; ++k) m[k] = __uint_as_float(ldw(L, a[3], k));
+    const uint32_t from = a[2] & 0xFFu, to = (a[2] >> 8) & 0xFFu;
+    if (ader(r)) {
+        const C3<D2> o = transformc_any<D2>({ ldd(L, c, 0), ldd(L, c, 1), ldd(L, c, 2) }, from, to, m, m + 9);
+        std2(L, r, 0, o.x);
+        std2(L, r, 1, o.y);
+        std2(L, r, 2, o.z);
+    } else {
+        const C3<float> o = transformc_any<float>({ ldf(L, c, 0, 0), ldf(L, c, 1, 0), ldf(L, c, 2, 0) }, from, to, m,
+                                                  m + 9);
+        stf(L, r, 0, o.x);
+        stf(L, r, 1, o.y);
+        stf(L, r, 2, o.z);
+    }
+}
+// osl_wavelength_color_vf (opcolor.cpp:446-456): the CIE matching functions
+// lerped at (lambda - 380) / 5 (zero outside 380..775 nm), to RGB, scaled
+// by 1 / 2.52 and clamped at zero; no derivatives.
+static __device__ void h_wavelength(const Lane& L, const uint32_t* a) {
+    const float lambda = ldf(L, a[1], 0, 0);
+    const float ii = (lambda - 380.0f) / 5.0f;
+    const int i = (int)ii;
+    float xyz[3] = { 0.0f, 0.0f, 0.0f };
+    if (!((i < 0) | (i >= 80))) {
+        const float rem = ii - (float)i;
+        for (int k = 0; k < 3; ++k) {
+            const float c0 = __uint_as_float(ldw(L, a[2], 9 + 3 * i + k));
+            const float c1 = __uint_as_float(ldw(L, a[2], 9 + 3 * i + 3 + k));
+            xyz[k] = c0 * (1.0f - rem) + c1 * rem;
+        }
+    }
+    float m[9];
+    for (int k = 0; k < 9; ++k) m[k] = __uint_as_float(ldw(L, a[2], k));
+    const C3<float> rgb = cmul33<float>({ xyz[0], xyz[1], xyz[2] }, m);
+    const float sc = (float)(1.0 / 2.52);
+    const float o[3] = { rgb.x * sc, rgb.y * sc, rgb.z * sc };
+    const uint32_t r = a[0];
+    for (int k = 0; k < 3; ++k) stf(L, r, k, o[k] < 0.0f ? 0.0f : o[k]);
+    if (ader(r))
+        for (int k = 0; k < 6; ++k) stf(L, r, 3 + k, 0.0f);
+}
+
 // ---- texture (src/liboslexec/optexture.cpp:54-111 osl_texture; the
 // filtering itself is OIIO's TextureSystem, which is not in the tree) ----
 // A mipmapped bilinear lookup: the footprint of (s, t)'s x/y derivatives in
@@ -2663,6 +2844,8 @@ __device__ __forceinline__ void exec_op(const RunCtx& R, Lane& L, uint32_t code,
     case OP_AREA:
     case OP_FILTERWIDTH: OSLG_TIER_CASE(4, h_deriv_misc(L, code, a)) break;
     case OP_LUMINANCE: OSLG_TIER_CASE(4, h_luminance(L, a)) break;
+    case OP_TRANSFORMC: OSLG_TIER_CASE(4, h_transformc(L, a)) break;
+    case OP_WAVELENGTH: OSLG_TIER_CASE(4, h_wavelength(L, a)) break;
     case OP_BLACKBODY: OSLG_TIER_CASE(4, h_blackbody(L, a)) break;
     case OP_TEXTURE: OSLG_TIER_CASE(4, h_texture(L, a, R.textures, R.ntextures, R.status)) break;
     case OP_ENVIRONMENT: OSLG_TIER_CASE(4, h_environment(L, a, R.textures, R.ntextures, R.status)) break;

@@ -28,6 +28,8 @@
 #include <cmath>
 #include <cstring>
 #include <functional>
+#include <map>
+#include <mutex>
 #include <set>
 #include <sstream>
 
@@ -182,6 +184,7 @@ const std::set<std::string>& deriv_propagating_ops() {
         "inversesqrt", "cbrt", "abs", "fabs", "mix", "clamp", "min", "max", "smoothstep", "select",
         "dot", "cross", "length", "normalize", "distance", "transform", "transformv", "transformn",
         "noise", "snoise", "pnoise", "psnoise", "spline", "splineinverse", "mod", "fmod", "luminance", "radians",
+        "transformc",
         "degrees", "erf", "erfc" };
     return s;
 }
@@ -1405,44 +1408,83 @@ struct Lowerer {
     // its inverse (cofactors over the determinant).
     struct ColorSys {
         float xyz2rgb[3][3];  // row-vector convention: rgb = XYZ * M
+        float rgb2xyz[3][3];  // its inverse, cofactors over the determinant (Imath Matrix33::inverse)
         std::array<float, 3> lum;
     };
-    static const ColorSys& rec709() {
-        static const ColorSys cs = []() {
-            ColorSys c;
-            const float xr = 0.64f, yr = 0.33f, xg = 0.30f, yg = 0.60f, xb = 0.15f, yb = 0.06f, xw = 0.3127f,
-                        yw = 0.3291f;
-            const float R[3] = { xr, yr, 1.0f - (xr + yr) }, G[3] = { xg, yg, 1.0f - (xg + yg) },
-                        B[3] = { xb, yb, 1.0f - (xb + yb) }, W[3] = { xw, yw, 1.0f - (xw + yw) };
-            float r[3] = { G[1] * B[2] - B[1] * G[2], B[0] * G[2] - G[0] * B[2], G[0] * B[1] - B[0] * G[1] };
-            float g[3] = { B[1] * R[2] - R[1] * B[2], R[0] * B[2] - B[0] * R[2], B[0] * R[1] - R[0] * B[1] };
-            float b[3] = { R[1] * G[2] - G[1] * R[2], G[0] * R[2] - R[0] * G[2], R[0] * G[1] - G[0] * R[1] };
-            float w[3] = { r[0] * W[0] + r[1] * W[1] + r[2] * W[2], g[0] * W[0] + g[1] * W[1] + g[2] * W[2],
-                           b[0] * W[0] + b[1] * W[1] + b[2] * W[2] };
+    // The colour systems ColorSystem knows by name (src/liboslexec/opcolor.cpp:
+    // 31-85): red, green, blue and white chromaticities (published standard
+    // primaries; IlluminantC/D65/E/ACES white points).
+    struct Chroma {
+        const char* name;
+        float xr, yr, xg, yg, xb, yb, xw, yw;
+    };
+    static const Chroma* chroma_of(const std::string& name) {
+        static const Chroma k[] = {
+            { "Rec709", 0.64f, 0.33f, 0.30f, 0.60f, 0.15f, 0.06f, 0.3127f, 0.3291f },
+            { "sRGB", 0.64f, 0.33f, 0.30f, 0.60f, 0.15f, 0.06f, 0.3127f, 0.3291f },
+            { "NTSC", 0.67f, 0.33f, 0.21f, 0.71f, 0.14f, 0.08f, 0.3101f, 0.3162f },
+            { "EBU", 0.64f, 0.33f, 0.29f, 0.60f, 0.15f, 0.06f, 0.3127f, 0.3291f },
+            { "PAL", 0.64f, 0.33f, 0.29f, 0.60f, 0.15f, 0.06f, 0.3127f, 0.3291f },
+            { "SECAM", 0.64f, 0.33f, 0.29f, 0.60f, 0.15f, 0.06f, 0.3127f, 0.3291f },
+            { "SMPTE", 0.630f, 0.340f, 0.310f, 0.595f, 0.155f, 0.070f, 0.3127f, 0.3291f },
+            { "HDTV", 0.670f, 0.330f, 0.210f, 0.710f, 0.150f, 0.060f, 0.3127f, 0.3291f },
+            { "CIE", 0.7355f, 0.2645f, 0.2658f, 0.7243f, 0.1669f, 0.0085f, 0.33333333f, 0.33333333f },
+            { "AdobeRGB", 0.64f, 0.33f, 0.21f, 0.71f, 0.15f, 0.06f, 0.3127f, 0.3291f },
+            { "XYZ", 1.0f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f, 0.33333333f, 0.33333333f },
+            { "ACES2065-1", 0.7347f, 0.2653f, 0.0f, 1.0f, 0.0001f, -0.077f, 0.32168f, 0.33767f },
+            { "ACEScg", 0.713f, 0.293f, 0.165f, 0.83f, 0.128f, 0.044f, 0.32168f, 0.33767f },
+        };
+        for (const Chroma& c : k)
+            if (name == c.name) return &c;
+        return nullptr;
+    }
+    static ColorSys make_color_system(const Chroma& ch) {
+        ColorSys c;
+        const float xr = ch.xr, yr = ch.yr, xg = ch.xg, yg = ch.yg, xb = ch.xb, yb = ch.yb, xw = ch.xw, yw = ch.yw;
+        const float R[3] = { xr, yr, 1.0f - (xr + yr) }, G[3] = { xg, yg, 1.0f - (xg + yg) },
+                    B[3] = { xb, yb, 1.0f - (xb + yb) }, W[3] = { xw, yw, 1.0f - (xw + yw) };
+        float r[3] = { G[1] * B[2] - B[1] * G[2], B[0] * G[2] - G[0] * B[2], G[0] * B[1] - B[0] * G[1] };
+        float g[3] = { B[1] * R[2] - R[1] * B[2], R[0] * B[2] - B[0] * R[2], B[0] * R[1] - R[0] * B[1] };
+        float b[3] = { R[1] * G[2] - G[1] * R[2], G[0] * R[2] - R[0] * G[2], R[0] * G[1] - G[0] * R[1] };
+        float w[3] = { r[0] * W[0] + r[1] * W[1] + r[2] * W[2], g[0] * W[0] + g[1] * W[1] + g[2] * W[2],
+                       b[0] * W[0] + b[1] * W[1] + b[2] * W[2] };
+        if (W[1] != 0.0f) {
             const float ws = 1.0f / W[1];
             for (float& x : w) x *= ws;
-            for (int i = 0; i < 3; ++i) { r[i] /= w[0]; g[i] /= w[1]; b[i] /= w[2]; }
-            const float M[3][3] = { { r[0], g[0], b[0] }, { r[1], g[1], b[1] }, { r[2], g[2], b[2] } };
-            std::memcpy(c.xyz2rgb, M, sizeof(M));
-            float C[3][3];  // adjugate
-            C[0][0] = M[1][1] * M[2][2] - M[2][1] * M[1][2];
-            C[0][1] = M[2][1] * M[0][2] - M[0][1] * M[2][2];
-            C[0][2] = M[0][1] * M[1][2] - M[1][1] * M[0][2];
-            C[1][0] = M[2][0] * M[1][2] - M[1][0] * M[2][2];
-            C[1][1] = M[0][0] * M[2][2] - M[2][0] * M[0][2];
-            C[1][2] = M[1][0] * M[0][2] - M[0][0] * M[1][2];
-            C[2][0] = M[1][0] * M[2][1] - M[2][0] * M[1][1];
-            C[2][1] = M[2][0] * M[0][1] - M[0][0] * M[2][1];
-            C[2][2] = M[0][0] * M[1][1] - M[1][0] * M[0][1];
-            const float det = M[0][0] * C[0][0] + M[0][1] * C[1][0] + M[0][2] * C[2][0];
-            c.lum = { C[0][1] / det, C[1][1] / det, C[2][1] / det };
-            const float lum2 = 1.0f - c.lum[0] - c.lum[1];
-            if (std::fabs(lum2 - c.lum[2]) < 0.001f) c.lum[2] = lum2;
-            return c;
-        }();
-        return cs;
+        }
+        for (int i = 0; i < 3; ++i) { r[i] /= w[0]; g[i] /= w[1]; b[i] /= w[2]; }
+        const float M[3][3] = { { r[0], g[0], b[0] }, { r[1], g[1], b[1] }, { r[2], g[2], b[2] } };
+        std::memcpy(c.xyz2rgb, M, sizeof(M));
+        float C[3][3];  // adjugate
+        C[0][0] = M[1][1] * M[2][2] - M[2][1] * M[1][2];
+        C[0][1] = M[2][1] * M[0][2] - M[0][1] * M[2][2];
+        C[0][2] = M[0][1] * M[1][2] - M[1][1] * M[0][2];
+        C[1][0] = M[2][0] * M[1][2] - M[1][0] * M[2][2];
+        C[1][1] = M[0][0] * M[2][2] - M[2][0] * M[0][2];
+        C[1][2] = M[1][0] * M[0][2] - M[0][0] * M[1][2];
+        C[2][0] = M[1][0] * M[2][1] - M[2][0] * M[1][1];
+        C[2][1] = M[2][0] * M[0][1] - M[0][0] * M[2][1];
+        C[2][2] = M[0][0] * M[1][1] - M[1][0] * M[0][1];
+        const float det = M[0][0] * C[0][0] + M[0][1] * C[1][0] + M[0][2] * C[2][0];
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) c.rgb2xyz[i][j] = C[i][j] / det;
+        c.lum = { C[0][1] / det, C[1][1] / det, C[2][1] / det };
+        const float lum2 = 1.0f - c.lum[0] - c.lum[1];
+        if (std::fabs(lum2 - c.lum[2]) < 0.001f) c.lum[2] = lum2;
+        return c;
     }
-    static std::array<float, 3> luminance_scale() { return rec709().lum; }
+    // the system's colour space (attribute "colorspace"), derived as
+    // ColorSystem::set_colorspace does (src/liboslexec/opcolor.cpp:140-190)
+    const ColorSys& csys() const {
+        static std::mutex mu;
+        static std::map<std::string, ColorSys> cache;
+        std::lock_guard<std::mutex> lock(mu);
+        auto it = cache.find(ss.opts.colorspace);
+        if (it != cache.end()) return it->second;
+        const Chroma* ch = chroma_of(ss.opts.colorspace);
+        return cache[ss.opts.colorspace] = make_color_system(ch ? *ch : *chroma_of("Rec709"));
+    }
+    std::array<float, 3> luminance_scale() const { return csys().lum; }
 
     // Blackbody table (src/liboslexec/opcolor.cpp:191-205,
     // opcolor_impl.h:131-260): Planck spectra at temperatures
@@ -1451,10 +1493,16 @@ struct Lowerer {
     // the power 1/5. Followed by the XYZ->RGB matrix and the CIE table for
     // temperatures past the table. expm1, cbrt and pow are evaluated in double precision
     // (the reference uses OIIO's fast approximations).
-    static const std::vector<float>& blackbody_pool() {
-        static const std::vector<float> pool = []() {
+    const std::vector<float>& blackbody_pool() const {
+        static std::mutex mu;
+        static std::map<std::string, std::vector<float>> cache;
+        std::lock_guard<std::mutex> lock(mu);
+        auto found = cache.find(ss.opts.colorspace);
+        if (found != cache.end()) return found->second;
+        const ColorSys& cs = csys();
+        std::vector<float>& pool = cache[ss.opts.colorspace];
+        pool = [&]() {
             std::vector<float> t;
-            const ColorSys& cs = rec709();
             float lastT = 0.0f;
             for (int i = 0; lastT <= 12000.0f; ++i) {
                 const float is = std::sqrt((float)i);
@@ -1839,6 +1887,40 @@ struct Lowerer {
     // src/liboslexec/llvm_gen.cpp:2025-2086; osl_transform_triple,
     // opmatrix.cpp:244-300): the same space twice copies p; an unknown space
     // copies p as well (the reference also reports it as an error).
+    // A colour space name the colour system knows (ColorSystem::transformc,
+    // src/liboslexec/opcolor.cpp:324-380; the system's own colour space
+    // is rgb); -1 for spaces only OpenColorIO could convert.
+    int color_space_code(const std::string& s) const {
+        if (s == "rgb" || s == "RGB" || s == "linear" || s == ss.opts.colorspace) return CS_RGB;
+        if (s == "hsv") return CS_HSV;
+        if (s == "hsl") return CS_HSL;
+        if (s == "YIQ") return CS_YIQ;
+        if (s == "XYZ") return CS_XYZ;
+        if (s == "xyY") return CS_XYY;
+        if (s == "sRGB") return CS_SRGB;
+        return -1;
+    }
+    // r = C converted from space `from` (gsym, -1: rgb) to `to` (-1: rgb)
+    bool lower_color_transform(int r, int c, int from, int to) {
+        auto code = [&](int gs, int& out) {
+            if (gs < 0) { out = CS_RGB; return true; }
+            if (!syms[gs].is_const) return fail("transformc: colour space names must be constant strings");
+            out = color_space_code(const_string(gs));
+            if (out < 0) return fail("colour space '" + const_string(gs) + "' needs OpenColorIO, which is not supported");
+            return true;
+        };
+        int f, t;
+        if (!code(from, f) || !code(to, t)) return false;
+        const ColorSys& cs = csys();
+        std::vector<float> tab;
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) tab.push_back(cs.xyz2rgb[i][j]);
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) tab.push_back(cs.rgb2xyz[i][j]);
+        emit(OP_TRANSFORMC, { A(r), A(c), (uint32_t)f | ((uint32_t)t << 8), A(const_floats(tab)) }, "transformc");
+        return true;
+    }
+
     bool lower_named_transform(const LOp& op) {
         const std::string& n = op.name;
         const size_t na = op.args.size();
@@ -2115,7 +2197,39 @@ struct Lowerer {
         if (n == "point" || n == "vector" || n == "normal" || n == "color") {
             if (na == 4) { emit(OP_CONSTRUCT3, { a(0), a(1), a(2), a(3) }, n); return true; }
             if (na == 2) { emit(OP_ASSIGN, { a(0), a(1), 1u, 1u, 1u }, n); return true; }
-            return fail(n + "(\"space\", ...) construction is not supported yet");
+            if (na == 5 && is_string(op.args[1])) {
+                // constructors in a named space: the triple, then from that
+                // space to rgb (osl_prepend_color_from) or to "common"
+                // (osl_prepend_point_from and its vector/normal forms)
+                emit(OP_CONSTRUCT3, { a(0), a(2), a(3), a(4) }, n);
+                if (n == "color") return lower_color_transform(op.args[0], op.args[0], op.args[1], -1);
+                LOp t;
+                t.name = n == "point" ? "transform" : n == "vector" ? "transformv" : "transformn";
+                GSym c;
+                c.name = "$space";
+                c.type.base = BT_STRING;
+                c.kind = SK_CONST;
+                c.is_const = true;
+                c.sval = { "common" };
+                t.args = { op.args[0], op.args[1], add_sym(c), op.args[0] };
+                return lower_named_transform(t);
+            }
+            return fail(n + ": unsupported constructor form");
+        }
+        if (n == "transformc") {  // transformc r [from] to C
+            if (na == 3) return lower_color_transform(op.args[0], op.args[2], -1, op.args[1]);
+            if (na == 4) return lower_color_transform(op.args[0], op.args[3], op.args[1], op.args[2]);
+            return fail("transformc takes ([from,] to, color)");
+        }
+        if (n == "wavelength_color") {
+            std::vector<float> t;
+            const ColorSys& cs = csys();
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) t.push_back(cs.xyz2rgb[i][j]);
+            for (int i = 0; i < 81; ++i)
+                for (int j = 0; j < 3; ++j) t.push_back(kCIE[i][j]);
+            emit(OP_WAVELENGTH, { a(0), a(1), A(const_floats(t)) }, n);
+            return true;
         }
         if (n == "matrix") {
             int r = op.args[0];
@@ -2309,6 +2423,7 @@ struct Lowerer {
             case OP_NORMALIZE: case OP_TRANSFORM: case OP_MMUL: case OP_AREF: case OP_AASSIGN:
             case OP_MDIV: case OP_TRANSPOSE: case OP_DETERMINANT: case OP_AREA: case OP_FILTERWIDTH:
             case OP_LUMINANCE: case OP_BLACKBODY: case OP_TEXTURE: case OP_SETMESSAGE: case OP_GETMESSAGE:
+            case OP_TRANSFORMC: case OP_WAVELENGTH:
             case OP_ENVIRONMENT:
                 t |= 4u;
                 break;

@@ -36,6 +36,20 @@ __device__ __forceinline__ D2 operator*(D2 a, D2 b) {
 }
 __device__ __forceinline__ D2 operator*(D2 a, float b) { return d2(a.v * b, a.dx * b, a.dy * b); }
 __device__ __forceinline__ D2 operator*(float b, D2 a) { return d2(a.v * b, a.dx * b, a.dy * b); }
+__device__ __forceinline__ D2 operator-(float a, D2 b) { return d2(a - b.v, -b.dx, -b.dy); }
+__device__ __forceinline__ D2 operator+(float a, D2 b) { return d2(a + b.v, b.dx, b.dy); }
+__device__ __forceinline__ D2 operator/(D2 a, D2 b) {
+    const float binv = 1.0f / b.v, ab = a.v / b.v;
+    return d2(ab, binv * (a.dx - ab * b.dx), binv * (a.dy - ab * b.dy));
+}
+__device__ __forceinline__ D2 operator/(float a, D2 b) {
+    const float binv = 1.0f / b.v, ab = a / b.v;
+    return d2(ab, binv * (-ab * b.dx), binv * (-ab * b.dy));
+}
+__device__ __forceinline__ D2 operator/(D2 a, float b) {
+    const float binv = 1.0f / b;
+    return d2(a.v / b, binv * a.dx, binv * a.dy);
+}
 
 __device__ __forceinline__ uint32_t rotl(uint32_t x, int k) { return __funnelshift_l(x, x, k); }
 

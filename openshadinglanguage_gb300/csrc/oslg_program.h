@@ -144,6 +144,10 @@ enum OpCode : uint16_t {
                      // term table in the OP_NOP carriers that follow
     OP_CL_BSDF_EVAL, // a0=terms a1..a5 as OP_BSDF_EVAL; term table follows
     OP_CL_BSDF_SAMPLE,// a0=terms a1..a6 as OP_BSDF_SAMPLE; term table follows
+    // colour spaces (ColorSystem, src/liboslexec/opcolor.cpp:270-380)
+    OP_TRANSFORMC,   // a0=r (triple) a1=C (triple) a2=from space | to space << 8
+                     // a3=colour system table (9 XYZ->RGB then 9 RGB->XYZ floats)
+    OP_WAVELENGTH,   // a0=r (triple) a1=lambda (float) a2=table (9 XYZ->RGB then 81 x 3 CIE)
     OP_COUNT
 };
 
@@ -166,6 +170,9 @@ inline uint32_t noise_word(uint32_t kind, bool periodic, int dims, bool vec, boo
 }
 
 static const uint32_t kNoArg = 0xFFFFFFFFu;
+
+// Colour spaces of OP_TRANSFORMC (rgb is the colour system's own space)
+enum ColorSpace : uint32_t { CS_RGB = 0, CS_HSV, CS_HSL, CS_YIQ, CS_XYZ, CS_XYY, CS_SRGB };
 
 // The string hash the lowering stores for string operands (FNV-1a, 32 bit),
 // usable in constant expressions (keyword names of closure parameters).

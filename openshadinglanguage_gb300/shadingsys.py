@@ -138,7 +138,10 @@ class ShadingSystem:
 
     # ---- configuration -------------------------------------------------------
     def attribute(self, name, value):
-        self._check(C.lib().oslg_attribute_int(self._h, name.encode(), int(value)))
+        if isinstance(value, str):
+            self._check(C.lib().oslg_attribute_string(self._h, name.encode(), value.encode()))
+        else:
+            self._check(C.lib().oslg_attribute_int(self._h, name.encode(), int(value)))
 
     def register_closure(self, name, closure_id):
         self._check(C.lib().oslg_register_closure(self._h, name.encode(), int(closure_id)))

@@ -564,6 +564,154 @@ void op_luminance(Point& P, const uint32_t* a) {
     for (int d = 0; d < nd; ++d) setf(P, a[0], d, getf(P, a[1], 0, d) * sx + getf(P, a[1], 1, d) * sy + getf(P, a[1], 2, d) * sz);
 }
 
+// ---- colour spaces: ColorSystem::transformc (opcolor.cpp:324-380) and the
+// Foley & van Dam conversions of opcolor_impl.h:240-490, for float and
+// Dual2 components (branches on values, Dual2 arithmetic of dual.h) ----
+namespace colorsp {
+inline float val(float x) { return x; }
+inline float val(const DF& x) { return x.v; }
+template <class S> S k(float v) { return S(v); }
+template <class S> S mn(const S& a, const S& b) { return val(a) < val(b) ? a : b; }
+template <class S> S mx(const S& a, const S& b) { return val(a) > val(b) ? a : b; }
+template <class S> struct C { S x, y, z; };
+template <class S> C<S> hsv2rgb(C<S> c) {
+    S h = c.x;
+    const S s = c.y, v = c.z;
+    if (val(s) < 0.0001f) return { v, v, v };
+    h = 6.0f * (h - std::floor(val(h)));
+    const float fh = std::floor(val(h));
+    const int hi = fh != fh ? 0 : (int)fh;
+    const S f = h - (float)hi;
+    const S p = v * (1.0f - s), q = v * (1.0f - s * f), t = v * (1.0f - s * (1.0f - f));
+    switch (hi) {
+    case 0: return { v, t, p };
+    case 1: return { q, v, p };
+    case 2: return { p, v, t };
+    case 3: return { p, q, v };
+    case 4: return { t, p, v };
+    default: return { v, p, q };
+    }
+}
+template <class S> C<S> rgb2hsv(C<S> c) {
+    const S lo = mn(c.x, mn(c.y, c.z)), hi = mx(c.x, mx(c.y, c.z));
+    const S delta = hi - lo;
+    S s = k<S>(0.0f), h = k<S>(0.0f);
+    if (val(hi) > 0.0f) s = delta / hi;
+    if (val(s) > 0.0f) {
+        float kk;
+        S a, b;
+        if (val(c.x) >= val(hi)) { kk = 0.0f / 6.0f; a = c.y; b = c.z; }
+        else if (val(c.y) >= val(hi)) { kk = 2.0f / 6.0f; a = c.z; b = c.x; }
+        else { kk = 4.0f / 6.0f; a = c.x; b = c.y; }
+        h = kk + (a - b) / (6.0f * delta);
+        if (val(h) < 0.0f) h = h + 1.0f;
+    }
+    return { h, s, hi };
+}
+template <class S> C<S> hsl2rgb(C<S> c) {
+    const S h = c.x, l = c.z;
+    S s = c.y;
+    const S v = val(l) <= 0.5f ? l * (1.0f + s) : l * (1.0f - s) + s;
+    if (val(v) <= 0.0f) return { k<S>(0.0f), k<S>(0.0f), k<S>(0.0f) };
+    const S lo = 2.0f * l - v;
+    s = (v - lo) / v;
+    return hsv2rgb<S>({ h, s, v });
+}
+template <class S> C<S> rgb2hsl(C<S> c) {
+    const S lo = mn(c.x, mn(c.y, c.z));
+    const C<S> hsv = rgb2hsv(c);
+    const S hi = hsv.z, l = (lo + hi) / 2.0f;
+    S s;
+    if (val(lo) == val(hi)) s = k<S>(0.0f);
+    else s = (hi - lo) / (val(l) <= 0.5f ? hi + lo : (2.0f - hi) - lo);
+    return { hsv.x, s, l };
+}
+template <class S> C<S> mul33(C<S> c, const float* m) {
+    return { c.x * m[0] + c.y * m[3] + c.z * m[6], c.x * m[1] + c.y * m[4] + c.z * m[7],
+             c.x * m[2] + c.y * m[5] + c.z * m[8] };
+}
+const float kYiq2Rgb[9] = { 1.0000f, 1.0000f, 1.0000f, 0.9557f, -0.2716f, -1.1082f, 0.6199f, -0.6469f, 1.7051f };
+const float kRgb2Yiq[9] = { 0.299f, 0.596f, 0.212f, 0.587f, -0.275f, -0.523f, 0.114f, -0.321f, 0.311f };
+template <class S> C<S> xyz2xyy(C<S> c) {
+    const S n = (c.x + c.y) + c.z;
+    const S ninv = val(n) >= 1.0e-6f ? 1.0f / n : k<S>(0.0f);
+    return { c.x * ninv, c.y * ninv, c.y };
+}
+template <class S> C<S> xyy2xyz(C<S> c) {
+    const S Yy = val(c.y) > 1.0e-6f ? c.z / c.y : k<S>(0.0f);
+    return { Yy * c.x, c.z, Yy * ((1.0f - c.x) - c.y) };
+}
+inline float pw(float x, float y) { return safe_pow(x, y); }
+inline DF pw(const DF& u, float y) {  // dual.h safe_pow, constant exponent
+    const float powuvm1 = safe_pow(u.v, y - 1.0f), powuv = powuvm1 * u.v;
+    const float logu = u.v > 0.0f ? safe_log(u.v) : 0.0f;
+    const float du = y * powuvm1, dv = logu * powuv;
+    return DF(powuv, du * u.dx + dv * 0.0f, du * u.dy + dv * 0.0f);
+}
+template <class S> S s2l(S x) { return val(x) <= 0.04045f ? x * (1.0f / 12.92f) : pw((x + 0.055f) * (1.0f / 1.055f), 2.4f); }
+template <class S> S l2s(S x) { return val(x) <= 0.0031308f ? 12.92f * x : 1.055f * pw(x, 1.f / 2.4f) - 0.055f; }
+template <class S> C<S> convert(C<S> c, uint32_t from, uint32_t to, const float* xyz2rgb, const float* rgb2xyz) {
+    C<S> rgb;
+    switch (from) {
+    case oslg::CS_HSV: rgb = hsv2rgb(c); break;
+    case oslg::CS_HSL: rgb = hsl2rgb(c); break;
+    case oslg::CS_YIQ: rgb = mul33(c, kYiq2Rgb); break;
+    case oslg::CS_XYZ: rgb = mul33(c, xyz2rgb); break;
+    case oslg::CS_XYY: rgb = mul33(xyy2xyz(c), xyz2rgb); break;
+    case oslg::CS_SRGB: rgb = { s2l(c.x), s2l(c.y), s2l(c.z) }; break;
+    default: rgb = c; break;
+    }
+    switch (to) {
+    case oslg::CS_HSV: return rgb2hsv(rgb);
+    case oslg::CS_HSL: return rgb2hsl(rgb);
+    case oslg::CS_YIQ: return mul33(rgb, kRgb2Yiq);
+    case oslg::CS_XYZ: return mul33(rgb, rgb2xyz);
+    case oslg::CS_XYY: return xyz2xyy(mul33(rgb, rgb2xyz));
+    case oslg::CS_SRGB: return { l2s(rgb.x), l2s(rgb.y), l2s(rgb.z) };
+    default: return rgb;
+    }
+}
+}  // namespace colorsp
+
+void op_transformc(Point& P, const uint32_t* a) {
+    float m[18];
+    for (int i = 0; i < 18; ++i) m[i] = bitsf(word(P, a[3], i));
+    const uint32_t from = a[2] & 0xFFu, to = (a[2] >> 8) & 0xFFu;
+    if (ader(a[0])) {
+        const colorsp::C<DF> o = colorsp::convert<DF>({ getd(P, a[1], 0), getd(P, a[1], 1), getd(P, a[1], 2) }, from,
+                                                      to, m, m + 9);
+        putd(P, a[0], 0, o.x);
+        putd(P, a[0], 1, o.y);
+        putd(P, a[0], 2, o.z);
+    } else {
+        const colorsp::C<float> o = colorsp::convert<float>(
+            { getf(P, a[1], 0, 0), getf(P, a[1], 1, 0), getf(P, a[1], 2, 0) }, from, to, m, m + 9);
+        setf(P, a[0], 0, o.x);
+        setf(P, a[0], 1, o.y);
+        setf(P, a[0], 2, o.z);
+    }
+}
+// osl_wavelength_color_vf (opcolor.cpp:446-456)
+void op_wavelength(Point& P, const uint32_t* a) {
+    const float lambda = getf(P, a[1], 0, 0);
+    const float ii = (lambda - 380.0f) / 5.0f;
+    const int i = (int)ii;
+    float xyz[3] = { 0.0f, 0.0f, 0.0f };
+    if (!((i < 0) | (i >= 80))) {
+        const float rem = ii - (float)i;
+        for (int c = 0; c < 3; ++c)
+            xyz[c] = bitsf(word(P, a[2], 9 + 3 * i + c)) * (1.0f - rem) + bitsf(word(P, a[2], 9 + 3 * i + 3 + c)) * rem;
+    }
+    float m[9];
+    for (int i2 = 0; i2 < 9; ++i2) m[i2] = bitsf(word(P, a[2], i2));
+    const colorsp::C<float> rgb = colorsp::mul33<float>({ xyz[0], xyz[1], xyz[2] }, m);
+    const float sc = (float)(1.0 / 2.52);
+    const float o[3] = { rgb.x * sc, rgb.y * sc, rgb.z * sc };
+    for (int c = 0; c < 3; ++c) setf(P, a[0], c, o[c] < 0.0f ? 0.0f : o[c]);
+    if (ader(a[0]))
+        for (int c = 0; c < 6; ++c) setf(P, a[0], 3 + c, 0.0f);
+}
+
 // ---- texture: mipmapped bilinear lookup (osl_texture, optexture.cpp:54-111;
 // the filter stands in for OIIO's TextureSystem, which is not in the tree) --
 struct OTexture {
@@ -1565,6 +1713,8 @@ struct Runner {
             case oslg::OP_AREA: op_area(P, a); break;
             case oslg::OP_FILTERWIDTH: op_filterwidth(P, a); break;
             case oslg::OP_LUMINANCE: op_luminance(P, a); break;
+            case oslg::OP_TRANSFORMC: op_transformc(P, a); break;
+            case oslg::OP_WAVELENGTH: op_wavelength(P, a); break;
             case oslg::OP_BLACKBODY: op_blackbody(P, a); break;
             case oslg::OP_TEXTURE: op_texture(P, a); break;
             case oslg::OP_ENVIRONMENT: op_environment(P, a); break;

@@ -109,7 +109,7 @@ def read_tiff(path):
 
 def read_exr(path):
     """Scanline OpenEXR with ZIP compression (16 lines per block) and HALF
-    channels, as written by the reference's testshade -od half: zlib, then
+    or FLOAT channels (testshade -od half / float): zlib, then
     undo the byte predictor and the even/odd byte split of the format."""
     d = open(path, "rb").read()
     assert d[:4] == b"\x76\x2f\x31\x01", "not an OpenEXR file"
@@ -128,14 +128,16 @@ def read_exr(path):
     assert attrs["compression"][0] == 3, "only ZIP compression is read here"
     x0, y0, x1, y1 = struct.unpack("<4i", attrs["dataWindow"])
     W, H = x1 - x0 + 1, y1 - y0 + 1
-    chans, c = [], attrs["channels"]
+    chans, ptypes, c = [], [], attrs["channels"]
     j = 0
     while c[j] != 0:
         n = c.index(b"\0", j)
         nm = c[j:n].decode()
         (ptype,) = struct.unpack("<i", c[n + 1:n + 5])
-        assert ptype == 1, "only HALF channels are read here"
+        assert ptype in (1, 2), "only HALF and FLOAT channels are read here"
+        assert not chans or ptype == ptypes[0], "one pixel type for every channel"
         chans.append(nm)
+        ptypes.append(ptype)
         j = n + 17
     nblocks = (H + 15) // 16
     offsets = struct.unpack("<%dQ" % nblocks, d[i:i + 8 * nblocks])
@@ -150,7 +152,7 @@ def read_exr(path):
         inter[0::2] = t[:half]
         inter[1::2] = t[half:]
         lines = min(16, H - (y - y0))
-        vals = np.frombuffer(inter.tobytes(), np.float16).reshape(lines, len(chans), W)
+        vals = np.frombuffer(inter.tobytes(), np.float16 if ptypes[0] == 1 else np.float32).reshape(lines, len(chans), W)
         img[y - y0:y - y0 + lines] = vals.transpose(0, 2, 1).astype(np.float32)
     return img, chans
 
@@ -164,6 +166,7 @@ EXR_IMAGES = {
     "furnace_diffuse": ["testsuite/render-furnace-diffuse/ref/out.exr"],
     "furnace_oren_nayar": ["testsuite/render-mx-furnace-oren-nayar/ref/out.exr"],
     "furnace_sheen": ["testsuite/render-mx-furnace-sheen/ref/out.exr"],
+    "wavelength_color": ["testsuite/wavelength_color/ref/out.exr"],
 }
 
 IMAGES = {
@@ -207,6 +210,9 @@ TEXTS = {
     "closure_conditional_out.txt": "testsuite/closure-conditional/ref/out.txt",
     "matrix_out.txt": "testsuite/matrix/ref/out.txt",
     "transform_out.txt": "testsuite/transform/ref/out.txt",
+    "transformc_out.txt": "testsuite/transformc/ref/out.txt",
+    "colorspace_out.txt": "testsuite/colorspace/ref/out.txt",
+    "color_out.txt": "testsuite/color/ref/out.txt",
 }
 
 
