@@ -677,13 +677,12 @@ int oslg_execute_batch_host(oslg_system* sys, oslg_group* group, int64_t npoints
         const Op* ops = reinterpret_cast<const Op*>(cg.blob.data() + sizeof(ProgramHeader));
         for (uint32_t i = 0; i < cg.header.nops; ++i) {
             const Op& op = ops[i];
-            const bool out = op.code == OP_STORE_OUTPUT || op.code == OP_STORE_CLOSURE || op.code == OP_BSDF_EVAL ||
-                             op.code == OP_BSDF_SAMPLE;
+            const bool out = writes_output_record(op.code);
             if (out && (int64_t)(int32_t)op.a[2] != output_stride)
                 return fail(sys, OSLG_ERR_ARG, "output_stride differs from the group's output record stride");
             if (op.code == OP_LOAD_USERDATA && (int64_t)(int32_t)op.a[2] != userdata_stride)
                 return fail(sys, OSLG_ERR_ARG, "userdata_stride differs from the group's userdata record stride");
-            if (op.code == OP_BSDF_SAMPLE && (int64_t)(int32_t)op.a[6] != userdata_stride)
+            if (reads_sample_record(op.code) && (int64_t)(int32_t)op.a[6] != userdata_stride)
                 return fail(sys, OSLG_ERR_ARG, "userdata_stride differs from the group's sampling record stride");
         }
         // chunks of at most an eighth of the points (>= 64K), three slots in flight
@@ -861,11 +860,9 @@ int oslg_group_record_strides(oslg_system* sys, oslg_group* group, int64_t* outp
         *userdata_stride = 0;
         for (uint32_t i = 0; i < cg.header.nops; ++i) {
             const Op& op = ops[i];
-            if (op.code == OP_STORE_OUTPUT || op.code == OP_STORE_CLOSURE || op.code == OP_BSDF_EVAL ||
-                op.code == OP_BSDF_SAMPLE)
-                *output_stride = (int64_t)(int32_t)op.a[2];
+            if (writes_output_record(op.code)) *output_stride = (int64_t)(int32_t)op.a[2];
             if (op.code == OP_LOAD_USERDATA) *userdata_stride = (int64_t)(int32_t)op.a[2];
-            if (op.code == OP_BSDF_SAMPLE) *userdata_stride = (int64_t)(int32_t)op.a[6];
+            if (reads_sample_record(op.code)) *userdata_stride = (int64_t)(int32_t)op.a[6];
         }
         return OSLG_OK;
     });

@@ -1376,7 +1376,7 @@ struct Lowerer {
             case OP_NOP: case OP_IF: case OP_ELSE: case OP_ENDIF: case OP_LOOP_BEGIN: case OP_LOOP_TEST:
             case OP_LOOP_STEP: case OP_LOOP_END: case OP_JUMP: case OP_BREAK: case OP_CONTINUE: case OP_RETURN:
             case OP_EXIT: case OP_LAYER_END: case OP_STORE_OUTPUT: case OP_STORE_CLOSURE: case OP_BSDF_EVAL:
-            case OP_BSDF_SAMPLE:
+            case OP_BSDF_SAMPLE: case OP_CL_STORE: case OP_CL_BSDF_EVAL: case OP_CL_BSDF_SAMPLE:
                 continue;
             default:
                 break;

@@ -171,6 +171,20 @@ inline uint32_t noise_word(uint32_t kind, bool periodic, int dims, bool vec, boo
 
 static const uint32_t kNoArg = 0xFFFFFFFFu;
 
+// Ops that write the point's output record at a1 (byte offset), a2 (stride),
+// and the sampling ops that read its userdata record at a5, a6.
+#ifdef __CUDACC__
+__host__ __device__
+#endif
+inline bool writes_output_record(uint32_t c) {
+    return c == OP_STORE_OUTPUT || c == OP_STORE_CLOSURE || c == OP_BSDF_EVAL || c == OP_BSDF_SAMPLE ||
+           c == OP_CL_STORE || c == OP_CL_BSDF_EVAL || c == OP_CL_BSDF_SAMPLE;
+}
+#ifdef __CUDACC__
+__host__ __device__
+#endif
+inline bool reads_sample_record(uint32_t c) { return c == OP_BSDF_SAMPLE || c == OP_CL_BSDF_SAMPLE; }
+
 // Colour spaces of OP_TRANSFORMC (rgb is the colour system's own space)
 enum ColorSpace : uint32_t { CS_RGB = 0, CS_HSV, CS_HSL, CS_YIQ, CS_XYZ, CS_XYY, CS_SRGB };
 
