@@ -95,6 +95,17 @@ typedef struct oslg_shaderglobals {
     oslg_field time, dtime, dPdtime;
     oslg_field Ps, dPsdx, dPsdy;
     oslg_field surfacearea;
+    /* Block<int> flipHandedness and backfacing (batched_shaderglobals.h:
+     * 136-140): with data, one int32 per point (data[i], nonzero = true);
+     * without, value[0] != 0 holds for every point. flipHandedness flips
+     * calculatenormal(); backfacing() returns backfacing. */
+    oslg_field flipHandedness;
+    oslg_field backfacing;
+    /* UniformShaderGlobals::raytype (batched_shaderglobals.h:47): the
+     * raytype bits of the rays being shaded; raytype(name) tests the bit
+     * of name's position in the system's "raytypes" list. */
+    int32_t raytype;
+    int32_t reserved[3];
 } oslg_shaderglobals;
 
 /* ---- ShadingSystem ------------------------------------------------------ */
@@ -114,7 +125,12 @@ int oslg_destroy_system(oslg_system* sys);
  * specialized kernels: 256-thread CTAs per SM that must fit, 2..8),
  * "strict_messages", "opt_constant_fold", "opt_elide_useless_ops" (as the
  * reference's ShadingSystem attributes of those names, shadingsys.cpp:1639-1684),
- * "max_loop_iterations" (loop back edges one point may take, summed over
+ * "userdata_isconnected" (isconnected() counts lockgeom=0 parameters as
+ * connected, shadingsys.cpp:1073), "fast_math" (1, the default: sin, cos,
+ * tan, asin, acos, atan, atan2, sinh, cosh, tanh, exp, exp2, expm1, log,
+ * log2, log10, pow, erf, erfc, cbrt and sincos use OpenImageIO's fast_*
+ * approximations as the reference's default USE_FAST_MATH build; 0: the
+ * correctly rounded forms), "max_loop_iterations" (loop back edges one point may take, summed over
  * the group's loops, before the launch ends with the loop-limit status
  * bit; 0 keeps the default 2^24; the reference has no such limit),
  * "host_direct_outputs" (host-buffer execution writes pinned output records
@@ -127,6 +143,12 @@ int oslg_attribute_int(oslg_system* sys, const char* name, int value);
  * shadingsys.cpp:1613). Groups lowered afterwards use it for luminance,
  * blackbody, wavelength_color and transformc. */
 int oslg_attribute_string(oslg_system* sys, const char* name, const char* value);
+/* ShadingSystem::attribute(name, TypeDesc(TypeString, n), values)
+ * (oslexec.h:324). String-array options: "raytypes" (at most 32 names;
+ * raytype(name) tests bit 1 << position; default camera, shadow,
+ * reflection, refraction, diffuse, glossy, subsurface, displacement as
+ * shadingsys.cpp:1256-1265). Groups lowered afterwards use it. */
+int oslg_attribute_strings(oslg_system* sys, const char* name, const char* const* values, int n);
 /* ShadingSystem::register_closure (oslexec.h:1041). Parameters are taken
  * positionally from the `closure` op's arguments. */
 int oslg_register_closure(oslg_system* sys, const char* name, int id);

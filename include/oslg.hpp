@@ -58,6 +58,8 @@ template <int W> struct VaryingShaderGlobals {
     Block<Vec3, W> dPdtime;
     Block<Vec3, W> Ps, dPsdx, dPsdy;
     Block<float, W> surfacearea;
+    Block<int, W> flipHandedness;
+    Block<int, W> backfacing;
 };
 
 template <int W> struct BatchedShaderGlobals {
@@ -129,7 +131,7 @@ public:
             int64_t out_stride = 0, ud_stride = 0;
             if (!ss_.ok(oslg_group_record_strides(ss_.sys_, group, &out_stride, &ud_stride))) return false;
             if (!run || batch_size == 0) return true;
-            oslg_shaderglobals sg = view(bsg.varying);
+            oslg_shaderglobals sg = view(bsg);
             return ss_.ok(oslg_execute_batch_host(ss_.sys_, group, batch_size, &sg, userdata_base_ptr, ud_stride,
                                                   output_base_ptr, out_stride, OSLG_HOST_PRESERVE_OUTPUTS));
         }
@@ -149,8 +151,14 @@ public:
             f.data = b.data;
             f.plane_stride = W;
         }
-        static oslg_shaderglobals view(const VaryingShaderGlobals<W>& v) {
+        static void put(oslg_field& f, const Block<int, W>& b) {  // int32 lanes
+            f.data = reinterpret_cast<const float*>(b.data);
+            f.plane_stride = W;
+        }
+        static oslg_shaderglobals view(const BatchedShaderGlobals<W>& bsg) {
+            const VaryingShaderGlobals<W>& v = bsg.varying;
             oslg_shaderglobals g = {};
+            g.raytype = bsg.uniform.raytype;
             put(g.P, v.P); put(g.dPdx, v.dPdx); put(g.dPdy, v.dPdy); put(g.dPdz, v.dPdz);
             put(g.I, v.I); put(g.dIdx, v.dIdx); put(g.dIdy, v.dIdy);
             put(g.N, v.N); put(g.Ng, v.Ng);
@@ -160,6 +168,8 @@ public:
             put(g.time, v.time); put(g.dtime, v.dtime); put(g.dPdtime, v.dPdtime);
             put(g.Ps, v.Ps); put(g.dPsdx, v.dPsdx); put(g.dPsdy, v.dPsdy);
             put(g.surfacearea, v.surfacearea);
+            put(g.flipHandedness, v.flipHandedness);
+            put(g.backfacing, v.backfacing);
             return g;
         }
         ShadingSystem& ss_;

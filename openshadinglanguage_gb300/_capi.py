@@ -42,7 +42,9 @@ class FieldC(ctypes.Structure):
 
 GLOBAL_FIELDS = ["P", "dPdx", "dPdy", "dPdz", "I", "dIdx", "dIdy", "N", "Ng", "u", "dudx", "dudy",
                  "v", "dvdx", "dvdy", "dPdu", "dPdv", "time", "dtime", "dPdtime", "Ps", "dPsdx",
-                 "dPsdy", "surfacearea"]
+                 "dPsdy", "surfacearea", "flipHandedness", "backfacing"]
+# fields whose per-point data is int32
+INT_GLOBAL_FIELDS = ("flipHandedness", "backfacing")
 
 
 class BatchTuningC(ctypes.Structure):
@@ -88,7 +90,8 @@ class WavefrontStatsC(ctypes.Structure):
 
 
 class ShaderGlobalsC(ctypes.Structure):
-    _fields_ = [(n, FieldC) for n in GLOBAL_FIELDS]
+    _fields_ = [(n, FieldC) for n in GLOBAL_FIELDS] + [("raytype", ctypes.c_int32),
+                                                       ("reserved", ctypes.c_int32 * 3)]
 
 
 _EXPORTS = {
@@ -96,6 +99,8 @@ _EXPORTS = {
     "oslg_destroy_system": (ctypes.c_int, [ctypes.c_void_p]),
     "oslg_attribute_int": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int]),
     "oslg_attribute_string": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p]),
+    "oslg_attribute_strings": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_char_p),
+                                              ctypes.c_int]),
     "oslg_register_closure": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int]),
     "oslg_load_memory_compiled_shader": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p]),
     "oslg_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),

@@ -207,6 +207,8 @@ int oslg_attribute_int(oslg_system* sys, const char* name, int value) {
     else if (n == "opt_constant_fold") sys->ss.opts.opt_constant_fold = value != 0;
     else if (n == "opt_elide_useless_ops") sys->ss.opts.opt_elide_useless_ops = value != 0;
     else if (n == "opt_static_closures") sys->ss.opts.opt_static_closures = value != 0;
+    else if (n == "userdata_isconnected") sys->ss.opts.userdata_isconnected = value != 0;
+    else if (n == "fast_math") sys->ss.opts.fast_math = value != 0;
     else if (n == "jit") sys->jit = value;
     else if (n == "jit_block") sys->jit_block = value;
     else if (n == "jit_pool_smem") sys->jit_pool_smem = value;
@@ -232,6 +234,22 @@ int oslg_attribute_string(oslg_system* sys, const char* name, const char* value)
         return fail(sys, OSLG_ERR_ARG, "unknown colour space '" + v + "'");
     }
     return fail(sys, OSLG_ERR_ARG, "unknown string attribute '" + n + "'");
+}
+
+int oslg_attribute_strings(oslg_system* sys, const char* name, const char* const* values, int n) {
+    if (!sys || !name || n < 0 || (n > 0 && !values)) return OSLG_ERR_ARG;
+    std::string nm(name);
+    if (nm == "raytypes") {
+        if (n > 32) return fail(sys, OSLG_ERR_ARG, "at most 32 raytypes");
+        std::vector<std::string> v;
+        for (int i = 0; i < n; ++i) {
+            if (!values[i]) return OSLG_ERR_ARG;
+            v.push_back(values[i]);
+        }
+        sys->ss.opts.raytypes = v;
+        return OSLG_OK;
+    }
+    return fail(sys, OSLG_ERR_ARG, "unknown string-array attribute '" + nm + "'");
 }
 
 int oslg_register_closure(oslg_system* sys, const char* name, int id) {
@@ -642,7 +660,7 @@ static int upload_textures(oslg_system* sys) {
 // ---- execution over host buffers --------------------------------------------------
 namespace {
 // components per shader-global field (GlobalId order)
-const int kGlobalComps[G_COUNT] = { 3, 3, 3, 3, 3, 3, 3, 3, 3, 1, 1, 1, 1, 1, 1, 3, 3, 1, 1, 3, 3, 3, 3, 1 };
+const int kGlobalComps[G_COUNT] = { 3, 3, 3, 3, 3, 3, 3, 3, 3, 1, 1, 1, 1, 1, 1, 3, 3, 1, 1, 3, 3, 3, 3, 1, 1, 1 };
 
 bool cu_ok(oslg_system* sys, cudaError_t e, const char* what, int* rc) {
     if (e == cudaSuccess) return true;

@@ -192,6 +192,14 @@ struct SystemOptions {
     int max_closure_components = 16;  // closure tree nodes per point when closures are made inside loops
     int max_closure_terms = 16;
     int max_loop_iterations = 0;  // loop back edges per point (0: the program format's default)
+    // transcendental ops in OpenImageIO's fast_* forms, as the reference's
+    // default build (USE_FAST_MATH=ON, CMakeLists.txt:145-150); 0: the
+    // math-library forms of a USE_FAST_MATH=OFF build
+    int fast_math = 1;
+    int userdata_isconnected = 0;  // "userdata_isconnected" (shadingsys.cpp:1073): lockgeom=0 params count as connected
+    // "raytypes" (shadingsys.cpp:1256-1265): raytype(name) tests bit 1 << position
+    std::vector<std::string> raytypes = { "camera", "shadow", "reflection", "refraction",
+                                          "diffuse", "glossy", "subsurface", "displacement" };
     int heap_in_smem = -1;  // -1 auto
     int threads_per_block = 256;
     int points_per_thread = 1;

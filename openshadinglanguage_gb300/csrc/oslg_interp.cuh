@@ -29,6 +29,7 @@
 #include <string>
 
 #include "oslg_exec.h"
+#include "oslg_fastmath.cuh"
 #include "oslg_gabor.cuh"
 #include "oslg_noise.cuh"
 #include "oslg_shading.cuh"
@@ -173,6 +174,15 @@ __device__ __forceinline__ float flog10_raw(float x) { return (float)log10((doub
 __device__ __forceinline__ float fpow_raw(float x, float y) { return (float)pow((double)x, (double)y); }
 static const float kFltMin = 1.17549435e-38f;
 static const float kFltMax = 3.40282347e+38f;
+// logb as OpenImageIO's fast_logb (fmath.h, the host path the reference's
+// logb op calls, llvm_ops.cpp:542-545): the unbiased exponent of |x|
+// clamped to the normal range, so 0 gives -126 and infinity 127
+__device__ __forceinline__ float logb_fast(float x) {
+    x = fabsf(x);
+    if (x < kFltMin) x = kFltMin;
+    if (x > kFltMax) x = kFltMax;
+    return (float)((int)(__float_as_uint(x) >> 23) - 127);
+}
 // OIIO safe_log/log2/log10: clamp the argument to the smallest normal
 __device__ __forceinline__ float safe_log(float x) { return flog_raw(x < kFltMin ? kFltMin : x); }
 __device__ __forceinline__ float safe_log2(float x) { return flog2_raw(x < kFltMin ? kFltMin : x); }
@@ -478,17 +488,66 @@ __device__ __forceinline__ bool truth(const Lane& L, uint32_t a) {
     return ldw(L, a, 0) != 0u;
 }
 
-// componentwise unary math with dual.h derivative rules
+// OpenImageIO fast_* forms of the transcendental ops with dual.h's fast_*
+// derivative rules (dual.h:836-1262); false when OPC has none
+template <int OPC>
+__device__ __forceinline__ bool unary_fast(float v, float& f, float& df, bool& zero_derivs) {
+    switch (OPC) {
+    case OP_SIN: fm::sincos(v, &f, &df); return true;
+    case OP_COS: { float sv; fm::sincos(v, &sv, &f); df = -sv; return true; }
+    case OP_TAN: { f = fm::tan(v); const float cs = fm::cos(v); df = 1.0f / (cs * cs); return true; }
+    case OP_ASIN:
+        f = fm::asin(v);
+        df = fabsf(v) < 1.0f ? 1.0f / sqrtf(1.0f - v * v) : 0.0f;
+        return true;
+    case OP_ACOS:
+        f = fm::acos(v);
+        df = fabsf(v) < 1.0f ? -1.0f / sqrtf(1.0f - v * v) : 0.0f;
+        return true;
+    case OP_ATAN: f = fm::atan(v); df = 1.0f / (1.0f + v * v); return true;
+    case OP_SINH: f = fm::sinh(v); df = fm::cosh(v); return true;
+    case OP_COSH: f = fm::cosh(v); df = fm::sinh(v); return true;
+    case OP_TANH: { f = fm::tanh(v); const float ch = fm::cosh(v); df = 1.0f / (ch * ch); return true; }
+    case OP_EXP: f = fm::exp(v); df = f; return true;
+    case OP_EXP2: f = fm::exp2(v); df = f * 0.693147180559945309417f; return true;
+    case OP_EXPM1: f = fm::expm1(v); df = fm::exp(v); return true;
+    case OP_LOG: f = fm::log(v); df = v < kFltMin ? 0.0f : 1.0f / v; return true;
+    case OP_LOG2: {
+        f = fm::log2(v);
+        const float aln2 = v * 0.693147180559945309417f;
+        df = aln2 < kFltMin ? 0.0f : 1.0f / aln2;
+        return true;
+    }
+    case OP_LOG10: {
+        f = fm::log10(v);
+        const float aln10 = v * 2.30258509299404568402f;
+        df = aln10 < kFltMin ? 0.0f : 1.0f / aln10;
+        return true;
+    }
+    case OP_ERF: f = fm::erf(v); df = fm::exp(-v * v) * 1.12837916709551257390f; return true;
+    case OP_ERFC: f = fm::erfc(v); df = fm::exp(-v * v) * -1.12837916709551257390f; return true;
+    case OP_CBRT:
+        if (v != 0.0f) { f = fm::cbrt(v); df = 1.0f / (3.0f * f * f); }
+        else { f = 0.0f; zero_derivs = true; }
+        return true;
+    default: return false;
+    }
+}
+
+// componentwise unary math with dual.h derivative rules; a2 = 1 selects
+// the fast forms
 template <int OPC>
 static __device__ void h_unary(const Lane& L, const uint32_t* a) {
     uint32_t r = a[0], x = a[1];
     int nc = anc(r);
     bool rd = ader(r);
+    const bool fast = a[2] == 1u;
     OSLG_SPEC_UNROLL
     for (int c = 0; c < nc; ++c) {
         float v = ldf(L, x, c, 0);
         float f, df = 0.0f;
         bool zero_derivs = false;
+        if (!(fast && unary_fast<OPC>(v, f, df, zero_derivs)))
         switch (OPC) {
         case OP_ABS: f = fabsf(v); df = v >= 0.0f ? 1.0f : -1.0f; break;
         case OP_FLOOR: f = floorf(v); zero_derivs = true; break;
@@ -528,6 +587,9 @@ static __device__ void h_unary(const Lane& L, const uint32_t* a) {
         case OP_LOG: f = safe_log(v); df = v < kFltMin ? 0.0f : 1.0f / v; break;
         case OP_LOG2: f = safe_log2(v); df = v < kFltMin ? 0.0f : 1.0f / (v * 0.693147180559945309417f); break;
         case OP_LOG10: f = safe_log10(v); df = v < kFltMin ? 0.0f : 1.0f / (v * 2.30258509299404568402f); break;
+        case OP_LOGB: f = logb_fast(v); zero_derivs = true; break;
+        case OP_ERF: f = (float)erf((double)v); df = 1.12837916709551257390f * fexp(-v * v); break;
+        case OP_ERFC: f = (float)erfc((double)v); df = -1.12837916709551257390f * fexp(-v * v); break;
         case OP_RADIANS: f = v * (3.14159265358979323846f / 180.0f); df = 3.14159265358979323846f / 180.0f; break;
         case OP_DEGREES: f = v * (180.0f / 3.14159265358979323846f); df = 180.0f / 3.14159265358979323846f; break;
         case OP_NEG: f = -v; df = -1.0f; break;
@@ -557,22 +619,23 @@ static __device__ void h_binary(const Lane& L, const uint32_t* a) {
     uint32_t r = a[0], x = a[1], y = a[2];
     int nc = anc(r);
     bool rd = ader(r);
+    const bool fast = a[3] == 1u;  // pow, atan2: the fast forms
     OSLG_SPEC_UNROLL
     for (int c = 0; c < nc; ++c) {
         D2 u = ldd(L, x, c), v = ldd(L, y, c);
         D2 res;
         if (OPC == OP_POW) {
             if (rd && (ader(x) || ader(y))) {
-                float powuvm1 = safe_pow(u.v, v.v - 1.0f);
+                float powuvm1 = fast ? fm::safe_pow(u.v, v.v - 1.0f) : safe_pow(u.v, v.v - 1.0f);
                 float powuv = powuvm1 * u.v;
-                float logu = u.v > 0.0f ? safe_log(u.v) : 0.0f;
+                float logu = u.v > 0.0f ? (fast ? fm::log(u.v) : safe_log(u.v)) : 0.0f;
                 float du = v.v * powuvm1, dv = logu * powuv;
                 res = d2(powuv, du * u.dx + dv * v.dx, du * u.dy + dv * v.dy);
             } else {
-                res = d2c(safe_pow(u.v, v.v));
+                res = d2c(fast ? fm::safe_pow(u.v, v.v) : safe_pow(u.v, v.v));
             }
         } else if (OPC == OP_ATAN2) {
-            float f = fatan2(u.v, v.v);
+            float f = fast ? fm::atan2(u.v, v.v) : fatan2(u.v, v.v);
             float denom = (v.v == 0.0f && u.v == 0.0f) ? 0.0f : 1.0f / (v.v * v.v + u.v * u.v);
             float dfdy = -v.v * denom, dfdx = u.v * denom;
             res = d2(f, dfdy * u.dx + dfdx * v.dx, dfdy * u.dy + dfdx * v.dy);
@@ -904,6 +967,41 @@ static __device__ void h_deriv_misc(const Lane& L, uint32_t code, const uint32_t
             stval(L, r, c, sqrtf(dx * dx + dy * dy));
         }
     }
+}
+
+// sincos (llvm_ops.cpp:298-430): sine and cosine of each component; each
+// result carries the derivatives its symbol asks for; a3 = 1: fast forms
+static __device__ void h_sincos(const Lane& L, const uint32_t* a) {
+    const uint32_t x = a[0], rs = a[1], rc = a[2];
+    const int nc = anc(x);
+    OSLG_SPEC_UNROLL
+    for (int c = 0; c < nc; ++c) {
+        const float v = ldf(L, x, c, 0), xdx = ldf(L, x, c, 1), xdy = ldf(L, x, c, 2);  // x may alias a result
+        float sv, cv;
+        if (a[3] == 1u) fm::sincos(v, &sv, &cv);
+        else { sv = fsin(v); cv = fcos(v); }
+        stf(L, rs, c, sv);
+        stf(L, rc, c, cv);
+        if (ader(rs)) { stf(L, rs, nc + c, cv * xdx); stf(L, rs, 2 * nc + c, cv * xdy); }
+        if (ader(rc)) { stf(L, rc, nc + c, -sv * xdx); stf(L, rc, 2 * nc + c, -sv * xdy); }
+    }
+}
+
+// calculatenormal (llvm_ops.cpp:915-934): dP/dx x dP/dy, operands swapped
+// when flipHandedness is set; not normalized, no derivatives
+static __device__ void h_calcnormal(const Lane& L, const uint32_t* a, const oslg_shaderglobals& G);
+// raytype (batched_llvm_gen.cpp:8520-8560): the raytype bits of the rays
+// being shaded against the name's bit, ShadingSystemImpl::raytype_bit
+// (shadingsys.cpp:3823-3829) looked up at run time for a varying name
+static __device__ void h_raytype(const Lane& L, const uint32_t* a, const oslg_shaderglobals& G) {
+    uint32_t bit = a[2];
+    if (a[1] != kNoArg) {
+        const uint32_t h = ldw(L, a[1], 0);
+        bit = 0;
+        for (int i = 0; i < (int)a[4]; ++i)
+            if (ldw(L, a[3], i) == h) { bit = 1u << i; break; }
+    }
+    stw(L, a[0], 0, ((uint32_t)G.raytype & bit) != 0u ? 1u : 0u);
 }
 
 // luminance: dot with the colour system's luminance scale (a2, a constant
@@ -1530,16 +1628,25 @@ __device__ __forceinline__ const oslg_field& gfield(const oslg_shaderglobals& G,
     case G_DPDU: return G.dPdu; case G_DPDV: return G.dPdv;
     case G_TIME: return G.time; case G_DTIME: return G.dtime; case G_DPDTIME: return G.dPdtime;
     case G_PS: return G.Ps; case G_DPSDX: return G.dPsdx; case G_DPSDY: return G.dPsdy;
+    case G_FLIPHANDEDNESS: return G.flipHandedness; case G_BACKFACING: return G.backfacing;
     default: return G.surfacearea;
     }
 }
 __device__ __forceinline__ float fld(const oslg_field& f, int c, int64_t pt) {
     return f.data ? __ldg(f.data + c * f.plane_stride + pt) : f.value[c];
 }
+// an int flag field: int32 per point, or value[0] != 0 for all
+__device__ __forceinline__ bool gflag(const oslg_field& f, int64_t pt) {
+    return f.data ? __ldg(reinterpret_cast<const int*>(f.data) + pt) != 0 : f.value[0] != 0.0f;
+}
 
 static __device__ void h_load_global(const Lane& L, const uint32_t* a, const oslg_shaderglobals& G) {
     uint32_t r = a[0];
     int id = (int)a[1];
+    if (global_is_int((uint32_t)id)) {  // flipHandedness, backfacing: 0 or 1
+        stw(L, r, 0, gflag(gfield(G, id), L.pt) ? 1u : 0u);
+        return;
+    }
     int nc = anc(r);
     const oslg_field& f = gfield(G, id);
     OSLG_SPEC_UNROLL
@@ -1557,6 +1664,16 @@ static __device__ void h_load_global(const Lane& L, const uint32_t* a, const osl
             stf(L, r, 2 * nc + c, dyid >= 0 ? fld(gfield(G, dyid), c, L.pt) : 0.0f);
         }
     }
+}
+
+static __device__ void h_calcnormal(const Lane& L, const uint32_t* a, const oslg_shaderglobals& G) {
+    const uint32_t r = a[0], p = a[1];
+    const V3 dx = v3(ldf(L, p, 0, 1), ldf(L, p, 1, 1), ldf(L, p, 2, 1));
+    const V3 dy = v3(ldf(L, p, 0, 2), ldf(L, p, 1, 2), ldf(L, p, 2, 2));
+    const V3 n = gflag(G.flipHandedness, L.pt) ? vcross(dy, dx) : vcross(dx, dy);
+    stval(L, r, 0, n.x);
+    stval(L, r, 1, n.y);
+    stval(L, r, 2, n.z);
 }
 
 // a3 bit 1: the record carries [val][dx][dy]; a destination with
@@ -2804,6 +2921,12 @@ __device__ __forceinline__ void exec_op(const RunCtx& R, Lane& L, uint32_t code,
     case OP_LOG: OSLG_TIER_CASE(4, h_unary<OP_LOG>(L, a)) break;
     case OP_LOG2: OSLG_TIER_CASE(4, h_unary<OP_LOG2>(L, a)) break;
     case OP_LOG10: OSLG_TIER_CASE(4, h_unary<OP_LOG10>(L, a)) break;
+    case OP_LOGB: OSLG_TIER_CASE(4, h_unary<OP_LOGB>(L, a)) break;
+    case OP_ERF: OSLG_TIER_CASE(4, h_unary<OP_ERF>(L, a)) break;
+    case OP_ERFC: OSLG_TIER_CASE(4, h_unary<OP_ERFC>(L, a)) break;
+    case OP_SINCOS: OSLG_TIER_CASE(4, h_sincos(L, a)) break;
+    case OP_CALCNORMAL: OSLG_TIER_CASE(4, h_calcnormal(L, a, *R.G)) break;
+    case OP_RAYTYPE: OSLG_TIER_CASE(4, h_raytype(L, a, *R.G)) break;
     case OP_RADIANS: h_unary<OP_RADIANS>(L, a); break;
     case OP_DEGREES: h_unary<OP_DEGREES>(L, a); break;
     case OP_ISNAN: stw(L, a[0], 0, isnan(ldf(L, a[1], 0, 0)) ? 1u : 0u); break;

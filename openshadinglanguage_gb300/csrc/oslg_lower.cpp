@@ -68,7 +68,7 @@ struct LOp {
 const char* kGlobalNames[G_COUNT] = { "P", "dPdx", "dPdy", "dPdz", "I", "dIdx", "dIdy", "N", "Ng",
                                       "u", "dudx", "dudy", "v", "dvdx", "dvdy", "dPdu", "dPdv",
                                       "time", "dtime", "dPdtime", "Ps", "dPsdx", "dPsdy",
-                                      "surfacearea" };
+                                      "surfacearea", "$flipHandedness", "$backfacing" };
 
 int global_id_of(const std::string& n) {
     for (int i = 0; i < (int)G_COUNT; ++i)
@@ -184,7 +184,7 @@ const std::set<std::string>& deriv_propagating_ops() {
         "inversesqrt", "cbrt", "abs", "fabs", "mix", "clamp", "min", "max", "smoothstep", "select",
         "dot", "cross", "length", "normalize", "distance", "transform", "transformv", "transformn",
         "noise", "snoise", "pnoise", "psnoise", "spline", "splineinverse", "mod", "fmod", "luminance", "radians",
-        "transformc",
+        "transformc", "sincos", "arraycopy",
         "degrees", "erf", "erfc" };
     return s;
 }
@@ -686,6 +686,13 @@ struct Lowerer {
             }
             return true;
         };
+        if (n == "isconstant") {
+            // constfold.cpp:3030-3045: a constant here stays one; the other
+            // case is decided when the op is lowered, after all folding
+            if (!syms[op.args[1]].is_const) return false;
+            out[0] = 1u;
+            return true;
+        }
         CVal x, y, z;
         const bool ctor = n == "color" || n == "point" || n == "vector" || n == "normal";
         if (n == "assign" || (ctor && na == 2)) {
@@ -2142,19 +2149,27 @@ struct Lowerer {
             { "cosh", OP_COSH }, { "tanh", OP_TANH }, { "exp", OP_EXP }, { "exp2", OP_EXP2 },
             { "expm1", OP_EXPM1 }, { "log", OP_LOG }, { "log2", OP_LOG2 }, { "log10", OP_LOG10 },
             { "radians", OP_RADIANS }, { "degrees", OP_DEGREES }, { "isnan", OP_ISNAN },
-            { "isinf", OP_ISINF }, { "isfinite", OP_ISFINITE } };
+            { "isinf", OP_ISINF }, { "isfinite", OP_ISFINITE }, { "logb", OP_LOGB }, { "erf", OP_ERF },
+            { "erfc", OP_ERFC } };
         if (n == "abs" || n == "fabs") {
             emit(is_int(op.args[0]) ? OP_IABS : OP_ABS, { a(0), a(1) }, n);
             return true;
         }
+        // ops the reference's default build computes with OpenImageIO's fast_*
+        // functions (wide_optranscendental.cpp:34-66, wide_optrigonometric.cpp:16-47)
+        static const std::set<uint16_t> fast_ops = { OP_SIN, OP_COS, OP_TAN, OP_ASIN, OP_ACOS, OP_ATAN,
+                                                     OP_SINH, OP_COSH, OP_TANH, OP_EXP, OP_EXP2, OP_EXPM1,
+                                                     OP_LOG, OP_LOG2, OP_LOG10, OP_ERF, OP_ERFC, OP_CBRT };
+        const uint32_t fast = ss.opts.fast_math ? 1u : 0u;
         auto un = unary.find(n);
         if (un != unary.end()) {
             if (na < 2) return fail(n + " needs 2 args");
-            emit(un->second, { a(0), a(1) }, n);
+            emit(un->second, { a(0), a(1), fast_ops.count(un->second) ? fast : 0u }, n);
             return true;
         }
         if (n == "pow" || n == "atan2" || n == "fmod") {
-            emit(n == "pow" ? OP_POW : n == "atan2" ? OP_ATAN2 : OP_FMOD, { a(0), a(1), a(2) }, n);
+            emit(n == "pow" ? OP_POW : n == "atan2" ? OP_ATAN2 : OP_FMOD, { a(0), a(1), a(2), n == "fmod" ? 0u : fast },
+                 n);
             return true;
         }
         if (n == "min" || n == "max") {
@@ -2186,6 +2201,45 @@ struct Lowerer {
         }
         if (n == "aassign") {
             emit(OP_AASSIGN, { a(0), a(1), a(2), (uint32_t)syms[op.args[0]].type.elems() }, n);
+            return true;
+        }
+        if (n == "arraycopy") {  // batched_llvm_gen.cpp:2257-2264: an assignment
+            emit(OP_ASSIGN, { a(0), a(1), (uint32_t)std::min(syms[op.args[0]].type.elems(), syms[op.args[1]].type.elems()),
+                              (uint32_t)syms[op.args[0]].type.elems(), (uint32_t)syms[op.args[1]].type.elems() },
+                 n);
+            return true;
+        }
+        if (n == "sincos") { emit(OP_SINCOS, { a(0), a(1), a(2), ss.opts.fast_math ? 1u : 0u }, n); return true; }
+        if (n == "calculatenormal") { emit(OP_CALCNORMAL, { a(0), a(1) }, n); return true; }
+        if (n == "backfacing") { emit(OP_LOAD_GLOBAL, { a(0), (uint32_t)G_BACKFACING }, n); return true; }
+        if (n == "surfacearea") { emit(OP_LOAD_GLOBAL, { a(0), (uint32_t)G_SURFACEAREA }, n); return true; }
+        if (n == "isconstant") {
+            // what folding did not turn into 1 is not constant
+            // (batched_llvm_gen.cpp:8079-8092)
+            const int c = const_int(syms[op.args[1]].is_const ? 1 : 0);
+            syms[c].slot = (int)pool_add(syms[c]);
+            emit(OP_ASSIGN, { a(0), A(c), 1u, 1u, 1u }, n);
+            return true;
+        }
+        if (n == "raytype") {
+            // batched_llvm_gen.cpp:8520-8560: a constant name's bit is known
+            // here; a varying name is looked up in the raytypes list
+            const std::vector<std::string>& rt = ss.opts.raytypes;
+            std::vector<float> hashes;
+            if (is_string(op.args[1]) && syms[op.args[1]].is_const) {
+                const std::string nm = const_string(op.args[1]);
+                uint32_t bit = 0;
+                for (size_t i = 0; i < rt.size() && i < 32; ++i)
+                    if (rt[i] == nm) { bit = 1u << i; break; }
+                emit(OP_RAYTYPE, { a(0), kNoArg, bit, kNoArg, 0u }, n);
+                return true;
+            }
+            GSym t;
+            t.name = "$raytypes"; t.type.base = BT_STRING; t.type.arraylen = (int)std::max<size_t>(1, rt.size());
+            t.kind = SK_CONST; t.is_const = true; t.sval = rt;
+            const int ts = add_sym(t);
+            syms[ts].slot = (int)pool_add(syms[ts]);
+            emit(OP_RAYTYPE, { a(0), a(1), 0u, A(ts), (uint32_t)std::min<size_t>(rt.size(), 32) }, n);
             return true;
         }
         if (n == "arraylength") {
@@ -2424,6 +2478,7 @@ struct Lowerer {
             case OP_MDIV: case OP_TRANSPOSE: case OP_DETERMINANT: case OP_AREA: case OP_FILTERWIDTH:
             case OP_LUMINANCE: case OP_BLACKBODY: case OP_TEXTURE: case OP_SETMESSAGE: case OP_GETMESSAGE:
             case OP_TRANSFORMC: case OP_WAVELENGTH:
+            case OP_LOGB: case OP_ERF: case OP_ERFC: case OP_SINCOS: case OP_CALCNORMAL: case OP_RAYTYPE:
             case OP_ENVIRONMENT:
                 t |= 4u;
                 break;
@@ -2433,9 +2488,51 @@ struct Lowerer {
         return t;
     }
 
+    // isconnected(x) as RuntimeOptimizer::resolve_isconnected
+    // (src/liboslexec/runtimeoptimize.cpp:2476-2505), before any folding: 1
+    // when a connection feeds the parameter (or, with userdata_isconnected, it
+    // is lockgeom=0), plus 2 when a later layer reads it or it is a renderer
+    // output (ShadingSystemImpl::is_renderer_output, shadingsys.cpp:3832-3860)
+    bool is_renderer_output(int li, const std::string& param) const {
+        const std::string name2 = g.layers[(size_t)li].layername + "." + param;
+        for (const SymLoc& sl : g.symlocs)
+            if (sl.arena == ARENA_OUTPUTS && (sl.name == param || sl.name == name2)) return true;
+        for (const std::string& ro : g.renderer_outputs)
+            if (ro == param || ro == name2) return true;
+        return false;
+    }
+    void resolve_isconnected() {
+        for (LOp& op : lops) {
+            if (op.name != "isconnected" || op.args.size() < 2) continue;
+            const GSym& s = syms[op.args[1]];
+            int val = 0;
+            if (s.layer >= 0 && (s.kind == SK_PARAM || s.kind == SK_OPARAM)) {
+                const Layer& L = g.layers[(size_t)s.layer];
+                bool up = false, down = false;
+                for (const Connection& c : L.connections) up = up || c.dstparam == s.name;
+                if (!up && ss.opts.userdata_isconnected) {
+                    const int msi = L.master->find_symbol(s.name);
+                    bool lockgeom = msi >= 0 ? L.master->symbols[(size_t)msi].lockgeom : true;
+                    for (const InstanceParam& p : L.params)
+                        if (p.name == s.name) lockgeom = p.lockgeom;
+                    up = !lockgeom;
+                }
+                for (int lj = s.layer + 1; lj <= last_layer(); ++lj)
+                    for (const Connection& c : g.layers[(size_t)lj].connections)
+                        down = down || (c.srclayer == s.layer && c.srcparam == s.name);
+                if (s.kind == SK_OPARAM && is_renderer_output(s.layer, s.name)) down = true;
+                val = (up ? 1 : 0) + (down ? 2 : 0);
+            }
+            op.args = { op.args[0], const_int(val) };
+            op.name = "assign";
+            op.argrw = "wr";
+        }
+    }
+
     bool run(CompiledGroup& out) {
         if (g.layers.empty()) return fail("group has no layers");
         if (!build_lops()) return false;
+        resolve_isconnected();
         if (!prepare_messages()) return false;
         if (ss.opts.opt_constant_fold) fold_constants();
         if (ss.opts.opt_elide_useless_ops) eliminate_dead_ops();

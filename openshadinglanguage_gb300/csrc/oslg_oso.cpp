@@ -4,6 +4,7 @@
 // instruction.
 #include <cctype>
 #include <cstdlib>
+#include <set>
 #include <sstream>
 
 #include "oslg_host.h"
@@ -150,6 +151,35 @@ std::string unquote(const std::string& s) {
     return s;
 }
 
+// The instruction names a .oso may use: the reference's op descriptor
+// table (src/liboslexec/shadingsys.cpp:1300-1466, setup_op_descriptors).
+// An instruction outside it is refused while parsing, as
+// OSOReaderToMaster::instruction does (src/liboslexec/loadshader.cpp:500-510);
+// ops this executor cannot lower are refused later, when a group is lowered.
+bool known_instruction(const std::string& n) {
+    static const std::set<std::string> ops = {
+        "aassign", "abs", "acos", "add", "and", "area", "aref", "arraycopy", "arraylength", "asin",
+        "assign", "atan", "atan2", "backfacing", "bitand", "bitor", "blackbody", "break",
+        "calculatenormal", "cbrt", "ceil", "cellnoise", "clamp", "closure", "color", "compassign",
+        "compl", "compref", "concat", "continue", "cos", "cosh", "cross", "degrees", "determinant",
+        "dict_find", "dict_next", "dict_value", "distance", "div", "dot", "Dx", "Dy", "Dz", "dowhile",
+        "end", "endswith", "environment", "eq", "erf", "erfc", "error", "exit", "exp", "exp2", "expm1",
+        "fabs", "filterwidth", "floor", "fmod", "for", "format", "fprintf", "functioncall",
+        "functioncall_nr", "ge", "getattribute", "getchar", "getmatrix", "getmessage",
+        "gettextureinfo", "gt", "hash", "hashnoise", "if", "inversesqrt", "isconnected",
+        "isconstant", "isfinite", "isinf", "isnan", "le", "length", "log", "log10", "log2", "logb",
+        "lt", "luminance", "matrix", "max", "mxcompassign", "mxcompref", "min", "mix", "mod", "mul",
+        "neg", "neq", "noise", "nop", "normal", "normalize", "or", "pnoise", "point",
+        "pointcloud_search", "pointcloud_get", "pointcloud_write", "pow", "printf", "psnoise",
+        "radians", "raytype", "regex_match", "regex_search", "return", "round", "select",
+        "setmessage", "shl", "shr", "sign", "sin", "sincos", "sinh", "smoothstep", "snoise",
+        "spline", "splineinverse", "split", "sqrt", "startswith", "step", "stof", "stoi", "strlen",
+        "strtof", "strtoi", "sub", "substr", "surfacearea", "tan", "tanh", "texture", "texture3d",
+        "trace", "transform", "transformc", "transformn", "transformv", "transpose", "trunc",
+        "useparam", "vector", "warning", "wavelength_color", "while", "xor" };
+    return ops.count(n) != 0;
+}
+
 }  // namespace
 
 bool parse_oso(const std::string& text, ShaderMaster& m, std::string& err) {
@@ -236,6 +266,11 @@ bool parse_oso(const std::string& text, ShaderMaster& m, std::string& err) {
     // resolve ops
     for (size_t k = 0; k < pending_ops.size(); ++k) {
         const std::vector<std::string>& tok = pending_ops[k];
+        if (!known_instruction(tok[0])) {
+            err = "Parsing shader \"" + m.name + "\": instruction \"" + tok[0]
+                + "\" is not known. Maybe compiled with a too-new oslc?";
+            return false;
+        }
         OsoOp op;
         op.name = tok[0];
         op.line = pending_lines[k];

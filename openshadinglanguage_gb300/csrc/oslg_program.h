@@ -20,7 +20,7 @@
 namespace oslg {
 
 static const uint32_t kProgramMagic = 0x4f534c47u;  // "OSLG"
-static const uint32_t kProgramVersion = 6;
+static const uint32_t kProgramVersion = 7;
 
 // ---- operand words ----------------------------------------------------------
 // bits 0..19  slot offset (heap) or index (constant pool)
@@ -148,6 +148,12 @@ enum OpCode : uint16_t {
     OP_TRANSFORMC,   // a0=r (triple) a1=C (triple) a2=from space | to space << 8
                      // a3=colour system table (9 XYZ->RGB then 9 RGB->XYZ floats)
     OP_WAVELENGTH,   // a0=r (triple) a1=lambda (float) a2=table (9 XYZ->RGB then 81 x 3 CIE)
+    // more componentwise unary math (as OP_ABS..): logb has no derivatives
+    OP_LOGB, OP_ERF, OP_ERFC,
+    OP_SINCOS,       // a0=x a1=sine result a2=cosine result (float or triple)
+    OP_CALCNORMAL,   // a0=r (triple) a1=P (triple with derivatives); reads flipHandedness
+    OP_RAYTYPE,      // a0=r (int) a1=name (string) or kNoArg a2=the name's bit (when a1 is
+                     // kNoArg) a3=raytype name hashes (ints) a4=count: r = raytype & bit != 0
     OP_COUNT
 };
 
@@ -214,8 +220,13 @@ enum GlobalId : uint32_t {
     G_TIME, G_DTIME, G_DPDTIME,
     G_PS, G_DPSDX, G_DPSDY,
     G_SURFACEAREA,
+    G_FLIPHANDEDNESS, G_BACKFACING,  // int fields
     G_COUNT
 };
+#ifdef __CUDACC__
+__host__ __device__
+#endif
+inline bool global_is_int(uint32_t id) { return id == G_FLIPHANDEDNESS || id == G_BACKFACING; }
 
 struct Op {
     uint16_t code;

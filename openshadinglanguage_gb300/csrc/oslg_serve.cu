@@ -24,7 +24,7 @@ int64_t now_ns() {
 int field_components(int gid) {
     switch (gid) {
     case G_U: case G_DUDX: case G_DUDY: case G_V: case G_DVDX: case G_DVDY: case G_TIME: case G_DTIME:
-    case G_SURFACEAREA:
+    case G_SURFACEAREA: case G_FLIPHANDEDNESS: case G_BACKFACING:
         return 1;
     default: return 3;
     }

@@ -284,9 +284,10 @@ std::string spec_source(const CompiledGroup& cg, int min_blocks) {
     emit_body(o, v, "");
     o << "}  // namespace\n\n";
     // registers per thread are capped at 65536 / (256 * min_blocks); by
-    // default 64 for closure programs (latency-bound: more resident warps)
-    // and 85 otherwise (measured on the layered-closure and fBm workloads)
-    if (min_blocks <= 0) min_blocks = B.any ? 4 : 3;
+    // default 48 for closure programs (latency-bound: more resident warps;
+    // 0.279 ms against 0.297 ms at 64 on the layered-closure workload) and
+    // 85 otherwise (the fBm workload)
+    if (min_blocks <= 0) min_blocks = B.any ? 5 : 3;
     o << "extern \"C\" __global__ void __launch_bounds__(256, " << std::max(2, std::min(8, min_blocks)) << ") "
       << kKernelName
       << "(const __grid_constant__ oslg::dev::KArgs k, int pool_in_smem, int fill_unwritten) {\n";

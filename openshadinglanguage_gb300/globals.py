@@ -21,11 +21,18 @@ def make_globals(**fields):
     """make_globals(u=tensor, v=tensor, dudx=1/W, P=(x,y,z), N=tensor[3,N] ...)
 
     A field given as an array (1-D for floats, [3, N] planes for triples)
-    is per point; a float or 3-tuple is uniform.
+    is per point; a float or 3-tuple is uniform. flipHandedness and
+    backfacing take int32 arrays (or a uniform number); raytype is the
+    uniform int of raytype bits.
     """
     g = C.ShaderGlobalsC()
     keep = []
     for name, val in fields.items():
+        if name == "raytype":
+            g.raytype = int(val)
+            continue
+        if name in C.INT_GLOBAL_FIELDS and hasattr(val, "dtype") and str(val.dtype) not in ("int32", "torch.int32"):
+            raise ValueError("global '%s' takes int32 values" % name)
         if name not in C.GLOBAL_FIELDS:
             raise KeyError("unknown shader global '%s'" % name)
         f = getattr(g, name)

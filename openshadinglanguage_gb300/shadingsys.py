@@ -140,6 +140,9 @@ class ShadingSystem:
     def attribute(self, name, value):
         if isinstance(value, str):
             self._check(C.lib().oslg_attribute_string(self._h, name.encode(), value.encode()))
+        elif isinstance(value, (list, tuple)):
+            arr = (ctypes.c_char_p * max(1, len(value)))(*[str(v).encode() for v in value])
+            self._check(C.lib().oslg_attribute_strings(self._h, name.encode(), arr, len(value)))
         else:
             self._check(C.lib().oslg_attribute_int(self._h, name.encode(), int(value)))
 

@@ -29,6 +29,7 @@
 #include "../include/oslg.h"
 #include "../openshadinglanguage_gb300/csrc/oslg_program.h"
 #include "oracle_bsdf.h"
+#include "oracle_fastmath.h"
 #include "oracle_gabor.h"
 #include "oracle_shading.h"
 #include "oracle_simplex.h"
@@ -104,6 +105,17 @@ inline void putv(Point& P, uint32_t r, int c, float v) { putd(P, r, c, DF(v)); }
 inline float f_sin(float x) { return (float)std::sin((double)x); }
 inline float f_cos(float x) { return (float)std::cos((double)x); }
 const float kMin = FLT_MIN;
+// OpenImageIO fast_logb (fmath.h; OpenImageIO 2.5, the host branch the
+// reference's logb calls, llvm_ops.cpp:542-545): exponent of |x| clamped
+// to the normal float range
+inline float fast_logb(float x) {
+    x = std::fabs(x);
+    if (x < FLT_MIN) x = FLT_MIN;
+    if (x > FLT_MAX) x = FLT_MAX;
+    uint32_t bits;
+    std::memcpy(&bits, &x, 4);
+    return (float)((int)(bits >> 23) - 127);
+}
 // OIIO safe_log / safe_pow / safe_fmod
 inline float safe_log(float x) { return (float)std::log((double)(x < kMin ? kMin : x)); }
 inline float safe_log2(float x) { return (float)std::log2((double)(x < kMin ? kMin : x)); }
@@ -250,6 +262,49 @@ void op_cmp(Point& P, const uint32_t* a, int K) {
 }
 
 // unary math per component (dual.h:829-1260 derivative rules)
+// OpenImageIO fast_* forms with dual.h's fast_* derivative rules
+// (dual.h:836-1262); false when the op has none
+bool unary_fast(uint16_t code, const DF& X, DF& res) {
+    namespace F = oracle_fm;
+    const float v = X.v;
+    switch (code) {
+    case oslg::OP_SIN: { float s, c; F::sincosf_(v, s, c); res = dualfunc(X, s, c); return true; }
+    case oslg::OP_COS: { float s, c; F::sincosf_(v, s, c); res = dualfunc(X, c, -s); return true; }
+    case oslg::OP_TAN: { float cs = F::cosf_(v); res = dualfunc(X, F::tanf_(v), 1.0f / (cs * cs)); return true; }
+    case oslg::OP_ASIN:
+        res = dualfunc(X, F::asinf_(v), std::fabs(v) < 1.0f ? 1.0f / std::sqrt(1.0f - v * v) : 0.0f);
+        return true;
+    case oslg::OP_ACOS:
+        res = dualfunc(X, F::acosf_(v), std::fabs(v) < 1.0f ? -1.0f / std::sqrt(1.0f - v * v) : 0.0f);
+        return true;
+    case oslg::OP_ATAN: res = dualfunc(X, F::atanf_(v), 1.0f / (1.0f + v * v)); return true;
+    case oslg::OP_SINH: res = dualfunc(X, F::sinhf_(v), F::coshf_(v)); return true;
+    case oslg::OP_COSH: res = dualfunc(X, F::coshf_(v), F::sinhf_(v)); return true;
+    case oslg::OP_TANH: { float ch = F::coshf_(v); res = dualfunc(X, F::tanhf_(v), 1.0f / (ch * ch)); return true; }
+    case oslg::OP_EXP: { float f = F::expf_(v); res = dualfunc(X, f, f); return true; }
+    case oslg::OP_EXP2: { float f = F::exp2f_(v); res = dualfunc(X, f, f * 0.693147180559945309417f); return true; }
+    case oslg::OP_EXPM1: res = dualfunc(X, F::expm1f_(v), F::expf_(v)); return true;
+    case oslg::OP_LOG: res = dualfunc(X, F::logf_(v), v < kMin ? 0.0f : 1.0f / v); return true;
+    case oslg::OP_LOG2: {
+        float aln2 = v * 0.693147180559945309417f;
+        res = dualfunc(X, F::log2f_(v), aln2 < kMin ? 0.0f : 1.0f / aln2);
+        return true;
+    }
+    case oslg::OP_LOG10: {
+        float aln10 = v * 2.30258509299404568402f;
+        res = dualfunc(X, F::log10f_(v), aln10 < kMin ? 0.0f : 1.0f / aln10);
+        return true;
+    }
+    case oslg::OP_ERF: res = dualfunc(X, F::erff_(v), F::expf_(-v * v) * 1.12837916709551257390f); return true;
+    case oslg::OP_ERFC: res = dualfunc(X, F::erfcf_(v), F::expf_(-v * v) * -1.12837916709551257390f); return true;
+    case oslg::OP_CBRT:
+        if (v != 0.0f) { float f = F::cbrtf_(v); res = dualfunc(X, f, 1.0f / (3.0f * f * f)); }
+        else res = DF(0.0f);
+        return true;
+    default: return false;
+    }
+}
+
 void op_unary(Point& P, const uint32_t* a, uint16_t code) {
     uint32_t r = a[0], x = a[1];
     int nc = anc(r);
@@ -258,6 +313,7 @@ void op_unary(Point& P, const uint32_t* a, uint16_t code) {
         float v = X.v;
         DF res;
         bool has = ader(x);
+        if (!(a[2] == 1u && unary_fast(code, X, res)))
         switch (code) {
         case oslg::OP_NEG: res = -X; break;
         case oslg::OP_ABS: res = v >= 0.0f ? DF(std::fabs(v), X.dx, X.dy) : -X; break;
@@ -303,6 +359,13 @@ void op_unary(Point& P, const uint32_t* a, uint16_t code) {
         case oslg::OP_LOG: res = dualfunc(X, safe_log(v), v < kMin ? 0.0f : 1.0f / v); break;
         case oslg::OP_LOG2: res = dualfunc(X, safe_log2(v), v < kMin ? 0.0f : 1.0f / (v * 0.693147180559945309417f)); break;
         case oslg::OP_LOG10: res = dualfunc(X, safe_log10(v), v < kMin ? 0.0f : 1.0f / (v * 2.30258509299404568402f)); break;
+        case oslg::OP_LOGB: res = DF(fast_logb(v)); break;
+        case oslg::OP_ERF:  // dual.h:1170-1179
+            res = dualfunc(X, (float)std::erf((double)v), (float)std::exp((double)(-v * v)) * 1.12837916709551257390f);
+            break;
+        case oslg::OP_ERFC:  // dual.h:1190-1199
+            res = dualfunc(X, (float)std::erfc((double)v), -1.12837916709551257390f * (float)std::exp((double)(-v * v)));
+            break;
         case oslg::OP_RADIANS: res = X * (3.14159265358979323846f / 180.0f); break;
         case oslg::OP_DEGREES: res = X * (180.0f / 3.14159265358979323846f); break;
         default: res = X; break;
@@ -318,25 +381,26 @@ void op_binary(Point& P, const uint32_t* a, uint16_t code) {
     uint32_t r = a[0], x = a[1], y = a[2];
     int nc = anc(r);
     bool rd = ader(r);
+    const bool fast = a[3] == 1u;  // pow, atan2
     for (int c = 0; c < nc; ++c) {
         DF u = getd(P, x, c), v = getd(P, y, c);
         DF res;
         switch (code) {
         case oslg::OP_POW:
             if (rd && (ader(x) || ader(y))) {
-                // dual.h:1059-1067
-                float powuvm1 = safe_pow(u.v, v.v - 1.0f);
+                // dual.h:1059-1067, fast form 1072-1080
+                float powuvm1 = fast ? oracle_fm::safe_powf_(u.v, v.v - 1.0f) : safe_pow(u.v, v.v - 1.0f);
                 float powuv = powuvm1 * u.v;
-                float logu = u.v > 0.0f ? safe_log(u.v) : 0.0f;
+                float logu = u.v > 0.0f ? (fast ? oracle_fm::logf_(u.v) : safe_log(u.v)) : 0.0f;
                 float du = v.v * powuvm1, dv = logu * powuv;
                 res = DF(powuv, du * u.dx + dv * v.dx, du * u.dy + dv * v.dy);
             } else {
-                res = DF(safe_pow(u.v, v.v));
+                res = DF(fast ? oracle_fm::safe_powf_(u.v, v.v) : safe_pow(u.v, v.v));
             }
             break;
         case oslg::OP_ATAN2: {
-            // dual.h:1018-1023 (y = first operand)
-            float f = (float)std::atan2((double)u.v, (double)v.v);
+            // dual.h:1018-1023 (y = first operand), fast form 1025-1031
+            float f = fast ? oracle_fm::atan2f_(u.v, v.v) : (float)std::atan2((double)u.v, (double)v.v);
             float denom = (v.v == 0.0f && u.v == 0.0f) ? 0.0f : 1.0f / (v.v * v.v + u.v * u.v);
             float dfdy = -v.v * denom, dfdx = u.v * denom;
             res = DF(f, dfdy * u.dx + dfdx * v.dx, dfdy * u.dy + dfdx * v.dy);
@@ -550,6 +614,21 @@ void op_area(Point& P, const uint32_t* a) {
     V3 dx(getf(P, a[1], 0, 1), getf(P, a[1], 1, 1), getf(P, a[1], 2, 1));
     V3 dy(getf(P, a[1], 0, 2), getf(P, a[1], 1, 2), getf(P, a[1], 2, 2));
     putv(P, a[0], 0, v3_length(v3_cross(dx, dy)));
+}
+// sincos (llvm_ops.cpp:298-430): a0 = x, a1 = sine, a2 = cosine
+void op_sincos(Point& P, const uint32_t* a) {
+    const uint32_t x = a[0], rs = a[1], rc = a[2];
+    const int nc = anc(x);
+    for (int c = 0; c < nc; ++c) {
+        const float v = getf(P, x, c, 0), xdx = getf(P, x, c, 1), xdy = getf(P, x, c, 2);
+        float sv, cv;
+        if (a[3] == 1u) oracle_fm::sincosf_(v, sv, cv);
+        else { sv = f_sin(v); cv = f_cos(v); }
+        setf(P, rs, c, sv);
+        setf(P, rc, c, cv);
+        if (ader(rs)) { setf(P, rs, nc + c, cv * xdx); setf(P, rs, 2 * nc + c, cv * xdy); }
+        if (ader(rc)) { setf(P, rc, nc + c, -sv * xdx); setf(P, rc, 2 * nc + c, -sv * xdy); }
+    }
 }
 void op_filterwidth(Point& P, const uint32_t* a) {
     for (int c = 0; c < anc(a[1]); ++c) {
@@ -1202,10 +1281,27 @@ const oslg_field& gfield(const oslg_shaderglobals& G, int id) {
     return f[id];
 }
 float fld(const oslg_field& f, int c, int64_t pt) { return f.data ? f.data[c * f.plane_stride + pt] : f.value[c]; }
+bool gflag(const oslg_field& f, int64_t pt) {
+    return f.data ? reinterpret_cast<const int32_t*>(f.data)[pt] != 0 : f.value[0] != 0.0f;
+}
+// calculatenormal (llvm_ops.cpp:915-934): cross(dPdx, dPdy), operands
+// swapped under flipHandedness
+void op_calcnormal(Point& P, const uint32_t* a, const oslg_shaderglobals& G) {
+    V3 dx(getf(P, a[1], 0, 1), getf(P, a[1], 1, 1), getf(P, a[1], 2, 1));
+    V3 dy(getf(P, a[1], 0, 2), getf(P, a[1], 1, 2), getf(P, a[1], 2, 2));
+    V3 n = gflag(G.flipHandedness, P.pt) ? v3_cross(dy, dx) : v3_cross(dx, dy);
+    putv(P, a[0], 0, n.x);
+    putv(P, a[0], 1, n.y);
+    putv(P, a[0], 2, n.z);
+}
 
 void op_load_global(Point& P, const uint32_t* a, const oslg_shaderglobals& G) {
     uint32_t r = a[0];
     int id = (int)a[1];
+    if (oslg::global_is_int((uint32_t)id)) {  // flipHandedness, backfacing: 0 or 1
+        setw(P, r, 0, gflag(gfield(G, id), P.pt) ? 1u : 0u);
+        return;
+    }
     int nc = anc(r);
     for (int c = 0; c < nc; ++c) setf(P, r, c, fld(gfield(G, id), c, P.pt));
     if (ader(r)) {
@@ -1613,9 +1709,22 @@ struct Runner {
             case oslg::OP_SIN: case oslg::OP_COS: case oslg::OP_TAN: case oslg::OP_ASIN: case oslg::OP_ACOS:
             case oslg::OP_ATAN: case oslg::OP_SINH: case oslg::OP_COSH: case oslg::OP_TANH: case oslg::OP_EXP:
             case oslg::OP_EXP2: case oslg::OP_EXPM1: case oslg::OP_LOG: case oslg::OP_LOG2: case oslg::OP_LOG10:
-            case oslg::OP_RADIANS: case oslg::OP_DEGREES:
+            case oslg::OP_RADIANS: case oslg::OP_DEGREES: case oslg::OP_LOGB: case oslg::OP_ERF: case oslg::OP_ERFC:
                 op_unary(P, a, op.code);
                 break;
+            case oslg::OP_SINCOS: op_sincos(P, a); break;
+            case oslg::OP_CALCNORMAL: op_calcnormal(P, a, G); break;
+            case oslg::OP_RAYTYPE: {  // batched_llvm_gen.cpp:8520-8560, shadingsys.cpp:3823-3829
+                uint32_t bit = a[2];
+                if (a[1] != oslg::kNoArg) {
+                    const uint32_t h = word(P, a[1], 0);
+                    bit = 0;
+                    for (uint32_t i = 0; i < a[4]; ++i)
+                        if (word(P, a[3], (int)i) == h) { bit = 1u << i; break; }
+                }
+                setw(P, a[0], 0, ((uint32_t)G.raytype & bit) != 0u ? 1u : 0u);
+                break;
+            }
             case oslg::OP_ISNAN: setw(P, a[0], 0, std::isnan(getf(P, a[1], 0, 0)) ? 1u : 0u); break;
             case oslg::OP_ISINF: setw(P, a[0], 0, std::isinf(getf(P, a[1], 0, 0)) ? 1u : 0u); break;
             case oslg::OP_ISFINITE: setw(P, a[0], 0, std::isfinite(getf(P, a[1], 0, 0)) ? 1u : 0u); break;

@@ -213,6 +213,13 @@ TEXTS = {
     "transformc_out.txt": "testsuite/transformc/ref/out.txt",
     "colorspace_out.txt": "testsuite/colorspace/ref/out.txt",
     "color_out.txt": "testsuite/color/ref/out.txt",
+    "raytype_out.txt": "testsuite/raytype/ref/out.txt",
+    "isconnected_out.txt": "testsuite/isconnected/ref/out.txt",
+    "isconstant_out.txt": "testsuite/isconstant/ref/out.txt",
+    "exponential_out.txt": "testsuite/exponential/ref/out.txt",
+    "hyperb_out.txt": "testsuite/hyperb/ref/out.txt",
+    "unknown_instruction_out.txt": "testsuite/unknown-instruction/ref/out.txt",
+    "unknown_instruction.oso": "testsuite/unknown-instruction/test.oso",
 }
 
 
