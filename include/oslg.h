@@ -299,6 +299,17 @@ int oslg_group_program(oslg_system* sys, oslg_group* group, void* buf, size_t ca
 int oslg_execute_batch(oslg_system* sys, oslg_group* group, int64_t npoints,
                        const oslg_shaderglobals* globals, void* userdata_base,
                        void* output_base, void* stream);
+/* BatchedExecutor<W>::execute with its wide_shadeindex (oslexec.h:1000-1004):
+ * point i reads its globals from element i of the SoA fields, and its
+ * userdata and output records at base + shadeindex[i] * stride
+ * (batched_llvm_instance.cpp:1219-1229), so a renderer that shades sorted or
+ * compacted hits scatters the results back to their pixels. `shadeindex`
+ * is a device array of npoints int32; every index must address a record
+ * inside both arenas, and two points with the same index write the same
+ * record in an unspecified order. */
+int oslg_execute_batch_indexed(oslg_system* sys, oslg_group* group, int64_t npoints,
+                               const oslg_shaderglobals* globals, const int32_t* shadeindex, void* userdata_base,
+                               void* output_base, void* stream);
 
 /* Same as oslg_execute_batch, then waits for the stream and reports any
  * status bit the kernel raised (closure arena overflow, bad opcode, array

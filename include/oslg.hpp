@@ -9,6 +9,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cstring>
 #include <string>
 #include <vector>
 
@@ -117,10 +118,60 @@ public:
         return ok(oslg_renderer_matrix(sys_, name.c_str(), m16));
     }
 
+    /* ShadingContext (oslexec.h:819-824 get_context / release_context): the
+     * per-thread scratch of a caller. Here it holds the host staging of the
+     * records a shadeindex scatters. */
+    class ShadingContext {
+        friend class ShadingSystem;
+        std::vector<unsigned char> userdata, outputs;
+    };
+    ShadingContext* get_context() { return new ShadingContext(); }
+    void release_context(ShadingContext* ctx) { delete ctx; }
+
     /* BatchedExecutor<W> (oslexec.h:990-1030) */
     template <int W> class BatchedExecutor {
     public:
         explicit BatchedExecutor(ShadingSystem& ss) : ss_(ss) {}
+        /* The reference's signature (oslexec.h:1000-1004): lane i reads its
+         * userdata from, and writes its outputs to, record wide_shadeindex[i]
+         * of the arenas (batched_llvm_instance.cpp:1219-1229). */
+        bool execute(ShadingContext& ctx, ShaderGroupRef group, int batch_size, const Block<int, W>& wide_shadeindex,
+                     BatchedShaderGlobals<W>& bsg, void* userdata_base_ptr, void* output_base_ptr, bool run = true) {
+            if (batch_size < 0 || batch_size > W) return ss_.fail("batch_size must be in [0, W]");
+            int64_t out_stride = 0, ud_stride = 0;
+            if (!ss_.ok(oslg_group_record_strides(ss_.sys_, group, &out_stride, &ud_stride))) return false;
+            if (!run || batch_size == 0) return true;
+            for (int i = 0; i < batch_size; ++i)
+                if (wide_shadeindex.data[i] < 0) return ss_.fail("shadeindex must be >= 0");
+            // gather the lanes' records, shade them contiguously, scatter back
+            ctx.userdata.resize((size_t)batch_size * (size_t)ud_stride);
+            ctx.outputs.resize((size_t)batch_size * (size_t)out_stride);
+            unsigned char* ud = static_cast<unsigned char*>(userdata_base_ptr);
+            unsigned char* out = static_cast<unsigned char*>(output_base_ptr);
+            for (int i = 0; i < batch_size; ++i) {
+                const size_t rec = (size_t)wide_shadeindex.data[i];
+                if (ud_stride > 0)
+                    std::memcpy(ctx.userdata.data() + i * ud_stride, ud + rec * ud_stride, (size_t)ud_stride);
+                if (out_stride > 0)
+                    std::memcpy(ctx.outputs.data() + i * out_stride, out + rec * out_stride, (size_t)out_stride);
+            }
+            oslg_shaderglobals sg = view(bsg);
+            if (!ss_.ok(oslg_execute_batch_host(ss_.sys_, group, batch_size, &sg,
+                                                ud_stride > 0 ? ctx.userdata.data() : nullptr, ud_stride,
+                                                out_stride > 0 ? ctx.outputs.data() : nullptr, out_stride,
+                                                OSLG_HOST_PRESERVE_OUTPUTS)))
+                return false;
+            for (int i = 0; i < batch_size && out_stride > 0; ++i)
+                std::memcpy(out + (size_t)wide_shadeindex.data[i] * out_stride, ctx.outputs.data() + i * out_stride,
+                            (size_t)out_stride);
+            return true;
+        }
+        /* N device points whose records are d_shadeindex[i] (device int32). */
+        bool execute(ShaderGroupRef group, int64_t npoints, const oslg_shaderglobals& device_globals,
+                     const int32_t* d_shadeindex, void* d_userdata, void* d_outputs, void* stream) {
+            return ss_.ok(oslg_execute_batch_indexed(ss_.sys_, group, npoints, &device_globals, d_shadeindex,
+                                                     d_userdata, d_outputs, stream));
+        }
         /* Shade lanes [0, batch_size) of a W-lane batch: inputs from the
          * batch's varying blocks, outputs and userdata in the arenas the
          * group's symlocs address. Output bytes the group does not write

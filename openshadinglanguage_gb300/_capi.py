@@ -126,6 +126,9 @@ _EXPORTS = {
     "oslg_execute_batch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                                           ctypes.POINTER(ShaderGlobalsC), ctypes.c_void_p, ctypes.c_void_p,
                                           ctypes.c_void_p]),
+    "oslg_execute_batch_indexed": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                                  ctypes.POINTER(ShaderGlobalsC), ctypes.c_void_p, ctypes.c_void_p,
+                                                  ctypes.c_void_p, ctypes.c_void_p]),
     "oslg_execute_batch_sync": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                                                ctypes.POINTER(ShaderGlobalsC), ctypes.c_void_p, ctypes.c_void_p,
                                                ctypes.c_void_p]),

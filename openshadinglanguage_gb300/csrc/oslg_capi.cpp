@@ -508,8 +508,9 @@ int oslg_group_program(oslg_system* sys, oslg_group* group, void* buf, size_t ca
     });
 }
 
-int oslg_execute_batch(oslg_system* sys, oslg_group* group, int64_t npoints, const oslg_shaderglobals* globals,
-                       void* userdata_base, void* output_base, void* stream) {
+namespace {
+int execute_batch_impl(oslg_system* sys, oslg_group* group, int64_t npoints, const oslg_shaderglobals* globals,
+                       const int32_t* shadeindex, void* userdata_base, void* output_base, void* stream) {
     if (!sys || !group || !globals || npoints < 0) return OSLG_ERR_ARG;
     return guarded(sys, [&]() {
         int rc = ensure_compiled(sys, group, true);
@@ -518,13 +519,26 @@ int oslg_execute_batch(oslg_system* sys, oslg_group* group, int64_t npoints, con
         const CompiledGroup& cg = *group->g.compiled;
         if (cg.spec)
             rc = spec_launch(sys->dev, *cg.spec, cg, npoints, *globals, userdata_base, output_base, stream, &err,
-                             sys->jit_block, sys->jit_pool_smem);
+                             sys->jit_block, sys->jit_pool_smem, false, shadeindex);
         else
             rc = device_execute(sys->dev, cg.header, cg.d_blob, npoints, *globals, userdata_base, output_base,
-                                stream, sys->launch, &err);
+                                stream, sys->launch, &err, shadeindex);
         if (rc != OSLG_OK) return fail(sys, rc, err);
         return OSLG_OK;
     });
+}
+}  // namespace
+
+int oslg_execute_batch(oslg_system* sys, oslg_group* group, int64_t npoints, const oslg_shaderglobals* globals,
+                       void* userdata_base, void* output_base, void* stream) {
+    return execute_batch_impl(sys, group, npoints, globals, nullptr, userdata_base, output_base, stream);
+}
+
+int oslg_execute_batch_indexed(oslg_system* sys, oslg_group* group, int64_t npoints,
+                               const oslg_shaderglobals* globals, const int32_t* shadeindex, void* userdata_base,
+                               void* output_base, void* stream) {
+    if (!shadeindex && npoints > 0) return OSLG_ERR_ARG;
+    return execute_batch_impl(sys, group, npoints, globals, shadeindex, userdata_base, output_base, stream);
 }
 
 // ---- textures ---------------------------------------------------------------------
@@ -586,6 +600,22 @@ int oslg_texture_create(oslg_system* sys, const char* name, int width, int heigh
             sys->ss.texture_ids[name] = id;
         }
         sys->textures_dirty = true;
+        TextureInfo info;
+        info.width = width;
+        info.height = height;
+        info.nchannels = nchannels;
+        info.constant = true;
+        const size_t ntex = (size_t)width * height;
+        for (int c = 0; c < nchannels; ++c) {
+            double sum = 0.0;
+            for (size_t i = 0; i < ntex; ++i) {
+                const float v = texels[i * nchannels + c];
+                sum += v;
+                info.constant = info.constant && v == texels[c];
+            }
+            info.average.push_back((float)(sum / (double)ntex));
+        }
+        sys->ss.texture_info[name] = info;
         if (index) *index = id;
         return OSLG_OK;
     });

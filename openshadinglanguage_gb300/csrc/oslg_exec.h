@@ -23,6 +23,9 @@ struct KArgs {
     oslg_shaderglobals G;
     const TexDesc* textures = nullptr;  // the system's registered textures
     int32_t ntextures = 0;
+    // record of point i in the userdata and output arenas: shadeindex[i]
+    // (BatchedExecutor::execute's wide_shadeindex); null: i
+    const int32_t* shadeindex = nullptr;
 };
 
 // One group's request inside a persistent batch launch.
@@ -101,7 +104,7 @@ void device_free(void* p);
 // Enqueue one plain per-group launch over [0, npoints).
 int device_execute(DeviceState& ds, const ProgramHeader& hdr, const void* d_blob, int64_t npoints,
                    const oslg_shaderglobals& G, void* userdata, void* outputs, void* stream,
-                   const LaunchConfig& cfg, std::string* err);
+                   const LaunchConfig& cfg, std::string* err, const int32_t* shadeindex = nullptr);
 
 // Read-and-clear the device status word (synchronises the stream).
 int device_read_status(DeviceState& ds, void* stream, uint32_t* bits, std::string* err);

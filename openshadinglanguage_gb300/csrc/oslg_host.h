@@ -205,11 +205,20 @@ struct SystemOptions {
     int points_per_thread = 1;
 };
 
+// What gettextureinfo reports about a registered texture (the queries of
+// RendererServices::get_texture_info over OpenImageIO's image info)
+struct TextureInfo {
+    int width = 0, height = 0, nchannels = 0;
+    std::vector<float> average;  // per channel, over the base level
+    bool constant = false;       // every texel the same (average == the texel)
+};
+
 class ShadingSystem {
 public:
     std::map<std::string, std::shared_ptr<ShaderMaster>> masters;
     std::map<std::string, int> closure_ids;  // registered closure name -> id
     std::map<std::string, int> texture_ids;  // registered texture name -> index
+    std::map<std::string, TextureInfo> texture_info;
     std::map<std::pair<std::string, std::string>, RendererAttribute> attributes;  // (object, name)
     std::map<std::string, std::array<float, 16>> named_matrices;  // space -> space-to-common matrix
     SystemOptions opts;

@@ -69,6 +69,7 @@ struct Lane {
     int hs;      // heap stride (points per CTA tile)
     int li;      // lane index within the tile
     int64_t pt;  // global point index
+    const int32_t* si = nullptr;  // arena record of each point (null: the point index)
 #ifdef OSLG_SPEC
     // A specialized kernel keeps symbol slots in a thread-local array (hs 1,
     // li 0, constant offsets: registers) and the closure node pools, which
@@ -93,6 +94,18 @@ __device__ __forceinline__ void ostore32(void* p, uint32_t w) {
 __device__ __forceinline__ void ostore32(void* p, uint32_t w) { *reinterpret_cast<uint32_t*>(p) = w; }
 #endif
 __device__ __forceinline__ void ostoref(void* p, float v) { ostore32(p, __float_as_uint(v)); }
+
+// The point's record in the userdata and output arenas: the caller's
+// shadeindex when given (base + shadeindex * stride, as
+// batched_llvm_instance.cpp:1219-1229 addresses them), else the point. A
+// kernel that stages its output records in shared memory writes them by
+// point and scatters them by shadeindex when it copies the tile out.
+__device__ __forceinline__ int64_t urec(const Lane& L) { return L.si ? (int64_t)__ldg(L.si + L.pt) : L.pt; }
+#ifdef OSLG_STAGE_STRIDE
+__device__ __forceinline__ int64_t orec(const Lane& L) { return L.pt; }
+#else
+__device__ __forceinline__ int64_t orec(const Lane& L) { return urec(L); }
+#endif
 
 __device__ __forceinline__ uint32_t aoff(uint32_t a) { return a & kArgOffsetMask; }
 __device__ __forceinline__ bool aconst(uint32_t a) { return (a & kArgConst) != 0; }
@@ -1681,7 +1694,7 @@ static __device__ void h_calcnormal(const Lane& L, const uint32_t* a, const oslg
 static __device__ void h_load_userdata(const Lane& L, const uint32_t* a, char* base) {
     uint32_t r = a[0];
     int nc = anc(r);
-    const char* p = base + (int64_t)a[1] + L.pt * (int64_t)(int32_t)a[2];
+    const char* p = base + (int64_t)a[1] + urec(L) * (int64_t)(int32_t)a[2];
     const bool src_d = (a[3] & 2u) != 0u;
     const uint32_t* q = reinterpret_cast<const uint32_t*>(p);
     for (int i = 0; i < nc; ++i) stw(L, r, i, q[i]);
@@ -1695,7 +1708,7 @@ static __device__ void h_store_output(const Lane& L, const uint32_t* a, char* ba
     uint32_t flags = a[3];
     int elems = (int)a[4];
     if (elems < 1) elems = 1;
-    char* p = base + (int64_t)a[1] + L.pt * (int64_t)(int32_t)a[2];
+    char* p = base + (int64_t)a[1] + orec(L) * (int64_t)(int32_t)a[2];
     int total = nc * elems;
     int nd = (flags & 1u) ? 3 : 1;
     OSLG_SPEC_UNROLL
@@ -1998,7 +2011,7 @@ __device__ void closure_walk(const Lane& L, const ClosurePools& P, uint32_t root
 // Output record per point: [count][per component: id, w.rgb, params x12]
 static __device__ void h_store_closure(const Lane& L, const uint32_t* a, char* base, const ClosurePools& P, uint32_t* st) {
     uint32_t root = ldw(L, a[0], 0), maxc = a[3];
-    uint32_t* o = reinterpret_cast<uint32_t*>(base + (int64_t)a[1] + L.pt * (int64_t)(int32_t)a[2]);
+    uint32_t* o = reinterpret_cast<uint32_t*>(base + (int64_t)a[1] + orec(L) * (int64_t)(int32_t)a[2]);
     uint32_t n = 0;
     closure_walk(L, P, root, st, [&](int id, const float* cw, uint32_t params) {
         if (n >= maxc) return;
@@ -2318,7 +2331,7 @@ static __device__ void h_bsdf_eval(const Lane& L, const uint32_t* a, char* base,
     const float one[3] = { 1.0f, 1.0f, 1.0f };
     lobes_prepare(L, B, wo, one, false);
     const BsdfSample r = lobes_eval(L, B, wo, wi);
-    float* o = reinterpret_cast<float*>(base + (int64_t)a[1] + L.pt * (int64_t)(int32_t)a[2]);
+    float* o = reinterpret_cast<float*>(base + (int64_t)a[1] + orec(L) * (int64_t)(int32_t)a[2]);
     ostoref(o + 0, r.w[0]);
     ostoref(o + 1, r.w[1]);
     ostoref(o + 2, r.w[2]);
@@ -2333,13 +2346,13 @@ static __device__ void h_bsdf_sample(const Lane& L, const uint32_t* a, char* bas
                                      const ClosurePools& P, uint32_t* st) {
     const uint32_t root = ldw(L, a[0], 0);
     const V3 wo = v3(-ldf(L, a[3], 0, 0), -ldf(L, a[3], 1, 0), -ldf(L, a[3], 2, 0));
-    const float* in = reinterpret_cast<const float*>(ud + (int64_t)a[5] + L.pt * (int64_t)(int32_t)a[6]);
+    const float* in = reinterpret_cast<const float*>(ud + (int64_t)a[5] + urec(L) * (int64_t)(int32_t)a[6]);
     Lobes B;
     lobes_build(L, P, root, a[4], st, B, in[7], in[8] != 0.0f, wo);
     const float pw[3] = { in[3], in[4], in[5] };
     lobes_prepare(L, B, wo, pw, in[6] != 0.0f);
     const BsdfSample r = lobes_sample(L, B, wo, in[0], in[1], in[2]);
-    float* o = reinterpret_cast<float*>(base + (int64_t)a[1] + L.pt * (int64_t)(int32_t)a[2]);
+    float* o = reinterpret_cast<float*>(base + (int64_t)a[1] + orec(L) * (int64_t)(int32_t)a[2]);
     const float vals[11] = { r.wi.x, r.wi.y, r.wi.z, r.w[0], r.w[1], r.w[2], r.pdf, B.Le[0], B.Le[1], B.Le[2],
                              r.roughness };
 #pragma unroll
@@ -2411,7 +2424,7 @@ __device__ __forceinline__ void lobes_collect_static(const Lane& L, const Op* ta
 // records as h_store_closure writes them
 static __device__ void h_cl_store(const Lane& L, const uint32_t* a, const Op* tab, char* base) {
     const uint32_t maxc = a[3];
-    uint32_t* o = reinterpret_cast<uint32_t*>(base + (int64_t)a[1] + L.pt * (int64_t)(int32_t)a[2]);
+    uint32_t* o = reinterpret_cast<uint32_t*>(base + (int64_t)a[1] + orec(L) * (int64_t)(int32_t)a[2]);
     uint32_t n = 0;
     closure_walk_static(L, tab, a[0], [&](int id, const float* cw, uint32_t params) {
         if (n >= maxc) return;
@@ -2432,7 +2445,7 @@ static __device__ void h_cl_bsdf_eval(const Lane& L, const uint32_t* a, const Op
     const float one[3] = { 1.0f, 1.0f, 1.0f };
     lobes_prepare<SymNodes>(L, B, wo, one, false);
     const BsdfSample r = lobes_eval<SymNodes>(L, B, wo, wi);
-    float* o = reinterpret_cast<float*>(base + (int64_t)a[1] + L.pt * (int64_t)(int32_t)a[2]);
+    float* o = reinterpret_cast<float*>(base + (int64_t)a[1] + orec(L) * (int64_t)(int32_t)a[2]);
     ostoref(o + 0, r.w[0]);
     ostoref(o + 1, r.w[1]);
     ostoref(o + 2, r.w[2]);
@@ -2441,13 +2454,13 @@ static __device__ void h_cl_bsdf_eval(const Lane& L, const uint32_t* a, const Op
 // as h_bsdf_sample
 static __device__ void h_cl_bsdf_sample(const Lane& L, const uint32_t* a, const Op* tab, char* base, const char* ud) {
     const V3 wo = v3(-ldf(L, a[3], 0, 0), -ldf(L, a[3], 1, 0), -ldf(L, a[3], 2, 0));
-    const float* in = reinterpret_cast<const float*>(ud + (int64_t)a[5] + L.pt * (int64_t)(int32_t)a[6]);
+    const float* in = reinterpret_cast<const float*>(ud + (int64_t)a[5] + urec(L) * (int64_t)(int32_t)a[6]);
     Lobes B;
     lobes_collect_static(L, tab, a[0], a[4], B, in[7], in[8] != 0.0f);
     const float pw[3] = { in[3], in[4], in[5] };
     lobes_prepare<SymNodes>(L, B, wo, pw, in[6] != 0.0f);
     const BsdfSample r = lobes_sample<SymNodes>(L, B, wo, in[0], in[1], in[2]);
-    float* o = reinterpret_cast<float*>(base + (int64_t)a[1] + L.pt * (int64_t)(int32_t)a[2]);
+    float* o = reinterpret_cast<float*>(base + (int64_t)a[1] + orec(L) * (int64_t)(int32_t)a[2]);
     const float vals[11] = { r.wi.x, r.wi.y, r.wi.z, r.w[0], r.w[1], r.w[2], r.pdf, B.Le[0], B.Le[1], B.Le[2],
                              r.roughness };
 #pragma unroll
@@ -3240,6 +3253,7 @@ __global__ void __launch_bounds__(256, 2) interp_kernel(const __grid_constant__ 
     L.pool = spool;
     L.hs = blockDim.x;
     L.li = threadIdx.x;
+    L.si = k.shadeindex;
     L.heap = SMEM ? sheap : (k.gheap + (size_t)blockIdx.x * (size_t)slots * blockDim.x);
 
     const int64_t ntiles = (k.npoints + blockDim.x - 1) / blockDim.x;

@@ -429,7 +429,7 @@ struct Lowerer {
         // getmessage (result, name, dest, state, store)
         if (op.name == "setmessage") return i == 2 || i == 3;
         if (op.name == "getmessage") return i == 0 || i == 2 || i == 3;
-        if (op.name == "getattribute") return i == 0 || i == (int)op.args.size() - 1;
+        if (op.name == "getattribute" || op.name == "gettextureinfo") return i == 0 || i == (int)op.args.size() - 1;
         if (op.name == "getmatrix") return i == 0 || i == 3;
         if (!op.argrw.empty() && i < (int)op.argrw.size())
             return op.argrw[i] == 'w' || op.argrw[i] == 'W';
@@ -1659,6 +1659,76 @@ struct Lowerer {
     // registered with oslg_texture_create. Options: wrap/swrap/twrap
     // (black, clamp, periodic, mirror; OIIO's default is black), width,
     // firstchannel.
+    // gettextureinfo(filename, [s, t,] dataname, data) over the registered
+    // textures (RendererServices::get_texture_info, rendservices.cpp:429-470,
+    // answering from OpenImageIO's image info): the answer is known
+    // when the group is lowered, so it becomes constants. A query whose data
+    // has the wrong type, an unknown name, or a texture that is not
+    // registered returns 0 and leaves data untouched, except "exists",
+    // which always succeeds.
+    bool lower_gettextureinfo(const LOp& op) {
+        const size_t na = op.args.size();
+        if (na != 4 && na != 6) return fail("gettextureinfo takes (filename, [s, t,] dataname, data)");
+        const int fsym = op.args[1], nsym = op.args[na - 2], dsym = op.args[na - 1];
+        if (!is_string(fsym) || !syms[fsym].is_const || !is_string(nsym) || !syms[nsym].is_const)
+            return fail("gettextureinfo: the file and data names must be constant strings");
+        const std::string file = const_string(fsym), what = const_string(nsym);
+        const TypeSpec dt = syms[dsym].type;
+        auto it = ss.texture_info.find(file);
+        const TextureInfo* ti = it == ss.texture_info.end() ? nullptr : &it->second;
+        std::vector<float> vals;
+        std::vector<std::string> strs;
+        bool ok = false;
+        const bool is_int_arr = dt.base == BT_INT && dt.arraylen > 0;
+        if (what == "exists" && dt.base == BT_INT && !dt.is_array()) {
+            vals = { ti ? 1.0f : 0.0f };
+            ok = true;
+        } else if (ti) {
+            const int w = ti->width, h = ti->height, nc = ti->nchannels;
+            if (what == "resolution" && is_int_arr && (dt.arraylen == 2 || dt.arraylen == 3)) {
+                vals = { (float)w, (float)h };
+                if (dt.arraylen == 3) vals.push_back(1.0f);
+                ok = true;
+            } else if (what == "channels" && dt.base == BT_INT && !dt.is_array()) {
+                vals = { (float)nc };
+                ok = true;
+            } else if ((what == "texturetype" || what == "textureformat") && dt.base == BT_STRING && !dt.is_array()) {
+                strs = { "Plain Texture" };
+                ok = true;
+            } else if ((what == "datawindow" || what == "displaywindow") && is_int_arr
+                       && (dt.arraylen == 4 || dt.arraylen == 6)) {
+                vals = dt.arraylen == 4 ? std::vector<float>{ 0.0f, 0.0f, (float)(w - 1), (float)(h - 1) }
+                                        : std::vector<float>{ 0.0f, 0.0f, 0.0f, (float)(w - 1), (float)(h - 1), 0.0f };
+                ok = true;
+            } else if ((what == "averagecolor" || (what == "constantcolor" && ti->constant)) && dt.base == BT_TRIPLE
+                       && !dt.is_array()) {
+                for (int c = 0; c < 3; ++c) vals.push_back(ti->average[(size_t)(nc >= 3 ? c : 0)]);
+                ok = true;
+            } else if ((what == "averagealpha" || (what == "constantalpha" && ti->constant)) && dt.base == BT_FLOAT
+                       && !dt.is_array() && (nc == 4 || nc == 2)) {
+                vals = { ti->average[(size_t)nc - 1] };
+                ok = true;
+            }
+        }
+        if (ok) {
+            GSym c;
+            c.name = "$texinfo";
+            c.type = dt;
+            c.kind = SK_CONST;
+            c.is_const = true;
+            c.cval = vals;
+            c.sval = strs;
+            const int cs = add_sym(c);
+            syms[cs].slot = (int)pool_add(syms[cs]);
+            const uint32_t el = (uint32_t)dt.elems();
+            emit(OP_ASSIGN, { A(dsym), A(cs), el, el, el }, "gettextureinfo");
+        }
+        const int rc = const_int(ok ? 1 : 0);
+        syms[rc].slot = (int)pool_add(syms[rc]);
+        emit(OP_ASSIGN, { A(op.args[0]), A(rc), 1u, 1u, 1u }, "gettextureinfo");
+        return true;
+    }
+
     bool lower_texture(const LOp& op) {
         const size_t na = op.args.size();
         if (na < 4) return fail("texture needs a result, a file name and s, t");
@@ -2411,6 +2481,7 @@ struct Lowerer {
             emit(OP_BLACKBODY, { a(0), a(1), A(tb), (uint32_t)((t.size() - 9 - 243) / 3) }, n);
             return true;
         }
+        if (n == "gettextureinfo") return lower_gettextureinfo(op);
         if (n == "texture") return lower_texture(op);
         if (n == "environment") return lower_environment(op);
         if (n == "getattribute") return lower_getattribute(op);

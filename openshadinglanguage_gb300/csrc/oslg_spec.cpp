@@ -301,6 +301,7 @@ std::string spec_source(const CompiledGroup& cg, int min_blocks) {
     o << "    R.textures = k.textures;\n    R.ntextures = k.ntextures;\n";
     o << "    float hreg[" << std::max(1u, sym) << "];\n";
     o << "    Lane L;\n    L.heap = hreg;\n    L.pool = kPool;\n    L.hs = 1;\n    L.li = 0;\n    L.pt = 0;\n";
+    o << "    L.si = k.shadeindex;\n";
     // dynamic shared memory: [staged records | written flags] then the closure pools
     o << "    const size_t stage_bytes = " << (stage ? "(size_t)blockDim.x * " + std::to_string(stage) + "u * 5u / 4u"
                                                     : std::string("0")) << ";\n";
@@ -325,9 +326,19 @@ std::string spec_source(const CompiledGroup& cg, int min_blocks) {
              "blockDim.x : (int64_t)blockDim.x;\n";
         o << "        uint32_t* gout = reinterpret_cast<uint32_t*>(k.outputs + tile * blockDim.x * (int64_t)rec);\n";
         o << "        const uint32_t* sw = reinterpret_cast<const uint32_t*>(smem);\n";
-        o << "        for (int64_t w = threadIdx.x; w < npt * (int64_t)(rec / 4u); w += blockDim.x)\n";
-        o << "            if (flags[w]) gout[w] = sw[w];\n";
-        o << "            else if (fill_unwritten) gout[w] = 0u;\n";
+        o << "        if (!k.shadeindex) {\n";
+        o << "            for (int64_t w = threadIdx.x; w < npt * (int64_t)(rec / 4u); w += blockDim.x)\n";
+        o << "                if (flags[w]) gout[w] = sw[w];\n";
+        o << "                else if (fill_unwritten) gout[w] = 0u;\n";
+        o << "        } else {  // each point's record goes to its shadeindex\n";
+        o << "            const int32_t* si = k.shadeindex + tile * blockDim.x;\n";
+        o << "            for (int64_t w = threadIdx.x; w < npt * (int64_t)(rec / 4u); w += blockDim.x) {\n";
+        o << "                const int64_t p = w / (int64_t)(rec / 4u), q = w - p * (int64_t)(rec / 4u);\n";
+        o << "                uint32_t* dst = reinterpret_cast<uint32_t*>(k.outputs + (int64_t)si[p] * (int64_t)rec) + q;\n";
+        o << "                if (flags[w]) *dst = sw[w];\n";
+        o << "                else if (fill_unwritten) *dst = 0u;\n";
+        o << "            }\n";
+        o << "        }\n";
         o << "        __syncthreads();\n";
     }
     o << "    }\n}\n";
@@ -465,7 +476,7 @@ int build_and_load(const std::string& src, const std::string& csrc, const std::s
 
 int spec_launch(DeviceState& ds, const SpecKernel& sk, const CompiledGroup& cg, int64_t npoints,
                 const oslg_shaderglobals& G, void* userdata, void* outputs, void* stream, std::string* err,
-                int block_req, int pool_req, bool fill_unwritten) {
+                int block_req, int pool_req, bool fill_unwritten, const int32_t* shadeindex) {
     if (npoints <= 0) return OSLG_OK;
     int rc = device_init(ds, err);
     if (rc != OSLG_OK) return rc;
@@ -496,6 +507,7 @@ int spec_launch(DeviceState& ds, const SpecKernel& sk, const CompiledGroup& cg, 
     k.npoints = npoints;
     k.userdata = static_cast<char*>(userdata);
     k.outputs = static_cast<char*>(outputs);
+    k.shadeindex = shadeindex;
     k.status = ds.d_status;
     k.G = G;
     k.textures = ds.d_textures;

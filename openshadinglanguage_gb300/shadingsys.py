@@ -249,6 +249,16 @@ class ShadingSystem:
                        ctypes.c_void_p(userdata_ptr or None), ctypes.c_void_p(output_ptr or None),
                        ctypes.c_void_p(stream or None)))
 
+    def execute_batch_indexed(self, group, npoints, globals_c, shadeindex_ptr, userdata_ptr=0, output_ptr=0,
+                              stream=0):
+        """BatchedExecutor::execute with wide_shadeindex: point i's userdata
+        and output records are record shadeindex[i] (a device int32 array)."""
+        self._check(C.lib().oslg_execute_batch_indexed(self._h, group.handle, int(npoints), ctypes.byref(globals_c),
+                                                       ctypes.c_void_p(shadeindex_ptr or None),
+                                                       ctypes.c_void_p(userdata_ptr or None),
+                                                       ctypes.c_void_p(output_ptr or None),
+                                                       ctypes.c_void_p(stream or None)))
+
     def execute_layer(self, group, layername, npoints, globals_c, userdata_ptr=0, output_ptr=0, stream=0):
         """BatchedExecutor::execute_init + execute_layer(layername): the
         layers up to and including `layername`, over device points."""

@@ -63,6 +63,26 @@ template <int W> static void run_width(oslg::ShadingSystem& ss, oslg::ShaderGrou
     }
 }
 
+// the reference's signature: context + wide_shadeindex; lane i's record is
+// shadeindex[i] (reversed, with one record never addressed)
+template <int W> static void run_width_indexed(oslg::ShadingSystem& ss, oslg::ShaderGroupRef g, int batch_size) {
+    oslg::BatchedShaderGlobals<W> bsg;
+    std::memset(&bsg.varying, 0, sizeof(bsg.varying));
+    oslg::Block<int, W> si;
+    for (int lane = 0; lane < W; ++lane) {
+        bsg.varying.u.set(lane, 0.25f * (float)lane + 0.03f);
+        bsg.varying.v.set(lane, 0.5f - 0.125f * (float)lane);
+        si.set(lane, batch_size - lane);  // records batch_size .. 1; record 0 untouched
+    }
+    std::vector<Record> out(W + 1, Record{ -7.0f, { -7.0f, -7.0f, -7.0f } });
+    oslg::ShadingSystem::ShadingContext* ctx = ss.get_context();
+    CHECK(ss.batched<W>().execute(*ctx, g, batch_size, si, bsg, nullptr, out.data()));
+    ss.release_context(ctx);
+    CHECK(out[0].o == -7.0f);
+    for (int lane = 0; lane < batch_size; ++lane)
+        CHECK(expect(out[(size_t)si.get(lane)], bsg.varying.u.get(lane), bsg.varying.v.get(lane)));
+}
+
 int main(int argc, char** argv) {
     const bool lower_only = argc > 1 && std::strcmp(argv[1], "lower") == 0;
     oslg::ShadingSystem ss;
@@ -88,6 +108,8 @@ int main(int argc, char** argv) {
     run_width<16>(ss, g, 13);
     run_width<8>(ss, g, 5);
     run_width<4>(ss, g, 4);
+    run_width_indexed<8>(ss, g, 8);
+    run_width_indexed<16>(ss, g, 11);
     // N points on the device
     const int n = 100003;
     std::vector<float> hu(n), hv(n);
@@ -112,6 +134,18 @@ int main(int argc, char** argv) {
     int bad = 0;
     for (int i = 0; i < n; ++i) bad += expect(out[i], hu[i], hv[i]) ? 0 : 1;
     CHECK(bad == 0);
+    // the same points with a device shadeindex: point i's record is n-1-i
+    std::vector<int32_t> hsi(n);
+    for (int i = 0; i < n; ++i) hsi[i] = n - 1 - i;
+    int32_t* dsi = nullptr;
+    CHECK(cudaMalloc(&dsi, n * 4) == cudaSuccess);
+    cudaMemcpy(dsi, hsi.data(), n * 4, cudaMemcpyHostToDevice);
+    CHECK(ss.batched<16>().execute(g, (int64_t)n, sg, dsi, nullptr, dout, nullptr));
+    cudaMemcpy(out.data(), dout, n * sizeof(Record), cudaMemcpyDeviceToHost);
+    bad = 0;
+    for (int i = 0; i < n; ++i) bad += expect(out[(size_t)hsi[i]], hu[i], hv[i]) ? 0 : 1;
+    CHECK(bad == 0);
+    cudaFree(dsi);
     cudaFree(du);
     cudaFree(dv);
     cudaFree(dout);

@@ -218,6 +218,7 @@ TEXTS = {
     "isconstant_out.txt": "testsuite/isconstant/ref/out.txt",
     "exponential_out.txt": "testsuite/exponential/ref/out.txt",
     "hyperb_out.txt": "testsuite/hyperb/ref/out.txt",
+    "gettextureinfo_out.txt": "testsuite/gettextureinfo/ref/out.txt",
     "unknown_instruction_out.txt": "testsuite/unknown-instruction/ref/out.txt",
     "unknown_instruction.oso": "testsuite/unknown-instruction/test.oso",
 }

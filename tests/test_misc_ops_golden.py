@@ -379,6 +379,90 @@ def test_logb_edges():
     assert [column(out, cols, "L.r%d" % i) for i in range(len(xs))] == [-126, -126, 0, 3, -126, 127, 127, -1]
 
 
+# ---- gettextureinfo -------------------------------------------------------------------------
+GREEN = np.array([26, 128, 26, 255], np.float32) / np.float32(255.0)  # oiiotool constant 0.1,0.5,0.1,1 as uint8
+
+
+def register_green(ss):
+    ss.texture_create("green.tx", np.tile(GREEN, (128, 128, 1)))
+
+
+def gettextureinfo_group(ss):
+    """testsuite/gettextureinfo/test.osl run on green.tx (maketx of a
+    128x128 constant uint8 image); strings are compared in the shader."""
+    b = OsoBuilder("gti_suite")
+    o = Outputs(b, "L")
+    S = lambda x: b.const("string", x)
+    fn = b.param("string", "filename", "green.tx")
+
+    def q(name, t, data=None):
+        d = data if data is not None else b.local(t, "d_" + name)
+        b.op("gettextureinfo", o("r_" + name, "int"), fn, S(name), d)
+        return d
+
+    res = q("resolution", "int[2]")
+    for i in range(2):
+        b.op("aref", o("res%d" % i, "int"), res, b.const("int", i))
+    b.op("assign", o("channels", "int"), q("channels", "int"))
+    for nm in ("texturetype", "textureformat"):
+        b.op("eq", o(nm + "_plain", "int"), q(nm, "string"), S("Plain Texture"))
+    for nm in ("datawindow", "displaywindow"):
+        w = q(nm, "int[4]")
+        for i in range(4):
+            b.op("aref", o("%s%d" % (nm, i), "int"), w, b.const("int", i))
+    b.op("assign", o("averagecolor", "color"), q("averagecolor", "color"))
+    b.op("assign", o("averagealpha"), q("averagealpha", "float"))
+    b.op("assign", o("constantcolor", "color"), q("constantcolor", "color"))
+    b.op("assign", o("constantalpha"), q("constantalpha", "float"))
+    fb = b.local("string", "foobar")
+    b.op("assign", fb, S("not found"))
+    q("foobar", "string", fb)
+    b.op("eq", o("foobar_kept", "int"), fb, S("not found"))
+    bad = b.local("string", "bad")
+    b.op("assign", bad, S("not found"))
+    b.op("gettextureinfo", o("r_bad", "int"), S("badfile"), S("textureformat"), bad)
+    b.op("eq", o("bad_kept", "int"), bad, S("not found"))
+    b.op("assign", o("exists", "int"), q("exists", "int"))
+    e3 = b.local("int", "e3")
+    b.op("gettextureinfo", o("r_exists3", "int"), S("badfile3"), S("exists"), e3)
+    b.op("assign", o("exists3", "int"), e3)
+    ss.LoadMemoryCompiledShader("gti_suite", b.text())
+    g = ss.ShaderGroupBegin("gti_g")
+    ss.Shader(g, "surface", "gti_suite", "L")
+    ss.ShaderGroupEnd(g)
+    rec, cols = place(ss, g, [o])
+    return g, rec, cols
+
+
+def test_gettextureinfo_matches_the_testsuite():
+    ss = og.ShadingSystem()
+    register_green(ss)
+    g, rec, cols = gettextureinfo_group(ss)
+    u, v = pixel_grid(1, 1)
+    out = run_oracle(g, rec, grid_globals(u, v, 1, 1), 1)
+    C = lambda k: column(out, cols, "L." + k)
+    F = "green.tx"
+    got = ["%s resolution: %d %d (%d)" % (F, C("res0"), C("res1"), C("r_resolution")),
+           "%s channels: %d (%d)" % (F, C("channels"), C("r_channels"))]
+    for nm in ("texturetype", "textureformat"):
+        assert C(nm + "_plain") == 1
+        got.append("%s %s: Plain Texture (%d)" % (F, nm, C("r_" + nm)))
+    for nm in ("datawindow", "displaywindow"):
+        got.append("%s %s: %d %d %d %d (%d)" % ((F, nm) + tuple(C("%s%d" % (nm, i)) for i in range(4))
+                                               + (C("r_" + nm),)))
+    for nm in ("averagecolor", "averagealpha", "constantcolor", "constantalpha"):
+        got.append("%s %s: %s" % (F, nm, fmt(C(nm))) if C("r_" + nm) else "%s unknown %s" % (F, nm))
+    assert C("foobar_kept") == 1 and C("bad_kept") == 1
+    got.append("%s foobar: not found (%d)" % (F, C("r_foobar")))
+    got.append("badfile data: not found (%d)" % C("r_bad"))
+    got.append("%s exists? %d (return %d)" % (F, C("exists"), C("r_exists")))
+    got.append("badfile3 exists? %d (return %d)" % (C("exists3"), C("r_exists3")))
+    text = ref_lines("gettextureinfo_out.txt")
+    block = text[len(text) - text[::-1].index("Executing...") :]
+    want = [ln for ln in block if not ln.startswith("ERROR")]
+    assert got == want, [(a, b) for a, b in zip(got, want) if a != b]
+
+
 # ---- unknown instruction ----------------------------------------------------------------
 def test_unknown_instruction_is_refused_like_the_reference():
     ss = og.ShadingSystem()
@@ -484,7 +568,8 @@ def test_sincos_calculatenormal_backfacing_surfacearea_arraycopy():
 # ---- GPU == oracle ------------------------------------------------------------------------
 @pytest.mark.gpu
 @pytest.mark.parametrize("jit", [0, 1])
-@pytest.mark.parametrize("which", ["raytype", "isconnected", "isconstant", "exponential", "hyperb", "geometry"])
+@pytest.mark.parametrize("which", ["raytype", "isconnected", "isconstant", "exponential", "hyperb", "gettextureinfo",
+                                   "geometry"])
 def test_gpu_misc_ops_equal_the_oracle(which, jit):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
@@ -503,6 +588,7 @@ def test_gpu_misc_ops_equal_the_oracle(which, jit):
     else:
         g, rec, _ = {"raytype": raytype_group, "isconstant": isconstant_group,
                      "exponential": exponential_group, "hyperb": hyperb_group,
+                     "gettextureinfo": lambda s: (register_green(s), gettextureinfo_group(s))[1],
                      "isconnected": lambda s: isconnected_group(s, True)}[which](ss)
         u, v = pixel_grid(W, H)
         du, dv = torch.from_numpy(u).cuda(), torch.from_numpy(v).cuda()
