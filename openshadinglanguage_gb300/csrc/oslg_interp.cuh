@@ -2692,7 +2692,9 @@ struct RunCtx {
 template <int PPT>
 struct Ctl {
     uint32_t validm, actm, extm, lretm;
+    uint32_t extm0;  // points that exited before the current layer
     uint32_t stk[PPT], cnd[PPT], brk[PPT], cnt[PPT], iters[PPT];
+    uint32_t fret[PPT];  // bit (tag - 1): the point returned from that user function
 };
 
 template <int PPT>
@@ -2701,10 +2703,11 @@ __device__ __forceinline__ void ctl_init(Ctl<PPT>& C, const RunCtx& R, Lane& L, 
     const int64_t pt0 = L.pt;
     C.validm = 0;
     C.extm = 0;
+    C.extm0 = 0;
     C.lretm = 0;
 #pragma unroll
     for (int j = 0; j < PPT; ++j) {
-        C.stk[j] = C.cnd[j] = C.brk[j] = C.cnt[j] = C.iters[j] = 0;
+        C.stk[j] = C.cnd[j] = C.brk[j] = C.cnt[j] = C.iters[j] = C.fret[j] = 0;
         if (pt0 + (int64_t)j * blockDim.x < npoints) C.validm |= 1u << j;
     }
     C.actm = C.validm;
@@ -2745,7 +2748,8 @@ __device__ __forceinline__ bool ctl_else(Ctl<PPT>& C, const uint32_t* a) {
     uint32_t nm = 0;
 #pragma unroll
     for (int j = 0; j < PPT; ++j) {
-        const bool off = ((C.extm | C.lretm) >> j & 1u) || (ll && (bit(C.brk[j], ll - 1) || bit(C.cnt[j], ll - 1)));
+        const bool off = ((C.extm | C.lretm) >> j & 1u) || C.fret[j] != 0u ||
+                         (ll && (bit(C.brk[j], ll - 1) || bit(C.cnt[j], ll - 1)));
         if (bit(C.stk[j], d) && !bit(C.cnd[j], d) && !off) nm |= 1u << j;
     }
     C.actm = nm;
@@ -2758,7 +2762,8 @@ __device__ __forceinline__ void ctl_endif(Ctl<PPT>& C, const uint32_t* a) {
     uint32_t nm = 0;
 #pragma unroll
     for (int j = 0; j < PPT; ++j) {
-        const bool off = ((C.extm | C.lretm) >> j & 1u) || (ll && (bit(C.brk[j], ll - 1) || bit(C.cnt[j], ll - 1)));
+        const bool off = ((C.extm | C.lretm) >> j & 1u) || C.fret[j] != 0u ||
+                         (ll && (bit(C.brk[j], ll - 1) || bit(C.cnt[j], ll - 1)));
         if (bit(C.stk[j], d) && !off) nm |= 1u << j;
     }
     C.actm = nm;
@@ -2792,7 +2797,8 @@ __device__ __forceinline__ void ctl_loop_step(Ctl<PPT>& C, const uint32_t* a) {
     uint32_t nm = 0;
 #pragma unroll
     for (int j = 0; j < PPT; ++j) {
-        if ((((C.actm >> j) & 1u) || bit(C.cnt[j], ll - 1)) && !bit(C.brk[j], ll - 1) && !((C.extm | C.lretm) >> j & 1u))
+        if ((((C.actm >> j) & 1u) || bit(C.cnt[j], ll - 1)) && !bit(C.brk[j], ll - 1) && !((C.extm | C.lretm) >> j & 1u)
+            && C.fret[j] == 0u)
             nm |= 1u << j;
         C.cnt[j] = setbit(C.cnt[j], ll - 1, false);
     }
@@ -2809,7 +2815,43 @@ __device__ __forceinline__ void ctl_loop_end(Ctl<PPT>& C, const uint32_t* a) {
         C.cnt[j] = setbit(C.cnt[j], ll - 1, false);
         // lanes that broke out of an enclosing loop stay off via the
         // enclosing ENDIF/LOOP_STEP recomputation
-        if (bit(C.stk[j], d) && !((C.extm | C.lretm) >> j & 1u)) nm |= 1u << j;
+        if (bit(C.stk[j], d) && !((C.extm | C.lretm) >> j & 1u) && C.fret[j] == 0u) nm |= 1u << j;
+    }
+    C.actm = nm;
+}
+// user-function bodies (oslc wraps each call in a functioncall op,
+// codegen.cpp:1890-1905): the points active at the call enter; a return
+// inside marks the point off until the body ends (other points go on, e.g.
+// into an else branch). Begin skips the body when no point of the warp
+// enters it.
+template <int PPT>
+__device__ __forceinline__ bool ctl_func_begin(Ctl<PPT>& C, const uint32_t* a) {
+    const int d = (int)a[1];
+    const int f = (int)a[3] - 1;
+#pragma unroll
+    for (int j = 0; j < PPT; ++j) {
+        C.stk[j] = setbit(C.stk[j], d, (C.actm >> j) & 1u);
+        C.fret[j] = setbit(C.fret[j], f, false);
+    }
+    return !__any_sync(FULL, C.actm != 0);
+}
+template <int PPT>
+__device__ __forceinline__ void ctl_func_return(Ctl<PPT>& C, const uint32_t* a) {
+    const int f = (int)a[3] - 1;
+#pragma unroll
+    for (int j = 0; j < PPT; ++j)
+        if ((C.actm >> j) & 1u) C.fret[j] = setbit(C.fret[j], f, true);
+    C.actm = 0;
+}
+template <int PPT>
+__device__ __forceinline__ void ctl_func_end(Ctl<PPT>& C, const uint32_t* a) {
+    const int d = (int)a[1];
+    const int f = (int)a[3] - 1;
+    uint32_t nm = 0;
+#pragma unroll
+    for (int j = 0; j < PPT; ++j) {
+        C.fret[j] = setbit(C.fret[j], f, false);
+        if (bit(C.stk[j], d) && !((C.extm | C.lretm) >> j & 1u) && C.fret[j] == 0u) nm |= 1u << j;
     }
     C.actm = nm;
 }
@@ -2848,7 +2890,18 @@ __device__ __forceinline__ void ctl_return(Ctl<PPT>& C) { C.lretm |= C.actm; C.a
 template <int PPT>
 __device__ __forceinline__ void ctl_exit(Ctl<PPT>& C) { C.extm |= C.actm; C.actm = 0; }
 template <int PPT>
-__device__ __forceinline__ void ctl_layer_end(Ctl<PPT>& C) { C.lretm = 0; C.actm = C.validm & ~C.extm; }
+__device__ __forceinline__ void ctl_layer_end(Ctl<PPT>& C) {
+    // the layer's output stores follow: they run for every point that ran
+    // the layer, also one that exited inside it (what it wrote before
+    // exit() is its result, as the reference's symloc outputs keep it)
+    C.lretm = 0;
+    C.actm = C.validm & ~C.extm0;
+}
+template <int PPT>
+__device__ __forceinline__ void ctl_stores_end(Ctl<PPT>& C, const uint32_t* a) {
+    C.extm0 = C.extm;
+    C.actm = a[0] ? C.validm : C.validm & ~C.extm;
+}
 
 // One data op for the point L addresses. next() gives the following op
 // (the closure and Gabor ops carry extra operands there) or null at the end;
@@ -3047,11 +3100,11 @@ __device__ __forceinline__ void run_tile(const RunCtx& R, Lane& L, int64_t npoin
     // for every active point of the thread; control state is per point.
     const uint32_t li0 = L.li;
     const int64_t pt0 = L.pt;
-    uint32_t validm = 0, actm, extm = 0, lretm = 0;
-    uint32_t stk[PPT], cnd[PPT], brk[PPT], cnt[PPT], iters[PPT];
+    uint32_t validm = 0, actm, extm = 0, lretm = 0, extm0 = 0;
+    uint32_t stk[PPT], cnd[PPT], brk[PPT], cnt[PPT], iters[PPT], fret[PPT];
 #pragma unroll
     for (int j = 0; j < PPT; ++j) {
-        stk[j] = cnd[j] = brk[j] = cnt[j] = iters[j] = 0;
+        stk[j] = cnd[j] = brk[j] = cnt[j] = iters[j] = fret[j] = 0;
         if (pt0 + (int64_t)j * blockDim.x < npoints) validm |= 1u << j;
     }
     actm = validm;
@@ -3095,7 +3148,8 @@ __device__ __forceinline__ void run_tile(const RunCtx& R, Lane& L, int64_t npoin
             uint32_t nm = 0;
 #pragma unroll
             for (int j = 0; j < PPT; ++j) {
-                const bool off = ((extm | lretm) >> j & 1u) || (ll && (bit(brk[j], ll - 1) || bit(cnt[j], ll - 1)));
+                const bool off = ((extm | lretm) >> j & 1u) || fret[j] != 0u ||
+                                 (ll && (bit(brk[j], ll - 1) || bit(cnt[j], ll - 1)));
                 if (bit(stk[j], d) && !bit(cnd[j], d) && !off) nm |= 1u << j;
             }
             actm = nm;
@@ -3108,7 +3162,8 @@ __device__ __forceinline__ void run_tile(const RunCtx& R, Lane& L, int64_t npoin
             uint32_t nm = 0;
 #pragma unroll
             for (int j = 0; j < PPT; ++j) {
-                const bool off = ((extm | lretm) >> j & 1u) || (ll && (bit(brk[j], ll - 1) || bit(cnt[j], ll - 1)));
+                const bool off = ((extm | lretm) >> j & 1u) || fret[j] != 0u ||
+                                 (ll && (bit(brk[j], ll - 1) || bit(cnt[j], ll - 1)));
                 if (bit(stk[j], d) && !off) nm |= 1u << j;
             }
             actm = nm;
@@ -3142,7 +3197,8 @@ __device__ __forceinline__ void run_tile(const RunCtx& R, Lane& L, int64_t npoin
             uint32_t nm = 0;
 #pragma unroll
             for (int j = 0; j < PPT; ++j) {
-                if ((((actm >> j) & 1u) || bit(cnt[j], ll - 1)) && !bit(brk[j], ll - 1) && !((extm | lretm) >> j & 1u))
+                if ((((actm >> j) & 1u) || bit(cnt[j], ll - 1)) && !bit(brk[j], ll - 1) && !((extm | lretm) >> j & 1u)
+                    && fret[j] == 0u)
                     nm |= 1u << j;
                 cnt[j] = setbit(cnt[j], ll - 1, false);
             }
@@ -3174,7 +3230,36 @@ __device__ __forceinline__ void run_tile(const RunCtx& R, Lane& L, int64_t npoin
                 cnt[j] = setbit(cnt[j], ll - 1, false);
                 // lanes that broke out of an enclosing loop stay off via the
                 // enclosing ENDIF/LOOP_STEP recomputation
-                if (bit(stk[j], d) && !((extm | lretm) >> j & 1u)) nm |= 1u << j;
+                if (bit(stk[j], d) && !((extm | lretm) >> j & 1u) && fret[j] == 0u) nm |= 1u << j;
+            }
+            actm = nm;
+            break;
+        }
+        case OP_FUNC_BEGIN: {  // as ctl_func_begin
+            const int d = (int)a[1], f = (int)a[3] - 1;
+#pragma unroll
+            for (int j = 0; j < PPT; ++j) {
+                stk[j] = setbit(stk[j], d, (actm >> j) & 1u);
+                fret[j] = setbit(fret[j], f, false);
+            }
+            if (!__any_sync(FULL, actm != 0)) { pc = (int)a[2]; continue; }
+            break;
+        }
+        case OP_FUNC_RETURN: {
+            const int f = (int)a[3] - 1;
+#pragma unroll
+            for (int j = 0; j < PPT; ++j)
+                if ((actm >> j) & 1u) fret[j] = setbit(fret[j], f, true);
+            actm = 0;
+            break;
+        }
+        case OP_FUNC_END: {
+            const int d = (int)a[1], f = (int)a[3] - 1;
+            uint32_t nm = 0;
+#pragma unroll
+            for (int j = 0; j < PPT; ++j) {
+                fret[j] = setbit(fret[j], f, false);
+                if (bit(stk[j], d) && !((extm | lretm) >> j & 1u) && fret[j] == 0u) nm |= 1u << j;
             }
             actm = nm;
             break;
@@ -3197,7 +3282,8 @@ __device__ __forceinline__ void run_tile(const RunCtx& R, Lane& L, int64_t npoin
         }
         case OP_RETURN: lretm |= actm; actm = 0; break;
         case OP_EXIT: extm |= actm; actm = 0; break;
-        case OP_LAYER_END: lretm = 0; actm = validm & ~extm; break;
+        case OP_LAYER_END: lretm = 0; actm = validm & ~extm0; break;  // as ctl_layer_end
+        case OP_STORES_END: extm0 = extm; actm = a[0] ? validm : validm & ~extm; break;
         default: {
             auto next = [&]() -> const Op* { return pc + 1 < R.nops ? R.sops + pc + 1 : nullptr; };
             uint32_t todo = actm;

@@ -203,6 +203,7 @@ struct Lowerer {
     std::vector<uint32_t> pool;  // constant pool words
     uint32_t heap_top = 0;
     uint32_t max_depth = 0;
+    std::vector<int> fret_ops;  // emitted OP_FUNC_RETURN ops (their end pc is patched)
     bool uses_closures = false;
     // messages: per name a state symbol, per (name, type) a value store
     std::map<std::string, int> msg_state;
@@ -356,7 +357,15 @@ struct Lowerer {
             copy_section(li, m.maincodebegin, m.maincodeend);
             LOp le; le.name = "__layer_end"; le.layer = li;
             lops.push_back(le);
+            // the layer's outputs are final here: stored for every point that
+            // ran the layer, including those that exited inside it
+            if (!push_stores(li)) return false;
+            LOp se; se.name = "__stores_end"; se.layer = li;
+            lops.push_back(se);
         }
+        // renderer-side work and stores of globals, for every point
+        LOp fin; fin.name = "__stores_end"; fin.imm[0] = 1;
+        lops.push_back(fin);
         // renderer-side BSDF evaluation of closure outputs
         for (const BsdfEvalRequest& be : g.bsdf_evals) {
             SymLoc tmp;
@@ -387,12 +396,18 @@ struct Lowerer {
             op.imm[0] = bs.offset; op.imm[1] = bs.stride; op.imm[2] = bs.in_offset; op.imm[3] = bs.in_stride;
             lops.push_back(op);
         }
-        // renderer outputs placed through symlocs
+        return push_stores(-1);
+    }
+
+    // Stores of the renderer outputs placed through symlocs whose symbol
+    // belongs to layer li (-1: shader globals), in symloc order.
+    bool push_stores(int li) {
         for (const SymLoc& sl : g.symlocs) {
             if (sl.arena != ARENA_OUTPUTS) continue;
             if (beyond_stop(sl.name)) continue;  // written by a layer that does not run
             int gs = resolve_symloc(sl);
             if (gs < 0) return fail("symloc '" + sl.name + "' does not name a symbol of the group");
+            if (syms[gs].layer != li) continue;
             LOp op; op.name = "__store_output"; op.args = { gs };
             op.imm[0] = sl.offset; op.imm[1] = sl.stride; op.imm[2] = sl.derivs ? 1 : 0;
             op.imm[3] = sl.type.arraylen > 0 ? sl.type.arraylen : 4;  // closure records kept
@@ -437,7 +452,7 @@ struct Lowerer {
             "if", "for", "while", "dowhile", "break", "continue", "return", "exit", "nop",
             "useparam", "__layer_end", "__store_output", "__bsdf_eval", "__bsdf_sample", "__cl_store",
             "__cl_bsdf_eval", "__cl_bsdf_sample", "functioncall",
-            "functioncall_nr",
+            "functioncall_nr", "__fret", "__stores_end",
             "printf", "warning", "error", "fprintf" };
         if (nowrite.count(op.name)) return false;
         if (op.name == "sincos") return i == 1 || i == 2;
@@ -783,18 +798,44 @@ struct Lowerer {
                 if (writes_arg(lops[k], (int)i)) w.insert(lops[k].args[i]);
     }
     int folded_ops = 0;
+    // After a return (conditional or not) some points skip the rest of the
+    // layer, and after an exit the rest of the group; the output stores still
+    // run for exited points. Values known only on the points that went on
+    // are dropped at the layer's end (return) or not substituted into the
+    // output stores (exit).
+    bool fold_ret_div = false, fold_exit_div = false;
+    std::set<int> fold_unsafe_ret, fold_unsafe_exit;
+    static bool output_stage(const LOp& op) {
+        return op.name == "__store_output" || op.name == "__bsdf_eval" || op.name == "__bsdf_sample";
+    }
+    bool range_has(int b, int e, const char* name) const {
+        for (int q = b; q < e; ++q)
+            if (lops[(size_t)q].name == name) return true;
+        return false;
+    }
+    void fold_written(const LOp& op) {
+        for (size_t i = 0; i < op.args.size(); ++i) {
+            if (!writes_arg(op, (int)i)) continue;
+            if (fold_ret_div) fold_unsafe_ret.insert(op.args[i]);
+            if (fold_exit_div) fold_unsafe_exit.insert(op.args[i]);
+        }
+    }
     void fold_op(LOp& op, std::map<int, int>& K, const std::set<int>& blocked) {
         static const std::set<std::string> control = { "if", "for", "while", "dowhile", "break", "continue",
                                                        "return", "exit", "nop", "useparam", "functioncall",
-                                                       "functioncall_nr" };
+                                                       "functioncall_nr", "__fret", "__layer_end",
+                                                       "__stores_end" };
         if (control.count(op.name) || op.args.empty()) return;
         if (op.param_init) {  // a parameter's uniform value
             if (blocked.count(op.param_gsym)) K.erase(op.param_gsym);
             else K[op.param_gsym] = op.args[1];
             return;
         }
+        fold_written(op);
+        const bool outs = output_stage(op);
         for (size_t i = 0; i < op.args.size(); ++i) {
             if (writes_arg(op, (int)i) || partial_write(op)) continue;
+            if (outs && fold_unsafe_exit.count(op.args[i])) continue;
             auto it = K.find(op.args[i]);
             if (it != K.end()) op.args[i] = it->second;
         }
@@ -816,6 +857,29 @@ struct Lowerer {
     void fold_range(int b, int e, std::map<int, int>& K, const std::set<int>& blocked) {
         for (int k = b; k < e;) {
             LOp& op = lops[k];
+            if (op.name == "return") fold_ret_div = true;
+            if (op.name == "exit") fold_exit_div = true;
+            if (op.name == "__layer_end") {
+                for (int s2 : fold_unsafe_ret) K.erase(s2);
+                fold_unsafe_ret.clear();
+                fold_ret_div = false;
+            }
+            if (op.name == "functioncall" || op.name == "functioncall_nr") {
+                // a body that a return leaves early: what it writes is known
+                // only on the points that went on
+                const int jend = op.jumps.empty() ? k + 1 : op.jumps[0];
+                if (range_has(k + 1, jend, "__fret")) {
+                    std::map<int, int> K1 = K;
+                    fold_range(k + 1, jend, K1, blocked);
+                    std::set<int> w;
+                    written_in(k + 1, jend, w);
+                    for (int s2 : w) K.erase(s2);
+                    k = jend;
+                    continue;
+                }
+                ++k;
+                continue;
+            }
             if (op.name == "if" && op.jumps.size() >= 2) {
                 const int je = op.jumps[0], jend = op.jumps[1];
                 // a known condition: the branch not taken never runs; the
@@ -871,7 +935,8 @@ struct Lowerer {
     // ---- dead-op elimination ----------------------------------------------------
     static bool has_effect(const LOp& op) {
         static const std::set<std::string> effects = {
-            "if", "for", "while", "dowhile", "break", "continue", "return", "exit", "__layer_end",
+            "if", "for", "while", "dowhile", "break", "continue", "return", "exit", "__layer_end", "__fret",
+            "__stores_end",
             "__store_output", "__bsdf_eval", "__bsdf_sample", "printf", "warning", "error", "fprintf",
             "functioncall", "functioncall_nr", "useparam", "setmessage", "getmessage" };
         return effects.count(op.name) != 0;
@@ -1020,7 +1085,7 @@ struct Lowerer {
         int adds = 0;
         for (int k = 0; k < n; ++k) {
             const LOp& op = lops[k];
-            if (op.name == "return" || op.name == "exit") return false;
+            if (op.name == "return" || op.name == "exit" || op.name == "__fret") return false;
             bool refs = false;
             for (int a : op.args) refs = refs || is_closure(a);
             if (!refs || op.name == "useparam") continue;
@@ -1298,19 +1363,44 @@ struct Lowerer {
         return (int)ops.size() - 1;
     }
 
-    bool emit_range(int b, int e, int depth, int loopl) {
+    bool emit_range(int b, int e, int depth, int loopl, int funcl = 0) {
         for (int k = b; k < e;) {
             const LOp& op = lops[k];
+            if (op.name == "functioncall" || op.name == "functioncall_nr") {
+                // a user function's inlined body (oslc, codegen.cpp:1890-1905):
+                // masked like a block when a return inside ends it early
+                const int jend = op.jumps.empty() ? k + 1 : op.jumps[0];
+                if (jend <= k || jend > e) return fail("functioncall with a bad end");
+                bool early = false;
+                for (int q = k + 1; q < jend; ++q) early = early || (lops[q].name == "__fret" && lops[q].imm[0] == k);
+                if (!early) {
+                    if (!emit_range(k + 1, jend, depth, loopl, funcl)) return false;
+                    k = jend;
+                    continue;
+                }
+                if ((uint32_t)depth + 1 > max_depth) max_depth = depth + 1;
+                if (depth >= 31) return fail("control flow nested too deeply");
+                const uint32_t tag = (uint32_t)depth + 1;
+                const int beg = emit(OP_FUNC_BEGIN, { 0u, (uint32_t)depth, 0u, tag }, "functioncall");
+                const size_t first_ret = fret_ops.size();
+                if (!emit_range(k + 1, jend, depth + 1, loopl, (int)tag)) return false;
+                const int endop = emit(OP_FUNC_END, { 0u, (uint32_t)depth, 0u, tag }, "functioncall");
+                ops[beg].a[2] = (uint32_t)endop;
+                for (size_t q = first_ret; q < fret_ops.size(); ++q)
+                    if (ops[fret_ops[q]].a[3] == tag) ops[fret_ops[q]].a[2] = (uint32_t)endop;
+                k = jend;
+                continue;
+            }
             if (op.name == "if") {
                 if (op.jumps.size() < 2) return fail("if without jump targets");
                 int je = op.jumps[0], jend = op.jumps[1];
                 if ((uint32_t)depth + 1 > max_depth) max_depth = depth + 1;
                 if (depth >= 31) return fail("control flow nested too deeply");
                 int ifop = emit(OP_IF, { A(op.args[0]), (uint32_t)depth, 0u, (uint32_t)loopl }, "if");
-                if (!emit_range(k + 1, je, depth + 1, loopl)) return false;
+                if (!emit_range(k + 1, je, depth + 1, loopl, funcl)) return false;
                 int elop = emit(OP_ELSE, { 0u, (uint32_t)depth, 0u, (uint32_t)loopl }, "if");
                 ops[ifop].a[2] = (uint32_t)elop;
-                if (!emit_range(je, jend, depth + 1, loopl)) return false;
+                if (!emit_range(je, jend, depth + 1, loopl, funcl)) return false;
                 int enop = emit(OP_ENDIF, { 0u, (uint32_t)depth, 0u, (uint32_t)loopl }, "if");
                 ops[elop].a[2] = (uint32_t)enop;
                 k = jend;
@@ -1323,20 +1413,26 @@ struct Lowerer {
                 if (depth >= 31) return fail("control flow nested too deeply");
                 uint32_t ll = (uint32_t)depth + 1;  // loop level tag = its depth + 1
                 emit(OP_LOOP_BEGIN, { 0u, (uint32_t)depth, 0u, ll }, op.name);
-                if (!emit_range(k + 1, jc, depth + 1, (int)ll)) return false;
+                if (!emit_range(k + 1, jc, depth + 1, (int)ll, funcl)) return false;
                 int jmp_body = -1;
                 if (op.name == "dowhile") jmp_body = emit(OP_JUMP, { 0u, 0u, 0u, 0u }, op.name);
                 int cond_start = (int)ops.size();
-                if (!emit_range(jc, jb, depth + 1, (int)ll)) return false;
+                if (!emit_range(jc, jb, depth + 1, (int)ll, funcl)) return false;
                 int test = emit(OP_LOOP_TEST, { A(op.args[0]), (uint32_t)depth, 0u, ll }, op.name);
                 if (jmp_body >= 0) ops[jmp_body].a[2] = (uint32_t)ops.size();
-                if (!emit_range(jb, js, depth + 1, (int)ll)) return false;
+                if (!emit_range(jb, js, depth + 1, (int)ll, funcl)) return false;
                 emit(OP_LOOP_STEP, { 0u, (uint32_t)depth, 0u, ll }, op.name);
-                if (!emit_range(js, jend, depth + 1, (int)ll)) return false;
+                if (!emit_range(js, jend, depth + 1, (int)ll, funcl)) return false;
                 emit(OP_JUMP, { 0u, 0u, (uint32_t)cond_start, 0u }, op.name);
                 int endop = emit(OP_LOOP_END, { 0u, (uint32_t)depth, 0u, ll }, op.name);
                 ops[test].a[2] = (uint32_t)endop;
                 k = jend;
+                continue;
+            }
+            if (op.name == "__fret") {  // return from the enclosing user function
+                if (!funcl) return fail("internal: function return outside a function body");
+                fret_ops.push_back(emit(OP_FUNC_RETURN, { 0u, 0u, 0u, (uint32_t)funcl }, "return"));
+                ++k;
                 continue;
             }
             if (!lower_op(op, depth, loopl)) return false;
@@ -1384,6 +1480,7 @@ struct Lowerer {
             case OP_LOOP_STEP: case OP_LOOP_END: case OP_JUMP: case OP_BREAK: case OP_CONTINUE: case OP_RETURN:
             case OP_EXIT: case OP_LAYER_END: case OP_STORE_OUTPUT: case OP_STORE_CLOSURE: case OP_BSDF_EVAL:
             case OP_BSDF_SAMPLE: case OP_CL_STORE: case OP_CL_BSDF_EVAL: case OP_CL_BSDF_SAMPLE:
+            case OP_FUNC_BEGIN: case OP_FUNC_RETURN: case OP_FUNC_END: case OP_STORES_END:
                 continue;
             default:
                 break;
@@ -2068,6 +2165,7 @@ struct Lowerer {
         if (n == "return") { emit(OP_RETURN, {}, n); return true; }
         if (n == "exit") { emit(OP_EXIT, {}, n); return true; }
         if (n == "__layer_end") { emit(OP_LAYER_END, {}, "layer"); return true; }
+        if (n == "__stores_end") { emit(OP_STORES_END, { (uint32_t)op.imm[0] }, "layer"); return true; }
         if (n == "__load_userdata") {
             int s = op.args[0];
             emit(OP_LOAD_USERDATA, { a(0), (uint32_t)op.imm[0], (uint32_t)op.imm[1],
@@ -2572,6 +2670,27 @@ struct Lowerer {
             if (ro == param || ro == name2) return true;
         return false;
     }
+    // A return inside a user function's body (between a functioncall op and
+    // its end label, innermost call) returns from that function; elsewhere
+    // it ends the layer (llvm_gen_return, batched_llvm_gen.cpp). Function
+    // returns become "__fret" with imm[0] = the functioncall's index.
+    bool mark_function_returns() {
+        std::vector<std::pair<int, int>> open;  // (functioncall index, end)
+        for (int k = 0; k < (int)lops.size(); ++k) {
+            while (!open.empty() && k >= open.back().second) open.pop_back();
+            LOp& op = lops[(size_t)k];
+            if (op.name == "functioncall" || op.name == "functioncall_nr") {
+                const int end = op.jumps.empty() ? k + 1 : op.jumps[0];
+                if (end <= k || end > (int)lops.size()) return fail("functioncall with a bad end");
+                open.push_back({ k, end });
+            } else if (op.name == "return" && !open.empty()) {
+                op.name = "__fret";
+                op.imm[0] = open.back().first;
+            }
+        }
+        return true;
+    }
+
     void resolve_isconnected() {
         for (LOp& op : lops) {
             if (op.name != "isconnected" || op.args.size() < 2) continue;
@@ -2603,6 +2722,7 @@ struct Lowerer {
     bool run(CompiledGroup& out) {
         if (g.layers.empty()) return fail("group has no layers");
         if (!build_lops()) return false;
+        if (!mark_function_returns()) return false;
         resolve_isconnected();
         if (!prepare_messages()) return false;
         if (ss.opts.opt_constant_fold) fold_constants();
@@ -2611,6 +2731,11 @@ struct Lowerer {
         analyze();
         assign_storage();
         if (!lower_all()) return false;
+        // mask markers with nothing after them
+        while (!ops.empty() && ops.back().code == OP_STORES_END) {
+            ops.pop_back();
+            op_names.pop_back();
+        }
         // closure pools live after the symbol heap
         ProgramHeader h;
         std::memset(&h, 0, sizeof(h));

@@ -64,7 +64,8 @@ enum OpCode : uint16_t {
     OP_CONTINUE,    // a3=loop level+1
     OP_RETURN,      // ends the current layer for the active lanes
     OP_EXIT,        // ends the whole group for the active lanes
-    OP_LAYER_END,   // re-enables lanes that returned from this layer
+    OP_LAYER_END,   // re-enables lanes that returned from this layer and those that
+                    // exited in it, for the layer's output stores that follow
     // data movement
     OP_LOAD_GLOBAL,   // a0=dst a1=global id
     OP_LOAD_USERDATA, // a0=dst a1=byte offset a2=byte stride a3=bit 0 int, bit 1 the
@@ -154,6 +155,13 @@ enum OpCode : uint16_t {
     OP_CALCNORMAL,   // a0=r (triple) a1=P (triple with derivatives); reads flipHandedness
     OP_RAYTYPE,      // a0=r (int) a1=name (string) or kNoArg a2=the name's bit (when a1 is
                      // kNoArg) a3=raytype name hashes (ints) a4=count: r = raytype & bit != 0
+    // user-function bodies with early returns (oslc's functioncall op): a
+    // return inside ends the body for the point; tag a3 = depth + 1
+    OP_FUNC_BEGIN,   // a1=depth a2=pc of the OP_FUNC_END a3=tag
+    OP_FUNC_RETURN,  // a2=pc of the OP_FUNC_END a3=tag
+    OP_FUNC_END,     // a1=depth a3=tag
+    OP_STORES_END,   // after a layer's output stores: lanes that exited stay off from
+                     // here; a0 = 1: the renderer-side section, every point
     OP_COUNT
 };
 

@@ -72,7 +72,9 @@ const char* kKernelName = "oslg_spec_kernel";
 const char* kFlags = "-cubin -gencode arch=compute_103a,code=sm_103a -std=c++17 -O3 -fmad=false";
 const char* kBatchFlags = "--split-compile=0";
 
-bool jump_op(uint16_t c) { return c == OP_IF || c == OP_ELSE || c == OP_LOOP_TEST || c == OP_JUMP; }
+bool jump_op(uint16_t c) {
+    return c == OP_IF || c == OP_ELSE || c == OP_LOOP_TEST || c == OP_JUMP || c == OP_FUNC_BEGIN;
+}
 
 uint32_t arg_ncomp(uint32_t a) {
     const uint32_t t = (a >> kArgTCShift) & 7u;
@@ -221,6 +223,10 @@ void emit_body(std::ostringstream& o, const ProgView& v, const std::string& sfx)
         case OP_RETURN: o << "        (void)a;\n        ctl_return<1>(C);\n"; break;
         case OP_EXIT: o << "        (void)a;\n        ctl_exit<1>(C);\n"; break;
         case OP_LAYER_END: o << "        (void)a;\n        ctl_layer_end<1>(C);\n"; break;
+        case OP_STORES_END: o << "        ctl_stores_end<1>(C, a);\n"; break;
+        case OP_FUNC_BEGIN: o << "        if (ctl_func_begin<1>(C, a)) goto " << dst(a[2]) << ";\n"; break;
+        case OP_FUNC_RETURN: o << "        ctl_func_return<1>(C, a);\n"; break;
+        case OP_FUNC_END: o << "        ctl_func_end<1>(C, a);\n"; break;
         default:
             if (i + 1 < n) {
                 // the next op, or every OP_NOP carrier that follows (operand

@@ -83,6 +83,22 @@ class _Loop:
         return False
 
 
+class _Function:
+    """A user function's inlined body: oslc wraps each call in a
+    functioncall op whose jump is the end of the body; a return inside
+    leaves the body."""
+
+    def __init__(self, b, idx):
+        self.b, self.idx = b, idx
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.b.ops[self.idx][2][0] = len(self.b.ops)
+        return False
+
+
 class OsoBuilder:
     def __init__(self, name, shadertype="shader"):
         self.name, self.shadertype = name, shadertype
@@ -128,6 +144,11 @@ class OsoBuilder:
     def if_(self, cond):
         self.ops.append(["if", [str(cond)], [0, 0]])
         return _If(self, len(self.ops) - 1)
+
+    def function(self, name):
+        """with b.function("f"): body ops (return = b.op("return"))."""
+        self.ops.append(["functioncall", [str(self.const("string", name))], [0]])
+        return _Function(self, len(self.ops) - 1)
 
     def loop(self, kind, cond):
         """kind: for | while | dowhile. Ops emitted before .cond() form the init block."""

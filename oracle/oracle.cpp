@@ -51,8 +51,8 @@ struct Prog {
     std::vector<int> loop_end_of_level;  // per op: for BREAK/CONTINUE
     std::vector<int> partner;            // IF->ELSE, ELSE->ENDIF, LOOP_TEST->LOOP_END
     std::vector<int> break_target, continue_target;
-    std::vector<int> layer_end_after;    // RETURN -> next LAYER_END
-    int outputs_start = 0;               // first op after the last LAYER_END
+    std::vector<int> layer_end_after;    // RETURN, EXIT -> the layer's LAYER_END
+    int final_section = 0;               // the STORES_END that opens the renderer-side section
 };
 
 struct Point {
@@ -1541,6 +1541,7 @@ struct Runner {
         // the loop limit: back edges this point takes, summed over every loop
         const uint32_t cap = oslg::max_loop_iterations(h);
         uint32_t iters = 0;
+        bool exited = false;
         for (int pc = 0; pc < nops;) {
             const Op& op = prog.ops[pc];
             const uint32_t* a = op.a;
@@ -1561,9 +1562,17 @@ struct Runner {
             case oslg::OP_BREAK: pc = prog.break_target[pc]; continue;
             case oslg::OP_CONTINUE: pc = prog.continue_target[pc]; continue;
             case oslg::OP_RETURN: pc = prog.layer_end_after[pc]; continue;
-            case oslg::OP_EXIT: pc = prog.outputs_start; continue;
+            // exit: the rest of the group is skipped, but the layer's output
+            // stores run (what the point wrote stays its result), then the
+            // renderer-side section
+            case oslg::OP_EXIT: exited = true; pc = prog.layer_end_after[pc]; continue;
+            case oslg::OP_STORES_END:
+                if (exited && a[0] == 0u) { pc = prog.final_section; continue; }
+                break;
+            // a return inside a user function's body ends the body (a2 = its end)
+            case oslg::OP_FUNC_RETURN: pc = (int)a[2]; continue;
             case oslg::OP_NOP: case oslg::OP_ENDIF: case oslg::OP_LOOP_BEGIN: case oslg::OP_LOOP_STEP:
-            case oslg::OP_LOOP_END: case oslg::OP_LAYER_END:
+            case oslg::OP_LOOP_END: case oslg::OP_LAYER_END: case oslg::OP_FUNC_BEGIN: case oslg::OP_FUNC_END:
                 break;
             case oslg::OP_LOAD_GLOBAL: op_load_global(P, a, G); break;
             case oslg::OP_LOAD_USERDATA: {
@@ -2033,13 +2042,13 @@ bool resolve(Prog& p, const void* blob, size_t bytes) {
                 if (o.code == oslg::OP_CONTINUE && q.code == oslg::OP_LOOP_STEP) { p.continue_target[i] = j; break; }
             }
         }
-        if (o.code == oslg::OP_RETURN)
+        if (o.code == oslg::OP_RETURN || o.code == oslg::OP_EXIT)
             for (int j = i + 1; j < n; ++j)
                 if (p.ops[j].code == oslg::OP_LAYER_END) { p.layer_end_after[i] = j; break; }
     }
-    p.outputs_start = n;
-    for (int j = n - 1; j >= 0; --j)
-        if (p.ops[j].code == oslg::OP_LAYER_END) { p.outputs_start = j + 1; break; }
+    p.final_section = n;
+    for (int j = 0; j < n; ++j)
+        if (p.ops[j].code == oslg::OP_STORES_END && p.ops[j].a[0] == 1u) { p.final_section = j; break; }
     return true;
 }
 
