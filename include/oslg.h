@@ -33,6 +33,7 @@ extern "C" {
 
 typedef struct oslg_system oslg_system;
 typedef struct oslg_group oslg_group;
+typedef struct oslg_symbol oslg_symbol;
 
 /* OIIO TypeDesc numbering (basetype / aggregate / vecsemantics), so a
  * caller holding an OIIO::TypeDesc can pass its fields straight through. */
@@ -310,6 +311,25 @@ int oslg_execute_batch(oslg_system* sys, oslg_group* group, int64_t npoints,
 int oslg_execute_batch_indexed(oslg_system* sys, oslg_group* group, int64_t npoints,
                                const oslg_shaderglobals* globals, const int32_t* shadeindex, void* userdata_base,
                                void* output_base, void* stream);
+
+/* ShadingSystem::find_symbol (oslexec.h:950-959): symbol `symbolname` of
+ * layer `layername`, or with layername NULL of the last layer that has one
+ * ("layer.symbol" names both). Finding a symbol retains it: the group is
+ * lowered again so that every device execution (oslg_execute_batch,
+ * _sync, _indexed) keeps the symbol's final values. Closures and shader
+ * globals are refused. The handle lives as long as the group. */
+int oslg_find_symbol(oslg_system* sys, oslg_group* group, const char* layername, const char* symbolname,
+                     const oslg_symbol** out);
+/* ShadingSystem::symbol_typedesc (oslexec.h:961-963) */
+int oslg_symbol_typedesc(const oslg_symbol* sym, oslg_typedesc* out);
+/* ShadingSystem::symbol_address (oslexec.h:965-971) for a batch: the device
+ * SoA view of the symbol's values after the group's most recent device
+ * execution. Word c of point i (c < components x array length; floats, or
+ * int32 for int symbols) is at ((float*)*address)[c * *plane_stride + i],
+ * point i being the launch's i-th point. OSLG_ERR_STATE when the group has
+ * not run since the symbol was found. */
+int oslg_symbol_address(oslg_system* sys, oslg_group* group, const oslg_symbol* sym, const void** address,
+                        int64_t* plane_stride);
 
 /* Same as oslg_execute_batch, then waits for the stream and reports any
  * status bit the kernel raised (closure arena overflow, bad opcode, array

@@ -60,6 +60,12 @@ struct oslg_system {
 
 struct oslg_group {
     oslg::ShaderGroup g;
+    // retained symbols' planes of the last device execution
+    float* d_symheap = nullptr;
+    size_t symheap_bytes = 0;
+    int64_t symheap_points = -1;
+    int symheap_words = 0;
+    ~oslg_group() { if (d_symheap) cudaFree(d_symheap); }
 };
 
 struct oslg_batch {
@@ -144,6 +150,27 @@ bool typedesc_to_spec(const oslg_typedesc& t, TypeSpec& ts) {
         return false;
     }
     return true;
+}
+
+oslg_typedesc spec_to_typedesc(const TypeSpec& ts) {
+    oslg_typedesc t;
+    std::memset(&t, 0, sizeof(t));
+    t.arraylen = ts.arraylen;
+    t.aggregate = OSLG_AGG_SCALAR;
+    t.vecsemantics = OSLG_VEC_NOXFORM;
+    if (ts.base == BT_INT) t.basetype = OSLG_BASE_INT32;
+    else if (ts.base == BT_STRING) t.basetype = OSLG_BASE_STRING;
+    else {
+        t.basetype = OSLG_BASE_FLOAT;
+        if (ts.base == BT_MATRIX) t.aggregate = OSLG_AGG_MATRIX44;
+        if (ts.base == BT_TRIPLE) {
+            t.aggregate = OSLG_AGG_VEC3;
+            t.vecsemantics = ts.vecsem == VS_COLOR ? OSLG_VEC_COLOR
+                           : ts.vecsem == VS_POINT ? OSLG_VEC_POINT
+                           : ts.vecsem == VS_NORMAL ? OSLG_VEC_NORMAL : OSLG_VEC_VECTOR;
+        }
+    }
+    return t;
 }
 
 template <class F> int guarded(oslg_system* sys, F&& f) {
@@ -517,17 +544,99 @@ int execute_batch_impl(oslg_system* sys, oslg_group* group, int64_t npoints, con
         if (rc != OSLG_OK) return rc;
         std::string err;
         const CompiledGroup& cg = *group->g.compiled;
+        LaunchExtras ex;
+        ex.shadeindex = shadeindex;
+        if (cg.retained_words > 0 && npoints > 0) {  // planes for find_symbol's symbols
+            const size_t need = (size_t)cg.retained_words * (size_t)npoints * sizeof(float);
+            if (need > group->symheap_bytes) {
+                if (group->d_symheap) cudaFree(group->d_symheap);
+                group->d_symheap = nullptr;
+                group->symheap_bytes = 0;
+                if (cudaMalloc(&group->d_symheap, need) != cudaSuccess)
+                    return fail(sys, OSLG_ERR_CUDA, "cudaMalloc of the retained-symbol planes");
+                group->symheap_bytes = need;
+            }
+            ex.symheap = group->d_symheap;
+            ex.symheap_stride = npoints;
+        }
         if (cg.spec)
             rc = spec_launch(sys->dev, *cg.spec, cg, npoints, *globals, userdata_base, output_base, stream, &err,
-                             sys->jit_block, sys->jit_pool_smem, false, shadeindex);
+                             sys->jit_block, sys->jit_pool_smem, false, &ex);
         else
             rc = device_execute(sys->dev, cg.header, cg.d_blob, npoints, *globals, userdata_base, output_base,
-                                stream, sys->launch, &err, shadeindex);
+                                stream, sys->launch, &err, &ex);
         if (rc != OSLG_OK) return fail(sys, rc, err);
+        group->symheap_points = cg.retained_words > 0 ? npoints : -1;
+        group->symheap_words = cg.retained_words;
         return OSLG_OK;
     });
 }
 }  // namespace
+
+int oslg_find_symbol(oslg_system* sys, oslg_group* group, const char* layername, const char* symbolname,
+                     const oslg_symbol** out) {
+    if (!sys || !group || !symbolname || !out) return OSLG_ERR_ARG;
+    *out = nullptr;
+    return guarded(sys, [&]() {
+        ShaderGroup& g = group->g;
+        std::string lname = layername ? layername : "", sname = symbolname;
+        if (lname.empty()) {  // "layer.symbol"
+            const size_t dot = sname.find('.');
+            if (dot != std::string::npos && g.find_layer(sname.substr(0, dot)) >= 0) {
+                lname = sname.substr(0, dot);
+                sname = sname.substr(dot + 1);
+            }
+        }
+        int li = -1, msi = -1;
+        for (int k = (int)g.layers.size() - 1; k >= 0 && msi < 0; --k) {  // last to first
+            if (!lname.empty() && g.layers[(size_t)k].layername != lname) continue;
+            const int m = g.layers[(size_t)k].master->find_symbol(sname);
+            if (m >= 0) { li = k; msi = m; }
+        }
+        if (msi < 0) return fail(sys, OSLG_ERR_ARG, "no symbol '" + sname + "' in the group");
+        const Symbol& ms = g.layers[(size_t)li].master->symbols[(size_t)msi];
+        if (ms.type.base == BT_CLOSURE || ms.kind == SK_GLOBAL)
+            return fail(sys, OSLG_ERR_ARG, "symbol '" + sname + "': closures and globals have no address here");
+        for (const auto& r : g.retained)
+            if (r->layer == li && r->name == sname) {
+                *out = reinterpret_cast<const oslg_symbol*>(r.get());
+                return OSLG_OK;
+            }
+        auto r = std::make_unique<ShaderGroup::Retained>();
+        r->layer = li;
+        r->name = sname;
+        r->type = ms.type;
+        r->plane = g.retained.empty() ? 0 : g.retained.back()->plane + g.retained.back()->words;
+        r->words = ms.type.ncomp() * ms.type.elems();
+        *out = reinterpret_cast<const oslg_symbol*>(r.get());
+        std::lock_guard<std::mutex> lock(g.mutex);
+        g.retained.push_back(std::move(r));
+        g.compiled.reset();  // its values must now be kept: lower again
+        g.layer_compiled.clear();
+        return OSLG_OK;
+    });
+}
+
+int oslg_symbol_typedesc(const oslg_symbol* sym, oslg_typedesc* out) {
+    if (!sym || !out) return OSLG_ERR_ARG;
+    const auto* r = reinterpret_cast<const ShaderGroup::Retained*>(sym);
+    *out = spec_to_typedesc(r->type);
+    return OSLG_OK;
+}
+
+int oslg_symbol_address(oslg_system* sys, oslg_group* group, const oslg_symbol* sym, const void** address,
+                        int64_t* plane_stride) {
+    if (!sys || !group || !sym || !address || !plane_stride) return OSLG_ERR_ARG;
+    const auto* r = reinterpret_cast<const ShaderGroup::Retained*>(sym);
+    bool mine = false;
+    for (const auto& q : group->g.retained) mine = mine || q.get() == r;
+    if (!mine) return fail(sys, OSLG_ERR_ARG, "the symbol was found in another group");
+    if (group->symheap_points < 0 || r->plane + r->words > group->symheap_words)
+        return fail(sys, OSLG_ERR_STATE, "symbol_address: execute the group after find_symbol");
+    *address = group->d_symheap + (size_t)r->plane * (size_t)group->symheap_points;
+    *plane_stride = group->symheap_points;
+    return OSLG_OK;
+}
 
 int oslg_execute_batch(oslg_system* sys, oslg_group* group, int64_t npoints, const oslg_shaderglobals* globals,
                        void* userdata_base, void* output_base, void* stream) {

@@ -26,7 +26,12 @@ struct KArgs {
     // record of point i in the userdata and output arenas: shadeindex[i]
     // (BatchedExecutor::execute's wide_shadeindex); null: i
     const int32_t* shadeindex = nullptr;
+    // retained symbols (find_symbol): word c of a retained symbol's plane
+    // block at symheap[(plane + c) * symheap_stride + point]; null: none
+    float* symheap = nullptr;
+    int64_t symheap_stride = 0;
 };
+
 
 // One group's request inside a persistent batch launch.
 struct BatchJob {
@@ -57,6 +62,13 @@ struct BatchArgs {
     int32_t ntextures = 0;
 };
 }  // namespace dev
+
+// Per-launch options beyond the program and its arenas.
+struct LaunchExtras {
+    const int32_t* shadeindex = nullptr;
+    float* symheap = nullptr;
+    int64_t symheap_stride = 0;
+};
 
 // One interpreter instantiation per feature tier (oslg_tier.cu compiled with
 // -DOSLG_TIER=N): TIER bits 1 noise/hash, 2 closures/BSDF/spline, 4 math.
@@ -104,7 +116,7 @@ void device_free(void* p);
 // Enqueue one plain per-group launch over [0, npoints).
 int device_execute(DeviceState& ds, const ProgramHeader& hdr, const void* d_blob, int64_t npoints,
                    const oslg_shaderglobals& G, void* userdata, void* outputs, void* stream,
-                   const LaunchConfig& cfg, std::string* err, const int32_t* shadeindex = nullptr);
+                   const LaunchConfig& cfg, std::string* err, const LaunchExtras* ex = nullptr);
 
 // Read-and-clear the device status word (synchronises the stream).
 int device_read_status(DeviceState& ds, void* stream, uint32_t* bits, std::string* err);

@@ -151,6 +151,7 @@ struct CompiledGroup {
     void* d_blob = nullptr;             // device copy (owned by the executor)
     int device = -1;
     std::shared_ptr<SpecKernel> spec;   // specialized kernel, when built
+    int retained_words = 0;             // symbol planes its OP_STORE_HEAP ops fill
 };
 
 // ShaderGroup (oslexec_pvt.h:1777)
@@ -165,6 +166,15 @@ struct ShaderGroup {
     std::mutex mutex;  // lowering happens once, under this lock
     std::unique_ptr<CompiledGroup> compiled;
     std::map<int, std::unique_ptr<CompiledGroup>> layer_compiled;  // programs ending at a layer
+    // symbols find_symbol retained: each execution keeps their values in
+    // `words` planes from `plane` on (ShadingSystem::symbol_address)
+    struct Retained {
+        int layer;
+        std::string name;
+        TypeSpec type;
+        int plane, words;
+    };
+    std::vector<std::unique_ptr<Retained>> retained;
     int find_layer(const std::string& n) const;
 };
 

@@ -2684,6 +2684,8 @@ struct RunCtx {
     char* outputs;
     uint32_t* status;
     uint32_t max_iters = kDefaultMaxLoopIterations;  // loop back edges per point
+    float* symheap = nullptr;  // retained symbols (KArgs::symheap)
+    int64_t symheap_stride = 0;
 };
 
 // Control state of the masked walk: per thread, PPT points with their
@@ -2993,6 +2995,12 @@ __device__ __forceinline__ void exec_op(const RunCtx& R, Lane& L, uint32_t code,
     case OP_SINCOS: OSLG_TIER_CASE(4, h_sincos(L, a)) break;
     case OP_CALCNORMAL: OSLG_TIER_CASE(4, h_calcnormal(L, a, *R.G)) break;
     case OP_RAYTYPE: OSLG_TIER_CASE(4, h_raytype(L, a, *R.G)) break;
+    case OP_STORE_HEAP:
+        // a retained symbol's words into its planes (values, by point)
+        if (R.symheap)
+            for (uint32_t c = 0; c < a[2]; ++c)
+                R.symheap[(int64_t)(a[1] + c) * R.symheap_stride + L.pt] = __uint_as_float(ldw(L, a[0], (int)c));
+        break;
     case OP_RADIANS: h_unary<OP_RADIANS>(L, a); break;
     case OP_DEGREES: h_unary<OP_DEGREES>(L, a); break;
     case OP_ISNAN: stw(L, a[0], 0, isnan(ldf(L, a[1], 0, 0)) ? 1u : 0u); break;
@@ -3334,6 +3342,8 @@ __global__ void __launch_bounds__(256, 2) interp_kernel(const __grid_constant__ 
     R.textures = k.textures;
     R.ntextures = k.ntextures;
     R.max_iters = max_loop_iterations(*H);
+    R.symheap = k.symheap;
+    R.symheap_stride = k.symheap_stride;
 
     Lane L;
     L.pool = spool;

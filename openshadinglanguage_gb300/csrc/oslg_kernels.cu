@@ -79,7 +79,7 @@ void device_free(void* p) {
 
 int device_execute(DeviceState& ds, const ProgramHeader& hdr, const void* d_blob, int64_t npoints,
                    const oslg_shaderglobals& G, void* userdata, void* outputs, void* stream,
-                   const LaunchConfig& cfg, std::string* err, const int32_t* shadeindex) {
+                   const LaunchConfig& cfg, std::string* err, const LaunchExtras* ex) {
     if (npoints <= 0) return OSLG_OK;
     int rc = device_init(ds, err);
     if (rc != OSLG_OK) return rc;
@@ -128,7 +128,11 @@ int device_execute(DeviceState& ds, const ProgramHeader& hdr, const void* d_blob
     k.npoints = npoints;
     k.userdata = static_cast<char*>(userdata);
     k.outputs = static_cast<char*>(outputs);
-    k.shadeindex = shadeindex;
+    if (ex) {
+        k.shadeindex = ex->shadeindex;
+        k.symheap = ex->symheap;
+        k.symheap_stride = ex->symheap_stride;
+    }
     k.status = ds.d_status;
     k.G = G;
     k.textures = ds.d_textures;

@@ -413,6 +413,14 @@ struct Lowerer {
             op.imm[3] = sl.type.arraylen > 0 ? sl.type.arraylen : 4;  // closure records kept
             lops.push_back(op);
         }
+        for (const auto& r : g.retained) {  // find_symbol's symbols of this layer
+            if (r->layer != li || li < 0 || (stop_layer >= 0 && li > stop_layer)) continue;
+            const int msi = g.layers[(size_t)li].master->find_symbol(r->name);
+            if (msi < 0) return fail("retained symbol '" + r->name + "' is not in its layer");
+            LOp op; op.name = "__store_heap"; op.args = { sym_of(li, msi) };
+            op.imm[0] = r->plane; op.imm[1] = r->words;
+            lops.push_back(op);
+        }
         return true;
     }
 
@@ -452,7 +460,7 @@ struct Lowerer {
             "if", "for", "while", "dowhile", "break", "continue", "return", "exit", "nop",
             "useparam", "__layer_end", "__store_output", "__bsdf_eval", "__bsdf_sample", "__cl_store",
             "__cl_bsdf_eval", "__cl_bsdf_sample", "functioncall",
-            "functioncall_nr", "__fret", "__stores_end",
+            "functioncall_nr", "__fret", "__stores_end", "__store_heap",
             "printf", "warning", "error", "fprintf" };
         if (nowrite.count(op.name)) return false;
         if (op.name == "sincos") return i == 1 || i == 2;
@@ -806,7 +814,8 @@ struct Lowerer {
     bool fold_ret_div = false, fold_exit_div = false;
     std::set<int> fold_unsafe_ret, fold_unsafe_exit;
     static bool output_stage(const LOp& op) {
-        return op.name == "__store_output" || op.name == "__bsdf_eval" || op.name == "__bsdf_sample";
+        return op.name == "__store_output" || op.name == "__bsdf_eval" || op.name == "__bsdf_sample"
+            || op.name == "__store_heap";
     }
     bool range_has(int b, int e, const char* name) const {
         for (int q = b; q < e; ++q)
@@ -936,7 +945,7 @@ struct Lowerer {
     static bool has_effect(const LOp& op) {
         static const std::set<std::string> effects = {
             "if", "for", "while", "dowhile", "break", "continue", "return", "exit", "__layer_end", "__fret",
-            "__stores_end",
+            "__stores_end", "__store_heap",
             "__store_output", "__bsdf_eval", "__bsdf_sample", "printf", "warning", "error", "fprintf",
             "functioncall", "functioncall_nr", "useparam", "setmessage", "getmessage" };
         return effects.count(op.name) != 0;
@@ -1480,7 +1489,7 @@ struct Lowerer {
             case OP_LOOP_STEP: case OP_LOOP_END: case OP_JUMP: case OP_BREAK: case OP_CONTINUE: case OP_RETURN:
             case OP_EXIT: case OP_LAYER_END: case OP_STORE_OUTPUT: case OP_STORE_CLOSURE: case OP_BSDF_EVAL:
             case OP_BSDF_SAMPLE: case OP_CL_STORE: case OP_CL_BSDF_EVAL: case OP_CL_BSDF_SAMPLE:
-            case OP_FUNC_BEGIN: case OP_FUNC_RETURN: case OP_FUNC_END: case OP_STORES_END:
+            case OP_FUNC_BEGIN: case OP_FUNC_RETURN: case OP_FUNC_END: case OP_STORES_END: case OP_STORE_HEAP:
                 continue;
             default:
                 break;
@@ -2165,6 +2174,10 @@ struct Lowerer {
         if (n == "return") { emit(OP_RETURN, {}, n); return true; }
         if (n == "exit") { emit(OP_EXIT, {}, n); return true; }
         if (n == "__layer_end") { emit(OP_LAYER_END, {}, "layer"); return true; }
+        if (n == "__store_heap") {
+            emit(OP_STORE_HEAP, { a(0), (uint32_t)op.imm[0], (uint32_t)op.imm[1] }, "symbol");
+            return true;
+        }
         if (n == "__stores_end") { emit(OP_STORES_END, { (uint32_t)op.imm[0] }, "layer"); return true; }
         if (n == "__load_userdata") {
             int s = op.args[0];
@@ -2754,6 +2767,9 @@ struct Lowerer {
             if (s.referenced && s.derivs) h.flags |= 2u;
         h.max_depth = max_depth;
         h.max_loop_iterations = (uint32_t)ss.opts.max_loop_iterations;
+        out.retained_words = 0;
+        for (const auto& r : g.retained)
+            if (stop_layer < 0 || r->layer <= stop_layer) out.retained_words = std::max(out.retained_words, r->plane + r->words);
         h.flags |= program_tier() << 8;
         if (h.heap_slots > kArgOffsetMask) return fail("symbol heap too large");
         out.header = h;

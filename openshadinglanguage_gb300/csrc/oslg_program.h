@@ -162,6 +162,8 @@ enum OpCode : uint16_t {
     OP_FUNC_END,     // a1=depth a3=tag
     OP_STORES_END,   // after a layer's output stores: lanes that exited stay off from
                      // here; a0 = 1: the renderer-side section, every point
+    OP_STORE_HEAP,   // a0=symbol a1=first plane a2=words: a retained symbol's values
+                     // (find_symbol / symbol_address) into the launch's symbol planes
     OP_COUNT
 };
 

@@ -305,6 +305,7 @@ std::string spec_source(const CompiledGroup& cg, int min_blocks) {
     o << "    R.uses_closures = " << (uses_cl ? "true" : "false") << ";\n";
     o << "    R.G = &k.G;\n    R.userdata = k.userdata;\n    R.outputs = k.outputs;\n    R.status = k.status;\n";
     o << "    R.textures = k.textures;\n    R.ntextures = k.ntextures;\n";
+    o << "    R.symheap = k.symheap;\n    R.symheap_stride = k.symheap_stride;\n";
     o << "    float hreg[" << std::max(1u, sym) << "];\n";
     o << "    Lane L;\n    L.heap = hreg;\n    L.pool = kPool;\n    L.hs = 1;\n    L.li = 0;\n    L.pt = 0;\n";
     o << "    L.si = k.shadeindex;\n";
@@ -482,7 +483,7 @@ int build_and_load(const std::string& src, const std::string& csrc, const std::s
 
 int spec_launch(DeviceState& ds, const SpecKernel& sk, const CompiledGroup& cg, int64_t npoints,
                 const oslg_shaderglobals& G, void* userdata, void* outputs, void* stream, std::string* err,
-                int block_req, int pool_req, bool fill_unwritten, const int32_t* shadeindex) {
+                int block_req, int pool_req, bool fill_unwritten, const LaunchExtras* ex) {
     if (npoints <= 0) return OSLG_OK;
     int rc = device_init(ds, err);
     if (rc != OSLG_OK) return rc;
@@ -513,7 +514,11 @@ int spec_launch(DeviceState& ds, const SpecKernel& sk, const CompiledGroup& cg, 
     k.npoints = npoints;
     k.userdata = static_cast<char*>(userdata);
     k.outputs = static_cast<char*>(outputs);
-    k.shadeindex = shadeindex;
+    if (ex) {
+        k.shadeindex = ex->shadeindex;
+        k.symheap = ex->symheap;
+        k.symheap_stride = ex->symheap_stride;
+    }
     k.status = ds.d_status;
     k.G = G;
     k.textures = ds.d_textures;

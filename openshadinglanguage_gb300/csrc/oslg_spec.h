@@ -64,6 +64,6 @@ int spec_build(const CompiledGroup& cg, const std::string& csrc_dir, const std::
 // wrote (otherwise they keep what the buffer held).
 int spec_launch(DeviceState& ds, const SpecKernel& k, const CompiledGroup& cg, int64_t npoints,
                 const oslg_shaderglobals& G, void* userdata, void* outputs, void* stream, std::string* err,
-                int block = 0, int pool_smem = -1, bool fill_unwritten = false, const int32_t* shadeindex = nullptr);
+                int block = 0, int pool_smem = -1, bool fill_unwritten = false, const LaunchExtras* ex = nullptr);
 
 }  // namespace oslg

@@ -259,6 +259,41 @@ class ShadingSystem:
                                                        ctypes.c_void_p(output_ptr or None),
                                                        ctypes.c_void_p(stream or None)))
 
+    def find_symbol(self, group, symbolname, layername=None):
+        """ShadingSystem::find_symbol: a handle to the symbol; from now on
+        every device execution of the group keeps its final values."""
+        h = ctypes.c_void_p()
+        self._check(C.lib().oslg_find_symbol(self._h, group.handle, layername.encode() if layername else None,
+                                             symbolname.encode(), ctypes.byref(h)))
+        return h.value
+
+    def symbol_typedesc(self, sym):
+        t = C.TypeDescC()
+        self._check(C.lib().oslg_symbol_typedesc(ctypes.c_void_p(sym), ctypes.byref(t)))
+        return TypeDesc(t.basetype, t.aggregate, t.vecsemantics, t.arraylen)
+
+    def symbol_address(self, group, sym):
+        """ShadingSystem::symbol_address for the last device execution:
+        (device address, plane stride); word c of point i at
+        address[c * stride + i]."""
+        p, stride = ctypes.c_void_p(), ctypes.c_int64()
+        self._check(C.lib().oslg_symbol_address(self._h, group.handle, ctypes.c_void_p(sym), ctypes.byref(p),
+                                                ctypes.byref(stride)))
+        return p.value, stride.value
+
+    def symbol_array(self, group, sym, npoints):
+        """The symbol's values as a (words, npoints) device array view
+        (__cuda_array_interface__, e.g. for torch.as_tensor)."""
+        t = self.symbol_typedesc(sym)
+        ptr, stride = self.symbol_address(group, sym)
+        words = t.nfloats
+
+        class _View:
+            __cuda_array_interface__ = {"shape": (words, int(npoints)), "typestr": "<i4" if t.basetype == C.BASE_INT32
+                                        else "<f4", "data": (ptr, True), "version": 3,
+                                        "strides": (4 * stride, 4)}
+        return _View()
+
     def execute_layer(self, group, layername, npoints, globals_c, userdata_ptr=0, output_ptr=0, stream=0):
         """BatchedExecutor::execute_init + execute_layer(layername): the
         layers up to and including `layername`, over device points."""

@@ -1573,6 +1573,7 @@ struct Runner {
             case oslg::OP_FUNC_RETURN: pc = (int)a[2]; continue;
             case oslg::OP_NOP: case oslg::OP_ENDIF: case oslg::OP_LOOP_BEGIN: case oslg::OP_LOOP_STEP:
             case oslg::OP_LOOP_END: case oslg::OP_LAYER_END: case oslg::OP_FUNC_BEGIN: case oslg::OP_FUNC_END:
+            case oslg::OP_STORE_HEAP:  // retained symbols are the executor's bookkeeping
                 break;
             case oslg::OP_LOAD_GLOBAL: op_load_global(P, a, G); break;
             case oslg::OP_LOAD_USERDATA: {
