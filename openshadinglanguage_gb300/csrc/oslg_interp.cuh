@@ -1479,51 +1479,65 @@ static __device__ void h_gabor(const Lane& L, const uint32_t* a, const uint32_t*
     }
 }
 
-static __device__ void h_noise(const Lane& L, const uint32_t* a) {
-    uint32_t r = a[0], S = a[1], T = a[2], kw = a[3];
+// Operands of one noise evaluation, by value: the inputs as Dual2 (zero
+// derivatives when the op takes none), the raw period operands, results.
+struct NoiseIO {
+    D2 xs[4];
+    float per[4];
+    float res[3], rdx[3], rdy[3];
+};
+
+// The evaluation proper. A kernel specialized to many programs (the
+// persistent batch kernels) compiles it once, out of line, for every noise
+// kind at run time; elsewhere it is inlined and the kind word is a constant.
+#ifdef OSLG_SPEC_BATCH
+static __device__ __noinline__
+#else
+static __device__ __forceinline__
+#endif
+void noise_eval(uint32_t kw, int ns, bool has_t, NoiseIO& io) {
     int kind = (int)(kw & 15u);
     bool periodic = (kw & 16u) != 0;
     int dims = (int)((kw >> 5) & 7u);
     bool vec = (kw & 256u) != 0;
     bool derivs = (kw & 512u) != 0;
-    int ns = anc(S);
     int nc = vec ? 3 : 1;
-    float res[3], rdx[3] = { 0, 0, 0 }, rdy[3] = { 0, 0, 0 };
+    float* res = io.res;
+    float* rdx = io.rdx;
+    float* rdy = io.rdy;
+    OSLG_SPEC_UNROLL
+    for (int c = 0; c < 3; ++c) rdx[c] = rdy[c] = 0.0f;
     Hasher H;
     H.periodic = periodic;
     H.px = H.py = H.pz = H.pw = 1;
     if (periodic) {
-        uint32_t SP = a[4], TP = a[5];
         if (ns == 3) {
-            H.px = period_of(ldf(L, SP, 0, 0)); H.py = period_of(ldf(L, SP, 1, 0)); H.pz = period_of(ldf(L, SP, 2, 0));
-            if (dims == 4) H.pw = period_of(ldf(L, TP, 0, 0));
+            H.px = period_of(io.per[0]); H.py = period_of(io.per[1]); H.pz = period_of(io.per[2]);
+            if (dims == 4) H.pw = period_of(io.per[3]);
         } else {
-            H.px = period_of(ldf(L, SP, 0, 0));
-            if (dims == 2) H.py = period_of(ldf(L, TP, 0, 0));
+            H.px = period_of(io.per[0]);
+            if (dims == 2) H.py = period_of(io.per[1]);
         }
     }
+    (void)has_t;
     if (kind == NK_CELL || kind == NK_HASH) {
         float xs[4];
         OSLG_SPEC_UNROLL
-        for (int i = 0; i < ns; ++i) xs[i] = ldf(L, S, i, 0);
-        if (T != kNoArg) xs[ns] = ldf(L, T, 0, 0);
+        for (int i = 0; i < 4; ++i) xs[i] = io.xs[i].v;
         if (periodic) {
             if (ns == 3) {
-                xs[0] = pwrap(xs[0], ldf(L, a[4], 0, 0)); xs[1] = pwrap(xs[1], ldf(L, a[4], 1, 0));
-                xs[2] = pwrap(xs[2], ldf(L, a[4], 2, 0));
-                if (dims == 4) xs[3] = pwrap(xs[3], ldf(L, a[5], 0, 0));
+                xs[0] = pwrap(xs[0], io.per[0]); xs[1] = pwrap(xs[1], io.per[1]);
+                xs[2] = pwrap(xs[2], io.per[2]);
+                if (dims == 4) xs[3] = pwrap(xs[3], io.per[3]);
             } else {
-                xs[0] = pwrap(xs[0], ldf(L, a[4], 0, 0));
-                if (dims == 2) xs[1] = pwrap(xs[1], ldf(L, a[5], 0, 0));
+                xs[0] = pwrap(xs[0], io.per[0]);
+                if (dims == 2) xs[1] = pwrap(xs[1], io.per[1]);
             }
         }
         intnoise(kind == NK_CELL, dims, xs, nc, res);
     } else if (kind == NK_PERLIN || kind == NK_UPERLIN) {
         if (derivs) {
-            D2 xs[4];
-            OSLG_SPEC_UNROLL
-            for (int i = 0; i < ns; ++i) xs[i] = ldd(L, S, i);
-            if (T != kNoArg) xs[ns] = ldd(L, T, 0);
+            const D2* xs = io.xs;
             D2 o[3];
             if (vec) {
                 switch (dims) {
@@ -1548,8 +1562,7 @@ static __device__ void h_noise(const Lane& L, const uint32_t* a) {
         } else {
             float xs[4];
             OSLG_SPEC_UNROLL
-            for (int i = 0; i < ns; ++i) xs[i] = ldf(L, S, i, 0);
-            if (T != kNoArg) xs[ns] = ldf(L, T, 0, 0);
+            for (int i = 0; i < 4; ++i) xs[i] = io.xs[i].v;
             if (vec) {
                 switch (dims) {
                 case 1: perlin1<float, 3>(H, xs[0], res); break;
@@ -1570,10 +1583,7 @@ static __device__ void h_noise(const Lane& L, const uint32_t* a) {
                 for (int c = 0; c < nc; ++c) res[c] = 0.5f * (res[c] + 1.0f);
         }
     } else if (kind == NK_SIMPLEX || kind == NK_USIMPLEX) {
-        D2 xs[4];
-        OSLG_SPEC_UNROLL
-        for (int i = 0; i < ns; ++i) xs[i] = ldd(L, S, i);
-        if (T != kNoArg) xs[ns] = ldd(L, T, 0);
+        const D2* xs = io.xs;
         OSLG_SPEC_UNROLL
         for (int c = 0; c < nc; ++c) {
             float g[4] = { 0, 0, 0, 0 };
@@ -1600,16 +1610,43 @@ static __device__ void h_noise(const Lane& L, const uint32_t* a) {
         OSLG_SPEC_UNROLL
         for (int c = 0; c < nc; ++c) res[c] = 0.0f;
     }
+}
+
+static __device__ void h_noise(const Lane& L, const uint32_t* a) {
+    const uint32_t r = a[0], S = a[1], T = a[2], kw = a[3];
+    const bool periodic = (kw & 16u) != 0;
+    const int dims = (int)((kw >> 5) & 7u);
+    const bool vec = (kw & 256u) != 0;
+    const bool derivs = (kw & 512u) != 0;
+    const int ns = anc(S);
+    const int nc = vec ? 3 : 1;
+    NoiseIO io;
+    OSLG_SPEC_UNROLL
+    for (int i = 0; i < 4; ++i) { io.xs[i] = d2c(0.0f); io.per[i] = 1.0f; }
+    OSLG_SPEC_UNROLL
+    for (int i = 0; i < ns; ++i) io.xs[i] = derivs ? ldd(L, S, i) : d2c(ldf(L, S, i, 0));
+    if (T != kNoArg) io.xs[ns] = derivs ? ldd(L, T, 0) : d2c(ldf(L, T, 0, 0));
+    if (periodic) {
+        const uint32_t SP = a[4], TP = a[5];
+        if (ns == 3) {
+            io.per[0] = ldf(L, SP, 0, 0); io.per[1] = ldf(L, SP, 1, 0); io.per[2] = ldf(L, SP, 2, 0);
+            if (dims == 4) io.per[3] = ldf(L, TP, 0, 0);
+        } else {
+            io.per[0] = ldf(L, SP, 0, 0);
+            if (dims == 2) io.per[1] = ldf(L, TP, 0, 0);
+        }
+    }
+    noise_eval(kw, ns, T != kNoArg, io);
     // float result from triple request or vice versa is handled by lowering;
     // scalar noise into a triple symbol broadcasts
     int rn = anc(r);
     OSLG_SPEC_UNROLL
     for (int c = 0; c < rn; ++c) {
         int sc = nc == 1 ? 0 : c;
-        stf(L, r, c, res[sc]);
+        stf(L, r, c, io.res[sc]);
         if (ader(r)) {
-            stf(L, r, rn + c, rdx[sc]);
-            stf(L, r, 2 * rn + c, rdy[sc]);
+            stf(L, r, rn + c, io.rdx[sc]);
+            stf(L, r, 2 * rn + c, io.rdy[sc]);
         }
     }
 }

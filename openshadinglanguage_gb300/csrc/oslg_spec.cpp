@@ -338,10 +338,13 @@ std::string spec_source(const CompiledGroup& cg, int min_blocks) {
         o << "                if (flags[w]) gout[w] = sw[w];\n";
         o << "                else if (fill_unwritten) gout[w] = 0u;\n";
         o << "        } else {  // each point's record goes to its shadeindex\n";
+        // 32-bit word indices (a tile is at most 256 records): division by
+        // the constant record size stays cheap and adds no register pressure
         o << "            const int32_t* si = k.shadeindex + tile * blockDim.x;\n";
-        o << "            for (int64_t w = threadIdx.x; w < npt * (int64_t)(rec / 4u); w += blockDim.x) {\n";
-        o << "                const int64_t p = w / (int64_t)(rec / 4u), q = w - p * (int64_t)(rec / 4u);\n";
-        o << "                uint32_t* dst = reinterpret_cast<uint32_t*>(k.outputs + (int64_t)si[p] * (int64_t)rec) + q;\n";
+        o << "            const uint32_t nw = (uint32_t)npt * (uint32_t)(rec / 4u);\n";
+        o << "            for (uint32_t w = threadIdx.x; w < nw; w += blockDim.x) {\n";
+        o << "                const uint32_t p = w / (uint32_t)(rec / 4u), q = w - p * (uint32_t)(rec / 4u);\n";
+        o << "                uint32_t* dst = reinterpret_cast<uint32_t*>(k.outputs + (int64_t)__ldg(si + p) * (int64_t)rec) + q;\n";
         o << "                if (flags[w]) *dst = sw[w];\n";
         o << "                else if (fill_unwritten) *dst = 0u;\n";
         o << "            }\n";
@@ -365,7 +368,7 @@ std::string spec_batch_source(const std::vector<const CompiledGroup*>& cases) {
     }
     std::ostringstream o;
     o << "// generated: persistent batch kernel specialized to " << cases.size() << " lowered programs\n";
-    o << "#define OSLG_SPEC 1\n";
+    o << "#define OSLG_SPEC 1\n#define OSLG_SPEC_BATCH 1\n";
     emit_bounds(o, B);
     o << "#include \"oslg_interp.cuh\"\n\nnamespace {\n";
     o << "using namespace oslg;\nusing namespace oslg::dev;\n\n";
