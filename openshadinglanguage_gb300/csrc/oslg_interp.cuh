@@ -3133,6 +3133,15 @@ __device__ __forceinline__ void exec_op(const RunCtx& R, Lane& L, uint32_t code,
     }
 }
 
+// One op whose code is known at compile time (specialized kernels): one
+// instantiation per opcode, in which the dispatch is already resolved, so
+// a program's call sites inline only their own handler. `nx` is the
+// following operand carrier (or null).
+template <int TIER, uint32_t CODE>
+__device__ __forceinline__ void exec_op_c(const RunCtx& R, Lane& L, const uint32_t* a, const Op* nx) {
+    exec_op<TIER>(R, L, CODE, a, [nx]() -> const Op* { return nx; });
+}
+
 // Run the whole program for one point per thread (L.pt; lanes past npoints
 // take part in the warp-uniform walk with no active bits). The mask ops
 // here are the ctl_* functions above written out over plain locals (the

@@ -242,11 +242,9 @@ void emit_body(std::ostringstream& o, const ProgView& v, const std::string& sfx)
                     put_args(o, x.a);
                     o << "}";
                 }
-                o << "};\n        if (C.actm) exec_op<7>(R, L, " << op.code
-                  << "u, a, [&]() -> const Op* { return nx; });\n";
+                o << "};\n        if (C.actm) exec_op_c<7, " << op.code << "u>(R, L, a, nx);\n";
             } else {
-                o << "        if (C.actm) exec_op<7>(R, L, " << op.code
-                  << "u, a, []() -> const Op* { return nullptr; });\n";
+                o << "        if (C.actm) exec_op_c<7, " << op.code << "u>(R, L, a, nullptr);\n";
             }
             break;
         }
