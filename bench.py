@@ -261,55 +261,80 @@ def bench_batching(torch, og, reps=5, jit=1):
            "autotuned": {k: best[k] for k in ("block", "points_per_thread", "heap_smem", "grid")},
            "candidates": len(cands), "launches_per_step": {"plain": len(reqs), "persistent": 1}}
     if jit:
-        # the same requests through a batch specialized to the 64 programs
+        # the same requests with every group specialized (the reference's
+        # per-group JIT): launched per group, and as one persistent kernel
+        # specialized to the 64 programs
         ssj = og.ShadingSystem()
         ssj.attribute("jit", 1)
+        gj = [workloads.c3_group(ssj, name, oso) for (name, oso, _, _) in specs]
+        t0 = time.perf_counter()
+        ssj.jit_groups(gj)
+        t_groups = time.perf_counter() - t0
+        jouts = [torch.zeros(npts * workloads.C3_REC, device="cuda") for (_, _, npts, _) in specs]
+
+        def plain_jit():
+            for k, g in enumerate(gj):
+                ssj.execute_batch(g, specs[k][2], reqs[k][2], 0, jouts[k].data_ptr(), sh)
+
+        t_plain_jit = timed(plain_jit)
+        torch.cuda.synchronize()
+
+        def same_as_plain():
+            return all(bool(np.all((a == bb) | (np.isnan(a) & np.isnan(bb))))
+                       for a, bb in zip(ref, (o.cpu().numpy() for o in jouts)))
+
+        same_plain_jit = same_as_plain()
+        for o in jouts:
+            o.zero_()
         bj = ssj.batch()
-        jouts = []
-        for k, (name, oso, npts, _) in enumerate(specs):
-            g = workloads.c3_group(ssj, name, oso)
-            o = torch.zeros(npts * workloads.C3_REC, device="cuda")
-            jouts.append(o)
-            bj.add(g, npts, reqs[k][2], 0, o.data_ptr())
+        for k, g in enumerate(gj):
+            bj.add(g, specs[k][2], reqs[k][2], 0, jouts[k].data_ptr())
         t0 = time.perf_counter()
         bestj, _ = bj.autotune(sh, reps=2)
         t_build = time.perf_counter() - t0
         bj.set_launch(block=bestj["block"], heap_smem=bestj["heap_smem"], use_graph=True, points_per_thread=1)
         t_jit = timed(lambda: bj.execute(sh))
         torch.cuda.synchronize()
-        same = all(bool(np.all((a == bb) | (np.isnan(a) & np.isnan(bb))))
-                   for a, bb in zip(ref, (o.cpu().numpy() for o in jouts)))
+        same = same_as_plain()
         bj.close()
-        out.update({"persistent_jit_ms": t_jit, "persistent_jit_mpts": total / t_jit / 1e3,
-                    "jit_speedup_vs_plain": t_plain / t_jit, "jit_build_and_tune_s": t_build,
-                    "jit_block": bestj["block"], "jit_same_bits_as_plain": same})
+        out.update({"plain_jit_ms": t_plain_jit, "plain_jit_mpts": total / t_plain_jit / 1e3,
+                    "persistent_jit_ms": t_jit, "persistent_jit_mpts": total / t_jit / 1e3,
+                    "jit_speedup_vs_plain": t_plain / t_jit,
+                    "persistent_jit_over_plain_jit": t_plain_jit / t_jit,
+                    "jit_groups_build_s": t_groups, "jit_batch_build_and_tune_s": t_build,
+                    "jit_block": bestj["block"], "jit_same_bits_as_plain": same and same_plain_jit})
     out["cpu"] = c3_cpu_baseline(og, workloads, specs)
     return out
 
 
-def c3_cpu_baseline(og, workloads, specs, frac=8):
+def c3_cpu_baseline(og, workloads, specs, frac=2, min_s=2.0):
     """The oracle over every group's first n/frac points (at least 2000) on
-    all host threads: points per second over the sampled points."""
+    all host threads, repeated until at least min_s seconds of work: points
+    per second over the sampled points."""
     from helpers import oracle_run
     from oracle.build import build as build_oracle
     build_oracle()
     ss = og.ShadingSystem()
-    pts, secs = 0, 0.0
+    work = []
     for k, (name, oso, npts, _) in enumerate(specs):
         g = workloads.c3_group(ss, name, oso)
         m = min(npts, max(2000, npts // frac))
         P = np.ascontiguousarray(workloads.c3_points(k, npts)[:, :m])
-        buf = np.zeros((m, workloads.C3_REC), np.float32)
-        blob = g.program_bytes()
-        t0 = time.perf_counter()
-        oracle_run(blob, m, og.make_globals(P=P), buf)
-        secs += time.perf_counter() - t0
-        pts += m
+        work.append((g.program_bytes(), m, og.make_globals(P=P), P, np.zeros((m, workloads.C3_REC), np.float32)))
+    pts, secs, rounds = 0, 0.0, 0
+    while secs < min_s:
+        for blob, m, G, _, buf in work:
+            t0 = time.perf_counter()
+            oracle_run(blob, m, G, buf)
+            secs += time.perf_counter() - t0
+            pts += m
+        rounds += 1
     return {"mpts_per_s": pts / secs / 1e6, "points": pts, "seconds": secs, "threads": os.cpu_count(),
-            "kind": "port", "sample": "first n/%d points (at least 2000) of each of the 64 groups" % frac}
+            "kind": "port", "sample": "first n/%d points (at least 2000) of each of the 64 groups, %d rounds"
+            % (frac, rounds)}
 
 
-def bench_serving(torch, og, nreq=600):
+def bench_serving(torch, og, nreq=600, jit=0):
     """Poisson request stream over the 64 groups (point counts log-uniform
     in [256, 262144]) at 10/50/90/100% of the server's measured peak, served
     with continuous batching and by the plain executor per request."""
@@ -335,11 +360,32 @@ def bench_serving(torch, og, nreq=600):
             "plain": {k: p[k] for k in ("p50_ms", "p99_ms", "throughput_mpts")}}
     st = srv.stats()
     srv.close()
-    return {"requests": nreq, "points": sum(r.n for r in reqs), "hbm_budget_gb": 40,
-            "peak_rps": peak_rps, "served_peak_mpts": peak["throughput_mpts"],
-            "plain_peak_mpts": plain_peak["throughput_mpts"], "loads": loads,
-            "arena_high_water_mb": st["arena_high_water"] / 2 ** 20, "waves": st["waves"],
-            "latency": "arrival to outputs in host memory (pinned), host monotonic clock"}
+    out = {"requests": nreq, "points": sum(r.n for r in reqs), "hbm_budget_gb": 40,
+           "peak_rps": peak_rps, "served_peak_mpts": peak["throughput_mpts"],
+           "plain_peak_mpts": plain_peak["throughput_mpts"], "loads": loads,
+           "arena_high_water_mb": st["arena_high_water"] / 2 ** 20, "waves": st["waves"],
+           "latency": "arrival to outputs in host memory (pinned), host monotonic clock"}
+    if jit:
+        # waves on one kernel specialized to the 64 programs (the same
+        # programs as the batching section: its cached kernel)
+        ssj = og.ShadingSystem()
+        ssj.attribute("jit", 1)
+        gj = [workloads.c3_group(ssj, name, oso) for (name, oso, _, _) in workloads.c3_specs()]
+        jreqs = serving.make_requests(torch, gj, nreq)
+        srvj = ssj.server(budget_bytes=40 << 30, streams=3)
+        for g in gj:
+            srvj.register(g)
+        t0 = time.perf_counter()
+        serving.run_server(srvj, jreqs[:50])
+        t_build = time.perf_counter() - t0
+        pj = serving.run_server(srvj, jreqs)
+        aj = serving.run_server(srvj, jreqs, rate_rps=0.9 * peak_rps)
+        srvj.close()
+        out.update({"served_jit_peak_mpts": pj["throughput_mpts"],
+                    "served_jit_over_plain_peak": pj["throughput_mpts"] / plain_peak["throughput_mpts"],
+                    "served_jit_at_90pct": {k: aj[k] for k in ("p50_ms", "p99_ms", "throughput_mpts")},
+                    "served_jit_first_wave_s": t_build})
+    return out
 
 
 def bench_wavefront(torch, og, frames=3, cpu_step=97, size=None, jit=1):
@@ -507,7 +553,8 @@ def main():
                     help="run only this measurement section and print it as one JSON line")
     ap.add_argument("--wf-size", default=None, help="wavefront frame WxHxSPP (default 1920x1080x4)")
     ap.add_argument("--batch-jit", type=int, default=0,
-                    help="batching section: also time the persistent kernel specialized to the 64 programs")
+                    help="batching and serving sections: also time every group specialized (per group, "
+                         "one persistent kernel for the 64 programs, and served waves on that kernel)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.section:
@@ -517,7 +564,7 @@ def main():
         build_native()
         torch.cuda.set_device(0)
         fn = {"batching": lambda: bench_batching(torch, og, jit=args.batch_jit),
-              "serving": lambda: bench_serving(torch, og),
+              "serving": lambda: bench_serving(torch, og, jit=args.batch_jit),
               "wavefront": lambda: bench_wavefront(torch, og, size=args.wf_size, jit=args.jit),
               "texture": lambda: bench_texture(torch, og)}[args.section]
         print(json.dumps({"section": args.section, args.section: fn()}))
@@ -680,14 +727,16 @@ def main():
     }
     if not args.no_extras and world == 1:
         line["batching"] = bench_batching(torch, og, jit=args.batch_jit)
-        line["serving"] = bench_serving(torch, og)
+        line["serving"] = bench_serving(torch, og, jit=args.batch_jit)
         line["wavefront"] = bench_wavefront(torch, og, jit=args.jit)
         line["texture"] = bench_texture(torch, og)
         # the systems targets as top-level keys, ahead of the long sections
         b, sv = line["batching"], line["serving"]
         summary = {"speedup_vs_plain": b["speedup_vs_plain"],
                    "jit_speedup_vs_plain": b.get("jit_speedup_vs_plain"),
-                   "served_over_plain_peak": sv["served_peak_mpts"] / sv["plain_peak_mpts"]}
+                   "persistent_jit_over_plain_jit": b.get("persistent_jit_over_plain_jit"),
+                   "served_over_plain_peak": sv["served_peak_mpts"] / sv["plain_peak_mpts"],
+                   "served_jit_over_plain_peak": sv.get("served_jit_over_plain_peak")}
         keys = list(line)
         at = keys.index("ms_per_step") + 1
         line = dict([(k, line[k]) for k in keys[:at]] + list(summary.items()) + [(k, line[k]) for k in keys[at:]])

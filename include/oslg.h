@@ -207,6 +207,11 @@ int oslg_group_bsdf_sample(oslg_system* sys, oslg_group* group, const char* clos
 /* ShadingSystem::optimize_group (oslexec.h:1093) + BatchedExecutor::jit_group
  * (oslexec.h:993): lowers the group to a device op program and uploads it. */
 int oslg_optimize_group(oslg_system* sys, oslg_group* group);
+/* BatchedExecutor<W>::jit_group / jit_all_groups (oslexec.h:986-992): lower
+ * and upload `groups` and, with attribute "jit", build their specialized
+ * kernels on `nthreads` threads (0: every hardware thread), so that first
+ * launches do not wait for compiles. */
+int oslg_jit_groups(oslg_system* sys, oslg_group* const* groups, int ngroups, int nthreads);
 /* BatchedExecutor::execute over HOST buffers (the reference's execute reads
  * and writes host memory). Shader-global fields with data != NULL are host
  * SoA planes (plane_stride apart); host_userdata and host_outputs hold one
@@ -460,7 +465,10 @@ typedef struct oslg_server_stats {
     int in_flight_waves, pending;
 } oslg_server_stats;
 
-/* opts NULL: defaults. Starts the worker thread. */
+/* opts NULL: defaults. Starts the worker thread. With the system's
+ * attribute "jit" set, waves run one persistent kernel specialized to the
+ * resident programs (built by the worker when that set changes; the same
+ * set gives the same kernel as a jit batch); otherwise the interpreter. */
 int oslg_server_create(oslg_system* sys, const oslg_server_options* opts, oslg_server** out);
 /* Finishes every submitted request, then stops. */
 int oslg_server_destroy(oslg_server* server);

@@ -129,6 +129,7 @@ _EXPORTS = {
     "oslg_execute_batch_indexed": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                                                   ctypes.POINTER(ShaderGlobalsC), ctypes.c_void_p, ctypes.c_void_p,
                                                   ctypes.c_void_p, ctypes.c_void_p]),
+    "oslg_jit_groups": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_int]),
     "oslg_find_symbol": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p,
                                         ctypes.POINTER(ctypes.c_void_p)]),
     "oslg_symbol_typedesc": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(TypeDescC)]),

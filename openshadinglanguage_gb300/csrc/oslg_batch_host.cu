@@ -205,13 +205,11 @@ int BatchExecutor::build_jit(DeviceState& ds, std::string* err) {
     std::stable_sort(order.begin(), order.end(),
                      [&](int a, int b) { return entries_[a].cost > entries_[b].cost; });
     std::vector<const CompiledGroup*> cases;
+    for (const BatchEntry& e : entries_) cases.push_back(e.cg);
+    canonical_cases(cases);
     std::vector<int> case_of(entries_.size(), 0);
-    for (int i : order) {
-        const CompiledGroup* cg = entries_[i].cg;
-        auto it = std::find(cases.begin(), cases.end(), cg);
-        case_of[i] = (int)(it - cases.begin());
-        if (it == cases.end()) cases.push_back(cg);
-    }
+    for (size_t i = 0; i < entries_.size(); ++i)
+        case_of[i] = (int)(std::find(cases.begin(), cases.end(), entries_[i].cg) - cases.begin());
     if (!spec_ || cases != spec_cases_) {
         if (jit_csrc_.empty()) {
             if (err) *err = "batch: no source directory for specialized kernels";

@@ -6,6 +6,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
+#include <thread>
 #include <cmath>
 #include <cstring>
 #include <exception>
@@ -475,7 +477,7 @@ static std::string library_dir() {
 
 static int upload_textures(oslg_system* sys);
 
-static int ensure_compiled(oslg_system* sys, oslg_group* group, bool upload) {
+static int ensure_compiled(oslg_system* sys, oslg_group* group, bool upload, bool allow_spec = true) {
     ShaderGroup& g = group->g;
     if (!g.ended) return fail(sys, OSLG_ERR_STATE, "group used before ShaderGroupEnd");
     if (upload && sys->textures_dirty) {
@@ -497,7 +499,7 @@ static int ensure_compiled(oslg_system* sys, oslg_group* group, bool upload) {
         if (rc != OSLG_OK) return fail(sys, rc, err);
         g.compiled->device = sys->dev.device;
     }
-    if (upload && sys->jit && !g.compiled->spec) {
+    if (upload && allow_spec && sys->jit && !g.compiled->spec) {
         auto sk = std::make_shared<SpecKernel>();
         std::string err;
         const std::string dir = library_dir();
@@ -506,6 +508,48 @@ static int ensure_compiled(oslg_system* sys, oslg_group* group, bool upload) {
         g.compiled->spec = sk;
     }
     return OSLG_OK;
+}
+
+int oslg_jit_groups(oslg_system* sys, oslg_group* const* groups, int ngroups, int nthreads) {
+    if (!sys || ngroups < 0 || (ngroups > 0 && !groups)) return OSLG_ERR_ARG;
+    return guarded(sys, [&]() {
+        // lower and upload every group here, then compile the specialized
+        // kernels on worker threads (each build is one nvcc process)
+        for (int i = 0; i < ngroups; ++i) {
+            if (!groups[i]) return fail(sys, OSLG_ERR_ARG, "null group");
+            int rc = ensure_compiled(sys, groups[i], true, false);
+            if (rc != OSLG_OK) return rc;
+        }
+        if (!sys->jit) return OSLG_OK;
+        const std::string dir = library_dir();
+        std::atomic<int> next{ 0 };
+        std::mutex emu;
+        std::string first_err;
+        auto work = [&]() {
+            for (int i = next++; i < ngroups; i = next++) {
+                ShaderGroup& g = groups[i]->g;
+                std::lock_guard<std::mutex> lock(g.mutex);
+                if (!g.compiled || g.compiled->spec) continue;
+                auto sk = std::make_shared<SpecKernel>();
+                std::string err;
+                if (spec_build(*g.compiled, dir + "/csrc", dir + "/_build/jit", sk.get(), &err, sys->jit_min_blocks) !=
+                    OSLG_OK) {
+                    std::lock_guard<std::mutex> el(emu);
+                    if (first_err.empty()) first_err = "group '" + g.name + "': " + err;
+                    continue;
+                }
+                g.compiled->spec = sk;
+            }
+        };
+        int nt = nthreads > 0 ? nthreads : (int)std::max(1u, std::thread::hardware_concurrency());
+        nt = std::min(nt, std::max(1, ngroups));
+        std::vector<std::thread> pool;
+        for (int t = 1; t < nt; ++t) pool.emplace_back(work);
+        work();
+        for (std::thread& t : pool) t.join();
+        if (!first_err.empty()) return fail(sys, OSLG_ERR_LOWER, first_err);
+        return OSLG_OK;
+    });
 }
 
 int oslg_optimize_group(oslg_system* sys, oslg_group* group) {
@@ -1282,6 +1326,10 @@ int oslg_server_create(oslg_system* sys, const oslg_server_options* opts, oslg_s
         }
         if (o.points_per_thread != 1 && o.points_per_thread != 2 && o.points_per_thread != 4)
             return fail(sys, OSLG_ERR_ARG, "points_per_thread must be 1, 2 or 4");
+        if (sys->jit) {  // waves run a kernel specialized to the resident programs
+            o.jit_csrc = library_dir() + "/csrc";
+            o.jit_cache = library_dir() + "/_build/jit";
+        }
         std::unique_ptr<oslg_server> s(new oslg_server);
         s->sys = sys;
         s->srv.reset(new ShadingServer(sys->dev, o));

@@ -34,6 +34,8 @@ const oslg_field* fields(const oslg_shaderglobals& G) { return &G.P; }
 // heap slots need at most this many per program in the worst case the
 // scratch reserve is sized for (larger programs grow the reserve on use)
 const uint32_t kReserveSlots = 256;
+// threads per CTA of a specialized wave (one point per thread)
+const int kSpecWaveBlock = 256;
 }  // namespace
 
 // ---- arena ---------------------------------------------------------------------------
@@ -279,9 +281,37 @@ void ShadingServer::on_wave_done(void* p) {
     self->cv_.notify_all();
 }
 
+// The specialized wave kernel for the resident programs (canonical order:
+// the same set gives the same kernel as the batch executor's).
+int ShadingServer::ensure_spec(std::string* err) {
+    std::vector<const CompiledGroup*> cases;
+    {
+        std::lock_guard<std::mutex> lk(mu_);
+        for (auto& kv : programs_) cases.push_back(kv.first);
+    }
+    canonical_cases(cases);
+    if (!spec_kernels_.empty() && cases == spec_cases_) return OSLG_OK;
+    auto k = std::make_unique<SpecBatchKernel>();
+    int rc = spec_batch_build(cases, opt_.jit_csrc, opt_.jit_cache, k.get(), err);
+    if (rc != OSLG_OK) return rc;
+    int per_sm = 0;
+    if (!ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k->kernel, kSpecWaveBlock, 0), err, "occupancy"))
+        return OSLG_ERR_CUDA;
+    spec_grid_ = ds_.sm_count * std::max(1, per_sm);
+    spec_kernels_.push_back(std::move(k));
+    spec_cases_ = cases;
+    return OSLG_OK;
+}
+
 int ShadingServer::launch_wave(Slot& s, std::vector<Request*>& wave, std::string* err) {
     cudaStream_t st = static_cast<cudaStream_t>(s.stream);
-    const int tile = opt_.block * opt_.points_per_thread;
+    const bool jit = !opt_.jit_csrc.empty();
+    if (jit) {
+        int rc = ensure_spec(err);
+        if (rc != OSLG_OK) return rc;
+    }
+    // specialized waves: one point per thread, closure pools in the slot's scratch
+    const int tile = jit ? kSpecWaveBlock : opt_.block * opt_.points_per_thread;
     const int maxt = opt_.block > 256 ? 512 : 256;
     uint32_t slots = 0, pbytes = 0;
     for (Request* r : wave) {
@@ -289,7 +319,8 @@ int ShadingServer::launch_wave(Slot& s, std::vector<Request*>& wave, std::string
         uint32_t pb = r->cg->header.nops * (uint32_t)sizeof(Op) + ((r->cg->header.nconst + 3u) & ~3u) * 4u;
         pbytes = std::max(pbytes, (pb + 15u) & ~15u);
     }
-    const size_t heap_need = (size_t)grid_ * slots * tile * sizeof(float);
+    const size_t heap_need = jit ? (size_t)spec_grid_ * spec_kernels_.back()->pool_slots * tile * sizeof(float)
+                                 : (size_t)grid_ * slots * tile * sizeof(float);
     if (heap_need > s.heap_bytes) {
         // a program larger than the reserve: grow this slot's scratch heap
         if (!ok(cudaStreamSynchronize(st), err, "sync")) return OSLG_ERR_CUDA;
@@ -359,6 +390,7 @@ int ShadingServer::launch_wave(Slot& s, std::vector<Request*>& wave, std::string
         J.userdata = nullptr;
         J.outputs = d_out;
         J.G = r->dG;
+        J.spec_case = jit ? (int)(std::find(spec_cases_.begin(), spec_cases_.end(), r->cg) - spec_cases_.begin()) : 0;
         const int64_t tiles = (r->n + tile - 1) / tile;
         for (int64_t t = 0; t < tiles; ++t) s.h_items[nitems++] = make_uint2((unsigned)j, (unsigned)t);
     }
@@ -380,9 +412,17 @@ int ShadingServer::launch_wave(Slot& s, std::vector<Request*>& wave, std::string
     a.ntextures = ds_.ntextures;
     a.prog_bytes = pbytes;
     a.heap_slots = slots;
-    if (!ok((cudaError_t)batch_variant_launch(maxt, opt_.points_per_thread, false, (unsigned)grid_,
-                                              (unsigned)opt_.block, pbytes, st, a),
-            err, "wave launch"))
+    if (jit) {
+        a.heap_slots = spec_kernels_.back()->pool_slots;
+        int pool_smem = 0;
+        void* kargs[] = { &a, &pool_smem };
+        if (!ok(cudaLaunchKernel(spec_kernels_.back()->kernel, dim3((unsigned)spec_grid_), dim3(kSpecWaveBlock), kargs,
+                                 0, st),
+                err, "specialized wave launch"))
+            return OSLG_ERR_CUDA;
+    } else if (!ok((cudaError_t)batch_variant_launch(maxt, opt_.points_per_thread, false, (unsigned)grid_,
+                                                     (unsigned)opt_.block, pbytes, st, a),
+                   err, "wave launch"))
         return OSLG_ERR_CUDA;
     for (auto& pr : order) {
         Request* r = pr.second;

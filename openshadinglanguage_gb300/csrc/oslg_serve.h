@@ -23,6 +23,9 @@
 #include <vector>
 
 #include "oslg_batch.h"
+#include "oslg_spec.h"
+
+#include <memory>
 
 namespace oslg {
 
@@ -53,6 +56,10 @@ struct ServerOptions {
     int64_t max_wave_points = 8 << 20;
     int max_wave_requests = 512;
     size_t arena_bytes = 0;  // request memory; 0: what the budget leaves after the scratch heaps
+    // waves run one persistent kernel specialized to the resident programs
+    // (built when the set of programs changes) when these name the
+    // interpreter headers and the kernel cache; empty: the interpreter
+    std::string jit_csrc, jit_cache;
 };
 
 struct RequestStats {
@@ -140,6 +147,12 @@ private:
     uint32_t prog_bytes_ = 0;     // largest program (shared-memory staging)
     int grid_ = 0, per_sm_ = 0;
     size_t shmem_ = 0;
+    // specialized waves: the kernel for spec_cases_ (every kernel built stays
+    // loaded until the server stops: waves in flight may use an older one)
+    int ensure_spec(std::string* err);
+    std::vector<std::unique_ptr<SpecBatchKernel>> spec_kernels_;
+    std::vector<const CompiledGroup*> spec_cases_;
+    int spec_grid_ = 0;
     ServerStats stats_{};
     std::string worker_error_;
 };

@@ -357,6 +357,16 @@ SpecBatchKernel::~SpecBatchKernel() {
     if (library) cudaLibraryUnload(static_cast<cudaLibrary_t>(library));
 }
 
+void canonical_cases(std::vector<const CompiledGroup*>& cases) {
+    std::sort(cases.begin(), cases.end());
+    cases.erase(std::unique(cases.begin(), cases.end()), cases.end());
+    auto key = [](const CompiledGroup* cg) {
+        return std::make_pair(fnv1a(std::string(cg->blob.begin(), cg->blob.end())), cg->blob.size());
+    };
+    std::stable_sort(cases.begin(), cases.end(),
+                     [&](const CompiledGroup* a, const CompiledGroup* b) { return key(a) < key(b); });
+}
+
 std::string spec_batch_source(const std::vector<const CompiledGroup*>& cases) {
     Bounds B;
     std::vector<ProgView> vs;

@@ -49,6 +49,10 @@ struct SpecBatchKernel {
     ~SpecBatchKernel();
 };
 std::string spec_batch_source(const std::vector<const CompiledGroup*>& cases);
+// Distinct programs in a canonical order (by program content), so that the
+// same set of programs gives the same batch kernel source, and cubin, in
+// every executor.
+void canonical_cases(std::vector<const CompiledGroup*>& cases);
 int spec_batch_build(const std::vector<const CompiledGroup*>& cases, const std::string& csrc_dir,
                      const std::string& cache_dir, SpecBatchKernel* out, std::string* err);
 

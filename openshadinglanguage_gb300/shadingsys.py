@@ -259,6 +259,12 @@ class ShadingSystem:
                                                        ctypes.c_void_p(output_ptr or None),
                                                        ctypes.c_void_p(stream or None)))
 
+    def jit_groups(self, groups, nthreads=0):
+        """BatchedExecutor::jit_all_groups: lower and upload the groups and,
+        with attribute jit, build their specialized kernels in parallel."""
+        arr = (ctypes.c_void_p * max(1, len(groups)))(*[g.handle for g in groups])
+        self._check(C.lib().oslg_jit_groups(self._h, arr, len(groups), int(nthreads)))
+
     def find_symbol(self, group, symbolname, layername=None):
         """ShadingSystem::find_symbol: a handle to the symbol; from now on
         every device execution of the group keeps its final values."""

@@ -171,3 +171,19 @@ def test_batch_with_closure_group_and_empty_requests():
     for r, o, p in zip(reqs, outs, plain):
         assert same(o.cpu().numpy(), p), r.name
     b.close()
+
+
+def test_jit_groups_builds_every_kernel(c3):
+    """jit_groups (BatchedExecutor::jit_all_groups) builds the specialized
+    kernels of several groups on worker threads; each group then runs its
+    own kernel with the plain interpreter's bits."""
+    ss, reqs, plain = c3
+    pick = list(range(3, len(reqs), 9))
+    ssj = og.ShadingSystem()
+    ssj.attribute("jit", 1)
+    jreqs = c3_requests(ssj, groups={reqs[i].k for i in pick})
+    ssj.jit_groups([r.g for r in jreqs], nthreads=4)
+    assert all(r.g.is_specialized() for r in jreqs)
+    got = run_plain(ssj, jreqs)
+    for i, r, a in zip(pick, jreqs, got):
+        assert same(a, plain[i]), r.name

@@ -158,3 +158,24 @@ def test_failed_request_fails_alone_in_a_mixed_wave(setup):
     assert s["failed"] == 1 and s["completed"] == len(part)
     srv.close()
     assert ss.device_status() == 0
+
+
+def test_jit_server_equals_plain(setup):
+    """With the system attribute "jit", waves run one kernel specialized to
+    the resident programs: the same outputs as the plain interpreter."""
+    ss, groups, reqs = setup
+    ssj = og.ShadingSystem()
+    ssj.attribute("jit", 1)
+    specs = workloads.c3_specs()
+    jgroups = [workloads.c3_group(ssj, name, oso) for (name, oso, n, t) in specs[:12]]
+    jreqs = serving.make_requests(torch, jgroups, 40, seed=7, lo=100, hi=40000)
+    srv = ssj.server(budget_bytes=1 << 30, streams=3, max_wave_points=60000)
+    for g in jgroups:
+        srv.register(g)
+    tickets = [srv.submit(r.group, r.n, r.G, r.out) for r in jreqs]
+    for t in tickets:
+        srv.wait(t)
+    for i, (r, ref) in enumerate(zip(jreqs, reqs)):
+        assert np.all(float_equal(r.out.numpy(), ref.ref)), "request %d" % i
+    assert srv.stats()["failed"] == 0 and ssj.device_status() == 0
+    srv.close()
