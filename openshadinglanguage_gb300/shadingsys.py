@@ -296,7 +296,7 @@ class ShadingSystem:
 
         class _View:
             __cuda_array_interface__ = {"shape": (words, int(npoints)), "typestr": "<i4" if t.basetype == C.BASE_INT32
-                                        else "<f4", "data": (ptr, True), "version": 3,
+                                        else "<f4", "data": (ptr, False), "version": 3,
                                         "strides": (4 * stride, 4)}
         return _View()
 
