@@ -42,8 +42,26 @@ def _newer(target, deps):
     return all(os.path.getmtime(d) <= t for d in deps)
 
 
+LUTS = os.path.join(CSRC, "oslg_bsdl_luts.inc")
+
+
+def bsdl_luts():
+    """Bake the BSDL energy-compensation tables (csrc/gen_bsdl_luts.cpp) into
+    csrc/oslg_bsdl_luts.inc unless it is newer than the baker."""
+    gen = os.path.join(CSRC, "gen_bsdl_luts.cpp")
+    if _newer(LUTS, [gen]):
+        return LUTS
+    os.makedirs(BUILD, exist_ok=True)
+    exe = os.path.join(BUILD, "gen_bsdl_luts")
+    _run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-pthread", gen, "-o", exe])
+    _run([exe, LUTS + ".tmp"])
+    os.replace(LUTS + ".tmp", LUTS)
+    return LUTS
+
+
 def build(verbose=False, ptxas_verbose=False):
     os.makedirs(BUILD, exist_ok=True)
+    bsdl_luts()
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh", ".inc"))]
     headers.append(os.path.join(HERE, "..", "include", "oslg.h"))
     jobs, objs = [], []

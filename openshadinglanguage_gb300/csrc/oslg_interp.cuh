@@ -1754,7 +1754,7 @@ static __device__ void h_store_output(const Lane& L, const uint32_t* a, char* ba
         for (int i = 0; i < total; ++i) {
             uint32_t w;
             if (d > 0 && !ader(s)) w = 0u;
-            else if (flags & 2u) w = (uint32_t)ldi(L, s, i);
+            else if (flags & 2u) w = atc(s) == TC_INT ? ldw(L, s, i) : (uint32_t)ldi(L, s, i);  // int arrays: element i
             else w = ldw(L, s, d * total + i);
             if (!(flags & 2u) && atc(s) == TC_INT) w = __float_as_uint((float)(int)w);
             ostore32(reinterpret_cast<uint32_t*>(p) + d * total + i, w);
@@ -1821,6 +1821,7 @@ static __device__ void h_aassign(const Lane& L, const uint32_t* a, uint32_t* st)
 // ---- closures (reference closure tree, node pool in the heap) -------------------------
 struct ClosurePools {
     uint32_t base, max_nodes;
+    uint32_t nf = kRecordFloats;  // floats per node (ProgramHeader::node_floats)
 };
 // closure node pool access (slots at and above the program's closure base)
 #ifdef OSLG_SPEC
@@ -1849,7 +1850,7 @@ struct SymNodes {
     static __device__ __forceinline__ uint32_t u(const Lane& L, uint32_t s) { return sgetu(L, s); }
 };
 __device__ __forceinline__ uint32_t node_slot(const ClosurePools& P, uint32_t node) {
-    return P.base + 1 + node * kNodeFloats;
+    return P.base + 1 + node * P.nf;
 }
 // returns node index + 1, or 0 when the pool is full
 __device__ __forceinline__ uint32_t cl_alloc(const Lane& L, const ClosurePools& P, uint32_t* st) {
@@ -1859,9 +1860,11 @@ __device__ __forceinline__ uint32_t cl_alloc(const Lane& L, const ClosurePools& 
     return n + 1;
 }
 
-// A component node [id][w.rgb][12 parameter words] at slot ns: the
-// closure op's parameters in order, int and string operands as their
-// words, floats as values, zero-padded.
+// A component node [id][w.rgb][parameter words] at slot ns: the closure
+// op's parameters in order, int and string operands as their words, floats
+// as values, zero-padded to kRecordParams words, or to kClosureParamFloats
+// when more are filled (the lowering sizes every node for what its closure
+// op fills).
 template <class NODES>
 __device__ __forceinline__ void closure_fill(const Lane& L, uint32_t ns, const uint32_t* a, const uint32_t* extra,
                                              const float* w) {
@@ -1893,7 +1896,10 @@ __device__ __forceinline__ void closure_fill(const Lane& L, uint32_t ns, const u
                                                                                : __float_as_uint(ldf(L, p, c, 0)));
         }
     }
-    for (; k < kClosureParamFloats; ++k) setu(ns + 4 + k, 0u);
+    const int kpad = k <= kRecordParams ? kRecordParams : kClosureParamFloats;
+    OSLG_SPEC_UNROLL
+    for (int j = 0; j < kClosureParamFloats; ++j)
+        if (j >= k && j < kpad) setu(ns + 4 + j, 0u);
 }
 
 // osl_allocate_(weighted_)closure_component (opclosure.cpp:83-117)
@@ -2045,17 +2051,18 @@ __device__ void closure_walk(const Lane& L, const ClosurePools& P, uint32_t root
     }
 }
 
-// Output record per point: [count][per component: id, w.rgb, params x12]
+// Output record per point: [count][per component: id, w.rgb, the first
+// kRecordParams parameter words]
 static __device__ void h_store_closure(const Lane& L, const uint32_t* a, char* base, const ClosurePools& P, uint32_t* st) {
     uint32_t root = ldw(L, a[0], 0), maxc = a[3];
     uint32_t* o = reinterpret_cast<uint32_t*>(base + (int64_t)a[1] + orec(L) * (int64_t)(int32_t)a[2]);
     uint32_t n = 0;
     closure_walk(L, P, root, st, [&](int id, const float* cw, uint32_t params) {
         if (n >= maxc) return;
-        uint32_t* q = o + 1 + n * kNodeFloats;
+        uint32_t* q = o + 1 + n * kRecordFloats;
         ostore32(q, (uint32_t)id);
         for (int k = 0; k < 3; ++k) ostore32(q + 1 + k, __float_as_uint(cw[k]));
-        for (int k = 0; k < kClosureParamFloats; ++k) ostore32(q + 4 + k, hgetu(L, params + k));
+        for (int k = 0; k < kRecordParams; ++k) ostore32(q + 4 + k, hgetu(L, params + k));
         ++n;
     });
     ostore32(o, n);
@@ -2067,9 +2074,30 @@ static __device__ void h_store_closure(const Lane& L, const uint32_t* a, char* b
 // (shading.cpp:1481-1530): emission accumulates Le; diffuse, oren_nayar and
 // GGX microfacet (refract 0/1/2) become lobes in walk order. Lobe
 // parameters stay in the heap (node params) and are read when used.
+// Lobe kinds this build compiles (bit k: LobeKind k); a specialized kernel
+// defines the kinds its program's closures make.
+#ifndef OSLG_LOBE_KINDS
+#define OSLG_LOBE_KINDS 0xFFu
+#endif
+__device__ __forceinline__ constexpr bool lobe_on(int k) { return ((OSLG_LOBE_KINDS) >> k) & 1u; }
+// the lobe kind of a component (testrender's process_closure), -1 for none
+template <class NODES>
+__device__ __forceinline__ int lobe_kind_of(const Lane& L, int id, uint32_t params, uint32_t ggx) {
+    int k = -1;
+    if (id == kIdDiffuse) k = LK_DIFFUSE;
+    else if (id == kIdOrenNayar) k = LK_OREN_NAYAR;
+    else if (id == kIdMxOrenNayarDiffuse) k = LK_MX_OREN_NAYAR;
+    else if (id == kIdMxSheen) k = LK_SHEEN;
+    else if (id == kIdMxDielectric) k = LK_MX_DIELECTRIC;
+    else if (id == kIdMicrofacet && lobe_on(LK_GGX) && NODES::u(L, params + 0) == ggx) {  // "ggx"
+        const int r = (int)NODES::u(L, params + 10);
+        if (r >= 0 && r <= 2) k = LK_GGX;
+    }
+    return k >= 0 && lobe_on(k) ? k : -1;
+}
 struct Lobes {
     int n;
-    int kind[OSLG_LOBES_MAX];  // 0 diffuse, 1 ggx, 2 oren-nayar, 3 sheen, 4 oren_nayar_diffuse_bsdf
+    int kind[OSLG_LOBES_MAX];  // LobeKind (oslg_program.h), -1 no lobe
     float w[OSLG_LOBES_MAX][3];
     float pdf[OSLG_LOBES_MAX];
     uint32_t p[OSLG_LOBES_MAX];
@@ -2097,19 +2125,11 @@ __device__ __forceinline__ void lobes_collect(const Lane& L, W&& walk, uint32_t 
     B.path_rough = path_rough;
     B.backfacing = backfacing;
     walk([&](int id, const float* cw, uint32_t params) {
-        int k = -1;
-        if (id == 1) {  // EMISSION_ID
+        if (id == kIdEmission) {
             for (int c = 0; c < 3; ++c) B.Le[c] = B.Le[c] + cw[c];
             return;
         }
-        if (id == 3) k = 0;  // DIFFUSE_ID
-        else if (id == 4) k = 2;  // OREN_NAYAR_ID
-        else if (id == kIdMxOrenNayarDiffuse) k = 4;
-        else if (id == kIdMxSheen) k = 3;
-        else if (id == 8 && NODES::u(L, params + 0) == ggx) {  // MICROFACET_ID "ggx"
-            const int r = (int)NODES::u(L, params + 10);
-            if (r >= 0 && r <= 2) k = 1;
-        }
+        const int k = lobe_kind_of<NODES>(L, id, params, ggx);
         if (k < 0 || B.n >= OSLG_LOBES_MAX) return;
 #ifdef OSLG_FIXED_INDEX
 #pragma unroll
@@ -2160,7 +2180,9 @@ __device__ __forceinline__ GGXLobe lobe_ggx(const Lane& L, uint32_t p) {
     return g;
 }
 // An int keyword parameter of a component (name hash, then the value) after
-// its fixed parameters; dflt when absent.
+// its fixed parameters; dflt when absent. The scan stops at the first zero
+// name word, which the zero padding of a node's unfilled words places
+// inside the node.
 template <class NODES>
 __device__ __forceinline__ int closure_keyword_int(const Lane& L, uint32_t params, int first, uint32_t key, int dflt) {
     int v = dflt;
@@ -2205,17 +2227,37 @@ __device__ __forceinline__ BsdfSample lobe_mxon(const Lane& L, uint32_t p, V3 wo
     s.wi = wi;
     return s;
 }
+// dielectric_bsdf(N, U, reflection_tint, transmission_tint, roughness_x,
+// roughness_y, ior, distribution [, "absorption", color]): parameter words
+// 0-15, then the keyword words 16-19 (absorption only when it comes first:
+// its colour fills the four)
+template <class NODES = PoolNodes>
+__device__ __forceinline__ DielLobeDev lobe_diel(const Lane& L, uint32_t p, V3 wo, float path_rough, bool backfacing) {
+    const float refl[3] = { NODES::f(L, p + 6), NODES::f(L, p + 7), NODES::f(L, p + 8) };
+    const float refr[3] = { NODES::f(L, p + 9), NODES::f(L, p + 10), NODES::f(L, p + 11) };
+    const bool ab = NODES::u(L, p + 16) == string_hash_const("absorption");
+    const float absorption[3] = { ab ? NODES::f(L, p + 17) : 0.0f, ab ? NODES::f(L, p + 18) : 0.0f,
+                                  ab ? NODES::f(L, p + 19) : 0.0f };
+    return diel_make(v3(NODES::f(L, p + 0), NODES::f(L, p + 1), NODES::f(L, p + 2)),
+                     v3(NODES::f(L, p + 3), NODES::f(L, p + 4), NODES::f(L, p + 5)), refl, refr, NODES::f(L, p + 12),
+                     NODES::f(L, p + 13), NODES::f(L, p + 14), absorption, wo, path_rough, backfacing);
+}
 template <class NODES = PoolNodes>
 __device__ __forceinline__ BsdfSample lobe_eval(const Lane& L, const Lobes& B, int i, V3 wo, V3 wi) {
     const uint32_t p = B.p[i];
-    if (B.kind[i] == 3) return sheen_eval(lobe_sheen<NODES>(L, B, p, wo), wo, wi);
-    if (B.kind[i] == 0) {
+    const int kind = B.kind[i];
+    if (lobe_on(LK_SHEEN) && kind == LK_SHEEN) return sheen_eval(lobe_sheen<NODES>(L, B, p, wo), wo, wi);
+    if (lobe_on(LK_DIFFUSE) && kind == LK_DIFFUSE) {
         BsdfSample s = diffuse_eval(v3(NODES::f(L, p + 0), NODES::f(L, p + 1), NODES::f(L, p + 2)), wi);
         s.wi = wi;
         return s;
     }
-    if (B.kind[i] == 1) return ggx_eval(lobe_ggx<NODES>(L, p), wo, wi);
-    if (B.kind[i] == 4) return lobe_mxon<NODES>(L, p, wo, wi, false, 0.0f, 0.0f);
+    if (lobe_on(LK_GGX) && kind == LK_GGX) return ggx_eval(lobe_ggx<NODES>(L, p), wo, wi);
+    if (lobe_on(LK_MX_OREN_NAYAR) && kind == LK_MX_OREN_NAYAR)
+        return lobe_mxon<NODES>(L, p, wo, wi, false, 0.0f, 0.0f);
+    if (lobe_on(LK_MX_DIELECTRIC) && kind == LK_MX_DIELECTRIC)
+        return diel_eval(lobe_diel<NODES>(L, p, wo, B.path_rough, B.backfacing), wo, wi);
+    if (!lobe_on(LK_OREN_NAYAR)) return bsdf_zero();
     const V3 N = v3(NODES::f(L, p + 0), NODES::f(L, p + 1), NODES::f(L, p + 2));
     const Frame f = bsdl_frame(bsdl_visible_normal(wo, N, N));
     BsdfSample s = on_eval_local(bsdl_clamp(NODES::f(L, p + 3), 0.0f, 1.0f), tolocal(f, wo), tolocal(f, wi));
@@ -2226,10 +2268,15 @@ template <class NODES = PoolNodes>
 __device__ __forceinline__ BsdfSample lobe_sample(const Lane& L, const Lobes& B, int i, V3 wo, float rx, float ry,
                                                   float rz) {
     const uint32_t p = B.p[i];
-    if (B.kind[i] == 3) return sheen_sample(lobe_sheen<NODES>(L, B, p, wo), wo, rx, ry);
-    if (B.kind[i] == 0) return diffuse_sample(v3(NODES::f(L, p + 0), NODES::f(L, p + 1), NODES::f(L, p + 2)), rx, ry);
-    if (B.kind[i] == 1) return ggx_sample(lobe_ggx<NODES>(L, p), wo, rx, ry, rz);
-    if (B.kind[i] == 4) return lobe_mxon<NODES>(L, p, wo, wo, true, rx, ry);
+    const int kind = B.kind[i];
+    if (lobe_on(LK_SHEEN) && kind == LK_SHEEN) return sheen_sample(lobe_sheen<NODES>(L, B, p, wo), wo, rx, ry);
+    if (lobe_on(LK_DIFFUSE) && kind == LK_DIFFUSE)
+        return diffuse_sample(v3(NODES::f(L, p + 0), NODES::f(L, p + 1), NODES::f(L, p + 2)), rx, ry);
+    if (lobe_on(LK_GGX) && kind == LK_GGX) return ggx_sample(lobe_ggx<NODES>(L, p), wo, rx, ry, rz);
+    if (lobe_on(LK_MX_OREN_NAYAR) && kind == LK_MX_OREN_NAYAR) return lobe_mxon<NODES>(L, p, wo, wo, true, rx, ry);
+    if (lobe_on(LK_MX_DIELECTRIC) && kind == LK_MX_DIELECTRIC)
+        return diel_sample(lobe_diel<NODES>(L, p, wo, B.path_rough, B.backfacing), wo, rx, ry, rz);
+    if (!lobe_on(LK_OREN_NAYAR)) return bsdf_zero();
     const V3 N = v3(NODES::f(L, p + 0), NODES::f(L, p + 1), NODES::f(L, p + 2));
     const Frame f = bsdl_frame(bsdl_visible_normal(wo, N, N));
     const V3 wo_l = tolocal(f, wo);
@@ -2244,15 +2291,18 @@ __device__ __forceinline__ void lobes_prepare(const Lane& L, Lobes& B, V3 wo, co
     float total = 0.0f;
     OSLG_FOR_LOBES(i, B) {
         float alb[3] = { 1.0f, 1.0f, 1.0f };
-        if (B.kind[i] == 1) {
+        if (lobe_on(LK_GGX) && B.kind[i] == LK_GGX) {
             const uint32_t p = B.p[i];
             const GGXLobe g = lobe_ggx<NODES>(L, p);
             alb[0] = alb[1] = alb[2] = ggx_albedo(g, v3(NODES::f(L, p + 1), NODES::f(L, p + 2), NODES::f(L, p + 3)), wo);
-        } else if (B.kind[i] == 3) {
+        } else if (lobe_on(LK_SHEEN) && B.kind[i] == LK_SHEEN) {
             const SheenLobeDev sh = lobe_sheen<NODES>(L, B, B.p[i], wo);
             for (int c = 0; c < 3; ++c) alb[c] = sh.tint[c] * (1 - sh.emiss);
-        } else if (B.kind[i] == 4) {  // BSDL albedo_impl: the closure's albedo
+        } else if (lobe_on(LK_MX_OREN_NAYAR) && B.kind[i] == LK_MX_OREN_NAYAR) {
+            // BSDL albedo_impl: the closure's albedo
             for (int c = 0; c < 3; ++c) alb[c] = NODES::f(L, B.p[i] + 3 + c);
+        } else if (lobe_on(LK_MX_DIELECTRIC) && B.kind[i] == LK_MX_DIELECTRIC) {
+            diel_albedo(lobe_diel<NODES>(L, B.p[i], wo, B.path_rough, B.backfacing), alb);
         }
         B.pdf[i] = (B.w[i][0] * (pw[0] * alb[0]) + B.w[i][1] * (pw[1] * alb[1]) + B.w[i][2] * (pw[2] * alb[2]))
                  / (pw[0] + pw[1] + pw[2]);
@@ -2339,13 +2389,17 @@ __device__ __forceinline__ void layer_opacity(const Lane& L, const ClosurePools&
                 for (int k = 0; k < 3; ++k) bw[k] = w[k] * cw[k];
                 push(hgetu(L, p + 1), bw);
                 cur = hgetu(L, p);
-            } else if (id == kIdMxSheen) {
+            } else if (lobe_on(LK_SHEEN) && id == kIdMxSheen) {
                 const float albedo[3] = { hget(L, p + 3), hget(L, p + 4), hget(L, p + 5) };
                 const SheenLobeDev sh =
                     sheen_make(v3(hget(L, p + 0), hget(L, p + 1), hget(L, p + 2)), albedo, hget(L, p + 6), wo,
                                path_rough, backfacing,
                                closure_keyword_int<PoolNodes>(L, p, 7, string_hash_const("mode"), 0));
                 for (int k = 0; k < 3; ++k) w[k] = w[k] * (cw[k] * (1.0f - sh.emiss));
+            } else if (lobe_on(LK_MX_DIELECTRIC) && id == kIdMxDielectric) {
+                float fo[3];
+                diel_filter_o(lobe_diel<PoolNodes>(L, p, wo, path_rough, backfacing), fo);
+                for (int k = 0; k < 3; ++k) w[k] = w[k] * (cw[k] * (1.0f - fo[k]));
             }
         }
         if (cur == 0u && sp > 0) {
@@ -2438,19 +2492,11 @@ __device__ __forceinline__ void lobes_collect_static(const Lane& L, const Op* ta
         float cw[3];
         for (int k = 0; k < 3; ++k) cw[k] = cwop == kNoArg ? sget(L, ns + 1 + k) : ldf(L, cwop, k, 0);
         const uint32_t params = ns + 4;
-        int k = -1;
-        if (id == 1) {  // EMISSION_ID
+        if (id == kIdEmission) {
             for (int c = 0; c < 3; ++c) B.Le[c] = B.Le[c] + cw[c];
             continue;
         }
-        if (id == 3) k = 0;  // DIFFUSE_ID
-        else if (id == 4) k = 2;  // OREN_NAYAR_ID
-        else if (id == kIdMxOrenNayarDiffuse) k = 4;
-        else if (id == kIdMxSheen) k = 3;
-        else if (id == 8 && sgetu(L, params + 0) == ggx) {  // MICROFACET_ID "ggx"
-            const int r = (int)sgetu(L, params + 10);
-            if (r >= 0 && r <= 2) k = 1;
-        }
+        const int k = lobe_kind_of<SymNodes>(L, id, params, ggx);
         if (k < 0 || count >= kBsdfMaxLobes) continue;
         B.kind[j] = k;
         for (int c = 0; c < 3; ++c) B.w[j][c] = cw[c];
@@ -2465,10 +2511,10 @@ static __device__ void h_cl_store(const Lane& L, const uint32_t* a, const Op* ta
     uint32_t n = 0;
     closure_walk_static(L, tab, a[0], [&](int id, const float* cw, uint32_t params) {
         if (n >= maxc) return;
-        uint32_t* q = o + 1 + n * kNodeFloats;
+        uint32_t* q = o + 1 + n * kRecordFloats;
         ostore32(q, (uint32_t)id);
         for (int k = 0; k < 3; ++k) ostore32(q + 1 + k, __float_as_uint(cw[k]));
-        for (int k = 0; k < kClosureParamFloats; ++k) ostore32(q + 4 + k, sgetu(L, params + k));
+        for (int k = 0; k < kRecordParams; ++k) ostore32(q + 4 + k, sgetu(L, params + k));
         ++n;
     });
     ostore32(o, n);
@@ -3380,6 +3426,7 @@ __global__ void __launch_bounds__(256, 2) interp_kernel(const __grid_constant__ 
     R.nops = nops;
     R.CP.base = H->closure_base;
     R.CP.max_nodes = H->max_comps;
+    R.CP.nf = node_floats(*H);
     R.uses_closures = (H->flags & 1u) != 0;
     R.G = &k.G;
     R.userdata = k.userdata;
@@ -3447,6 +3494,7 @@ __global__ void __launch_bounds__(MAXT, 512 / MAXT) batch_kernel(const __grid_co
             R.nops = nops;
             R.CP.base = H->closure_base;
             R.CP.max_nodes = H->max_comps;
+            R.CP.nf = node_floats(*H);
             R.uses_closures = (H->flags & 1u) != 0;
             R.G = &J->G;
             R.userdata = J->userdata;

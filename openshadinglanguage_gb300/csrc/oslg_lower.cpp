@@ -205,6 +205,7 @@ struct Lowerer {
     uint32_t max_depth = 0;
     std::vector<int> fret_ops;  // emitted OP_FUNC_RETURN ops (their end pc is patched)
     bool uses_closures = false;
+    bool wide_nodes = false;  // some closure fills more than kRecordParams parameter words
     // messages: per name a state symbol, per (name, type) a value store
     std::map<std::string, int> msg_state;
     std::map<std::string, int> msg_store;
@@ -1147,7 +1148,8 @@ struct Lowerer {
             if (closure_writer(op)) {
                 const int r = op.args[0];
                 if (op.name == "closure") {
-                    const int b = new_sym("$clnode", BT_FLOAT, kNodeFloats);
+                    const int b = new_sym("$clnode", BT_FLOAT,
+                                          closure_param_words(op) > kRecordParams ? kNodeFloats : kRecordFloats);
                     LOp nd = op;
                     nd.name = "__cl_node";
                     nd.args[0] = b;
@@ -1508,6 +1510,20 @@ struct Lowerer {
     bool is_matrix(int gs) const { return syms[gs].type.base == BT_MATRIX; }
     bool is_triple(int gs) const { return syms[gs].type.base == BT_TRIPLE; }
     bool is_string(int gs) const { return syms[gs].type.base == BT_STRING; }
+    // Parameter words the device's closure_fill writes for closure op `op`
+    // (an upper bound): each operand's components, at most 16, at most
+    // kClosureParamFloats in all.
+    int closure_param_words(const LOp& op) const {
+        const size_t na = op.args.size();
+        size_t ni = 1;
+        if (na > 1 && !is_string(op.args[1])) ni = 2;
+        int w = 0;
+        for (size_t i = ni + 1; i < na && i < ni + 12; ++i) {
+            const TypeSpec& t = syms[op.args[i]].type;
+            w += std::min(16, std::max(1, t.ncomp() * t.elems()));
+        }
+        return std::min(w, kClosureParamFloats);
+    }
 
     std::string const_string(int gs) const {
         const GSym& s = syms[gs];
@@ -2620,6 +2636,7 @@ struct Lowerer {
         if (n == "closure") {
             // closure r [weight] name args...   (llvm_gen_closure, batched_llvm_gen.cpp:7310)
             uses_closures = true;
+            if (closure_param_words(op) > kRecordParams) wide_nodes = true;
             size_t ni = 1;
             int weight = -1;
             if (na > 1 && !is_string(op.args[1])) { weight = op.args[1]; ni = 2; }
@@ -2759,7 +2776,8 @@ struct Lowerer {
         h.closure_base = heap_top;
         h.max_comps = uses_closures ? (uint32_t)closure_nodes : 0u;
         h.max_terms = 0u;
-        uint32_t closure_slots = uses_closures ? 1 + h.max_comps * kNodeFloats : 0;
+        h.node_floats = wide_nodes ? (uint32_t)kNodeFloats : 0u;
+        uint32_t closure_slots = uses_closures ? 1 + h.max_comps * node_floats(h) : 0;
         h.heap_slots = heap_top + closure_slots;
         if (h.heap_slots == 0) h.heap_slots = 1;
         h.flags = (uses_closures ? 1u : 0u);

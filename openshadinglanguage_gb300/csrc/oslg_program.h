@@ -20,7 +20,7 @@
 namespace oslg {
 
 static const uint32_t kProgramMagic = 0x4f534c47u;  // "OSLG"
-static const uint32_t kProgramVersion = 7;
+static const uint32_t kProgramVersion = 8;
 
 // ---- operand words ----------------------------------------------------------
 // bits 0..19  slot offset (heap) or index (constant pool)
@@ -214,7 +214,24 @@ constexpr uint32_t string_hash_const(const char* s, uint32_t h = 2166136261u) {
 }
 // testrender's closure ids (src/testrender/shading.h:25-61) the BSDF code reads
 static const int kIdEmission = 1, kIdDiffuse = 3, kIdOrenNayar = 4, kIdMicrofacet = 8,
-                 kIdMxOrenNayarDiffuse = 15, kIdMxSheen = 23, kIdMxLayer = 27;
+                 kIdMxOrenNayarDiffuse = 15, kIdMxDielectric = 17, kIdMxSheen = 23, kIdMxLayer = 27;
+// Lobe kinds of the BSDF code (bit k of a lobe-kind mask): the closure id
+// each comes from; a specialized kernel compiles only the kinds its
+// program's closures can make.
+enum LobeKind : int { LK_DIFFUSE = 0, LK_GGX = 1, LK_OREN_NAYAR = 2, LK_SHEEN = 3, LK_MX_OREN_NAYAR = 4,
+                      LK_MX_DIELECTRIC = 5 };
+#ifdef __CUDACC__
+__host__ __device__
+#endif
+inline uint32_t lobe_kind_bits(int closure_id) {
+    return closure_id == kIdDiffuse              ? 1u << LK_DIFFUSE
+         : closure_id == kIdMicrofacet           ? 1u << LK_GGX
+         : closure_id == kIdOrenNayar            ? 1u << LK_OREN_NAYAR
+         : closure_id == kIdMxSheen              ? 1u << LK_SHEEN
+         : closure_id == kIdMxOrenNayarDiffuse   ? 1u << LK_MX_OREN_NAYAR
+         : closure_id == kIdMxDielectric         ? 1u << LK_MX_DIELECTRIC
+                                                 : 0u;
+}
 
 // Shader-globals the program can load (OP_LOAD_GLOBAL a1). Each triple
 // global with derivatives names its dx / dy fields so the loader can fill
@@ -248,13 +265,22 @@ static_assert(sizeof(Op) == 32, "Op must be 32 bytes");
 
 // Closure storage inside the heap (per point): a node pool holding the
 // reference's closure tree (src/include/OSL/oslclosure.h:65-147):
-//   component  [id >= 0][w.r w.g w.b][params x 12]
+//   component  [id >= 0][w.r w.g w.b][params x 12 or x 20]
 //   MUL        [-1][w.r w.g w.b][child]
 //   ADD        [-2][.  .  .  ][A][B]
 // The pool starts with its node count. A closure value (one heap slot, int
-// bits) is node index + 1; 0 is the null closure.
-static const int kClosureParamFloats = 12;
-static const int kNodeFloats = 16;
+// bits) is node index + 1; 0 is the null closure. A node holds
+// kClosureParamFloats parameter words when some closure of the program
+// needs more than kRecordParams of them (dielectric_bsdf: N, U, two tints,
+// two roughnesses, IOR and distribution are 16 words before its keyword
+// parameters), else kRecordParams; the header's node_floats says which.
+// Parameter words a component does not fill are zero up to its capacity.
+static const int kClosureParamFloats = 20;
+static const int kNodeFloats = 4 + kClosureParamFloats;
+// Closure output records (OP_STORE_CLOSURE / OP_CL_STORE): per component
+// [id][w.rgb][the first kRecordParams parameter words].
+static const int kRecordParams = 12;
+static const int kRecordFloats = 4 + kRecordParams;
 static const int kClosureMul = -1;
 static const int kClosureAdd = -2;
 static const int kClosureWalkStack = 16;  // testrender's traversal stack
@@ -285,7 +311,8 @@ struct ProgramHeader {
     uint32_t max_terms;     // unused
     uint32_t max_depth;     // deepest if/loop nesting (<= 32)
     uint32_t max_loop_iterations;  // loop back edges one point may take (0: kDefaultMaxLoopIterations)
-    uint32_t reserved[5];
+    uint32_t node_floats;   // floats per closure pool node (0: kRecordFloats)
+    uint32_t reserved[4];
 };
 static_assert(sizeof(ProgramHeader) == 64, "header must be 64 bytes");
 
@@ -302,6 +329,10 @@ __host__ __device__
 inline uint32_t max_loop_iterations(const ProgramHeader& h) {
     return h.max_loop_iterations ? h.max_loop_iterations : kDefaultMaxLoopIterations;
 }
+#ifdef __CUDACC__
+__host__ __device__
+#endif
+inline uint32_t node_floats(const ProgramHeader& h) { return h.node_floats ? h.node_floats : (uint32_t)kRecordFloats; }
 
 // Texture wrap modes (OP_TEXTURE), the names of OIIO's TextureOpt::Wrap.
 enum TexWrap : uint32_t { TW_PERIODIC = 0, TW_CLAMP = 1, TW_BLACK = 2, TW_MIRROR = 3 };

@@ -12,6 +12,7 @@
 //   CompositeBSDF prepare/eval with MIS::update_eval (shading.h:319-374,
 //   sampling.h:175-205).
 #pragma once
+#include "oslg_fastmath.cuh"
 #include "oslg_fmath.cuh"
 #include "oslg_noise.cuh"
 #include "oslg_program.h"
@@ -701,6 +702,348 @@ __device__ __forceinline__ BsdfSample sheen_sample(const SheenLobeDev& L, V3 wo,
     s.roughness = L.rough;
     s.wi = bsdl_world(L.f, s.wi);
     return s;
+}
+
+
+// ---- BSDL mtx::DielectricLobe (libbsdl MTX/bsdf_dielectric_impl.h) --------------------
+// dielectric_bsdf(N, U, reflection_tint, transmission_tint, roughness_x,
+// roughness_y, ior, distribution) as testrender wraps it (BSDL_WRAP,
+// shading.cpp:73-115: Nf = Ngf = N, outer IOR 1, no spectral sampling):
+// GGX microfacets (microfacet_tools_impl.h GGXDist) with reflection only
+// (Turquin multiple-scattering, :343-391) when the transmission tint is
+// black, else reflection + refraction sampled with bounded visible normals
+// and renormalized by the tabulated energy 1 - E_ms. The energy tables are
+// baked at build time by gen_bsdl_luts.cpp, the way BSDL's genluts does.
+// "absorption" (a colour keyword parameter) scales the reflection-only
+// lobe's opacity; the thin-film and dispersion keywords change nothing in
+// this configuration (no thin film is set on the lobe, lambda_0 is 0).
+#define OSLG_LUT_QUAL static __device__ const
+#include "oslg_bsdl_luts.inc"
+#undef OSLG_LUT_QUAL
+
+// BSDL's MIN / MAX / CLAMP / LERP (tools.h:84-117)
+__device__ __forceinline__ float bmin(float a, float b) { return a < b ? a : b; }
+__device__ __forceinline__ float bmax(float a, float b) { return a > b ? a : b; }
+__device__ __forceinline__ float bclamp(float x, float a, float b) { return bmin(bmax(x, a), b); }
+__device__ __forceinline__ float blerp(float f, float a, float b) {
+    f = bclamp(f, 0.0f, 1.0f);
+    return (1 - f) * a + f * b;
+}
+__device__ __forceinline__ float bsqr(float x) { return x * x; }
+
+// BSDL Frame(Z, X) (tools.h:483-495)
+__device__ __forceinline__ Frame bsdl_frame_zx(V3 z, V3 x) {
+    if (bsdl_max_abs(x) < 1e-4f || fabsf(vdot(z, vnormalize_imath(x))) > 0.999f) return bsdl_frame(z);
+    Frame f;
+    f.w = z;
+    f.v = vnormalize_imath(vcross(z, x));
+    f.u = vcross(f.v, z);
+    return f;
+}
+
+// TabulatedEnergyCurve<T>::Emiss_eval (microfacet_tools_impl.h:113-212) over
+// a baked table [NF][16 roughness][16 cosines]; cosines (i/15)^2 when SQ,
+// else i/15. The roughness index is kept inside the table (BSDL reads past
+// it for roughness above 1).
+template <int NF, bool SQ>
+__device__ __forceinline__ float lut_cosine(int i) {
+    const float t = float(i) * (1.0f / 15);
+    return fmaxf(SQ ? t * t : t, 1e-6f);
+}
+template <int NF>
+__device__ __forceinline__ float lut_interp(const float* T, float rough, float findex, int i) {
+    float rf = rough * 15;
+    int ra = (int)rf;
+    ra = ra < 0 ? 0 : (ra > 15 ? 15 : ra);
+    const int rb = min(ra + 1, 15);
+    rf -= ra;
+    if (NF == 1) return blerp(rf, __ldg(T + ra * 16 + i), __ldg(T + rb * 16 + i));
+    float ff = findex * (NF - 1);
+    int fa = (int)ff;
+    fa = fa < 0 ? 0 : (fa > NF - 1 ? NF - 1 : fa);
+    const int fb = min(fa + 1, NF - 1);
+    ff -= fa;
+    return blerp(ff, blerp(rf, __ldg(T + (fa * 16 + ra) * 16 + i), __ldg(T + (fa * 16 + rb) * 16 + i)),
+                 blerp(rf, __ldg(T + (fb * 16 + ra) * 16 + i), __ldg(T + (fb * 16 + rb) * 16 + i)));
+}
+template <int NF, bool SQ>
+__device__ float lut_emiss(const float* T, float rough, float findex, float c) {
+    float cos0 = lut_cosine<NF, SQ>(0);
+    if (c <= cos0) return lut_interp<NF>(T, rough, findex, 0);
+    for (int i = 1; i < 16; ++i) {
+        const float cos1 = lut_cosine<NF, SQ>(i);
+        if (c < cos1) {
+            const float q = (c - cos0) / (cos1 - cos0);
+            return blerp(q, lut_interp<NF>(T, rough, findex, i - 1), lut_interp<NF>(T, rough, findex, i));
+        }
+        cos0 = cos1;
+    }
+    return lut_interp<NF>(T, rough, findex, 15);
+}
+
+// GGXDist (microfacet_tools_decl.h:13-47, microfacet_tools_impl.h:17-112)
+struct GGXDistDev {
+    float ax, ay;
+};
+__device__ __forceinline__ GGXDistDev ggxd_make(float rough, float aniso, bool flip) {
+    GGXDistDev d;
+    d.ax = bsqr(rough);
+    d.ay = d.ax;
+    if (flip) aniso = -aniso;
+    d.ax = fmaxf(d.ax * (1 + aniso), 1e-5f);
+    d.ay = fmaxf(d.ay * (1 - aniso), 1e-5f);
+    return d;
+}
+__device__ __forceinline__ float ggxd_D(const GGXDistDev& d, V3 h) {
+    const float cp = bsqr(h.x / d.ax), sp = bsqr(h.y / d.ay), c2 = bsqr(h.z);
+    const float s2 = cp + sp;
+    return 1.0f / (3.14159265358979323846f * d.ax * d.ay * bsqr(c2 + s2));
+}
+__device__ __forceinline__ float ggxd_G1(const GGXDistDev& d, V3 w) {
+    w = v3(w.x * d.ax, w.y * d.ay, w.z);
+    return 2.0f * w.z / (w.z + vlen_imath(w));
+}
+__device__ __forceinline__ float ggxd_G2_G1(const GGXDistDev& d, V3 wi, V3 wo) {
+    wi = v3(wi.x * d.ax, wi.y * d.ay, wi.z);
+    wo = v3(wo.x * d.ax, wo.y * d.ay, wo.z);
+    const float nl = vlen_imath(wi), nv = vlen_imath(wo);
+    return wi.z * (wo.z + nv) / (wo.z * nl + wi.z * nv);
+}
+// Eto and Tokuyoshi, "Bounded VNDF Sampling for Smith-GGX Reflections"
+// (eq. 5, 6, 8): the reflection-bounded micro normal and D_refl / D
+__device__ __forceinline__ float ggxd_bvn_k(const GGXDistDev& d, V3 wo) {
+    const float a = bclamp(bmin(d.ax, d.ay), 0.0f, 1.0f);
+    const float s = 1 + sqrtf(bsqr(wo.x) + bsqr(wo.y));
+    const float a2 = bsqr(a), s2 = bsqr(s);
+    return (1 - a2) * s2 / (s2 + a2 * bsqr(wo.z));
+}
+__device__ __forceinline__ V3 ggxd_sample_for_refl(const GGXDistDev& d, V3 wo, float randu, float randv) {
+    const V3 i_std = vnormalize_imath(v3(wo.x * d.ax, wo.y * d.ay, wo.z));
+    const float phi = (2.0f * 3.14159265358979323846f) * randu;
+    const float k = ggxd_bvn_k(d, wo);
+    const float b = k * i_std.z;
+    const float z = (1 - randv) * (1 + b) - b;
+    const float st = sqrtf(bclamp(1 - bsqr(z), 0.0f, 1.0f));
+    const V3 o_std = v3(st * fm::cos(phi), st * fm::sin(phi), z);
+    const V3 m_std = vadd(i_std, o_std);
+    return vnormalize_imath(v3(m_std.x * d.ax, m_std.y * d.ay, m_std.z));
+}
+__device__ __forceinline__ float ggxd_D_refl_D(const GGXDistDev& d, V3 wo) {
+    const float l2 = (wo.x * d.ax) * (wo.x * d.ax) + (wo.y * d.ay) * (wo.y * d.ay);
+    const float t = sqrtf(l2 + bsqr(wo.z));
+    const float k = ggxd_bvn_k(d, wo);
+    return 2 * wo.z / (k * wo.z + t);
+}
+
+// DielectricFresnel (MTX/bsdf_dielectric_impl.h:21-64)
+__device__ __forceinline__ float diel_fresnel_eta(float e, bool backside) {
+    if (backside) e = 1 / e;
+    return e >= 1 ? bclamp(e, 1.001f, 5.0f) : bclamp(e, 1 / 5.0f, 1 / 1.001f);
+}
+__device__ __forceinline__ float diel_fresnel(float eta, float c) {
+    float g = (eta - 1.0f) * (eta + 1.0f) + c * c;
+    if (g > 0) {
+        g = sqrtf(g);
+        const float A = (g - c) / (g + c);
+        const float B = (c * (g + c) - 1) / (c * (g - c) + 1);
+        return 0.5f * A * A * (1 + B * B);
+    }
+    return 1.0f;
+}
+__device__ __forceinline__ float diel_table_index(float eta) {
+    const float seta = bclamp(eta < 1 ? 1 / eta : eta, 1.001f, 5.0f);
+    const float x = (seta - 1.001f) * (1 / (5.0f - 1.001f));
+    return sqrtf(x);
+}
+// BSDL reflect / refract (tools.h:301-334)
+__device__ __forceinline__ V3 bsdl_reflect(V3 E, V3 N) { return vsub(vmul(N, 2 * vdot(N, E)), E); }
+__device__ __forceinline__ V3 bsdl_refract(V3 E, V3 N, float eta) {
+    if (eta == 0) return v3(0.0f, 0.0f, 0.0f);
+    float cosi = vdot(E, N), neta;
+    V3 Nn;
+    if (cosi > 0) {
+        neta = 1 / eta;
+        Nn = N;
+    } else {
+        cosi = -cosi;
+        neta = eta;
+        Nn = vneg(N);
+    }
+    const float arg = 1 - (neta * neta * (1 - (cosi * cosi)));
+    if (arg >= 0) {
+        const float dnp = sqrtf(arg);
+        const float nK = (neta * cosi) - dnp;
+        return vnormalize_imath(vadd(vmul(E, -neta), vmul(Nn, nK)));
+    }
+    return v3(0.0f, 0.0f, 0.0f);
+}
+
+struct DielLobeDev {
+    Frame f;          // BSDL Frame(visible normal, U)
+    GGXDistDev d;
+    float eta;        // DielectricFresnel::eta
+    float spec_ems;   // DielectricBSDF::E_ms (reflection only: MiniMicrofacetGGX)
+    float ems;        // DielectricLobe::E_ms
+    float rough;      // the lobe's (regularized) roughness
+    float refl[3], refr[3], wo_abs[3];
+    bool dorefl, dorefr;
+};
+// DielectricLobe::DielectricLobe (MTX/bsdf_dielectric_impl.h:245-316)
+__device__ __forceinline__ DielLobeDev diel_make(V3 N, V3 U, const float* refl, const float* refr, float rx_in,
+                                                 float ry_in, float ior, const float* absorption, V3 wo,
+                                                 float path_rough, bool backfacing) {
+    DielLobeDev D;
+    D.f = bsdl_frame_zx(bsdl_visible_normal(wo, N, N), U);
+    for (int c = 0; c < 3; ++c) {
+        D.refl[c] = refl[c];
+        D.refr[c] = refr[c];
+        D.wo_abs[c] = 1.0f;
+    }
+    D.dorefl = bmax(refl[0], bmax(refl[1], refl[2])) > 0;
+    D.dorefr = bmax(refr[0], bmax(refr[1], refr[2])) > 0;
+    const float rx = bclamp(rx_in, 1e-4f, 2.0f), ry = bclamp(ry_in, 1e-4f, 2.0f);
+    const float axr = fmaxf(rx, ry), ayr = fminf(rx, ry);
+    const float b = ayr / axr;
+    const float aniso = (1 - b) / (1 + b);
+    const float roughness = 1.0f - (1.0f - sqrtf(axr / (1 + aniso))) * (1.0f - path_rough);
+    const float cosNO = vdot(D.f.w, wo);
+    const float IOR = bclamp(ior, 1.001f, 5.0f);
+    D.eta = diel_fresnel_eta(IOR / 1.0f, backfacing);
+    D.d = ggxd_make(roughness, aniso, rx < ry);
+    D.spec_ems = D.dorefr ? 0.0f : lut_emiss<1, true>(kLutMiniGGX, roughness, 0.0f, cosNO);
+    const float tix = diel_table_index(D.eta);
+    D.ems = 0.0f;
+    if (D.dorefl && !D.dorefr) D.ems = lut_emiss<32, false>(kLutDielReflFront, roughness, tix, cosNO);
+    else if (D.dorefr)
+        D.ems = lut_emiss<32, false>(backfacing ? kLutDielBothBack : kLutDielBothFront, roughness, tix, cosNO);
+    D.rough = roughness;
+    if (bmax(absorption[0], bmax(absorption[1], absorption[2])) > 0 && D.dorefl && !D.dorefr) {
+        const float sinNO2 = 1 - bsqr(cosNO);
+        const float inveta2 = bsqr(1 / D.eta);
+        const float cos_p = sqrtf(1 - fminf(1.0f, inveta2 * sinNO2));
+        const float dist = 1 / fmaxf(cos_p, 1.17549435e-38f);
+        for (int c = 0; c < 3; ++c) D.wo_abs[c] = fm::exp(-absorption[c] * dist);
+    }
+    return D;
+}
+// eval_turquin_microms_reflection (microfacet_tools_impl.h:343-373) and
+// DielectricBSDF::eval (MTX/bsdf_dielectric_impl.h:110-185), local frame;
+// the weight is one value for all channels
+__device__ __forceinline__ BsdfSample diel_spec_eval(const DielLobeDev& L, V3 wo, V3 wi) {
+    BsdfSample s = bsdf_zero();
+    const float cosNO = wo.z, cosNI = wi.z;
+    if (!L.dorefr) {
+        if (cosNI <= 0 || cosNO <= 0) return s;
+        const V3 m = vnormalize_imath(vadd(wo, wi));
+        const float cosMO = vdot(m, wo);
+        const float D = ggxd_D(L.d, m);
+        const float D_refl_D = ggxd_D_refl_D(L.d, wo);
+        const float D_refl = D_refl_D * D;
+        const float G1 = ggxd_G1(L.d, wo);
+        const float pdf = D_refl / (4 * cosNO);
+        const float out = ggxd_G2_G1(L.d, wi, wo) * G1 / D_refl_D;
+        const float F = diel_fresnel(L.eta, cosMO);
+        const float msf = L.spec_ems / fmaxf(0.01f, 1 - L.spec_ems);
+        const float O = out * F * (1 + F * msf);
+        s.w[0] = s.w[1] = s.w[2] = O;
+        s.pdf = pdf;
+        s.wi = wi;
+        return s;
+    }
+    if (cosNI > 0) {
+        const V3 m = vnormalize_imath(vadd(wo, wi));
+        const float cosMO = vdot(m, wo);
+        if (cosMO <= 0) return s;
+        const float D = ggxd_D(L.d, m);
+        const float G1 = ggxd_G1(L.d, wo);
+        const float F = diel_fresnel(L.eta, cosMO);
+        if (F <= 0) return s;
+        const float D_refl_D = ggxd_D_refl_D(L.d, wo);
+        const float D_refl = D_refl_D * D;
+        const float out = F * (ggxd_G2_G1(L.d, wi, wo) * G1 / (D_refl_D * F));
+        s.w[0] = s.w[1] = s.w[2] = out;
+        s.pdf = D_refl / (4.0f * cosNO) * F;
+        s.wi = wi;
+        return s;
+    }
+    if (cosNI < 0) {
+        const float eta = L.eta;
+        const V3 Ht = vmul(vnormalize_imath(vadd(vmul(wi, eta), wo)), eta > 1 ? -1.0f : 1.0f);
+        const float cosHO = vdot(Ht, wo), cosHI = vdot(Ht, wi);
+        if (cosHO <= 0 || cosHI >= 0) return s;
+        const float Ft = 1.0f - diel_fresnel(eta, cosHO);
+        if (Ht.z <= 0 || Ft <= 0) return s;
+        const float D = ggxd_D(L.d, Ht);
+        const float G1 = ggxd_G1(L.d, wo);
+        const float J = (-cosHI * cosHO * bsqr(eta)) / (wo.z * bsqr(cosHI * eta + cosHO));
+        const float D_refl_D = ggxd_D_refl_D(L.d, wo);
+        const float D_refl = D_refl_D * D;
+        const float out = Ft * (ggxd_G2_G1(L.d, v3(wi.x, wi.y, -wi.z), wo) * G1 / (D_refl_D * Ft));
+        s.w[0] = s.w[1] = s.w[2] = out;
+        s.pdf = D_refl * J * Ft;
+        s.wi = wi;
+        return s;
+    }
+    return s;
+}
+// sample_turquin_microms_reflection (microfacet_tools_impl.h:375-391) and
+// DielectricBSDF::sample (MTX/bsdf_dielectric_impl.h:187-216)
+__device__ __forceinline__ BsdfSample diel_spec_sample(const DielLobeDev& L, V3 wo, float ru, float rv, float rw) {
+    if (!L.dorefr) {
+        if (wo.z <= 0) return bsdf_zero();
+        const V3 m = ggxd_sample_for_refl(L.d, wo, ru, rv);
+        const V3 wi = bsdl_reflect(wo, m);
+        if (wi.z <= 0) return bsdf_zero();
+        return diel_spec_eval(L, wo, wi);
+    }
+    const V3 m = ggxd_sample_for_refl(L.d, wo, ru, rv);
+    const float cosMO = vdot(wo, m);
+    if (cosMO <= 0) return bsdf_zero();
+    const float F = diel_fresnel(L.eta, cosMO);
+    const bool choose_reflect = rw < F;
+    const V3 wi = choose_reflect ? bsdl_reflect(wo, m) : bsdl_refract(wo, m, L.eta);
+    if ((choose_reflect && wi.z <= 0) || (!choose_reflect && wi.z >= 0)) return bsdf_zero();
+    return diel_spec_eval(L, wo, wi);
+}
+// DielectricLobe::eval_impl / sample_impl (MTX/bsdf_dielectric_impl.h:318-
+// 360) through BSDL_WRAP (world directions in and out)
+__device__ __forceinline__ void diel_finish(const DielLobeDev& L, BsdfSample& s) {
+    if (L.dorefr) {
+        const float inv = 1 / fmaxf(0.01f, 1 - L.ems);
+        for (int c = 0; c < 3; ++c) s.w[c] *= inv;
+    }
+}
+__device__ __forceinline__ BsdfSample diel_eval(const DielLobeDev& L, V3 wo, V3 wi) {
+    if (!L.dorefl && !L.dorefr) {
+        BsdfSample z = bsdf_zero();
+        z.wi = wi;
+        return z;
+    }
+    BsdfSample s = diel_spec_eval(L, tolocal(L.f, wo), tolocal(L.f, wi));
+    diel_finish(L, s);
+    const float* tint = s.wi.z > 0 ? L.refl : L.refr;
+    for (int c = 0; c < 3; ++c) s.w[c] *= tint[c];
+    s.roughness = L.rough;
+    s.wi = wi;
+    return s;
+}
+__device__ __forceinline__ BsdfSample diel_sample(const DielLobeDev& L, V3 wo, float rx, float ry, float rz) {
+    if (!L.dorefl && !L.dorefr) return bsdf_zero();
+    BsdfSample s = diel_spec_sample(L, tolocal(L.f, wo), rx, ry, rz);
+    diel_finish(L, s);
+    if (bsdl_max_abs(s.wi) < 1e-4f) return bsdf_zero();
+    const float* tint = s.wi.z > 0 ? L.refl : L.refr;
+    for (int c = 0; c < 3; ++c) s.w[c] *= tint[c];
+    s.roughness = L.rough;
+    s.wi = bsdl_world(L.f, s.wi);
+    return s;
+}
+// albedo_impl and filter_o (MTX/bsdf_dielectric_decl.h:146-157)
+__device__ __forceinline__ void diel_albedo(const DielLobeDev& L, float* alb) {
+    for (int c = 0; c < 3; ++c) alb[c] = !L.dorefr ? L.refl[c] * (1 - L.ems) : 1.0f;
+}
+__device__ __forceinline__ void diel_filter_o(const DielLobeDev& L, float* f) {
+    for (int c = 0; c < 3; ++c) f[c] = !L.dorefr ? L.ems * L.wo_abs[c] : 0.0f;
 }
 
 }  // namespace dev

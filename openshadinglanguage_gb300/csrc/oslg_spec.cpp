@@ -99,7 +99,7 @@ uint32_t staging_stride(const Op* ops, int n) {
         case OP_CL_STORE:
             off = op.a[1];
             st = (int32_t)op.a[2];
-            size = 4ll * (1 + (int64_t)op.a[3] * kNodeFloats);
+            size = 4ll * (1 + (int64_t)op.a[3] * kRecordFloats);
             break;
         case OP_BSDF_EVAL:
         case OP_CL_BSDF_EVAL: off = op.a[1]; st = (int32_t)op.a[2]; size = 16; break;
@@ -135,6 +135,14 @@ struct ProgView {
     bool uses_cl;
     uint32_t sym, cpool;
 };
+
+// The lobe kinds (LobeKind bits) the closures of a program can make.
+uint32_t lobe_kinds(const ProgView& v) {
+    uint32_t m = 0;
+    for (int i = 0; i < v.n; ++i)
+        if (v.ops[i].code == OP_CLOSURE || v.ops[i].code == OP_CLOSURE_NODE) m |= lobe_kind_bits((int)v.ops[i].a[1]);
+    return m;
+}
 
 ProgView view(const CompiledGroup& cg) {
     ProgView v;
@@ -260,6 +268,7 @@ void emit_job(std::ostringstream& o, const ProgView& v, const std::string& sfx) 
     o << "__device__ __noinline__ void spec_job" << sfx << "(RunCtx& R, Lane& L, int64_t npoints) {\n";
     o << "    R.nops = " << v.n << ";\n";
     o << "    R.CP.base = " << v.h->closure_base << "u;\n    R.CP.max_nodes = " << v.h->max_comps << "u;\n";
+    o << "    R.CP.nf = " << node_floats(*v.h) << "u;\n";
     o << "    R.uses_closures = " << (v.uses_cl ? "true" : "false") << ";\n";
     o << "    float hreg[" << std::max(1u, v.sym) << "];\n";
     o << "    L.heap = hreg;\n    L.pool = kPool" << sfx << ";\n    L.cbase = " << v.h->closure_base << "u;\n";
@@ -281,6 +290,7 @@ std::string spec_source(const CompiledGroup& cg, int min_blocks) {
     o << "// generated: kernel specialized to one lowered program (" << n << " ops, " << sym
       << " symbol slots, " << cpool << " closure-pool slots)\n";
     o << "#define OSLG_SPEC 1\n";
+    o << "#define OSLG_LOBE_KINDS 0x" << std::hex << lobe_kinds(v) << std::dec << "u\n";
     if (stage) o << "#define OSLG_STAGE_STRIDE " << stage << "\n";
     emit_bounds(o, B);
     o << "#include \"oslg_interp.cuh\"\n\nnamespace {\n";
@@ -300,6 +310,7 @@ std::string spec_source(const CompiledGroup& cg, int min_blocks) {
     else o << "    extern __shared__ __align__(16) unsigned char smem[];\n";
     o << "    RunCtx R;\n    R.sops = nullptr;\n    R.nops = " << n << ";\n";
     o << "    R.CP.base = " << h.closure_base << "u;\n    R.CP.max_nodes = " << h.max_comps << "u;\n";
+    o << "    R.CP.nf = " << node_floats(h) << "u;\n";
     o << "    R.uses_closures = " << (uses_cl ? "true" : "false") << ";\n";
     o << "    R.G = &k.G;\n    R.userdata = k.userdata;\n    R.outputs = k.outputs;\n    R.status = k.status;\n";
     o << "    R.textures = k.textures;\n    R.ntextures = k.ntextures;\n";
@@ -377,6 +388,9 @@ std::string spec_batch_source(const std::vector<const CompiledGroup*>& cases) {
     std::ostringstream o;
     o << "// generated: persistent batch kernel specialized to " << cases.size() << " lowered programs\n";
     o << "#define OSLG_SPEC 1\n#define OSLG_SPEC_BATCH 1\n";
+    uint32_t kinds = 0;
+    for (const ProgView& pv : vs) kinds |= lobe_kinds(pv);
+    o << "#define OSLG_LOBE_KINDS 0x" << std::hex << kinds << std::dec << "u\n";
     emit_bounds(o, B);
     o << "#include \"oslg_interp.cuh\"\n\nnamespace {\n";
     o << "using namespace oslg;\nusing namespace oslg::dev;\n\n";

@@ -8,8 +8,9 @@ C3  random groups   64 seeded random op DAGs of 20-200 ops with noise,
                     counts log-uniform in [1K, 1M], P uniform in [-10,10]^3
 C5  materials       16 seeded 2-4 layer material groups (noise patterns,
                     tint, a closure sum of diffuse / oren_nayar / GGX
-                    microfacet / GGX dielectric / emission) with a BSDF
-                    sample output for the wavefront path tracer
+                    microfacet / BSDL dielectric_bsdf (IOR 1.3-1.7) /
+                    sheen / emission) with a BSDF sample output for the
+                    wavefront path tracer
 """
 import numpy as np
 
@@ -395,13 +396,19 @@ def _c5_surface(name, lobes):
             b.op("closure", cl, b.const("string", "oren_nayar"), N, c(extra))
         elif kind == "sheen":  # sheen_bsdf(N, albedo, roughness): albedo from the tint
             b.op("closure", cl, b.const("string", "sheen_bsdf"), N, tint, c(extra))
-        elif kind in ("ggx", "dielectric"):
+        elif kind == "ggx":
             alpha, t = b.tmp("float"), b.tmp("float")
             b.op("mul", t, c(0.6), r)
             b.op("add", alpha, c(0.05), t)
-            eta = extra if kind == "dielectric" else 1.5
             b.op("closure", cl, b.const("string", "microfacet"), b.const("string", "ggx"), N, dPdu, alpha, alpha,
-                 c(eta), b.const("int", 2 if kind == "dielectric" else 0))
+                 c(1.5), b.const("int", 0))
+        elif kind == "dielectric":  # dielectric_bsdf(N, U, reflection, transmission, rx, ry, ior, "ggx")
+            alpha, t = b.tmp("float"), b.tmp("float")
+            b.op("mul", t, c(0.6), r)
+            b.op("add", alpha, c(0.05), t)
+            one = b.const("color", [1.0, 1.0, 1.0])
+            b.op("closure", cl, b.const("string", "dielectric_bsdf"), N, dPdu, one, one, alpha, alpha, c(extra),
+                 b.const("string", "ggx"))
         else:  # emission, modulated by the pattern
             b.op("closure", cl, b.const("string", "emission"))
         tw = b.tmp("color")

@@ -16,12 +16,24 @@ SOURCES = ["oracle.cpp", "oracle_wavefront.cpp"]
 HEADERS = sorted(f for f in os.listdir(HERE) if f.endswith(".h"))
 
 
+def _product_build():
+    """The product's build recipe, loaded by path (not through the package)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "_oslg_product_build", os.path.join(HERE, "..", "openshadinglanguage_gb300", "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
 def build(force=False):
     os.makedirs(OUT_DIR, exist_ok=True)
     deps = [os.path.join(HERE, f) for f in SOURCES + HEADERS]
     deps.append(os.path.join(HERE, "..", "openshadinglanguage_gb300", "csrc", "oslg_program.h"))
     deps.append(os.path.join(HERE, "..", "include", "oslg.h"))
     deps.append(os.path.join(HERE, "..", "openshadinglanguage_gb300", "csrc", "oslg_zeltner_ltc.inc"))
+    # the BSDL energy tables the product bakes (data shared with the oracle)
+    deps.append(_product_build().bsdl_luts())
     if not force and os.path.exists(LIB) and all(os.path.getmtime(d) <= os.path.getmtime(LIB) for d in deps):
         return LIB
     cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-shared",

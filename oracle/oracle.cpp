@@ -1319,9 +1319,10 @@ void op_load_global(Point& P, const uint32_t* a, const oslg_shaderglobals& G) {
 }
 
 // Closure tree (src/include/OSL/oslclosure.h:65-147) in a per-point node
-// pool: [count][nodes of kNodeFloats]; a closure value is node index + 1.
-struct CPools { uint32_t base, maxn; };
-inline uint32_t nslot(const CPools& C, uint32_t node) { return C.base + 1 + node * oslg::kNodeFloats; }
+// pool: [count][nodes of nf words (ProgramHeader::node_floats)]; a closure
+// value is node index + 1.
+struct CPools { uint32_t base, maxn, nf; };
+inline uint32_t nslot(const CPools& C, uint32_t node) { return C.base + 1 + node * C.nf; }
 inline uint32_t cl_alloc(Point& P, const CPools& C) {
     uint32_t n = P.heap[C.base];
     if (n >= C.maxn) { P.status |= oslg::ST_CLOSURE_OVERFLOW; return 0u; }
@@ -1409,6 +1410,18 @@ inline int keyword_int(const Point& P, uint32_t p, int first, const char* name, 
     return dflt;
 }
 
+// dielectric_bsdf(N, U, reflection_tint, transmission_tint, roughness_x,
+// roughness_y, ior, distribution): words 0-15; a leading "absorption"
+// keyword fills words 16-19 with its name and colour
+inline MxDielectric mx_dielectric(const Point& P, uint32_t p, const V3& wo, float path_roughness, bool backfacing) {
+    auto f = [&](uint32_t s) { return bitsf(P.heap[s]); };
+    V3 absorption(0.0f);
+    if (P.heap[p + 16] == oslg::string_hash_const("absorption")) absorption = V3(f(p + 17), f(p + 18), f(p + 19));
+    return MxDielectric(V3(f(p + 0), f(p + 1), f(p + 2)), V3(f(p + 3), f(p + 4), f(p + 5)),
+                        V3(f(p + 6), f(p + 7), f(p + 8)), V3(f(p + 9), f(p + 10), f(p + 11)), f(p + 12), f(p + 13),
+                        f(p + 14), absorption, wo, path_roughness, backfacing);
+}
+
 template <class WALK>
 void collect_lobes(Point& P, WALK&& walk, const V3& wo, uint32_t ggx_hash, CompositeLobes* L, float path_roughness,
                    bool backfacing) {
@@ -1436,6 +1449,8 @@ void collect_lobes(Point& P, WALK&& walk, const V3& wo, uint32_t ggx_hash, Compo
         } else if (id == oslg::kIdMxSheen) {  // sheen_bsdf(N, albedo, roughness, "mode", int)
             L->add_sheen(cw, SheenConty(V3(f(p + 0), f(p + 1), f(p + 2)), V3(f(p + 3), f(p + 4), f(p + 5)), f(p + 6), wo,
                                         path_roughness, backfacing, keyword_int(P, p, 7, "mode", 0)));
+        } else if (id == oslg::kIdMxDielectric) {
+            L->add_mx_dielectric(cw, mx_dielectric(P, p, wo, path_roughness, backfacing));
         } else if (id == 8 && P.heap[p] == ggx_hash) {  // MICROFACET_ID, "ggx"
             int refract = (int32_t)P.heap[p + 10];
             if (refract < 0 || refract > 2) return;
@@ -1487,6 +1502,8 @@ V3 layer_opacity(Point& P, const CPools& C, uint32_t top, const V3& wo, float pa
                 const SheenConty sh(V3(f(p + 0), f(p + 1), f(p + 2)), V3(f(p + 3), f(p + 4), f(p + 5)), f(p + 6), wo,
                                     path_roughness, backfacing, keyword_int(P, p, 7, "mode", 0));
                 w = w * (cw * V3(1.0f - sh.emiss));
+            } else if (id == oslg::kIdMxDielectric) {  // testrender shading.cpp:1242-1248
+                w = w * (cw * (V3(1.0f) - mx_dielectric(P, p, wo, path_roughness, backfacing).filter_o()));
             }
         }
         if (cur == 0u && sp > 0) {
@@ -1535,7 +1552,7 @@ struct Runner {
 
     void run_point(Point& P) {
         const oslg::ProgramHeader& h = *prog.h;
-        CPools C{ h.closure_base, h.max_comps };
+        CPools C{ h.closure_base, h.max_comps, oslg::node_floats(h) };
         if (h.flags & 1u) P.heap[C.base] = 0u;
         int nops = (int)h.nops;
         // the loop limit: back edges this point takes, summed over every loop
@@ -1595,7 +1612,7 @@ struct Runner {
                     for (int i = 0; i < total; ++i) {
                         uint32_t w;
                         if (d > 0 && !ader(s)) w = 0u;
-                        else if (flags & 2u) w = (uint32_t)geti(P, s, i);
+                        else if (flags & 2u) w = atc(s) == oslg::TC_INT ? word(P, s, i) : (uint32_t)geti(P, s, i);
                         else w = word(P, s, d * total + i);
                         if (!(flags & 2u) && atc(s) == oslg::TC_INT) w = fbits((float)(int32_t)w);
                         q[d * total + i] = w;
@@ -1881,7 +1898,9 @@ struct Runner {
                                                    ? word(P, params[i], c)
                                                    : fbits(getf(P, params[i], c, 0));
                 }
-                for (; k < oslg::kClosureParamFloats; ++k) P.heap[ns + 4 + k] = fbits(0.0f);
+                // zero padding to the node's capacity: 12 words, 20 when more are filled
+                const int kpad = k <= oslg::kRecordParams ? oslg::kRecordParams : oslg::kClosureParamFloats;
+                for (; k < kpad; ++k) P.heap[ns + 4 + k] = fbits(0.0f);
                 if (!stat) setw(P, a[0], 0, h);
                 break;
             }
@@ -1925,10 +1944,10 @@ struct Runner {
                 };
                 walk([&](int id, const V3& cw, uint32_t params) {
                     if (n >= maxc) return;
-                    uint32_t* rec = q + 1 + n * oslg::kNodeFloats;
+                    uint32_t* rec = q + 1 + n * oslg::kRecordFloats;
                     rec[0] = (uint32_t)id;
                     rec[1] = fbits(cw.x); rec[2] = fbits(cw.y); rec[3] = fbits(cw.z);
-                    for (int k = 0; k < oslg::kClosureParamFloats; ++k) rec[4 + k] = P.heap[params + k];
+                    for (int k = 0; k < oslg::kRecordParams; ++k) rec[4 + k] = P.heap[params + k];
                     ++n;
                 });
                 q[0] = n;

@@ -22,6 +22,7 @@
 #include <cmath>
 #include <new>
 
+#include "oracle_fastmath.h"
 #include "oracle_fmath.h"
 #include "oracle_shading.h"
 
@@ -274,6 +275,7 @@ inline V3 bsdl_sample_cos_hemisphere(float randu, float randv) {
 }
 struct BsdlFrame {
     V3 X, Y, Z;
+    BsdlFrame() = default;
     explicit BsdlFrame(const V3& z) : Z(z) {
         const float s = std::copysign(1.0f, z.z);
         const float a = -1.0f / (s + z.z);
@@ -281,12 +283,22 @@ struct BsdlFrame {
         X = V3(1.0f + s * z.x * z.x * a, s * b, -s * z.x);
         Y = V3(b, s + z.y * z.y * a, -z.y);
     }
+    // Frame(Z, X) (tools.h:483-495): X along x but orthogonal to Z
+    BsdlFrame(const V3& z, const V3& x);
     V3 local(const V3& a) const { return V3(dotv(a, X), dotv(a, Y), dotv(a, Z)); }
     V3 world(const V3& a) const {
         return V3(X.x * a.x + Y.x * a.y + Z.x * a.z, X.y * a.x + Y.y * a.y + Z.y * a.z, X.z * a.x + Y.z * a.y + Z.z * a.z);
     }
 };
 inline float bsdl_max_abs(const V3& v) { return std::max(std::fabs(v.x), std::max(std::fabs(v.y), std::fabs(v.z))); }
+inline BsdlFrame::BsdlFrame(const V3& z, const V3& x) : X(x), Z(z) {
+    if (bsdl_max_abs(X) < 1e-4f || std::fabs(dotv(Z, imath_normalize(X))) > 0.999f) {
+        *this = BsdlFrame(z);
+    } else {
+        Y = imath_normalize(crossv(Z, X));
+        X = crossv(Y, Z);
+    }
+}
 // BsdfGlobals::visible_normal (bsdf_impl.h:51-78)
 inline V3 bsdl_visible_normal(const V3& wo, const V3& Ngf, const V3& N) {
     if (dotv(wo, N) > 0.0f) return N;
@@ -534,13 +546,333 @@ struct SheenConty {
     }
 };
 
+// ---- BSDL mtx::DielectricLobe (libbsdl MTX/bsdf_dielectric_{decl,impl}.h) ----
+// as testrender wraps it (BSDL_WRAP, shading.cpp:73-115: Nf = Ngf = N,
+// outer IOR 1, lambda_0 0). The energy tables are the build's baked
+// tables (gen_bsdl_luts.cpp, BSDL genluts' method), shared as data.
+#define OSLG_LUT_QUAL static const
+#include "../openshadinglanguage_gb300/csrc/oslg_bsdl_luts.inc"
+#undef OSLG_LUT_QUAL
+
+namespace bsdl_mx {
+template <class T> inline T MIN(T a, T b) { return a < b ? a : b; }
+template <class T> inline T MAX(T a, T b) { return a > b ? a : b; }
+inline float CLAMP(float x, float a, float b) { return MIN(MAX(x, a), b); }
+inline float LERP(float f, float a, float b) {
+    f = CLAMP(f, 0, 1);
+    return (1 - f) * a + f * b;
+}
+inline float SQR(float x) { return x * x; }
+const float PI = 3.14159265358979323846f;
+
+// TabulatedEnergyCurve (microfacet_tools_impl.h:113-212) over a baked table
+// [Nf][16][16]; squared: cosines (i/15)^2 (MiniMicrofacetGGX), else i/15
+struct EnergyCurve {
+    const float* E;
+    int Nf;
+    bool squared;
+    float roughness, fresnel_index;
+    float cosine(int i) const {
+        const float t = float(i) * (1.0f / (16 - 1));
+        return std::max(squared ? SQR(t) : t, 1e-6f);
+    }
+    float interpolate_emiss(int i) const {
+        float rf = roughness * (16 - 1);
+        int ra = std::min(std::max((int)rf, 0), 15);  // BSDL reads past the table above roughness 1
+        int rb = std::min(ra + 1, 16 - 1);
+        rf -= ra;
+        if (Nf == 1) return LERP(rf, E[ra * 16 + i], E[rb * 16 + i]);
+        float ff = fresnel_index * (Nf - 1);
+        int fa = std::min(std::max((int)ff, 0), Nf - 1);
+        int fb = std::min(fa + 1, Nf - 1);
+        ff -= fa;
+        return LERP(ff, LERP(rf, E[(fa * 16 + ra) * 16 + i], E[(fa * 16 + rb) * 16 + i]),
+                    LERP(rf, E[(fb * 16 + ra) * 16 + i], E[(fb * 16 + rb) * 16 + i]));
+    }
+    float Emiss_eval(float c) const {
+        float cos0 = cosine(0);
+        if (c <= cos0) return interpolate_emiss(0);
+        for (int i = 1; i < 16; i++) {
+            const float cos1 = cosine(i);
+            if (c < cos1) {
+                float q = (c - cos0) / (cos1 - cos0);
+                return LERP(q, interpolate_emiss(i - 1), interpolate_emiss(i));
+            }
+            cos0 = cos1;
+        }
+        return interpolate_emiss(16 - 1);
+    }
+};
+
+// GGXDist (microfacet_tools_decl.h:13-47, microfacet_tools_impl.h:17-112)
+struct GGXDist {
+    float ax = 0, ay = 0;
+    GGXDist() = default;
+    GGXDist(float rough, float aniso, bool flip_aniso) : ax(SQR(rough)), ay(ax) {
+        if (flip_aniso) aniso = -aniso;
+        ax = std::max(ax * (1 + aniso), 1e-5f);
+        ay = std::max(ay * (1 - aniso), 1e-5f);
+    }
+    float D(const V3& Hr) const {
+        const float cosPhi2st2 = SQR(Hr.x / ax);
+        const float sinPhi2st2 = SQR(Hr.y / ay);
+        const float cosThetaM2 = SQR(Hr.z);
+        const float sinThetaM2 = cosPhi2st2 + sinPhi2st2;
+        return 1.0f / (PI * ax * ay * SQR(cosThetaM2 + sinThetaM2));
+    }
+    float G1(V3 w) const {
+        w = V3(w.x * ax, w.y * ay, w.z);
+        return 2.0f * w.z / (w.z + imath_len(w));
+    }
+    float G2_G1(V3 wi, V3 wo) const {
+        wi = V3(wi.x * ax, wi.y * ay, wi.z);
+        wo = V3(wo.x * ax, wo.y * ay, wo.z);
+        const float nl = imath_len(wi);
+        const float nv = imath_len(wo);
+        return wi.z * (wo.z + nv) / (wo.z * nl + wi.z * nv);
+    }
+    // Eto & Tokuyoshi, bounded VNDF sampling for Smith-GGX reflections
+    V3 sample_for_refl(const V3& wo, float randu, float randv) const {
+        V3 i_std = imath_normalize(V3(wo.x * ax, wo.y * ay, wo.z));
+        const float phi = 2.0f * PI * randu;
+        const float a = CLAMP(std::min(ax, ay), 0.0f, 1.0f);
+        const float s = 1 + std::sqrt(SQR(wo.x) + SQR(wo.y));
+        const float a2 = SQR(a);
+        const float s2 = SQR(s);
+        const float k = (1 - a2) * s2 / (s2 + a2 * SQR(wo.z));
+        const float b = k * i_std.z;
+        const float z = (1 - randv) * (1 + b) - b;
+        const float sinTheta = std::sqrt(CLAMP(1 - SQR(z), 0.0f, 1.0f));
+        V3 o_std(sinTheta * oracle_fm::cosf_(phi), sinTheta * oracle_fm::sinf_(phi), z);
+        V3 m_std = i_std + o_std;
+        return imath_normalize(V3(m_std.x * ax, m_std.y * ay, m_std.z));
+    }
+    float D_refl_D(const V3& wo) const {
+        const float aix = wo.x * ax, aiy = wo.y * ay;
+        const float len2 = aix * aix + aiy * aiy;
+        const float t = std::sqrt(len2 + SQR(wo.z));
+        const float a = CLAMP(std::min(ax, ay), 0.0f, 1.0f);
+        const float s = 1 + std::sqrt(SQR(wo.x) + SQR(wo.y));
+        const float a2 = SQR(a);
+        const float s2 = SQR(s);
+        const float k = (1 - a2) * s2 / (s2 + a2 * SQR(wo.z));
+        return 2 * wo.z / (k * wo.z + t);
+    }
+};
+
+// DielectricFresnel (MTX/bsdf_dielectric_impl.h:21-64)
+struct DielectricFresnel {
+    float eta = 1.5f;
+    DielectricFresnel() = default;
+    DielectricFresnel(float e, bool backside) {
+        if (backside) e = 1 / e;
+        eta = e >= 1 ? CLAMP(e, 1.001f, 5.0f) : CLAMP(e, 1 / 5.0f, 1 / 1.001f);
+    }
+    float eval(float c) const {
+        float g = (eta - 1.0f) * (eta + 1.0f) + c * c;
+        if (g > 0) {
+            g = std::sqrt(g);
+            float A = (g - c) / (g + c);
+            float B = (c * (g + c) - 1) / (c * (g - c) + 1);
+            return 0.5f * A * A * (1 + B * B);
+        }
+        return 1.0f;
+    }
+    float table_index() const {
+        const float seta = CLAMP(eta < 1 ? 1 / eta : eta, 1.001f, 5.0f);
+        const float x = (seta - 1.001f) * (1 / (5.0f - 1.001f));
+        return std::sqrt(x);
+    }
+};
+
+// BSDL reflect / refract (tools.h:301-334)
+inline V3 reflect(const V3& E, const V3& N) { return N * (2 * dotv(N, E)) - E; }
+inline V3 refract(const V3& E, const V3& N, float eta) {
+    V3 R(0.0f);
+    if (eta == 0) return R;
+    V3 Nn;
+    float cosi = dotv(E, N), neta;
+    if (cosi > 0) {
+        neta = 1 / eta;
+        Nn = N;
+    } else {
+        cosi = -cosi;
+        neta = eta;
+        Nn = -N;
+    }
+    float arg = 1 - (neta * neta * (1 - (cosi * cosi)));
+    if (arg >= 0) {
+        float dnp = std::sqrt(arg);
+        float nK = (neta * cosi) - dnp;
+        R = imath_normalize(E * (-neta) + Nn * nK);
+    }
+    return R;
+}
+
+// DielectricBSDF<DielectricFresnel> (MTX/bsdf_dielectric_impl.h:66-216)
+struct DielectricBSDF {
+    GGXDist d;
+    DielectricFresnel f;
+    float E_ms = 0.0f;
+    bool dorefr = false;
+    DielectricBSDF() = default;
+    DielectricBSDF(const GGXDist& dist, const DielectricFresnel& fr, float cosNO, float roughness, bool refr)
+        : d(dist), f(fr), dorefr(refr) {
+        if (!dorefr) E_ms = EnergyCurve{ kLutMiniGGX, 1, true, roughness, 0.0f }.Emiss_eval(cosNO);
+    }
+    // eval_turquin_microms_reflection (microfacet_tools_impl.h:343-373)
+    Sample turquin_eval(const V3& wo, const V3& wi) const {
+        const float cosNO = wo.z, cosNI = wi.z;
+        if (cosNI <= 0 || cosNO <= 0) return Sample();
+        V3 m = imath_normalize(wo + wi);
+        float cosMO = dotv(m, wo);
+        const float D = d.D(m);
+        float D_refl_D = d.D_refl_D(wo);
+        float D_refl = D_refl_D * D;
+        const float G1 = d.G1(wo);
+        float pdf = D_refl / (4 * cosNO);
+        const float out = d.G2_G1(wi, wo) * G1 / D_refl_D;
+        const float F = f.eval(cosMO);
+        const float msf = E_ms / std::max(0.01f, 1 - E_ms);
+        Sample s;
+        s.wi = wi;
+        s.weight = V3(out * F * (1 + F * msf));
+        s.pdf = pdf;
+        return s;
+    }
+    Sample eval(const V3& wo, const V3& wi) const {
+        if (!dorefr) return turquin_eval(wo, wi);
+        const float cosNO = wo.z;
+        const float cosNI = wi.z;
+        Sample s;
+        if (cosNI > 0) {
+            const V3 m = imath_normalize(wo + wi);
+            const float cosMO = dotv(m, wo);
+            if (cosMO <= 0) return Sample();
+            const float D = d.D(m);
+            const float G1 = d.G1(wo);
+            const float F = f.eval(cosMO);
+            if (F <= 0) return Sample();
+            const float D_refl_D = d.D_refl_D(wo);
+            const float D_refl = D_refl_D * D;
+            s.weight = V3(F * (d.G2_G1(wi, wo) * G1 / (D_refl_D * F)));
+            s.pdf = D_refl / (4.0f * cosNO) * F;
+            s.wi = wi;
+            return s;
+        } else if (cosNI < 0) {
+            const V3 Ht = imath_normalize(f.eta * wi + wo) * ((f.eta > 1) ? -1.0f : 1.0f);
+            const float cosHO = dotv(Ht, wo);
+            const float cosHI = dotv(Ht, wi);
+            if (cosHO <= 0 || cosHI >= 0) return Sample();
+            const float Ft = 1.0f - f.eval(cosHO);
+            if (Ht.z <= 0 || Ft <= 0) return Sample();
+            const float D = d.D(Ht);
+            const float G1 = d.G1(wo);
+            float J = (-cosHI * cosHO * SQR(f.eta)) / (wo.z * SQR(cosHI * f.eta + cosHO));
+            const float D_refl_D = d.D_refl_D(wo);
+            const float D_refl = D_refl_D * D;
+            s.pdf = D_refl * J * Ft;
+            s.weight = V3(Ft * (d.G2_G1(V3(wi.x, wi.y, -wi.z), wo) * G1 / (D_refl_D * Ft)));
+            s.wi = wi;
+            return s;
+        }
+        return Sample();
+    }
+    Sample sample(const V3& wo, float randu, float randv, float randw) const {
+        if (!dorefr) {  // sample_turquin_microms_reflection (:375-391)
+            if (wo.z <= 0) return Sample();
+            V3 m = d.sample_for_refl(wo, randu, randv);
+            V3 wi = reflect(wo, m);
+            if (wi.z <= 0) return Sample();
+            return turquin_eval(wo, wi);
+        }
+        V3 m = d.sample_for_refl(wo, randu, randv);
+        const float cosMO = dotv(wo, m);
+        if (cosMO <= 0) return Sample();
+        const float F = f.eval(cosMO);
+        bool choose_reflect = randw < F;
+        const V3 wi = choose_reflect ? reflect(wo, m) : refract(wo, m, f.eta);
+        if ((choose_reflect && wi.z <= 0) || (!choose_reflect && wi.z >= 0)) return Sample();
+        return eval(wo, wi);
+    }
+};
+}  // namespace bsdl_mx
+
+// DielectricLobe (MTX/bsdf_dielectric_impl.h:245-366) through BSDL_WRAP
+struct MxDielectric {
+    BsdlFrame frame;
+    bsdl_mx::DielectricBSDF spec;
+    V3 refl_tint, refr_tint, wo_absorption = V3(1.0f);
+    float E_ms = 0.0f, rough = 0.0f;
+    bool dorefl = false, dorefr = false;
+    MxDielectric(const V3& N, const V3& U, const V3& refl, const V3& refr, float roughness_x, float roughness_y,
+                 float ior, const V3& absorption, const V3& wo, float path_roughness, bool backfacing)
+        : refl_tint(refl), refr_tint(refr) {
+        using namespace bsdl_mx;
+        frame = BsdlFrame(bsdl_visible_normal(wo, N, N), U);
+        dorefl = MAX(refl.x, MAX(refl.y, refl.z)) > 0;
+        dorefr = MAX(refr.x, MAX(refr.y, refr.z)) > 0;
+        const float rx = CLAMP(roughness_x, 1e-4f, 2.0f);
+        const float ry = CLAMP(roughness_y, 1e-4f, 2.0f);
+        const float ax = std::max(rx, ry);
+        const float ay = std::min(rx, ry);
+        const float b = ay / ax;
+        const float aniso = (1 - b) / (1 + b);
+        const float roughness = 1.0f - (1.0f - std::sqrt(ax / (1 + aniso))) * (1.0f - path_roughness);
+        const float cosNO = dotv(frame.Z, wo);
+        const float IOR = CLAMP(ior, 1.001f, 5.0f);
+        DielectricFresnel fresnel(IOR / 1.0f, backfacing);
+        spec = DielectricBSDF(GGXDist(roughness, aniso, rx < ry), fresnel, cosNO, roughness, dorefr);
+        if (dorefl && !dorefr)
+            E_ms = EnergyCurve{ kLutDielReflFront, 32, false, roughness, fresnel.table_index() }.Emiss_eval(cosNO);
+        else if (dorefr)
+            E_ms = EnergyCurve{ backfacing ? kLutDielBothBack : kLutDielBothFront, 32, false, roughness,
+                                fresnel.table_index() }
+                       .Emiss_eval(cosNO);
+        rough = roughness;
+        if (MAX(absorption.x, MAX(absorption.y, absorption.z)) > 0 && dorefl && !dorefr) {
+            const float sinNO2 = 1 - SQR(cosNO);
+            const float inveta2 = SQR(1 / fresnel.eta);
+            const float cos_p = std::sqrt(1 - std::min(1.0f, inveta2 * sinNO2));
+            const float dist = 1 / std::max(cos_p, 1.17549435e-38f);
+            for (int i = 0; i < 3; ++i) wo_absorption[i] = oracle_fm::expf_(-absorption[i] * dist);
+        }
+    }
+    V3 tint(float cosNI) const { return cosNI > 0 ? refl_tint : refr_tint; }
+    Sample eval(const V3& wo, const V3& wi) const {
+        Sample r;
+        r.wi = wi;
+        if (!dorefl && !dorefr) return r;
+        Sample s = spec.eval(frame.local(wo), frame.local(wi));
+        if (dorefr) s.weight = s.weight * (1 / std::max(0.01f, 1 - E_ms));
+        s.weight = s.weight * tint(s.wi.z);
+        r.weight = s.weight;
+        r.pdf = s.pdf;
+        r.roughness = rough;
+        return r;
+    }
+    Sample sample(const V3& wo, float rx, float ry, float rz) const {
+        if (!dorefl && !dorefr) return Sample();
+        Sample s = spec.sample(frame.local(wo), rx, ry, rz);
+        if (dorefr) s.weight = s.weight * (1 / std::max(0.01f, 1 - E_ms));
+        if (bsdl_max_abs(s.wi) < 1e-4f) return Sample();
+        s.weight = s.weight * tint(s.wi.z);
+        s.roughness = rough;
+        s.wi = frame.world(s.wi);
+        return s;
+    }
+    V3 albedo() const { return !dorefr ? refl_tint * (1 - E_ms) : V3(1.0f); }
+    V3 filter_o() const { return !dorefr ? E_ms * wo_absorption : V3(0.0f); }
+};
+
 // The lobes testrender builds from a closure tree, with their weights.
 struct CompositeLobes {
-    enum Kind { DIFFUSE, GGX, OREN_NAYAR, SHEEN };
+    enum Kind { DIFFUSE, GGX, OREN_NAYAR, SHEEN, MX_DIELECTRIC };
     int kind[kMaxLobes];
     V3 w[kMaxLobes];
     float pdfs[kMaxLobes];
-    static constexpr size_t kStore = std::max(sizeof(MicrofacetGGX), std::max(sizeof(OrenNayarQON), sizeof(SheenConty)));
+    static constexpr size_t kStore = std::max(std::max(sizeof(MicrofacetGGX), sizeof(MxDielectric)),
+                                              std::max(sizeof(OrenNayarQON), sizeof(SheenConty)));
     alignas(16) unsigned char storage[kMaxLobes][kStore];
     V3 N[kMaxLobes];
     int n = 0;
@@ -550,6 +882,7 @@ struct CompositeLobes {
     const OrenNayarQON& on(int i) const { return *reinterpret_cast<const OrenNayarQON*>(storage[i]); }
     const MicrofacetGGX& mf(int i) const { return *reinterpret_cast<const MicrofacetGGX*>(storage[i]); }
     const SheenConty& sh(int i) const { return *reinterpret_cast<const SheenConty*>(storage[i]); }
+    const MxDielectric& mxd(int i) const { return *reinterpret_cast<const MxDielectric*>(storage[i]); }
 
     void add_diffuse(const V3& cw, const V3& normal) {
         if (n_full()) return;
@@ -574,12 +907,19 @@ struct CompositeLobes {
         new (storage[n]) SheenConty(o);
         ++n;
     }
+    void add_mx_dielectric(const V3& cw, const MxDielectric& o) {
+        if (n_full()) return;
+        kind[n] = MX_DIELECTRIC; w[n] = cw;
+        new (storage[n]) MxDielectric(o);
+        ++n;
+    }
     bool n_full() const { return n >= kMaxLobes; }
 
     V3 albedo(int i, const V3& wo) const {
         if (kind[i] == GGX) return mf(i).albedo(wo);
         if (kind[i] == SHEEN) return sh(i).albedo();
         if (kind[i] == OREN_NAYAR) return on(i).alb;
+        if (kind[i] == MX_DIELECTRIC) return mxd(i).albedo();
         return V3(1.0f);
     }
     Sample eval_lobe(int i, const V3& wo, const V3& wi) const {
@@ -590,12 +930,14 @@ struct CompositeLobes {
         }
         if (kind[i] == GGX) return mf(i).eval(wo, wi);
         if (kind[i] == SHEEN) return sh(i).eval(wo, wi);
+        if (kind[i] == MX_DIELECTRIC) return mxd(i).eval(wo, wi);
         return on(i).eval(wo, wi);
     }
     Sample sample_lobe(int i, const V3& wo, float rx, float ry, float rz) const {
         if (kind[i] == DIFFUSE) return diffuse_sample(N[i], rx, ry);
         if (kind[i] == GGX) return mf(i).sample(wo, rx, ry, rz);
         if (kind[i] == SHEEN) return sh(i).sample(wo, rx, ry);
+        if (kind[i] == MX_DIELECTRIC) return mxd(i).sample(wo, rx, ry, rz);
         return on(i).sample(wo, rx, ry);
     }
     // CompositeBSDF::prepare (shading.h:322-350)
