@@ -388,6 +388,41 @@ def bench_serving(torch, og, nreq=600, jit=0):
     return out
 
 
+def host_link_peak(torch, bytes_in, bytes_out, reps=5):
+    """The host link's copy peaks for the e2e step's byte counts: plain
+    cudaMemcpyAsync of pinned host buffers of bytes_in (H2D) and bytes_out
+    (D2H), each alone, then both at once on two streams; the floor of the
+    e2e step is its copies at these rates."""
+    h_in = torch.empty(bytes_in // 4, dtype=torch.float32).pin_memory()
+    h_out = torch.empty(bytes_out // 4, dtype=torch.float32).pin_memory()
+    d_in = torch.empty_like(h_in, device="cuda")
+    d_out = torch.empty_like(h_out, device="cuda")
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        return min(ts)
+
+    def both():
+        with torch.cuda.stream(s1):
+            d_in.copy_(h_in, non_blocking=True)
+        with torch.cuda.stream(s2):
+            h_out.copy_(d_out, non_blocking=True)
+    t_h2d = timed(lambda: d_in.copy_(h_in, non_blocking=True))
+    t_d2h = timed(lambda: h_out.copy_(d_out, non_blocking=True))
+    t_both = timed(both)
+    return {"h2d_gbs": bytes_in / t_h2d / 1e9, "d2h_gbs": bytes_out / t_d2h / 1e9,
+            "duplex_ms": 1e3 * t_both, "ms_floor": 1e3 * t_both,
+            "method": "pinned cudaMemcpyAsync, best of %d, host clock" % reps}
+
+
 def bench_wavefront(torch, og, frames=3, cpu_step=97, size=None, jit=1):
     """Wavefront path tracing of the seeded 1000-primitive scene with the 16
     layered materials: 1920x1080x4 paths, up to 8 hits, Russian roulette
@@ -427,11 +462,16 @@ def bench_wavefront(torch, og, frames=3, cpu_step=97, size=None, jit=1):
     prof = wf.stats()
     status = ss.device_status()
     nhits = s["total_hits"]
-    # CPU: the oracle's path loop over a strided sample of the same frame
+    # CPU: the oracle's path loop over a strided sample of the same frame,
+    # the stride shrunk until the sample takes at least 2 s
     oracle_wavefront(o, prims, mats, begin=0, step=cpu_step * 8)  # warm-up on a smaller sample
-    t0 = time.perf_counter()
-    crad, chits, _ = oracle_wavefront(o, prims, mats, begin=0, step=cpu_step)
-    cpu_s = time.perf_counter() - t0
+    while True:
+        t0 = time.perf_counter()
+        crad, chits, _ = oracle_wavefront(o, prims, mats, begin=0, step=cpu_step)
+        cpu_s = time.perf_counter() - t0
+        if cpu_s >= 2.0 or cpu_step == 1:
+            break
+        cpu_step = max(1, int(cpu_step * cpu_s / 3.0))
     ncpu = crad.shape[1]
     wf.close()
     stages = dict(zip(("trace", "plan", "scatter", "shade", "update"), prof["ms_stage"]))
@@ -529,6 +569,11 @@ def cpu_reference(wl, og, budget_s=2.0):
     return n / dt / 1e6, n, reps
 
 
+def progress(msg):
+    """A timestamped progress line on stderr (the JSON line is stdout's only line)."""
+    print("[bench %s] %s" % (time.strftime("%H:%M:%S"), msg), file=sys.stderr, flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -552,9 +597,10 @@ def main():
     ap.add_argument("--section", choices=["batching", "serving", "wavefront", "texture"],
                     help="run only this measurement section and print it as one JSON line")
     ap.add_argument("--wf-size", default=None, help="wavefront frame WxHxSPP (default 1920x1080x4)")
-    ap.add_argument("--batch-jit", type=int, default=0,
+    ap.add_argument("--batch-jit", type=int, default=1,
                     help="batching and serving sections: also time every group specialized (per group, "
-                         "one persistent kernel for the 64 programs, and served waves on that kernel)")
+                         "one persistent kernel for the 64 programs, and served waves on that kernel); "
+                         "about 100 s of kernel builds on a cold cache")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.section:
@@ -620,6 +666,7 @@ def main():
         dist.init_process_group("nccl")
     else:
         torch.cuda.set_device(0)
+    progress("building %s" % wl.name)
     wl.build(torch, og, shaders)
     if args.jit:
         wl.ss.attribute("jit", 1)  # the first launch (warm-up) builds and loads the kernel
@@ -668,6 +715,7 @@ def main():
     status = wl.ss.device_status()
 
     # end to end through the public API with host buffers
+    progress("e2e")
     for _ in range(2):
         wl.e2e_step(torch, sh)
     torch.cuda.synchronize()
@@ -684,6 +732,7 @@ def main():
     barrier()
     e_ms = 1e3 * float(np.mean(e_times))
     e2e_value = wl.n * world / (e_ms * 1e-3) / 1e6
+    link = host_link_peak(torch, wl.bytes_in, wl.bytes_out)
 
     if rank != 0:
         if world > 1:
@@ -712,7 +761,10 @@ def main():
                    "kernel": "specialized per group (jit)" if args.jit else "interpreter",
                    "parity": "bit-exact to the CPU oracle (non-FMA reference order) for floats and ints"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": wl.bytes_in,
-                "d2h_bytes_per_step": wl.bytes_out, "ms_per_step": e_ms},
+                "d2h_bytes_per_step": wl.bytes_out, "ms_per_step": e_ms,
+                "link": dict(link, frac=link["ms_floor"] / e_ms,
+                             note="frac = the step's copies at the measured link peaks (H2D and D2H "
+                                  "overlapped) / the e2e step")},
         "gpu_launches": args.steps,
         "clocks": clocks,
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
@@ -726,10 +778,15 @@ def main():
         "device_status": status,
     }
     if not args.no_extras and world == 1:
+        progress("batching")
         line["batching"] = bench_batching(torch, og, jit=args.batch_jit)
+        progress("serving")
         line["serving"] = bench_serving(torch, og, jit=args.batch_jit)
+        progress("wavefront")
         line["wavefront"] = bench_wavefront(torch, og, jit=args.jit)
+        progress("texture")
         line["texture"] = bench_texture(torch, og)
+        progress("sections done")
         # the systems targets as top-level keys, ahead of the long sections
         b, sv = line["batching"], line["serving"]
         summary = {"speedup_vs_plain": b["speedup_vs_plain"],

@@ -187,13 +187,16 @@ int oslg_add_symlocs(oslg_system* sys, oslg_group* group, const oslg_symloc* loc
  * (src/testrender/shading.cpp:1450-1500 walk, shading.h:322-374 prepare and
  * eval). Writes {weight.r, weight.g, weight.b, pdf} (4 floats) at
  * output_base + offset + i*stride. Lobes: diffuse, oren_nayar, microfacet
- * "ggx" (refract 0/1/2); other closure ids contribute nothing. */
+ * "ggx" (refract 0/1/2), oren_nayar_diffuse_bsdf, sheen_bsdf and
+ * dielectric_bsdf, under layer() as testrender layers them; other closure
+ * ids contribute nothing. */
 int oslg_group_bsdf_eval(oslg_system* sys, oslg_group* group, const char* closure,
                          const float wi[3], int64_t offset, int64_t stride);
 /* Renderer-side sampling of a closure output, the per-hit step of
  * testrender's path loop (src/testrender/simpleraytracer.cpp:1038-1079):
- * the closure tree is walked (emission adds to Le; diffuse, oren_nayar and
- * microfacet "ggx" with refract 0/1/2 and sheen_bsdf become lobes),
+ * the closure tree is walked (emission adds to Le; diffuse, oren_nayar,
+ * microfacet "ggx" with refract 0/1/2, oren_nayar_diffuse_bsdf, sheen_bsdf
+ * and dielectric_bsdf become lobes),
  * prepared with the path weight and sampled (src/testrender/shading.h:322-398).
  * Reads {rx, ry, rz, path_weight.rgb, absorb, ray_roughness, backfacing}
  * (9 floats; the last two feed BSDL's roughness regularization and

@@ -2189,8 +2189,9 @@ __device__ __forceinline__ int closure_keyword_int(const Lane& L, uint32_t param
     bool done = false;
     OSLG_SPEC_UNROLL
     for (int k = first; k + 1 < kClosureParamFloats; k += 2) {
+        if (done) continue;  // no read past the first zero name (a 16-float node ends there)
         const uint32_t w = NODES::u(L, params + k);
-        if (done || w == 0u) {
+        if (w == 0u) {
             done = true;
             continue;
         }

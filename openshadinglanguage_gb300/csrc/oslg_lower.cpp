@@ -1513,6 +1513,18 @@ struct Lowerer {
     // Parameter words the device's closure_fill writes for closure op `op`
     // (an upper bound): each operand's components, at most 16, at most
     // kClosureParamFloats in all.
+    // The BSDF code reads a lobe's fixed parameter words where they must be
+    // (testrender's parameter structs, shading.h:66-211, and BSDL's lobe
+    // Data): a closure op with fewer is refused rather than read past.
+    bool closure_params_complete(const std::string& cname, const LOp& op) {
+        static const std::map<std::string, int> fixed = {
+            { "diffuse", 3 }, { "oren_nayar", 4 }, { "microfacet", 11 }, { "oren_nayar_diffuse_bsdf", 7 },
+            { "sheen_bsdf", 7 }, { "dielectric_bsdf", 16 } };
+        auto it = fixed.find(cname);
+        if (it == fixed.end() || closure_param_words(op) >= it->second) return true;
+        return fail("closure '" + cname + "' needs " + std::to_string(it->second) + " parameter words, has " +
+                    std::to_string(closure_param_words(op)));
+    }
     int closure_param_words(const LOp& op) const {
         const size_t na = op.args.size();
         size_t ni = 1;
@@ -2210,6 +2222,7 @@ struct Lowerer {
             std::string cname = const_string(op.args[ni]);
             auto it = ss.closure_ids.find(cname);
             if (it == ss.closure_ids.end()) return fail("closure '" + cname + "' is not registered");
+            if (!closure_params_complete(cname, op)) return false;
             std::vector<uint32_t> params;
             for (size_t i = ni + 1; i < na && params.size() < 11; ++i) params.push_back(A(op.args[i]));
             while (params.size() < 11) params.push_back(kNoArg);
@@ -2643,6 +2656,7 @@ struct Lowerer {
             std::string cname = const_string(op.args[ni]);
             auto it = ss.closure_ids.find(cname);
             if (it == ss.closure_ids.end()) return fail("closure '" + cname + "' is not registered");
+            if (!closure_params_complete(cname, op)) return false;
             std::vector<uint32_t> params;
             for (size_t i = ni + 1; i < na && params.size() < 11; ++i) params.push_back(A(op.args[i]));
             while (params.size() < 11) params.push_back(kNoArg);

@@ -721,6 +721,15 @@ __device__ __forceinline__ BsdfSample sheen_sample(const SheenLobeDev& L, V3 wo,
 #include "oslg_bsdl_luts.inc"
 #undef OSLG_LUT_QUAL
 
+// The dielectric's construction, evaluation and sampling are calls in
+// persistent batch kernels: a batch body instantiates a lobe's code once per
+// lobe position and MIS pair, which inlined would multiply its compile time.
+#ifdef OSLG_SPEC_BATCH
+#define OSLG_DIEL_FN __noinline__
+#else
+#define OSLG_DIEL_FN __forceinline__
+#endif
+
 // BSDL's MIN / MAX / CLAMP / LERP (tools.h:84-117)
 __device__ __forceinline__ float bmin(float a, float b) { return a < b ? a : b; }
 __device__ __forceinline__ float bmax(float a, float b) { return a > b ? a : b; }
@@ -889,7 +898,7 @@ struct DielLobeDev {
     bool dorefl, dorefr;
 };
 // DielectricLobe::DielectricLobe (MTX/bsdf_dielectric_impl.h:245-316)
-__device__ __forceinline__ DielLobeDev diel_make(V3 N, V3 U, const float* refl, const float* refr, float rx_in,
+__device__ OSLG_DIEL_FN DielLobeDev diel_make(V3 N, V3 U, const float* refl, const float* refr, float rx_in,
                                                  float ry_in, float ior, const float* absorption, V3 wo,
                                                  float path_rough, bool backfacing) {
     DielLobeDev D;
@@ -1013,7 +1022,7 @@ __device__ __forceinline__ void diel_finish(const DielLobeDev& L, BsdfSample& s)
         for (int c = 0; c < 3; ++c) s.w[c] *= inv;
     }
 }
-__device__ __forceinline__ BsdfSample diel_eval(const DielLobeDev& L, V3 wo, V3 wi) {
+__device__ OSLG_DIEL_FN BsdfSample diel_eval(const DielLobeDev& L, V3 wo, V3 wi) {
     if (!L.dorefl && !L.dorefr) {
         BsdfSample z = bsdf_zero();
         z.wi = wi;
@@ -1027,7 +1036,7 @@ __device__ __forceinline__ BsdfSample diel_eval(const DielLobeDev& L, V3 wo, V3 
     s.wi = wi;
     return s;
 }
-__device__ __forceinline__ BsdfSample diel_sample(const DielLobeDev& L, V3 wo, float rx, float ry, float rz) {
+__device__ OSLG_DIEL_FN BsdfSample diel_sample(const DielLobeDev& L, V3 wo, float rx, float ry, float rz) {
     if (!L.dorefl && !L.dorefr) return bsdf_zero();
     BsdfSample s = diel_spec_sample(L, tolocal(L.f, wo), rx, ry, rz);
     diel_finish(L, s);
