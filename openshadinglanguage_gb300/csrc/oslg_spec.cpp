@@ -169,7 +169,10 @@ void add_bounds(Bounds& B, const ProgView& v) {
     int adds = 0;
     for (int i = 0; i < v.n; ++i) {
         loops = loops || v.ops[i].code == OP_LOOP_BEGIN || v.ops[i].code == OP_JUMP;
-        adds += v.ops[i].code == OP_CLOSURE_ADD;
+        // a layer(top, base) closure branches like an ADD: the walk pushes its
+        // base, and top and base both hold lobes
+        adds += v.ops[i].code == OP_CLOSURE_ADD ||
+                (v.ops[i].code == OP_CLOSURE && (int)v.ops[i].a[1] == kIdMxLayer);
         if (v.ops[i].code == OP_CL_BSDF_EVAL || v.ops[i].code == OP_CL_BSDF_SAMPLE || v.ops[i].code == OP_CL_STORE) {
             B.any = true;
             B.lobes = std::max(B.lobes, std::min((int)kBsdfMaxLobes, std::max(1, (int)v.ops[i].a[0])));
