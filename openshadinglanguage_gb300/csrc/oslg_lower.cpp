@@ -2423,6 +2423,15 @@ struct Lowerer {
         if (n == "calculatenormal") { emit(OP_CALCNORMAL, { a(0), a(1) }, n); return true; }
         if (n == "backfacing") { emit(OP_LOAD_GLOBAL, { a(0), (uint32_t)G_BACKFACING }, n); return true; }
         if (n == "surfacearea") { emit(OP_LOAD_GLOBAL, { a(0), (uint32_t)G_SURFACEAREA }, n); return true; }
+        if (n == "trace") {
+            // RendererServices::trace (rendservices.cpp:511-517): the default
+            // renderer services trace nothing and report no hit; a sourced
+            // getmessage("trace", ...) then finds nothing either
+            const int c = const_int(0);
+            syms[c].slot = (int)pool_add(syms[c]);
+            emit(OP_ASSIGN, { a(0), A(c), 1u, 1u, 1u }, n);
+            return true;
+        }
         if (n == "isconstant") {
             // what folding did not turn into 1 is not constant
             // (batched_llvm_gen.cpp:8079-8092)
