@@ -721,13 +721,15 @@ __device__ __forceinline__ BsdfSample sheen_sample(const SheenLobeDev& L, V3 wo,
 #include "oslg_bsdl_luts.inc"
 #undef OSLG_LUT_QUAL
 
-// The dielectric's construction, evaluation and sampling are calls in
-// persistent batch kernels: a batch body instantiates a lobe's code once per
-// lobe position and MIS pair, which inlined would multiply its compile time.
-#ifdef OSLG_SPEC_BATCH
-#define OSLG_DIEL_FN __noinline__
-#else
+// The dielectric's construction, evaluation and sampling are calls except
+// in a kernel specialized to one group: a persistent batch body instantiates
+// a lobe's code once per lobe position and MIS pair (inlined, that would
+// multiply its compile time), and the interpreter carries every lobe kind,
+// where inlining this one would cost registers on every path.
+#if defined(OSLG_SPEC) && !defined(OSLG_SPEC_BATCH)
 #define OSLG_DIEL_FN __forceinline__
+#else
+#define OSLG_DIEL_FN __noinline__
 #endif
 
 // BSDL's MIN / MAX / CLAMP / LERP (tools.h:84-117)
@@ -898,7 +900,7 @@ struct DielLobeDev {
     bool dorefl, dorefr;
 };
 // DielectricLobe::DielectricLobe (MTX/bsdf_dielectric_impl.h:245-316)
-__device__ OSLG_DIEL_FN DielLobeDev diel_make(V3 N, V3 U, const float* refl, const float* refr, float rx_in,
+static __device__ OSLG_DIEL_FN DielLobeDev diel_make(V3 N, V3 U, const float* refl, const float* refr, float rx_in,
                                                  float ry_in, float ior, const float* absorption, V3 wo,
                                                  float path_rough, bool backfacing) {
     DielLobeDev D;
@@ -1022,7 +1024,7 @@ __device__ __forceinline__ void diel_finish(const DielLobeDev& L, BsdfSample& s)
         for (int c = 0; c < 3; ++c) s.w[c] *= inv;
     }
 }
-__device__ OSLG_DIEL_FN BsdfSample diel_eval(const DielLobeDev& L, V3 wo, V3 wi) {
+static __device__ OSLG_DIEL_FN BsdfSample diel_eval(const DielLobeDev& L, V3 wo, V3 wi) {
     if (!L.dorefl && !L.dorefr) {
         BsdfSample z = bsdf_zero();
         z.wi = wi;
@@ -1036,7 +1038,7 @@ __device__ OSLG_DIEL_FN BsdfSample diel_eval(const DielLobeDev& L, V3 wo, V3 wi)
     s.wi = wi;
     return s;
 }
-__device__ OSLG_DIEL_FN BsdfSample diel_sample(const DielLobeDev& L, V3 wo, float rx, float ry, float rz) {
+static __device__ OSLG_DIEL_FN BsdfSample diel_sample(const DielLobeDev& L, V3 wo, float rx, float ry, float rz) {
     if (!L.dorefl && !L.dorefr) return bsdf_zero();
     BsdfSample s = diel_spec_sample(L, tolocal(L.f, wo), rx, ry, rz);
     diel_finish(L, s);
