@@ -299,6 +299,35 @@ std::string spec_source(const CompiledGroup& cg, int min_blocks) {
     o << "#include \"oslg_interp.cuh\"\n\nnamespace {\n";
     o << "using namespace oslg;\nusing namespace oslg::dev;\n\n";
     emit_body(o, v, "");
+    if (stage) {
+        // the tile's copy-out is a call of its own, so that the shading
+        // body's register allocation does not depend on it
+        o << "__device__ __noinline__ void spec_copy_out(const KArgs& k, const unsigned char* smem, int64_t tile, "
+             "int fill_unwritten) {\n";
+        o << "        const size_t rec = " << stage << "u;\n";
+        o << "        const unsigned char* flags = smem + (size_t)blockDim.x * rec;\n";
+        o << "    const int64_t npt = k.npoints - tile * blockDim.x < (int64_t)blockDim.x ? k.npoints - tile * "
+             "blockDim.x : (int64_t)blockDim.x;\n";
+        o << "    uint32_t* gout = reinterpret_cast<uint32_t*>(k.outputs + tile * blockDim.x * (int64_t)rec);\n";
+        o << "    const uint32_t* sw = reinterpret_cast<const uint32_t*>(smem);\n";
+        o << "    if (!k.shadeindex) {\n";
+        o << "        for (int64_t w = threadIdx.x; w < npt * (int64_t)(rec / 4u); w += blockDim.x)\n";
+        o << "            if (flags[w]) gout[w] = sw[w];\n";
+        o << "            else if (fill_unwritten) gout[w] = 0u;\n";
+        o << "    } else {  // each point's record goes to its shadeindex\n";
+        // 32-bit word indices (a tile is at most 256 records): division by
+        // the constant record size stays cheap and adds no register pressure
+        o << "        const int32_t* si = k.shadeindex + tile * blockDim.x;\n";
+        o << "        const uint32_t nw = (uint32_t)npt * (uint32_t)(rec / 4u);\n";
+        o << "        for (uint32_t w = threadIdx.x; w < nw; w += blockDim.x) {\n";
+        o << "            const uint32_t p = w / (uint32_t)(rec / 4u), q = w - p * (uint32_t)(rec / 4u);\n";
+        o << "            uint32_t* dst = reinterpret_cast<uint32_t*>(k.outputs + (int64_t)__ldg(si + p) * (int64_t)rec) + q;\n";
+        o << "            if (flags[w]) *dst = sw[w];\n";
+        o << "            else if (fill_unwritten) *dst = 0u;\n";
+        o << "        }\n";
+        o << "    }\n";
+        o << "}\n";
+    }
     o << "}  // namespace\n\n";
     // registers per thread are capped at 65536 / (256 * min_blocks); by
     // default 48 for closure programs (latency-bound: more resident warps;
@@ -341,26 +370,7 @@ std::string spec_source(const CompiledGroup& cg, int min_blocks) {
     o << "        L.pt = tile * blockDim.x + threadIdx.x;\n        spec_body(R, L, k.npoints);\n";
     if (stage) {
         o << "        __syncthreads();\n";
-        o << "        const int64_t npt = k.npoints - tile * blockDim.x < (int64_t)blockDim.x ? k.npoints - tile * "
-             "blockDim.x : (int64_t)blockDim.x;\n";
-        o << "        uint32_t* gout = reinterpret_cast<uint32_t*>(k.outputs + tile * blockDim.x * (int64_t)rec);\n";
-        o << "        const uint32_t* sw = reinterpret_cast<const uint32_t*>(smem);\n";
-        o << "        if (!k.shadeindex) {\n";
-        o << "            for (int64_t w = threadIdx.x; w < npt * (int64_t)(rec / 4u); w += blockDim.x)\n";
-        o << "                if (flags[w]) gout[w] = sw[w];\n";
-        o << "                else if (fill_unwritten) gout[w] = 0u;\n";
-        o << "        } else {  // each point's record goes to its shadeindex\n";
-        // 32-bit word indices (a tile is at most 256 records): division by
-        // the constant record size stays cheap and adds no register pressure
-        o << "            const int32_t* si = k.shadeindex + tile * blockDim.x;\n";
-        o << "            const uint32_t nw = (uint32_t)npt * (uint32_t)(rec / 4u);\n";
-        o << "            for (uint32_t w = threadIdx.x; w < nw; w += blockDim.x) {\n";
-        o << "                const uint32_t p = w / (uint32_t)(rec / 4u), q = w - p * (uint32_t)(rec / 4u);\n";
-        o << "                uint32_t* dst = reinterpret_cast<uint32_t*>(k.outputs + (int64_t)__ldg(si + p) * (int64_t)rec) + q;\n";
-        o << "                if (flags[w]) *dst = sw[w];\n";
-        o << "                else if (fill_unwritten) *dst = 0u;\n";
-        o << "            }\n";
-        o << "        }\n";
+        o << "        spec_copy_out(k, smem, tile, fill_unwritten);\n";
         o << "        __syncthreads();\n";
     }
     o << "    }\n}\n";
